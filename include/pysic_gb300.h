@@ -1,0 +1,176 @@
+/*
+ * pysic_gb300.h -- C ABI of the GB300 energy/force engine behind the Pysic API.
+ *
+ * The reference crosses from Python into its Fortran core through the f2py
+ * module `pysic_interface` (fortran/PyInterface.f90), imported as
+ * `pysic.pysic_fortran` (pysic/calculator.py:16).  This library replaces that
+ * module.  Each entry point below names the f2py routine it stands in for.
+ *
+ * Conventions
+ *  - Plain C types only; every function returns an int status (PG_OK = 0) and
+ *    pg_last_error() returns a message for the calling thread's last failure.
+ *  - Atom indices are 0-based; positions, forces and offsets are N x 3 in
+ *    C order (the reference transposes (3,N) Fortran arrays in Python,
+ *    calculator.py:941, 1496).
+ *  - cell is 3 x 3 row-major with the cell vectors as rows (ASE layout); inv
+ *    is its inverse (numpy.linalg.inv(cell)).
+ *  - Stress/virial components are ordered xx, yy, zz, yz, xz, xy and hold the
+ *    reference's potential part sum(r_a * F_b) (calculator.py:513-534 turns it
+ *    into -(kinetic + virial)/V).
+ *  - Interaction records are the reference's own records after the Python
+ *    layer's target permutation (calculator.py:1063-1447); target filters are
+ *    64-bit masks over atom types.
+ *  - All state is owned by an opaque context; host arrays are only read or
+ *    written during the call.  One context per thread; each context has its
+ *    own CUDA stream on the current device.
+ */
+#ifndef PYSIC_GB300_H
+#define PYSIC_GB300_H
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define PG_OK 0
+#define PG_ERR_INVALID 1        /* invalid argument                                   */
+#define PG_ERR_CUDA 2           /* CUDA runtime error or device out of memory          */
+#define PG_ERR_NOT_READY 3      /* cell / atoms / neighbour lists not set              */
+#define PG_ERR_UNSUPPORTED 4    /* interaction the engine does not evaluate            */
+#define PG_ERR_NOT_CONVERGED 5  /* charge relaxation hit its step limit                */
+#define PG_ERR_TIMEOUT 6        /* a device-side wait ran out (bounded spin)           */
+#define PG_ERR_SMALL_CELL 7     /* cell narrower than the cutoff: cell list not usable */
+
+#define PG_PREC_FP64 0   /* every operation in FP64                                   */
+#define PG_PREC_MIXED 1  /* FP32 per pair/triplet, FP64 (compensated) accumulation     */
+
+#define PG_WANT_ENERGY 1
+#define PG_WANT_FORCES 2  /* forces and virial */
+#define PG_WANT_ENEGS 4   /* electronegativities */
+
+typedef struct pg_context pg_context;
+
+/* Thread-local message of the last failing call ("" if none). */
+const char* pg_last_error(void);
+/* Library version string. */
+const char* pg_version(void);
+
+/* Create / destroy an engine context.  Replaces the module-global state set up by
+ * start_potentials / start_bond_order_factors (PyInterface.f90:51-80, called at
+ * import, pysic/core.py:19-30) and torn down by release (PyInterface.f90:1023-1036). */
+int pg_create(pg_context** ctx);
+int pg_destroy(pg_context* ctx);
+
+/* create_cell(vectors, inverse, periodicity), PyInterface.f90:208-222 */
+int pg_create_cell(pg_context* ctx, const double* cell, const double* inv, const int32_t* pbc);
+
+/* create_atoms(masses, charges, positions, momenta, tags, elements), PyInterface.f90:250-268.
+ * Elements and tags arrive already folded into atom types (0 .. 63). */
+int pg_create_atoms(pg_context* ctx, int32_t n, const double* positions, const double* charges,
+                    const int32_t* types);
+/* update_atom_coordinates(positions, momenta), PyInterface.f90:277-286 */
+int pg_update_atom_coordinates(pg_context* ctx, const double* positions);
+/* update_atom_charges(charges), PyInterface.f90:295-302 */
+int pg_update_atom_charges(pg_context* ctx, const double* charges);
+/* Read back the engine's copy of the charges (used after pg_relax_charges). */
+int pg_get_atom_charges(pg_context* ctx, double* charges);
+
+/* allocate_potentials(n) + add_potential(...) for every pair record,
+ * PyInterface.f90:370-380, 433-480.  kind: 0 LJ, 1 exponential, 2 Buckingham;
+ * params: 4 per record (unused tail zero); soft: cutoff - cutoff_margin;
+ * group: bond-order group (-1 none). */
+int pg_set_pair_potentials(pg_context* ctx, int32_t n_types, int32_t n_records, const int32_t* kind,
+                           const double* params, const double* cutoff, const double* soft,
+                           const uint64_t* mask1, const uint64_t* mask2, const int32_t* group);
+/* add_potential(...) for single-atom records (charge_self: params epsilon, n). */
+int pg_set_single_potentials(pg_context* ctx, int32_t n_records, const int32_t* kind, const double* params,
+                             const uint64_t* mask);
+/* allocate_bond_order_factors(n) + add_bond_order_factor(...), PyInterface.f90:384-395, 482-526.
+ * Tersoff records: params beta, eta, a, c, d, h, mu. */
+int pg_set_bond_order_factors(pg_context* ctx, int32_t n_records, const double* params, const double* cutoff,
+                              const double* soft, const uint64_t* mask1, const uint64_t* mask2,
+                              const uint64_t* mask3, const int32_t* group);
+/* set_ewald_parameters(real_cut, k_radius, reciprocal_cut, sigma, epsilon, scaler),
+ * PyInterface.f90:1039-1046.  scaler has one entry per atom. */
+int pg_set_ewald(pg_context* ctx, double real_cut, double k_radius, const int32_t* kmax, double sigma,
+                 double epsilon, const double* scaler);
+/* Switch Ewald summation off (the reference does this by re-initialising the core). */
+int pg_clear_ewald(pg_context* ctx);
+
+/* generate_neighbor_lists(n_atoms, cutoffs), PyInterface.f90:1062-1072: the cell-list
+ * build of FastNeighborList (calculator.py:62-108).  cutoffs already include the
+ * list skin; skin is passed separately so the engine can derive its short list
+ * for bond-order terms.  The lists are bit-identical, order included, to
+ * core_build_neighbor_lists (Core.f90:8148-8280).  Fails with PG_ERR_SMALL_CELL
+ * when the cell is narrower than the largest cutoff (the reference then uses
+ * ASE's list, calculator.py:829-848). */
+int pg_generate_neighbor_lists(pg_context* ctx, const double* cutoffs, double skin);
+/* The list the reference takes from ASE's NeighborList when the cell is narrower
+ * than the cutoff (calculator.py:829-848, 905-915 -> create_neighbor_list,
+ * PyInterface.f90:528-546), built on the device: both directions, no self pair,
+ * i and j neighbours when |r_j + n.cell - r_i| < c_i + c_j.  Ordered by partner,
+ * then image offset. */
+int pg_generate_all_pairs_lists(pg_context* ctx, const double* cutoffs, double skin);
+/* get_number_of_neighbors_of_atom, PyInterface.f90:1075-1082, for all atoms at once. */
+int pg_get_neighbor_counts(pg_context* ctx, int32_t* counts);
+/* get_neighbor_list_of_atom, PyInterface.f90:1085-1096, for all atoms at once:
+ * neighbours (0-based) and offsets (3 per entry) in CSR order. */
+int pg_get_neighbor_lists(pg_context* ctx, int32_t* neighbors, int32_t* offsets);
+/* create_neighbor_list(atom, neighbors, offsets), PyInterface.f90:528-546, for all
+ * atoms at once: install lists built elsewhere (ASE's list for small cells). */
+int pg_create_neighbor_lists(pg_context* ctx, const int32_t* counts, const int32_t* neighbors,
+                             const int32_t* offsets, double skin);
+
+/* calculate_energy(energy), PyInterface.f90:652-660 */
+int pg_calculate_energy(pg_context* ctx, int32_t precision, double* energy);
+/* calculate_forces(n_atoms, forces, stress), PyInterface.f90:668-677 */
+int pg_calculate_forces(pg_context* ctx, int32_t precision, double* forces, double* stress);
+/* calculate_electronegativities(n_atoms, enegs), PyInterface.f90:684-692 */
+int pg_calculate_electronegativities(pg_context* ctx, int32_t precision, double* enegs);
+/* One fused evaluation of any of energy, forces + virial and electronegativities
+ * (flags: PG_WANT_*).  The reference needs one full pass per quantity
+ * (calculator.py:940, 968).  Null output pointers are skipped. */
+int pg_calculate(pg_context* ctx, int32_t precision, int32_t flags, double* energy, double* forces,
+                 double* stress, double* enegs);
+
+/* Damped charge dynamics of ChargeRelaxation 'dynamic' (pysic/charges/relaxation.py:417-450)
+ * run on the device: the loop calls the electronegativity kernels without host
+ * round trips.  rates (q-dot) is read and written back so that successive calls
+ * warm-start like the reference's persistent charge_rates (relaxation.py:431-432).
+ * The stopping test is the reference's: max(chi - mean(chi)) < tolerance (signed
+ * max, relaxation.py:449) or step count reached.  On return charges holds the
+ * relaxed charges, *steps the steps taken, *error the final signed max and
+ * *max_dq the largest |q change| of the last step. */
+int pg_relax_charges(pg_context* ctx, int32_t precision, int32_t n_steps, double timestep, double inertia,
+                     double friction, double tolerance, double* rates, double* charges, int32_t* steps,
+                     double* error, double* max_dq);
+
+/* Per ordered bond (CSR entry of the engine's short list) Tersoff sums zeta_ij of
+ * group 0: the quantity core_calculate_pair_bond_order_factor (Core.f90:2439-2637)
+ * accumulates.  Diagnostic; n_entries receives the short-list length. */
+int pg_get_bond_zeta(pg_context* ctx, double* zeta, int64_t capacity, int64_t* n_entries);
+
+/* Tile size of the bond-order kernels: lanes per atom (4, 8, 16 or 32); 0 lets the
+ * built-in autotuner choose on the next evaluation. */
+int pg_set_lanes_per_atom(pg_context* ctx, int32_t lanes);
+int pg_get_lanes_per_atom(pg_context* ctx, int32_t* lanes);
+
+/* ---- device-resident evaluation (benchmarks, MD drivers) ----------------
+ * pg_device_evaluate launches one evaluation on the context's stream using the
+ * positions and charges already on the device and leaves energy, virial, forces
+ * and electronegativities in device memory; pg_device_results copies them out.
+ * pg_device_positions exposes the device position buffer (N x 3 doubles) so a
+ * caller can update it in place. */
+int pg_device_evaluate(pg_context* ctx, int32_t precision, int32_t flags);
+int pg_device_synchronize(pg_context* ctx);
+int pg_device_results(pg_context* ctx, double* energy, double* forces, double* stress, double* enegs);
+int pg_device_positions(pg_context* ctx, double** device_ptr);
+/* The CUDA stream the context launches on (cudaStream_t as void*). */
+int pg_get_stream(pg_context* ctx, void** stream);
+/* Kernel launches issued by the last pg_device_evaluate / pg_calculate. */
+int pg_last_launch_count(pg_context* ctx, int32_t* launches);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

@@ -1,0 +1,1024 @@
+/*
+ * oracle.c -- FP64 CPU restatement of the Pysic Fortran core.
+ *
+ * TEST INFRASTRUCTURE: this file is the parity oracle.  Only tests/,
+ * __graft_entry__.smoke() and bench.py's cpu_baseline / reference leg load it,
+ * and only to check or time the reference algorithm; the product library
+ * never links it.
+ *
+ * Each function follows the reference routine named in its comment, keeping
+ * the reference's loop order and the left-to-right order of its floating-point
+ * expressions, so that for one thread the results reproduce the reference's
+ * arithmetic on a compiler that does not fuse multiply-adds (the recipe in
+ * oracle/Makefile builds with -ffp-contract=off).  Paths are relative to the
+ * Pysic project root.
+ */
+#include "oracle.h"
+
+#include <math.h>
+#include <pthread.h>
+#include <stdlib.h>
+#include <string.h>
+
+/* Utility.f90:11 */
+static const double PI = 3.14159265358979323846;
+
+/* ------------------------------------------------------------------ */
+/* Geometry (fortran/Geometry.f90)                                      */
+/* ------------------------------------------------------------------ */
+
+typedef struct {
+    double vc[3][3];  /* cell%vectors(r,c): component r of cell vector c      */
+    double ic[3][3];  /* cell%inverse_cell(r,c)                               */
+    double rc[3][3];  /* cell%reciprocal_cell(r,c) = 2 pi inverse(c,r)        */
+    double volume;
+    int pbc[3];
+} fcell;
+
+/* generate_supercell, Geometry.f90:177-195 (with the Python-side transposes of
+ * pysic/calculator.py:1555-1565: vectors = cell^T, inverse = inv(cell)^T). */
+static void make_cell(const orc_system* s, fcell* C) {
+    for (int r = 0; r < 3; ++r)
+        for (int c = 0; c < 3; ++c) {
+            C->vc[r][c] = s->cell[c * 3 + r];
+            C->ic[r][c] = s->inv[c * 3 + r];
+        }
+    const double twopi = 2.0 * PI;
+    for (int r = 0; r < 3; ++r)
+        for (int c = 0; c < 3; ++c) C->rc[r][c] = twopi * C->ic[c][r];
+    /* volume = |(v1 x v2) . v3|, Geometry.f90:192 with Quaternions.f90:475-500 */
+    double a[3], b[3], d[3];
+    for (int r = 0; r < 3; ++r) {
+        a[r] = C->vc[r][0];
+        b[r] = C->vc[r][1];
+        d[r] = C->vc[r][2];
+    }
+    double x0 = a[1] * b[2] - a[2] * b[1];
+    double x1 = a[2] * b[0] - a[0] * b[2];
+    double x2 = a[0] * b[1] - a[1] * b[0];
+    C->volume = fabs(x0 * d[0] + x1 * d[1] + x2 * d[2]);
+    for (int i = 0; i < 3; ++i) C->pbc[i] = s->pbc[i] != 0;
+}
+
+/* relative_coordinates, Geometry.f90:510-519 (matmul, summed over c in order) */
+static void rel_coords(const fcell* C, const double p[3], double rel[3]) {
+    for (int r = 0; r < 3; ++r) rel[r] = C->ic[r][0] * p[0] + C->ic[r][1] * p[1] + C->ic[r][2] * p[2];
+}
+
+/* absolute_coordinates, Geometry.f90:531-540 */
+static void abs_coords(const fcell* C, const double rel[3], double p[3]) {
+    for (int r = 0; r < 3; ++r) p[r] = C->vc[r][0] * rel[0] + C->vc[r][1] * rel[1] + C->vc[r][2] * rel[2];
+}
+
+/* wrapped_coordinates, Geometry.f90:597-619 */
+static void wrapped_coords(const fcell* C, const double p[3], double w[3], int off[3]) {
+    double rel[3];
+    rel_coords(C, p, rel);
+    for (int i = 0; i < 3; ++i) {
+        off[i] = 0;
+        if (C->pbc[i]) {
+            off[i] = -(int)floor(rel[i]);
+            rel[i] = rel[i] + (double)off[i];
+        }
+    }
+    abs_coords(C, rel, w);
+}
+
+/* separation_vector, Geometry.f90:449-466 */
+static void separation(const fcell* C, const double* r1, const double* r2, const int off[3], double s[3]) {
+    for (int c = 0; c < 3; ++c) s[c] = r2[c] - r1[c];
+    for (int i = 0; i < 3; ++i)
+        for (int c = 0; c < 3; ++c) s[c] = s[c] + (double)off[i] * C->vc[c][i];
+}
+
+/* .o. dot product, Quaternions.f90:475-484 */
+static inline double dot3(const double a[3], const double b[3]) { return a[0] * b[0] + a[1] * b[1] + a[2] * b[2]; }
+
+/* pick, Geometry.f90:648-676 */
+static int pick(int i1, int i2, const int off[3]) {
+    if (i2 > i1) return 1;
+    if (i2 == i1 && off[0] >= 0) {
+        if (off[0] > 0) return 1;
+        if (off[1] > 0) return 1;
+        if (off[1] == 0 && off[2] > 0) return 1;
+    }
+    return 0;
+}
+
+/* get_optimal_splitting, Geometry.f90:679-707 */
+static void optimal_splitting(const fcell* C, double max_cut, int splits[3]) {
+    for (int i = 0; i < 3; ++i) {
+        int v1 = (i + 1) % 3, v2 = (i + 2) % 3;
+        double a[3], b[3], n[3], v[3];
+        for (int r = 0; r < 3; ++r) {
+            a[r] = C->vc[r][v1];
+            b[r] = C->vc[r][v2];
+            v[r] = C->vc[r][i];
+        }
+        n[0] = a[1] * b[2] - a[2] * b[1];
+        n[1] = a[2] * b[0] - a[0] * b[2];
+        n[2] = a[0] * b[1] - a[1] * b[0];
+        double length = fabs(dot3(v, n)) / sqrt(dot3(n, n));
+        if (max_cut < 0.1e-4)
+            splits[i] = (int)floor(10.0 * length);
+        else
+            splits[i] = (int)floor(length / max_cut);
+        if (splits[i] > 40) splits[i] = 40;
+    }
+}
+
+typedef struct {
+    int* atoms;
+    int n, cap;
+} ivec;
+
+static void ivec_push(ivec* v, int x) {
+    if (v->n == v->cap) {
+        v->cap = v->cap ? 2 * v->cap : 16;
+        v->atoms = (int*)realloc(v->atoms, sizeof(int) * (size_t)v->cap);
+    }
+    v->atoms[v->n++] = x;
+}
+
+typedef struct {
+    int* data; /* 4 ints per entry: neighbour, offset x3 */
+    int n, cap;
+} nbvec;
+
+static void nbvec_push(nbvec* v, int j, const int o[3]) {
+    if (v->n == v->cap) {
+        v->cap = v->cap ? 2 * v->cap : 32;
+        v->data = (int*)realloc(v->data, sizeof(int) * 4 * (size_t)v->cap);
+    }
+    int* d = v->data + 4 * (size_t)v->n;
+    d[0] = j;
+    d[1] = o[0];
+    d[2] = o[1];
+    d[3] = o[2];
+    v->n++;
+}
+
+/* generate_neighbor_lists (PyInterface.f90:1062-1072) ->
+ * core_create_space_partitioning (Core.f90:8130-8141): get_optimal_splitting,
+ * divide_cell (Geometry.f90:751-865), find_subcell_for_atom (Geometry.f90:884-924) ->
+ * core_build_neighbor_lists (Core.f90:8148-8280). */
+int64_t orc_build_neighbors(const orc_system* s, const double* cutoffs, int32_t* counts, int32_t* out_idx,
+                            int32_t* out_off, int64_t cap) {
+    const int n = s->n;
+    if (n < 0) return -1;
+    fcell C;
+    make_cell(s, &C);
+    double max_cut = 0.0;
+    for (int i = 0; i < n; ++i)
+        if (i == 0 || cutoffs[i] > max_cut) max_cut = cutoffs[i];
+    int sp[3];
+    optimal_splitting(&C, max_cut, sp);
+    for (int a = 0; a < 3; ++a)
+        if (sp[a] < 1) return -1; /* the Python layer never builds the fast list then */
+    const int nx = sp[0] + 2, ny = sp[1] + 2, nz = sp[2] + 2;
+    const size_t ncell = (size_t)nx * ny * nz;
+    ivec* cells = (ivec*)calloc(ncell, sizeof(ivec));
+    int* cell_of = (int*)malloc(sizeof(int) * 3 * (size_t)(n > 0 ? n : 1));
+    int* wrap = (int*)malloc(sizeof(int) * 3 * (size_t)(n > 0 ? n : 1));
+    /* find_subcell_for_atom for atoms 1..n in order */
+    for (int i = 0; i < n; ++i) {
+        double w[3], f[3];
+        int off[3];
+        wrapped_coords(&C, s->pos + 3 * (size_t)i, w, off);
+        for (int a = 0; a < 3; ++a) wrap[3 * i + a] = off[a];
+        rel_coords(&C, w, f);
+        for (int a = 0; a < 3; ++a) {
+            int k = (int)floor(f[a] * (double)sp[a]);
+            int idx;
+            if (C.pbc[a]) {
+                idx = k % sp[a] + 1; /* Fortran mod: sign of the dividend */
+            } else {
+                idx = k + 1;
+                if (idx < 0) idx = 0;
+                if (idx > sp[a] + 1) idx = sp[a] + 1;
+            }
+            cell_of[3 * i + a] = idx;
+        }
+        ivec_push(&cells[((size_t)cell_of[3 * i + 2] * ny + cell_of[3 * i + 1]) * nx + cell_of[3 * i]], i);
+    }
+    nbvec* lists = (nbvec*)calloc((size_t)(n > 0 ? n : 1), sizeof(nbvec));
+    for (int i1 = 0; i1 < n; ++i1) {
+        const int* ci = cell_of + 3 * i1;
+        const int* w1 = wrap + 3 * i1;
+        for (int kn = -1; kn <= 1; ++kn)
+            for (int jn = -1; jn <= 1; ++jn)
+                for (int in = -1; in <= 1; ++in) {
+                    /* divide_cell neighbour map, Geometry.f90:820-858 */
+                    int nb[3] = {ci[0] + in, ci[1] + jn, ci[2] + kn};
+                    int noff[3] = {0, 0, 0};
+                    int include = 1;
+                    for (int a = 0; a < 3; ++a) {
+                        if (C.pbc[a]) {
+                            while (nb[a] > sp[a]) {
+                                nb[a] -= sp[a];
+                                noff[a] += 1;
+                            }
+                            while (nb[a] < 1) {
+                                nb[a] += sp[a];
+                                noff[a] -= 1;
+                            }
+                        } else if (nb[a] < 0 || nb[a] > sp[a] + 1) {
+                            include = 0;
+                            nb[a] = 0;
+                        }
+                    }
+                    if (!include) continue;
+                    const ivec* cl = &cells[((size_t)nb[2] * ny + nb[1]) * nx + nb[0]];
+                    for (int t = 0; t < cl->n; ++t) {
+                        const int i2 = cl->atoms[t];
+                        const int* w2 = wrap + 3 * i2;
+                        if (!pick(i1, i2, noff)) continue;
+                        int o[3], mo[3];
+                        for (int a = 0; a < 3; ++a) {
+                            o[a] = noff[a] - w1[a] + w2[a];
+                            mo[a] = -noff[a] + w1[a] - w2[a];
+                        }
+                        double sep[3];
+                        separation(&C, s->pos + 3 * (size_t)i1, s->pos + 3 * (size_t)i2, o, sep);
+                        double d2 = dot3(sep, sep);
+                        if (d2 < cutoffs[i1] * cutoffs[i1]) nbvec_push(&lists[i1], i2, o);
+                        if (d2 < cutoffs[i2] * cutoffs[i2]) nbvec_push(&lists[i2], i1, mo);
+                    }
+                }
+    }
+    int64_t total = 0;
+    for (int i = 0; i < n; ++i) {
+        counts[i] = lists[i].n;
+        total += lists[i].n;
+    }
+    if (out_idx && out_off && cap >= total) {
+        int64_t p = 0;
+        for (int i = 0; i < n; ++i)
+            for (int e = 0; e < lists[i].n; ++e, ++p) {
+                const int* d = lists[i].data + 4 * (size_t)e;
+                out_idx[p] = d[0];
+                out_off[3 * p] = d[1];
+                out_off[3 * p + 1] = d[2];
+                out_off[3 * p + 2] = d[3];
+            }
+    }
+    for (size_t c = 0; c < ncell; ++c) free(cells[c].atoms);
+    for (int i = 0; i < n; ++i) free(lists[i].data);
+    free(cells);
+    free(lists);
+    free(cell_of);
+    free(wrap);
+    return total;
+}
+
+/* ------------------------------------------------------------------ */
+/* Evaluators (fortran/Potentials.f90)                                  */
+/* ------------------------------------------------------------------ */
+
+/* smoothening_factor, Potentials.f90:442-457 */
+static double smooth_factor(double r, double hard, double soft) {
+    if (r > hard) return 0.0;
+    if (r < soft) return 1.0;
+    return 0.5 * (1.0 + cos(PI * (r - soft) / (hard - soft)));
+}
+
+/* smoothening_derivative, Potentials.f90:483-498 */
+static double smooth_deriv(double r, double hard, double soft) {
+    if (r > hard) return 0.0;
+    if (r < soft) return 0.0;
+    return -(0.5 * PI / (hard - soft) * sin(PI * (r - soft) / (hard - soft)));
+}
+
+/* evaluate_energy_LJ (2990-3005), _exp (3665-3680), _buckingham (4030-4045) */
+static double pair_energy(int kind, const double* p, double r1) {
+    if (kind == 0) {
+        double ratio = p[1] / r1;
+        double r6 = ratio * ratio * ratio * ratio * ratio * ratio;
+        return p[0] * (r6 * r6 - r6);
+    } else if (kind == 1) {
+        return p[0] * exp(-(p[1] * r1));
+    } else {
+        double ratio = r1 / p[2];
+        double r6 = 1.0 / (ratio * ratio * ratio * ratio * ratio * ratio);
+        return p[0] * exp(-ratio) - p[1] * r6;
+    }
+}
+
+/* evaluate_force_LJ (2971-2983), _exp (3643-3655), _buckingham (4009-4022): force on atom 1 */
+static void pair_force(int kind, const double* p, const double sep[3], double r1, double f[3]) {
+    if (kind == 0) {
+        double ratio = p[1] / r1;
+        double r6 = ratio * ratio * ratio * ratio * ratio * ratio;
+        double pre = p[0] * (6.0 * r6 - 12.0 * r6 * r6);
+        for (int c = 0; c < 3; ++c) f[c] = pre * sep[c] / (r1 * r1);
+    } else if (kind == 1) {
+        double pre = p[1] * p[0] * exp(-(p[1] * r1));
+        for (int c = 0; c < 3; ++c) f[c] = -(pre * sep[c] / r1);
+    } else {
+        double ratio = r1 / p[2];
+        double r6 = 1.0 / (ratio * ratio * ratio * ratio * ratio * ratio);
+        double pre = -p[0] * ratio * exp(-ratio) + p[1] * 6.0 * r6;
+        for (int c = 0; c < 3; ++c) f[c] = pre * sep[c] / (r1 * r1);
+    }
+}
+
+/* evaluate_pair_bond_order_factor_tersoff, Potentials.f90:5744-5795.
+ * sep1 = separations(:,1), sep2 = separations(:,2) */
+static double tersoff_factor(const double* bp, double cut, double soft, const double sep1[3], const double sep2[3],
+                             double r1, double r2) {
+    double t1[3] = {-sep1[0], -sep1[1], -sep1[2]};
+    double cosine = dot3(t1, sep2) / (r1 * r2);
+    double mu = bp[6], a1 = bp[2], cc1 = bp[3] * bp[3], dd1 = bp[4] * bp[4], h1 = bp[5];
+    double decay1 = smooth_factor(r2, cut, soft);
+    double xi1 = decay1 * exp(pow(a1 * (r1 - r2), mu));
+    double gee1 = 1.0 + cc1 / dd1 - cc1 / (dd1 + (h1 - cosine) * (h1 - cosine));
+    return xi1 * gee1;
+}
+
+/* evaluate_pair_bond_order_gradient_tersoff, Potentials.f90:5806-5902.
+ * g[a][c]: component c of the gradient with respect to atom a (a = 0: atoms(1),
+ * 1: atoms(2) the centre, 2: atoms(3)). */
+static void tersoff_gradient(const double* bp, double cut, double soft, const double sep1[3], const double sep2[3],
+                             double r1, double r2, double g[3][3]) {
+    double t1[3], t2[3], u1[3], u2[3];
+    for (int c = 0; c < 3; ++c) {
+        t1[c] = -sep1[c];
+        t2[c] = sep2[c];
+        u1[c] = t1[c] / r1;
+        u2[c] = t2[c] / r2;
+    }
+    double dot = dot3(t1, t2);
+    double ratio = 1.0 / (r1 * r2);
+    double cosine = dot * ratio;
+    double nr1[3][3] = {{0}}, nr2[3][3] = {{0}}, nc[3][3], tm2[3][3] = {{0}};
+    double t3[3], t4[3];
+    for (int c = 0; c < 3; ++c) {
+        nr1[1][c] = -u1[c];
+        nr1[0][c] = u1[c];
+        nr2[1][c] = -u2[c];
+        nr2[2][c] = u2[c];
+        t3[c] = t2[c] - dot / (r1 * r1) * t1[c];
+        t4[c] = t1[c] - dot / (r2 * r2) * t2[c];
+    }
+    for (int c = 0; c < 3; ++c) {
+        nc[0][c] = t3[c] * ratio;
+        nc[1][c] = -(t3[c] + t4[c]) * ratio;
+        nc[2][c] = t4[c] * ratio;
+    }
+    double mu = bp[6], a1 = bp[2], cc1 = bp[3] * bp[3], dd1 = bp[4] * bp[4], h1 = bp[5];
+    double decay1 = smooth_factor(r2, cut, soft);
+    double dfac = smooth_deriv(r2, cut, soft);
+    double t6[3] = {u2[0] * dfac, u2[1] * dfac, u2[2] * dfac};
+    for (int c = 0; c < 3; ++c) {
+        tm2[1][c] = -t6[c];
+        tm2[2][c] = t6[c];
+    }
+    double e1a = pow(a1 * (r1 - r2), mu - 1.0);
+    double e1b = a1 * (r1 - r2) * e1a;
+    double xi1 = exp(e1b);
+    double hc = h1 - cosine;
+    double gee1 = 1.0 + cc1 / dd1 - cc1 / (dd1 + hc * hc);
+    double sc = decay1 * (exp(e1b) * a1 * mu * e1a);
+    double nxi[3][3], ng[3][3];
+    for (int a = 0; a < 3; ++a)
+        for (int c = 0; c < 3; ++c) nxi[a][c] = tm2[a][c] * xi1 + sc * (nr1[a][c] - nr2[a][c]);
+    xi1 = xi1 * decay1;
+    double X = dd1 + hc * hc;
+    double pre = -(cc1 / (X * X) * 2.0 * hc);
+    for (int a = 0; a < 3; ++a)
+        for (int c = 0; c < 3; ++c) ng[a][c] = pre * nc[a][c];
+    for (int a = 0; a < 3; ++a)
+        for (int c = 0; c < 3; ++c) g[a][c] = nxi[a][c] * gee1 + xi1 * ng[a][c];
+}
+
+/* post_process_bond_order_factor_tersoff, Potentials.f90:5910-5921 */
+static double tersoff_post(const double* bp, double raw) {
+    double beta = bp[0], eta = bp[1];
+    return pow(1.0 + pow(beta * raw, eta), -1.0 / (2.0 * eta));
+}
+
+/* post_process_bond_order_gradient_tersoff, Potentials.f90:5929-5961 (scalar
+ * part: the routine multiplies its raw_gradient argument by this value). */
+static double tersoff_post_grad_scale(const double* bp, double raw, double g) {
+    double beta = bp[0], eta = bp[1];
+    if (eta == 0.0) return 0.0;
+    if (raw == 0.0 && eta <= 1.0) return 0.0;
+    double inv_eta = -1.0 / (2.0 * eta);
+    return inv_eta * pow(1.0 + pow(beta * raw, eta), inv_eta - 1.0) * eta * pow(beta * raw, eta - 1.0) * beta * g;
+}
+
+/* ------------------------------------------------------------------ */
+/* Core loop (fortran/Core.f90)                                         */
+/* ------------------------------------------------------------------ */
+
+typedef struct {
+    const orc_system* s;
+    const orc_model* m;
+    const orc_nblist* nb;
+    fcell C;
+    double* maxbr; /* per atom: max_bond_radius, Core.f90:1030-1067 */
+    double* smooth_soft;
+    int* smoothened;
+} ctx_t;
+
+static inline int has(uint64_t mask, int t) { return (int)((mask >> t) & 1u); }
+
+/* first post-processing factor of the atom's element in the group:
+ * core_post_process_pair_bond_order_factor, Core.f90:2763-2807 */
+static int post_index(const ctx_t* X, int t, int group) {
+    const orc_model* m = X->m;
+    for (int b = 0; b < m->n_bond; ++b)
+        if (has(m->bond_mask1[b], t) && m->bond_group[b] == group) return b;
+    return -1;
+}
+
+/* core_calculate_pair_bond_order_factor, Core.f90:2439-2637 */
+static void pair_bo_sums(const ctx_t* X, int i, int j, const double sep[3], double d, int group, double sums[2]) {
+    const orc_system* s = X->s;
+    const orc_model* m = X->m;
+    const orc_nblist* nb = X->nb;
+    sums[0] = sums[1] = 0.0;
+    double s1[3] = {-sep[0], -sep[1], -sep[2]};
+    for (int pass = 0; pass < 2; ++pass) {
+        const int c = pass == 0 ? i : j;     /* centre */
+        const int o = pass == 0 ? j : i;     /* other end of the bond */
+        if (pass == 1)
+            for (int q = 0; q < 3; ++q) s1[q] = sep[q];
+        const int tc = s->type[c], to = s->type[o];
+        for (int e = nb->start[c]; e < nb->start[c + 1]; ++e) {
+            const int k = nb->idx[e];
+            double s2[3];
+            separation(&X->C, s->pos + 3 * (size_t)c, s->pos + 3 * (size_t)k, nb->off + 3 * (size_t)e, s2);
+            double d2 = sqrt(dot3(s2, s2));
+            if (!(s1[0] + s2[0] != 0.0 || s1[1] + s2[1] != 0.0 || s1[2] + s2[2] != 0.0)) continue;
+            if (!(d2 < X->maxbr[c])) continue;
+            const int tk = s->type[k];
+            for (int b = 0; b < m->n_bond; ++b) {
+                if (!has(m->bond_mask1[b], tc) || m->bond_group[b] != group) continue;
+                if (!has(m->bond_mask2[b], to)) continue;
+                if (!has(m->bond_mask3[b], tk)) continue;
+                sums[pass] += tersoff_factor(m->bond_params + 7 * (size_t)b, m->bond_cutoff[b], m->bond_soft[b], s1,
+                                             s2, d, d2);
+            }
+        }
+    }
+}
+
+/* core_add_pair_bond_order_forces, Core.f90:4952-5353 */
+static void pair_bo_forces(const ctx_t* X, int i, int j, double prefactor, const double sep[3], double d, int group,
+                           const double sums[2], double* F, double* stress) {
+    const orc_system* s = X->s;
+    const orc_model* m = X->m;
+    const orc_nblist* nb = X->nb;
+    double virial[2][6] = {{0}};
+    int pp[2];
+    double pf[2] = {0, 0};
+    pp[0] = post_index(X, s->type[i], group);
+    pp[1] = post_index(X, s->type[j], group);
+    for (int q = 0; q < 2; ++q)
+        if (pp[q] >= 0) pf[q] = tersoff_post_grad_scale(m->bond_params + 7 * (size_t)pp[q], sums[q], 1.0);
+    double s1[3] = {-sep[0], -sep[1], -sep[2]};
+    for (int pass = 0; pass < 2; ++pass) {
+        const int c = pass == 0 ? i : j;
+        const int o = pass == 0 ? j : i;
+        if (pass == 1)
+            for (int q = 0; q < 3; ++q) s1[q] = sep[q];
+        const int tc = s->type[c], to = s->type[o];
+        for (int e = nb->start[c]; e < nb->start[c + 1]; ++e) {
+            const int k = nb->idx[e];
+            double s2[3];
+            separation(&X->C, s->pos + 3 * (size_t)c, s->pos + 3 * (size_t)k, nb->off + 3 * (size_t)e, s2);
+            double d2 = sqrt(dot3(s2, s2));
+            if (!(s1[0] + s2[0] != 0.0 || s1[1] + s2[1] != 0.0 || s1[2] + s2[2] != 0.0)) continue;
+            if (!(d2 < X->maxbr[c])) continue;
+            const int tk = s->type[k];
+            for (int b = 0; b < m->n_bond; ++b) {
+                if (!has(m->bond_mask1[b], tc) || m->bond_group[b] != group) continue;
+                if (!has(m->bond_mask2[b], to)) continue;
+                if (!has(m->bond_mask3[b], tk)) continue;
+                double g[3][3], ng[3][3];
+                tersoff_gradient(m->bond_params + 7 * (size_t)b, m->bond_cutoff[b], m->bond_soft[b], s1, s2, d, d2, g);
+                for (int a = 0; a < 3; ++a)
+                    for (int q = 0; q < 3; ++q)
+                        ng[a][q] = pp[pass] >= 0 ? -(pf[pass] * prefactor * g[a][q]) : -(prefactor * g[a][q]);
+                for (int q = 0; q < 3; ++q) {
+                    F[3 * (size_t)o + q] += ng[0][q];
+                    F[3 * (size_t)c + q] += ng[1][q];
+                    F[3 * (size_t)k + q] += ng[2][q];
+                }
+                double* v = virial[pass];
+                v[0] = v[0] - s1[0] * g[0][0] + s2[0] * g[2][0];
+                v[1] = v[1] - s1[1] * g[0][1] + s2[1] * g[2][1];
+                v[2] = v[2] - s1[2] * g[0][2] + s2[2] * g[2][2];
+                v[3] = v[3] - s1[1] * g[0][2] + s2[1] * g[2][2];
+                v[4] = v[4] - s1[0] * g[0][2] + s2[0] * g[2][2];
+                v[5] = v[5] - s1[0] * g[0][1] + s2[0] * g[2][1];
+            }
+        }
+    }
+    double tv[2][6];
+    for (int q = 0; q < 2; ++q)
+        for (int c = 0; c < 6; ++c)
+            tv[q][c] = pp[q] >= 0 ? tersoff_post_grad_scale(m->bond_params + 7 * (size_t)pp[q], sums[q], virial[q][c])
+                                  : virial[q][c];
+    for (int c = 0; c < 6; ++c) stress[c] = stress[c] - prefactor * (tv[0][c] + tv[1][c]);
+}
+
+static double post_process(const ctx_t* X, int t, int group, double raw) {
+    int b = post_index(X, t, group);
+    if (b < 0) return raw;
+    return tersoff_post(X->m->bond_params + 7 * (size_t)b, raw);
+}
+
+typedef struct {
+    const ctx_t* X;
+    int what, a0, a1;
+    double energy;
+    double stress[6];
+    double* F;     /* per-thread n x 3 */
+    double* chi;   /* per-thread n */
+} loop_job;
+
+/* The per-atom body of core_loop_over_local_interactions, Core.f90:3249-3946,
+ * for atoms [a0, a1). Singlets: core_evaluate_local_singlet (4095-4239);
+ * inline Ewald real space (3416-3460); doublets: core_evaluate_local_doublet_
+ * energy_B (4257-4385) and _forces_B (5371-5606). */
+static void* loop_range(void* arg) {
+    loop_job* J = (loop_job*)arg;
+    const ctx_t* X = J->X;
+    const orc_system* s = X->s;
+    const orc_model* m = X->m;
+    const orc_nblist* nb = X->nb;
+    const double eps = m->ewald_eps, sig = m->ewald_sigma;
+    const double inv_eps_4pi = 1.0 / (4.0 * PI * eps);
+    const double inv_sigma_sqrt_2 = 1.0 / (sqrt(2.0) * sig);
+    const double inv_sigma_sqrt_2pi = 1.0 / (sqrt(2.0 * PI) * sig);
+    const double inv_sigma_sq_2 = inv_sigma_sqrt_2 * inv_sigma_sqrt_2;
+    const double inv_sigma_sqrt_2perpi = 2.0 * inv_sigma_sqrt_2pi;
+    double* F = J->F;
+    double* chi = J->chi;
+    double* st = J->stress;
+    for (int i = J->a0; i < J->a1; ++i) {
+        const int ti = s->type[i];
+        const double qi = s->charge[i];
+        for (int r = 0; r < m->n_single; ++r) {
+            if (!has(m->single_mask[r], ti)) continue;
+            const double* p = m->single_params + 2 * (size_t)r;
+            int n = (int)p[1];
+            if (J->what == 0) J->energy += p[0] * __builtin_powi(qi, n);
+            else if (J->what == 2) chi[i] += -(p[0] * n * __builtin_powi(qi, n - 1));
+        }
+        for (int e = nb->start[i]; e < nb->start[i + 1]; ++e) {
+            const int j = nb->idx[e];
+            const int* o = nb->off + 3 * (size_t)e;
+            if (!pick(i, j, o)) continue;
+            const int tj = s->type[j];
+            double sep[3];
+            separation(&X->C, s->pos + 3 * (size_t)i, s->pos + 3 * (size_t)j, o, sep);
+            double d = sqrt(dot3(sep, sep));
+            double dir[3] = {0, 0, 0};
+            if (d != 0.0)
+                for (int c = 0; c < 3; ++c) dir[c] = sep[c] / d;
+            if (m->ewald && d < m->ewald_rc) {
+                const double q1 = qi, q2 = s->charge[j];
+                if (J->what == 0) {
+                    J->energy += q1 * q2 * (1.0 - erf(d * inv_sigma_sqrt_2)) / d * inv_eps_4pi;
+                } else if (J->what == 1) {
+                    double inv_dist = 1.0 / d;
+                    double pre = -(inv_eps_4pi * q1 * q2 *
+                                   ((1.0 - erf(d * inv_sigma_sqrt_2)) * inv_dist * inv_dist +
+                                    inv_sigma_sqrt_2perpi * exp(-(d * d * inv_sigma_sq_2)) * inv_dist));
+                    double tf[3];
+                    for (int c = 0; c < 3; ++c) tf[c] = pre * sep[c] * inv_dist;
+                    for (int c = 0; c < 3; ++c) {
+                        F[3 * (size_t)i + c] += tf[c];
+                        F[3 * (size_t)j + c] -= tf[c];
+                    }
+                    st[0] -= sep[0] * tf[0];
+                    st[1] -= sep[1] * tf[1];
+                    st[2] -= sep[2] * tf[2];
+                    st[3] -= sep[1] * tf[2];
+                    st[4] -= sep[0] * tf[2];
+                    st[5] -= sep[0] * tf[1];
+                } else {
+                    double tmp = -(inv_eps_4pi / d * (1.0 - erf(d * inv_sigma_sqrt_2)));
+                    chi[i] += q2 * tmp;
+                    chi[j] += q1 * tmp;
+                }
+            }
+            if (J->what == 2) continue; /* non-charge pair potentials have zero electronegativity */
+            for (int r = 0; r < m->n_pair; ++r) {
+                if (!has(m->pair_mask1[r], ti)) continue;
+                if (!(m->pair_cutoff[r] > d)) continue;
+                if (!has(m->pair_mask2[r], tj)) continue;
+                const int kind = m->pair_kind[r];
+                const double* p = m->pair_params + 4 * (size_t)r;
+                const int grp = m->pair_group[r];
+                const int sm = X->smoothened[r];
+                const double rc = m->pair_cutoff[r], rs = X->smooth_soft[r];
+                if (J->what == 0) {
+                    double B1 = 0, B2 = 0;
+                    if (grp >= 0) {
+                        double sums[2];
+                        pair_bo_sums(X, i, j, sep, d, grp, sums);
+                        B1 = post_process(X, ti, grp, sums[0]);
+                        B2 = post_process(X, tj, grp, sums[1]);
+                    }
+                    double cut = sm ? smooth_factor(d, rc, rs) : 1.0;
+                    double v = pair_energy(kind, p, d);
+                    if (grp >= 0) J->energy += v * cut * (0.0 + 0.0 + B1 + B2) * 0.5;
+                    else J->energy += v * cut;
+                } else {
+                    double v = (grp >= 0 || sm) ? pair_energy(kind, p, d) : 0.0;
+                    double cut = 1.0, cg[3] = {0, 0, 0};
+                    if (sm) {
+                        cut = smooth_factor(d, rc, rs);
+                        double dv = smooth_deriv(d, rc, rs);
+                        for (int c = 0; c < 3; ++c) cg[c] = dir[c] * dv;
+                    }
+                    double B1 = 0, B2 = 0;
+                    if (grp >= 0) {
+                        double sums[2];
+                        pair_bo_sums(X, i, j, sep, d, grp, sums);
+                        B1 = post_process(X, ti, grp, sums[0]);
+                        B2 = post_process(X, tj, grp, sums[1]);
+                        pair_bo_forces(X, i, j, 0.5 * v * cut, sep, d, grp, sums, F, st);
+                    }
+                    double f1[3], p1[3], p2[3];
+                    pair_force(kind, p, sep, d, f1);
+                    for (int c = 0; c < 3; ++c) {
+                        if (grp >= 0) {
+                            double bsum = (0.0 + 0.0 + B1 + B2) * 0.5;
+                            p1[c] = (f1[c] * cut + v * cg[c]) * bsum;
+                            p2[c] = (-f1[c] * cut - v * cg[c]) * bsum;
+                        } else {
+                            p1[c] = f1[c] * cut + v * cg[c];
+                            p2[c] = -f1[c] * cut - v * cg[c];
+                        }
+                    }
+                    for (int c = 0; c < 3; ++c) {
+                        F[3 * (size_t)i + c] += p1[c];
+                        F[3 * (size_t)j + c] += p2[c];
+                    }
+                    st[0] += sep[0] * p2[0];
+                    st[1] += sep[1] * p2[1];
+                    st[2] += sep[2] * p2[2];
+                    st[3] += sep[1] * p2[2];
+                    st[4] += sep[0] * p2[2];
+                    st[5] += sep[0] * p2[1];
+                }
+            }
+        }
+    }
+    return NULL;
+}
+
+/* k-space Ewald: calculate_ewald_energy (Potentials.f90:1428-1653),
+ * calculate_ewald_forces (1675-1971), calculate_ewald_electronegativities
+ * (1992-2249), all with include_realspace = .false. and no dipole correction
+ * (Core.f90:3983-4060). */
+typedef struct {
+    const ctx_t* X;
+    int what, a0, a1, nk;
+    const double* kv;   /* 4 per listed k: kx, ky, kz, weight flag (k3 == 0 ? 1 : 2) */
+    double* S;          /* 2 per k (per-thread partial) */
+    double e2, e4;
+} sk_job;
+
+static void* sk_range(void* arg) {
+    sk_job* J = (sk_job*)arg;
+    const orc_system* s = J->X->s;
+    const orc_model* m = J->X->m;
+    for (int i = J->a0; i < J->a1; ++i) {
+        const double q1 = s->charge[i] * m->ewald_scaler[i];
+        if (J->what != 2 && q1 == 0.0) continue;
+        const double* r = s->pos + 3 * (size_t)i;
+        for (int k = 0; k < J->nk; ++k) {
+            const double* kv = J->kv + 4 * (size_t)k;
+            double dot = kv[0] * r[0] + kv[1] * r[1] + kv[2] * r[2];
+            if (J->what == 0) {
+                double sine = q1 * sin(dot), cosine = q1 * cos(dot);
+                J->S[2 * k] += cosine;
+                J->S[2 * k + 1] += sine;
+            } else {
+                double sn = sin(dot), cs = cos(dot);
+                J->S[2 * k] += q1 * cs;
+                J->S[2 * k + 1] += -(q1 * sn);
+            }
+        }
+        J->e2 += q1 * q1;
+        J->e4 += q1;
+    }
+    return NULL;
+}
+
+typedef struct {
+    const ctx_t* X;
+    int what, a0, a1, nk;
+    const double* kv;
+    const double* S;
+    double* F;
+    double* chi;
+    double stress[6];
+    double qsum;
+} kf_job;
+
+static void* kf_range(void* arg) {
+    kf_job* J = (kf_job*)arg;
+    const orc_system* s = J->X->s;
+    const orc_model* m = J->X->m;
+    const double sig = m->ewald_sigma, eps = m->ewald_eps;
+    const double inv_eps_2v = 1.0 / (2.0 * J->X->C.volume * eps);
+    const double inv_eps_4pi = 1.0 / (4.0 * PI * eps);
+    const double inv_sigma_sqrt_2pi = 1.0 / (sqrt(2.0 * PI) * sig);
+    for (int i = J->a0; i < J->a1; ++i) {
+        const double q1 = s->charge[i] * m->ewald_scaler[i];
+        const double* r = s->pos + 3 * (size_t)i;
+        if (J->what == 1) {
+            double f[3] = {0, 0, 0};
+            for (int k = 0; k < J->nk; ++k) {
+                const double* kv = J->kv + 4 * (size_t)k;
+                double dist = kv[0] * kv[0] + kv[1] * kv[1] + kv[2] * kv[2];
+                double dot = kv[0] * r[0] + kv[1] * r[1] + kv[2] * r[2];
+                double sn = sin(dot), cs = cos(dot);
+                double kq[3] = {q1 * kv[0], q1 * kv[1], q1 * kv[2]};
+                double w = kv[3] == 1.0 ? 2.0 : 4.0;
+                double pre = inv_eps_2v * exp(-(sig * sig * dist * 0.5)) / dist * w;
+                for (int c = 0; c < 3; ++c) {
+                    double nf1 = -sn * kq[c], nf2 = cs * kq[c];
+                    f[c] = f[c] - pre * (J->S[2 * k] * nf1 - J->S[2 * k + 1] * nf2);
+                }
+            }
+            for (int c = 0; c < 3; ++c) J->F[3 * (size_t)i + c] = f[c];
+            J->stress[0] += r[0] * (f[0] + 0.0);
+            J->stress[1] += r[1] * (f[1] + 0.0);
+            J->stress[2] += r[2] * (f[2] + 0.0);
+            J->stress[3] += r[1] * (f[2] + 0.0);
+            J->stress[4] += r[0] * (f[2] + 0.0);
+            J->stress[5] += r[0] * (f[1] + 0.0);
+        } else {
+            double x = J->chi[i] - m->ewald_scaler[i] * inv_eps_2v * (-(sig * sig * J->qsum));
+            for (int k = 0; k < J->nk; ++k) {
+                const double* kv = J->kv + 4 * (size_t)k;
+                double dist = kv[0] * kv[0] + kv[1] * kv[1] + kv[2] * kv[2];
+                double dot = kv[0] * r[0] + kv[1] * r[1] + kv[2] * r[2];
+                double sn = sin(dot), cs = cos(dot);
+                double w = kv[3] == 1.0 ? 2.0 : 4.0;
+                x = x - inv_eps_2v * exp(-(sig * sig * dist * 0.5)) / dist * w * (J->S[2 * k] * cs - J->S[2 * k + 1] * sn);
+            }
+            J->chi[i] = x;
+        }
+        (void)inv_eps_4pi;
+        (void)inv_sigma_sqrt_2pi;
+    }
+    return NULL;
+}
+
+static void run_jobs(void* (*fn)(void*), void* jobs, size_t stride, int threads) {
+    if (threads <= 1) {
+        fn(jobs);
+        return;
+    }
+    pthread_t* th = (pthread_t*)malloc(sizeof(pthread_t) * (size_t)threads);
+    for (int t = 0; t < threads; ++t) pthread_create(&th[t], NULL, fn, (char*)jobs + stride * (size_t)t);
+    for (int t = 0; t < threads; ++t) pthread_join(th[t], NULL);
+    free(th);
+}
+
+/* The listed k vectors in the reference loop order (k1, k2 outer, k3 >= 0 inner). */
+static int list_kvectors(const ctx_t* X, double** out) {
+    const orc_model* m = X->m;
+    const int K1 = m->ewald_kmax[0], K2 = m->ewald_kmax[1], K3 = m->ewald_kmax[2];
+    const double kcsq = m->ewald_kc * m->ewald_kc;
+    size_t cap = (size_t)(2 * K1 + 1) * (2 * K2 + 1) * (K3 + 1);
+    double* kv = (double*)malloc(sizeof(double) * 4 * (cap ? cap : 1));
+    int nk = 0;
+    for (int k1 = -K1; k1 <= K1; ++k1)
+        for (int k2 = -K2; k2 <= K2; ++k2)
+            for (int k3 = 0; k3 <= K3; ++k3) {
+                if (!(k1 != 0 || k2 != 0 || k3 != 0)) continue;
+                double v[3];
+                for (int c = 0; c < 3; ++c)
+                    v[c] = (double)k1 * X->C.rc[c][0] + (double)k2 * X->C.rc[c][1] + (double)k3 * X->C.rc[c][2];
+                if (dot3(v, v) < kcsq) {
+                    double* d = kv + 4 * (size_t)nk++;
+                    d[0] = v[0];
+                    d[1] = v[1];
+                    d[2] = v[2];
+                    d[3] = k3 == 0 ? 1.0 : 2.0;
+                }
+            }
+    *out = kv;
+    return nk;
+}
+
+static void ewald_kspace(const ctx_t* X, int what, int threads, double* energy, double* F, double* stress,
+                         double* chi) {
+    const orc_system* s = X->s;
+    const orc_model* m = X->m;
+    const int n = s->n;
+    double* kv;
+    const int nk = list_kvectors(X, &kv);
+    sk_job* sj = (sk_job*)calloc((size_t)threads, sizeof(sk_job));
+    for (int t = 0; t < threads; ++t) {
+        sj[t].X = X;
+        sj[t].what = what;
+        sj[t].a0 = (int)((int64_t)n * t / threads);
+        sj[t].a1 = (int)((int64_t)n * (t + 1) / threads);
+        sj[t].nk = nk;
+        sj[t].kv = kv;
+        sj[t].S = (double*)calloc(2 * (size_t)(nk ? nk : 1), sizeof(double));
+    }
+    run_jobs(sk_range, sj, sizeof(sk_job), threads);
+    double* S = sj[0].S;
+    double e2 = sj[0].e2, e4 = sj[0].e4;
+    for (int t = 1; t < threads; ++t) {
+        for (int k = 0; k < 2 * nk; ++k) S[k] += sj[t].S[k];
+        e2 += sj[t].e2;
+        e4 += sj[t].e4;
+    }
+    const double sig = m->ewald_sigma, eps = m->ewald_eps;
+    const double inv_eps_4pi = 1.0 / (4.0 * PI * eps);
+    const double inv_eps_2v = 1.0 / (2.0 * X->C.volume * eps);
+    const double inv_sigma_sqrt_2pi = 1.0 / (sqrt(2.0 * PI) * sig);
+    if (what == 0) {
+        double e3 = 0.0;
+        for (int k = 0; k < nk; ++k) {
+            const double* d = kv + 4 * (size_t)k;
+            double dist = d[0] * d[0] + d[1] * d[1] + d[2] * d[2];
+            double ex = exp(-(sig * sig * dist * 0.5)) / dist;
+            double s2 = S[2 * k] * S[2 * k] + S[2 * k + 1] * S[2 * k + 1];
+            if (d[3] == 1.0) e3 = e3 + ex * s2;
+            else e3 = e3 + 2.0 * ex * s2;
+        }
+        double en[7];
+        en[0] = 0.0 * inv_eps_4pi;
+        en[1] = -(e2 * inv_eps_4pi * inv_sigma_sqrt_2pi);
+        en[2] = e3 * inv_eps_2v;
+        en[3] = -(e4 * e4 * 0.5 * inv_eps_2v * sig * sig);
+        en[4] = 0.0;
+        en[5] = 0.0;
+        en[6] = 0.0;
+        double tot = 0.0;
+        for (int c = 0; c < 7; ++c) tot += en[c];
+        *energy = tot;
+    } else {
+        kf_job* kj = (kf_job*)calloc((size_t)threads, sizeof(kf_job));
+        double* self = NULL;
+        if (what == 2) {
+            /* self term and charge sum: Potentials.f90:2121-2125 */
+            self = (double*)calloc((size_t)(n ? n : 1), sizeof(double));
+            for (int i = 0; i < n; ++i) {
+                double q1 = s->charge[i] * m->ewald_scaler[i];
+                self[i] = 0.0 + 2.0 * q1 * inv_eps_4pi * inv_sigma_sqrt_2pi;
+            }
+        }
+        for (int t = 0; t < threads; ++t) {
+            kj[t].X = X;
+            kj[t].what = what;
+            kj[t].a0 = sj[t].a0;
+            kj[t].a1 = sj[t].a1;
+            kj[t].nk = nk;
+            kj[t].kv = kv;
+            kj[t].S = S;
+            kj[t].F = F;
+            kj[t].chi = self;
+            kj[t].qsum = e4;
+        }
+        run_jobs(kf_range, kj, sizeof(kf_job), threads);
+        if (what == 1) {
+            for (int c = 0; c < 6; ++c) {
+                double v = 0.0;
+                for (int t = 0; t < threads; ++t) v += kj[t].stress[c];
+                stress[c] = v;
+            }
+        } else {
+            for (int i = 0; i < n; ++i) chi[i] = self[i];
+            free(self);
+        }
+        free(kj);
+    }
+    for (int t = 0; t < threads; ++t) free(sj[t].S);
+    free(sj);
+    free(kv);
+}
+
+static void setup_ctx(ctx_t* X, const orc_system* s, const orc_model* m, const orc_nblist* nb) {
+    X->s = s;
+    X->m = m;
+    X->nb = nb;
+    make_cell(s, &X->C);
+    const int n = s->n;
+    X->maxbr = (double*)calloc((size_t)(n ? n : 1), sizeof(double));
+    for (int i = 0; i < n; ++i) {
+        double mc = 0.0;
+        for (int b = 0; b < m->n_bond; ++b)
+            if (has(m->bond_mask1[b], s->type[i]) && m->bond_cutoff[b] > mc) mc = m->bond_cutoff[b];
+        X->maxbr[i] = mc;
+    }
+    /* create_potential, Potentials.f90:2382-2388 */
+    X->smooth_soft = (double*)calloc((size_t)(m->n_pair ? m->n_pair : 1), sizeof(double));
+    X->smoothened = (int*)calloc((size_t)(m->n_pair ? m->n_pair : 1), sizeof(int));
+    for (int r = 0; r < m->n_pair; ++r) {
+        if (m->pair_soft[r] > 0.0 && m->pair_soft[r] < m->pair_cutoff[r]) {
+            X->smooth_soft[r] = m->pair_soft[r];
+            X->smoothened[r] = 1;
+        } else {
+            X->smooth_soft[r] = m->pair_cutoff[r];
+            X->smoothened[r] = 0;
+        }
+    }
+}
+
+static void free_ctx(ctx_t* X) {
+    free(X->maxbr);
+    free(X->smooth_soft);
+    free(X->smoothened);
+}
+
+/* core_calculate_energy / forces / electronegativities, Core.f90:7910-7979,
+ * driving core_loop_over_local_interactions, Core.f90:3249-4082. */
+int orc_evaluate(const orc_system* s, const orc_model* m, const orc_nblist* nb, int what, int threads, double* energy,
+                 double* forces, double* stress, double* enegs) {
+    if (what < 0 || what > 2) return -1;
+    if (threads < 1) threads = 1;
+    if (threads > s->n && s->n > 0) threads = s->n;
+    ctx_t X;
+    setup_ctx(&X, s, m, nb);
+    const int n = s->n;
+    loop_job* jobs = (loop_job*)calloc((size_t)threads, sizeof(loop_job));
+    for (int t = 0; t < threads; ++t) {
+        jobs[t].X = &X;
+        jobs[t].what = what;
+        jobs[t].a0 = (int)((int64_t)n * t / threads);
+        jobs[t].a1 = (int)((int64_t)n * (t + 1) / threads);
+        if (what == 1) jobs[t].F = (double*)calloc(3 * (size_t)(n ? n : 1), sizeof(double));
+        if (what == 2) jobs[t].chi = (double*)calloc((size_t)(n ? n : 1), sizeof(double));
+    }
+    run_jobs(loop_range, jobs, sizeof(loop_job), threads);
+    if (what == 0) {
+        double e = 0.0;
+        for (int t = 0; t < threads; ++t) e += jobs[t].energy;
+        if (m->ewald) {
+            double ek;
+            ewald_kspace(&X, 0, threads, &ek, NULL, NULL, NULL);
+            e = e + ek;
+        }
+        *energy = e;
+    } else if (what == 1) {
+        for (size_t c = 0; c < 3 * (size_t)n; ++c) {
+            double v = 0.0;
+            for (int t = 0; t < threads; ++t) v += jobs[t].F[c];
+            forces[c] = v;
+        }
+        for (int c = 0; c < 6; ++c) {
+            double v = 0.0;
+            for (int t = 0; t < threads; ++t) v += jobs[t].stress[c];
+            stress[c] = v;
+        }
+        if (m->ewald) {
+            double* fk = (double*)calloc(3 * (size_t)(n ? n : 1), sizeof(double));
+            double sk[6];
+            ewald_kspace(&X, 1, threads, NULL, fk, sk, NULL);
+            for (size_t c = 0; c < 3 * (size_t)n; ++c) forces[c] = forces[c] + fk[c];
+            for (int c = 0; c < 6; ++c) stress[c] = stress[c] + sk[c];
+            free(fk);
+        }
+    } else {
+        for (int i = 0; i < n; ++i) {
+            double v = 0.0;
+            for (int t = 0; t < threads; ++t) v += jobs[t].chi[i];
+            enegs[i] = v;
+        }
+        if (m->ewald) {
+            double* ck = (double*)calloc((size_t)(n ? n : 1), sizeof(double));
+            ewald_kspace(&X, 2, threads, NULL, NULL, NULL, ck);
+            for (int i = 0; i < n; ++i) enegs[i] = enegs[i] + ck[i];
+            free(ck);
+        }
+    }
+    for (int t = 0; t < threads; ++t) {
+        free(jobs[t].F);
+        free(jobs[t].chi);
+    }
+    free(jobs);
+    free_ctx(&X);
+    return 0;
+}
+
+int orc_bond_zeta(const orc_system* s, const orc_model* m, const orc_nblist* nb, int group, double* zeta) {
+    ctx_t X;
+    setup_ctx(&X, s, m, nb);
+    for (int i = 0; i < s->n; ++i)
+        for (int e = nb->start[i]; e < nb->start[i + 1]; ++e) {
+            const int j = nb->idx[e];
+            double sep[3];
+            separation(&X.C, s->pos + 3 * (size_t)i, s->pos + 3 * (size_t)j, nb->off + 3 * (size_t)e, sep);
+            double d = sqrt(dot3(sep, sep));
+            double sums[2];
+            pair_bo_sums(&X, i, j, sep, d, group, sums);
+            zeta[e] = sums[0];
+        }
+    free_ctx(&X);
+    return 0;
+}

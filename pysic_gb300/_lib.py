@@ -1,0 +1,135 @@
+"""ctypes binding of the engine's C ABI (include/pysic_gb300.h).
+
+This module is the Python side of the drop-in boundary: it takes the place of
+the f2py extension ``pysic.pysic_fortran`` (pysic/calculator.py:16).  There is
+no fallback: if the compiled library is missing, importing the engine fails
+with an error that says how to build it.
+"""
+import ctypes
+import os
+
+import numpy as np
+
+from .error import EngineError
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "libpysic_gb300.so")
+
+PG_OK = 0
+PG_ERR_INVALID = 1
+PG_ERR_CUDA = 2
+PG_ERR_NOT_READY = 3
+PG_ERR_UNSUPPORTED = 4
+PG_ERR_NOT_CONVERGED = 5
+PG_ERR_TIMEOUT = 6
+PG_ERR_SMALL_CELL = 7
+
+PREC_FP64 = 0
+PREC_MIXED = 1
+WANT_ENERGY = 1
+WANT_FORCES = 2
+WANT_ENEGS = 4
+
+_c_double_p = ctypes.POINTER(ctypes.c_double)
+_c_int_p = ctypes.POINTER(ctypes.c_int32)
+_c_u64_p = ctypes.POINTER(ctypes.c_uint64)
+_c_i64_p = ctypes.POINTER(ctypes.c_int64)
+_ctx = ctypes.c_void_p
+
+_SIGNATURES = {
+    "pg_last_error": (ctypes.c_char_p, []),
+    "pg_version": (ctypes.c_char_p, []),
+    "pg_create": (ctypes.c_int, [ctypes.POINTER(ctypes.c_void_p)]),
+    "pg_destroy": (ctypes.c_int, [_ctx]),
+    "pg_create_cell": (ctypes.c_int, [_ctx, _c_double_p, _c_double_p, _c_int_p]),
+    "pg_create_atoms": (ctypes.c_int, [_ctx, ctypes.c_int32, _c_double_p, _c_double_p, _c_int_p]),
+    "pg_update_atom_coordinates": (ctypes.c_int, [_ctx, _c_double_p]),
+    "pg_update_atom_charges": (ctypes.c_int, [_ctx, _c_double_p]),
+    "pg_get_atom_charges": (ctypes.c_int, [_ctx, _c_double_p]),
+    "pg_set_pair_potentials": (ctypes.c_int, [_ctx, ctypes.c_int32, ctypes.c_int32, _c_int_p, _c_double_p,
+                                              _c_double_p, _c_double_p, _c_u64_p, _c_u64_p, _c_int_p]),
+    "pg_set_single_potentials": (ctypes.c_int, [_ctx, ctypes.c_int32, _c_int_p, _c_double_p, _c_u64_p]),
+    "pg_set_bond_order_factors": (ctypes.c_int, [_ctx, ctypes.c_int32, _c_double_p, _c_double_p, _c_double_p,
+                                                 _c_u64_p, _c_u64_p, _c_u64_p, _c_int_p]),
+    "pg_set_ewald": (ctypes.c_int, [_ctx, ctypes.c_double, ctypes.c_double, _c_int_p, ctypes.c_double,
+                                    ctypes.c_double, _c_double_p]),
+    "pg_clear_ewald": (ctypes.c_int, [_ctx]),
+    "pg_generate_neighbor_lists": (ctypes.c_int, [_ctx, _c_double_p, ctypes.c_double]),
+    "pg_generate_all_pairs_lists": (ctypes.c_int, [_ctx, _c_double_p, ctypes.c_double]),
+    "pg_get_neighbor_counts": (ctypes.c_int, [_ctx, _c_int_p]),
+    "pg_get_neighbor_lists": (ctypes.c_int, [_ctx, _c_int_p, _c_int_p]),
+    "pg_create_neighbor_lists": (ctypes.c_int, [_ctx, _c_int_p, _c_int_p, _c_int_p, ctypes.c_double]),
+    "pg_calculate_energy": (ctypes.c_int, [_ctx, ctypes.c_int32, _c_double_p]),
+    "pg_calculate_forces": (ctypes.c_int, [_ctx, ctypes.c_int32, _c_double_p, _c_double_p]),
+    "pg_calculate_electronegativities": (ctypes.c_int, [_ctx, ctypes.c_int32, _c_double_p]),
+    "pg_calculate": (ctypes.c_int, [_ctx, ctypes.c_int32, ctypes.c_int32, _c_double_p, _c_double_p, _c_double_p,
+                                    _c_double_p]),
+    "pg_relax_charges": (ctypes.c_int, [_ctx, ctypes.c_int32, ctypes.c_int32, ctypes.c_double, ctypes.c_double,
+                                        ctypes.c_double, ctypes.c_double, _c_double_p, _c_double_p, _c_int_p,
+                                        _c_double_p, _c_double_p]),
+    "pg_get_bond_zeta": (ctypes.c_int, [_ctx, _c_double_p, ctypes.c_int64, _c_i64_p]),
+    "pg_set_lanes_per_atom": (ctypes.c_int, [_ctx, ctypes.c_int32]),
+    "pg_get_lanes_per_atom": (ctypes.c_int, [_ctx, _c_int_p]),
+    "pg_device_evaluate": (ctypes.c_int, [_ctx, ctypes.c_int32, ctypes.c_int32]),
+    "pg_device_synchronize": (ctypes.c_int, [_ctx]),
+    "pg_device_results": (ctypes.c_int, [_ctx, _c_double_p, _c_double_p, _c_double_p, _c_double_p]),
+    "pg_device_positions": (ctypes.c_int, [_ctx, ctypes.POINTER(_c_double_p)]),
+    "pg_get_stream": (ctypes.c_int, [_ctx, ctypes.POINTER(ctypes.c_void_p)]),
+    "pg_last_launch_count": (ctypes.c_int, [_ctx, _c_int_p]),
+}
+
+_lib = None
+
+
+def exported_symbols():
+    return list(_SIGNATURES.keys())
+
+
+def load(path=LIB_PATH):
+    """Load the engine library (once).  Raises ImportError if it was not built."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    if not os.path.exists(path):
+        raise ImportError("GB300 engine library not found at {0}; build it with "
+                          "`python -m pysic_gb300.build` (needs nvcc)".format(path))
+    lib = ctypes.CDLL(path)
+    for name, (res, args) in _SIGNATURES.items():
+        fn = getattr(lib, name)
+        fn.restype = res
+        fn.argtypes = args
+    _lib = lib
+    return lib
+
+
+def check(status):
+    if status != PG_OK:
+        msg = _lib.pg_last_error().decode(errors="replace") if _lib is not None else ""
+        raise EngineError(status, msg)
+
+
+def dptr(a):
+    return a.ctypes.data_as(_c_double_p)
+
+
+def iptr(a):
+    return a.ctypes.data_as(_c_int_p)
+
+
+def u64ptr(a):
+    return a.ctypes.data_as(_c_u64_p)
+
+
+def as_f64(a, shape=None):
+    a = np.ascontiguousarray(a, dtype=np.float64)
+    if shape is not None:
+        a = a.reshape(shape)
+    return a
+
+
+def as_i32(a):
+    return np.ascontiguousarray(a, dtype=np.int32)
+
+
+def as_u64(a):
+    return np.ascontiguousarray(a, dtype=np.uint64)

@@ -1,0 +1,532 @@
+// api.cu -- the C ABI of include/pysic_gb300.h: context life cycle, state
+// setters, the evaluation pipeline and the lane-count autotuner.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+#include <string>
+
+#include "common.cuh"
+
+namespace {
+thread_local std::string g_last_error;
+
+template <typename F>
+int guarded(F&& f) {
+    try {
+        f();
+        g_last_error.clear();
+        return PG_OK;
+    } catch (const pg::Error& e) {
+        g_last_error = e.what();
+        return e.status;
+    } catch (const std::bad_alloc&) {
+        g_last_error = "host out of memory";
+        return PG_ERR_CUDA;
+    } catch (const std::exception& e) {
+        g_last_error = e.what();
+        return PG_ERR_INVALID;
+    }
+}
+
+void use_device(pg_context* ctx) { PG_CUDA(cudaSetDevice(ctx->device)); }
+
+void check_ctx(pg_context* ctx) { pg::require(ctx != nullptr, PG_ERR_INVALID, "null context"); }
+}  // namespace
+
+namespace pg {
+
+// generate_supercell, Geometry.f90:177-195, with the transposes of
+// pysic/calculator.py:1555-1565 (vectors = cell^T, inverse = inv(cell)^T).
+void make_cell(const double* cell, const double* inv, const int32_t* pbc, Cell& C) {
+    for (int r = 0; r < 3; ++r)
+        for (int c = 0; c < 3; ++c) {
+            C.vc[r][c] = cell[c * 3 + r];
+            C.ic[r][c] = inv[c * 3 + r];
+        }
+    const double twopi = 2.0 * 3.14159265358979323846;
+    for (int r = 0; r < 3; ++r)
+        for (int c = 0; c < 3; ++c) C.rc[r][c] = twopi * C.ic[c][r];
+    double a[3], b[3], d[3];
+    for (int r = 0; r < 3; ++r) {
+        a[r] = C.vc[r][0];
+        b[r] = C.vc[r][1];
+        d[r] = C.vc[r][2];
+    }
+    const double x0 = a[1] * b[2] - a[2] * b[1];
+    const double x1 = a[2] * b[0] - a[0] * b[2];
+    const double x2 = a[0] * b[1] - a[1] * b[0];
+    C.volume = std::fabs(x0 * d[0] + x1 * d[1] + x2 * d[2]);
+    for (int i = 0; i < 3; ++i) C.pbc[i] = pbc[i] != 0;
+}
+
+CellK cell_kernel_view(const Cell& C) {
+    CellK k;
+    std::memcpy(k.vc, C.vc, sizeof(k.vc));
+    std::memcpy(k.ic, C.ic, sizeof(k.ic));
+    for (int i = 0; i < 3; ++i) k.pbc[i] = C.pbc[i];
+    return k;
+}
+
+static int pair_lanes(const pg_context* ctx) {
+    const double avg = ctx->n > 0 ? (double)ctx->nb_total / ctx->n : 0.0;
+    if (avg >= 48.0) return 32;
+    if (avg >= 16.0) return 16;
+    return 8;
+}
+
+static void prepare(pg_context* ctx) {
+    require(ctx->have_cell, PG_ERR_NOT_READY, "no cell: call pg_create_cell first");
+    require(ctx->have_atoms, PG_ERR_NOT_READY, "no atoms: call pg_create_atoms first");
+    require(ctx->have_list, PG_ERR_NOT_READY, "no neighbour lists: build or install them first");
+    if (ctx->tables_dirty) fold_tables(ctx);
+    if (ctx->have_bond_terms && ctx->short_dirty) build_short_list(ctx);
+    if (ctx->ewald) ewald_prepare(ctx);
+}
+
+// one evaluation, enqueued on ctx->stream; G: lanes per atom of the bond kernels
+static void enqueue(pg_context* ctx, int precision, int flags, int G) {
+    const int n = ctx->n;
+    const bool wantF = flags & PG_WANT_FORCES, wantC = flags & PG_WANT_ENEGS, wantE = flags & PG_WANT_ENERGY;
+    ctx->out_f.resize(3 * (size_t)std::max(n, 1));
+    ctx->out_chi.resize((size_t)std::max(n, 1));
+    ctx->out_tot.resize(8);
+    const bool run_pair = ctx->have_pair_kernel_terms || ctx->ewald || ctx->have_singles;
+    const bool run_bond = ctx->have_bond_terms && (wantE || wantF);
+    const int Gp = pair_lanes(ctx);
+    int slots = 0;
+    if (run_pair) slots += pair_kernel_blocks(n, Gp);
+    if (run_bond) slots += bond_blocks(n, G);
+    if (ctx->ewald) slots += ewald_partial_slots(ctx);
+    ctx->red_part.resize(8 * (size_t)std::max(slots, 1));
+    bool first_f = true, first_chi = true;
+    int used = 0;
+    if (run_pair) {
+        launch_pair_kernel_impl(ctx, precision, flags, first_f, first_chi, Gp, ctx->red_part.p + 8 * used);
+        used += pair_kernel_blocks(n, Gp);
+        if (wantF) first_f = false;
+        if (wantC) first_chi = false;
+    }
+    if (run_bond) {
+        used += launch_bond_order_impl(ctx, precision, flags, first_f, G, ctx->red_part.p + 8 * used);
+        if (wantF) first_f = false;
+    }
+    if (ctx->ewald) {
+        launch_ewald_kspace(ctx, precision, flags, first_f, first_chi, ctx->red_part.p + 8 * used);
+        used += ewald_partial_slots(ctx);
+        if (wantF) first_f = false;
+        if (wantC) first_chi = false;
+    }
+    if (wantF && first_f) PG_CUDA(cudaMemsetAsync(ctx->out_f.p, 0, sizeof(double) * 3 * n, ctx->stream));
+    if (wantC && first_chi) PG_CUDA(cudaMemsetAsync(ctx->out_chi.p, 0, sizeof(double) * n, ctx->stream));
+    if (used > 0) launch_final_reduce(ctx, used);
+    else PG_CUDA(cudaMemsetAsync(ctx->out_tot.p, 0, sizeof(double) * 8, ctx->stream));
+}
+
+// pick the lanes-per-atom tile of the bond-order kernels by timing each
+static int autotune_lanes(pg_context* ctx, int precision, int flags) {
+    const int options[4] = {4, 8, 16, 32};
+    cudaEvent_t e0, e1;
+    PG_CUDA(cudaEventCreate(&e0));
+    PG_CUDA(cudaEventCreate(&e1));
+    int best = 8;
+    float best_ms = 1e30f;
+    for (int o = 0; o < 4; ++o) {
+        const int G = options[o];
+        enqueue(ctx, precision, flags, G);  // warm-up
+        PG_CUDA(cudaEventRecord(e0, ctx->stream));
+        for (int r = 0; r < 3; ++r) enqueue(ctx, precision, flags, G);
+        PG_CUDA(cudaEventRecord(e1, ctx->stream));
+        PG_CUDA(cudaEventSynchronize(e1));
+        float ms = 0;
+        PG_CUDA(cudaEventElapsedTime(&ms, e0, e1));
+        if (ms < best_ms) {
+            best_ms = ms;
+            best = G;
+        }
+    }
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    return best;
+}
+
+void evaluate(pg_context* ctx, int precision, int flags) {
+    require(precision == PG_PREC_FP64 || precision == PG_PREC_MIXED, PG_ERR_INVALID, "unknown precision");
+    prepare(ctx);
+    int G = ctx->lanes;
+    if (G == 0 && ctx->have_bond_terms) {
+        if (ctx->tuned_lanes[precision] == 0) ctx->tuned_lanes[precision] = autotune_lanes(ctx, precision, flags);
+        G = ctx->tuned_lanes[precision];
+    }
+    if (G == 0) G = 8;
+    ctx->launches = 0;
+    enqueue(ctx, precision, flags, G);
+}
+
+static void copy_results(pg_context* ctx, int flags, double* energy, double* forces, double* stress, double* enegs) {
+    double tot[8] = {0};
+    cudaStream_t st = ctx->stream;
+    if (energy || stress) PG_CUDA(cudaMemcpyAsync(tot, ctx->out_tot.p, sizeof(tot), cudaMemcpyDeviceToHost, st));
+    if (forces && (flags & PG_WANT_FORCES)) ctx->out_f.download(forces, 3 * (size_t)ctx->n, st);
+    if (enegs && (flags & PG_WANT_ENEGS)) ctx->out_chi.download(enegs, (size_t)ctx->n, st);
+    PG_CUDA(cudaStreamSynchronize(st));
+    if (energy && (flags & PG_WANT_ENERGY)) *energy = tot[0];
+    if (stress && (flags & PG_WANT_FORCES))
+        for (int c = 0; c < 6; ++c) stress[c] = tot[1 + c];
+}
+
+}  // namespace pg
+
+extern "C" {
+
+const char* pg_last_error(void) { return g_last_error.c_str(); }
+
+const char* pg_version(void) { return "pysic_gb300 0.1 (sm_103a)"; }
+
+int pg_create(pg_context** out) {
+    return guarded([&] {
+        pg::require(out != nullptr, PG_ERR_INVALID, "null output pointer");
+        *out = nullptr;
+        int dev = 0;
+        PG_CUDA(cudaGetDevice(&dev));
+        pg_context* ctx = new pg_context();
+        ctx->device = dev;
+        cudaError_t e = cudaStreamCreateWithFlags(&ctx->stream, cudaStreamNonBlocking);
+        if (e != cudaSuccess) {
+            delete ctx;
+            throw pg::Error(PG_ERR_CUDA, std::string("cudaStreamCreate: ") + cudaGetErrorString(e));
+        }
+        *out = ctx;
+    });
+}
+
+int pg_destroy(pg_context* ctx) {
+    return guarded([&] {
+        if (!ctx) return;
+        cudaSetDevice(ctx->device);
+        cudaStreamSynchronize(ctx->stream);
+        cudaStreamDestroy(ctx->stream);
+        delete ctx;
+    });
+}
+
+int pg_create_cell(pg_context* ctx, const double* cell, const double* inv, const int32_t* pbc) {
+    return guarded([&] {
+        check_ctx(ctx);
+        pg::require(cell && inv && pbc, PG_ERR_INVALID, "null cell argument");
+        pg::make_cell(cell, inv, pbc, ctx->cell);
+        std::memcpy(ctx->cell_rows, cell, sizeof(ctx->cell_rows));
+        std::memcpy(ctx->inv_rows, inv, sizeof(ctx->inv_rows));
+        ctx->have_cell = true;
+        ctx->have_list = false;
+        ctx->ew_tables_dirty = true;
+    });
+}
+
+int pg_create_atoms(pg_context* ctx, int32_t n, const double* positions, const double* charges,
+                    const int32_t* types) {
+    return guarded([&] {
+        check_ctx(ctx);
+        use_device(ctx);
+        pg::require(n >= 0, PG_ERR_INVALID, "negative atom count");
+        pg::require(n == 0 || (positions && charges && types), PG_ERR_INVALID, "null atom arrays");
+        for (int i = 0; i < n; ++i) pg::require(types[i] >= 0 && types[i] < 64, PG_ERR_INVALID, "type out of range");
+        for (int i = 0; i < 3 * n; ++i)
+            pg::require(std::isfinite(positions[i]), PG_ERR_INVALID, "non-finite atom position");
+        ctx->n = n;
+        ctx->pos.upload(positions, 3 * (size_t)n, ctx->stream);
+        ctx->charge.upload(charges, (size_t)n, ctx->stream);
+        ctx->type.upload(types, (size_t)n, ctx->stream);
+        ctx->h_type.assign(types, types + n);
+        PG_CUDA(cudaStreamSynchronize(ctx->stream));
+        ctx->have_atoms = true;
+        ctx->have_list = false;
+    });
+}
+
+int pg_update_atom_coordinates(pg_context* ctx, const double* positions) {
+    return guarded([&] {
+        check_ctx(ctx);
+        use_device(ctx);
+        pg::require(ctx->have_atoms, PG_ERR_NOT_READY, "no atoms");
+        for (int i = 0; i < 3 * ctx->n; ++i)
+            pg::require(std::isfinite(positions[i]), PG_ERR_INVALID, "non-finite atom position");
+        ctx->pos.upload(positions, 3 * (size_t)ctx->n, ctx->stream);
+        PG_CUDA(cudaStreamSynchronize(ctx->stream));
+    });
+}
+
+int pg_update_atom_charges(pg_context* ctx, const double* charges) {
+    return guarded([&] {
+        check_ctx(ctx);
+        use_device(ctx);
+        pg::require(ctx->have_atoms, PG_ERR_NOT_READY, "no atoms");
+        ctx->charge.upload(charges, (size_t)ctx->n, ctx->stream);
+        PG_CUDA(cudaStreamSynchronize(ctx->stream));
+    });
+}
+
+int pg_get_atom_charges(pg_context* ctx, double* charges) {
+    return guarded([&] {
+        check_ctx(ctx);
+        use_device(ctx);
+        pg::require(ctx->have_atoms, PG_ERR_NOT_READY, "no atoms");
+        ctx->charge.download(charges, (size_t)ctx->n, ctx->stream);
+        PG_CUDA(cudaStreamSynchronize(ctx->stream));
+    });
+}
+
+int pg_set_pair_potentials(pg_context* ctx, int32_t n_types, int32_t n, const int32_t* kind, const double* params,
+                           const double* cutoff, const double* soft, const uint64_t* mask1, const uint64_t* mask2,
+                           const int32_t* group) {
+    return guarded([&] {
+        check_ctx(ctx);
+        pg::require(n_types >= 0 && n_types <= 64, PG_ERR_INVALID, "n_types must be within 0..64");
+        pg::require(n >= 0, PG_ERR_INVALID, "negative record count");
+        for (int r = 0; r < n; ++r)
+            pg::require(kind[r] >= 0 && kind[r] <= 2, PG_ERR_UNSUPPORTED, "unknown pair potential kind");
+        ctx->n_types = n_types;
+        ctx->pr_kind.assign(kind, kind + n);
+        ctx->pr_params.assign(params, params + 4 * (size_t)n);
+        ctx->pr_cut.assign(cutoff, cutoff + n);
+        ctx->pr_soft.assign(soft, soft + n);
+        ctx->pr_m1.assign(mask1, mask1 + n);
+        ctx->pr_m2.assign(mask2, mask2 + n);
+        ctx->pr_group.assign(group, group + n);
+        ctx->tables_dirty = true;
+    });
+}
+
+int pg_set_single_potentials(pg_context* ctx, int32_t n, const int32_t* kind, const double* params,
+                             const uint64_t* mask) {
+    return guarded([&] {
+        check_ctx(ctx);
+        pg::require(n >= 0, PG_ERR_INVALID, "negative record count");
+        for (int r = 0; r < n; ++r) pg::require(kind[r] == 0, PG_ERR_UNSUPPORTED, "unknown single-atom kind");
+        ctx->sr_kind.assign(kind, kind + n);
+        ctx->sr_params.assign(params, params + 2 * (size_t)n);
+        ctx->sr_m.assign(mask, mask + n);
+        ctx->tables_dirty = true;
+    });
+}
+
+int pg_set_bond_order_factors(pg_context* ctx, int32_t n, const double* params, const double* cutoff,
+                              const double* soft, const uint64_t* mask1, const uint64_t* mask2,
+                              const uint64_t* mask3, const int32_t* group) {
+    return guarded([&] {
+        check_ctx(ctx);
+        pg::require(n >= 0, PG_ERR_INVALID, "negative record count");
+        ctx->br_params.assign(params, params + 7 * (size_t)n);
+        ctx->br_cut.assign(cutoff, cutoff + n);
+        ctx->br_soft.assign(soft, soft + n);
+        ctx->br_m1.assign(mask1, mask1 + n);
+        ctx->br_m2.assign(mask2, mask2 + n);
+        ctx->br_m3.assign(mask3, mask3 + n);
+        ctx->br_group.assign(group, group + n);
+        ctx->tables_dirty = true;
+    });
+}
+
+int pg_set_ewald(pg_context* ctx, double real_cut, double k_radius, const int32_t* kmax, double sigma, double epsilon,
+                 const double* scaler) {
+    return guarded([&] {
+        check_ctx(ctx);
+        pg::require(ctx->have_atoms, PG_ERR_NOT_READY, "set atoms before Ewald parameters");
+        pg::require(sigma > 0 && epsilon > 0 && real_cut >= 0 && k_radius >= 0, PG_ERR_INVALID,
+                    "invalid Ewald parameters");
+        for (int a = 0; a < 3; ++a) pg::require(kmax[a] >= 0 && kmax[a] <= 512, PG_ERR_INVALID, "invalid k limit");
+        ctx->ewald = true;
+        ctx->ew_rc = real_cut;
+        ctx->ew_kc = k_radius;
+        ctx->ew_sigma = sigma;
+        ctx->ew_eps = epsilon;
+        for (int a = 0; a < 3; ++a) ctx->ew_kmax[a] = kmax[a];
+        ctx->ew_scaler.upload(scaler, (size_t)ctx->n, ctx->stream);
+        PG_CUDA(cudaStreamSynchronize(ctx->stream));
+        ctx->ew_tables_dirty = true;
+    });
+}
+
+int pg_clear_ewald(pg_context* ctx) {
+    return guarded([&] {
+        check_ctx(ctx);
+        ctx->ewald = false;
+    });
+}
+
+int pg_generate_neighbor_lists(pg_context* ctx, const double* cutoffs, double skin) {
+    return guarded([&] {
+        check_ctx(ctx);
+        use_device(ctx);
+        pg::require(ctx->have_cell && ctx->have_atoms, PG_ERR_NOT_READY, "set cell and atoms first");
+        pg::require(skin >= 0, PG_ERR_INVALID, "negative skin");
+        for (int i = 0; i < ctx->n; ++i)
+            pg::require(std::isfinite(cutoffs[i]) && cutoffs[i] >= 0, PG_ERR_INVALID, "invalid cutoff");
+        ctx->skin = skin;
+        pg::build_neighbor_lists(ctx, cutoffs);
+    });
+}
+
+int pg_generate_all_pairs_lists(pg_context* ctx, const double* cutoffs, double skin) {
+    return guarded([&] {
+        check_ctx(ctx);
+        use_device(ctx);
+        pg::require(ctx->have_cell && ctx->have_atoms, PG_ERR_NOT_READY, "set cell and atoms first");
+        pg::require(skin >= 0, PG_ERR_INVALID, "negative skin");
+        for (int i = 0; i < ctx->n; ++i)
+            pg::require(std::isfinite(cutoffs[i]) && cutoffs[i] >= 0, PG_ERR_INVALID, "invalid cutoff");
+        ctx->skin = skin;
+        pg::build_allpairs_lists(ctx, cutoffs);
+    });
+}
+
+int pg_get_neighbor_counts(pg_context* ctx, int32_t* counts) {
+    return guarded([&] {
+        check_ctx(ctx);
+        use_device(ctx);
+        pg::require(ctx->have_list, PG_ERR_NOT_READY, "no neighbour lists");
+        std::vector<int> st(ctx->n + 1);
+        ctx->nb_start.download(st.data(), ctx->n + 1, ctx->stream);
+        PG_CUDA(cudaStreamSynchronize(ctx->stream));
+        for (int i = 0; i < ctx->n; ++i) counts[i] = st[i + 1] - st[i];
+    });
+}
+
+int pg_get_neighbor_lists(pg_context* ctx, int32_t* neighbors, int32_t* offsets) {
+    return guarded([&] {
+        check_ctx(ctx);
+        use_device(ctx);
+        pg::require(ctx->have_list, PG_ERR_NOT_READY, "no neighbour lists");
+        ctx->nb_idx.download(neighbors, (size_t)ctx->nb_total, ctx->stream);
+        ctx->nb_off.download(offsets, 3 * (size_t)ctx->nb_total, ctx->stream);
+        PG_CUDA(cudaStreamSynchronize(ctx->stream));
+    });
+}
+
+int pg_create_neighbor_lists(pg_context* ctx, const int32_t* counts, const int32_t* neighbors, const int32_t* offsets,
+                             double skin) {
+    return guarded([&] {
+        check_ctx(ctx);
+        use_device(ctx);
+        pg::require(ctx->have_atoms, PG_ERR_NOT_READY, "no atoms");
+        ctx->skin = skin;
+        pg::install_neighbor_lists(ctx, counts, neighbors, offsets);
+    });
+}
+
+int pg_calculate(pg_context* ctx, int32_t precision, int32_t flags, double* energy, double* forces, double* stress,
+                 double* enegs) {
+    return guarded([&] {
+        check_ctx(ctx);
+        use_device(ctx);
+        pg::evaluate(ctx, precision, flags);
+        pg::copy_results(ctx, flags, energy, forces, stress, enegs);
+    });
+}
+
+int pg_calculate_energy(pg_context* ctx, int32_t precision, double* energy) {
+    return pg_calculate(ctx, precision, PG_WANT_ENERGY, energy, nullptr, nullptr, nullptr);
+}
+
+int pg_calculate_forces(pg_context* ctx, int32_t precision, double* forces, double* stress) {
+    return pg_calculate(ctx, precision, PG_WANT_FORCES, nullptr, forces, stress, nullptr);
+}
+
+int pg_calculate_electronegativities(pg_context* ctx, int32_t precision, double* enegs) {
+    return pg_calculate(ctx, precision, PG_WANT_ENEGS, nullptr, nullptr, nullptr, enegs);
+}
+
+int pg_relax_charges(pg_context* ctx, int32_t precision, int32_t n_steps, double timestep, double inertia,
+                     double friction, double tolerance, double* rates, double* charges, int32_t* steps, double* error,
+                     double* max_dq) {
+    return guarded([&] {
+        check_ctx(ctx);
+        use_device(ctx);
+        pg::require(inertia != 0.0, PG_ERR_INVALID, "zero charge inertia");
+        pg::require(n_steps >= 0, PG_ERR_INVALID, "negative step count");
+        int s = 0;
+        pg::relax_charges(ctx, precision, n_steps, timestep, inertia, friction, tolerance, rates, charges, &s, error,
+                          max_dq);
+        *steps = s;
+    });
+}
+
+int pg_get_bond_zeta(pg_context* ctx, double* zeta, int64_t capacity, int64_t* n_entries) {
+    return guarded([&] {
+        check_ctx(ctx);
+        use_device(ctx);
+        pg::prepare(ctx);
+        pg::require(ctx->have_bond_terms, PG_ERR_NOT_READY, "no bond-order factors");
+        *n_entries = ctx->sh_total;
+        if (zeta && capacity >= ctx->sh_total) {
+            pg::bond_zeta_diag(ctx);
+            ctx->bo_zeta.download(zeta, (size_t)ctx->sh_total, ctx->stream);
+            PG_CUDA(cudaStreamSynchronize(ctx->stream));
+        }
+    });
+}
+
+int pg_set_lanes_per_atom(pg_context* ctx, int32_t lanes) {
+    return guarded([&] {
+        check_ctx(ctx);
+        pg::require(lanes == 0 || lanes == 4 || lanes == 8 || lanes == 16 || lanes == 32, PG_ERR_INVALID,
+                    "lanes per atom must be 0, 4, 8, 16 or 32");
+        ctx->lanes = lanes;
+    });
+}
+
+int pg_get_lanes_per_atom(pg_context* ctx, int32_t* lanes) {
+    return guarded([&] {
+        check_ctx(ctx);
+        *lanes = ctx->lanes;
+        if (*lanes == 0) *lanes = std::max(ctx->tuned_lanes[0], ctx->tuned_lanes[1]);
+    });
+}
+
+int pg_device_evaluate(pg_context* ctx, int32_t precision, int32_t flags) {
+    return guarded([&] {
+        check_ctx(ctx);
+        use_device(ctx);
+        pg::evaluate(ctx, precision, flags);
+    });
+}
+
+int pg_device_synchronize(pg_context* ctx) {
+    return guarded([&] {
+        check_ctx(ctx);
+        PG_CUDA(cudaStreamSynchronize(ctx->stream));
+    });
+}
+
+int pg_device_results(pg_context* ctx, double* energy, double* forces, double* stress, double* enegs) {
+    return guarded([&] {
+        check_ctx(ctx);
+        use_device(ctx);
+        pg::copy_results(ctx, PG_WANT_ENERGY | PG_WANT_FORCES | PG_WANT_ENEGS, energy, forces, stress, enegs);
+    });
+}
+
+int pg_device_positions(pg_context* ctx, double** device_ptr) {
+    return guarded([&] {
+        check_ctx(ctx);
+        pg::require(ctx->have_atoms, PG_ERR_NOT_READY, "no atoms");
+        *device_ptr = ctx->pos.p;
+    });
+}
+
+int pg_get_stream(pg_context* ctx, void** stream) {
+    return guarded([&] {
+        check_ctx(ctx);
+        *stream = (void*)ctx->stream;
+    });
+}
+
+int pg_last_launch_count(pg_context* ctx, int32_t* launches) {
+    return guarded([&] {
+        check_ctx(ctx);
+        *launches = ctx->launches;
+    });
+}
+
+}  // extern "C"

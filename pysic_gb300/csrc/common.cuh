@@ -1,0 +1,263 @@
+// common.cuh -- shared types of the GB300 engine: device buffers, the engine
+// context, interaction tables and error handling.
+#pragma once
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include <stdexcept>
+#include <string>
+#include <vector>
+
+#include "../../include/pysic_gb300.h"
+
+namespace pg {
+
+struct Error : std::runtime_error {
+    int status;
+    Error(int s, const std::string& m) : std::runtime_error(m), status(s) {}
+};
+
+#define PG_CUDA(call)                                                                                  \
+    do {                                                                                               \
+        cudaError_t e_ = (call);                                                                       \
+        if (e_ != cudaSuccess)                                                                         \
+            throw ::pg::Error(PG_ERR_CUDA, std::string(#call) + ": " + cudaGetErrorString(e_));         \
+    } while (0)
+
+#define PG_CHECK_LAUNCH() PG_CUDA(cudaGetLastError())
+
+inline void require(bool ok, int status, const std::string& msg) {
+    if (!ok) throw Error(status, msg);
+}
+
+// Grow-only device buffer.
+template <typename T>
+struct DevBuf {
+    T* p = nullptr;
+    size_t cap = 0;
+    size_t n = 0;
+    DevBuf() = default;
+    DevBuf(const DevBuf&) = delete;
+    DevBuf& operator=(const DevBuf&) = delete;
+    ~DevBuf() {
+        if (p) cudaFree(p);
+    }
+    void resize(size_t count) {
+        if (count > cap) {
+            if (p) cudaFree(p);
+            p = nullptr;
+            size_t c = count + count / 8 + 16;
+            PG_CUDA(cudaMalloc(&p, c * sizeof(T)));
+            cap = c;
+        }
+        n = count;
+    }
+    void upload(const T* h, size_t count, cudaStream_t s) {
+        resize(count);
+        if (count) PG_CUDA(cudaMemcpyAsync(p, h, count * sizeof(T), cudaMemcpyHostToDevice, s));
+    }
+    void download(T* h, size_t count, cudaStream_t s) const {
+        if (count) PG_CUDA(cudaMemcpyAsync(h, p, count * sizeof(T), cudaMemcpyDeviceToHost, s));
+    }
+    void zero(cudaStream_t s) {
+        if (n) PG_CUDA(cudaMemsetAsync(p, 0, n * sizeof(T), s));
+    }
+};
+
+// Host-side copy of the cell in the reference's layout (Geometry.f90:50-145).
+struct Cell {
+    double vc[3][3];  // cell%vectors(r,c): component r of cell vector c
+    double ic[3][3];  // cell%inverse_cell(r,c)
+    double rc[3][3];  // reciprocal_cell(r,c) = 2 pi inverse(c,r)
+    double volume;
+    int pbc[3];
+};
+
+// Kernel-side view of the cell (passed by value).
+struct CellK {
+    double vc[3][3];
+    double ic[3][3];
+    int pbc[3];
+};
+
+// One pair term folded per type pair (an interaction record whose two target
+// masks contain the pair of types).
+struct PairTerm {
+    int kind;      // 0 LJ, 1 exponential, 2 Buckingham
+    int group;     // -1: plain, else bond-order group
+    int smooth;    // smoothing active (create_potential, Potentials.f90:2382-2388)
+    int in_bond_kernel;  // evaluated by the bond-order kernels (short list) rather than the pair kernel
+    double p[4];
+    double rc, rs;
+};
+
+// Tersoff triplet parameters for (centre type, j type, k type) of group 0.
+struct TripletTerm {
+    double a, c2, d2, h, mu, rc, rs;
+    int valid;
+};
+
+// Post-processing (B(zeta)) parameters per centre type for group 0.
+struct PostTerm {
+    double beta, eta;
+    int valid;
+};
+
+struct SingleTerm {
+    int kind;
+    double eps;
+    int n;
+};
+
+// 16- and 32-byte aligned 4-vectors (bond geometry, per-bond forces)
+struct alignas(16) F4 {
+    float x, y, z, w;
+};
+struct alignas(32) D4 {
+    double x, y, z, w;
+};
+
+}  // namespace pg
+
+// ---- the engine context --------------------------------------------------
+struct pg_context {
+    int device = 0;
+    cudaStream_t stream = nullptr;
+
+    // system
+    int n = 0;
+    bool have_cell = false, have_atoms = false;
+    pg::Cell cell{};
+    double cell_rows[9]{}, inv_rows[9]{};
+    pg::DevBuf<double> pos;     // n x 3
+    pg::DevBuf<double> charge;  // n
+    pg::DevBuf<int> type;       // n
+    std::vector<int> h_type;
+
+    // interaction records (host copies) and folded tables
+    int n_types = 0;
+    std::vector<int> pr_kind, pr_group;
+    std::vector<double> pr_params, pr_cut, pr_soft;
+    std::vector<uint64_t> pr_m1, pr_m2;
+    std::vector<int> sr_kind;
+    std::vector<double> sr_params;
+    std::vector<uint64_t> sr_m;
+    std::vector<double> br_params, br_cut, br_soft;
+    std::vector<uint64_t> br_m1, br_m2, br_m3;
+    std::vector<int> br_group;
+    bool tables_dirty = true;
+    bool have_bond_terms = false, have_pair_kernel_terms = false, have_singles = false;
+    double bo_radius = 0.0;          // largest cutoff handled by the bond-order kernels
+    pg::DevBuf<pg::PairTerm> d_pair_terms;
+    pg::DevBuf<int2> d_pair_index;     // per (ti, tj): offset, count into d_pair_terms
+    pg::DevBuf<pg::TripletTerm> d_trip;  // n_types^3
+    pg::DevBuf<pg::PostTerm> d_post;     // n_types
+    pg::DevBuf<double> d_maxbr;          // per type: max bond-order cutoff (max_bond_radius)
+    pg::DevBuf<pg::SingleTerm> d_single_terms;
+    pg::DevBuf<int2> d_single_index;     // per type
+
+    // Ewald
+    bool ewald = false;
+    double ew_rc = 0, ew_kc = 0, ew_sigma = 0, ew_eps = 0;
+    int ew_kmax[3] = {0, 0, 0};
+    pg::DevBuf<double> ew_scaler;
+    bool ew_tables_dirty = true;
+    int ew_nk = 0, ew_ncol = 0, ew_nseg = 0;
+    pg::DevBuf<int4> ew_seg;       // per segment: n1, n2, n3 start, count (+ k index base in .w via separate array)
+    pg::DevBuf<int> ew_seg_k0;     // first listed-k index of each segment
+    pg::DevBuf<pg::F4> ew_kvec;    // per listed k: kx, ky, kz, weight * exp(-s^2 k^2/2)/k^2 (FP32)
+    pg::DevBuf<pg::D4> ew_kvec64; // same in FP64
+    pg::DevBuf<double2> ew_S;      // structure factor per listed k (FP64 accumulated)
+    pg::DevBuf<float2> ew_Spart;   // per (atom chunk, k) partial sums
+    pg::DevBuf<double2> ew_Spart64;
+    pg::DevBuf<uint32_t> ew_frac;  // per atom: fixed-point fractional coordinates (3)
+    int ew_chunks = 0;
+
+    // neighbour lists: full list (CSR) and the short list of bond-order terms
+    bool have_list = false;
+    double skin = 0.5;
+    pg::DevBuf<int> nb_start, nb_idx, nb_off;  // nb_off: 3 per entry
+    pg::DevBuf<int> nb_g0;                     // per atom: entries coming from lower-index atoms
+    long long nb_total = 0;
+    bool short_dirty = true;
+    bool short_is_full = false;
+    pg::DevBuf<int> sh_start, sh_idx, sh_off, sh_rev, sh_count;
+    pg::DevBuf<long long> sh_tri;  // per atom: base of its n_i^2 triplet block
+    long long sh_total = 0, sh_tri_total = 0;
+    int sh_maxn = 0;
+
+    // neighbour-build scratch
+    pg::DevBuf<int> cell_of, cell_start, sorted_atoms, wrap, keys_a, keys_b, vals_a, vals_b, radix_hist, count_tmp,
+        invisible;
+    pg::DevBuf<long long> g0_keys;
+    pg::DevBuf<int4> g0_vals;
+    pg::DevBuf<int> g0_start;
+    pg::DevBuf<double> cutoffs;
+    pg::DevBuf<int> scan_tmp;
+
+    // bond-order scratch
+    pg::DevBuf<pg::F4> bo_fj, bo_fk;      // mixed precision
+    pg::DevBuf<pg::D4> bo_fj64, bo_fk64; // FP64
+    pg::DevBuf<double> bo_fc;             // centre-role forces per atom (3)
+    pg::DevBuf<double> bo_zeta;           // per short entry (diagnostics)
+    int lanes = 0;                        // 0: autotune
+    int tuned_lanes[2] = {0, 0};
+
+    // outputs
+    pg::DevBuf<double> out_f;     // n x 3
+    pg::DevBuf<double> out_chi;   // n
+    pg::DevBuf<double> out_e;     // n per-atom energy
+    pg::DevBuf<double> out_w;     // n x 6 per-atom virial
+    pg::DevBuf<double> out_tot;   // energy, virial[6], k-space energy, extras
+    pg::DevBuf<double> red_part;  // reduction partials
+
+    // charge relaxation
+    pg::DevBuf<double> rq_rate, rq_force, rq_stat;
+
+    int launches = 0;
+};
+
+namespace pg {
+
+// Fortran-style build of the cell arrays from the row-major cell and inverse.
+void make_cell(const double* cell, const double* inv, const int32_t* pbc, Cell& C);
+CellK cell_kernel_view(const Cell& C);
+
+// neighbor.cu
+void build_neighbor_lists(pg_context* ctx, const double* h_cutoffs);
+void build_short_list(pg_context* ctx);
+void build_allpairs_lists(pg_context* ctx, const double* h_cutoffs);
+void install_neighbor_lists(pg_context* ctx, const int32_t* counts, const int32_t* idx, const int32_t* off);
+
+// tables.cu
+void fold_tables(pg_context* ctx);
+
+// pair.cu: returns nothing; writes one partial per block into `partial`
+int pair_kernel_blocks(int n, int G);
+void launch_pair_kernel_impl(pg_context* ctx, int precision, int flags, bool first_f, bool first_chi, int G,
+                             double* partial);
+
+// tersoff.cu: returns the number of partial slots written
+int bond_blocks(int n, int G);
+int launch_bond_order_impl(pg_context* ctx, int precision, int flags, bool first_f, int G, double* partial);
+void bond_zeta_diag(pg_context* ctx);
+
+// ewald.cu
+void ewald_prepare(pg_context* ctx);
+int ewald_partial_slots(pg_context* ctx);
+void launch_ewald_kspace(pg_context* ctx, int precision, int flags, bool first_f, bool first_chi, double* partial);
+
+// reduce.cu
+void launch_final_reduce(pg_context* ctx, int nslots);
+
+// relax.cu
+void relax_charges(pg_context* ctx, int precision, int n_steps, double dt, double inertia, double friction,
+                   double tolerance, double* rates, double* charges, int* steps, double* error, double* max_dq);
+
+// api.cu
+void evaluate(pg_context* ctx, int precision, int flags);
+
+// utilities
+void exclusive_scan_int(const int* in, int* out, int n, cudaStream_t s, DevBuf<int>& tmp, int* total_host);
+
+}  // namespace pg

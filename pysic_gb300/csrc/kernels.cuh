@@ -1,0 +1,188 @@
+// kernels.cuh -- device-side physics shared by the pair, bond-order and batched
+// kernels, templated on the per-term arithmetic type R (double for the FP64
+// path, float for the mixed path).
+#pragma once
+#include <cuda_runtime.h>
+
+#include "common.cuh"
+
+namespace pg {
+
+template <typename R>
+struct V3 {
+    R x, y, z;
+};
+
+template <typename R>
+__device__ __forceinline__ R rcp_(R x) {
+    return R(1) / x;
+}
+
+__device__ __forceinline__ void sincospi_(float x, float* s, float* c) { sincospif(x, s, c); }
+__device__ __forceinline__ void sincospi_(double x, double* s, double* c) { sincospi(x, s, c); }
+__device__ __forceinline__ float exp_(float x) { return expf(x); }
+__device__ __forceinline__ double exp_(double x) { return exp(x); }
+__device__ __forceinline__ float pow_(float x, float y) { return powf(x, y); }
+__device__ __forceinline__ double pow_(double x, double y) { return pow(x, y); }
+__device__ __forceinline__ float sqrt_(float x) { return sqrtf(x); }
+__device__ __forceinline__ double sqrt_(double x) { return sqrt(x); }
+__device__ __forceinline__ float erfc_(float x) { return erfcf(x); }
+__device__ __forceinline__ double erfc_(double x) { return erfc(x); }
+
+// Smooth cutoff f(r) = 1/2 (1 + cos(pi (r - rs)/(rc - rs))) on [rs, rc] and its
+// derivative (smoothening_factor / smoothening_derivative, Potentials.f90:442-498).
+template <typename R>
+__device__ __forceinline__ void smooth(R r, R rc, R rs, R& f, R& fp) {
+    if (r > rc) {
+        f = R(0);
+        fp = R(0);
+    } else if (r < rs) {
+        f = R(1);
+        fp = R(0);
+    } else {
+        const R w = rc - rs;
+        R s, c;
+        sincospi_((r - rs) / w, &s, &c);
+        f = R(0.5) * (R(1) + c);
+        fp = R(-0.5) * R(3.14159265358979323846) / w * s;
+    }
+}
+
+// V(r) and the radial derivative dV/dr of LJ (Potentials.f90:2971-3005),
+// exponential (3643-3680) and Buckingham (4009-4045); no factor 4 in LJ.
+template <typename R>
+__device__ __forceinline__ void pair_eval(int kind, R p0, R p1, R p2, R r, R& V, R& dV) {
+    if (kind == 0) {
+        const R ratio = p1 / r;
+        const R r2 = ratio * ratio;
+        const R r6 = r2 * r2 * r2;
+        V = p0 * (r6 * r6 - r6);
+        dV = p0 * (R(6) * r6 - R(12) * r6 * r6) / r;
+    } else if (kind == 1) {
+        const R e = p0 * exp_(-p1 * r);
+        V = e;
+        dV = -p1 * e;
+    } else {
+        const R ratio = r / p2;
+        const R q2 = R(1) / (ratio * ratio);
+        const R r6 = q2 * q2 * q2;
+        const R e = p0 * exp_(-ratio);
+        V = e - p1 * r6;
+        dV = (-e * ratio + R(6) * p1 * r6) / r;
+    }
+}
+
+// Tersoff triplet parameters in working precision
+template <typename R>
+struct Trip {
+    R a, c2, d2, h, mu, rc, rs;
+};
+
+template <typename R>
+__device__ __forceinline__ Trip<R> load_trip(const TripletTerm& T) {
+    Trip<R> t;
+    t.a = (R)T.a;
+    t.c2 = (R)T.c2;
+    t.d2 = (R)T.d2;
+    t.h = (R)T.h;
+    t.mu = (R)T.mu;
+    t.rc = (R)T.rc;
+    t.rs = (R)T.rs;
+    return t;
+}
+
+// Angular function g = 1 + c^2/d^2 - c^2/(d^2 + (h - cos)^2) of
+// evaluate_pair_bond_order_factor_tersoff (Potentials.f90:5790), written in the
+// algebraically equal form 1 + c^2 x / (d^2 (d^2 + x)), x = (h - cos)^2, which
+// does not cancel catastrophically in FP32 (c^2/d^2 is ~4e7 for silicon);
+// dg/dcos = -2 c^2 (h - cos) / (d^2 + x)^2.
+template <typename R>
+__device__ __forceinline__ void angular(const Trip<R>& t, R cs, R& g, R& dg) {
+    const R hc = t.h - cs;
+    const R x = hc * hc;
+    const R den = t.d2 + x;
+    const R inv = R(1) / den;
+    g = R(1) + t.c2 * x * inv / t.d2;
+    dg = R(-2) * t.c2 * hc * inv * inv;
+}
+
+// exp((a (r1 - r2))^mu) and its derivative with respect to r1 - r2
+template <typename R>
+__device__ __forceinline__ void radial_exp(const Trip<R>& t, R dr, R& X, R& Xp) {
+    if (t.a == R(0)) {
+        X = R(1);
+        Xp = R(0);
+    } else {
+        const R u = t.a * dr;
+        const R um1 = pow_(u, t.mu - R(1));
+        X = exp_(u * um1);
+        Xp = X * t.mu * t.a * um1;
+    }
+}
+
+// zeta term xi_ijk g_ijk for bond ij (vector a, length r1) and neighbour k
+// (vector b, length r2), Potentials.f90:5744-5795
+template <typename R>
+__device__ __forceinline__ R tersoff_term(const Trip<R>& t, const V3<R>& a, R r1, const V3<R>& b, R r2) {
+    R f, fp;
+    smooth(r2, t.rc, t.rs, f, fp);
+    if (f == R(0)) return R(0);
+    const R cs = (a.x * b.x + a.y * b.y + a.z * b.z) / (r1 * r2);
+    R g, dg;
+    angular(t, cs, g, dg);
+    R X, Xp;
+    radial_exp(t, r1 - r2, X, Xp);
+    return f * X * g;
+}
+
+// gradient of the zeta term with respect to the positions of j and k
+// (the gradient with respect to the centre i is minus their sum);
+// Potentials.f90:5806-5902 computes the same derivatives.
+template <typename R>
+__device__ __forceinline__ bool tersoff_grad(const Trip<R>& t, const V3<R>& a, R r1, const V3<R>& b, R r2, V3<R>& gj,
+                                             V3<R>& gk) {
+    R f, fp;
+    smooth(r2, t.rc, t.rs, f, fp);
+    if (f == R(0) && fp == R(0)) return false;
+    const R i1 = R(1) / r1, i2 = R(1) / r2;
+    const V3<R> ua{a.x * i1, a.y * i1, a.z * i1};
+    const V3<R> ub{b.x * i2, b.y * i2, b.z * i2};
+    const R cs = ua.x * ub.x + ua.y * ub.y + ua.z * ub.z;
+    R g, dg;
+    angular(t, cs, g, dg);
+    R X, Xp;
+    radial_exp(t, r1 - r2, X, Xp);
+    const R xi = f * X;
+    // d/dr_j : g f Xp ua + xi dg (ub - cs ua)/r1
+    const R cj = g * f * Xp - xi * dg * cs * i1;
+    const R cjb = xi * dg * i1;
+    gj.x = cj * ua.x + cjb * ub.x;
+    gj.y = cj * ua.y + cjb * ub.y;
+    gj.z = cj * ua.z + cjb * ub.z;
+    // d/dr_k : g (fp X - f Xp) ub + xi dg (ua - cs ub)/r2
+    const R ck = g * (fp * X - f * Xp) - xi * dg * cs * i2;
+    const R cka = xi * dg * i2;
+    gk.x = ck * ub.x + cka * ua.x;
+    gk.y = ck * ub.y + cka * ua.y;
+    gk.z = ck * ub.z + cka * ua.z;
+    return true;
+}
+
+// B(zeta) = (1 + (beta zeta)^eta)^(-1/(2 eta)) and dB/dzeta
+// (post_process_bond_order_factor_tersoff / _gradient_tersoff, Potentials.f90:5910-5961)
+template <typename R>
+__device__ __forceinline__ void post_process(R beta, R eta, R zeta, R& B, R& dB) {
+    const R tt = pow_(beta * zeta, eta);
+    B = pow_(R(1) + tt, R(-0.5) / eta);
+    dB = zeta > R(0) ? R(-0.5) * B * tt / ((R(1) + tt) * zeta) : R(0);
+}
+
+// warp-segment reductions over groups of G lanes
+template <int G, typename T>
+__device__ __forceinline__ T group_sum(T v) {
+#pragma unroll
+    for (int o = G / 2; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o, G);
+    return v;
+}
+
+}  // namespace pg

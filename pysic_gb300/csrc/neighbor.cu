@@ -1,0 +1,811 @@
+// neighbor.cu -- FastNeighborList on the GPU.
+//
+// Reproduces core_create_space_partitioning + core_build_neighbor_lists
+// (fortran/Core.f90:8130-8280, fortran/Geometry.f90:597-924) bit for bit,
+// entry order included:
+//
+//  1. nb_assign: per atom, wrapped_coordinates and find_subcell_for_atom
+//     (the same FP64 operations in the same order, no fused multiply-add).
+//  2. A stable, atomics-free LSD radix sort of atoms by subcell id: the
+//     subcell contents come out in ascending atom index, as the serial
+//     insertion loop leaves them.
+//  3. nb_scan<COUNT/FILL>: one warp per atom walks its 27 stencil subcells.
+//     In the reference, atom a's list receives entries from the sweeps of
+//     lower-index atoms b (ordered by b, then by b's stencil slot) followed by
+//     the entries of a's own sweep (stencil order, subcell order; a periodic
+//     self image adds (a, o) then (a, -o)).  Because a is found in b's slot s
+//     exactly when b is in a's slot 26 - s with the opposite subcell offset,
+//     and the separation seen from b is the exact negation of the one seen
+//     from a, every entry can be produced from a's own stencil.  Entries of the
+//     first kind carry the sort key (b, 26 - s); atoms that the reference puts
+//     into an out-of-range subcell of a periodic axis are swept but never
+//     found by others, and are handled by an explicit pass.
+//  4. nb_sort_g0: per atom, the lower-index entries are placed by rank of key.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <vector>
+
+#include "common.cuh"
+
+namespace pg {
+
+namespace {
+
+struct Split {
+    int sp[3];
+    int nx, ny, nz;
+};
+
+// wrapped_coordinates + find_subcell_for_atom (Geometry.f90:597-619, 884-924)
+__global__ void nb_assign(int n, const double* __restrict__ pos, CellK C, Split S, int* __restrict__ cell_of,
+                          int* __restrict__ key, int* __restrict__ val, int* __restrict__ wrap,
+                          int* __restrict__ invisible) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    double p[3] = {pos[3 * i], pos[3 * i + 1], pos[3 * i + 2]};
+    double rel[3];
+    for (int r = 0; r < 3; ++r)
+        rel[r] = __dadd_rn(__dadd_rn(__dmul_rn(C.ic[r][0], p[0]), __dmul_rn(C.ic[r][1], p[1])),
+                           __dmul_rn(C.ic[r][2], p[2]));
+    int off[3];
+    for (int a = 0; a < 3; ++a) {
+        off[a] = 0;
+        if (C.pbc[a]) {
+            off[a] = -(int)floor(rel[a]);
+            rel[a] = __dadd_rn(rel[a], (double)off[a]);
+        }
+    }
+    double w[3];
+    for (int r = 0; r < 3; ++r)
+        w[r] = __dadd_rn(__dadd_rn(__dmul_rn(C.vc[r][0], rel[0]), __dmul_rn(C.vc[r][1], rel[1])),
+                         __dmul_rn(C.vc[r][2], rel[2]));
+    double f[3];
+    for (int r = 0; r < 3; ++r)
+        f[r] = __dadd_rn(__dadd_rn(__dmul_rn(C.ic[r][0], w[0]), __dmul_rn(C.ic[r][1], w[1])),
+                         __dmul_rn(C.ic[r][2], w[2]));
+    int idx[3];
+    int inv = 0;
+    for (int a = 0; a < 3; ++a) {
+        double x = floor(__dmul_rn(f[a], (double)S.sp[a]));
+        x = fmin(fmax(x, -1.0e9), 1.0e9);
+        int k = (int)x;
+        if (C.pbc[a]) {
+            idx[a] = k % S.sp[a] + 1;  // Fortran mod: sign of the dividend
+            if (idx[a] < 1 || idx[a] > S.sp[a]) inv = 1;
+        } else {
+            idx[a] = min(S.sp[a] + 1, max(0, k + 1));
+        }
+    }
+    // index 0 of a periodic axis is possible only by rounding; lower values are not
+    for (int a = 0; a < 3; ++a) idx[a] = max(idx[a], 0);
+    int c = (idx[2] * S.ny + idx[1]) * S.nx + idx[0];
+    cell_of[3 * i] = idx[0];
+    cell_of[3 * i + 1] = idx[1];
+    cell_of[3 * i + 2] = idx[2];
+    key[i] = c;
+    val[i] = i;
+    wrap[3 * i] = off[0];
+    wrap[3 * i + 1] = off[1];
+    wrap[3 * i + 2] = off[2];
+    invisible[i] = inv;
+}
+
+// ---- stable LSD radix sort (8-bit digits), atomics-free -------------------
+constexpr int RS_THREADS = 256;
+constexpr int RS_ROUNDS = 4;
+constexpr int RS_TILE = RS_THREADS * RS_ROUNDS;
+
+__global__ void radix_hist(int n, const int* __restrict__ keys, int shift, int nblocks, int* __restrict__ hist) {
+    __shared__ int whist[RS_THREADS / 32][256];
+    const int tid = threadIdx.x, lane = tid & 31, w = tid >> 5;
+    for (int d = lane; d < 256; d += 32) whist[w][d] = 0;
+    __syncwarp();
+    const int tile0 = blockIdx.x * RS_TILE;
+    for (int r = 0; r < RS_ROUNDS; ++r) {
+        int e = tile0 + r * RS_THREADS + tid;
+        int d = e < n ? (keys[e] >> shift) & 255 : -1;
+        unsigned peers = __match_any_sync(0xffffffffu, d);
+        int leader = __ffs(peers) - 1;
+        if (d >= 0 && lane == leader) whist[w][d] += __popc(peers);
+        __syncwarp();
+    }
+    __syncthreads();
+    int sum = 0;
+    for (int ww = 0; ww < RS_THREADS / 32; ++ww) sum += whist[ww][tid];
+    hist[tid * nblocks + blockIdx.x] = sum;
+}
+
+__global__ void radix_scatter(int n, const int* __restrict__ keys, const int* __restrict__ vals, int shift,
+                              int nblocks, const int* __restrict__ offs, int* __restrict__ okeys,
+                              int* __restrict__ ovals) {
+    __shared__ int whist[RS_THREADS / 32][256];
+    __shared__ int run[256];
+    const int tid = threadIdx.x, lane = tid & 31, w = tid >> 5;
+    run[tid] = offs[tid * nblocks + blockIdx.x];
+    const int tile0 = blockIdx.x * RS_TILE;
+    for (int r = 0; r < RS_ROUNDS; ++r) {
+        for (int ww = 0; ww < RS_THREADS / 32; ++ww) whist[ww][tid] = 0;
+        __syncthreads();
+        int e = tile0 + r * RS_THREADS + tid;
+        int k = e < n ? keys[e] : 0;
+        int d = e < n ? (k >> shift) & 255 : -1;
+        unsigned peers = __match_any_sync(0xffffffffu, d);
+        int leader = __ffs(peers) - 1;
+        if (d >= 0 && lane == leader) whist[w][d] = __popc(peers);
+        __syncthreads();
+        if (d >= 0) {
+            int rank = run[d] + __popc(peers & ((1u << lane) - 1u));
+            for (int ww = 0; ww < w; ++ww) rank += whist[ww][d];
+            okeys[rank] = k;
+            ovals[rank] = vals[e];
+        }
+        __syncthreads();
+        int add = 0;
+        for (int ww = 0; ww < RS_THREADS / 32; ++ww) add += whist[ww][tid];
+        run[tid] += add;
+        __syncthreads();
+    }
+}
+
+__global__ void cell_starts(int n, int ncell, const int* __restrict__ skeys, int* __restrict__ start) {
+    int p = blockIdx.x * blockDim.x + threadIdx.x;
+    if (p > n) return;
+    int lo = p == 0 ? -1 : skeys[p - 1];
+    int hi = p == n ? ncell : skeys[p];
+    for (int c = lo + 1; c <= hi && c <= ncell; ++c) start[c] = p;
+}
+
+// single-block exclusive scan (build-time sizes only)
+template <typename T, typename U>
+__global__ void scan_single_block(const T* __restrict__ in, U* __restrict__ out, int n, U* __restrict__ total,
+                                  int square) {
+    __shared__ U part[1024];
+    const int t = threadIdx.x, nt = blockDim.x;
+    const long long per = ((long long)n + nt - 1) / nt;
+    long long b = per * t, e = min((long long)n, b + per);
+    U s = 0;
+    for (long long i = b; i < e; ++i) {
+        U v = (U)in[i];
+        s += square ? v * v : v;
+    }
+    part[t] = s;
+    __syncthreads();
+    for (int off = 1; off < nt; off <<= 1) {
+        U v = t >= off ? part[t - off] : 0;
+        __syncthreads();
+        part[t] += v;
+        __syncthreads();
+    }
+    U run = t == 0 ? 0 : part[t - 1];
+    for (long long i = b; i < e; ++i) {
+        out[i] = run;
+        U v = (U)in[i];
+        run += square ? v * v : v;
+    }
+    if (t == nt - 1) {
+        out[n] = part[nt - 1];
+        if (total) *total = part[nt - 1];
+    }
+}
+
+// subcell stencil of divide_cell (Geometry.f90:820-858)
+__device__ __forceinline__ bool stencil(const int ci[3], int s, const int sp[3], const int pbc[3], int nb[3],
+                                        int noff[3]) {
+    const int d[3] = {s % 3 - 1, (s / 3) % 3 - 1, s / 9 - 1};
+    bool inc = true;
+    for (int a = 0; a < 3; ++a) {
+        nb[a] = ci[a] + d[a];
+        noff[a] = 0;
+        if (pbc[a]) {
+            while (nb[a] > sp[a]) {
+                nb[a] -= sp[a];
+                noff[a] += 1;
+            }
+            while (nb[a] < 1) {
+                nb[a] += sp[a];
+                noff[a] -= 1;
+            }
+        } else if (nb[a] < 0 || nb[a] > sp[a] + 1) {
+            inc = false;
+            nb[a] = 0;
+        }
+    }
+    return inc;
+}
+
+// separation_vector + .o. (Geometry.f90:449-466, Quaternions.f90:475-484)
+__device__ __forceinline__ double sep_d2(const CellK& C, const double* ra, const double* rb, const int o[3]) {
+    double s[3];
+    for (int c = 0; c < 3; ++c) s[c] = __dsub_rn(rb[c], ra[c]);
+    for (int i = 0; i < 3; ++i)
+        for (int c = 0; c < 3; ++c) s[c] = __dadd_rn(s[c], __dmul_rn((double)o[i], C.vc[c][i]));
+    return __dadd_rn(__dadd_rn(__dmul_rn(s[0], s[0]), __dmul_rn(s[1], s[1])), __dmul_rn(s[2], s[2]));
+}
+
+__device__ __forceinline__ bool lex_positive(const int o[3]) {
+    if (o[0] != 0) return o[0] > 0;
+    if (o[1] != 0) return o[1] > 0;
+    return o[2] > 0;
+}
+
+struct ScanArgs {
+    int n;
+    const double* pos;
+    const double* cut;
+    const int* cell_of;
+    const int* wrap;
+    const int* cstart;
+    const int* sorted;
+    const int* invisible;
+    const int* inv_list;
+    int n_inv;
+    CellK C;
+    Split S;
+    // outputs
+    int* g0count;
+    int* g1count;
+    const int* start;    // CSR start (FILL)
+    const int* g0start;  // start of the atom's lower-index entries in the key buffer (FILL)
+    long long* g0key;
+    int4* g0val;
+    int* idx;
+    int* off;
+};
+
+template <bool FILL>
+__global__ void nb_scan(ScanArgs A) {
+    const int lane = threadIdx.x & 31;
+    const int a = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    if (a >= A.n) return;
+    const double ra[3] = {A.pos[3 * a], A.pos[3 * a + 1], A.pos[3 * a + 2]};
+    const double cut2 = __dmul_rn(A.cut[a], A.cut[a]);
+    const int ci[3] = {A.cell_of[3 * a], A.cell_of[3 * a + 1], A.cell_of[3 * a + 2]};
+    const int wa[3] = {A.wrap[3 * a], A.wrap[3 * a + 1], A.wrap[3 * a + 2]};
+    const bool visible = A.invisible[a] == 0;
+    const int lt = (1u << lane) - 1u;
+    int n0 = 0, n1 = 0;
+    int base1 = 0, base0 = 0;
+    if (FILL) {
+        base1 = A.start[a] + A.g0count[a];
+        base0 = A.g0start[a];
+    }
+    for (int s = 0; s < 27; ++s) {
+        int nb[3], noff[3];
+        if (!stencil(ci, s, A.S.sp, A.C.pbc, nb, noff)) continue;
+        const int c = (nb[2] * A.S.ny + nb[1]) * A.S.nx + nb[0];
+        const int beg = A.cstart[c], end = A.cstart[c + 1];
+        const bool self_pos = lex_positive(noff);
+        for (int t0 = beg; t0 < end; t0 += 32) {
+            const int t = t0 + lane;
+            int b = -1, mult = 0, grp = -1;
+            int o[3] = {0, 0, 0};
+            if (t < end) {
+                b = A.sorted[t];
+                if (b > a) {
+                    grp = 1;
+                    mult = 1;
+                } else if (b == a) {
+                    if (self_pos) {
+                        grp = 1;
+                        mult = 2;
+                    }
+                } else if (visible) {
+                    grp = 0;
+                    mult = 1;
+                }
+                if (mult) {
+                    for (int q = 0; q < 3; ++q) o[q] = noff[q] - wa[q] + A.wrap[3 * b + q];
+                    const double rb[3] = {A.pos[3 * b], A.pos[3 * b + 1], A.pos[3 * b + 2]};
+                    if (!(sep_d2(A.C, ra, rb, o) < cut2)) mult = 0;
+                }
+            }
+            const unsigned m0 = __ballot_sync(0xffffffffu, mult && grp == 0);
+            const unsigned m1 = __ballot_sync(0xffffffffu, mult && grp == 1);
+            const unsigned m2 = __ballot_sync(0xffffffffu, mult == 2);
+            if (FILL && mult) {
+                if (grp == 0) {
+                    int p = base0 + n0 + __popc(m0 & lt);
+                    A.g0key[p] = ((long long)b << 5) | (long long)(26 - s);
+                    A.g0val[p] = make_int4(b, o[0], o[1], o[2]);
+                } else {
+                    int p = base1 + n1 + __popc(m1 & lt) + __popc(m2 & lt);
+                    A.idx[p] = b;
+                    A.off[3 * p] = o[0];
+                    A.off[3 * p + 1] = o[1];
+                    A.off[3 * p + 2] = o[2];
+                    if (mult == 2) {
+                        A.idx[p + 1] = b;
+                        A.off[3 * p + 3] = -o[0];
+                        A.off[3 * p + 4] = -o[1];
+                        A.off[3 * p + 5] = -o[2];
+                    }
+                }
+            }
+            n0 += __popc(m0);
+            n1 += __popc(m1) + __popc(m2);
+        }
+    }
+    // lower-index atoms in out-of-range subcells of a periodic axis: their
+    // sweep can reach a, but a's stencil never reaches them
+    if (visible && A.n_inv > 0) {
+        for (int q0 = 0; q0 < A.n_inv; q0 += 32) {
+            const int q = q0 + lane;
+            int cnt = 0;
+            int b = q < A.n_inv ? A.inv_list[q] : a;
+            long long keys[27];
+            int4 vals[27];
+            if (b < a) {
+                const int cb[3] = {A.cell_of[3 * b], A.cell_of[3 * b + 1], A.cell_of[3 * b + 2]};
+                const int wb[3] = {A.wrap[3 * b], A.wrap[3 * b + 1], A.wrap[3 * b + 2]};
+                const double rb[3] = {A.pos[3 * b], A.pos[3 * b + 1], A.pos[3 * b + 2]};
+                for (int s = 0; s < 27; ++s) {
+                    int nb[3], noff[3];
+                    if (!stencil(cb, s, A.S.sp, A.C.pbc, nb, noff)) continue;
+                    if (nb[0] != ci[0] || nb[1] != ci[1] || nb[2] != ci[2]) continue;
+                    int o[3];
+                    for (int k = 0; k < 3; ++k) o[k] = -noff[k] + wb[k] - wa[k];
+                    if (sep_d2(A.C, ra, rb, o) < cut2) {
+                        keys[cnt] = ((long long)b << 5) | (long long)s;
+                        vals[cnt] = make_int4(b, o[0], o[1], o[2]);
+                        ++cnt;
+                    }
+                }
+            }
+            // inclusive prefix of cnt over lanes
+            int incl = cnt;
+            for (int d = 1; d < 32; d <<= 1) {
+                int v = __shfl_up_sync(0xffffffffu, incl, d);
+                if (lane >= d) incl += v;
+            }
+            const int excl = incl - cnt;
+            const int tot = __shfl_sync(0xffffffffu, incl, 31);
+            if (FILL)
+                for (int k = 0; k < cnt; ++k) {
+                    A.g0key[base0 + n0 + excl + k] = keys[k];
+                    A.g0val[base0 + n0 + excl + k] = vals[k];
+                }
+            n0 += tot;
+        }
+    }
+    if (!FILL && lane == 0) {
+        A.g0count[a] = n0;
+        A.g1count[a] = n1;
+    }
+}
+
+__global__ void add_counts(int n, const int* __restrict__ a, const int* __restrict__ b, int* __restrict__ c) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) c[i] = a[i] + b[i];
+}
+
+// place the lower-index entries of each atom by the rank of their key
+__global__ void nb_sort_g0(int n, const int* __restrict__ g0count, const int* __restrict__ g0start,
+                           const int* __restrict__ start, const long long* __restrict__ key,
+                           const int4* __restrict__ val, int* __restrict__ idx, int* __restrict__ off) {
+    const int lane = threadIdx.x & 31;
+    const int a = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    if (a >= n) return;
+    const int m = g0count[a], b0 = g0start[a], dst = start[a];
+    for (int e = lane; e < m; e += 32) {
+        const long long k = key[b0 + e];
+        int rank = 0;
+        for (int f = 0; f < m; ++f) rank += key[b0 + f] < k;
+        const int4 v = val[b0 + e];
+        idx[dst + rank] = v.x;
+        off[3 * (dst + rank)] = v.y;
+        off[3 * (dst + rank) + 1] = v.z;
+        off[3 * (dst + rank) + 2] = v.w;
+    }
+}
+
+__global__ void compact_flags(int n, const int* __restrict__ flag, const int* __restrict__ pos, int* __restrict__ out) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n && flag[i]) out[pos[i]] = i;
+}
+
+// ---- short list for bond-order terms -----------------------------------------
+__device__ __forceinline__ double entry_d2(const CellK& C, const double* __restrict__ pos, int a, int b, const int* o) {
+    const double ra[3] = {pos[3 * a], pos[3 * a + 1], pos[3 * a + 2]};
+    const double rb[3] = {pos[3 * b], pos[3 * b + 1], pos[3 * b + 2]};
+    return sep_d2(C, ra, rb, o);
+}
+
+__global__ void short_count(int n, const double* __restrict__ pos, CellK C, const int* __restrict__ start,
+                            const int* __restrict__ idx, const int* __restrict__ off, double r2,
+                            int* __restrict__ cnt) {
+    int a = blockIdx.x * blockDim.x + threadIdx.x;
+    if (a >= n) return;
+    int c = 0;
+    for (int e = start[a]; e < start[a + 1]; ++e)
+        if (entry_d2(C, pos, a, idx[e], off + 3 * e) < r2) ++c;
+    cnt[a] = c;
+}
+
+__global__ void short_fill(int n, const double* __restrict__ pos, CellK C, const int* __restrict__ start,
+                           const int* __restrict__ idx, const int* __restrict__ off, double r2,
+                           const int* __restrict__ sstart, int* __restrict__ sidx, int* __restrict__ soff) {
+    int a = blockIdx.x * blockDim.x + threadIdx.x;
+    if (a >= n) return;
+    int p = sstart[a];
+    for (int e = start[a]; e < start[a + 1]; ++e)
+        if (entry_d2(C, pos, a, idx[e], off + 3 * e) < r2) {
+            sidx[p] = idx[e];
+            soff[3 * p] = off[3 * e];
+            soff[3 * p + 1] = off[3 * e + 1];
+            soff[3 * p + 2] = off[3 * e + 2];
+            ++p;
+        }
+}
+
+__global__ void short_reverse(int n, const int* __restrict__ start, const int* __restrict__ idx,
+                              const int* __restrict__ off, int* __restrict__ rev, int* __restrict__ cnt) {
+    int a = blockIdx.x * blockDim.x + threadIdx.x;
+    if (a >= n) return;
+    cnt[a] = start[a + 1] - start[a];
+    for (int e = start[a]; e < start[a + 1]; ++e) {
+        const int b = idx[e];
+        int r = -1;
+        for (int f = start[b]; f < start[b + 1]; ++f)
+            if (idx[f] == a && off[3 * f] == -off[3 * e] && off[3 * f + 1] == -off[3 * e + 1] &&
+                off[3 * f + 2] == -off[3 * e + 2]) {
+                r = f;
+                break;
+            }
+        rev[e] = r;
+    }
+}
+
+__global__ void max_reduce(int n, const int* __restrict__ v, int* __restrict__ out) {
+    __shared__ int sm[1024];
+    int m = 0;
+    for (int i = threadIdx.x; i < n; i += blockDim.x) m = max(m, v[i]);
+    sm[threadIdx.x] = m;
+    __syncthreads();
+    for (int s = blockDim.x / 2; s > 0; s >>= 1) {
+        if (threadIdx.x < s) sm[threadIdx.x] = max(sm[threadIdx.x], sm[threadIdx.x + s]);
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) *out = sm[0];
+}
+
+__global__ void min_reduce(int n, const int* __restrict__ v, int* __restrict__ out) {
+    __shared__ int sm[1024];
+    int m = 0x7fffffff;
+    for (int i = threadIdx.x; i < n; i += blockDim.x) m = min(m, v[i]);
+    sm[threadIdx.x] = m;
+    __syncthreads();
+    for (int s = blockDim.x / 2; s > 0; s >>= 1) {
+        if (threadIdx.x < s) sm[threadIdx.x] = min(sm[threadIdx.x], sm[threadIdx.x + s]);
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) *out = sm[0];
+}
+
+// ---- all-pairs list for cells narrower than the cutoff --------------------
+// The reference hands such systems to ASE's NeighborList (calculator.py:829-848,
+// 905-915): both directions, no self pair, atoms i and j are neighbours when
+// |r_j + n.cell - r_i| < c_i + c_j (cutoffs include the skin).  Order here:
+// partner index, then image offsets in lexicographic order.
+template <bool FILL>
+__global__ void allpairs_scan(int n, const double* __restrict__ pos, const double* __restrict__ cut, CellK C,
+                              int3 nimg, const int* __restrict__ start, int* __restrict__ cnt, int* __restrict__ idx,
+                              int* __restrict__ off) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const double ri[3] = {pos[3 * i], pos[3 * i + 1], pos[3 * i + 2]};
+    int c = 0;
+    const int base = FILL ? start[i] : 0;
+    for (int j = 0; j < n; ++j) {
+        const double rj[3] = {pos[3 * j], pos[3 * j + 1], pos[3 * j + 2]};
+        const double rr = cut[i] + cut[j];
+        const double rr2 = rr * rr;
+        for (int a = -nimg.x; a <= nimg.x; ++a)
+            for (int b = -nimg.y; b <= nimg.y; ++b)
+                for (int d = -nimg.z; d <= nimg.z; ++d) {
+                    if (j == i && a == 0 && b == 0 && d == 0) continue;
+                    const int o[3] = {a, b, d};
+                    if (sep_d2(C, ri, rj, o) < rr2) {
+                        if (FILL) {
+                            idx[base + c] = j;
+                            off[3 * (base + c)] = a;
+                            off[3 * (base + c) + 1] = b;
+                            off[3 * (base + c) + 2] = d;
+                        }
+                        ++c;
+                    }
+                }
+    }
+    if (!FILL) cnt[i] = c;
+}
+
+inline int blocks(long long n, int t) { return (int)((n + t - 1) / t); }
+
+}  // namespace
+
+// get_optimal_splitting, Geometry.f90:679-707 (host, no fused multiply-add)
+static void optimal_splitting(const Cell& C, double max_cut, int sp[3]) {
+    for (int i = 0; i < 3; ++i) {
+        int v1 = (i + 1) % 3, v2 = (i + 2) % 3;
+        double a[3], b[3], nn[3], v[3];
+        for (int r = 0; r < 3; ++r) {
+            a[r] = C.vc[r][v1];
+            b[r] = C.vc[r][v2];
+            v[r] = C.vc[r][i];
+        }
+        nn[0] = a[1] * b[2] - a[2] * b[1];
+        nn[1] = a[2] * b[0] - a[0] * b[2];
+        nn[2] = a[0] * b[1] - a[1] * b[0];
+        double len = std::fabs(v[0] * nn[0] + v[1] * nn[1] + v[2] * nn[2]) /
+                     std::sqrt(nn[0] * nn[0] + nn[1] * nn[1] + nn[2] * nn[2]);
+        if (max_cut < 0.1e-4)
+            sp[i] = (int)std::floor(10.0 * len);
+        else
+            sp[i] = (int)std::floor(len / max_cut);
+        if (sp[i] > 40) sp[i] = 40;
+    }
+}
+
+void exclusive_scan_int(const int* in, int* out, int n, cudaStream_t s, DevBuf<int>& tmp, int* total_host) {
+    tmp.resize(1);
+    scan_single_block<int, int><<<1, 1024, 0, s>>>(in, out, n, tmp.p, 0);
+    PG_CHECK_LAUNCH();
+    if (total_host) {
+        PG_CUDA(cudaMemcpyAsync(total_host, tmp.p, sizeof(int), cudaMemcpyDeviceToHost, s));
+        PG_CUDA(cudaStreamSynchronize(s));
+    }
+}
+
+void build_neighbor_lists(pg_context* ctx, const double* h_cutoffs) {
+    const int n = ctx->n;
+    cudaStream_t st = ctx->stream;
+    double max_cut = 0.0;
+    for (int i = 0; i < n; ++i)
+        if (i == 0 || h_cutoffs[i] > max_cut) max_cut = h_cutoffs[i];
+    int sp[3];
+    optimal_splitting(ctx->cell, max_cut, sp);
+    for (int a = 0; a < 3; ++a)
+        require(sp[a] >= 1, PG_ERR_SMALL_CELL,
+                "cell narrower than the neighbour cutoff: the cell-list build does not apply");
+    Split S;
+    for (int a = 0; a < 3; ++a) S.sp[a] = sp[a];
+    S.nx = sp[0] + 2;
+    S.ny = sp[1] + 2;
+    S.nz = sp[2] + 2;
+    const int ncell = S.nx * S.ny * S.nz;
+    CellK C = cell_kernel_view(ctx->cell);
+
+    ctx->cutoffs.upload(h_cutoffs, n, st);
+    ctx->cell_of.resize(3 * (size_t)std::max(n, 1));
+    ctx->wrap.resize(3 * (size_t)std::max(n, 1));
+    ctx->keys_a.resize(std::max(n, 1));
+    ctx->keys_b.resize(std::max(n, 1));
+    ctx->vals_a.resize(std::max(n, 1));
+    ctx->vals_b.resize(std::max(n, 1));
+    ctx->invisible.resize(std::max(n, 1) + 1);
+    ctx->cell_start.resize(ncell + 1);
+    if (n > 0) {
+        nb_assign<<<blocks(n, 256), 256, 0, st>>>(n, ctx->pos.p, C, S, ctx->cell_of.p, ctx->keys_a.p, ctx->vals_a.p,
+                                                  ctx->wrap.p, ctx->invisible.p);
+        PG_CHECK_LAUNCH();
+    }
+    // radix sort by subcell id
+    int bits = 1;
+    while ((1 << bits) < ncell) ++bits;
+    const int passes = (bits + 7) / 8;
+    const int nblk = std::max(1, blocks(n, RS_TILE));
+    ctx->radix_hist.resize((size_t)256 * nblk + 1);
+    ctx->count_tmp.resize((size_t)256 * nblk + 1);
+    int *k_in = ctx->keys_a.p, *v_in = ctx->vals_a.p, *k_out = ctx->keys_b.p, *v_out = ctx->vals_b.p;
+    for (int p = 0; p < passes && n > 0; ++p) {
+        radix_hist<<<nblk, RS_THREADS, 0, st>>>(n, k_in, 8 * p, nblk, ctx->radix_hist.p);
+        PG_CHECK_LAUNCH();
+        scan_single_block<int, int><<<1, 1024, 0, st>>>(ctx->radix_hist.p, ctx->count_tmp.p, 256 * nblk, nullptr, 0);
+        PG_CHECK_LAUNCH();
+        radix_scatter<<<nblk, RS_THREADS, 0, st>>>(n, k_in, v_in, 8 * p, nblk, ctx->count_tmp.p, k_out, v_out);
+        PG_CHECK_LAUNCH();
+        std::swap(k_in, k_out);
+        std::swap(v_in, v_out);
+    }
+    const int* sorted_keys = k_in;
+    const int* sorted_vals = v_in;
+    cell_starts<<<blocks(n + 1, 256), 256, 0, st>>>(n, ncell, sorted_keys, ctx->cell_start.p);
+    PG_CHECK_LAUNCH();
+    ctx->sorted_atoms.resize(std::max(n, 1));
+    if (n > 0)
+        PG_CUDA(cudaMemcpyAsync(ctx->sorted_atoms.p, sorted_vals, sizeof(int) * n, cudaMemcpyDeviceToDevice, st));
+
+    // atoms in out-of-range periodic subcells
+    ctx->scan_tmp.resize(std::max(n, 1) + 1);
+    int n_inv = 0;
+    exclusive_scan_int(ctx->invisible.p, ctx->scan_tmp.p, n, st, ctx->count_tmp, &n_inv);
+    DevBuf<int>& inv_list = ctx->keys_b;  // free after the sort
+    if (n_inv > 0) {
+        compact_flags<<<blocks(n, 256), 256, 0, st>>>(n, ctx->invisible.p, ctx->scan_tmp.p, inv_list.p);
+        PG_CHECK_LAUNCH();
+    }
+    // inv_list may alias the sort's output buffer: copy the sorted atoms first (done above)
+
+    ScanArgs A{};
+    A.n = n;
+    A.pos = ctx->pos.p;
+    A.cut = ctx->cutoffs.p;
+    A.cell_of = ctx->cell_of.p;
+    A.wrap = ctx->wrap.p;
+    A.cstart = ctx->cell_start.p;
+    A.sorted = ctx->sorted_atoms.p;
+    A.invisible = ctx->invisible.p;
+    A.inv_list = inv_list.p;
+    A.n_inv = n_inv;
+    A.C = C;
+    A.S = S;
+    ctx->nb_g0.resize(std::max(n, 1));
+    ctx->vals_a.resize(std::max(n, 1));
+    A.g0count = ctx->nb_g0.p;
+    A.g1count = ctx->vals_a.p;
+    if (n > 0) {
+        nb_scan<false><<<blocks((long long)n * 32, 256), 256, 0, st>>>(A);
+        PG_CHECK_LAUNCH();
+    }
+    // CSR starts and lower-index key buffer starts
+    ctx->nb_start.resize(n + 1);
+    ctx->g0_start.resize(n + 1);
+    ctx->keys_a.resize(std::max(n, 1));
+    if (n > 0) {
+        add_counts<<<blocks(n, 256), 256, 0, st>>>(n, ctx->nb_g0.p, ctx->vals_a.p, ctx->keys_a.p);
+        PG_CHECK_LAUNCH();
+    }
+    int total = 0, total0 = 0;
+    exclusive_scan_int(ctx->keys_a.p, ctx->nb_start.p, n, st, ctx->count_tmp, &total);
+    exclusive_scan_int(ctx->nb_g0.p, ctx->g0_start.p, n, st, ctx->count_tmp, &total0);
+    ctx->nb_total = total;
+    ctx->nb_idx.resize(std::max(total, 1));
+    ctx->nb_off.resize(3 * (size_t)std::max(total, 1));
+    ctx->g0_keys.resize(std::max(total0, 1));
+    ctx->g0_vals.resize(std::max(total0, 1));
+    A.start = ctx->nb_start.p;
+    A.g0start = ctx->g0_start.p;
+    A.g0key = ctx->g0_keys.p;
+    A.g0val = ctx->g0_vals.p;
+    A.idx = ctx->nb_idx.p;
+    A.off = ctx->nb_off.p;
+    if (n > 0) {
+        nb_scan<true><<<blocks((long long)n * 32, 256), 256, 0, st>>>(A);
+        PG_CHECK_LAUNCH();
+        nb_sort_g0<<<blocks((long long)n * 32, 256), 256, 0, st>>>(n, ctx->nb_g0.p, ctx->g0_start.p, ctx->nb_start.p,
+                                                                  ctx->g0_keys.p, ctx->g0_vals.p, ctx->nb_idx.p,
+                                                                  ctx->nb_off.p);
+        PG_CHECK_LAUNCH();
+    }
+    PG_CUDA(cudaStreamSynchronize(st));
+    ctx->have_list = true;
+    ctx->short_dirty = true;
+}
+
+
+void build_allpairs_lists(pg_context* ctx, const double* h_cutoffs) {
+    const int n = ctx->n;
+    cudaStream_t st = ctx->stream;
+    double mc = 0.0;
+    for (int i = 0; i < n; ++i) mc = std::max(mc, h_cutoffs[i]);
+    const Cell& Cc = ctx->cell;
+    int ni[3];
+    for (int i = 0; i < 3; ++i) {
+        ni[i] = 0;
+        if (!Cc.pbc[i]) continue;
+        int v1 = (i + 1) % 3, v2 = (i + 2) % 3;
+        double a[3], b[3], nn[3], v[3];
+        for (int r = 0; r < 3; ++r) {
+            a[r] = Cc.vc[r][v1];
+            b[r] = Cc.vc[r][v2];
+            v[r] = Cc.vc[r][i];
+        }
+        nn[0] = a[1] * b[2] - a[2] * b[1];
+        nn[1] = a[2] * b[0] - a[0] * b[2];
+        nn[2] = a[0] * b[1] - a[1] * b[0];
+        double len = std::fabs(v[0] * nn[0] + v[1] * nn[1] + v[2] * nn[2]) /
+                     std::sqrt(nn[0] * nn[0] + nn[1] * nn[1] + nn[2] * nn[2]);
+        require(len > 0.0, PG_ERR_INVALID, "degenerate periodic cell");
+        ni[i] = (int)std::ceil(2.0 * mc / len);
+        require(ni[i] <= 64, PG_ERR_INVALID, "cutoff spans too many periodic images");
+    }
+    CellK C = cell_kernel_view(Cc);
+    ctx->cutoffs.upload(h_cutoffs, n, st);
+    ctx->nb_g0.resize(std::max(n, 1));
+    ctx->nb_start.resize(n + 1);
+    const int3 nimg = make_int3(ni[0], ni[1], ni[2]);
+    if (n > 0) {
+        allpairs_scan<false><<<blocks(n, 128), 128, 0, st>>>(n, ctx->pos.p, ctx->cutoffs.p, C, nimg, nullptr,
+                                                             ctx->nb_g0.p, nullptr, nullptr);
+        PG_CHECK_LAUNCH();
+    }
+    int total = 0;
+    exclusive_scan_int(ctx->nb_g0.p, ctx->nb_start.p, n, st, ctx->count_tmp, &total);
+    ctx->nb_total = total;
+    ctx->nb_idx.resize(std::max(total, 1));
+    ctx->nb_off.resize(3 * (size_t)std::max(total, 1));
+    if (n > 0) {
+        allpairs_scan<true><<<blocks(n, 128), 128, 0, st>>>(n, ctx->pos.p, ctx->cutoffs.p, C, nimg, ctx->nb_start.p,
+                                                            nullptr, ctx->nb_idx.p, ctx->nb_off.p);
+        PG_CHECK_LAUNCH();
+    }
+    PG_CUDA(cudaStreamSynchronize(st));
+    ctx->have_list = true;
+    ctx->short_dirty = true;
+}
+
+void install_neighbor_lists(pg_context* ctx, const int32_t* counts, const int32_t* idx, const int32_t* off) {
+    const int n = ctx->n;
+    std::vector<int> start(n + 1, 0);
+    for (int i = 0; i < n; ++i) {
+        require(counts[i] >= 0, PG_ERR_INVALID, "negative neighbour count");
+        start[i + 1] = start[i] + counts[i];
+    }
+    const int total = start[n];
+    for (int e = 0; e < total; ++e) require(idx[e] >= 0 && idx[e] < n, PG_ERR_INVALID, "neighbour index out of range");
+    ctx->nb_start.upload(start.data(), n + 1, ctx->stream);
+    ctx->nb_idx.resize(std::max(total, 1));
+    ctx->nb_off.resize(3 * (size_t)std::max(total, 1));
+    if (total) {
+        PG_CUDA(cudaMemcpyAsync(ctx->nb_idx.p, idx, sizeof(int) * total, cudaMemcpyHostToDevice, ctx->stream));
+        PG_CUDA(cudaMemcpyAsync(ctx->nb_off.p, off, sizeof(int) * 3 * total, cudaMemcpyHostToDevice, ctx->stream));
+    }
+    PG_CUDA(cudaStreamSynchronize(ctx->stream));
+    ctx->nb_total = total;
+    ctx->have_list = true;
+    ctx->short_dirty = true;
+}
+
+void build_short_list(pg_context* ctx) {
+    const int n = ctx->n;
+    cudaStream_t st = ctx->stream;
+    const double r = ctx->bo_radius + ctx->skin;
+    CellK C = cell_kernel_view(ctx->cell);
+    ctx->sh_count.resize(std::max(n, 1));
+    ctx->sh_start.resize(n + 1);
+    if (n > 0) {
+        short_count<<<blocks(n, 128), 128, 0, st>>>(n, ctx->pos.p, C, ctx->nb_start.p, ctx->nb_idx.p, ctx->nb_off.p,
+                                                   r * r, ctx->sh_count.p);
+        PG_CHECK_LAUNCH();
+    }
+    int total = 0;
+    exclusive_scan_int(ctx->sh_count.p, ctx->sh_start.p, n, st, ctx->count_tmp, &total);
+    ctx->sh_total = total;
+    ctx->sh_idx.resize(std::max(total, 1));
+    ctx->sh_off.resize(3 * (size_t)std::max(total, 1));
+    ctx->sh_rev.resize(std::max(total, 1));
+    if (n > 0) {
+        short_fill<<<blocks(n, 128), 128, 0, st>>>(n, ctx->pos.p, C, ctx->nb_start.p, ctx->nb_idx.p, ctx->nb_off.p,
+                                                  r * r, ctx->sh_start.p, ctx->sh_idx.p, ctx->sh_off.p);
+        PG_CHECK_LAUNCH();
+        short_reverse<<<blocks(n, 128), 128, 0, st>>>(n, ctx->sh_start.p, ctx->sh_idx.p, ctx->sh_off.p, ctx->sh_rev.p,
+                                                     ctx->sh_count.p);
+        PG_CHECK_LAUNCH();
+    }
+    // triplet block bases: exclusive scan of n_i^2
+    ctx->sh_tri.resize(n + 1);
+    DevBuf<long long> tot;
+    tot.resize(1);
+    scan_single_block<int, long long><<<1, 1024, 0, st>>>(ctx->sh_count.p, ctx->sh_tri.p, n, tot.p, 1);
+    PG_CHECK_LAUNCH();
+    long long tri_total = 0;
+    PG_CUDA(cudaMemcpyAsync(&tri_total, tot.p, sizeof(long long), cudaMemcpyDeviceToHost, st));
+    DevBuf<int> mx;
+    mx.resize(2);
+    max_reduce<<<1, 1024, 0, st>>>(n, ctx->sh_count.p, mx.p);
+    PG_CHECK_LAUNCH();
+    // every short entry must have its reverse entry
+    min_reduce<<<1, 1024, 0, st>>>(std::max(total, 1) * (total > 0), ctx->sh_rev.p, mx.p + 1);
+    PG_CHECK_LAUNCH();
+    int h[2] = {0, 0};
+    PG_CUDA(cudaMemcpyAsync(h, mx.p, sizeof(int) * 2, cudaMemcpyDeviceToHost, st));
+    PG_CUDA(cudaStreamSynchronize(st));
+    ctx->sh_tri_total = tri_total;
+    ctx->sh_maxn = h[0];
+    require(total == 0 || h[1] >= 0, PG_ERR_INVALID,
+            "neighbour lists are not symmetric: a bond has no reverse entry (lists must be built both ways)");
+    ctx->short_dirty = false;
+}
+
+}  // namespace pg

@@ -1,0 +1,207 @@
+// pair.cu -- pair potentials, real-space Ewald and single-atom charge terms.
+//
+// Replaces, for non-bond-order terms, the doublet part of
+// core_loop_over_local_interactions (Core.f90:3249-3946 with
+// core_evaluate_local_doublet_energy_B / _forces_B, 4257-4385 and 5371-5606),
+// the inline real-space Ewald sum (Core.f90:3416-3460) and the singlet loop
+// (core_evaluate_local_singlet, 4095-4239).
+//
+// The reference visits each pair once (pick, Geometry.f90:648-676) and
+// scatters the force to both atoms.  Here a group of G lanes owns atom i and
+// walks i's full list, so each pair is evaluated from both ends: atom i takes
+// half the pair energy, its own force and half the pair virial.  Every force
+// and electronegativity is a gather; no atomics, bit-reproducible.
+#include "common.cuh"
+#include "kernels.cuh"
+
+namespace pg {
+
+struct PairArgs {
+    int n, T;
+    const double* pos;
+    const double* charge;
+    const int* type;
+    CellK C;
+    const int* start;
+    const int* idx;
+    const int* off;
+    const PairTerm* terms;
+    const int2* index;
+    const SingleTerm* sterms;
+    const int2* sindex;
+    int ewald;
+    double ew_rc, ew_is2, ew_k, ew_c2, ew_isq2;  // 1/(sqrt2 sigma), 1/(4 pi eps), 2/(sqrt(2 pi) sigma), 1/(2 sigma^2)
+    int flags;
+    int first_f, first_chi;
+    double* out_f;
+    double* out_chi;
+    double* partial;  // per block: energy, virial[6], pad
+};
+
+__device__ __forceinline__ double powi_(double x, int n) {
+    double r = 1.0;
+    for (int k = 0; k < n; ++k) r *= x;
+    return r;
+}
+
+template <typename R, int G>
+__global__ void __launch_bounds__(256) pair_kernel(PairArgs A) {
+    __shared__ double red[256 / G][8];
+    const int lane = threadIdx.x % G;
+    const int slot = threadIdx.x / G;
+    const int i = blockIdx.x * (blockDim.x / G) + slot;
+    const bool act = i < A.n;
+    R fx = 0, fy = 0, fz = 0, en = 0, chi = 0;
+    R w0 = 0, w1 = 0, w2 = 0, w3 = 0, w4 = 0, w5 = 0;
+    const bool wantE = A.flags & PG_WANT_ENERGY, wantF = A.flags & PG_WANT_FORCES, wantC = A.flags & PG_WANT_ENEGS;
+    int ti = 0;
+    double qi = 0;
+    if (act) {
+        ti = A.type[i];
+        qi = A.charge[i];
+        const double xi = A.pos[3 * i], yi = A.pos[3 * i + 1], zi = A.pos[3 * i + 2];
+        const int e1 = A.start[i + 1];
+        for (int e = A.start[i] + lane; e < e1; e += G) {
+            const int j = A.idx[e];
+            const double o0 = A.off[3 * e], o1 = A.off[3 * e + 1], o2 = A.off[3 * e + 2];
+            // separation_vector (Geometry.f90:449-466) in FP64
+            double sx = A.pos[3 * j] - xi, sy = A.pos[3 * j + 1] - yi, sz = A.pos[3 * j + 2] - zi;
+            sx += o0 * A.C.vc[0][0] + o1 * A.C.vc[0][1] + o2 * A.C.vc[0][2];
+            sy += o0 * A.C.vc[1][0] + o1 * A.C.vc[1][1] + o2 * A.C.vc[1][2];
+            sz += o0 * A.C.vc[2][0] + o1 * A.C.vc[2][1] + o2 * A.C.vc[2][2];
+            const R x = (R)sx, y = (R)sy, z = (R)sz;
+            const R r = sqrt_(x * x + y * y + z * z);
+            if (r == R(0)) continue;
+            const R ir = R(1) / r;
+            R U = 0, dU = 0;
+            if (A.ewald && r < (R)A.ew_rc) {
+                const R qq = (R)(qi * A.charge[j]);
+                const R ec = erfc_(r * (R)A.ew_is2);
+                const R k = (R)A.ew_k;
+                U += k * qq * ec * ir;
+                if (wantF) dU -= k * qq * (ec * ir * ir + (R)A.ew_c2 * exp_(-r * r * (R)A.ew_isq2) * ir);
+                if (wantC) chi -= (R)A.charge[j] * k * ec * ir;
+            }
+            const int tj = A.type[j];
+            const int2 ix = A.index[ti * A.T + tj];
+            for (int t = ix.x; t < ix.x + ix.y; ++t) {
+                const PairTerm P = A.terms[t];
+                if (P.in_bond_kernel || !(r < (R)P.rc)) continue;
+                R V, dV;
+                pair_eval<R>(P.kind, (R)P.p[0], (R)P.p[1], (R)P.p[2], r, V, dV);
+                if (P.smooth) {
+                    R f, fp;
+                    smooth<R>(r, (R)P.rc, (R)P.rs, f, fp);
+                    dV = dV * f + V * fp;
+                    V = V * f;
+                }
+                U += V;
+                dU += dV;
+            }
+            en += R(0.5) * U;
+            // force on i: U'(r) r_hat; half of the pair virial sep (x) F_j, F_j = -U' r_hat
+            const R c = dU * ir;
+            fx += c * x;
+            fy += c * y;
+            fz += c * z;
+            const R h = R(-0.5) * c;
+            w0 += h * x * x;
+            w1 += h * y * y;
+            w2 += h * z * z;
+            w3 += h * y * z;
+            w4 += h * x * z;
+            w5 += h * x * y;
+        }
+    }
+    double d[11] = {(double)fx, (double)fy, (double)fz, (double)en, (double)chi, (double)w0, (double)w1,
+                    (double)w2,  (double)w3, (double)w4, (double)w5};
+#pragma unroll
+    for (int q = 0; q < 11; ++q) d[q] = group_sum<G>(d[q]);
+    if (act && lane == 0) {
+        // single-atom terms (charge_self: epsilon q^n, chi = -epsilon n q^(n-1); Potentials.f90:4341-4375)
+        const int2 sx = A.sindex[ti];
+        for (int t = sx.x; t < sx.x + sx.y; ++t) {
+            const SingleTerm S = A.sterms[t];
+            d[3] += S.eps * powi_(qi, S.n);
+            d[4] += -(S.eps * S.n * powi_(qi, S.n - 1));
+        }
+        if (wantF) {
+            if (A.first_f) {
+                A.out_f[3 * i] = d[0];
+                A.out_f[3 * i + 1] = d[1];
+                A.out_f[3 * i + 2] = d[2];
+            } else {
+                A.out_f[3 * i] += d[0];
+                A.out_f[3 * i + 1] += d[1];
+                A.out_f[3 * i + 2] += d[2];
+            }
+        }
+        if (wantC) {
+            if (A.first_chi) A.out_chi[i] = d[4];
+            else A.out_chi[i] += d[4];
+        }
+    }
+    if (lane == 0) {
+        red[slot][0] = act ? d[3] : 0.0;
+        for (int q = 0; q < 6; ++q) red[slot][1 + q] = act ? d[5 + q] : 0.0;
+    }
+    __syncthreads();
+    if (threadIdx.x < 7) {
+        double s = 0;
+        for (int k = 0; k < (int)(blockDim.x / G); ++k) s += red[k][threadIdx.x];
+        A.partial[8 * blockIdx.x + threadIdx.x] = s;
+    }
+    (void)wantE;
+}
+
+int pair_kernel_blocks(int n, int G) { return (n + (256 / G) - 1) / (256 / G); }
+
+void launch_pair_kernel_impl(pg_context* ctx, int precision, int flags, bool first_f, bool first_chi, int G,
+                             double* partial) {
+    PairArgs A{};
+    A.n = ctx->n;
+    A.T = std::max(ctx->n_types, 1);
+    A.pos = ctx->pos.p;
+    A.charge = ctx->charge.p;
+    A.type = ctx->type.p;
+    A.C = cell_kernel_view(ctx->cell);
+    A.start = ctx->nb_start.p;
+    A.idx = ctx->nb_idx.p;
+    A.off = ctx->nb_off.p;
+    A.terms = ctx->d_pair_terms.p;
+    A.index = ctx->d_pair_index.p;
+    A.sterms = ctx->d_single_terms.p;
+    A.sindex = ctx->d_single_index.p;
+    A.ewald = ctx->ewald ? 1 : 0;
+    if (ctx->ewald) {
+        const double pi = 3.14159265358979323846;
+        A.ew_rc = ctx->ew_rc;
+        A.ew_is2 = 1.0 / (std::sqrt(2.0) * ctx->ew_sigma);
+        A.ew_k = 1.0 / (4.0 * pi * ctx->ew_eps);
+        A.ew_c2 = 2.0 / (std::sqrt(2.0 * pi) * ctx->ew_sigma);
+        A.ew_isq2 = A.ew_is2 * A.ew_is2;
+    }
+    A.flags = flags;
+    A.first_f = first_f;
+    A.first_chi = first_chi;
+    A.out_f = ctx->out_f.p;
+    A.out_chi = ctx->out_chi.p;
+    A.partial = partial;
+    const int nbk = pair_kernel_blocks(ctx->n, G);
+    cudaStream_t st = ctx->stream;
+#define PG_PAIR_LAUNCH(R_, G_) pair_kernel<R_, G_><<<nbk, 256, 0, st>>>(A)
+    if (precision == PG_PREC_FP64) {
+        if (G == 8) PG_PAIR_LAUNCH(double, 8);
+        else if (G == 16) PG_PAIR_LAUNCH(double, 16);
+        else PG_PAIR_LAUNCH(double, 32);
+    } else {
+        if (G == 8) PG_PAIR_LAUNCH(float, 8);
+        else if (G == 16) PG_PAIR_LAUNCH(float, 16);
+        else PG_PAIR_LAUNCH(float, 32);
+    }
+#undef PG_PAIR_LAUNCH
+    PG_CHECK_LAUNCH();
+    ctx->launches++;
+}
+
+}  // namespace pg

@@ -1,0 +1,137 @@
+// tables.cu -- fold the interaction records into dense per-type tables.
+//
+// The reference walks, for every pair of atoms, the list of records that
+// target the first atom and tests the second atom's element, tag or index
+// (core_evaluate_local_doublet_*_B, Core.f90:4257-5606 with
+// potential_affects_atom, Potentials.f90:1195-1259).  Here that test is done
+// once per pair of atom types: table[ti][tj] lists the pair terms that apply,
+// trip[ti][tj][tk] the Tersoff parameters of a triplet, post[ti] the
+// B(zeta) parameters of a centre type (core_post_process_pair_bond_order_factor,
+// Core.f90:2763-2807: the first matching factor), maxbr[ti] the largest
+// bond-order cutoff of the type (max_bond_radius, Core.f90:1030-1067).
+#include <algorithm>
+#include <vector>
+
+#include "common.cuh"
+
+namespace pg {
+
+static inline bool has(uint64_t m, int t) { return (m >> t) & 1ull; }
+
+void fold_tables(pg_context* ctx) {
+    const int T = std::max(ctx->n_types, 1);
+    cudaStream_t st = ctx->stream;
+    for (int t : ctx->h_type)
+        require(t < T, PG_ERR_INVALID, "atom type outside the interaction tables (set the potentials after the atoms)");
+    const int nb = (int)ctx->br_cut.size();
+    for (int b = 0; b < nb; ++b)
+        require(ctx->br_group[b] == 0, PG_ERR_UNSUPPORTED,
+                "the GB300 engine evaluates one bond-order group (one Coordinator) per calculator");
+
+    // bond-order tables
+    std::vector<TripletTerm> trip((size_t)T * T * T);
+    for (auto& t : trip) t = TripletTerm{0, 0, 0, 0, 0, 0, 0, 0};
+    std::vector<PostTerm> post(T, PostTerm{0, 0, 0});
+    std::vector<double> maxbr(T, 0.0);
+    double bo_radius = 0.0;
+    for (int b = 0; b < nb; ++b) {
+        const double* p = &ctx->br_params[7 * (size_t)b];
+        bo_radius = std::max(bo_radius, ctx->br_cut[b]);
+        for (int ti = 0; ti < T; ++ti) {
+            if (!has(ctx->br_m1[b], ti)) continue;
+            if (ctx->br_cut[b] > maxbr[ti]) maxbr[ti] = ctx->br_cut[b];
+            if (!post[ti].valid) post[ti] = PostTerm{p[0], p[1], 1};
+            for (int tj = 0; tj < T; ++tj) {
+                if (!has(ctx->br_m2[b], tj)) continue;
+                for (int tk = 0; tk < T; ++tk) {
+                    if (!has(ctx->br_m3[b], tk)) continue;
+                    TripletTerm& tt = trip[((size_t)ti * T + tj) * T + tk];
+                    require(!tt.valid, PG_ERR_UNSUPPORTED,
+                            "two Tersoff factors act on the same (i, j, k) element triple");
+                    tt.a = p[2];
+                    tt.c2 = p[3] * p[3];
+                    tt.d2 = p[4] * p[4];
+                    tt.h = p[5];
+                    tt.mu = p[6];
+                    tt.rc = ctx->br_cut[b];
+                    tt.rs = ctx->br_soft[b];
+                    tt.valid = 1;
+                }
+            }
+        }
+    }
+    // pair terms: bond-order scaled terms define the bond-order kernel's reach
+    const int np = (int)ctx->pr_cut.size();
+    for (int r = 0; r < np; ++r)
+        if (ctx->pr_group[r] >= 0) {
+            require(nb > 0, PG_ERR_INVALID, "a potential has a coordinator without bond-order factors");
+            require(ctx->pr_group[r] == 0, PG_ERR_UNSUPPORTED,
+                    "the GB300 engine evaluates one bond-order group (one Coordinator) per calculator");
+            bo_radius = std::max(bo_radius, ctx->pr_cut[r]);
+        }
+    const bool bond = nb > 0;
+    ctx->have_bond_terms = bond;
+    ctx->bo_radius = bo_radius;
+
+    std::vector<PairTerm> terms;
+    std::vector<int2> index((size_t)T * T, make_int2(0, 0));
+    bool pair_kernel_terms = false;
+    for (int ti = 0; ti < T; ++ti)
+        for (int tj = 0; tj < T; ++tj) {
+            int2& ix = index[(size_t)ti * T + tj];
+            ix.x = (int)terms.size();
+            for (int r = 0; r < np; ++r) {
+                if (!has(ctx->pr_m1[r], ti) || !has(ctx->pr_m2[r], tj)) continue;
+                PairTerm t{};
+                t.kind = ctx->pr_kind[r];
+                t.group = ctx->pr_group[r];
+                for (int q = 0; q < 4; ++q) t.p[q] = ctx->pr_params[4 * (size_t)r + q];
+                t.rc = ctx->pr_cut[r];
+                const double soft = ctx->pr_soft[r];
+                if (soft > 0.0 && soft < t.rc) {
+                    t.smooth = 1;
+                    t.rs = soft;
+                } else {
+                    t.smooth = 0;
+                    t.rs = t.rc;
+                }
+                t.in_bond_kernel = bond && (t.group >= 0 || t.rc <= bo_radius);
+                if (!t.in_bond_kernel) pair_kernel_terms = true;
+                terms.push_back(t);
+            }
+            ix.y = (int)terms.size() - ix.x;
+        }
+    // single-atom terms
+    std::vector<SingleTerm> sterms;
+    std::vector<int2> sindex(T, make_int2(0, 0));
+    const int ns = (int)ctx->sr_kind.size();
+    for (int t = 0; t < T; ++t) {
+        sindex[t].x = (int)sterms.size();
+        for (int r = 0; r < ns; ++r)
+            if (has(ctx->sr_m[r], t)) {
+                SingleTerm s{};
+                s.kind = ctx->sr_kind[r];
+                s.eps = ctx->sr_params[2 * (size_t)r];
+                s.n = (int)ctx->sr_params[2 * (size_t)r + 1];
+                sterms.push_back(s);
+            }
+        sindex[t].y = (int)sterms.size() - sindex[t].x;
+    }
+    ctx->have_singles = !sterms.empty();
+    ctx->have_pair_kernel_terms = pair_kernel_terms;
+
+    if (terms.empty()) terms.push_back(PairTerm{});
+    if (sterms.empty()) sterms.push_back(SingleTerm{});
+    ctx->d_pair_terms.upload(terms.data(), terms.size(), st);
+    ctx->d_pair_index.upload(index.data(), index.size(), st);
+    ctx->d_trip.upload(trip.data(), trip.size(), st);
+    ctx->d_post.upload(post.data(), post.size(), st);
+    ctx->d_maxbr.upload(maxbr.data(), maxbr.size(), st);
+    ctx->d_single_terms.upload(sterms.data(), sterms.size(), st);
+    ctx->d_single_index.upload(sindex.data(), sindex.size(), st);
+    PG_CUDA(cudaStreamSynchronize(st));
+    ctx->tables_dirty = false;
+    ctx->short_dirty = true;
+}
+
+}  // namespace pg

@@ -1,0 +1,377 @@
+// tersoff.cu -- pair-bond-order (Tersoff) energy and forces.
+//
+// Replaces, for bond-order scaled pair potentials, core_evaluate_local_doublet_
+// energy_B / _forces_B (Core.f90:4257-4385, 5371-5606) together with
+// core_calculate_pair_bond_order_factor (2439-2637),
+// core_post_process_pair_bond_order_factor (2763-2807) and
+// core_add_pair_bond_order_forces (4952-5353).
+//
+// Energy of an unordered pair i-j in the reference:
+//     V(r) f(r) (B_ij + B_ji)/2 + (plain pair terms) V f
+// = sum over the two ordered bonds of  1/2 V f B_ij  (+ 1/2 of the plain terms),
+// with B_ij = B(zeta_ij), zeta_ij = sum_k xi_ijk g_ijk over i's neighbours.
+//
+// Two kernels, one group of G lanes per atom, one lane per ordered bond:
+//  bond_pass   per bond i->j: zeta_ij, B, dB/dzeta, the bond energy, the radial
+//              pair force and the three-body gradient of zeta_ij.  The part that
+//              acts on i is summed in registers; the parts that act on j and on
+//              each k are written to per-bond / per-triplet slots (FP32 in the
+//              mixed path) so that no other atom's force is touched.
+//  gather_pass per atom m: own centre part + the j-parts of the bonds i->m
+//              (through the reverse-bond index) + the k-parts of every bond
+//              i->x with k = m.  Summed in FP64.  No atomics: each force is
+//              produced by exactly one lane group, bit-reproducibly.
+// The virial uses the reference's convention sum(r_rel (x) F): pair part
+// r_ij (x) F_j, three-body part r_ij (x) F_j + r_ik (x) F_k (Core.f90:5146-5172).
+#include "common.cuh"
+#include "kernels.cuh"
+
+namespace pg {
+
+template <typename R>
+struct Vec4T;
+template <>
+struct Vec4T<float> {
+    using T = F4;
+};
+template <>
+struct Vec4T<double> {
+    using T = D4;
+};
+
+struct BondArgs {
+    int n, T;
+    const double* pos;
+    const int* type;
+    CellK C;
+    const int* start;
+    const int* idx;
+    const int* off;
+    const int* rev;
+    const long long* tri;
+    const PairTerm* terms;
+    const int2* index;
+    const TripletTerm* trip;
+    const PostTerm* post;
+    const double* maxbr;
+    int flags;
+    int first_f;
+    void* geo;
+    void* fj;
+    void* fk;
+    double* fc;
+    double* out_f;
+    double* partial;
+    double* zeta_out;
+};
+
+template <typename R, int G>
+__global__ void __launch_bounds__(128) bond_pass(BondArgs A) {
+    using V4 = typename Vec4T<R>::T;
+    __shared__ double red[128 / G][8];
+    V4* geo = (V4*)A.geo;
+    V4* fj = (V4*)A.fj;
+    V4* fk = (V4*)A.fk;
+    const int lane = threadIdx.x % G;
+    const int slot = threadIdx.x / G;
+    const int i = blockIdx.x * (blockDim.x / G) + slot;
+    const bool act = i < A.n;
+    const int s = act ? A.start[i] : 0;
+    const int ni = act ? A.start[i + 1] - s : 0;
+    // geometry of i's bonds: FP64 separation, then the working precision
+    if (act) {
+        const double xi = A.pos[3 * i], yi = A.pos[3 * i + 1], zi = A.pos[3 * i + 2];
+        for (int e = lane; e < ni; e += G) {
+            const int j = A.idx[s + e];
+            const double o0 = A.off[3 * (s + e)], o1 = A.off[3 * (s + e) + 1], o2 = A.off[3 * (s + e) + 2];
+            double sx = A.pos[3 * j] - xi, sy = A.pos[3 * j + 1] - yi, sz = A.pos[3 * j + 2] - zi;
+            sx += o0 * A.C.vc[0][0] + o1 * A.C.vc[0][1] + o2 * A.C.vc[0][2];
+            sy += o0 * A.C.vc[1][0] + o1 * A.C.vc[1][1] + o2 * A.C.vc[1][2];
+            sz += o0 * A.C.vc[2][0] + o1 * A.C.vc[2][1] + o2 * A.C.vc[2][2];
+            V4 g;
+            g.x = (R)sx;
+            g.y = (R)sy;
+            g.z = (R)sz;
+            g.w = sqrt_(g.x * g.x + g.y * g.y + g.z * g.z);
+            geo[s + e] = g;
+        }
+    }
+    __syncwarp();
+    R Fx = 0, Fy = 0, Fz = 0, En = 0;
+    R W0 = 0, W1 = 0, W2 = 0, W3 = 0, W4 = 0, W5 = 0;
+    if (act) {
+        const int ti = A.type[i];
+        const R maxbr = (R)A.maxbr[ti];
+        const PostTerm pp = A.post[ti];
+        const long long tri = A.tri[i];
+        for (int e = lane; e < ni; e += G) {
+            const V4 gij = geo[s + e];
+            const V3<R> a{gij.x, gij.y, gij.z};
+            const R r = gij.w;
+            const int tj = A.type[A.idx[s + e]];
+            const int2 ix = A.index[ti * A.T + tj];
+            bool any = false, bo = false;
+            for (int t = ix.x; t < ix.x + ix.y; ++t) {
+                const PairTerm& P = A.terms[t];
+                if (P.in_bond_kernel && r < (R)P.rc) {
+                    any = true;
+                    bo |= P.group >= 0;
+                }
+            }
+            R fjx = 0, fjy = 0, fjz = 0;
+            V4* row = fk + tri + (long long)e * ni;
+            if (!any || r == R(0)) {
+                for (int k = 0; k < ni; ++k)
+                    if (k != e) row[k] = V4{0, 0, 0, 0};
+                fj[s + e] = V4{0, 0, 0, 0};
+                continue;
+            }
+            const TripletTerm* trow = A.trip + ((long long)ti * A.T + tj) * A.T;
+            R zeta = 0, B = 1, dB = 0;
+            if (bo) {
+                for (int k = 0; k < ni; ++k) {
+                    if (k == e) continue;
+                    const V4 gik = geo[s + k];
+                    if (!(gik.w < maxbr)) continue;
+                    const TripletTerm& TT = trow[A.type[A.idx[s + k]]];
+                    if (!TT.valid) continue;
+                    zeta += tersoff_term<R>(load_trip<R>(TT), a, r, V3<R>{gik.x, gik.y, gik.z}, gik.w);
+                }
+                if (pp.valid) post_process<R>((R)pp.beta, (R)pp.eta, zeta, B, dB);
+                else {
+                    B = zeta;
+                    dB = 1;
+                }
+                if (A.zeta_out) A.zeta_out[s + e] = (double)zeta;
+            }
+            R U = 0, dU = 0, P = 0;
+            for (int t = ix.x; t < ix.x + ix.y; ++t) {
+                const PairTerm& PT = A.terms[t];
+                if (!PT.in_bond_kernel || !(r < (R)PT.rc)) continue;
+                R V, dV;
+                pair_eval<R>(PT.kind, (R)PT.p[0], (R)PT.p[1], (R)PT.p[2], r, V, dV);
+                if (PT.smooth) {
+                    R f, fp;
+                    smooth<R>(r, (R)PT.rc, (R)PT.rs, f, fp);
+                    dV = dV * f + V * fp;
+                    V = V * f;
+                }
+                if (PT.group < 0) {
+                    U += V;
+                    dU += dV;
+                } else {
+                    U += V * B;
+                    dU += dV * B;
+                    P += V;
+                }
+            }
+            En += R(0.5) * U;
+            // radial part: force on i = +1/2 U' r_hat, on j the opposite
+            const R c = R(0.5) * dU / r;
+            Fx += c * a.x;
+            Fy += c * a.y;
+            Fz += c * a.z;
+            fjx = -c * a.x;
+            fjy = -c * a.y;
+            fjz = -c * a.z;
+            W0 += a.x * fjx;
+            W1 += a.y * fjy;
+            W2 += a.z * fjz;
+            W3 += a.y * fjz;
+            W4 += a.x * fjz;
+            W5 += a.x * fjy;
+            // three-body part: F = -(1/2 V f dB/dzeta) grad zeta_ij
+            const R pref = R(0.5) * P * dB;
+            for (int k = 0; k < ni; ++k) {
+                if (k == e) continue;
+                V4 out{0, 0, 0, 0};
+                if (bo && pref != R(0)) {
+                    const V4 gik = geo[s + k];
+                    if (gik.w < maxbr) {
+                        const TripletTerm& TT = trow[A.type[A.idx[s + k]]];
+                        if (TT.valid) {
+                            V3<R> gj, gk;
+                            const V3<R> b{gik.x, gik.y, gik.z};
+                            if (tersoff_grad<R>(load_trip<R>(TT), a, r, b, gik.w, gj, gk)) {
+                                const R jx = -pref * gj.x, jy = -pref * gj.y, jz = -pref * gj.z;
+                                const R kx = -pref * gk.x, ky = -pref * gk.y, kz = -pref * gk.z;
+                                fjx += jx;
+                                fjy += jy;
+                                fjz += jz;
+                                Fx -= jx + kx;
+                                Fy -= jy + ky;
+                                Fz -= jz + kz;
+                                W0 += a.x * jx + b.x * kx;
+                                W1 += a.y * jy + b.y * ky;
+                                W2 += a.z * jz + b.z * kz;
+                                W3 += a.y * jz + b.y * kz;
+                                W4 += a.x * jz + b.x * kz;
+                                W5 += a.x * jy + b.x * ky;
+                                out = V4{kx, ky, kz, 0};
+                            }
+                        }
+                    }
+                }
+                row[k] = out;
+            }
+            fj[s + e] = V4{fjx, fjy, fjz, 0};
+        }
+    }
+    double d[10] = {(double)Fx, (double)Fy, (double)Fz, (double)En, (double)W0,
+                    (double)W1, (double)W2, (double)W3, (double)W4, (double)W5};
+#pragma unroll
+    for (int q = 0; q < 10; ++q) d[q] = group_sum<G>(d[q]);
+    if (act && lane == 0) {
+        A.fc[3 * i] = d[0];
+        A.fc[3 * i + 1] = d[1];
+        A.fc[3 * i + 2] = d[2];
+    }
+    if (lane == 0)
+        for (int q = 0; q < 7; ++q) red[slot][q] = act ? d[3 + q] : 0.0;
+    __syncthreads();
+    if (A.partial && threadIdx.x < 7) {
+        double sum = 0;
+        for (int k = 0; k < (int)(blockDim.x / G); ++k) sum += red[k][threadIdx.x];
+        A.partial[8 * blockIdx.x + threadIdx.x] = sum;
+    }
+}
+
+template <typename R, int G>
+__global__ void __launch_bounds__(128) gather_pass(BondArgs A) {
+    using V4 = typename Vec4T<R>::T;
+    const V4* fj = (const V4*)A.fj;
+    const V4* fk = (const V4*)A.fk;
+    const int lane = threadIdx.x % G;
+    const int slot = threadIdx.x / G;
+    const int m = blockIdx.x * (blockDim.x / G) + slot;
+    const bool act = m < A.n;
+    R Fx = 0, Fy = 0, Fz = 0;
+    if (act) {
+        const int s = A.start[m], nm = A.start[m + 1] - s;
+        for (int e = lane; e < nm; e += G) {
+            const int rv = A.rev[s + e];
+            const int i = A.idx[s + e];
+            const int si = A.start[i], ni = A.start[i + 1] - si;
+            const int p = rv - si;
+            const long long tri = A.tri[i];
+            const V4 a = fj[rv];
+            Fx += a.x;
+            Fy += a.y;
+            Fz += a.z;
+            for (int q = 0; q < ni; ++q) {
+                if (q == p) continue;
+                const V4 b = fk[tri + (long long)q * ni + p];
+                Fx += b.x;
+                Fy += b.y;
+                Fz += b.z;
+            }
+        }
+    }
+    double fx = group_sum<G>((double)Fx), fy = group_sum<G>((double)Fy), fz = group_sum<G>((double)Fz);
+    if (act && lane == 0) {
+        fx += A.fc[3 * m];
+        fy += A.fc[3 * m + 1];
+        fz += A.fc[3 * m + 2];
+        if (A.first_f) {
+            A.out_f[3 * m] = fx;
+            A.out_f[3 * m + 1] = fy;
+            A.out_f[3 * m + 2] = fz;
+        } else {
+            A.out_f[3 * m] += fx;
+            A.out_f[3 * m + 1] += fy;
+            A.out_f[3 * m + 2] += fz;
+        }
+    }
+}
+
+int bond_blocks(int n, int G) { return (n + (128 / G) - 1) / (128 / G); }
+
+static void prepare_scratch(pg_context* ctx, int precision) {
+    const size_t ne = (size_t)std::max<long long>(ctx->sh_total, 1);
+    const size_t nt = (size_t)std::max<long long>(ctx->sh_tri_total, 1);
+    if (precision == PG_PREC_FP64) {
+        ctx->bo_fj64.resize(2 * ne);  // first half: bond geometry, second half: j parts
+        ctx->bo_fk64.resize(nt);
+    } else {
+        ctx->bo_fj.resize(2 * ne);
+        ctx->bo_fk.resize(nt);
+    }
+    ctx->bo_fc.resize(3 * (size_t)std::max(ctx->n, 1));
+}
+
+static BondArgs bond_args(pg_context* ctx, int precision, int flags, bool first_f, double* partial) {
+    BondArgs A{};
+    A.n = ctx->n;
+    A.T = std::max(ctx->n_types, 1);
+    A.pos = ctx->pos.p;
+    A.type = ctx->type.p;
+    A.C = cell_kernel_view(ctx->cell);
+    A.start = ctx->sh_start.p;
+    A.idx = ctx->sh_idx.p;
+    A.off = ctx->sh_off.p;
+    A.rev = ctx->sh_rev.p;
+    A.tri = ctx->sh_tri.p;
+    A.terms = ctx->d_pair_terms.p;
+    A.index = ctx->d_pair_index.p;
+    A.trip = ctx->d_trip.p;
+    A.post = ctx->d_post.p;
+    A.maxbr = ctx->d_maxbr.p;
+    A.flags = flags;
+    A.first_f = first_f;
+    const size_t ne = (size_t)std::max<long long>(ctx->sh_total, 1);
+    if (precision == PG_PREC_FP64) {
+        A.geo = ctx->bo_fj64.p;
+        A.fj = ctx->bo_fj64.p + ne;
+        A.fk = ctx->bo_fk64.p;
+    } else {
+        A.geo = ctx->bo_fj.p;
+        A.fj = ctx->bo_fj.p + ne;
+        A.fk = ctx->bo_fk.p;
+    }
+    A.fc = ctx->bo_fc.p;
+    A.out_f = ctx->out_f.p;
+    A.partial = partial;
+    A.zeta_out = nullptr;
+    return A;
+}
+
+template <typename R, int G>
+static void launch_pair(const BondArgs& A, int n, cudaStream_t st, bool forces) {
+    bond_pass<R, G><<<bond_blocks(n, G), 128, 0, st>>>(A);
+    if (forces) gather_pass<R, G><<<bond_blocks(n, G), 128, 0, st>>>(A);
+}
+
+template <typename R>
+static void launch_by_lanes(const BondArgs& A, int n, cudaStream_t st, int G, bool forces) {
+    switch (G) {
+        case 4: launch_pair<R, 4>(A, n, st, forces); break;
+        case 8: launch_pair<R, 8>(A, n, st, forces); break;
+        case 16: launch_pair<R, 16>(A, n, st, forces); break;
+        default: launch_pair<R, 32>(A, n, st, forces); break;
+    }
+}
+
+// returns the number of partial slots written
+int launch_bond_order_impl(pg_context* ctx, int precision, int flags, bool first_f, int G, double* partial) {
+    prepare_scratch(ctx, precision);
+    BondArgs A = bond_args(ctx, precision, flags, first_f, partial);
+    const bool forces = (flags & PG_WANT_FORCES) != 0;
+    if (precision == PG_PREC_FP64) launch_by_lanes<double>(A, ctx->n, ctx->stream, G, forces);
+    else launch_by_lanes<float>(A, ctx->n, ctx->stream, G, forces);
+    PG_CHECK_LAUNCH();
+    ctx->launches += forces ? 2 : 1;
+    return bond_blocks(ctx->n, G);
+}
+
+void bond_zeta_diag(pg_context* ctx) {
+    prepare_scratch(ctx, PG_PREC_FP64);
+    ctx->bo_zeta.resize((size_t)std::max<long long>(ctx->sh_total, 1));
+    ctx->bo_zeta.zero(ctx->stream);
+    BondArgs A = bond_args(ctx, PG_PREC_FP64, PG_WANT_ENERGY, true, nullptr);
+    A.zeta_out = ctx->bo_zeta.p;
+    bond_pass<double, 8><<<bond_blocks(ctx->n, 8), 128, 0, ctx->stream>>>(A);
+    PG_CHECK_LAUNCH();
+    PG_CUDA(cudaStreamSynchronize(ctx->stream));
+}
+
+}  // namespace pg

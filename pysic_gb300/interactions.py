@@ -1,0 +1,500 @@
+"""User-facing interaction objects: Potential, BondOrderParameters, Coordinator,
+CoulombSummation.
+
+These mirror pysic/interactions/local.py:284-776, bondorder.py:7-534 and
+coulomb.py:6-218 of the reference: same constructor arguments, parameter
+orders, target-list format ([[a, b], [c, d]]), cutoff / cutoff-margin
+semantics (soft cutoff = cutoff - margin) and equality rules.  They hold no
+engine state; the calculator compiles them into interaction records when a
+calculation is requested (pysic_gb300/model.py).
+"""
+import copy
+
+from . import core
+from .error import InvalidCoordinatorError, InvalidParametersError, InvalidPotentialError, InvalidSummationError, warn
+
+
+def _accepts_target_list(targets, n_targets):
+    try:
+        for a_set in targets:
+            if not isinstance(a_set, (list, tuple)) or len(a_set) != n_targets:
+                return False
+        return True
+    except TypeError:
+        return False
+
+
+def _normalise_targets(targets, n_targets, err):
+    if targets is None:
+        return None
+    if _accepts_target_list(targets, n_targets):
+        return [list(t) for t in targets]
+    if _accepts_target_list([targets], n_targets):
+        return [list(targets)]
+    raise err("Invalid number of targets.")
+
+
+def _different(lists):
+    out = []
+    for group in lists or []:
+        for x in group:
+            if x not in out:
+                out.append(x)
+    return out
+
+
+class Potential(object):
+    """A local potential acting on 1-4 targets (pysic/interactions/local.py:284-776)."""
+
+    def __init__(self, potential_type, symbols=None, tags=None, indices=None, parameters=None, cutoff=0.0,
+                 cutoff_margin=0.0, coordinator=None):
+        if not core.is_valid_potential(potential_type):
+            raise InvalidPotentialError('There is no potential called "{0}".'.format(potential_type))
+        self.potential_type = potential_type
+        self.symbols = None
+        self.tags = None
+        self.indices = None
+        self.cutoff = cutoff
+        self.cutoff_margin = 0.0
+        self.coordinator = None
+        self.set_cutoff_margin(cutoff_margin)
+        self.n_targets = core.number_of_targets(potential_type)
+        self.names_of_params = core.names_of_parameters(potential_type)
+        self.set_symbols(symbols)
+        self.set_tags(tags)
+        self.set_indices(indices)
+        self.parameters = [0.0] * len(self.names_of_params) if parameters is None else list(parameters)
+        if len(self.parameters) != len(self.names_of_params):
+            raise InvalidPotentialError('The potential "{0}" requires {1} parameters: {2}'.format(
+                potential_type, len(self.names_of_params), self.names_of_params))
+        self.set_coordinator(coordinator)
+
+    def __eq__(self, other):
+        try:
+            return (self.symbols == other.symbols and self.tags == other.tags and self.indices == other.indices
+                    and self.potential_type == other.potential_type and self.parameters == other.parameters
+                    and self.cutoff == other.cutoff and self.coordinator == other.coordinator)
+        except AttributeError:
+            return False
+
+    def __ne__(self, other):
+        return not self.__eq__(other)
+
+    def __repr__(self):
+        return ("Potential('{0}',symbols={1},tags={2},indices={3},parameters={4},cutoff={5},cutoff_margin={6},"
+                "coordinator={7})").format(self.potential_type, self.symbols, self.tags, self.indices,
+                                           self.parameters, self.cutoff, self.cutoff_margin, self.coordinator)
+
+    def get_number_of_parameters(self):
+        return core.number_of_parameters(self.potential_type)
+
+    def get_symbols(self):
+        return self.symbols
+
+    def get_tags(self):
+        return self.tags
+
+    def get_indices(self):
+        return self.indices
+
+    def get_different_symbols(self):
+        return _different(self.symbols)
+
+    def get_different_tags(self):
+        return _different(self.tags)
+
+    def get_different_indices(self):
+        return _different(self.indices)
+
+    def get_parameter_values(self):
+        return self.parameters
+
+    def get_parameter_names(self):
+        return self.names_of_params
+
+    def get_parameter_value(self, param_name):
+        return self.parameters[core.index_of_parameter(self.potential_type, param_name)]
+
+    def get_potential_type(self):
+        return self.potential_type
+
+    def get_cutoff(self):
+        return self.cutoff
+
+    def get_cutoff_margin(self):
+        return self.cutoff_margin
+
+    def get_soft_cutoff(self):
+        return self.cutoff - self.cutoff_margin
+
+    def get_number_of_targets(self):
+        return self.n_targets
+
+    def accepts_target_list(self, targets):
+        return _accepts_target_list(targets, self.n_targets)
+
+    def get_coordinator(self):
+        return self.coordinator
+
+    def set_coordinator(self, coordinator):
+        self.coordinator = coordinator
+
+    def set_symbols(self, symbols):
+        if symbols is None:
+            return
+        self.symbols = _normalise_targets(symbols, self.n_targets, InvalidPotentialError)
+
+    def set_tags(self, tags):
+        if tags is None:
+            return
+        self.tags = _normalise_targets(tags, self.n_targets, InvalidPotentialError)
+
+    def set_indices(self, indices):
+        if indices is None:
+            return
+        self.indices = _normalise_targets(indices, self.n_targets, InvalidPotentialError)
+
+    def _add(self, attr, values):
+        new = _normalise_targets(values, self.n_targets, InvalidPotentialError)
+        cur = getattr(self, attr)
+        setattr(self, attr, (cur or []) + new)
+
+    def add_symbols(self, symbols):
+        self._add("symbols", symbols)
+
+    def add_tags(self, tags):
+        self._add("tags", tags)
+
+    def add_indices(self, indices):
+        self._add("indices", indices)
+
+    def set_parameters(self, values):
+        self.set_parameter_values(values)
+
+    def set_parameter_values(self, values):
+        if len(values) != self.get_number_of_parameters():
+            raise InvalidPotentialError("The potential '{0}' takes {1} parameters, not {2}.".format(
+                self.potential_type, self.get_number_of_parameters(), len(values)))
+        self.parameters = list(values)
+
+    def set_parameter_value(self, parameter_name, value):
+        index = core.index_of_parameter(self.potential_type, parameter_name)
+        if index < 0:
+            raise InvalidPotentialError("The potential '{0}' does not have a parameter '{1}'".format(
+                self.potential_type, parameter_name))
+        self.parameters[index] = value
+
+    def set_cutoff(self, cutoff):
+        self.cutoff = cutoff
+
+    def set_cutoff_margin(self, margin):
+        if margin < 0.0:
+            raise InvalidPotentialError("A negative cutoff margin of {0} was given.".format(margin))
+        if margin > self.cutoff:
+            raise InvalidPotentialError(
+                "A cutoff margin ({0}) longer than the hard cutoff ({1}) was given.".format(margin, self.cutoff))
+        self.cutoff_margin = margin
+
+    def set_soft_cutoff(self, cutoff):
+        self.set_cutoff_margin(self.cutoff - cutoff)
+
+    def get_potentials(self):
+        return [self]
+
+    def is_multiplier(self):
+        return [False]
+
+    def describe(self):
+        core.description_of_potential(self.potential_type, self.parameters, self.cutoff, self.symbols, self.tags,
+                                      self.indices)
+
+
+class BondOrderParameters:
+    """Parameters of one bond-order factor (pysic/interactions/bondorder.py:7-376).
+
+    ``parameters`` is ``[[scaling ...], [local ...]]``; for 'tersoff' that is
+    ``[[beta, eta], [a, c, d, h, mu]]`` (Potentials.f90:5715-5728)."""
+
+    def __init__(self, bond_order_type, cutoff=0.0, cutoff_margin=0.0, parameters=None, symbols=None):
+        if not core.is_valid_bond_order_factor(bond_order_type):
+            raise InvalidParametersError('There is no bond order factor called "{0}"'.format(bond_order_type))
+        self.bond_order_type = bond_order_type
+        self.cutoff = cutoff
+        self.cutoff_margin = 0.0
+        self.set_cutoff_margin(cutoff_margin)
+        self.n_targets = core.number_of_targets(bond_order_type)
+        self.names_of_params = core.names_of_parameters(bond_order_type)
+        self.n_params = core.number_of_parameters(bond_order_type)
+        self.level = core.level_of_factor(bond_order_type)
+        if parameters is None:
+            self.parameters = [[0.0] * self.n_params[0], [0.0] * self.n_params[1]]
+        else:
+            self.set_parameters(parameters)
+        self.symbols = None
+        self.set_symbols(symbols)
+
+    def __repr__(self):
+        return "BondOrderParameters( bond_order_type='{0}',cutoff={1},cutoff_margin={2},parameters={3},symbols={4} )"\
+            .format(self.bond_order_type, self.cutoff, self.cutoff_margin, self.parameters, self.symbols)
+
+    def __eq__(self, other):
+        try:
+            return (self.bond_order_type == other.bond_order_type and self.cutoff == other.cutoff
+                    and self.cutoff_margin == other.cutoff_margin and self.parameters == other.parameters
+                    and self.symbols == other.symbols)
+        except AttributeError:
+            return False
+
+    def __ne__(self, other):
+        return not self.__eq__(other)
+
+    def accepts_parameters(self, params):
+        if len(params) != len(self.n_params):
+            return False
+        return all(len(params[i]) == self.n_params[i] for i in range(len(self.n_params)))
+
+    def get_number_of_parameters(self):
+        return self.n_params
+
+    def includes_scaling(self):
+        return self.n_params[0] > 0
+
+    def get_level(self):
+        return self.level
+
+    def get_number_of_targets(self):
+        return self.n_targets
+
+    def get_parameters_as_list(self):
+        return [p for group in self.parameters for p in group]
+
+    def set_symbols(self, symbols):
+        if symbols is None:
+            return
+        self.symbols = _normalise_targets(symbols, self.n_targets, InvalidParametersError)
+
+    def add_symbols(self, symbols):
+        new = _normalise_targets(symbols, self.n_targets, InvalidParametersError)
+        self.symbols = (self.symbols or []) + new
+
+    def get_symbols(self):
+        return self.symbols
+
+    def get_different_symbols(self):
+        return _different(self.symbols)
+
+    def get_parameter_values(self):
+        return self.parameters
+
+    def get_parameter_names(self):
+        return self.names_of_params
+
+    def get_parameter_value(self, param_name):
+        idx = core.index_of_parameter(self.bond_order_type, param_name)
+        return self.parameters[idx[0]][idx[1]]
+
+    def get_bond_order_type(self):
+        return self.bond_order_type
+
+    def get_cutoff(self):
+        return self.cutoff
+
+    def get_cutoff_margin(self):
+        return self.cutoff_margin
+
+    def get_soft_cutoff(self):
+        return self.cutoff - self.cutoff_margin
+
+    def set_parameter_values(self, values):
+        self.set_parameters(values)
+
+    def set_parameter_value(self, parameter_name, value):
+        idx = core.index_of_parameter(self.bond_order_type, parameter_name)
+        if idx is None:
+            raise InvalidParametersError("The bond order factor '{0}' does not have a parameter '{1}'".format(
+                self.bond_order_type, parameter_name))
+        self.parameters[idx[0]][idx[1]] = value
+
+    def set_cutoff(self, cutoff):
+        self.cutoff = cutoff
+
+    def set_cutoff_margin(self, margin):
+        if margin < 0.0:
+            raise InvalidParametersError("A negative cutoff margin of {0} was given.".format(margin))
+        if margin > self.cutoff:
+            raise InvalidParametersError(
+                "A cutoff margin ({0}) longer than the hard cutoff ({1}) was given.".format(margin, self.cutoff))
+        self.cutoff_margin = margin
+
+    def set_soft_cutoff(self, cutoff):
+        self.set_cutoff_margin(self.cutoff - cutoff)
+
+    def accepts_target_list(self, targets):
+        return _accepts_target_list(targets, self.n_targets)
+
+    def set_parameters(self, params):
+        """Accepts [[scaling], [local]] or a flat list (bondorder.py:351-376)."""
+        params = copy.deepcopy(list(params))
+        if len(params) == len(self.n_params) and all(isinstance(p, (list, tuple)) for p in params):
+            if self.accepts_parameters(params):
+                self.parameters = [list(p) for p in params]
+                return
+        if len(params) == self.n_params[0] + self.n_params[1] and not any(isinstance(p, (list, tuple))
+                                                                          for p in params):
+            new = [params[:self.n_params[0]], params[self.n_params[0]:]]
+            warn("Using parameters \n{0}\ninstead of \n{1}".format(new, params), 3)
+            self.parameters = new
+            return
+        raise InvalidParametersError('The bond order factor "{0}" requires {1} parameters.'.format(
+            self.bond_order_type, self.n_params))
+
+
+class Coordinator:
+    """A group of bond-order factors scaling a potential
+    (pysic/interactions/bondorder.py:379-534).
+
+    In the GB300 engine the per-bond factors live on the device; the
+    Fortran-core queries (bond-order factors and gradients per atom) are
+    served by the calculator the coordinator is used in."""
+
+    def __init__(self, bond_order_parameters=None):
+        self.bond_order_params = []
+        self.bond_order_factors = None
+        if bond_order_parameters is not None:
+            self.set_bond_order_parameters(bond_order_parameters)
+        self.group_index = -1
+        self._calculator = None
+
+    def __eq__(self, other):
+        try:
+            return self.group_index == other.group_index and self.bond_order_params == other.bond_order_params
+        except AttributeError:
+            return False
+
+    def __ne__(self, other):
+        return not self.__eq__(other)
+
+    def __repr__(self):
+        return "Coordinator(bond_order_parameters={0})".format(self.bond_order_params)
+
+    def get_bond_order_parameters(self):
+        return self.bond_order_params
+
+    def set_bond_order_parameters(self, params):
+        self.bond_order_params = list(params) if isinstance(params, list) else [params]
+
+    def add_bond_order_parameters(self, params):
+        if isinstance(params, list):
+            self.bond_order_params.extend(params)
+        else:
+            self.bond_order_params.append(params)
+
+    def set_group_index(self, index):
+        self.group_index = index
+
+    def get_group_index(self):
+        return self.group_index
+
+    def calculate_bond_order_factors(self):
+        """Per-atom (level-1) bond-order factors (Core.f90:2015-2404).  A group made
+        only of pairwise (level-2) factors such as 'tersoff' has none, and the
+        reference returns zeros for it; so does this engine."""
+        if self._calculator is None:
+            raise InvalidCoordinatorError("The coordinator is not attached to a calculator.")
+        n = len(self._calculator.get_atoms())
+        for b in self.bond_order_params:
+            if b.get_level() == 1:
+                raise InvalidCoordinatorError("per-atom bond-order factors are not evaluated by the GB300 engine")
+        import numpy as np
+        self.bond_order_factors = np.zeros(n)
+
+    def get_bond_order_factors(self):
+        return self.bond_order_factors
+
+
+class CoulombSummation:
+    """Ewald summation parameters (pysic/interactions/coulomb.py:6-176):
+    ``[real_cutoff, k_cutoff, sigma, epsilon]`` and optional per-atom charge scalers."""
+
+    summation_modes = ["ewald"]
+    summation_parameters = {"ewald": ["real_cutoff", "k_cutoff", "sigma", "epsilon"]}
+    summation_parameter_descriptions = {"ewald": ["real space cutoff radius", "reciprocal space cutoff radius",
+                                                  "ewald summation split parameter", "vacuum permittivity"]}
+
+    def __init__(self, method="ewald", parameters=None, scaler=None):
+        self.set_summation(method)
+        self.set_parameters(parameters)
+        self.set_scaling_factors(scaler)
+
+    def __eq__(self, other):
+        try:
+            return self.method == other.method and self.parameters == other.parameters and \
+                _same_scaler(self.scaler, other.scaler)
+        except AttributeError:
+            return False
+
+    def __ne__(self, other):
+        return not self == other
+
+    def __repr__(self):
+        return "CoulombSummation(method='{0}',parameters={1},scaler={2})".format(self.method, self.parameters,
+                                                                                  self.scaler)
+
+    def set_summation(self, method):
+        if method not in CoulombSummation.summation_modes:
+            raise InvalidSummationError("no such summation mode " + str(method))
+        self.method = method
+        self.initialize_parameters()
+
+    def initialize_parameters(self):
+        self.parameters = {p: 0.0 for p in CoulombSummation.summation_parameters[self.method]}
+
+    def set_parameters(self, parameters):
+        self.set_parameter_values(parameters)
+
+    def set_parameter_values(self, parameters):
+        if parameters is None:
+            return
+        names = CoulombSummation.summation_parameters[self.method]
+        if len(parameters) != len(names):
+            raise InvalidSummationError("The summation mode {0} requires {1} parameters.".format(
+                self.method, len(names)))
+        for key, value in zip(names, parameters):
+            self.parameters[key] = value
+
+    def set_parameter_value(self, parameter_name, value):
+        self.parameters[parameter_name] = value
+
+    def set_scaling_factors(self, scaler):
+        self.scaler = scaler
+
+    def get_scaling_factors(self):
+        return self.scaler
+
+    def get_summation(self):
+        return self.method
+
+    def get_parameters(self):
+        return self.parameters
+
+    def get_realspace_cutoff(self):
+        if self.method == "ewald":
+            return self.parameters["real_cutoff"]
+        return 0.0
+
+
+def _same_scaler(a, b):
+    if a is None or b is None:
+        return a is None and b is None
+    return list(a) == list(b)
+
+
+def estimate_ewald_parameters(real_cutoff=10.0, accuracy="normal"):
+    """First guess (real_cutoff, k_cutoff, sigma, epsilon) by the scaling rules
+    of pysic/interactions/coulomb.py:179-218; epsilon = 0.00552635 e^2/(eV A)."""
+    epsilon = 0.00552635
+    rules = {"low": (2.0, 2.0), "normal": (3.0, 3.0), "high": (4.0, 4.0), "real": (3.0, 2.0),
+             "reciprocal": (2.0, 3.0)}
+    sdiv, kmul = rules[accuracy]
+    sigma = real_cutoff / sdiv
+    return (real_cutoff, kmul / sigma, sigma, epsilon)

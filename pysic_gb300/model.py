@@ -1,0 +1,246 @@
+"""Compile Pysic interaction objects into the flat interaction records the
+engine consumes.
+
+The reference pushes potentials into its Fortran core one record at a time:
+pysic/calculator.py:1063-1447 permutes every target tuple (an A-B pair
+potential becomes the records A-B and B-A, an A-A potential one record),
+leaves bond-order factor symbols unpermuted (calculator.py:1372, 1410-1416),
+assigns one group index per distinct Coordinator (1217-1233) and calls
+add_potential / add_bond_order_factor (PyInterface.f90:433-526).  The core
+then filters records per atom by element, tag or index
+(potential_affects_atom, Potentials.f90:1195-1259).
+
+Here the same record list is built once, and the per-atom filters are turned
+into *types*: atoms that no filter can tell apart share a type, and every
+record carries one 64-bit type mask per target position.  The records keep
+the reference's order, so the oracle can walk them exactly like the core,
+while the GPU kernels fold them into dense per-type-pair tables.
+"""
+from itertools import permutations
+
+import numpy as np
+
+from . import core
+from .error import InvalidParametersError, InvalidPotentialError
+
+MAX_TYPES = 64
+
+
+def _distinct_permutations(targets):
+    return list(dict.fromkeys(permutations(targets)))
+
+
+class Model:
+    """Interaction records of one calculator for one atomic structure."""
+
+    def __init__(self):
+        self.n_types = 0
+        self.types = np.zeros(0, dtype=np.int32)
+        self.type_signatures = []
+        self.pair_kind = []
+        self.pair_params = []
+        self.pair_cutoff = []
+        self.pair_soft = []
+        self.pair_mask1 = []
+        self.pair_mask2 = []
+        self.pair_group = []
+        self.single_kind = []
+        self.single_params = []
+        self.single_mask = []
+        self.bond_params = []
+        self.bond_cutoff = []
+        self.bond_soft = []
+        self.bond_mask1 = []
+        self.bond_mask2 = []
+        self.bond_mask3 = []
+        self.bond_group = []
+        self.n_groups = 0
+        self.coordinators = []
+        self.ewald = None
+
+    # arrays in the layout of the C ABI
+    def arrays(self):
+        d = {}
+        d["pair_kind"] = np.array(self.pair_kind, dtype=np.int32)
+        d["pair_params"] = np.array(self.pair_params, dtype=np.float64).reshape(-1, 4)
+        d["pair_cutoff"] = np.array(self.pair_cutoff, dtype=np.float64)
+        d["pair_soft"] = np.array(self.pair_soft, dtype=np.float64)
+        d["pair_mask1"] = np.array(self.pair_mask1, dtype=np.uint64)
+        d["pair_mask2"] = np.array(self.pair_mask2, dtype=np.uint64)
+        d["pair_group"] = np.array(self.pair_group, dtype=np.int32)
+        d["single_kind"] = np.array(self.single_kind, dtype=np.int32)
+        d["single_params"] = np.array(self.single_params, dtype=np.float64).reshape(-1, 2)
+        d["single_mask"] = np.array(self.single_mask, dtype=np.uint64)
+        d["bond_params"] = np.array(self.bond_params, dtype=np.float64).reshape(-1, 7)
+        d["bond_cutoff"] = np.array(self.bond_cutoff, dtype=np.float64)
+        d["bond_soft"] = np.array(self.bond_soft, dtype=np.float64)
+        d["bond_mask1"] = np.array(self.bond_mask1, dtype=np.uint64)
+        d["bond_mask2"] = np.array(self.bond_mask2, dtype=np.uint64)
+        d["bond_mask3"] = np.array(self.bond_mask3, dtype=np.uint64)
+        d["bond_group"] = np.array(self.bond_group, dtype=np.int32)
+        return d
+
+
+def assign_types(atoms, potentials):
+    """Group atoms into types: element, plus tag if any potential targets tags,
+    plus index if some potential targets that index."""
+    symbols = list(atoms.get_chemical_symbols())
+    tags = np.asarray(atoms.get_tags())
+    use_tags = any(p.get_tags() for p in potentials)
+    targeted = set()
+    for p in potentials:
+        for t in p.get_indices() or []:
+            targeted.update(int(x) for x in t)
+    sig_of = {}
+    types = np.zeros(len(symbols), dtype=np.int32)
+    for i, s in enumerate(symbols):
+        sig = (s, int(tags[i]) if use_tags else None, i if i in targeted else None)
+        if sig not in sig_of:
+            sig_of[sig] = len(sig_of)
+        types[i] = sig_of[sig]
+    if len(sig_of) > MAX_TYPES:
+        raise InvalidPotentialError("more than {0} distinguishable atom types".format(MAX_TYPES))
+    sigs = [None] * len(sig_of)
+    for s, t in sig_of.items():
+        sigs[t] = s
+    return types, sigs
+
+
+def _mask(sigs, element=None, tag=None, index=None):
+    m = 0
+    for t, (e, g, i) in enumerate(sigs):
+        if (element is not None and e == element) or (tag is not None and g is not None and g == tag) or \
+                (index is not None and i is not None and i == index):
+            m |= 1 << t
+    return m
+
+
+def compile_model(atoms, potentials, coulomb=None):
+    potentials = list(potentials or [])
+    M = Model()
+    M.types, M.type_signatures = assign_types(atoms, potentials)
+    M.n_types = len(M.type_signatures)
+    sigs = M.type_signatures
+
+    # distinct coordinators -> groups (calculator.py:1077-1090, 1217-1233)
+    coords = []
+    for pot in potentials:
+        c = pot.get_coordinator()
+        if c is None:
+            continue
+        if not any(c.get_bond_order_parameters() == k.get_bond_order_parameters() for k in coords):
+            coords.append(c)
+    M.coordinators = coords
+    M.n_groups = len(coords)
+
+    def group_of(pot):
+        c = pot.get_coordinator()
+        if c is None:
+            return -1
+        for g, k in enumerate(coords):
+            if c.get_bond_order_parameters() == k.get_bond_order_parameters():
+                c.set_group_index(g)
+                return g
+        return -1
+
+    for pot in potentials:
+        kind = pot.get_potential_type()
+        core.check_engine_support(kind)
+        nt = pot.get_number_of_targets()
+        params = [float(x) for x in pot.get_parameter_values()]
+        grp = group_of(pot)
+        targets = []  # (position filters) tuples of (element, tag, index) per position
+        for t in pot.get_symbols() or []:
+            for perm in _distinct_permutations(t):
+                targets.append([(e, None, None) for e in perm])
+        for t in pot.get_tags() or []:
+            for perm in _distinct_permutations(t):
+                targets.append([(None, int(g), None) for g in perm])
+        for t in pot.get_indices() or []:
+            for perm in _distinct_permutations(t):
+                targets.append([(None, None, int(i)) for i in perm])
+        if nt == 2:
+            if kind not in core.PAIR_KIND:
+                raise InvalidPotentialError("'{0}' is not a pair potential of the GB300 engine".format(kind))
+            for tg in targets:
+                M.pair_kind.append(core.PAIR_KIND[kind])
+                M.pair_params.append((params + [0.0] * 4)[:4])
+                M.pair_cutoff.append(float(pot.get_cutoff()))
+                M.pair_soft.append(float(pot.get_soft_cutoff()))
+                M.pair_mask1.append(_mask(sigs, *tg[0]))
+                M.pair_mask2.append(_mask(sigs, *tg[1]))
+                M.pair_group.append(grp)
+        elif nt == 1:
+            if kind not in core.SINGLE_KIND:
+                raise InvalidPotentialError("'{0}' is not a single-atom term of the GB300 engine".format(kind))
+            if grp >= 0:
+                raise InvalidPotentialError("bond-order scaling of single-atom terms is not evaluated by the GB300 "
+                                            "engine")
+            for tg in targets:
+                M.single_kind.append(core.SINGLE_KIND[kind])
+                M.single_params.append((params + [0.0] * 2)[:2])
+                M.single_mask.append(_mask(sigs, *tg[0]))
+        else:
+            raise InvalidPotentialError("{0}-body potentials are not evaluated by the GB300 engine".format(nt))
+
+    for g, c in enumerate(coords):
+        for bond in c.get_bond_order_parameters():
+            bkind = bond.get_bond_order_type()
+            core.check_engine_support(bkind)
+            if bond.get_level() != 2:
+                raise InvalidParametersError("per-atom bond-order factors are not evaluated by the GB300 engine")
+            flat = [float(x) for x in bond.get_parameters_as_list()]
+            for tg in bond.get_symbols() or []:
+                M.bond_params.append(flat)
+                M.bond_cutoff.append(float(bond.get_cutoff()))
+                M.bond_soft.append(float(bond.get_soft_cutoff()))
+                M.bond_mask1.append(_mask(sigs, element=tg[0]))
+                M.bond_mask2.append(_mask(sigs, element=tg[1]))
+                M.bond_mask3.append(_mask(sigs, element=tg[2]))
+                M.bond_group.append(g)
+
+    if coulomb is not None:
+        M.ewald = ewald_settings(atoms, coulomb)
+    return M
+
+
+def ewald_settings(atoms, coulomb):
+    """k-space truncation of pysic/calculator.py:1450-1482."""
+    p = coulomb.get_parameters()
+    rcut, kcut, sigma, eps = p["real_cutoff"], p["k_cutoff"], p["sigma"], p["epsilon"]
+    reci = 2.0 * np.pi * np.asarray(atoms.get_reciprocal_cell())
+    volume = np.dot(reci[0], np.cross(reci[1], reci[2]))
+    k1 = int(kcut * np.linalg.norm(np.cross(reci[1], reci[2])) / volume + 0.5)
+    k2 = int(kcut * np.linalg.norm(np.cross(reci[0], reci[2])) / volume + 0.5)
+    k3 = int(kcut * np.linalg.norm(np.cross(reci[0], reci[1])) / volume + 0.5)
+    n = len(atoms)
+    scaler = coulomb.get_scaling_factors()
+    if scaler is None:
+        scaler = np.ones(n)
+    elif len(scaler) != n:
+        raise InvalidParametersError("Length of the scaling factor vector does not match the number of atoms.")
+    return {"rc": float(rcut), "kc": float(kcut), "kmax": np.array([k1, k2, k3], dtype=np.int32),
+            "sigma": float(sigma), "eps": float(eps), "scaler": np.asarray(scaler, dtype=np.float64)}
+
+
+def individual_cutoffs(atoms, potentials, coulomb=None, scaler=1.0):
+    """Per-atom interaction range, pysic/calculator.py:860-915."""
+    potentials = list(potentials or [])
+    symbols = atoms.get_chemical_symbols()
+    tags = atoms.get_tags()
+    base = coulomb.get_realspace_cutoff() if coulomb is not None else 0.0
+    cuts = []
+    for index, (sym, tag) in enumerate(zip(symbols, tags)):
+        mc = base
+        for pot in potentials:
+            active = sym in pot.get_different_symbols() or tag in pot.get_different_tags() or \
+                index in pot.get_different_indices()
+            if active and pot.get_cutoff() > mc:
+                mc = pot.get_cutoff()
+            c = pot.get_coordinator()
+            if c is not None:
+                for bond in c.get_bond_order_parameters():
+                    if sym in bond.get_different_symbols() and bond.get_cutoff() > mc:
+                        mc = bond.get_cutoff()
+        cuts.append(mc * scaler)
+    return cuts

@@ -1,0 +1,228 @@
+"""Charge relaxation (pysic/charges/relaxation.py:11-550).
+
+'dynamic' runs the reference's damped charge dynamics (relaxation.py:417-450)
+entirely on the device through pg_relax_charges: the electronegativity kernels
+and the velocity-Verlet-with-friction update are launched back to back
+without host round trips, and only the convergence statistics come back.
+'potentiostat' (453-481) drives the same GPU electronegativity evaluation
+from the host.  'optimize' (483-488) uses SciPy's SLSQP on the GPU energy and
+gradient when SciPy is available.
+"""
+import numpy as np
+
+from .error import InvalidRelaxationError, warn
+
+
+class ChargeRelaxation:
+    relaxation_modes = ["dynamic", "potentiostat", "optimize"]
+    relaxation_parameters = {
+        "dynamic": ["n_steps", "timestep", "inertia", "friction", "tolerance"],
+        "potentiostat": ["n_steps", "timestep", "inertia", "potential"],
+        "optimize": ["n_steps", "tolerance"],
+    }
+    relaxation_parameter_descriptions = {
+        "dynamic": ["number of time steps of charge dynamics between molecular dynamics",
+                    "time step of charge dynamics", "fictional charge mass",
+                    "friction coefficient for damped charge dynamics", "convergence tolerance"],
+        "potentiostat": ["number of time steps of charge dynamics between molecular dynamics",
+                         "time step of charge dynamics", "fictional charge mass", "external potential"],
+        "optimize": ["maximum number of optimization steps", "convergence tolerance"],
+    }
+
+    def __init__(self, relaxation="dynamic", calculator=None, parameters=None, atoms=None):
+        self.calculator = None
+        self.set_relaxation(relaxation)
+        self.set_calculator(calculator)
+        self.set_parameters(parameters)
+        self.set_atoms(atoms)
+        self.piped_relaxation = None
+        self.charge_rates = None
+        self.observers = []
+        self.last_steps = 0
+        self.last_error = None
+        self.last_max_dq = None
+        self.last_converged = None
+
+    def __eq__(self, other):
+        try:
+            return (self.relaxation == other.relaxation and self.calculator is other.calculator
+                    and self.parameters == other.parameters and self.atoms is other.atoms)
+        except AttributeError:
+            return False
+
+    def __ne__(self, other):
+        return not self == other
+
+    def __repr__(self):
+        return "ChargeRelaxation('{0}',calculator={1},parameters={2},atoms={3})".format(
+            self.relaxation, self.calculator, self.parameters, self.atoms)
+
+    # --- configuration ---------------------------------------------------------
+    def set_relaxation_pipe(self, relaxation, pass_info=True):
+        if relaxation is self:
+            raise InvalidRelaxationError("Trying to create a looped relaxation pipe.")
+        if relaxation is not None:
+            for rel in relaxation.get_relaxation_pipe():
+                if rel is self:
+                    raise InvalidRelaxationError("Trying to create a looped relaxation pipe.")
+        self.piped_relaxation = relaxation
+        if pass_info and relaxation is not None:
+            for rel in self.get_relaxation_pipe():
+                rel.set_calculator(self.calculator)
+                rel.set_atoms(self.atoms)
+
+    def clear_relaxation_pipe(self):
+        self.piped_relaxation = None
+
+    def get_relaxation_pipe(self, recursive=True):
+        if not recursive:
+            return self.piped_relaxation
+        pipe = []
+        nxt = self.piped_relaxation
+        while nxt is not None:
+            pipe.append(nxt)
+            nxt = nxt.piped_relaxation
+        return pipe
+
+    def set_calculator(self, calculator, reciprocal=False):
+        if self.calculator is not None and self.calculator is not calculator:
+            try:
+                self.calculator.set_charge_relaxation(None)
+            except AttributeError:
+                pass
+        self.calculator = calculator
+        if reciprocal and calculator is not None:
+            calculator.set_charge_relaxation(self)
+
+    def get_calculator(self):
+        return self.calculator
+
+    def set_relaxation(self, relaxation):
+        if relaxation not in ChargeRelaxation.relaxation_modes:
+            raise InvalidRelaxationError("no such relaxation mode " + str(relaxation))
+        self.relaxation = relaxation
+        self.initialize_parameters()
+
+    def get_relaxation(self):
+        return self.relaxation
+
+    def initialize_parameters(self):
+        self.parameters = {p: 0.0 for p in ChargeRelaxation.relaxation_parameters[self.relaxation]}
+
+    def set_parameters(self, parameters):
+        self.set_parameter_values(parameters)
+
+    def set_parameter_values(self, parameters):
+        """Values in the order of ``relaxation_parameters[mode]``.  (The
+        reference zips them with a dict's key order, relaxation.py:273, which in
+        Python 2 is not the documented order; here the documented order is used.)"""
+        if parameters is None:
+            return
+        names = ChargeRelaxation.relaxation_parameters[self.relaxation]
+        if len(parameters) != len(names):
+            raise InvalidRelaxationError("The relaxation mode {0} requires {1} parameters.".format(
+                self.relaxation, len(names)))
+        for k, v in zip(names, parameters):
+            self.parameters[k] = v
+
+    def set_parameter_value(self, parameter_name, value):
+        self.parameters[parameter_name] = value
+
+    def get_parameters(self):
+        return self.parameters
+
+    def set_atoms(self, atoms, pass_to_calculator=False):
+        self.atoms = atoms
+        if pass_to_calculator:
+            self.calculator.set_atoms(atoms)
+
+    def get_atoms(self):
+        return self.atoms
+
+    # --- relaxation --------------------------------------------------------------
+    def charge_relaxation(self, precision=None):
+        """Relax the charges of the calculator's structure and return them."""
+        calc = self.calculator
+        atoms = calc.get_atoms()
+        try:
+            charges = np.array(atoms.get_initial_charges(), dtype=np.float64)
+        except AttributeError:
+            charges = np.array(atoms.get_charges(), dtype=np.float64)
+        if self.relaxation == "dynamic":
+            p = self.parameters
+            if self.charge_rates is None:
+                self.charge_rates = np.zeros(len(atoms))
+            calc.set_core()
+            prec = calc._prec() if precision is None else precision
+            r = calc.engine.relax_charges(prec, int(p["n_steps"]), p["timestep"], p["inertia"], p["friction"],
+                                          p["tolerance"], self.charge_rates)
+            charges = r["charges"]
+            self.charge_rates = r["rates"]
+            self.last_steps = r["steps"]
+            self.last_error = r["error"]
+            self.last_max_dq = r["max_dq"]
+            self.last_converged = r["converged"]
+            self._set(atoms, charges)
+            self.call_observers(self.last_steps)
+        elif self.relaxation == "potentiostat":
+            p = self.parameters
+            dt, inv_mq, ext = p["timestep"], 1.0 / p["inertia"], p["potential"]
+            if self.charge_rates is None:
+                self.charge_rates = np.zeros(len(atoms))
+            force = calc.get_electronegativities(atoms) - ext
+            for step in range(int(p["n_steps"])):
+                charges = charges + self.charge_rates * dt + force * inv_mq * dt * dt
+                self.charge_rates = self.charge_rates + force * 0.5 * inv_mq * dt
+                self._set(atoms, charges)
+                force = calc.get_electronegativities(atoms) - ext
+                self.charge_rates = self.charge_rates + force * 0.5 * inv_mq * dt
+                self.call_observers(step + 1)
+        elif self.relaxation == "optimize":
+            try:
+                from scipy.optimize import fmin_slsqp
+            except ImportError:
+                raise InvalidRelaxationError("'optimize' needs SciPy")
+            total = float(np.sum(charges))
+
+            def energy(q, *args):
+                self._set(atoms, q)
+                return calc.get_potential_energy(skip_charge_relaxation=True)
+
+            def grad(q, *args):
+                self._set(atoms, q)
+                return -calc.get_electronegativities()
+
+            charges = fmin_slsqp(energy, charges, fprime=grad, eqcons=[lambda q, *a: np.sum(q) - total],
+                                 acc=self.parameters["tolerance"], iter=int(self.parameters["n_steps"]), disp=0)
+            self._set(atoms, charges)
+        if self.atoms is not None:
+            try:
+                self.atoms.set_initial_charges(charges)
+            except AttributeError:
+                self.atoms.set_charges(charges)
+        if self.piped_relaxation is not None:
+            charges = self.piped_relaxation.charge_relaxation()
+        return charges
+
+    @staticmethod
+    def _set(atoms, q):
+        try:
+            atoms.set_initial_charges(q)
+        except AttributeError:
+            atoms.set_charges(q)
+
+    def add_observer(self, function, interval=1, *args, **kwargs):
+        if not hasattr(function, "__call__"):
+            function = function.write
+        self.observers.append((function, interval, args, kwargs))
+
+    def clear_observers(self):
+        self.observers = []
+
+    def call_observers(self, step):
+        for function, interval, args, kwargs in self.observers:
+            try:
+                if step % interval == 0:
+                    function(*args, **kwargs)
+            except Exception as exc:  # observers must not break a relaxation
+                warn("observer failed: {0}".format(exc), 3)

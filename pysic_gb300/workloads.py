@@ -1,0 +1,178 @@
+"""Seeded synthetic structures and interaction sets of the benchmark workloads.
+
+The reference publishes no benchmark inputs, so every workload is a seeded
+synthetic structure with the shapes and parameters of the five benchmark
+configurations:
+
+1. ``lj_fcc``        Lennard-Jones fcc crystal, 6x6x6 cells, a = 5.26 A (864 atoms)
+2. ``tersoff_si``    diamond silicon, a = 5.431 A, 8^3 (4096) or 16^3 (32768) atoms
+3. ``ewald_nacl``    rock salt 10^3 cells (8000 ions) with Ewald + Buckingham
+4. ``batched_si``    512 periodic Si boxes with log-uniform atom counts
+5. ``sio2_relax``    SiO2-like boxes for charge relaxation
+
+Noise is Gaussian with the stated sigma from ``numpy.random.default_rng(seed)``.
+"""
+import math
+
+import numpy as np
+
+from .atoms import Atoms
+from .interactions import BondOrderParameters, Coordinator, CoulombSummation, Potential
+
+EPS0 = 0.00552635  # e^2/(eV A), pysic/interactions/coulomb.py:201
+
+
+def _lattice(basis, n, a0):
+    g = np.array([[i, j, k] for i in range(n) for j in range(n) for k in range(n)], dtype=np.float64)
+    return ((g[:, None, :] + np.asarray(basis)[None, :, :]).reshape(-1, 3)) * a0
+
+
+def lj_fcc(n=6, a0=5.26, noise=0.05, seed=0, symbol="X"):
+    basis = [[0, 0, 0], [0, 0.5, 0.5], [0.5, 0, 0.5], [0.5, 0.5, 0]]
+    pos = _lattice(basis, n, a0)
+    pos = pos + np.random.default_rng(seed).normal(0.0, noise, pos.shape)
+    return Atoms([symbol] * len(pos), pos, cell=np.eye(3) * a0 * n, pbc=True)
+
+
+def lj_potentials(symbol="X", epsilon=0.0104, sigma=3.40, cutoff=8.5):
+    """pysic LJ is epsilon[(s/r)^12 - (s/r)^6] (no factor 4, Potentials.f90:3003):
+    epsilon is taken literally."""
+    return [Potential("LJ", symbols=[[symbol, symbol]], parameters=[epsilon, sigma], cutoff=cutoff)]
+
+
+def diamond_si(n=8, a0=5.431, noise=0.10, seed=0):
+    basis = [[0, 0, 0], [0, 0.5, 0.5], [0.5, 0, 0.5], [0.5, 0.5, 0], [0.25, 0.25, 0.25], [0.25, 0.75, 0.75],
+             [0.75, 0.25, 0.75], [0.75, 0.75, 0.25]]
+    pos = _lattice(basis, n, a0)
+    if noise > 0:
+        pos = pos + np.random.default_rng(seed).normal(0.0, noise, pos.shape)
+    return Atoms(["Si"] * len(pos), pos, cell=np.eye(3) * a0 * n, pbc=True)
+
+
+TERSOFF_SI = {"A": 1830.8, "B": 471.18, "lambda1": 2.4799, "lambda2": 1.7322, "beta": 1.1e-6, "n": 0.78734,
+              "c": 100390.0, "d": 16.217, "h": -0.59825, "R": 2.7, "D": 0.3}
+
+
+def tersoff_si_potentials(p=TERSOFF_SI):
+    """Tersoff (1988) silicon in pysic terms: repulsive and attractive
+    'exponential' pair potentials, the attractive one scaled by a 'tersoff'
+    bond-order factor; cutoff R + D with margin 2D, so pysic's smooth cutoff
+    1/2(1 + cos) on [R - D, R + D] equals Tersoff's 1/2 - 1/2 sin(pi/2 (r - R)/D)."""
+    rc, margin = p["R"] + p["D"], 2.0 * p["D"]
+    bo = BondOrderParameters("tersoff", cutoff=rc, cutoff_margin=margin, symbols=[["Si", "Si", "Si"]],
+                             parameters=[[p["beta"], p["n"]], [0.0, p["c"], p["d"], p["h"], 3.0]])
+    crd = Coordinator([bo])
+    rep = Potential("exponential", symbols=[["Si", "Si"]], parameters=[p["A"], p["lambda1"]], cutoff=rc,
+                    cutoff_margin=margin)
+    att = Potential("exponential", symbols=[["Si", "Si"]], parameters=[-p["B"], p["lambda2"]], cutoff=rc,
+                    cutoff_margin=margin, coordinator=crd)
+    return [rep, att]
+
+
+def rocksalt_nacl(n=10, a0=5.64, noise=0.05, seed=0):
+    na = [[0, 0, 0], [0, 0.5, 0.5], [0.5, 0, 0.5], [0.5, 0.5, 0]]
+    cl = [[0.5, 0, 0], [0.5, 0.5, 0.5], [0, 0, 0.5], [0, 0.5, 0]]
+    pos = _lattice(na + cl, n, a0)
+    symbols = (["Na"] * 4 + ["Cl"] * 4) * (len(pos) // 8)
+    charges = np.tile(np.array([1.0] * 4 + [-1.0] * 4), len(pos) // 8)
+    pos = pos + np.random.default_rng(seed).normal(0.0, noise, pos.shape)
+    return Atoms(symbols, pos, cell=np.eye(3) * a0 * n, pbc=True, charges=charges)
+
+
+def ewald_kcut(sigma, rel_tail=1e-6):
+    """Reciprocal cutoff where exp(-sigma^2 k^2 / 2) falls to rel_tail."""
+    return math.sqrt(-2.0 * math.log(rel_tail)) / sigma
+
+
+def nacl_potentials(A=1000.0, rho=0.30, C=10.0, cutoff=10.0, sigma=2.5, real_cutoff=10.0, k_cutoff=None):
+    """Buckingham A e^(-r/rho) - C/r^6 on unlike pairs: pysic's Buckingham is
+    A e^(-r/sigma) - C' (sigma/r)^6 (Potentials.f90:3990-3998), so C' = C / rho^6."""
+    buck = Potential("Buckingham", symbols=[["Na", "Cl"]], parameters=[A, C / rho ** 6, rho], cutoff=cutoff)
+    if k_cutoff is None:
+        k_cutoff = ewald_kcut(sigma)
+    coul = CoulombSummation("ewald", [real_cutoff, k_cutoff, sigma, EPS0])
+    return [buck], coul
+
+
+def random_box(symbols, density_per_a3, min_dist, seed, max_tries=200000):
+    """Uniform random positions in a cubic periodic box with rejection below
+    min_dist (minimum image)."""
+    n = len(symbols)
+    L = (n / density_per_a3) ** (1.0 / 3.0)
+    rng = np.random.default_rng(seed)
+    pos = np.zeros((n, 3))
+    placed = 0
+    tries = 0
+    # cell grid for the rejection test
+    nc = max(1, int(L // min_dist))
+    grid = {}
+    cw = L / nc
+    while placed < n:
+        tries += 1
+        if tries > max_tries * max(1, n // 1000):
+            raise RuntimeError("random packing failed")
+        p = rng.uniform(0.0, L, 3)
+        c = tuple((p // cw).astype(int) % nc)
+        ok = True
+        for dx in (-1, 0, 1):
+            for dy in (-1, 0, 1):
+                for dz in (-1, 0, 1):
+                    key = ((c[0] + dx) % nc, (c[1] + dy) % nc, (c[2] + dz) % nc)
+                    for q in grid.get(key, ()):
+                        d = pos[q] - p
+                        d -= L * np.round(d / L)
+                        if d @ d < min_dist * min_dist:
+                            ok = False
+                            break
+                    if not ok:
+                        break
+                if not ok:
+                    break
+            if not ok:
+                break
+        if not ok:
+            continue
+        pos[placed] = p
+        grid.setdefault(c, []).append(placed)
+        placed += 1
+    return Atoms(list(symbols), pos, cell=np.eye(3) * L, pbc=True)
+
+
+SI_DENSITY = 2.33 * 6.02214076e23 / 28.0855 * 1e-24  # atoms per A^3 (0.04996)
+
+
+def batched_si(n_systems=512, lo=64, hi=2048, seed=0):
+    """Atom counts log-uniform in [lo, hi], cubic boxes at 2.33 g/cm^3, uniform
+    random positions with rejection below 2.0 A."""
+    rng = np.random.default_rng(seed)
+    counts = np.floor(np.exp(rng.uniform(math.log(lo), math.log(hi), n_systems))).astype(int)
+    return [random_box(["Si"] * int(c), SI_DENSITY, 2.0, seed * 100003 + k) for k, c in enumerate(counts)]
+
+
+def batched_potentials():
+    return tersoff_si_potentials() + [Potential("LJ", symbols=[["Si", "Si"]], parameters=[0.01, 2.1], cutoff=5.0)]
+
+
+SIO2_DENSITY = 2.2 * 6.02214076e23 / 60.0843 * 3 * 1e-24  # atoms per A^3
+
+
+def sio2_box(n_si=1000, seed=0):
+    symbols = ["Si"] * n_si + ["O"] * (2 * n_si)
+    return random_box(symbols, SIO2_DENSITY, 1.5, seed)
+
+
+SIO2_CHARGE_PARAMS = {"Si": (4.17, 6.97), "O": (8.74, 13.36)}
+
+
+def sio2_potentials(real_cutoff=10.0, sigma=2.5, k_cutoff=None, half_hardness=True):
+    """Charge self energy chi q + (J/2) q^2 per element as two 'charge_self'
+    terms (epsilon q^n, n = 1 and 2).  half_hardness=True uses J/2 for the
+    quadratic term (the usual QEq convention)."""
+    pots = []
+    for el, (chi, J) in SIO2_CHARGE_PARAMS.items():
+        pots.append(Potential("charge_self", symbols=[[el]], parameters=[chi, 1]))
+        pots.append(Potential("charge_self", symbols=[[el]], parameters=[J / 2.0 if half_hardness else J, 2]))
+    if k_cutoff is None:
+        k_cutoff = ewald_kcut(sigma)
+    coul = CoulombSummation("ewald", [real_cutoff, k_cutoff, sigma, EPS0])
+    return pots, coul

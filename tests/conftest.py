@@ -1,0 +1,23 @@
+import os
+import sys
+
+import pytest
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+for p in (ROOT, os.path.join(ROOT, "oracle"), os.path.join(ROOT, "tests")):
+    if p not in sys.path:
+        sys.path.insert(0, p)
+
+
+def pytest_configure(config):
+    config.addinivalue_line("markers", "gpu: needs a CUDA GPU (runs on the GB300 box)")
+
+
+@pytest.fixture(scope="session")
+def engine_lib():
+    """The compiled engine library (built on demand; nvcc cross-compiles without a GPU)."""
+    from pysic_gb300 import _lib, build
+
+    if not os.path.exists(_lib.LIB_PATH):
+        build.build()
+    return _lib.load()

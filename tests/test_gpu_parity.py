@@ -1,0 +1,163 @@
+"""GPU parity: the engine against the FP64 oracle on the same seeded inputs.
+
+Tolerances:
+- neighbour lists: bit-identical (indices, offsets and order);
+- FP64 path: energy within 1e-12 relative, forces within 1e-10 eV/A,
+  virial within 1e-9 relative (summation order differs from the oracle);
+- mixed path: energy within 1e-5 eV/atom, forces within 1e-4 eV/A of the
+  FP64 result (the spec accuracy target).
+"""
+import numpy as np
+import pytest
+
+import pysic_gb300 as pysic
+from helpers import engine_all, oracle_all, oracle_lists
+from pysic_gb300 import workloads as W
+
+pytestmark = pytest.mark.gpu
+
+
+def _lists_equal(atoms, pots, coulomb=None, skin=0.5):
+    calc = pysic.Pysic(atoms, pots, coulomb=coulomb)
+    calc.set_core()
+    c, i, o = calc.engine.neighbor_lists()
+    rc, ri, ro = oracle_lists(atoms, pots, coulomb, skin)
+    assert np.array_equal(c, rc)
+    assert np.array_equal(i, ri)
+    assert np.array_equal(o, ro)
+    return c
+
+
+def _rand_cell(seed, scale=10.0):
+    rng = np.random.default_rng(seed)
+    cell = np.eye(3) * scale + rng.uniform(-0.25, 0.25, (3, 3)) * scale
+    return cell
+
+
+def test_neighbor_lists_bit_exact_lj_fcc():
+    c = _lists_equal(W.lj_fcc(), W.lj_potentials())
+    assert 70 < c.mean() < 90
+
+
+def test_neighbor_lists_bit_exact_silicon():
+    _lists_equal(W.diamond_si(8, seed=1), W.tersoff_si_potentials())
+
+
+@pytest.mark.parametrize("seed", [0, 1, 2, 3])
+def test_neighbor_lists_bit_exact_triclinic(seed):
+    rng = np.random.default_rng(100 + seed)
+    cell = _rand_cell(seed, 12.0)
+    n = 150
+    frac = rng.uniform(-0.3, 1.3, (n, 3))  # also atoms outside the cell
+    atoms = pysic.Atoms(["Ar"] * n, frac @ cell, cell=cell, pbc=[True, seed % 2 == 0, True])
+    pots = [pysic.Potential("LJ", symbols=[["Ar", "Ar"]], parameters=[0.01, 3.0], cutoff=2.5 + 0.5 * seed)]
+    _lists_equal(atoms, pots)
+
+
+def test_neighbor_lists_bit_exact_small_cells():
+    # one and two subcells per axis: periodic images of the same atom appear
+    rng = np.random.default_rng(5)
+    for L, rc in ((4.5, 2.5), (7.5, 3.0), (9.0, 3.9), (12.0, 3.2)):
+        n = 40
+        atoms = pysic.Atoms(["Ar"] * n, rng.uniform(0, L, (n, 3)), cell=np.eye(3) * L, pbc=True)
+        pots = [pysic.Potential("LJ", symbols=[["Ar", "Ar"]], parameters=[0.01, 2.0], cutoff=rc)]
+        _lists_equal(atoms, pots)
+
+
+def test_neighbor_lists_lattice_sites_on_boundaries():
+    # perfect lattice in a sheared cell: wrapped fractional coordinates land on 0
+    cell = np.array([[5.0, 0, 0], [2.5, 4.33, 0], [0, 0, 5.0]])
+    g = np.array([[i, j, k] for i in range(3) for j in range(3) for k in range(3)], dtype=float) / 3.0
+    big = cell * 3
+    atoms = pysic.Atoms(["Ar"] * len(g), g @ big, cell=big, pbc=True)
+    pots = [pysic.Potential("LJ", symbols=[["Ar", "Ar"]], parameters=[0.01, 2.0], cutoff=4.0)]
+    _lists_equal(atoms, pots)
+
+
+def test_neighbor_lists_nonperiodic():
+    rng = np.random.default_rng(8)
+    atoms = pysic.Atoms(["Ar"] * 200, rng.uniform(-2, 22, (200, 3)), cell=np.eye(3) * 20.0, pbc=False)
+    pots = [pysic.Potential("LJ", symbols=[["Ar", "Ar"]], parameters=[0.01, 2.0], cutoff=4.0)]
+    _lists_equal(atoms, pots)
+
+
+def test_golden_vectors_on_gpu():
+    atoms = pysic.Atoms("He2", [[0.0, 0.0, 0.0], [0.0, 0.0, 3.0]])
+    pot = pysic.Potential("LJ", symbols=[["He", "He"]], parameters=[0.1, 2.5], cutoff=10.0)
+    calc = pysic.Pysic(atoms, [pot])
+    assert calc.get_potential_energy() == pytest.approx(-0.022274132189576905, rel=1e-14)
+    np.testing.assert_allclose(calc.get_forces(), [[0, 0, 0.02211693], [0, 0, -0.02211693]], atol=5e-9)
+    atoms = pysic.Atoms("COH", [[0.0, 0.0, 0.0], [2.0, 0.0, 0.0], [2.0, 2.0, 2.0]])
+    p1 = pysic.Potential("LJ", symbols=["C", "O"], parameters=[1, 1], cutoff=10.0)
+    p2 = pysic.Potential("LJ", symbols=["O", "H"], parameters=[1, 1], cutoff=10.0)
+    calc = pysic.Pysic(atoms, [p1, p2])
+    assert calc.get_potential_energy() == pytest.approx(-0.0173301696777, abs=5e-14)
+    np.testing.assert_allclose(calc.get_forces(), [[0.04541016, 0, 0], [-0.04541016, 0.00291824, 0.00291824],
+                                                   [0, -0.00291824, -0.00291824]], atol=5e-9)
+
+
+def _check_fp64(atoms, pots, coulomb=None, lanes=0):
+    ref = oracle_all(atoms, pots, coulomb)
+    got = engine_all(atoms, pots, coulomb, "fp64", lanes)
+    assert got["energy"] == pytest.approx(ref["energy"], rel=1e-12, abs=1e-11)
+    assert np.abs(got["forces"] - ref["forces"]).max() < 1e-10 * max(1.0, np.abs(ref["forces"]).max())
+    np.testing.assert_allclose(got["stress"], ref["stress"], rtol=1e-9, atol=1e-9 * np.abs(ref["stress"]).max())
+    return ref, got
+
+
+def test_lj_fcc_fp64_parity():
+    _check_fp64(W.lj_fcc(), W.lj_potentials())
+
+
+@pytest.mark.parametrize("lanes", [4, 8, 16, 32])
+def test_tersoff_fp64_parity(lanes):
+    _check_fp64(W.diamond_si(3, seed=11), W.tersoff_si_potentials(), lanes=lanes)
+
+
+def test_tersoff_mixed_accuracy_4096():
+    atoms = W.diamond_si(8, seed=12)
+    pots = W.tersoff_si_potentials()
+    ref, got64 = _check_fp64(atoms, pots)
+    mixed = engine_all(atoms, pots, precision="mixed")
+    n = len(atoms)
+    assert abs(mixed["energy"] - got64["energy"]) / n < 1e-5
+    assert np.abs(mixed["forces"] - got64["forces"]).max() < 1e-4
+
+
+def test_tersoff_zeta_matches_oracle():
+    import oracle
+
+    atoms = W.diamond_si(2, seed=13)
+    pots = W.tersoff_si_potentials()
+    calc = pysic.Pysic(atoms, pots)
+    z = calc.get_bond_zeta()
+    ref = oracle_all(atoms, pots)
+    c, i, o = ref["lists"]
+    zr = oracle.bond_zeta(atoms.get_positions(), atoms.get_cell(), atoms.get_pbc(), ref["model"], c, i, o)
+    np.testing.assert_allclose(z, zr, rtol=1e-12, atol=1e-9)
+
+
+def test_results_are_bit_reproducible():
+    atoms = W.diamond_si(4, seed=14)
+    pots = W.tersoff_si_potentials()
+    calc = pysic.Pysic(atoms, pots, precision="mixed")
+    calc.set_core()
+    a = calc.engine.calculate(calc._prec())
+    b = calc.engine.calculate(calc._prec())
+    assert a["energy"] == b["energy"]
+    assert np.array_equal(a["forces"], b["forces"])
+
+
+def test_md_style_position_update():
+    """positions move less than skin/2: the list is reused, offsets stay valid"""
+    atoms = W.diamond_si(3, seed=15)
+    pots = W.tersoff_si_potentials()
+    calc = pysic.Pysic(atoms, pots)
+    calc.get_forces()
+    nl = calc.get_neighbor_lists()
+    moved = atoms.copy()
+    moved.set_positions(atoms.get_positions() + np.random.default_rng(1).normal(0, 0.05, (len(atoms), 3)))
+    f = calc.get_forces(moved)
+    assert calc.get_neighbor_lists().nupdates == nl.nupdates
+    ref = oracle_all(moved, pots, lists=oracle_lists(atoms, pots))
+    assert np.abs(f - ref["forces"]).max() < 1e-10

@@ -1,0 +1,191 @@
+"""CPU tests of the oracle: the pins that make it trustworthy.
+
+- known-answer values from the reference's documentation
+  (doc/run examples.rst:106-145, doc/pysic class.rst:88-157),
+- the published Tersoff (1988) silicon cohesive energy, -4.63 eV/atom at a = 5.432 A,
+- finite-difference forces and electronegativities, the reference's own
+  self-check (pysic/calculator.py:1639-1832),
+- Newton's third law and translation invariance,
+- neighbour-list invariants of the restated FastNeighborList.
+"""
+import numpy as np
+import pytest
+
+import oracle
+import pysic_gb300 as pysic
+from helpers import oracle_all, oracle_lists
+from pysic_gb300 import workloads as W
+from pysic_gb300.model import compile_model, individual_cutoffs
+
+
+def _allpairs(atoms, cuts):
+    n = len(atoms)
+    pos = atoms.get_positions()
+    c, i, o = [], [], []
+    for a in range(n):
+        k = 0
+        for b in range(n):
+            if a != b and np.linalg.norm(pos[b] - pos[a]) < cuts[a] + cuts[b]:
+                i.append(b)
+                o.append([0, 0, 0])
+                k += 1
+        c.append(k)
+    return np.array(c), np.array(i), np.array(o).reshape(-1, 3)
+
+
+def _nonperiodic(atoms, pots):
+    cuts = np.array(individual_cutoffs(atoms, pots)) + 0.5
+    return oracle_all(atoms, pots, lists=_allpairs(atoms, cuts))
+
+
+def test_he2_golden():
+    """doc/run examples.rst:106-145"""
+    atoms = pysic.Atoms("He2", [[0.0, 0.0, 0.0], [0.0, 0.0, 3.0]])
+    pot = pysic.Potential("LJ", cutoff=10.0)
+    pot.set_symbols(["He", "He"])
+    pot.set_parameter_value("epsilon", 0.1)
+    pot.set_parameter_value("sigma", 2.5)
+    r = _nonperiodic(atoms, [pot])
+    assert r["energy"] == -0.022274132189576905
+    np.testing.assert_allclose(r["forces"], [[0, 0, 0.02211693], [0, 0, -0.02211693]], atol=5e-9)
+
+
+def test_coh_golden():
+    """doc/pysic class.rst:88-157"""
+    atoms = pysic.Atoms("COH", [[0.0, 0.0, 0.0], [2.0, 0.0, 0.0], [2.0, 2.0, 2.0]])
+    p1 = pysic.Potential("LJ", symbols=["C", "O"], parameters=[1, 1], cutoff=10.0)
+    p2 = pysic.Potential("LJ", symbols=["O", "H"], parameters=[1, 1], cutoff=10.0)
+    assert _nonperiodic(atoms, [p1])["energy"] == pytest.approx(-0.015380859375, abs=1e-15)
+    assert _nonperiodic(atoms, [p2])["energy"] == pytest.approx(-0.00194931030273, abs=5e-15)
+    r = _nonperiodic(atoms, [p1, p2])
+    assert r["energy"] == pytest.approx(-0.0173301696777, abs=5e-14)
+    np.testing.assert_allclose(r["forces"], [[0.04541016, 0, 0], [-0.04541016, 0.00291824, 0.00291824],
+                                             [0, -0.00291824, -0.00291824]], atol=5e-9)
+
+
+def test_tersoff_silicon_known_answer():
+    """Tersoff, Phys. Rev. B 38, 9902 (1988): E_coh = -4.63 eV/atom at a = 5.432 A."""
+    atoms = W.diamond_si(2, a0=5.432, noise=0.0)
+    r = oracle_all(atoms, W.tersoff_si_potentials())
+    assert r["energy"] / len(atoms) == pytest.approx(-4.63, abs=5e-3)
+    assert np.abs(r["forces"]).max() < 1e-10
+
+
+def _fd_forces(atoms, pots, idx, h=1e-4, coulomb=None):
+    lists = oracle_lists(atoms, pots, coulomb, skin=1.0)
+    model = compile_model(atoms, pots, coulomb)
+    out = []
+    for c in range(3):
+        e = []
+        for s in (+h, -h):
+            pos = atoms.get_positions()
+            pos[idx, c] += s
+            e.append(oracle.evaluate(pos, atoms.get_initial_charges(), atoms.get_cell(), atoms.get_pbc(), model,
+                                     *lists, what="energy"))
+        out.append(-(e[0] - e[1]) / (2 * h))
+    f, _ = oracle.evaluate(atoms.get_positions(), atoms.get_initial_charges(), atoms.get_cell(), atoms.get_pbc(),
+                           model, *lists, what="forces")
+    return np.array(out), f[idx]
+
+
+@pytest.mark.parametrize("idx", [0, 5, 11])
+def test_tersoff_forces_match_finite_differences(idx):
+    atoms = W.diamond_si(2, noise=0.12, seed=3)
+    fd, f = _fd_forces(atoms, W.tersoff_si_potentials(), idx)
+    np.testing.assert_allclose(f, fd, atol=2e-6, rtol=1e-6)
+
+
+def test_tersoff_stress_matches_strain_derivative():
+    """virial W = -dE/d(strain) for a homogeneous deformation."""
+    atoms = W.diamond_si(2, noise=0.08, seed=4)
+    pots = W.tersoff_si_potentials()
+    r = oracle_all(atoms, pots)
+    model = compile_model(atoms, pots)
+    h = 1e-6
+    e = []
+    for s in (+h, -h):
+        eps = np.eye(3)
+        eps[0, 0] += s
+        a2 = atoms.copy()
+        a2.set_cell(atoms.get_cell() @ eps, scale_atoms=True)
+        lists = oracle_lists(a2, pots)
+        e.append(oracle.evaluate(a2.get_positions(), a2.get_initial_charges(), a2.get_cell(), a2.get_pbc(), model,
+                                 *lists, what="energy"))
+    dE = (e[0] - e[1]) / (2 * h)
+    assert r["stress"][0] == pytest.approx(-dE, rel=1e-6, abs=1e-6)
+
+
+def test_lj_newton_and_translation():
+    atoms = W.lj_fcc(3, noise=0.1, seed=1)
+    pots = W.lj_potentials(cutoff=6.0)
+    r = oracle_all(atoms, pots)
+    assert np.abs(r["forces"].sum(axis=0)).max() < 1e-12
+    a2 = atoms.copy()
+    a2.set_positions(atoms.get_positions() + np.array([0.3, -1.1, 2.7]))
+    r2 = oracle_all(a2, pots)
+    assert r2["energy"] == pytest.approx(r["energy"], rel=1e-12)
+
+
+def test_neighbor_list_symmetry_and_cutoff():
+    atoms = W.diamond_si(3, noise=0.1, seed=2)
+    pots = W.tersoff_si_potentials()
+    c, idx, off = oracle_lists(atoms, pots)
+    start = np.concatenate([[0], np.cumsum(c)])
+    pos, cell = atoms.get_positions(), atoms.get_cell()
+    entries = set()
+    for a in range(len(atoms)):
+        for e in range(start[a], start[a + 1]):
+            d = np.linalg.norm(pos[idx[e]] + off[e] @ cell - pos[a])
+            assert d < 3.5
+            entries.add((a, idx[e], tuple(off[e])))
+    for (a, b, o) in entries:
+        assert (b, a, tuple(-np.array(o))) in entries
+    # completeness against brute force over images
+    for a in range(0, len(atoms), 17):
+        want = set()
+        for b in range(len(atoms)):
+            for n1 in (-1, 0, 1):
+                for n2 in (-1, 0, 1):
+                    for n3 in (-1, 0, 1):
+                        if a == b and n1 == n2 == n3 == 0:
+                            continue
+                        d = np.linalg.norm(pos[b] + np.array([n1, n2, n3]) @ cell - pos[a])
+                        if d < 3.5:
+                            want.add(b)
+        got = set(idx[start[a]:start[a + 1]].tolist())
+        assert got == want
+
+
+def test_electronegativity_matches_charge_derivative():
+    atoms = W.sio2_box(40, seed=5)
+    pots, coul = W.sio2_potentials(real_cutoff=5.0, sigma=1.6)
+    q = np.random.default_rng(0).normal(0, 0.3, len(atoms))
+    q -= q.mean()
+    atoms.set_initial_charges(q)
+    model = compile_model(atoms, pots, coul)
+    lists = oracle_lists(atoms, pots, coul)
+    chi = oracle.evaluate(atoms.get_positions(), q, atoms.get_cell(), atoms.get_pbc(), model, *lists, what="enegs")
+    for i in (0, 7, 50):
+        e = []
+        for s in (1e-4, -1e-4):
+            qq = q.copy()
+            qq[i] += s
+            e.append(oracle.evaluate(atoms.get_positions(), qq, atoms.get_cell(), atoms.get_pbc(), model, *lists,
+                                     what="energy"))
+        assert chi[i] == pytest.approx(-(e[0] - e[1]) / 2e-4, rel=1e-6, abs=1e-7)
+
+
+def test_ewald_forces_match_finite_differences():
+    atoms = W.rocksalt_nacl(2, noise=0.1, seed=6)
+    pots, coul = W.nacl_potentials(sigma=1.4, real_cutoff=5.0, cutoff=5.0)
+    fd, f = _fd_forces(atoms, pots, 3, h=1e-5, coulomb=coul)
+    np.testing.assert_allclose(f, fd, atol=1e-5, rtol=1e-5)
+
+
+def test_threaded_oracle_matches_serial():
+    atoms = W.diamond_si(3, noise=0.1, seed=9)
+    pots = W.tersoff_si_potentials()
+    a = oracle_all(atoms, pots, threads=1)
+    b = oracle_all(atoms, pots, threads=4)
+    assert b["energy"] == pytest.approx(a["energy"], rel=1e-13)
+    np.testing.assert_allclose(b["forces"], a["forces"], atol=1e-11)
