@@ -1,0 +1,442 @@
+#!/usr/bin/env python
+"""Benchmark of the GB300 engine: Tersoff-silicon atom-steps/s, mixed precision
+against the plain FP64 kernels, on the 16x16x16 diamond cell (32768 atoms).
+
+One step = one energy + forces + virial evaluation of the whole structure
+(neighbour list built once; positions fixed, as in the benchmark definition:
+repeated evaluations at fixed positions).  The L2 cache (126 MB) is flushed
+between timed steps by writing a 256 MB buffer; steps are timed with CUDA
+events on the engine's stream.
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+                  [--workload NAME]
+
+--impl reference times the CPU restatement of the reference's Fortran core
+(the Fortran itself cannot be compiled on these machines: no Fortran
+compiler) on all host cores, on the same workload.  With torchrun (N > 1) each
+rank runs an independent replica on its own GPU (the workload does not shard:
+replicas only).
+"""
+import argparse
+import json
+import math
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "Tersoff-Si atom-steps/s mixed vs FP64 on GPU @1e-5 eV/atom; charge-relax gain"
+
+# algorithmic cost per atom of one Tersoff energy + force evaluation: positions
+# (16 B), neighbour entries (4 x 8 B), forces (24 B) = 72 B/atom; ~2.0 kFLOP/atom
+TERSOFF_BYTES_PER_ATOM = 72.0
+TERSOFF_FLOP_PER_ATOM = 2.0e3
+FP32_NOMINAL_TFLOPS = 152 * 128 * 2 * 2.07e9 / 1e12  # 152 SMs x 128 FP32 lanes x FMA x max clock
+
+
+def workload(name):
+    from pysic_gb300 import workloads as W
+
+    if name == "tersoff_si_32768":
+        return W.diamond_si(16, seed=0), W.tersoff_si_potentials(), None, "diamond Si 16x16x16 cells, a=5.431, noise 0.10"
+    if name == "tersoff_si_4096":
+        return W.diamond_si(8, seed=0), W.tersoff_si_potentials(), None, "diamond Si 8x8x8 cells, a=5.431, noise 0.10"
+    if name == "lj_fcc_864":
+        return W.lj_fcc(), W.lj_potentials(), None, "LJ fcc 6x6x6 cells, a=5.26, noise 0.05, cutoff 8.5"
+    if name == "ewald_nacl_8000":
+        pots, coul = W.nacl_potentials()
+        return W.rocksalt_nacl(), pots, coul, "rock salt 10x10x10 cells, Buckingham + Ewald (rc 10, sigma 2.5)"
+    raise SystemExit("unknown workload " + name)
+
+
+def peaks():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            d = json.load(f)
+        return float(d["hbm_gbs"]), "measured"
+    except (OSError, KeyError, ValueError):
+        return 6800.0, "fallback"
+
+
+def profile_traffic(kernel, workload_name):
+    """dram bytes per launch from the committed ncu summary, if there is one."""
+    path = os.path.join(ROOT, "profiles", "{0}_{1}.md".format(kernel, workload_name))
+    try:
+        for line in open(path):
+            if line.lower().startswith("traffic_bytes_per_launch:"):
+                return float(line.split(":", 1)[1].split()[0])
+    except OSError:
+        pass
+    return None
+
+
+class ClockSampler:
+    """nvidia-smi clock / throttle sampling during the timed region."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index):
+        self.gpu = gpu_index
+        self.proc = None
+        self.lines = []
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.gpu), "--query-gpu=" + self.FIELDS,
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.thread = threading.Thread(target=self._read, daemon=True)
+            self.thread.start()
+        except OSError:
+            self.proc = None
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def stop(self):
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"], "samples": 0}
+        time.sleep(0.25)
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        sm, mx, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            parts = [p.strip() for p in ln.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                sm.append(float(parts[1]))
+                mx.append(float(parts[2]))
+            except ValueError:
+                continue
+            for nm, v in zip(names, parts[5:9]):
+                if v.lower() == "active":
+                    reasons.add(nm)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def setup(name, precision, device):
+    import pysic_gb300 as pysic
+    from pysic_gb300.engine import Engine
+
+    atoms, pots, coul, desc = workload(name)
+    calc = pysic.Pysic(atoms, pots, coulomb=coul, precision=precision)
+    calc._engine = Engine(device=device)
+    calc.set_core()
+    return atoms, calc, desc
+
+
+def device_time(torch, engine, prec, flags, steps, warmup, flush):
+    """Per-step CUDA-event times (ms) on the engine's stream, L2 flushed before each step."""
+    stream = torch.cuda.ExternalStream(engine.stream_handle())
+    for _ in range(warmup):
+        with torch.cuda.stream(stream):
+            flush.fill_(1.0)
+        engine.device_evaluate(prec, flags)
+    engine.device_synchronize()
+    ev0 = [torch.cuda.Event(enable_timing=True) for _ in range(steps)]
+    ev1 = [torch.cuda.Event(enable_timing=True) for _ in range(steps)]
+    launches = 0
+    for k in range(steps):
+        with torch.cuda.stream(stream):
+            flush.fill_(float(k))
+            ev0[k].record(stream)
+        engine.device_evaluate(prec, flags)
+        launches += engine.launch_count()
+        with torch.cuda.stream(stream):
+            ev1[k].record(stream)
+    stream.synchronize()
+    return [a.elapsed_time(b) for a, b in zip(ev0, ev1)], launches
+
+
+def kernel_time(torch, engine, prec, flags, steps, flush):
+    """Average duration of each kernel group, from events recorded by the engine
+    around its own launches (same stream)."""
+    engine.set_kernel_timing(True)
+    stream = torch.cuda.ExternalStream(engine.stream_handle())
+    acc = {}
+    for k in range(steps + 2):
+        with torch.cuda.stream(stream):
+            flush.fill_(float(k))
+        engine.device_evaluate(prec, flags)
+        t = engine.kernel_times()
+        if k >= 2:
+            for key, v in t.items():
+                acc.setdefault(key, []).append(v)
+    engine.set_kernel_timing(False)
+    return {k: statistics.mean(v) for k, v in acc.items()}
+
+
+def e2e_time(torch, engine, atoms, prec, flags, steps, warmup):
+    """The C-ABI call a user makes, with host buffers: every step copies the
+    positions in from pinned host memory and the energy, forces and virial out."""
+    from pysic_gb300 import _lib as L
+
+    n = len(atoms)
+    pos = torch.empty((n, 3), dtype=torch.float64, pin_memory=True).numpy()
+    pos[:] = atoms.get_positions()
+    e = torch.empty(1, dtype=torch.float64, pin_memory=True).numpy()
+    f = torch.empty((n, 3), dtype=torch.float64, pin_memory=True).numpy()
+    s = torch.empty(6, dtype=torch.float64, pin_memory=True).numpy()
+    c = torch.empty(n, dtype=torch.float64, pin_memory=True).numpy()
+    for _ in range(warmup):
+        engine.update_positions(pos)
+        engine.calculate_into(prec, flags, e, f, s, c)
+    t0 = time.perf_counter()
+    for _ in range(steps):
+        engine.update_positions(pos)
+        engine.calculate_into(prec, flags, e, f, s, c)
+    dt = time.perf_counter() - t0
+    h2d = pos.nbytes
+    d2h = e.nbytes + f.nbytes + s.nbytes
+    del L
+    return dt, h2d, d2h
+
+
+def cpu_baseline(name, seconds, threads):
+    """The oracle (FP64 CPU restatement of the reference loops) on a bounded
+    sample: whole energy + force evaluations of the same structure."""
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import oracle
+    from pysic_gb300.model import compile_model, individual_cutoffs
+
+    atoms, pots, coul, _ = workload(name)
+    model = compile_model(atoms, pots, coul)
+    cuts = np.array(individual_cutoffs(atoms, pots, coul)) + 0.5
+    lists = oracle.neighbors(atoms.get_positions(), atoms.get_cell(), atoms.get_pbc(), cuts)
+    args = (atoms.get_positions(), atoms.get_initial_charges(), atoms.get_cell(), atoms.get_pbc(), model) + tuple(lists)
+    evals = 0
+    t0 = time.perf_counter()
+    while True:
+        oracle.evaluate(*args, what="energy", threads=threads)
+        oracle.evaluate(*args, what="forces", threads=threads)
+        evals += 1
+        dt = time.perf_counter() - t0
+        if dt >= seconds:
+            break
+    return len(atoms) * evals / dt, evals, dt, len(atoms)
+
+
+def dist_env():
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return world, rank, local
+
+
+def run_reference(args):
+    world, rank, local = dist_env()
+    if world > 1:
+        import torch.distributed as dist
+
+        dist.init_process_group("gloo")
+        if rank != 0:
+            dist.barrier()
+            dist.destroy_process_group()
+            return
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import oracle
+    from pysic_gb300.model import compile_model, individual_cutoffs
+
+    threads = os.cpu_count() or 1
+    atoms, pots, coul, desc = workload(args.workload)
+    model = compile_model(atoms, pots, coul)
+    cuts = np.array(individual_cutoffs(atoms, pots, coul)) + 0.5
+    lists = oracle.neighbors(atoms.get_positions(), atoms.get_cell(), atoms.get_pbc(), cuts)
+    a = (atoms.get_positions(), atoms.get_initial_charges(), atoms.get_cell(), atoms.get_pbc(), model) + tuple(lists)
+    for _ in range(args.warmup):
+        oracle.evaluate(*a, what="energy", threads=threads)
+        oracle.evaluate(*a, what="forces", threads=threads)
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        oracle.evaluate(*a, what="energy", threads=threads)
+        oracle.evaluate(*a, what="forces", threads=threads)
+    dt = time.perf_counter() - t0
+    value = len(atoms) * args.steps / dt
+    line = {"impl": "reference", "metric": METRIC, "value": value, "unit": "atom-steps/s", "n_gpus": args.gpus,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * dt / args.steps,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+            "config": {"workload": args.workload, "atoms": len(atoms), "structure": desc,
+                       "implementation": "C restatement of the Fortran core loops (oracle/oracle.c), "
+                                         "energy pass + force pass per step, as the reference does"},
+            "cpu_baseline": {"value": value, "unit": "atom-steps/s", "cores": threads, "kind": "port",
+                             "sample": "{0} full energy+force evaluations of {1} atoms".format(args.steps,
+                                                                                                len(atoms)),
+                             "mpi_ranks": 0},
+            "e2e": {"value": value, "unit": "atom-steps/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line))
+    sys.stdout.flush()
+    if world > 1:
+        import torch.distributed as dist
+
+        dist.barrier()
+        dist.destroy_process_group()
+
+
+def run_ours(args):
+    import torch
+
+    world, rank, local = dist_env()
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+
+        torch.cuda.set_device(local)
+        dist.init_process_group("nccl", device_id=torch.device("cuda", local))
+    from pysic_gb300 import _lib as L
+
+    prec = L.PREC_MIXED if args.precision == "mixed" else L.PREC_FP64
+    flags = L.WANT_ENERGY | L.WANT_FORCES
+    atoms, calc, desc = setup(args.workload, args.precision, local)
+    engine = calc.engine
+    n = len(atoms)
+    flush = torch.empty(64 * 1024 * 1024, dtype=torch.float32, device="cuda:%d" % local)  # 256 MB > L2
+
+    # warm-up (includes the lane-count autotuner and the graph capture)
+    engine.calculate(prec)
+    if dist is not None:
+        dist.barrier()
+    torch.cuda.synchronize()
+    sampler = ClockSampler(local)
+    sampler.start()
+    t_wall0 = time.perf_counter()
+    times, launches = device_time(torch, engine, prec, flags, args.steps, args.warmup, flush)
+    t_wall = time.perf_counter() - t_wall0
+    clocks = sampler.stop()
+    total_ms = sum(times)
+    if dist is not None:
+        t = torch.tensor([total_ms], dtype=torch.float64, device="cuda:%d" % local)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        total_ms = float(t.item())
+    value = world * n * args.steps / (total_ms / 1e3)
+
+    extra = {}
+    # the FP64 kernels on the same workload (the metric's denominator)
+    prec64 = L.PREC_FP64
+    engine.calculate(prec64)
+    t64, _ = device_time(torch, engine, prec64, flags, max(10, args.steps // 4), args.warmup, flush)
+    v64 = n * len(t64) / (sum(t64) / 1e3)
+    r_mixed = engine.calculate(prec)
+    r_64 = engine.calculate(prec64)
+    extra["fp64"] = {"value": v64, "unit": "atom-steps/s", "ms_per_step": statistics.mean(t64)}
+    extra["speedup_vs_fp64"] = value / world / v64
+    extra["accuracy_vs_fp64"] = {
+        "energy_err_eV_per_atom": abs(r_mixed["energy"] - r_64["energy"]) / n,
+        "max_force_err_eV_per_A": float(np.abs(r_mixed["forces"] - r_64["forces"]).max()),
+        "virial_rel_err": float(np.abs(r_mixed["stress"] - r_64["stress"]).max() /
+                                max(1e-30, np.abs(r_64["stress"]).max()))}
+
+    # kernel-level times and the roofline of the dominant kernel
+    kt = kernel_time(torch, engine, prec, flags, min(50, args.steps), flush)
+    dominant = max(kt, key=kt.get)
+    peak, peak_kind = peaks()
+    if args.workload.startswith("tersoff"):
+        alg_bytes = TERSOFF_BYTES_PER_ATOM * n
+        alg_flop = TERSOFF_FLOP_PER_ATOM * n
+        kname = "bond_pass"
+    else:
+        alg_bytes = 48.0 * n
+        alg_flop = None
+        kname = dominant
+    t_k = kt.get(kname, kt[dominant]) / 1e3
+    achieved = alg_bytes / t_k / 1e9
+    traffic = profile_traffic(kname, args.workload)
+    roof = {"bound": "hbm", "kernel": kname, "achieved": achieved, "peak": peak, "unit": "GB/s",
+            "frac": achieved / peak, "traffic": traffic, "peak_source": peak_kind,
+            "note": "not HBM-bound: the working set stays in L2; the FP32 pipe figure is in 'pipe'"}
+    if alg_flop:
+        extra["pipe"] = {"kernel": kname, "achieved_tflops_fp32": alg_flop / t_k / 1e12,
+                         "nominal_peak_tflops_fp32": FP32_NOMINAL_TFLOPS,
+                         "frac_of_nominal": alg_flop / t_k / 1e12 / FP32_NOMINAL_TFLOPS}
+    extra["kernel_ms"] = kt
+
+    # end to end through the C ABI with host buffers
+    e2e_dt, h2d, d2h = e2e_time(torch, engine, atoms, prec, flags, args.steps, args.warmup)
+    e2e = {"value": n * args.steps / e2e_dt, "unit": "atom-steps/s", "h2d_bytes_per_step": h2d,
+           "d2h_bytes_per_step": d2h, "ms_per_step": 1e3 * e2e_dt / args.steps}
+
+    cpu = None
+    if world == 1 and rank == 0 and not args.no_cpu_baseline:
+        threads = os.cpu_count() or 1
+        v, evals, dt, natoms = cpu_baseline(args.workload, args.cpu_seconds, threads)
+        cpu = {"value": v, "unit": "atom-steps/s", "cores": threads, "kind": "port",
+               "sample": "{0} full energy+force evaluations of {1} atoms in {2:.1f} s (oracle, FP64)".format(
+                   evals, natoms, dt), "mpi_ranks": 0}
+
+    if rank == 0:
+        line = {"metric": METRIC, "value": value, "unit": "atom-steps/s", "n_gpus": world, "steps": args.steps,
+                "warmup": args.warmup, "ms_per_step": total_ms / args.steps, "higher_is_better": True,
+                "scaling": "weak", "vs_baseline": None, "dtype": "f32" if prec == L.PREC_MIXED else "f64",
+                "data": "synthetic",
+                "config": {"workload": args.workload, "atoms": n, "structure": desc,
+                           "precision": args.precision + (" (FP32 per pair/triplet, FP64 accumulation)"
+                                                          if prec == L.PREC_MIXED else ""),
+                           "l2": "flushed before every step (256 MB write)",
+                           "neighbor_list": "built once before timing (fixed positions)",
+                           "lanes_per_atom": engine.get_lanes(), "replicas": world},
+                "e2e": e2e, "gpu_launches": launches, "roofline": roof, "cpu_baseline": cpu, "clocks": clocks,
+                "wall_s_timed_region": t_wall}
+        line.update(extra)
+        print(json.dumps(line))
+        sys.stdout.flush()
+    if dist is not None:
+        dist.barrier()
+        dist.destroy_process_group()
+
+
+def run_profile(args):
+    """Short fixed sequence for ncu: build, then `--steps` evaluations with a
+    fixed lanes-per-atom tile (no autotuner launches)."""
+    from pysic_gb300 import _lib as L
+
+    prec = L.PREC_MIXED if args.precision == "mixed" else L.PREC_FP64
+    atoms, calc, _ = setup(args.workload, args.precision, 0)
+    eng = calc.engine
+    eng.set_lanes(args.lanes)
+    for _ in range(args.steps):
+        eng.device_evaluate(prec, L.WANT_ENERGY | L.WANT_FORCES)
+    eng.device_synchronize()
+    r = eng.calculate(prec)
+    print(json.dumps({"profile_run": args.workload, "precision": args.precision, "lanes": args.lanes,
+                      "energy_per_atom": r["energy"] / len(atoms)}))
+
+
+def main():
+    p = argparse.ArgumentParser(description=__doc__, formatter_class=argparse.RawDescriptionHelpFormatter)
+    p.add_argument("--profile", action="store_true", help="short fixed run for ncu captures")
+    p.add_argument("--lanes", type=int, default=8, help="lanes per atom in --profile mode")
+    p.add_argument("--gpus", type=int, default=1)
+    p.add_argument("--steps", type=int, default=100)
+    p.add_argument("--warmup", type=int, default=5)
+    p.add_argument("--impl", choices=["ours", "reference"], default="ours")
+    p.add_argument("--workload", default="tersoff_si_32768")
+    p.add_argument("--precision", choices=["mixed", "fp64"], default="mixed")
+    p.add_argument("--cpu-seconds", type=float, default=12.0)
+    p.add_argument("--no-cpu-baseline", action="store_true")
+    args = p.parse_args()
+    args.warmup = max(3, args.warmup)
+    if args.profile:
+        run_profile(args)
+    elif args.impl == "reference":
+        run_reference(args)
+    else:
+        run_ours(args)
+
+
+if __name__ == "__main__":
+    main()

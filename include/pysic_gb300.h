@@ -60,6 +60,8 @@ const char* pg_version(void);
  * import, pysic/core.py:19-30) and torn down by release (PyInterface.f90:1023-1036). */
 int pg_create(pg_context** ctx);
 int pg_destroy(pg_context* ctx);
+/* Same on an explicit CUDA device (one replica per GPU); device < 0 keeps the current one. */
+int pg_create_on(pg_context** ctx, int32_t device);
 
 /* create_cell(vectors, inverse, periodicity), PyInterface.f90:208-222 */
 int pg_create_cell(pg_context* ctx, const double* cell, const double* inv, const int32_t* pbc);
@@ -169,6 +171,13 @@ int pg_device_positions(pg_context* ctx, double** device_ptr);
 int pg_get_stream(pg_context* ctx, void** stream);
 /* Kernel launches issued by the last pg_device_evaluate / pg_calculate. */
 int pg_last_launch_count(pg_context* ctx, int32_t* launches);
+/* Record CUDA events around the kernel groups of each evaluation;
+ * pg_get_kernel_times waits for the last evaluation and returns five durations
+ * in ms: pair kernel, bond-order pass, gather pass, k-space Ewald, reduction. */
+int pg_set_kernel_timing(pg_context* ctx, int32_t enable);
+int pg_get_kernel_times(pg_context* ctx, float* ms);
+/* Replay each evaluation sequence from a captured CUDA graph (default on). */
+int pg_set_graphs(pg_context* ctx, int32_t enable);
 
 #ifdef __cplusplus
 }

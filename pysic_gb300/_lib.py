@@ -41,6 +41,7 @@ _SIGNATURES = {
     "pg_version": (ctypes.c_char_p, []),
     "pg_create": (ctypes.c_int, [ctypes.POINTER(ctypes.c_void_p)]),
     "pg_destroy": (ctypes.c_int, [_ctx]),
+    "pg_create_on": (ctypes.c_int, [ctypes.POINTER(ctypes.c_void_p), ctypes.c_int32]),
     "pg_create_cell": (ctypes.c_int, [_ctx, _c_double_p, _c_double_p, _c_int_p]),
     "pg_create_atoms": (ctypes.c_int, [_ctx, ctypes.c_int32, _c_double_p, _c_double_p, _c_int_p]),
     "pg_update_atom_coordinates": (ctypes.c_int, [_ctx, _c_double_p]),
@@ -76,6 +77,9 @@ _SIGNATURES = {
     "pg_device_positions": (ctypes.c_int, [_ctx, ctypes.POINTER(_c_double_p)]),
     "pg_get_stream": (ctypes.c_int, [_ctx, ctypes.POINTER(ctypes.c_void_p)]),
     "pg_last_launch_count": (ctypes.c_int, [_ctx, _c_int_p]),
+    "pg_set_kernel_timing": (ctypes.c_int, [_ctx, ctypes.c_int32]),
+    "pg_get_kernel_times": (ctypes.c_int, [_ctx, ctypes.POINTER(ctypes.c_float)]),
+    "pg_set_graphs": (ctypes.c_int, [_ctx, ctypes.c_int32]),
 }
 
 _lib = None

@@ -69,7 +69,7 @@ CellK cell_kernel_view(const Cell& C) {
     return k;
 }
 
-static int pair_lanes(const pg_context* ctx) {
+int pair_lanes_for(const pg_context* ctx) {
     const double avg = ctx->n > 0 ? (double)ctx->nb_total / ctx->n : 0.0;
     if (avg >= 48.0) return 32;
     if (avg >= 16.0) return 16;
@@ -94,7 +94,7 @@ static void enqueue(pg_context* ctx, int precision, int flags, int G) {
     ctx->out_tot.resize(8);
     const bool run_pair = ctx->have_pair_kernel_terms || ctx->ewald || ctx->have_singles;
     const bool run_bond = ctx->have_bond_terms && (wantE || wantF);
-    const int Gp = pair_lanes(ctx);
+    const int Gp = pair_lanes_for(ctx);
     int slots = 0;
     if (run_pair) slots += pair_kernel_blocks(n, Gp);
     if (run_bond) slots += bond_blocks(n, G);
@@ -102,26 +102,36 @@ static void enqueue(pg_context* ctx, int precision, int flags, int G) {
     ctx->red_part.resize(8 * (size_t)std::max(slots, 1));
     bool first_f = true, first_chi = true;
     int used = 0;
+    auto mark = [&](int k) {
+        if (ctx->timing) PG_CUDA(cudaEventRecord(ctx->tev[k], ctx->stream));
+    };
+    mark(0);
     if (run_pair) {
         launch_pair_kernel_impl(ctx, precision, flags, first_f, first_chi, Gp, ctx->red_part.p + 8 * used);
         used += pair_kernel_blocks(n, Gp);
         if (wantF) first_f = false;
         if (wantC) first_chi = false;
     }
+    mark(1);
     if (run_bond) {
-        used += launch_bond_order_impl(ctx, precision, flags, first_f, G, ctx->red_part.p + 8 * used);
+        used += launch_bond_order_impl(ctx, precision, flags, first_f, G, ctx->red_part.p + 8 * used, [&] { mark(2); });
         if (wantF) first_f = false;
+    } else {
+        mark(2);
     }
+    mark(3);
     if (ctx->ewald) {
         launch_ewald_kspace(ctx, precision, flags, first_f, first_chi, ctx->red_part.p + 8 * used);
         used += ewald_partial_slots(ctx);
         if (wantF) first_f = false;
         if (wantC) first_chi = false;
     }
+    mark(4);
     if (wantF && first_f) PG_CUDA(cudaMemsetAsync(ctx->out_f.p, 0, sizeof(double) * 3 * n, ctx->stream));
     if (wantC && first_chi) PG_CUDA(cudaMemsetAsync(ctx->out_chi.p, 0, sizeof(double) * n, ctx->stream));
     if (used > 0) launch_final_reduce(ctx, used);
     else PG_CUDA(cudaMemsetAsync(ctx->out_tot.p, 0, sizeof(double) * 8, ctx->stream));
+    mark(5);
 }
 
 // pick the lanes-per-atom tile of the bond-order kernels by timing each
@@ -160,8 +170,49 @@ void evaluate(pg_context* ctx, int precision, int flags) {
         G = ctx->tuned_lanes[precision];
     }
     if (G == 0) G = 8;
+    if (!ctx->use_graphs) {
+        ctx->launches = 0;
+        enqueue(ctx, precision, flags, G);
+        return;
+    }
+    // replay a captured sequence if nothing it depends on has changed
+    for (auto it = ctx->graphs.begin(); it != ctx->graphs.end(); ++it) {
+        if (it->precision != precision || it->flags != flags || it->lanes != G) continue;
+        if (it->state == ctx->state_epoch && it->alloc == alloc_epoch()) {
+            PG_CUDA(cudaGraphLaunch(it->exec, ctx->stream));
+            ctx->launches = it->launches;
+            return;
+        }
+        cudaGraphExecDestroy(it->exec);
+        ctx->graphs.erase(it);
+        break;
+    }
+    // run once directly (sizes every buffer), then capture the same sequence
     ctx->launches = 0;
     enqueue(ctx, precision, flags, G);
+    const int launches = ctx->launches;
+    const unsigned long long alloc_before = alloc_epoch();
+    cudaGraph_t graph = nullptr;
+    PG_CUDA(cudaStreamBeginCapture(ctx->stream, cudaStreamCaptureModeThreadLocal));
+    try {
+        enqueue(ctx, precision, flags, G);
+    } catch (...) {
+        cudaStreamEndCapture(ctx->stream, &graph);
+        if (graph) cudaGraphDestroy(graph);
+        throw;
+    }
+    PG_CUDA(cudaStreamEndCapture(ctx->stream, &graph));
+    if (alloc_epoch() != alloc_before) {  // a buffer grew during capture: do not keep the graph
+        cudaGraphDestroy(graph);
+        ctx->launches = launches;
+        return;
+    }
+    cudaGraphExec_t exec = nullptr;
+    cudaError_t e = cudaGraphInstantiate(&exec, graph, 0);
+    cudaGraphDestroy(graph);
+    PG_CUDA(e);
+    ctx->graphs.push_back(pg_context::Graph{precision, flags, G, launches, ctx->state_epoch, alloc_epoch(), exec});
+    ctx->launches = launches;
 }
 
 static void copy_results(pg_context* ctx, int flags, double* energy, double* forces, double* stress, double* enegs) {
@@ -184,11 +235,14 @@ const char* pg_last_error(void) { return g_last_error.c_str(); }
 
 const char* pg_version(void) { return "pysic_gb300 0.1 (sm_103a)"; }
 
-int pg_create(pg_context** out) {
+int pg_create(pg_context** out) { return pg_create_on(out, -1); }
+
+int pg_create_on(pg_context** out, int32_t device) {
     return guarded([&] {
         pg::require(out != nullptr, PG_ERR_INVALID, "null output pointer");
         *out = nullptr;
         int dev = 0;
+        if (device >= 0) PG_CUDA(cudaSetDevice(device));
         PG_CUDA(cudaGetDevice(&dev));
         pg_context* ctx = new pg_context();
         ctx->device = dev;
@@ -219,6 +273,7 @@ int pg_create_cell(pg_context* ctx, const double* cell, const double* inv, const
         std::memcpy(ctx->cell_rows, cell, sizeof(ctx->cell_rows));
         std::memcpy(ctx->inv_rows, inv, sizeof(ctx->inv_rows));
         ctx->have_cell = true;
+        ctx->state_epoch++;
         ctx->have_list = false;
         ctx->ew_tables_dirty = true;
     });
@@ -241,6 +296,7 @@ int pg_create_atoms(pg_context* ctx, int32_t n, const double* positions, const d
         ctx->h_type.assign(types, types + n);
         PG_CUDA(cudaStreamSynchronize(ctx->stream));
         ctx->have_atoms = true;
+        ctx->state_epoch++;
         ctx->have_list = false;
     });
 }
@@ -345,6 +401,7 @@ int pg_set_ewald(pg_context* ctx, double real_cut, double k_radius, const int32_
         ctx->ew_scaler.upload(scaler, (size_t)ctx->n, ctx->stream);
         PG_CUDA(cudaStreamSynchronize(ctx->stream));
         ctx->ew_tables_dirty = true;
+        ctx->state_epoch++;
     });
 }
 
@@ -352,6 +409,7 @@ int pg_clear_ewald(pg_context* ctx) {
     return guarded([&] {
         check_ctx(ctx);
         ctx->ewald = false;
+        ctx->state_epoch++;
     });
 }
 
@@ -445,10 +503,8 @@ int pg_relax_charges(pg_context* ctx, int32_t precision, int32_t n_steps, double
         use_device(ctx);
         pg::require(inertia != 0.0, PG_ERR_INVALID, "zero charge inertia");
         pg::require(n_steps >= 0, PG_ERR_INVALID, "negative step count");
-        int s = 0;
-        pg::relax_charges(ctx, precision, n_steps, timestep, inertia, friction, tolerance, rates, charges, &s, error,
+        pg::relax_charges(ctx, precision, n_steps, timestep, inertia, friction, tolerance, rates, charges, steps, error,
                           max_dq);
-        *steps = s;
     });
 }
 
@@ -473,6 +529,7 @@ int pg_set_lanes_per_atom(pg_context* ctx, int32_t lanes) {
         pg::require(lanes == 0 || lanes == 4 || lanes == 8 || lanes == 16 || lanes == 32, PG_ERR_INVALID,
                     "lanes per atom must be 0, 4, 8, 16 or 32");
         ctx->lanes = lanes;
+        ctx->state_epoch++;
     });
 }
 
@@ -519,6 +576,34 @@ int pg_get_stream(pg_context* ctx, void** stream) {
     return guarded([&] {
         check_ctx(ctx);
         *stream = (void*)ctx->stream;
+    });
+}
+
+int pg_set_kernel_timing(pg_context* ctx, int32_t enable) {
+    return guarded([&] {
+        check_ctx(ctx);
+        use_device(ctx);
+        if (enable && !ctx->tev[0])
+            for (auto& e : ctx->tev) PG_CUDA(cudaEventCreate(&e));
+        ctx->timing = enable != 0;
+        ctx->state_epoch++;
+    });
+}
+
+int pg_get_kernel_times(pg_context* ctx, float* ms) {
+    return guarded([&] {
+        check_ctx(ctx);
+        use_device(ctx);
+        pg::require(ctx->timing, PG_ERR_NOT_READY, "kernel timing is off");
+        PG_CUDA(cudaEventSynchronize(ctx->tev[5]));
+        for (int k = 0; k < 5; ++k) PG_CUDA(cudaEventElapsedTime(&ms[k], ctx->tev[k], ctx->tev[k + 1]));
+    });
+}
+
+int pg_set_graphs(pg_context* ctx, int32_t enable) {
+    return guarded([&] {
+        check_ctx(ctx);
+        ctx->use_graphs = enable != 0;
     });
 }
 

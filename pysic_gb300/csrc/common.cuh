@@ -4,6 +4,7 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 
+#include <functional>
 #include <stdexcept>
 #include <string>
 #include <vector>
@@ -30,6 +31,13 @@ inline void require(bool ok, int status, const std::string& msg) {
     if (!ok) throw Error(status, msg);
 }
 
+// Bumped on every device (re)allocation: captured CUDA graphs hold raw
+// pointers and are replayed only while this has not changed.
+inline unsigned long long& alloc_epoch() {
+    static unsigned long long e = 0;
+    return e;
+}
+
 // Grow-only device buffer.
 template <typename T>
 struct DevBuf {
@@ -49,6 +57,7 @@ struct DevBuf {
             size_t c = count + count / 8 + 16;
             PG_CUDA(cudaMalloc(&p, c * sizeof(T)));
             cap = c;
+            ++alloc_epoch();
         }
         n = count;
     }
@@ -170,8 +179,9 @@ struct pg_context {
     pg::DevBuf<double2> ew_S;      // structure factor per listed k (FP64 accumulated)
     pg::DevBuf<float2> ew_Spart;   // per (atom chunk, k) partial sums
     pg::DevBuf<double2> ew_Spart64;
-    pg::DevBuf<uint32_t> ew_frac;  // per atom: fixed-point fractional coordinates (3)
-    int ew_chunks = 0;
+    pg::DevBuf<uint32_t> ew_frac;  // per atom: fixed-point fractional coordinates (4 words)
+    pg::DevBuf<double> ew_qs, ew_qpart, ew_Ssum;
+    pg::DevBuf<double> ew_spart_bytes, ew_fpart_bytes, ew_wS_bytes;  // raw storage, precision-dependent layout
 
     // neighbour lists: full list (CSR) and the short list of bond-order terms
     bool have_list = false;
@@ -213,8 +223,28 @@ struct pg_context {
 
     // charge relaxation
     pg::DevBuf<double> rq_rate, rq_force, rq_stat;
+    pg::DevBuf<int> rq_flag;
 
     int launches = 0;
+
+    // captured evaluation sequences (one per precision / flags / lanes)
+    struct Graph {
+        int precision, flags, lanes, launches;
+        unsigned long long state, alloc;
+        cudaGraphExec_t exec;
+    };
+    std::vector<Graph> graphs;
+    bool use_graphs = true;
+    // optional CUDA events around the kernel groups: pair, bond pass, gather pass, k-space, reduce
+    bool timing = false;
+    cudaEvent_t tev[6] = {nullptr, nullptr, nullptr, nullptr, nullptr, nullptr};
+    unsigned long long state_epoch = 1;  // bumped whenever kernel arguments change
+
+    ~pg_context() {
+        for (auto& g : graphs) cudaGraphExecDestroy(g.exec);
+        for (auto& e : tev)
+            if (e) cudaEventDestroy(e);
+    }
 };
 
 namespace pg {
@@ -239,13 +269,16 @@ void launch_pair_kernel_impl(pg_context* ctx, int precision, int flags, bool fir
 
 // tersoff.cu: returns the number of partial slots written
 int bond_blocks(int n, int G);
-int launch_bond_order_impl(pg_context* ctx, int precision, int flags, bool first_f, int G, double* partial);
+int launch_bond_order_impl(pg_context* ctx, int precision, int flags, bool first_f, int G, double* partial,
+                           const std::function<void()>& between);
 void bond_zeta_diag(pg_context* ctx);
 
 // ewald.cu
 void ewald_prepare(pg_context* ctx);
 int ewald_partial_slots(pg_context* ctx);
 void launch_ewald_kspace(pg_context* ctx, int precision, int flags, bool first_f, bool first_chi, double* partial);
+void launch_ewald_kspace_skip(pg_context* ctx, int precision, int flags, bool first_f, bool first_chi, double* partial,
+                              const int* skip);
 
 // reduce.cu
 void launch_final_reduce(pg_context* ctx, int nslots);

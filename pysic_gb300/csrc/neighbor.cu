@@ -680,6 +680,7 @@ void build_neighbor_lists(pg_context* ctx, const double* h_cutoffs) {
     }
     PG_CUDA(cudaStreamSynchronize(st));
     ctx->have_list = true;
+    ctx->state_epoch++;
     ctx->short_dirty = true;
 }
 
@@ -732,6 +733,7 @@ void build_allpairs_lists(pg_context* ctx, const double* h_cutoffs) {
     }
     PG_CUDA(cudaStreamSynchronize(st));
     ctx->have_list = true;
+    ctx->state_epoch++;
     ctx->short_dirty = true;
 }
 
@@ -754,6 +756,7 @@ void install_neighbor_lists(pg_context* ctx, const int32_t* counts, const int32_
     PG_CUDA(cudaStreamSynchronize(ctx->stream));
     ctx->nb_total = total;
     ctx->have_list = true;
+    ctx->state_epoch++;
     ctx->short_dirty = true;
 }
 
@@ -806,6 +809,7 @@ void build_short_list(pg_context* ctx) {
     require(total == 0 || h[1] >= 0, PG_ERR_INVALID,
             "neighbour lists are not symmetric: a bond has no reverse entry (lists must be built both ways)");
     ctx->short_dirty = false;
+    ctx->state_epoch++;
 }
 
 }  // namespace pg

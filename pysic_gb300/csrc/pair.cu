@@ -36,6 +36,7 @@ struct PairArgs {
     double* out_f;
     double* out_chi;
     double* partial;  // per block: energy, virial[6], pad
+    const int* skip;  // optional device flag: nonzero = do nothing
 };
 
 __device__ __forceinline__ double powi_(double x, int n) {
@@ -50,6 +51,7 @@ __global__ void __launch_bounds__(256) pair_kernel(PairArgs A) {
     const int lane = threadIdx.x % G;
     const int slot = threadIdx.x / G;
     const int i = blockIdx.x * (blockDim.x / G) + slot;
+    if (A.skip && *A.skip) return;
     const bool act = i < A.n;
     R fx = 0, fy = 0, fz = 0, en = 0, chi = 0;
     R w0 = 0, w1 = 0, w2 = 0, w3 = 0, w4 = 0, w5 = 0;
@@ -83,7 +85,8 @@ __global__ void __launch_bounds__(256) pair_kernel(PairArgs A) {
                 if (wantC) chi -= (R)A.charge[j] * k * ec * ir;
             }
             const int tj = A.type[j];
-            const int2 ix = A.index[ti * A.T + tj];
+            // charge-independent pair terms have zero electronegativity
+            const int2 ix = (wantE || wantF) ? A.index[ti * A.T + tj] : make_int2(0, 0);
             for (int t = ix.x; t < ix.x + ix.y; ++t) {
                 const PairTerm P = A.terms[t];
                 if (P.in_bond_kernel || !(r < (R)P.rc)) continue;
@@ -156,9 +159,10 @@ __global__ void __launch_bounds__(256) pair_kernel(PairArgs A) {
 
 int pair_kernel_blocks(int n, int G) { return (n + (256 / G) - 1) / (256 / G); }
 
-void launch_pair_kernel_impl(pg_context* ctx, int precision, int flags, bool first_f, bool first_chi, int G,
-                             double* partial) {
+void launch_pair_kernel_skip(pg_context* ctx, int precision, int flags, bool first_f, bool first_chi, int G,
+                             double* partial, const int* skip) {
     PairArgs A{};
+    A.skip = skip;
     A.n = ctx->n;
     A.T = std::max(ctx->n_types, 1);
     A.pos = ctx->pos.p;
@@ -202,6 +206,11 @@ void launch_pair_kernel_impl(pg_context* ctx, int precision, int flags, bool fir
 #undef PG_PAIR_LAUNCH
     PG_CHECK_LAUNCH();
     ctx->launches++;
+}
+
+void launch_pair_kernel_impl(pg_context* ctx, int precision, int flags, bool first_f, bool first_chi, int G,
+                             double* partial) {
+    launch_pair_kernel_skip(ctx, precision, flags, first_f, first_chi, G, partial, nullptr);
 }
 
 }  // namespace pg

@@ -1,13 +1,223 @@
-// relax.cu -- device-resident damped charge dynamics (placeholder).
+// relax.cu -- ChargeRelaxation 'dynamic' kept on the device.
+//
+// The reference loop (pysic/charges/relaxation.py:417-450) crosses into the
+// Fortran core for every electronegativity evaluation and copies the arrays
+// back each step.  Here one step is a fixed sequence of launches on the
+// context's stream:
+//
+//   rx_update      q += q' dt + (F - gamma q') dt^2 / M ;  q' = (1 - gamma dt/2) q' + F dt / (2M)
+//   electronegativity kernels (pair kernel + k-space Ewald) on the new q
+//   rx_mean        mean(chi) over all atoms (deterministic FP64 sum)
+//   rx_force       F = chi - mean ;  q' = (q' + F dt/(2M)) / (1 + gamma dt/2) ;  max F, max |dq|
+//   rx_stop        error = max F (signed, relaxation.py:449); stop when error <= tol or steps reached
+//
+// Every kernel first reads a device flag and returns at once when the loop has
+// stopped, so the host can enqueue a chunk of steps and read back only the
+// flag and the statistics once per chunk.  Convergence statistics and charge
+// sums are kept in FP64.
+#include <algorithm>
+#include <vector>
+
 #include "common.cuh"
 
 namespace pg {
 
+void launch_pair_kernel_skip(pg_context* ctx, int precision, int flags, bool first_f, bool first_chi, int G,
+                             double* partial, const int* skip);
+int pair_lanes_for(const pg_context* ctx);
+
+namespace {
+
+constexpr int RT = 256;
+
+struct RxArgs {
+    int n;
+    double* q;
+    double* rate;
+    double* force;
+    const double* chi;
+    double dt, inv_m, friction, tol;
+    int n_steps;
+    int* flag;        // [0] stop flag, [1] steps taken
+    double* stat;     // [0] error, [1] max |dq| of the last step, [2] mean chi
+    double* part;     // per block: sum chi, max F, max |dq|
+    int nblocks;
+};
+
+__global__ void rx_update(RxArgs A) {
+    __shared__ double sm[RT];
+    if (A.flag[0]) return;
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    double dq = 0.0;
+    if (i < A.n) {
+        const double r = A.rate[i], f = A.force[i];
+        dq = r * A.dt + (f - A.friction * r) * A.inv_m * A.dt * A.dt;
+        A.q[i] += dq;
+        A.rate[i] = (1.0 - 0.5 * A.friction * A.dt) * r + f * 0.5 * A.inv_m * A.dt;
+    }
+    sm[threadIdx.x] = fabs(dq);
+    __syncthreads();
+    for (int s = blockDim.x / 2; s > 0; s >>= 1) {
+        if (threadIdx.x < s) sm[threadIdx.x] = fmax(sm[threadIdx.x], sm[threadIdx.x + s]);
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) A.part[3 * blockIdx.x + 2] = sm[0];
+}
+
+// mean of chi: per-block sums in rx_block_sums, then a single block adds them in order
+__global__ void rx_block_sums(RxArgs A) {
+    __shared__ double sm[RT];
+    if (A.flag[0]) return;
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    sm[threadIdx.x] = i < A.n ? A.chi[i] : 0.0;
+    __syncthreads();
+    for (int s = blockDim.x / 2; s > 0; s >>= 1) {
+        if (threadIdx.x < s) sm[threadIdx.x] += sm[threadIdx.x + s];
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) A.part[3 * blockIdx.x] = sm[0];
+}
+
+__global__ void rx_mean(RxArgs A) {
+    if (A.flag[0]) return;
+    if (threadIdx.x == 0) {
+        double s = 0.0, c = 0.0;
+        for (int b = 0; b < A.nblocks; ++b) {
+            const double y = A.part[3 * b] - c;
+            const double t = s + y;
+            c = (t - s) - y;
+            s = t;
+        }
+        A.stat[2] = s / A.n;
+    }
+}
+
+template <bool INIT>
+__global__ void rx_force(RxArgs A) {
+    __shared__ double sm[RT];
+    if (A.flag[0]) return;
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    double f = -1e300;
+    if (i < A.n) {
+        f = A.chi[i] - A.stat[2];
+        A.force[i] = f;
+        if (!INIT) A.rate[i] = (A.rate[i] + f * 0.5 * A.inv_m * A.dt) / (1.0 + 0.5 * A.friction * A.dt);
+    }
+    sm[threadIdx.x] = f;
+    __syncthreads();
+    for (int s = blockDim.x / 2; s > 0; s >>= 1) {
+        if (threadIdx.x < s) sm[threadIdx.x] = fmax(sm[threadIdx.x], sm[threadIdx.x + s]);
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) A.part[3 * blockIdx.x + 1] = sm[0];
+}
+
+__global__ void rx_stop(RxArgs A) {
+    if (A.flag[0]) return;
+    if (threadIdx.x == 0) {
+        double e = -1e300, dq = 0.0;
+        for (int b = 0; b < A.nblocks; ++b) {
+            e = fmax(e, A.part[3 * b + 1]);
+            dq = fmax(dq, A.part[3 * b + 2]);
+        }
+        const int steps = A.flag[1] + 1;
+        A.flag[1] = steps;
+        A.stat[0] = e;
+        A.stat[1] = dq;
+        if (!(e > A.tol) || steps >= A.n_steps) A.flag[0] = 1;
+    }
+}
+
+__global__ void rx_init_stat(RxArgs A) {
+    if (threadIdx.x == 0) {
+        double e = -1e300;
+        for (int b = 0; b < A.nblocks; ++b) e = fmax(e, A.part[3 * b + 1]);
+        A.stat[0] = e;
+        A.stat[1] = 0.0;
+    }
+}
+
+}  // namespace
+
+// electronegativities of the current charges into ctx->out_chi, stopped by `skip`
+static void enqueue_chi(pg_context* ctx, int precision, const int* skip) {
+    const int G = pair_lanes_for(ctx);
+    double* part = ctx->red_part.p;
+    launch_pair_kernel_skip(ctx, precision, PG_WANT_ENEGS, true, true, G, part, skip);
+    if (ctx->ewald) launch_ewald_kspace_skip(ctx, precision, PG_WANT_ENEGS, true, false, part, skip);
+}
+
 void relax_charges(pg_context* ctx, int precision, int n_steps, double dt, double inertia, double friction,
                    double tolerance, double* rates, double* charges, int* steps, double* error, double* max_dq) {
-    (void)ctx; (void)precision; (void)n_steps; (void)dt; (void)inertia; (void)friction; (void)tolerance;
-    (void)rates; (void)charges; (void)steps; (void)error; (void)max_dq;
-    require(false, PG_ERR_UNSUPPORTED, "charge relaxation is not available in this build");
+    require(ctx->have_list && ctx->have_atoms, PG_ERR_NOT_READY, "set atoms, potentials and lists first");
+    if (ctx->tables_dirty) fold_tables(ctx);
+    if (ctx->ewald) ewald_prepare(ctx);
+    const int n = ctx->n;
+    cudaStream_t st = ctx->stream;
+    const int nb = std::max(1, (n + RT - 1) / RT);
+    ctx->out_chi.resize((size_t)std::max(n, 1));
+    ctx->out_f.resize(3 * (size_t)std::max(n, 1));
+    const int G = pair_lanes_for(ctx);
+    const int slots = (n + (256 / G) - 1) / (256 / G) + (ctx->ewald ? ewald_partial_slots(ctx) : 0) + 1;
+    ctx->red_part.resize(8 * (size_t)slots);
+    ctx->rq_rate.upload(rates, (size_t)n, st);
+    ctx->rq_force.resize((size_t)std::max(n, 1));
+    ctx->rq_stat.resize(4 + 3 * (size_t)nb);
+    ctx->rq_flag.resize(2);
+    PG_CUDA(cudaMemsetAsync(ctx->rq_flag.p, 0, sizeof(int) * 2, st));
+    RxArgs A{};
+    A.n = n;
+    A.q = ctx->charge.p;
+    A.rate = ctx->rq_rate.p;
+    A.force = ctx->rq_force.p;
+    A.chi = ctx->out_chi.p;
+    A.dt = dt;
+    A.inv_m = 1.0 / inertia;
+    A.friction = friction;
+    A.tol = tolerance;
+    A.n_steps = n_steps;
+    A.flag = ctx->rq_flag.p;
+    A.stat = ctx->rq_stat.p;
+    A.part = ctx->rq_stat.p + 4;
+    A.nblocks = nb;
+    ctx->launches = 0;
+    // initial differences (relaxation.py:433)
+    enqueue_chi(ctx, precision, A.flag);
+    rx_block_sums<<<nb, RT, 0, st>>>(A);
+    rx_mean<<<1, 32, 0, st>>>(A);
+    rx_force<true><<<nb, RT, 0, st>>>(A);
+    rx_init_stat<<<1, 32, 0, st>>>(A);
+    PG_CHECK_LAUNCH();
+    int h_flag[2] = {0, 0};
+    double h_stat[3] = {2.0 * tolerance, 0.0, 0.0};
+    if (n_steps <= 0 || !(2.0 * tolerance > tolerance)) h_flag[0] = 1;
+    // chunks of steps: all kernels test the stop flag, the host polls once per chunk
+    int chunk = 4;
+    const int max_launch_chunks = 1 << 20;
+    for (int c = 0; c < max_launch_chunks && !h_flag[0]; ++c) {
+        for (int s = 0; s < chunk; ++s) {
+            rx_update<<<nb, RT, 0, st>>>(A);
+            enqueue_chi(ctx, precision, A.flag);
+            rx_block_sums<<<nb, RT, 0, st>>>(A);
+            rx_mean<<<1, 32, 0, st>>>(A);
+            rx_force<false><<<nb, RT, 0, st>>>(A);
+            rx_stop<<<1, 32, 0, st>>>(A);
+        }
+        PG_CHECK_LAUNCH();
+        PG_CUDA(cudaMemcpyAsync(h_flag, A.flag, sizeof(h_flag), cudaMemcpyDeviceToHost, st));
+        PG_CUDA(cudaStreamSynchronize(st));
+        chunk = std::min(chunk * 2, 64);
+    }
+    PG_CUDA(cudaMemcpyAsync(h_stat, A.stat, sizeof(double) * 3, cudaMemcpyDeviceToHost, st));
+    PG_CUDA(cudaMemcpyAsync(rates, A.rate, sizeof(double) * n, cudaMemcpyDeviceToHost, st));
+    PG_CUDA(cudaMemcpyAsync(charges, A.q, sizeof(double) * n, cudaMemcpyDeviceToHost, st));
+    PG_CUDA(cudaMemcpyAsync(h_flag, A.flag, sizeof(h_flag), cudaMemcpyDeviceToHost, st));
+    PG_CUDA(cudaStreamSynchronize(st));
+    *steps = h_flag[1];
+    *error = h_stat[0];
+    *max_dq = h_stat[1];
+    if (h_flag[1] >= n_steps && h_stat[0] > tolerance)
+        throw Error(PG_ERR_NOT_CONVERGED, "charge relaxation reached its step limit before the tolerance");
 }
 
 }  // namespace pg

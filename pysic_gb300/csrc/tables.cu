@@ -131,6 +131,7 @@ void fold_tables(pg_context* ctx) {
     ctx->d_single_index.upload(sindex.data(), sindex.size(), st);
     PG_CUDA(cudaStreamSynchronize(st));
     ctx->tables_dirty = false;
+    ctx->state_epoch++;
     ctx->short_dirty = true;
 }
 

@@ -23,6 +23,8 @@
 //              produced by exactly one lane group, bit-reproducibly.
 // The virial uses the reference's convention sum(r_rel (x) F): pair part
 // r_ij (x) F_j, three-body part r_ij (x) F_j + r_ik (x) F_k (Core.f90:5146-5172).
+#include <functional>
+
 #include "common.cuh"
 #include "kernels.cuh"
 
@@ -120,15 +122,10 @@ __global__ void __launch_bounds__(128) bond_pass(BondArgs A) {
             }
             R fjx = 0, fjy = 0, fjz = 0;
             V4* row = fk + tri + (long long)e * ni;
-            if (!any || r == R(0)) {
-                for (int k = 0; k < ni; ++k)
-                    if (k != e) row[k] = V4{0, 0, 0, 0};
-                fj[s + e] = V4{0, 0, 0, 0};
-                continue;
-            }
             const TripletTerm* trow = A.trip + ((long long)ti * A.T + tj) * A.T;
+            // zeta_ij (core_calculate_pair_bond_order_factor, first neighbour loop)
             R zeta = 0, B = 1, dB = 0;
-            if (bo) {
+            if ((bo || A.zeta_out) && r != R(0)) {
                 for (int k = 0; k < ni; ++k) {
                     if (k == e) continue;
                     const V4 gik = geo[s + k];
@@ -137,12 +134,20 @@ __global__ void __launch_bounds__(128) bond_pass(BondArgs A) {
                     if (!TT.valid) continue;
                     zeta += tersoff_term<R>(load_trip<R>(TT), a, r, V3<R>{gik.x, gik.y, gik.z}, gik.w);
                 }
+            }
+            if (A.zeta_out) A.zeta_out[s + e] = (double)zeta;
+            if (!any || r == R(0)) {
+                for (int k = 0; k < ni; ++k)
+                    if (k != e) row[k] = V4{0, 0, 0, 0};
+                fj[s + e] = V4{0, 0, 0, 0};
+                continue;
+            }
+            if (bo) {
                 if (pp.valid) post_process<R>((R)pp.beta, (R)pp.eta, zeta, B, dB);
                 else {
                     B = zeta;
                     dB = 1;
                 }
-                if (A.zeta_out) A.zeta_out[s + e] = (double)zeta;
             }
             R U = 0, dU = 0, P = 0;
             for (int t = ix.x; t < ix.x + ix.y; ++t) {
@@ -336,28 +341,31 @@ static BondArgs bond_args(pg_context* ctx, int precision, int flags, bool first_
 }
 
 template <typename R, int G>
-static void launch_pair(const BondArgs& A, int n, cudaStream_t st, bool forces) {
+static void launch_pair(const BondArgs& A, int n, cudaStream_t st, bool forces, const std::function<void()>& between) {
     bond_pass<R, G><<<bond_blocks(n, G), 128, 0, st>>>(A);
+    between();
     if (forces) gather_pass<R, G><<<bond_blocks(n, G), 128, 0, st>>>(A);
 }
 
 template <typename R>
-static void launch_by_lanes(const BondArgs& A, int n, cudaStream_t st, int G, bool forces) {
+static void launch_by_lanes(const BondArgs& A, int n, cudaStream_t st, int G, bool forces,
+                            const std::function<void()>& between) {
     switch (G) {
-        case 4: launch_pair<R, 4>(A, n, st, forces); break;
-        case 8: launch_pair<R, 8>(A, n, st, forces); break;
-        case 16: launch_pair<R, 16>(A, n, st, forces); break;
-        default: launch_pair<R, 32>(A, n, st, forces); break;
+        case 4: launch_pair<R, 4>(A, n, st, forces, between); break;
+        case 8: launch_pair<R, 8>(A, n, st, forces, between); break;
+        case 16: launch_pair<R, 16>(A, n, st, forces, between); break;
+        default: launch_pair<R, 32>(A, n, st, forces, between); break;
     }
 }
 
-// returns the number of partial slots written
-int launch_bond_order_impl(pg_context* ctx, int precision, int flags, bool first_f, int G, double* partial) {
+// returns the number of partial slots written; `between` runs between the two passes
+int launch_bond_order_impl(pg_context* ctx, int precision, int flags, bool first_f, int G, double* partial,
+                           const std::function<void()>& between) {
     prepare_scratch(ctx, precision);
     BondArgs A = bond_args(ctx, precision, flags, first_f, partial);
     const bool forces = (flags & PG_WANT_FORCES) != 0;
-    if (precision == PG_PREC_FP64) launch_by_lanes<double>(A, ctx->n, ctx->stream, G, forces);
-    else launch_by_lanes<float>(A, ctx->n, ctx->stream, G, forces);
+    if (precision == PG_PREC_FP64) launch_by_lanes<double>(A, ctx->n, ctx->stream, G, forces, between);
+    else launch_by_lanes<float>(A, ctx->n, ctx->stream, G, forces, between);
     PG_CHECK_LAUNCH();
     ctx->launches += forces ? 2 : 1;
     return bond_blocks(ctx->n, G);

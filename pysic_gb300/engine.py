@@ -1,6 +1,7 @@
 """Python handle on one engine context (the GB300 replacement of the
 reference's Fortran core state, fortran/Core.f90:13-98)."""
 import ctypes
+import os
 
 import numpy as np
 
@@ -12,10 +13,12 @@ class Engine:
     """Owns one ``pg_context``: cell, atoms, interaction records, neighbour
     lists and device buffers.  Every method maps to one C-ABI call."""
 
-    def __init__(self):
+    def __init__(self, device=None):
         self.lib = L.load()
         ctx = ctypes.c_void_p()
-        L.check(self.lib.pg_create(ctypes.byref(ctx)))
+        if device is None:
+            device = int(os.environ.get("PYSIC_GB300_DEVICE", "-1"))
+        L.check(self.lib.pg_create_on(ctypes.byref(ctx), int(device)))
         self.ctx = ctx
         self.n = 0
 
@@ -185,6 +188,24 @@ class Engine:
         v = ctypes.c_int32(0)
         L.check(self.lib.pg_last_launch_count(self.ctx, ctypes.byref(v)))
         return v.value
+
+    def set_kernel_timing(self, enable):
+        L.check(self.lib.pg_set_kernel_timing(self.ctx, 1 if enable else 0))
+
+    def kernel_times(self):
+        """Durations (ms) of the last evaluation's kernel groups: pair, bond
+        pass, gather pass, k-space Ewald, reduction."""
+        ms = (ctypes.c_float * 5)()
+        L.check(self.lib.pg_get_kernel_times(self.ctx, ms))
+        return dict(zip(("pair", "bond_pass", "gather_pass", "kspace", "reduce"), list(ms)))
+
+    def set_graphs(self, enable):
+        L.check(self.lib.pg_set_graphs(self.ctx, 1 if enable else 0))
+
+    def calculate_into(self, precision, flags, energy, forces, stress, enegs):
+        """pg_calculate into caller-provided (e.g. pinned) host arrays."""
+        L.check(self.lib.pg_calculate(self.ctx, precision, flags, L.dptr(energy), L.dptr(forces), L.dptr(stress),
+                                      L.dptr(enegs)))
 
 
 __all__ = ["Engine", "EngineError"]

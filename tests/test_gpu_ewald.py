@@ -1,0 +1,119 @@
+"""GPU parity of Ewald summation, charge terms and device-resident charge relaxation.
+
+Tolerances: FP64 path within 1e-11 relative (energy), 1e-9 eV/A (forces),
+1e-9 eV/e (electronegativities) of the oracle; mixed path within 1e-5 eV/atom
+and 1e-3 eV/A of the FP64 path; relaxation: same step count and charges
+within 1e-8 e (FP64).
+"""
+import numpy as np
+import pytest
+
+import oracle
+import pysic_gb300 as pysic
+from helpers import engine_all, oracle_all, oracle_lists
+from pysic_gb300 import workloads as W
+from pysic_gb300.model import compile_model
+
+pytestmark = pytest.mark.gpu
+
+
+def _nacl_small():
+    atoms = W.rocksalt_nacl(3, noise=0.1, seed=21)
+    pots, coul = W.nacl_potentials(sigma=1.6, real_cutoff=6.0, cutoff=6.0)
+    return atoms, pots, coul
+
+
+def test_ewald_fp64_parity():
+    atoms, pots, coul = _nacl_small()
+    ref = oracle_all(atoms, pots, coul)
+    got = engine_all(atoms, pots, coul, "fp64")
+    assert got["energy"] == pytest.approx(ref["energy"], rel=1e-11)
+    assert np.abs(got["forces"] - ref["forces"]).max() < 1e-9
+    assert np.abs(got["enegs"] - ref["enegs"]).max() < 1e-9
+    np.testing.assert_allclose(got["stress"], ref["stress"], rtol=1e-9, atol=1e-9 * np.abs(ref["stress"]).max())
+
+
+def test_ewald_triclinic_and_scaler_fp64_parity():
+    rng = np.random.default_rng(3)
+    cell = np.array([[11.0, 0.0, 0.0], [2.5, 10.5, 0.0], [-1.0, 1.5, 12.0]])
+    n = 60
+    pos = rng.uniform(0, 1, (n, 3)) @ cell
+    q = rng.normal(0, 0.5, n)
+    q -= q.mean()
+    atoms = pysic.Atoms(["Na"] * (n // 2) + ["Cl"] * (n // 2), pos, cell=cell, pbc=True, charges=q)
+    scaler = list(rng.uniform(0.5, 1.5, n))
+    coul = pysic.CoulombSummation("ewald", [4.0, W.ewald_kcut(1.3), 1.3, W.EPS0], scaler=scaler)
+    pots = [pysic.Potential("Buckingham", symbols=[["Na", "Cl"]], parameters=[1000.0, 13717.42, 0.3], cutoff=4.0)]
+    ref = oracle_all(atoms, pots, coul)
+    got = engine_all(atoms, pots, coul, "fp64")
+    assert got["energy"] == pytest.approx(ref["energy"], rel=1e-11)
+    assert np.abs(got["forces"] - ref["forces"]).max() < 1e-9
+    assert np.abs(got["enegs"] - ref["enegs"]).max() < 1e-9
+
+
+def test_ewald_nacl_8000_mixed_vs_fp64():
+    atoms = W.rocksalt_nacl()
+    pots, coul = W.nacl_potentials()
+    a64 = engine_all(atoms, pots, coul, "fp64")
+    am = engine_all(atoms, pots, coul, "mixed")
+    n = len(atoms)
+    print("NaCl 8000 mixed-fp64: dE/atom", abs(am["energy"] - a64["energy"]) / n, "max dF",
+          np.abs(am["forces"] - a64["forces"]).max())
+    assert abs(am["energy"] - a64["energy"]) / n < 1e-5
+    assert np.abs(am["forces"] - a64["forces"]).max() < 1e-3
+
+
+def test_charge_self_and_ewald_enegs_fp64():
+    atoms = W.sio2_box(100, seed=4)
+    pots, coul = W.sio2_potentials(real_cutoff=6.0, sigma=1.8)
+    q = np.random.default_rng(1).normal(0, 0.4, len(atoms))
+    q -= q.mean()
+    atoms.set_initial_charges(q)
+    ref = oracle_all(atoms, pots, coul)
+    got = engine_all(atoms, pots, coul, "fp64")
+    assert got["energy"] == pytest.approx(ref["energy"], rel=1e-11)
+    assert np.abs(got["enegs"] - ref["enegs"]).max() < 1e-9
+
+
+def test_charge_relaxation_matches_oracle_loop():
+    atoms = W.sio2_box(100, seed=5)
+    pots, coul = W.sio2_potentials(real_cutoff=6.0, sigma=1.8)
+    params = dict(n_steps=400, timestep=0.1, inertia=1.0, friction=4.0, tolerance=1e-4)
+    calc = pysic.Pysic(atoms, pots, coulomb=coul, precision="fp64")
+    rel = pysic.ChargeRelaxation("dynamic", calculator=calc,
+                                 parameters=[params[k] for k in ("n_steps", "timestep", "inertia", "friction",
+                                                                 "tolerance")])
+    q_gpu = rel.charge_relaxation()
+    model = compile_model(atoms, pots, coul)
+    lists = oracle_lists(atoms, pots, coul)
+    r = oracle.relax_charges(atoms.get_positions(), np.zeros(len(atoms)), atoms.get_cell(), atoms.get_pbc(), model,
+                             *lists, **params)
+    assert rel.last_steps == r["steps"]
+    assert r["steps"] < params["n_steps"]
+    np.testing.assert_allclose(q_gpu, r["charges"], atol=1e-8)
+    assert abs(q_gpu.sum()) < 1e-9
+
+
+def test_charge_relaxation_warm_rates_persist():
+    atoms = W.sio2_box(60, seed=6)
+    pots, coul = W.sio2_potentials(real_cutoff=5.0, sigma=1.6)
+    calc = pysic.Pysic(atoms, pots, coulomb=coul)
+    rel = pysic.ChargeRelaxation("dynamic", calculator=calc, parameters=[5, 0.1, 1.0, 4.0, 1e-12])
+    rel.charge_relaxation()
+    assert rel.last_steps == 5 and rel.last_converged is False
+    assert np.abs(rel.charge_rates).max() > 0
+
+
+def test_graph_replay_matches_direct_launches():
+    atoms, pots, coul = _nacl_small()
+    calc = pysic.Pysic(atoms, pots, coulomb=coul, precision="mixed")
+    calc.set_core()
+    eng = calc.engine
+    a = eng.calculate(1, energy=True, forces=True, enegs=True)
+    b = eng.calculate(1, energy=True, forces=True, enegs=True)  # graph replay
+    eng.set_graphs(False)
+    c = eng.calculate(1, energy=True, forces=True, enegs=True)
+    for x in (b, c):
+        assert x["energy"] == a["energy"]
+        assert np.array_equal(x["forces"], a["forces"])
+        assert np.array_equal(x["enegs"], a["enegs"])
