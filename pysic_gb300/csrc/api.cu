@@ -170,7 +170,8 @@ void evaluate(pg_context* ctx, int precision, int flags) {
         G = ctx->tuned_lanes[precision];
     }
     if (G == 0) G = 8;
-    if (!ctx->use_graphs) {
+    // events recorded inside a capture cannot be waited on: time with direct launches
+    if (!ctx->use_graphs || ctx->timing) {
         ctx->launches = 0;
         enqueue(ctx, precision, flags, G);
         return;

@@ -90,27 +90,43 @@ struct CellK {
 };
 
 // One pair term folded per type pair (an interaction record whose two target
-// masks contain the pair of types).
-struct PairTerm {
-    int kind;      // 0 LJ, 1 exponential, 2 Buckingham
-    int group;     // -1: plain, else bond-order group
-    int smooth;    // smoothing active (create_potential, Potentials.f90:2382-2388)
+// masks contain the pair of types).  Every table exists in FP64 and in FP32 so
+// that the mixed-precision kernels never convert parameters per term.
+template <typename R>
+struct PairT {
+    int kind;            // 0 LJ, 1 exponential, 2 Buckingham
+    int group;           // -1: plain, else bond-order group
+    int smooth;          // smoothing active (create_potential, Potentials.f90:2382-2388)
     int in_bond_kernel;  // evaluated by the bond-order kernels (short list) rather than the pair kernel
-    double p[4];
-    double rc, rs;
+    R p0, p1, p2, rc, rs;
 };
 
 // Tersoff triplet parameters for (centre type, j type, k type) of group 0.
-struct TripletTerm {
-    double a, c2, d2, h, mu, rc, rs;
+template <typename R>
+struct TripT {
+    R a, c2, d2, h, mu, rc, rs;
     int valid;
 };
 
 // Post-processing (B(zeta)) parameters per centre type for group 0.
-struct PostTerm {
-    double beta, eta;
+template <typename R>
+struct PostT {
+    R beta, eta;
     int valid;
 };
+
+template <typename R, typename S>
+inline PairT<R> cast_pair(const PairT<S>& a) {
+    return PairT<R>{a.kind, a.group, a.smooth, a.in_bond_kernel, (R)a.p0, (R)a.p1, (R)a.p2, (R)a.rc, (R)a.rs};
+}
+template <typename R, typename S>
+inline TripT<R> cast_trip(const TripT<S>& a) {
+    return TripT<R>{(R)a.a, (R)a.c2, (R)a.d2, (R)a.h, (R)a.mu, (R)a.rc, (R)a.rs, a.valid};
+}
+template <typename R, typename S>
+inline PostT<R> cast_post(const PostT<S>& a) {
+    return PostT<R>{(R)a.beta, (R)a.eta, a.valid};
+}
 
 struct SingleTerm {
     int kind;
@@ -157,11 +173,15 @@ struct pg_context {
     bool tables_dirty = true;
     bool have_bond_terms = false, have_pair_kernel_terms = false, have_singles = false;
     double bo_radius = 0.0;          // largest cutoff handled by the bond-order kernels
-    pg::DevBuf<pg::PairTerm> d_pair_terms;
+    pg::DevBuf<pg::PairT<double>> d_pair_terms;
+    pg::DevBuf<pg::PairT<float>> d_pair_terms32;
     pg::DevBuf<int2> d_pair_index;     // per (ti, tj): offset, count into d_pair_terms
-    pg::DevBuf<pg::TripletTerm> d_trip;  // n_types^3
-    pg::DevBuf<pg::PostTerm> d_post;     // n_types
+    pg::DevBuf<pg::TripT<double>> d_trip;  // n_types^3
+    pg::DevBuf<pg::TripT<float>> d_trip32;
+    pg::DevBuf<pg::PostT<double>> d_post;  // n_types
+    pg::DevBuf<pg::PostT<float>> d_post32;
     pg::DevBuf<double> d_maxbr;          // per type: max bond-order cutoff (max_bond_radius)
+    pg::DevBuf<float> d_maxbr32;
     pg::DevBuf<pg::SingleTerm> d_single_terms;
     pg::DevBuf<int2> d_single_index;     // per type
 
@@ -193,6 +213,11 @@ struct pg_context {
     bool short_is_full = false;
     pg::DevBuf<int> sh_start, sh_idx, sh_off, sh_rev, sh_count;
     pg::DevBuf<long long> sh_tri;  // per atom: base of its n_i^2 triplet block
+    // mixed path: bond vectors at short-list build time (FP64 -> FP32) and the
+    // positions they were taken at; an evaluation adds the FP32 displacements
+    pg::DevBuf<pg::F4> sh_sep0;
+    pg::DevBuf<double> sh_pos0;
+    pg::DevBuf<pg::F4> disp32;
     long long sh_total = 0, sh_tri_total = 0;
     int sh_maxn = 0;
 

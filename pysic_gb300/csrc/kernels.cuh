@@ -13,11 +13,6 @@ struct V3 {
     R x, y, z;
 };
 
-template <typename R>
-__device__ __forceinline__ R rcp_(R x) {
-    return R(1) / x;
-}
-
 __device__ __forceinline__ void sincospi_(float x, float* s, float* c) { sincospif(x, s, c); }
 __device__ __forceinline__ void sincospi_(double x, double* s, double* c) { sincospi(x, s, c); }
 __device__ __forceinline__ float exp_(float x) { return expf(x); }
@@ -72,23 +67,16 @@ __device__ __forceinline__ void pair_eval(int kind, R p0, R p1, R p2, R r, R& V,
     }
 }
 
-// Tersoff triplet parameters in working precision
+// V f and d(V f)/dr of one pair term, smoothing included
 template <typename R>
-struct Trip {
-    R a, c2, d2, h, mu, rc, rs;
-};
-
-template <typename R>
-__device__ __forceinline__ Trip<R> load_trip(const TripletTerm& T) {
-    Trip<R> t;
-    t.a = (R)T.a;
-    t.c2 = (R)T.c2;
-    t.d2 = (R)T.d2;
-    t.h = (R)T.h;
-    t.mu = (R)T.mu;
-    t.rc = (R)T.rc;
-    t.rs = (R)T.rs;
-    return t;
+__device__ __forceinline__ void pair_term(const PairT<R>& P, R r, R& V, R& dV) {
+    pair_eval<R>(P.kind, P.p0, P.p1, P.p2, r, V, dV);
+    if (P.smooth) {
+        R f, fp;
+        smooth<R>(r, P.rc, P.rs, f, fp);
+        dV = dV * f + V * fp;
+        V = V * f;
+    }
 }
 
 // Angular function g = 1 + c^2/d^2 - c^2/(d^2 + (h - cos)^2) of
@@ -97,7 +85,7 @@ __device__ __forceinline__ Trip<R> load_trip(const TripletTerm& T) {
 // does not cancel catastrophically in FP32 (c^2/d^2 is ~4e7 for silicon);
 // dg/dcos = -2 c^2 (h - cos) / (d^2 + x)^2.
 template <typename R>
-__device__ __forceinline__ void angular(const Trip<R>& t, R cs, R& g, R& dg) {
+__device__ __forceinline__ void angular(const TripT<R>& t, R cs, R& g, R& dg) {
     const R hc = t.h - cs;
     const R x = hc * hc;
     const R den = t.d2 + x;
@@ -108,7 +96,7 @@ __device__ __forceinline__ void angular(const Trip<R>& t, R cs, R& g, R& dg) {
 
 // exp((a (r1 - r2))^mu) and its derivative with respect to r1 - r2
 template <typename R>
-__device__ __forceinline__ void radial_exp(const Trip<R>& t, R dr, R& X, R& Xp) {
+__device__ __forceinline__ void radial_exp(const TripT<R>& t, R dr, R& X, R& Xp) {
     if (t.a == R(0)) {
         X = R(1);
         Xp = R(0);
@@ -123,7 +111,7 @@ __device__ __forceinline__ void radial_exp(const Trip<R>& t, R dr, R& X, R& Xp) 
 // zeta term xi_ijk g_ijk for bond ij (vector a, length r1) and neighbour k
 // (vector b, length r2), Potentials.f90:5744-5795
 template <typename R>
-__device__ __forceinline__ R tersoff_term(const Trip<R>& t, const V3<R>& a, R r1, const V3<R>& b, R r2) {
+__device__ __forceinline__ R tersoff_term(const TripT<R>& t, const V3<R>& a, R r1, const V3<R>& b, R r2) {
     R f, fp;
     smooth(r2, t.rc, t.rs, f, fp);
     if (f == R(0)) return R(0);
@@ -139,7 +127,7 @@ __device__ __forceinline__ R tersoff_term(const Trip<R>& t, const V3<R>& a, R r1
 // (the gradient with respect to the centre i is minus their sum);
 // Potentials.f90:5806-5902 computes the same derivatives.
 template <typename R>
-__device__ __forceinline__ bool tersoff_grad(const Trip<R>& t, const V3<R>& a, R r1, const V3<R>& b, R r2, V3<R>& gj,
+__device__ __forceinline__ bool tersoff_grad(const TripT<R>& t, const V3<R>& a, R r1, const V3<R>& b, R r2, V3<R>& gj,
                                              V3<R>& gk) {
     R f, fp;
     smooth(r2, t.rc, t.rs, f, fp);
@@ -183,6 +171,28 @@ __device__ __forceinline__ T group_sum(T v) {
 #pragma unroll
     for (int o = G / 2; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o, G);
     return v;
+}
+
+// Compensated group sum of FP32 values (Knuth two-sum at every step); the
+// FP64 result carries the rounding errors the FP32 additions made.
+template <int G>
+__device__ __forceinline__ double group_sum_c(float v) {
+    float s = v, c = 0.0f;
+#pragma unroll
+    for (int o = G / 2; o > 0; o >>= 1) {
+        const float so = __shfl_xor_sync(0xffffffffu, s, o, G);
+        const float co = __shfl_xor_sync(0xffffffffu, c, o, G);
+        const float t = s + so;
+        const float bp = t - s;
+        const float err = (s - (t - bp)) + (so - bp);
+        s = t;
+        c = c + co + err;
+    }
+    return (double)s + (double)c;
+}
+template <int G>
+__device__ __forceinline__ double group_sum_c(double v) {
+    return group_sum<G>(v);
 }
 
 }  // namespace pg

@@ -439,6 +439,21 @@ __global__ void short_fill(int n, const double* __restrict__ pos, CellK C, const
         }
 }
 
+// separation_vector (Geometry.f90:449-466) of every short-list entry, rounded to FP32
+__global__ void short_sep0(int n, const double* __restrict__ pos, CellK C, const int* __restrict__ start,
+                           const int* __restrict__ idx, const int* __restrict__ off, F4* __restrict__ sep0) {
+    int a = blockIdx.x * blockDim.x + threadIdx.x;
+    if (a >= n) return;
+    for (int e = start[a]; e < start[a + 1]; ++e) {
+        const int b = idx[e];
+        double s[3];
+        for (int c = 0; c < 3; ++c) s[c] = __dsub_rn(pos[3 * b + c], pos[3 * a + c]);
+        for (int i = 0; i < 3; ++i)
+            for (int c = 0; c < 3; ++c) s[c] = __dadd_rn(s[c], __dmul_rn((double)off[3 * e + i], C.vc[c][i]));
+        sep0[e] = F4{(float)s[0], (float)s[1], (float)s[2], 0.0f};
+    }
+}
+
 __global__ void short_reverse(int n, const int* __restrict__ start, const int* __restrict__ idx,
                               const int* __restrict__ off, int* __restrict__ rev, int* __restrict__ cnt) {
     int a = blockIdx.x * blockDim.x + threadIdx.x;
@@ -785,6 +800,15 @@ void build_short_list(pg_context* ctx) {
         short_reverse<<<blocks(n, 128), 128, 0, st>>>(n, ctx->sh_start.p, ctx->sh_idx.p, ctx->sh_off.p, ctx->sh_rev.p,
                                                      ctx->sh_count.p);
         PG_CHECK_LAUNCH();
+    }
+    // bond vectors and positions of this build, for the mixed-precision kernels
+    ctx->sh_sep0.resize(std::max(total, 1));
+    ctx->sh_pos0.resize(3 * (size_t)std::max(n, 1));
+    if (n > 0) {
+        short_sep0<<<blocks(n, 128), 128, 0, st>>>(n, ctx->pos.p, C, ctx->sh_start.p, ctx->sh_idx.p, ctx->sh_off.p,
+                                                  ctx->sh_sep0.p);
+        PG_CHECK_LAUNCH();
+        PG_CUDA(cudaMemcpyAsync(ctx->sh_pos0.p, ctx->pos.p, sizeof(double) * 3 * n, cudaMemcpyDeviceToDevice, st));
     }
     // triplet block bases: exclusive scan of n_i^2
     ctx->sh_tri.resize(n + 1);

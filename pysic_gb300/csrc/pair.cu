@@ -25,7 +25,7 @@ struct PairArgs {
     const int* start;
     const int* idx;
     const int* off;
-    const PairTerm* terms;
+    const void* terms;  // PairT<R>
     const int2* index;
     const SingleTerm* sterms;
     const int2* sindex;
@@ -88,16 +88,10 @@ __global__ void __launch_bounds__(256) pair_kernel(PairArgs A) {
             // charge-independent pair terms have zero electronegativity
             const int2 ix = (wantE || wantF) ? A.index[ti * A.T + tj] : make_int2(0, 0);
             for (int t = ix.x; t < ix.x + ix.y; ++t) {
-                const PairTerm P = A.terms[t];
-                if (P.in_bond_kernel || !(r < (R)P.rc)) continue;
+                const PairT<R> P = ((const PairT<R>*)A.terms)[t];
+                if (P.in_bond_kernel || !(r < P.rc)) continue;
                 R V, dV;
-                pair_eval<R>(P.kind, (R)P.p[0], (R)P.p[1], (R)P.p[2], r, V, dV);
-                if (P.smooth) {
-                    R f, fp;
-                    smooth<R>(r, (R)P.rc, (R)P.rs, f, fp);
-                    dV = dV * f + V * fp;
-                    V = V * f;
-                }
+                pair_term<R>(P, r, V, dV);
                 U += V;
                 dU += dV;
             }
@@ -172,7 +166,7 @@ void launch_pair_kernel_skip(pg_context* ctx, int precision, int flags, bool fir
     A.start = ctx->nb_start.p;
     A.idx = ctx->nb_idx.p;
     A.off = ctx->nb_off.p;
-    A.terms = ctx->d_pair_terms.p;
+    A.terms = precision == PG_PREC_FP64 ? (const void*)ctx->d_pair_terms.p : (const void*)ctx->d_pair_terms32.p;
     A.index = ctx->d_pair_index.p;
     A.sterms = ctx->d_single_terms.p;
     A.sindex = ctx->d_single_index.p;

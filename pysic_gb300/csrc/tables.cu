@@ -29,9 +29,9 @@ void fold_tables(pg_context* ctx) {
                 "the GB300 engine evaluates one bond-order group (one Coordinator) per calculator");
 
     // bond-order tables
-    std::vector<TripletTerm> trip((size_t)T * T * T);
-    for (auto& t : trip) t = TripletTerm{0, 0, 0, 0, 0, 0, 0, 0};
-    std::vector<PostTerm> post(T, PostTerm{0, 0, 0});
+    std::vector<TripT<double>> trip((size_t)T * T * T);
+    for (auto& t : trip) t = TripT<double>{0, 0, 0, 0, 0, 0, 0, 0};
+    std::vector<PostT<double>> post(T, PostT<double>{0, 0, 0});
     std::vector<double> maxbr(T, 0.0);
     double bo_radius = 0.0;
     for (int b = 0; b < nb; ++b) {
@@ -40,12 +40,12 @@ void fold_tables(pg_context* ctx) {
         for (int ti = 0; ti < T; ++ti) {
             if (!has(ctx->br_m1[b], ti)) continue;
             if (ctx->br_cut[b] > maxbr[ti]) maxbr[ti] = ctx->br_cut[b];
-            if (!post[ti].valid) post[ti] = PostTerm{p[0], p[1], 1};
+            if (!post[ti].valid) post[ti] = PostT<double>{p[0], p[1], 1};
             for (int tj = 0; tj < T; ++tj) {
                 if (!has(ctx->br_m2[b], tj)) continue;
                 for (int tk = 0; tk < T; ++tk) {
                     if (!has(ctx->br_m3[b], tk)) continue;
-                    TripletTerm& tt = trip[((size_t)ti * T + tj) * T + tk];
+                    TripT<double>& tt = trip[((size_t)ti * T + tj) * T + tk];
                     require(!tt.valid, PG_ERR_UNSUPPORTED,
                             "two Tersoff factors act on the same (i, j, k) element triple");
                     tt.a = p[2];
@@ -73,7 +73,7 @@ void fold_tables(pg_context* ctx) {
     ctx->have_bond_terms = bond;
     ctx->bo_radius = bo_radius;
 
-    std::vector<PairTerm> terms;
+    std::vector<PairT<double>> terms;
     std::vector<int2> index((size_t)T * T, make_int2(0, 0));
     bool pair_kernel_terms = false;
     for (int ti = 0; ti < T; ++ti)
@@ -82,10 +82,12 @@ void fold_tables(pg_context* ctx) {
             ix.x = (int)terms.size();
             for (int r = 0; r < np; ++r) {
                 if (!has(ctx->pr_m1[r], ti) || !has(ctx->pr_m2[r], tj)) continue;
-                PairTerm t{};
+                PairT<double> t{};
                 t.kind = ctx->pr_kind[r];
                 t.group = ctx->pr_group[r];
-                for (int q = 0; q < 4; ++q) t.p[q] = ctx->pr_params[4 * (size_t)r + q];
+                t.p0 = ctx->pr_params[4 * (size_t)r];
+                t.p1 = ctx->pr_params[4 * (size_t)r + 1];
+                t.p2 = ctx->pr_params[4 * (size_t)r + 2];
                 t.rc = ctx->pr_cut[r];
                 const double soft = ctx->pr_soft[r];
                 if (soft > 0.0 && soft < t.rc) {
@@ -120,13 +122,24 @@ void fold_tables(pg_context* ctx) {
     ctx->have_singles = !sterms.empty();
     ctx->have_pair_kernel_terms = pair_kernel_terms;
 
-    if (terms.empty()) terms.push_back(PairTerm{});
+    if (terms.empty()) terms.push_back(PairT<double>{});
     if (sterms.empty()) sterms.push_back(SingleTerm{});
+    std::vector<PairT<float>> terms32(terms.size());
+    for (size_t q = 0; q < terms.size(); ++q) terms32[q] = cast_pair<float>(terms[q]);
+    std::vector<TripT<float>> trip32(trip.size());
+    for (size_t q = 0; q < trip.size(); ++q) trip32[q] = cast_trip<float>(trip[q]);
+    std::vector<PostT<float>> post32(post.size());
+    for (size_t q = 0; q < post.size(); ++q) post32[q] = cast_post<float>(post[q]);
+    std::vector<float> maxbr32(maxbr.begin(), maxbr.end());
     ctx->d_pair_terms.upload(terms.data(), terms.size(), st);
+    ctx->d_pair_terms32.upload(terms32.data(), terms32.size(), st);
     ctx->d_pair_index.upload(index.data(), index.size(), st);
     ctx->d_trip.upload(trip.data(), trip.size(), st);
+    ctx->d_trip32.upload(trip32.data(), trip32.size(), st);
     ctx->d_post.upload(post.data(), post.size(), st);
+    ctx->d_post32.upload(post32.data(), post32.size(), st);
     ctx->d_maxbr.upload(maxbr.data(), maxbr.size(), st);
+    ctx->d_maxbr32.upload(maxbr32.data(), maxbr32.size(), st);
     ctx->d_single_terms.upload(sterms.data(), sterms.size(), st);
     ctx->d_single_index.upload(sindex.data(), sindex.size(), st);
     PG_CUDA(cudaStreamSynchronize(st));

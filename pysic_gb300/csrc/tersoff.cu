@@ -19,10 +19,18 @@
 //              mixed path) so that no other atom's force is touched.
 //  gather_pass per atom m: own centre part + the j-parts of the bonds i->m
 //              (through the reverse-bond index) + the k-parts of every bond
-//              i->x with k = m.  Summed in FP64.  No atomics: each force is
-//              produced by exactly one lane group, bit-reproducibly.
+//              i->x with k = m.  No atomics: each force is produced by exactly
+//              one lane group, bit-reproducibly.
 // The virial uses the reference's convention sum(r_rel (x) F): pair part
 // r_ij (x) F_j, three-body part r_ij (x) F_j + r_ik (x) F_k (Core.f90:5146-5172).
+//
+// Precision.  The FP64 path computes every bond vector from the FP64 positions
+// like separation_vector (Geometry.f90:449-466).  The mixed path keeps FP64 out
+// of the per-term work: bond vectors are taken once per short-list build in
+// FP64 (rounded to FP32), and every evaluation adds the FP32 displacement of
+// both atoms since that build (prepared per atom in FP64 by disp_pass).  Lane
+// partial sums are FP32; the lanes of an atom are combined with a compensated
+// (two-sum) reduction and the per-atom totals are FP64.
 #include <functional>
 
 #include "common.cuh"
@@ -51,11 +59,13 @@ struct BondArgs {
     const int* off;
     const int* rev;
     const long long* tri;
-    const PairTerm* terms;
+    const void* terms;  // PairT<R>
     const int2* index;
-    const TripletTerm* trip;
-    const PostTerm* post;
-    const double* maxbr;
+    const void* trip;   // TripT<R>
+    const void* post;   // PostT<R>
+    const void* maxbr;  // R
+    const F4* sep0;     // mixed path: bond vectors at list build
+    const F4* disp;     // mixed path: per-atom displacement since the build
     int flags;
     int first_f;
     void* geo;
@@ -67,6 +77,38 @@ struct BondArgs {
     double* zeta_out;
 };
 
+// per-atom displacement since the short-list build, FP64 difference rounded to FP32
+__global__ void disp_pass(int n, const double* __restrict__ pos, const double* __restrict__ pos0, F4* __restrict__ d) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    d[i] = F4{(float)(pos[3 * i] - pos0[3 * i]), (float)(pos[3 * i + 1] - pos0[3 * i + 1]),
+              (float)(pos[3 * i + 2] - pos0[3 * i + 2]), 0.0f};
+}
+
+template <typename R>
+__device__ __forceinline__ typename Vec4T<R>::T bond_vector(const BondArgs& A, int i, int e, double xi, double yi,
+                                                            double zi);
+
+template <>
+__device__ __forceinline__ D4 bond_vector<double>(const BondArgs& A, int i, int e, double xi, double yi, double zi) {
+    const int j = A.idx[e];
+    const double o0 = A.off[3 * e], o1 = A.off[3 * e + 1], o2 = A.off[3 * e + 2];
+    double sx = A.pos[3 * j] - xi, sy = A.pos[3 * j + 1] - yi, sz = A.pos[3 * j + 2] - zi;
+    sx += o0 * A.C.vc[0][0] + o1 * A.C.vc[0][1] + o2 * A.C.vc[0][2];
+    sy += o0 * A.C.vc[1][0] + o1 * A.C.vc[1][1] + o2 * A.C.vc[1][2];
+    sz += o0 * A.C.vc[2][0] + o1 * A.C.vc[2][1] + o2 * A.C.vc[2][2];
+    return D4{sx, sy, sz, sqrt(sx * sx + sy * sy + sz * sz)};
+}
+
+template <>
+__device__ __forceinline__ F4 bond_vector<float>(const BondArgs& A, int i, int e, double, double, double) {
+    const int j = A.idx[e];
+    const F4 s0 = A.sep0[e];
+    const F4 dj = A.disp[j], di = A.disp[i];
+    const float x = s0.x + (dj.x - di.x), y = s0.y + (dj.y - di.y), z = s0.z + (dj.z - di.z);
+    return F4{x, y, z, sqrtf(x * x + y * y + z * z)};
+}
+
 template <typename R, int G>
 __global__ void __launch_bounds__(128) bond_pass(BondArgs A) {
     using V4 = typename Vec4T<R>::T;
@@ -74,37 +116,25 @@ __global__ void __launch_bounds__(128) bond_pass(BondArgs A) {
     V4* geo = (V4*)A.geo;
     V4* fj = (V4*)A.fj;
     V4* fk = (V4*)A.fk;
+    const PairT<R>* terms = (const PairT<R>*)A.terms;
     const int lane = threadIdx.x % G;
     const int slot = threadIdx.x / G;
     const int i = blockIdx.x * (blockDim.x / G) + slot;
     const bool act = i < A.n;
     const int s = act ? A.start[i] : 0;
     const int ni = act ? A.start[i + 1] - s : 0;
-    // geometry of i's bonds: FP64 separation, then the working precision
+    // geometry of i's bonds in the working precision
     if (act) {
         const double xi = A.pos[3 * i], yi = A.pos[3 * i + 1], zi = A.pos[3 * i + 2];
-        for (int e = lane; e < ni; e += G) {
-            const int j = A.idx[s + e];
-            const double o0 = A.off[3 * (s + e)], o1 = A.off[3 * (s + e) + 1], o2 = A.off[3 * (s + e) + 2];
-            double sx = A.pos[3 * j] - xi, sy = A.pos[3 * j + 1] - yi, sz = A.pos[3 * j + 2] - zi;
-            sx += o0 * A.C.vc[0][0] + o1 * A.C.vc[0][1] + o2 * A.C.vc[0][2];
-            sy += o0 * A.C.vc[1][0] + o1 * A.C.vc[1][1] + o2 * A.C.vc[1][2];
-            sz += o0 * A.C.vc[2][0] + o1 * A.C.vc[2][1] + o2 * A.C.vc[2][2];
-            V4 g;
-            g.x = (R)sx;
-            g.y = (R)sy;
-            g.z = (R)sz;
-            g.w = sqrt_(g.x * g.x + g.y * g.y + g.z * g.z);
-            geo[s + e] = g;
-        }
+        for (int e = lane; e < ni; e += G) geo[s + e] = bond_vector<R>(A, i, s + e, xi, yi, zi);
     }
     __syncwarp();
     R Fx = 0, Fy = 0, Fz = 0, En = 0;
     R W0 = 0, W1 = 0, W2 = 0, W3 = 0, W4 = 0, W5 = 0;
     if (act) {
         const int ti = A.type[i];
-        const R maxbr = (R)A.maxbr[ti];
-        const PostTerm pp = A.post[ti];
+        const R maxbr = ((const R*)A.maxbr)[ti];
+        const PostT<R> pp = ((const PostT<R>*)A.post)[ti];
         const long long tri = A.tri[i];
         for (int e = lane; e < ni; e += G) {
             const V4 gij = geo[s + e];
@@ -114,15 +144,15 @@ __global__ void __launch_bounds__(128) bond_pass(BondArgs A) {
             const int2 ix = A.index[ti * A.T + tj];
             bool any = false, bo = false;
             for (int t = ix.x; t < ix.x + ix.y; ++t) {
-                const PairTerm& P = A.terms[t];
-                if (P.in_bond_kernel && r < (R)P.rc) {
+                const PairT<R>& P = terms[t];
+                if (P.in_bond_kernel && r < P.rc) {
                     any = true;
                     bo |= P.group >= 0;
                 }
             }
             R fjx = 0, fjy = 0, fjz = 0;
             V4* row = fk + tri + (long long)e * ni;
-            const TripletTerm* trow = A.trip + ((long long)ti * A.T + tj) * A.T;
+            const TripT<R>* trow = (const TripT<R>*)A.trip + ((long long)ti * A.T + tj) * A.T;
             // zeta_ij (core_calculate_pair_bond_order_factor, first neighbour loop)
             R zeta = 0, B = 1, dB = 0;
             if ((bo || A.zeta_out) && r != R(0)) {
@@ -130,9 +160,9 @@ __global__ void __launch_bounds__(128) bond_pass(BondArgs A) {
                     if (k == e) continue;
                     const V4 gik = geo[s + k];
                     if (!(gik.w < maxbr)) continue;
-                    const TripletTerm& TT = trow[A.type[A.idx[s + k]]];
+                    const TripT<R>& TT = trow[A.type[A.idx[s + k]]];
                     if (!TT.valid) continue;
-                    zeta += tersoff_term<R>(load_trip<R>(TT), a, r, V3<R>{gik.x, gik.y, gik.z}, gik.w);
+                    zeta += tersoff_term<R>(TT, a, r, V3<R>{gik.x, gik.y, gik.z}, gik.w);
                 }
             }
             if (A.zeta_out) A.zeta_out[s + e] = (double)zeta;
@@ -143,7 +173,7 @@ __global__ void __launch_bounds__(128) bond_pass(BondArgs A) {
                 continue;
             }
             if (bo) {
-                if (pp.valid) post_process<R>((R)pp.beta, (R)pp.eta, zeta, B, dB);
+                if (pp.valid) post_process<R>(pp.beta, pp.eta, zeta, B, dB);
                 else {
                     B = zeta;
                     dB = 1;
@@ -151,16 +181,10 @@ __global__ void __launch_bounds__(128) bond_pass(BondArgs A) {
             }
             R U = 0, dU = 0, P = 0;
             for (int t = ix.x; t < ix.x + ix.y; ++t) {
-                const PairTerm& PT = A.terms[t];
-                if (!PT.in_bond_kernel || !(r < (R)PT.rc)) continue;
+                const PairT<R>& PT = terms[t];
+                if (!PT.in_bond_kernel || !(r < PT.rc)) continue;
                 R V, dV;
-                pair_eval<R>(PT.kind, (R)PT.p[0], (R)PT.p[1], (R)PT.p[2], r, V, dV);
-                if (PT.smooth) {
-                    R f, fp;
-                    smooth<R>(r, (R)PT.rc, (R)PT.rs, f, fp);
-                    dV = dV * f + V * fp;
-                    V = V * f;
-                }
+                pair_term<R>(PT, r, V, dV);
                 if (PT.group < 0) {
                     U += V;
                     dU += dV;
@@ -193,11 +217,11 @@ __global__ void __launch_bounds__(128) bond_pass(BondArgs A) {
                 if (bo && pref != R(0)) {
                     const V4 gik = geo[s + k];
                     if (gik.w < maxbr) {
-                        const TripletTerm& TT = trow[A.type[A.idx[s + k]]];
+                        const TripT<R>& TT = trow[A.type[A.idx[s + k]]];
                         if (TT.valid) {
                             V3<R> gj, gk;
                             const V3<R> b{gik.x, gik.y, gik.z};
-                            if (tersoff_grad<R>(load_trip<R>(TT), a, r, b, gik.w, gj, gk)) {
+                            if (tersoff_grad<R>(TT, a, r, b, gik.w, gj, gk)) {
                                 const R jx = -pref * gj.x, jy = -pref * gj.y, jz = -pref * gj.z;
                                 const R kx = -pref * gk.x, ky = -pref * gk.y, kz = -pref * gk.z;
                                 fjx += jx;
@@ -222,17 +246,24 @@ __global__ void __launch_bounds__(128) bond_pass(BondArgs A) {
             fj[s + e] = V4{fjx, fjy, fjz, 0};
         }
     }
-    double d[10] = {(double)Fx, (double)Fy, (double)Fz, (double)En, (double)W0,
-                    (double)W1, (double)W2, (double)W3, (double)W4, (double)W5};
-#pragma unroll
-    for (int q = 0; q < 10; ++q) d[q] = group_sum<G>(d[q]);
+    const double d0 = group_sum_c<G>(Fx), d1 = group_sum_c<G>(Fy), d2 = group_sum_c<G>(Fz);
+    const double de = group_sum_c<G>(En);
+    const double w0 = group_sum_c<G>(W0), w1 = group_sum_c<G>(W1), w2 = group_sum_c<G>(W2);
+    const double w3 = group_sum_c<G>(W3), w4 = group_sum_c<G>(W4), w5 = group_sum_c<G>(W5);
     if (act && lane == 0) {
-        A.fc[3 * i] = d[0];
-        A.fc[3 * i + 1] = d[1];
-        A.fc[3 * i + 2] = d[2];
+        A.fc[3 * i] = d0;
+        A.fc[3 * i + 1] = d1;
+        A.fc[3 * i + 2] = d2;
     }
-    if (lane == 0)
-        for (int q = 0; q < 7; ++q) red[slot][q] = act ? d[3 + q] : 0.0;
+    if (lane == 0) {
+        red[slot][0] = act ? de : 0.0;
+        red[slot][1] = act ? w0 : 0.0;
+        red[slot][2] = act ? w1 : 0.0;
+        red[slot][3] = act ? w2 : 0.0;
+        red[slot][4] = act ? w3 : 0.0;
+        red[slot][5] = act ? w4 : 0.0;
+        red[slot][6] = act ? w5 : 0.0;
+    }
     __syncthreads();
     if (A.partial && threadIdx.x < 7) {
         double sum = 0;
@@ -272,7 +303,7 @@ __global__ void __launch_bounds__(128) gather_pass(BondArgs A) {
             }
         }
     }
-    double fx = group_sum<G>((double)Fx), fy = group_sum<G>((double)Fy), fz = group_sum<G>((double)Fz);
+    double fx = group_sum_c<G>(Fx), fy = group_sum_c<G>(Fy), fz = group_sum_c<G>(Fz);
     if (act && lane == 0) {
         fx += A.fc[3 * m];
         fy += A.fc[3 * m + 1];
@@ -300,6 +331,7 @@ static void prepare_scratch(pg_context* ctx, int precision) {
     } else {
         ctx->bo_fj.resize(2 * ne);
         ctx->bo_fk.resize(nt);
+        ctx->disp32.resize((size_t)std::max(ctx->n, 1));
     }
     ctx->bo_fc.resize(3 * (size_t)std::max(ctx->n, 1));
 }
@@ -316,22 +348,28 @@ static BondArgs bond_args(pg_context* ctx, int precision, int flags, bool first_
     A.off = ctx->sh_off.p;
     A.rev = ctx->sh_rev.p;
     A.tri = ctx->sh_tri.p;
-    A.terms = ctx->d_pair_terms.p;
     A.index = ctx->d_pair_index.p;
-    A.trip = ctx->d_trip.p;
-    A.post = ctx->d_post.p;
-    A.maxbr = ctx->d_maxbr.p;
     A.flags = flags;
     A.first_f = first_f;
     const size_t ne = (size_t)std::max<long long>(ctx->sh_total, 1);
     if (precision == PG_PREC_FP64) {
+        A.terms = ctx->d_pair_terms.p;
+        A.trip = ctx->d_trip.p;
+        A.post = ctx->d_post.p;
+        A.maxbr = ctx->d_maxbr.p;
         A.geo = ctx->bo_fj64.p;
         A.fj = ctx->bo_fj64.p + ne;
         A.fk = ctx->bo_fk64.p;
     } else {
+        A.terms = ctx->d_pair_terms32.p;
+        A.trip = ctx->d_trip32.p;
+        A.post = ctx->d_post32.p;
+        A.maxbr = ctx->d_maxbr32.p;
         A.geo = ctx->bo_fj.p;
         A.fj = ctx->bo_fj.p + ne;
         A.fk = ctx->bo_fk.p;
+        A.sep0 = ctx->sh_sep0.p;
+        A.disp = ctx->disp32.p;
     }
     A.fc = ctx->bo_fc.p;
     A.out_f = ctx->out_f.p;
@@ -364,8 +402,13 @@ int launch_bond_order_impl(pg_context* ctx, int precision, int flags, bool first
     prepare_scratch(ctx, precision);
     BondArgs A = bond_args(ctx, precision, flags, first_f, partial);
     const bool forces = (flags & PG_WANT_FORCES) != 0;
-    if (precision == PG_PREC_FP64) launch_by_lanes<double>(A, ctx->n, ctx->stream, G, forces, between);
-    else launch_by_lanes<float>(A, ctx->n, ctx->stream, G, forces, between);
+    if (precision == PG_PREC_FP64) {
+        launch_by_lanes<double>(A, ctx->n, ctx->stream, G, forces, between);
+    } else {
+        disp_pass<<<(ctx->n + 255) / 256, 256, 0, ctx->stream>>>(ctx->n, ctx->pos.p, ctx->sh_pos0.p, ctx->disp32.p);
+        ctx->launches++;
+        launch_by_lanes<float>(A, ctx->n, ctx->stream, G, forces, between);
+    }
     PG_CHECK_LAUNCH();
     ctx->launches += forces ? 2 : 1;
     return bond_blocks(ctx->n, G);

@@ -164,10 +164,13 @@ def sio2_box(n_si=1000, seed=0):
 SIO2_CHARGE_PARAMS = {"Si": (4.17, 6.97), "O": (8.74, 13.36)}
 
 
-def sio2_potentials(real_cutoff=10.0, sigma=2.5, k_cutoff=None, half_hardness=True):
-    """Charge self energy chi q + (J/2) q^2 per element as two 'charge_self'
-    terms (epsilon q^n, n = 1 and 2).  half_hardness=True uses J/2 for the
-    quadratic term (the usual QEq convention)."""
+def sio2_potentials(real_cutoff=10.0, sigma=2.5, k_cutoff=None, half_hardness=False):
+    """Charge self energy chi q + J q^2 per element as two 'charge_self'
+    terms (epsilon q^n, n = 1 and 2).  With J as the quadratic coefficient the
+    charge Hessian of these random structures (Si-O pairs down to 1.5 A, point
+    charges) is positive definite; with J/2 (half_hardness=True) the close
+    Si-O Coulomb coupling (14.4/1.5 = 9.6 eV) exceeds the hardness and the
+    energy has no minimum in q, so damped dynamics diverge."""
     pots = []
     for el, (chi, J) in SIO2_CHARGE_PARAMS.items():
         pots.append(Potential("charge_self", symbols=[[el]], parameters=[chi, 1]))

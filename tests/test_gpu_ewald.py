@@ -47,7 +47,8 @@ def test_ewald_triclinic_and_scaler_fp64_parity():
     ref = oracle_all(atoms, pots, coul)
     got = engine_all(atoms, pots, coul, "fp64")
     assert got["energy"] == pytest.approx(ref["energy"], rel=1e-11)
-    assert np.abs(got["forces"] - ref["forces"]).max() < 1e-9
+    # random positions without rejection: some Buckingham forces reach 1e7 eV/A
+    assert np.abs(got["forces"] - ref["forces"]).max() < 1e-12 * max(1.0, np.abs(ref["forces"]).max())
     assert np.abs(got["enegs"] - ref["enegs"]).max() < 1e-9
 
 
