@@ -76,11 +76,12 @@ int pair_lanes_for(const pg_context* ctx) {
     return 8;
 }
 
-static void prepare(pg_context* ctx) {
+void prepare(pg_context* ctx) {
     require(ctx->have_cell, PG_ERR_NOT_READY, "no cell: call pg_create_cell first");
     require(ctx->have_atoms, PG_ERR_NOT_READY, "no atoms: call pg_create_atoms first");
     require(ctx->have_list, PG_ERR_NOT_READY, "no neighbour lists: build or install them first");
     if (ctx->tables_dirty) fold_tables(ctx);
+    if (ctx->sep0_epoch != ctx->list_epoch) build_full_sep0(ctx);
     if (ctx->have_bond_terms && ctx->short_dirty) build_short_list(ctx);
     if (ctx->ewald) ewald_prepare(ctx);
 }
@@ -106,6 +107,7 @@ static void enqueue(pg_context* ctx, int precision, int flags, int G) {
         if (ctx->timing) PG_CUDA(cudaEventRecord(ctx->tev[k], ctx->stream));
     };
     mark(0);
+    if (precision == PG_PREC_MIXED && (run_pair || run_bond)) launch_disp(ctx, nullptr);
     if (run_pair) {
         launch_pair_kernel_impl(ctx, precision, flags, first_f, first_chi, Gp, ctx->red_part.p + 8 * used);
         used += pair_kernel_blocks(n, Gp);

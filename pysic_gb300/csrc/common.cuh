@@ -213,11 +213,14 @@ struct pg_context {
     bool short_is_full = false;
     pg::DevBuf<int> sh_start, sh_idx, sh_off, sh_rev, sh_count;
     pg::DevBuf<long long> sh_tri;  // per atom: base of its n_i^2 triplet block
-    // mixed path: bond vectors at short-list build time (FP64 -> FP32) and the
-    // positions they were taken at; an evaluation adds the FP32 displacements
-    pg::DevBuf<pg::F4> sh_sep0;
-    pg::DevBuf<double> sh_pos0;
+    pg::DevBuf<int> sh_type;       // per short entry: type of the partner atom
+    // mixed path: bond vectors of both lists taken once per list generation in
+    // FP64 (rounded to FP32) at the positions pos0; an evaluation adds the FP32
+    // displacements pos - pos0 of the two atoms
+    pg::DevBuf<pg::F4> sh_sep0, nb_sep0;
+    pg::DevBuf<double> pos0;
     pg::DevBuf<pg::F4> disp32;
+    unsigned long long list_epoch = 0, sep0_epoch = ~0ull;
     long long sh_total = 0, sh_tri_total = 0;
     int sh_maxn = 0;
 
@@ -281,6 +284,8 @@ CellK cell_kernel_view(const Cell& C);
 // neighbor.cu
 void build_neighbor_lists(pg_context* ctx, const double* h_cutoffs);
 void build_short_list(pg_context* ctx);
+void build_full_sep0(pg_context* ctx);
+void launch_disp(pg_context* ctx, const int* skip);
 void build_allpairs_lists(pg_context* ctx, const double* h_cutoffs);
 void install_neighbor_lists(pg_context* ctx, const int32_t* counts, const int32_t* idx, const int32_t* off);
 
@@ -314,6 +319,7 @@ void relax_charges(pg_context* ctx, int precision, int n_steps, double dt, doubl
 
 // api.cu
 void evaluate(pg_context* ctx, int precision, int flags);
+void prepare(pg_context* ctx);  // fold tables, start a list generation, short list, Ewald tables
 
 // utilities
 void exclusive_scan_int(const int* in, int* out, int n, cudaStream_t s, DevBuf<int>& tmp, int* total_host);

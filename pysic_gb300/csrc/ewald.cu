@@ -27,6 +27,7 @@
 #include <vector>
 
 #include "common.cuh"
+#include "fixed.cuh"
 #include "kernels.cuh"
 
 namespace pg {
@@ -131,17 +132,21 @@ __global__ void ew_prep(EwArgs A) {
         q = A.charge[i] * A.scaler[i];
         A.qs[i] = q;
     }
-    sq[threadIdx.x] = q;
-    sq2[threadIdx.x] = q * q;
+    // block sums of q and q^2: shuffle trees (no sequential FP64 chain)
+    double a = group_sum<32>(q), b = group_sum<32>(q * q);
+    if ((threadIdx.x & 31) == 0) {
+        sq[threadIdx.x >> 5] = a;
+        sq2[threadIdx.x >> 5] = b;
+    }
     __syncthreads();
-    if (threadIdx.x == 0) {
-        double a = 0, b = 0;
-        for (int k = 0; k < (int)blockDim.x; ++k) {
-            a += sq[k];
-            b += sq2[k];
+    if (threadIdx.x < 32) {
+        const int nw = blockDim.x >> 5;
+        a = group_sum<32>(threadIdx.x < nw ? sq[threadIdx.x] : 0.0);
+        b = group_sum<32>(threadIdx.x < nw ? sq2[threadIdx.x] : 0.0);
+        if (threadIdx.x == 0) {
+            A.qpart[2 * blockIdx.x] = a;
+            A.qpart[2 * blockIdx.x + 1] = b;
         }
-        A.qpart[2 * blockIdx.x] = a;
-        A.qpart[2 * blockIdx.x + 1] = b;
     }
 }
 
@@ -203,46 +208,88 @@ __global__ void __launch_bounds__(EW_THREADS) ew_sfac(EwArgs A) {
     }
 }
 
+// sum of the chunk partials of one k: compensated FP32 (two-sum) in the mixed
+// path, plain FP64 in the FP64 path
+__device__ __forceinline__ void add_c(float v, float& s, float& c) {
+    const float t = s + v;
+    const float bp = t - s;
+    c += (s - (t - bp)) + (v - bp);
+    s = t;
+}
+template <typename R>
+__device__ __forceinline__ double2 chunk_sum(const C2<R>* sp, int chunks, int nk, int k);
+template <>
+__device__ __forceinline__ double2 chunk_sum<float>(const C2<float>* sp, int chunks, int nk, int k) {
+    float rs = 0.f, rc = 0.f, is = 0.f, ic = 0.f;
+    for (int c = 0; c < chunks; ++c) {
+        const C2<float> v = sp[(long long)c * nk + k];
+        add_c(v.re, rs, rc);
+        add_c(v.im, is, ic);
+    }
+    return make_double2((double)rs + (double)rc, (double)is + (double)ic);
+}
+template <>
+__device__ __forceinline__ double2 chunk_sum<double>(const C2<double>* sp, int chunks, int nk, int k) {
+    double re = 0.0, im = 0.0;
+    for (int c = 0; c < chunks; ++c) {
+        const C2<double> v = sp[(long long)c * nk + k];
+        re += v.re;
+        im += v.im;
+    }
+    return make_double2(re, im);
+}
+
 template <typename R>
 __global__ void ew_sreduce(EwArgs A) {
-    __shared__ double se[256];
+    __shared__ Fx128 se[8], sq1[8], sq2[8];
     if (A.skip && *A.skip) return;
     const int k = blockIdx.x * blockDim.x + threadIdx.x;
     double e = 0.0;
     if (k < A.nk) {
-        double re = 0.0, im = 0.0;
-        const C2<R>* sp = (const C2<R>*)A.Spart;
-        for (int c = 0; c < A.chunks; ++c) {
-            const C2<R> v = sp[(long long)c * A.nk + k];
-            re += (double)v.re;
-            im += (double)v.im;
-        }
-        A.S[k] = make_double2(re, im);
+        const double2 S = chunk_sum<R>((const C2<R>*)A.Spart, A.chunks, A.nk, k);
+        A.S[k] = S;
         const double ck = A.kvec64[k].w;
-        ((C2<R>*)A.wS)[k] = C2<R>{(R)(ck * re), (R)(ck * im)};
-        e = ck * (re * re + im * im);
+        ((C2<R>*)A.wS)[k] = C2<R>{(R)(ck * S.x), (R)(ck * S.y)};
+        e = ck * (S.x * S.x + S.y * S.y);
     }
-    se[threadIdx.x] = e;
+    // block sum of c_k |S_k|^2, exact in fixed point
+    Fx128 acc = fx_warp_sum(fx_from_double(e));
+    if ((threadIdx.x & 31) == 0) se[threadIdx.x >> 5] = acc;
+    // block 0: sum q and sum q^2 over the prep blocks
+    Fx128 a1 = fx_zero(), a2 = fx_zero();
+    if (blockIdx.x == 0) {
+        for (int b = threadIdx.x; b < A.prep_blocks; b += blockDim.x) {
+            a1 = fx_add(a1, fx_from_double(A.qpart[2 * b]));
+            a2 = fx_add(a2, fx_from_double(A.qpart[2 * b + 1]));
+        }
+        a1 = fx_warp_sum(a1);
+        a2 = fx_warp_sum(a2);
+        if ((threadIdx.x & 31) == 0) {
+            sq1[threadIdx.x >> 5] = a1;
+            sq2[threadIdx.x >> 5] = a2;
+        }
+    }
     __syncthreads();
-    if (threadIdx.x == 0) {
-        double s = 0;
-        for (int t = 0; t < (int)blockDim.x; ++t) s += se[t];
-        double* p = A.partial_k + 8 * blockIdx.x;
-        p[0] = s * A.inv_eps_2v;
-        for (int c = 1; c < 7; ++c) p[c] = 0.0;
+    if (threadIdx.x < 32) {
+        const int nw = blockDim.x >> 5;
+        acc = fx_warp_sum(threadIdx.x < nw ? se[threadIdx.x] : fx_zero());
         if (blockIdx.x == 0) {
-            // sum q, sum q^2 in block order; self and background energies
-            // (Potentials.f90:1643-1646)
-            double q1 = 0, q2 = 0;
-            for (int b = 0; b < A.prep_blocks; ++b) {
-                q1 += A.qpart[2 * b];
-                q2 += A.qpart[2 * b + 1];
+            a1 = fx_warp_sum(threadIdx.x < nw ? sq1[threadIdx.x] : fx_zero());
+            a2 = fx_warp_sum(threadIdx.x < nw ? sq2[threadIdx.x] : fx_zero());
+        }
+        if (threadIdx.x == 0) {
+            double* p = A.partial_k + 8 * blockIdx.x;
+            p[0] = fx_to_double(acc) * A.inv_eps_2v;
+            for (int c = 1; c < 7; ++c) p[c] = 0.0;
+            if (blockIdx.x == 0) {
+                // self and background energies (Potentials.f90:1643-1646)
+                const double q1 = fx_to_double(a1), q2 = fx_to_double(a2);
+                A.Ssum[0] = q1;
+                A.Ssum[1] = q2;
+                double* ps = A.partial_k + 8 * gridDim.x;
+                ps[0] = -(q2 * A.inv_eps_4pi * A.inv_sigma_sqrt_2pi) - q1 * q1 * 0.5 * A.inv_eps_2v * A.sigma2;
+                for (int c = 1; c < 7; ++c) ps[c] = 0.0;
             }
-            A.Ssum[0] = q1;
-            A.Ssum[1] = q2;
-            double* ps = A.partial_k + 8 * gridDim.x;
-            ps[0] = -(q2 * A.inv_eps_4pi * A.inv_sigma_sqrt_2pi) - q1 * q1 * 0.5 * A.inv_eps_2v * A.sigma2;
-            for (int c = 1; c < 7; ++c) ps[c] = 0.0;
         }
     }
 }
@@ -359,13 +406,20 @@ __global__ void ew_finish(EwArgs A) {
             else A.out_chi[i] += x;
         }
     }
-    for (int c = 0; c < 6; ++c) sw[threadIdx.x][c] = w[c];
+    // block sums of the six stress components: shuffle trees
+    const int wl = threadIdx.x & 31, wid = threadIdx.x >> 5;
+    for (int c = 0; c < 6; ++c) {
+        const double v = group_sum<32>(w[c]);
+        if (wl == 0) sw[wid][c] = v;
+    }
     __syncthreads();
-    if (threadIdx.x < 6) {
-        double s = 0;
-        for (int t = 0; t < (int)blockDim.x; ++t) s += sw[t][threadIdx.x];
+    if (threadIdx.x < 32) {
+        const int nw = blockDim.x >> 5;
         double* p = A.partial_w + 8 * blockIdx.x;
-        p[1 + threadIdx.x] = s;
+        for (int c = 0; c < 6; ++c) {
+            const double v = group_sum<32>(threadIdx.x < nw ? sw[threadIdx.x][c] : 0.0);
+            if (threadIdx.x == 0) p[1 + c] = v;
+        }
         if (threadIdx.x == 0) p[0] = 0.0;
     }
 }

@@ -173,10 +173,21 @@ __device__ __forceinline__ T group_sum(T v) {
     return v;
 }
 
-// Compensated group sum of FP32 values (Knuth two-sum at every step); the
-// FP64 result carries the rounding errors the FP32 additions made.
+// Compensated sum over a group of G lanes: FP32 partials are combined with a
+// two-sum at every step, and the (sum, error) pair is widened to FP64 once.
+// The value is the same in every lane; call .d() in the lane that stores it so
+// that only one lane per atom touches the FP64 pipe.
+struct CSum {
+    float s, c;
+    __device__ __forceinline__ double d() const { return (double)s + (double)c; }
+};
+struct DSum {
+    double s;
+    __device__ __forceinline__ double d() const { return s; }
+};
+
 template <int G>
-__device__ __forceinline__ double group_sum_c(float v) {
+__device__ __forceinline__ CSum group_sum_c(float v) {
     float s = v, c = 0.0f;
 #pragma unroll
     for (int o = G / 2; o > 0; o >>= 1) {
@@ -188,11 +199,11 @@ __device__ __forceinline__ double group_sum_c(float v) {
         s = t;
         c = c + co + err;
     }
-    return (double)s + (double)c;
+    return CSum{s, c};
 }
 template <int G>
-__device__ __forceinline__ double group_sum_c(double v) {
-    return group_sum<G>(v);
+__device__ __forceinline__ DSum group_sum_c(double v) {
+    return DSum{group_sum<G>(v)};
 }
 
 }  // namespace pg

@@ -454,6 +454,11 @@ __global__ void short_sep0(int n, const double* __restrict__ pos, CellK C, const
     }
 }
 
+__global__ void entry_types(int m, const int* __restrict__ idx, const int* __restrict__ type, int* __restrict__ out) {
+    int e = blockIdx.x * blockDim.x + threadIdx.x;
+    if (e < m) out[e] = type[idx[e]];
+}
+
 __global__ void short_reverse(int n, const int* __restrict__ start, const int* __restrict__ idx,
                               const int* __restrict__ off, int* __restrict__ rev, int* __restrict__ cnt) {
     int a = blockIdx.x * blockDim.x + threadIdx.x;
@@ -695,6 +700,7 @@ void build_neighbor_lists(pg_context* ctx, const double* h_cutoffs) {
     }
     PG_CUDA(cudaStreamSynchronize(st));
     ctx->have_list = true;
+    ctx->list_epoch++;
     ctx->state_epoch++;
     ctx->short_dirty = true;
 }
@@ -748,6 +754,7 @@ void build_allpairs_lists(pg_context* ctx, const double* h_cutoffs) {
     }
     PG_CUDA(cudaStreamSynchronize(st));
     ctx->have_list = true;
+    ctx->list_epoch++;
     ctx->state_epoch++;
     ctx->short_dirty = true;
 }
@@ -771,8 +778,28 @@ void install_neighbor_lists(pg_context* ctx, const int32_t* counts, const int32_
     PG_CUDA(cudaStreamSynchronize(ctx->stream));
     ctx->nb_total = total;
     ctx->have_list = true;
+    ctx->list_epoch++;
     ctx->state_epoch++;
     ctx->short_dirty = true;
+}
+
+// Start a list generation: remember the positions and take the full list's
+// bond vectors there (used by the mixed-precision pair kernel).
+void build_full_sep0(pg_context* ctx) {
+    const int n = ctx->n;
+    cudaStream_t st = ctx->stream;
+    CellK C = cell_kernel_view(ctx->cell);
+    ctx->pos0.resize(3 * (size_t)std::max(n, 1));
+    ctx->nb_sep0.resize((size_t)std::max<long long>(ctx->nb_total, 1));
+    if (n > 0) {
+        PG_CUDA(cudaMemcpyAsync(ctx->pos0.p, ctx->pos.p, sizeof(double) * 3 * n, cudaMemcpyDeviceToDevice, st));
+        short_sep0<<<blocks(n, 128), 128, 0, st>>>(n, ctx->pos0.p, C, ctx->nb_start.p, ctx->nb_idx.p, ctx->nb_off.p,
+                                                  ctx->nb_sep0.p);
+        PG_CHECK_LAUNCH();
+    }
+    ctx->sep0_epoch = ctx->list_epoch;
+    ctx->short_dirty = true;
+    ctx->state_epoch++;
 }
 
 void build_short_list(pg_context* ctx) {
@@ -780,10 +807,11 @@ void build_short_list(pg_context* ctx) {
     cudaStream_t st = ctx->stream;
     const double r = ctx->bo_radius + ctx->skin;
     CellK C = cell_kernel_view(ctx->cell);
+    const double* p0 = ctx->pos0.p;  // positions of this list generation
     ctx->sh_count.resize(std::max(n, 1));
     ctx->sh_start.resize(n + 1);
     if (n > 0) {
-        short_count<<<blocks(n, 128), 128, 0, st>>>(n, ctx->pos.p, C, ctx->nb_start.p, ctx->nb_idx.p, ctx->nb_off.p,
+        short_count<<<blocks(n, 128), 128, 0, st>>>(n, p0, C, ctx->nb_start.p, ctx->nb_idx.p, ctx->nb_off.p,
                                                    r * r, ctx->sh_count.p);
         PG_CHECK_LAUNCH();
     }
@@ -794,21 +822,23 @@ void build_short_list(pg_context* ctx) {
     ctx->sh_off.resize(3 * (size_t)std::max(total, 1));
     ctx->sh_rev.resize(std::max(total, 1));
     if (n > 0) {
-        short_fill<<<blocks(n, 128), 128, 0, st>>>(n, ctx->pos.p, C, ctx->nb_start.p, ctx->nb_idx.p, ctx->nb_off.p,
+        short_fill<<<blocks(n, 128), 128, 0, st>>>(n, p0, C, ctx->nb_start.p, ctx->nb_idx.p, ctx->nb_off.p,
                                                   r * r, ctx->sh_start.p, ctx->sh_idx.p, ctx->sh_off.p);
         PG_CHECK_LAUNCH();
         short_reverse<<<blocks(n, 128), 128, 0, st>>>(n, ctx->sh_start.p, ctx->sh_idx.p, ctx->sh_off.p, ctx->sh_rev.p,
                                                      ctx->sh_count.p);
         PG_CHECK_LAUNCH();
     }
-    // bond vectors and positions of this build, for the mixed-precision kernels
+    // bond vectors of this list generation and partner types
     ctx->sh_sep0.resize(std::max(total, 1));
-    ctx->sh_pos0.resize(3 * (size_t)std::max(n, 1));
+    ctx->sh_type.resize(std::max(total, 1));
     if (n > 0) {
-        short_sep0<<<blocks(n, 128), 128, 0, st>>>(n, ctx->pos.p, C, ctx->sh_start.p, ctx->sh_idx.p, ctx->sh_off.p,
+        short_sep0<<<blocks(n, 128), 128, 0, st>>>(n, p0, C, ctx->sh_start.p, ctx->sh_idx.p, ctx->sh_off.p,
                                                   ctx->sh_sep0.p);
         PG_CHECK_LAUNCH();
-        PG_CUDA(cudaMemcpyAsync(ctx->sh_pos0.p, ctx->pos.p, sizeof(double) * 3 * n, cudaMemcpyDeviceToDevice, st));
+        entry_types<<<blocks(std::max(total, 1), 256), 256, 0, st>>>(total, ctx->sh_idx.p, ctx->type.p,
+                                                                    ctx->sh_type.p);
+        PG_CHECK_LAUNCH();
     }
     // triplet block bases: exclusive scan of n_i^2
     ctx->sh_tri.resize(n + 1);

@@ -37,7 +37,34 @@ struct PairArgs {
     double* out_chi;
     double* partial;  // per block: energy, virial[6], pad
     const int* skip;  // optional device flag: nonzero = do nothing
+    const F4* sep0;   // mixed path: bond vectors at list build
+    const F4* disp;   // mixed path: displacements since the build
 };
+
+// bond vector of entry e of atom i: FP64 from the positions, or (mixed path)
+// build-time vector plus the FP32 displacements of both atoms
+template <typename R>
+__device__ __forceinline__ void pair_vector(const PairArgs& A, int i, int e, double xi, double yi, double zi, R& x,
+                                            R& y, R& z);
+template <>
+__device__ __forceinline__ void pair_vector<double>(const PairArgs& A, int i, int e, double xi, double yi, double zi,
+                                                    double& x, double& y, double& z) {
+    const int j = A.idx[e];
+    const double o0 = A.off[3 * e], o1 = A.off[3 * e + 1], o2 = A.off[3 * e + 2];
+    // separation_vector (Geometry.f90:449-466)
+    x = A.pos[3 * j] - xi + (o0 * A.C.vc[0][0] + o1 * A.C.vc[0][1] + o2 * A.C.vc[0][2]);
+    y = A.pos[3 * j + 1] - yi + (o0 * A.C.vc[1][0] + o1 * A.C.vc[1][1] + o2 * A.C.vc[1][2]);
+    z = A.pos[3 * j + 2] - zi + (o0 * A.C.vc[2][0] + o1 * A.C.vc[2][1] + o2 * A.C.vc[2][2]);
+}
+template <>
+__device__ __forceinline__ void pair_vector<float>(const PairArgs& A, int i, int e, double, double, double, float& x,
+                                                   float& y, float& z) {
+    const int j = A.idx[e];
+    const F4 s0 = A.sep0[e], dj = A.disp[j], di = A.disp[i];
+    x = s0.x + (dj.x - di.x);
+    y = s0.y + (dj.y - di.y);
+    z = s0.z + (dj.z - di.z);
+}
 
 __device__ __forceinline__ double powi_(double x, int n) {
     double r = 1.0;
@@ -65,13 +92,8 @@ __global__ void __launch_bounds__(256) pair_kernel(PairArgs A) {
         const int e1 = A.start[i + 1];
         for (int e = A.start[i] + lane; e < e1; e += G) {
             const int j = A.idx[e];
-            const double o0 = A.off[3 * e], o1 = A.off[3 * e + 1], o2 = A.off[3 * e + 2];
-            // separation_vector (Geometry.f90:449-466) in FP64
-            double sx = A.pos[3 * j] - xi, sy = A.pos[3 * j + 1] - yi, sz = A.pos[3 * j + 2] - zi;
-            sx += o0 * A.C.vc[0][0] + o1 * A.C.vc[0][1] + o2 * A.C.vc[0][2];
-            sy += o0 * A.C.vc[1][0] + o1 * A.C.vc[1][1] + o2 * A.C.vc[1][2];
-            sz += o0 * A.C.vc[2][0] + o1 * A.C.vc[2][1] + o2 * A.C.vc[2][2];
-            const R x = (R)sx, y = (R)sy, z = (R)sz;
+            R x, y, z;
+            pair_vector<R>(A, i, e, xi, yi, zi, x, y, z);
             const R r = sqrt_(x * x + y * y + z * z);
             if (r == R(0)) continue;
             const R ir = R(1) / r;
@@ -110,10 +132,13 @@ __global__ void __launch_bounds__(256) pair_kernel(PairArgs A) {
             w5 += h * x * y;
         }
     }
-    double d[11] = {(double)fx, (double)fy, (double)fz, (double)en, (double)chi, (double)w0, (double)w1,
-                    (double)w2,  (double)w3, (double)w4, (double)w5};
+    const R lanev[11] = {fx, fy, fz, en, chi, w0, w1, w2, w3, w4, w5};
+    double d[11];
 #pragma unroll
-    for (int q = 0; q < 11; ++q) d[q] = group_sum<G>(d[q]);
+    for (int q = 0; q < 11; ++q) {
+        const auto sq = group_sum_c<G>(lanev[q]);
+        d[q] = lane == 0 ? sq.d() : 0.0;
+    }
     if (act && lane == 0) {
         // single-atom terms (charge_self: epsilon q^n, chi = -epsilon n q^(n-1); Potentials.f90:4341-4375)
         const int2 sx = A.sindex[ti];
@@ -143,15 +168,33 @@ __global__ void __launch_bounds__(256) pair_kernel(PairArgs A) {
         for (int q = 0; q < 6; ++q) red[slot][1 + q] = act ? d[5 + q] : 0.0;
     }
     __syncthreads();
-    if (threadIdx.x < 7) {
-        double s = 0;
-        for (int k = 0; k < (int)(blockDim.x / G); ++k) s += red[k][threadIdx.x];
-        A.partial[8 * blockIdx.x + threadIdx.x] = s;
+    const int nslot = blockDim.x / G;
+    const int wid = threadIdx.x >> 5, wl = threadIdx.x & 31;
+    const int nw = (blockDim.x + 31) >> 5;
+    for (int c = wid; c < 7; c += nw) {
+        double v = 0.0;
+        for (int k = wl; k < nslot; k += 32) v += red[k][c];
+        v = group_sum<32>(v);
+        if (wl == 0) A.partial[8 * blockIdx.x + c] = v;
     }
     (void)wantE;
 }
 
-int pair_kernel_blocks(int n, int G) { return (n + (256 / G) - 1) / (256 / G); }
+// atoms per block: enough blocks to cover every SM twice, at most 256 threads
+int pair_atoms_per_block(int n, int G) {
+    const int maxa = 256 / G;
+    int a = (n + 2 * 152 - 1) / (2 * 152);
+    if (a < 1) a = 1;
+    if (a > maxa) a = maxa;
+    const int warp_atoms = 32 / G > 0 ? 32 / G : 1;  // whole warps
+    a = ((a + warp_atoms - 1) / warp_atoms) * warp_atoms;
+    return a > maxa ? maxa : a;
+}
+
+int pair_kernel_blocks(int n, int G) {
+    const int a = pair_atoms_per_block(n, G);
+    return (n + a - 1) / a;
+}
 
 void launch_pair_kernel_skip(pg_context* ctx, int precision, int flags, bool first_f, bool first_chi, int G,
                              double* partial, const int* skip) {
@@ -186,8 +229,11 @@ void launch_pair_kernel_skip(pg_context* ctx, int precision, int flags, bool fir
     A.out_chi = ctx->out_chi.p;
     A.partial = partial;
     const int nbk = pair_kernel_blocks(ctx->n, G);
+    const int threads = pair_atoms_per_block(ctx->n, G) * G;
+    A.sep0 = ctx->nb_sep0.p;
+    A.disp = ctx->disp32.p;
     cudaStream_t st = ctx->stream;
-#define PG_PAIR_LAUNCH(R_, G_) pair_kernel<R_, G_><<<nbk, 256, 0, st>>>(A)
+#define PG_PAIR_LAUNCH(R_, G_) pair_kernel<R_, G_><<<nbk, threads, 0, st>>>(A)
     if (precision == PG_PREC_FP64) {
         if (G == 8) PG_PAIR_LAUNCH(double, 8);
         else if (G == 16) PG_PAIR_LAUNCH(double, 16);

@@ -150,15 +150,15 @@ static void enqueue_chi(pg_context* ctx, int precision, const int* skip) {
 void relax_charges(pg_context* ctx, int precision, int n_steps, double dt, double inertia, double friction,
                    double tolerance, double* rates, double* charges, int* steps, double* error, double* max_dq) {
     require(ctx->have_list && ctx->have_atoms, PG_ERR_NOT_READY, "set atoms, potentials and lists first");
-    if (ctx->tables_dirty) fold_tables(ctx);
-    if (ctx->ewald) ewald_prepare(ctx);
+    prepare(ctx);
     const int n = ctx->n;
     cudaStream_t st = ctx->stream;
     const int nb = std::max(1, (n + RT - 1) / RT);
     ctx->out_chi.resize((size_t)std::max(n, 1));
     ctx->out_f.resize(3 * (size_t)std::max(n, 1));
     const int G = pair_lanes_for(ctx);
-    const int slots = (n + (256 / G) - 1) / (256 / G) + (ctx->ewald ? ewald_partial_slots(ctx) : 0) + 1;
+    // the pair kernel and the k-space passes both write their partials from slot 0
+    const int slots = std::max(pair_kernel_blocks(n, G), ctx->ewald ? ewald_partial_slots(ctx) : 0) + 1;
     ctx->red_part.resize(8 * (size_t)slots);
     ctx->rq_rate.upload(rates, (size_t)n, st);
     ctx->rq_force.resize((size_t)std::max(n, 1));
@@ -181,6 +181,8 @@ void relax_charges(pg_context* ctx, int precision, int n_steps, double dt, doubl
     A.part = ctx->rq_stat.p + 4;
     A.nblocks = nb;
     ctx->launches = 0;
+    // positions stay fixed during the relaxation: displacements once
+    if (precision == PG_PREC_MIXED) launch_disp(ctx, nullptr);
     // initial differences (relaxation.py:433)
     enqueue_chi(ctx, precision, A.flag);
     rx_block_sums<<<nb, RT, 0, st>>>(A);

@@ -64,6 +64,7 @@ struct BondArgs {
     const void* trip;   // TripT<R>
     const void* post;   // PostT<R>
     const void* maxbr;  // R
+    const int* etype;   // per entry: partner type
     const F4* sep0;     // mixed path: bond vectors at list build
     const F4* disp;     // mixed path: per-atom displacement since the build
     int flags;
@@ -78,8 +79,10 @@ struct BondArgs {
 };
 
 // per-atom displacement since the short-list build, FP64 difference rounded to FP32
-__global__ void disp_pass(int n, const double* __restrict__ pos, const double* __restrict__ pos0, F4* __restrict__ d) {
+__global__ void disp_pass(int n, const double* __restrict__ pos, const double* __restrict__ pos0, F4* __restrict__ d,
+                          const int* skip) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (skip && *skip) return;
     if (i >= n) return;
     d[i] = F4{(float)(pos[3 * i] - pos0[3 * i]), (float)(pos[3 * i + 1] - pos0[3 * i + 1]),
               (float)(pos[3 * i + 2] - pos0[3 * i + 2]), 0.0f};
@@ -109,24 +112,42 @@ __device__ __forceinline__ F4 bond_vector<float>(const BondArgs& A, int i, int e
     return F4{x, y, z, sqrtf(x * x + y * y + z * z)};
 }
 
+constexpr int CAP = 32;  // bonds per atom staged in shared memory
+
 template <typename R, int G>
 __global__ void __launch_bounds__(128) bond_pass(BondArgs A) {
     using V4 = typename Vec4T<R>::T;
-    __shared__ double red[128 / G][8];
-    V4* geo = (V4*)A.geo;
-    V4* fj = (V4*)A.fj;
-    V4* fk = (V4*)A.fk;
+    constexpr int AP = 128 / G;  // atoms per block
+    __shared__ V4 sgeo[AP * CAP];
+    __shared__ int styp[AP * CAP];
+    __shared__ TripT<R> strip[64];
+    __shared__ double red[AP][8];
     const PairT<R>* terms = (const PairT<R>*)A.terms;
+    const int T3 = A.T * A.T * A.T;
+    const TripT<R>* trip = (const TripT<R>*)A.trip;
+    if (T3 <= 64) {
+        for (int q = threadIdx.x; q < T3; q += blockDim.x) strip[q] = trip[q];
+        trip = strip;
+    }
+    __syncthreads();
     const int lane = threadIdx.x % G;
     const int slot = threadIdx.x / G;
-    const int i = blockIdx.x * (blockDim.x / G) + slot;
+    const int i = blockIdx.x * AP + slot;
     const bool act = i < A.n;
     const int s = act ? A.start[i] : 0;
     const int ni = act ? A.start[i + 1] - s : 0;
+    const bool staged = ni <= CAP;
+    V4* geo = staged ? sgeo + slot * CAP : (V4*)A.geo + s;
+    const int* typ = staged ? styp + slot * CAP : A.etype + s;
+    V4* fj = (V4*)A.fj;
+    V4* fk = (V4*)A.fk;
     // geometry of i's bonds in the working precision
     if (act) {
         const double xi = A.pos[3 * i], yi = A.pos[3 * i + 1], zi = A.pos[3 * i + 2];
-        for (int e = lane; e < ni; e += G) geo[s + e] = bond_vector<R>(A, i, s + e, xi, yi, zi);
+        for (int e = lane; e < ni; e += G) {
+            geo[e] = bond_vector<R>(A, i, s + e, xi, yi, zi);
+            if (staged) styp[slot * CAP + e] = A.etype[s + e];
+        }
     }
     __syncwarp();
     R Fx = 0, Fy = 0, Fz = 0, En = 0;
@@ -137,10 +158,10 @@ __global__ void __launch_bounds__(128) bond_pass(BondArgs A) {
         const PostT<R> pp = ((const PostT<R>*)A.post)[ti];
         const long long tri = A.tri[i];
         for (int e = lane; e < ni; e += G) {
-            const V4 gij = geo[s + e];
+            const V4 gij = geo[e];
             const V3<R> a{gij.x, gij.y, gij.z};
             const R r = gij.w;
-            const int tj = A.type[A.idx[s + e]];
+            const int tj = typ[e];
             const int2 ix = A.index[ti * A.T + tj];
             bool any = false, bo = false;
             for (int t = ix.x; t < ix.x + ix.y; ++t) {
@@ -152,15 +173,15 @@ __global__ void __launch_bounds__(128) bond_pass(BondArgs A) {
             }
             R fjx = 0, fjy = 0, fjz = 0;
             V4* row = fk + tri + (long long)e * ni;
-            const TripT<R>* trow = (const TripT<R>*)A.trip + ((long long)ti * A.T + tj) * A.T;
+            const TripT<R>* trow = trip + (ti * A.T + tj) * A.T;
             // zeta_ij (core_calculate_pair_bond_order_factor, first neighbour loop)
             R zeta = 0, B = 1, dB = 0;
             if ((bo || A.zeta_out) && r != R(0)) {
                 for (int k = 0; k < ni; ++k) {
                     if (k == e) continue;
-                    const V4 gik = geo[s + k];
+                    const V4 gik = geo[k];
                     if (!(gik.w < maxbr)) continue;
-                    const TripT<R>& TT = trow[A.type[A.idx[s + k]]];
+                    const TripT<R>& TT = trow[typ[k]];
                     if (!TT.valid) continue;
                     zeta += tersoff_term<R>(TT, a, r, V3<R>{gik.x, gik.y, gik.z}, gik.w);
                 }
@@ -215,9 +236,9 @@ __global__ void __launch_bounds__(128) bond_pass(BondArgs A) {
                 if (k == e) continue;
                 V4 out{0, 0, 0, 0};
                 if (bo && pref != R(0)) {
-                    const V4 gik = geo[s + k];
+                    const V4 gik = geo[k];
                     if (gik.w < maxbr) {
-                        const TripT<R>& TT = trow[A.type[A.idx[s + k]]];
+                        const TripT<R>& TT = trow[typ[k]];
                         if (TT.valid) {
                             V3<R> gj, gk;
                             const V3<R> b{gik.x, gik.y, gik.z};
@@ -246,29 +267,34 @@ __global__ void __launch_bounds__(128) bond_pass(BondArgs A) {
             fj[s + e] = V4{fjx, fjy, fjz, 0};
         }
     }
-    const double d0 = group_sum_c<G>(Fx), d1 = group_sum_c<G>(Fy), d2 = group_sum_c<G>(Fz);
-    const double de = group_sum_c<G>(En);
-    const double w0 = group_sum_c<G>(W0), w1 = group_sum_c<G>(W1), w2 = group_sum_c<G>(W2);
-    const double w3 = group_sum_c<G>(W3), w4 = group_sum_c<G>(W4), w5 = group_sum_c<G>(W5);
-    if (act && lane == 0) {
-        A.fc[3 * i] = d0;
-        A.fc[3 * i + 1] = d1;
-        A.fc[3 * i + 2] = d2;
-    }
+    const auto d0 = group_sum_c<G>(Fx), d1 = group_sum_c<G>(Fy), d2 = group_sum_c<G>(Fz);
+    const auto de = group_sum_c<G>(En);
+    const auto w0 = group_sum_c<G>(W0), w1 = group_sum_c<G>(W1), w2 = group_sum_c<G>(W2);
+    const auto w3 = group_sum_c<G>(W3), w4 = group_sum_c<G>(W4), w5 = group_sum_c<G>(W5);
     if (lane == 0) {
-        red[slot][0] = act ? de : 0.0;
-        red[slot][1] = act ? w0 : 0.0;
-        red[slot][2] = act ? w1 : 0.0;
-        red[slot][3] = act ? w2 : 0.0;
-        red[slot][4] = act ? w3 : 0.0;
-        red[slot][5] = act ? w4 : 0.0;
-        red[slot][6] = act ? w5 : 0.0;
+        if (act) {
+            A.fc[3 * i] = d0.d();
+            A.fc[3 * i + 1] = d1.d();
+            A.fc[3 * i + 2] = d2.d();
+        }
+        red[slot][0] = act ? de.d() : 0.0;
+        red[slot][1] = act ? w0.d() : 0.0;
+        red[slot][2] = act ? w1.d() : 0.0;
+        red[slot][3] = act ? w2.d() : 0.0;
+        red[slot][4] = act ? w3.d() : 0.0;
+        red[slot][5] = act ? w4.d() : 0.0;
+        red[slot][6] = act ? w5.d() : 0.0;
     }
     __syncthreads();
-    if (A.partial && threadIdx.x < 7) {
-        double sum = 0;
-        for (int k = 0; k < (int)(blockDim.x / G); ++k) sum += red[k][threadIdx.x];
-        A.partial[8 * blockIdx.x + threadIdx.x] = sum;
+    // block partials: one warp per component, shuffle tree over the block's atoms
+    const int wid = threadIdx.x >> 5, wl = threadIdx.x & 31;
+    if (A.partial && wid < 4) {
+        for (int c = wid; c < 7; c += 4) {
+            double v = 0.0;
+            for (int k = wl; k < AP; k += 32) v += red[k][c];
+            v = group_sum<32>(v);
+            if (wl == 0) A.partial[8 * blockIdx.x + c] = v;
+        }
     }
 }
 
@@ -303,11 +329,11 @@ __global__ void __launch_bounds__(128) gather_pass(BondArgs A) {
             }
         }
     }
-    double fx = group_sum_c<G>(Fx), fy = group_sum_c<G>(Fy), fz = group_sum_c<G>(Fz);
+    const auto sx = group_sum_c<G>(Fx), sy = group_sum_c<G>(Fy), sz = group_sum_c<G>(Fz);
     if (act && lane == 0) {
-        fx += A.fc[3 * m];
-        fy += A.fc[3 * m + 1];
-        fz += A.fc[3 * m + 2];
+        const double fx = sx.d() + A.fc[3 * m];
+        const double fy = sy.d() + A.fc[3 * m + 1];
+        const double fz = sz.d() + A.fc[3 * m + 2];
         if (A.first_f) {
             A.out_f[3 * m] = fx;
             A.out_f[3 * m + 1] = fy;
@@ -331,7 +357,6 @@ static void prepare_scratch(pg_context* ctx, int precision) {
     } else {
         ctx->bo_fj.resize(2 * ne);
         ctx->bo_fk.resize(nt);
-        ctx->disp32.resize((size_t)std::max(ctx->n, 1));
     }
     ctx->bo_fc.resize(3 * (size_t)std::max(ctx->n, 1));
 }
@@ -348,6 +373,7 @@ static BondArgs bond_args(pg_context* ctx, int precision, int flags, bool first_
     A.off = ctx->sh_off.p;
     A.rev = ctx->sh_rev.p;
     A.tri = ctx->sh_tri.p;
+    A.etype = ctx->sh_type.p;
     A.index = ctx->d_pair_index.p;
     A.flags = flags;
     A.first_f = first_f;
@@ -402,16 +428,18 @@ int launch_bond_order_impl(pg_context* ctx, int precision, int flags, bool first
     prepare_scratch(ctx, precision);
     BondArgs A = bond_args(ctx, precision, flags, first_f, partial);
     const bool forces = (flags & PG_WANT_FORCES) != 0;
-    if (precision == PG_PREC_FP64) {
-        launch_by_lanes<double>(A, ctx->n, ctx->stream, G, forces, between);
-    } else {
-        disp_pass<<<(ctx->n + 255) / 256, 256, 0, ctx->stream>>>(ctx->n, ctx->pos.p, ctx->sh_pos0.p, ctx->disp32.p);
-        ctx->launches++;
-        launch_by_lanes<float>(A, ctx->n, ctx->stream, G, forces, between);
-    }
+    if (precision == PG_PREC_FP64) launch_by_lanes<double>(A, ctx->n, ctx->stream, G, forces, between);
+    else launch_by_lanes<float>(A, ctx->n, ctx->stream, G, forces, between);
     PG_CHECK_LAUNCH();
     ctx->launches += forces ? 2 : 1;
     return bond_blocks(ctx->n, G);
+}
+
+void launch_disp(pg_context* ctx, const int* skip) {
+    ctx->disp32.resize((size_t)std::max(ctx->n, 1));
+    disp_pass<<<(ctx->n + 255) / 256, 256, 0, ctx->stream>>>(ctx->n, ctx->pos.p, ctx->pos0.p, ctx->disp32.p, skip);
+    PG_CHECK_LAUNCH();
+    ctx->launches++;
 }
 
 void bond_zeta_diag(pg_context* ctx) {
