@@ -92,47 +92,40 @@ static void enqueue(pg_context* ctx, int precision, int flags, int G) {
     const bool wantF = flags & PG_WANT_FORCES, wantC = flags & PG_WANT_ENEGS, wantE = flags & PG_WANT_ENERGY;
     ctx->out_f.resize(3 * (size_t)std::max(n, 1));
     ctx->out_chi.resize((size_t)std::max(n, 1));
-    ctx->out_tot.resize(8);
+    ctx->out_acc.resize(8);
     const bool run_pair = ctx->have_pair_kernel_terms || ctx->ewald || ctx->have_singles;
     const bool run_bond = ctx->have_bond_terms && (wantE || wantF);
     const int Gp = pair_lanes_for(ctx);
-    int slots = 0;
-    if (run_pair) slots += pair_kernel_blocks(n, Gp);
-    if (run_bond) slots += bond_blocks(n, G);
-    if (ctx->ewald) slots += ewald_partial_slots(ctx);
-    ctx->red_part.resize(8 * (size_t)std::max(slots, 1));
+    Fx128* acc = ctx->out_acc.p;
     bool first_f = true, first_chi = true;
-    int used = 0;
     auto mark = [&](int k) {
         if (ctx->timing) PG_CUDA(cudaEventRecord(ctx->tev[k], ctx->stream));
     };
     mark(0);
+    // the totals are integers that every kernel adds to: clear them first
+    PG_CUDA(cudaMemsetAsync(acc, 0, sizeof(Fx128) * 8, ctx->stream));
     if (precision == PG_PREC_MIXED && (run_pair || run_bond)) launch_disp(ctx, nullptr);
     if (run_pair) {
-        launch_pair_kernel_impl(ctx, precision, flags, first_f, first_chi, Gp, ctx->red_part.p + 8 * used);
-        used += pair_kernel_blocks(n, Gp);
+        launch_pair_kernel_impl(ctx, precision, flags, first_f, first_chi, Gp, acc);
         if (wantF) first_f = false;
         if (wantC) first_chi = false;
     }
     mark(1);
     if (run_bond) {
-        used += launch_bond_order_impl(ctx, precision, flags, first_f, G, ctx->red_part.p + 8 * used, [&] { mark(2); });
+        launch_bond_order_impl(ctx, precision, flags, first_f, G, acc, [&] { mark(2); });
         if (wantF) first_f = false;
     } else {
         mark(2);
     }
     mark(3);
     if (ctx->ewald) {
-        launch_ewald_kspace(ctx, precision, flags, first_f, first_chi, ctx->red_part.p + 8 * used);
-        used += ewald_partial_slots(ctx);
+        launch_ewald_kspace(ctx, precision, flags, first_f, first_chi, acc);
         if (wantF) first_f = false;
         if (wantC) first_chi = false;
     }
     mark(4);
     if (wantF && first_f) PG_CUDA(cudaMemsetAsync(ctx->out_f.p, 0, sizeof(double) * 3 * n, ctx->stream));
     if (wantC && first_chi) PG_CUDA(cudaMemsetAsync(ctx->out_chi.p, 0, sizeof(double) * n, ctx->stream));
-    if (used > 0) launch_final_reduce(ctx, used);
-    else PG_CUDA(cudaMemsetAsync(ctx->out_tot.p, 0, sizeof(double) * 8, ctx->stream));
     mark(5);
 }
 
@@ -219,12 +212,14 @@ void evaluate(pg_context* ctx, int precision, int flags) {
 }
 
 static void copy_results(pg_context* ctx, int flags, double* energy, double* forces, double* stress, double* enegs) {
+    Fx128 acc[8] = {};
     double tot[8] = {0};
     cudaStream_t st = ctx->stream;
-    if (energy || stress) PG_CUDA(cudaMemcpyAsync(tot, ctx->out_tot.p, sizeof(tot), cudaMemcpyDeviceToHost, st));
+    if (energy || stress) PG_CUDA(cudaMemcpyAsync(acc, ctx->out_acc.p, sizeof(acc), cudaMemcpyDeviceToHost, st));
     if (forces && (flags & PG_WANT_FORCES)) ctx->out_f.download(forces, 3 * (size_t)ctx->n, st);
     if (enegs && (flags & PG_WANT_ENEGS)) ctx->out_chi.download(enegs, (size_t)ctx->n, st);
     PG_CUDA(cudaStreamSynchronize(st));
+    for (int c = 0; c < 7; ++c) tot[c] = fx_to_double(acc[c]);
     if (energy && (flags & PG_WANT_ENERGY)) *energy = tot[0];
     if (stress && (flags & PG_WANT_FORCES))
         for (int c = 0; c < 6; ++c) stress[c] = tot[1 + c];
@@ -309,8 +304,9 @@ int pg_update_atom_coordinates(pg_context* ctx, const double* positions) {
         check_ctx(ctx);
         use_device(ctx);
         pg::require(ctx->have_atoms, PG_ERR_NOT_READY, "no atoms");
-        for (int i = 0; i < 3 * ctx->n; ++i)
-            pg::require(std::isfinite(positions[i]), PG_ERR_INVALID, "non-finite atom position");
+        bool finite = true;
+        for (int i = 0; i < 3 * ctx->n; ++i) finite &= std::isfinite(positions[i]);
+        pg::require(finite, PG_ERR_INVALID, "non-finite atom position");
         ctx->pos.upload(positions, 3 * (size_t)ctx->n, ctx->stream);
         PG_CUDA(cudaStreamSynchronize(ctx->stream));
     });

@@ -10,6 +10,7 @@
 #include <vector>
 
 #include "../../include/pysic_gb300.h"
+#include "fixed.cuh"
 
 namespace pg {
 
@@ -27,6 +28,11 @@ struct Error : std::runtime_error {
 
 #define PG_CHECK_LAUNCH() PG_CUDA(cudaGetLastError())
 
+// the literal overload builds no std::string unless the check fails (some
+// checks run once per atom)
+inline void require(bool ok, int status, const char* msg) {
+    if (!ok) throw Error(status, msg);
+}
 inline void require(bool ok, int status, const std::string& msg) {
     if (!ok) throw Error(status, msg);
 }
@@ -244,10 +250,7 @@ struct pg_context {
     // outputs
     pg::DevBuf<double> out_f;     // n x 3
     pg::DevBuf<double> out_chi;   // n
-    pg::DevBuf<double> out_e;     // n per-atom energy
-    pg::DevBuf<double> out_w;     // n x 6 per-atom virial
-    pg::DevBuf<double> out_tot;   // energy, virial[6], k-space energy, extras
-    pg::DevBuf<double> red_part;  // reduction partials
+    pg::DevBuf<pg::Fx128> out_acc;  // energy, virial[6], spare: exact fixed-point totals (fixed.cuh)
 
     // charge relaxation
     pg::DevBuf<double> rq_rate, rq_force, rq_stat;
@@ -292,26 +295,25 @@ void install_neighbor_lists(pg_context* ctx, const int32_t* counts, const int32_
 // tables.cu
 void fold_tables(pg_context* ctx);
 
-// pair.cu: returns nothing; writes one partial per block into `partial`
+// pair.cu, tersoff.cu, ewald.cu: energy and virial are added to the totals
+// `acc` (null: not wanted); forces and electronegativities are written
+// (first_*) or added to the per-atom outputs
 int pair_kernel_blocks(int n, int G);
 void launch_pair_kernel_impl(pg_context* ctx, int precision, int flags, bool first_f, bool first_chi, int G,
-                             double* partial);
+                             Fx128* acc);
+void launch_pair_kernel_skip(pg_context* ctx, int precision, int flags, bool first_f, bool first_chi, int G,
+                             Fx128* acc, const int* skip);
 
-// tersoff.cu: returns the number of partial slots written
 int bond_blocks(int n, int G);
-int launch_bond_order_impl(pg_context* ctx, int precision, int flags, bool first_f, int G, double* partial,
-                           const std::function<void()>& between);
+void launch_bond_order_impl(pg_context* ctx, int precision, int flags, bool first_f, int G, Fx128* acc,
+                            const std::function<void()>& between);
 void bond_zeta_diag(pg_context* ctx);
 
 // ewald.cu
 void ewald_prepare(pg_context* ctx);
-int ewald_partial_slots(pg_context* ctx);
-void launch_ewald_kspace(pg_context* ctx, int precision, int flags, bool first_f, bool first_chi, double* partial);
-void launch_ewald_kspace_skip(pg_context* ctx, int precision, int flags, bool first_f, bool first_chi, double* partial,
+void launch_ewald_kspace(pg_context* ctx, int precision, int flags, bool first_f, bool first_chi, Fx128* acc);
+void launch_ewald_kspace_skip(pg_context* ctx, int precision, int flags, bool first_f, bool first_chi, Fx128* acc,
                               const int* skip);
-
-// reduce.cu
-void launch_final_reduce(pg_context* ctx, int nslots);
 
 // relax.cu
 void relax_charges(pg_context* ctx, int precision, int n_steps, double dt, double inertia, double friction,

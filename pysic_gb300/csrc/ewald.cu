@@ -14,13 +14,15 @@
 // phase factor is advanced by multiplying with exp(2 pi i f3) within segments
 // of at most 8 consecutive k vectors.
 //
-// Passes (all gathers, no atomics):
+// Passes (per-atom and per-k values are gathers; only the energy / virial
+// totals are exact fixed-point integer atomics, fixed.cuh):
 //  ew_prep     per atom: fixed-point fractions, scaled charge; block sums of q, q^2
 //  ew_sfac     per (segment, atom chunk): partial structure factors
-//  ew_sreduce  per k: sum the chunk partials in FP64, c_k |S_k|^2 partials;
-//              block 0 also forms sum q, sum q^2 and the self + background energy
+//  ew_sreduce  per k: sum the chunk partials (compensated FP32 or FP64),
+//              c_k |S_k|^2 into the energy total; block 0 also forms sum q,
+//              sum q^2 and the self + background energy
 //  ew_field    per (atom, k split): force / electronegativity partials
-//  ew_finish   per atom: FP64 sum of the splits, constants, self/background
+//  ew_finish   per atom: sum of the splits, constants, self/background
 //              electronegativity, output, the reference's stress term r (x) F.
 #include <algorithm>
 #include <cmath>
@@ -102,8 +104,7 @@ struct EwArgs {
     int flags, first_f, first_chi;
     double* out_f;
     double* out_chi;
-    double* partial_k;    // energy partials of ew_sreduce (+1 slot self/background)
-    double* partial_w;    // stress partials of ew_finish
+    Fx128* acc;           // global energy / virial totals (null: not wanted)
     const int* skip;      // optional device flag: nonzero = do nothing
 };
 
@@ -250,7 +251,7 @@ __global__ void ew_sreduce(EwArgs A) {
         A.S[k] = S;
         const double ck = A.kvec64[k].w;
         ((C2<R>*)A.wS)[k] = C2<R>{(R)(ck * S.x), (R)(ck * S.y)};
-        e = ck * (S.x * S.x + S.y * S.y);
+        e = ck * (S.x * S.x + S.y * S.y) * A.inv_eps_2v;
     }
     // block sum of c_k |S_k|^2, exact in fixed point
     Fx128 acc = fx_warp_sum(fx_from_double(e));
@@ -278,17 +279,14 @@ __global__ void ew_sreduce(EwArgs A) {
             a2 = fx_warp_sum(threadIdx.x < nw ? sq2[threadIdx.x] : fx_zero());
         }
         if (threadIdx.x == 0) {
-            double* p = A.partial_k + 8 * blockIdx.x;
-            p[0] = fx_to_double(acc) * A.inv_eps_2v;
-            for (int c = 1; c < 7; ++c) p[c] = 0.0;
+            if (A.acc) fx_atomic_add(&A.acc[0], acc);
             if (blockIdx.x == 0) {
                 // self and background energies (Potentials.f90:1643-1646)
                 const double q1 = fx_to_double(a1), q2 = fx_to_double(a2);
                 A.Ssum[0] = q1;
                 A.Ssum[1] = q2;
-                double* ps = A.partial_k + 8 * gridDim.x;
-                ps[0] = -(q2 * A.inv_eps_4pi * A.inv_sigma_sqrt_2pi) - q1 * q1 * 0.5 * A.inv_eps_2v * A.sigma2;
-                for (int c = 1; c < 7; ++c) ps[c] = 0.0;
+                const double eb = -(q2 * A.inv_eps_4pi * A.inv_sigma_sqrt_2pi) - q1 * q1 * 0.5 * A.inv_eps_2v * A.sigma2;
+                if (A.acc) fx_atomic_add(&A.acc[0], fx_from_double(eb));
             }
         }
     }
@@ -363,17 +361,38 @@ __global__ void __launch_bounds__(EW_THREADS) ew_field(EwArgs A) {
     }
 }
 
+// sum of the k-split partials of one atom: compensated FP32 (two-sum) widened
+// once in the mixed path, FP64 in the FP64 path
+template <typename R>
+__device__ __forceinline__ void split_sum(const R* fp, int splits, int n, int i, double f[4]);
+template <>
+__device__ __forceinline__ void split_sum<float>(const float* fp, int splits, int n, int i, double f[4]) {
+    float s[4] = {0, 0, 0, 0}, c[4] = {0, 0, 0, 0};
+    for (int q = 0; q < splits; ++q) {
+        const F4 v = *(const F4*)(fp + 4 * ((long long)q * n + i));
+        add_c(v.x, s[0], c[0]);
+        add_c(v.y, s[1], c[1]);
+        add_c(v.z, s[2], c[2]);
+        add_c(v.w, s[3], c[3]);
+    }
+    for (int k = 0; k < 4; ++k) f[k] = (double)s[k] + (double)c[k];
+}
+template <>
+__device__ __forceinline__ void split_sum<double>(const double* fp, int splits, int n, int i, double f[4]) {
+    for (int k = 0; k < 4; ++k) f[k] = 0.0;
+    for (int q = 0; q < splits; ++q)
+        for (int k = 0; k < 4; ++k) f[k] += fp[4 * ((long long)q * n + i) + k];
+}
+
 template <typename R>
 __global__ void ew_finish(EwArgs A) {
-    __shared__ double sw[EW_THREADS][6];
+    __shared__ Fx128 sw[EW_THREADS / 32][6];
     if (A.skip && *A.skip) return;
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     double w[6] = {0, 0, 0, 0, 0, 0};
     if (i < A.n) {
-        double f[4] = {0, 0, 0, 0};
-        const R* fp = (const R*)A.Fpart;
-        for (int s = 0; s < A.splits; ++s)
-            for (int c = 0; c < 4; ++c) f[c] += (double)fp[4 * ((long long)s * A.n + i) + c];
+        double f[4];
+        split_sum<R>((const R*)A.Fpart, A.splits, A.n, i, f);
         const double q = A.qs[i];
         const double pre = q / A.volume_eps;
         const double F0 = pre * f[0], F1 = pre * f[1], F2 = pre * f[2];
@@ -406,21 +425,20 @@ __global__ void ew_finish(EwArgs A) {
             else A.out_chi[i] += x;
         }
     }
-    // block sums of the six stress components: shuffle trees
+    // block sums of the six stress components, exact in fixed point
+    if (A.acc == nullptr || !(A.flags & PG_WANT_FORCES)) return;
     const int wl = threadIdx.x & 31, wid = threadIdx.x >> 5;
     for (int c = 0; c < 6; ++c) {
-        const double v = group_sum<32>(w[c]);
+        const Fx128 v = fx_warp_sum(fx_from_double(w[c]));
         if (wl == 0) sw[wid][c] = v;
     }
     __syncthreads();
     if (threadIdx.x < 32) {
         const int nw = blockDim.x >> 5;
-        double* p = A.partial_w + 8 * blockIdx.x;
         for (int c = 0; c < 6; ++c) {
-            const double v = group_sum<32>(threadIdx.x < nw ? sw[threadIdx.x][c] : 0.0);
-            if (threadIdx.x == 0) p[1 + c] = v;
+            const Fx128 v = fx_warp_sum(threadIdx.x < nw ? sw[threadIdx.x][c] : fx_zero());
+            if (threadIdx.x == 0) fx_atomic_add(&A.acc[1 + c], v);
         }
-        if (threadIdx.x == 0) p[0] = 0.0;
     }
 }
 
@@ -496,12 +514,6 @@ static void ew_shape(const pg_context* ctx, int& chunks, int& chunk, int& splits
     fin_blocks = cdiv(n, EW_THREADS);
 }
 
-int ewald_partial_slots(pg_context* ctx) {
-    int chunks, chunk, splits, sps, pb, kb, fb;
-    ew_shape(ctx, chunks, chunk, splits, sps, pb, kb, fb);
-    return kb + 1 + fb;
-}
-
 template <typename R>
 static void ew_launch(pg_context* ctx, EwArgs& A, int prep_blocks, int kred_blocks, int fin_blocks) {
     cudaStream_t st = ctx->stream;
@@ -517,7 +529,7 @@ static void ew_launch(pg_context* ctx, EwArgs& A, int prep_blocks, int kred_bloc
     PG_CHECK_LAUNCH();
 }
 
-void launch_ewald_kspace_skip(pg_context* ctx, int precision, int flags, bool first_f, bool first_chi, double* partial,
+void launch_ewald_kspace_skip(pg_context* ctx, int precision, int flags, bool first_f, bool first_chi, Fx128* acc,
                               const int* skip) {
     const int n = ctx->n;
     int chunks, chunk, splits, sps, prep_blocks, kred_blocks, fin_blocks;
@@ -567,19 +579,14 @@ void launch_ewald_kspace_skip(pg_context* ctx, int precision, int flags, bool fi
     A.first_chi = first_chi;
     A.out_f = ctx->out_f.p;
     A.out_chi = ctx->out_chi.p;
-    A.partial_k = partial;
-    A.partial_w = partial + 8 * (kred_blocks + 1);
+    A.acc = (flags & (PG_WANT_ENERGY | PG_WANT_FORCES)) ? acc : nullptr;
     A.skip = skip;
     if (precision == PG_PREC_FP64) ew_launch<double>(ctx, A, prep_blocks, kred_blocks, fin_blocks);
     else ew_launch<float>(ctx, A, prep_blocks, kred_blocks, fin_blocks);
-    if (!(flags & (PG_WANT_FORCES | PG_WANT_ENEGS))) {
-        // no finishing pass: clear its partial slots
-        PG_CUDA(cudaMemsetAsync(A.partial_w, 0, sizeof(double) * 8 * fin_blocks, ctx->stream));
-    }
 }
 
-void launch_ewald_kspace(pg_context* ctx, int precision, int flags, bool first_f, bool first_chi, double* partial) {
-    launch_ewald_kspace_skip(ctx, precision, flags, first_f, first_chi, partial, nullptr);
+void launch_ewald_kspace(pg_context* ctx, int precision, int flags, bool first_f, bool first_chi, Fx128* acc) {
+    launch_ewald_kspace_skip(ctx, precision, flags, first_f, first_chi, acc, nullptr);
 }
 
 }  // namespace pg

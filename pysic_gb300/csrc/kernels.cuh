@@ -5,6 +5,7 @@
 #include <cuda_runtime.h>
 
 #include "common.cuh"
+#include "fixed.cuh"
 
 namespace pg {
 
@@ -173,37 +174,53 @@ __device__ __forceinline__ T group_sum(T v) {
     return v;
 }
 
-// Compensated sum over a group of G lanes: FP32 partials are combined with a
-// two-sum at every step, and the (sum, error) pair is widened to FP64 once.
-// The value is the same in every lane; call .d() in the lane that stores it so
-// that only one lane per atom touches the FP64 pipe.
-struct CSum {
-    float s, c;
-    __device__ __forceinline__ double d() const { return (double)s + (double)c; }
+// Sum over a group of G lanes, the same value in every lane.  Mixed path: each
+// lane's FP32 partial becomes 2^-32 fixed point and the group adds integers,
+// exactly (fixed.cuh), so no lane touches the FP64 pipe.  FP64 path: an FP64
+// shuffle tree.
+struct XSum {
+    long long f;
+    __device__ __forceinline__ double d() const { return fix_to_double(f); }
+    __device__ __forceinline__ Fx128 fx() const { return fx_from_fix(f); }
 };
 struct DSum {
     double s;
     __device__ __forceinline__ double d() const { return s; }
+    __device__ __forceinline__ Fx128 fx() const { return fx_from_double(s); }
 };
 
 template <int G>
-__device__ __forceinline__ CSum group_sum_c(float v) {
-    float s = v, c = 0.0f;
+__device__ __forceinline__ XSum group_sum_c(float v) {
+    long long f = fix_from_float(v);
 #pragma unroll
-    for (int o = G / 2; o > 0; o >>= 1) {
-        const float so = __shfl_xor_sync(0xffffffffu, s, o, G);
-        const float co = __shfl_xor_sync(0xffffffffu, c, o, G);
-        const float t = s + so;
-        const float bp = t - s;
-        const float err = (s - (t - bp)) + (so - bp);
-        s = t;
-        c = c + co + err;
-    }
-    return CSum{s, c};
+    for (int o = G / 2; o > 0; o >>= 1) f += __shfl_xor_sync(0xffffffffu, f, o, G);
+    return XSum{f};
 }
 template <int G>
 __device__ __forceinline__ DSum group_sum_c(double v) {
     return DSum{group_sum<G>(v)};
+}
+
+// write (first) or add a group sum into a per-atom FP64 output; the mixed
+// path adds in fixed point
+__device__ __forceinline__ void store_sum(double* p, const XSum& v, bool first) {
+    *p = first ? v.d() : fix_to_double(v.f + fix_from_double(*p));
+}
+__device__ __forceinline__ void store_sum(double* p, const DSum& v, bool first) { *p = first ? v.s : *p + v.s; }
+
+// Adds a block's energy and virial -- tot[slot][0..6], one row per atom slot,
+// filled before the call -- to the global totals acc[0..6] (null: none).
+// Called by every thread of the block; blockDim.x is a multiple of 32.
+__device__ __forceinline__ void block_totals(const Fx128 (*tot)[7], int nslot, Fx128* acc) {
+    __syncthreads();
+    if (acc == nullptr) return;
+    const int wid = threadIdx.x >> 5, wl = threadIdx.x & 31, nw = blockDim.x >> 5;
+    for (int c = wid; c < 7; c += nw) {
+        Fx128 v = fx_zero();
+        for (int k = wl; k < nslot; k += 32) v = fx_add(v, tot[k][c]);
+        v = fx_warp_sum(v);
+        if (wl == 0) fx_atomic_add(&acc[c], v);
+    }
 }
 
 }  // namespace pg

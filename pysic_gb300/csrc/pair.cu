@@ -35,10 +35,10 @@ struct PairArgs {
     int first_f, first_chi;
     double* out_f;
     double* out_chi;
-    double* partial;  // per block: energy, virial[6], pad
+    Fx128* acc;       // global energy / virial totals (null: not wanted)
     const int* skip;  // optional device flag: nonzero = do nothing
     const F4* sep0;   // mixed path: bond vectors at list build
-    const F4* disp;   // mixed path: displacements since the build
+    const F4* disp;   // mixed path: displacements since the build (xyz) and FP32 charge (w)
 };
 
 // bond vector of entry e of atom i: FP64 from the positions, or (mixed path)
@@ -66,6 +66,19 @@ __device__ __forceinline__ void pair_vector<float>(const PairArgs& A, int i, int
     z = s0.z + (dj.z - di.z);
 }
 
+// charge of atom j in the working precision (mixed path: the FP32 copy kept
+// beside the displacement)
+template <typename R>
+__device__ __forceinline__ R charge_of(const PairArgs& A, int j);
+template <>
+__device__ __forceinline__ double charge_of<double>(const PairArgs& A, int j) {
+    return A.charge[j];
+}
+template <>
+__device__ __forceinline__ float charge_of<float>(const PairArgs& A, int j) {
+    return A.disp[j].w;
+}
+
 __device__ __forceinline__ double powi_(double x, int n) {
     double r = 1.0;
     for (int k = 0; k < n; ++k) r *= x;
@@ -74,7 +87,7 @@ __device__ __forceinline__ double powi_(double x, int n) {
 
 template <typename R, int G>
 __global__ void __launch_bounds__(256) pair_kernel(PairArgs A) {
-    __shared__ double red[256 / G][8];
+    __shared__ Fx128 tot[256 / G][7];
     const int lane = threadIdx.x % G;
     const int slot = threadIdx.x / G;
     const int i = blockIdx.x * (blockDim.x / G) + slot;
@@ -84,11 +97,17 @@ __global__ void __launch_bounds__(256) pair_kernel(PairArgs A) {
     R w0 = 0, w1 = 0, w2 = 0, w3 = 0, w4 = 0, w5 = 0;
     const bool wantE = A.flags & PG_WANT_ENERGY, wantF = A.flags & PG_WANT_FORCES, wantC = A.flags & PG_WANT_ENEGS;
     int ti = 0;
-    double qi = 0;
     if (act) {
         ti = A.type[i];
-        qi = A.charge[i];
-        const double xi = A.pos[3 * i], yi = A.pos[3 * i + 1], zi = A.pos[3 * i + 2];
+        const R qi = charge_of<R>(A, i);
+        const R ew_rc = (R)A.ew_rc, ew_is2 = (R)A.ew_is2, ew_k = (R)A.ew_k, ew_c2 = (R)A.ew_c2,
+                ew_isq2 = (R)A.ew_isq2;
+        double xi = 0, yi = 0, zi = 0;
+        if constexpr (sizeof(R) == 8) {
+            xi = A.pos[3 * i];
+            yi = A.pos[3 * i + 1];
+            zi = A.pos[3 * i + 2];
+        }
         const int e1 = A.start[i + 1];
         for (int e = A.start[i] + lane; e < e1; e += G) {
             const int j = A.idx[e];
@@ -98,13 +117,13 @@ __global__ void __launch_bounds__(256) pair_kernel(PairArgs A) {
             if (r == R(0)) continue;
             const R ir = R(1) / r;
             R U = 0, dU = 0;
-            if (A.ewald && r < (R)A.ew_rc) {
-                const R qq = (R)(qi * A.charge[j]);
-                const R ec = erfc_(r * (R)A.ew_is2);
-                const R k = (R)A.ew_k;
-                U += k * qq * ec * ir;
-                if (wantF) dU -= k * qq * (ec * ir * ir + (R)A.ew_c2 * exp_(-r * r * (R)A.ew_isq2) * ir);
-                if (wantC) chi -= (R)A.charge[j] * k * ec * ir;
+            if (A.ewald && r < ew_rc) {
+                const R qj = charge_of<R>(A, j);
+                const R qq = qi * qj;
+                const R ec = erfc_(r * ew_is2);
+                U += ew_k * qq * ec * ir;
+                if (wantF) dU -= ew_k * qq * (ec * ir * ir + ew_c2 * exp_(-r * r * ew_isq2) * ir);
+                if (wantC) chi -= qj * ew_k * ec * ir;
             }
             const int tj = A.type[j];
             // charge-independent pair terms have zero electronegativity
@@ -132,52 +151,47 @@ __global__ void __launch_bounds__(256) pair_kernel(PairArgs A) {
             w5 += h * x * y;
         }
     }
-    const R lanev[11] = {fx, fy, fz, en, chi, w0, w1, w2, w3, w4, w5};
-    double d[11];
-#pragma unroll
-    for (int q = 0; q < 11; ++q) {
-        const auto sq = group_sum_c<G>(lanev[q]);
-        d[q] = lane == 0 ? sq.d() : 0.0;
-    }
+    const auto sfx = group_sum_c<G>(fx), sfy = group_sum_c<G>(fy), sfz = group_sum_c<G>(fz);
+    auto schi = group_sum_c<G>(chi);
     if (act && lane == 0) {
-        // single-atom terms (charge_self: epsilon q^n, chi = -epsilon n q^(n-1); Potentials.f90:4341-4375)
+        // single-atom terms in FP64 (charge_self: epsilon q^n, chi = -epsilon n q^(n-1);
+        // Potentials.f90:4341-4375)
         const int2 sx = A.sindex[ti];
-        for (int t = sx.x; t < sx.x + sx.y; ++t) {
-            const SingleTerm S = A.sterms[t];
-            d[3] += S.eps * powi_(qi, S.n);
-            d[4] += -(S.eps * S.n * powi_(qi, S.n - 1));
+        double es = 0.0;
+        if (sx.y > 0) {
+            const double qd = A.charge[i];
+            double cs = 0.0;
+            for (int t = sx.x; t < sx.x + sx.y; ++t) {
+                const SingleTerm S = A.sterms[t];
+                es += S.eps * powi_(qd, S.n);
+                cs += -(S.eps * S.n * powi_(qd, S.n - 1));
+            }
+            if constexpr (sizeof(R) == 4) schi.f += fix_from_double(cs);
+            else schi.s += cs;
         }
         if (wantF) {
-            if (A.first_f) {
-                A.out_f[3 * i] = d[0];
-                A.out_f[3 * i + 1] = d[1];
-                A.out_f[3 * i + 2] = d[2];
-            } else {
-                A.out_f[3 * i] += d[0];
-                A.out_f[3 * i + 1] += d[1];
-                A.out_f[3 * i + 2] += d[2];
-            }
+            store_sum(A.out_f + 3 * i, sfx, A.first_f);
+            store_sum(A.out_f + 3 * i + 1, sfy, A.first_f);
+            store_sum(A.out_f + 3 * i + 2, sfz, A.first_f);
         }
-        if (wantC) {
-            if (A.first_chi) A.out_chi[i] = d[4];
-            else A.out_chi[i] += d[4];
+        if (wantC) store_sum(A.out_chi + i, schi, A.first_chi);
+        tot[slot][0] = fx_from_double(es);
+    }
+    if (A.acc && (wantE || wantF)) {
+        const auto se = group_sum_c<G>(en);
+        const auto v0 = group_sum_c<G>(w0), v1 = group_sum_c<G>(w1), v2 = group_sum_c<G>(w2);
+        const auto v3 = group_sum_c<G>(w3), v4 = group_sum_c<G>(w4), v5 = group_sum_c<G>(w5);
+        if (lane == 0) {
+            tot[slot][0] = act ? fx_add(tot[slot][0], se.fx()) : fx_zero();
+            tot[slot][1] = act ? v0.fx() : fx_zero();
+            tot[slot][2] = act ? v1.fx() : fx_zero();
+            tot[slot][3] = act ? v2.fx() : fx_zero();
+            tot[slot][4] = act ? v3.fx() : fx_zero();
+            tot[slot][5] = act ? v4.fx() : fx_zero();
+            tot[slot][6] = act ? v5.fx() : fx_zero();
         }
+        block_totals(tot, blockDim.x / G, A.acc);
     }
-    if (lane == 0) {
-        red[slot][0] = act ? d[3] : 0.0;
-        for (int q = 0; q < 6; ++q) red[slot][1 + q] = act ? d[5 + q] : 0.0;
-    }
-    __syncthreads();
-    const int nslot = blockDim.x / G;
-    const int wid = threadIdx.x >> 5, wl = threadIdx.x & 31;
-    const int nw = (blockDim.x + 31) >> 5;
-    for (int c = wid; c < 7; c += nw) {
-        double v = 0.0;
-        for (int k = wl; k < nslot; k += 32) v += red[k][c];
-        v = group_sum<32>(v);
-        if (wl == 0) A.partial[8 * blockIdx.x + c] = v;
-    }
-    (void)wantE;
 }
 
 // atoms per block: enough blocks to cover every SM twice, at most 256 threads
@@ -197,7 +211,7 @@ int pair_kernel_blocks(int n, int G) {
 }
 
 void launch_pair_kernel_skip(pg_context* ctx, int precision, int flags, bool first_f, bool first_chi, int G,
-                             double* partial, const int* skip) {
+                             Fx128* acc, const int* skip) {
     PairArgs A{};
     A.skip = skip;
     A.n = ctx->n;
@@ -227,7 +241,7 @@ void launch_pair_kernel_skip(pg_context* ctx, int precision, int flags, bool fir
     A.first_chi = first_chi;
     A.out_f = ctx->out_f.p;
     A.out_chi = ctx->out_chi.p;
-    A.partial = partial;
+    A.acc = acc;
     const int nbk = pair_kernel_blocks(ctx->n, G);
     const int threads = pair_atoms_per_block(ctx->n, G) * G;
     A.sep0 = ctx->nb_sep0.p;
@@ -249,8 +263,8 @@ void launch_pair_kernel_skip(pg_context* ctx, int precision, int flags, bool fir
 }
 
 void launch_pair_kernel_impl(pg_context* ctx, int precision, int flags, bool first_f, bool first_chi, int G,
-                             double* partial) {
-    launch_pair_kernel_skip(ctx, precision, flags, first_f, first_chi, G, partial, nullptr);
+                             Fx128* acc) {
+    launch_pair_kernel_skip(ctx, precision, flags, first_f, first_chi, G, acc, nullptr);
 }
 
 }  // namespace pg

@@ -22,8 +22,6 @@
 
 namespace pg {
 
-void launch_pair_kernel_skip(pg_context* ctx, int precision, int flags, bool first_f, bool first_chi, int G,
-                             double* partial, const int* skip);
 int pair_lanes_for(const pg_context* ctx);
 
 namespace {
@@ -42,6 +40,7 @@ struct RxArgs {
     double* stat;     // [0] error, [1] max |dq| of the last step, [2] mean chi
     double* part;     // per block: sum chi, max F, max |dq|
     int nblocks;
+    F4* disp;         // mixed path: the FP32 charge copy in .w follows q (null: FP64 path)
 };
 
 __global__ void rx_update(RxArgs A) {
@@ -52,7 +51,9 @@ __global__ void rx_update(RxArgs A) {
     if (i < A.n) {
         const double r = A.rate[i], f = A.force[i];
         dq = r * A.dt + (f - A.friction * r) * A.inv_m * A.dt * A.dt;
-        A.q[i] += dq;
+        const double q = A.q[i] + dq;
+        A.q[i] = q;
+        if (A.disp) A.disp[i].w = (float)q;
         A.rate[i] = (1.0 - 0.5 * A.friction * A.dt) * r + f * 0.5 * A.inv_m * A.dt;
     }
     sm[threadIdx.x] = fabs(dq);
@@ -142,9 +143,8 @@ __global__ void rx_init_stat(RxArgs A) {
 // electronegativities of the current charges into ctx->out_chi, stopped by `skip`
 static void enqueue_chi(pg_context* ctx, int precision, const int* skip) {
     const int G = pair_lanes_for(ctx);
-    double* part = ctx->red_part.p;
-    launch_pair_kernel_skip(ctx, precision, PG_WANT_ENEGS, true, true, G, part, skip);
-    if (ctx->ewald) launch_ewald_kspace_skip(ctx, precision, PG_WANT_ENEGS, true, false, part, skip);
+    launch_pair_kernel_skip(ctx, precision, PG_WANT_ENEGS, true, true, G, nullptr, skip);
+    if (ctx->ewald) launch_ewald_kspace_skip(ctx, precision, PG_WANT_ENEGS, true, false, nullptr, skip);
 }
 
 void relax_charges(pg_context* ctx, int precision, int n_steps, double dt, double inertia, double friction,
@@ -156,10 +156,6 @@ void relax_charges(pg_context* ctx, int precision, int n_steps, double dt, doubl
     const int nb = std::max(1, (n + RT - 1) / RT);
     ctx->out_chi.resize((size_t)std::max(n, 1));
     ctx->out_f.resize(3 * (size_t)std::max(n, 1));
-    const int G = pair_lanes_for(ctx);
-    // the pair kernel and the k-space passes both write their partials from slot 0
-    const int slots = std::max(pair_kernel_blocks(n, G), ctx->ewald ? ewald_partial_slots(ctx) : 0) + 1;
-    ctx->red_part.resize(8 * (size_t)slots);
     ctx->rq_rate.upload(rates, (size_t)n, st);
     ctx->rq_force.resize((size_t)std::max(n, 1));
     ctx->rq_stat.resize(4 + 3 * (size_t)nb);
@@ -181,8 +177,12 @@ void relax_charges(pg_context* ctx, int precision, int n_steps, double dt, doubl
     A.part = ctx->rq_stat.p + 4;
     A.nblocks = nb;
     ctx->launches = 0;
-    // positions stay fixed during the relaxation: displacements once
-    if (precision == PG_PREC_MIXED) launch_disp(ctx, nullptr);
+    // positions stay fixed during the relaxation: displacements (and the FP32
+    // charges beside them) once; rx_update keeps the charges current
+    if (precision == PG_PREC_MIXED) {
+        launch_disp(ctx, nullptr);
+        A.disp = ctx->disp32.p;
+    }
     // initial differences (relaxation.py:433)
     enqueue_chi(ctx, precision, A.flag);
     rx_block_sums<<<nb, RT, 0, st>>>(A);

@@ -72,20 +72,21 @@ struct BondArgs {
     void* geo;
     void* fj;
     void* fk;
-    double* fc;
+    void* fc;          // per atom: i part of the force (FP64, or 2^-32 fixed point in the mixed path)
     double* out_f;
-    double* partial;
+    Fx128* acc;        // global energy / virial totals (null: not wanted)
     double* zeta_out;
 };
 
-// per-atom displacement since the short-list build, FP64 difference rounded to FP32
-__global__ void disp_pass(int n, const double* __restrict__ pos, const double* __restrict__ pos0, F4* __restrict__ d,
-                          const int* skip) {
+// per-atom displacement since the list build (FP64 difference rounded to FP32)
+// and the FP32 charge, one 16-byte record per atom for the mixed-path kernels
+__global__ void disp_pass(int n, const double* __restrict__ pos, const double* __restrict__ pos0,
+                          const double* __restrict__ q, F4* __restrict__ d, const int* skip) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (skip && *skip) return;
     if (i >= n) return;
     d[i] = F4{(float)(pos[3 * i] - pos0[3 * i]), (float)(pos[3 * i + 1] - pos0[3 * i + 1]),
-              (float)(pos[3 * i + 2] - pos0[3 * i + 2]), 0.0f};
+              (float)(pos[3 * i + 2] - pos0[3 * i + 2]), (float)q[i]};
 }
 
 template <typename R>
@@ -121,7 +122,7 @@ __global__ void __launch_bounds__(128) bond_pass(BondArgs A) {
     __shared__ V4 sgeo[AP * CAP];
     __shared__ int styp[AP * CAP];
     __shared__ TripT<R> strip[64];
-    __shared__ double red[AP][8];
+    __shared__ Fx128 tot[AP][7];
     const PairT<R>* terms = (const PairT<R>*)A.terms;
     const int T3 = A.T * A.T * A.T;
     const TripT<R>* trip = (const TripT<R>*)A.trip;
@@ -273,29 +274,27 @@ __global__ void __launch_bounds__(128) bond_pass(BondArgs A) {
     const auto w3 = group_sum_c<G>(W3), w4 = group_sum_c<G>(W4), w5 = group_sum_c<G>(W5);
     if (lane == 0) {
         if (act) {
-            A.fc[3 * i] = d0.d();
-            A.fc[3 * i + 1] = d1.d();
-            A.fc[3 * i + 2] = d2.d();
+            if constexpr (sizeof(R) == 4) {
+                long long* fc = (long long*)A.fc + 3 * i;
+                fc[0] = d0.f;
+                fc[1] = d1.f;
+                fc[2] = d2.f;
+            } else {
+                double* fc = (double*)A.fc + 3 * i;
+                fc[0] = d0.s;
+                fc[1] = d1.s;
+                fc[2] = d2.s;
+            }
         }
-        red[slot][0] = act ? de.d() : 0.0;
-        red[slot][1] = act ? w0.d() : 0.0;
-        red[slot][2] = act ? w1.d() : 0.0;
-        red[slot][3] = act ? w2.d() : 0.0;
-        red[slot][4] = act ? w3.d() : 0.0;
-        red[slot][5] = act ? w4.d() : 0.0;
-        red[slot][6] = act ? w5.d() : 0.0;
+        tot[slot][0] = act ? de.fx() : fx_zero();
+        tot[slot][1] = act ? w0.fx() : fx_zero();
+        tot[slot][2] = act ? w1.fx() : fx_zero();
+        tot[slot][3] = act ? w2.fx() : fx_zero();
+        tot[slot][4] = act ? w3.fx() : fx_zero();
+        tot[slot][5] = act ? w4.fx() : fx_zero();
+        tot[slot][6] = act ? w5.fx() : fx_zero();
     }
-    __syncthreads();
-    // block partials: one warp per component, shuffle tree over the block's atoms
-    const int wid = threadIdx.x >> 5, wl = threadIdx.x & 31;
-    if (A.partial && wid < 4) {
-        for (int c = wid; c < 7; c += 4) {
-            double v = 0.0;
-            for (int k = wl; k < AP; k += 32) v += red[k][c];
-            v = group_sum<32>(v);
-            if (wl == 0) A.partial[8 * blockIdx.x + c] = v;
-        }
-    }
+    block_totals(tot, AP, A.acc);
 }
 
 template <typename R, int G>
@@ -329,20 +328,23 @@ __global__ void __launch_bounds__(128) gather_pass(BondArgs A) {
             }
         }
     }
-    const auto sx = group_sum_c<G>(Fx), sy = group_sum_c<G>(Fy), sz = group_sum_c<G>(Fz);
+    auto sx = group_sum_c<G>(Fx), sy = group_sum_c<G>(Fy), sz = group_sum_c<G>(Fz);
     if (act && lane == 0) {
-        const double fx = sx.d() + A.fc[3 * m];
-        const double fy = sy.d() + A.fc[3 * m + 1];
-        const double fz = sz.d() + A.fc[3 * m + 2];
-        if (A.first_f) {
-            A.out_f[3 * m] = fx;
-            A.out_f[3 * m + 1] = fy;
-            A.out_f[3 * m + 2] = fz;
+        // plus the i part left by the bond pass
+        if constexpr (sizeof(R) == 4) {
+            const long long* fc = (const long long*)A.fc + 3 * m;
+            sx.f += fc[0];
+            sy.f += fc[1];
+            sz.f += fc[2];
         } else {
-            A.out_f[3 * m] += fx;
-            A.out_f[3 * m + 1] += fy;
-            A.out_f[3 * m + 2] += fz;
+            const double* fc = (const double*)A.fc + 3 * m;
+            sx.s += fc[0];
+            sy.s += fc[1];
+            sz.s += fc[2];
         }
+        store_sum(A.out_f + 3 * m, sx, A.first_f);
+        store_sum(A.out_f + 3 * m + 1, sy, A.first_f);
+        store_sum(A.out_f + 3 * m + 2, sz, A.first_f);
     }
 }
 
@@ -361,7 +363,7 @@ static void prepare_scratch(pg_context* ctx, int precision) {
     ctx->bo_fc.resize(3 * (size_t)std::max(ctx->n, 1));
 }
 
-static BondArgs bond_args(pg_context* ctx, int precision, int flags, bool first_f, double* partial) {
+static BondArgs bond_args(pg_context* ctx, int precision, int flags, bool first_f, Fx128* acc) {
     BondArgs A{};
     A.n = ctx->n;
     A.T = std::max(ctx->n_types, 1);
@@ -399,7 +401,7 @@ static BondArgs bond_args(pg_context* ctx, int precision, int flags, bool first_
     }
     A.fc = ctx->bo_fc.p;
     A.out_f = ctx->out_f.p;
-    A.partial = partial;
+    A.acc = acc;
     A.zeta_out = nullptr;
     return A;
 }
@@ -422,22 +424,22 @@ static void launch_by_lanes(const BondArgs& A, int n, cudaStream_t st, int G, bo
     }
 }
 
-// returns the number of partial slots written; `between` runs between the two passes
-int launch_bond_order_impl(pg_context* ctx, int precision, int flags, bool first_f, int G, double* partial,
-                           const std::function<void()>& between) {
+// `between` runs between the two passes
+void launch_bond_order_impl(pg_context* ctx, int precision, int flags, bool first_f, int G, Fx128* acc,
+                            const std::function<void()>& between) {
     prepare_scratch(ctx, precision);
-    BondArgs A = bond_args(ctx, precision, flags, first_f, partial);
+    BondArgs A = bond_args(ctx, precision, flags, first_f, acc);
     const bool forces = (flags & PG_WANT_FORCES) != 0;
     if (precision == PG_PREC_FP64) launch_by_lanes<double>(A, ctx->n, ctx->stream, G, forces, between);
     else launch_by_lanes<float>(A, ctx->n, ctx->stream, G, forces, between);
     PG_CHECK_LAUNCH();
     ctx->launches += forces ? 2 : 1;
-    return bond_blocks(ctx->n, G);
 }
 
 void launch_disp(pg_context* ctx, const int* skip) {
     ctx->disp32.resize((size_t)std::max(ctx->n, 1));
-    disp_pass<<<(ctx->n + 255) / 256, 256, 0, ctx->stream>>>(ctx->n, ctx->pos.p, ctx->pos0.p, ctx->disp32.p, skip);
+    disp_pass<<<(ctx->n + 255) / 256, 256, 0, ctx->stream>>>(ctx->n, ctx->pos.p, ctx->pos0.p, ctx->charge.p, ctx->disp32.p,
+                                                                 skip);
     PG_CHECK_LAUNCH();
     ctx->launches++;
 }
