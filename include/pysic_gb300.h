@@ -169,6 +169,27 @@ int pg_device_results(pg_context* ctx, double* energy, double* forces, double* s
 int pg_device_positions(pg_context* ctx, double** device_ptr);
 /* The CUDA stream the context launches on (cudaStream_t as void*). */
 int pg_get_stream(pg_context* ctx, void** stream);
+
+/* Bond-order (Tersoff) energy, virial and forces without any device allocation
+ * during the call.  No counterpart in the reference, whose f2py calls always
+ * allocate their NumPy outputs.
+ * All per-call scratch comes from one static device array of
+ * PG_NOALLOC_SCRATCH_BYTES; a system that needs more is rejected with
+ * PG_ERR_INVALID and a message giving both sizes.  d_forces (N x 3 doubles) and
+ * d_totals (7 doubles: energy, then the virial xx, yy, zz, yz, xz, xy) are device
+ * pointers owned by the caller; the work is enqueued on the context's stream
+ * (pg_get_stream) and the call returns without waiting.
+ *  - Only contexts whose every term runs in the bond-order kernels (no Ewald,
+ *    charge or out-of-bond pair terms): PG_ERR_UNSUPPORTED otherwise.
+ *  - Tables and lists must be current: call pg_calculate once after the last
+ *    change of potentials, lists or lanes (PG_ERR_NOT_READY otherwise).
+ *  - The first call on a device looks up the static array's address; make it
+ *    before any stream capture.
+ *  - The array is shared by every context on the device: calls that overlap in
+ *    time race on it and must be ordered by the caller. */
+#define PG_NOALLOC_SCRATCH_BYTES (32u << 20)
+int pg_bond_order_noalloc(pg_context* ctx, int32_t precision, double* d_forces, double* d_totals);
+
 /* Kernel launches issued by the last pg_device_evaluate / pg_calculate. */
 int pg_last_launch_count(pg_context* ctx, int32_t* launches);
 /* Record CUDA events around the kernel groups of each evaluation;

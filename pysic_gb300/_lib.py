@@ -76,6 +76,7 @@ _SIGNATURES = {
     "pg_device_results": (ctypes.c_int, [_ctx, _c_double_p, _c_double_p, _c_double_p, _c_double_p]),
     "pg_device_positions": (ctypes.c_int, [_ctx, ctypes.POINTER(_c_double_p)]),
     "pg_get_stream": (ctypes.c_int, [_ctx, ctypes.POINTER(ctypes.c_void_p)]),
+    "pg_bond_order_noalloc": (ctypes.c_int, [_ctx, ctypes.c_int32, ctypes.c_void_p, ctypes.c_void_p]),
     "pg_last_launch_count": (ctypes.c_int, [_ctx, _c_int_p]),
     "pg_set_kernel_timing": (ctypes.c_int, [_ctx, ctypes.c_int32]),
     "pg_get_kernel_times": (ctypes.c_int, [_ctx, ctypes.POINTER(ctypes.c_float)]),

@@ -578,6 +578,14 @@ int pg_get_stream(pg_context* ctx, void** stream) {
     });
 }
 
+int pg_bond_order_noalloc(pg_context* ctx, int32_t precision, double* d_forces, double* d_totals) {
+    return guarded([&] {
+        check_ctx(ctx);
+        use_device(ctx);
+        pg::bond_order_noalloc(ctx, precision, d_forces, d_totals);
+    });
+}
+
 int pg_set_kernel_timing(pg_context* ctx, int32_t enable) {
     return guarded([&] {
         check_ctx(ctx);

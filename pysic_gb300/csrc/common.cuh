@@ -308,6 +308,8 @@ int bond_blocks(int n, int G);
 void launch_bond_order_impl(pg_context* ctx, int precision, int flags, bool first_f, int G, Fx128* acc,
                             const std::function<void()>& between);
 void bond_zeta_diag(pg_context* ctx);
+// noalloc.cu: the bond-order passes on static scratch (pg_bond_order_noalloc)
+void bond_order_noalloc(pg_context* ctx, int precision, double* d_forces, double* d_totals);
 
 // ewald.cu
 void ewald_prepare(pg_context* ctx);

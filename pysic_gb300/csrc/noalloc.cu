@@ -1,0 +1,98 @@
+// noalloc.cu -- the bond-order evaluation with every per-call buffer in one
+// static device array, for callers that must not allocate device memory while
+// the call runs.
+//
+// The regular evaluation grows its scratch buffers (bond geometry, per-bond and
+// per-triplet force parts, per-atom i parts, displacements) with cudaMalloc on
+// first use and whenever the lists grow.  This variant takes all of them from
+// g_scratch, a file-scope __device__ array of PG_NOALLOC_SCRATCH_BYTES, and
+// writes its results into device buffers the caller owns.
+//
+// Set-up: the first call on a device, with that device current, looks up the
+// array's address once with cudaGetSymbolAddress (which may load this
+// library's device code); make that first call before any stream capture.
+// Zeroing: only the 128-bit energy / virial totals must start at zero; they are
+// cleared with cudaMemsetAsync at the start of every call.  Every other region
+// is written before it is read within the call.
+// Concurrency: the array is shared by every context on the device, so two calls
+// that overlap in time (other threads, other streams) race on it; callers must
+// order them.
+#include <mutex>
+
+#include "common.cuh"
+
+namespace pg {
+
+void launch_bond_order_scratch(pg_context* ctx, int precision, int G, void* geo_fj, void* fk, void* fc, F4* disp,
+                               Fx128* acc, double* out_f);
+
+namespace {
+
+static __device__ __align__(256) unsigned char g_scratch[PG_NOALLOC_SCRATCH_BYTES];
+
+constexpr int MAX_DEVICES = 64;
+std::mutex g_mu;
+void* g_addr[MAX_DEVICES] = {};
+
+void* scratch_address(int device) {
+    require(device >= 0 && device < MAX_DEVICES, PG_ERR_INVALID, "device index out of range");
+    std::lock_guard<std::mutex> lock(g_mu);
+    if (g_addr[device] == nullptr) {
+        void* p = nullptr;
+        PG_CUDA(cudaGetSymbolAddress(&p, g_scratch));
+        g_addr[device] = p;
+    }
+    return g_addr[device];
+}
+
+size_t align256(size_t b) { return (b + 255) & ~(size_t)255; }
+
+// the rounded totals: energy, then the virial (xx, yy, zz, yz, xz, xy)
+__global__ void totals_to_double(const Fx128* __restrict__ acc, double* __restrict__ out) {
+    const int c = threadIdx.x;
+    if (c < 7) out[c] = fx_to_double(acc[c]);
+}
+
+}  // namespace
+
+void bond_order_noalloc(pg_context* ctx, int precision, double* d_forces, double* d_totals) {
+    require(precision == PG_PREC_FP64 || precision == PG_PREC_MIXED, PG_ERR_INVALID, "unknown precision");
+    require(d_forces != nullptr && d_totals != nullptr, PG_ERR_INVALID, "null output pointer");
+    require(ctx->have_bond_terms, PG_ERR_NOT_READY, "no bond-order factors");
+    require(!ctx->have_pair_kernel_terms && !ctx->ewald && !ctx->have_singles, PG_ERR_UNSUPPORTED,
+            "the no-allocation call covers contexts whose every term runs in the bond-order kernels "
+            "(no Ewald, single-atom or out-of-bond pair terms)");
+    // everything the regular path builds lazily must already exist
+    require(ctx->have_list && !ctx->tables_dirty && ctx->sep0_epoch == ctx->list_epoch && !ctx->short_dirty,
+            PG_ERR_NOT_READY,
+            "tables or lists are not prepared: evaluate once with pg_calculate after the last change, "
+            "then use the no-allocation call");
+    int G = ctx->lanes != 0 ? ctx->lanes : ctx->tuned_lanes[precision];
+    if (G == 0) G = 8;
+    const size_t n = (size_t)std::max(ctx->n, 1);
+    const size_t ne = (size_t)std::max<long long>(ctx->sh_total, 1);
+    const size_t nt = (size_t)std::max<long long>(ctx->sh_tri_total, 1);
+    const size_t rec = precision == PG_PREC_FP64 ? sizeof(D4) : sizeof(F4);
+    const size_t b_acc = align256(8 * sizeof(Fx128));
+    const size_t b_disp = align256(n * sizeof(F4));
+    const size_t b_fc = align256(3 * n * sizeof(double));
+    const size_t b_fj = align256(2 * ne * rec);
+    const size_t b_fk = align256(nt * rec);
+    const size_t need = b_acc + b_disp + b_fc + b_fj + b_fk;
+    if (need > (size_t)PG_NOALLOC_SCRATCH_BYTES)
+        throw Error(PG_ERR_INVALID, "the no-allocation bond-order call needs " + std::to_string(need) +
+                                        " bytes of scratch for this system; its static limit is " +
+                                        std::to_string((size_t)PG_NOALLOC_SCRATCH_BYTES) + " bytes");
+    unsigned char* base = (unsigned char*)scratch_address(ctx->device);
+    Fx128* acc = (Fx128*)base;
+    F4* disp = (F4*)(base + b_acc);
+    void* fc = base + b_acc + b_disp;
+    void* fj = base + b_acc + b_disp + b_fc;
+    void* fk = base + b_acc + b_disp + b_fc + b_fj;
+    PG_CUDA(cudaMemsetAsync(acc, 0, sizeof(Fx128) * 8, ctx->stream));
+    launch_bond_order_scratch(ctx, precision, G, fj, fk, fc, disp, acc, d_forces);
+    totals_to_double<<<1, 32, 0, ctx->stream>>>(acc, d_totals);
+    PG_CHECK_LAUNCH();
+}
+
+}  // namespace pg

@@ -436,6 +436,32 @@ void launch_bond_order_impl(pg_context* ctx, int precision, int flags, bool firs
     ctx->launches += forces ? 2 : 1;
 }
 
+// The two passes on scratch the caller provides instead of the context's
+// buffers (the no-allocation entry point): geo_fj holds 2 records per short-list
+// entry, fk one per triplet slot, fc 3 values per atom, disp (mixed path) one
+// record per atom.  Energy and virial go to acc, forces to out_f (written).
+void launch_bond_order_scratch(pg_context* ctx, int precision, int G, void* geo_fj, void* fk, void* fc, F4* disp,
+                               Fx128* acc, double* out_f) {
+    BondArgs A = bond_args(ctx, precision, PG_WANT_ENERGY | PG_WANT_FORCES, true, acc);
+    const size_t ne = (size_t)std::max<long long>(ctx->sh_total, 1);
+    const size_t rec = precision == PG_PREC_FP64 ? sizeof(D4) : sizeof(F4);
+    A.geo = geo_fj;
+    A.fj = (char*)geo_fj + ne * rec;
+    A.fk = fk;
+    A.fc = fc;
+    A.out_f = out_f;
+    auto none = [] {};
+    if (precision == PG_PREC_FP64) {
+        launch_by_lanes<double>(A, ctx->n, ctx->stream, G, true, none);
+    } else {
+        disp_pass<<<(ctx->n + 255) / 256, 256, 0, ctx->stream>>>(ctx->n, ctx->pos.p, ctx->pos0.p, ctx->charge.p, disp,
+                                                                 nullptr);
+        A.disp = disp;
+        launch_by_lanes<float>(A, ctx->n, ctx->stream, G, true, none);
+    }
+    PG_CHECK_LAUNCH();
+}
+
 void launch_disp(pg_context* ctx, const int* skip) {
     ctx->disp32.resize((size_t)std::max(ctx->n, 1));
     disp_pass<<<(ctx->n + 255) / 256, 256, 0, ctx->stream>>>(ctx->n, ctx->pos.p, ctx->pos0.p, ctx->charge.p, ctx->disp32.p,
