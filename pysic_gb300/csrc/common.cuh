@@ -110,7 +110,7 @@ struct PairT {
 // Tersoff triplet parameters for (centre type, j type, k type) of group 0.
 template <typename R>
 struct TripT {
-    R a, c2, d2, h, mu, rc, rs;
+    R a, c2, d2, h, mu, rc, rs, c2d2;  // c2d2 = c^2 / d^2
     int valid;
 };
 
@@ -127,7 +127,7 @@ inline PairT<R> cast_pair(const PairT<S>& a) {
 }
 template <typename R, typename S>
 inline TripT<R> cast_trip(const TripT<S>& a) {
-    return TripT<R>{(R)a.a, (R)a.c2, (R)a.d2, (R)a.h, (R)a.mu, (R)a.rc, (R)a.rs, a.valid};
+    return TripT<R>{(R)a.a, (R)a.c2, (R)a.d2, (R)a.h, (R)a.mu, (R)a.rc, (R)a.rs, (R)a.c2d2, a.valid};
 }
 template <typename R, typename S>
 inline PostT<R> cast_post(const PostT<S>& a) {
@@ -188,6 +188,12 @@ struct pg_context {
     pg::DevBuf<pg::PostT<float>> d_post32;
     pg::DevBuf<double> d_maxbr;          // per type: max bond-order cutoff (max_bond_radius)
     pg::DevBuf<float> d_maxbr32;
+    // per (centre type, k type): bond-order cutoff rc, rs of the triplets, valid
+    // for every j type when bcut_uniform (then f(r_ik) is computed once per bond)
+    pg::DevBuf<double2> d_bcut;
+    pg::DevBuf<float2> d_bcut32;
+    bool bcut_uniform = false;
+    int n_pair_terms = 0;  // records in d_pair_terms
     pg::DevBuf<pg::SingleTerm> d_single_terms;
     pg::DevBuf<int2> d_single_index;     // per type
 
@@ -218,7 +224,7 @@ struct pg_context {
     bool short_dirty = true;
     bool short_is_full = false;
     pg::DevBuf<int> sh_start, sh_idx, sh_off, sh_rev, sh_count;
-    pg::DevBuf<long long> sh_tri;  // per atom: base of its n_i^2 triplet block
+    pg::DevBuf<int> sh_order;      // atoms in order of their short-list length (lane groups of equal work)
     pg::DevBuf<int> sh_type;       // per short entry: type of the partner atom
     // mixed path: bond vectors of both lists taken once per list generation in
     // FP64 (rounded to FP32) at the positions pos0; an evaluation adds the FP32
@@ -227,7 +233,7 @@ struct pg_context {
     pg::DevBuf<double> pos0;
     pg::DevBuf<pg::F4> disp32;
     unsigned long long list_epoch = 0, sep0_epoch = ~0ull;
-    long long sh_total = 0, sh_tri_total = 0;
+    long long sh_total = 0;
     int sh_maxn = 0;
 
     // neighbour-build scratch
@@ -240,8 +246,8 @@ struct pg_context {
     pg::DevBuf<int> scan_tmp;
 
     // bond-order scratch
-    pg::DevBuf<pg::F4> bo_fj, bo_fk;      // mixed precision
-    pg::DevBuf<pg::D4> bo_fj64, bo_fk64; // FP64
+    pg::DevBuf<pg::F4> bo_fj;             // mixed precision: 3 records per short entry
+    pg::DevBuf<pg::D4> bo_fj64;           // FP64: 3 records per short entry
     pg::DevBuf<double> bo_fc;             // centre-role forces per atom (3)
     pg::DevBuf<double> bo_zeta;           // per short entry (diagnostics)
     int lanes = 0;                        // 0: autotune

@@ -24,6 +24,10 @@ __device__ __forceinline__ float sqrt_(float x) { return sqrtf(x); }
 __device__ __forceinline__ double sqrt_(double x) { return sqrt(x); }
 __device__ __forceinline__ float erfc_(float x) { return erfcf(x); }
 __device__ __forceinline__ double erfc_(double x) { return erfc(x); }
+// reciprocal: the FP32 path uses the fast approximate division (a few ulp),
+// the FP64 path the correctly rounded one
+__device__ __forceinline__ float rcp_(float x) { return __fdividef(1.0f, x); }
+__device__ __forceinline__ double rcp_(double x) { return 1.0 / x; }
 
 // Smooth cutoff f(r) = 1/2 (1 + cos(pi (r - rs)/(rc - rs))) on [rs, rc] and its
 // derivative (smoothening_factor / smoothening_derivative, Potentials.f90:442-498).
@@ -82,7 +86,7 @@ __device__ __forceinline__ void pair_term(const PairT<R>& P, R r, R& V, R& dV) {
 
 // Angular function g = 1 + c^2/d^2 - c^2/(d^2 + (h - cos)^2) of
 // evaluate_pair_bond_order_factor_tersoff (Potentials.f90:5790), written in the
-// algebraically equal form 1 + c^2 x / (d^2 (d^2 + x)), x = (h - cos)^2, which
+// algebraically equal form 1 + (c^2/d^2) x / (d^2 + x), x = (h - cos)^2, which
 // does not cancel catastrophically in FP32 (c^2/d^2 is ~4e7 for silicon);
 // dg/dcos = -2 c^2 (h - cos) / (d^2 + x)^2.
 template <typename R>
@@ -90,8 +94,8 @@ __device__ __forceinline__ void angular(const TripT<R>& t, R cs, R& g, R& dg) {
     const R hc = t.h - cs;
     const R x = hc * hc;
     const R den = t.d2 + x;
-    const R inv = R(1) / den;
-    g = R(1) + t.c2 * x * inv / t.d2;
+    const R inv = rcp_(den);
+    g = R(1) + t.c2d2 * x * inv;
     dg = R(-2) * t.c2 * hc * inv * inv;
 }
 
@@ -157,6 +161,41 @@ __device__ __forceinline__ bool tersoff_grad(const TripT<R>& t, const V3<R>& a, 
     return true;
 }
 
+// The same zeta term and gradient from per-bond quantities computed once per
+// bond instead of once per triplet: unit vectors ua, ub, inverse lengths and
+// the cutoff factor f(r_ik), f'(r_ik) of bond ik.
+template <typename R>
+__device__ __forceinline__ R tersoff_term_c(const TripT<R>& t, const V3<R>& ua, R r1, const V3<R>& ub, R r2, R f) {
+    const R cs = ua.x * ub.x + ua.y * ub.y + ua.z * ub.z;
+    R g, dg;
+    angular(t, cs, g, dg);
+    R X, Xp;
+    radial_exp(t, r1 - r2, X, Xp);
+    return f * X * g;
+}
+
+template <typename R>
+__device__ __forceinline__ void tersoff_grad_c(const TripT<R>& t, const V3<R>& ua, R r1, R i1, const V3<R>& ub, R r2,
+                                               R i2, R f, R fp, V3<R>& gj, V3<R>& gk) {
+    const R cs = ua.x * ub.x + ua.y * ub.y + ua.z * ub.z;
+    R g, dg;
+    angular(t, cs, g, dg);
+    R X, Xp;
+    radial_exp(t, r1 - r2, X, Xp);
+    const R xi = f * X;
+    const R xdg = xi * dg;
+    const R cj = g * f * Xp - xdg * cs * i1;
+    const R cjb = xdg * i1;
+    gj.x = cj * ua.x + cjb * ub.x;
+    gj.y = cj * ua.y + cjb * ub.y;
+    gj.z = cj * ua.z + cjb * ub.z;
+    const R ck = g * (fp * X - f * Xp) - xdg * cs * i2;
+    const R cka = xdg * i2;
+    gk.x = ck * ub.x + cka * ua.x;
+    gk.y = ck * ub.y + cka * ua.y;
+    gk.z = ck * ub.z + cka * ua.z;
+}
+
 // B(zeta) = (1 + (beta zeta)^eta)^(-1/(2 eta)) and dB/dzeta
 // (post_process_bond_order_factor_tersoff / _gradient_tersoff, Potentials.f90:5910-5961)
 template <typename R>
@@ -164,6 +203,30 @@ __device__ __forceinline__ void post_process(R beta, R eta, R zeta, R& B, R& dB)
     const R tt = pow_(beta * zeta, eta);
     B = pow_(R(1) + tt, R(-0.5) / eta);
     dB = zeta > R(0) ? R(-0.5) * B * tt / ((R(1) + tt) * zeta) : R(0);
+}
+// FP32: x^y written as 2^(y log2 x), and (1 + t)^p as exp(p log1p(t)) so that
+// the small t = (beta zeta)^eta keeps its relative accuracy
+template <>
+__device__ __forceinline__ void post_process<float>(float beta, float eta, float zeta, float& B, float& dB) {
+    if (zeta > 0.0f) {
+        const float tt = exp2f(eta * log2f(beta * zeta));
+        B = expf(__fdividef(-0.5f, eta) * log1pf(tt));
+        dB = __fdividef(-0.5f * B * tt, (1.0f + tt) * zeta);
+    } else {
+        B = 1.0f;
+        dB = 0.0f;
+    }
+}
+
+// Slot of the atom a lane group handles.  The atoms, sorted by list length,
+// are cut into warp-sized runs that are dealt round-robin over the blocks, so
+// that the lanes of a warp loop equally long and every block gets a similar
+// mix of light and heavy warps.  A bijection onto [0, gridDim.x * blockDim.x / G).
+template <int G>
+__device__ __forceinline__ int dealt_slot() {
+    constexpr int APW = 32 / G;
+    const int wi = threadIdx.x >> 5, si = (threadIdx.x & 31) / G;
+    return (wi * (int)gridDim.x + (int)blockIdx.x) * APW + si;
 }
 
 // warp-segment reductions over groups of G lanes
@@ -174,10 +237,8 @@ __device__ __forceinline__ T group_sum(T v) {
     return v;
 }
 
-// Sum over a group of G lanes, the same value in every lane.  Mixed path: each
-// lane's FP32 partial becomes 2^-32 fixed point and the group adds integers,
-// exactly (fixed.cuh), so no lane touches the FP64 pipe.  FP64 path: an FP64
-// shuffle tree.
+// Per-atom group sums: XSum (mixed path) holds 2^-32 fixed point, DSum (FP64
+// path) an FP64 value; fixed.cuh explains the fixed-point formats.
 struct XSum {
     long long f;
     __device__ __forceinline__ double d() const { return fix_to_double(f); }
@@ -189,17 +250,22 @@ struct DSum {
     __device__ __forceinline__ Fx128 fx() const { return fx_from_double(s); }
 };
 
+// Group sum in the working precision and, in the mixed path, one conversion to
+// 2^-32 fixed point afterwards: an FP32 shuffle tree over the G lanes of an atom
+// (a fixed order, so deterministic), exact from there on.
 template <int G>
-__device__ __forceinline__ XSum group_sum_c(float v) {
-    long long f = fix_from_float(v);
-#pragma unroll
-    for (int o = G / 2; o > 0; o >>= 1) f += __shfl_xor_sync(0xffffffffu, f, o, G);
-    return XSum{f};
+__device__ __forceinline__ XSum group_sum_f(float v) {
+    return XSum{fix_from_float(group_sum<G>(v))};
 }
 template <int G>
-__device__ __forceinline__ DSum group_sum_c(double v) {
+__device__ __forceinline__ DSum group_sum_f(double v) {
     return DSum{group_sum<G>(v)};
 }
+
+// sum over the 32 lanes of a warp in the working precision, widened exactly to
+// a 128-bit total (the same in every lane)
+__device__ __forceinline__ Fx128 warp_total(float v) { return fx_from_float(group_sum<32>(v)); }
+__device__ __forceinline__ Fx128 warp_total(double v) { return fx_from_double(group_sum<32>(v)); }
 
 // write (first) or add a group sum into a per-atom FP64 output; the mixed
 // path adds in fixed point
@@ -208,18 +274,30 @@ __device__ __forceinline__ void store_sum(double* p, const XSum& v, bool first) 
 }
 __device__ __forceinline__ void store_sum(double* p, const DSum& v, bool first) { *p = first ? v.s : *p + v.s; }
 
-// Adds a block's energy and virial -- tot[slot][0..6], one row per atom slot,
-// filled before the call -- to the global totals acc[0..6] (null: none).
-// Called by every thread of the block; blockDim.x is a multiple of 32.
-__device__ __forceinline__ void block_totals(const Fx128 (*tot)[7], int nslot, Fx128* acc) {
-    __syncthreads();
+// Adds a block's energy and virial to the global totals acc[0..6] (null: none)
+// without a block-wide barrier.  v holds the 7 totals of the calling warp
+// (read in lane 0).  Each warp publishes its sums in shared memory; the last
+// warp of the block to arrive adds all of them to acc.  `done` is a shared
+// counter set to zero before the block's first barrier.
+__device__ __forceinline__ void block_totals_publish(const Fx128 (&v)[7], Fx128 (*wsum)[7], unsigned* done,
+                                                     Fx128* acc) {
     if (acc == nullptr) return;
-    const int wid = threadIdx.x >> 5, wl = threadIdx.x & 31, nw = blockDim.x >> 5;
-    for (int c = wid; c < 7; c += nw) {
-        Fx128 v = fx_zero();
-        for (int k = wl; k < nslot; k += 32) v = fx_add(v, tot[k][c]);
-        v = fx_warp_sum(v);
-        if (wl == 0) fx_atomic_add(&acc[c], v);
+    const int wl = threadIdx.x & 31, w = threadIdx.x >> 5, nw = blockDim.x >> 5;
+    if (wl == 0) {
+#pragma unroll
+        for (int c = 0; c < 7; ++c) wsum[w][c] = v[c];
+        __threadfence_block();
+        if (atomicAdd(done, 1u) == (unsigned)(nw - 1)) {
+            __threadfence_block();
+            for (int c = 0; c < 7; ++c) {
+                Fx128 t = fx_zero();
+                for (int k = 0; k < nw; ++k) {
+                    const volatile Fx128* q = &wsum[k][c];
+                    t = fx_add(t, Fx128{q->lo, q->hi});
+                }
+                fx_atomic_add(&acc[c], t);
+            }
+        }
     }
 }
 

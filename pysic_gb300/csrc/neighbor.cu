@@ -840,14 +840,6 @@ void build_short_list(pg_context* ctx) {
                                                                     ctx->sh_type.p);
         PG_CHECK_LAUNCH();
     }
-    // triplet block bases: exclusive scan of n_i^2
-    ctx->sh_tri.resize(n + 1);
-    DevBuf<long long> tot;
-    tot.resize(1);
-    scan_single_block<int, long long><<<1, 1024, 0, st>>>(ctx->sh_count.p, ctx->sh_tri.p, n, tot.p, 1);
-    PG_CHECK_LAUNCH();
-    long long tri_total = 0;
-    PG_CUDA(cudaMemcpyAsync(&tri_total, tot.p, sizeof(long long), cudaMemcpyDeviceToHost, st));
     DevBuf<int> mx;
     mx.resize(2);
     max_reduce<<<1, 1024, 0, st>>>(n, ctx->sh_count.p, mx.p);
@@ -858,10 +850,22 @@ void build_short_list(pg_context* ctx) {
     int h[2] = {0, 0};
     PG_CUDA(cudaMemcpyAsync(h, mx.p, sizeof(int) * 2, cudaMemcpyDeviceToHost, st));
     PG_CUDA(cudaStreamSynchronize(st));
-    ctx->sh_tri_total = tri_total;
     ctx->sh_maxn = h[0];
     require(total == 0 || h[1] >= 0, PG_ERR_INVALID,
             "neighbour lists are not symmetric: a bond has no reverse entry (lists must be built both ways)");
+    // atoms grouped by list length (stable counting sort), so that the lane
+    // groups of one warp loop over the same number of bonds
+    std::vector<int> cnt((size_t)std::max(n, 1)), order((size_t)std::max(n, 1));
+    if (n > 0) PG_CUDA(cudaMemcpyAsync(cnt.data(), ctx->sh_count.p, sizeof(int) * n, cudaMemcpyDeviceToHost, st));
+    PG_CUDA(cudaStreamSynchronize(st));
+    {
+        std::vector<int> first((size_t)h[0] + 2, 0);
+        for (int m = 0; m < n; ++m) first[(size_t)cnt[m] + 1]++;
+        for (size_t c = 1; c < first.size(); ++c) first[c] += first[c - 1];
+        for (int m = 0; m < n; ++m) order[(size_t)first[(size_t)cnt[m]]++] = m;
+    }
+    ctx->sh_order.upload(order.data(), order.size(), st);
+    PG_CUDA(cudaStreamSynchronize(st));
     ctx->short_dirty = false;
     ctx->state_epoch++;
 }

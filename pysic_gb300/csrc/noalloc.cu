@@ -2,8 +2,8 @@
 // static device array, for callers that must not allocate device memory while
 // the call runs.
 //
-// The regular evaluation grows its scratch buffers (bond geometry, per-bond and
-// per-triplet force parts, per-atom i parts, displacements) with cudaMalloc on
+// The regular evaluation grows its scratch buffers (bond geometry, per-bond
+// force parts, per-atom centre parts, displacements) with cudaMalloc on
 // first use and whenever the lists grow.  This variant takes all of them from
 // g_scratch, a file-scope __device__ array of PG_NOALLOC_SCRATCH_BYTES, and
 // writes its results into device buffers the caller owns.
@@ -23,8 +23,8 @@
 
 namespace pg {
 
-void launch_bond_order_scratch(pg_context* ctx, int precision, int G, void* geo_fj, void* fk, void* fc, F4* disp,
-                               Fx128* acc, double* out_f);
+void launch_bond_order_scratch(pg_context* ctx, int precision, int G, void* bonds, void* fc, F4* disp, Fx128* acc,
+                               double* out_f);
 
 namespace {
 
@@ -71,14 +71,12 @@ void bond_order_noalloc(pg_context* ctx, int precision, double* d_forces, double
     if (G == 0) G = 8;
     const size_t n = (size_t)std::max(ctx->n, 1);
     const size_t ne = (size_t)std::max<long long>(ctx->sh_total, 1);
-    const size_t nt = (size_t)std::max<long long>(ctx->sh_tri_total, 1);
     const size_t rec = precision == PG_PREC_FP64 ? sizeof(D4) : sizeof(F4);
     const size_t b_acc = align256(8 * sizeof(Fx128));
     const size_t b_disp = align256(n * sizeof(F4));
     const size_t b_fc = align256(3 * n * sizeof(double));
-    const size_t b_fj = align256(2 * ne * rec);
-    const size_t b_fk = align256(nt * rec);
-    const size_t need = b_acc + b_disp + b_fc + b_fj + b_fk;
+    const size_t b_bonds = align256(3 * ne * rec);
+    const size_t need = b_acc + b_disp + b_fc + b_bonds;
     if (need > (size_t)PG_NOALLOC_SCRATCH_BYTES)
         throw Error(PG_ERR_INVALID, "the no-allocation bond-order call needs " + std::to_string(need) +
                                         " bytes of scratch for this system; its static limit is " +
@@ -87,10 +85,9 @@ void bond_order_noalloc(pg_context* ctx, int precision, double* d_forces, double
     Fx128* acc = (Fx128*)base;
     F4* disp = (F4*)(base + b_acc);
     void* fc = base + b_acc + b_disp;
-    void* fj = base + b_acc + b_disp + b_fc;
-    void* fk = base + b_acc + b_disp + b_fc + b_fj;
+    void* bonds = base + b_acc + b_disp + b_fc;
     PG_CUDA(cudaMemsetAsync(acc, 0, sizeof(Fx128) * 8, ctx->stream));
-    launch_bond_order_scratch(ctx, precision, G, fj, fk, fc, disp, acc, d_forces);
+    launch_bond_order_scratch(ctx, precision, G, bonds, fc, disp, acc, d_forces);
     totals_to_double<<<1, 32, 0, ctx->stream>>>(acc, d_totals);
     PG_CHECK_LAUNCH();
 }

@@ -87,7 +87,10 @@ __device__ __forceinline__ double powi_(double x, int n) {
 
 template <typename R, int G>
 __global__ void __launch_bounds__(256) pair_kernel(PairArgs A) {
-    __shared__ Fx128 tot[256 / G][7];
+    __shared__ Fx128 wsum[256 / 32][7];
+    __shared__ unsigned done;
+    if (threadIdx.x == 0) done = 0u;
+    __syncthreads();
     const int lane = threadIdx.x % G;
     const int slot = threadIdx.x / G;
     const int i = blockIdx.x * (blockDim.x / G) + slot;
@@ -151,46 +154,43 @@ __global__ void __launch_bounds__(256) pair_kernel(PairArgs A) {
             w5 += h * x * y;
         }
     }
-    const auto sfx = group_sum_c<G>(fx), sfy = group_sum_c<G>(fy), sfz = group_sum_c<G>(fz);
-    auto schi = group_sum_c<G>(chi);
+    // single-atom terms in FP64 (charge_self: epsilon q^n, chi = -epsilon n q^(n-1);
+    // Potentials.f90:4341-4375), added by the group's lane 0
+    double cs = 0.0;
     if (act && lane == 0) {
-        // single-atom terms in FP64 (charge_self: epsilon q^n, chi = -epsilon n q^(n-1);
-        // Potentials.f90:4341-4375)
         const int2 sx = A.sindex[ti];
-        double es = 0.0;
         if (sx.y > 0) {
             const double qd = A.charge[i];
-            double cs = 0.0;
+            double es = 0.0;
             for (int t = sx.x; t < sx.x + sx.y; ++t) {
                 const SingleTerm S = A.sterms[t];
                 es += S.eps * powi_(qd, S.n);
                 cs += -(S.eps * S.n * powi_(qd, S.n - 1));
             }
-            if constexpr (sizeof(R) == 4) schi.f += fix_from_double(cs);
-            else schi.s += cs;
+            en += (R)es;
         }
-        if (wantF) {
+    }
+    if (wantF) {
+        const auto sfx = group_sum_f<G>(fx), sfy = group_sum_f<G>(fy), sfz = group_sum_f<G>(fz);
+        if (act && lane == 0) {
             store_sum(A.out_f + 3 * i, sfx, A.first_f);
             store_sum(A.out_f + 3 * i + 1, sfy, A.first_f);
             store_sum(A.out_f + 3 * i + 2, sfz, A.first_f);
         }
-        if (wantC) store_sum(A.out_chi + i, schi, A.first_chi);
-        tot[slot][0] = fx_from_double(es);
     }
-    if (A.acc && (wantE || wantF)) {
-        const auto se = group_sum_c<G>(en);
-        const auto v0 = group_sum_c<G>(w0), v1 = group_sum_c<G>(w1), v2 = group_sum_c<G>(w2);
-        const auto v3 = group_sum_c<G>(w3), v4 = group_sum_c<G>(w4), v5 = group_sum_c<G>(w5);
-        if (lane == 0) {
-            tot[slot][0] = act ? fx_add(tot[slot][0], se.fx()) : fx_zero();
-            tot[slot][1] = act ? v0.fx() : fx_zero();
-            tot[slot][2] = act ? v1.fx() : fx_zero();
-            tot[slot][3] = act ? v2.fx() : fx_zero();
-            tot[slot][4] = act ? v3.fx() : fx_zero();
-            tot[slot][5] = act ? v4.fx() : fx_zero();
-            tot[slot][6] = act ? v5.fx() : fx_zero();
+    if (wantC) {
+        auto schi = group_sum_f<G>(chi);
+        if (act && lane == 0) {
+            if constexpr (sizeof(R) == 4) schi.f += fix_from_double(cs);
+            else schi.s += cs;
+            store_sum(A.out_chi + i, schi, A.first_chi);
         }
-        block_totals(tot, blockDim.x / G, A.acc);
+    }
+    // energy and virial: warp sums, exact from there on
+    if (A.acc && (wantE || wantF)) {
+        const Fx128 v[7] = {warp_total(en), warp_total(w0), warp_total(w1), warp_total(w2),
+                            warp_total(w3), warp_total(w4), warp_total(w5)};
+        block_totals_publish(v, wsum, &done, A.acc);
     }
 }
 

@@ -30,7 +30,7 @@ void fold_tables(pg_context* ctx) {
 
     // bond-order tables
     std::vector<TripT<double>> trip((size_t)T * T * T);
-    for (auto& t : trip) t = TripT<double>{0, 0, 0, 0, 0, 0, 0, 0};
+    for (auto& t : trip) t = TripT<double>{};
     std::vector<PostT<double>> post(T, PostT<double>{0, 0, 0});
     std::vector<double> maxbr(T, 0.0);
     double bo_radius = 0.0;
@@ -51,6 +51,7 @@ void fold_tables(pg_context* ctx) {
                     tt.a = p[2];
                     tt.c2 = p[3] * p[3];
                     tt.d2 = p[4] * p[4];
+                    tt.c2d2 = tt.c2 / tt.d2;
                     tt.h = p[5];
                     tt.mu = p[6];
                     tt.rc = ctx->br_cut[b];
@@ -60,6 +61,30 @@ void fold_tables(pg_context* ctx) {
             }
         }
     }
+    // cutoff of bond ik per (ti, tk): one pair (rc, rs) shared by all tj, or not uniform
+    std::vector<double2> bcut((size_t)T * T, make_double2(0.0, 0.0));
+    bool uniform = true;
+    for (int ti = 0; ti < T; ++ti)
+        for (int tk = 0; tk < T; ++tk) {
+            bool seen = false;
+            for (int tj = 0; tj < T; ++tj) {
+                const TripT<double>& tt = trip[((size_t)ti * T + tj) * T + tk];
+                if (!tt.valid) continue;
+                double2& c = bcut[(size_t)ti * T + tk];
+                if (!seen) {
+                    c = make_double2(tt.rc, tt.rs);
+                    seen = true;
+                } else if (c.x != tt.rc || c.y != tt.rs) {
+                    uniform = false;
+                }
+            }
+        }
+    ctx->bcut_uniform = uniform;
+    std::vector<float2> bcut32(bcut.size());
+    for (size_t q = 0; q < bcut.size(); ++q) bcut32[q] = make_float2((float)bcut[q].x, (float)bcut[q].y);
+    ctx->d_bcut.upload(bcut.data(), bcut.size(), st);
+    ctx->d_bcut32.upload(bcut32.data(), bcut32.size(), st);
+
     // pair terms: bond-order scaled terms define the bond-order kernel's reach
     const int np = (int)ctx->pr_cut.size();
     for (int r = 0; r < np; ++r)
@@ -131,6 +156,7 @@ void fold_tables(pg_context* ctx) {
     std::vector<PostT<float>> post32(post.size());
     for (size_t q = 0; q < post.size(); ++q) post32[q] = cast_post<float>(post[q]);
     std::vector<float> maxbr32(maxbr.begin(), maxbr.end());
+    ctx->n_pair_terms = (int)terms.size();
     ctx->d_pair_terms.upload(terms.data(), terms.size(), st);
     ctx->d_pair_terms32.upload(terms32.data(), terms32.size(), st);
     ctx->d_pair_index.upload(index.data(), index.size(), st);

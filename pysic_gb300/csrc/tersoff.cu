@@ -29,8 +29,12 @@
 // of the per-term work: bond vectors are taken once per short-list build in
 // FP64 (rounded to FP32), and every evaluation adds the FP32 displacement of
 // both atoms since that build (prepared per atom in FP64 by disp_pass).  Lane
-// partial sums are FP32; the lanes of an atom are combined with a compensated
-// (two-sum) reduction and the per-atom totals are FP64.
+// partial sums are FP32; the lanes of an atom are combined exactly in integer
+// fixed point and the energy / virial totals are exact 128-bit integers
+// (fixed.cuh), so the mixed path issues no FP64 instruction at all.
+// Per bond, the staging step keeps the unit vector, 1/r and (when every j
+// type shares it) the bond-order cutoff factor f(r_ik), which every triplet
+// through the bond reuses.
 #include <functional>
 
 #include "common.cuh"
@@ -58,20 +62,23 @@ struct BondArgs {
     const int* idx;
     const int* off;
     const int* rev;
-    const long long* tri;
     const void* terms;  // PairT<R>
     const int2* index;
     const void* trip;   // TripT<R>
     const void* post;   // PostT<R>
     const void* maxbr;  // R
+    const void* bcut;   // per (ti, tk): rc, rs of bond ik (Vec2T<R>)
+    int bcut_uniform;   // bcut holds for every tj
     const int* etype;   // per entry: partner type
+    const int* order;   // lane-group slot -> atom (atoms grouped by list length)
+    int n_terms;        // pair records in terms
     const F4* sep0;     // mixed path: bond vectors at list build
     const F4* disp;     // mixed path: per-atom displacement since the build
     int flags;
     int first_f;
     void* geo;
     void* fj;
-    void* fk;
+    void* kacc;        // per entry i->k: the k parts of i's bonds on k (unstaged atoms' scratch)
     void* fc;          // per atom: i part of the force (FP64, or 2^-32 fixed point in the mixed path)
     double* out_f;
     Fx128* acc;        // global energy / virial totals (null: not wanted)
@@ -113,57 +120,125 @@ __device__ __forceinline__ F4 bond_vector<float>(const BondArgs& A, int i, int e
     return F4{x, y, z, sqrtf(x * x + y * y + z * z)};
 }
 
-constexpr int CAP = 32;  // bonds per atom staged in shared memory
+template <typename R>
+struct Vec2T;
+template <>
+struct Vec2T<float> {
+    using T = float2;
+};
+template <>
+struct Vec2T<double> {
+    using T = double2;
+};
 
 template <typename R, int G>
-__global__ void __launch_bounds__(128) bond_pass(BondArgs A) {
+__global__ void __launch_bounds__(128, sizeof(R) == 4 ? 7 : 4) bond_pass(BondArgs A) {
     using V4 = typename Vec4T<R>::T;
+    using V2 = typename Vec2T<R>::T;
     constexpr int AP = 128 / G;  // atoms per block
-    __shared__ V4 sgeo[AP * CAP];
-    __shared__ int styp[AP * CAP];
+    // bonds per atom staged in shared memory with their unit vectors and cutoff
+    // factors; an atom with more bonds reads its geometry from global memory
+    // and recomputes the rest per triplet
+    constexpr int CAP = (sizeof(R) == 4 && G > 4) ? 16 : 8;
+    constexpr int CAPP = CAP + 1;  // padded stride: the groups of a warp hit different banks
+    __shared__ V4 sgeo[AP * CAPP];
+    __shared__ V4 sunit[AP * CAPP];
+    __shared__ V2 scut[AP * CAPP];
+    __shared__ V4 sbacc[AP * CAPP];
+    __shared__ int styp[AP * CAPP];
     __shared__ TripT<R> strip[64];
-    __shared__ Fx128 tot[AP][7];
+    __shared__ PairT<R> sterm[32];
+    __shared__ int2 sindex[64];
+    __shared__ Fx128 wsum[128 / 32][7];
+    __shared__ unsigned done;
+    // small interaction tables in shared memory
     const PairT<R>* terms = (const PairT<R>*)A.terms;
-    const int T3 = A.T * A.T * A.T;
+    const int2* index = A.index;
+    const int T2 = A.T * A.T, T3 = T2 * A.T;
     const TripT<R>* trip = (const TripT<R>*)A.trip;
     if (T3 <= 64) {
         for (int q = threadIdx.x; q < T3; q += blockDim.x) strip[q] = trip[q];
         trip = strip;
     }
+    if (A.n_terms <= 32 && T2 <= 64) {
+        for (int q = threadIdx.x; q < A.n_terms; q += blockDim.x) sterm[q] = terms[q];
+        for (int q = threadIdx.x; q < T2; q += blockDim.x) sindex[q] = index[q];
+        terms = sterm;
+        index = sindex;
+    }
+    if (threadIdx.x == 0) done = 0u;
     __syncthreads();
     const int lane = threadIdx.x % G;
     const int slot = threadIdx.x / G;
-    const int i = blockIdx.x * AP + slot;
-    const bool act = i < A.n;
+    const int gslot = A.order ? dealt_slot<G>() : blockIdx.x * AP + slot;
+    const bool act = gslot < A.n;
+    const int i = act ? (A.order ? A.order[gslot] : gslot) : 0;
     const int s = act ? A.start[i] : 0;
     const int ni = act ? A.start[i + 1] - s : 0;
     const bool staged = ni <= CAP;
-    V4* geo = staged ? sgeo + slot * CAP : (V4*)A.geo + s;
-    const int* typ = staged ? styp + slot * CAP : A.etype + s;
+    V4* geo = staged ? sgeo + slot * CAPP : (V4*)A.geo + s;
+    const int* typ = staged ? styp + slot * CAPP : A.etype + s;
+    V4* unit = sunit + slot * CAPP;  // staged atoms: unit vector, 1/r
+    V2* cut = scut + slot * CAPP;    // staged atoms with uniform cutoffs: f(r), f'(r)
+    const bool cached_cut = staged && A.bcut_uniform;
+    const int ti = act ? A.type[i] : 0;
     V4* fj = (V4*)A.fj;
-    V4* fk = (V4*)A.fk;
-    // geometry of i's bonds in the working precision
+    // geometry of i's bonds in the working precision, and per bond what every
+    // triplet through it reuses
     if (act) {
-        const double xi = A.pos[3 * i], yi = A.pos[3 * i + 1], zi = A.pos[3 * i + 2];
+        double xi = 0, yi = 0, zi = 0;
+        if constexpr (sizeof(R) == 8) {
+            xi = A.pos[3 * i];
+            yi = A.pos[3 * i + 1];
+            zi = A.pos[3 * i + 2];
+        }
         for (int e = lane; e < ni; e += G) {
-            geo[e] = bond_vector<R>(A, i, s + e, xi, yi, zi);
-            if (staged) styp[slot * CAP + e] = A.etype[s + e];
+            const V4 g = bond_vector<R>(A, i, s + e, xi, yi, zi);
+            geo[e] = g;
+            if (staged) {
+                const int te = A.etype[s + e];
+                styp[slot * CAPP + e] = te;
+                const R ir = g.w > R(0) ? rcp_(g.w) : R(0);
+                unit[e] = V4{g.x * ir, g.y * ir, g.z * ir, ir};
+                if (A.bcut_uniform) {
+                    const V2 c = ((const V2*)A.bcut)[ti * A.T + te];
+                    R f, fp;
+                    smooth<R>(g.w, c.x, c.y, f, fp);
+                    cut[e] = V2{f, fp};
+                }
+            }
         }
     }
     __syncwarp();
+    // unit vector and inverse length of bond k
+    auto unit_of = [&](int k, const V4& g, V3<R>& u, R& ir) {
+        if (staged) {
+            const V4 v = unit[k];
+            u = V3<R>{v.x, v.y, v.z};
+            ir = v.w;
+        } else {
+            ir = g.w > R(0) ? rcp_(g.w) : R(0);
+            u = V3<R>{g.x * ir, g.y * ir, g.z * ir};
+        }
+    };
     R Fx = 0, Fy = 0, Fz = 0, En = 0;
     R W0 = 0, W1 = 0, W2 = 0, W3 = 0, W4 = 0, W5 = 0;
+    // per bond e (owned by lane e % G): the force on its partner j so far, and
+    // in .w the three-body prefactor 1/2 V f dB/dzeta
+    V4* bacc = staged ? sbacc + slot * CAPP : fj + s;
+    V4* kacc = (V4*)A.kacc + s;  // per bond k: the group's k parts, written once
+    const R maxbr = act ? ((const R*)A.maxbr)[ti] : R(0);
     if (act) {
-        const int ti = A.type[i];
-        const R maxbr = ((const R*)A.maxbr)[ti];
         const PostT<R> pp = ((const PostT<R>*)A.post)[ti];
-        const long long tri = A.tri[i];
         for (int e = lane; e < ni; e += G) {
             const V4 gij = geo[e];
             const V3<R> a{gij.x, gij.y, gij.z};
             const R r = gij.w;
             const int tj = typ[e];
-            const int2 ix = A.index[ti * A.T + tj];
+            V3<R> ua;
+            R i1;
+            unit_of(e, gij, ua, i1);
+            const int2 ix = index[ti * A.T + tj];
             bool any = false, bo = false;
             for (int t = ix.x; t < ix.x + ix.y; ++t) {
                 const PairT<R>& P = terms[t];
@@ -172,8 +247,6 @@ __global__ void __launch_bounds__(128) bond_pass(BondArgs A) {
                     bo |= P.group >= 0;
                 }
             }
-            R fjx = 0, fjy = 0, fjz = 0;
-            V4* row = fk + tri + (long long)e * ni;
             const TripT<R>* trow = trip + (ti * A.T + tj) * A.T;
             // zeta_ij (core_calculate_pair_bond_order_factor, first neighbour loop)
             R zeta = 0, B = 1, dB = 0;
@@ -184,14 +257,19 @@ __global__ void __launch_bounds__(128) bond_pass(BondArgs A) {
                     if (!(gik.w < maxbr)) continue;
                     const TripT<R>& TT = trow[typ[k]];
                     if (!TT.valid) continue;
-                    zeta += tersoff_term<R>(TT, a, r, V3<R>{gik.x, gik.y, gik.z}, gik.w);
+                    R f, fp;
+                    if (cached_cut) f = cut[k].x;
+                    else smooth<R>(gik.w, TT.rc, TT.rs, f, fp);
+                    if (f == R(0)) continue;
+                    V3<R> ub;
+                    R i2;
+                    unit_of(k, gik, ub, i2);
+                    zeta += tersoff_term_c<R>(TT, ua, r, ub, gik.w, f);
                 }
             }
             if (A.zeta_out) A.zeta_out[s + e] = (double)zeta;
             if (!any || r == R(0)) {
-                for (int k = 0; k < ni; ++k)
-                    if (k != e) row[k] = V4{0, 0, 0, 0};
-                fj[s + e] = V4{0, 0, 0, 0};
+                bacc[e] = V4{0, 0, 0, 0};
                 continue;
             }
             if (bo) {
@@ -202,11 +280,21 @@ __global__ void __launch_bounds__(128) bond_pass(BondArgs A) {
                 }
             }
             R U = 0, dU = 0, P = 0;
+            // the cutoff factor of bond e, reused by pair terms with the same cutoff
+            V2 bc{R(-1), R(-1)};
+            if (cached_cut) bc = ((const V2*)A.bcut)[ti * A.T + tj];
             for (int t = ix.x; t < ix.x + ix.y; ++t) {
                 const PairT<R>& PT = terms[t];
                 if (!PT.in_bond_kernel || !(r < PT.rc)) continue;
                 R V, dV;
-                pair_term<R>(PT, r, V, dV);
+                if (PT.smooth && PT.rc == bc.x && PT.rs == bc.y) {
+                    pair_eval<R>(PT.kind, PT.p0, PT.p1, PT.p2, r, V, dV);
+                    const V2 fc = cut[e];
+                    dV = dV * fc.x + V * fc.y;
+                    V = V * fc.x;
+                } else {
+                    pair_term<R>(PT, r, V, dV);
+                }
                 if (PT.group < 0) {
                     U += V;
                     dU += dV;
@@ -218,60 +306,87 @@ __global__ void __launch_bounds__(128) bond_pass(BondArgs A) {
             }
             En += R(0.5) * U;
             // radial part: force on i = +1/2 U' r_hat, on j the opposite
-            const R c = R(0.5) * dU / r;
+            const R c = R(0.5) * dU * i1;
             Fx += c * a.x;
             Fy += c * a.y;
             Fz += c * a.z;
-            fjx = -c * a.x;
-            fjy = -c * a.y;
-            fjz = -c * a.z;
-            W0 += a.x * fjx;
-            W1 += a.y * fjy;
-            W2 += a.z * fjz;
-            W3 += a.y * fjz;
-            W4 += a.x * fjz;
-            W5 += a.x * fjy;
-            // three-body part: F = -(1/2 V f dB/dzeta) grad zeta_ij
-            const R pref = R(0.5) * P * dB;
-            for (int k = 0; k < ni; ++k) {
-                if (k == e) continue;
-                V4 out{0, 0, 0, 0};
-                if (bo && pref != R(0)) {
-                    const V4 gik = geo[k];
-                    if (gik.w < maxbr) {
-                        const TripT<R>& TT = trow[typ[k]];
-                        if (TT.valid) {
-                            V3<R> gj, gk;
-                            const V3<R> b{gik.x, gik.y, gik.z};
-                            if (tersoff_grad<R>(TT, a, r, b, gik.w, gj, gk)) {
-                                const R jx = -pref * gj.x, jy = -pref * gj.y, jz = -pref * gj.z;
-                                const R kx = -pref * gk.x, ky = -pref * gk.y, kz = -pref * gk.z;
-                                fjx += jx;
-                                fjy += jy;
-                                fjz += jz;
-                                Fx -= jx + kx;
-                                Fy -= jy + ky;
-                                Fz -= jz + kz;
-                                W0 += a.x * jx + b.x * kx;
-                                W1 += a.y * jy + b.y * ky;
-                                W2 += a.z * jz + b.z * kz;
-                                W3 += a.y * jz + b.y * kz;
-                                W4 += a.x * jz + b.x * kz;
-                                W5 += a.x * jy + b.x * ky;
-                                out = V4{kx, ky, kz, 0};
-                            }
-                        }
-                    }
-                }
-                row[k] = out;
-            }
-            fj[s + e] = V4{fjx, fjy, fjz, 0};
+            W0 -= a.x * c * a.x;
+            W1 -= a.y * c * a.y;
+            W2 -= a.z * c * a.z;
+            W3 -= a.y * c * a.z;
+            W4 -= a.x * c * a.z;
+            W5 -= a.x * c * a.y;
+            bacc[e] = V4{-c * a.x, -c * a.y, -c * a.z, bo ? R(0.5) * P * dB : R(0)};
         }
     }
-    const auto d0 = group_sum_c<G>(Fx), d1 = group_sum_c<G>(Fy), d2 = group_sum_c<G>(Fz);
-    const auto de = group_sum_c<G>(En);
-    const auto w0 = group_sum_c<G>(W0), w1 = group_sum_c<G>(W1), w2 = group_sum_c<G>(W2);
-    const auto w3 = group_sum_c<G>(W3), w4 = group_sum_c<G>(W4), w5 = group_sum_c<G>(W5);
+    // Three-body part, F = -(1/2 V f dB/dzeta) grad zeta_ij, with the loop over
+    // k outside: for each k the k parts of all bonds e of i are summed over the
+    // group with shuffles, so the force on k from atom i leaves as one record.
+    // The lanes of a warp run to the warp's longest list (empty turns for the
+    // shorter ones) because the shuffles need every lane.
+    const int nloop = (int)__reduce_max_sync(0xffffffffu, (unsigned)ni);
+    for (int k = 0; k < nloop; ++k) {
+        R kx = 0, ky = 0, kz = 0;
+        if (k < ni) {
+            const V4 gik = geo[k];
+            if (gik.w < maxbr) {
+                const int tk = typ[k];
+                V3<R> ub;
+                R i2;
+                unit_of(k, gik, ub, i2);
+                for (int e = lane; e < ni; e += G) {
+                    if (e == k) continue;
+                    V4 be = bacc[e];
+                    const R pref = be.w;
+                    if (pref == R(0)) continue;
+                    const TripT<R>& TT = trip[(ti * A.T + typ[e]) * A.T + tk];
+                    if (!TT.valid) continue;
+                    R f, fp;
+                    if (cached_cut) {
+                        const V2 cc = cut[k];
+                        f = cc.x;
+                        fp = cc.y;
+                    } else {
+                        smooth<R>(gik.w, TT.rc, TT.rs, f, fp);
+                    }
+                    if (f == R(0) && fp == R(0)) continue;
+                    const V4 gij = geo[e];
+                    V3<R> ua, gj, gk;
+                    R i1;
+                    unit_of(e, gij, ua, i1);
+                    tersoff_grad_c<R>(TT, ua, gij.w, i1, ub, gik.w, i2, f, fp, gj, gk);
+                    const R jx = -pref * gj.x, jy = -pref * gj.y, jz = -pref * gj.z;
+                    const R qx = -pref * gk.x, qy = -pref * gk.y, qz = -pref * gk.z;
+                    be.x += jx;
+                    be.y += jy;
+                    be.z += jz;
+                    bacc[e] = be;
+                    kx += qx;
+                    ky += qy;
+                    kz += qz;
+                    Fx -= jx + qx;
+                    Fy -= jy + qy;
+                    Fz -= jz + qz;
+                    W0 += gij.x * jx + gik.x * qx;
+                    W1 += gij.y * jy + gik.y * qy;
+                    W2 += gij.z * jz + gik.z * qz;
+                    W3 += gij.y * jz + gik.y * qz;
+                    W4 += gij.x * jz + gik.x * qz;
+                    W5 += gij.x * jy + gik.x * qy;
+                }
+            }
+        }
+        kx = group_sum<G>(kx);
+        ky = group_sum<G>(ky);
+        kz = group_sum<G>(kz);
+        if (k < ni && lane == k % G) kacc[k] = V4{kx, ky, kz, 0};
+    }
+    // per entry i->x: the force of this atom's bonds on x (j part + k parts)
+    for (int e = lane; e < ni; e += G) {
+        const V4 be = bacc[e], ke = kacc[e];
+        fj[s + e] = V4{be.x + ke.x, be.y + ke.y, be.z + ke.z, 0};
+    }
+    const auto d0 = group_sum_f<G>(Fx), d1 = group_sum_f<G>(Fy), d2 = group_sum_f<G>(Fz);
     if (lane == 0) {
         if (act) {
             if constexpr (sizeof(R) == 4) {
@@ -286,51 +401,39 @@ __global__ void __launch_bounds__(128) bond_pass(BondArgs A) {
                 fc[2] = d2.s;
             }
         }
-        tot[slot][0] = act ? de.fx() : fx_zero();
-        tot[slot][1] = act ? w0.fx() : fx_zero();
-        tot[slot][2] = act ? w1.fx() : fx_zero();
-        tot[slot][3] = act ? w2.fx() : fx_zero();
-        tot[slot][4] = act ? w3.fx() : fx_zero();
-        tot[slot][5] = act ? w4.fx() : fx_zero();
-        tot[slot][6] = act ? w5.fx() : fx_zero();
     }
-    block_totals(tot, AP, A.acc);
+    // energy and virial: warp sums (empty slots hold zeros), exact from there on
+    if (A.acc) {
+        const Fx128 v[7] = {warp_total(En), warp_total(W0), warp_total(W1), warp_total(W2),
+                            warp_total(W3), warp_total(W4), warp_total(W5)};
+        block_totals_publish(v, wsum, &done, A.acc);
+    }
 }
 
 template <typename R, int G>
 __global__ void __launch_bounds__(128) gather_pass(BondArgs A) {
     using V4 = typename Vec4T<R>::T;
     const V4* fj = (const V4*)A.fj;
-    const V4* fk = (const V4*)A.fk;
     const int lane = threadIdx.x % G;
     const int slot = threadIdx.x / G;
-    const int m = blockIdx.x * (blockDim.x / G) + slot;
-    const bool act = m < A.n;
+    const int gslot = A.order ? dealt_slot<G>() : blockIdx.x * (blockDim.x / G) + slot;
+    const bool act = gslot < A.n;
+    const int m = act ? (A.order ? A.order[gslot] : gslot) : 0;
     R Fx = 0, Fy = 0, Fz = 0;
     if (act) {
+        // every neighbour i left the force of its bonds on m in its entry i->m,
+        // the reverse of m's entry m->i
         const int s = A.start[m], nm = A.start[m + 1] - s;
         for (int e = lane; e < nm; e += G) {
-            const int rv = A.rev[s + e];
-            const int i = A.idx[s + e];
-            const int si = A.start[i], ni = A.start[i + 1] - si;
-            const int p = rv - si;
-            const long long tri = A.tri[i];
-            const V4 a = fj[rv];
+            const V4 a = fj[A.rev[s + e]];
             Fx += a.x;
             Fy += a.y;
             Fz += a.z;
-            for (int q = 0; q < ni; ++q) {
-                if (q == p) continue;
-                const V4 b = fk[tri + (long long)q * ni + p];
-                Fx += b.x;
-                Fy += b.y;
-                Fz += b.z;
-            }
         }
     }
-    auto sx = group_sum_c<G>(Fx), sy = group_sum_c<G>(Fy), sz = group_sum_c<G>(Fz);
+    auto sx = group_sum_f<G>(Fx), sy = group_sum_f<G>(Fy), sz = group_sum_f<G>(Fz);
     if (act && lane == 0) {
-        // plus the i part left by the bond pass
+        // plus the part on m as a centre, left by the bond pass
         if constexpr (sizeof(R) == 4) {
             const long long* fc = (const long long*)A.fc + 3 * m;
             sx.f += fc[0];
@@ -352,14 +455,9 @@ int bond_blocks(int n, int G) { return (n + (128 / G) - 1) / (128 / G); }
 
 static void prepare_scratch(pg_context* ctx, int precision) {
     const size_t ne = (size_t)std::max<long long>(ctx->sh_total, 1);
-    const size_t nt = (size_t)std::max<long long>(ctx->sh_tri_total, 1);
-    if (precision == PG_PREC_FP64) {
-        ctx->bo_fj64.resize(2 * ne);  // first half: bond geometry, second half: j parts
-        ctx->bo_fk64.resize(nt);
-    } else {
-        ctx->bo_fj.resize(2 * ne);
-        ctx->bo_fk.resize(nt);
-    }
+    // per short-list entry: bond geometry | force on the partner | k-part sums
+    if (precision == PG_PREC_FP64) ctx->bo_fj64.resize(3 * ne);
+    else ctx->bo_fj.resize(3 * ne);
     ctx->bo_fc.resize(3 * (size_t)std::max(ctx->n, 1));
 }
 
@@ -374,9 +472,11 @@ static BondArgs bond_args(pg_context* ctx, int precision, int flags, bool first_
     A.idx = ctx->sh_idx.p;
     A.off = ctx->sh_off.p;
     A.rev = ctx->sh_rev.p;
-    A.tri = ctx->sh_tri.p;
     A.etype = ctx->sh_type.p;
+    A.order = ctx->sh_order.p;
+    A.n_terms = ctx->n_pair_terms;
     A.index = ctx->d_pair_index.p;
+    A.bcut_uniform = ctx->bcut_uniform ? 1 : 0;
     A.flags = flags;
     A.first_f = first_f;
     const size_t ne = (size_t)std::max<long long>(ctx->sh_total, 1);
@@ -385,17 +485,19 @@ static BondArgs bond_args(pg_context* ctx, int precision, int flags, bool first_
         A.trip = ctx->d_trip.p;
         A.post = ctx->d_post.p;
         A.maxbr = ctx->d_maxbr.p;
+        A.bcut = ctx->d_bcut.p;
         A.geo = ctx->bo_fj64.p;
         A.fj = ctx->bo_fj64.p + ne;
-        A.fk = ctx->bo_fk64.p;
+        A.kacc = ctx->bo_fj64.p + 2 * ne;
     } else {
         A.terms = ctx->d_pair_terms32.p;
         A.trip = ctx->d_trip32.p;
         A.post = ctx->d_post32.p;
         A.maxbr = ctx->d_maxbr32.p;
+        A.bcut = ctx->d_bcut32.p;
         A.geo = ctx->bo_fj.p;
         A.fj = ctx->bo_fj.p + ne;
-        A.fk = ctx->bo_fk.p;
+        A.kacc = ctx->bo_fj.p + 2 * ne;
         A.sep0 = ctx->sh_sep0.p;
         A.disp = ctx->disp32.p;
     }
@@ -437,17 +539,17 @@ void launch_bond_order_impl(pg_context* ctx, int precision, int flags, bool firs
 }
 
 // The two passes on scratch the caller provides instead of the context's
-// buffers (the no-allocation entry point): geo_fj holds 2 records per short-list
-// entry, fk one per triplet slot, fc 3 values per atom, disp (mixed path) one
-// record per atom.  Energy and virial go to acc, forces to out_f (written).
-void launch_bond_order_scratch(pg_context* ctx, int precision, int G, void* geo_fj, void* fk, void* fc, F4* disp,
-                               Fx128* acc, double* out_f) {
+// buffers (the no-allocation entry point): bonds holds 3 records per short-list
+// entry, fc 3 values per atom, disp (mixed path) one record per atom.  Energy
+// and virial go to acc, forces to out_f (written).
+void launch_bond_order_scratch(pg_context* ctx, int precision, int G, void* bonds, void* fc, F4* disp, Fx128* acc,
+                               double* out_f) {
     BondArgs A = bond_args(ctx, precision, PG_WANT_ENERGY | PG_WANT_FORCES, true, acc);
     const size_t ne = (size_t)std::max<long long>(ctx->sh_total, 1);
     const size_t rec = precision == PG_PREC_FP64 ? sizeof(D4) : sizeof(F4);
-    A.geo = geo_fj;
-    A.fj = (char*)geo_fj + ne * rec;
-    A.fk = fk;
+    A.geo = bonds;
+    A.fj = (char*)bonds + ne * rec;
+    A.kacc = (char*)bonds + 2 * ne * rec;
     A.fc = fc;
     A.out_f = out_f;
     auto none = [] {};

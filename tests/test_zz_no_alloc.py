@@ -60,7 +60,7 @@ def test_noalloc_matches_regular_call_twice(precision):
 
 
 def test_noalloc_rejects_systems_beyond_the_static_limit():
-    atoms, calc = _calc(20, "fp64")  # 64000 atoms: about 55 MB of FP64 scratch
+    atoms, calc = _calc(24, "fp64")  # 110592 atoms: about 48 MB of FP64 scratch
     calc.engine.calculate(L.PREC_FP64, energy=True, forces=False)
     st, msg, _, _ = _noalloc(calc, L.PREC_FP64, len(atoms))
     assert st == L.PG_ERR_INVALID
