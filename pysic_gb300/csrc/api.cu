@@ -96,15 +96,16 @@ static void enqueue(pg_context* ctx, int precision, int flags, int G) {
     const bool run_pair = ctx->have_pair_kernel_terms || ctx->ewald || ctx->have_singles;
     const bool run_bond = ctx->have_bond_terms && (wantE || wantF);
     const int Gp = pair_lanes_for(ctx);
-    Fx128* acc = ctx->out_acc.p;
+    FxAcc* acc = ctx->out_acc.p;
     bool first_f = true, first_chi = true;
     auto mark = [&](int k) {
         if (ctx->timing) PG_CUDA(cudaEventRecord(ctx->tev[k], ctx->stream));
     };
     mark(0);
-    // the totals are integers that every kernel adds to: clear them first
-    PG_CUDA(cudaMemsetAsync(acc, 0, sizeof(Fx128) * 8, ctx->stream));
-    if (precision == PG_PREC_MIXED && (run_pair || run_bond)) launch_disp(ctx, nullptr);
+    // the totals are integers that every kernel adds to: clear them first (the
+    // mixed path's displacement pass does it on the way)
+    if (precision == PG_PREC_MIXED && (run_pair || run_bond)) launch_disp(ctx, nullptr, acc);
+    else PG_CUDA(cudaMemsetAsync(acc, 0, sizeof(FxAcc) * 8, ctx->stream));
     if (run_pair) {
         launch_pair_kernel_impl(ctx, precision, flags, first_f, first_chi, Gp, acc);
         if (wantF) first_f = false;
@@ -212,14 +213,14 @@ void evaluate(pg_context* ctx, int precision, int flags) {
 }
 
 static void copy_results(pg_context* ctx, int flags, double* energy, double* forces, double* stress, double* enegs) {
-    Fx128 acc[8] = {};
+    FxAcc acc[8] = {};
     double tot[8] = {0};
     cudaStream_t st = ctx->stream;
     if (energy || stress) PG_CUDA(cudaMemcpyAsync(acc, ctx->out_acc.p, sizeof(acc), cudaMemcpyDeviceToHost, st));
     if (forces && (flags & PG_WANT_FORCES)) ctx->out_f.download(forces, 3 * (size_t)ctx->n, st);
     if (enegs && (flags & PG_WANT_ENEGS)) ctx->out_chi.download(enegs, (size_t)ctx->n, st);
     PG_CUDA(cudaStreamSynchronize(st));
-    for (int c = 0; c < 7; ++c) tot[c] = fx_to_double(acc[c]);
+    for (int c = 0; c < 7; ++c) tot[c] = fx_to_double(fx_from_limbs(acc[c]));
     if (energy && (flags & PG_WANT_ENERGY)) *energy = tot[0];
     if (stress && (flags & PG_WANT_FORCES))
         for (int c = 0; c < 6; ++c) stress[c] = tot[1 + c];

@@ -5,6 +5,7 @@
 #include <stdint.h>
 
 #include <functional>
+#include <utility>
 #include <stdexcept>
 #include <string>
 #include <vector>
@@ -134,6 +135,47 @@ inline PostT<R> cast_post(const PostT<S>& a) {
     return PostT<R>{(R)a.beta, (R)a.eta, a.valid};
 }
 
+// Programmatic dependent launch: a kernel launched with launch_pdl may start
+// while its predecessor in the stream finishes; it runs its prologue (reads of
+// data that the predecessor does not write) and then calls pdl_wait(), which
+// returns once the predecessor has completed and its writes are visible.  A
+// kernel calls pdl_trigger() to let its own dependent start early.  Both are
+// no-ops for kernels launched the ordinary way.
+__device__ __forceinline__ void pdl_wait() { asm volatile("griddepcontrol.wait;" ::: "memory"); }
+__device__ __forceinline__ void pdl_trigger() { asm volatile("griddepcontrol.launch_dependents;" ::: "memory"); }
+
+template <typename... KArgs, typename... Args>
+inline void launch_pdl(void (*kernel)(KArgs...), dim3 grid, dim3 block, cudaStream_t st, Args&&... args) {
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = grid;
+    cfg.blockDim = block;
+    cfg.dynamicSmemBytes = 0;
+    cfg.stream = st;
+    cudaLaunchAttribute at[1];
+    at[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+    at[0].val.programmaticStreamSerializationAllowed = 1;
+    cfg.attrs = at;
+    cfg.numAttrs = 1;
+    PG_CUDA(cudaLaunchKernelEx(&cfg, kernel, std::forward<Args>(args)...));
+}
+
+// Parameters of the single-species Tersoff fast path, by index.
+constexpr int PG_SPEC_MAX_TERMS = 3;
+enum SpecIndex {
+    SP_RC = 0,
+    SP_RS,
+    SP_BETA,
+    SP_ETA,
+    SP_A,
+    SP_C2,
+    SP_D2,
+    SP_C2D2,
+    SP_H,
+    SP_MU,
+    SP_TERMS,  // then p0, p1 of each exponential pair term
+    SP_COUNT = SP_TERMS + 2 * PG_SPEC_MAX_TERMS
+};
+
 struct SingleTerm {
     int kind;
     double eps;
@@ -194,6 +236,10 @@ struct pg_context {
     pg::DevBuf<float2> d_bcut32;
     bool bcut_uniform = false;
     int n_pair_terms = 0;  // records in d_pair_terms
+    // single-species Tersoff fast path (tables.cu): parameters by value
+    bool spec_ok = false;
+    double spec[pg::SP_COUNT] = {};
+    int spec_nterm = 0, spec_bomask = 0;
     pg::DevBuf<pg::SingleTerm> d_single_terms;
     pg::DevBuf<int2> d_single_index;     // per type
 
@@ -256,7 +302,7 @@ struct pg_context {
     // outputs
     pg::DevBuf<double> out_f;     // n x 3
     pg::DevBuf<double> out_chi;   // n
-    pg::DevBuf<pg::Fx128> out_acc;  // energy, virial[6], spare: exact fixed-point totals (fixed.cuh)
+    pg::DevBuf<pg::FxAcc> out_acc;  // energy, virial[6], spare: exact fixed-point totals (fixed.cuh)
 
     // charge relaxation
     pg::DevBuf<double> rq_rate, rq_force, rq_stat;
@@ -294,7 +340,7 @@ CellK cell_kernel_view(const Cell& C);
 void build_neighbor_lists(pg_context* ctx, const double* h_cutoffs);
 void build_short_list(pg_context* ctx);
 void build_full_sep0(pg_context* ctx);
-void launch_disp(pg_context* ctx, const int* skip);
+void launch_disp(pg_context* ctx, const int* skip, FxAcc* zero8 = nullptr);
 void build_allpairs_lists(pg_context* ctx, const double* h_cutoffs);
 void install_neighbor_lists(pg_context* ctx, const int32_t* counts, const int32_t* idx, const int32_t* off);
 
@@ -306,12 +352,12 @@ void fold_tables(pg_context* ctx);
 // (first_*) or added to the per-atom outputs
 int pair_kernel_blocks(int n, int G);
 void launch_pair_kernel_impl(pg_context* ctx, int precision, int flags, bool first_f, bool first_chi, int G,
-                             Fx128* acc);
+                             FxAcc* acc);
 void launch_pair_kernel_skip(pg_context* ctx, int precision, int flags, bool first_f, bool first_chi, int G,
-                             Fx128* acc, const int* skip);
+                             FxAcc* acc, const int* skip);
 
 int bond_blocks(int n, int G);
-void launch_bond_order_impl(pg_context* ctx, int precision, int flags, bool first_f, int G, Fx128* acc,
+void launch_bond_order_impl(pg_context* ctx, int precision, int flags, bool first_f, int G, FxAcc* acc,
                             const std::function<void()>& between);
 void bond_zeta_diag(pg_context* ctx);
 // noalloc.cu: the bond-order passes on static scratch (pg_bond_order_noalloc)
@@ -319,8 +365,8 @@ void bond_order_noalloc(pg_context* ctx, int precision, double* d_forces, double
 
 // ewald.cu
 void ewald_prepare(pg_context* ctx);
-void launch_ewald_kspace(pg_context* ctx, int precision, int flags, bool first_f, bool first_chi, Fx128* acc);
-void launch_ewald_kspace_skip(pg_context* ctx, int precision, int flags, bool first_f, bool first_chi, Fx128* acc,
+void launch_ewald_kspace(pg_context* ctx, int precision, int flags, bool first_f, bool first_chi, FxAcc* acc);
+void launch_ewald_kspace_skip(pg_context* ctx, int precision, int flags, bool first_f, bool first_chi, FxAcc* acc,
                               const int* skip);
 
 // relax.cu

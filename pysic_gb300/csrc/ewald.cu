@@ -104,7 +104,7 @@ struct EwArgs {
     int flags, first_f, first_chi;
     double* out_f;
     double* out_chi;
-    Fx128* acc;           // global energy / virial totals (null: not wanted)
+    FxAcc* acc;           // global energy / virial totals (null: not wanted)
     const int* skip;      // optional device flag: nonzero = do nothing
 };
 
@@ -279,14 +279,14 @@ __global__ void ew_sreduce(EwArgs A) {
             a2 = fx_warp_sum(threadIdx.x < nw ? sq2[threadIdx.x] : fx_zero());
         }
         if (threadIdx.x == 0) {
-            if (A.acc) fx_atomic_add(&A.acc[0], acc);
+            if (A.acc) fx_red(&A.acc[0], acc);
             if (blockIdx.x == 0) {
                 // self and background energies (Potentials.f90:1643-1646)
                 const double q1 = fx_to_double(a1), q2 = fx_to_double(a2);
                 A.Ssum[0] = q1;
                 A.Ssum[1] = q2;
                 const double eb = -(q2 * A.inv_eps_4pi * A.inv_sigma_sqrt_2pi) - q1 * q1 * 0.5 * A.inv_eps_2v * A.sigma2;
-                if (A.acc) fx_atomic_add(&A.acc[0], fx_from_double(eb));
+                if (A.acc) fx_red(&A.acc[0], fx_from_double(eb));
             }
         }
     }
@@ -437,7 +437,7 @@ __global__ void ew_finish(EwArgs A) {
         const int nw = blockDim.x >> 5;
         for (int c = 0; c < 6; ++c) {
             const Fx128 v = fx_warp_sum(threadIdx.x < nw ? sw[threadIdx.x][c] : fx_zero());
-            if (threadIdx.x == 0) fx_atomic_add(&A.acc[1 + c], v);
+            if (threadIdx.x == 0) fx_red(&A.acc[1 + c], v);
         }
     }
 }
@@ -529,7 +529,7 @@ static void ew_launch(pg_context* ctx, EwArgs& A, int prep_blocks, int kred_bloc
     PG_CHECK_LAUNCH();
 }
 
-void launch_ewald_kspace_skip(pg_context* ctx, int precision, int flags, bool first_f, bool first_chi, Fx128* acc,
+void launch_ewald_kspace_skip(pg_context* ctx, int precision, int flags, bool first_f, bool first_chi, FxAcc* acc,
                               const int* skip) {
     const int n = ctx->n;
     int chunks, chunk, splits, sps, prep_blocks, kred_blocks, fin_blocks;
@@ -585,7 +585,7 @@ void launch_ewald_kspace_skip(pg_context* ctx, int precision, int flags, bool fi
     else ew_launch<float>(ctx, A, prep_blocks, kred_blocks, fin_blocks);
 }
 
-void launch_ewald_kspace(pg_context* ctx, int precision, int flags, bool first_f, bool first_chi, Fx128* acc) {
+void launch_ewald_kspace(pg_context* ctx, int precision, int flags, bool first_f, bool first_chi, FxAcc* acc) {
     launch_ewald_kspace_skip(ctx, precision, flags, first_f, first_chi, acc, nullptr);
 }
 

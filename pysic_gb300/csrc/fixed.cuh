@@ -8,10 +8,10 @@
 //   * totals (energy, virial) are signed 128-bit integers in units of 2^-64
 //     (Fx128).  Every FP32 or FP64 term is converted exactly from its bit
 //     pattern, block sums are integer shuffles, and each block adds its sums to
-//     one global accumulator with two 64-bit integer atomics.  Integer addition
-//     is associative, so the total is exact and independent of the order in
-//     which blocks finish: deterministic by construction.  It is rounded to
-//     FP64 once, on the host.
+//     one global accumulator with three 64-bit integer reductions (FxAcc).
+//     Integer addition is associative, so the total is exact and independent
+//     of the order in which blocks finish: deterministic by construction.  It
+//     is rounded to FP64 once, on the host.
 //   * per-atom values of the mixed path (forces, electronegativities) are
 //     signed 64-bit integers in units of 2^-32 (about 2.3e-10).  FP32 lane
 //     partials are converted with rounding to nearest, summed exactly as
@@ -124,12 +124,37 @@ __device__ __forceinline__ Fx128 fx_from_fix(long long v) {
     return r;
 }
 
-// one block's sum into a global total: low word first, its carry into the high word
-__device__ __forceinline__ void fx_atomic_add(Fx128* dst, Fx128 v) {
-    if ((v.lo | (unsigned long long)v.hi) == 0ull) return;
-    const unsigned long long old = atomicAdd(&dst->lo, v.lo);
-    const unsigned long long carry = (old + v.lo < old) ? 1ull : 0ull;
-    atomicAdd((unsigned long long*)&dst->hi, (unsigned long long)v.hi + carry);
+// A global 128-bit total kept as three 64-bit limb sums (bits 0-41, 42-83 and
+// 84-127 of the two's complement value).  A block adds its value with three
+// independent reductions that return nothing, so no thread waits for a round
+// trip and no carry has to be passed between words; every limb sum stays exact
+// for up to 2^22 additions.  fx_from_limbs puts the limbs back together
+// (modulo 2^128, which is exact for any total that fits in 128 bits).
+struct FxAcc {
+    unsigned long long l[3];
+};
+
+__device__ __forceinline__ void fx_red(FxAcc* dst, Fx128 v) {
+    const unsigned long long lo = v.lo, hi = (unsigned long long)v.hi;
+    const unsigned long long m42 = (1ull << 42) - 1ull;
+    const unsigned long long l0 = lo & m42;
+    const unsigned long long l1 = ((lo >> 42) | (hi << 22)) & m42;
+    const unsigned long long l2 = hi >> 20;
+    if (l0) atomicAdd(&dst->l[0], l0);
+    if (l1) atomicAdd(&dst->l[1], l1);
+    if (l2) atomicAdd(&dst->l[2], l2);
+}
+
+__host__ __device__ __forceinline__ Fx128 fx_from_limbs(const FxAcc& a) {
+    // t = l0 + l1 2^42 + l2 2^84 (mod 2^128), with explicit carries
+    const unsigned long long l0 = a.l[0], l1 = a.l[1], l2 = a.l[2];
+    unsigned long long lo = l0, hi = 0ull;
+    const unsigned long long s1lo = l1 << 42, s1hi = l1 >> 22;
+    const unsigned long long t = lo + s1lo;
+    hi += s1hi + (t < lo ? 1ull : 0ull);
+    lo = t;
+    hi += l2 << 20;  // l2 2^84 has no bits below 2^64
+    return Fx128{lo, (long long)hi};
 }
 
 // ---- per-atom 2^-32 fixed point ----

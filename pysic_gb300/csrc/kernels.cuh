@@ -280,7 +280,7 @@ __device__ __forceinline__ void store_sum(double* p, const DSum& v, bool first) 
 // warp of the block to arrive adds all of them to acc.  `done` is a shared
 // counter set to zero before the block's first barrier.
 __device__ __forceinline__ void block_totals_publish(const Fx128 (&v)[7], Fx128 (*wsum)[7], unsigned* done,
-                                                     Fx128* acc) {
+                                                     FxAcc* acc) {
     if (acc == nullptr) return;
     const int wl = threadIdx.x & 31, w = threadIdx.x >> 5, nw = blockDim.x >> 5;
     if (wl == 0) {
@@ -295,7 +295,7 @@ __device__ __forceinline__ void block_totals_publish(const Fx128 (&v)[7], Fx128 
                     const volatile Fx128* q = &wsum[k][c];
                     t = fx_add(t, Fx128{q->lo, q->hi});
                 }
-                fx_atomic_add(&acc[c], t);
+                fx_red(&acc[c], t);
             }
         }
     }

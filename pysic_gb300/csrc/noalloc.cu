@@ -23,7 +23,7 @@
 
 namespace pg {
 
-void launch_bond_order_scratch(pg_context* ctx, int precision, int G, void* bonds, void* fc, F4* disp, Fx128* acc,
+void launch_bond_order_scratch(pg_context* ctx, int precision, int G, void* bonds, void* fc, F4* disp, FxAcc* acc,
                                double* out_f);
 
 namespace {
@@ -48,9 +48,9 @@ void* scratch_address(int device) {
 size_t align256(size_t b) { return (b + 255) & ~(size_t)255; }
 
 // the rounded totals: energy, then the virial (xx, yy, zz, yz, xz, xy)
-__global__ void totals_to_double(const Fx128* __restrict__ acc, double* __restrict__ out) {
+__global__ void totals_to_double(const FxAcc* __restrict__ acc, double* __restrict__ out) {
     const int c = threadIdx.x;
-    if (c < 7) out[c] = fx_to_double(acc[c]);
+    if (c < 7) out[c] = fx_to_double(fx_from_limbs(acc[c]));
 }
 
 }  // namespace
@@ -72,7 +72,7 @@ void bond_order_noalloc(pg_context* ctx, int precision, double* d_forces, double
     const size_t n = (size_t)std::max(ctx->n, 1);
     const size_t ne = (size_t)std::max<long long>(ctx->sh_total, 1);
     const size_t rec = precision == PG_PREC_FP64 ? sizeof(D4) : sizeof(F4);
-    const size_t b_acc = align256(8 * sizeof(Fx128));
+    const size_t b_acc = align256(8 * sizeof(FxAcc));
     const size_t b_disp = align256(n * sizeof(F4));
     const size_t b_fc = align256(3 * n * sizeof(double));
     const size_t b_bonds = align256(3 * ne * rec);
@@ -82,11 +82,11 @@ void bond_order_noalloc(pg_context* ctx, int precision, double* d_forces, double
                                         " bytes of scratch for this system; its static limit is " +
                                         std::to_string((size_t)PG_NOALLOC_SCRATCH_BYTES) + " bytes");
     unsigned char* base = (unsigned char*)scratch_address(ctx->device);
-    Fx128* acc = (Fx128*)base;
+    FxAcc* acc = (FxAcc*)base;
     F4* disp = (F4*)(base + b_acc);
     void* fc = base + b_acc + b_disp;
     void* bonds = base + b_acc + b_disp + b_fc;
-    PG_CUDA(cudaMemsetAsync(acc, 0, sizeof(Fx128) * 8, ctx->stream));
+    PG_CUDA(cudaMemsetAsync(acc, 0, sizeof(FxAcc) * 8, ctx->stream));
     launch_bond_order_scratch(ctx, precision, G, bonds, fc, disp, acc, d_forces);
     totals_to_double<<<1, 32, 0, ctx->stream>>>(acc, d_totals);
     PG_CHECK_LAUNCH();

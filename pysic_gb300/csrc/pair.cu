@@ -35,7 +35,7 @@ struct PairArgs {
     int first_f, first_chi;
     double* out_f;
     double* out_chi;
-    Fx128* acc;       // global energy / virial totals (null: not wanted)
+    FxAcc* acc;       // global energy / virial totals (null: not wanted)
     const int* skip;  // optional device flag: nonzero = do nothing
     const F4* sep0;   // mixed path: bond vectors at list build
     const F4* disp;   // mixed path: displacements since the build (xyz) and FP32 charge (w)
@@ -211,7 +211,7 @@ int pair_kernel_blocks(int n, int G) {
 }
 
 void launch_pair_kernel_skip(pg_context* ctx, int precision, int flags, bool first_f, bool first_chi, int G,
-                             Fx128* acc, const int* skip) {
+                             FxAcc* acc, const int* skip) {
     PairArgs A{};
     A.skip = skip;
     A.n = ctx->n;
@@ -263,7 +263,7 @@ void launch_pair_kernel_skip(pg_context* ctx, int precision, int flags, bool fir
 }
 
 void launch_pair_kernel_impl(pg_context* ctx, int precision, int flags, bool first_f, bool first_chi, int G,
-                             Fx128* acc) {
+                             FxAcc* acc) {
     launch_pair_kernel_skip(ctx, precision, flags, first_f, first_chi, G, acc, nullptr);
 }
 

@@ -147,6 +147,43 @@ void fold_tables(pg_context* ctx) {
     ctx->have_singles = !sterms.empty();
     ctx->have_pair_kernel_terms = pair_kernel_terms;
 
+    // Single-species Tersoff (one type, one triplet, exponential pair terms that
+    // all share the bond-order cutoff): the bond-order kernels take every
+    // parameter as a kernel argument instead of looking tables up per triplet.
+    ctx->spec_ok = false;
+    if (T == 1 && trip[0].valid && post[0].valid && index[0].y >= 1 && index[0].y <= PG_SPEC_MAX_TERMS &&
+        maxbr[0] == trip[0].rc) {
+        const TripT<double>& t0 = trip[0];
+        bool ok = true;
+        int mask = 0;
+        for (int q = 0; q < index[0].y; ++q) {
+            const PairT<double>& pt = terms[(size_t)index[0].x + q];
+            ok = ok && pt.in_bond_kernel && pt.kind == 1 && pt.smooth && pt.rc == t0.rc && pt.rs == t0.rs;
+            if (pt.group >= 0) mask |= 1 << q;
+        }
+        if (ok && mask != 0) {
+            double* v = ctx->spec;
+            v[SP_RC] = t0.rc;
+            v[SP_RS] = t0.rs;
+            v[SP_BETA] = post[0].beta;
+            v[SP_ETA] = post[0].eta;
+            v[SP_A] = t0.a;
+            v[SP_C2] = t0.c2;
+            v[SP_D2] = t0.d2;
+            v[SP_C2D2] = t0.c2d2;
+            v[SP_H] = t0.h;
+            v[SP_MU] = t0.mu;
+            for (int q = 0; q < index[0].y; ++q) {
+                const PairT<double>& pt = terms[(size_t)index[0].x + q];
+                v[SP_TERMS + 2 * q] = pt.p0;
+                v[SP_TERMS + 2 * q + 1] = pt.p1;
+            }
+            ctx->spec_nterm = index[0].y;
+            ctx->spec_bomask = mask;
+            ctx->spec_ok = true;
+        }
+    }
+
     if (terms.empty()) terms.push_back(PairT<double>{});
     if (sterms.empty()) sterms.push_back(SingleTerm{});
     std::vector<PairT<float>> terms32(terms.size());

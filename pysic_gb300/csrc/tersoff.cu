@@ -74,6 +74,9 @@ struct BondArgs {
     int n_terms;        // pair records in terms
     const F4* sep0;     // mixed path: bond vectors at list build
     const F4* disp;     // mixed path: per-atom displacement since the build
+    float spf[SP_COUNT];  // single-species fast path parameters, FP32 copy
+    double spd[SP_COUNT]; // and FP64
+    int spec, spec_nterm, spec_bomask;
     int flags;
     int first_f;
     void* geo;
@@ -81,15 +84,19 @@ struct BondArgs {
     void* kacc;        // per entry i->k: the k parts of i's bonds on k (unstaged atoms' scratch)
     void* fc;          // per atom: i part of the force (FP64, or 2^-32 fixed point in the mixed path)
     double* out_f;
-    Fx128* acc;        // global energy / virial totals (null: not wanted)
+    FxAcc* acc;        // global energy / virial totals (null: not wanted)
     double* zeta_out;
 };
 
 // per-atom displacement since the list build (FP64 difference rounded to FP32)
-// and the FP32 charge, one 16-byte record per atom for the mixed-path kernels
+// and the FP32 charge, one 16-byte record per atom for the mixed-path kernels;
+// block 0 also clears the energy / virial totals (zero8, 8 records; may be null)
+// that the kernels after it add to
 __global__ void disp_pass(int n, const double* __restrict__ pos, const double* __restrict__ pos0,
-                          const double* __restrict__ q, F4* __restrict__ d, const int* skip) {
+                          const double* __restrict__ q, F4* __restrict__ d, const int* skip, FxAcc* zero8) {
+    pdl_trigger();
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (zero8 && i < 8) zero8[i] = FxAcc{{0ull, 0ull, 0ull}};
     if (skip && *skip) return;
     if (i >= n) return;
     d[i] = F4{(float)(pos[3 * i] - pos0[3 * i]), (float)(pos[3 * i + 1] - pos0[3 * i + 1]),
@@ -131,7 +138,9 @@ struct Vec2T<double> {
     using T = double2;
 };
 
-template <typename R, int G>
+// SPEC: single-species Tersoff, every parameter a kernel argument (no table
+// lookups per bond or triplet); the same arithmetic as the table path.
+template <typename R, int G, bool SPEC>
 __global__ void __launch_bounds__(128, sizeof(R) == 4 ? 7 : 4) bond_pass(BondArgs A) {
     using V4 = typename Vec4T<R>::T;
     using V2 = typename Vec2T<R>::T;
@@ -167,6 +176,7 @@ __global__ void __launch_bounds__(128, sizeof(R) == 4 ? 7 : 4) bond_pass(BondArg
         index = sindex;
     }
     if (threadIdx.x == 0) done = 0u;
+    pdl_trigger();
     __syncthreads();
     const int lane = threadIdx.x % G;
     const int slot = threadIdx.x / G;
@@ -176,13 +186,31 @@ __global__ void __launch_bounds__(128, sizeof(R) == 4 ? 7 : 4) bond_pass(BondArg
     const int s = act ? A.start[i] : 0;
     const int ni = act ? A.start[i + 1] - s : 0;
     const bool staged = ni <= CAP;
+    auto SPV = [&](int k) -> R {
+        if constexpr (sizeof(R) == 4) return A.spf[k];
+        else return A.spd[k];
+    };
     V4* geo = staged ? sgeo + slot * CAPP : (V4*)A.geo + s;
     const int* typ = staged ? styp + slot * CAPP : A.etype + s;
     V4* unit = sunit + slot * CAPP;  // staged atoms: unit vector, 1/r
     V2* cut = scut + slot * CAPP;    // staged atoms with uniform cutoffs: f(r), f'(r)
-    const bool cached_cut = staged && A.bcut_uniform;
-    const int ti = act ? A.type[i] : 0;
+    const bool cached_cut = staged && (SPEC || A.bcut_uniform);
+    const int ti = (act && !SPEC) ? A.type[i] : 0;
+    TripT<R> TS{};
+    if constexpr (SPEC)
+        TS = TripT<R>{SPV(SP_A), SPV(SP_C2), SPV(SP_D2), SPV(SP_H), SPV(SP_MU), SPV(SP_RC), SPV(SP_RS), SPV(SP_C2D2), 1};
+    // triplet parameters of (i, j, k) and the partner type of entry k
+    auto trip_of = [&](int tj, int tk) -> const TripT<R>& {
+        if constexpr (SPEC) return TS;
+        else return trip[(ti * A.T + tj) * A.T + tk];
+    };
+    auto type_of = [&](int k) -> int {
+        if constexpr (SPEC) return 0;
+        else return typ[k];
+    };
     V4* fj = (V4*)A.fj;
+    // the displacements (mixed path) and the totals come from the kernel before
+    pdl_wait();
     // geometry of i's bonds in the working precision, and per bond what every
     // triplet through it reuses
     if (act) {
@@ -196,15 +224,21 @@ __global__ void __launch_bounds__(128, sizeof(R) == 4 ? 7 : 4) bond_pass(BondArg
             const V4 g = bond_vector<R>(A, i, s + e, xi, yi, zi);
             geo[e] = g;
             if (staged) {
-                const int te = A.etype[s + e];
-                styp[slot * CAPP + e] = te;
                 const R ir = g.w > R(0) ? rcp_(g.w) : R(0);
                 unit[e] = V4{g.x * ir, g.y * ir, g.z * ir, ir};
-                if (A.bcut_uniform) {
-                    const V2 c = ((const V2*)A.bcut)[ti * A.T + te];
+                if constexpr (SPEC) {
                     R f, fp;
-                    smooth<R>(g.w, c.x, c.y, f, fp);
+                    smooth<R>(g.w, SPV(SP_RC), SPV(SP_RS), f, fp);
                     cut[e] = V2{f, fp};
+                } else {
+                    const int te = A.etype[s + e];
+                    styp[slot * CAPP + e] = te;
+                    if (A.bcut_uniform) {
+                        const V2 c = ((const V2*)A.bcut)[ti * A.T + te];
+                        R f, fp;
+                        smooth<R>(g.w, c.x, c.y, f, fp);
+                        cut[e] = V2{f, fp};
+                    }
                 }
             }
         }
@@ -227,27 +261,35 @@ __global__ void __launch_bounds__(128, sizeof(R) == 4 ? 7 : 4) bond_pass(BondArg
     // in .w the three-body prefactor 1/2 V f dB/dzeta
     V4* bacc = staged ? sbacc + slot * CAPP : fj + s;
     V4* kacc = (V4*)A.kacc + s;  // per bond k: the group's k parts, written once
-    const R maxbr = act ? ((const R*)A.maxbr)[ti] : R(0);
+    R maxbr = R(0);
+    if constexpr (SPEC) maxbr = SPV(SP_RC);
+    else if (act) maxbr = ((const R*)A.maxbr)[ti];
     if (act) {
-        const PostT<R> pp = ((const PostT<R>*)A.post)[ti];
+        PostT<R> pp{};
+        if constexpr (SPEC) pp = PostT<R>{SPV(SP_BETA), SPV(SP_ETA), 1};
+        else pp = ((const PostT<R>*)A.post)[ti];
         for (int e = lane; e < ni; e += G) {
             const V4 gij = geo[e];
             const V3<R> a{gij.x, gij.y, gij.z};
             const R r = gij.w;
-            const int tj = typ[e];
+            const int tj = type_of(e);
             V3<R> ua;
             R i1;
             unit_of(e, gij, ua, i1);
-            const int2 ix = index[ti * A.T + tj];
+            int2 ix = make_int2(0, 0);
             bool any = false, bo = false;
-            for (int t = ix.x; t < ix.x + ix.y; ++t) {
-                const PairT<R>& P = terms[t];
-                if (P.in_bond_kernel && r < P.rc) {
-                    any = true;
-                    bo |= P.group >= 0;
+            if constexpr (SPEC) {
+                any = bo = r < SPV(SP_RC);
+            } else {
+                ix = index[ti * A.T + tj];
+                for (int t = ix.x; t < ix.x + ix.y; ++t) {
+                    const PairT<R>& P = terms[t];
+                    if (P.in_bond_kernel && r < P.rc) {
+                        any = true;
+                        bo |= P.group >= 0;
+                    }
                 }
             }
-            const TripT<R>* trow = trip + (ti * A.T + tj) * A.T;
             // zeta_ij (core_calculate_pair_bond_order_factor, first neighbour loop)
             R zeta = 0, B = 1, dB = 0;
             if ((bo || A.zeta_out) && r != R(0)) {
@@ -255,7 +297,7 @@ __global__ void __launch_bounds__(128, sizeof(R) == 4 ? 7 : 4) bond_pass(BondArg
                     if (k == e) continue;
                     const V4 gik = geo[k];
                     if (!(gik.w < maxbr)) continue;
-                    const TripT<R>& TT = trow[typ[k]];
+                    const TripT<R>& TT = trip_of(tj, type_of(k));
                     if (!TT.valid) continue;
                     R f, fp;
                     if (cached_cut) f = cut[k].x;
@@ -280,9 +322,35 @@ __global__ void __launch_bounds__(128, sizeof(R) == 4 ? 7 : 4) bond_pass(BondArg
                 }
             }
             R U = 0, dU = 0, P = 0;
+            if constexpr (SPEC) {
+                // exponential terms p0 exp(-p1 r) with the bond-order cutoff
+                R f, fp;
+                if (cached_cut) {
+                    const V2 fc = cut[e];
+                    f = fc.x;
+                    fp = fc.y;
+                } else {
+                    smooth<R>(r, SPV(SP_RC), SPV(SP_RS), f, fp);
+                }
+#pragma unroll
+                for (int q = 0; q < PG_SPEC_MAX_TERMS; ++q) {
+                    if (q >= A.spec_nterm) break;
+                    const R p1 = SPV(SP_TERMS + 2 * q + 1);
+                    const R ex = SPV(SP_TERMS + 2 * q) * exp_(-p1 * r);
+                    const R V = ex * f, dV = ex * (fp - p1 * f);
+                    if ((A.spec_bomask >> q) & 1) {
+                        U += V * B;
+                        dU += dV * B;
+                        P += V;
+                    } else {
+                        U += V;
+                        dU += dV;
+                    }
+                }
+            }
             // the cutoff factor of bond e, reused by pair terms with the same cutoff
             V2 bc{R(-1), R(-1)};
-            if (cached_cut) bc = ((const V2*)A.bcut)[ti * A.T + tj];
+            if (!SPEC && cached_cut) bc = ((const V2*)A.bcut)[ti * A.T + tj];
             for (int t = ix.x; t < ix.x + ix.y; ++t) {
                 const PairT<R>& PT = terms[t];
                 if (!PT.in_bond_kernel || !(r < PT.rc)) continue;
@@ -330,7 +398,7 @@ __global__ void __launch_bounds__(128, sizeof(R) == 4 ? 7 : 4) bond_pass(BondArg
         if (k < ni) {
             const V4 gik = geo[k];
             if (gik.w < maxbr) {
-                const int tk = typ[k];
+                const int tk = type_of(k);
                 V3<R> ub;
                 R i2;
                 unit_of(k, gik, ub, i2);
@@ -339,7 +407,7 @@ __global__ void __launch_bounds__(128, sizeof(R) == 4 ? 7 : 4) bond_pass(BondArg
                     V4 be = bacc[e];
                     const R pref = be.w;
                     if (pref == R(0)) continue;
-                    const TripT<R>& TT = trip[(ti * A.T + typ[e]) * A.T + tk];
+                    const TripT<R>& TT = trip_of(type_of(e), tk);
                     if (!TT.valid) continue;
                     R f, fp;
                     if (cached_cut) {
@@ -420,6 +488,7 @@ __global__ void __launch_bounds__(128) gather_pass(BondArgs A) {
     const bool act = gslot < A.n;
     const int m = act ? (A.order ? A.order[gslot] : gslot) : 0;
     R Fx = 0, Fy = 0, Fz = 0;
+    pdl_wait();  // the bond pass's records
     if (act) {
         // every neighbour i left the force of its bonds on m in its entry i->m,
         // the reverse of m's entry m->i
@@ -461,7 +530,7 @@ static void prepare_scratch(pg_context* ctx, int precision) {
     ctx->bo_fc.resize(3 * (size_t)std::max(ctx->n, 1));
 }
 
-static BondArgs bond_args(pg_context* ctx, int precision, int flags, bool first_f, Fx128* acc) {
+static BondArgs bond_args(pg_context* ctx, int precision, int flags, bool first_f, FxAcc* acc) {
     BondArgs A{};
     A.n = ctx->n;
     A.T = std::max(ctx->n_types, 1);
@@ -477,6 +546,13 @@ static BondArgs bond_args(pg_context* ctx, int precision, int flags, bool first_
     A.n_terms = ctx->n_pair_terms;
     A.index = ctx->d_pair_index.p;
     A.bcut_uniform = ctx->bcut_uniform ? 1 : 0;
+    A.spec = ctx->spec_ok ? 1 : 0;
+    A.spec_nterm = ctx->spec_nterm;
+    A.spec_bomask = ctx->spec_bomask;
+    for (int q = 0; q < SP_COUNT; ++q) {
+        A.spd[q] = ctx->spec[q];
+        A.spf[q] = (float)ctx->spec[q];
+    }
     A.flags = flags;
     A.first_f = first_f;
     const size_t ne = (size_t)std::max<long long>(ctx->sh_total, 1);
@@ -510,9 +586,12 @@ static BondArgs bond_args(pg_context* ctx, int precision, int flags, bool first_
 
 template <typename R, int G>
 static void launch_pair(const BondArgs& A, int n, cudaStream_t st, bool forces, const std::function<void()>& between) {
-    bond_pass<R, G><<<bond_blocks(n, G), 128, 0, st>>>(A);
+    // each pass may start while its predecessor drains (programmatic dependent launch)
+    const dim3 grid(bond_blocks(n, G)), block(128);
+    if (A.spec) launch_pdl(bond_pass<R, G, true>, grid, block, st, A);
+    else launch_pdl(bond_pass<R, G, false>, grid, block, st, A);
     between();
-    if (forces) gather_pass<R, G><<<bond_blocks(n, G), 128, 0, st>>>(A);
+    if (forces) launch_pdl(gather_pass<R, G>, grid, block, st, A);
 }
 
 template <typename R>
@@ -527,7 +606,7 @@ static void launch_by_lanes(const BondArgs& A, int n, cudaStream_t st, int G, bo
 }
 
 // `between` runs between the two passes
-void launch_bond_order_impl(pg_context* ctx, int precision, int flags, bool first_f, int G, Fx128* acc,
+void launch_bond_order_impl(pg_context* ctx, int precision, int flags, bool first_f, int G, FxAcc* acc,
                             const std::function<void()>& between) {
     prepare_scratch(ctx, precision);
     BondArgs A = bond_args(ctx, precision, flags, first_f, acc);
@@ -542,7 +621,7 @@ void launch_bond_order_impl(pg_context* ctx, int precision, int flags, bool firs
 // buffers (the no-allocation entry point): bonds holds 3 records per short-list
 // entry, fc 3 values per atom, disp (mixed path) one record per atom.  Energy
 // and virial go to acc, forces to out_f (written).
-void launch_bond_order_scratch(pg_context* ctx, int precision, int G, void* bonds, void* fc, F4* disp, Fx128* acc,
+void launch_bond_order_scratch(pg_context* ctx, int precision, int G, void* bonds, void* fc, F4* disp, FxAcc* acc,
                                double* out_f) {
     BondArgs A = bond_args(ctx, precision, PG_WANT_ENERGY | PG_WANT_FORCES, true, acc);
     const size_t ne = (size_t)std::max<long long>(ctx->sh_total, 1);
@@ -557,17 +636,17 @@ void launch_bond_order_scratch(pg_context* ctx, int precision, int G, void* bond
         launch_by_lanes<double>(A, ctx->n, ctx->stream, G, true, none);
     } else {
         disp_pass<<<(ctx->n + 255) / 256, 256, 0, ctx->stream>>>(ctx->n, ctx->pos.p, ctx->pos0.p, ctx->charge.p, disp,
-                                                                 nullptr);
+                                                                 nullptr, nullptr);
         A.disp = disp;
         launch_by_lanes<float>(A, ctx->n, ctx->stream, G, true, none);
     }
     PG_CHECK_LAUNCH();
 }
 
-void launch_disp(pg_context* ctx, const int* skip) {
+void launch_disp(pg_context* ctx, const int* skip, FxAcc* zero8) {
     ctx->disp32.resize((size_t)std::max(ctx->n, 1));
     disp_pass<<<(ctx->n + 255) / 256, 256, 0, ctx->stream>>>(ctx->n, ctx->pos.p, ctx->pos0.p, ctx->charge.p, ctx->disp32.p,
-                                                                 skip);
+                                                                 skip, zero8);
     PG_CHECK_LAUNCH();
     ctx->launches++;
 }
@@ -578,7 +657,7 @@ void bond_zeta_diag(pg_context* ctx) {
     ctx->bo_zeta.zero(ctx->stream);
     BondArgs A = bond_args(ctx, PG_PREC_FP64, PG_WANT_ENERGY, true, nullptr);
     A.zeta_out = ctx->bo_zeta.p;
-    bond_pass<double, 8><<<bond_blocks(ctx->n, 8), 128, 0, ctx->stream>>>(A);
+    bond_pass<double, 8, false><<<bond_blocks(ctx->n, 8), 128, 0, ctx->stream>>>(A);
     PG_CHECK_LAUNCH();
     PG_CUDA(cudaStreamSynchronize(ctx->stream));
 }

@@ -49,7 +49,11 @@ int main(){
     for(int k=0;k<50;++k){ float x=(float)(u(g)*1000); a=fx_add(a,fx_from_float(x)); s+=x; long long f=fix_from_float(x); fs+=f; b=fx_add(b,fx_from_fix(f)); }
     double d=fx_to_double(a); if (std::fabs(d-(double)s)>1e-12*std::fabs((double)s)+1e-15){if(bad++<5)printf("fx %.17g %.17Lg\n",d,s);}
     double e=fx_to_double(b), e2=(double)((long double)fs/4294967296.0L); if (std::fabs(e-e2)>1e-12*std::fabs(e2)){if(bad++<5)printf("fxf %.17g %.17g\n",e,e2);}
-    Fx128 acc=fx_zero(); Fx128 m=fx_from_double(-d); fx_atomic_add(&acc,a); fx_atomic_add(&acc,m); if (std::fabs(fx_to_double(acc))>1e-9){if(bad++<5)printf("atom %.17g\n",fx_to_double(acc));}
+    FxAcc acc{{0,0,0}}; Fx128 m=fx_from_double(-d); fx_red(&acc,a); fx_red(&acc,m); fx_red(&acc,b); fx_red(&acc,fx_neg(b));
+    if (std::fabs(fx_to_double(fx_from_limbs(acc)))>1e-9){if(bad++<5)printf("limbs %.17g\n",fx_to_double(fx_from_limbs(acc)));}
+    FxAcc acc2{{0,0,0}}; Fx128 ref=fx_zero();
+    for(int k=0;k<40;++k){ Fx128 v=fx_from_double(u(g)*std::pow(10.0,(int)(g()%20)-6)); fx_red(&acc2,v); ref=fx_add(ref,v); }
+    Fx128 got=fx_from_limbs(acc2); if(got.lo!=ref.lo||got.hi!=ref.hi){if(bad++<5)printf("limbsum mismatch\n");}
   }
   printf("nan: %g %g %g\n", fix_to_double(fix_from_float(NAN)), fx_to_double(fx_from_double(INFINITY)), fx_to_double(fx_from_float(-INFINITY)));
   printf("bad=%ld\n",bad);

@@ -114,6 +114,40 @@ def test_tersoff_fp64_parity(lanes):
     _check_fp64(W.diamond_si(3, seed=11), W.tersoff_si_potentials(), lanes=lanes)
 
 
+def _two_species_tersoff():
+    """Silicon parameters on two element labels: the kernels take their table
+    path (two atom types) instead of the single-species fast path, for the
+    same physics."""
+    p = W.TERSOFF_SI
+    rc, margin = p["R"] + p["D"], 2.0 * p["D"]
+    els = ["Si", "Ge"]
+    triples = [[a, b, c] for a in els for b in els for c in els]
+    pairs = [["Si", "Si"], ["Si", "Ge"], ["Ge", "Ge"]]
+    bo = pysic.BondOrderParameters("tersoff", cutoff=rc, cutoff_margin=margin, symbols=triples,
+                                   parameters=[[p["beta"], p["n"]], [0.0, p["c"], p["d"], p["h"], 3.0]])
+    crd = pysic.Coordinator([bo])
+    rep = pysic.Potential("exponential", symbols=pairs, parameters=[p["A"], p["lambda1"]], cutoff=rc,
+                          cutoff_margin=margin)
+    att = pysic.Potential("exponential", symbols=pairs, parameters=[-p["B"], p["lambda2"]], cutoff=rc,
+                          cutoff_margin=margin, coordinator=crd)
+    return [rep, att]
+
+
+@pytest.mark.parametrize("lanes", [4, 8])
+def test_tersoff_table_path_matches_fast_path(lanes):
+    atoms = W.diamond_si(3, seed=14)
+    mixed_atoms = atoms.copy()
+    symbols = ["Si" if k % 3 else "Ge" for k in range(len(atoms))]
+    mixed_atoms = pysic.Atoms(symbols, atoms.get_positions(), cell=atoms.get_cell(), pbc=atoms.get_pbc())
+    ref, got = _check_fp64(mixed_atoms, _two_species_tersoff(), lanes=lanes)
+    fast = engine_all(atoms, W.tersoff_si_potentials(), precision="fp64", lanes=lanes)
+    assert got["energy"] == pytest.approx(fast["energy"], rel=1e-12)
+    assert np.abs(got["forces"] - fast["forces"]).max() < 1e-10
+    mixed = engine_all(mixed_atoms, _two_species_tersoff(), precision="mixed", lanes=lanes)
+    assert abs(mixed["energy"] - got["energy"]) / len(atoms) < 1e-5
+    assert np.abs(mixed["forces"] - got["forces"]).max() < 1e-4
+
+
 def test_tersoff_mixed_accuracy_4096():
     atoms = W.diamond_si(8, seed=12)
     pots = W.tersoff_si_potentials()
