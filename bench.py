@@ -67,6 +67,7 @@ def peaks():
 
 def profile_traffic(kernel, workload_name):
     """dram bytes per launch from the committed ncu summary, if there is one."""
+    kernel = {"kspace": "ew_field", "pair": "pair_kernel"}.get(kernel, kernel)
     path = os.path.join(ROOT, "profiles", "{0}_{1}.md".format(kernel, workload_name))
     try:
         for line in open(path):

@@ -130,30 +130,37 @@ static void enqueue(pg_context* ctx, int precision, int flags, int G) {
     mark(5);
 }
 
-// pick the lanes-per-atom tile of the bond-order kernels by timing each
+// Pick the lanes-per-atom tile of the bond-order kernels: each candidate is
+// timed over several single evaluations (device events around each) and
+// judged by its fastest one, so that host launch jitter does not decide.
 static int autotune_lanes(pg_context* ctx, int precision, int flags) {
     const int options[4] = {4, 8, 16, 32};
-    cudaEvent_t e0, e1;
-    PG_CUDA(cudaEventCreate(&e0));
-    PG_CUDA(cudaEventCreate(&e1));
+    constexpr int REPS = 6;
+    cudaEvent_t ev[REPS + 1];
+    for (auto& e : ev) PG_CUDA(cudaEventCreate(&e));
     int best = 8;
     float best_ms = 1e30f;
     for (int o = 0; o < 4; ++o) {
         const int G = options[o];
         enqueue(ctx, precision, flags, G);  // warm-up
-        PG_CUDA(cudaEventRecord(e0, ctx->stream));
-        for (int r = 0; r < 3; ++r) enqueue(ctx, precision, flags, G);
-        PG_CUDA(cudaEventRecord(e1, ctx->stream));
-        PG_CUDA(cudaEventSynchronize(e1));
-        float ms = 0;
-        PG_CUDA(cudaEventElapsedTime(&ms, e0, e1));
-        if (ms < best_ms) {
-            best_ms = ms;
+        for (int r = 0; r < REPS; ++r) {
+            PG_CUDA(cudaEventRecord(ev[r], ctx->stream));
+            enqueue(ctx, precision, flags, G);
+        }
+        PG_CUDA(cudaEventRecord(ev[REPS], ctx->stream));
+        PG_CUDA(cudaEventSynchronize(ev[REPS]));
+        float fastest = 1e30f;
+        for (int r = 0; r < REPS; ++r) {
+            float ms = 0;
+            PG_CUDA(cudaEventElapsedTime(&ms, ev[r], ev[r + 1]));
+            fastest = std::min(fastest, ms);
+        }
+        if (fastest < best_ms) {
+            best_ms = fastest;
             best = G;
         }
     }
-    cudaEventDestroy(e0);
-    cudaEventDestroy(e1);
+    for (auto& e : ev) cudaEventDestroy(e);
     return best;
 }
 
