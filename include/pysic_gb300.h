@@ -49,6 +49,7 @@ extern "C" {
 #define PG_WANT_ENEGS 4   /* electronegativities */
 
 typedef struct pg_context pg_context;
+typedef struct pg_mlp pg_mlp;
 
 /* Thread-local message of the last failing call ("" if none). */
 const char* pg_last_error(void);
@@ -189,6 +190,34 @@ int pg_get_stream(pg_context* ctx, void** stream);
  *    time race on it and must be ordered by the caller. */
 #define PG_NOALLOC_SCRATCH_BYTES (32u << 20)
 int pg_bond_order_noalloc(pg_context* ctx, int32_t precision, double* d_forces, double* d_totals);
+
+/* ---- learned warm start for charge relaxation ------------------------------
+ * No counterpart in the reference, whose ChargeRelaxation starts from the
+ * current charges (pysic/charges/relaxation.py:394-450).
+ *
+ * pg_descriptors: per atom, n_types x n_gauss radial features
+ *   sum_j exp(-(r_ij - mu_k)^2 / (2 width^2)) (1 + cos(pi r_ij / cutoff)) / 2 over
+ *   neighbours j of each type with r_ij < cutoff, mu_k evenly spaced on [r0, r1];
+ *   out is N x (n_types * n_gauss) floats, type-major.  Needs lists at least as
+ *   long as cutoff (built by pg_generate_neighbor_lists / _all_pairs_lists).
+ * pg_mlp_*: a network n_in -> n_h1 -> n_h2 -> 1 with tanh activations, BF16
+ *   weights and FP32 arithmetic, trained on the GPU (mean squared error, Adam).
+ *   Parameters are FP32 in the order W1 (n_h1 x n_in, row-major), b1, W2
+ *   (n_h2 x n_h1), b2, w3 (n_h2), b3.  pg_mlp_gradients returns the loss and
+ *   its gradient for the given samples (no update), for gradient checks. */
+int pg_descriptors(pg_context* ctx, int32_t n_gauss, double r0, double r1, double width, double cutoff,
+                   float* out);
+int pg_mlp_create(pg_mlp** mlp, int32_t n_in, int32_t n_h1, int32_t n_h2, int32_t device);
+int pg_mlp_destroy(pg_mlp* mlp);
+int pg_mlp_param_count(pg_mlp* mlp, int64_t* count);
+int pg_mlp_set_params(pg_mlp* mlp, const float* params, int64_t count);
+int pg_mlp_get_params(pg_mlp* mlp, float* params, int64_t count);
+int pg_mlp_add_samples(pg_mlp* mlp, const float* x, const float* y, int64_t n);
+int pg_mlp_clear_samples(pg_mlp* mlp);
+int pg_mlp_train(pg_mlp* mlp, int32_t epochs, int32_t batch, float learning_rate, uint64_t seed,
+                 float* epoch_loss);
+int pg_mlp_gradients(pg_mlp* mlp, const float* x, const float* y, int64_t n, float* grad, double* loss);
+int pg_mlp_predict(pg_mlp* mlp, const float* x, int64_t n, float* y);
 
 /* Kernel launches issued by the last pg_device_evaluate / pg_calculate. */
 int pg_last_launch_count(pg_context* ctx, int32_t* launches);

@@ -34,6 +34,7 @@ _c_double_p = ctypes.POINTER(ctypes.c_double)
 _c_int_p = ctypes.POINTER(ctypes.c_int32)
 _c_u64_p = ctypes.POINTER(ctypes.c_uint64)
 _c_i64_p = ctypes.POINTER(ctypes.c_int64)
+_c_float_p = ctypes.POINTER(ctypes.c_float)
 _ctx = ctypes.c_void_p
 
 _SIGNATURES = {
@@ -81,6 +82,21 @@ _SIGNATURES = {
     "pg_set_kernel_timing": (ctypes.c_int, [_ctx, ctypes.c_int32]),
     "pg_get_kernel_times": (ctypes.c_int, [_ctx, ctypes.POINTER(ctypes.c_float)]),
     "pg_set_graphs": (ctypes.c_int, [_ctx, ctypes.c_int32]),
+    "pg_descriptors": (ctypes.c_int, [_ctx, ctypes.c_int32, ctypes.c_double, ctypes.c_double, ctypes.c_double,
+                                      ctypes.c_double, _c_float_p]),
+    "pg_mlp_create": (ctypes.c_int, [ctypes.POINTER(ctypes.c_void_p), ctypes.c_int32, ctypes.c_int32,
+                                     ctypes.c_int32, ctypes.c_int32]),
+    "pg_mlp_destroy": (ctypes.c_int, [ctypes.c_void_p]),
+    "pg_mlp_param_count": (ctypes.c_int, [ctypes.c_void_p, _c_i64_p]),
+    "pg_mlp_set_params": (ctypes.c_int, [ctypes.c_void_p, _c_float_p, ctypes.c_int64]),
+    "pg_mlp_get_params": (ctypes.c_int, [ctypes.c_void_p, _c_float_p, ctypes.c_int64]),
+    "pg_mlp_add_samples": (ctypes.c_int, [ctypes.c_void_p, _c_float_p, _c_float_p, ctypes.c_int64]),
+    "pg_mlp_clear_samples": (ctypes.c_int, [ctypes.c_void_p]),
+    "pg_mlp_train": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int32, ctypes.c_int32, ctypes.c_float, ctypes.c_uint64,
+                                    _c_float_p]),
+    "pg_mlp_gradients": (ctypes.c_int, [ctypes.c_void_p, _c_float_p, _c_float_p, ctypes.c_int64, _c_float_p,
+                                        _c_double_p]),
+    "pg_mlp_predict": (ctypes.c_int, [ctypes.c_void_p, _c_float_p, ctypes.c_int64, _c_float_p]),
 }
 
 _lib = None
@@ -115,6 +131,10 @@ def check(status):
 
 def dptr(a):
     return a.ctypes.data_as(_c_double_p)
+
+
+def fptr(a):
+    return a.ctypes.data_as(_c_float_p)
 
 
 def iptr(a):

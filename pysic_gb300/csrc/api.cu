@@ -594,6 +594,95 @@ int pg_bond_order_noalloc(pg_context* ctx, int32_t precision, double* d_forces, 
     });
 }
 
+int pg_descriptors(pg_context* ctx, int32_t n_gauss, double r0, double r1, double width, double cutoff,
+                   float* out) {
+    return guarded([&] {
+        check_ctx(ctx);
+        use_device(ctx);
+        pg::require(out != nullptr, PG_ERR_INVALID, "null output pointer");
+        pg::descriptors(ctx, n_gauss, r0, r1, width, cutoff, out);
+    });
+}
+
+static void check_mlp(pg_mlp* m) {
+    pg::require(m != nullptr, PG_ERR_INVALID, "null network");
+    PG_CUDA(cudaSetDevice(m->device));
+}
+
+int pg_mlp_create(pg_mlp** mlp, int32_t n_in, int32_t n_h1, int32_t n_h2, int32_t device) {
+    return guarded([&] {
+        pg::require(mlp != nullptr, PG_ERR_INVALID, "null output pointer");
+        *mlp = nullptr;
+        pg::mlp_create(mlp, n_in, n_h1, n_h2, device);
+    });
+}
+
+int pg_mlp_destroy(pg_mlp* mlp) {
+    return guarded([&] {
+        if (mlp) {
+            cudaSetDevice(mlp->device);
+            delete mlp;
+        }
+    });
+}
+
+int pg_mlp_param_count(pg_mlp* mlp, int64_t* count) {
+    return guarded([&] {
+        check_mlp(mlp);
+        *count = mlp->n_params;
+    });
+}
+
+int pg_mlp_set_params(pg_mlp* mlp, const float* params, int64_t count) {
+    return guarded([&] {
+        check_mlp(mlp);
+        pg::mlp_set_params(mlp, params, count);
+    });
+}
+
+int pg_mlp_get_params(pg_mlp* mlp, float* params, int64_t count) {
+    return guarded([&] {
+        check_mlp(mlp);
+        pg::mlp_get_params(mlp, params, count);
+    });
+}
+
+int pg_mlp_add_samples(pg_mlp* mlp, const float* x, const float* y, int64_t n) {
+    return guarded([&] {
+        check_mlp(mlp);
+        pg::mlp_add_samples(mlp, x, y, n);
+    });
+}
+
+int pg_mlp_clear_samples(pg_mlp* mlp) {
+    return guarded([&] {
+        check_mlp(mlp);
+        pg::mlp_clear_samples(mlp);
+    });
+}
+
+int pg_mlp_train(pg_mlp* mlp, int32_t epochs, int32_t batch, float learning_rate, uint64_t seed,
+                 float* epoch_loss) {
+    return guarded([&] {
+        check_mlp(mlp);
+        pg::mlp_train(mlp, epochs, batch, learning_rate, seed, epoch_loss);
+    });
+}
+
+int pg_mlp_gradients(pg_mlp* mlp, const float* x, const float* y, int64_t n, float* grad, double* loss) {
+    return guarded([&] {
+        check_mlp(mlp);
+        pg::mlp_gradients(mlp, x, y, n, grad, loss);
+    });
+}
+
+int pg_mlp_predict(pg_mlp* mlp, const float* x, int64_t n, float* y) {
+    return guarded([&] {
+        check_mlp(mlp);
+        pg::mlp_predict(mlp, x, n, y);
+    });
+}
+
 int pg_set_kernel_timing(pg_context* ctx, int32_t enable) {
     return guarded([&] {
         check_ctx(ctx);

@@ -1,6 +1,7 @@
 // common.cuh -- shared types of the GB300 engine: device buffers, the engine
 // context, interaction tables and error handling.
 #pragma once
+#include <cuda_bf16.h>
 #include <cuda_runtime.h>
 #include <stdint.h>
 
@@ -263,6 +264,8 @@ struct pg_context {
 
     // neighbour lists: full list (CSR) and the short list of bond-order terms
     bool have_list = false;
+    double list_min_cutoff = 0.0;   // smallest per-atom list radius (0: unknown)
+    pg::DevBuf<float> mlp_desc;     // descriptors of the warm-start network
     double skin = 0.5;
     pg::DevBuf<int> nb_start, nb_idx, nb_off;  // nb_off: 3 per entry
     pg::DevBuf<int> nb_g0;                     // per atom: entries coming from lower-index atoms
@@ -330,6 +333,25 @@ struct pg_context {
     }
 };
 
+// The warm-start network (mlp.cu).
+struct pg_mlp {
+    int device = 0;
+    int n_in = 0, n_h1 = 0, n_h2 = 0;
+    long long n_params = 0;
+    cudaStream_t stream = nullptr;
+    pg::DevBuf<float> w, m, v, grad;   // FP32 master, Adam moments, gradient
+    pg::DevBuf<__nv_bfloat16> wb;      // BF16 copy read by the forward pass
+    pg::DevBuf<float> x, y;            // training samples
+    long long n_samples = 0;
+    pg::DevBuf<int> order;             // sample order of the current epoch
+    pg::DevBuf<float> h1, h2, out, dz1, dz2, dy, lpart;  // per-batch activations
+    pg::DevBuf<float> px, py;          // prediction scratch
+    long long step = 0;
+    ~pg_mlp() {
+        if (stream) cudaStreamDestroy(stream);
+    }
+};
+
 namespace pg {
 
 // Fortran-style build of the cell arrays from the row-major cell and inverse.
@@ -368,6 +390,17 @@ void ewald_prepare(pg_context* ctx);
 void launch_ewald_kspace(pg_context* ctx, int precision, int flags, bool first_f, bool first_chi, FxAcc* acc);
 void launch_ewald_kspace_skip(pg_context* ctx, int precision, int flags, bool first_f, bool first_chi, FxAcc* acc,
                               const int* skip);
+
+// mlp.cu: descriptors and the warm-start network (struct pg_mlp)
+void descriptors(pg_context* ctx, int n_gauss, double r0, double r1, double width, double cutoff, float* out);
+void mlp_create(pg_mlp** out, int n_in, int n_h1, int n_h2, int device);
+void mlp_set_params(pg_mlp* M, const float* params, long long n);
+void mlp_get_params(pg_mlp* M, float* params, long long n);
+void mlp_add_samples(pg_mlp* M, const float* x, const float* y, long long n);
+void mlp_clear_samples(pg_mlp* M);
+void mlp_train(pg_mlp* M, int epochs, int batch, float lr, unsigned long long seed, float* epoch_loss);
+void mlp_gradients(pg_mlp* M, const float* x, const float* y, long long n, float* grad, double* loss);
+void mlp_predict(pg_mlp* M, const float* x, long long n, float* y);
 
 // relax.cu
 void relax_charges(pg_context* ctx, int precision, int n_steps, double dt, double inertia, double friction,

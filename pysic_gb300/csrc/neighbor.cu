@@ -583,6 +583,8 @@ void build_neighbor_lists(pg_context* ctx, const double* h_cutoffs) {
     double max_cut = 0.0;
     for (int i = 0; i < n; ++i)
         if (i == 0 || h_cutoffs[i] > max_cut) max_cut = h_cutoffs[i];
+    // every atom's list holds all partners closer than its own cutoff
+    ctx->list_min_cutoff = n > 0 ? *std::min_element(h_cutoffs, h_cutoffs + n) : 0.0;
     int sp[3];
     optimal_splitting(ctx->cell, max_cut, sp);
     for (int a = 0; a < 3; ++a)
@@ -711,6 +713,7 @@ void build_allpairs_lists(pg_context* ctx, const double* h_cutoffs) {
     cudaStream_t st = ctx->stream;
     double mc = 0.0;
     for (int i = 0; i < n; ++i) mc = std::max(mc, h_cutoffs[i]);
+    ctx->list_min_cutoff = n > 0 ? *std::min_element(h_cutoffs, h_cutoffs + n) : 0.0;
     const Cell& Cc = ctx->cell;
     int ni[3];
     for (int i = 0; i < 3; ++i) {
@@ -761,6 +764,7 @@ void build_allpairs_lists(pg_context* ctx, const double* h_cutoffs) {
 
 void install_neighbor_lists(pg_context* ctx, const int32_t* counts, const int32_t* idx, const int32_t* off) {
     const int n = ctx->n;
+    ctx->list_min_cutoff = 0.0;  // unknown reach
     std::vector<int> start(n + 1, 0);
     for (int i = 0; i < n; ++i) {
         require(counts[i] >= 0, PG_ERR_INVALID, "negative neighbour count");

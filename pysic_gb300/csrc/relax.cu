@@ -16,6 +16,7 @@
 // flag and the statistics once per chunk.  Convergence statistics and charge
 // sums are kept in FP64.
 #include <algorithm>
+#include <cmath>
 #include <vector>
 
 #include "common.cuh"
@@ -102,6 +103,9 @@ __global__ void rx_force(RxArgs A) {
     if (i < A.n) {
         f = A.chi[i] - A.stat[2];
         A.force[i] = f;
+        // a non-finite force must not vanish in fmax (which drops NaN): it
+        // becomes +inf, so the stop test sees it and the loop ends as diverged
+        if (!isfinite(f)) f = __longlong_as_double(0x7ff0000000000000ll);
         if (!INIT) A.rate[i] = (A.rate[i] + f * 0.5 * A.inv_m * A.dt) / (1.0 + 0.5 * A.friction * A.dt);
     }
     sm[threadIdx.x] = f;
@@ -125,7 +129,9 @@ __global__ void rx_stop(RxArgs A) {
         A.flag[1] = steps;
         A.stat[0] = e;
         A.stat[1] = dq;
-        if (!(e > A.tol) || steps >= A.n_steps) A.flag[0] = 1;
+        // stop on convergence, on the step limit, or when the error is no
+        // longer a finite number (diverging dynamics)
+        if (e <= A.tol || steps >= A.n_steps || !isfinite(e)) A.flag[0] = 1;
     }
 }
 
@@ -218,7 +224,9 @@ void relax_charges(pg_context* ctx, int precision, int n_steps, double dt, doubl
     *steps = h_flag[1];
     *error = h_stat[0];
     *max_dq = h_stat[1];
-    if (h_flag[1] >= n_steps && h_stat[0] > tolerance)
+    if (!std::isfinite(h_stat[0]))
+        throw Error(PG_ERR_NOT_CONVERGED, "charge relaxation diverged (non-finite electronegativity differences)");
+    if (!(h_stat[0] <= tolerance))
         throw Error(PG_ERR_NOT_CONVERGED, "charge relaxation reached its step limit before the tolerance");
 }
 

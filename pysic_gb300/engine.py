@@ -189,6 +189,13 @@ class Engine:
         L.check(self.lib.pg_last_launch_count(self.ctx, ctypes.byref(v)))
         return v.value
 
+    def descriptors(self, n_types, n_gauss, r0, r1, width, cutoff):
+        """Per-atom radial descriptors (n_types * n_gauss floats per atom)."""
+        out = np.zeros((self.n, n_types * n_gauss), dtype=np.float32)
+        L.check(self.lib.pg_descriptors(self.ctx, int(n_gauss), float(r0), float(r1), float(width), float(cutoff),
+                                        L.fptr(out)))
+        return out
+
     def set_kernel_timing(self, enable):
         L.check(self.lib.pg_set_kernel_timing(self.ctx, 1 if enable else 0))
 

@@ -29,8 +29,9 @@ class ChargeRelaxation:
         "optimize": ["maximum number of optimization steps", "convergence tolerance"],
     }
 
-    def __init__(self, relaxation="dynamic", calculator=None, parameters=None, atoms=None):
+    def __init__(self, relaxation="dynamic", calculator=None, parameters=None, atoms=None, warm_start=None):
         self.calculator = None
+        self.warm_start = warm_start  # a trained mlp.ChargeNetwork, or None
         self.set_relaxation(relaxation)
         self.set_calculator(calculator)
         self.set_parameters(parameters)
@@ -42,6 +43,14 @@ class ChargeRelaxation:
         self.last_error = None
         self.last_max_dq = None
         self.last_converged = None
+        self.last_warm_start_seconds = 0.0
+
+    def set_warm_start(self, network):
+        """Start the 'dynamic' relaxation from the charges a trained
+        ChargeNetwork predicts (None: from the current charges, as the
+        reference does).  The relaxation itself is unchanged and runs to the
+        same tolerance."""
+        self.warm_start = network
 
     def __eq__(self, other):
         try:
@@ -152,11 +161,23 @@ class ChargeRelaxation:
             p = self.parameters
             if self.charge_rates is None:
                 self.charge_rates = np.zeros(len(atoms))
+            if self.warm_start is not None:
+                import time
+
+                t0 = time.perf_counter()
+                charges = self.warm_start.predict_charges(calc, total_charge=float(np.sum(charges)))
+                self._set(atoms, charges)
+                self.charge_rates = np.zeros(len(atoms))
+                self.last_warm_start_seconds = time.perf_counter() - t0
             calc.set_core()
             prec = calc._prec() if precision is None else precision
             r = calc.engine.relax_charges(prec, int(p["n_steps"]), p["timestep"], p["inertia"], p["friction"],
                                           p["tolerance"], self.charge_rates)
             charges = r["charges"]
+            # the engine's own copy of the charges is now the relaxed one
+            pushed = getattr(calc, "_pushed", None)
+            if pushed is not None:
+                pushed["charges"] = np.array(charges, dtype=np.float64)
             self.charge_rates = r["rates"]
             self.last_steps = r["steps"]
             self.last_error = r["error"]

@@ -96,45 +96,57 @@ def nacl_potentials(A=1000.0, rho=0.30, C=10.0, cutoff=10.0, sigma=2.5, real_cut
 
 def random_box(symbols, density_per_a3, min_dist, seed, max_tries=200000):
     """Uniform random positions in a cubic periodic box with rejection below
-    min_dist (minimum image)."""
+    min_dist (minimum image): random sequential addition, with candidates
+    drawn in batches and tested against a cell grid, and the candidates of a
+    batch accepted in draw order."""
     n = len(symbols)
     L = (n / density_per_a3) ** (1.0 / 3.0)
     rng = np.random.default_rng(seed)
+    md2 = min_dist * min_dist
+    nc = max(1, int(L // min_dist))
+    cw = L / nc
+    K = int(max(4, math.ceil(3.0 * density_per_a3 * cw ** 3) + 2))  # slots per grid cell, grown on demand
+    occ = np.full((nc, nc, nc, K), -1, dtype=np.int64)
+    cnt = np.zeros((nc, nc, nc), dtype=np.int64)
+    offs = np.array([[a, b, c] for a in (-1, 0, 1) for b in (-1, 0, 1) for c in (-1, 0, 1)])
+    if nc < 3:  # every cell is a neighbour of every other: one shared cell list
+        offs = np.array([[a, b, c] for a in range(nc) for b in range(nc) for c in range(nc)])
     pos = np.zeros((n, 3))
     placed = 0
     tries = 0
-    # cell grid for the rejection test
-    nc = max(1, int(L // min_dist))
-    grid = {}
-    cw = L / nc
     while placed < n:
-        tries += 1
         if tries > max_tries * max(1, n // 1000):
             raise RuntimeError("random packing failed")
-        p = rng.uniform(0.0, L, 3)
-        c = tuple((p // cw).astype(int) % nc)
-        ok = True
-        for dx in (-1, 0, 1):
-            for dy in (-1, 0, 1):
-                for dz in (-1, 0, 1):
-                    key = ((c[0] + dx) % nc, (c[1] + dy) % nc, (c[2] + dz) % nc)
-                    for q in grid.get(key, ()):
-                        d = pos[q] - p
-                        d -= L * np.round(d / L)
-                        if d @ d < min_dist * min_dist:
-                            ok = False
-                            break
-                    if not ok:
-                        break
-                if not ok:
-                    break
-            if not ok:
-                break
-        if not ok:
+        m = int(min(768, max(64, 2 * (n - placed))))
+        cand = rng.uniform(0.0, L, (m, 3))
+        tries += m
+        cell = (cand // cw).astype(np.int64) % nc
+        near = (cell[:, None, :] + offs[None, :, :]) % nc
+        nb = occ[near[..., 0], near[..., 1], near[..., 2]].reshape(m, -1)
+        d = pos[np.maximum(nb, 0)] - cand[:, None, :]
+        d -= L * np.round(d / L)
+        clash = (nb >= 0) & ((d * d).sum(-1) < md2)
+        idx = np.nonzero(~clash.any(axis=1))[0]
+        if len(idx) == 0:
             continue
-        pos[placed] = p
-        grid.setdefault(c, []).append(placed)
-        placed += 1
+        p = cand[idx]
+        dd = p[:, None, :] - p[None, :, :]
+        dd -= L * np.round(dd / L)
+        conflict = (dd * dd).sum(-1) < md2
+        keep = np.ones(len(idx), dtype=bool)
+        for a in range(len(idx)):
+            if keep[a]:
+                keep[a + 1:] &= ~conflict[a, a + 1:]
+        for q in idx[keep][: n - placed]:
+            cx, cy, cz = cell[q]
+            k = cnt[cx, cy, cz]
+            if k >= K:
+                occ = np.concatenate([occ, np.full((nc, nc, nc, K), -1, dtype=np.int64)], axis=3)
+                K *= 2
+            occ[cx, cy, cz, k] = placed
+            cnt[cx, cy, cz] = k + 1
+            pos[placed] = cand[q]
+            placed += 1
     return Atoms(list(symbols), pos, cell=np.eye(3) * L, pbc=True)
 
 

@@ -1,0 +1,111 @@
+"""GPU checks of the learned warm start (csrc/mlp.cu) against the FP64 NumPy
+oracle (oracle/mlp_oracle.py).
+
+Tolerances: the engine reads BF16 weights and sums in FP32, the oracle uses
+the same BF16-rounded weights in FP64, so forward values agree to ~1e-6
+relative and gradients (sums over the batch) to 1e-4 relative to the largest
+component.  Descriptors: FP32 against FP64, 1e-5 relative.
+"""
+import os
+import sys
+
+import numpy as np
+import pytest
+
+import mlp_oracle as MO
+import pysic_gb300 as pysic
+from pysic_gb300 import workloads as W
+from pysic_gb300.mlp import ChargeNetwork
+
+pytestmark = pytest.mark.gpu
+
+GOLDEN = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
+
+
+def _net(n_in=10, h1=12, h2=8, seed=0):
+    net = ChargeNetwork(n_in, h1, h2)
+    rng = np.random.default_rng(seed)
+    p = rng.normal(0, 0.4, net.n_params).astype(np.float32)
+    net.set_params(p)
+    return net, MO.bf16(p)
+
+
+def test_forward_matches_oracle():
+    net, pb = _net()
+    rng = np.random.default_rng(1)
+    x = rng.normal(0, 1, (500, 10)).astype(np.float32)
+    got = net.predict(x)  # identity normalisation
+    ref, _, _ = MO.forward(pb, x, 10, 12, 8)
+    np.testing.assert_allclose(got, ref, rtol=1e-5, atol=1e-5)
+
+
+def test_gradients_match_oracle():
+    net, pb = _net(seed=2)
+    rng = np.random.default_rng(3)
+    x = rng.normal(0, 1, (300, 10)).astype(np.float32)
+    y = rng.normal(0, 1, 300).astype(np.float32)
+    loss, g = net.gradients(x, y)
+    ref_loss, ref_g = MO.loss_and_grad(pb, x, y, 10, 12, 8)
+    assert loss == pytest.approx(ref_loss, rel=1e-5)
+    assert np.abs(g - ref_g).max() <= 1e-4 * np.abs(ref_g).max()
+
+
+def test_descriptors_match_oracle():
+    sys.path.insert(0, GOLDEN)
+    import cases
+
+    g = np.load(os.path.join(GOLDEN, "oracle_cases.npz"))
+    atoms, pots, coul = cases.restore("sio2_120", g)
+    calc = pysic.Pysic(atoms, pots, coulomb=coul)
+    calc.set_core()
+    c, i, o = calc.engine.neighbor_lists()
+    d = dict(n_gauss=8, r0=0.8, r1=5.0, width=0.35, cutoff=5.0)
+    got = calc.engine.descriptors(calc._model.n_types, **d)
+    ref = MO.descriptors(atoms.get_positions(), atoms.get_cell(), calc._model.types, calc._model.n_types,
+                         c, i, o, **d)
+    np.testing.assert_allclose(got, ref, rtol=1e-5, atol=1e-5 * np.abs(ref).max())
+
+
+def test_training_reduces_loss_and_is_deterministic():
+    rng = np.random.default_rng(4)
+    x = rng.normal(0, 1, (6000, 10)).astype(np.float32)
+    w = rng.normal(0, 1, 10)
+    y = np.tanh(x @ w / 3.0).astype(np.float32)
+    runs = []
+    for _ in range(2):
+        net, _ = _net(seed=5)
+        net.add_samples(x, y)
+        losses = net.train(8, batch=512, learning_rate=3e-3, seed=11)
+        runs.append((losses, net.get_params()))
+    losses, p = runs[0]
+    assert losses[-1] < 0.25 * losses[0]
+    assert np.array_equal(p, runs[1][1])
+
+
+def test_warm_start_relaxation_reaches_the_same_charges():
+    from pysic_gb300.train_warm_start import relax
+
+    params = {"n_steps": 4000, "timestep": 0.1, "inertia": 1.0, "friction": 4.0, "tolerance": 1e-4}
+    pots, coul = W.sio2_potentials(real_cutoff=5.5, sigma=1.6)
+    net = ChargeNetwork(2 * 16 + 2, 32, 32, elements=["Si", "O"])
+    xs, ys = [], []
+    calc = None
+    for seed in range(200, 216):  # training boxes
+        atoms = W.sio2_box(40, seed=seed)
+        calc = pysic.Pysic(atoms, pots, coulomb=coul, precision="mixed")
+        q, rel = relax(calc, params)
+        assert rel.last_converged
+        xs.append(net.descriptors(calc))
+        ys.append(q)
+    x, y = np.concatenate(xs), np.concatenate(ys)
+    net.normalise_from(x, y)
+    net.add_samples(x, y)
+    net.train(60, batch=256, learning_rate=3e-3, seed=1)
+    test_atoms = W.sio2_box(40, seed=7)  # held out
+    calc = pysic.Pysic(test_atoms, pots, coulomb=coul, precision="mixed")
+    q_cold, cold = relax(calc, params)
+    q_warm, warm = relax(calc, params, network=net)
+    assert cold.last_converged and warm.last_converged
+    assert warm.last_steps <= cold.last_steps
+    np.testing.assert_allclose(q_warm, q_cold, atol=2e-4)
+    assert abs(q_warm.sum()) < 1e-9
