@@ -446,6 +446,98 @@ def run_ours(args):
         dist.destroy_process_group()
 
 
+def _batched_structure(k):
+    import math
+
+    from pysic_gb300 import workloads as W
+
+    rng = np.random.default_rng(0)
+    counts = np.floor(np.exp(rng.uniform(math.log(64), math.log(2048), 512))).astype(int)
+    a = W.random_box(["Si"] * int(counts[k]), W.SI_DENSITY, 2.0, k)
+    return a.get_positions(), a.get_cell()[0, 0]
+
+
+def run_batch(args):
+    """512 uneven silicon boxes (Tersoff + LJ): one launch per kernel for all
+    systems (graph replay) against one evaluation per system."""
+    import multiprocessing as mp
+
+    with mp.get_context("spawn").Pool(os.cpu_count() or 1) as pool:
+        structs = pool.map(_batched_structure, range(512), chunksize=8)
+    import torch
+
+    import pysic_gb300 as pysic
+    from pysic_gb300 import workloads as W
+    from pysic_gb300.batch import BatchedPysic
+
+    pots = W.batched_potentials()
+    calcs = []
+    for pos, L_ in structs:
+        atoms = pysic.Atoms(["Si"] * len(pos), pos, cell=np.eye(3) * L_, pbc=True)
+        c = pysic.Pysic(atoms, pots, precision=args.precision)
+        c.set_core()
+        calcs.append(c)
+    n_atoms = sum(len(p) for p, _ in structs)
+    batch = BatchedPysic(calcs)
+    flush = torch.empty(64 * 1024 * 1024, dtype=torch.float32, device="cuda")
+    stream = torch.cuda.ExternalStream(batch.stream_handle())
+
+    def timed(prec, steps):
+        for _ in range(args.warmup):
+            batch.evaluate(prec)
+        batch.synchronize()
+        ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(steps)]
+        t0 = time.perf_counter()
+        for k in range(steps):
+            with torch.cuda.stream(stream):
+                flush.fill_(float(k))
+                ev[k][0].record(stream)
+            batch.evaluate(prec)
+            with torch.cuda.stream(stream):
+                ev[k][1].record(stream)
+        batch.synchronize()
+        wall = time.perf_counter() - t0
+        return [a.elapsed_time(b) for a, b in ev], wall
+
+    sampler = ClockSampler(0)
+    sampler.start()
+    times, wall_b = timed(args.precision, args.steps)
+    clocks = sampler.stop()
+    launches = batch.launch_count()
+    ms = statistics.mean(times)
+    # one evaluation per system (each context's own captured graph on its own stream)
+    for _ in range(args.warmup):
+        batch.evaluate(args.precision, mode="each")
+    batch.synchronize()
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        batch.evaluate(args.precision, mode="each")
+    batch.synchronize()
+    wall_each = (time.perf_counter() - t0) / args.steps
+    launches_each = batch.launch_count()
+    t64, _ = timed("fp64", max(5, args.steps // 4))
+    pl, bl = batch.get_lanes(args.precision)
+    line = {"metric": METRIC, "value": n_atoms / (ms / 1e3), "unit": "atom-steps/s", "n_gpus": 1,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32" if args.precision == "mixed" else "f64",
+            "data": "synthetic",
+            "config": {"workload": "batched_si_512", "systems": 512, "atoms": n_atoms,
+                       "structure": "Si boxes, atom counts log-uniform in [64, 2048], 2.33 g/cm^3, random with "
+                                    "rejection below 2.0 A; Tersoff + LJ (0.01 eV, 2.1 A, cutoff 5)",
+                       "precision": args.precision, "l2": "flushed before every step (256 MB write)",
+                       "tiles": {"pair_lanes": pl, "bond_lanes": bl}},
+            "systems_per_s": 512 / (ms / 1e3), "gpu_launches": launches * args.steps,
+            "batched_wall_ms_per_step": 1e3 * wall_b / args.steps,
+            "per_system": {"wall_ms_per_step": 1e3 * wall_each, "atom_steps_per_s": n_atoms / wall_each,
+                           "launches_per_step": launches_each,
+                           "note": "every system evaluated on its own: its own captured graph on its own stream"},
+            "batched_vs_per_system_wall": wall_each / (wall_b / args.steps),
+            "fp64": {"value": n_atoms / (statistics.mean(t64) / 1e3), "ms_per_step": statistics.mean(t64)},
+            "clocks": clocks}
+    line["speedup_vs_fp64"] = line["value"] / line["fp64"]["value"]
+    print(json.dumps(line))
+
+
 def run_profile(args):
     """Short fixed sequence for ncu: build, then `--steps` evaluations with a
     fixed lanes-per-atom tile (no autotuner launches)."""
@@ -480,6 +572,8 @@ def main():
     args.warmup = max(3, args.warmup)
     if args.profile:
         run_profile(args)
+    elif args.workload == "batched_si_512" and args.impl != "reference":
+        run_batch(args)
     elif args.impl == "reference":
         run_reference(args)
     else:

@@ -49,6 +49,7 @@ extern "C" {
 #define PG_WANT_ENEGS 4   /* electronegativities */
 
 typedef struct pg_context pg_context;
+typedef struct pg_batch pg_batch;
 typedef struct pg_mlp pg_mlp;
 
 /* Thread-local message of the last failing call ("" if none). */
@@ -218,6 +219,24 @@ int pg_mlp_train(pg_mlp* mlp, int32_t epochs, int32_t batch, float learning_rate
                  float* epoch_loss);
 int pg_mlp_gradients(pg_mlp* mlp, const float* x, const float* y, int64_t n, float* grad, double* loss);
 int pg_mlp_predict(pg_mlp* mlp, const float* x, int64_t n, float* y);
+
+/* ---- many independent systems ------------------------------------------------
+ * No counterpart in the reference, which holds one system per process.  A batch
+ * borrows fully set-up contexts (same device; pair and bond-order terms, no
+ * Ewald) and evaluates them all with one launch per kernel over a tile list
+ * (system, block), replayed from a CUDA graph (mode 0), or each on its own
+ * (mode 1, one pg_device_evaluate per context).  Results stay in each context:
+ * read them with pg_device_results after pg_batch_synchronize.  Lanes per atom
+ * of the pair and bond-order kernels: 0 lets the batch time the candidates. */
+int pg_batch_create(pg_batch** batch, int32_t device);
+int pg_batch_destroy(pg_batch* batch);
+int pg_batch_add(pg_batch* batch, pg_context* ctx);
+int pg_batch_set_lanes(pg_batch* batch, int32_t pair_lanes, int32_t bond_lanes);
+int pg_batch_get_lanes(pg_batch* batch, int32_t precision, int32_t* pair_lanes, int32_t* bond_lanes);
+int pg_batch_evaluate(pg_batch* batch, int32_t precision, int32_t flags, int32_t mode);
+int pg_batch_synchronize(pg_batch* batch);
+int pg_batch_get_stream(pg_batch* batch, void** stream);
+int pg_batch_last_launch_count(pg_batch* batch, int32_t* launches);
 
 /* Kernel launches issued by the last pg_device_evaluate / pg_calculate. */
 int pg_last_launch_count(pg_context* ctx, int32_t* launches);

@@ -82,6 +82,15 @@ _SIGNATURES = {
     "pg_set_kernel_timing": (ctypes.c_int, [_ctx, ctypes.c_int32]),
     "pg_get_kernel_times": (ctypes.c_int, [_ctx, ctypes.POINTER(ctypes.c_float)]),
     "pg_set_graphs": (ctypes.c_int, [_ctx, ctypes.c_int32]),
+    "pg_batch_create": (ctypes.c_int, [ctypes.POINTER(ctypes.c_void_p), ctypes.c_int32]),
+    "pg_batch_destroy": (ctypes.c_int, [ctypes.c_void_p]),
+    "pg_batch_add": (ctypes.c_int, [ctypes.c_void_p, _ctx]),
+    "pg_batch_set_lanes": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int32, ctypes.c_int32]),
+    "pg_batch_get_lanes": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int32, _c_int_p, _c_int_p]),
+    "pg_batch_evaluate": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int32, ctypes.c_int32, ctypes.c_int32]),
+    "pg_batch_synchronize": (ctypes.c_int, [ctypes.c_void_p]),
+    "pg_batch_get_stream": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(ctypes.c_void_p)]),
+    "pg_batch_last_launch_count": (ctypes.c_int, [ctypes.c_void_p, _c_int_p]),
     "pg_descriptors": (ctypes.c_int, [_ctx, ctypes.c_int32, ctypes.c_double, ctypes.c_double, ctypes.c_double,
                                       ctypes.c_double, _c_float_p]),
     "pg_mlp_create": (ctypes.c_int, [ctypes.POINTER(ctypes.c_void_p), ctypes.c_int32, ctypes.c_int32,

@@ -1,0 +1,75 @@
+"""Many independent systems evaluated together (no counterpart in the
+reference, which holds one system per process).
+
+    batch = BatchedPysic([calc_1, calc_2, ...])
+    batch.evaluate(precision="mixed")          # one launch per kernel for all
+    results = batch.results()                  # energy, forces, stress per system
+
+Every calculator is set up as usual (atoms, potentials, neighbour lists); the
+batch borrows their engine contexts and evaluates all of them with one launch
+of each kernel over a tile list (pg_batch_* in the C ABI).  ``mode="each"``
+evaluates them one by one instead, for comparison.
+"""
+import ctypes
+
+import numpy as np
+
+from . import _lib as L
+
+_PREC = {"fp64": L.PREC_FP64, "mixed": L.PREC_MIXED}
+
+
+class BatchedPysic:
+    def __init__(self, calculators, device=-1, pair_lanes=0, bond_lanes=0):
+        self.lib = L.load()
+        self.calculators = list(calculators)
+        h = ctypes.c_void_p()
+        L.check(self.lib.pg_batch_create(ctypes.byref(h), int(device)))
+        self.h = h
+        for c in self.calculators:
+            c.set_core()
+            L.check(self.lib.pg_batch_add(self.h, c.engine.ctx))
+        if pair_lanes or bond_lanes:
+            self.set_lanes(pair_lanes, bond_lanes)
+
+    def __del__(self):
+        try:
+            if getattr(self, "h", None):
+                self.lib.pg_batch_destroy(self.h)
+                self.h = None
+        except Exception:
+            pass
+
+    def set_lanes(self, pair_lanes=0, bond_lanes=0):
+        L.check(self.lib.pg_batch_set_lanes(self.h, int(pair_lanes), int(bond_lanes)))
+
+    def get_lanes(self, precision="mixed"):
+        p, q = ctypes.c_int32(0), ctypes.c_int32(0)
+        L.check(self.lib.pg_batch_get_lanes(self.h, _PREC[precision], ctypes.byref(p), ctypes.byref(q)))
+        return p.value, q.value
+
+    def evaluate(self, precision="mixed", forces=True, mode="batched"):
+        """Enqueue one energy (+ forces and virial) evaluation of every system;
+        returns without waiting."""
+        flags = L.WANT_ENERGY | (L.WANT_FORCES if forces else 0)
+        L.check(self.lib.pg_batch_evaluate(self.h, _PREC[precision], flags, 0 if mode == "batched" else 1))
+
+    def synchronize(self):
+        L.check(self.lib.pg_batch_synchronize(self.h))
+
+    def stream_handle(self):
+        s = ctypes.c_void_p()
+        L.check(self.lib.pg_batch_get_stream(self.h, ctypes.byref(s)))
+        return s.value or 0
+
+    def launch_count(self):
+        v = ctypes.c_int32(0)
+        L.check(self.lib.pg_batch_last_launch_count(self.h, ctypes.byref(v)))
+        return v.value
+
+    def results(self):
+        self.synchronize()
+        return [c.engine.device_results() for c in self.calculators]
+
+    def energies(self):
+        return np.array([r["energy"] for r in self.results()])

@@ -683,6 +683,75 @@ int pg_mlp_predict(pg_mlp* mlp, const float* x, int64_t n, float* y) {
     });
 }
 
+static void check_batch(pg_batch* b) { pg::require(b != nullptr, PG_ERR_INVALID, "null batch"); }
+
+int pg_batch_create(pg_batch** batch, int32_t device) {
+    return guarded([&] {
+        pg::require(batch != nullptr, PG_ERR_INVALID, "null output pointer");
+        *batch = nullptr;
+        pg::batch_create(batch, device);
+    });
+}
+
+int pg_batch_destroy(pg_batch* batch) {
+    return guarded([&] {
+        if (batch) pg::batch_destroy(batch);
+    });
+}
+
+int pg_batch_add(pg_batch* batch, pg_context* ctx) {
+    return guarded([&] {
+        check_batch(batch);
+        check_ctx(ctx);
+        pg::batch_add(batch, ctx);
+    });
+}
+
+int pg_batch_set_lanes(pg_batch* batch, int32_t pair_lanes, int32_t bond_lanes) {
+    return guarded([&] {
+        check_batch(batch);
+        pg::batch_set_lanes(batch, pair_lanes, bond_lanes);
+    });
+}
+
+int pg_batch_get_lanes(pg_batch* batch, int32_t precision, int32_t* pair_lanes, int32_t* bond_lanes) {
+    return guarded([&] {
+        check_batch(batch);
+        int p = 0, q = 0;
+        pg::batch_get_lanes(batch, precision, &p, &q);
+        *pair_lanes = p;
+        *bond_lanes = q;
+    });
+}
+
+int pg_batch_evaluate(pg_batch* batch, int32_t precision, int32_t flags, int32_t mode) {
+    return guarded([&] {
+        check_batch(batch);
+        pg::batch_evaluate(batch, precision, flags, mode);
+    });
+}
+
+int pg_batch_synchronize(pg_batch* batch) {
+    return guarded([&] {
+        check_batch(batch);
+        pg::batch_synchronize(batch);
+    });
+}
+
+int pg_batch_get_stream(pg_batch* batch, void** stream) {
+    return guarded([&] {
+        check_batch(batch);
+        *stream = (void*)pg::batch_stream(batch);
+    });
+}
+
+int pg_batch_last_launch_count(pg_batch* batch, int32_t* launches) {
+    return guarded([&] {
+        check_batch(batch);
+        *launches = pg::batch_launches(batch);
+    });
+}
+
 int pg_set_kernel_timing(pg_context* ctx, int32_t enable) {
     return guarded([&] {
         check_ctx(ctx);

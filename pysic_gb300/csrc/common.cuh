@@ -402,6 +402,17 @@ void mlp_train(pg_mlp* M, int epochs, int batch, float lr, unsigned long long se
 void mlp_gradients(pg_mlp* M, const float* x, const float* y, long long n, float* grad, double* loss);
 void mlp_predict(pg_mlp* M, const float* x, long long n, float* y);
 
+// batch.cu: many systems per launch (struct pg_batch)
+void batch_create(pg_batch** out, int device);
+void batch_destroy(pg_batch* b);
+void batch_add(pg_batch* b, pg_context* c);
+void batch_set_lanes(pg_batch* b, int pair_lanes, int bond_lanes);
+void batch_get_lanes(pg_batch* b, int precision, int* pair_lanes, int* bond_lanes);
+void batch_evaluate(pg_batch* b, int precision, int flags, int mode);
+void batch_synchronize(pg_batch* b);
+int batch_launches(const pg_batch* b);
+cudaStream_t batch_stream(const pg_batch* b);
+
 // relax.cu
 void relax_charges(pg_context* ctx, int precision, int n_steps, double dt, double inertia, double friction,
                    double tolerance, double* rates, double* charges, int* steps, double* error, double* max_dq);

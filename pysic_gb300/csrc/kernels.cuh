@@ -221,12 +221,13 @@ __device__ __forceinline__ void post_process<float>(float beta, float eta, float
 // Slot of the atom a lane group handles.  The atoms, sorted by list length,
 // are cut into warp-sized runs that are dealt round-robin over the blocks, so
 // that the lanes of a warp loop equally long and every block gets a similar
-// mix of light and heavy warps.  A bijection onto [0, gridDim.x * blockDim.x / G).
+// mix of light and heavy warps.  blk is the block's index among the nblk
+// blocks of one system; a bijection onto [0, nblk * blockDim.x / G).
 template <int G>
-__device__ __forceinline__ int dealt_slot() {
+__device__ __forceinline__ int dealt_slot(int blk, int nblk) {
     constexpr int APW = 32 / G;
     const int wi = threadIdx.x >> 5, si = (threadIdx.x & 31) / G;
-    return (wi * (int)gridDim.x + (int)blockIdx.x) * APW + si;
+    return (wi * nblk + blk) * APW + si;
 }
 
 // warp-segment reductions over groups of G lanes

@@ -11,35 +11,12 @@
 // walks i's full list, so each pair is evaluated from both ends: atom i takes
 // half the pair energy, its own force and half the pair virial.  Every force
 // and electronegativity is a gather; no atomics, bit-reproducible.
+#include "args.cuh"
 #include "common.cuh"
 #include "kernels.cuh"
 
 namespace pg {
 
-struct PairArgs {
-    int n, T;
-    const double* pos;
-    const double* charge;
-    const int* type;
-    CellK C;
-    const int* start;
-    const int* idx;
-    const int* off;
-    const void* terms;  // PairT<R>
-    const int2* index;
-    const SingleTerm* sterms;
-    const int2* sindex;
-    int ewald;
-    double ew_rc, ew_is2, ew_k, ew_c2, ew_isq2;  // 1/(sqrt2 sigma), 1/(4 pi eps), 2/(sqrt(2 pi) sigma), 1/(2 sigma^2)
-    int flags;
-    int first_f, first_chi;
-    double* out_f;
-    double* out_chi;
-    FxAcc* acc;       // global energy / virial totals (null: not wanted)
-    const int* skip;  // optional device flag: nonzero = do nothing
-    const F4* sep0;   // mixed path: bond vectors at list build
-    const F4* disp;   // mixed path: displacements since the build (xyz) and FP32 charge (w)
-};
 
 // bond vector of entry e of atom i: FP64 from the positions, or (mixed path)
 // build-time vector plus the FP32 displacements of both atoms
@@ -86,14 +63,14 @@ __device__ __forceinline__ double powi_(double x, int n) {
 }
 
 template <typename R, int G>
-__global__ void __launch_bounds__(256) pair_kernel(PairArgs A) {
+__device__ __forceinline__ void pair_body(const PairArgs& A, int blk) {
     __shared__ Fx128 wsum[256 / 32][7];
     __shared__ unsigned done;
     if (threadIdx.x == 0) done = 0u;
     __syncthreads();
     const int lane = threadIdx.x % G;
     const int slot = threadIdx.x / G;
-    const int i = blockIdx.x * (blockDim.x / G) + slot;
+    const int i = blk * (blockDim.x / G) + slot;
     if (A.skip && *A.skip) return;
     const bool act = i < A.n;
     R fx = 0, fy = 0, fz = 0, en = 0, chi = 0;
@@ -194,6 +171,22 @@ __global__ void __launch_bounds__(256) pair_kernel(PairArgs A) {
     }
 }
 
+template <typename R, int G>
+__global__ void __launch_bounds__(256) pair_kernel(const __grid_constant__ PairArgs A) {
+    pair_body<R, G>(A, blockIdx.x);
+}
+
+// many systems in one launch (tiles[t] = system, block of that system)
+template <typename R, int G>
+__global__ void __launch_bounds__(256)
+    pair_kernel_batch(const PairArgs* __restrict__ sys, const int2* __restrict__ tiles, int ntiles) {
+    for (int t = blockIdx.x; t < ntiles; t += gridDim.x) {
+        const int2 tl = tiles[t];
+        pair_body<R, G>(sys[tl.x], tl.y);
+        __syncthreads();
+    }
+}
+
 // atoms per block: enough blocks to cover every SM twice, at most 256 threads
 int pair_atoms_per_block(int n, int G) {
     const int maxa = 256 / G;
@@ -210,8 +203,8 @@ int pair_kernel_blocks(int n, int G) {
     return (n + a - 1) / a;
 }
 
-void launch_pair_kernel_skip(pg_context* ctx, int precision, int flags, bool first_f, bool first_chi, int G,
-                             FxAcc* acc, const int* skip) {
+PairArgs make_pair_args(pg_context* ctx, int precision, int flags, bool first_f, bool first_chi, FxAcc* acc,
+                        const int* skip) {
     PairArgs A{};
     A.skip = skip;
     A.n = ctx->n;
@@ -242,10 +235,16 @@ void launch_pair_kernel_skip(pg_context* ctx, int precision, int flags, bool fir
     A.out_f = ctx->out_f.p;
     A.out_chi = ctx->out_chi.p;
     A.acc = acc;
-    const int nbk = pair_kernel_blocks(ctx->n, G);
-    const int threads = pair_atoms_per_block(ctx->n, G) * G;
     A.sep0 = ctx->nb_sep0.p;
     A.disp = ctx->disp32.p;
+    return A;
+}
+
+void launch_pair_kernel_skip(pg_context* ctx, int precision, int flags, bool first_f, bool first_chi, int G,
+                             FxAcc* acc, const int* skip) {
+    const PairArgs A = make_pair_args(ctx, precision, flags, first_f, first_chi, acc, skip);
+    const int nbk = pair_kernel_blocks(ctx->n, G);
+    const int threads = pair_atoms_per_block(ctx->n, G) * G;
     cudaStream_t st = ctx->stream;
 #define PG_PAIR_LAUNCH(R_, G_) pair_kernel<R_, G_><<<nbk, threads, 0, st>>>(A)
     if (precision == PG_PREC_FP64) {
@@ -260,6 +259,22 @@ void launch_pair_kernel_skip(pg_context* ctx, int precision, int flags, bool fir
 #undef PG_PAIR_LAUNCH
     PG_CHECK_LAUNCH();
     ctx->launches++;
+}
+
+void launch_pair_batch(const PairArgs* sys, const int2* tiles, int ntiles, int grid, int threads, int precision, int G,
+                       cudaStream_t st) {
+#define PG_PAIR_BATCH(R_, G_) pair_kernel_batch<R_, G_><<<grid, threads, 0, st>>>(sys, tiles, ntiles)
+    if (precision == PG_PREC_FP64) {
+        if (G == 8) PG_PAIR_BATCH(double, 8);
+        else if (G == 16) PG_PAIR_BATCH(double, 16);
+        else PG_PAIR_BATCH(double, 32);
+    } else {
+        if (G == 8) PG_PAIR_BATCH(float, 8);
+        else if (G == 16) PG_PAIR_BATCH(float, 16);
+        else PG_PAIR_BATCH(float, 32);
+    }
+#undef PG_PAIR_BATCH
+    PG_CHECK_LAUNCH();
 }
 
 void launch_pair_kernel_impl(pg_context* ctx, int precision, int flags, bool first_f, bool first_chi, int G,

@@ -151,14 +151,20 @@ void fold_tables(pg_context* ctx) {
     // all share the bond-order cutoff): the bond-order kernels take every
     // parameter as a kernel argument instead of looking tables up per triplet.
     ctx->spec_ok = false;
-    if (T == 1 && trip[0].valid && post[0].valid && index[0].y >= 1 && index[0].y <= PG_SPEC_MAX_TERMS &&
-        maxbr[0] == trip[0].rc) {
+    if (T == 1 && trip[0].valid && post[0].valid && maxbr[0] == trip[0].rc) {
         const TripT<double>& t0 = trip[0];
-        bool ok = true;
-        int mask = 0;
+        // the pair terms that run in the bond-order kernels (terms with a longer
+        // reach, e.g. an added Lennard-Jones, stay in the pair kernel)
+        std::vector<const PairT<double>*> bt;
         for (int q = 0; q < index[0].y; ++q) {
             const PairT<double>& pt = terms[(size_t)index[0].x + q];
-            ok = ok && pt.in_bond_kernel && pt.kind == 1 && pt.smooth && pt.rc == t0.rc && pt.rs == t0.rs;
+            if (pt.in_bond_kernel) bt.push_back(&pt);
+        }
+        bool ok = !bt.empty() && (int)bt.size() <= PG_SPEC_MAX_TERMS;
+        int mask = 0;
+        for (size_t q = 0; ok && q < bt.size(); ++q) {
+            const PairT<double>& pt = *bt[q];
+            ok = pt.kind == 1 && pt.smooth && pt.rc == t0.rc && pt.rs == t0.rs;
             if (pt.group >= 0) mask |= 1 << q;
         }
         if (ok && mask != 0) {
@@ -173,12 +179,11 @@ void fold_tables(pg_context* ctx) {
             v[SP_C2D2] = t0.c2d2;
             v[SP_H] = t0.h;
             v[SP_MU] = t0.mu;
-            for (int q = 0; q < index[0].y; ++q) {
-                const PairT<double>& pt = terms[(size_t)index[0].x + q];
-                v[SP_TERMS + 2 * q] = pt.p0;
-                v[SP_TERMS + 2 * q + 1] = pt.p1;
+            for (size_t q = 0; q < bt.size(); ++q) {
+                v[SP_TERMS + 2 * q] = bt[q]->p0;
+                v[SP_TERMS + 2 * q + 1] = bt[q]->p1;
             }
-            ctx->spec_nterm = index[0].y;
+            ctx->spec_nterm = (int)bt.size();
             ctx->spec_bomask = mask;
             ctx->spec_ok = true;
         }

@@ -36,71 +36,38 @@
 // type shares it) the bond-order cutoff factor f(r_ik), which every triplet
 // through the bond reuses.
 #include <functional>
+#include <type_traits>
 
+#include "args.cuh"
 #include "common.cuh"
 #include "kernels.cuh"
 
 namespace pg {
 
-template <typename R>
-struct Vec4T;
-template <>
-struct Vec4T<float> {
-    using T = F4;
-};
-template <>
-struct Vec4T<double> {
-    using T = D4;
-};
-
-struct BondArgs {
-    int n, T;
-    const double* pos;
-    const int* type;
-    CellK C;
-    const int* start;
-    const int* idx;
-    const int* off;
-    const int* rev;
-    const void* terms;  // PairT<R>
-    const int2* index;
-    const void* trip;   // TripT<R>
-    const void* post;   // PostT<R>
-    const void* maxbr;  // R
-    const void* bcut;   // per (ti, tk): rc, rs of bond ik (Vec2T<R>)
-    int bcut_uniform;   // bcut holds for every tj
-    const int* etype;   // per entry: partner type
-    const int* order;   // lane-group slot -> atom (atoms grouped by list length)
-    int n_terms;        // pair records in terms
-    const F4* sep0;     // mixed path: bond vectors at list build
-    const F4* disp;     // mixed path: per-atom displacement since the build
-    float spf[SP_COUNT];  // single-species fast path parameters, FP32 copy
-    double spd[SP_COUNT]; // and FP64
-    int spec, spec_nterm, spec_bomask;
-    int flags;
-    int first_f;
-    void* geo;
-    void* fj;
-    void* kacc;        // per entry i->k: the k parts of i's bonds on k (unstaged atoms' scratch)
-    void* fc;          // per atom: i part of the force (FP64, or 2^-32 fixed point in the mixed path)
-    double* out_f;
-    FxAcc* acc;        // global energy / virial totals (null: not wanted)
-    double* zeta_out;
-};
 
 // per-atom displacement since the list build (FP64 difference rounded to FP32)
 // and the FP32 charge, one 16-byte record per atom for the mixed-path kernels;
 // block 0 also clears the energy / virial totals (zero8, 8 records; may be null)
 // that the kernels after it add to
-__global__ void disp_pass(int n, const double* __restrict__ pos, const double* __restrict__ pos0,
-                          const double* __restrict__ q, F4* __restrict__ d, const int* skip, FxAcc* zero8) {
+__device__ __forceinline__ void disp_body(const DispArgs& A, int i) {
+    if (A.zero8 && i < 8) A.zero8[i] = FxAcc{{0ull, 0ull, 0ull}};
+    if (A.skip && *A.skip) return;
+    if (i >= A.n || A.d == nullptr) return;
+    const double* pos = A.pos;
+    const double* pos0 = A.pos0;
+    A.d[i] = F4{(float)(pos[3 * i] - pos0[3 * i]), (float)(pos[3 * i + 1] - pos0[3 * i + 1]),
+                (float)(pos[3 * i + 2] - pos0[3 * i + 2]), (float)A.q[i]};
+}
+__global__ void disp_pass(const __grid_constant__ DispArgs A) {
     pdl_trigger();
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (zero8 && i < 8) zero8[i] = FxAcc{{0ull, 0ull, 0ull}};
-    if (skip && *skip) return;
-    if (i >= n) return;
-    d[i] = F4{(float)(pos[3 * i] - pos0[3 * i]), (float)(pos[3 * i + 1] - pos0[3 * i + 1]),
-              (float)(pos[3 * i + 2] - pos0[3 * i + 2]), (float)q[i]};
+    disp_body(A, blockIdx.x * blockDim.x + threadIdx.x);
+}
+__global__ void disp_pass_batch(const DispArgs* __restrict__ sys, const int2* __restrict__ tiles, int ntiles) {
+    pdl_trigger();
+    for (int t = blockIdx.x; t < ntiles; t += gridDim.x) {
+        const int2 tl = tiles[t];
+        disp_body(sys[tl.x], tl.y * blockDim.x + threadIdx.x);
+    }
 }
 
 template <typename R>
@@ -141,7 +108,7 @@ struct Vec2T<double> {
 // SPEC: single-species Tersoff, every parameter a kernel argument (no table
 // lookups per bond or triplet); the same arithmetic as the table path.
 template <typename R, int G, bool SPEC>
-__global__ void __launch_bounds__(128, sizeof(R) == 4 ? 7 : 4) bond_pass(BondArgs A) {
+__device__ __forceinline__ void bond_body(const BondArgs& A, int blk, int nblk) {
     using V4 = typename Vec4T<R>::T;
     using V2 = typename Vec2T<R>::T;
     constexpr int AP = 128 / G;  // atoms per block
@@ -180,7 +147,7 @@ __global__ void __launch_bounds__(128, sizeof(R) == 4 ? 7 : 4) bond_pass(BondArg
     __syncthreads();
     const int lane = threadIdx.x % G;
     const int slot = threadIdx.x / G;
-    const int gslot = A.order ? dealt_slot<G>() : blockIdx.x * AP + slot;
+    const int gslot = A.order ? dealt_slot<G>(blk, nblk) : blk * AP + slot;
     const bool act = gslot < A.n;
     const int i = act ? (A.order ? A.order[gslot] : gslot) : 0;
     const int s = act ? A.start[i] : 0;
@@ -479,12 +446,12 @@ __global__ void __launch_bounds__(128, sizeof(R) == 4 ? 7 : 4) bond_pass(BondArg
 }
 
 template <typename R, int G>
-__global__ void __launch_bounds__(128) gather_pass(BondArgs A) {
+__device__ __forceinline__ void gather_body(const BondArgs& A, int blk, int nblk) {
     using V4 = typename Vec4T<R>::T;
     const V4* fj = (const V4*)A.fj;
     const int lane = threadIdx.x % G;
     const int slot = threadIdx.x / G;
-    const int gslot = A.order ? dealt_slot<G>() : blockIdx.x * (blockDim.x / G) + slot;
+    const int gslot = A.order ? dealt_slot<G>(blk, nblk) : blk * (blockDim.x / G) + slot;
     const bool act = gslot < A.n;
     const int m = act ? (A.order ? A.order[gslot] : gslot) : 0;
     R Fx = 0, Fy = 0, Fz = 0;
@@ -520,9 +487,39 @@ __global__ void __launch_bounds__(128) gather_pass(BondArgs A) {
     }
 }
 
+// One system: the kernel argument is read in place (no copy to local memory).
+template <typename R, int G, bool SPEC>
+__global__ void __launch_bounds__(128, sizeof(R) == 4 ? 7 : 4) bond_pass(const __grid_constant__ BondArgs A) {
+    bond_body<R, G, SPEC>(A, blockIdx.x, gridDim.x);
+}
+template <typename R, int G>
+__global__ void __launch_bounds__(128) gather_pass(const __grid_constant__ BondArgs A) {
+    gather_body<R, G>(A, blockIdx.x, gridDim.x);
+}
+
+// Many systems in one launch: tiles[t] = (system, block of that system); the
+// resident blocks walk the tile list.
+template <typename R, int G, bool SPEC>
+__global__ void __launch_bounds__(128, sizeof(R) == 4 ? 7 : 4)
+    bond_pass_batch(const BondArgs* __restrict__ sys, const int2* __restrict__ tiles, int ntiles) {
+    for (int t = blockIdx.x; t < ntiles; t += gridDim.x) {
+        const int2 tl = tiles[t];
+        bond_body<R, G, SPEC>(sys[tl.x], tl.y, sys[tl.x].nblocks);
+        __syncthreads();
+    }
+}
+template <typename R, int G>
+__global__ void __launch_bounds__(128)
+    gather_pass_batch(const BondArgs* __restrict__ sys, const int2* __restrict__ tiles, int ntiles) {
+    for (int t = blockIdx.x; t < ntiles; t += gridDim.x) {
+        const int2 tl = tiles[t];
+        gather_body<R, G>(sys[tl.x], tl.y, sys[tl.x].nblocks);
+    }
+}
+
 int bond_blocks(int n, int G) { return (n + (128 / G) - 1) / (128 / G); }
 
-static void prepare_scratch(pg_context* ctx, int precision) {
+void prepare_bond_scratch(pg_context* ctx, int precision) {
     const size_t ne = (size_t)std::max<long long>(ctx->sh_total, 1);
     // per short-list entry: bond geometry | force on the partner | k-part sums
     if (precision == PG_PREC_FP64) ctx->bo_fj64.resize(3 * ne);
@@ -530,7 +527,19 @@ static void prepare_scratch(pg_context* ctx, int precision) {
     ctx->bo_fc.resize(3 * (size_t)std::max(ctx->n, 1));
 }
 
-static BondArgs bond_args(pg_context* ctx, int precision, int flags, bool first_f, FxAcc* acc) {
+DispArgs make_disp_args(pg_context* ctx, F4* d, const int* skip, FxAcc* zero8) {
+    DispArgs A{};
+    A.n = ctx->n;
+    A.pos = ctx->pos.p;
+    A.pos0 = ctx->pos0.p;
+    A.q = ctx->charge.p;
+    A.d = d;
+    A.skip = skip;
+    A.zero8 = zero8;
+    return A;
+}
+
+BondArgs make_bond_args(pg_context* ctx, int precision, int flags, bool first_f, FxAcc* acc) {
     BondArgs A{};
     A.n = ctx->n;
     A.T = std::max(ctx->n_types, 1);
@@ -608,8 +617,8 @@ static void launch_by_lanes(const BondArgs& A, int n, cudaStream_t st, int G, bo
 // `between` runs between the two passes
 void launch_bond_order_impl(pg_context* ctx, int precision, int flags, bool first_f, int G, FxAcc* acc,
                             const std::function<void()>& between) {
-    prepare_scratch(ctx, precision);
-    BondArgs A = bond_args(ctx, precision, flags, first_f, acc);
+    prepare_bond_scratch(ctx, precision);
+    BondArgs A = make_bond_args(ctx, precision, flags, first_f, acc);
     const bool forces = (flags & PG_WANT_FORCES) != 0;
     if (precision == PG_PREC_FP64) launch_by_lanes<double>(A, ctx->n, ctx->stream, G, forces, between);
     else launch_by_lanes<float>(A, ctx->n, ctx->stream, G, forces, between);
@@ -623,7 +632,7 @@ void launch_bond_order_impl(pg_context* ctx, int precision, int flags, bool firs
 // and virial go to acc, forces to out_f (written).
 void launch_bond_order_scratch(pg_context* ctx, int precision, int G, void* bonds, void* fc, F4* disp, FxAcc* acc,
                                double* out_f) {
-    BondArgs A = bond_args(ctx, precision, PG_WANT_ENERGY | PG_WANT_FORCES, true, acc);
+    BondArgs A = make_bond_args(ctx, precision, PG_WANT_ENERGY | PG_WANT_FORCES, true, acc);
     const size_t ne = (size_t)std::max<long long>(ctx->sh_total, 1);
     const size_t rec = precision == PG_PREC_FP64 ? sizeof(D4) : sizeof(F4);
     A.geo = bonds;
@@ -635,8 +644,7 @@ void launch_bond_order_scratch(pg_context* ctx, int precision, int G, void* bond
     if (precision == PG_PREC_FP64) {
         launch_by_lanes<double>(A, ctx->n, ctx->stream, G, true, none);
     } else {
-        disp_pass<<<(ctx->n + 255) / 256, 256, 0, ctx->stream>>>(ctx->n, ctx->pos.p, ctx->pos0.p, ctx->charge.p, disp,
-                                                                 nullptr, nullptr);
+        disp_pass<<<(ctx->n + 255) / 256, 256, 0, ctx->stream>>>(make_disp_args(ctx, disp, nullptr, nullptr));
         A.disp = disp;
         launch_by_lanes<float>(A, ctx->n, ctx->stream, G, true, none);
     }
@@ -645,21 +653,48 @@ void launch_bond_order_scratch(pg_context* ctx, int precision, int G, void* bond
 
 void launch_disp(pg_context* ctx, const int* skip, FxAcc* zero8) {
     ctx->disp32.resize((size_t)std::max(ctx->n, 1));
-    disp_pass<<<(ctx->n + 255) / 256, 256, 0, ctx->stream>>>(ctx->n, ctx->pos.p, ctx->pos0.p, ctx->charge.p, ctx->disp32.p,
-                                                                 skip, zero8);
+    disp_pass<<<(ctx->n + 255) / 256, 256, 0, ctx->stream>>>(make_disp_args(ctx, ctx->disp32.p, skip, zero8));
     PG_CHECK_LAUNCH();
     ctx->launches++;
 }
 
 void bond_zeta_diag(pg_context* ctx) {
-    prepare_scratch(ctx, PG_PREC_FP64);
+    prepare_bond_scratch(ctx, PG_PREC_FP64);
     ctx->bo_zeta.resize((size_t)std::max<long long>(ctx->sh_total, 1));
     ctx->bo_zeta.zero(ctx->stream);
-    BondArgs A = bond_args(ctx, PG_PREC_FP64, PG_WANT_ENERGY, true, nullptr);
+    BondArgs A = make_bond_args(ctx, PG_PREC_FP64, PG_WANT_ENERGY, true, nullptr);
     A.zeta_out = ctx->bo_zeta.p;
     bond_pass<double, 8, false><<<bond_blocks(ctx->n, 8), 128, 0, ctx->stream>>>(A);
     PG_CHECK_LAUNCH();
     PG_CUDA(cudaStreamSynchronize(ctx->stream));
+}
+
+void launch_bond_batch(const BondArgs* sys, const int2* tiles, int ntiles, int grid, int precision, int G, bool spec,
+                       bool forces, cudaStream_t st) {
+    const dim3 g(grid), b(128);
+    auto go = [&](auto rtag, auto gtag) {
+        using R = decltype(rtag);
+        constexpr int GG = decltype(gtag)::value;
+        if (spec) launch_pdl(bond_pass_batch<R, GG, true>, g, b, st, sys, tiles, ntiles);
+        else launch_pdl(bond_pass_batch<R, GG, false>, g, b, st, sys, tiles, ntiles);
+        if (forces) launch_pdl(gather_pass_batch<R, GG>, g, b, st, sys, tiles, ntiles);
+    };
+    auto by_lanes = [&](auto rtag) {
+        switch (G) {
+            case 4: go(rtag, std::integral_constant<int, 4>{}); break;
+            case 8: go(rtag, std::integral_constant<int, 8>{}); break;
+            case 16: go(rtag, std::integral_constant<int, 16>{}); break;
+            default: go(rtag, std::integral_constant<int, 32>{}); break;
+        }
+    };
+    if (precision == PG_PREC_FP64) by_lanes(double{});
+    else by_lanes(float{});
+    PG_CHECK_LAUNCH();
+}
+
+void launch_disp_batch(const DispArgs* sys, const int2* tiles, int ntiles, int grid, cudaStream_t st) {
+    disp_pass_batch<<<grid, 256, 0, st>>>(sys, tiles, ntiles);
+    PG_CHECK_LAUNCH();
 }
 
 }  // namespace pg
