@@ -86,6 +86,53 @@ __global__ void desc_kernel(DescArgs A) {
     }
 }
 
+// Fast form for NG Gaussians and at most TMAX types: lanes over the atom's
+// entries (one separation per entry instead of one per feature), features in
+// registers, then a fixed-order shuffle tree per feature.
+template <int NG, int TMAX>
+__global__ void desc_kernel_lanes(DescArgs A) {
+    const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const int lane = threadIdx.x & 31;
+    if (warp >= A.n) return;  // whole warps leave together
+    const int i = warp;
+    const double xi = A.pos[3 * i], yi = A.pos[3 * i + 1], zi = A.pos[3 * i + 2];
+    float acc[TMAX][NG];
+#pragma unroll
+    for (int t = 0; t < TMAX; ++t)
+#pragma unroll
+        for (int k = 0; k < NG; ++k) acc[t][k] = 0.0f;
+    for (int e = A.start[i] + lane; e < A.start[i + 1]; e += 32) {
+        const int j = A.idx[e];
+        const double o0 = A.off[3 * e], o1 = A.off[3 * e + 1], o2 = A.off[3 * e + 2];
+        const double x = A.pos[3 * j] - xi + (o0 * A.C.vc[0][0] + o1 * A.C.vc[0][1] + o2 * A.C.vc[0][2]);
+        const double y = A.pos[3 * j + 1] - yi + (o0 * A.C.vc[1][0] + o1 * A.C.vc[1][1] + o2 * A.C.vc[1][2]);
+        const double z = A.pos[3 * j + 2] - zi + (o0 * A.C.vc[2][0] + o1 * A.C.vc[2][1] + o2 * A.C.vc[2][2]);
+        const float r = (float)sqrt(x * x + y * y + z * z);
+        if (!(r < A.rc)) continue;
+        const int tj = A.type[j];
+        const float fc = 0.5f * (1.0f + cospif(r / A.rc));
+#pragma unroll
+        for (int t = 0; t < TMAX; ++t) {
+            if (t != tj) continue;
+#pragma unroll
+            for (int k = 0; k < NG; ++k) {
+                const float d = r - (A.r0 + A.dmu * (float)k);
+                acc[t][k] += expf(-d * d * A.inv2w2) * fc;
+            }
+        }
+    }
+    const int nf = A.T * NG;
+#pragma unroll
+    for (int t = 0; t < TMAX; ++t)
+#pragma unroll
+        for (int k = 0; k < NG; ++k) {
+            float v = acc[t][k];
+#pragma unroll
+            for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+            if (lane == 0 && t < A.T) A.out[(long long)i * nf + t * NG + k] = v;
+        }
+}
+
 // ---- network -----------------------------------------------------------------
 
 // parameters (BF16) into shared memory as FP32
@@ -255,7 +302,10 @@ void descriptors(pg_context* ctx, int n_gauss, double r0, double r1, double widt
     A.rc = (float)cutoff;
     A.out = ctx->mlp_desc.p;
     if (ctx->n > 0) {
-        desc_kernel<<<cdiv((long long)ctx->n * 32, 128), 128, 0, ctx->stream>>>(A);
+        if (n_gauss == 16 && T <= 2)
+            desc_kernel_lanes<16, 2><<<cdiv((long long)ctx->n * 32, 128), 128, 0, ctx->stream>>>(A);
+        else
+            desc_kernel<<<cdiv((long long)ctx->n * 32, 128), 128, 0, ctx->stream>>>(A);
         PG_CHECK_LAUNCH();
     }
     ctx->mlp_desc.download(out, (size_t)ctx->n * nf, ctx->stream);

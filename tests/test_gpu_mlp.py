@@ -50,7 +50,8 @@ def test_gradients_match_oracle():
     assert np.abs(g - ref_g).max() <= 1e-4 * np.abs(ref_g).max()
 
 
-def test_descriptors_match_oracle():
+@pytest.mark.parametrize("n_gauss", [8, 16])
+def test_descriptors_match_oracle(n_gauss):
     sys.path.insert(0, GOLDEN)
     import cases
 
@@ -59,7 +60,7 @@ def test_descriptors_match_oracle():
     calc = pysic.Pysic(atoms, pots, coulomb=coul)
     calc.set_core()
     c, i, o = calc.engine.neighbor_lists()
-    d = dict(n_gauss=8, r0=0.8, r1=5.0, width=0.35, cutoff=5.0)
+    d = dict(n_gauss=n_gauss, r0=0.8, r1=5.0, width=0.35, cutoff=5.0)
     got = calc.engine.descriptors(calc._model.n_types, **d)
     ref = MO.descriptors(atoms.get_positions(), atoms.get_cell(), calc._model.types, calc._model.n_types,
                          c, i, o, **d)
