@@ -26,6 +26,7 @@
 //              electronegativity, output, the reference's stress term r (x) F.
 #include <algorithm>
 #include <cmath>
+#include <type_traits>
 #include <vector>
 
 #include "common.cuh"
@@ -294,25 +295,33 @@ __global__ void ew_sreduce(EwArgs A) {
 
 constexpr int SEG_TILE = 64;
 
+// two atoms per thread: every staged k record is read once for both
+constexpr int FIELD_ATOMS = 2;
+
 template <typename R>
 __global__ void __launch_bounds__(EW_THREADS) ew_field(EwArgs A) {
+    using V4 = typename std::conditional<sizeof(R) == 4, F4, D4>::type;
     __shared__ int4 sseg[SEG_TILE];
     __shared__ int sk0[SEG_TILE];
-    __shared__ R skx[SEG_TILE * SEG], sky[SEG_TILE * SEG], skz[SEG_TILE * SEG], sSc[SEG_TILE * SEG],
-        sSs[SEG_TILE * SEG];
+    __shared__ V4 sk[SEG_TILE * SEG];  // kx, ky, kz, c_k Re S(k)
+    __shared__ R sSs[SEG_TILE * SEG];  // c_k Im S(k)
     if (A.skip && *A.skip) return;
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
     const int split = blockIdx.y;
     const int s0 = split * A.seg_per_split, s1 = min(A.nseg, s0 + A.seg_per_split);
-    const bool act = i < A.n;
     using U = typename Frac<R>::U;
     using U4 = typename Frac<R>::U4;
-    U4 f;
-    f.x = f.y = f.z = f.w = 0;
-    if (act) f = ((const U4*)A.frac)[i];
-    R c3, s3;
-    phase<R>(f.z, c3, s3);
-    R fx = 0, fy = 0, fz = 0, ch = 0;
+    int ia[FIELD_ATOMS];
+    U4 f[FIELD_ATOMS];
+    R c3[FIELD_ATOMS], s3[FIELD_ATOMS];
+    R fx[FIELD_ATOMS], fy[FIELD_ATOMS], fz[FIELD_ATOMS], ch[FIELD_ATOMS];
+#pragma unroll
+    for (int a = 0; a < FIELD_ATOMS; ++a) {
+        ia[a] = (blockIdx.x * FIELD_ATOMS + a) * blockDim.x + threadIdx.x;
+        f[a].x = f[a].y = f[a].z = f[a].w = 0;
+        if (ia[a] < A.n) f[a] = ((const U4*)A.frac)[ia[a]];
+        phase<R>(f[a].z, c3[a], s3[a]);
+        fx[a] = fy[a] = fz[a] = ch[a] = 0;
+    }
     const C2<R>* wS = (const C2<R>*)A.wS;
     const R* kv = (const R*)A.kvecR;
     for (int b = s0; b < s1; b += SEG_TILE) {
@@ -325,39 +334,46 @@ __global__ void __launch_bounds__(EW_THREADS) ew_field(EwArgs A) {
             sk0[t] = A.seg_k0[b + t] - kb;
         }
         for (int t = threadIdx.x; t < ke - kb; t += blockDim.x) {
-            skx[t] = kv[4 * (kb + t)];
-            sky[t] = kv[4 * (kb + t) + 1];
-            skz[t] = kv[4 * (kb + t) + 2];
             const C2<R> v = wS[kb + t];
-            sSc[t] = v.re;
+            sk[t] = V4{kv[4 * (kb + t)], kv[4 * (kb + t) + 1], kv[4 * (kb + t) + 2], v.re};
             sSs[t] = v.im;
         }
         __syncthreads();
         for (int q = 0; q < m; ++q) {
             const int4 sg = sseg[q];
             const int k0 = sk0[q];
-            const U ph = (U)(long long)sg.x * f.x + (U)(long long)sg.y * f.y + (U)(long long)sg.z * f.z;
-            R c, s;
-            phase<R>(ph, c, s);
+            R c[FIELD_ATOMS], sn[FIELD_ATOMS];
+#pragma unroll
+            for (int a = 0; a < FIELD_ATOMS; ++a) {
+                const U ph = (U)(long long)sg.x * f[a].x + (U)(long long)sg.y * f[a].y + (U)(long long)sg.z * f[a].z;
+                phase<R>(ph, c[a], sn[a]);
+            }
             for (int t = 0; t < sg.w; ++t) {
-                const R Sc = sSc[k0 + t], Ss = sSs[k0 + t];
-                const R ff = Sc * s - Ss * c;
-                fx += ff * skx[k0 + t];
-                fy += ff * sky[k0 + t];
-                fz += ff * skz[k0 + t];
-                ch += Sc * c + Ss * s;
-                const R nr = c * c3 - s * s3;
-                s = c * s3 + s * c3;
-                c = nr;
+                const V4 kk = sk[k0 + t];
+                const R Ss = sSs[k0 + t];
+#pragma unroll
+                for (int a = 0; a < FIELD_ATOMS; ++a) {
+                    const R ff = kk.w * sn[a] - Ss * c[a];
+                    fx[a] += ff * kk.x;
+                    fy[a] += ff * kk.y;
+                    fz[a] += ff * kk.z;
+                    ch[a] += kk.w * c[a] + Ss * sn[a];
+                    const R nr = c[a] * c3[a] - sn[a] * s3[a];
+                    sn[a] = c[a] * s3[a] + sn[a] * c3[a];
+                    c[a] = nr;
+                }
             }
         }
     }
-    if (act) {
-        R* out = (R*)A.Fpart + 4 * ((long long)split * A.n + i);
-        out[0] = fx;
-        out[1] = fy;
-        out[2] = fz;
-        out[3] = ch;
+#pragma unroll
+    for (int a = 0; a < FIELD_ATOMS; ++a) {
+        if (ia[a] < A.n) {
+            R* out = (R*)A.Fpart + 4 * ((long long)split * A.n + ia[a]);
+            out[0] = fx[a];
+            out[1] = fy[a];
+            out[2] = fz[a];
+            out[3] = ch[a];
+        }
     }
 }
 
@@ -504,7 +520,7 @@ static void ew_shape(const pg_context* ctx, int& chunks, int& chunk, int& splits
     chunks = std::min(chunks, std::max(1, n / 32));
     chunk = cdiv(n, chunks);
     chunks = cdiv(n, chunk);
-    const int atom_blocks = cdiv(n, EW_THREADS);
+    const int atom_blocks = cdiv(n, EW_THREADS * FIELD_ATOMS);
     splits = std::max(1, std::min(32, cdiv(4 * 152, atom_blocks)));
     splits = std::min(splits, nseg);
     sps = cdiv(nseg, splits);
@@ -522,7 +538,7 @@ static void ew_launch(pg_context* ctx, EwArgs& A, int prep_blocks, int kred_bloc
     ew_sreduce<R><<<kred_blocks, 256, 0, st>>>(A);
     ctx->launches += 3;
     if (A.flags & (PG_WANT_FORCES | PG_WANT_ENEGS)) {
-        ew_field<R><<<dim3(cdiv(A.n, EW_THREADS), A.splits), EW_THREADS, 0, st>>>(A);
+        ew_field<R><<<dim3(cdiv(A.n, EW_THREADS * FIELD_ATOMS), A.splits), EW_THREADS, 0, st>>>(A);
         ew_finish<R><<<fin_blocks, EW_THREADS, 0, st>>>(A);
         ctx->launches += 2;
     }
