@@ -206,7 +206,9 @@ __global__ void __launch_bounds__(EW_THREADS) ew_sfac(EwArgs A) {
     }
     if (g < A.nseg) {
         C2<R>* out = (C2<R>*)A.Spart + (long long)chunk * A.nk + A.seg_k0[g];
-        for (int t = 0; t < sg.w; ++t) out[t] = acc[t];
+#pragma unroll
+        for (int t = 0; t < SEG; ++t)
+            if (t < sg.w) out[t] = acc[t];
     }
 }
 
