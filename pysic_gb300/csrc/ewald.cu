@@ -220,25 +220,46 @@ __device__ __forceinline__ void add_c(float v, float& s, float& c) {
     c += (s - (t - bp)) + (v - bp);
     s = t;
 }
+// Sum of the chunk partials of one k by KL lanes: lane l takes chunks l,
+// l + KL, ...; the lanes are then combined by a fixed shuffle tree.  Mixed
+// path: compensated FP32 (two-sum) throughout, widened once; FP64 path: FP64.
+constexpr int KL = 8;
+
 template <typename R>
-__device__ __forceinline__ double2 chunk_sum(const C2<R>* sp, int chunks, int nk, int k);
+__device__ __forceinline__ double2 chunk_sum(const C2<R>* sp, int chunks, int nk, int k, int l);
 template <>
-__device__ __forceinline__ double2 chunk_sum<float>(const C2<float>* sp, int chunks, int nk, int k) {
+__device__ __forceinline__ double2 chunk_sum<float>(const C2<float>* sp, int chunks, int nk, int k, int l) {
     float rs = 0.f, rc = 0.f, is = 0.f, ic = 0.f;
-    for (int c = 0; c < chunks; ++c) {
-        const C2<float> v = sp[(long long)c * nk + k];
-        add_c(v.re, rs, rc);
-        add_c(v.im, is, ic);
+    if (k < nk)
+        for (int c = l; c < chunks; c += KL) {
+            const C2<float> v = sp[(long long)c * nk + k];
+            add_c(v.re, rs, rc);
+            add_c(v.im, is, ic);
+        }
+#pragma unroll
+    for (int o = KL / 2; o > 0; o >>= 1) {
+        const float ors = __shfl_xor_sync(0xffffffffu, rs, o, KL), orc = __shfl_xor_sync(0xffffffffu, rc, o, KL);
+        const float ois = __shfl_xor_sync(0xffffffffu, is, o, KL), oic = __shfl_xor_sync(0xffffffffu, ic, o, KL);
+        add_c(ors, rs, rc);
+        rc += orc;
+        add_c(ois, is, ic);
+        ic += oic;
     }
     return make_double2((double)rs + (double)rc, (double)is + (double)ic);
 }
 template <>
-__device__ __forceinline__ double2 chunk_sum<double>(const C2<double>* sp, int chunks, int nk, int k) {
+__device__ __forceinline__ double2 chunk_sum<double>(const C2<double>* sp, int chunks, int nk, int k, int l) {
     double re = 0.0, im = 0.0;
-    for (int c = 0; c < chunks; ++c) {
-        const C2<double> v = sp[(long long)c * nk + k];
-        re += v.re;
-        im += v.im;
+    if (k < nk)
+        for (int c = l; c < chunks; c += KL) {
+            const C2<double> v = sp[(long long)c * nk + k];
+            re += v.re;
+            im += v.im;
+        }
+#pragma unroll
+    for (int o = KL / 2; o > 0; o >>= 1) {
+        re += __shfl_xor_sync(0xffffffffu, re, o, KL);
+        im += __shfl_xor_sync(0xffffffffu, im, o, KL);
     }
     return make_double2(re, im);
 }
@@ -247,10 +268,11 @@ template <typename R>
 __global__ void ew_sreduce(EwArgs A) {
     __shared__ Fx128 se[8], sq1[8], sq2[8];
     if (A.skip && *A.skip) return;
-    const int k = blockIdx.x * blockDim.x + threadIdx.x;
+    const int k = (blockIdx.x * blockDim.x + threadIdx.x) / KL;
+    const int l = threadIdx.x % KL;
     double e = 0.0;
-    if (k < A.nk) {
-        const double2 S = chunk_sum<R>((const C2<R>*)A.Spart, A.chunks, A.nk, k);
+    const double2 S = chunk_sum<R>((const C2<R>*)A.Spart, A.chunks, A.nk, k, l);
+    if (k < A.nk && l == 0) {
         A.S[k] = S;
         const double ck = A.kvec64[k].w;
         ((C2<R>*)A.wS)[k] = C2<R>{(R)(ck * S.x), (R)(ck * S.y)};
@@ -379,38 +401,57 @@ __global__ void __launch_bounds__(EW_THREADS) ew_field(EwArgs A) {
     }
 }
 
-// sum of the k-split partials of one atom: compensated FP32 (two-sum) widened
-// once in the mixed path, FP64 in the FP64 path
+// Sum of the k-split partials of one atom by FL lanes (lane l takes splits l,
+// l + FL, ...), combined by a fixed shuffle tree: compensated FP32 (two-sum)
+// widened once in the mixed path, FP64 in the FP64 path.  Every lane of the
+// group ends with the sums.
+constexpr int FL = 8;
+
 template <typename R>
-__device__ __forceinline__ void split_sum(const R* fp, int splits, int n, int i, double f[4]);
+__device__ __forceinline__ void split_sum(const R* fp, int splits, int n, int i, int l, double f[4]);
 template <>
-__device__ __forceinline__ void split_sum<float>(const float* fp, int splits, int n, int i, double f[4]) {
+__device__ __forceinline__ void split_sum<float>(const float* fp, int splits, int n, int i, int l, double f[4]) {
     float s[4] = {0, 0, 0, 0}, c[4] = {0, 0, 0, 0};
-    for (int q = 0; q < splits; ++q) {
-        const F4 v = *(const F4*)(fp + 4 * ((long long)q * n + i));
-        add_c(v.x, s[0], c[0]);
-        add_c(v.y, s[1], c[1]);
-        add_c(v.z, s[2], c[2]);
-        add_c(v.w, s[3], c[3]);
-    }
+    if (i < n)
+        for (int q = l; q < splits; q += FL) {
+            const F4 v = *(const F4*)(fp + 4 * ((long long)q * n + i));
+            add_c(v.x, s[0], c[0]);
+            add_c(v.y, s[1], c[1]);
+            add_c(v.z, s[2], c[2]);
+            add_c(v.w, s[3], c[3]);
+        }
+#pragma unroll
+    for (int o = FL / 2; o > 0; o >>= 1)
+#pragma unroll
+        for (int k = 0; k < 4; ++k) {
+            const float os = __shfl_xor_sync(0xffffffffu, s[k], o, FL), oc = __shfl_xor_sync(0xffffffffu, c[k], o, FL);
+            add_c(os, s[k], c[k]);
+            c[k] += oc;
+        }
     for (int k = 0; k < 4; ++k) f[k] = (double)s[k] + (double)c[k];
 }
 template <>
-__device__ __forceinline__ void split_sum<double>(const double* fp, int splits, int n, int i, double f[4]) {
+__device__ __forceinline__ void split_sum<double>(const double* fp, int splits, int n, int i, int l, double f[4]) {
     for (int k = 0; k < 4; ++k) f[k] = 0.0;
-    for (int q = 0; q < splits; ++q)
-        for (int k = 0; k < 4; ++k) f[k] += fp[4 * ((long long)q * n + i) + k];
+    if (i < n)
+        for (int q = l; q < splits; q += FL)
+            for (int k = 0; k < 4; ++k) f[k] += fp[4 * ((long long)q * n + i) + k];
+#pragma unroll
+    for (int o = FL / 2; o > 0; o >>= 1)
+#pragma unroll
+        for (int k = 0; k < 4; ++k) f[k] += __shfl_xor_sync(0xffffffffu, f[k], o, FL);
 }
 
 template <typename R>
 __global__ void ew_finish(EwArgs A) {
     __shared__ Fx128 sw[EW_THREADS / 32][6];
     if (A.skip && *A.skip) return;
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    const int i = (blockIdx.x * blockDim.x + threadIdx.x) / FL;
+    const int l = threadIdx.x % FL;
     double w[6] = {0, 0, 0, 0, 0, 0};
-    if (i < A.n) {
-        double f[4];
-        split_sum<R>((const R*)A.Fpart, A.splits, A.n, i, f);
+    double f[4];
+    split_sum<R>((const R*)A.Fpart, A.splits, A.n, i, l, f);
+    if (i < A.n && l == 0) {
         const double q = A.qs[i];
         const double pre = q / A.volume_eps;
         const double F0 = pre * f[0], F1 = pre * f[1], F2 = pre * f[2];
@@ -528,8 +569,8 @@ static void ew_shape(const pg_context* ctx, int& chunks, int& chunk, int& splits
     sps = cdiv(nseg, splits);
     splits = cdiv(nseg, sps);
     prep_blocks = cdiv(n, EW_THREADS);
-    kred_blocks = cdiv(std::max(ctx->ew_nk, 1), 256);
-    fin_blocks = cdiv(n, EW_THREADS);
+    kred_blocks = cdiv((long long)std::max(ctx->ew_nk, 1) * KL, 256);
+    fin_blocks = cdiv((long long)n * FL, EW_THREADS);
 }
 
 template <typename R>

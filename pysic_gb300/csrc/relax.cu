@@ -144,6 +144,91 @@ __global__ void rx_init_stat(RxArgs A) {
     }
 }
 
+// The whole per-step bookkeeping in one block, for systems of up to
+// FUSED_MAX atoms: mean of chi, forces and the second half of the rate update,
+// the stop test and -- unless the loop stops -- the next step's charge update
+// (so one step is the electronegativity kernels plus this one launch).  Same
+// formulas and order of operations as rx_update ... rx_stop; sums in FP64 in a
+// fixed order.  stat[3] carries the largest |dq| of the update to the next
+// stop test.
+constexpr int FUSED_THREADS = 1024;
+constexpr int FUSED_MAX = 65536;
+
+__device__ __forceinline__ double block_reduce(double v, bool is_max, double* sh) {
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5, nw = blockDim.x >> 5;
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+        const double u = __shfl_xor_sync(0xffffffffu, v, o);
+        v = is_max ? fmax(v, u) : v + u;
+    }
+    __syncthreads();
+    if (lane == 0) sh[w] = v;
+    __syncthreads();
+    if (w == 0) {
+        v = lane < nw ? sh[lane] : (is_max ? -1e300 : 0.0);
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) {
+            const double u = __shfl_xor_sync(0xffffffffu, v, o);
+            v = is_max ? fmax(v, u) : v + u;
+        }
+        if (lane == 0) sh[0] = v;
+    }
+    __syncthreads();
+    return sh[0];
+}
+
+template <bool INIT>
+__global__ void __launch_bounds__(FUSED_THREADS) rx_fused(RxArgs A) {
+    __shared__ double sh[32];
+    __shared__ int s_stop;
+    if (A.flag[0]) return;
+    const int t = threadIdx.x, nt = blockDim.x;
+    double s = 0.0;
+    for (int i = t; i < A.n; i += nt) s += A.chi[i];
+    const double mean = block_reduce(s, false, sh) / A.n;
+    double e = -1e300;
+    for (int i = t; i < A.n; i += nt) {
+        double f = A.chi[i] - mean;
+        A.force[i] = f;
+        if (!INIT) A.rate[i] = (A.rate[i] + f * 0.5 * A.inv_m * A.dt) / (1.0 + 0.5 * A.friction * A.dt);
+        if (!isfinite(f)) f = __longlong_as_double(0x7ff0000000000000ll);
+        e = fmax(e, f);
+    }
+    e = block_reduce(e, true, sh);
+    if (t == 0) {
+        int stop;
+        if (INIT) {
+            A.stat[0] = e;
+            A.stat[1] = 0.0;
+            // the reference's loop starts from error = 2 tol and runs while error > tol
+            stop = A.n_steps <= 0 || !(2.0 * A.tol > A.tol);
+        } else {
+            const int steps = A.flag[1] + 1;
+            A.flag[1] = steps;
+            A.stat[0] = e;
+            A.stat[1] = A.stat[3];
+            stop = e <= A.tol || steps >= A.n_steps || !isfinite(e);
+        }
+        if (stop) A.flag[0] = 1;
+        s_stop = stop;
+    }
+    __syncthreads();
+    if (s_stop) return;
+    // the next step's update (rx_update)
+    double dqm = 0.0;
+    for (int i = t; i < A.n; i += nt) {
+        const double r = A.rate[i], f = A.force[i];
+        const double dq = r * A.dt + (f - A.friction * r) * A.inv_m * A.dt * A.dt;
+        const double q = A.q[i] + dq;
+        A.q[i] = q;
+        if (A.disp) A.disp[i].w = (float)q;
+        A.rate[i] = (1.0 - 0.5 * A.friction * A.dt) * r + f * 0.5 * A.inv_m * A.dt;
+        dqm = fmax(dqm, fabs(dq));
+    }
+    dqm = block_reduce(dqm, true, sh);
+    if (t == 0) A.stat[3] = dqm;
+}
+
 }  // namespace
 
 // electronegativities of the current charges into ctx->out_chi, stopped by `skip`
@@ -151,6 +236,26 @@ static void enqueue_chi(pg_context* ctx, int precision, const int* skip) {
     const int G = pair_lanes_for(ctx);
     launch_pair_kernel_skip(ctx, precision, PG_WANT_ENEGS, true, true, G, nullptr, skip);
     if (ctx->ewald) launch_ewald_kspace_skip(ctx, precision, PG_WANT_ENEGS, true, false, nullptr, skip);
+}
+
+// results of a finished loop to the host; not converging is an error status
+static void finish_relax(pg_context* ctx, const RxArgs& A, int n, double tolerance, double* rates, double* charges,
+                         int* steps, double* error, double* max_dq) {
+    cudaStream_t st = ctx->stream;
+    int h_flag[2] = {0, 0};
+    double h_stat[3] = {0.0, 0.0, 0.0};
+    PG_CUDA(cudaMemcpyAsync(h_stat, A.stat, sizeof(double) * 3, cudaMemcpyDeviceToHost, st));
+    PG_CUDA(cudaMemcpyAsync(rates, A.rate, sizeof(double) * n, cudaMemcpyDeviceToHost, st));
+    PG_CUDA(cudaMemcpyAsync(charges, A.q, sizeof(double) * n, cudaMemcpyDeviceToHost, st));
+    PG_CUDA(cudaMemcpyAsync(h_flag, A.flag, sizeof(h_flag), cudaMemcpyDeviceToHost, st));
+    PG_CUDA(cudaStreamSynchronize(st));
+    *steps = h_flag[1];
+    *error = h_stat[0];
+    *max_dq = h_stat[1];
+    if (!std::isfinite(h_stat[0]))
+        throw Error(PG_ERR_NOT_CONVERGED, "charge relaxation diverged (non-finite electronegativity differences)");
+    if (!(h_stat[0] <= tolerance))
+        throw Error(PG_ERR_NOT_CONVERGED, "charge relaxation reached its step limit before the tolerance");
 }
 
 void relax_charges(pg_context* ctx, int precision, int n_steps, double dt, double inertia, double friction,
@@ -189,8 +294,57 @@ void relax_charges(pg_context* ctx, int precision, int n_steps, double dt, doubl
         launch_disp(ctx, nullptr);
         A.disp = ctx->disp32.p;
     }
+    const bool fused = n <= FUSED_MAX;
     // initial differences (relaxation.py:433)
     enqueue_chi(ctx, precision, A.flag);
+    if (fused) {
+        rx_fused<true><<<1, FUSED_THREADS, 0, st>>>(A);
+        PG_CHECK_LAUNCH();
+        // one step (electronegativity kernels + bookkeeping) as a CUDA graph,
+        // replayed: every kernel of it checks the stop flag first.  The buffers
+        // it uses were sized by the initial evaluation above.
+        cudaGraphExec_t step = nullptr;
+        if (ctx->use_graphs) {
+            cudaGraph_t g = nullptr;
+            PG_CUDA(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
+            try {
+                enqueue_chi(ctx, precision, A.flag);
+                rx_fused<false><<<1, FUSED_THREADS, 0, st>>>(A);
+            } catch (...) {
+                cudaStreamEndCapture(st, &g);
+                if (g) cudaGraphDestroy(g);
+                throw;
+            }
+            PG_CUDA(cudaStreamEndCapture(st, &g));
+            const cudaError_t e = cudaGraphInstantiate(&step, g, 0);
+            cudaGraphDestroy(g);
+            PG_CUDA(e);
+        }
+        struct Drop {
+            cudaGraphExec_t& x;
+            ~Drop() {
+                if (x) cudaGraphExecDestroy(x);
+            }
+        } drop{step};
+        int h_flag[2] = {0, 0};
+        int chunk = 4;
+        for (int c = 0; c < (1 << 20) && !h_flag[0]; ++c) {
+            for (int k = 0; k < chunk; ++k) {
+                if (step) {
+                    PG_CUDA(cudaGraphLaunch(step, st));
+                } else {
+                    enqueue_chi(ctx, precision, A.flag);
+                    rx_fused<false><<<1, FUSED_THREADS, 0, st>>>(A);
+                }
+            }
+            PG_CHECK_LAUNCH();
+            PG_CUDA(cudaMemcpyAsync(h_flag, A.flag, sizeof(h_flag), cudaMemcpyDeviceToHost, st));
+            PG_CUDA(cudaStreamSynchronize(st));
+            chunk = std::min(chunk * 2, 64);
+        }
+        finish_relax(ctx, A, n, tolerance, rates, charges, steps, error, max_dq);
+        return;
+    }
     rx_block_sums<<<nb, RT, 0, st>>>(A);
     rx_mean<<<1, 32, 0, st>>>(A);
     rx_force<true><<<nb, RT, 0, st>>>(A);
@@ -216,18 +370,8 @@ void relax_charges(pg_context* ctx, int precision, int n_steps, double dt, doubl
         PG_CUDA(cudaStreamSynchronize(st));
         chunk = std::min(chunk * 2, 64);
     }
-    PG_CUDA(cudaMemcpyAsync(h_stat, A.stat, sizeof(double) * 3, cudaMemcpyDeviceToHost, st));
-    PG_CUDA(cudaMemcpyAsync(rates, A.rate, sizeof(double) * n, cudaMemcpyDeviceToHost, st));
-    PG_CUDA(cudaMemcpyAsync(charges, A.q, sizeof(double) * n, cudaMemcpyDeviceToHost, st));
-    PG_CUDA(cudaMemcpyAsync(h_flag, A.flag, sizeof(h_flag), cudaMemcpyDeviceToHost, st));
-    PG_CUDA(cudaStreamSynchronize(st));
-    *steps = h_flag[1];
-    *error = h_stat[0];
-    *max_dq = h_stat[1];
-    if (!std::isfinite(h_stat[0]))
-        throw Error(PG_ERR_NOT_CONVERGED, "charge relaxation diverged (non-finite electronegativity differences)");
-    if (!(h_stat[0] <= tolerance))
-        throw Error(PG_ERR_NOT_CONVERGED, "charge relaxation reached its step limit before the tolerance");
+    (void)h_stat;
+    finish_relax(ctx, A, n, tolerance, rates, charges, steps, error, max_dq);
 }
 
 }  // namespace pg
