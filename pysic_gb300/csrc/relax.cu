@@ -3,18 +3,24 @@
 // The reference loop (pysic/charges/relaxation.py:417-450) crosses into the
 // Fortran core for every electronegativity evaluation and copies the arrays
 // back each step.  Here one step is a fixed sequence of launches on the
-// context's stream:
+// context's stream, captured once as a CUDA graph and replayed:
 //
-//   rx_update      q += q' dt + (F - gamma q') dt^2 / M ;  q' = (1 - gamma dt/2) q' + F dt / (2M)
-//   electronegativity kernels (pair kernel + k-space Ewald) on the new q
-//   rx_mean        mean(chi) over all atoms (deterministic FP64 sum)
-//   rx_force       F = chi - mean ;  q' = (q' + F dt/(2M)) / (1 + gamma dt/2) ;  max F, max |dq|
-//   rx_stop        error = max F (signed, relaxation.py:449); stop when error <= tol or steps reached
+//   electronegativity kernels (pair kernel + k-space Ewald) on the current q
+//   rx_mean    block sums of chi; the last block to finish forms mean(chi)
+//   rx_force   F = chi - mean;  q' = (q' + F dt/(2M)) / (1 + gamma dt/2);
+//              the last block takes error = max F (signed, relaxation.py:449)
+//              and decides: stop when error <= tol, at the step limit, or when
+//              the error is not finite (diverging dynamics)
+//   rx_update  unless stopped: q += q' dt + (F - gamma q') dt^2 / M;
+//              q' = (1 - gamma dt/2) q' + F dt / (2M); the last block takes max |dq|
 //
-// Every kernel first reads a device flag and returns at once when the loop has
-// stopped, so the host can enqueue a chunk of steps and read back only the
-// flag and the statistics once per chunk.  Convergence statistics and charge
-// sums are kept in FP64.
+// The initial pass (relaxation.py:433) is the electronegativities, rx_mean,
+// rx_force<INIT> and the first rx_update.  Every kernel first reads a device
+// flag and returns at once when the loop has stopped, so the host enqueues
+// chunks of steps and reads back only the flag once per chunk.  The "last
+// block" of a kernel is found with an integer ticket (an atomic counter, no
+// waiting); it combines the per-block partials in block order, so every
+// statistic is deterministic.  Charges, rates and statistics are FP64.
 #include <algorithm>
 #include <cmath>
 #include <vector>
@@ -37,15 +43,101 @@ struct RxArgs {
     const double* chi;
     double dt, inv_m, friction, tol;
     int n_steps;
-    int* flag;        // [0] stop flag, [1] steps taken
-    double* stat;     // [0] error, [1] max |dq| of the last step, [2] mean chi
+    int* flag;        // [0] stop flag, [1] steps taken, [2..4] tickets of rx_mean, rx_force, rx_update
+    double* stat;     // [0] error, [1] max |dq| reported, [2] mean chi, [3] max |dq| of the last update
     double* part;     // per block: sum chi, max F, max |dq|
     int nblocks;
     F4* disp;         // mixed path: the FP32 charge copy in .w follows q (null: FP64 path)
 };
 
-__global__ void rx_update(RxArgs A) {
-    __shared__ double sm[RT];
+// block-wide sum or max; the result is valid in thread 0
+__device__ __forceinline__ double block_reduce(double v, bool is_max, double* sh) {
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5, nw = blockDim.x >> 5;
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+        const double u = __shfl_xor_sync(0xffffffffu, v, o);
+        v = is_max ? fmax(v, u) : v + u;
+    }
+    if (lane == 0) sh[w] = v;
+    __syncthreads();
+    if (w == 0) {
+        v = lane < nw ? sh[lane] : (is_max ? -1e300 : 0.0);
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) {
+            const double u = __shfl_xor_sync(0xffffffffu, v, o);
+            v = is_max ? fmax(v, u) : v + u;
+        }
+    }
+    return v;
+}
+
+// true in thread 0 of the block that takes the last ticket: by then every other
+// block has published its partial (fence before the ticket).  The last block
+// puts the counter back to zero for the next launch.
+__device__ __forceinline__ bool last_block(int* ticket) {
+    __shared__ int is_last;
+    if (threadIdx.x == 0) {
+        __threadfence();
+        const int last = atomicAdd(ticket, 1) == (int)gridDim.x - 1;
+        if (last) *ticket = 0;
+        is_last = last;
+    }
+    __syncthreads();
+    return is_last && threadIdx.x == 0;
+}
+
+__global__ void __launch_bounds__(RT) rx_mean(RxArgs A) {
+    __shared__ double sh[RT / 32];
+    if (A.flag[0]) return;
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    const double s = block_reduce(i < A.n ? A.chi[i] : 0.0, false, sh);
+    if (threadIdx.x == 0) A.part[3 * blockIdx.x] = s;
+    if (last_block(A.flag + 2)) {
+        const volatile double* p = A.part;
+        double t = 0.0;
+        for (int b = 0; b < A.nblocks; ++b) t += p[3 * b];
+        A.stat[2] = t / A.n;
+    }
+}
+
+template <bool INIT>
+__global__ void __launch_bounds__(RT) rx_force(RxArgs A) {
+    __shared__ double sh[RT / 32];
+    if (A.flag[0]) return;
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    double f = -1e300;
+    if (i < A.n) {
+        f = A.chi[i] - A.stat[2];
+        A.force[i] = f;
+        if (!INIT) A.rate[i] = (A.rate[i] + f * 0.5 * A.inv_m * A.dt) / (1.0 + 0.5 * A.friction * A.dt);
+        // a non-finite force must not vanish in fmax (which drops NaN): it
+        // becomes +inf, so the stop test sees it and the loop ends as diverged
+        if (!isfinite(f)) f = __longlong_as_double(0x7ff0000000000000ll);
+    }
+    const double m = block_reduce(f, true, sh);
+    if (threadIdx.x == 0) A.part[3 * blockIdx.x + 1] = m;
+    if (last_block(A.flag + 3)) {
+        const volatile double* p = A.part;
+        double e = -1e300;
+        for (int b = 0; b < A.nblocks; ++b) e = fmax(e, p[3 * b + 1]);
+        A.stat[0] = e;
+        int stop;
+        if (INIT) {
+            A.stat[1] = 0.0;
+            // the reference's loop starts from error = 2 tol and runs while error > tol
+            stop = A.n_steps <= 0 || !(2.0 * A.tol > A.tol);
+        } else {
+            const int steps = A.flag[1] + 1;
+            A.flag[1] = steps;
+            A.stat[1] = A.stat[3];
+            stop = e <= A.tol || steps >= A.n_steps || !isfinite(e);
+        }
+        if (stop) A.flag[0] = 1;
+    }
+}
+
+__global__ void __launch_bounds__(RT) rx_update(RxArgs A) {
+    __shared__ double sh[RT / 32];
     if (A.flag[0]) return;
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     double dq = 0.0;
@@ -57,176 +149,14 @@ __global__ void rx_update(RxArgs A) {
         if (A.disp) A.disp[i].w = (float)q;
         A.rate[i] = (1.0 - 0.5 * A.friction * A.dt) * r + f * 0.5 * A.inv_m * A.dt;
     }
-    sm[threadIdx.x] = fabs(dq);
-    __syncthreads();
-    for (int s = blockDim.x / 2; s > 0; s >>= 1) {
-        if (threadIdx.x < s) sm[threadIdx.x] = fmax(sm[threadIdx.x], sm[threadIdx.x + s]);
-        __syncthreads();
+    const double m = block_reduce(fabs(dq), true, sh);
+    if (threadIdx.x == 0) A.part[3 * blockIdx.x + 2] = m;
+    if (last_block(A.flag + 4)) {
+        const volatile double* p = A.part;
+        double d = 0.0;
+        for (int b = 0; b < A.nblocks; ++b) d = fmax(d, p[3 * b + 2]);
+        A.stat[3] = d;
     }
-    if (threadIdx.x == 0) A.part[3 * blockIdx.x + 2] = sm[0];
-}
-
-// mean of chi: per-block sums in rx_block_sums, then a single block adds them in order
-__global__ void rx_block_sums(RxArgs A) {
-    __shared__ double sm[RT];
-    if (A.flag[0]) return;
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    sm[threadIdx.x] = i < A.n ? A.chi[i] : 0.0;
-    __syncthreads();
-    for (int s = blockDim.x / 2; s > 0; s >>= 1) {
-        if (threadIdx.x < s) sm[threadIdx.x] += sm[threadIdx.x + s];
-        __syncthreads();
-    }
-    if (threadIdx.x == 0) A.part[3 * blockIdx.x] = sm[0];
-}
-
-__global__ void rx_mean(RxArgs A) {
-    if (A.flag[0]) return;
-    if (threadIdx.x == 0) {
-        double s = 0.0, c = 0.0;
-        for (int b = 0; b < A.nblocks; ++b) {
-            const double y = A.part[3 * b] - c;
-            const double t = s + y;
-            c = (t - s) - y;
-            s = t;
-        }
-        A.stat[2] = s / A.n;
-    }
-}
-
-template <bool INIT>
-__global__ void rx_force(RxArgs A) {
-    __shared__ double sm[RT];
-    if (A.flag[0]) return;
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    double f = -1e300;
-    if (i < A.n) {
-        f = A.chi[i] - A.stat[2];
-        A.force[i] = f;
-        // a non-finite force must not vanish in fmax (which drops NaN): it
-        // becomes +inf, so the stop test sees it and the loop ends as diverged
-        if (!isfinite(f)) f = __longlong_as_double(0x7ff0000000000000ll);
-        if (!INIT) A.rate[i] = (A.rate[i] + f * 0.5 * A.inv_m * A.dt) / (1.0 + 0.5 * A.friction * A.dt);
-    }
-    sm[threadIdx.x] = f;
-    __syncthreads();
-    for (int s = blockDim.x / 2; s > 0; s >>= 1) {
-        if (threadIdx.x < s) sm[threadIdx.x] = fmax(sm[threadIdx.x], sm[threadIdx.x + s]);
-        __syncthreads();
-    }
-    if (threadIdx.x == 0) A.part[3 * blockIdx.x + 1] = sm[0];
-}
-
-__global__ void rx_stop(RxArgs A) {
-    if (A.flag[0]) return;
-    if (threadIdx.x == 0) {
-        double e = -1e300, dq = 0.0;
-        for (int b = 0; b < A.nblocks; ++b) {
-            e = fmax(e, A.part[3 * b + 1]);
-            dq = fmax(dq, A.part[3 * b + 2]);
-        }
-        const int steps = A.flag[1] + 1;
-        A.flag[1] = steps;
-        A.stat[0] = e;
-        A.stat[1] = dq;
-        // stop on convergence, on the step limit, or when the error is no
-        // longer a finite number (diverging dynamics)
-        if (e <= A.tol || steps >= A.n_steps || !isfinite(e)) A.flag[0] = 1;
-    }
-}
-
-__global__ void rx_init_stat(RxArgs A) {
-    if (threadIdx.x == 0) {
-        double e = -1e300;
-        for (int b = 0; b < A.nblocks; ++b) e = fmax(e, A.part[3 * b + 1]);
-        A.stat[0] = e;
-        A.stat[1] = 0.0;
-    }
-}
-
-// The whole per-step bookkeeping in one block, for systems of up to
-// FUSED_MAX atoms: mean of chi, forces and the second half of the rate update,
-// the stop test and -- unless the loop stops -- the next step's charge update
-// (so one step is the electronegativity kernels plus this one launch).  Same
-// formulas and order of operations as rx_update ... rx_stop; sums in FP64 in a
-// fixed order.  stat[3] carries the largest |dq| of the update to the next
-// stop test.
-constexpr int FUSED_THREADS = 1024;
-constexpr int FUSED_MAX = 65536;
-
-__device__ __forceinline__ double block_reduce(double v, bool is_max, double* sh) {
-    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5, nw = blockDim.x >> 5;
-#pragma unroll
-    for (int o = 16; o > 0; o >>= 1) {
-        const double u = __shfl_xor_sync(0xffffffffu, v, o);
-        v = is_max ? fmax(v, u) : v + u;
-    }
-    __syncthreads();
-    if (lane == 0) sh[w] = v;
-    __syncthreads();
-    if (w == 0) {
-        v = lane < nw ? sh[lane] : (is_max ? -1e300 : 0.0);
-#pragma unroll
-        for (int o = 16; o > 0; o >>= 1) {
-            const double u = __shfl_xor_sync(0xffffffffu, v, o);
-            v = is_max ? fmax(v, u) : v + u;
-        }
-        if (lane == 0) sh[0] = v;
-    }
-    __syncthreads();
-    return sh[0];
-}
-
-template <bool INIT>
-__global__ void __launch_bounds__(FUSED_THREADS) rx_fused(RxArgs A) {
-    __shared__ double sh[32];
-    __shared__ int s_stop;
-    if (A.flag[0]) return;
-    const int t = threadIdx.x, nt = blockDim.x;
-    double s = 0.0;
-    for (int i = t; i < A.n; i += nt) s += A.chi[i];
-    const double mean = block_reduce(s, false, sh) / A.n;
-    double e = -1e300;
-    for (int i = t; i < A.n; i += nt) {
-        double f = A.chi[i] - mean;
-        A.force[i] = f;
-        if (!INIT) A.rate[i] = (A.rate[i] + f * 0.5 * A.inv_m * A.dt) / (1.0 + 0.5 * A.friction * A.dt);
-        if (!isfinite(f)) f = __longlong_as_double(0x7ff0000000000000ll);
-        e = fmax(e, f);
-    }
-    e = block_reduce(e, true, sh);
-    if (t == 0) {
-        int stop;
-        if (INIT) {
-            A.stat[0] = e;
-            A.stat[1] = 0.0;
-            // the reference's loop starts from error = 2 tol and runs while error > tol
-            stop = A.n_steps <= 0 || !(2.0 * A.tol > A.tol);
-        } else {
-            const int steps = A.flag[1] + 1;
-            A.flag[1] = steps;
-            A.stat[0] = e;
-            A.stat[1] = A.stat[3];
-            stop = e <= A.tol || steps >= A.n_steps || !isfinite(e);
-        }
-        if (stop) A.flag[0] = 1;
-        s_stop = stop;
-    }
-    __syncthreads();
-    if (s_stop) return;
-    // the next step's update (rx_update)
-    double dqm = 0.0;
-    for (int i = t; i < A.n; i += nt) {
-        const double r = A.rate[i], f = A.force[i];
-        const double dq = r * A.dt + (f - A.friction * r) * A.inv_m * A.dt * A.dt;
-        const double q = A.q[i] + dq;
-        A.q[i] = q;
-        if (A.disp) A.disp[i].w = (float)q;
-        A.rate[i] = (1.0 - 0.5 * A.friction * A.dt) * r + f * 0.5 * A.inv_m * A.dt;
-        dqm = fmax(dqm, fabs(dq));
-    }
-    dqm = block_reduce(dqm, true, sh);
-    if (t == 0) A.stat[3] = dqm;
 }
 
 }  // namespace
@@ -270,8 +200,9 @@ void relax_charges(pg_context* ctx, int precision, int n_steps, double dt, doubl
     ctx->rq_rate.upload(rates, (size_t)n, st);
     ctx->rq_force.resize((size_t)std::max(n, 1));
     ctx->rq_stat.resize(4 + 3 * (size_t)nb);
-    ctx->rq_flag.resize(2);
-    PG_CUDA(cudaMemsetAsync(ctx->rq_flag.p, 0, sizeof(int) * 2, st));
+    ctx->rq_flag.resize(8);
+    // stop flag, step count and the three tickets start at zero
+    PG_CUDA(cudaMemsetAsync(ctx->rq_flag.p, 0, sizeof(int) * 8, st));
     RxArgs A{};
     A.n = n;
     A.q = ctx->charge.p;
@@ -294,83 +225,54 @@ void relax_charges(pg_context* ctx, int precision, int n_steps, double dt, doubl
         launch_disp(ctx, nullptr);
         A.disp = ctx->disp32.p;
     }
-    const bool fused = n <= FUSED_MAX;
-    // initial differences (relaxation.py:433)
+    // initial differences (relaxation.py:433) and the first update
     enqueue_chi(ctx, precision, A.flag);
-    if (fused) {
-        rx_fused<true><<<1, FUSED_THREADS, 0, st>>>(A);
-        PG_CHECK_LAUNCH();
-        // one step (electronegativity kernels + bookkeeping) as a CUDA graph,
-        // replayed: every kernel of it checks the stop flag first.  The buffers
-        // it uses were sized by the initial evaluation above.
-        cudaGraphExec_t step = nullptr;
-        if (ctx->use_graphs) {
-            cudaGraph_t g = nullptr;
-            PG_CUDA(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
-            try {
-                enqueue_chi(ctx, precision, A.flag);
-                rx_fused<false><<<1, FUSED_THREADS, 0, st>>>(A);
-            } catch (...) {
-                cudaStreamEndCapture(st, &g);
-                if (g) cudaGraphDestroy(g);
-                throw;
-            }
-            PG_CUDA(cudaStreamEndCapture(st, &g));
-            const cudaError_t e = cudaGraphInstantiate(&step, g, 0);
-            cudaGraphDestroy(g);
-            PG_CUDA(e);
-        }
-        struct Drop {
-            cudaGraphExec_t& x;
-            ~Drop() {
-                if (x) cudaGraphExecDestroy(x);
-            }
-        } drop{step};
-        int h_flag[2] = {0, 0};
-        int chunk = 4;
-        for (int c = 0; c < (1 << 20) && !h_flag[0]; ++c) {
-            for (int k = 0; k < chunk; ++k) {
-                if (step) {
-                    PG_CUDA(cudaGraphLaunch(step, st));
-                } else {
-                    enqueue_chi(ctx, precision, A.flag);
-                    rx_fused<false><<<1, FUSED_THREADS, 0, st>>>(A);
-                }
-            }
-            PG_CHECK_LAUNCH();
-            PG_CUDA(cudaMemcpyAsync(h_flag, A.flag, sizeof(h_flag), cudaMemcpyDeviceToHost, st));
-            PG_CUDA(cudaStreamSynchronize(st));
-            chunk = std::min(chunk * 2, 64);
-        }
-        finish_relax(ctx, A, n, tolerance, rates, charges, steps, error, max_dq);
-        return;
-    }
-    rx_block_sums<<<nb, RT, 0, st>>>(A);
-    rx_mean<<<1, 32, 0, st>>>(A);
+    rx_mean<<<nb, RT, 0, st>>>(A);
     rx_force<true><<<nb, RT, 0, st>>>(A);
-    rx_init_stat<<<1, 32, 0, st>>>(A);
+    rx_update<<<nb, RT, 0, st>>>(A);
     PG_CHECK_LAUNCH();
+    auto one_step = [&] {
+        enqueue_chi(ctx, precision, A.flag);
+        rx_mean<<<nb, RT, 0, st>>>(A);
+        rx_force<false><<<nb, RT, 0, st>>>(A);
+        rx_update<<<nb, RT, 0, st>>>(A);
+    };
+    // one step as a CUDA graph, replayed; the buffers it uses were sized by the
+    // initial pass above
+    cudaGraphExec_t step = nullptr;
+    if (ctx->use_graphs) {
+        cudaGraph_t g = nullptr;
+        PG_CUDA(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
+        try {
+            one_step();
+        } catch (...) {
+            cudaStreamEndCapture(st, &g);
+            if (g) cudaGraphDestroy(g);
+            throw;
+        }
+        PG_CUDA(cudaStreamEndCapture(st, &g));
+        const cudaError_t e = cudaGraphInstantiate(&step, g, 0);
+        cudaGraphDestroy(g);
+        PG_CUDA(e);
+    }
+    struct Drop {
+        cudaGraphExec_t& x;
+        ~Drop() {
+            if (x) cudaGraphExecDestroy(x);
+        }
+    } drop{step};
     int h_flag[2] = {0, 0};
-    double h_stat[3] = {2.0 * tolerance, 0.0, 0.0};
-    if (n_steps <= 0 || !(2.0 * tolerance > tolerance)) h_flag[0] = 1;
-    // chunks of steps: all kernels test the stop flag, the host polls once per chunk
     int chunk = 4;
-    const int max_launch_chunks = 1 << 20;
-    for (int c = 0; c < max_launch_chunks && !h_flag[0]; ++c) {
-        for (int s = 0; s < chunk; ++s) {
-            rx_update<<<nb, RT, 0, st>>>(A);
-            enqueue_chi(ctx, precision, A.flag);
-            rx_block_sums<<<nb, RT, 0, st>>>(A);
-            rx_mean<<<1, 32, 0, st>>>(A);
-            rx_force<false><<<nb, RT, 0, st>>>(A);
-            rx_stop<<<1, 32, 0, st>>>(A);
+    for (int c = 0; c < (1 << 20) && !h_flag[0]; ++c) {
+        for (int k = 0; k < chunk; ++k) {
+            if (step) PG_CUDA(cudaGraphLaunch(step, st));
+            else one_step();
         }
         PG_CHECK_LAUNCH();
         PG_CUDA(cudaMemcpyAsync(h_flag, A.flag, sizeof(h_flag), cudaMemcpyDeviceToHost, st));
         PG_CUDA(cudaStreamSynchronize(st));
         chunk = std::min(chunk * 2, 64);
     }
-    (void)h_stat;
     finish_relax(ctx, A, n, tolerance, rates, charges, steps, error, max_dq);
 }
 
