@@ -205,7 +205,15 @@ int pg_bond_order_noalloc(pg_context* ctx, int32_t precision, double* d_forces, 
  *   weights and FP32 arithmetic, trained on the GPU (mean squared error, Adam).
  *   Parameters are FP32 in the order W1 (n_h1 x n_in, row-major), b1, W2
  *   (n_h2 x n_h1), b2, w3 (n_h2), b3.  pg_mlp_gradients returns the loss and
- *   its gradient for the given samples (no update), for gradient checks. */
+ *   its gradient for the given samples (no update), for gradient checks.
+ * pg_mlp_predict_charges: the warm start of a context's structure without
+ *   leaving the device: descriptors (as pg_descriptors), per-type columns added
+ *   in type order into per-element columns (type_element[t] = element index
+ *   of type t, n_types entries), the one-hot element code appended, inputs
+ *   (x - x_mean) / x_scale, the network, q = y * y_scale + y_mean in FP64,
+ *   then shifted by (sum q - total_charge) / N.  The charges replace the
+ *   context's own; charges (N doubles, may be null) receives a copy.  The
+ *   network needs n_in = n_elements x (n_gauss + 1). */
 int pg_descriptors(pg_context* ctx, int32_t n_gauss, double r0, double r1, double width, double cutoff,
                    float* out);
 int pg_mlp_create(pg_mlp** mlp, int32_t n_in, int32_t n_h1, int32_t n_h2, int32_t device);
@@ -219,6 +227,10 @@ int pg_mlp_train(pg_mlp* mlp, int32_t epochs, int32_t batch, float learning_rate
                  float* epoch_loss);
 int pg_mlp_gradients(pg_mlp* mlp, const float* x, const float* y, int64_t n, float* grad, double* loss);
 int pg_mlp_predict(pg_mlp* mlp, const float* x, int64_t n, float* y);
+int pg_mlp_predict_charges(pg_mlp* mlp, pg_context* ctx, int32_t n_gauss, double r0, double r1, double width,
+                           double cutoff, int32_t n_elements, const int32_t* type_element, const float* x_mean,
+                           const float* x_scale, double y_mean, double y_scale, double total_charge,
+                           double* charges);
 
 /* ---- many independent systems ------------------------------------------------
  * No counterpart in the reference, which holds one system per process.  A batch

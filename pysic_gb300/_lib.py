@@ -106,6 +106,10 @@ _SIGNATURES = {
     "pg_mlp_gradients": (ctypes.c_int, [ctypes.c_void_p, _c_float_p, _c_float_p, ctypes.c_int64, _c_float_p,
                                         _c_double_p]),
     "pg_mlp_predict": (ctypes.c_int, [ctypes.c_void_p, _c_float_p, ctypes.c_int64, _c_float_p]),
+    "pg_mlp_predict_charges": (ctypes.c_int, [ctypes.c_void_p, _ctx, ctypes.c_int32, ctypes.c_double,
+                                              ctypes.c_double, ctypes.c_double, ctypes.c_double, ctypes.c_int32,
+                                              _c_int_p, _c_float_p, _c_float_p, ctypes.c_double, ctypes.c_double,
+                                              ctypes.c_double, _c_double_p]),
 }
 
 _lib = None

@@ -325,22 +325,31 @@ class Pysic:
             self.create_neighbor_lists()
             self.neighbor_list.build(s, self._engine)
         else:
-            cell_changed = not (np.array_equal(p["cell"], s.get_cell()) and np.array_equal(p["pbc"], s.get_pbc()))
+            cell, pbc = s.get_cell(), s.get_pbc()
+            cell_changed = not (np.array_equal(p["cell"], cell) and np.array_equal(p["pbc"], pbc))
             if cell_changed:
-                self._engine.set_cell(s.get_cell(), s.get_pbc())
+                self._engine.set_cell(cell, pbc)
                 if self.coulomb is not None:
                     self._model.ewald = None
                     from .model import ewald_settings
                     self._engine.set_ewald(ewald_settings(s, self.coulomb))
-            if not np.array_equal(p["positions"], s.get_positions()) or cell_changed:
-                self._engine.update_positions(s.get_positions())
-            if not np.array_equal(p["charges"], _charges_of(s)):
-                self._engine.update_charges(_charges_of(s))
+            pos = s.get_positions()
+            if not np.array_equal(p["positions"], pos) or cell_changed:
+                self._engine.update_positions(pos)
+            q = _charges_of(s)
+            if not np.array_equal(p["charges"], q):
+                self._engine.update_charges(q)
             if self.neighbor_list is None or not p.get("lists", False) or cell_changed:
                 self.create_neighbor_lists()
                 self.neighbor_list.build(s, self._engine)
             else:
                 self.neighbor_list.update(s, self._engine)
+            # the interaction set compared equal above: its stored copy stays
+            self.charges = q
+            # get_positions / get_cell / ... hand out copies: kept as they are
+            p.update({"positions": np.asarray(pos, dtype=np.float64), "charges": np.array(q, dtype=np.float64),
+                      "cell": cell, "pbc": pbc, "lists": True})
+            return
         self.charges = _charges_of(s)
         self._pushed = {"n": len(s), "positions": s.get_positions(), "charges": _charges_of(s),
                         "cell": s.get_cell(), "pbc": s.get_pbc(), "symbols": s.get_chemical_symbols(),

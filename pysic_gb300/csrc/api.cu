@@ -87,6 +87,20 @@ void prepare(pg_context* ctx) {
 }
 
 // one evaluation, enqueued on ctx->stream; G: lanes per atom of the bond kernels
+// true when no value is an infinity or a NaN: the exponent field is not all
+// ones.  A branch-free integer test over the bit patterns, so the per-call
+// check of a large coordinate array costs a few microseconds.
+static bool all_finite(const double* v, size_t n) {
+    constexpr uint64_t EXP = 0x7ff0000000000000ull;
+    uint64_t bad = 0;
+    for (size_t i = 0; i < n; ++i) {
+        uint64_t u;
+        std::memcpy(&u, v + i, sizeof(u));
+        bad |= (uint64_t)((u & EXP) == EXP);
+    }
+    return bad == 0;
+}
+
 static void enqueue(pg_context* ctx, int precision, int flags, int G) {
     const int n = ctx->n;
     const bool wantF = flags & PG_WANT_FORCES, wantC = flags & PG_WANT_ENEGS, wantE = flags & PG_WANT_ENERGY;
@@ -293,8 +307,7 @@ int pg_create_atoms(pg_context* ctx, int32_t n, const double* positions, const d
         pg::require(n >= 0, PG_ERR_INVALID, "negative atom count");
         pg::require(n == 0 || (positions && charges && types), PG_ERR_INVALID, "null atom arrays");
         for (int i = 0; i < n; ++i) pg::require(types[i] >= 0 && types[i] < 64, PG_ERR_INVALID, "type out of range");
-        for (int i = 0; i < 3 * n; ++i)
-            pg::require(std::isfinite(positions[i]), PG_ERR_INVALID, "non-finite atom position");
+        pg::require(n == 0 || pg::all_finite(positions, 3 * (size_t)n), PG_ERR_INVALID, "non-finite atom position");
         ctx->n = n;
         ctx->pos.upload(positions, 3 * (size_t)n, ctx->stream);
         ctx->charge.upload(charges, (size_t)n, ctx->stream);
@@ -312,9 +325,8 @@ int pg_update_atom_coordinates(pg_context* ctx, const double* positions) {
         check_ctx(ctx);
         use_device(ctx);
         pg::require(ctx->have_atoms, PG_ERR_NOT_READY, "no atoms");
-        bool finite = true;
-        for (int i = 0; i < 3 * ctx->n; ++i) finite &= std::isfinite(positions[i]);
-        pg::require(finite, PG_ERR_INVALID, "non-finite atom position");
+        pg::require(ctx->n == 0 || pg::all_finite(positions, 3 * (size_t)ctx->n), PG_ERR_INVALID,
+                    "non-finite atom position");
         ctx->pos.upload(positions, 3 * (size_t)ctx->n, ctx->stream);
         PG_CUDA(cudaStreamSynchronize(ctx->stream));
     });
@@ -680,6 +692,24 @@ int pg_mlp_predict(pg_mlp* mlp, const float* x, int64_t n, float* y) {
     return guarded([&] {
         check_mlp(mlp);
         pg::mlp_predict(mlp, x, n, y);
+    });
+}
+
+int pg_mlp_predict_charges(pg_mlp* mlp, pg_context* ctx, int32_t n_gauss, double r0, double r1, double width,
+                           double cutoff, int32_t n_elements, const int32_t* type_element, const float* x_mean,
+                           const float* x_scale, double y_mean, double y_scale, double total_charge,
+                           double* charges) {
+    return guarded([&] {
+        check_mlp(mlp);
+        check_ctx(ctx);
+        use_device(ctx);
+        pg::require(type_element && x_mean && x_scale, PG_ERR_INVALID, "null input arrays");
+        pg::require(std::isfinite(y_mean) && std::isfinite(y_scale) && std::isfinite(total_charge), PG_ERR_INVALID,
+                    "non-finite output scaling or total charge");
+        pg::require(n_gauss >= 1 && width > 0 && cutoff > 0 && r1 >= r0, PG_ERR_INVALID,
+                    "invalid descriptor parameters");
+        pg::mlp_predict_charges(mlp, ctx, n_gauss, r0, r1, width, cutoff, n_elements, type_element, x_mean, x_scale,
+                                y_mean, y_scale, total_charge, charges);
     });
 }
 

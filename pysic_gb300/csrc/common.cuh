@@ -266,6 +266,8 @@ struct pg_context {
     bool have_list = false;
     double list_min_cutoff = 0.0;   // smallest per-atom list radius (0: unknown)
     pg::DevBuf<float> mlp_desc;     // descriptors of the warm-start network
+    pg::DevBuf<float> mlp_fold;     // per prediction: type -> element, input mean and scale
+    pg::DevBuf<double> mlp_q;       // per prediction: charges before the total-charge shift, block sums
     double skin = 0.5;
     pg::DevBuf<int> nb_start, nb_idx, nb_off;  // nb_off: 3 per entry
     pg::DevBuf<int> nb_g0;                     // per atom: entries coming from lower-index atoms
@@ -308,7 +310,7 @@ struct pg_context {
     pg::DevBuf<pg::FxAcc> out_acc;  // energy, virial[6], spare: exact fixed-point totals (fixed.cuh)
 
     // charge relaxation
-    pg::DevBuf<double> rq_rate, rq_force, rq_stat;
+    pg::DevBuf<double> rq_rate, rq_save, rq_stat;
     pg::DevBuf<int> rq_flag;
 
     int launches = 0;
@@ -401,6 +403,9 @@ void mlp_clear_samples(pg_mlp* M);
 void mlp_train(pg_mlp* M, int epochs, int batch, float lr, unsigned long long seed, float* epoch_loss);
 void mlp_gradients(pg_mlp* M, const float* x, const float* y, long long n, float* grad, double* loss);
 void mlp_predict(pg_mlp* M, const float* x, long long n, float* y);
+void mlp_predict_charges(pg_mlp* M, pg_context* ctx, int n_gauss, double r0, double r1, double width, double cutoff,
+                         int n_elements, const int* type_element, const float* x_mean, const float* x_scale,
+                         double y_mean, double y_scale, double total_charge, double* charges);
 
 // batch.cu: many systems per launch (struct pg_batch)
 void batch_create(pg_batch** out, int device);

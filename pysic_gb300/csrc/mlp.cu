@@ -20,6 +20,8 @@
 // thread per parameter), so training is deterministic.
 #include <algorithm>
 #include <cmath>
+#include <cstring>
+#include <memory>
 #include <random>
 #include <vector>
 
@@ -267,13 +269,152 @@ __global__ void to_bf16(int np, const float* __restrict__ w, __nv_bfloat16* __re
     if (p < np) wb[p] = __float2bfloat16_rn(w[p]);
 }
 
+// ---- inference -----------------------------------------------------------------
+
+// Parameters in shared memory with odd row strides, so that the lanes of a
+// warp (one hidden unit each) read different banks.
+struct PadLayout {
+    int n_in, n_h1, n_h2, p1, p2;
+    __host__ __device__ explicit PadLayout(const Layout& L)
+        : n_in(L.n_in), n_h1(L.n_h1), n_h2(L.n_h2), p1(L.n_in | 1), p2(L.n_h1 | 1) {}
+    __host__ __device__ int w1() const { return 0; }
+    __host__ __device__ int b1() const { return n_h1 * p1; }
+    __host__ __device__ int w2() const { return b1() + n_h1; }
+    __host__ __device__ int b2() const { return w2() + n_h2 * p2; }
+    __host__ __device__ int w3() const { return b2() + n_h2; }
+    __host__ __device__ int b3() const { return w3() + n_h2; }
+    __host__ __device__ int total() const { return b3() + 1; }
+};
+
+// What the charge prediction needs besides the network: the raw descriptors
+// (per atom type and Gaussian), the element of each type, the input
+// normalisation and the output scale.
+struct FoldArgs {
+    const float* raw;       // n x (T * G)
+    const int* type;        // per atom
+    const int* elem;        // per type: element index
+    const float* x_mean;    // n_in
+    const float* x_scale;   // n_in
+    int T, G, E;
+    double y_mean, y_scale;
+    double* q;              // per atom: predicted charge before the total-charge shift
+    double* part;           // per block: sum of q (block order)
+};
+
+constexpr int INF_THREADS = 256;
+constexpr int INF_WARPS = INF_THREADS / 32;
+
+// One warp per sample (grid-stride), lanes over the hidden units.  Every unit
+// is the same sequential FMA chain as in mlp_forward, and the output the same
+// chain over the second layer, so both kernels give identical results.
+// FOLD: the inputs are formed from the raw descriptors as the host-side
+// fold does (per-type columns added in type order into per-element columns,
+// one-hot element code, (x - mean) / scale), and the charge
+// y * y_scale + y_mean is written in FP64 with per-block sums in a fixed order.
+template <bool FOLD>
+__global__ void __launch_bounds__(INF_THREADS) mlp_infer(Layout L0, const __nv_bfloat16* __restrict__ wb,
+                                                         const float* __restrict__ x, int n, float* __restrict__ out,
+                                                         FoldArgs F) {
+    extern __shared__ float sw[];
+    __shared__ float sx[INF_WARPS][MAX_IN], sh1[INF_WARPS][MAX_H], sh2[INF_WARPS][MAX_H];
+    __shared__ double sq[INF_WARPS];
+    const PadLayout P(L0);
+    for (int q = threadIdx.x; q < L0.total(); q += blockDim.x) {
+        int d;
+        if (q < L0.b1()) d = P.w1() + (q / L0.n_in) * P.p1 + q % L0.n_in;
+        else if (q < L0.w2()) d = P.b1() + (q - L0.b1());
+        else if (q < L0.b2()) d = P.w2() + ((q - L0.w2()) / L0.n_h1) * P.p2 + (q - L0.w2()) % L0.n_h1;
+        else d = P.b2() + (q - L0.b2());  // b2, w3, b3 keep their order
+        sw[d] = __bfloat162float(wb[q]);
+    }
+    __syncthreads();
+    const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    double qsum = 0.0;
+    for (int s = blockIdx.x * INF_WARPS + w; s < n; s += gridDim.x * INF_WARPS) {
+        for (int a = lane; a < L0.n_in; a += 32) {
+            float v;
+            if constexpr (FOLD) {
+                const int EG = F.E * F.G;
+                if (a < EG) {
+                    const int e = a / F.G, k = a % F.G;
+                    v = 0.0f;
+                    for (int t = 0; t < F.T; ++t)
+                        if (F.elem[t] == e) v += F.raw[(long long)s * F.T * F.G + t * F.G + k];
+                } else {
+                    v = F.elem[F.type[s]] == a - EG ? 1.0f : 0.0f;
+                }
+                v = __fdiv_rn(__fsub_rn(v, F.x_mean[a]), F.x_scale[a]);
+            } else {
+                v = x[(long long)s * L0.n_in + a];
+            }
+            sx[w][a] = v;
+        }
+        __syncwarp();
+        for (int j = lane; j < L0.n_h1; j += 32) {
+            const float* wr = sw + P.w1() + j * P.p1;
+            float z = sw[P.b1() + j];
+            for (int a = 0; a < L0.n_in; ++a) z = fmaf(wr[a], sx[w][a], z);
+            sh1[w][j] = tanhf(z);
+        }
+        __syncwarp();
+        for (int k = lane; k < L0.n_h2; k += 32) {
+            const float* wr = sw + P.w2() + k * P.p2;
+            float z = sw[P.b2() + k];
+            for (int j = 0; j < L0.n_h1; ++j) z = fmaf(wr[j], sh1[w][j], z);
+            sh2[w][k] = tanhf(z);
+        }
+        __syncwarp();
+        if (lane == 0) {
+            float y = sw[P.b3()];
+            for (int k = 0; k < L0.n_h2; ++k) y = fmaf(sw[P.w3() + k], sh2[w][k], y);
+            if constexpr (FOLD) {
+                const double qv = __dadd_rn(__dmul_rn((double)y, F.y_scale), F.y_mean);
+                F.q[s] = qv;
+                qsum += qv;
+            } else {
+                out[s] = y;
+            }
+        }
+        __syncwarp();
+    }
+    if constexpr (FOLD) {
+        if (lane == 0) sq[w] = qsum;
+        __syncthreads();
+        if (threadIdx.x == 0) {
+            double t = 0.0;
+            for (int k = 0; k < INF_WARPS; ++k) t += sq[k];
+            F.part[blockIdx.x] = t;
+        }
+    }
+}
+
+// q_i - (sum q - total) / n into the charges; every block forms the sum from
+// the block partials in the same order
+__global__ void mlp_charge_shift(const double* __restrict__ q, const double* __restrict__ part, int nparts, int n,
+                                 double total, double* __restrict__ charge) {
+    __shared__ double shift;
+    if (threadIdx.x == 0) {
+        double t = 0.0;
+        for (int b = 0; b < nparts; ++b) t += part[b];
+        shift = (t - total) / n;
+    }
+    __syncthreads();
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) charge[i] = q[i] - shift;
+}
+
 inline int cdiv(long long a, long long b) { return (int)((a + b - 1) / b); }
+
+// blocks of the inference kernel: at most two per SM, each reading the
+// parameters into shared memory once
+inline int infer_blocks(long long n) { return std::max(1, std::min(cdiv(n, INF_WARPS), 2 * 152)); }
 
 }  // namespace
 
 Layout mlp_layout(const pg_mlp* M) { return Layout{M->n_in, M->n_h1, M->n_h2}; }
 
 size_t mlp_smem(const pg_mlp* M) { return sizeof(float) * (size_t)M->n_params; }
+size_t infer_smem(const pg_mlp* M) { return sizeof(float) * (size_t)PadLayout(mlp_layout(M)).total(); }
 
 // ---- host side ---------------------------------------------------------------
 
@@ -308,8 +449,10 @@ void descriptors(pg_context* ctx, int n_gauss, double r0, double r1, double widt
             desc_kernel<<<cdiv((long long)ctx->n * 32, 128), 128, 0, ctx->stream>>>(A);
         PG_CHECK_LAUNCH();
     }
-    ctx->mlp_desc.download(out, (size_t)ctx->n * nf, ctx->stream);
-    PG_CUDA(cudaStreamSynchronize(ctx->stream));
+    if (out) {
+        ctx->mlp_desc.download(out, (size_t)ctx->n * nf, ctx->stream);
+        PG_CUDA(cudaStreamSynchronize(ctx->stream));
+    }
 }
 
 void mlp_create(pg_mlp** out, int n_in, int n_h1, int n_h2, int device) {
@@ -318,23 +461,25 @@ void mlp_create(pg_mlp** out, int n_in, int n_h1, int n_h2, int device) {
     if (device >= 0) PG_CUDA(cudaSetDevice(device));
     int dev = 0;
     PG_CUDA(cudaGetDevice(&dev));
-    pg_mlp* M = new pg_mlp();
+    std::unique_ptr<pg_mlp> hold(new pg_mlp());
+    pg_mlp* M = hold.get();
     M->device = dev;
     M->n_in = n_in;
     M->n_h1 = n_h1;
     M->n_h2 = n_h2;
     M->n_params = Layout{n_in, n_h1, n_h2}.total();
-    cudaError_t e = cudaStreamCreateWithFlags(&M->stream, cudaStreamNonBlocking);
-    if (e != cudaSuccess) {
-        delete M;
-        PG_CUDA(e);
-    }
-    const size_t smem = mlp_smem(M);
-    if (smem > 48 * 1024) {
-        PG_CUDA(cudaFuncSetAttribute(mlp_forward<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-        PG_CUDA(cudaFuncSetAttribute(mlp_forward<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-        PG_CUDA(cudaFuncSetAttribute(mlp_backward, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-    }
+    PG_CUDA(cudaStreamCreateWithFlags(&M->stream, cudaStreamNonBlocking));
+    // shared-memory limits of the network kernels, set once to what the
+    // largest network allowed here needs (a per-network value would shrink
+    // the limit under a larger network created before)
+    const Layout big{MAX_IN, MAX_H, MAX_H};
+    const int fwd_max = (int)(sizeof(float) * (size_t)big.total());
+    const int inf_max = (int)(sizeof(float) * (size_t)PadLayout(big).total());
+    PG_CUDA(cudaFuncSetAttribute(mlp_infer<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, inf_max));
+    PG_CUDA(cudaFuncSetAttribute(mlp_infer<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, inf_max));
+    PG_CUDA(cudaFuncSetAttribute(mlp_forward<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, fwd_max));
+    PG_CUDA(cudaFuncSetAttribute(mlp_forward<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, fwd_max));
+    PG_CUDA(cudaFuncSetAttribute(mlp_backward, cudaFuncAttributeMaxDynamicSharedMemorySize, fwd_max));
     // Glorot-uniform weights and zero biases from a fixed seed
     std::vector<float> w((size_t)M->n_params, 0.0f);
     std::mt19937_64 rng(0x5eedull);
@@ -355,7 +500,7 @@ void mlp_create(pg_mlp** out, int n_in, int n_h1, int n_h2, int device) {
     to_bf16<<<cdiv(M->n_params, 256), 256, 0, M->stream>>>((int)M->n_params, M->w.p, M->wb.p);
     PG_CHECK_LAUNCH();
     PG_CUDA(cudaStreamSynchronize(M->stream));
-    *out = M;
+    *out = hold.release();
 }
 
 void mlp_set_params(pg_mlp* M, const float* params, long long n) {
@@ -479,11 +624,55 @@ void mlp_predict(pg_mlp* M, const float* x, long long n, float* y) {
     M->px.resize((size_t)n * M->n_in);
     M->py.resize((size_t)n);
     M->px.upload(x, (size_t)n * M->n_in, M->stream);
-    mlp_forward<false><<<cdiv(n, MLP_THREADS), MLP_THREADS, mlp_smem(M), M->stream>>>(
-        mlp_layout(M), M->wb.p, M->px.p, nullptr, (int)n, M->py.p, nullptr, nullptr);
+    mlp_infer<false><<<infer_blocks(n), INF_THREADS, infer_smem(M), M->stream>>>(mlp_layout(M), M->wb.p, M->px.p,
+                                                                                  (int)n, M->py.p, FoldArgs{});
     PG_CHECK_LAUNCH();
     M->py.download(y, (size_t)n, M->stream);
     PG_CUDA(cudaStreamSynchronize(M->stream));
+}
+
+void mlp_predict_charges(pg_mlp* M, pg_context* ctx, int n_gauss, double r0, double r1, double width, double cutoff,
+                         int n_elements, const int* type_element, const float* x_mean, const float* x_scale,
+                         double y_mean, double y_scale, double total_charge, double* charges) {
+    require(M->device == ctx->device, PG_ERR_INVALID, "network and context on different devices");
+    const int T = std::max(ctx->n_types, 1);
+    require(n_elements >= 1 && M->n_in == n_elements * (n_gauss + 1), PG_ERR_INVALID,
+            "network inputs must be n_elements x (n_gauss + 1)");
+    for (int t = 0; t < T; ++t)
+        require(type_element[t] >= 0 && type_element[t] < n_elements, PG_ERR_INVALID, "type without an element");
+    const int n = ctx->n;
+    // descriptors into ctx->mlp_desc, on the context's stream
+    descriptors(ctx, n_gauss, r0, r1, width, cutoff, nullptr);
+    if (n == 0) return;
+    // small per-call inputs in one upload: type -> element, mean, scale
+    std::vector<float> h((size_t)T + 2 * (size_t)M->n_in);
+    static_assert(sizeof(float) == sizeof(int), "packed upload");
+    std::memcpy(h.data(), type_element, sizeof(int) * T);
+    std::memcpy(h.data() + T, x_mean, sizeof(float) * M->n_in);
+    std::memcpy(h.data() + T + M->n_in, x_scale, sizeof(float) * M->n_in);
+    ctx->mlp_fold.upload(h.data(), h.size(), ctx->stream);
+    const int nb = infer_blocks(n);
+    ctx->mlp_q.resize((size_t)n + (size_t)nb);
+    FoldArgs F{};
+    F.raw = ctx->mlp_desc.p;
+    F.type = ctx->type.p;
+    F.elem = (const int*)ctx->mlp_fold.p;
+    F.x_mean = ctx->mlp_fold.p + T;
+    F.x_scale = ctx->mlp_fold.p + T + M->n_in;
+    F.T = T;
+    F.G = n_gauss;
+    F.E = n_elements;
+    F.y_mean = y_mean;
+    F.y_scale = y_scale;
+    F.q = ctx->mlp_q.p;
+    F.part = ctx->mlp_q.p + n;
+    // the weights may have been written on the network's own stream
+    PG_CUDA(cudaStreamSynchronize(M->stream));
+    mlp_infer<true><<<nb, INF_THREADS, infer_smem(M), ctx->stream>>>(mlp_layout(M), M->wb.p, nullptr, n, nullptr, F);
+    mlp_charge_shift<<<cdiv(n, 256), 256, 0, ctx->stream>>>(F.q, F.part, nb, n, total_charge, ctx->charge.p);
+    PG_CHECK_LAUNCH();
+    if (charges) ctx->charge.download(charges, (size_t)n, ctx->stream);
+    PG_CUDA(cudaStreamSynchronize(ctx->stream));
 }
 
 }  // namespace pg

@@ -7,20 +7,21 @@
 //
 //   electronegativity kernels (pair kernel + k-space Ewald) on the current q
 //   rx_mean    block sums of chi; the last block to finish forms mean(chi)
-//   rx_force   F = chi - mean;  q' = (q' + F dt/(2M)) / (1 + gamma dt/2);
+//   rx_step    F = chi - mean;  q' = (q' + F dt/(2M)) / (1 + gamma dt/2);
+//              save (q, q') as the result of this step, then already
+//              q += q' dt + (F - gamma q') dt^2 / M;  q' = (1 - gamma dt/2) q' + F dt / (2M);
 //              the last block takes error = max F (signed, relaxation.py:449)
 //              and decides: stop when error <= tol, at the step limit, or when
 //              the error is not finite (diverging dynamics)
-//   rx_update  unless stopped: q += q' dt + (F - gamma q') dt^2 / M;
-//              q' = (1 - gamma dt/2) q' + F dt / (2M); the last block takes max |dq|
 //
-// The initial pass (relaxation.py:433) is the electronegativities, rx_mean,
-// rx_force<INIT> and the first rx_update.  Every kernel first reads a device
-// flag and returns at once when the loop has stopped, so the host enqueues
-// chunks of steps and reads back only the flag once per chunk.  The "last
-// block" of a kernel is found with an integer ticket (an atomic counter, no
-// waiting); it combines the per-block partials in block order, so every
-// statistic is deterministic.  Charges, rates and statistics are FP64.
+// The initial pass (relaxation.py:433) is the electronegativities, rx_mean and
+// rx_step<INIT>.  Every kernel first reads a device flag and returns at once
+// when the loop has stopped, so the host enqueues chunks of steps and reads
+// back only the flag once per chunk; the saved (q, q') of the stopping step
+// are the result.  The "last block" of a kernel is found with an integer
+// ticket (an atomic counter, no waiting); it combines the per-block partials
+// in block order, so every statistic is deterministic.  Charges, rates and
+// statistics are FP64.
 #include <algorithm>
 #include <cmath>
 #include <vector>
@@ -39,11 +40,12 @@ struct RxArgs {
     int n;
     double* q;
     double* rate;
-    double* force;
+    double* q_save;   // q and q' at the last stop test: the result when the loop stops
+    double* rate_save;
     const double* chi;
     double dt, inv_m, friction, tol;
     int n_steps;
-    int* flag;        // [0] stop flag, [1] steps taken, [2..4] tickets of rx_mean, rx_force, rx_update
+    int* flag;        // [0] stop flag, [1] steps taken, [2], [3] tickets of rx_mean, rx_step
     double* stat;     // [0] error, [1] max |dq| reported, [2] mean chi, [3] max |dq| of the last update
     double* part;     // per block: sum chi, max F, max |dq|
     int nblocks;
@@ -100,27 +102,47 @@ __global__ void __launch_bounds__(RT) rx_mean(RxArgs A) {
     }
 }
 
+// Forces, the second half of the rate update, the stop test and -- without
+// waiting for the test -- the next update.  Before updating, each atom saves
+// its charge and its completed rate: they are the loop's result if the last
+// block decides to stop here, and the speculative update is then simply never
+// used (every later kernel sees the flag and returns).
 template <bool INIT>
-__global__ void __launch_bounds__(RT) rx_force(RxArgs A) {
+__global__ void __launch_bounds__(RT) rx_step(RxArgs A) {
     __shared__ double sh[RT / 32];
     if (A.flag[0]) return;
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    double f = -1e300;
+    double fm = -1e300, dq = 0.0;
     if (i < A.n) {
-        f = A.chi[i] - A.stat[2];
-        A.force[i] = f;
-        if (!INIT) A.rate[i] = (A.rate[i] + f * 0.5 * A.inv_m * A.dt) / (1.0 + 0.5 * A.friction * A.dt);
+        const double f = A.chi[i] - A.stat[2];
+        double r = A.rate[i];
+        if (!INIT) r = (r + f * 0.5 * A.inv_m * A.dt) / (1.0 + 0.5 * A.friction * A.dt);
+        const double q0 = A.q[i];
+        A.q_save[i] = q0;
+        A.rate_save[i] = r;
+        dq = r * A.dt + (f - A.friction * r) * A.inv_m * A.dt * A.dt;
+        const double q = q0 + dq;
+        A.q[i] = q;
+        if (A.disp) A.disp[i].w = (float)q;
+        A.rate[i] = (1.0 - 0.5 * A.friction * A.dt) * r + f * 0.5 * A.inv_m * A.dt;
         // a non-finite force must not vanish in fmax (which drops NaN): it
         // becomes +inf, so the stop test sees it and the loop ends as diverged
-        if (!isfinite(f)) f = __longlong_as_double(0x7ff0000000000000ll);
+        fm = isfinite(f) ? f : __longlong_as_double(0x7ff0000000000000ll);
     }
-    const double m = block_reduce(f, true, sh);
-    if (threadIdx.x == 0) A.part[3 * blockIdx.x + 1] = m;
+    const double m = block_reduce(fm, true, sh);
+    __syncthreads();
+    const double d = block_reduce(fabs(dq), true, sh);
+    if (threadIdx.x == 0) {
+        A.part[3 * blockIdx.x + 1] = m;
+        A.part[3 * blockIdx.x + 2] = d;
+    }
     if (last_block(A.flag + 3)) {
         const volatile double* p = A.part;
-        double e = -1e300;
-        for (int b = 0; b < A.nblocks; ++b) e = fmax(e, p[3 * b + 1]);
-        A.stat[0] = e;
+        double e = -1e300, dmax = 0.0;
+        for (int b = 0; b < A.nblocks; ++b) {
+            e = fmax(e, p[3 * b + 1]);
+            dmax = fmax(dmax, p[3 * b + 2]);
+        }
         int stop;
         if (INIT) {
             A.stat[1] = 0.0;
@@ -129,33 +151,12 @@ __global__ void __launch_bounds__(RT) rx_force(RxArgs A) {
         } else {
             const int steps = A.flag[1] + 1;
             A.flag[1] = steps;
-            A.stat[1] = A.stat[3];
+            A.stat[1] = A.stat[3];  // |dq| of the update that led to these charges
             stop = e <= A.tol || steps >= A.n_steps || !isfinite(e);
         }
+        A.stat[0] = e;
+        A.stat[3] = dmax;
         if (stop) A.flag[0] = 1;
-    }
-}
-
-__global__ void __launch_bounds__(RT) rx_update(RxArgs A) {
-    __shared__ double sh[RT / 32];
-    if (A.flag[0]) return;
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    double dq = 0.0;
-    if (i < A.n) {
-        const double r = A.rate[i], f = A.force[i];
-        dq = r * A.dt + (f - A.friction * r) * A.inv_m * A.dt * A.dt;
-        const double q = A.q[i] + dq;
-        A.q[i] = q;
-        if (A.disp) A.disp[i].w = (float)q;
-        A.rate[i] = (1.0 - 0.5 * A.friction * A.dt) * r + f * 0.5 * A.inv_m * A.dt;
-    }
-    const double m = block_reduce(fabs(dq), true, sh);
-    if (threadIdx.x == 0) A.part[3 * blockIdx.x + 2] = m;
-    if (last_block(A.flag + 4)) {
-        const volatile double* p = A.part;
-        double d = 0.0;
-        for (int b = 0; b < A.nblocks; ++b) d = fmax(d, p[3 * b + 2]);
-        A.stat[3] = d;
     }
 }
 
@@ -175,8 +176,10 @@ static void finish_relax(pg_context* ctx, const RxArgs& A, int n, double toleran
     int h_flag[2] = {0, 0};
     double h_stat[3] = {0.0, 0.0, 0.0};
     PG_CUDA(cudaMemcpyAsync(h_stat, A.stat, sizeof(double) * 3, cudaMemcpyDeviceToHost, st));
-    PG_CUDA(cudaMemcpyAsync(rates, A.rate, sizeof(double) * n, cudaMemcpyDeviceToHost, st));
-    PG_CUDA(cudaMemcpyAsync(charges, A.q, sizeof(double) * n, cudaMemcpyDeviceToHost, st));
+    // the state saved at the stopping test; the context keeps those charges
+    PG_CUDA(cudaMemcpyAsync(A.q, A.q_save, sizeof(double) * n, cudaMemcpyDeviceToDevice, st));
+    PG_CUDA(cudaMemcpyAsync(rates, A.rate_save, sizeof(double) * n, cudaMemcpyDeviceToHost, st));
+    PG_CUDA(cudaMemcpyAsync(charges, A.q_save, sizeof(double) * n, cudaMemcpyDeviceToHost, st));
     PG_CUDA(cudaMemcpyAsync(h_flag, A.flag, sizeof(h_flag), cudaMemcpyDeviceToHost, st));
     PG_CUDA(cudaStreamSynchronize(st));
     *steps = h_flag[1];
@@ -198,16 +201,17 @@ void relax_charges(pg_context* ctx, int precision, int n_steps, double dt, doubl
     ctx->out_chi.resize((size_t)std::max(n, 1));
     ctx->out_f.resize(3 * (size_t)std::max(n, 1));
     ctx->rq_rate.upload(rates, (size_t)n, st);
-    ctx->rq_force.resize((size_t)std::max(n, 1));
+    ctx->rq_save.resize(2 * (size_t)std::max(n, 1));
     ctx->rq_stat.resize(4 + 3 * (size_t)nb);
     ctx->rq_flag.resize(8);
-    // stop flag, step count and the three tickets start at zero
+    // stop flag, step count and the tickets start at zero
     PG_CUDA(cudaMemsetAsync(ctx->rq_flag.p, 0, sizeof(int) * 8, st));
     RxArgs A{};
     A.n = n;
     A.q = ctx->charge.p;
     A.rate = ctx->rq_rate.p;
-    A.force = ctx->rq_force.p;
+    A.q_save = ctx->rq_save.p;
+    A.rate_save = ctx->rq_save.p + std::max(n, 1);
     A.chi = ctx->out_chi.p;
     A.dt = dt;
     A.inv_m = 1.0 / inertia;
@@ -220,7 +224,7 @@ void relax_charges(pg_context* ctx, int precision, int n_steps, double dt, doubl
     A.nblocks = nb;
     ctx->launches = 0;
     // positions stay fixed during the relaxation: displacements (and the FP32
-    // charges beside them) once; rx_update keeps the charges current
+    // charges beside them) once; rx_step keeps the charges current
     if (precision == PG_PREC_MIXED) {
         launch_disp(ctx, nullptr);
         A.disp = ctx->disp32.p;
@@ -228,14 +232,12 @@ void relax_charges(pg_context* ctx, int precision, int n_steps, double dt, doubl
     // initial differences (relaxation.py:433) and the first update
     enqueue_chi(ctx, precision, A.flag);
     rx_mean<<<nb, RT, 0, st>>>(A);
-    rx_force<true><<<nb, RT, 0, st>>>(A);
-    rx_update<<<nb, RT, 0, st>>>(A);
+    rx_step<true><<<nb, RT, 0, st>>>(A);
     PG_CHECK_LAUNCH();
     auto one_step = [&] {
         enqueue_chi(ctx, precision, A.flag);
         rx_mean<<<nb, RT, 0, st>>>(A);
-        rx_force<false><<<nb, RT, 0, st>>>(A);
-        rx_update<<<nb, RT, 0, st>>>(A);
+        rx_step<false><<<nb, RT, 0, st>>>(A);
     };
     // one step as a CUDA graph, replayed; the buffers it uses were sized by the
     // initial pass above

@@ -150,6 +150,30 @@ class ChargeNetwork:
 
     def predict_charges(self, calc, total_charge=0.0):
         """Starting charges for the calculator's structure, shifted so that
-        they add up to total_charge (the relaxation conserves the sum)."""
+        they add up to total_charge (the relaxation conserves the sum).  The
+        whole prediction runs on the device (pg_mlp_predict_charges) and the
+        engine keeps the predicted charges; a copy is returned."""
+        d = self.descriptor
+        calc.set_core()
+        model = calc._model
+        type_el = np.array([self._element_index(sig[0]) for sig in model.type_signatures], dtype=np.int32)
+        q = np.zeros(len(model.types))
+        xm = np.ascontiguousarray(self.x_mean, dtype=np.float32)
+        xs = np.ascontiguousarray(self.x_scale, dtype=np.float32)
+        L.check(self.lib.pg_mlp_predict_charges(
+            self.h, calc.engine.ctx, int(d["n_gauss"]), float(d["r0"]), float(d["r1"]), float(d["width"]),
+            float(d["cutoff"]), len(self.elements), L.iptr(type_el), L.fptr(xm), L.fptr(xs),
+            float(self.y_mean), float(self.y_scale), float(total_charge), L.dptr(q)))
+        return q
+
+    def predict_charges_host(self, calc, total_charge=0.0):
+        """The same prediction through the host: descriptors copied out, folded
+        and normalised with NumPy, the network on the device, the shift in
+        NumPy.  For comparisons with predict_charges."""
         q = self.predict(self.descriptors(calc))
         return q - (q.sum() - total_charge) / len(q)
+
+    def _element_index(self, el):
+        if not self.elements or el not in self.elements:
+            raise ValueError("the network was not trained for element " + str(el))
+        return self.elements.index(el)

@@ -167,6 +167,10 @@ class ChargeRelaxation:
                 t0 = time.perf_counter()
                 charges = self.warm_start.predict_charges(calc, total_charge=float(np.sum(charges)))
                 self._set(atoms, charges)
+                # the engine already holds the predicted charges
+                pushed = getattr(calc, "_pushed", None)
+                if pushed is not None:
+                    pushed["charges"] = np.array(charges, dtype=np.float64)
                 self.charge_rates = np.zeros(len(atoms))
                 self.last_warm_start_seconds = time.perf_counter() - t0
             calc.set_core()

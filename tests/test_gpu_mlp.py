@@ -30,13 +30,32 @@ def _net(n_in=10, h1=12, h2=8, seed=0):
     return net, MO.bf16(p)
 
 
-def test_forward_matches_oracle():
-    net, pb = _net()
+@pytest.mark.parametrize("sizes", [(10, 12, 8), (40, 33, 50), (64, 128, 128)])
+def test_forward_matches_oracle(sizes):
+    n_in, h1, h2 = sizes
+    net, pb = _net(n_in, h1, h2)
     rng = np.random.default_rng(1)
-    x = rng.normal(0, 1, (500, 10)).astype(np.float32)
+    x = rng.normal(0, 1, (2001, n_in)).astype(np.float32)
     got = net.predict(x)  # identity normalisation
-    ref, _, _ = MO.forward(pb, x, 10, 12, 8)
+    ref, _, _ = MO.forward(pb, x, n_in, h1, h2)
     np.testing.assert_allclose(got, ref, rtol=1e-5, atol=1e-5)
+
+
+def test_device_warm_start_matches_host_path():
+    """pg_mlp_predict_charges (descriptors, fold, normalisation, network and
+    total-charge shift on the device) against the host route with the
+    shipped SiO2 network."""
+    net = ChargeNetwork.load(os.path.join(os.path.dirname(pysic.__file__), "data", "sio2_warm_start.npz"))
+    pots, coul = W.sio2_potentials(real_cutoff=5.5, sigma=1.6)
+    for seed, total in ((31, 0.0), (32, 0.3)):
+        calc = pysic.Pysic(W.sio2_box(60, seed=seed), pots, coulomb=coul, precision="mixed")
+        calc.set_core()
+        host = net.predict_charges_host(calc, total_charge=total)
+        dev = net.predict_charges(calc, total_charge=total)
+        np.testing.assert_allclose(dev, host, rtol=0, atol=1e-12)
+        assert dev.sum() == pytest.approx(total, abs=1e-12)
+        # the engine holds the predicted charges
+        np.testing.assert_array_equal(calc.engine.get_charges(), dev)
 
 
 def test_gradients_match_oracle():
