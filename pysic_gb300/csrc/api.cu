@@ -87,18 +87,52 @@ void prepare(pg_context* ctx) {
 }
 
 // one evaluation, enqueued on ctx->stream; G: lanes per atom of the bond kernels
-// true when no value is an infinity or a NaN: the exponent field is not all
-// ones.  A branch-free integer test over the bit patterns, so the per-call
-// check of a large coordinate array costs a few microseconds.
+// true when no value is an infinity or a NaN (one-time checks of new atoms)
 static bool all_finite(const double* v, size_t n) {
-    constexpr uint64_t EXP = 0x7ff0000000000000ull;
-    uint64_t bad = 0;
-    for (size_t i = 0; i < n; ++i) {
-        uint64_t u;
-        std::memcpy(&u, v + i, sizeof(u));
-        bad |= (uint64_t)((u & EXP) == EXP);
-    }
-    return bad == 0;
+    bool ok = true;
+    for (size_t i = 0; i < n; ++i) ok &= std::isfinite(v[i]);
+    return ok;
+}
+
+namespace {
+
+// any non-finite value in p[0, n) sets *bad (every writer stores the same 1)
+__global__ void coords_finite(const double* __restrict__ p, long long n, int* __restrict__ bad) {
+    int b = 0;
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x)
+        b |= !isfinite(p[i]);
+    if (__syncthreads_or(b) && threadIdx.x == 0) *bad = 1;
+}
+
+// the checked coordinates into place, unless the check failed
+__global__ void coords_commit(const double* __restrict__ in, double* __restrict__ out, long long n,
+                              const int* __restrict__ bad) {
+    if (*bad) return;
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x)
+        out[i] = in[i];
+}
+
+}  // namespace
+
+// New coordinates for the context: copied to a staging buffer, checked for
+// non-finite values on the device and moved into place only if all are
+// finite, so that a rejected update leaves the old coordinates.  One
+// synchronisation; the host never walks the array.
+static void update_coordinates(pg_context* ctx, const double* positions) {
+    const long long m = 3ll * ctx->n;
+    if (m == 0) return;
+    cudaStream_t st = ctx->stream;
+    ctx->pos_in.upload(positions, (size_t)m, st);
+    ctx->pos_bad.resize(1);
+    PG_CUDA(cudaMemsetAsync(ctx->pos_bad.p, 0, sizeof(int), st));
+    const int blocks = (int)std::min<long long>((m + 255) / 256, 4 * 152);
+    coords_finite<<<blocks, 256, 0, st>>>(ctx->pos_in.p, m, ctx->pos_bad.p);
+    coords_commit<<<blocks, 256, 0, st>>>(ctx->pos_in.p, ctx->pos.p, m, ctx->pos_bad.p);
+    PG_CHECK_LAUNCH();
+    int* bad = ctx->h_flag.get(1);
+    PG_CUDA(cudaMemcpyAsync(bad, ctx->pos_bad.p, sizeof(int), cudaMemcpyDeviceToHost, st));
+    PG_CUDA(cudaStreamSynchronize(st));
+    require(*bad == 0, PG_ERR_INVALID, "non-finite atom position");
 }
 
 static void enqueue(pg_context* ctx, int precision, int flags, int G) {
@@ -234,10 +268,11 @@ void evaluate(pg_context* ctx, int precision, int flags) {
 }
 
 static void copy_results(pg_context* ctx, int flags, double* energy, double* forces, double* stress, double* enegs) {
-    FxAcc acc[8] = {};
+    FxAcc* acc = ctx->h_acc.get(8);
+    std::memset((void*)acc, 0, sizeof(FxAcc) * 8);
     double tot[8] = {0};
     cudaStream_t st = ctx->stream;
-    if (energy || stress) PG_CUDA(cudaMemcpyAsync(acc, ctx->out_acc.p, sizeof(acc), cudaMemcpyDeviceToHost, st));
+    if (energy || stress) PG_CUDA(cudaMemcpyAsync(acc, ctx->out_acc.p, sizeof(FxAcc) * 8, cudaMemcpyDeviceToHost, st));
     if (forces && (flags & PG_WANT_FORCES)) ctx->out_f.download(forces, 3 * (size_t)ctx->n, st);
     if (enegs && (flags & PG_WANT_ENEGS)) ctx->out_chi.download(enegs, (size_t)ctx->n, st);
     PG_CUDA(cudaStreamSynchronize(st));
@@ -325,10 +360,8 @@ int pg_update_atom_coordinates(pg_context* ctx, const double* positions) {
         check_ctx(ctx);
         use_device(ctx);
         pg::require(ctx->have_atoms, PG_ERR_NOT_READY, "no atoms");
-        pg::require(ctx->n == 0 || pg::all_finite(positions, 3 * (size_t)ctx->n), PG_ERR_INVALID,
-                    "non-finite atom position");
-        ctx->pos.upload(positions, 3 * (size_t)ctx->n, ctx->stream);
-        PG_CUDA(cudaStreamSynchronize(ctx->stream));
+        pg::require(ctx->n == 0 || positions != nullptr, PG_ERR_INVALID, "null positions");
+        pg::update_coordinates(ctx, positions);
     });
 }
 

@@ -81,6 +81,30 @@ struct DevBuf {
     }
 };
 
+// Page-locked host memory for small per-call results (totals, flags), so that
+// their device-to-host copies are asynchronous and share one synchronisation.
+template <typename T>
+struct PinnedBuf {
+    T* p = nullptr;
+    size_t cap = 0;
+    PinnedBuf() = default;
+    PinnedBuf(const PinnedBuf&) = delete;
+    PinnedBuf& operator=(const PinnedBuf&) = delete;
+    ~PinnedBuf() {
+        if (p) cudaFreeHost(p);
+    }
+    T* get(size_t count) {
+        if (count > cap) {
+            if (p) cudaFreeHost(p);
+            p = nullptr;
+            cap = 0;
+            PG_CUDA(cudaMallocHost(&p, count * sizeof(T)));
+            cap = count;
+        }
+        return p;
+    }
+};
+
 // Host-side copy of the cell in the reference's layout (Geometry.f90:50-145).
 struct Cell {
     double vc[3][3];  // cell%vectors(r,c): component r of cell vector c
@@ -204,6 +228,10 @@ struct pg_context {
     pg::Cell cell{};
     double cell_rows[9]{}, inv_rows[9]{};
     pg::DevBuf<double> pos;     // n x 3
+    pg::DevBuf<double> pos_in;  // coordinate updates land here first and are checked on the device
+    pg::DevBuf<int> pos_bad;    // 1 element: nonzero when an update held a non-finite value
+    pg::PinnedBuf<pg::FxAcc> h_acc; // energy / virial totals on their way to the host
+    pg::PinnedBuf<int> h_flag;
     pg::DevBuf<double> charge;  // n
     pg::DevBuf<int> type;       // n
     std::vector<int> h_type;

@@ -196,3 +196,31 @@ def test_md_style_position_update():
     assert calc.get_neighbor_lists().nupdates == nl.nupdates
     ref = oracle_all(moved, pots, lists=oracle_lists(atoms, pots))
     assert np.abs(f - ref["forces"]).max() < 1e-10
+
+
+def test_rejected_coordinate_update_keeps_the_old_positions():
+    """pg_update_atom_coordinates checks the new coordinates on the device and
+    moves them into place only when every value is finite."""
+    from pysic_gb300 import _lib as L
+
+    atoms = W.diamond_si(2, noise=0.1, seed=3)
+    calc = pysic.Pysic(atoms, W.tersoff_si_potentials())
+    e0 = calc.get_potential_energy()
+    f0 = calc.get_forces()
+    eng = calc.engine
+    for bad in (np.nan, np.inf, -np.inf):
+        pos = atoms.get_positions()
+        pos[5, 1] = bad
+        with pytest.raises(L.EngineError) as err:
+            eng.update_positions(pos)
+        assert err.value.status == L.PG_ERR_INVALID
+        r = eng.calculate(L.PREC_FP64, energy=True, forces=True)
+        assert r["energy"] == e0
+        assert np.array_equal(r["forces"], f0)
+    # a valid update afterwards is taken
+    moved = atoms.get_positions() + 0.01
+    eng.update_positions(moved)
+    r = eng.calculate(L.PREC_FP64, energy=True, forces=True)
+    ref = oracle_all(pysic.Atoms(atoms.get_chemical_symbols(), moved, cell=atoms.get_cell(), pbc=atoms.get_pbc()),
+                     W.tersoff_si_potentials(), lists=oracle_lists(atoms, W.tersoff_si_potentials()))
+    assert np.abs(r["forces"] - ref["forces"]).max() < 1e-10
