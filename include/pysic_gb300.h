@@ -149,6 +149,17 @@ int pg_relax_charges(pg_context* ctx, int32_t precision, int32_t n_steps, double
                      double friction, double tolerance, double* rates, double* charges, int32_t* steps,
                      double* error, double* max_dq);
 
+/* ChargeRelaxation 'potentiostat' (pysic/charges/relaxation.py:453-481) on the
+ * device: undamped charge dynamics driven by chi - potential (no mean
+ * subtracted, so the total charge follows the external potential) for exactly
+ * n_steps steps.  rates is read and written back as for pg_relax_charges;
+ * charges receives the final charges and *max_dchi (may be null) the final
+ * max(chi - potential).  PG_ERR_NOT_CONVERGED only when the dynamics diverge
+ * (non-finite electronegativities). */
+int pg_relax_charges_potentiostat(pg_context* ctx, int32_t precision, int32_t n_steps, double timestep,
+                                  double inertia, double potential, double* rates, double* charges,
+                                  double* max_dchi);
+
 /* Per ordered bond (CSR entry of the engine's short list) Tersoff sums zeta_ij of
  * group 0: the quantity core_calculate_pair_bond_order_factor (Core.f90:2439-2637)
  * accumulates.  Diagnostic; n_entries receives the short-list length. */

@@ -248,3 +248,25 @@ def relax_charges(positions, charges, cell, pbc, model, counts, idx, off, n_step
         error = force.max()
         max_dq = float(np.abs(dq).max())
     return {"charges": q, "rates": rates, "steps": step, "error": float(error), "max_dq": max_dq}
+
+
+def relax_potentiostat(positions, charges, cell, pbc, model, counts, idx, off, n_steps, timestep, inertia,
+                       potential, rates=None, threads=1):
+    """ChargeRelaxation 'potentiostat', pysic/charges/relaxation.py:453-481:
+    undamped charge dynamics driven by chi - potential for n_steps steps."""
+    q = np.array(charges, dtype=np.float64)
+    rates = np.zeros(len(q)) if rates is None else np.array(rates, dtype=np.float64)
+    dt = timestep
+    dt2 = dt * dt
+    inv_mq = 1.0 / inertia
+
+    def force_of(qq):
+        return evaluate(positions, qq, cell, pbc, model, counts, idx, off, "enegs", threads) - potential
+
+    force = force_of(q)
+    for _ in range(int(n_steps)):
+        q = q + (rates * dt + force * inv_mq * dt2)
+        rates = rates + force * 0.5 * inv_mq * dt
+        force = force_of(q)
+        rates = rates + force * 0.5 * inv_mq * dt
+    return {"charges": q, "rates": rates, "steps": int(n_steps), "max_dchi": float(force.max())}

@@ -69,6 +69,9 @@ _SIGNATURES = {
     "pg_relax_charges": (ctypes.c_int, [_ctx, ctypes.c_int32, ctypes.c_int32, ctypes.c_double, ctypes.c_double,
                                         ctypes.c_double, ctypes.c_double, _c_double_p, _c_double_p, _c_int_p,
                                         _c_double_p, _c_double_p]),
+    "pg_relax_charges_potentiostat": (ctypes.c_int, [_ctx, ctypes.c_int32, ctypes.c_int32, ctypes.c_double,
+                                                     ctypes.c_double, ctypes.c_double, _c_double_p, _c_double_p,
+                                                     _c_double_p]),
     "pg_get_bond_zeta": (ctypes.c_int, [_ctx, _c_double_p, ctypes.c_int64, _c_i64_p]),
     "pg_set_lanes_per_atom": (ctypes.c_int, [_ctx, ctypes.c_int32]),
     "pg_get_lanes_per_atom": (ctypes.c_int, [_ctx, _c_int_p]),

@@ -555,8 +555,25 @@ int pg_relax_charges(pg_context* ctx, int32_t precision, int32_t n_steps, double
         use_device(ctx);
         pg::require(inertia != 0.0, PG_ERR_INVALID, "zero charge inertia");
         pg::require(n_steps >= 0, PG_ERR_INVALID, "negative step count");
-        pg::relax_charges(ctx, precision, n_steps, timestep, inertia, friction, tolerance, rates, charges, steps, error,
-                          max_dq);
+        pg::relax_charges(ctx, precision, pg::PG_RELAX_DYNAMIC, n_steps, timestep, inertia, friction, tolerance, 0.0,
+                          rates, charges, steps, error, max_dq);
+    });
+}
+
+int pg_relax_charges_potentiostat(pg_context* ctx, int32_t precision, int32_t n_steps, double timestep,
+                                  double inertia, double potential, double* rates, double* charges, double* max_dchi) {
+    return guarded([&] {
+        check_ctx(ctx);
+        use_device(ctx);
+        pg::require(inertia != 0.0, PG_ERR_INVALID, "zero charge inertia");
+        pg::require(n_steps >= 0, PG_ERR_INVALID, "negative step count");
+        pg::require(std::isfinite(potential) && std::isfinite(timestep), PG_ERR_INVALID,
+                    "non-finite potential or time step");
+        int steps = 0;
+        double err = 0.0, dq = 0.0;
+        pg::relax_charges(ctx, precision, pg::PG_RELAX_POTENTIOSTAT, n_steps, timestep, inertia, 0.0, 0.0, potential,
+                          rates, charges, &steps, &err, &dq);
+        if (max_dchi) *max_dchi = err;
     });
 }
 

@@ -446,9 +446,12 @@ void batch_synchronize(pg_batch* b);
 int batch_launches(const pg_batch* b);
 cudaStream_t batch_stream(const pg_batch* b);
 
-// relax.cu
-void relax_charges(pg_context* ctx, int precision, int n_steps, double dt, double inertia, double friction,
-                   double tolerance, double* rates, double* charges, int* steps, double* error, double* max_dq);
+// relax.cu: mode PG_RELAX_DYNAMIC (damped, to a tolerance) or
+// PG_RELAX_POTENTIOSTAT (undamped, fixed external potential, fixed step count)
+constexpr int PG_RELAX_DYNAMIC = 0, PG_RELAX_POTENTIOSTAT = 1;
+void relax_charges(pg_context* ctx, int precision, int mode, int n_steps, double dt, double inertia, double friction,
+                   double tolerance, double potential, double* rates, double* charges, int* steps, double* error,
+                   double* max_dq);
 
 // api.cu
 void evaluate(pg_context* ctx, int precision, int flags);

@@ -43,7 +43,11 @@ struct RxArgs {
     double* q_save;   // q and q' at the last stop test: the result when the loop stops
     double* rate_save;
     const double* chi;
-    double dt, inv_m, friction, tol;
+    // the reference's coefficients, formed on the host in its order of
+    // operations: dt^2, 1 - gamma dt / 2, 1 / (1 + gamma dt / 2), 1 / (2 M)
+    double dt, dt2, inv_m, half_inv_m, friction, c_half, future, tol;
+    double potential;  // potentiostat: the external potential that replaces mean(chi)
+    int potentiostat;  // 1: fixed step count, no tolerance test (relaxation.py:453-481)
     int n_steps;
     int* flag;        // [0] stop flag, [1] steps taken, [2], [3] tickets of rx_mean, rx_step
     double* stat;     // [0] error, [1] max |dq| reported, [2] mean chi, [3] max |dq| of the last update
@@ -114,17 +118,21 @@ __global__ void __launch_bounds__(RT) rx_step(RxArgs A) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     double fm = -1e300, dq = 0.0;
     if (i < A.n) {
-        const double f = A.chi[i] - A.stat[2];
+        // the reference's formulas, rounded after every operation as NumPy
+        // does (no contraction into fused multiply-adds)
+        const double f = __dsub_rn(A.chi[i], A.potentiostat ? A.potential : A.stat[2]);
+        const double half = __dmul_rn(__dmul_rn(f, A.half_inv_m), A.dt);  // F / (2 M) dt
         double r = A.rate[i];
-        if (!INIT) r = (r + f * 0.5 * A.inv_m * A.dt) / (1.0 + 0.5 * A.friction * A.dt);
+        if (!INIT) r = __dmul_rn(A.future, __dadd_rn(r, half));
         const double q0 = A.q[i];
         A.q_save[i] = q0;
         A.rate_save[i] = r;
-        dq = r * A.dt + (f - A.friction * r) * A.inv_m * A.dt * A.dt;
-        const double q = q0 + dq;
+        dq = __dadd_rn(__dmul_rn(r, A.dt),
+                       __dmul_rn(__dmul_rn(__dsub_rn(f, __dmul_rn(A.friction, r)), A.inv_m), A.dt2));
+        const double q = __dadd_rn(q0, dq);
         A.q[i] = q;
         if (A.disp) A.disp[i].w = (float)q;
-        A.rate[i] = (1.0 - 0.5 * A.friction * A.dt) * r + f * 0.5 * A.inv_m * A.dt;
+        A.rate[i] = __dadd_rn(__dmul_rn(A.c_half, r), half);
         // a non-finite force must not vanish in fmax (which drops NaN): it
         // becomes +inf, so the stop test sees it and the loop ends as diverged
         fm = isfinite(f) ? f : __longlong_as_double(0x7ff0000000000000ll);
@@ -147,12 +155,12 @@ __global__ void __launch_bounds__(RT) rx_step(RxArgs A) {
         if (INIT) {
             A.stat[1] = 0.0;
             // the reference's loop starts from error = 2 tol and runs while error > tol
-            stop = A.n_steps <= 0 || !(2.0 * A.tol > A.tol);
+            stop = A.n_steps <= 0 || (!A.potentiostat && !(2.0 * A.tol > A.tol));
         } else {
             const int steps = A.flag[1] + 1;
             A.flag[1] = steps;
             A.stat[1] = A.stat[3];  // |dq| of the update that led to these charges
-            stop = e <= A.tol || steps >= A.n_steps || !isfinite(e);
+            stop = (!A.potentiostat && e <= A.tol) || steps >= A.n_steps || !isfinite(e);
         }
         A.stat[0] = e;
         A.stat[3] = dmax;
@@ -191,8 +199,9 @@ static void finish_relax(pg_context* ctx, const RxArgs& A, int n, double toleran
         throw Error(PG_ERR_NOT_CONVERGED, "charge relaxation reached its step limit before the tolerance");
 }
 
-void relax_charges(pg_context* ctx, int precision, int n_steps, double dt, double inertia, double friction,
-                   double tolerance, double* rates, double* charges, int* steps, double* error, double* max_dq) {
+void relax_charges(pg_context* ctx, int precision, int mode, int n_steps, double dt, double inertia, double friction,
+                   double tolerance, double potential, double* rates, double* charges, int* steps, double* error,
+                   double* max_dq) {
     require(ctx->have_list && ctx->have_atoms, PG_ERR_NOT_READY, "set atoms, potentials and lists first");
     prepare(ctx);
     const int n = ctx->n;
@@ -213,10 +222,17 @@ void relax_charges(pg_context* ctx, int precision, int n_steps, double dt, doubl
     A.q_save = ctx->rq_save.p;
     A.rate_save = ctx->rq_save.p + std::max(n, 1);
     A.chi = ctx->out_chi.p;
+    const bool pstat = mode == PG_RELAX_POTENTIOSTAT;
     A.dt = dt;
+    A.dt2 = dt * dt;
     A.inv_m = 1.0 / inertia;
-    A.friction = friction;
+    A.half_inv_m = 0.5 * A.inv_m;  // F * 0.5 * (1/M) rounds like F * (0.5 / M): 0.5 scales exactly
+    A.friction = pstat ? 0.0 : friction;
+    A.c_half = 1.0 - 0.5 * A.friction * dt;
+    A.future = 1.0 / (1.0 + 0.5 * A.friction * dt);
     A.tol = tolerance;
+    A.potential = potential;
+    A.potentiostat = pstat ? 1 : 0;
     A.n_steps = n_steps;
     A.flag = ctx->rq_flag.p;
     A.stat = ctx->rq_stat.p;
@@ -229,14 +245,15 @@ void relax_charges(pg_context* ctx, int precision, int n_steps, double dt, doubl
         launch_disp(ctx, nullptr);
         A.disp = ctx->disp32.p;
     }
-    // initial differences (relaxation.py:433) and the first update
+    // initial differences (relaxation.py:433) and the first update; the
+    // potentiostat subtracts its fixed potential instead of the mean
     enqueue_chi(ctx, precision, A.flag);
-    rx_mean<<<nb, RT, 0, st>>>(A);
+    if (!pstat) rx_mean<<<nb, RT, 0, st>>>(A);
     rx_step<true><<<nb, RT, 0, st>>>(A);
     PG_CHECK_LAUNCH();
     auto one_step = [&] {
         enqueue_chi(ctx, precision, A.flag);
-        rx_mean<<<nb, RT, 0, st>>>(A);
+        if (!pstat) rx_mean<<<nb, RT, 0, st>>>(A);
         rx_step<false><<<nb, RT, 0, st>>>(A);
     };
     // one step as a CUDA graph, replayed; the buffers it uses were sized by the
@@ -275,7 +292,7 @@ void relax_charges(pg_context* ctx, int precision, int n_steps, double dt, doubl
         PG_CUDA(cudaStreamSynchronize(st));
         chunk = std::min(chunk * 2, 64);
     }
-    finish_relax(ctx, A, n, tolerance, rates, charges, steps, error, max_dq);
+    finish_relax(ctx, A, n, pstat ? INFINITY : tolerance, rates, charges, steps, error, max_dq);
 }
 
 }  // namespace pg

@@ -144,6 +144,15 @@ class Engine:
         return {"charges": q, "rates": rates, "steps": steps.value, "error": err.value, "max_dq": dq.value,
                 "converged": st == L.PG_OK}
 
+    def relax_charges_potentiostat(self, precision, n_steps, timestep, inertia, potential, rates):
+        rates = L.as_f64(rates).copy()
+        q = np.zeros(self.n)
+        m = ctypes.c_double(0)
+        L.check(self.lib.pg_relax_charges_potentiostat(self.ctx, precision, int(n_steps), float(timestep),
+                                                       float(inertia), float(potential), L.dptr(rates), L.dptr(q),
+                                                       ctypes.byref(m)))
+        return {"charges": q, "rates": rates, "steps": int(n_steps), "max_dchi": m.value}
+
     def bond_zeta(self):
         n = ctypes.c_int64(0)
         L.check(self.lib.pg_get_bond_zeta(self.ctx, None, 0, ctypes.byref(n)))

@@ -4,10 +4,16 @@
 entirely on the device through pg_relax_charges: the electronegativity kernels
 and the velocity-Verlet-with-friction update are launched back to back
 without host round trips, and only the convergence statistics come back.
-'potentiostat' (453-481) drives the same GPU electronegativity evaluation
-from the host.  'optimize' (483-488) uses SciPy's SLSQP on the GPU energy and
-gradient when SciPy is available.
+'potentiostat' (453-481) runs on the device the same way
+(pg_relax_charges_potentiostat: undamped, chi minus a fixed external
+potential, a fixed number of steps).  With observers attached the device loop
+returns to the host at every step where one is due, so that each sees the
+atoms' charges of its step as in the reference (510-550); the cut loop takes
+the same steps as the uncut one.  'optimize' (483-488) uses SciPy's SLSQP on
+the GPU energy and gradient when SciPy is available.
 """
+import math
+
 import numpy as np
 
 from .error import InvalidRelaxationError, warn
@@ -175,33 +181,34 @@ class ChargeRelaxation:
                 self.last_warm_start_seconds = time.perf_counter() - t0
             calc.set_core()
             prec = calc._prec() if precision is None else precision
-            r = calc.engine.relax_charges(prec, int(p["n_steps"]), p["timestep"], p["inertia"], p["friction"],
-                                          p["tolerance"], self.charge_rates)
+            n_steps = int(p["n_steps"])
+
+            def run(k):
+                return calc.engine.relax_charges(prec, k, p["timestep"], p["inertia"], p["friction"],
+                                                 p["tolerance"], self.charge_rates)
+
+            r = self._run_segments(calc, atoms, n_steps, run)
             charges = r["charges"]
-            # the engine's own copy of the charges is now the relaxed one
-            pushed = getattr(calc, "_pushed", None)
-            if pushed is not None:
-                pushed["charges"] = np.array(charges, dtype=np.float64)
-            self.charge_rates = r["rates"]
-            self.last_steps = r["steps"]
             self.last_error = r["error"]
             self.last_max_dq = r["max_dq"]
             self.last_converged = r["converged"]
-            self._set(atoms, charges)
-            self.call_observers(self.last_steps)
         elif self.relaxation == "potentiostat":
             p = self.parameters
-            dt, inv_mq, ext = p["timestep"], 1.0 / p["inertia"], p["potential"]
             if self.charge_rates is None:
                 self.charge_rates = np.zeros(len(atoms))
-            force = calc.get_electronegativities(atoms) - ext
-            for step in range(int(p["n_steps"])):
-                charges = charges + self.charge_rates * dt + force * inv_mq * dt * dt
-                self.charge_rates = self.charge_rates + force * 0.5 * inv_mq * dt
-                self._set(atoms, charges)
-                force = calc.get_electronegativities(atoms) - ext
-                self.charge_rates = self.charge_rates + force * 0.5 * inv_mq * dt
-                self.call_observers(step + 1)
+            calc.set_core()
+            prec = calc._prec() if precision is None else precision
+
+            def run(k):
+                r = calc.engine.relax_charges_potentiostat(prec, k, p["timestep"], p["inertia"], p["potential"],
+                                                           self.charge_rates)
+                r["converged"] = False  # no tolerance: the step count decides
+                r["error"] = r["max_dchi"]
+                return r
+
+            r = self._run_segments(calc, atoms, int(p["n_steps"]), run)
+            charges = r["charges"]
+            self.last_error = r["max_dchi"]
         elif self.relaxation == "optimize":
             try:
                 from scipy.optimize import fmin_slsqp
@@ -228,6 +235,47 @@ class ChargeRelaxation:
         if self.piped_relaxation is not None:
             charges = self.piped_relaxation.charge_relaxation()
         return charges
+
+    def _observer_stride(self):
+        """Steps between returns to the host: every step at which an observer
+        may be due (the gcd of the intervals; 1 for an interval that is not an
+        integer, which the reference then calls every step).  None: no
+        observers, one device run."""
+        if not self.observers:
+            return None
+        g = 0
+        for _, interval, _, _ in self.observers:
+            iv = int(interval) if isinstance(interval, (int, np.integer)) and interval > 0 else 1
+            g = math.gcd(g, iv)
+        return max(g, 1)
+
+    def _run_segments(self, calc, atoms, n_steps, run):
+        """The device loop, cut where observers are due.  A segment restarts
+        from the charges and rates the previous one left and recomputes their
+        electronegativities, the value the reference carries over, so the cut
+        run takes the same steps as an uncut one.  Observers see the atoms'
+        charges of their step (relaxation.py:510-550)."""
+        stride = self._observer_stride()
+        total = 0
+        while True:
+            k = n_steps - total if stride is None else min(stride, n_steps - total)
+            r = run(max(k, 0))
+            total += r["steps"]
+            self.last_steps = total
+            self.charge_rates = r["rates"]
+            self._set(atoms, r["charges"])
+            # the engine's own copy of the charges is now the relaxed one
+            pushed = getattr(calc, "_pushed", None)
+            if pushed is not None:
+                pushed["charges"] = np.array(r["charges"], dtype=np.float64)
+            if stride is not None and r["steps"] > 0:
+                self.call_observers(total)
+            diverged = not np.isfinite(r["error"])
+            if stride is None or r["converged"] or diverged or total >= n_steps or k <= 0:
+                break
+        self.last_steps = total
+        r["steps"] = total
+        return r
 
     @staticmethod
     def _set(atoms, q):

@@ -118,3 +118,60 @@ def test_graph_replay_matches_direct_launches():
         assert x["energy"] == a["energy"]
         assert np.array_equal(x["forces"], a["forces"])
         assert np.array_equal(x["enegs"], a["enegs"])
+
+
+def test_potentiostat_matches_oracle_loop():
+    """'potentiostat' (relaxation.py:453-481) on the device against the oracle:
+    undamped dynamics under a fixed external potential, total charge free."""
+    atoms = W.sio2_box(60, seed=8)
+    pots, coul = W.sio2_potentials(real_cutoff=5.5, sigma=1.6)
+    q0 = np.where(np.array(atoms.get_chemical_symbols()) == "Si", 0.3, -0.15)
+    atoms.set_initial_charges(q0)
+    params = dict(n_steps=25, timestep=0.02, inertia=1.0, potential=6.0)
+    calc = pysic.Pysic(atoms, pots, coulomb=coul, precision="fp64")
+    rel = pysic.ChargeRelaxation("potentiostat", calculator=calc,
+                                 parameters=[params[k] for k in ("n_steps", "timestep", "inertia", "potential")])
+    q_gpu = rel.charge_relaxation()
+    model = compile_model(atoms, pots, coul)
+    lists = oracle_lists(atoms, pots, coul)
+    r = oracle.relax_potentiostat(atoms.get_positions(), q0, atoms.get_cell(), atoms.get_pbc(), model, *lists,
+                                  **params)
+    assert rel.last_steps == 25
+    np.testing.assert_allclose(q_gpu, r["charges"], atol=1e-9)
+    np.testing.assert_allclose(rel.charge_rates, r["rates"], atol=1e-9)
+    assert abs(q_gpu.sum() - q0.sum()) > 1e-3  # the potentiostat moves the total charge
+
+
+def test_observers_see_every_due_step_and_do_not_change_the_run():
+    """Observers are called at the steps their intervals name, with the atoms
+    holding that step's charges; cutting the device loop for them leaves the
+    relaxation's steps and charges as they are without observers."""
+    atoms = W.sio2_box(60, seed=9)
+    pots, coul = W.sio2_potentials(real_cutoff=5.5, sigma=1.6)
+    params = [400, 0.1, 1.0, 4.0, 1e-4]
+
+    def make():
+        a = atoms.copy()
+        a.set_initial_charges(np.zeros(len(a)))
+        calc = pysic.Pysic(a, pots, coulomb=coul, precision="fp64")
+        return calc, pysic.ChargeRelaxation("dynamic", calculator=calc, parameters=params)
+
+    calc0, plain = make()
+    q_plain = plain.charge_relaxation()
+    calc1, watched = make()
+    seen = []
+    watched.add_observer(lambda: seen.append((watched.last_steps, calc1.get_atoms().get_initial_charges())),
+                         interval=7)
+    seen_steps = []
+    watched.add_observer(lambda: seen_steps.append(1), interval=21)
+    q_watched = watched.charge_relaxation()
+    assert watched.last_steps == plain.last_steps
+    assert np.array_equal(q_watched, q_plain)
+    assert len(seen) == plain.last_steps // 7
+    assert len(seen_steps) == plain.last_steps // 21
+    # the charges an observer saw at step 14 are the oracle's after 14 steps
+    model = compile_model(atoms, pots, coul)
+    lists = oracle_lists(atoms, pots, coul)
+    r = oracle.relax_charges(atoms.get_positions(), np.zeros(len(atoms)), atoms.get_cell(), atoms.get_pbc(), model,
+                             *lists, n_steps=14, timestep=0.1, inertia=1.0, friction=4.0, tolerance=1e-4)
+    np.testing.assert_allclose(seen[1][1], r["charges"], atol=1e-9)
