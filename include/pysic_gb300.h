@@ -80,13 +80,17 @@ int pg_update_atom_charges(pg_context* ctx, const double* charges);
 int pg_get_atom_charges(pg_context* ctx, double* charges);
 
 /* allocate_potentials(n) + add_potential(...) for every pair record,
- * PyInterface.f90:370-380, 433-480.  kind: 0 LJ, 1 exponential, 2 Buckingham;
- * params: 4 per record (unused tail zero); soft: cutoff - cutoff_margin;
+ * PyInterface.f90:370-380, 433-480.  kind: 0 LJ (epsilon, sigma), 1 exponential
+ * (epsilon, zeta), 2 Buckingham (A, C, sigma), 3 spring (k, R_0; shifted by its
+ * value at the cutoff), 4 power (epsilon, a, n), 5 shift_power (epsilon, r1, r2,
+ * n); params: 4 per record (unused tail zero); soft: cutoff - cutoff_margin;
  * group: bond-order group (-1 none). */
 int pg_set_pair_potentials(pg_context* ctx, int32_t n_types, int32_t n_records, const int32_t* kind,
                            const double* params, const double* cutoff, const double* soft,
                            const uint64_t* mask1, const uint64_t* mask2, const int32_t* group);
-/* add_potential(...) for single-atom records (charge_self: params epsilon, n). */
+/* add_potential(...) for single-atom records, params 4 per record: kind 0
+ * charge_self (epsilon, n), 1 constant (V), 2 force (Fx, Fy, Fz; energy -F . r
+ * at the absolute position).  Single-atom terms add nothing to the virial. */
 int pg_set_single_potentials(pg_context* ctx, int32_t n_records, const int32_t* kind, const double* params,
                              const uint64_t* mask);
 /* allocate_bond_order_factors(n) + add_bond_order_factor(...), PyInterface.f90:384-395, 482-526.

@@ -289,23 +289,34 @@ static double smooth_deriv(double r, double hard, double soft) {
     return -(0.5 * PI / (hard - soft) * sin(PI * (r - soft) / (hard - soft)));
 }
 
-/* evaluate_energy_LJ (2990-3005), _exp (3665-3680), _buckingham (4030-4045) */
-static double pair_energy(int kind, const double* p, double r1) {
+/* evaluate_energy_LJ (2990-3005), _exp (3665-3680), _buckingham (4030-4045),
+ * _spring (3069-3085), _power (4141-4152), _shift (4827-4842); cut is the
+ * potential's hard cutoff (the spring is shifted by its value there) */
+static double pair_energy(int kind, const double* p, double cut, double r1) {
     if (kind == 0) {
         double ratio = p[1] / r1;
         double r6 = ratio * ratio * ratio * ratio * ratio * ratio;
         return p[0] * (r6 * r6 - r6);
     } else if (kind == 1) {
         return p[0] * exp(-(p[1] * r1));
-    } else {
+    } else if (kind == 2) {
         double ratio = r1 / p[2];
         double r6 = 1.0 / (ratio * ratio * ratio * ratio * ratio * ratio);
         return p[0] * exp(-ratio) - p[1] * r6;
+    } else if (kind == 3) {
+        double r2 = r1 - p[1], r6 = cut - p[1];
+        return r2 * r2 < r6 * r6 ? p[0] * 0.5 * (r2 * r2 - r6 * r6) : 0.0;
+    } else if (kind == 4) {
+        double ratio = p[1] / r1;
+        return p[0] * pow(ratio, p[2]);
+    } else {
+        return p[0] * pow((p[1] - r1) / (p[1] - p[2]), p[3]);
     }
 }
 
-/* evaluate_force_LJ (2971-2983), _exp (3643-3655), _buckingham (4009-4022): force on atom 1 */
-static void pair_force(int kind, const double* p, const double sep[3], double r1, double f[3]) {
+/* evaluate_force_LJ (2971-2983), _exp (3643-3655), _buckingham (4009-4022),
+ * _spring (3042-3060), _power (4119-4132), _shift (4803-4818): force on atom 1 */
+static void pair_force(int kind, const double* p, double cut, const double sep[3], double r1, double f[3]) {
     if (kind == 0) {
         double ratio = p[1] / r1;
         double r6 = ratio * ratio * ratio * ratio * ratio * ratio;
@@ -314,11 +325,20 @@ static void pair_force(int kind, const double* p, const double sep[3], double r1
     } else if (kind == 1) {
         double pre = p[1] * p[0] * exp(-(p[1] * r1));
         for (int c = 0; c < 3; ++c) f[c] = -(pre * sep[c] / r1);
-    } else {
+    } else if (kind == 2) {
         double ratio = r1 / p[2];
         double r6 = 1.0 / (ratio * ratio * ratio * ratio * ratio * ratio);
         double pre = -p[0] * ratio * exp(-ratio) + p[1] * 6.0 * r6;
         for (int c = 0; c < 3; ++c) f[c] = pre * sep[c] / (r1 * r1);
+    } else if (kind == 3) {
+        double r2 = r1 - p[1], r6 = cut - p[1];
+        for (int c = 0; c < 3; ++c) f[c] = r2 * r2 < r6 * r6 ? p[0] * r2 * sep[c] / r1 : 0.0;
+    } else if (kind == 4) {
+        double n = p[2], ratio = p[1] / r1;
+        for (int c = 0; c < 3; ++c) f[c] = p[0] * (-n * pow(ratio, n)) * sep[c] / (r1 * r1);
+    } else {
+        double a = p[1], b = p[2], n = p[3];
+        for (int c = 0; c < 3; ++c) f[c] = -p[0] * n / (a - b) * pow((a - r1) / (a - b), n - 1.0) * sep[c] / r1;
     }
 }
 
@@ -563,10 +583,20 @@ static void* loop_range(void* arg) {
         const double qi = s->charge[i];
         for (int r = 0; r < m->n_single; ++r) {
             if (!has(m->single_mask[r], ti)) continue;
-            const double* p = m->single_params + 2 * (size_t)r;
-            int n = (int)p[1];
-            if (J->what == 0) J->energy += p[0] * __builtin_powi(qi, n);
-            else if (J->what == 2) chi[i] += -(p[0] * n * __builtin_powi(qi, n - 1));
+            const double* p = m->single_params + 4 * (size_t)r;
+            const int kind = m->single_kind[r];
+            if (kind == 0) { /* charge_self, Potentials.f90:4341-4375 */
+                int n = (int)p[1];
+                if (J->what == 0) J->energy += p[0] * __builtin_powi(qi, n);
+                else if (J->what == 2) chi[i] += -(p[0] * n * __builtin_powi(qi, n - 1));
+            } else if (kind == 1) { /* constant potential, 3942-3966 */
+                if (J->what == 0) J->energy += p[0];
+            } else { /* constant force, 3122-3147: F on the atom, energy -F . position */
+                const double* x = s->pos + 3 * (size_t)i;
+                if (J->what == 0) J->energy += -(p[0] * x[0] + p[1] * x[1] + p[2] * x[2]);
+                else if (J->what == 1)
+                    for (int c = 0; c < 3; ++c) F[3 * (size_t)i + c] += p[c];
+            }
         }
         for (int e = nb->start[i]; e < nb->start[i + 1]; ++e) {
             const int j = nb->idx[e];
@@ -625,11 +655,11 @@ static void* loop_range(void* arg) {
                         B2 = post_process(X, tj, grp, sums[1]);
                     }
                     double cut = sm ? smooth_factor(d, rc, rs) : 1.0;
-                    double v = pair_energy(kind, p, d);
+                    double v = pair_energy(kind, p, rc, d);
                     if (grp >= 0) J->energy += v * cut * (0.0 + 0.0 + B1 + B2) * 0.5;
                     else J->energy += v * cut;
                 } else {
-                    double v = (grp >= 0 || sm) ? pair_energy(kind, p, d) : 0.0;
+                    double v = (grp >= 0 || sm) ? pair_energy(kind, p, rc, d) : 0.0;
                     double cut = 1.0, cg[3] = {0, 0, 0};
                     if (sm) {
                         cut = smooth_factor(d, rc, rs);
@@ -645,7 +675,7 @@ static void* loop_range(void* arg) {
                         pair_bo_forces(X, i, j, 0.5 * v * cut, sep, d, grp, sums, F, st);
                     }
                     double f1[3], p1[3], p2[3];
-                    pair_force(kind, p, sep, d, f1);
+                    pair_force(kind, p, rc, sep, d, f1);
                     for (int c = 0; c < 3; ++c) {
                         if (grp >= 0) {
                             double bsum = (0.0 + 0.0 + B1 + B2) * 0.5;

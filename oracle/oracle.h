@@ -41,7 +41,7 @@ typedef struct {
 typedef struct {
     int32_t n_types;
     int32_t n_pair;
-    const int32_t* pair_kind;     /* 0 LJ, 1 exponential, 2 Buckingham */
+    const int32_t* pair_kind;     /* 0 LJ, 1 exponential, 2 Buckingham, 3 spring, 4 power, 5 shift_power */
     const double* pair_params;    /* 4 per record */
     const double* pair_cutoff;
     const double* pair_soft;      /* cutoff - cutoff_margin, as passed to add_potential */
@@ -49,8 +49,8 @@ typedef struct {
     const uint64_t* pair_mask2;   /* type bitmask of target position 2 */
     const int32_t* pair_group;    /* -1 = not scaled by a bond-order factor */
     int32_t n_single;
-    const int32_t* single_kind;   /* 0 charge_self */
-    const double* single_params;  /* 2 per record: epsilon, n */
+    const int32_t* single_kind;   /* 0 charge_self, 1 constant, 2 force */
+    const double* single_params;  /* 4 per record: (epsilon, n) | (V) | (Fx, Fy, Fz) */
     const uint64_t* single_mask;
     int32_t n_bond;
     const double* bond_params;    /* 7 per record: beta, eta, a, c, d, h, mu */

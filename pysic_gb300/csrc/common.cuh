@@ -126,11 +126,11 @@ struct CellK {
 // that the mixed-precision kernels never convert parameters per term.
 template <typename R>
 struct PairT {
-    int kind;            // 0 LJ, 1 exponential, 2 Buckingham
+    int kind;            // 0 LJ, 1 exponential, 2 Buckingham, 3 spring, 4 power, 5 shift_power
     int group;           // -1: plain, else bond-order group
     int smooth;          // smoothing active (create_potential, Potentials.f90:2382-2388)
     int in_bond_kernel;  // evaluated by the bond-order kernels (short list) rather than the pair kernel
-    R p0, p1, p2, rc, rs;
+    R p0, p1, p2, p3, rc, rs;
 };
 
 // Tersoff triplet parameters for (centre type, j type, k type) of group 0.
@@ -149,7 +149,7 @@ struct PostT {
 
 template <typename R, typename S>
 inline PairT<R> cast_pair(const PairT<S>& a) {
-    return PairT<R>{a.kind, a.group, a.smooth, a.in_bond_kernel, (R)a.p0, (R)a.p1, (R)a.p2, (R)a.rc, (R)a.rs};
+    return PairT<R>{a.kind, a.group, a.smooth, a.in_bond_kernel, (R)a.p0, (R)a.p1, (R)a.p2, (R)a.p3, (R)a.rc, (R)a.rs};
 }
 template <typename R, typename S>
 inline TripT<R> cast_trip(const TripT<S>& a) {
@@ -201,10 +201,12 @@ enum SpecIndex {
     SP_COUNT = SP_TERMS + 2 * PG_SPEC_MAX_TERMS
 };
 
+// single-atom terms: 0 charge_self (eps q^n: p[0] = eps, n = (int)p[1]),
+// 1 constant (V = p[0]), 2 constant force (F = p[0..2], V = -F . r)
 struct SingleTerm {
     int kind;
-    double eps;
     int n;
+    double p[3];
 };
 
 // 16- and 32-byte aligned 4-vectors (bond geometry, per-bond forces)

@@ -51,31 +51,63 @@ __device__ __forceinline__ void smooth(R r, R rc, R rs, R& f, R& fp) {
 // V(r) and the radial derivative dV/dr of LJ (Potentials.f90:2971-3005),
 // exponential (3643-3680) and Buckingham (4009-4045); no factor 4 in LJ.
 template <typename R>
-__device__ __forceinline__ void pair_eval(int kind, R p0, R p1, R p2, R r, R& V, R& dV) {
-    if (kind == 0) {
-        const R ratio = p1 / r;
-        const R r2 = ratio * ratio;
-        const R r6 = r2 * r2 * r2;
-        V = p0 * (r6 * r6 - r6);
-        dV = p0 * (R(6) * r6 - R(12) * r6 * r6) / r;
-    } else if (kind == 1) {
-        const R e = p0 * exp_(-p1 * r);
-        V = e;
-        dV = -p1 * e;
-    } else {
-        const R ratio = r / p2;
-        const R q2 = R(1) / (ratio * ratio);
-        const R r6 = q2 * q2 * q2;
-        const R e = p0 * exp_(-ratio);
-        V = e - p1 * r6;
-        dV = (-e * ratio + R(6) * p1 * r6) / r;
+__device__ __forceinline__ void pair_eval(const PairT<R>& P, R r, R& V, R& dV) {
+    const R p0 = P.p0, p1 = P.p1, p2 = P.p2;
+    switch (P.kind) {
+        case 0: {  // LJ: eps ((s/r)^12 - (s/r)^6), no factor 4 (evaluate_energy_LJ, Potentials.f90:2993-3005)
+            const R ratio = p1 / r;
+            const R r2 = ratio * ratio;
+            const R r6 = r2 * r2 * r2;
+            V = p0 * (r6 * r6 - r6);
+            dV = p0 * (R(6) * r6 - R(12) * r6 * r6) / r;
+            break;
+        }
+        case 1: {  // exponential: eps exp(-zeta r) (3666-3677)
+            const R e = p0 * exp_(-p1 * r);
+            V = e;
+            dV = -p1 * e;
+            break;
+        }
+        case 2: {  // Buckingham: A exp(-r/s) - C (s/r)^6 (4033-4045)
+            const R ratio = r / p2;
+            const R q2 = R(1) / (ratio * ratio);
+            const R r6 = q2 * q2 * q2;
+            const R e = p0 * exp_(-ratio);
+            V = e - p1 * r6;
+            dV = (-e * ratio + R(6) * p1 * r6) / r;
+            break;
+        }
+        case 3: {  // spring: k/2 ((r - R0)^2 - (rc - R0)^2) while |r - R0| < |rc - R0|, else 0 (3042-3085)
+            const R d = r - p1, dc = P.rc - p1;
+            if (d * d < dc * dc) {
+                V = p0 * R(0.5) * (d * d - dc * dc);
+                dV = p0 * d;
+            } else {
+                V = R(0);
+                dV = R(0);
+            }
+            break;
+        }
+        case 4: {  // power: eps (a/r)^n (4119-4152)
+            const R t = p0 * pow_(p1 / r, p2);
+            V = t;
+            dV = -p2 * t / r;
+            break;
+        }
+        default: {  // shift_power: eps ((r1 - r)/(r1 - r2))^n (4803-4842)
+            const R w = p1 - p2;
+            const R x = (p1 - r) / w;
+            V = p0 * pow_(x, P.p3);
+            dV = -p0 * P.p3 / w * pow_(x, P.p3 - R(1));
+            break;
+        }
     }
 }
 
 // V f and d(V f)/dr of one pair term, smoothing included
 template <typename R>
 __device__ __forceinline__ void pair_term(const PairT<R>& P, R r, R& V, R& dV) {
-    pair_eval<R>(P.kind, P.p0, P.p1, P.p2, r, V, dV);
+    pair_eval<R>(P, r, V, dV);
     if (P.smooth) {
         R f, fp;
         smooth<R>(r, P.rc, P.rs, f, fp);

@@ -131,25 +131,42 @@ __device__ __forceinline__ void pair_body(const PairArgs& A, int blk) {
             w5 += h * x * y;
         }
     }
-    // single-atom terms in FP64 (charge_self: epsilon q^n, chi = -epsilon n q^(n-1);
-    // Potentials.f90:4341-4375), added by the group's lane 0
-    double cs = 0.0;
+    // single-atom terms in FP64, added by the group's lane 0
+    // (core_evaluate_local_singlet, Core.f90:4095-4239): charge_self eps q^n with
+    // chi = -eps n q^(n-1) (Potentials.f90:4341-4375), constant V (3959-3966),
+    // constant force F with energy -F . r at the absolute position (3122-3147);
+    // singlets add nothing to the virial
+    double cs = 0.0, es = 0.0, sf0 = 0.0, sf1 = 0.0, sf2 = 0.0;
     if (act && lane == 0) {
         const int2 sx = A.sindex[ti];
-        if (sx.y > 0) {
-            const double qd = A.charge[i];
-            double es = 0.0;
-            for (int t = sx.x; t < sx.x + sx.y; ++t) {
-                const SingleTerm S = A.sterms[t];
-                es += S.eps * powi_(qd, S.n);
-                cs += -(S.eps * S.n * powi_(qd, S.n - 1));
+        for (int t = sx.x; t < sx.x + sx.y; ++t) {
+            const SingleTerm S = A.sterms[t];
+            if (S.kind == 0) {
+                const double qd = A.charge[i];
+                es += S.p[0] * powi_(qd, S.n);
+                cs += -(S.p[0] * S.n * powi_(qd, S.n - 1));
+            } else if (S.kind == 1) {
+                es += S.p[0];
+            } else {
+                es -= S.p[0] * A.pos[3 * i] + S.p[1] * A.pos[3 * i + 1] + S.p[2] * A.pos[3 * i + 2];
+                sf0 += S.p[0];
+                sf1 += S.p[1];
+                sf2 += S.p[2];
             }
-            en += (R)es;
         }
     }
     if (wantF) {
-        const auto sfx = group_sum_f<G>(fx), sfy = group_sum_f<G>(fy), sfz = group_sum_f<G>(fz);
+        auto sfx = group_sum_f<G>(fx), sfy = group_sum_f<G>(fy), sfz = group_sum_f<G>(fz);
         if (act && lane == 0) {
+            if constexpr (sizeof(R) == 4) {
+                sfx.f += fix_from_double(sf0);
+                sfy.f += fix_from_double(sf1);
+                sfz.f += fix_from_double(sf2);
+            } else {
+                sfx.s += sf0;
+                sfy.s += sf1;
+                sfz.s += sf2;
+            }
             store_sum(A.out_f + 3 * i, sfx, A.first_f);
             store_sum(A.out_f + 3 * i + 1, sfy, A.first_f);
             store_sum(A.out_f + 3 * i + 2, sfz, A.first_f);
@@ -165,8 +182,9 @@ __device__ __forceinline__ void pair_body(const PairArgs& A, int blk) {
     }
     // energy and virial: warp sums, exact from there on
     if (A.acc && (wantE || wantF)) {
-        const Fx128 v[7] = {warp_total(en), warp_total(w0), warp_total(w1), warp_total(w2),
-                            warp_total(w3), warp_total(w4), warp_total(w5)};
+        // the single-atom energies join the total exactly, outside the working precision
+        const Fx128 v[7] = {fx_add(warp_total(en), fx_warp_sum(fx_from_double(es))), warp_total(w0), warp_total(w1),
+                            warp_total(w2), warp_total(w3), warp_total(w4), warp_total(w5)};
         block_totals_publish(v, wsum, &done, A.acc);
     }
 }

@@ -113,6 +113,7 @@ void fold_tables(pg_context* ctx) {
                 t.p0 = ctx->pr_params[4 * (size_t)r];
                 t.p1 = ctx->pr_params[4 * (size_t)r + 1];
                 t.p2 = ctx->pr_params[4 * (size_t)r + 2];
+                t.p3 = ctx->pr_params[4 * (size_t)r + 3];
                 t.rc = ctx->pr_cut[r];
                 const double soft = ctx->pr_soft[r];
                 if (soft > 0.0 && soft < t.rc) {
@@ -138,8 +139,8 @@ void fold_tables(pg_context* ctx) {
             if (has(ctx->sr_m[r], t)) {
                 SingleTerm s{};
                 s.kind = ctx->sr_kind[r];
-                s.eps = ctx->sr_params[2 * (size_t)r];
-                s.n = (int)ctx->sr_params[2 * (size_t)r + 1];
+                for (int c = 0; c < 3; ++c) s.p[c] = ctx->sr_params[4 * (size_t)r + c];
+                s.n = s.kind == 0 ? (int)s.p[1] : 0;  // charge_self: the reference's integer n = int(param2)
                 sterms.push_back(s);
             }
         sindex[t].y = (int)sterms.size() - sindex[t].x;

@@ -323,7 +323,7 @@ __device__ __forceinline__ void bond_body(const BondArgs& A, int blk, int nblk) 
                 if (!PT.in_bond_kernel || !(r < PT.rc)) continue;
                 R V, dV;
                 if (PT.smooth && PT.rc == bc.x && PT.rs == bc.y) {
-                    pair_eval<R>(PT.kind, PT.p0, PT.p1, PT.p2, r, V, dV);
+                    pair_eval<R>(PT, r, V, dV);
                     const V2 fc = cut[e];
                     dV = dV * fc.x + V * fc.y;
                     V = V * fc.x;

@@ -69,7 +69,7 @@ class Model:
         d["pair_mask2"] = np.array(self.pair_mask2, dtype=np.uint64)
         d["pair_group"] = np.array(self.pair_group, dtype=np.int32)
         d["single_kind"] = np.array(self.single_kind, dtype=np.int32)
-        d["single_params"] = np.array(self.single_params, dtype=np.float64).reshape(-1, 2)
+        d["single_params"] = np.array(self.single_params, dtype=np.float64).reshape(-1, 4)
         d["single_mask"] = np.array(self.single_mask, dtype=np.uint64)
         d["bond_params"] = np.array(self.bond_params, dtype=np.float64).reshape(-1, 7)
         d["bond_cutoff"] = np.array(self.bond_cutoff, dtype=np.float64)
@@ -178,7 +178,7 @@ def compile_model(atoms, potentials, coulomb=None):
                                             "engine")
             for tg in targets:
                 M.single_kind.append(core.SINGLE_KIND[kind])
-                M.single_params.append((params + [0.0] * 2)[:2])
+                M.single_params.append((params + [0.0] * 4)[:4])
                 M.single_mask.append(_mask(sigs, *tg[0]))
         else:
             raise InvalidPotentialError("{0}-body potentials are not evaluated by the GB300 engine".format(nt))

@@ -100,10 +100,28 @@ def test_types_fold_tags_and_indices():
     assert len(M.pair_kind) == 3  # (1,1) once, (0,2) and (2,0)
 
 
-def test_unsupported_potential_rejected_at_compile():
+@pytest.mark.parametrize("kind,symbols", [("step", [["Si", "Si"]]), ("charge_pair", [["Si", "Si"]]),
+                                          ("dihedral", [["Si", "Si", "Si", "Si"]])])
+def test_unsupported_potential_rejected_at_compile(kind, symbols):
     atoms = W.diamond_si(1)
     with pytest.raises(pysic.InvalidPotentialError):
-        compile_model(atoms, [pysic.Potential("spring", symbols=[["Si", "Si"]], cutoff=3.0)])
+        compile_model(atoms, [pysic.Potential(kind, symbols=symbols, cutoff=3.0)])
+
+
+def test_new_pair_and_single_kinds_compile():
+    atoms = W.diamond_si(1)
+    pots = [pysic.Potential("spring", symbols=[["Si", "Si"]], parameters=[2.0, 2.3], cutoff=3.0),
+            pysic.Potential("power", symbols=[["Si", "Si"]], parameters=[0.5, 2.0, 3.0], cutoff=3.0),
+            pysic.Potential("shift_power", symbols=[["Si", "Si"]], parameters=[0.5, 3.2, 2.0, 2.0], cutoff=3.0),
+            pysic.Potential("constant", symbols=[["Si"]], parameters=[-0.25]),
+            pysic.Potential("force", symbols=[["Si"]], parameters=[0.1, -0.2, 0.3])]
+    M = compile_model(atoms, pots)
+    assert list(M.pair_kind) == [3, 4, 5]
+    assert list(M.single_kind) == [1, 2]
+    a = M.arrays()
+    assert a["single_params"].shape == (2, 4)
+    np.testing.assert_array_equal(a["single_params"][1], [0.1, -0.2, 0.3, 0.0])
+    np.testing.assert_array_equal(a["pair_params"][2], [0.5, 3.2, 2.0, 2.0])
 
 
 def test_charge_relaxation_api():

@@ -224,3 +224,33 @@ def test_rejected_coordinate_update_keeps_the_old_positions():
     ref = oracle_all(pysic.Atoms(atoms.get_chemical_symbols(), moved, cell=atoms.get_cell(), pbc=atoms.get_pbc()),
                      W.tersoff_si_potentials(), lists=oracle_lists(atoms, W.tersoff_si_potentials()))
     assert np.abs(r["forces"] - ref["forces"]).max() < 1e-10
+
+
+def _more_kinds():
+    P = pysic.Potential
+    atoms = W.lj_fcc(3, noise=0.08, seed=31)
+    pots = [P("spring", symbols=[["X", "X"]], parameters=[0.3, 3.7], cutoff=5.0),
+            P("power", symbols=[["X", "X"]], parameters=[0.05, 3.0, 6.5], cutoff=6.0, cutoff_margin=0.5),
+            P("shift_power", symbols=[["X", "X"]], parameters=[0.02, 6.5, 3.0, 3.0], cutoff=6.0),
+            P("constant", symbols=[["X"]], parameters=[-0.1]),
+            P("force", symbols=[["X"]], parameters=[0.05, -0.02, 0.01])]
+    return atoms, pots
+
+
+def test_spring_power_shift_power_constant_force_fp64_parity():
+    """The pair kinds spring, power, shift_power (Potentials.f90:3042-3085,
+    4119-4152, 4803-4842) and the single-atom constant and constant-force terms
+    (3122-3147, 3942-3966) against the oracle."""
+    atoms, pots = _more_kinds()
+    ref, got = _check_fp64(atoms, pots)
+    # the constant forces show in the forces and leave the virial alone
+    assert abs(ref["forces"][:, 0].sum() - 0.05 * len(atoms)) < 1e-9
+
+
+def test_spring_power_shift_power_constant_force_mixed():
+    atoms, pots = _more_kinds()
+    ref = oracle_all(atoms, pots)
+    got = engine_all(atoms, pots, None, "mixed")
+    n = len(atoms)
+    assert abs(got["energy"] - ref["energy"]) / n <= 1e-5
+    assert np.abs(got["forces"] - ref["forces"]).max() <= 1e-4 * max(1.0, np.abs(ref["forces"]).max())
