@@ -215,6 +215,12 @@ static int autotune_lanes(pg_context* ctx, int precision, int flags) {
 void evaluate(pg_context* ctx, int precision, int flags) {
     require(precision == PG_PREC_FP64 || precision == PG_PREC_MIXED, PG_ERR_INVALID, "unknown precision");
     prepare(ctx);
+    if (ctx->n == 0) {  // no atoms: zero totals, nothing to launch
+        ctx->out_acc.resize(8);
+        PG_CUDA(cudaMemsetAsync(ctx->out_acc.p, 0, sizeof(FxAcc) * 8, ctx->stream));
+        ctx->launches = 0;
+        return;
+    }
     int G = ctx->lanes;
     if (G == 0 && ctx->have_bond_terms) {
         if (ctx->tuned_lanes[precision] == 0) ctx->tuned_lanes[precision] = autotune_lanes(ctx, precision, flags);

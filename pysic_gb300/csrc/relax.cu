@@ -205,6 +205,12 @@ void relax_charges(pg_context* ctx, int precision, int mode, int n_steps, double
     require(ctx->have_list && ctx->have_atoms, PG_ERR_NOT_READY, "set atoms, potentials and lists first");
     prepare(ctx);
     const int n = ctx->n;
+    if (n == 0) {  // nothing to relax
+        *steps = 0;
+        *error = 0.0;
+        *max_dq = 0.0;
+        return;
+    }
     cudaStream_t st = ctx->stream;
     const int nb = std::max(1, (n + RT - 1) / RT);
     ctx->out_chi.resize((size_t)std::max(n, 1));
