@@ -69,9 +69,10 @@ struct BondArgs {
     int nblocks;          // blocks of this system in the bond and gather passes (many-system launch)
     int flags;
     int first_f;
-    void* geo;
-    void* fj;
-    void* kacc;        // per entry i->k: the k parts of i's bonds on k (unstaged atoms' scratch)
+    void* geo;         // per entry: bond geometry (atoms with more bonds than shared memory holds)
+    void* fj;          // per entry m->x: the force of x's bonds on m, written by x through rev
+    void* kacc;        // per entry i->k: the k parts of i's bonds on k
+    void* bscr;        // per entry: running j parts of unstaged atoms' bonds
     void* fc;          // per atom: i part of the force (FP64, or 2^-32 fixed point in the mixed path)
     double* out_f;
     FxAcc* acc;        // global energy / virial totals (null: not wanted)

@@ -327,8 +327,8 @@ struct pg_context {
     pg::DevBuf<int> scan_tmp;
 
     // bond-order scratch
-    pg::DevBuf<pg::F4> bo_fj;             // mixed precision: 3 records per short entry
-    pg::DevBuf<pg::D4> bo_fj64;           // FP64: 3 records per short entry
+    pg::DevBuf<pg::F4> bo_fj;             // mixed precision: 4 records per short entry
+    pg::DevBuf<pg::D4> bo_fj64;           // FP64: 4 records per short entry
     pg::DevBuf<double> bo_fc;             // centre-role forces per atom (3)
     pg::DevBuf<double> bo_zeta;           // per short entry (diagnostics)
     int lanes = 0;                        // 0: autotune

@@ -75,7 +75,7 @@ void bond_order_noalloc(pg_context* ctx, int precision, double* d_forces, double
     const size_t b_acc = align256(8 * sizeof(FxAcc));
     const size_t b_disp = align256(n * sizeof(F4));
     const size_t b_fc = align256(3 * n * sizeof(double));
-    const size_t b_bonds = align256(3 * ne * rec);
+    const size_t b_bonds = align256(4 * ne * rec);
     const size_t need = b_acc + b_disp + b_fc + b_bonds;
     if (need > (size_t)PG_NOALLOC_SCRATCH_BYTES)
         throw Error(PG_ERR_INVALID, "the no-allocation bond-order call needs " + std::to_string(need) +

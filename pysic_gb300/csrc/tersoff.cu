@@ -176,6 +176,16 @@ __device__ __forceinline__ void bond_body(const BondArgs& A, int blk, int nblk) 
         else return typ[k];
     };
     V4* fj = (V4*)A.fj;
+    // the lane's first bond: partner index and build-time bond vector are not
+    // written by the kernel before, so they are fetched ahead of the wait
+    int j_pre = 0;
+    F4 s0_pre{};
+    if constexpr (sizeof(R) == 4) {
+        if (act && lane < ni) {
+            j_pre = A.idx[s + lane];
+            s0_pre = A.sep0[s + lane];
+        }
+    }
     // the displacements (mixed path) and the totals come from the kernel before
     pdl_wait();
     // geometry of i's bonds in the working precision, and per bond what every
@@ -188,7 +198,19 @@ __device__ __forceinline__ void bond_body(const BondArgs& A, int blk, int nblk) 
             zi = A.pos[3 * i + 2];
         }
         for (int e = lane; e < ni; e += G) {
-            const V4 g = bond_vector<R>(A, i, s + e, xi, yi, zi);
+            V4 g;
+            if constexpr (sizeof(R) == 4) {
+                if (e == lane) {
+                    const F4 dj = A.disp[j_pre], di = A.disp[i];
+                    const float x = s0_pre.x + (dj.x - di.x), y = s0_pre.y + (dj.y - di.y),
+                                z = s0_pre.z + (dj.z - di.z);
+                    g = F4{x, y, z, sqrtf(x * x + y * y + z * z)};
+                } else {
+                    g = bond_vector<R>(A, i, s + e, xi, yi, zi);
+                }
+            } else {
+                g = bond_vector<R>(A, i, s + e, xi, yi, zi);
+            }
             geo[e] = g;
             if (staged) {
                 const R ir = g.w > R(0) ? rcp_(g.w) : R(0);
@@ -226,7 +248,7 @@ __device__ __forceinline__ void bond_body(const BondArgs& A, int blk, int nblk) 
     R W0 = 0, W1 = 0, W2 = 0, W3 = 0, W4 = 0, W5 = 0;
     // per bond e (owned by lane e % G): the force on its partner j so far, and
     // in .w the three-body prefactor 1/2 V f dB/dzeta
-    V4* bacc = staged ? sbacc + slot * CAPP : fj + s;
+    V4* bacc = staged ? sbacc + slot * CAPP : (V4*)A.bscr + s;
     V4* kacc = (V4*)A.kacc + s;  // per bond k: the group's k parts, written once
     R maxbr = R(0);
     if constexpr (SPEC) maxbr = SPV(SP_RC);
@@ -416,10 +438,12 @@ __device__ __forceinline__ void bond_body(const BondArgs& A, int blk, int nblk) 
         kz = group_sum<G>(kz);
         if (k < ni && lane == k % G) kacc[k] = V4{kx, ky, kz, 0};
     }
-    // per entry i->x: the force of this atom's bonds on x (j part + k parts)
+    // per entry i->x: the force of this atom's bonds on x (j part + k parts),
+    // stored in x's own entry x->i (the reverse), so that the gather pass reads
+    // each atom's records contiguously
     for (int e = lane; e < ni; e += G) {
         const V4 be = bacc[e], ke = kacc[e];
-        fj[s + e] = V4{be.x + ke.x, be.y + ke.y, be.z + ke.z, 0};
+        fj[A.rev[s + e]] = V4{be.x + ke.x, be.y + ke.y, be.z + ke.z, 0};
     }
     const auto d0 = group_sum_f<G>(Fx), d1 = group_sum_f<G>(Fy), d2 = group_sum_f<G>(Fz);
     if (lane == 0) {
@@ -451,17 +475,18 @@ __device__ __forceinline__ void gather_body(const BondArgs& A, int blk, int nblk
     const V4* fj = (const V4*)A.fj;
     const int lane = threadIdx.x % G;
     const int slot = threadIdx.x / G;
-    const int gslot = A.order ? dealt_slot<G>(blk, nblk) : blk * (blockDim.x / G) + slot;
-    const bool act = gslot < A.n;
-    const int m = act ? (A.order ? A.order[gslot] : gslot) : 0;
+    // atoms in index order: every atom's records are short and contiguous, so
+    // no load balancing by list length is needed here
+    const int m = blk * (blockDim.x / G) + slot;
+    const bool act = m < A.n;
     R Fx = 0, Fy = 0, Fz = 0;
+    // the list bounds are not written by the bond pass: read before the wait
+    const int s = act ? A.start[m] : 0, nm = act ? A.start[m + 1] - s : 0;
     pdl_wait();  // the bond pass's records
     if (act) {
-        // every neighbour i left the force of its bonds on m in its entry i->m,
-        // the reverse of m's entry m->i
-        const int s = A.start[m], nm = A.start[m + 1] - s;
+        // every neighbour x left the force of its bonds on m in m's entry m->x
         for (int e = lane; e < nm; e += G) {
-            const V4 a = fj[A.rev[s + e]];
+            const V4 a = fj[s + e];
             Fx += a.x;
             Fy += a.y;
             Fz += a.z;
@@ -521,9 +546,10 @@ int bond_blocks(int n, int G) { return (n + (128 / G) - 1) / (128 / G); }
 
 void prepare_bond_scratch(pg_context* ctx, int precision) {
     const size_t ne = (size_t)std::max<long long>(ctx->sh_total, 1);
-    // per short-list entry: bond geometry | force on the partner | k-part sums
-    if (precision == PG_PREC_FP64) ctx->bo_fj64.resize(3 * ne);
-    else ctx->bo_fj.resize(3 * ne);
+    // per short-list entry: bond geometry | force from the partner's bonds | k-part
+    // sums | unstaged j parts
+    if (precision == PG_PREC_FP64) ctx->bo_fj64.resize(4 * ne);
+    else ctx->bo_fj.resize(4 * ne);
     ctx->bo_fc.resize(3 * (size_t)std::max(ctx->n, 1));
 }
 
@@ -574,6 +600,7 @@ BondArgs make_bond_args(pg_context* ctx, int precision, int flags, bool first_f,
         A.geo = ctx->bo_fj64.p;
         A.fj = ctx->bo_fj64.p + ne;
         A.kacc = ctx->bo_fj64.p + 2 * ne;
+        A.bscr = ctx->bo_fj64.p + 3 * ne;
     } else {
         A.terms = ctx->d_pair_terms32.p;
         A.trip = ctx->d_trip32.p;
@@ -583,6 +610,7 @@ BondArgs make_bond_args(pg_context* ctx, int precision, int flags, bool first_f,
         A.geo = ctx->bo_fj.p;
         A.fj = ctx->bo_fj.p + ne;
         A.kacc = ctx->bo_fj.p + 2 * ne;
+        A.bscr = ctx->bo_fj.p + 3 * ne;
         A.sep0 = ctx->sh_sep0.p;
         A.disp = ctx->disp32.p;
     }
@@ -627,7 +655,7 @@ void launch_bond_order_impl(pg_context* ctx, int precision, int flags, bool firs
 }
 
 // The two passes on scratch the caller provides instead of the context's
-// buffers (the no-allocation entry point): bonds holds 3 records per short-list
+// buffers (the no-allocation entry point): bonds holds 4 records per short-list
 // entry, fc 3 values per atom, disp (mixed path) one record per atom.  Energy
 // and virial go to acc, forces to out_f (written).
 void launch_bond_order_scratch(pg_context* ctx, int precision, int G, void* bonds, void* fc, F4* disp, FxAcc* acc,
@@ -638,6 +666,7 @@ void launch_bond_order_scratch(pg_context* ctx, int precision, int G, void* bond
     A.geo = bonds;
     A.fj = (char*)bonds + ne * rec;
     A.kacc = (char*)bonds + 2 * ne * rec;
+    A.bscr = (char*)bonds + 3 * ne * rec;
     A.fc = fc;
     A.out_f = out_f;
     auto none = [] {};
