@@ -60,6 +60,7 @@ struct BondArgs {
     int bcut_uniform;   // bcut holds for every tj
     const int* etype;   // per entry: partner type
     const int* order;   // lane-group slot -> atom (atoms grouped by list length)
+    const int4* slot;   // per slot: atom, first short entry, entry count (one load instead of a chain)
     int n_terms;        // pair records in terms
     const F4* sep0;     // mixed path: bond vectors at list build
     const F4* disp;     // mixed path: per-atom displacement since the build

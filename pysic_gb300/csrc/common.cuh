@@ -305,6 +305,7 @@ struct pg_context {
     bool short_dirty = true;
     bool short_is_full = false;
     pg::DevBuf<int> sh_start, sh_idx, sh_off, sh_rev, sh_count;
+    pg::DevBuf<int4> sh_slot;  // per lane-group slot: atom, first entry, count (sh_order applied)
     pg::DevBuf<int> sh_order;      // atoms in order of their short-list length (lane groups of equal work)
     pg::DevBuf<int> sh_type;       // per short entry: type of the partner atom
     // mixed path: bond vectors of both lists taken once per list generation in

@@ -869,6 +869,17 @@ void build_short_list(pg_context* ctx) {
         for (int m = 0; m < n; ++m) order[(size_t)first[(size_t)cnt[m]]++] = m;
     }
     ctx->sh_order.upload(order.data(), order.size(), st);
+    // the same order with each atom's entry range, for a single load per slot
+    std::vector<int4> slot((size_t)std::max(n, 1), make_int4(0, 0, 0, 0));
+    {
+        std::vector<int> first((size_t)std::max(n, 1), 0);
+        for (int m = 1; m < n; ++m) first[(size_t)m] = first[(size_t)m - 1] + cnt[(size_t)m - 1];
+        for (int k = 0; k < n; ++k) {
+            const int m = order[(size_t)k];
+            slot[(size_t)k] = make_int4(m, first[(size_t)m], cnt[(size_t)m], 0);
+        }
+    }
+    ctx->sh_slot.upload(slot.data(), slot.size(), st);
     PG_CUDA(cudaStreamSynchronize(st));
     ctx->short_dirty = false;
     ctx->state_epoch++;

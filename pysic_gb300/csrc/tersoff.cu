@@ -149,9 +149,19 @@ __device__ __forceinline__ void bond_body(const BondArgs& A, int blk, int nblk) 
     const int slot = threadIdx.x / G;
     const int gslot = A.order ? dealt_slot<G>(blk, nblk) : blk * AP + slot;
     const bool act = gslot < A.n;
-    const int i = act ? (A.order ? A.order[gslot] : gslot) : 0;
-    const int s = act ? A.start[i] : 0;
-    const int ni = act ? A.start[i + 1] - s : 0;
+    int i = 0, s = 0, ni = 0;
+    if (act) {
+        if (A.slot) {
+            const int4 rec = A.slot[gslot];
+            i = rec.x;
+            s = rec.y;
+            ni = rec.z;
+        } else {
+            i = A.order ? A.order[gslot] : gslot;
+            s = A.start[i];
+            ni = A.start[i + 1] - s;
+        }
+    }
     const bool staged = ni <= CAP;
     auto SPV = [&](int k) -> R {
         if constexpr (sizeof(R) == 4) return A.spf[k];
@@ -578,6 +588,7 @@ BondArgs make_bond_args(pg_context* ctx, int precision, int flags, bool first_f,
     A.rev = ctx->sh_rev.p;
     A.etype = ctx->sh_type.p;
     A.order = ctx->sh_order.p;
+    A.slot = ctx->sh_slot.p;
     A.n_terms = ctx->n_pair_terms;
     A.index = ctx->d_pair_index.p;
     A.bcut_uniform = ctx->bcut_uniform ? 1 : 0;
