@@ -164,6 +164,19 @@ int pg_relax_charges_potentiostat(pg_context* ctx, int32_t precision, int32_t n_
                                   double inertia, double potential, double* rates, double* charges,
                                   double* max_dchi);
 
+/* ChargeRelaxation 'optimize' (pysic/charges/relaxation.py:483-488; the
+ * reference calls SciPy's SLSQP on the energy and electronegativities) for
+ * energies quadratic in the charges (Ewald and charge_self with n <= 2): the
+ * constrained minimum at fixed total charge by projected conjugate gradients on
+ * the device.  Stops when max |chi - mean(chi)| <= tolerance (recomputed from
+ * the final charges) or after max_iterations; charges receives the result (the
+ * context keeps it), *iterations and *error the count and the final max |chi -
+ * mean(chi)|.  PG_ERR_UNSUPPORTED for other energies (the caller falls back to
+ * SLSQP), PG_ERR_NOT_CONVERGED at the iteration limit or for a non-convex
+ * energy. */
+int pg_optimize_charges(pg_context* ctx, int32_t precision, int32_t max_iterations, double tolerance,
+                        double* charges, int32_t* iterations, double* error);
+
 /* Per ordered bond (CSR entry of the engine's short list) Tersoff sums zeta_ij of
  * group 0: the quantity core_calculate_pair_bond_order_factor (Core.f90:2439-2637)
  * accumulates.  Diagnostic; n_entries receives the short-list length. */

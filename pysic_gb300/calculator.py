@@ -287,8 +287,13 @@ class Pysic:
             quantities = [quantities]
         attr = {"energy": "energy", "forces": "forces", "stress": "stress",
                 "electronegativities": "electronegativities"}
+        # the structure changed in place since the last evaluation (charges set
+        # through get_atoms(), as the relaxations do): every cached result is stale
+        if self._engine_stale():
+            self._invalidate()
+            return True
         need = [getattr(self, attr[q]) is None for q in quantities if q in attr]
-        return any(need) or self._engine_stale()
+        return any(need)
 
     # --- engine synchronisation (set_core, calculator.py:998-1637) ------------
     def _engine_stale(self):

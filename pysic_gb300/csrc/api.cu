@@ -567,6 +567,27 @@ int pg_relax_charges(pg_context* ctx, int32_t precision, int32_t n_steps, double
     });
 }
 
+int pg_optimize_charges(pg_context* ctx, int32_t precision, int32_t max_iterations, double tolerance,
+                        double* charges, int32_t* iterations, double* error) {
+    return guarded([&] {
+        check_ctx(ctx);
+        use_device(ctx);
+        pg::require(max_iterations >= 0, PG_ERR_INVALID, "negative iteration count");
+        pg::require(charges && iterations && error, PG_ERR_INVALID, "null output pointer");
+        int it = 0;
+        double err = 0.0;
+        try {
+            pg::optimize_charges(ctx, precision, max_iterations, tolerance, charges, &it, &err);
+        } catch (...) {
+            *iterations = it;
+            *error = err;
+            throw;
+        }
+        *iterations = it;
+        *error = err;
+    });
+}
+
 int pg_relax_charges_potentiostat(pg_context* ctx, int32_t precision, int32_t n_steps, double timestep,
                                   double inertia, double potential, double* rates, double* charges, double* max_dchi) {
     return guarded([&] {

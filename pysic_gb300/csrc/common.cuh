@@ -343,6 +343,8 @@ struct pg_context {
     // charge relaxation
     pg::DevBuf<double> rq_rate, rq_save, rq_stat;
     pg::DevBuf<int> rq_flag;
+    pg::DevBuf<double> cg_buf;  // charge optimisation: q, r, p, H p, chi(0), partials, scalars
+    pg::DevBuf<int> cg_flag;
 
     int launches = 0;
 
@@ -452,6 +454,9 @@ cudaStream_t batch_stream(const pg_batch* b);
 // relax.cu: mode PG_RELAX_DYNAMIC (damped, to a tolerance) or
 // PG_RELAX_POTENTIOSTAT (undamped, fixed external potential, fixed step count)
 constexpr int PG_RELAX_DYNAMIC = 0, PG_RELAX_POTENTIOSTAT = 1;
+// optimize.cu: the constrained energy minimum over the charges (quadratic energies)
+void optimize_charges(pg_context* ctx, int precision, int max_iter, double tolerance, double* charges, int* iterations,
+                      double* error);
 void relax_charges(pg_context* ctx, int precision, int mode, int n_steps, double dt, double inertia, double friction,
                    double tolerance, double potential, double* rates, double* charges, int* steps, double* error,
                    double* max_dq);

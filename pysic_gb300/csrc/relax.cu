@@ -27,6 +27,7 @@
 #include <vector>
 
 #include "common.cuh"
+#include "reduce.cuh"
 
 namespace pg {
 
@@ -55,42 +56,6 @@ struct RxArgs {
     int nblocks;
     F4* disp;         // mixed path: the FP32 charge copy in .w follows q (null: FP64 path)
 };
-
-// block-wide sum or max; the result is valid in thread 0
-__device__ __forceinline__ double block_reduce(double v, bool is_max, double* sh) {
-    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5, nw = blockDim.x >> 5;
-#pragma unroll
-    for (int o = 16; o > 0; o >>= 1) {
-        const double u = __shfl_xor_sync(0xffffffffu, v, o);
-        v = is_max ? fmax(v, u) : v + u;
-    }
-    if (lane == 0) sh[w] = v;
-    __syncthreads();
-    if (w == 0) {
-        v = lane < nw ? sh[lane] : (is_max ? -1e300 : 0.0);
-#pragma unroll
-        for (int o = 16; o > 0; o >>= 1) {
-            const double u = __shfl_xor_sync(0xffffffffu, v, o);
-            v = is_max ? fmax(v, u) : v + u;
-        }
-    }
-    return v;
-}
-
-// true in thread 0 of the block that takes the last ticket: by then every other
-// block has published its partial (fence before the ticket).  The last block
-// puts the counter back to zero for the next launch.
-__device__ __forceinline__ bool last_block(int* ticket) {
-    __shared__ int is_last;
-    if (threadIdx.x == 0) {
-        __threadfence();
-        const int last = atomicAdd(ticket, 1) == (int)gridDim.x - 1;
-        if (last) *ticket = 0;
-        is_last = last;
-    }
-    __syncthreads();
-    return is_last && threadIdx.x == 0;
-}
 
 __global__ void __launch_bounds__(RT) rx_mean(RxArgs A) {
     __shared__ double sh[RT / 32];

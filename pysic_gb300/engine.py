@@ -144,6 +144,21 @@ class Engine:
         return {"charges": q, "rates": rates, "steps": steps.value, "error": err.value, "max_dq": dq.value,
                 "converged": st == L.PG_OK}
 
+    def optimize_charges(self, precision, max_iterations, tolerance):
+        """Constrained energy minimum over the charges on the device
+        (pg_optimize_charges).  Returns None when the energy is not quadratic
+        in the charges (the caller then uses SLSQP)."""
+        q = np.zeros(self.n)
+        it = ctypes.c_int32(0)
+        err = ctypes.c_double(0)
+        st = self.lib.pg_optimize_charges(self.ctx, precision, int(max_iterations), float(tolerance), L.dptr(q),
+                                          ctypes.byref(it), ctypes.byref(err))
+        if st == L.PG_ERR_UNSUPPORTED:
+            return None
+        if st not in (L.PG_OK, L.PG_ERR_NOT_CONVERGED):
+            L.check(st)
+        return {"charges": q, "iterations": it.value, "error": err.value, "converged": st == L.PG_OK}
+
     def relax_charges_potentiostat(self, precision, n_steps, timestep, inertia, potential, rates):
         rates = L.as_f64(rates).copy()
         q = np.zeros(self.n)

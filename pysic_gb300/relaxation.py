@@ -9,8 +9,11 @@ without host round trips, and only the convergence statistics come back.
 potential, a fixed number of steps).  With observers attached the device loop
 returns to the host at every step where one is due, so that each sees the
 atoms' charges of its step as in the reference (510-550); the cut loop takes
-the same steps as the uncut one.  'optimize' (483-488) uses SciPy's SLSQP on
-the GPU energy and gradient when SciPy is available.
+the same steps as the uncut one.  'optimize' (483-488) finds the constrained
+energy minimum on the device by projected conjugate gradients when the energy
+is quadratic in the charges (pg_optimize_charges; it stops on
+max |chi - mean(chi)| <= tolerance), else it runs SciPy's SLSQP on the GPU
+energy and gradient as the reference does.
 """
 import math
 
@@ -210,6 +213,20 @@ class ChargeRelaxation:
             charges = r["charges"]
             self.last_error = r["max_dchi"]
         elif self.relaxation == "optimize":
+            # on the device when the energy is quadratic in the charges
+            calc.set_core()
+            prec = calc._prec() if precision is None else precision
+            r = calc.engine.optimize_charges(prec, int(self.parameters["n_steps"]), self.parameters["tolerance"])
+            if r is not None:
+                charges = r["charges"]
+                self._set(atoms, charges)
+                pushed = getattr(calc, "_pushed", None)
+                if pushed is not None:
+                    pushed["charges"] = np.array(charges, dtype=np.float64)
+                self.last_steps = r["iterations"]
+                self.last_error = r["error"]
+                self.last_converged = r["converged"]
+                return self._finish(charges)
             try:
                 from scipy.optimize import fmin_slsqp
             except ImportError:
@@ -227,6 +244,11 @@ class ChargeRelaxation:
             charges = fmin_slsqp(energy, charges, fprime=grad, eqcons=[lambda q, *a: np.sum(q) - total],
                                  acc=self.parameters["tolerance"], iter=int(self.parameters["n_steps"]), disp=0)
             self._set(atoms, charges)
+        return self._finish(charges)
+
+    def _finish(self, charges):
+        """The reference's epilogue (relaxation.py:492-503): the attached
+        structure gets the charges, then a piped relaxation runs."""
         if self.atoms is not None:
             try:
                 self.atoms.set_initial_charges(charges)

@@ -175,3 +175,46 @@ def test_observers_see_every_due_step_and_do_not_change_the_run():
     r = oracle.relax_charges(atoms.get_positions(), np.zeros(len(atoms)), atoms.get_cell(), atoms.get_pbc(), model,
                              *lists, n_steps=14, timestep=0.1, inertia=1.0, friction=4.0, tolerance=1e-4)
     np.testing.assert_allclose(seen[1][1], r["charges"], atol=1e-9)
+
+
+def _optimize_case():
+    atoms = W.sio2_box(60, seed=10)
+    atoms.set_initial_charges(np.zeros(len(atoms)))
+    pots, coul = W.sio2_potentials(real_cutoff=5.5, sigma=1.6)
+    return atoms, pots, coul
+
+
+@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+def test_optimize_on_device_reaches_the_dynamic_minimum(precision):
+    """'optimize' (relaxation.py:483-488) by projected conjugate gradients on
+    the device: the constrained minimum the damped dynamics converge to, in far
+    fewer electronegativity evaluations, total charge unchanged."""
+    atoms, pots, coul = _optimize_case()
+    calc = pysic.Pysic(atoms.copy(), pots, coulomb=coul, precision="fp64")
+    dyn = pysic.ChargeRelaxation("dynamic", calculator=calc, parameters=[4000, 0.05, 1.0, 3.0, 1e-9])
+    q_dyn = dyn.charge_relaxation()
+    assert dyn.last_converged
+    calc2 = pysic.Pysic(atoms.copy(), pots, coulomb=coul, precision=precision)
+    tol = 1e-9 if precision == "fp64" else 1e-4
+    opt = pysic.ChargeRelaxation("optimize", calculator=calc2, parameters=[500, tol])
+    q_opt = opt.charge_relaxation()
+    assert opt.last_converged and opt.last_error <= tol
+    assert opt.last_steps < dyn.last_steps / 3
+    np.testing.assert_allclose(q_opt, q_dyn, atol=1e-8 if precision == "fp64" else 2e-5)
+    assert abs(q_opt.sum()) < 1e-9
+    # the engine keeps the optimised charges
+    np.testing.assert_array_equal(calc2.engine.get_charges(), q_opt)
+
+
+def test_optimize_falls_back_to_slsqp_for_non_quadratic_energies():
+    pytest.importorskip("scipy")
+    atoms, pots, coul = _optimize_case()
+    pots = pots + [pysic.Potential("charge_self", symbols=[["O"]], parameters=[0.05, 4])]
+    calc = pysic.Pysic(atoms.copy(), pots, coulomb=coul, precision="fp64")
+    calc.set_core()
+    assert calc.engine.optimize_charges(0, 100, 1e-6) is None
+    opt = pysic.ChargeRelaxation("optimize", calculator=calc, parameters=[200, 1e-8])
+    q = opt.charge_relaxation()
+    chi = calc.get_electronegativities()
+    assert np.abs(chi - chi.mean()).max() < 1e-3
+    assert abs(q.sum()) < 1e-6
