@@ -164,6 +164,21 @@ int pg_relax_charges_potentiostat(pg_context* ctx, int32_t precision, int32_t n_
                                   double inertia, double potential, double* rates, double* charges,
                                   double* max_dchi);
 
+/* Velocity Verlet molecular dynamics on the device, step for step what ASE's
+ * VelocityVerlet.step does around Pysic.get_forces (p += dt/2 F; r += dt p / m;
+ * F(r); p += dt/2 F, each operation rounded once), without host round trips.
+ * pg_md_set_state uploads masses (N) and momenta (N x 3); pg_md_verlet runs up
+ * to n_steps steps on the context's coordinates and stops early when an atom
+ * has moved more than skin/2 since the neighbour lists were built (*rebuild =
+ * 1; the step is then left after its drift): rebuild the lists
+ * (pg_generate_neighbor_lists reads the device coordinates) and call again,
+ * which completes that step first.  *steps_done counts completed steps.
+ * pg_md_get_state downloads momenta and positions (either may be null). */
+int pg_md_set_state(pg_context* ctx, const double* masses, const double* momenta);
+int pg_md_verlet(pg_context* ctx, int32_t precision, int32_t n_steps, double timestep, double skin,
+                 int32_t* steps_done, int32_t* rebuild);
+int pg_md_get_state(pg_context* ctx, double* momenta, double* positions);
+
 /* ChargeRelaxation 'optimize' (pysic/charges/relaxation.py:483-488; the
  * reference calls SciPy's SLSQP on the energy and electronegativities) for
  * energies quadratic in the charges (Ewald and charge_self with n <= 2): the

@@ -69,6 +69,10 @@ _SIGNATURES = {
     "pg_relax_charges": (ctypes.c_int, [_ctx, ctypes.c_int32, ctypes.c_int32, ctypes.c_double, ctypes.c_double,
                                         ctypes.c_double, ctypes.c_double, _c_double_p, _c_double_p, _c_int_p,
                                         _c_double_p, _c_double_p]),
+    "pg_md_set_state": (ctypes.c_int, [_ctx, _c_double_p, _c_double_p]),
+    "pg_md_verlet": (ctypes.c_int, [_ctx, ctypes.c_int32, ctypes.c_int32, ctypes.c_double, ctypes.c_double,
+                                    _c_int_p, _c_int_p]),
+    "pg_md_get_state": (ctypes.c_int, [_ctx, _c_double_p, _c_double_p]),
     "pg_optimize_charges": (ctypes.c_int, [_ctx, ctypes.c_int32, ctypes.c_int32, ctypes.c_double, _c_double_p,
                                            _c_int_p, _c_double_p]),
     "pg_relax_charges_potentiostat": (ctypes.c_int, [_ctx, ctypes.c_int32, ctypes.c_int32, ctypes.c_double,

@@ -113,6 +113,21 @@ class FastNeighborList:
         d2 = ((np.asarray(atoms.get_positions()) - self.positions) ** 2).sum(axis=1)
         return bool(d2.max() > (0.5 * self.skin) ** 2)
 
+    def rebuild_on_device(self, engine, positions):
+        """Rebuild the engine's lists from its own (device) coordinates, as the
+        device dynamics loop asks; ``positions`` are those coordinates.  The
+        host copy of the lists is refreshed by ``refresh_from(engine)``."""
+        if self.all_pairs:
+            engine.build_all_pairs(self.cutoffs, self.skin)
+        else:
+            engine.build_neighbors(self.cutoffs, self.skin)
+        self.positions = np.array(positions)
+        self.nupdates += 1
+
+    def refresh_from(self, engine):
+        counts, idx, off = engine.neighbor_lists()
+        self._store(counts, idx, off)
+
     def update(self, atoms, engine=None):
         if self.needs_update(atoms):
             self.build(atoms, engine)

@@ -135,7 +135,9 @@ static void update_coordinates(pg_context* ctx, const double* positions) {
     require(*bad == 0, PG_ERR_INVALID, "non-finite atom position");
 }
 
-static void enqueue(pg_context* ctx, int precision, int flags, int G) {
+// skip (may be null): a device flag every kernel reads first; nonzero makes the
+// whole evaluation a no-op (loops replayed from a graph stop this way)
+void enqueue_evaluation(pg_context* ctx, int precision, int flags, int G, const int* skip) {
     const int n = ctx->n;
     const bool wantF = flags & PG_WANT_FORCES, wantC = flags & PG_WANT_ENEGS, wantE = flags & PG_WANT_ENERGY;
     ctx->out_f.resize(3 * (size_t)std::max(n, 1));
@@ -152,23 +154,23 @@ static void enqueue(pg_context* ctx, int precision, int flags, int G) {
     mark(0);
     // the totals are integers that every kernel adds to: clear them first (the
     // mixed path's displacement pass does it on the way)
-    if (precision == PG_PREC_MIXED && (run_pair || run_bond)) launch_disp(ctx, nullptr, acc);
+    if (precision == PG_PREC_MIXED && (run_pair || run_bond)) launch_disp(ctx, skip, acc);
     else PG_CUDA(cudaMemsetAsync(acc, 0, sizeof(FxAcc) * 8, ctx->stream));
     if (run_pair) {
-        launch_pair_kernel_impl(ctx, precision, flags, first_f, first_chi, Gp, acc);
+        launch_pair_kernel_skip(ctx, precision, flags, first_f, first_chi, Gp, acc, skip);
         if (wantF) first_f = false;
         if (wantC) first_chi = false;
     }
     mark(1);
     if (run_bond) {
-        launch_bond_order_impl(ctx, precision, flags, first_f, G, acc, [&] { mark(2); });
+        launch_bond_order_impl(ctx, precision, flags, first_f, G, acc, [&] { mark(2); }, skip);
         if (wantF) first_f = false;
     } else {
         mark(2);
     }
     mark(3);
     if (ctx->ewald) {
-        launch_ewald_kspace(ctx, precision, flags, first_f, first_chi, acc);
+        launch_ewald_kspace_skip(ctx, precision, flags, first_f, first_chi, acc, skip);
         if (wantF) first_f = false;
         if (wantC) first_chi = false;
     }
@@ -190,10 +192,10 @@ static int autotune_lanes(pg_context* ctx, int precision, int flags) {
     float best_ms = 1e30f;
     for (int o = 0; o < 4; ++o) {
         const int G = options[o];
-        enqueue(ctx, precision, flags, G);  // warm-up
+        enqueue_evaluation(ctx, precision, flags, G, nullptr);  // warm-up
         for (int r = 0; r < REPS; ++r) {
             PG_CUDA(cudaEventRecord(ev[r], ctx->stream));
-            enqueue(ctx, precision, flags, G);
+            enqueue_evaluation(ctx, precision, flags, G, nullptr);
         }
         PG_CUDA(cudaEventRecord(ev[REPS], ctx->stream));
         PG_CUDA(cudaEventSynchronize(ev[REPS]));
@@ -230,7 +232,7 @@ void evaluate(pg_context* ctx, int precision, int flags) {
     // events recorded inside a capture cannot be waited on: time with direct launches
     if (!ctx->use_graphs || ctx->timing) {
         ctx->launches = 0;
-        enqueue(ctx, precision, flags, G);
+        enqueue_evaluation(ctx, precision, flags, G, nullptr);
         return;
     }
     // replay a captured sequence if nothing it depends on has changed
@@ -247,13 +249,13 @@ void evaluate(pg_context* ctx, int precision, int flags) {
     }
     // run once directly (sizes every buffer), then capture the same sequence
     ctx->launches = 0;
-    enqueue(ctx, precision, flags, G);
+    enqueue_evaluation(ctx, precision, flags, G, nullptr);
     const int launches = ctx->launches;
     const unsigned long long alloc_before = alloc_epoch();
     cudaGraph_t graph = nullptr;
     PG_CUDA(cudaStreamBeginCapture(ctx->stream, cudaStreamCaptureModeThreadLocal));
     try {
-        enqueue(ctx, precision, flags, G);
+        enqueue_evaluation(ctx, precision, flags, G, nullptr);
     } catch (...) {
         cudaStreamEndCapture(ctx->stream, &graph);
         if (graph) cudaGraphDestroy(graph);
@@ -585,6 +587,37 @@ int pg_optimize_charges(pg_context* ctx, int32_t precision, int32_t max_iteratio
         }
         *iterations = it;
         *error = err;
+    });
+}
+
+int pg_md_set_state(pg_context* ctx, const double* masses, const double* momenta) {
+    return guarded([&] {
+        check_ctx(ctx);
+        use_device(ctx);
+        pg::require(ctx->n == 0 || (masses && momenta), PG_ERR_INVALID, "null arrays");
+        pg::md_set_state(ctx, masses, momenta);
+    });
+}
+
+int pg_md_get_state(pg_context* ctx, double* momenta, double* positions) {
+    return guarded([&] {
+        check_ctx(ctx);
+        use_device(ctx);
+        pg::md_get_state(ctx, momenta, positions);
+    });
+}
+
+int pg_md_verlet(pg_context* ctx, int32_t precision, int32_t n_steps, double timestep, double skin,
+                 int32_t* steps_done, int32_t* rebuild) {
+    return guarded([&] {
+        check_ctx(ctx);
+        use_device(ctx);
+        pg::require(steps_done && rebuild, PG_ERR_INVALID, "null output pointer");
+        pg::require(n_steps >= 0, PG_ERR_INVALID, "negative step count");
+        int s = 0, r = 0;
+        pg::md_run(ctx, precision, n_steps, timestep, skin, &s, &r);
+        *steps_done = s;
+        *rebuild = r;
     });
 }
 

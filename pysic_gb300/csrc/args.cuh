@@ -78,6 +78,7 @@ struct BondArgs {
     double* out_f;
     FxAcc* acc;        // global energy / virial totals (null: not wanted)
     double* zeta_out;
+    const int* skip;   // optional device flag: nonzero = do nothing
 };
 
 struct DispArgs {

@@ -345,6 +345,9 @@ struct pg_context {
     pg::DevBuf<int> rq_flag;
     pg::DevBuf<double> cg_buf;  // charge optimisation: q, r, p, H p, chi(0), partials, scalars
     pg::DevBuf<int> cg_flag;
+    pg::DevBuf<double> md_p, md_m;  // dynamics: momenta (n x 3), masses
+    pg::DevBuf<int> md_flag;
+    bool md_ready = false, md_pending = false;  // state set; a step waits for its forces after a rebuild
 
     int launches = 0;
 
@@ -415,7 +418,7 @@ void launch_pair_kernel_skip(pg_context* ctx, int precision, int flags, bool fir
 
 int bond_blocks(int n, int G);
 void launch_bond_order_impl(pg_context* ctx, int precision, int flags, bool first_f, int G, FxAcc* acc,
-                            const std::function<void()>& between);
+                            const std::function<void()>& between, const int* skip = nullptr);
 void bond_zeta_diag(pg_context* ctx);
 // noalloc.cu: the bond-order passes on static scratch (pg_bond_order_noalloc)
 void bond_order_noalloc(pg_context* ctx, int precision, double* d_forces, double* d_totals);
@@ -454,6 +457,11 @@ cudaStream_t batch_stream(const pg_batch* b);
 // relax.cu: mode PG_RELAX_DYNAMIC (damped, to a tolerance) or
 // PG_RELAX_POTENTIOSTAT (undamped, fixed external potential, fixed step count)
 constexpr int PG_RELAX_DYNAMIC = 0, PG_RELAX_POTENTIOSTAT = 1;
+// md.cu: velocity Verlet on the device (pg_md_*)
+void md_set_state(pg_context* ctx, const double* masses, const double* momenta);
+void md_get_state(pg_context* ctx, double* momenta, double* positions);
+void md_run(pg_context* ctx, int precision, int n_steps, double dt, double skin, int* steps_done, int* rebuild);
+void evaluate(pg_context* ctx, int precision, int flags);
 // optimize.cu: the constrained energy minimum over the charges (quadratic energies)
 void optimize_charges(pg_context* ctx, int precision, int max_iter, double tolerance, double* charges, int* iterations,
                       double* error);

@@ -198,6 +198,7 @@ __device__ __forceinline__ void bond_body(const BondArgs& A, int blk, int nblk) 
     }
     // the displacements (mixed path) and the totals come from the kernel before
     pdl_wait();
+    if (A.skip && *A.skip) return;  // uniform over the block
     // geometry of i's bonds in the working precision, and per bond what every
     // triplet through it reuses
     if (act) {
@@ -493,6 +494,7 @@ __device__ __forceinline__ void gather_body(const BondArgs& A, int blk, int nblk
     // the list bounds are not written by the bond pass: read before the wait
     const int s = act ? A.start[m] : 0, nm = act ? A.start[m + 1] - s : 0;
     pdl_wait();  // the bond pass's records
+    if (A.skip && *A.skip) return;
     if (act) {
         // every neighbour x left the force of its bonds on m in m's entry m->x
         for (int e = lane; e < nm; e += G) {
@@ -655,9 +657,10 @@ static void launch_by_lanes(const BondArgs& A, int n, cudaStream_t st, int G, bo
 
 // `between` runs between the two passes
 void launch_bond_order_impl(pg_context* ctx, int precision, int flags, bool first_f, int G, FxAcc* acc,
-                            const std::function<void()>& between) {
+                            const std::function<void()>& between, const int* skip) {
     prepare_bond_scratch(ctx, precision);
     BondArgs A = make_bond_args(ctx, precision, flags, first_f, acc);
+    A.skip = skip;
     const bool forces = (flags & PG_WANT_FORCES) != 0;
     if (precision == PG_PREC_FP64) launch_by_lanes<double>(A, ctx->n, ctx->stream, G, forces, between);
     else launch_by_lanes<float>(A, ctx->n, ctx->stream, G, forces, between);

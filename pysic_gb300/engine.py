@@ -144,6 +144,26 @@ class Engine:
         return {"charges": q, "rates": rates, "steps": steps.value, "error": err.value, "max_dq": dq.value,
                 "converged": st == L.PG_OK}
 
+    # ---- molecular dynamics (pg_md_*) ------------------------------------------
+    def md_set_state(self, masses, momenta):
+        m = L.as_f64(masses)
+        p = L.as_f64(momenta, (-1, 3))
+        L.check(self.lib.pg_md_set_state(self.ctx, L.dptr(m), L.dptr(p)))
+
+    def md_verlet(self, precision, n_steps, timestep, skin):
+        """Up to n_steps velocity Verlet steps; (steps completed, rebuild needed)."""
+        s = ctypes.c_int32(0)
+        r = ctypes.c_int32(0)
+        L.check(self.lib.pg_md_verlet(self.ctx, precision, int(n_steps), float(timestep), float(skin),
+                                      ctypes.byref(s), ctypes.byref(r)))
+        return s.value, bool(r.value)
+
+    def md_get_state(self):
+        p = np.zeros((self.n, 3))
+        r = np.zeros((self.n, 3))
+        L.check(self.lib.pg_md_get_state(self.ctx, L.dptr(p), L.dptr(r)))
+        return p, r
+
     def optimize_charges(self, precision, max_iterations, tolerance):
         """Constrained energy minimum over the charges on the device
         (pg_optimize_charges).  Returns None when the energy is not quadratic

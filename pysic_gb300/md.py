@@ -1,0 +1,97 @@
+"""Velocity Verlet molecular dynamics with the steps on the device.
+
+The reference runs MD through ASE (doc/run examples.rst): ASE's
+VelocityVerlet.step (ase/md/verlet.py) reads the momenta, asks the Pysic
+calculator for forces and writes the positions back, every step crossing into
+the Fortran core.  ``VelocityVerlet`` here keeps ASE's interface (timestep in
+ASE units, ``run(steps)``, ``attach(function, interval)``, ``nsteps``) and its
+update, operation for operation, but the steps run on the GPU
+(pg_md_verlet): forces, both kicks and the drift stay in device memory, the
+neighbour list is rebuilt when an atom has moved more than skin/2 (the
+FastNeighborList / ASE update policy), and the host is visited only for
+rebuilds and for observers.  ASE itself is not needed.
+"""
+import math
+
+import numpy as np
+
+from .error import MissingAtomsError
+
+
+class VelocityVerlet:
+    def __init__(self, atoms, timestep, precision=None):
+        self.atoms = atoms
+        self.dt = float(timestep)
+        self.precision = precision
+        self.nsteps = 0
+        self.observers = []
+
+    def get_time(self):
+        return self.nsteps * self.dt
+
+    def attach(self, function, interval=1, *args, **kwargs):
+        """Call function(*args, **kwargs) after every `interval` steps (and
+        before the first step), as ASE's Dynamics.attach does."""
+        if not hasattr(function, "__call__"):
+            function = function.write
+        self.observers.append((function, int(interval), args, kwargs))
+
+    def call_observers(self):
+        for function, interval, args, kwargs in self.observers:
+            if interval > 0 and self.nsteps % interval == 0:
+                function(*args, **kwargs)
+
+    def _stride(self):
+        g = 0
+        for _, interval, _, _ in self.observers:
+            if interval > 0:
+                g = math.gcd(g, interval)
+        return g or None
+
+    def _sync_atoms(self, calc, eng):
+        """The device state into the atoms and the calculator's copy of them."""
+        p, r = eng.md_get_state()
+        self.atoms.set_positions(r)
+        self.atoms.set_momenta(p)
+        s = calc.get_atoms()
+        s.set_positions(r)
+        s.set_momenta(p)
+        pushed = getattr(calc, "_pushed", None)
+        if pushed is not None:
+            pushed["positions"] = np.array(r)
+        calc._invalidate()
+        return r
+
+    def run(self, steps=50):
+        calc = self.atoms.get_calculator()
+        if calc is None:
+            raise MissingAtomsError("the atoms have no Pysic calculator")
+        calc.set_atoms(self.atoms)
+        calc.set_core()  # engine, tables and lists up to date for these atoms
+        eng = calc.engine
+        nl = calc.get_neighbor_lists()
+        prec = calc._prec() if self.precision is None else self.precision
+        eng.md_set_state(self.atoms.get_masses(), self.atoms.get_momenta())
+        if self.nsteps == 0:
+            self.call_observers()
+        stride = self._stride()
+        left = int(steps)
+        rebuilt = False
+        while left > 0:
+            k = left if stride is None else min(left, stride - self.nsteps % stride)
+            while k > 0:
+                done, rebuild = eng.md_verlet(prec, k, self.dt, nl.skin)
+                k -= done
+                left -= done
+                self.nsteps += done
+                if rebuild:
+                    _, r = eng.md_get_state()
+                    nl.rebuild_on_device(eng, r)
+                    rebuilt = True
+            if stride is not None:
+                self._sync_atoms(calc, eng)
+                self.call_observers()
+        self._sync_atoms(calc, eng)
+        if rebuilt:
+            nl.refresh_from(eng)
+        return True

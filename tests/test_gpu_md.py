@@ -1,0 +1,100 @@
+"""Velocity Verlet on the device (pg_md_verlet) against ASE's update written
+out on the host around the same force evaluations.
+
+The host loop is VelocityVerlet.step of ase/md/verlet.py in NumPy:
+p += 0.5 dt F; r = r + dt p / m; F = calc.get_forces(); p += 0.5 dt F, with
+the calculator updating its neighbour list by the skin/2 rule.  The device
+loop uses the same force kernels on the same coordinates and the same
+rounding, so the trajectories agree bit for bit, list rebuilds included.
+"""
+import numpy as np
+import pytest
+
+import pysic_gb300 as pysic
+from pysic_gb300 import workloads as W
+
+pytestmark = pytest.mark.gpu
+
+FS = 0.09822694788464063  # one femtosecond in ASE time units
+
+
+def _hot_silicon(seed=3, temperature=3000.0):
+    atoms = W.diamond_si(3, noise=0.05, seed=seed)
+    kT = 8.617333262e-5 * temperature
+    m = atoms.get_masses()[:, None]
+    p = np.random.default_rng(seed).normal(0.0, 1.0, (len(atoms), 3)) * np.sqrt(m * kT)
+    p -= p.mean(axis=0)
+    atoms.set_momenta(p)
+    return atoms
+
+
+def _host_verlet(atoms, calc, dt, steps):
+    atoms.set_calculator(calc)
+    f = atoms.get_forces()
+    m = atoms.get_masses()[:, None]
+    for _ in range(steps):
+        p = atoms.get_momenta()
+        p += 0.5 * dt * f
+        r = atoms.get_positions()
+        atoms.set_positions(r + dt * p / m)
+        atoms.set_momenta(p)
+        f = atoms.get_forces()
+        atoms.set_momenta(atoms.get_momenta() + 0.5 * dt * f)
+    return atoms.get_positions(), atoms.get_momenta()
+
+
+@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+def test_device_verlet_matches_the_host_loop_with_rebuilds(precision):
+    dt, steps = 2.0 * FS, 40
+    a_host = _hot_silicon()
+    calc_h = pysic.Pysic(a_host, W.tersoff_si_potentials(), precision=precision)
+    r_h, p_h = _host_verlet(a_host, calc_h, dt, steps)
+    rebuilds_host = calc_h.get_neighbor_lists().nupdates
+
+    a_dev = _hot_silicon()
+    calc_d = pysic.Pysic(a_dev, W.tersoff_si_potentials(), precision=precision)
+    a_dev.set_calculator(calc_d)
+    dyn = pysic.VelocityVerlet(a_dev, dt)
+    dyn.run(steps)
+    assert dyn.nsteps == steps
+    assert calc_d.get_neighbor_lists().nupdates == rebuilds_host > 1
+    np.testing.assert_array_equal(a_dev.get_positions(), r_h)
+    np.testing.assert_array_equal(a_dev.get_momenta(), p_h)
+    # the calculator answers for the final positions without a stale result
+    np.testing.assert_array_equal(a_dev.get_forces(), calc_h.get_forces(a_host))
+
+
+def test_observers_cut_the_run_without_changing_it():
+    dt = 2.0 * FS
+    a1 = _hot_silicon(seed=5)
+    a1.set_calculator(pysic.Pysic(a1, W.tersoff_si_potentials()))
+    pysic.VelocityVerlet(a1, dt).run(30)
+
+    a2 = _hot_silicon(seed=5)
+    a2.set_calculator(pysic.Pysic(a2, W.tersoff_si_potentials()))
+    dyn = pysic.VelocityVerlet(a2, dt)
+    seen = []
+    dyn.attach(lambda: seen.append((dyn.nsteps, a2.get_positions().copy())), interval=7)
+    dyn.run(30)
+    assert [s for s, _ in seen] == [0, 7, 14, 21, 28]
+    np.testing.assert_array_equal(a2.get_positions(), a1.get_positions())
+    np.testing.assert_array_equal(a2.get_momenta(), a1.get_momenta())
+
+
+def test_energy_is_conserved():
+    """NVE: total energy drifts by far less than its thermal fluctuation."""
+    atoms = _hot_silicon(seed=7, temperature=600.0)
+    calc = pysic.Pysic(atoms, W.tersoff_si_potentials())
+    atoms.set_calculator(calc)
+    dyn = pysic.VelocityVerlet(atoms, 1.0 * FS)
+    m = atoms.get_masses()[:, None]
+
+    def total():
+        return atoms.get_potential_energy() + 0.5 * float((atoms.get_momenta() ** 2 / m).sum())
+
+    e0 = total()
+    energies = []
+    dyn.attach(lambda: energies.append(total()), interval=50)
+    dyn.run(400)
+    kinetic = 0.5 * float((atoms.get_momenta() ** 2 / m).sum())
+    assert max(abs(e - e0) for e in energies) < 2e-3 * kinetic
