@@ -292,6 +292,53 @@ def run_reference(args):
 RELAX_REPEATS = 3
 
 
+def md_throughput(name, precision, device, steps):
+    """Velocity Verlet of the benchmark structure at 1000 K (dt 1 fs): the
+    device loop (pysic_gb300.VelocityVerlet, neighbour rebuilds included)
+    against ASE's update driven from the host around Pysic.get_forces, the way
+    the reference runs MD.  Wall-clock atom-steps/s of each."""
+    import pysic_gb300 as pysic
+
+    fs = 0.09822694788464063
+    atoms, pots, coul, _ = workload(name)
+    kT = 8.617333262e-5 * 1000.0
+    m = atoms.get_masses()[:, None]
+    p0 = np.random.default_rng(1).normal(0.0, 1.0, (len(atoms), 3)) * np.sqrt(m * kT)
+    p0 -= p0.mean(axis=0)
+
+    def fresh():
+        a = atoms.copy()
+        a.set_momenta(p0)
+        a.set_calculator(pysic.Pysic(a, pots, coulomb=coul, precision=precision))
+        return a
+
+    a = fresh()
+    dyn = pysic.VelocityVerlet(a, fs)
+    dyn.run(5)  # warm-up: lists, tables, graphs
+    t0 = time.perf_counter()
+    dyn.run(steps)
+    t_dev = time.perf_counter() - t0
+    rebuilds = a.get_calculator().get_neighbor_lists().nupdates
+    b = fresh()
+    f = b.get_forces()
+    host_steps = max(5, steps // 10)
+    t0 = time.perf_counter()
+    for _ in range(host_steps):
+        p = b.get_momenta()
+        p += 0.5 * fs * f
+        b.set_positions(b.get_positions() + fs * p / m)
+        b.set_momenta(p)
+        f = b.get_forces()
+        b.set_momenta(b.get_momenta() + 0.5 * fs * f)
+    t_host = time.perf_counter() - t0
+    n = len(atoms)
+    return {"steps": steps, "temperature_K": 1000.0, "timestep_fs": 1.0, "precision": precision,
+            "device_atom_steps_per_s": n * steps / t_dev, "device_us_per_step": 1e6 * t_dev / steps,
+            "list_builds": rebuilds,
+            "host_driven_atom_steps_per_s": n * host_steps / t_host, "host_driven_us_per_step": 1e6 * t_host / host_steps,
+            "note": "wall clock; the host-driven loop is ASE's VelocityVerlet update around Pysic.get_forces"}
+
+
 def charge_relax_gain(n_configs, device):
     """The metric's second part: plain 'dynamic' charge relaxation of SiO2
     boxes (1000 Si + 2000 O, seeds 0.. held out from training) from zero
@@ -439,6 +486,8 @@ def run_ours(args):
     e2e_dt, h2d, d2h = e2e_time(torch, engine, atoms, prec, flags, args.steps, args.warmup)
     if world == 1 and args.workload.startswith("tersoff_si_32768") and args.relax_configs > 0:
         extra["charge_relax"] = charge_relax_gain(args.relax_configs, local)
+    if world == 1 and args.workload.startswith("tersoff_si") and args.md_steps > 0:
+        extra["md"] = md_throughput(args.workload, args.precision, local, args.md_steps)
     e2e = {"value": n * args.steps / e2e_dt, "unit": "atom-steps/s", "h2d_bytes_per_step": h2d,
            "d2h_bytes_per_step": d2h, "ms_per_step": 1e3 * e2e_dt / args.steps}
 
@@ -593,6 +642,8 @@ def main():
     p.add_argument("--cpu-seconds", type=float, default=12.0)
     p.add_argument("--no-cpu-baseline", action="store_true")
     p.add_argument("--relax-configs", type=int, default=3, help="SiO2 boxes for the charge-relax gain (0: skip)")
+    p.add_argument("--md-steps", type=int, default=300, help="device velocity Verlet steps reported beside the metric "
+                                                              "(0: skip)")
     args = p.parse_args()
     args.warmup = max(3, args.warmup)
     if args.profile:

@@ -219,8 +219,11 @@ __device__ __forceinline__ bool stencil(const int ci[3], int s, const int sp[3],
 __device__ __forceinline__ double sep_d2(const CellK& C, const double* ra, const double* rb, const int o[3]) {
     double s[3];
     for (int c = 0; c < 3; ++c) s[c] = __dsub_rn(rb[c], ra[c]);
+    // a zero offset adds +-0 to each component, which leaves the squared
+    // distance exactly as it is: skipped
     for (int i = 0; i < 3; ++i)
-        for (int c = 0; c < 3; ++c) s[c] = __dadd_rn(s[c], __dmul_rn((double)o[i], C.vc[c][i]));
+        if (o[i] != 0)
+            for (int c = 0; c < 3; ++c) s[c] = __dadd_rn(s[c], __dmul_rn((double)o[i], C.vc[c][i]));
     return __dadd_rn(__dadd_rn(__dmul_rn(s[0], s[0]), __dmul_rn(s[1], s[1])), __dmul_rn(s[2], s[2]));
 }
 
@@ -254,11 +257,17 @@ struct ScanArgs {
     int* off;
 };
 
+constexpr int SCAN_THREADS = 256;
+
 template <bool FILL>
-__global__ void nb_scan(ScanArgs A) {
-    const int lane = threadIdx.x & 31;
+__global__ void __launch_bounds__(SCAN_THREADS) nb_scan(ScanArgs A) {
+    // per warp: the atom's 27 stencil subcells (first sorted slot, candidate
+    // prefix, image offset), so that the candidates of all 27 are walked as
+    // one stream with every lane busy -- the FP64 distance test dominates
+    __shared__ int s_beg[SCAN_THREADS / 32][27], s_pre[SCAN_THREADS / 32][28], s_off[SCAN_THREADS / 32][27][3];
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
     const int a = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-    if (a >= A.n) return;
+    if (a >= A.n) return;  // whole warps
     const double ra[3] = {A.pos[3 * a], A.pos[3 * a + 1], A.pos[3 * a + 2]};
     const double cut2 = __dmul_rn(A.cut[a], A.cut[a]);
     const int ci[3] = {A.cell_of[3 * a], A.cell_of[3 * a + 1], A.cell_of[3 * a + 2]};
@@ -271,61 +280,86 @@ __global__ void nb_scan(ScanArgs A) {
         base1 = A.start[a] + A.g0count[a];
         base0 = A.g0start[a];
     }
-    for (int s = 0; s < 27; ++s) {
+    int len = 0;
+    if (lane < 27) {
         int nb[3], noff[3];
-        if (!stencil(ci, s, A.S.sp, A.C.pbc, nb, noff)) continue;
-        const int c = (nb[2] * A.S.ny + nb[1]) * A.S.nx + nb[0];
-        const int beg = A.cstart[c], end = A.cstart[c + 1];
-        const bool self_pos = lex_positive(noff);
-        for (int t0 = beg; t0 < end; t0 += 32) {
-            const int t = t0 + lane;
-            int b = -1, mult = 0, grp = -1;
-            int o[3] = {0, 0, 0};
-            if (t < end) {
-                b = A.sorted[t];
-                if (b > a) {
-                    grp = 1;
-                    mult = 1;
-                } else if (b == a) {
-                    if (self_pos) {
-                        grp = 1;
-                        mult = 2;
-                    }
-                } else if (visible) {
-                    grp = 0;
-                    mult = 1;
-                }
-                if (mult) {
-                    for (int q = 0; q < 3; ++q) o[q] = noff[q] - wa[q] + A.wrap[3 * b + q];
-                    const double rb[3] = {A.pos[3 * b], A.pos[3 * b + 1], A.pos[3 * b + 2]};
-                    if (!(sep_d2(A.C, ra, rb, o) < cut2)) mult = 0;
-                }
-            }
-            const unsigned m0 = __ballot_sync(0xffffffffu, mult && grp == 0);
-            const unsigned m1 = __ballot_sync(0xffffffffu, mult && grp == 1);
-            const unsigned m2 = __ballot_sync(0xffffffffu, mult == 2);
-            if (FILL && mult) {
-                if (grp == 0) {
-                    int p = base0 + n0 + __popc(m0 & lt);
-                    A.g0key[p] = ((long long)b << 5) | (long long)(26 - s);
-                    A.g0val[p] = make_int4(b, o[0], o[1], o[2]);
-                } else {
-                    int p = base1 + n1 + __popc(m1 & lt) + __popc(m2 & lt);
-                    A.idx[p] = b;
-                    A.off[3 * p] = o[0];
-                    A.off[3 * p + 1] = o[1];
-                    A.off[3 * p + 2] = o[2];
-                    if (mult == 2) {
-                        A.idx[p + 1] = b;
-                        A.off[3 * p + 3] = -o[0];
-                        A.off[3 * p + 4] = -o[1];
-                        A.off[3 * p + 5] = -o[2];
-                    }
-                }
-            }
-            n0 += __popc(m0);
-            n1 += __popc(m1) + __popc(m2);
+        int beg = 0;
+        if (stencil(ci, lane, A.S.sp, A.C.pbc, nb, noff)) {
+            const int c = (nb[2] * A.S.ny + nb[1]) * A.S.nx + nb[0];
+            beg = A.cstart[c];
+            len = A.cstart[c + 1] - beg;
         }
+        s_beg[w][lane] = beg;
+        for (int q = 0; q < 3; ++q) s_off[w][lane][q] = noff[q];
+    }
+    int incl = len;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        const int v = __shfl_up_sync(0xffffffffu, incl, o);
+        if (lane >= o) incl += v;
+    }
+    if (lane == 0) s_pre[w][0] = 0;
+    if (lane < 27) s_pre[w][lane + 1] = incl;
+    const int total = __shfl_sync(0xffffffffu, incl, 26);
+    __syncwarp();
+    // candidates in stencil order, then sorted order within a subcell: the
+    // order of the reference's loops (Core.f90:8190-8202)
+    for (int u0 = 0; u0 < total; u0 += 32) {
+        const int u = u0 + lane;
+        int b = -1, mult = 0, grp = -1, s = 0;
+        int o[3] = {0, 0, 0};
+        if (u < total) {
+            int lo = 0, hi = 26;  // the last subcell whose prefix is <= u
+            while (lo < hi) {
+                const int mid = (lo + hi + 1) >> 1;
+                if (s_pre[w][mid] <= u) lo = mid;
+                else hi = mid - 1;
+            }
+            s = lo;
+            const int noff[3] = {s_off[w][s][0], s_off[w][s][1], s_off[w][s][2]};
+            b = A.sorted[s_beg[w][s] + (u - s_pre[w][s])];
+            if (b > a) {
+                grp = 1;
+                mult = 1;
+            } else if (b == a) {
+                if (lex_positive(noff)) {
+                    grp = 1;
+                    mult = 2;
+                }
+            } else if (visible) {
+                grp = 0;
+                mult = 1;
+            }
+            if (mult) {
+                for (int q = 0; q < 3; ++q) o[q] = noff[q] - wa[q] + A.wrap[3 * b + q];
+                const double rb[3] = {A.pos[3 * b], A.pos[3 * b + 1], A.pos[3 * b + 2]};
+                if (!(sep_d2(A.C, ra, rb, o) < cut2)) mult = 0;
+            }
+        }
+        const unsigned m0 = __ballot_sync(0xffffffffu, mult && grp == 0);
+        const unsigned m1 = __ballot_sync(0xffffffffu, mult && grp == 1);
+        const unsigned m2 = __ballot_sync(0xffffffffu, mult == 2);
+        if (FILL && mult) {
+            if (grp == 0) {
+                int p = base0 + n0 + __popc(m0 & lt);
+                A.g0key[p] = ((long long)b << 5) | (long long)(26 - s);
+                A.g0val[p] = make_int4(b, o[0], o[1], o[2]);
+            } else {
+                int p = base1 + n1 + __popc(m1 & lt) + __popc(m2 & lt);
+                A.idx[p] = b;
+                A.off[3 * p] = o[0];
+                A.off[3 * p + 1] = o[1];
+                A.off[3 * p + 2] = o[2];
+                if (mult == 2) {
+                    A.idx[p + 1] = b;
+                    A.off[3 * p + 3] = -o[0];
+                    A.off[3 * p + 4] = -o[1];
+                    A.off[3 * p + 5] = -o[2];
+                }
+            }
+        }
+        n0 += __popc(m0);
+        n1 += __popc(m1) + __popc(m2);
     }
     // lower-index atoms in out-of-range subcells of a periodic axis: their
     // sweep can reach a, but a's stencil never reaches them
@@ -667,7 +701,7 @@ void build_neighbor_lists(pg_context* ctx, const double* h_cutoffs) {
     A.g0count = ctx->nb_g0.p;
     A.g1count = ctx->vals_a.p;
     if (n > 0) {
-        nb_scan<false><<<blocks((long long)n * 32, 256), 256, 0, st>>>(A);
+        nb_scan<false><<<blocks((long long)n * 32, SCAN_THREADS), SCAN_THREADS, 0, st>>>(A);
         PG_CHECK_LAUNCH();
     }
     // CSR starts and lower-index key buffer starts
@@ -693,7 +727,7 @@ void build_neighbor_lists(pg_context* ctx, const double* h_cutoffs) {
     A.idx = ctx->nb_idx.p;
     A.off = ctx->nb_off.p;
     if (n > 0) {
-        nb_scan<true><<<blocks((long long)n * 32, 256), 256, 0, st>>>(A);
+        nb_scan<true><<<blocks((long long)n * 32, SCAN_THREADS), SCAN_THREADS, 0, st>>>(A);
         PG_CHECK_LAUNCH();
         nb_sort_g0<<<blocks((long long)n * 32, 256), 256, 0, st>>>(n, ctx->nb_g0.p, ctx->g0_start.p, ctx->nb_start.p,
                                                                   ctx->g0_keys.p, ctx->g0_vals.p, ctx->nb_idx.p,
