@@ -83,11 +83,16 @@ int pg_get_atom_charges(pg_context* ctx, double* charges);
  * PyInterface.f90:370-380, 433-480.  kind: 0 LJ (epsilon, sigma), 1 exponential
  * (epsilon, zeta), 2 Buckingham (A, C, sigma), 3 spring (k, R_0; shifted by its
  * value at the cutoff), 4 power (epsilon, a, n), 5 shift_power (epsilon, r1, r2,
- * n); params: 4 per record (unused tail zero); soft: cutoff - cutoff_margin;
- * group: bond-order group (-1 none). */
+ * n), 6 tabulated (first row, row count, range, scale; rows set with
+ * pg_set_pair_tables); params: 4 per record (unused tail zero); soft: cutoff -
+ * cutoff_margin; group: bond-order group (-1 none). */
 int pg_set_pair_potentials(pg_context* ctx, int32_t n_types, int32_t n_records, const int32_t* kind,
                            const double* params, const double* cutoff, const double* soft,
                            const uint64_t* mask1, const uint64_t* mask2, const int32_t* group);
+/* The tables of every tabulated pair record, concatenated: n_rows rows of (V,
+ * d) as read_table (Utility.f90:384-433) reads table_XXXX.txt; evaluated as
+ * evaluate_energy_table / _force_table (Potentials.f90:4227-4298). */
+int pg_set_pair_tables(pg_context* ctx, int64_t n_rows, const double* rows);
 /* add_potential(...) for single-atom records, params 4 per record: kind 0
  * charge_self (epsilon, n), 1 constant (V), 2 force (Fx, Fy, Fz; energy -F . r
  * at the absolute position).  Single-atom terms add nothing to the virial. */

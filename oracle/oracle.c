@@ -292,7 +292,7 @@ static double smooth_deriv(double r, double hard, double soft) {
 /* evaluate_energy_LJ (2990-3005), _exp (3665-3680), _buckingham (4030-4045),
  * _spring (3069-3085), _power (4141-4152), _shift (4827-4842); cut is the
  * potential's hard cutoff (the spring is shifted by its value there) */
-static double pair_energy(int kind, const double* p, double cut, double r1) {
+static double pair_energy(int kind, const double* p, double cut, double r1, const double* table) {
     if (kind == 0) {
         double ratio = p[1] / r1;
         double r6 = ratio * ratio * ratio * ratio * ratio * ratio;
@@ -309,14 +309,25 @@ static double pair_energy(int kind, const double* p, double cut, double r1) {
     } else if (kind == 4) {
         double ratio = p[1] / r1;
         return p[0] * pow(ratio, p[2]);
-    } else {
+    } else if (kind == 5) {
         return p[0] * pow((p[1] - r1) / (p[1] - p[2]), p[3]);
+    } else { /* evaluate_energy_table (4267-4298): rows (V, d) from p[0], p[1] rows, range p[2], scale p[3] */
+        const double* T = table + 2 * (int64_t)p[0];
+        const int n_values = (int)p[1];
+        const double max_r = p[2];
+        const double dr = max_r / (n_values - 1);
+        if (r1 >= max_r) return T[2 * (n_values - 1)];
+        const int l = (int)floor(r1 / dr); /* lower_index - 1 */
+        const double t = r1 / dr - l, t2 = t * t, t3 = t2 * t;
+        return p[3] * (T[2 * l] * (2 * t3 - 3 * t2 + 1) + T[2 * l + 1] * dr / max_r * (t3 - 2 * t2 + t) +
+                       T[2 * l + 2] * (3 * t2 - 2 * t3) + T[2 * l + 3] * dr / max_r * (t3 - t2));
     }
 }
 
 /* evaluate_force_LJ (2971-2983), _exp (3643-3655), _buckingham (4009-4022),
  * _spring (3042-3060), _power (4119-4132), _shift (4803-4818): force on atom 1 */
-static void pair_force(int kind, const double* p, double cut, const double sep[3], double r1, double f[3]) {
+static void pair_force(int kind, const double* p, double cut, const double sep[3], double r1, double f[3],
+                       const double* table) {
     if (kind == 0) {
         double ratio = p[1] / r1;
         double r6 = ratio * ratio * ratio * ratio * ratio * ratio;
@@ -336,9 +347,21 @@ static void pair_force(int kind, const double* p, double cut, const double sep[3
     } else if (kind == 4) {
         double n = p[2], ratio = p[1] / r1;
         for (int c = 0; c < 3; ++c) f[c] = p[0] * (-n * pow(ratio, n)) * sep[c] / (r1 * r1);
-    } else {
+    } else if (kind == 5) {
         double a = p[1], b = p[2], n = p[3];
         for (int c = 0; c < 3; ++c) f[c] = -p[0] * n / (a - b) * pow((a - r1) / (a - b), n - 1.0) * sep[c] / r1;
+    } else { /* evaluate_force_table (4227-4258) */
+        const double* T = table + 2 * (int64_t)p[0];
+        const int n_values = (int)p[1];
+        const double max_r = p[2];
+        const double dr = max_r / (n_values - 1);
+        for (int c = 0; c < 3; ++c) f[c] = 0.0;
+        if (r1 >= max_r) return;
+        const int l = (int)floor(r1 / dr);
+        const double t = r1 / dr - l, t2 = t * t;
+        const double pre = p[3] * (T[2 * l] / dr * 6 * (t2 - t) + T[2 * l + 1] / max_r * (3 * t2 - 4 * t + 1) +
+                                   T[2 * l + 2] / dr * 6 * (t - t2) + T[2 * l + 3] / max_r * (3 * t2 - 2 * t));
+        for (int c = 0; c < 3; ++c) f[c] = pre / r1 * sep[c];
     }
 }
 
@@ -655,11 +678,11 @@ static void* loop_range(void* arg) {
                         B2 = post_process(X, tj, grp, sums[1]);
                     }
                     double cut = sm ? smooth_factor(d, rc, rs) : 1.0;
-                    double v = pair_energy(kind, p, rc, d);
+                    double v = pair_energy(kind, p, rc, d, m->pair_table);
                     if (grp >= 0) J->energy += v * cut * (0.0 + 0.0 + B1 + B2) * 0.5;
                     else J->energy += v * cut;
                 } else {
-                    double v = (grp >= 0 || sm) ? pair_energy(kind, p, rc, d) : 0.0;
+                    double v = (grp >= 0 || sm) ? pair_energy(kind, p, rc, d, m->pair_table) : 0.0;
                     double cut = 1.0, cg[3] = {0, 0, 0};
                     if (sm) {
                         cut = smooth_factor(d, rc, rs);
@@ -675,7 +698,7 @@ static void* loop_range(void* arg) {
                         pair_bo_forces(X, i, j, 0.5 * v * cut, sep, d, grp, sums, F, st);
                     }
                     double f1[3], p1[3], p2[3];
-                    pair_force(kind, p, rc, sep, d, f1);
+                    pair_force(kind, p, rc, sep, d, f1, m->pair_table);
                     for (int c = 0; c < 3; ++c) {
                         if (grp >= 0) {
                             double bsum = (0.0 + 0.0 + B1 + B2) * 0.5;

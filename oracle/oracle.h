@@ -41,7 +41,8 @@ typedef struct {
 typedef struct {
     int32_t n_types;
     int32_t n_pair;
-    const int32_t* pair_kind;     /* 0 LJ, 1 exponential, 2 Buckingham, 3 spring, 4 power, 5 shift_power */
+    const int32_t* pair_kind;     /* 0 LJ, 1 exponential, 2 Buckingham, 3 spring, 4 power, 5 shift_power,
+                                     6 tabulated (params: first row, rows, range, scale) */
     const double* pair_params;    /* 4 per record */
     const double* pair_cutoff;
     const double* pair_soft;      /* cutoff - cutoff_margin, as passed to add_potential */
@@ -64,6 +65,8 @@ typedef struct {
     double ewald_rc, ewald_kc, ewald_sigma, ewald_eps;
     int32_t ewald_kmax[3];
     const double* ewald_scaler;   /* n */
+    const double* pair_table;     /* tabulated potentials: rows (V, d), concatenated */
+    int64_t n_table_rows;
 } orc_model;
 
 /* CSR neighbour list: entries of atom i are [start[i], start[i+1]). */

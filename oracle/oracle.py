@@ -35,7 +35,8 @@ class _Model(ctypes.Structure):
                 ("bond_soft", _dp), ("bond_mask1", _up), ("bond_mask2", _up), ("bond_mask3", _up),
                 ("bond_group", _ip), ("ewald", ctypes.c_int32), ("ewald_rc", ctypes.c_double),
                 ("ewald_kc", ctypes.c_double), ("ewald_sigma", ctypes.c_double), ("ewald_eps", ctypes.c_double),
-                ("ewald_kmax", ctypes.c_int32 * 3), ("ewald_scaler", _dp)]
+                ("ewald_kmax", ctypes.c_int32 * 3), ("ewald_scaler", _dp), ("pair_table", _dp),
+                ("n_table_rows", ctypes.c_int64)]
 
 
 class _NbList(ctypes.Structure):
@@ -132,6 +133,8 @@ def _model(keep, M, n):
     m.pair_mask1 = _u(keep.u64(a["pair_mask1"]))
     m.pair_mask2 = _u(keep.u64(a["pair_mask2"]))
     m.pair_group = _i(keep.i32(a["pair_group"]))
+    m.pair_table = _d(keep.f64(a["pair_table"]))
+    m.n_table_rows = len(a["pair_table"]) // 2
     m.n_single = len(a["single_kind"])
     m.single_kind = _i(keep.i32(a["single_kind"]))
     m.single_params = _d(keep.f64(a["single_params"]))

@@ -401,7 +401,7 @@ int pg_set_pair_potentials(pg_context* ctx, int32_t n_types, int32_t n, const in
         pg::require(n_types >= 0 && n_types <= 64, PG_ERR_INVALID, "n_types must be within 0..64");
         pg::require(n >= 0, PG_ERR_INVALID, "negative record count");
         for (int r = 0; r < n; ++r)
-            pg::require(kind[r] >= 0 && kind[r] <= 5, PG_ERR_UNSUPPORTED, "unknown pair potential kind");
+            pg::require(kind[r] >= 0 && kind[r] <= 6, PG_ERR_UNSUPPORTED, "unknown pair potential kind");
         ctx->n_types = n_types;
         ctx->pr_kind.assign(kind, kind + n);
         ctx->pr_params.assign(params, params + 4 * (size_t)n);
@@ -410,6 +410,15 @@ int pg_set_pair_potentials(pg_context* ctx, int32_t n_types, int32_t n, const in
         ctx->pr_m1.assign(mask1, mask1 + n);
         ctx->pr_m2.assign(mask2, mask2 + n);
         ctx->pr_group.assign(group, group + n);
+        ctx->tables_dirty = true;
+    });
+}
+
+int pg_set_pair_tables(pg_context* ctx, int64_t n_rows, const double* rows) {
+    return guarded([&] {
+        check_ctx(ctx);
+        pg::require(n_rows >= 0 && (n_rows == 0 || rows != nullptr), PG_ERR_INVALID, "invalid table rows");
+        ctx->pr_table.assign(rows, rows + 2 * n_rows);
         ctx->tables_dirty = true;
     });
 }

@@ -17,6 +17,7 @@ struct PairArgs {
     const int* off;
     const void* terms;  // PairT<R>
     const int2* index;
+    const void* tab;    // tabulated potentials' rows (R)
     const SingleTerm* sterms;
     const int2* sindex;
     int ewald;
@@ -53,6 +54,7 @@ struct BondArgs {
     const int* rev;
     const void* terms;  // PairT<R>
     const int2* index;
+    const void* tab;    // tabulated potentials' rows (R)
     const void* trip;   // TripT<R>
     const void* post;   // PostT<R>
     const void* maxbr;  // R

@@ -50,8 +50,9 @@ __device__ __forceinline__ void smooth(R r, R rc, R rs, R& f, R& fp) {
 
 // V(r) and the radial derivative dV/dr of LJ (Potentials.f90:2971-3005),
 // exponential (3643-3680) and Buckingham (4009-4045); no factor 4 in LJ.
+// tab: the rows (V, d) of every tabulated potential, 2 values per row
 template <typename R>
-__device__ __forceinline__ void pair_eval(const PairT<R>& P, R r, R& V, R& dV) {
+__device__ __forceinline__ void pair_eval(const PairT<R>& P, R r, R& V, R& dV, const R* tab) {
     const R p0 = P.p0, p1 = P.p1, p2 = P.p2;
     switch (P.kind) {
         case 0: {  // LJ: eps ((s/r)^12 - (s/r)^6), no factor 4 (evaluate_energy_LJ, Potentials.f90:2993-3005)
@@ -94,11 +95,31 @@ __device__ __forceinline__ void pair_eval(const PairT<R>& P, R r, R& V, R& dV) {
             dV = -p2 * t / r;
             break;
         }
-        default: {  // shift_power: eps ((r1 - r)/(r1 - r2))^n (4803-4842)
+        case 5: {  // shift_power: eps ((r1 - r)/(r1 - r2))^n (4803-4842)
             const R w = p1 - p2;
             const R x = (p1 - r) / w;
             V = p0 * pow_(x, P.p3);
             dV = -p0 * P.p3 / w * pow_(x, P.p3 - R(1));
+            break;
+        }
+        default: {  // tabulated: cubic Hermite on rows (V, d), range p0, scale p1 (4227-4298);
+                    // beyond the range the last V, unscaled, as the reference returns it
+            const R* T = tab + 2 * (long long)P.t0;
+            const int nv = P.tn;
+            if (r >= p0) {
+                V = T[2 * (nv - 1)];
+                dV = R(0);
+            } else {
+                const R dr = p0 / (R)(nv - 1);
+                const R x = r / dr;
+                const int l = min(max((int)x, 0), nv - 2);
+                const R t = x - (R)l, t2 = t * t, t3 = t2 * t;
+                const R* a = T + 2 * l;
+                V = p1 * (a[0] * (R(2) * t3 - R(3) * t2 + R(1)) + a[1] * dr / p0 * (t3 - R(2) * t2 + t) +
+                          a[2] * (R(3) * t2 - R(2) * t3) + a[3] * dr / p0 * (t3 - t2));
+                dV = p1 * (a[0] / dr * R(6) * (t2 - t) + a[1] / p0 * (R(3) * t2 - R(4) * t + R(1)) +
+                           a[2] / dr * R(6) * (t - t2) + a[3] / p0 * (R(3) * t2 - R(2) * t));
+            }
             break;
         }
     }
@@ -106,8 +127,8 @@ __device__ __forceinline__ void pair_eval(const PairT<R>& P, R r, R& V, R& dV) {
 
 // V f and d(V f)/dr of one pair term, smoothing included
 template <typename R>
-__device__ __forceinline__ void pair_term(const PairT<R>& P, R r, R& V, R& dV) {
-    pair_eval<R>(P, r, V, dV);
+__device__ __forceinline__ void pair_term(const PairT<R>& P, R r, R& V, R& dV, const R* tab) {
+    pair_eval<R>(P, r, V, dV, tab);
     if (P.smooth) {
         R f, fp;
         smooth<R>(r, P.rc, P.rs, f, fp);

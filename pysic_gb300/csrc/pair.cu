@@ -112,7 +112,7 @@ __device__ __forceinline__ void pair_body(const PairArgs& A, int blk) {
                 const PairT<R> P = ((const PairT<R>*)A.terms)[t];
                 if (P.in_bond_kernel || !(r < P.rc)) continue;
                 R V, dV;
-                pair_term<R>(P, r, V, dV);
+                pair_term<R>(P, r, V, dV, (const R*)A.tab);
                 U += V;
                 dU += dV;
             }
@@ -235,6 +235,7 @@ PairArgs make_pair_args(pg_context* ctx, int precision, int flags, bool first_f,
     A.idx = ctx->nb_idx.p;
     A.off = ctx->nb_off.p;
     A.terms = precision == PG_PREC_FP64 ? (const void*)ctx->d_pair_terms.p : (const void*)ctx->d_pair_terms32.p;
+    A.tab = precision == PG_PREC_FP64 ? (const void*)ctx->d_tab64.p : (const void*)ctx->d_tab32.p;
     A.index = ctx->d_pair_index.p;
     A.sterms = ctx->d_single_terms.p;
     A.sindex = ctx->d_single_index.p;

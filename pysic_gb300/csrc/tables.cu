@@ -114,6 +114,16 @@ void fold_tables(pg_context* ctx) {
                 t.p1 = ctx->pr_params[4 * (size_t)r + 1];
                 t.p2 = ctx->pr_params[4 * (size_t)r + 2];
                 t.p3 = ctx->pr_params[4 * (size_t)r + 3];
+                if (t.kind == 6) {  // tabulated: params first row, rows, range, scale
+                    t.t0 = (int)t.p0;
+                    t.tn = (int)t.p1;
+                    // the kernels index rows t0 .. t0 + tn - 1 only: checked here
+                    require(t.t0 >= 0 && t.tn >= 2 && (size_t)t.t0 + (size_t)t.tn <= ctx->pr_table.size() / 2 &&
+                                t.p2 > 0.0,
+                            PG_ERR_INVALID, "tabulated potential: table rows or range out of bounds");
+                    t.p0 = t.p2;  // range
+                    t.p1 = t.p3;  // scale
+                }
                 t.rc = ctx->pr_cut[r];
                 const double soft = ctx->pr_soft[r];
                 if (soft > 0.0 && soft < t.rc) {
@@ -211,6 +221,13 @@ void fold_tables(pg_context* ctx) {
     ctx->d_maxbr32.upload(maxbr32.data(), maxbr32.size(), st);
     ctx->d_single_terms.upload(sterms.data(), sterms.size(), st);
     ctx->d_single_index.upload(sindex.data(), sindex.size(), st);
+    {
+        std::vector<double> t64 = ctx->pr_table;
+        if (t64.empty()) t64.assign(2, 0.0);
+        std::vector<float> t32(t64.begin(), t64.end());
+        ctx->d_tab64.upload(t64.data(), t64.size(), st);
+        ctx->d_tab32.upload(t32.data(), t32.size(), st);
+    }
     PG_CUDA(cudaStreamSynchronize(st));
     ctx->tables_dirty = false;
     ctx->state_epoch++;

@@ -356,12 +356,12 @@ __device__ __forceinline__ void bond_body(const BondArgs& A, int blk, int nblk) 
                 if (!PT.in_bond_kernel || !(r < PT.rc)) continue;
                 R V, dV;
                 if (PT.smooth && PT.rc == bc.x && PT.rs == bc.y) {
-                    pair_eval<R>(PT, r, V, dV);
+                    pair_eval<R>(PT, r, V, dV, (const R*)A.tab);
                     const V2 fc = cut[e];
                     dV = dV * fc.x + V * fc.y;
                     V = V * fc.x;
                 } else {
-                    pair_term<R>(PT, r, V, dV);
+                    pair_term<R>(PT, r, V, dV, (const R*)A.tab);
                 }
                 if (PT.group < 0) {
                     U += V;
@@ -606,6 +606,7 @@ BondArgs make_bond_args(pg_context* ctx, int precision, int flags, bool first_f,
     const size_t ne = (size_t)std::max<long long>(ctx->sh_total, 1);
     if (precision == PG_PREC_FP64) {
         A.terms = ctx->d_pair_terms.p;
+        A.tab = ctx->d_tab64.p;
         A.trip = ctx->d_trip.p;
         A.post = ctx->d_post.p;
         A.maxbr = ctx->d_maxbr.p;
@@ -616,6 +617,7 @@ BondArgs make_bond_args(pg_context* ctx, int precision, int flags, bool first_f,
         A.bscr = ctx->bo_fj64.p + 3 * ne;
     } else {
         A.terms = ctx->d_pair_terms32.p;
+        A.tab = ctx->d_tab32.p;
         A.trip = ctx->d_trip32.p;
         A.post = ctx->d_post32.p;
         A.maxbr = ctx->d_maxbr32.p;

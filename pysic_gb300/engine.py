@@ -62,6 +62,8 @@ class Engine:
 
     def set_model(self, model):
         a = model.arrays()
+        tab = L.as_f64(a["pair_table"])
+        L.check(self.lib.pg_set_pair_tables(self.ctx, len(tab) // 2, L.dptr(tab)))
         npair = len(a["pair_kind"])
         L.check(self.lib.pg_set_pair_potentials(
             self.ctx, model.n_types, npair, L.iptr(a["pair_kind"]), L.dptr(a["pair_params"]),

@@ -39,6 +39,7 @@ class Model:
         self.type_signatures = []
         self.pair_kind = []
         self.pair_params = []
+        self.pair_table = []  # tabulated potentials: rows (V, d), concatenated
         self.pair_cutoff = []
         self.pair_soft = []
         self.pair_mask1 = []
@@ -63,6 +64,7 @@ class Model:
         d = {}
         d["pair_kind"] = np.array(self.pair_kind, dtype=np.int32)
         d["pair_params"] = np.array(self.pair_params, dtype=np.float64).reshape(-1, 4)
+        d["pair_table"] = np.array(self.pair_table, dtype=np.float64).reshape(-1)
         d["pair_cutoff"] = np.array(self.pair_cutoff, dtype=np.float64)
         d["pair_soft"] = np.array(self.pair_soft, dtype=np.float64)
         d["pair_mask1"] = np.array(self.pair_mask1, dtype=np.uint64)
@@ -115,6 +117,29 @@ def _mask(sigs, element=None, tag=None, index=None):
     return m
 
 
+def read_table(ident):
+    """Rows (V, d) of table_XXXX.txt in the working directory, XXXX the id in
+    four digits (read_table, Utility.f90:384-433; file name as in
+    create_potential, Potentials.f90:2460-2466)."""
+    name = "table_{0:04d}.txt".format(int(ident))
+    try:
+        rows = np.loadtxt(name, ndmin=2, dtype=np.float64)
+    except OSError:
+        raise InvalidPotentialError("tabulated potential: no table file " + name)
+    if rows.shape[1] < 2 or rows.shape[0] < 2:
+        raise InvalidPotentialError("tabulated potential: " + name + " needs at least two rows of V and d")
+    return rows[:, :2]
+
+
+def _table_record(M, params):
+    """[id, range, scale] -> [first row, rows, range, scale] with the rows
+    appended to the model's table."""
+    rows = read_table(params[0])
+    first = len(M.pair_table) // 2
+    M.pair_table.extend(rows.reshape(-1).tolist())
+    return [float(first), float(len(rows)), float(params[1]), float(params[2])]
+
+
 def compile_model(atoms, potentials, coulomb=None):
     potentials = list(potentials or [])
     M = Model()
@@ -162,6 +187,8 @@ def compile_model(atoms, potentials, coulomb=None):
         if nt == 2:
             if kind not in core.PAIR_KIND:
                 raise InvalidPotentialError("'{0}' is not a pair potential of the GB300 engine".format(kind))
+            if kind == "tabulated":
+                params = _table_record(M, params)
             for tg in targets:
                 M.pair_kind.append(core.PAIR_KIND[kind])
                 M.pair_params.append((params + [0.0] * 4)[:4])

@@ -254,3 +254,28 @@ def test_spring_power_shift_power_constant_force_mixed():
     n = len(atoms)
     assert abs(got["energy"] - ref["energy"]) / n <= 1e-5
     assert np.abs(got["forces"] - ref["forces"]).max() <= 1e-4 * max(1.0, np.abs(ref["forces"]).max())
+
+
+@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+def test_tabulated_potential_parity(precision, tmp_path, monkeypatch):
+    """'tabulated' (Potentials.f90:4227-4298) from table_0003.txt, smoothed at
+    its cutoff, with LJ on the side, against the oracle."""
+    monkeypatch.chdir(tmp_path)
+    r = np.linspace(0.0, 6.0, 121)
+    v = 0.3 * np.exp(-r / 0.8) - 0.05 * np.exp(-((r - 3.4) ** 2))
+    dvdr = -0.3 / 0.8 * np.exp(-r / 0.8) + 0.1 * (r - 3.4) * np.exp(-((r - 3.4) ** 2))
+    np.savetxt(str(tmp_path / "table_0003.txt"), np.column_stack([v, 6.0 * dvdr]))
+    P = pysic.Potential
+    atoms = W.lj_fcc(3, noise=0.1, seed=33)
+    pots = [P("tabulated", symbols=[["X", "X"]], parameters=[3, 6.0, 1.2], cutoff=5.5, cutoff_margin=0.5),
+            P("LJ", symbols=[["X", "X"]], parameters=[0.0104, 3.4], cutoff=7.0)]
+    ref = oracle_all(atoms, pots)
+    got = engine_all(atoms, pots, None, precision)
+    n = len(atoms)
+    if precision == "fp64":
+        assert got["energy"] == pytest.approx(ref["energy"], rel=1e-12, abs=1e-11)
+        assert np.abs(got["forces"] - ref["forces"]).max() < 1e-10 * max(1.0, np.abs(ref["forces"]).max())
+        np.testing.assert_allclose(got["stress"], ref["stress"], rtol=1e-9, atol=1e-9 * np.abs(ref["stress"]).max())
+    else:
+        assert abs(got["energy"] - ref["energy"]) / n <= 1e-5
+        assert np.abs(got["forces"] - ref["forces"]).max() <= 1e-4 * max(1.0, np.abs(ref["forces"]).max())

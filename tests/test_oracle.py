@@ -8,6 +8,8 @@
 - Newton's third law and translation invariance,
 - neighbour-list invariants of the restated FastNeighborList.
 """
+import os
+
 import numpy as np
 import pytest
 
@@ -189,3 +191,41 @@ def test_threaded_oracle_matches_serial():
     b = oracle_all(atoms, pots, threads=4)
     assert b["energy"] == pytest.approx(a["energy"], rel=1e-13)
     np.testing.assert_allclose(b["forces"], a["forces"], atol=1e-11)
+
+
+def _write_exp_table(path, ident, max_r, n, A=2.0, rho=0.6):
+    """A table of V = A exp(-r/rho) with d = max_r dV/dr (the derivative with
+    respect to r / max_r, as the Hermite form of evaluate_energy_table uses
+    it)."""
+    r = np.linspace(0.0, max_r, n)
+    v = A * np.exp(-r / rho)
+    d = max_r * (-v / rho)
+    np.savetxt(os.path.join(path, "table_{0:04d}.txt".format(ident)), np.column_stack([v, d]))
+    return A, rho
+
+
+def test_oracle_tabulated_potential_interpolates_its_table(tmp_path, monkeypatch):
+    """evaluate_energy_table / _force_table (Potentials.f90:4227-4298) in the
+    oracle: a fine table of an exponential reproduces it (cubic Hermite), and
+    beyond the range the energy is the last tabulated value, unscaled, and the
+    force zero -- as the reference writes it."""
+    monkeypatch.chdir(tmp_path)
+    A, rho = _write_exp_table(str(tmp_path), 7, 5.0, 401)
+    scale = 1.5
+    pos = np.array([[0.0, 0.0, 0.0], [1.37, 0.4, -0.2], [7.5, 7.5, 7.5]])
+    atoms = pysic.Atoms(["X"] * 3, pos, cell=np.eye(3) * 30.0, pbc=False)
+    pot = pysic.Potential("tabulated", symbols=[["X", "X"]], parameters=[7, 5.0, scale], cutoff=14.0)
+    model = compile_model(atoms, [pot])
+    cuts = np.full(3, 14.0)
+    c, i, o = oracle.neighbors(pos, atoms.get_cell(), atoms.get_pbc(), cuts)
+    args = (pos, np.zeros(3), atoms.get_cell(), atoms.get_pbc(), model, c, i, o)
+    e = oracle.evaluate(*args, what="energy")
+    f, _ = oracle.evaluate(*args, what="forces")
+    d01 = np.linalg.norm(pos[1] - pos[0])
+    # pair 0-1 inside the range; pairs with atom 2 beyond it: each adds the last
+    # row's V unscaled
+    expect = scale * A * np.exp(-d01 / rho) + 2 * A * np.exp(-5.0 / rho)
+    assert e == pytest.approx(expect, rel=1e-9)
+    fmag = scale * A / rho * np.exp(-d01 / rho)
+    np.testing.assert_allclose(f[1], fmag * (pos[1] - pos[0]) / d01, rtol=1e-7)
+    np.testing.assert_array_equal(f[2], np.zeros(3))
