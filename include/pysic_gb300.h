@@ -89,6 +89,16 @@ int pg_get_atom_charges(pg_context* ctx, double* charges);
 int pg_set_pair_potentials(pg_context* ctx, int32_t n_types, int32_t n_records, const int32_t* kind,
                            const double* params, const double* cutoff, const double* soft,
                            const uint64_t* mask1, const uint64_t* mask2, const int32_t* group);
+/* add_potential(...) for three-body records (kind 0: bond_bend, params epsilon,
+ * theta_0, n, m; V = epsilon (cos^n theta - cos^n theta_0)^m, Potentials.f90:
+ * 3159-3314), one record per distinct permutation of each target tuple as
+ * calculator.py adds them: type masks of target positions 1, 2, 3 and of the
+ * types that may sit in the middle (the unpermuted tuple's second element).
+ * At most 64 records.  Triplets are found as core_loop_over_local_interactions
+ * finds them (Core.f90:3540-3943). */
+int pg_set_triplet_potentials(pg_context* ctx, int32_t n_records, const int32_t* kind, const double* params,
+                              const double* cutoff, const double* soft, const uint64_t* mask1,
+                              const uint64_t* mask2, const uint64_t* mask3, const uint64_t* center);
 /* The tables of every tabulated pair record, concatenated: n_rows rows of (V,
  * d) as read_table (Utility.f90:384-433) reads table_XXXX.txt; evaluated as
  * evaluate_energy_table / _force_table (Potentials.f90:4227-4298). */

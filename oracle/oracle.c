@@ -582,6 +582,80 @@ typedef struct {
     double* chi;   /* per-thread n */
 } loop_job;
 
+/* One bond_bend term of the triplet x - c - y, s1 = x -> c, s2 = c -> y:
+ * evaluate_energy_bond_bending / evaluate_force_bond_bending (Potentials.f90:
+ * 3206-3314; the derived cos(theta_0)^n of 3183-3194) with the cut factors and
+ * the virial of core_evaluate_local_triplet_B (Core.f90:6760-6991). */
+static int ipow_i(double x, int k, double* out) {
+    double v = 1.0;
+    for (int q = 0; q < (k < 0 ? -k : k); ++q) v *= x;
+    *out = k < 0 ? 1.0 / v : v;
+    return 0;
+}
+
+static void tri_term(const orc_model* m, int r, loop_job* J, int x, int c, int y, const double s1[3], double d1,
+                     const double s2[3], double d2) {
+    const double* p = m->tri_params + 4 * (size_t)r;
+    const int n = (int)p[2], mm = (int)p[3];
+    const double derived = pow(cos(p[1]), p[2]);
+    const double rc = m->tri_cutoff[r], soft = m->tri_soft[r];
+    const int smoothened = soft > 0.0 && soft < rc;
+    double f1 = 1.0, f2 = 1.0, g1[3] = {0, 0, 0}, g2[3] = {0, 0, 0};
+    if (smoothened) {
+        f1 = smooth_factor(d1, rc, soft);
+        f2 = smooth_factor(d2, rc, soft);
+        const double q1 = smooth_deriv(d1, rc, soft), q2 = smooth_deriv(d2, rc, soft);
+        for (int k = 0; k < 3; ++k) {
+            g1[k] = s1[k] / d1 * q1; /* smoothening_gradient: f'(d) times the direction */
+            g2[k] = s2[k] / d2 * q2;
+        }
+    }
+    /* energy: r3 = (-sep1) . sep2, (r3 / (r1 r2))^n - derived, eps r6^m */
+    double t1[3] = {-s1[0], -s1[1], -s1[2]};
+    const double r3 = dot3(t1, s2);
+    double cn, e6;
+    ipow_i(r3 / (d1 * d2), n, &cn);
+    ipow_i(cn - derived, mm, &e6);
+    const double v = p[0] * e6;
+    if (J->what == 0) {
+        J->energy += v * f1 * f2;
+        return;
+    }
+    if (J->what != 1) return;
+    /* forces of evaluate_force_bond_bending */
+    double tmp3[3], tmp4[3];
+    for (int k = 0; k < 3; ++k) {
+        tmp3[k] = s2[k] - r3 / (d1 * d1) * t1[k];
+        tmp4[k] = t1[k] - r3 / (d2 * d2) * s2[k];
+    }
+    const double ratio = 1.0 / (d1 * d2);
+    const double cosplain = r3 * ratio;
+    double cospower, dm;
+    ipow_i(cosplain, n - 1, &cospower);
+    ipow_i(cospower * cosplain - derived, mm - 1, &dm);
+    const double r6 = p[0] * (mm * n) * dm * cospower;
+    double fx[3], fc[3], fy[3];
+    for (int k = 0; k < 3; ++k) {
+        const double a = -tmp3[k] * ratio * r6, b = (tmp3[k] + tmp4[k]) * ratio * r6, w = -tmp4[k] * ratio * r6;
+        const double e = smoothened ? v : 0.0;
+        fx[k] = a * f1 * f2 + g1[k] * f2 * e;
+        fc[k] = b * f1 * f2 + (-g1[k] * f2 + g2[k] * f1) * e;
+        fy[k] = w * f1 * f2 - g2[k] * f1 * e;
+    }
+    for (int k = 0; k < 3; ++k) {
+        J->F[3 * (size_t)x + k] += fx[k];
+        J->F[3 * (size_t)c + k] += fc[k];
+        J->F[3 * (size_t)y + k] += fy[k];
+    }
+    double* st = J->stress;
+    st[0] += s1[0] * fc[0] + (s1[0] + s2[0]) * fy[0];
+    st[1] += s1[1] * fc[1] + (s1[1] + s2[1]) * fy[1];
+    st[2] += s1[2] * fc[2] + (s1[2] + s2[2]) * fy[2];
+    st[3] += s1[1] * fc[2] + (s1[1] + s2[1]) * fy[2];
+    st[4] += s1[0] * fc[2] + (s1[0] + s2[0]) * fy[2];
+    st[5] += s1[0] * fc[1] + (s1[0] + s2[0]) * fy[1];
+}
+
 /* The per-atom body of core_loop_over_local_interactions, Core.f90:3249-3946,
  * for atoms [a0, a1). Singlets: core_evaluate_local_singlet (4095-4239);
  * inline Ewald real space (3416-3460); doublets: core_evaluate_local_doublet_
@@ -719,6 +793,50 @@ static void* loop_range(void* arg) {
                     st[3] += sep[1] * p2[2];
                     st[4] += sep[0] * p2[2];
                     st[5] += sep[0] * p2[1];
+                }
+            }
+            /* three-body records (Core.f90:3540-3943): the doublet routines flag
+               the many-body potentials of this pair, then the two triplet loops */
+            if (m->n_tri > 0 && d != 0.0) {
+                uint64_t rm = 0;
+                for (int r = 0; r < m->n_tri; ++r) {
+                    const uint64_t many = m->tri_mask1[r] | m->tri_mask2[r] | m->tri_mask3[r];
+                    if (m->tri_cutoff[r] > d && has(many, ti) && has(m->tri_mask2[r], tj)) rm |= 1ull << r;
+                }
+                if (rm) {
+                    const double s21[3] = {-sep[0], -sep[1], -sep[2]};
+                    /* atom2 - atom1 - atom3, atom3 among atom1's neighbours */
+                    for (int l = nb->start[i]; l < nb->start[i + 1]; ++l) {
+                        const int k = nb->idx[l];
+                        const int* ol = nb->off + 3 * (size_t)l;
+                        const int o23[3] = {ol[0] - o[0], ol[1] - o[1], ol[2] - o[2]};
+                        if (!pick(j, k, o23)) continue;
+                        double s13[3];
+                        separation(&X->C, s->pos + 3 * (size_t)i, s->pos + 3 * (size_t)k, ol, s13);
+                        const double d13 = sqrt(dot3(s13, s13));
+                        if (d13 == 0.0) continue;
+                        const int tk = s->type[k];
+                        for (int r = 0; r < m->n_tri; ++r)
+                            if (((rm >> r) & 1) && has(m->tri_mask3[r], tk) && has(m->tri_center[r], ti) &&
+                                m->tri_cutoff[r] > d13)
+                                tri_term(m, r, J, j, i, k, s21, d, s13, d13);
+                    }
+                    /* atom1 - atom2 - atom3, atom3 among atom2's neighbours */
+                    for (int l = nb->start[j]; l < nb->start[j + 1]; ++l) {
+                        const int k = nb->idx[l];
+                        const int* ol = nb->off + 3 * (size_t)l;
+                        const int o13[3] = {ol[0] + o[0], ol[1] + o[1], ol[2] + o[2]};
+                        if (!pick(i, k, o13)) continue;
+                        double s23[3];
+                        separation(&X->C, s->pos + 3 * (size_t)j, s->pos + 3 * (size_t)k, ol, s23);
+                        const double d23 = sqrt(dot3(s23, s23));
+                        if (d23 == 0.0) continue;
+                        const int tk = s->type[k];
+                        for (int r = 0; r < m->n_tri; ++r)
+                            if (((rm >> r) & 1) && has(m->tri_mask3[r], tk) && has(m->tri_center[r], tj) &&
+                                m->tri_cutoff[r] > d23)
+                                tri_term(m, r, J, i, j, k, sep, d, s23, d23);
+                    }
                 }
             }
         }

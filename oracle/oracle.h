@@ -67,6 +67,15 @@ typedef struct {
     const double* ewald_scaler;   /* n */
     const double* pair_table;     /* tabulated potentials: rows (V, d), concatenated */
     int64_t n_table_rows;
+    int32_t n_tri;                /* three-body records (bond_bend), one per permutation */
+    const int32_t* tri_kind;
+    const double* tri_params;     /* 4 per record: epsilon, theta_0, n, m */
+    const double* tri_cutoff;
+    const double* tri_soft;
+    const uint64_t* tri_mask1;
+    const uint64_t* tri_mask2;
+    const uint64_t* tri_mask3;
+    const uint64_t* tri_center;   /* types that may be the middle atom */
 } orc_model;
 
 /* CSR neighbour list: entries of atom i are [start[i], start[i+1]). */

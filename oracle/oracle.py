@@ -36,7 +36,9 @@ class _Model(ctypes.Structure):
                 ("bond_group", _ip), ("ewald", ctypes.c_int32), ("ewald_rc", ctypes.c_double),
                 ("ewald_kc", ctypes.c_double), ("ewald_sigma", ctypes.c_double), ("ewald_eps", ctypes.c_double),
                 ("ewald_kmax", ctypes.c_int32 * 3), ("ewald_scaler", _dp), ("pair_table", _dp),
-                ("n_table_rows", ctypes.c_int64)]
+                ("n_table_rows", ctypes.c_int64), ("n_tri", ctypes.c_int32), ("tri_kind", _ip), ("tri_params", _dp),
+                ("tri_cutoff", _dp), ("tri_soft", _dp), ("tri_mask1", _up), ("tri_mask2", _up), ("tri_mask3", _up),
+                ("tri_center", _up)]
 
 
 class _NbList(ctypes.Structure):
@@ -135,6 +137,15 @@ def _model(keep, M, n):
     m.pair_group = _i(keep.i32(a["pair_group"]))
     m.pair_table = _d(keep.f64(a["pair_table"]))
     m.n_table_rows = len(a["pair_table"]) // 2
+    m.n_tri = len(a["tri_kind"])
+    m.tri_kind = _i(keep.i32(a["tri_kind"]))
+    m.tri_params = _d(keep.f64(a["tri_params"]))
+    m.tri_cutoff = _d(keep.f64(a["tri_cutoff"]))
+    m.tri_soft = _d(keep.f64(a["tri_soft"]))
+    m.tri_mask1 = _u(keep.u64(a["tri_mask1"]))
+    m.tri_mask2 = _u(keep.u64(a["tri_mask2"]))
+    m.tri_mask3 = _u(keep.u64(a["tri_mask3"]))
+    m.tri_center = _u(keep.u64(a["tri_center"]))
     m.n_single = len(a["single_kind"])
     m.single_kind = _i(keep.i32(a["single_kind"]))
     m.single_params = _d(keep.f64(a["single_params"]))

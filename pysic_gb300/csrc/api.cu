@@ -145,6 +145,7 @@ void enqueue_evaluation(pg_context* ctx, int precision, int flags, int G, const 
     ctx->out_acc.resize(8);
     const bool run_pair = ctx->have_pair_kernel_terms || ctx->ewald || ctx->have_singles;
     const bool run_bond = ctx->have_bond_terms && (wantE || wantF);
+    const bool run_tri = ctx->have_triplets && (wantE || wantF);
     const int Gp = pair_lanes_for(ctx);
     FxAcc* acc = ctx->out_acc.p;
     bool first_f = true, first_chi = true;
@@ -154,7 +155,7 @@ void enqueue_evaluation(pg_context* ctx, int precision, int flags, int G, const 
     mark(0);
     // the totals are integers that every kernel adds to: clear them first (the
     // mixed path's displacement pass does it on the way)
-    if (precision == PG_PREC_MIXED && (run_pair || run_bond)) launch_disp(ctx, skip, acc);
+    if (precision == PG_PREC_MIXED && (run_pair || run_bond || run_tri)) launch_disp(ctx, skip, acc);
     else PG_CUDA(cudaMemsetAsync(acc, 0, sizeof(FxAcc) * 8, ctx->stream));
     if (run_pair) {
         launch_pair_kernel_skip(ctx, precision, flags, first_f, first_chi, Gp, acc, skip);
@@ -167,6 +168,10 @@ void enqueue_evaluation(pg_context* ctx, int precision, int flags, int G, const 
         if (wantF) first_f = false;
     } else {
         mark(2);
+    }
+    if (run_tri) {
+        launch_triplets(ctx, precision, flags, first_f, acc, skip);
+        if (wantF) first_f = false;
     }
     mark(3);
     if (ctx->ewald) {
@@ -410,6 +415,28 @@ int pg_set_pair_potentials(pg_context* ctx, int32_t n_types, int32_t n, const in
         ctx->pr_m1.assign(mask1, mask1 + n);
         ctx->pr_m2.assign(mask2, mask2 + n);
         ctx->pr_group.assign(group, group + n);
+        ctx->tables_dirty = true;
+    });
+}
+
+int pg_set_triplet_potentials(pg_context* ctx, int32_t n, const int32_t* kind, const double* params,
+                              const double* cutoff, const double* soft, const uint64_t* mask1, const uint64_t* mask2,
+                              const uint64_t* mask3, const uint64_t* center) {
+    return guarded([&] {
+        check_ctx(ctx);
+        pg::require(n >= 0 && n <= pg::PG_MAX_TRIPLET_RECORDS, PG_ERR_UNSUPPORTED,
+                    "three-body records: at most 64 (distinct permutations of all target tuples)");
+        pg::require(n == 0 || (kind && params && cutoff && soft && mask1 && mask2 && mask3 && center), PG_ERR_INVALID,
+                    "null record arrays");
+        for (int r = 0; r < n; ++r) pg::require(kind[r] == 0, PG_ERR_UNSUPPORTED, "unknown three-body kind");
+        ctx->tr_kind.assign(kind, kind + n);
+        ctx->tr_params.assign(params, params + 4 * (size_t)n);
+        ctx->tr_cut.assign(cutoff, cutoff + n);
+        ctx->tr_soft.assign(soft, soft + n);
+        ctx->tr_m1.assign(mask1, mask1 + n);
+        ctx->tr_m2.assign(mask2, mask2 + n);
+        ctx->tr_m3.assign(mask3, mask3 + n);
+        ctx->tr_center.assign(center, center + n);
         ctx->tables_dirty = true;
     });
 }

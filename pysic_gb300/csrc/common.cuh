@@ -148,6 +148,17 @@ struct PostT {
     int valid;
 };
 
+// Three-body record (bond_bend: V = eps (cos^n theta - cos^n theta_0)^m,
+// Potentials.f90:3206-3314) with the target masks of the reference's
+// permuted record: position 2 and 3 types, the types at any position, and the
+// types that may sit in the middle (the unpermuted tuple's second element).
+template <typename R>
+struct TriT {
+    R eps, c0, rc, rs;  // c0 = cos(theta_0)^n, the reference's derived parameter
+    int n, m, smooth, kind;
+    unsigned long long m2, m3, many, center;
+};
+
 template <typename R, typename S>
 inline PairT<R> cast_pair(const PairT<S>& a) {
     return PairT<R>{a.kind, a.group, a.smooth, a.in_bond_kernel, (R)a.p0, (R)a.p1, (R)a.p2, (R)a.p3, (R)a.rc, (R)a.rs,
@@ -253,6 +264,7 @@ struct pg_context {
     std::vector<int> br_group;
     bool tables_dirty = true;
     bool have_bond_terms = false, have_pair_kernel_terms = false, have_singles = false;
+    bool have_triplets = false;
     double bo_radius = 0.0;          // largest cutoff handled by the bond-order kernels
     pg::DevBuf<pg::PairT<double>> d_pair_terms;
     pg::DevBuf<pg::PairT<float>> d_pair_terms32;
@@ -264,6 +276,13 @@ struct pg_context {
     pg::DevBuf<pg::TripT<float>> d_trip32;
     pg::DevBuf<pg::PostT<double>> d_post;  // n_types
     pg::DevBuf<pg::PostT<float>> d_post32;
+    std::vector<int> tr_kind;            // three-body records as set through the C ABI
+    std::vector<double> tr_params, tr_cut, tr_soft;
+    std::vector<uint64_t> tr_m1, tr_m2, tr_m3, tr_center;
+    pg::DevBuf<pg::TriT<double>> d_tri;  // folded records, FP64 and FP32
+    pg::DevBuf<pg::TriT<float>> d_tri32;
+    int n_tri = 0;
+    pg::DevBuf<long long> tri_facc;      // per atom x 3: three-body forces in 2^-40 fixed point
     pg::DevBuf<double> d_maxbr;          // per type: max bond-order cutoff (max_bond_radius)
     pg::DevBuf<float> d_maxbr32;
     // per (centre type, k type): bond-order cutoff rc, rs of the triplets, valid
@@ -467,6 +486,9 @@ void md_set_state(pg_context* ctx, const double* masses, const double* momenta);
 void md_get_state(pg_context* ctx, double* momenta, double* positions);
 void md_run(pg_context* ctx, int precision, int n_steps, double dt, double skin, int* steps_done, int* rebuild);
 void evaluate(pg_context* ctx, int precision, int flags);
+// triplet.cu: three-body potentials (bond_bend)
+constexpr int PG_MAX_TRIPLET_RECORDS = 64;
+void launch_triplets(pg_context* ctx, int precision, int flags, bool first_f, FxAcc* acc, const int* skip);
 // optimize.cu: the constrained energy minimum over the charges (quadratic energies)
 void optimize_charges(pg_context* ctx, int precision, int max_iter, double tolerance, double* charges, int* iterations,
                       double* error);

@@ -59,7 +59,8 @@ void bond_order_noalloc(pg_context* ctx, int precision, double* d_forces, double
     require(precision == PG_PREC_FP64 || precision == PG_PREC_MIXED, PG_ERR_INVALID, "unknown precision");
     require(d_forces != nullptr && d_totals != nullptr, PG_ERR_INVALID, "null output pointer");
     require(ctx->have_bond_terms, PG_ERR_NOT_READY, "no bond-order factors");
-    require(!ctx->have_pair_kernel_terms && !ctx->ewald && !ctx->have_singles, PG_ERR_UNSUPPORTED,
+    require(!ctx->have_pair_kernel_terms && !ctx->ewald && !ctx->have_singles && !ctx->have_triplets,
+            PG_ERR_UNSUPPORTED,
             "the no-allocation call covers contexts whose every term runs in the bond-order kernels "
             "(no Ewald, single-atom or out-of-bond pair terms)");
     // everything the regular path builds lazily must already exist

@@ -221,6 +221,37 @@ void fold_tables(pg_context* ctx) {
     ctx->d_maxbr32.upload(maxbr32.data(), maxbr32.size(), st);
     ctx->d_single_terms.upload(sterms.data(), sterms.size(), st);
     ctx->d_single_index.upload(sindex.data(), sindex.size(), st);
+    // three-body records: the derived cos(theta_0)^n (calculate_derived_parameters_
+    // bond_bending, Potentials.f90:3183-3194) and the integer exponents n, m
+    {
+        const int nt3 = (int)ctx->tr_kind.size();
+        std::vector<TriT<double>> tri((size_t)std::max(nt3, 1));
+        std::vector<TriT<float>> tri32((size_t)std::max(nt3, 1));
+        for (int r = 0; r < nt3; ++r) {
+            const double* p = ctx->tr_params.data() + 4 * (size_t)r;
+            TriT<double> t{};
+            t.kind = ctx->tr_kind[r];
+            t.eps = p[0];
+            t.c0 = std::pow(std::cos(p[1]), p[2]);
+            t.n = (int)p[2];
+            t.m = (int)p[3];
+            t.rc = ctx->tr_cut[r];
+            const double soft = ctx->tr_soft[r];
+            t.smooth = soft > 0.0 && soft < t.rc;
+            t.rs = t.smooth ? soft : t.rc;
+            t.m2 = ctx->tr_m2[r];
+            t.m3 = ctx->tr_m3[r];
+            t.many = ctx->tr_m1[r] | ctx->tr_m2[r] | ctx->tr_m3[r];
+            t.center = ctx->tr_center[r];
+            tri[(size_t)r] = t;
+            tri32[(size_t)r] = TriT<float>{(float)t.eps, (float)t.c0, (float)t.rc, (float)t.rs, t.n, t.m, t.smooth,
+                                           t.kind, t.m2, t.m3, t.many, t.center};
+        }
+        ctx->n_tri = nt3;
+        ctx->have_triplets = nt3 > 0;
+        ctx->d_tri.upload(tri.data(), tri.size(), st);
+        ctx->d_tri32.upload(tri32.data(), tri32.size(), st);
+    }
     {
         std::vector<double> t64 = ctx->pr_table;
         if (t64.empty()) t64.assign(2, 0.0);

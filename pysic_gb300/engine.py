@@ -64,6 +64,10 @@ class Engine:
         a = model.arrays()
         tab = L.as_f64(a["pair_table"])
         L.check(self.lib.pg_set_pair_tables(self.ctx, len(tab) // 2, L.dptr(tab)))
+        L.check(self.lib.pg_set_triplet_potentials(
+            self.ctx, len(a["tri_kind"]), L.iptr(a["tri_kind"]), L.dptr(a["tri_params"]), L.dptr(a["tri_cutoff"]),
+            L.dptr(a["tri_soft"]), L.u64ptr(a["tri_mask1"]), L.u64ptr(a["tri_mask2"]), L.u64ptr(a["tri_mask3"]),
+            L.u64ptr(a["tri_center"])))
         npair = len(a["pair_kind"])
         L.check(self.lib.pg_set_pair_potentials(
             self.ctx, model.n_types, npair, L.iptr(a["pair_kind"]), L.dptr(a["pair_params"]),

@@ -55,6 +55,16 @@ class Model:
         self.bond_mask2 = []
         self.bond_mask3 = []
         self.bond_group = []
+        # three-body potentials (bond_bend), one record per distinct permutation
+        # of each target tuple, as the reference adds them
+        self.tri_kind = []
+        self.tri_params = []
+        self.tri_cutoff = []
+        self.tri_soft = []
+        self.tri_mask1 = []
+        self.tri_mask2 = []
+        self.tri_mask3 = []
+        self.tri_center = []  # types whose element is the tuple's middle one (original_elements(2))
         self.n_groups = 0
         self.coordinators = []
         self.ewald = None
@@ -80,6 +90,14 @@ class Model:
         d["bond_mask2"] = np.array(self.bond_mask2, dtype=np.uint64)
         d["bond_mask3"] = np.array(self.bond_mask3, dtype=np.uint64)
         d["bond_group"] = np.array(self.bond_group, dtype=np.int32)
+        d["tri_kind"] = np.array(self.tri_kind, dtype=np.int32)
+        d["tri_params"] = np.array(self.tri_params, dtype=np.float64).reshape(-1, 4)
+        d["tri_cutoff"] = np.array(self.tri_cutoff, dtype=np.float64)
+        d["tri_soft"] = np.array(self.tri_soft, dtype=np.float64)
+        d["tri_mask1"] = np.array(self.tri_mask1, dtype=np.uint64)
+        d["tri_mask2"] = np.array(self.tri_mask2, dtype=np.uint64)
+        d["tri_mask3"] = np.array(self.tri_mask3, dtype=np.uint64)
+        d["tri_center"] = np.array(self.tri_center, dtype=np.uint64)
         return d
 
 
@@ -207,6 +225,28 @@ def compile_model(atoms, potentials, coulomb=None):
                 M.single_kind.append(core.SINGLE_KIND[kind])
                 M.single_params.append((params + [0.0] * 4)[:4])
                 M.single_mask.append(_mask(sigs, *tg[0]))
+        elif nt == 3:
+            if kind not in core.TRIPLET_KIND:
+                raise InvalidPotentialError("'{0}' is not a three-body potential of the GB300 engine".format(kind))
+            if grp >= 0:
+                raise InvalidPotentialError("bond-order scaling of three-body potentials is not evaluated by the "
+                                            "GB300 engine")
+            if pot.get_tags() or pot.get_indices():
+                raise InvalidPotentialError("three-body potentials are evaluated for element targets only")
+            # create_potential (Potentials.f90:2353-2472) keeps the unpermuted
+            # tuple as original_elements; the evaluator requires its middle
+            # element at the centre atom (Potentials.f90:3206-3314)
+            for t in pot.get_symbols() or []:
+                centre = _mask(sigs, t[1], None, None)
+                for perm in _distinct_permutations(t):
+                    M.tri_kind.append(core.TRIPLET_KIND[kind])
+                    M.tri_params.append((params + [0.0] * 4)[:4])
+                    M.tri_cutoff.append(float(pot.get_cutoff()))
+                    M.tri_soft.append(float(pot.get_soft_cutoff()))
+                    M.tri_mask1.append(_mask(sigs, perm[0], None, None))
+                    M.tri_mask2.append(_mask(sigs, perm[1], None, None))
+                    M.tri_mask3.append(_mask(sigs, perm[2], None, None))
+                    M.tri_center.append(centre)
         else:
             raise InvalidPotentialError("{0}-body potentials are not evaluated by the GB300 engine".format(nt))
 

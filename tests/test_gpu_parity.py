@@ -279,3 +279,36 @@ def test_tabulated_potential_parity(precision, tmp_path, monkeypatch):
     else:
         assert abs(got["energy"] - ref["energy"]) / n <= 1e-5
         assert np.abs(got["forces"] - ref["forces"]).max() <= 1e-4 * max(1.0, np.abs(ref["forces"]).max())
+
+
+def _bend_pots():
+    P = pysic.Potential
+    return [P("bond_bend", symbols=[["O", "Si", "O"]], parameters=[1.3, 1.9106, 1, 2], cutoff=2.4, cutoff_margin=0.4),
+            P("bond_bend", symbols=[["Si", "O", "Si"]], parameters=[0.7, 2.6, 2, 2], cutoff=2.2),
+            P("exponential", symbols=[["Si", "O"]], parameters=[40.0, 3.0], cutoff=3.0, cutoff_margin=0.5)]
+
+
+@pytest.mark.parametrize("n_si", [12, 200])
+def test_bond_bend_fp64_parity(n_si):
+    """Three-body bond_bend (Potentials.f90:3159-3314) found as the reference's
+    triplet loops find it (Core.f90:3540-3943), against the oracle."""
+    _check_fp64(W.sio2_box(n_si, seed=22), _bend_pots())
+
+
+def test_bond_bend_mixed_accuracy():
+    atoms = W.sio2_box(200, seed=23)
+    pots = _bend_pots()
+    ref = oracle_all(atoms, pots)
+    got = engine_all(atoms, pots, None, "mixed")
+    n = len(atoms)
+    assert abs(got["energy"] - ref["energy"]) / n <= 1e-5
+    assert np.abs(got["forces"] - ref["forces"]).max() <= 1e-4 * max(1.0, np.abs(ref["forces"]).max())
+    np.testing.assert_allclose(got["stress"], ref["stress"], rtol=1e-4, atol=1e-4 * np.abs(ref["stress"]).max())
+
+
+def test_bond_bend_results_are_bit_reproducible():
+    atoms = W.sio2_box(200, seed=24)
+    a = engine_all(atoms, _bend_pots(), None, "fp64")
+    b = engine_all(atoms, _bend_pots(), None, "fp64")
+    assert a["energy"] == b["energy"]
+    assert np.array_equal(a["forces"], b["forces"])

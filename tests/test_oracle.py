@@ -229,3 +229,39 @@ def test_oracle_tabulated_potential_interpolates_its_table(tmp_path, monkeypatch
     fmag = scale * A / rho * np.exp(-d01 / rho)
     np.testing.assert_allclose(f[1], fmag * (pos[1] - pos[0]) / d01, rtol=1e-7)
     np.testing.assert_array_equal(f[2], np.zeros(3))
+
+
+def _bend_case():
+    atoms = W.sio2_box(12, seed=21)
+    P = pysic.Potential
+    pots = [P("bond_bend", symbols=[["O", "Si", "O"]], parameters=[1.3, 1.9106, 1, 2], cutoff=2.4,
+              cutoff_margin=0.4),
+            P("bond_bend", symbols=[["Si", "O", "Si"]], parameters=[0.7, 2.6, 2, 2], cutoff=2.2)]
+    return atoms, pots
+
+
+def test_oracle_bond_bend_forces_are_the_energy_gradient():
+    """bond_bend (Potentials.f90:3159-3314) in the oracle's triplet loops:
+    forces equal minus the finite-difference gradient of the energy, smooth
+    cutoff included."""
+    atoms, pots = _bend_case()
+    model = compile_model(atoms, pots)
+    lists = oracle_lists(atoms, pots)
+    pos0 = atoms.get_positions()
+
+    def energy(p):
+        return oracle.evaluate(p, atoms.get_initial_charges(), atoms.get_cell(), atoms.get_pbc(), model, *lists,
+                               what="energy")
+
+    f, _ = oracle.evaluate(pos0, atoms.get_initial_charges(), atoms.get_cell(), atoms.get_pbc(), model, *lists,
+                           what="forces")
+    assert np.abs(f).max() > 0.1
+    h = 1e-6
+    rng = np.random.default_rng(0)
+    for a in rng.choice(len(atoms), 6, replace=False):
+        for c in range(3):
+            p1, p2 = pos0.copy(), pos0.copy()
+            p1[a, c] += h
+            p2[a, c] -= h
+            num = -(energy(p1) - energy(p2)) / (2 * h)
+            assert f[a, c] == pytest.approx(num, abs=2e-5)
