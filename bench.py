@@ -531,15 +531,16 @@ def _batched_structure(k):
     return a.get_positions(), a.get_cell()[0, 0]
 
 
-def run_batch(args):
-    """512 uneven silicon boxes (Tersoff + LJ): one launch per kernel for all
-    systems (graph replay) against one evaluation per system."""
-    import multiprocessing as mp
+def _build_batch(precision, systems=512):
+    """The first `systems` of the 512 systems of the many-system workload, set
+    up and batched (structures made in worker processes for the full set)."""
+    if systems >= 512:
+        import multiprocessing as mp
 
-    with mp.get_context("spawn").Pool(os.cpu_count() or 1) as pool:
-        structs = pool.map(_batched_structure, range(512), chunksize=8)
-    import torch
-
+        with mp.get_context("spawn").Pool(os.cpu_count() or 1) as pool:
+            structs = pool.map(_batched_structure, range(512), chunksize=8)
+    else:
+        structs = [_batched_structure(k) for k in range(systems)]
     import pysic_gb300 as pysic
     from pysic_gb300 import workloads as W
     from pysic_gb300.batch import BatchedPysic
@@ -548,11 +549,18 @@ def run_batch(args):
     calcs = []
     for pos, L_ in structs:
         atoms = pysic.Atoms(["Si"] * len(pos), pos, cell=np.eye(3) * L_, pbc=True)
-        c = pysic.Pysic(atoms, pots, precision=args.precision)
+        c = pysic.Pysic(atoms, pots, precision=precision)
         c.set_core()
         calcs.append(c)
-    n_atoms = sum(len(p) for p, _ in structs)
-    batch = BatchedPysic(calcs)
+    return BatchedPysic(calcs), sum(len(p) for p, _ in structs)
+
+
+def run_batch(args):
+    """512 uneven silicon boxes (Tersoff + LJ): one launch per kernel for all
+    systems (graph replay) against one evaluation per system."""
+    batch, n_atoms = _build_batch(args.precision)
+    import torch
+
     flush = torch.empty(64 * 1024 * 1024, dtype=torch.float32, device="cuda")
     stream = torch.cuda.ExternalStream(batch.stream_handle())
 
@@ -618,6 +626,15 @@ def run_profile(args):
     from pysic_gb300 import _lib as L
 
     prec = L.PREC_MIXED if args.precision == "mixed" else L.PREC_FP64
+    if args.workload == "batched_si_512":
+        # the batched launches only: set-up, then `--steps` evaluations of all 512 systems
+        batch, n_atoms = _build_batch(args.precision, args.systems)
+        for _ in range(args.steps):
+            batch.evaluate(args.precision)
+        batch.synchronize()
+        print(json.dumps({"profile_run": args.workload, "precision": args.precision, "systems": args.systems,
+                          "atoms": n_atoms}))
+        return
     atoms, calc, _ = setup(args.workload, args.precision, 0)
     eng = calc.engine
     eng.set_lanes(args.lanes)
@@ -633,6 +650,7 @@ def main():
     p = argparse.ArgumentParser(description=__doc__, formatter_class=argparse.RawDescriptionHelpFormatter)
     p.add_argument("--profile", action="store_true", help="short fixed run for ncu captures")
     p.add_argument("--lanes", type=int, default=8, help="lanes per atom in --profile mode")
+    p.add_argument("--systems", type=int, default=512, help="systems of the many-system workload in --profile mode")
     p.add_argument("--gpus", type=int, default=1)
     p.add_argument("--steps", type=int, default=100)
     p.add_argument("--warmup", type=int, default=5)
