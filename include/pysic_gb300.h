@@ -84,8 +84,10 @@ int pg_get_atom_charges(pg_context* ctx, double* charges);
  * (epsilon, zeta), 2 Buckingham (A, C, sigma), 3 spring (k, R_0; shifted by its
  * value at the cutoff), 4 power (epsilon, a, n), 5 shift_power (epsilon, r1, r2,
  * n), 6 tabulated (first row, row count, range, scale; rows set with
- * pg_set_pair_tables); params: 4 per record (unused tail zero); soft: cutoff -
- * cutoff_margin; group: bond-order group (-1 none). */
+ * pg_set_pair_tables), 7 charge_pair (epsilon, n1, n2: epsilon q1^n1 q2^n2 with
+ * the first-target types of pg_set_pair_first_targets); params: 4 per record
+ * (unused tail zero); soft: cutoff - cutoff_margin; group: bond-order group
+ * (-1 none). */
 int pg_set_pair_potentials(pg_context* ctx, int32_t n_types, int32_t n_records, const int32_t* kind,
                            const double* params, const double* cutoff, const double* soft,
                            const uint64_t* mask1, const uint64_t* mask2, const int32_t* group);
@@ -99,6 +101,10 @@ int pg_set_pair_potentials(pg_context* ctx, int32_t n_types, int32_t n_records, 
 int pg_set_triplet_potentials(pg_context* ctx, int32_t n_records, const int32_t* kind, const double* params,
                               const double* cutoff, const double* soft, const uint64_t* mask1,
                               const uint64_t* mask2, const uint64_t* mask3, const uint64_t* center);
+/* Per pair record: the types of its unpermuted first target
+ * (original_elements(1) of create_potential, Potentials.f90:2353-2472), which
+ * decide charge_pair's exponent order (Potentials.f90:4415-4513). */
+int pg_set_pair_first_targets(pg_context* ctx, int32_t n_records, const uint64_t* masks);
 /* The tables of every tabulated pair record, concatenated: n_rows rows of (V,
  * d) as read_table (Utility.f90:384-433) reads table_XXXX.txt; evaluated as
  * evaluate_energy_table / _force_table (Potentials.f90:4227-4298). */

@@ -733,16 +733,53 @@ static void* loop_range(void* arg) {
                     chi[j] += q1 * tmp;
                 }
             }
-            if (J->what == 2) continue; /* non-charge pair potentials have zero electronegativity */
             for (int r = 0; r < m->n_pair; ++r) {
                 if (!has(m->pair_mask1[r], ti)) continue;
                 if (!(m->pair_cutoff[r] > d)) continue;
                 if (!has(m->pair_mask2[r], tj)) continue;
                 const int kind = m->pair_kind[r];
+                /* non-charge pair potentials have zero electronegativity */
+                if (J->what == 2 && kind != 7) continue;
                 const double* p = m->pair_params + 4 * (size_t)r;
                 const int grp = m->pair_group[r];
                 const int sm = X->smoothened[r];
                 const double rc = m->pair_cutoff[r], rs = X->smooth_soft[r];
+                if (kind == 7) {
+                    /* charge_pair, Potentials.f90:4415-4513: epsilon q1^n1 q2^n2, the
+                       exponents swapped unless atom1 is the unpermuted first target;
+                       no force routine, so only the cut factor's gradient acts */
+                    const double q1 = s->charge[i], q2 = s->charge[j];
+                    const int direct = has(m->pair_first[r], ti);
+                    const int n1 = direct ? (int)p[1] : (int)p[2], n2 = direct ? (int)p[2] : (int)p[1];
+                    const double v = p[0] * (__builtin_powi(q1, n1) * __builtin_powi(q2, n2));
+                    const double cut = sm ? smooth_factor(d, rc, rs) : 1.0;
+                    if (J->what == 0) {
+                        J->energy += v * cut;
+                    } else if (J->what == 1) {
+                        if (sm) {
+                            const double dv = smooth_deriv(d, rc, rs);
+                            double p2[3];
+                            for (int c = 0; c < 3; ++c) {
+                                const double g = dir[c] * dv;
+                                F[3 * (size_t)i + c] += v * g;
+                                p2[c] = -v * g;
+                                F[3 * (size_t)j + c] += p2[c];
+                            }
+                            st[0] += sep[0] * p2[0];
+                            st[1] += sep[1] * p2[1];
+                            st[2] += sep[2] * p2[2];
+                            st[3] += sep[1] * p2[2];
+                            st[4] += sep[0] * p2[2];
+                            st[5] += sep[0] * p2[1];
+                        }
+                    } else {
+                        const double e1 = n1 > 0 ? -p[0] * (n1 * __builtin_powi(q1, n1 - 1) * __builtin_powi(q2, n2)) : 0.0;
+                        const double e2 = n2 > 0 ? -p[0] * (n2 * __builtin_powi(q1, n1) * __builtin_powi(q2, n2 - 1)) : 0.0;
+                        chi[i] += e1 * cut;
+                        chi[j] += e2 * cut;
+                    }
+                    continue;
+                }
                 if (J->what == 0) {
                     double B1 = 0, B2 = 0;
                     if (grp >= 0) {

@@ -42,7 +42,8 @@ typedef struct {
     int32_t n_types;
     int32_t n_pair;
     const int32_t* pair_kind;     /* 0 LJ, 1 exponential, 2 Buckingham, 3 spring, 4 power, 5 shift_power,
-                                     6 tabulated (params: first row, rows, range, scale) */
+                                     6 tabulated (params: first row, rows, range, scale),
+                                     7 charge_pair (epsilon, n1, n2) */
     const double* pair_params;    /* 4 per record */
     const double* pair_cutoff;
     const double* pair_soft;      /* cutoff - cutoff_margin, as passed to add_potential */
@@ -76,6 +77,7 @@ typedef struct {
     const uint64_t* tri_mask2;
     const uint64_t* tri_mask3;
     const uint64_t* tri_center;   /* types that may be the middle atom */
+    const uint64_t* pair_first;   /* per pair record: types of the unpermuted first target */
 } orc_model;
 
 /* CSR neighbour list: entries of atom i are [start[i], start[i+1]). */

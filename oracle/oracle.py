@@ -38,7 +38,7 @@ class _Model(ctypes.Structure):
                 ("ewald_kmax", ctypes.c_int32 * 3), ("ewald_scaler", _dp), ("pair_table", _dp),
                 ("n_table_rows", ctypes.c_int64), ("n_tri", ctypes.c_int32), ("tri_kind", _ip), ("tri_params", _dp),
                 ("tri_cutoff", _dp), ("tri_soft", _dp), ("tri_mask1", _up), ("tri_mask2", _up), ("tri_mask3", _up),
-                ("tri_center", _up)]
+                ("tri_center", _up), ("pair_first", _up)]
 
 
 class _NbList(ctypes.Structure):
@@ -146,6 +146,7 @@ def _model(keep, M, n):
     m.tri_mask2 = _u(keep.u64(a["tri_mask2"]))
     m.tri_mask3 = _u(keep.u64(a["tri_mask3"]))
     m.tri_center = _u(keep.u64(a["tri_center"]))
+    m.pair_first = _u(keep.u64(a["pair_first"]))
     m.n_single = len(a["single_kind"])
     m.single_kind = _i(keep.i32(a["single_kind"]))
     m.single_params = _d(keep.f64(a["single_params"]))

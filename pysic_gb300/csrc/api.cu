@@ -406,7 +406,7 @@ int pg_set_pair_potentials(pg_context* ctx, int32_t n_types, int32_t n, const in
         pg::require(n_types >= 0 && n_types <= 64, PG_ERR_INVALID, "n_types must be within 0..64");
         pg::require(n >= 0, PG_ERR_INVALID, "negative record count");
         for (int r = 0; r < n; ++r)
-            pg::require(kind[r] >= 0 && kind[r] <= 6, PG_ERR_UNSUPPORTED, "unknown pair potential kind");
+            pg::require(kind[r] >= 0 && kind[r] <= 7, PG_ERR_UNSUPPORTED, "unknown pair potential kind");
         ctx->n_types = n_types;
         ctx->pr_kind.assign(kind, kind + n);
         ctx->pr_params.assign(params, params + 4 * (size_t)n);
@@ -437,6 +437,15 @@ int pg_set_triplet_potentials(pg_context* ctx, int32_t n, const int32_t* kind, c
         ctx->tr_m2.assign(mask2, mask2 + n);
         ctx->tr_m3.assign(mask3, mask3 + n);
         ctx->tr_center.assign(center, center + n);
+        ctx->tables_dirty = true;
+    });
+}
+
+int pg_set_pair_first_targets(pg_context* ctx, int32_t n, const uint64_t* masks) {
+    return guarded([&] {
+        check_ctx(ctx);
+        pg::require(n >= 0 && (n == 0 || masks != nullptr), PG_ERR_INVALID, "invalid first-target masks");
+        ctx->pr_first.assign(masks, masks + n);
         ctx->tables_dirty = true;
     });
 }

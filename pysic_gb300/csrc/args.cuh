@@ -21,6 +21,7 @@ struct PairArgs {
     const SingleTerm* sterms;
     const int2* sindex;
     int ewald;
+    int qpair;  // charge-dependent pair terms present: their electronegativities are wanted too
     double ew_rc, ew_is2, ew_k, ew_c2, ew_isq2;  // 1/(sqrt2 sigma), 1/(4 pi eps), 2/(sqrt(2 pi) sigma), 1/(2 sigma^2)
     int flags;
     int first_f, first_chi;

@@ -126,12 +126,14 @@ struct CellK {
 // that the mixed-precision kernels never convert parameters per term.
 template <typename R>
 struct PairT {
-    int kind;            // 0 LJ, 1 exponential, 2 Buckingham, 3 spring, 4 power, 5 shift_power, 6 tabulated
+    int kind;            // 0 LJ, 1 exponential, 2 Buckingham, 3 spring, 4 power, 5 shift_power, 6 tabulated,
+                         // 7 charge_pair
     int group;           // -1: plain, else bond-order group
     int smooth;          // smoothing active (create_potential, Potentials.f90:2382-2388)
     int in_bond_kernel;  // evaluated by the bond-order kernels (short list) rather than the pair kernel
     R p0, p1, p2, p3, rc, rs;
     int t0, tn;          // tabulated: first row and row count in the context's table rows
+    unsigned long long first;  // charge_pair: types of the unpermuted first target (original_elements(1))
 };
 
 // Tersoff triplet parameters for (centre type, j type, k type) of group 0.
@@ -162,7 +164,7 @@ struct TriT {
 template <typename R, typename S>
 inline PairT<R> cast_pair(const PairT<S>& a) {
     return PairT<R>{a.kind, a.group, a.smooth, a.in_bond_kernel, (R)a.p0, (R)a.p1, (R)a.p2, (R)a.p3, (R)a.rc, (R)a.rs,
-                    a.t0, a.tn};
+                    a.t0, a.tn, a.first};
 }
 template <typename R, typename S>
 inline TripT<R> cast_trip(const TripT<S>& a) {
@@ -270,6 +272,8 @@ struct pg_context {
     pg::DevBuf<pg::PairT<float>> d_pair_terms32;
     pg::DevBuf<int2> d_pair_index;     // per (ti, tj): offset, count into d_pair_terms
     std::vector<double> pr_table;      // tabulated potentials: rows (V, d) of every table, concatenated
+    std::vector<uint64_t> pr_first;    // per pair record: types of its unpermuted first target
+    bool have_charge_pairs = false;    // a charge-dependent pair term (charge_pair)
     pg::DevBuf<double> d_tab64;        // the rows on the device, FP64 and FP32
     pg::DevBuf<float> d_tab32;
     pg::DevBuf<pg::TripT<double>> d_trip;  // n_types^3

@@ -102,8 +102,8 @@ __device__ __forceinline__ void pair_eval(const PairT<R>& P, R r, R& V, R& dV, c
             dV = -p0 * P.p3 / w * pow_(x, P.p3 - R(1));
             break;
         }
-        default: {  // tabulated: cubic Hermite on rows (V, d), range p0, scale p1 (4227-4298);
-                    // beyond the range the last V, unscaled, as the reference returns it
+        case 6: {  // tabulated: cubic Hermite on rows (V, d), range p0, scale p1 (4227-4298);
+                   // beyond the range the last V, unscaled, as the reference returns it
             const R* T = tab + 2 * (long long)P.t0;
             const int nv = P.tn;
             if (r >= p0) {
@@ -122,7 +122,32 @@ __device__ __forceinline__ void pair_eval(const PairT<R>& P, R r, R& V, R& dV, c
             }
             break;
         }
+        default:  // charge-dependent terms are evaluated by the pair kernel itself
+            V = R(0);
+            dV = R(0);
+            break;
     }
+}
+
+// pick (Core.f90): each pair once -- the higher index, or for one atom and
+// its own image the lexicographically positive offset
+__device__ __forceinline__ bool pick(int i1, int i2, int o0, int o1, int o2) {
+    if (i2 > i1) return true;
+    if (i2 == i1 && o0 >= 0) {
+        if (o0 > 0) return true;
+        if (o1 > 0) return true;
+        if (o1 == 0 && o2 > 0) return true;
+    }
+    return false;
+}
+
+// x^k for an integer k (the reference's integer powers), negative k as 1 / x^-k
+template <typename R>
+__device__ __forceinline__ R ipow(R x, int k) {
+    R r = R(1);
+    const int a = k < 0 ? -k : k;
+    for (int q = 0; q < a; ++q) r *= x;
+    return k < 0 ? R(1) / r : r;
 }
 
 // V f and d(V f)/dr of one pair term, smoothing included

@@ -229,6 +229,8 @@ void optimize_charges(pg_context* ctx, int precision, int max_iter, double toler
                 "charge optimisation on the device needs an energy quadratic in the charges (charge_self n <= 2)");
     }
     prepare(ctx);
+    require(!ctx->have_charge_pairs, PG_ERR_UNSUPPORTED,
+            "charge optimisation on the device needs an energy quadratic in the charges (no charge_pair terms)");
     const int n = ctx->n;
     *iterations = 0;
     *error = 0.0;

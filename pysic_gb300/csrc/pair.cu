@@ -107,10 +107,34 @@ __device__ __forceinline__ void pair_body(const PairArgs& A, int blk) {
             }
             const int tj = A.type[j];
             // charge-independent pair terms have zero electronegativity
-            const int2 ix = (wantE || wantF) ? A.index[ti * A.T + tj] : make_int2(0, 0);
+            const int2 ix = (wantE || wantF || (wantC && A.qpair)) ? A.index[ti * A.T + tj] : make_int2(0, 0);
             for (int t = ix.x; t < ix.x + ix.y; ++t) {
                 const PairT<R> P = ((const PairT<R>*)A.terms)[t];
                 if (P.in_bond_kernel || !(r < P.rc)) continue;
+                if (P.kind == 7) {
+                    // charge_pair: eps q1^n1 q2^n2 of the pair's (atom1, atom2) as the
+                    // reference's loop picks them; the exponents follow the unpermuted
+                    // first target (evaluate_energy/electronegativity_charge_pair,
+                    // Potentials.f90:4415-4513).  No r dependence but the smooth cutoff.
+                    const bool first = pick(i, j, A.off[3 * e], A.off[3 * e + 1], A.off[3 * e + 2]);
+                    const R qj = charge_of<R>(A, j);
+                    const R q1 = first ? qi : qj, q2 = first ? qj : qi;
+                    const bool direct = (P.first >> (first ? ti : tj)) & 1ull;
+                    const int n1 = direct ? (int)P.p1 : (int)P.p2, n2 = direct ? (int)P.p2 : (int)P.p1;
+                    R f = R(1), fp = R(0);
+                    if (P.smooth) smooth<R>(r, P.rc, P.rs, f, fp);
+                    const R v = P.p0 * (ipow(q1, n1) * ipow(q2, n2));
+                    U += v * f;
+                    dU += v * fp;
+                    if (wantC) {
+                        const int nm = first ? n1 : n2;  // the exponent of this atom's charge
+                        if (nm > 0)
+                            chi -= (first ? P.p0 * (R(n1) * ipow(q1, n1 - 1) * ipow(q2, n2))
+                                          : P.p0 * (R(n2) * ipow(q1, n1) * ipow(q2, n2 - 1))) * f;
+                    }
+                    continue;
+                }
+                if (!(wantE || wantF)) continue;
                 R V, dV;
                 pair_term<R>(P, r, V, dV, (const R*)A.tab);
                 U += V;
@@ -240,6 +264,7 @@ PairArgs make_pair_args(pg_context* ctx, int precision, int flags, bool first_f,
     A.sterms = ctx->d_single_terms.p;
     A.sindex = ctx->d_single_index.p;
     A.ewald = ctx->ewald ? 1 : 0;
+    A.qpair = ctx->have_charge_pairs ? 1 : 0;
     if (ctx->ewald) {
         const double pi = 3.14159265358979323846;
         A.ew_rc = ctx->ew_rc;

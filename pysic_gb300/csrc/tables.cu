@@ -100,7 +100,7 @@ void fold_tables(pg_context* ctx) {
 
     std::vector<PairT<double>> terms;
     std::vector<int2> index((size_t)T * T, make_int2(0, 0));
-    bool pair_kernel_terms = false;
+    bool pair_kernel_terms = false, charge_pairs = false;
     for (int ti = 0; ti < T; ++ti)
         for (int tj = 0; tj < T; ++tj) {
             int2& ix = index[(size_t)ti * T + tj];
@@ -124,6 +124,7 @@ void fold_tables(pg_context* ctx) {
                     t.p0 = t.p2;  // range
                     t.p1 = t.p3;  // scale
                 }
+                t.first = r < (int)ctx->pr_first.size() ? ctx->pr_first[r] : 0ull;
                 t.rc = ctx->pr_cut[r];
                 const double soft = ctx->pr_soft[r];
                 if (soft > 0.0 && soft < t.rc) {
@@ -133,7 +134,9 @@ void fold_tables(pg_context* ctx) {
                     t.smooth = 0;
                     t.rs = t.rc;
                 }
-                t.in_bond_kernel = bond && (t.group >= 0 || t.rc <= bo_radius);
+                // charge-dependent pair terms stay in the pair kernel (electronegativities)
+                t.in_bond_kernel = bond && t.kind != 7 && (t.group >= 0 || t.rc <= bo_radius);
+                if (t.kind == 7) charge_pairs = true;
                 if (!t.in_bond_kernel) pair_kernel_terms = true;
                 terms.push_back(t);
             }
@@ -157,6 +160,7 @@ void fold_tables(pg_context* ctx) {
     }
     ctx->have_singles = !sterms.empty();
     ctx->have_pair_kernel_terms = pair_kernel_terms;
+    ctx->have_charge_pairs = charge_pairs;
 
     // Single-species Tersoff (one type, one triplet, exponential pair terms that
     // all share the bond-order cutoff): the bond-order kernels take every

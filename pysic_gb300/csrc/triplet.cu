@@ -51,26 +51,6 @@ struct TriArgs {
     const int* skip;
 };
 
-// pick (Core.f90): each pair once -- the higher index, or for one atom and
-// its own image the lexicographically positive offset
-__device__ __forceinline__ bool pick(int i1, int i2, int o0, int o1, int o2) {
-    if (i2 > i1) return true;
-    if (i2 == i1 && o0 >= 0) {
-        if (o0 > 0) return true;
-        if (o1 > 0) return true;
-        if (o1 == 0 && o2 > 0) return true;
-    }
-    return false;
-}
-
-template <typename R>
-__device__ __forceinline__ R ipow(R x, int k) {
-    R r = R(1);
-    const int a = k < 0 ? -k : k;
-    for (int q = 0; q < a; ++q) r *= x;
-    return k < 0 ? R(1) / r : r;
-}
-
 // bond vector of list entry e of atom a (the separation a -> partner)
 template <typename R>
 __device__ __forceinline__ V3<R> entry_vector(const TriArgs& A, int a, int e);

@@ -62,6 +62,8 @@ class Engine:
 
     def set_model(self, model):
         a = model.arrays()
+        first = np.ascontiguousarray(a["pair_first"], dtype=np.uint64)
+        L.check(self.lib.pg_set_pair_first_targets(self.ctx, len(first), L.u64ptr(first)))
         tab = L.as_f64(a["pair_table"])
         L.check(self.lib.pg_set_pair_tables(self.ctx, len(tab) // 2, L.dptr(tab)))
         L.check(self.lib.pg_set_triplet_potentials(

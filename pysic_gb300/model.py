@@ -40,6 +40,7 @@ class Model:
         self.pair_kind = []
         self.pair_params = []
         self.pair_table = []  # tabulated potentials: rows (V, d), concatenated
+        self.pair_first = []  # types of each record's unpermuted first target
         self.pair_cutoff = []
         self.pair_soft = []
         self.pair_mask1 = []
@@ -75,6 +76,7 @@ class Model:
         d["pair_kind"] = np.array(self.pair_kind, dtype=np.int32)
         d["pair_params"] = np.array(self.pair_params, dtype=np.float64).reshape(-1, 4)
         d["pair_table"] = np.array(self.pair_table, dtype=np.float64).reshape(-1)
+        d["pair_first"] = np.array(self.pair_first, dtype=np.uint64)
         d["pair_cutoff"] = np.array(self.pair_cutoff, dtype=np.float64)
         d["pair_soft"] = np.array(self.pair_soft, dtype=np.float64)
         d["pair_mask1"] = np.array(self.pair_mask1, dtype=np.uint64)
@@ -193,21 +195,28 @@ def compile_model(atoms, potentials, coulomb=None):
         params = [float(x) for x in pot.get_parameter_values()]
         grp = group_of(pot)
         targets = []  # (position filters) tuples of (element, tag, index) per position
+        firsts = []   # the unpermuted tuple's first target of each record (original_elements(1))
         for t in pot.get_symbols() or []:
             for perm in _distinct_permutations(t):
                 targets.append([(e, None, None) for e in perm])
+                firsts.append((t[0], None, None))
         for t in pot.get_tags() or []:
             for perm in _distinct_permutations(t):
                 targets.append([(None, int(g), None) for g in perm])
+                firsts.append((None, int(t[0]), None))
         for t in pot.get_indices() or []:
             for perm in _distinct_permutations(t):
                 targets.append([(None, None, int(i)) for i in perm])
+                firsts.append((None, None, int(t[0])))
         if nt == 2:
             if kind not in core.PAIR_KIND:
                 raise InvalidPotentialError("'{0}' is not a pair potential of the GB300 engine".format(kind))
             if kind == "tabulated":
                 params = _table_record(M, params)
-            for tg in targets:
+            if kind == "charge_pair" and grp >= 0:
+                raise InvalidPotentialError("bond-order scaling of charge_pair is not evaluated by the GB300 engine")
+            for tg, first in zip(targets, firsts):
+                M.pair_first.append(_mask(sigs, *first))
                 M.pair_kind.append(core.PAIR_KIND[kind])
                 M.pair_params.append((params + [0.0] * 4)[:4])
                 M.pair_cutoff.append(float(pot.get_cutoff()))

@@ -218,3 +218,48 @@ def test_optimize_falls_back_to_slsqp_for_non_quadratic_energies():
     chi = calc.get_electronegativities()
     assert np.abs(chi - chi.mean()).max() < 1e-3
     assert abs(q.sum()) < 1e-6
+
+
+def _qpair_case():
+    atoms = W.sio2_box(100, seed=26)
+    q = np.where(np.array(atoms.get_chemical_symbols()) == "Si", 0.5, -0.25)
+    atoms.set_initial_charges(q + np.random.default_rng(4).normal(0.0, 0.05, len(q)))
+    pots, coul = W.sio2_potentials(real_cutoff=5.5, sigma=1.6)
+    P = pysic.Potential
+    pots = pots + [P("charge_pair", symbols=[["Si", "O"]], parameters=[0.4, 2, 1], cutoff=3.0, cutoff_margin=0.8),
+                   P("charge_pair", symbols=[["O", "O"]], parameters=[0.3, 1, 1], cutoff=2.8, cutoff_margin=0.5)]
+    return atoms, pots, coul
+
+
+def test_charge_pair_fp64_parity():
+    """charge_pair (Potentials.f90:4415-4513) beside Ewald and charge_self:
+    energy, smooth-cutoff forces, virial and electronegativities."""
+    atoms, pots, coul = _qpair_case()
+    ref = oracle_all(atoms, pots, coul)
+    got = engine_all(atoms, pots, coul, "fp64")
+    assert got["energy"] == pytest.approx(ref["energy"], rel=1e-11)
+    assert np.abs(got["forces"] - ref["forces"]).max() < 1e-9 * max(1.0, np.abs(ref["forces"]).max())
+    np.testing.assert_allclose(got["stress"], ref["stress"], rtol=1e-9, atol=1e-9 * np.abs(ref["stress"]).max())
+    assert np.abs(got["enegs"] - ref["enegs"]).max() < 1e-9
+
+
+def test_charge_pair_mixed_and_relaxation():
+    atoms, pots, coul = _qpair_case()
+    ref = oracle_all(atoms, pots, coul)
+    got = engine_all(atoms, pots, coul, "mixed")
+    assert abs(got["energy"] - ref["energy"]) / len(atoms) <= 1e-5
+    assert np.abs(got["enegs"] - ref["enegs"]).max() < 1e-4
+    # the damped relaxation sees the charge_pair electronegativities
+    params = dict(n_steps=600, timestep=0.05, inertia=1.0, friction=3.0, tolerance=1e-4)
+    calc = pysic.Pysic(atoms.copy(), pots, coulomb=coul, precision="fp64")
+    rel = pysic.ChargeRelaxation("dynamic", calculator=calc,
+                                 parameters=[params[k] for k in ("n_steps", "timestep", "inertia", "friction",
+                                                                 "tolerance")])
+    q_gpu = rel.charge_relaxation()
+    model = compile_model(atoms, pots, coul)
+    r = oracle.relax_charges(atoms.get_positions(), atoms.get_initial_charges(), atoms.get_cell(), atoms.get_pbc(),
+                             model, *oracle_lists(atoms, pots, coul), **params)
+    assert rel.last_steps == r["steps"]
+    np.testing.assert_allclose(q_gpu, r["charges"], atol=1e-8)
+    # not quadratic in the charges: 'optimize' leaves the device solver
+    assert calc.engine.optimize_charges(0, 10, 1e-4) is None

@@ -48,11 +48,17 @@ def test_device_verlet_matches_the_host_loop_with_rebuilds(precision):
     dt, steps = 2.0 * FS, 40
     a_host = _hot_silicon()
     calc_h = pysic.Pysic(a_host, W.tersoff_si_potentials(), precision=precision)
+    # one tile for both contexts: the autotuner times its candidates per
+    # context, and another lanes-per-atom split sums in another order
+    calc_h.set_core()
+    calc_h.engine.set_lanes(4)
     r_h, p_h = _host_verlet(a_host, calc_h, dt, steps)
     rebuilds_host = calc_h.get_neighbor_lists().nupdates
 
     a_dev = _hot_silicon()
     calc_d = pysic.Pysic(a_dev, W.tersoff_si_potentials(), precision=precision)
+    calc_d.set_core()
+    calc_d.engine.set_lanes(4)
     a_dev.set_calculator(calc_d)
     dyn = pysic.VelocityVerlet(a_dev, dt)
     dyn.run(steps)
@@ -66,12 +72,18 @@ def test_device_verlet_matches_the_host_loop_with_rebuilds(precision):
 
 def test_observers_cut_the_run_without_changing_it():
     dt = 2.0 * FS
+    def calc_for(a):
+        c = pysic.Pysic(a, W.tersoff_si_potentials())
+        c.set_core()
+        c.engine.set_lanes(4)
+        return c
+
     a1 = _hot_silicon(seed=5)
-    a1.set_calculator(pysic.Pysic(a1, W.tersoff_si_potentials()))
+    a1.set_calculator(calc_for(a1))
     pysic.VelocityVerlet(a1, dt).run(30)
 
     a2 = _hot_silicon(seed=5)
-    a2.set_calculator(pysic.Pysic(a2, W.tersoff_si_potentials()))
+    a2.set_calculator(calc_for(a2))
     dyn = pysic.VelocityVerlet(a2, dt)
     seen = []
     dyn.attach(lambda: seen.append((dyn.nsteps, a2.get_positions().copy())), interval=7)

@@ -265,3 +265,38 @@ def test_oracle_bond_bend_forces_are_the_energy_gradient():
             p2[a, c] -= h
             num = -(energy(p1) - energy(p2)) / (2 * h)
             assert f[a, c] == pytest.approx(num, abs=2e-5)
+
+
+def test_oracle_charge_pair_derivatives():
+    """charge_pair (Potentials.f90:4415-4513) in the oracle: electronegativities
+    are minus the charge derivatives of the energy and forces minus its position
+    gradient (the smooth cutoff's), with the exponent order of the unpermuted
+    first target."""
+    atoms = W.sio2_box(12, seed=25)
+    q = np.random.default_rng(3).normal(0.0, 0.5, len(atoms))
+    atoms.set_initial_charges(q)
+    P = pysic.Potential
+    pots = [P("charge_pair", symbols=[["Si", "O"]], parameters=[0.4, 2, 1], cutoff=3.0, cutoff_margin=0.8),
+            P("charge_pair", symbols=[["O", "O"]], parameters=[-0.2, 1, 3], cutoff=2.6, cutoff_margin=0.5)]
+    model = compile_model(atoms, pots)
+    lists = oracle_lists(atoms, pots)
+    pos = atoms.get_positions()
+
+    def ev(p, qq, what):
+        return oracle.evaluate(p, qq, atoms.get_cell(), atoms.get_pbc(), model, *lists, what=what)
+
+    chi = ev(pos, q, "enegs")
+    f, _ = ev(pos, q, "forces")
+    assert np.abs(chi).max() > 0.05 and np.abs(f).max() > 0.01
+    h = 1e-6
+    for a in (0, 5, 17, 30):
+        dq = np.zeros(len(q))
+        dq[a] = h
+        num = -(ev(pos, q + dq, "energy") - ev(pos, q - dq, "energy")) / (2 * h)
+        assert chi[a] == pytest.approx(num, abs=1e-6)
+        for c in range(3):
+            p1, p2 = pos.copy(), pos.copy()
+            p1[a, c] += h
+            p2[a, c] -= h
+            numf = -(ev(p1, q, "energy") - ev(p2, q, "energy")) / (2 * h)
+            assert f[a, c] == pytest.approx(numf, abs=1e-6)
