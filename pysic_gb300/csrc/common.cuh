@@ -371,6 +371,7 @@ struct pg_context {
     // charge relaxation
     pg::DevBuf<double> rq_rate, rq_save, rq_stat;
     pg::DevBuf<int> rq_flag;
+    pg::DevBuf<double> chi_k;   // relaxation loops: real-space Ewald kernel per full-list entry (R)
     pg::DevBuf<double> cg_buf;  // charge optimisation: q, r, p, H p, chi(0), partials, scalars
     pg::DevBuf<int> cg_flag;
     pg::DevBuf<double> md_p, md_m;  // dynamics: momenta (n x 3), masses
@@ -490,6 +491,11 @@ void md_set_state(pg_context* ctx, const double* masses, const double* momenta);
 void md_get_state(pg_context* ctx, double* momenta, double* positions);
 void md_run(pg_context* ctx, int precision, int n_steps, double dt, double skin, int* steps_done, int* rebuild);
 void evaluate(pg_context* ctx, int precision, int flags);
+// api.cu: lanes per atom of the pair kernel for this context's list lengths
+int pair_lanes_for(const pg_context* ctx);
+// pair.cu: the fixed real-space Ewald electronegativity matrix of a relaxation loop
+bool chi_cache_prepare(pg_context* ctx, int precision);
+void launch_chi_cache_apply(pg_context* ctx, int precision, const int* skip);
 // triplet.cu: three-body potentials (bond_bend)
 constexpr int PG_MAX_TRIPLET_RECORDS = 64;
 void launch_triplets(pg_context* ctx, int precision, int flags, bool first_f, FxAcc* acc, const int* skip);

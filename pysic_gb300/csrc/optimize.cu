@@ -208,17 +208,14 @@ __global__ void __launch_bounds__(OT) cg_restore(CgArgs A) {
 
 }  // namespace
 
-static void enqueue_chi_on(pg_context* ctx, int precision) {
-    const int G = pair_lanes_for(ctx);
-    launch_pair_kernel_skip(ctx, precision, PG_WANT_ENEGS, true, true, G, nullptr, nullptr);
-    if (ctx->ewald) launch_ewald_kspace_skip(ctx, precision, PG_WANT_ENEGS, true, false, nullptr, nullptr);
-}
-
+// electronegativities of the current charges; the real-space part from the
+// cached matrix of the loop (charge_pair terms are excluded here)
 static void enqueue_chi_skip(pg_context* ctx, int precision, const int* skip) {
-    const int G = pair_lanes_for(ctx);
-    launch_pair_kernel_skip(ctx, precision, PG_WANT_ENEGS, true, true, G, nullptr, skip);
+    launch_chi_cache_apply(ctx, precision, skip);
     if (ctx->ewald) launch_ewald_kspace_skip(ctx, precision, PG_WANT_ENEGS, true, false, nullptr, skip);
 }
+
+static void enqueue_chi_on(pg_context* ctx, int precision) { enqueue_chi_skip(ctx, precision, nullptr); }
 
 void optimize_charges(pg_context* ctx, int precision, int max_iter, double tolerance, double* charges, int* iterations,
                       double* error) {
@@ -264,6 +261,7 @@ void optimize_charges(pg_context* ctx, int precision, int max_iter, double toler
         launch_disp(ctx, nullptr);
         A.disp = ctx->disp32.p;
     }
+    require(chi_cache_prepare(ctx, precision), PG_ERR_UNSUPPORTED, "charge optimisation needs a linear chi");
     // c0 = chi(0)
     cg_begin<<<nb, OT, 0, st>>>(A);
     enqueue_chi_on(ctx, precision);

@@ -136,9 +136,14 @@ __global__ void __launch_bounds__(RT) rx_step(RxArgs A) {
 }  // namespace
 
 // electronegativities of the current charges into ctx->out_chi, stopped by `skip`
-static void enqueue_chi(pg_context* ctx, int precision, const int* skip) {
-    const int G = pair_lanes_for(ctx);
-    launch_pair_kernel_skip(ctx, precision, PG_WANT_ENEGS, true, true, G, nullptr, skip);
+// (the real-space part from the loop's cached matrix when it has one)
+static void enqueue_chi(pg_context* ctx, int precision, const int* skip, bool cached) {
+    if (cached) {
+        launch_chi_cache_apply(ctx, precision, skip);
+    } else {
+        const int G = pair_lanes_for(ctx);
+        launch_pair_kernel_skip(ctx, precision, PG_WANT_ENEGS, true, true, G, nullptr, skip);
+    }
     if (ctx->ewald) launch_ewald_kspace_skip(ctx, precision, PG_WANT_ENEGS, true, false, nullptr, skip);
 }
 
@@ -216,14 +221,15 @@ void relax_charges(pg_context* ctx, int precision, int mode, int n_steps, double
         launch_disp(ctx, nullptr);
         A.disp = ctx->disp32.p;
     }
+    const bool cached = chi_cache_prepare(ctx, precision);
     // initial differences (relaxation.py:433) and the first update; the
     // potentiostat subtracts its fixed potential instead of the mean
-    enqueue_chi(ctx, precision, A.flag);
+    enqueue_chi(ctx, precision, A.flag, cached);
     if (!pstat) rx_mean<<<nb, RT, 0, st>>>(A);
     rx_step<true><<<nb, RT, 0, st>>>(A);
     PG_CHECK_LAUNCH();
     auto one_step = [&] {
-        enqueue_chi(ctx, precision, A.flag);
+        enqueue_chi(ctx, precision, A.flag, cached);
         if (!pstat) rx_mean<<<nb, RT, 0, st>>>(A);
         rx_step<false><<<nb, RT, 0, st>>>(A);
     };
