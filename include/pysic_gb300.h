@@ -119,6 +119,21 @@ int pg_set_single_potentials(pg_context* ctx, int32_t n_records, const int32_t* 
 int pg_set_bond_order_factors(pg_context* ctx, int32_t n_records, const double* params, const double* cutoff,
                               const double* soft, const uint64_t* mask1, const uint64_t* mask2,
                               const uint64_t* mask3, const int32_t* group);
+/* add_bond_order_factor(...) (PyInterface.f90:482-526) for the per-atom
+ * (level-1) factors, one record per target tuple, unpermuted: kind 0 neighbors,
+ * 1 power_bond (params a, n), 2 c_scale (epsilon, N, C, gamma, min),
+ * 3 sqrt_scale (epsilon) (Potentials.f90:5581-5673, 5972-6063, 6223-6436);
+ * params 5 per record; mask2 is unused by the one-target scalers; group: the
+ * Coordinator's group, shared with the pair and single-atom records.  At most 4
+ * such groups; a group cannot also hold Tersoff factors. */
+int pg_set_atom_factors(pg_context* ctx, int32_t n_records, const int32_t* kind, const double* params,
+                        const double* cutoff, const double* soft, const uint64_t* mask1, const uint64_t* mask2,
+                        const int32_t* group);
+/* The Coordinator group of each record set by pg_set_single_potentials (-1:
+ * none), whose per-atom factor scales the term (core_evaluate_local_singlet,
+ * Core.f90:4095-4239); constant and force terms only.  pg_set_single_potentials
+ * resets every group to -1. */
+int pg_set_single_groups(pg_context* ctx, int32_t n_records, const int32_t* group);
 /* set_ewald_parameters(real_cut, k_radius, reciprocal_cut, sigma, epsilon, scaler),
  * PyInterface.f90:1039-1046.  scaler has one entry per atom. */
 int pg_set_ewald(pg_context* ctx, double real_cut, double k_radius, const int32_t* kmax, double sigma,
@@ -212,6 +227,13 @@ int pg_md_get_state(pg_context* ctx, double* momenta, double* positions);
  * energy. */
 int pg_optimize_charges(pg_context* ctx, int32_t precision, int32_t max_iterations, double tolerance,
                         double* charges, int32_t* iterations, double* error);
+
+/* Per-atom bond-order factors of a Coordinator group after an evaluation at the
+ * current positions (core_get_bond_order_factors, Core.f90:759-783, behind
+ * calculate_bond_order_factors, PyInterface.f90): B_i = post(sum), the sum
+ * itself without a scaler; zeros for a group without per-atom factors.
+ * n entries. */
+int pg_get_atom_factors(pg_context* ctx, int32_t precision, int32_t group, double* factors);
 
 /* Per ordered bond (CSR entry of the engine's short list) Tersoff sums zeta_ij of
  * group 0: the quantity core_calculate_pair_bond_order_factor (Core.f90:2439-2637)

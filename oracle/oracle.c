@@ -462,6 +462,9 @@ typedef struct {
     double* maxbr; /* per atom: max_bond_radius, Core.f90:1030-1067 */
     double* smooth_soft;
     int* smoothened;
+    int n_groups;      /* groups with per-atom factors: 0 .. n_groups-1 */
+    double* af_raw;    /* n_groups x n: per-atom bond-order sums */
+    double* af_fac;    /* n_groups x n: post-processed per-atom factors (saved_bond_order_factors) */
 } ctx_t;
 
 static inline int has(uint64_t mask, int t) { return (int)((mask >> t) & 1u); }
@@ -573,6 +576,160 @@ static double post_process(const ctx_t* X, int t, int group, double raw) {
     return tersoff_post(X->m->bond_params + 7 * (size_t)b, raw);
 }
 
+/* ---- per-atom (level-1) bond-order factors ---- */
+
+/* evaluate_bond_order_factor_coordination (Potentials.f90:5631-5645) and
+ * _power (6293-6306): the symmetric two-target factor c(r) */
+static double afac_value(const orc_model* m, int r, double d) {
+    const double* p = m->afac_params + 5 * (size_t)r;
+    const double f = smooth_factor(d, m->afac_cutoff[r], m->afac_soft[r]);
+    if (m->afac_kind[r] == 0) return f;
+    return f * pow(p[0] / d, p[1]);
+}
+
+/* evaluate_bond_order_gradient_coordination (5656-5673) and _power (6317-6347):
+ * g11 = gradient of atom 1's term with respect to atom 1, g12 with respect to atom 2 */
+static void afac_gradient(const orc_model* m, int r, const double sep[3], double d, double g11[3], double g12[3]) {
+    const double* p = m->afac_params + 5 * (size_t)r;
+    const double inv = 1.0 / d;
+    const double dv = smooth_deriv(d, m->afac_cutoff[r], m->afac_soft[r]);
+    double t[3];
+    for (int c = 0; c < 3; ++c) t[c] = sep[c] * inv * dv;
+    if (m->afac_kind[r] == 0) {
+        for (int c = 0; c < 3; ++c) {
+            g11[c] = -t[c];
+            g12[c] = t[c];
+        }
+        return;
+    }
+    const double n = p[1], ratio_n = pow(p[0] * inv, n);
+    const double decay = smooth_factor(d, m->afac_cutoff[r], m->afac_soft[r]);
+    for (int c = 0; c < 3; ++c) {
+        g11[c] = -t[c] * ratio_n + n * decay * ratio_n * inv * inv * sep[c];
+        g12[c] = -g11[c];
+    }
+}
+
+/* first post-processing per-atom factor of the atom's element in the group
+ * (core_post_process_bond_order_factors, Core.f90:2697-2712) */
+static int afac_post_index(const orc_model* m, int t, int group) {
+    for (int r = 0; r < m->n_afac; ++r)
+        if ((m->afac_kind[r] == 2 || m->afac_kind[r] == 3) && has(m->afac_mask1[r], t) && m->afac_group[r] == group)
+            return r;
+    return -1;
+}
+
+/* post_process_bond_order_factor_scaler_1 (Potentials.f90:6021-6035) and _sqrt (6402-6414) */
+static double afac_post(const orc_model* m, int r, double raw) {
+    const double* p = m->afac_params + 5 * (size_t)r;
+    if (m->afac_kind[r] == 3) return raw <= 0.0 ? 0.0 : p[0] * sqrt(raw);
+    const double dN = (raw - p[1]) * p[2];
+    return dN > p[4] ? p[0] * dN / (1.0 + exp(p[3] * dN)) : 0.0;
+}
+
+/* post_process_bond_order_gradient_scaler_1 (6044-6063) and _sqrt (6423-6436), one component */
+static double afac_post_grad(const orc_model* m, int r, double raw, double g) {
+    const double* p = m->afac_params + 5 * (size_t)r;
+    if (m->afac_kind[r] == 3) return raw <= 0.0 ? 0.0 : p[0] / (2.0 * sqrt(raw)) * g;
+    const double dN = (raw - p[1]) * p[2];
+    if (!(dN > p[4])) return 0.0;
+    const double expo = exp(p[3] * dN), inv_exp = 1.0 / (1.0 + expo);
+    return p[0] * p[2] * (inv_exp - dN * inv_exp * inv_exp * p[3] * expo) * g;
+}
+
+/* core_calculate_bond_order_factors (Core.f90:2015-2404), two-target level-1
+ * part: every picked pair adds the factor of each record of atom1's element
+ * (position 1) whose position 2 matches atom2 to both atoms' sums; then
+ * core_post_process_bond_order_factors (2671-2735) */
+static void afac_sums(ctx_t* X) {
+    const orc_system* s = X->s;
+    const orc_model* m = X->m;
+    const orc_nblist* nb = X->nb;
+    const int n = s->n;
+    X->af_raw = (double*)calloc((size_t)X->n_groups * (size_t)(n ? n : 1), sizeof(double));
+    X->af_fac = (double*)calloc((size_t)X->n_groups * (size_t)(n ? n : 1), sizeof(double));
+    for (int g = 0; g < X->n_groups; ++g) {
+        double* raw = X->af_raw + (size_t)g * n;
+        for (int i = 0; i < n; ++i) {
+            const int ti = s->type[i];
+            for (int e = nb->start[i]; e < nb->start[i + 1]; ++e) {
+                const int j = nb->idx[e];
+                const int* o = nb->off + 3 * (size_t)e;
+                if (!pick(i, j, o)) continue;
+                double sep[3];
+                separation(&X->C, s->pos + 3 * (size_t)i, s->pos + 3 * (size_t)j, o, sep);
+                const double d = sqrt(dot3(sep, sep));
+                if (!(d < X->maxbr[i])) continue;
+                const int tj = s->type[j];
+                for (int r = 0; r < m->n_afac; ++r) {
+                    if (m->afac_kind[r] > 1 || !has(m->afac_mask1[r], ti)) continue;
+                    if (m->afac_group[r] != g || !(m->afac_cutoff[r] > d)) continue;
+                    if (!has(m->afac_mask2[r], tj)) continue;
+                    const double c = afac_value(m, r, d);
+                    raw[i] += c;
+                    raw[j] += c;
+                }
+            }
+        }
+        for (int i = 0; i < n; ++i) {
+            const int r = afac_post_index(m, s->type[i], g);
+            X->af_fac[(size_t)g * n + i] = r >= 0 ? afac_post(m, r, raw[i]) : raw[i];
+        }
+    }
+}
+
+static double saved_factor(const ctx_t* X, int group, int i) {
+    return group < X->n_groups ? X->af_fac[(size_t)group * X->s->n + i] : 0.0;
+}
+
+/* core_add_bond_order_forces, Core.f90:4745-4933: -prefactor times the gradient
+ * of atom a's per-atom factor, over all of a's neighbours (no pick) */
+static void afac_forces(const ctx_t* X, int group, int a, double prefactor, double* F, double* stress) {
+    if (group >= X->n_groups) return;
+    const orc_system* s = X->s;
+    const orc_model* m = X->m;
+    const orc_nblist* nb = X->nb;
+    const int ta = s->type[a];
+    const double raw = X->af_raw[(size_t)group * s->n + a];
+    const int post = afac_post_index(m, ta, group);
+    double virial[6] = {0, 0, 0, 0, 0, 0};
+    for (int e = nb->start[a]; e < nb->start[a + 1]; ++e) {
+        const int j = nb->idx[e];
+        double sep[3];
+        separation(&X->C, s->pos + 3 * (size_t)a, s->pos + 3 * (size_t)j, nb->off + 3 * (size_t)e, sep);
+        const double d = sqrt(dot3(sep, sep));
+        if (!(d < X->maxbr[a])) continue;
+        const int tj = s->type[j];
+        for (int r = 0; r < m->n_afac; ++r) {
+            if (!has(m->afac_mask1[r], ta) || m->afac_group[r] != group || !(m->afac_cutoff[r] > d)) continue;
+            if (!has(m->afac_mask2[r], tj) || m->afac_kind[r] > 1) continue;
+            double g11[3], g12[3], n1[3], n2[3];
+            afac_gradient(m, r, sep, d, g11, g12);
+            for (int c = 0; c < 3; ++c) {
+                if (post >= 0) {
+                    n1[c] = -(prefactor * afac_post_grad(m, post, raw, g11[c]));
+                    n2[c] = -(prefactor * afac_post_grad(m, post, raw, g12[c]));
+                } else {
+                    n1[c] = -(prefactor * g11[c]);
+                    n2[c] = -(prefactor * g12[c]);
+                }
+                F[3 * (size_t)a + c] += n1[c];
+                F[3 * (size_t)j + c] += n2[c];
+            }
+            virial[0] += sep[0] * g12[0];
+            virial[1] += sep[1] * g12[1];
+            virial[2] += sep[2] * g12[2];
+            virial[3] += sep[1] * g12[2];
+            virial[4] += sep[0] * g12[2];
+            virial[5] += sep[0] * g12[1];
+        }
+    }
+    for (int c = 0; c < 6; ++c) {
+        const double tv = post >= 0 ? afac_post_grad(m, post, raw, virial[c]) : virial[c];
+        stress[c] = stress[c] - prefactor * tv;
+    }
+}
+
 typedef struct {
     const ctx_t* X;
     int what, a0, a1;
@@ -682,17 +839,32 @@ static void* loop_range(void* arg) {
             if (!has(m->single_mask[r], ti)) continue;
             const double* p = m->single_params + 4 * (size_t)r;
             const int kind = m->single_kind[r];
+            const int grp = m->single_group ? m->single_group[r] : -1;
+            /* the singlet's energy V and electronegativity; with a coordinator,
+               core_evaluate_local_singlet (Core.f90:4095-4239) scales them by the
+               atom's factor and replaces the singlet's own force by -V grad(B_i) */
+            double V = 0.0, E = 0.0, Fs[3] = {0, 0, 0};
             if (kind == 0) { /* charge_self, Potentials.f90:4341-4375 */
                 int n = (int)p[1];
-                if (J->what == 0) J->energy += p[0] * __builtin_powi(qi, n);
-                else if (J->what == 2) chi[i] += -(p[0] * n * __builtin_powi(qi, n - 1));
+                V = p[0] * __builtin_powi(qi, n);
+                E = -(p[0] * n * __builtin_powi(qi, n - 1));
             } else if (kind == 1) { /* constant potential, 3942-3966 */
-                if (J->what == 0) J->energy += p[0];
+                V = p[0];
             } else { /* constant force, 3122-3147: F on the atom, energy -F . position */
                 const double* x = s->pos + 3 * (size_t)i;
-                if (J->what == 0) J->energy += -(p[0] * x[0] + p[1] * x[1] + p[2] * x[2]);
+                V = -(p[0] * x[0] + p[1] * x[1] + p[2] * x[2]);
+                for (int c = 0; c < 3; ++c) Fs[c] = p[c];
+            }
+            if (grp >= 0) {
+                const double B = saved_factor(X, grp, i);
+                if (J->what == 0) J->energy += V * B;
+                else if (J->what == 1) afac_forces(X, grp, i, V, F, st);
+                else chi[i] += E * B;
+            } else {
+                if (J->what == 0) J->energy += V;
                 else if (J->what == 1)
-                    for (int c = 0; c < 3; ++c) F[3 * (size_t)i + c] += p[c];
+                    for (int c = 0; c < 3; ++c) F[3 * (size_t)i + c] += Fs[c];
+                else if (kind == 0) chi[i] += E;
             }
         }
         for (int e = nb->start[i]; e < nb->start[i + 1]; ++e) {
@@ -790,7 +962,8 @@ static void* loop_range(void* arg) {
                     }
                     double cut = sm ? smooth_factor(d, rc, rs) : 1.0;
                     double v = pair_energy(kind, p, rc, d, m->pair_table);
-                    if (grp >= 0) J->energy += v * cut * (0.0 + 0.0 + B1 + B2) * 0.5;
+                    if (grp >= 0)
+                        J->energy += v * cut * (saved_factor(X, grp, i) + saved_factor(X, grp, j) + B1 + B2) * 0.5;
                     else J->energy += v * cut;
                 } else {
                     double v = (grp >= 0 || sm) ? pair_energy(kind, p, rc, d, m->pair_table) : 0.0;
@@ -806,13 +979,15 @@ static void* loop_range(void* arg) {
                         pair_bo_sums(X, i, j, sep, d, grp, sums);
                         B1 = post_process(X, ti, grp, sums[0]);
                         B2 = post_process(X, tj, grp, sums[1]);
+                        afac_forces(X, grp, i, 0.5 * v * cut, F, st);
+                        afac_forces(X, grp, j, 0.5 * v * cut, F, st);
                         pair_bo_forces(X, i, j, 0.5 * v * cut, sep, d, grp, sums, F, st);
                     }
                     double f1[3], p1[3], p2[3];
                     pair_force(kind, p, rc, sep, d, f1, m->pair_table);
                     for (int c = 0; c < 3; ++c) {
                         if (grp >= 0) {
-                            double bsum = (0.0 + 0.0 + B1 + B2) * 0.5;
+                            double bsum = (saved_factor(X, grp, i) + saved_factor(X, grp, j) + B1 + B2) * 0.5;
                             p1[c] = (f1[c] * cut + v * cg[c]) * bsum;
                             p2[c] = (-f1[c] * cut - v * cg[c]) * bsum;
                         } else {
@@ -1122,6 +1297,8 @@ static void setup_ctx(ctx_t* X, const orc_system* s, const orc_model* m, const o
         double mc = 0.0;
         for (int b = 0; b < m->n_bond; ++b)
             if (has(m->bond_mask1[b], s->type[i]) && m->bond_cutoff[b] > mc) mc = m->bond_cutoff[b];
+        for (int r = 0; r < m->n_afac; ++r)
+            if (has(m->afac_mask1[r], s->type[i]) && m->afac_cutoff[r] > mc) mc = m->afac_cutoff[r];
         X->maxbr[i] = mc;
     }
     /* create_potential, Potentials.f90:2382-2388 */
@@ -1136,12 +1313,22 @@ static void setup_ctx(ctx_t* X, const orc_system* s, const orc_model* m, const o
             X->smoothened[r] = 0;
         }
     }
+    /* core_fill_bond_order_storage (Core.f90:553-571): the per-atom factors of
+       every group, once per evaluation */
+    X->n_groups = 0;
+    for (int r = 0; r < m->n_afac; ++r)
+        if (m->afac_group[r] + 1 > X->n_groups) X->n_groups = m->afac_group[r] + 1;
+    X->af_raw = NULL;
+    X->af_fac = NULL;
+    if (X->n_groups > 0) afac_sums(X);
 }
 
 static void free_ctx(ctx_t* X) {
     free(X->maxbr);
     free(X->smooth_soft);
     free(X->smoothened);
+    free(X->af_raw);
+    free(X->af_fac);
 }
 
 /* core_calculate_energy / forces / electronegativities, Core.f90:7910-7979,
@@ -1227,6 +1414,18 @@ int orc_bond_zeta(const orc_system* s, const orc_model* m, const orc_nblist* nb,
             pair_bo_sums(&X, i, j, sep, d, group, sums);
             zeta[e] = sums[0];
         }
+    free_ctx(&X);
+    return 0;
+}
+
+int orc_atom_factors(const orc_system* s, const orc_model* m, const orc_nblist* nb, int group, double* raw,
+                     double* factor) {
+    ctx_t X;
+    setup_ctx(&X, s, m, nb);
+    for (int i = 0; i < s->n; ++i) {
+        raw[i] = group < X.n_groups ? X.af_raw[(size_t)group * s->n + i] : 0.0;
+        factor[i] = saved_factor(&X, group, i);
+    }
     free_ctx(&X);
     return 0;
 }

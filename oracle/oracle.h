@@ -78,6 +78,19 @@ typedef struct {
     const uint64_t* tri_mask3;
     const uint64_t* tri_center;   /* types that may be the middle atom */
     const uint64_t* pair_first;   /* per pair record: types of the unpermuted first target */
+    /* per-atom (level-1) bond-order factors, one record per target tuple,
+       unpermuted (calculator.py:1372-1430); they share the group numbering of
+       pair_group / bond_group */
+    int32_t n_afac;
+    const int32_t* afac_kind;     /* 0 neighbors, 1 power_bond, 2 c_scale, 3 sqrt_scale */
+    const double* afac_params;    /* 5 per record: power_bond (a, n); c_scale (epsilon, N, C, gamma, min);
+                                     sqrt_scale (epsilon) */
+    const double* afac_cutoff;
+    const double* afac_soft;
+    const uint64_t* afac_mask1;
+    const uint64_t* afac_mask2;   /* 0 for the one-target scalers */
+    const int32_t* afac_group;
+    const int32_t* single_group;  /* per single record: -1 or the group of its coordinator (null: all -1) */
 } orc_model;
 
 /* CSR neighbour list: entries of atom i are [start[i], start[i+1]). */
@@ -100,6 +113,11 @@ int orc_evaluate(const orc_system* sys, const orc_model* model, const orc_nblist
 
 /* Per ordered pair bond-order sums for group g: for entry e of atom i's list, zeta of (i -> j).
  * Helper used to validate the per-bond factors of the GPU path. */
+/* Per-atom bond-order sums and factors of group g (core_calculate_bond_order_factors,
+ * Core.f90:2015-2404, and core_post_process_bond_order_factors, 2671-2735): raw[n], factor[n]. */
+int orc_atom_factors(const orc_system* sys, const orc_model* model, const orc_nblist* nb,
+                     int group, double* raw, double* factor);
+
 int orc_bond_zeta(const orc_system* sys, const orc_model* model, const orc_nblist* nb,
                   int group, double* zeta_per_entry);
 

@@ -38,7 +38,9 @@ class _Model(ctypes.Structure):
                 ("ewald_kmax", ctypes.c_int32 * 3), ("ewald_scaler", _dp), ("pair_table", _dp),
                 ("n_table_rows", ctypes.c_int64), ("n_tri", ctypes.c_int32), ("tri_kind", _ip), ("tri_params", _dp),
                 ("tri_cutoff", _dp), ("tri_soft", _dp), ("tri_mask1", _up), ("tri_mask2", _up), ("tri_mask3", _up),
-                ("tri_center", _up), ("pair_first", _up)]
+                ("tri_center", _up), ("pair_first", _up), ("n_afac", ctypes.c_int32), ("afac_kind", _ip),
+                ("afac_params", _dp), ("afac_cutoff", _dp), ("afac_soft", _dp), ("afac_mask1", _up),
+                ("afac_mask2", _up), ("afac_group", _ip), ("single_group", _ip)]
 
 
 class _NbList(ctypes.Structure):
@@ -151,6 +153,15 @@ def _model(keep, M, n):
     m.single_kind = _i(keep.i32(a["single_kind"]))
     m.single_params = _d(keep.f64(a["single_params"]))
     m.single_mask = _u(keep.u64(a["single_mask"]))
+    m.single_group = _i(keep.i32(a["single_group"]))
+    m.n_afac = len(a["afac_kind"])
+    m.afac_kind = _i(keep.i32(a["afac_kind"]))
+    m.afac_params = _d(keep.f64(a["afac_params"]))
+    m.afac_cutoff = _d(keep.f64(a["afac_cutoff"]))
+    m.afac_soft = _d(keep.f64(a["afac_soft"]))
+    m.afac_mask1 = _u(keep.u64(a["afac_mask1"]))
+    m.afac_mask2 = _u(keep.u64(a["afac_mask2"]))
+    m.afac_group = _i(keep.i32(a["afac_group"]))
     m.n_bond = len(a["bond_cutoff"])
     m.bond_params = _d(keep.f64(a["bond_params"]))
     m.bond_cutoff = _d(keep.f64(a["bond_cutoff"]))
@@ -221,6 +232,18 @@ def evaluate(positions, charges, cell, pbc, model, counts, idx, off, what="energ
     if what == "forces":
         return f[:s.n], st
     return c[:s.n]
+
+
+def atom_factors(positions, cell, pbc, model, counts, idx, off, group=0):
+    """Per-atom bond-order sums and factors of one Coordinator group."""
+    keep = _Keep()
+    s = _system(keep, positions, None, model.types, cell, pbc)
+    m = _model(keep, model, s.n)
+    nb = _nblist(keep, counts, idx, off)
+    raw = np.zeros(max(s.n, 1))
+    fac = np.zeros(max(s.n, 1))
+    lib().orc_atom_factors(ctypes.byref(s), ctypes.byref(m), ctypes.byref(nb), int(group), _d(raw), _d(fac))
+    return raw[:s.n], fac[:s.n]
 
 
 def bond_zeta(positions, cell, pbc, model, counts, idx, off, group=0):

@@ -55,6 +55,10 @@ _SIGNATURES = {
     "pg_set_triplet_potentials": (ctypes.c_int, [_ctx, ctypes.c_int32, _c_int_p, _c_double_p, _c_double_p,
                                                  _c_double_p, _c_u64_p, _c_u64_p, _c_u64_p, _c_u64_p]),
     "pg_set_single_potentials": (ctypes.c_int, [_ctx, ctypes.c_int32, _c_int_p, _c_double_p, _c_u64_p]),
+    "pg_set_single_groups": (ctypes.c_int, [_ctx, ctypes.c_int32, _c_int_p]),
+    "pg_get_atom_factors": (ctypes.c_int, [_ctx, ctypes.c_int32, ctypes.c_int32, _c_double_p]),
+    "pg_set_atom_factors": (ctypes.c_int, [_ctx, ctypes.c_int32, _c_int_p, _c_double_p, _c_double_p, _c_double_p,
+                                           _c_u64_p, _c_u64_p, _c_int_p]),
     "pg_set_bond_order_factors": (ctypes.c_int, [_ctx, ctypes.c_int32, _c_double_p, _c_double_p, _c_double_p,
                                                  _c_u64_p, _c_u64_p, _c_u64_p, _c_int_p]),
     "pg_set_ewald": (ctypes.c_int, [_ctx, ctypes.c_double, ctypes.c_double, _c_int_p, ctypes.c_double,

@@ -18,7 +18,7 @@ import numpy as np
 from . import _lib as L
 from .engine import Engine
 from .error import EngineError, InvalidPotentialError, MissingAtomsError, warn
-from .interactions import CoulombSummation, Potential  # noqa: F401  (re-exported API)
+from .interactions import CompoundPotential, CoulombSummation, Potential  # noqa: F401  (re-exported API)
 from .model import compile_model, individual_cutoffs
 
 
@@ -232,13 +232,19 @@ class Pysic:
 
     def add_potential(self, potential):
         for p in (potential if isinstance(potential, list) else [potential]):
-            if hasattr(p, "build") and not isinstance(p, Potential):
+            if isinstance(p, CompoundPotential):
                 p.build(self)
             else:
                 self.potentials.append(p)
+                # Coordinator queries (calculate_bond_order_factors) go to this calculator
+                if p.get_coordinator() is not None:
+                    p.get_coordinator()._calculator = self
         self._invalidate()
 
     def remove_potential(self, potential):
+        if isinstance(potential, CompoundPotential):
+            potential.remove(self)
+            return
         pots = list(self.potentials)
         pots.remove(potential)
         self.set_potentials(pots)

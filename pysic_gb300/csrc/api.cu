@@ -143,7 +143,7 @@ void enqueue_evaluation(pg_context* ctx, int precision, int flags, int G, const 
     ctx->out_f.resize(3 * (size_t)std::max(n, 1));
     ctx->out_chi.resize((size_t)std::max(n, 1));
     ctx->out_acc.resize(8);
-    const bool run_pair = ctx->have_pair_kernel_terms || ctx->ewald || ctx->have_singles;
+    const bool run_pair = ctx->have_pair_kernel_terms || ctx->ewald || ctx->have_singles || ctx->n_agroups > 0;
     const bool run_bond = ctx->have_bond_terms && (wantE || wantF);
     const bool run_tri = ctx->have_triplets && (wantE || wantF);
     const int Gp = pair_lanes_for(ctx);
@@ -157,10 +157,17 @@ void enqueue_evaluation(pg_context* ctx, int precision, int flags, int G, const 
     // mixed path's displacement pass does it on the way)
     if (precision == PG_PREC_MIXED && (run_pair || run_bond || run_tri)) launch_disp(ctx, skip, acc);
     else PG_CUDA(cudaMemsetAsync(acc, 0, sizeof(FxAcc) * 8, ctx->stream));
+    // per-atom bond-order factors: B and dB/dsum before the terms they scale
+    const bool run_af = ctx->n_agroups > 0 && (wantE || wantF);
+    if (run_af) launch_atom_factors(ctx, precision, 0, false, nullptr, skip);
     if (run_pair) {
         launch_pair_kernel_skip(ctx, precision, flags, first_f, first_chi, Gp, acc, skip);
         if (wantF) first_f = false;
         if (wantC) first_chi = false;
+    }
+    if (run_af && wantF) {
+        launch_atom_factors(ctx, precision, 1, first_f, acc, skip);
+        first_f = false;
     }
     mark(1);
     if (run_bond) {
@@ -469,6 +476,40 @@ int pg_set_single_potentials(pg_context* ctx, int32_t n, const int32_t* kind, co
         ctx->sr_kind.assign(kind, kind + n);
         ctx->sr_params.assign(params, params + 4 * (size_t)n);
         ctx->sr_m.assign(mask, mask + n);
+        ctx->sr_group.assign((size_t)n, -1);
+        ctx->tables_dirty = true;
+    });
+}
+
+int pg_set_single_groups(pg_context* ctx, int32_t n, const int32_t* group) {
+    return guarded([&] {
+        check_ctx(ctx);
+        pg::require(n == (int)ctx->sr_kind.size() && (n == 0 || group != nullptr), PG_ERR_INVALID,
+                    "one group per single-atom record");
+        ctx->sr_group.assign(group, group + n);
+        ctx->tables_dirty = true;
+    });
+}
+
+int pg_set_atom_factors(pg_context* ctx, int32_t n, const int32_t* kind, const double* params, const double* cutoff,
+                        const double* soft, const uint64_t* mask1, const uint64_t* mask2, const int32_t* group) {
+    return guarded([&] {
+        check_ctx(ctx);
+        pg::require(n >= 0, PG_ERR_INVALID, "negative record count");
+        pg::require(n == 0 || (kind && params && cutoff && soft && mask1 && mask2 && group), PG_ERR_INVALID,
+                    "null record arrays");
+        for (int r = 0; r < n; ++r) {
+            pg::require(kind[r] >= 0 && kind[r] <= 3, PG_ERR_UNSUPPORTED, "unknown per-atom bond-order factor kind");
+            pg::require(std::isfinite(cutoff[r]) && std::isfinite(soft[r]) && group[r] >= 0, PG_ERR_INVALID,
+                        "invalid per-atom bond-order factor record");
+        }
+        ctx->af_kind.assign(kind, kind + n);
+        ctx->af_params.assign(params, params + 5 * (size_t)n);
+        ctx->af_cut.assign(cutoff, cutoff + n);
+        ctx->af_soft.assign(soft, soft + n);
+        ctx->af_m1.assign(mask1, mask1 + n);
+        ctx->af_m2.assign(mask2, mask2 + n);
+        ctx->af_group.assign(group, group + n);
         ctx->tables_dirty = true;
     });
 }
@@ -586,6 +627,33 @@ int pg_calculate(pg_context* ctx, int32_t precision, int32_t flags, double* ener
         use_device(ctx);
         pg::evaluate(ctx, precision, flags);
         pg::copy_results(ctx, flags, energy, forces, stress, enegs);
+    });
+}
+
+int pg_get_atom_factors(pg_context* ctx, int32_t precision, int32_t group, double* factors) {
+    return guarded([&] {
+        check_ctx(ctx);
+        use_device(ctx);
+        pg::require(factors != nullptr, PG_ERR_INVALID, "null output");
+        pg::evaluate(ctx, precision, PG_WANT_ENERGY);  // runs the factor pass of every group
+        const int n = ctx->n;
+        auto it = ctx->agroup_of.find(group);
+        if (it == ctx->agroup_of.end() || n == 0) {  // no per-atom factors in the group: zeros, as the reference
+            std::fill(factors, factors + n, 0.0);
+            return;
+        }
+        const size_t o = (size_t)it->second * (size_t)n;
+        if (precision == PG_PREC_FP64) {
+            PG_CUDA(cudaMemcpyAsync(factors, ctx->af_B.p + o, sizeof(double) * n, cudaMemcpyDeviceToHost,
+                                    ctx->stream));
+        } else {
+            std::vector<float> tmp((size_t)n);
+            PG_CUDA(cudaMemcpyAsync(tmp.data(), (const float*)ctx->af_B.p + o, sizeof(float) * n,
+                                    cudaMemcpyDeviceToHost, ctx->stream));
+            PG_CUDA(cudaStreamSynchronize(ctx->stream));
+            for (int i = 0; i < n; ++i) factors[i] = tmp[(size_t)i];
+        }
+        PG_CUDA(cudaStreamSynchronize(ctx->stream));
     });
 }
 

@@ -31,6 +31,14 @@ struct PairArgs {
     const int* skip;  // optional device flag: nonzero = do nothing
     const F4* sep0;   // mixed path: bond vectors at list build
     const F4* disp;   // mixed path: displacements since the build (xyz) and FP32 charge (w)
+    // per-atom (level-1) bond-order factors
+    int ng;                // groups (0: none)
+    const void* af;        // AfT<R>
+    const int2* af_index;  // per (atom1 type, atom2 type)
+    const void* af_post;   // AfPostT<R> per (group, type)
+    void* afB;             // per (group, atom), R: factor
+    void* afS;             // dB/dsum
+    void* afW;             // prefactor times dB/dsum (written by the pair kernel)
 };
 
 template <typename R>
@@ -99,6 +107,7 @@ PairArgs make_pair_args(pg_context* ctx, int precision, int flags, bool first_f,
                         const int* skip);
 BondArgs make_bond_args(pg_context* ctx, int precision, int flags, bool first_f, FxAcc* acc);
 DispArgs make_disp_args(pg_context* ctx, F4* d, const int* skip, FxAcc* zero8);
+void set_atom_factor_args(pg_context* ctx, int precision, PairArgs& A);  // atomfactor.cu
 void prepare_bond_scratch(pg_context* ctx, int precision);
 int pair_atoms_per_block(int n, int G);
 

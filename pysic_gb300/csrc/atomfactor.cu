@@ -1,0 +1,320 @@
+// atomfactor.cu -- per-atom (level-1) bond-order factors: neighbors,
+// power_bond, c_scale, sqrt_scale.
+//
+// Replaces, for Coordinators of per-atom factors, core_calculate_bond_order_
+// factors (Core.f90:2015-2404, the two-target level-1 part),
+// core_post_process_bond_order_factors (2671-2735) and
+// core_add_bond_order_forces (4745-4933), as the singlet and doublet loops use
+// them (core_evaluate_local_singlet, 4095-4239; core_evaluate_local_doublet_
+// energy_B / _forces_B, 4257-4385, 5371-5606).
+//
+// In the reference an atom's raw sum b_i collects, over the pairs the loop
+// picks (pick, Geometry.f90:648-676), the factor c(r) of every record whose
+// position 1 holds atom1's element and position 2 atom2's, added to both
+// atoms; B_i = post(b_i) with the first scaler of the atom's element in the
+// group.  A term scaled by the group multiplies its energy by B_i (single-atom)
+// or (B_i + B_j)/2 (pair), and its prefactor P_i (the singlet's V, or half of
+// each pair's V f) multiplies -grad B_i, taken over all of atom i's neighbours
+// (no pick) with the records of atom i's element at position 1.
+//
+// Three launches, one group of G lanes per atom, every result a gather:
+//   af_sum     b_i over i's full list (the pick decides which atom is atom1,
+//              so which records apply), B_i and S_i = dB/db at b_i
+//   pair       (pair.cu) the scaled energies and forces, and W_i = S_i P_i
+//   af_force   F_k = sum_j c'(r_kj) u_kj [W_k (records k, j) + W_j (records
+//              j, k)], u_kj the unit vector from k to j; virial of atom k's
+//              own terms, sep (x) (-W_k c' u) as the reference sums it
+// No atomics; with a fixed tile the results are bit-reproducible.
+#include <algorithm>
+#include <map>
+#include <vector>
+
+#include "args.cuh"
+#include "common.cuh"
+#include "kernels.cuh"
+#include "pairvec.cuh"
+
+namespace pg {
+
+namespace {
+
+template <typename R>
+__device__ __forceinline__ void add_at(R (&a)[PG_MAX_AGROUPS], int g, R v) {
+#pragma unroll
+    for (int q = 0; q < PG_MAX_AGROUPS; ++q)
+        if (q == g) a[q] += v;
+}
+
+// c(r) and dc/dr of a two-target record (evaluate_bond_order_factor_ /
+// _gradient_coordination, Potentials.f90:5631-5673; _power, 6293-6347)
+template <typename R>
+__device__ __forceinline__ void af_term(const AfT<R>& F, R r, R& c, R& dc) {
+    R f, fp;
+    smooth<R>(r, F.rc, F.rs, f, fp);
+    if (F.kind == 0) {
+        c = f;
+        dc = fp;
+        return;
+    }
+    const R rn = pow_(F.a / r, F.n);
+    c = f * rn;
+    dc = rn * (fp - F.n * f / r);
+}
+
+template <typename R, int G>
+__global__ void __launch_bounds__(256) af_sum(const __grid_constant__ PairArgs A) {
+    if (A.skip && *A.skip) return;
+    const int lane = threadIdx.x % G;
+    const int i = blockIdx.x * (blockDim.x / G) + threadIdx.x / G;
+    const bool act = i < A.n;
+    R b[PG_MAX_AGROUPS] = {};
+    int ti = 0;
+    if (act) {
+        ti = A.type[i];
+        double xi = 0, yi = 0, zi = 0;
+        if constexpr (sizeof(R) == 8) {
+            xi = A.pos[3 * i];
+            yi = A.pos[3 * i + 1];
+            zi = A.pos[3 * i + 2];
+        }
+        const AfT<R>* recs = (const AfT<R>*)A.af;
+        for (int e = A.start[i] + lane; e < A.start[i + 1]; e += G) {
+            const int j = A.idx[e];
+            R x, y, z;
+            pair_vector<R>(A, i, e, xi, yi, zi, x, y, z);
+            const R r = sqrt_(x * x + y * y + z * z);
+            if (r == R(0)) continue;
+            const int tj = A.type[j];
+            // the reference visits the pair once, from the atom pick makes atom1
+            const bool first = pick(i, j, A.off[3 * e], A.off[3 * e + 1], A.off[3 * e + 2]);
+            const int2 ix = A.af_index[first ? ti * A.T + tj : tj * A.T + ti];
+            for (int t = ix.x; t < ix.x + ix.y; ++t) {
+                const AfT<R> F = recs[t];
+                if (!(r < F.rc)) continue;
+                R c, dc;
+                af_term<R>(F, r, c, dc);
+                add_at<R>(b, F.group, c);
+            }
+        }
+    }
+    R* Bv = (R*)A.afB;
+    R* Sv = (R*)A.afS;
+    const AfPostT<R>* post = (const AfPostT<R>*)A.af_post;
+#pragma unroll
+    for (int g = 0; g < PG_MAX_AGROUPS; ++g) {
+        if (g >= A.ng) break;
+        const auto s = group_sum_f<G>(b[g]);
+        if (!(act && lane == 0)) continue;
+        const R raw = (R)s.d();
+        const AfPostT<R> P = post[g * A.T + ti];
+        R B, S;
+        if (P.kind == 3) {  // sqrt_scale: epsilon sqrt(b), 0 for b <= 0
+            if (raw <= R(0)) {
+                B = R(0);
+                S = R(0);
+            } else {
+                const R sq = sqrt_(raw);
+                B = P.p[0] * sq;
+                S = P.p[0] / (R(2) * sq);
+            }
+        } else if (P.kind == 2) {  // c_scale: epsilon dN / (1 + exp(gamma dN)), dN = C (b - N) > min
+            const R dN = (raw - P.p[1]) * P.p[2];
+            if (dN > P.p[4]) {
+                const R ex = exp_(P.p[3] * dN), ie = R(1) / (R(1) + ex);
+                B = P.p[0] * dN * ie;
+                S = P.p[0] * P.p[2] * (ie - dN * ie * ie * P.p[3] * ex);
+            } else {
+                B = R(0);
+                S = R(0);
+            }
+        } else {
+            B = raw;
+            S = R(1);
+        }
+        Bv[(size_t)g * A.n + i] = B;
+        Sv[(size_t)g * A.n + i] = S;
+    }
+}
+
+template <typename R, int G>
+__global__ void __launch_bounds__(256) af_force(const __grid_constant__ PairArgs A) {
+    __shared__ Fx128 wsum[256 / 32][7];
+    __shared__ unsigned done;
+    if (threadIdx.x == 0) done = 0u;
+    __syncthreads();
+    if (A.skip && *A.skip) return;
+    const int lane = threadIdx.x % G;
+    const int k = blockIdx.x * (blockDim.x / G) + threadIdx.x / G;
+    const bool act = k < A.n;
+    const R* W = (const R*)A.afW;
+    R fx = 0, fy = 0, fz = 0;
+    R w0 = 0, w1 = 0, w2 = 0, w3 = 0, w4 = 0, w5 = 0;
+    if (act) {
+        const int tk = A.type[k];
+        R wk[PG_MAX_AGROUPS] = {};
+#pragma unroll
+        for (int g = 0; g < PG_MAX_AGROUPS; ++g)
+            if (g < A.ng) wk[g] = W[(size_t)g * A.n + k];
+        double xk = 0, yk = 0, zk = 0;
+        if constexpr (sizeof(R) == 8) {
+            xk = A.pos[3 * k];
+            yk = A.pos[3 * k + 1];
+            zk = A.pos[3 * k + 2];
+        }
+        const AfT<R>* recs = (const AfT<R>*)A.af;
+        for (int e = A.start[k] + lane; e < A.start[k + 1]; e += G) {
+            const int j = A.idx[e];
+            R x, y, z;
+            pair_vector<R>(A, k, e, xk, yk, zk, x, y, z);
+            const R r = sqrt_(x * x + y * y + z * z);
+            if (r == R(0)) continue;
+            const int tj = A.type[j];
+            R own = 0, other = 0;
+            const int2 io = A.af_index[tk * A.T + tj];  // k's factor: k at position 1
+            for (int t = io.x; t < io.x + io.y; ++t) {
+                const AfT<R> F = recs[t];
+                if (!(r < F.rc)) continue;
+                R c, dc;
+                af_term<R>(F, r, c, dc);
+                R wg = 0;
+#pragma unroll
+                for (int q = 0; q < PG_MAX_AGROUPS; ++q)
+                    if (q == F.group) wg = wk[q];
+                own += dc * wg;
+            }
+            const int2 ir2 = A.af_index[tj * A.T + tk];  // j's factor: j at position 1
+            for (int t = ir2.x; t < ir2.x + ir2.y; ++t) {
+                const AfT<R> F = recs[t];
+                if (!(r < F.rc)) continue;
+                R c, dc;
+                af_term<R>(F, r, c, dc);
+                other += dc * W[(size_t)F.group * A.n + j];
+            }
+            const R ir = R(1) / r;
+            const R cf = (own + other) * ir;
+            fx += cf * x;
+            fy += cf * y;
+            fz += cf * z;
+            const R h = -own * ir;
+            w0 += h * x * x;
+            w1 += h * y * y;
+            w2 += h * z * z;
+            w3 += h * y * z;
+            w4 += h * x * z;
+            w5 += h * x * y;
+        }
+    }
+    auto sfx = group_sum_f<G>(fx), sfy = group_sum_f<G>(fy), sfz = group_sum_f<G>(fz);
+    if (act && lane == 0) {
+        store_sum(A.out_f + 3 * k, sfx, A.first_f);
+        store_sum(A.out_f + 3 * k + 1, sfy, A.first_f);
+        store_sum(A.out_f + 3 * k + 2, sfz, A.first_f);
+    }
+    if (A.acc) {
+        const Fx128 v[7] = {fx_zero(), warp_total(w0), warp_total(w1), warp_total(w2),
+                            warp_total(w3), warp_total(w4), warp_total(w5)};
+        block_totals_publish(v, wsum, &done, A.acc);
+    }
+}
+
+}  // namespace
+
+// Fold the per-atom factor records into per-(atom1 type, atom2 type) lists and
+// per-(group, type) scalers.  gmap: coordinator group id -> level-1 index.
+void fold_atom_factors(pg_context* ctx, const std::map<int, int>& gmap) {
+    const int T = std::max(ctx->n_types, 1);
+    const int nr = (int)ctx->af_kind.size();
+    auto has = [](uint64_t m, int t) { return ((m >> t) & 1ull) != 0; };
+    std::vector<AfT<double>> recs;
+    std::vector<int2> index((size_t)T * T, make_int2(0, 0));
+    for (int ta = 0; ta < T; ++ta)
+        for (int tb = 0; tb < T; ++tb) {
+            int2& ix = index[(size_t)ta * T + tb];
+            ix.x = (int)recs.size();
+            for (int r = 0; r < nr; ++r) {
+                if (ctx->af_kind[r] > 1 || !has(ctx->af_m1[r], ta) || !has(ctx->af_m2[r], tb)) continue;
+                const double* p = &ctx->af_params[5 * (size_t)r];
+                AfT<double> F{};
+                F.kind = ctx->af_kind[r];
+                F.group = gmap.at(ctx->af_group[r]);
+                F.rc = ctx->af_cut[r];
+                // smoothening_factor with soft = cutoff - margin; evaluated below the cutoff only
+                F.rs = std::min(ctx->af_soft[r], ctx->af_cut[r]);
+                F.a = p[0];
+                F.n = p[1];
+                recs.push_back(F);
+            }
+            ix.y = (int)recs.size() - ix.x;
+        }
+    const int ng = std::max(ctx->n_agroups, 1);
+    std::vector<AfPostT<double>> post((size_t)ng * T);
+    for (auto& q : post) q = AfPostT<double>{-1, {0, 0, 0, 0, 0}};
+    for (int t = 0; t < T; ++t)
+        for (int r = 0; r < nr; ++r) {
+            if (ctx->af_kind[r] < 2 || !has(ctx->af_m1[r], t)) continue;
+            AfPostT<double>& q = post[(size_t)gmap.at(ctx->af_group[r]) * T + t];
+            if (q.kind >= 0) continue;  // the first scaler of the element in the group
+            q.kind = ctx->af_kind[r];
+            for (int c = 0; c < 5; ++c) q.p[c] = ctx->af_params[5 * (size_t)r + c];
+        }
+    if (recs.empty()) recs.push_back(AfT<double>{});
+    std::vector<AfT<float>> recs32(recs.size());
+    for (size_t q = 0; q < recs.size(); ++q)
+        recs32[q] = AfT<float>{recs[q].kind, recs[q].group, (float)recs[q].rc, (float)recs[q].rs, (float)recs[q].a,
+                               (float)recs[q].n};
+    std::vector<AfPostT<float>> post32(post.size());
+    for (size_t q = 0; q < post.size(); ++q) {
+        post32[q].kind = post[q].kind;
+        for (int c = 0; c < 5; ++c) post32[q].p[c] = (float)post[q].p[c];
+    }
+    cudaStream_t st = ctx->stream;
+    ctx->d_af.upload(recs.data(), recs.size(), st);
+    ctx->d_af32.upload(recs32.data(), recs32.size(), st);
+    ctx->d_af_index.upload(index.data(), index.size(), st);
+    ctx->d_af_post.upload(post.data(), post.size(), st);
+    ctx->d_af_post32.upload(post32.data(), post32.size(), st);
+}
+
+void set_atom_factor_args(pg_context* ctx, int precision, PairArgs& A) {
+    A.ng = ctx->n_agroups;
+    if (A.ng == 0) return;
+    const size_t m = (size_t)ctx->n_agroups * (size_t)std::max(ctx->n, 1);
+    ctx->af_B.resize(m);
+    ctx->af_S.resize(m);
+    ctx->af_W.resize(m);
+    A.af = precision == PG_PREC_FP64 ? (const void*)ctx->d_af.p : (const void*)ctx->d_af32.p;
+    A.af_index = ctx->d_af_index.p;
+    A.af_post = precision == PG_PREC_FP64 ? (const void*)ctx->d_af_post.p : (const void*)ctx->d_af_post32.p;
+    A.afB = ctx->af_B.p;
+    A.afS = ctx->af_S.p;
+    A.afW = ctx->af_W.p;
+}
+
+// stage 0: the sums and factors (before the pair kernel); stage 1: the forces
+// (after it, adding to out_f)
+void launch_atom_factors(pg_context* ctx, int precision, int stage, bool first_f, FxAcc* acc, const int* skip) {
+    const int G = pair_lanes_for(ctx);
+    PairArgs A = make_pair_args(ctx, precision, PG_WANT_FORCES, first_f, true, acc, skip);
+    const int nbk = pair_kernel_blocks(ctx->n, G), threads = pair_atoms_per_block(ctx->n, G) * G;
+    cudaStream_t st = ctx->stream;
+#define PG_AF_LAUNCH(K_, R_, G_) K_<R_, G_><<<nbk, threads, 0, st>>>(A)
+#define PG_AF_G(K_, R_)                   \
+    do {                                  \
+        if (G == 8) PG_AF_LAUNCH(K_, R_, 8);  \
+        else if (G == 16) PG_AF_LAUNCH(K_, R_, 16); \
+        else PG_AF_LAUNCH(K_, R_, 32);    \
+    } while (0)
+    if (stage == 0) {
+        if (precision == PG_PREC_FP64) PG_AF_G(af_sum, double);
+        else PG_AF_G(af_sum, float);
+    } else {
+        if (precision == PG_PREC_FP64) PG_AF_G(af_force, double);
+        else PG_AF_G(af_force, float);
+    }
+#undef PG_AF_G
+#undef PG_AF_LAUNCH
+    PG_CHECK_LAUNCH();
+    ctx->launches++;
+}
+
+}  // namespace pg

@@ -67,9 +67,9 @@ void size_buffers(pg_batch* b, int precision) {
     for (pg_context* c : b->sys) {
         require(c->device == b->device, PG_ERR_INVALID, "every system of a batch must live on the batch's device");
         prepare(c);
-        require(!c->ewald && !c->have_triplets, PG_ERR_UNSUPPORTED,
-                "the many-system launch covers pair and bond-order terms; evaluate Ewald or three-body systems one "
-                "by one");
+        require(!c->ewald && !c->have_triplets && c->n_agroups == 0, PG_ERR_UNSUPPORTED,
+                "the many-system launch covers pair and Tersoff bond-order terms; evaluate Ewald, three-body or "
+                "per-atom bond-order systems one by one");
         const size_t n = (size_t)std::max(c->n, 1);
         c->out_f.resize(3 * n);
         c->out_chi.resize(n);

@@ -9,6 +9,7 @@
 #include <utility>
 #include <stdexcept>
 #include <string>
+#include <map>
 #include <vector>
 
 #include "../../include/pysic_gb300.h"
@@ -134,6 +135,29 @@ struct PairT {
     R p0, p1, p2, p3, rc, rs;
     int t0, tn;          // tabulated: first row and row count in the context's table rows
     unsigned long long first;  // charge_pair: types of the unpermuted first target (original_elements(1))
+    int agroup;          // -1, or the per-atom bond-order group whose factors scale the term
+};
+
+// Per-atom (level-1) bond-order factors: at most this many groups (Coordinators
+// of per-atom factors) per calculator.
+constexpr int PG_MAX_AGROUPS = 4;
+
+// Two-target per-atom factor record of an oriented type pair (atom1 type,
+// atom2 type): kind 0 neighbors f(r), 1 power_bond f(r) (a/r)^n
+// (Potentials.f90:5631-5645, 6293-6306).
+template <typename R>
+struct AfT {
+    int kind, group;  // group: level-1 group index
+    R rc, rs, a, n;
+};
+
+// Post-processing of a level-1 group's sum for one atom type: kind -1 none,
+// 2 c_scale (epsilon, N, C, gamma, min), 3 sqrt_scale (epsilon)
+// (Potentials.f90:6021-6063, 6402-6436).
+template <typename R>
+struct AfPostT {
+    int kind;
+    R p[5];
 };
 
 // Tersoff triplet parameters for (centre type, j type, k type) of group 0.
@@ -164,7 +188,7 @@ struct TriT {
 template <typename R, typename S>
 inline PairT<R> cast_pair(const PairT<S>& a) {
     return PairT<R>{a.kind, a.group, a.smooth, a.in_bond_kernel, (R)a.p0, (R)a.p1, (R)a.p2, (R)a.p3, (R)a.rc, (R)a.rs,
-                    a.t0, a.tn, a.first};
+                    a.t0, a.tn, a.first, a.agroup};
 }
 template <typename R, typename S>
 inline TripT<R> cast_trip(const TripT<S>& a) {
@@ -221,6 +245,7 @@ enum SpecIndex {
 struct SingleTerm {
     int kind;
     int n;
+    int agroup;  // -1, or the per-atom bond-order group whose factor scales the term
     double p[3];
 };
 
@@ -301,6 +326,21 @@ struct pg_context {
     int spec_nterm = 0, spec_bomask = 0;
     pg::DevBuf<pg::SingleTerm> d_single_terms;
     pg::DevBuf<int2> d_single_index;     // per type
+    // per-atom (level-1) bond-order factors (atomfactor.cu)
+    std::vector<int> af_kind, af_group;  // records as set through the C ABI
+    std::vector<double> af_params, af_cut, af_soft;
+    std::vector<uint64_t> af_m1, af_m2;
+    std::vector<int> sr_group;           // per single record: coordinator group or -1
+    int n_agroups = 0;                   // level-1 groups in use
+    std::map<int, int> agroup_of;        // coordinator group -> level-1 group
+    pg::DevBuf<pg::AfT<double>> d_af;    // folded per oriented type pair, FP64 and FP32
+    pg::DevBuf<pg::AfT<float>> d_af32;
+    pg::DevBuf<int2> d_af_index;         // per (atom1 type, atom2 type): offset, count into d_af
+    pg::DevBuf<pg::AfPostT<double>> d_af_post;  // per (group, type)
+    pg::DevBuf<pg::AfPostT<float>> d_af_post32;
+    // per (group, atom), in the working precision: the factor B, dB/dsum and
+    // W = (the atom's prefactor) dB/dsum
+    pg::DevBuf<double> af_B, af_S, af_W;
 
     // Ewald
     bool ewald = false;
@@ -496,6 +536,10 @@ int pair_lanes_for(const pg_context* ctx);
 // pair.cu: the fixed real-space Ewald electronegativity matrix of a relaxation loop
 bool chi_cache_prepare(pg_context* ctx, int precision);
 void launch_chi_cache_apply(pg_context* ctx, int precision, const int* skip);
+// atomfactor.cu: per-atom (level-1) bond-order factors; stage 0 computes the
+// factors (before the pair kernel), stage 1 adds their forces and virial
+void fold_atom_factors(pg_context* ctx, const std::map<int, int>& gmap);
+void launch_atom_factors(pg_context* ctx, int precision, int stage, bool first_f, FxAcc* acc, const int* skip);
 // triplet.cu: three-body potentials (bond_bend)
 constexpr int PG_MAX_TRIPLET_RECORDS = 64;
 void launch_triplets(pg_context* ctx, int precision, int flags, bool first_f, FxAcc* acc, const int* skip);

@@ -16,47 +16,10 @@
 #include "args.cuh"
 #include "common.cuh"
 #include "kernels.cuh"
+#include "pairvec.cuh"
 
 namespace pg {
 
-
-// bond vector of entry e of atom i: FP64 from the positions, or (mixed path)
-// build-time vector plus the FP32 displacements of both atoms
-template <typename R>
-__device__ __forceinline__ void pair_vector(const PairArgs& A, int i, int e, double xi, double yi, double zi, R& x,
-                                            R& y, R& z);
-template <>
-__device__ __forceinline__ void pair_vector<double>(const PairArgs& A, int i, int e, double xi, double yi, double zi,
-                                                    double& x, double& y, double& z) {
-    const int j = A.idx[e];
-    const double o0 = A.off[3 * e], o1 = A.off[3 * e + 1], o2 = A.off[3 * e + 2];
-    // separation_vector (Geometry.f90:449-466)
-    x = A.pos[3 * j] - xi + (o0 * A.C.vc[0][0] + o1 * A.C.vc[0][1] + o2 * A.C.vc[0][2]);
-    y = A.pos[3 * j + 1] - yi + (o0 * A.C.vc[1][0] + o1 * A.C.vc[1][1] + o2 * A.C.vc[1][2]);
-    z = A.pos[3 * j + 2] - zi + (o0 * A.C.vc[2][0] + o1 * A.C.vc[2][1] + o2 * A.C.vc[2][2]);
-}
-template <>
-__device__ __forceinline__ void pair_vector<float>(const PairArgs& A, int i, int e, double, double, double, float& x,
-                                                   float& y, float& z) {
-    const int j = A.idx[e];
-    const F4 s0 = A.sep0[e], dj = A.disp[j], di = A.disp[i];
-    x = s0.x + (dj.x - di.x);
-    y = s0.y + (dj.y - di.y);
-    z = s0.z + (dj.z - di.z);
-}
-
-// charge of atom j in the working precision (mixed path: the FP32 copy kept
-// beside the displacement)
-template <typename R>
-__device__ __forceinline__ R charge_of(const PairArgs& A, int j);
-template <>
-__device__ __forceinline__ double charge_of<double>(const PairArgs& A, int j) {
-    return A.charge[j];
-}
-template <>
-__device__ __forceinline__ float charge_of<float>(const PairArgs& A, int j) {
-    return A.disp[j].w;
-}
 
 __device__ __forceinline__ double powi_(double x, int n) {
     double r = 1.0;
@@ -77,6 +40,7 @@ __device__ __forceinline__ void pair_body(const PairArgs& A, int blk) {
     const bool act = i < A.n;
     R fx = 0, fy = 0, fz = 0, en = 0, chi = 0;
     R w0 = 0, w1 = 0, w2 = 0, w3 = 0, w4 = 0, w5 = 0;
+    R pre[PG_MAX_AGROUPS] = {};  // per-atom factor groups: this atom's prefactors (half of each pair's V f)
     const bool wantE = A.flags & PG_WANT_ENERGY, wantF = A.flags & PG_WANT_FORCES, wantC = A.flags & PG_WANT_ENEGS;
     int ti = 0;
     if (act) {
@@ -139,6 +103,18 @@ __device__ __forceinline__ void pair_body(const PairArgs& A, int blk) {
                 if (!(wantE || wantF)) continue;
                 R V, dV;
                 pair_term<R>(P, r, V, dV, (const R*)A.tab);
+                if (P.agroup >= 0) {
+                    // scaled by the pair's mean per-atom factor (B_i + B_j)/2
+                    // (Core.f90:4345-4350, 5553-5560); half of V f is each atom's
+                    // prefactor of the gradient of its factor (5486-5491)
+                    const R* B = (const R*)A.afB + (size_t)P.agroup * A.n;
+                    const R bm = R(0.5) * (B[i] + B[j]);
+#pragma unroll
+                    for (int q = 0; q < PG_MAX_AGROUPS; ++q)
+                        if (q == P.agroup) pre[q] += R(0.5) * V;
+                    V *= bm;
+                    dV *= bm;
+                }
                 U += V;
                 dU += dV;
             }
@@ -162,7 +138,10 @@ __device__ __forceinline__ void pair_body(const PairArgs& A, int blk) {
     // chi = -eps n q^(n-1) (Potentials.f90:4341-4375), constant V (3959-3966),
     // constant force F with energy -F . r at the absolute position (3122-3147);
     // singlets add nothing to the virial
+    // With a per-atom factor (constant and force only) the energy is V B_i and the
+    // term's own force gives way to -V grad B_i (V joins the prefactor).
     double cs = 0.0, es = 0.0, sf0 = 0.0, sf1 = 0.0, sf2 = 0.0;
+    double spre[PG_MAX_AGROUPS] = {};
     if (act && lane == 0) {
         const int2 sx = A.sindex[ti];
         for (int t = sx.x; t < sx.x + sx.y; ++t) {
@@ -171,13 +150,34 @@ __device__ __forceinline__ void pair_body(const PairArgs& A, int blk) {
                 const double qd = A.charge[i];
                 es += S.p[0] * powi_(qd, S.n);
                 cs += -(S.p[0] * S.n * powi_(qd, S.n - 1));
-            } else if (S.kind == 1) {
-                es += S.p[0];
             } else {
-                es -= S.p[0] * A.pos[3 * i] + S.p[1] * A.pos[3 * i + 1] + S.p[2] * A.pos[3 * i + 2];
-                sf0 += S.p[0];
-                sf1 += S.p[1];
-                sf2 += S.p[2];
+                const double V =
+                    S.kind == 1 ? S.p[0] : -(S.p[0] * A.pos[3 * i] + S.p[1] * A.pos[3 * i + 1] + S.p[2] * A.pos[3 * i + 2]);
+                if (S.agroup >= 0) {
+                    if (wantE || wantF) es += V * (double)((const R*)A.afB)[(size_t)S.agroup * A.n + i];
+#pragma unroll
+                    for (int q = 0; q < PG_MAX_AGROUPS; ++q)
+                        if (q == S.agroup) spre[q] += V;
+                } else {
+                    es += V;
+                    if (S.kind == 2) {
+                        sf0 += S.p[0];
+                        sf1 += S.p[1];
+                        sf2 += S.p[2];
+                    }
+                }
+            }
+        }
+    }
+    // W_i = dB/dsum times the prefactor, for the per-atom factor forces
+    if (wantF && A.ng > 0) {
+#pragma unroll
+        for (int q = 0; q < PG_MAX_AGROUPS; ++q) {
+            if (q >= A.ng) break;
+            const auto sp = group_sum_f<G>(pre[q]);
+            if (act && lane == 0) {
+                const size_t o = (size_t)q * A.n + i;
+                ((R*)A.afW)[o] = (R)(((const R*)A.afS)[o] * (sp.d() + spre[q]));
             }
         }
     }
@@ -337,6 +337,7 @@ PairArgs make_pair_args(pg_context* ctx, int precision, int flags, bool first_f,
     A.acc = acc;
     A.sep0 = ctx->nb_sep0.p;
     A.disp = ctx->disp32.p;
+    set_atom_factor_args(ctx, precision, A);
     return A;
 }
 

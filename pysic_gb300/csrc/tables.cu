@@ -24,9 +24,29 @@ void fold_tables(pg_context* ctx) {
     for (int t : ctx->h_type)
         require(t < T, PG_ERR_INVALID, "atom type outside the interaction tables (set the potentials after the atoms)");
     const int nb = (int)ctx->br_cut.size();
-    for (int b = 0; b < nb; ++b)
-        require(ctx->br_group[b] == 0, PG_ERR_UNSUPPORTED,
-                "the GB300 engine evaluates one bond-order group (one Coordinator) per calculator");
+    // Coordinator groups: the one group of Tersoff factors (evaluated by the
+    // bond-order kernels as group 0) and up to PG_MAX_AGROUPS groups of per-atom
+    // factors (atomfactor.cu)
+    int tersoff_gid = -1;
+    for (int b = 0; b < nb; ++b) {
+        if (tersoff_gid < 0) tersoff_gid = ctx->br_group[b];
+        require(ctx->br_group[b] == tersoff_gid && tersoff_gid >= 0, PG_ERR_UNSUPPORTED,
+                "the GB300 engine evaluates one group (one Coordinator) of Tersoff factors per calculator");
+    }
+    std::map<int, int> gmap;  // coordinator group -> per-atom factor group
+    for (size_t r = 0; r < ctx->af_kind.size(); ++r) {
+        const int g = ctx->af_group[r];
+        require(g >= 0 && g != tersoff_gid, PG_ERR_UNSUPPORTED,
+                "a Coordinator mixing per-atom and Tersoff factors is not evaluated by the GB300 engine");
+        if (!gmap.count(g)) {
+            require((int)gmap.size() < PG_MAX_AGROUPS, PG_ERR_UNSUPPORTED,
+                    "more than 4 Coordinators of per-atom bond-order factors");
+            const int k = (int)gmap.size();
+            gmap[g] = k;
+        }
+    }
+    ctx->n_agroups = (int)gmap.size();
+    ctx->agroup_of = gmap;
 
     // bond-order tables
     std::vector<TripT<double>> trip((size_t)T * T * T);
@@ -89,10 +109,9 @@ void fold_tables(pg_context* ctx) {
     const int np = (int)ctx->pr_cut.size();
     for (int r = 0; r < np; ++r)
         if (ctx->pr_group[r] >= 0) {
-            require(nb > 0, PG_ERR_INVALID, "a potential has a coordinator without bond-order factors");
-            require(ctx->pr_group[r] == 0, PG_ERR_UNSUPPORTED,
-                    "the GB300 engine evaluates one bond-order group (one Coordinator) per calculator");
-            bo_radius = std::max(bo_radius, ctx->pr_cut[r]);
+            require(ctx->pr_group[r] == tersoff_gid || gmap.count(ctx->pr_group[r]), PG_ERR_INVALID,
+                    "a potential has a coordinator without bond-order factors");
+            if (ctx->pr_group[r] == tersoff_gid) bo_radius = std::max(bo_radius, ctx->pr_cut[r]);
         }
     const bool bond = nb > 0;
     ctx->have_bond_terms = bond;
@@ -109,7 +128,11 @@ void fold_tables(pg_context* ctx) {
                 if (!has(ctx->pr_m1[r], ti) || !has(ctx->pr_m2[r], tj)) continue;
                 PairT<double> t{};
                 t.kind = ctx->pr_kind[r];
-                t.group = ctx->pr_group[r];
+                const int g = ctx->pr_group[r];
+                t.group = g >= 0 && g == tersoff_gid ? 0 : -1;
+                t.agroup = g >= 0 && g != tersoff_gid ? gmap.at(g) : -1;
+                require(!(t.agroup >= 0 && t.kind == 7), PG_ERR_UNSUPPORTED,
+                        "bond-order scaling of charge_pair is not evaluated by the GB300 engine");
                 t.p0 = ctx->pr_params[4 * (size_t)r];
                 t.p1 = ctx->pr_params[4 * (size_t)r + 1];
                 t.p2 = ctx->pr_params[4 * (size_t)r + 2];
@@ -135,7 +158,7 @@ void fold_tables(pg_context* ctx) {
                     t.rs = t.rc;
                 }
                 // charge-dependent pair terms stay in the pair kernel (electronegativities)
-                t.in_bond_kernel = bond && t.kind != 7 && (t.group >= 0 || t.rc <= bo_radius);
+                t.in_bond_kernel = bond && t.kind != 7 && t.agroup < 0 && (t.group >= 0 || t.rc <= bo_radius);
                 if (t.kind == 7) charge_pairs = true;
                 if (!t.in_bond_kernel) pair_kernel_terms = true;
                 terms.push_back(t);
@@ -152,6 +175,15 @@ void fold_tables(pg_context* ctx) {
             if (has(ctx->sr_m[r], t)) {
                 SingleTerm s{};
                 s.kind = ctx->sr_kind[r];
+                const int g = r < (int)ctx->sr_group.size() ? ctx->sr_group[r] : -1;
+                s.agroup = -1;
+                if (g >= 0) {
+                    require(gmap.count(g) > 0, PG_ERR_UNSUPPORTED,
+                            "single-atom terms are scaled by per-atom bond-order factors only");
+                    require(s.kind != 0, PG_ERR_UNSUPPORTED,
+                            "bond-order scaling of charge_self is not evaluated by the GB300 engine");
+                    s.agroup = gmap.at(g);
+                }
                 for (int c = 0; c < 3; ++c) s.p[c] = ctx->sr_params[4 * (size_t)r + c];
                 s.n = s.kind == 0 ? (int)s.p[1] : 0;  // charge_self: the reference's integer n = int(param2)
                 sterms.push_back(s);
@@ -225,6 +257,7 @@ void fold_tables(pg_context* ctx) {
     ctx->d_maxbr32.upload(maxbr32.data(), maxbr32.size(), st);
     ctx->d_single_terms.upload(sterms.data(), sterms.size(), st);
     ctx->d_single_index.upload(sindex.data(), sindex.size(), st);
+    fold_atom_factors(ctx, gmap);
     // three-body records: the derived cos(theta_0)^n (calculate_derived_parameters_
     // bond_bending, Potentials.f90:3183-3194) and the integer exponents n, m
     {

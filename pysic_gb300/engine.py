@@ -78,6 +78,11 @@ class Engine:
         L.check(self.lib.pg_set_single_potentials(
             self.ctx, len(a["single_kind"]), L.iptr(a["single_kind"]), L.dptr(a["single_params"]),
             L.u64ptr(a["single_mask"])))
+        L.check(self.lib.pg_set_single_groups(self.ctx, len(a["single_kind"]), L.iptr(a["single_group"])))
+        L.check(self.lib.pg_set_atom_factors(
+            self.ctx, len(a["afac_kind"]), L.iptr(a["afac_kind"]), L.dptr(a["afac_params"]),
+            L.dptr(a["afac_cutoff"]), L.dptr(a["afac_soft"]), L.u64ptr(a["afac_mask1"]), L.u64ptr(a["afac_mask2"]),
+            L.iptr(a["afac_group"])))
         L.check(self.lib.pg_set_bond_order_factors(
             self.ctx, len(a["bond_cutoff"]), L.dptr(a["bond_params"]), L.dptr(a["bond_cutoff"]),
             L.dptr(a["bond_soft"]), L.u64ptr(a["bond_mask1"]), L.u64ptr(a["bond_mask2"]), L.u64ptr(a["bond_mask3"]),
@@ -195,6 +200,12 @@ class Engine:
                                                        float(inertia), float(potential), L.dptr(rates), L.dptr(q),
                                                        ctypes.byref(m)))
         return {"charges": q, "rates": rates, "steps": int(n_steps), "max_dchi": m.value}
+
+    def atom_factors(self, group, precision=L.PREC_FP64):
+        """Per-atom bond-order factors of a Coordinator group at the current positions."""
+        out = np.zeros(max(self.n, 1))
+        L.check(self.lib.pg_get_atom_factors(self.ctx, int(precision), int(group), L.dptr(out)))
+        return out[:self.n]
 
     def bond_zeta(self):
         n = ctypes.c_int64(0)

@@ -374,6 +374,14 @@ class Coordinator:
     def __ne__(self, other):
         return not self.__eq__(other)
 
+    def __deepcopy__(self, memo):
+        # the calculator the coordinator reports to is shared, not copied
+        new = Coordinator.__new__(Coordinator)
+        memo[id(self)] = new
+        for k, v in self.__dict__.items():
+            setattr(new, k, v if k == "_calculator" else copy.deepcopy(v, memo))
+        return new
+
     def __repr__(self):
         return "Coordinator(bond_order_parameters={0})".format(self.bond_order_params)
 
@@ -396,17 +404,16 @@ class Coordinator:
         return self.group_index
 
     def calculate_bond_order_factors(self):
-        """Per-atom (level-1) bond-order factors (Core.f90:2015-2404).  A group made
-        only of pairwise (level-2) factors such as 'tersoff' has none, and the
-        reference returns zeros for it; so does this engine."""
-        if self._calculator is None:
+        """Per-atom (level-1) bond-order factors B_i of this group at the current
+        positions (bondorder.py:493-506 -> core_get_bond_order_factors,
+        Core.f90:759-783), computed on the device.  A group made only of
+        pairwise (level-2) factors such as 'tersoff' has none, and the reference
+        returns zeros for it; so does this engine."""
+        calc = self._calculator
+        if calc is None:
             raise InvalidCoordinatorError("The coordinator is not attached to a calculator.")
-        n = len(self._calculator.get_atoms())
-        for b in self.bond_order_params:
-            if b.get_level() == 1:
-                raise InvalidCoordinatorError("per-atom bond-order factors are not evaluated by the GB300 engine")
-        import numpy as np
-        self.bond_order_factors = np.zeros(n)
+        calc.set_core()
+        self.bond_order_factors = calc.engine.atom_factors(self.group_index, calc._prec())
 
     def get_bond_order_factors(self):
         return self.bond_order_factors
@@ -498,3 +505,136 @@ def estimate_ewald_parameters(real_cutoff=10.0, accuracy="normal"):
     sdiv, kmul = rules[accuracy]
     sigma = real_cutoff / sdiv
     return (real_cutoff, kmul / sigma, sigma, epsilon)
+
+
+class CompoundPotential(Potential):
+    """A potential assembled from elementary Potential objects
+    (pysic/interactions/compound.py:8-213): the calculator adds its pieces,
+    which define_elements() builds, one by one."""
+
+    def __init__(self, n_targets, n_params, symbols=None, tags=None, indices=None, parameters=None, cutoff=0.0,
+                 cutoff_margin=0.0):
+        self.n_targets = n_targets
+        self.n_params = n_params
+        self.symbols = None
+        self.tags = None
+        self.indices = None
+        self.cutoff = cutoff
+        self.cutoff_margin = 0.0
+        self.coordinator = None
+        self.parameters = [0.0] * n_params if parameters is None else list(parameters)
+        self.set_cutoff_margin(cutoff_margin)
+        self.set_symbols(symbols)
+        self.set_tags(tags)
+        self.set_indices(indices)
+        self.potential_type = None
+        self.names_of_params = ["anonymous"] * n_params
+        self.descriptions_of_params = ["description missing"] * n_params
+        self.description = "This compound potential has no description."
+        self.pieces = []
+
+    def __eq__(self, other):
+        try:
+            if (self.potential_type != other.potential_type or self.symbols != other.symbols
+                    or self.tags != other.tags or self.indices != other.indices
+                    or self.parameters != other.parameters or self.cutoff != other.cutoff):
+                return False
+            return len(self.pieces) == len(other.pieces) and all(a == b for a, b in zip(self.pieces, other.pieces))
+        except AttributeError:
+            return False
+
+    def __ne__(self, other):
+        return not self.__eq__(other)
+
+    def __repr__(self):
+        return "{0}(symbols={1},tags={2},indices={3},parameters={4},cutoff={5},cutoff_margin={6})".format(
+            type(self).__name__, self.symbols, self.tags, self.indices, self.parameters, self.cutoff,
+            self.cutoff_margin)
+
+    def get_number_of_parameters(self):
+        return self.n_params
+
+    def get_parameter_names(self):
+        return self.names_of_params
+
+    def set_potential_type(self, potential_type):
+        self.potential_type = potential_type
+
+    def get_elements(self):
+        return self.pieces
+
+    def build(self, calculator):
+        self.define_elements()
+        for piece in self.pieces:
+            calculator.add_potential(piece)
+
+    def remove(self, calculator):
+        self.define_elements()
+        for piece in self.pieces:
+            try:
+                calculator.remove_potential(piece)
+            except ValueError:
+                warn("Could not remove a potential {0} from the calculator.".format(piece.get_potential_type()), 2)
+
+    def define_elements(self):
+        self.pieces = []
+
+    def describe(self):
+        print("potential '{0}'\n{1}-body interaction\n{2}".format(self.potential_type, self.n_targets,
+                                                                 self.description))
+
+
+class SuttonChenPotential(CompoundPotential):
+    """U = epsilon [ sum_ij (a/r)^n - c sum_i sqrt(rho_i) ], rho_i = sum_j (a/r)^m
+    (pysic/interactions/suttonchen.py:8-176), parameters [epsilon, a, c, n, m].
+
+    The pieces are the reference's: a 'power' pair potential eps (a/r)^n on the
+    given targets, and per element a 'constant' potential eps scaled by a
+    Coordinator of 'sqrt_scale' (epsilon = -c) over 'power_bond' (a, m) on the
+    element pairs that the element leads.  Element targets only."""
+
+    def __init__(self, symbols=None, tags=None, indices=None, parameters=None, cutoff=0.0, cutoff_margin=0.0):
+        super(SuttonChenPotential, self).__init__(n_params=5, n_targets=2, symbols=symbols, tags=tags,
+                                                  indices=indices, parameters=parameters, cutoff=cutoff,
+                                                  cutoff_margin=cutoff_margin)
+        self.density_symbols = None
+        self.set_potential_type("suttonchen")
+        self.names_of_params = ["epsilon", "a", "c", "n", "m"]
+        self.descriptions_of_params = ["energy scale constant", "lenght scale or lattice constant",
+                                       "density coefficient", "power decay exponent", "density decay exponent"]
+        self.description = ("A potential of type\n U = epsilon [ sum_ij (a/r)^n - c sum_i sqrt(rho) ],\nwhere\n"
+                            " rho = sum_j (a/r)^m.\nand r is the interatomic distance.")
+
+    def set_density_symbols(self, symbols):
+        self.density_symbols = symbols
+
+    def define_elements(self):
+        if self.tags or self.indices:
+            raise InvalidPotentialError("the Sutton-Chen density terms are built for element targets only")
+        eps, a, c, n, m = [float(x) for x in self.parameters]
+        pair = Potential("power", symbols=self.symbols, cutoff=self.cutoff, cutoff_margin=self.cutoff_margin)
+        pair.set_parameter_value("epsilon", eps)
+        pair.set_parameter_value("a", a)
+        pair.set_parameter_value("n", n)
+        self.pieces = [pair]
+        elements, pairs = [], []
+        for t in self.symbols or []:
+            for e in t:
+                if e not in elements:
+                    elements.append(e)
+            pairs.append(list(t))
+            if len(t) == 2 and t[0] != t[1]:
+                pairs.append([t[1], t[0]])
+        for e in elements:
+            if self.density_symbols is not None and e not in self.density_symbols:
+                continue
+            scaler = BondOrderParameters("sqrt_scale")
+            scaler.set_parameter_value("epsilon", -c)
+            scaler.set_symbols([[e]])
+            density = BondOrderParameters("power_bond", cutoff=self.cutoff, cutoff_margin=self.cutoff_margin)
+            density.set_parameter_value("a", a)
+            density.set_parameter_value("n", m)
+            density.set_symbols([p for p in pairs if p[0] == e])
+            piece = Potential("constant", parameters=[eps], symbols=[[e]])
+            piece.set_coordinator(Coordinator([scaler, density]))
+            self.pieces.append(piece)

@@ -49,6 +49,15 @@ class Model:
         self.single_kind = []
         self.single_params = []
         self.single_mask = []
+        self.single_group = []
+        # per-atom (level-1) bond-order factors, one record per target tuple
+        self.afac_kind = []
+        self.afac_params = []
+        self.afac_cutoff = []
+        self.afac_soft = []
+        self.afac_mask1 = []
+        self.afac_mask2 = []
+        self.afac_group = []
         self.bond_params = []
         self.bond_cutoff = []
         self.bond_soft = []
@@ -85,6 +94,14 @@ class Model:
         d["single_kind"] = np.array(self.single_kind, dtype=np.int32)
         d["single_params"] = np.array(self.single_params, dtype=np.float64).reshape(-1, 4)
         d["single_mask"] = np.array(self.single_mask, dtype=np.uint64)
+        d["single_group"] = np.array(self.single_group, dtype=np.int32)
+        d["afac_kind"] = np.array(self.afac_kind, dtype=np.int32)
+        d["afac_params"] = np.array(self.afac_params, dtype=np.float64).reshape(-1, 5)
+        d["afac_cutoff"] = np.array(self.afac_cutoff, dtype=np.float64)
+        d["afac_soft"] = np.array(self.afac_soft, dtype=np.float64)
+        d["afac_mask1"] = np.array(self.afac_mask1, dtype=np.uint64)
+        d["afac_mask2"] = np.array(self.afac_mask2, dtype=np.uint64)
+        d["afac_group"] = np.array(self.afac_group, dtype=np.int32)
         d["bond_params"] = np.array(self.bond_params, dtype=np.float64).reshape(-1, 7)
         d["bond_cutoff"] = np.array(self.bond_cutoff, dtype=np.float64)
         d["bond_soft"] = np.array(self.bond_soft, dtype=np.float64)
@@ -227,13 +244,13 @@ def compile_model(atoms, potentials, coulomb=None):
         elif nt == 1:
             if kind not in core.SINGLE_KIND:
                 raise InvalidPotentialError("'{0}' is not a single-atom term of the GB300 engine".format(kind))
-            if grp >= 0:
-                raise InvalidPotentialError("bond-order scaling of single-atom terms is not evaluated by the GB300 "
-                                            "engine")
+            if grp >= 0 and kind == "charge_self":
+                raise InvalidPotentialError("bond-order scaling of charge_self is not evaluated by the GB300 engine")
             for tg in targets:
                 M.single_kind.append(core.SINGLE_KIND[kind])
                 M.single_params.append((params + [0.0] * 4)[:4])
                 M.single_mask.append(_mask(sigs, *tg[0]))
+                M.single_group.append(grp)
         elif nt == 3:
             if kind not in core.TRIPLET_KIND:
                 raise InvalidPotentialError("'{0}' is not a three-body potential of the GB300 engine".format(kind))
@@ -263,9 +280,20 @@ def compile_model(atoms, potentials, coulomb=None):
         for bond in c.get_bond_order_parameters():
             bkind = bond.get_bond_order_type()
             core.check_engine_support(bkind)
-            if bond.get_level() != 2:
-                raise InvalidParametersError("per-atom bond-order factors are not evaluated by the GB300 engine")
             flat = [float(x) for x in bond.get_parameters_as_list()]
+            if bkind in core.ATOM_FACTOR_KIND:
+                # per-atom factors keep the reference's global order (coordinator,
+                # factor, target tuple): the first scaler of an element wins
+                # (core_post_process_bond_order_factors, Core.f90:2697-2712)
+                for tg in bond.get_symbols() or []:
+                    M.afac_kind.append(core.ATOM_FACTOR_KIND[bkind])
+                    M.afac_params.append((flat + [0.0] * 5)[:5])
+                    M.afac_cutoff.append(float(bond.get_cutoff()))
+                    M.afac_soft.append(float(bond.get_soft_cutoff()))
+                    M.afac_mask1.append(_mask(sigs, element=tg[0]))
+                    M.afac_mask2.append(_mask(sigs, element=tg[1]) if len(tg) > 1 else 0)
+                    M.afac_group.append(g)
+                continue
             for tg in bond.get_symbols() or []:
                 M.bond_params.append(flat)
                 M.bond_cutoff.append(float(bond.get_cutoff()))

@@ -40,6 +40,28 @@ def lj_potentials(symbol="X", epsilon=0.0104, sigma=3.40, cutoff=8.5):
     return [Potential("LJ", symbols=[[symbol, symbol]], parameters=[epsilon, sigma], cutoff=cutoff)]
 
 
+# Sutton & Chen, Phil. Mag. Lett. 61, 139 (1990): copper (eps eV, a A, c, n, m)
+SUTTON_CHEN_CU = (1.2382e-2, 3.61, 39.432, 9.0, 6.0)
+
+
+def fcc_alloy(n=4, a0=3.61, symbols=("Cu", "Ag"), fraction=0.5, noise=0.05, seed=0):
+    """fcc crystal with the sites of the second element drawn at the given fraction."""
+    atoms = lj_fcc(n=n, a0=a0, noise=noise, seed=seed, symbol=symbols[0])
+    if len(symbols) == 1:
+        return atoms
+    rng = np.random.default_rng(seed + 1)
+    sym = np.where(rng.random(len(atoms)) < fraction, symbols[1], symbols[0])
+    return Atoms(list(sym), atoms.get_positions(), cell=atoms.get_cell(), pbc=True)
+
+
+def sutton_chen_potentials(symbols=("Cu",), p=SUTTON_CHEN_CU, cutoff=5.0, cutoff_margin=0.5):
+    """One Sutton-Chen compound on every element pair of the given elements."""
+    from .interactions import SuttonChenPotential
+
+    pairs = [[a, b] for i, a in enumerate(symbols) for b in symbols[i:]]
+    return [SuttonChenPotential(symbols=pairs, parameters=list(p), cutoff=cutoff, cutoff_margin=cutoff_margin)]
+
+
 def diamond_si(n=8, a0=5.431, noise=0.10, seed=0):
     basis = [[0, 0, 0], [0, 0.5, 0.5], [0.5, 0, 0.5], [0.5, 0.5, 0], [0.25, 0.25, 0.25], [0.25, 0.75, 0.75],
              [0.75, 0.25, 0.75], [0.75, 0.75, 0.25]]

@@ -137,3 +137,52 @@ def test_workloads_shapes():
     a = W.rocksalt_nacl()
     assert len(a) == 8000 and a.get_initial_charges().sum() == 0
     assert W.ewald_kcut(2.5) == pytest.approx(2.1, abs=0.03)
+
+
+def test_sutton_chen_pieces_and_factor_records():
+    """SuttonChenPotential builds the reference's pieces (suttonchen.py:68-176):
+    a power pair potential and, per element, a constant scaled by sqrt_scale
+    over power_bond on the element pairs that element leads; the factor records
+    keep the unpermuted targets in the reference's order."""
+    atoms = W.fcc_alloy(2, symbols=("Cu", "Ag"), seed=1)
+    calc = pysic.Pysic()
+    calc.add_potential(W.sutton_chen_potentials(("Cu", "Ag")))
+    pots = calc.get_potentials()
+    assert [p.get_potential_type() for p in pots] == ["power", "constant", "constant"]
+    assert pots[0].get_symbols() == [["Cu", "Cu"], ["Cu", "Ag"], ["Ag", "Ag"]]
+    dens = pots[2].get_coordinator().get_bond_order_parameters()
+    assert [b.get_bond_order_type() for b in dens] == ["sqrt_scale", "power_bond"]
+    assert dens[0].get_parameter_value("epsilon") == -W.SUTTON_CHEN_CU[2]
+    assert dens[1].get_symbols() == [["Ag", "Cu"], ["Ag", "Ag"]]
+    M = compile_model(atoms, pots)
+    assert M.afac_kind == [3, 1, 1, 3, 1, 1]
+    assert M.afac_group == [0, 0, 0, 1, 1, 1]
+    assert M.single_group == [0, 1]
+    assert M.pair_group == [-1] * len(M.pair_group)
+
+
+def test_scaled_charge_self_rejected():
+    atoms = W.fcc_alloy(2, symbols=("Cu",))
+    count = pysic.BondOrderParameters("neighbors", cutoff=3.0, symbols=[["Cu", "Cu"]])
+    pot = pysic.Potential("charge_self", symbols=[["Cu"]], parameters=[1.0, 2], coordinator=pysic.Coordinator([count]))
+    with pytest.raises(pysic.InvalidPotentialError):
+        compile_model(atoms, [pot])
+
+
+def test_coordinator_copies_share_their_calculator():
+    """A Coordinator attached to a calculator (engine handles inside) deep-copies
+    with the calculator shared, as the calculator's change tracking needs."""
+    import copy
+    import ctypes
+
+    class _Calc:
+        handle = ctypes.pointer(ctypes.c_int(1))
+
+    count = pysic.BondOrderParameters("neighbors", cutoff=3.0, symbols=[["Cu", "Cu"]])
+    pot = pysic.Potential("constant", symbols=[["Cu"]], parameters=[1.0], coordinator=pysic.Coordinator([count]))
+    calc = _Calc()
+    pot.get_coordinator()._calculator = calc
+    dup = copy.deepcopy(pot)
+    assert dup == pot
+    assert dup.get_coordinator()._calculator is calc
+    assert dup.get_coordinator().get_bond_order_parameters()[0] is not count

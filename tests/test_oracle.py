@@ -300,3 +300,109 @@ def test_oracle_charge_pair_derivatives():
             p2[a, c] -= h
             numf = -(ev(p1, q, "energy") - ev(p2, q, "energy")) / (2 * h)
             assert f[a, c] == pytest.approx(numf, abs=1e-6)
+
+
+# ---- per-atom (level-1) bond-order factors ----------------------------------
+
+def _sc_closed_form(atoms, p, cutoff, margin):
+    """Sutton-Chen energy from its formula (minimum image, cutoff < L/2), with the
+    reference's smooth cutoff on both the pair and the density terms."""
+    eps, a, c, n, m = p
+    pos = atoms.get_positions()
+    L = np.diag(atoms.get_cell())
+    soft = cutoff - margin
+    e_pair, rho = 0.0, np.zeros(len(atoms))
+    for i in range(len(atoms)):
+        d = pos - pos[i]
+        d -= L * np.round(d / L)
+        r = np.linalg.norm(d, axis=1)
+        r[i] = np.inf
+        sel = r < cutoff
+        rr = r[sel]
+        f = np.where(rr < soft, 1.0, 0.5 * (1 + np.cos(np.pi * (rr - soft) / (cutoff - soft))))
+        e_pair += 0.5 * np.sum(eps * f * (a / rr) ** n)
+        rho[i] = np.sum(f * (a / rr) ** m)
+    return e_pair - eps * c * np.sum(np.sqrt(rho))
+
+
+def test_oracle_sutton_chen_closed_form_and_gradient():
+    """Sutton-Chen as the reference assembles it (suttonchen.py:68-176: a power
+    pair potential plus a constant scaled by sqrt_scale over power_bond) in the
+    oracle's per-atom factor loops (Core.f90:2015-2404, 2671-2735, 4745-4933):
+    energy equal to the closed form, forces minus its gradient, virial minus
+    its strain derivative."""
+    atoms = W.fcc_alloy(4, a0=3.61, symbols=("Cu",), noise=0.06, seed=5)
+    pots = W.sutton_chen_potentials(("Cu",), cutoff=5.0, cutoff_margin=0.6)
+    calc = pysic.Pysic()
+    for p in pots:
+        calc.add_potential(p)
+    pots = calc.get_potentials()
+    assert [q.get_potential_type() for q in pots] == ["power", "constant"]
+    r = oracle_all(atoms, pots)
+    assert r["energy"] == pytest.approx(_sc_closed_form(atoms, W.SUTTON_CHEN_CU, 5.0, 0.6), rel=1e-12)
+    # cohesive energy of the perfect crystal in the known range for this cutoff
+    perfect = W.fcc_alloy(4, a0=3.61, symbols=("Cu",), noise=0.0)
+    assert oracle_all(perfect, pots)["energy"] / len(perfect) == pytest.approx(-3.2, abs=0.4)
+    fd, f = _fd_forces(atoms, pots, 7, h=1e-5)
+    np.testing.assert_allclose(f, fd, atol=2e-7, rtol=1e-6)
+    model = compile_model(atoms, pots)
+    h = 1e-6
+    e = []
+    for s in (+h, -h):
+        eps = np.eye(3)
+        eps[1, 1] += s
+        a2 = atoms.copy()
+        a2.set_cell(atoms.get_cell() @ eps, scale_atoms=True)
+        e.append(oracle.evaluate(a2.get_positions(), a2.get_initial_charges(), a2.get_cell(), a2.get_pbc(), model,
+                                 *oracle_lists(a2, pots), what="energy"))
+    assert r["stress"][1] == pytest.approx(-(e[0] - e[1]) / (2 * h), rel=1e-6, abs=1e-7)
+
+
+def test_oracle_scaled_pair_potential_gradient():
+    """A pair potential scaled by a c_scale-processed neighbour count (the
+    doublet's (B_i + B_j)/2, Core.f90:4345-4350, 5486-5560): forces are minus the
+    energy gradient for a single element."""
+    atoms = W.fcc_alloy(4, a0=3.61, symbols=("Cu",), noise=0.08, seed=6)
+    count = pysic.BondOrderParameters("neighbors", cutoff=3.2, cutoff_margin=0.7, symbols=[["Cu", "Cu"]])
+    scale = pysic.BondOrderParameters("c_scale", parameters=[[0.8, 11.0, 0.5, 0.3, -50.0], []], symbols=[["Cu"]])
+    pot = pysic.Potential("exponential", symbols=[["Cu", "Cu"]], parameters=[1.5, 1.2], cutoff=4.0,
+                          cutoff_margin=0.5, coordinator=pysic.Coordinator([scale, count]))
+    raw, fac = oracle.atom_factors(atoms.get_positions(), atoms.get_cell(), atoms.get_pbc(),
+                                   compile_model(atoms, [pot]), *oracle_lists(atoms, [pot]))
+    assert raw.min() > 8 and raw.max() < 16 and np.ptp(fac) > 0.05
+    for idx in (3, 50):
+        fd, f = _fd_forces(atoms, [pot], idx, h=1e-5)
+        np.testing.assert_allclose(f, fd, atol=2e-7, rtol=1e-6)
+
+
+def test_oracle_atom_factor_sums_follow_the_picked_pair():
+    """For an element pair A-B the reference adds a factor record only from the
+    atom that pick makes atom1 (Core.f90:2040-2095): with the record [Cu, Ag]
+    alone, each Cu-Ag pair counts once in both atoms' sums when the Cu atom is
+    atom1 and not at all otherwise."""
+    atoms = W.fcc_alloy(3, a0=3.61, symbols=("Cu", "Ag"), noise=0.05, seed=7)
+    count = pysic.BondOrderParameters("neighbors", cutoff=3.0, symbols=[["Cu", "Ag"]])
+    pot = pysic.Potential("constant", parameters=[1.0], symbols=[["Cu"]], coordinator=pysic.Coordinator([count]))
+    model = compile_model(atoms, [pot])
+    c, idx, off = oracle_lists(atoms, [pot])
+    raw, fac = oracle.atom_factors(atoms.get_positions(), atoms.get_cell(), atoms.get_pbc(), model, c, idx, off)
+    sym = np.array(atoms.get_chemical_symbols())
+    pos, cell = atoms.get_positions(), atoms.get_cell()
+    expect = np.zeros(len(atoms))
+    start = np.concatenate([[0], np.cumsum(c)])
+    for i in range(len(atoms)):
+        for e in range(start[i], start[i + 1]):
+            j, o = idx[e], off[e]
+            d = np.linalg.norm(pos[j] + o @ cell - pos[i])
+            # pick, Geometry.f90:648-676: atom1 is the lower index; an atom and
+            # its own image by the sign of the first nonzero offset
+            if i == j:
+                first = next(x for x in o if x != 0) > 0
+            else:
+                first = i < j
+            if first and sym[i] == "Cu" and sym[j] == "Ag" and d < 3.0:
+                expect[i] += 1
+                expect[j] += 1
+    np.testing.assert_array_equal(raw, expect)
+    np.testing.assert_array_equal(fac, expect)
+    assert oracle_all(atoms, [pot])["energy"] == pytest.approx(expect[sym == "Cu"].sum(), abs=1e-12)
