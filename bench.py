@@ -53,6 +53,13 @@ def workload(name):
     if name == "ewald_nacl_8000":
         pots, coul = W.nacl_potentials()
         return W.rocksalt_nacl(), pots, coul, "rock salt 10x10x10 cells, Buckingham + Ewald (rc 10, sigma 2.5)"
+    if name == "sutton_chen_cu_32000":
+        from pysic_gb300 import Pysic
+
+        calc = Pysic()
+        calc.add_potential(W.sutton_chen_potentials(("Cu",), cutoff=5.0, cutoff_margin=0.5))
+        return (W.fcc_alloy(20, symbols=("Cu",), noise=0.05, seed=0), calc.get_potentials(), None,
+                "fcc Cu 20x20x20 cells, a=3.61, noise 0.05, Sutton-Chen (cutoff 5.0, margin 0.5)")
     raise SystemExit("unknown workload " + name)
 
 

@@ -243,6 +243,10 @@ int pg_get_bond_zeta(pg_context* ctx, double* zeta, int64_t capacity, int64_t* n
 /* Tile size of the bond-order kernels: lanes per atom (4, 8, 16 or 32); 0 lets the
  * built-in autotuner choose on the next evaluation. */
 int pg_set_lanes_per_atom(pg_context* ctx, int32_t lanes);
+/* Tile size of the full-list kernels (pair, per-atom factors, cached Ewald
+ * matrix): lanes per atom (8, 16 or 32); 0 chooses by list length and atom
+ * count. */
+int pg_set_pair_lanes(pg_context* ctx, int32_t lanes);
 int pg_get_lanes_per_atom(pg_context* ctx, int32_t* lanes);
 
 /* ---- device-resident evaluation (benchmarks, MD drivers) ----------------

@@ -69,11 +69,17 @@ CellK cell_kernel_view(const Cell& C) {
     return k;
 }
 
+// Lanes per atom of the full-list kernels: as few as keep the GPU busy.  Each
+// group of lanes ends with its atom's reductions (force, energy, virial), so
+// short lists on many atoms run best at 8 lanes (Sutton-Chen, 32k atoms, ~54
+// neighbours: 8 lanes 1.7x faster than 32); small systems take more lanes per
+// atom while there are fewer than 64k threads and at least 4 entries per lane.
 int pair_lanes_for(const pg_context* ctx) {
+    if (ctx->pair_lanes) return ctx->pair_lanes;
     const double avg = ctx->n > 0 ? (double)ctx->nb_total / ctx->n : 0.0;
-    if (avg >= 48.0) return 32;
-    if (avg >= 16.0) return 16;
-    return 8;
+    int G = 8;
+    while (G < 32 && (long long)ctx->n * G < 65536 && avg >= 4.0 * G) G *= 2;
+    return G;
 }
 
 void prepare(pg_context* ctx) {
@@ -772,6 +778,16 @@ int pg_set_lanes_per_atom(pg_context* ctx, int32_t lanes) {
         pg::require(lanes == 0 || lanes == 4 || lanes == 8 || lanes == 16 || lanes == 32, PG_ERR_INVALID,
                     "lanes per atom must be 0, 4, 8, 16 or 32");
         ctx->lanes = lanes;
+        ctx->state_epoch++;
+    });
+}
+
+int pg_set_pair_lanes(pg_context* ctx, int32_t lanes) {
+    return guarded([&] {
+        check_ctx(ctx);
+        pg::require(lanes == 0 || lanes == 8 || lanes == 16 || lanes == 32, PG_ERR_INVALID,
+                    "pair lanes per atom must be 0, 8, 16 or 32");
+        ctx->pair_lanes = lanes;
         ctx->state_epoch++;
     });
 }

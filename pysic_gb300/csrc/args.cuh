@@ -36,6 +36,8 @@ struct PairArgs {
     const void* af;        // AfT<R>
     const int2* af_index;  // per (atom1 type, atom2 type)
     const void* af_post;   // AfPostT<R> per (group, type)
+    const void* aff;       // AfT<R> force records
+    const int2* aff_index; // per (type k, type j)
     void* afB;             // per (group, atom), R: factor
     void* afS;             // dB/dsum
     void* afW;             // prefactor times dB/dsum (written by the pair kernel)

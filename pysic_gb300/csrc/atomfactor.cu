@@ -22,8 +22,9 @@
 //              so which records apply), B_i and S_i = dB/db at b_i
 //   pair       (pair.cu) the scaled energies and forces, and W_i = S_i P_i
 //   af_force   F_k = sum_j c'(r_kj) u_kj [W_k (records k, j) + W_j (records
-//              j, k)], u_kj the unit vector from k to j; virial of atom k's
-//              own terms, sep (x) (-W_k c' u) as the reference sums it
+//              j, k)], u_kj the unit vector from k to j, a record of both
+//              lists evaluated once; virial of atom k's own terms,
+//              sep (x) (-W_k c' u) as the reference sums it
 // No atomics; with a fixed tile the results are bit-reproducible.
 #include <algorithm>
 #include <map>
@@ -48,7 +49,7 @@ __device__ __forceinline__ void add_at(R (&a)[PG_MAX_AGROUPS], int g, R v) {
 // c(r) and dc/dr of a two-target record (evaluate_bond_order_factor_ /
 // _gradient_coordination, Potentials.f90:5631-5673; _power, 6293-6347)
 template <typename R>
-__device__ __forceinline__ void af_term(const AfT<R>& F, R r, R& c, R& dc) {
+__device__ __forceinline__ void af_term(const AfT<R>& F, R r, R ir, R& c, R& dc) {
     R f, fp;
     smooth<R>(r, F.rc, F.rs, f, fp);
     if (F.kind == 0) {
@@ -56,9 +57,9 @@ __device__ __forceinline__ void af_term(const AfT<R>& F, R r, R& c, R& dc) {
         dc = fp;
         return;
     }
-    const R rn = pow_(F.a / r, F.n);
+    const R rn = powk(F.a * ir, F.n, F.ni);
     c = f * rn;
-    dc = rn * (fp - F.n * f / r);
+    dc = rn * (fp - F.n * f * ir);
 }
 
 template <typename R, int G>
@@ -88,11 +89,12 @@ __global__ void __launch_bounds__(256) af_sum(const __grid_constant__ PairArgs A
             // the reference visits the pair once, from the atom pick makes atom1
             const bool first = pick(i, j, A.off[3 * e], A.off[3 * e + 1], A.off[3 * e + 2]);
             const int2 ix = A.af_index[first ? ti * A.T + tj : tj * A.T + ti];
+            const R ir = rcp_(r);
             for (int t = ix.x; t < ix.x + ix.y; ++t) {
                 const AfT<R> F = recs[t];
                 if (!(r < F.rc)) continue;
                 R c, dc;
-                af_term<R>(F, r, c, dc);
+                af_term<R>(F, r, ir, c, dc);
                 add_at<R>(b, F.group, c);
             }
         }
@@ -161,7 +163,10 @@ __global__ void __launch_bounds__(256) af_force(const __grid_constant__ PairArgs
             yk = A.pos[3 * k + 1];
             zk = A.pos[3 * k + 2];
         }
-        const AfT<R>* recs = (const AfT<R>*)A.af;
+        // one list per (k type, j type): the records of k's factor (k at position
+        // 1, flag 1) and of j's factor (j at position 1, flag 2), a record that is
+        // both evaluated once
+        const AfT<R>* recs = (const AfT<R>*)A.aff;
         for (int e = A.start[k] + lane; e < A.start[k + 1]; e += G) {
             const int j = A.idx[e];
             R x, y, z;
@@ -169,28 +174,23 @@ __global__ void __launch_bounds__(256) af_force(const __grid_constant__ PairArgs
             const R r = sqrt_(x * x + y * y + z * z);
             if (r == R(0)) continue;
             const int tj = A.type[j];
+            const R ir = rcp_(r);
             R own = 0, other = 0;
-            const int2 io = A.af_index[tk * A.T + tj];  // k's factor: k at position 1
+            const int2 io = A.aff_index[tk * A.T + tj];
             for (int t = io.x; t < io.x + io.y; ++t) {
                 const AfT<R> F = recs[t];
                 if (!(r < F.rc)) continue;
                 R c, dc;
-                af_term<R>(F, r, c, dc);
-                R wg = 0;
+                af_term<R>(F, r, ir, c, dc);
+                if (F.flags & 1) {
+                    R wg = 0;
 #pragma unroll
-                for (int q = 0; q < PG_MAX_AGROUPS; ++q)
-                    if (q == F.group) wg = wk[q];
-                own += dc * wg;
+                    for (int q = 0; q < PG_MAX_AGROUPS; ++q)
+                        if (q == F.group) wg = wk[q];
+                    own += dc * wg;
+                }
+                if (F.flags & 2) other += dc * W[(size_t)F.group * A.n + j];
             }
-            const int2 ir2 = A.af_index[tj * A.T + tk];  // j's factor: j at position 1
-            for (int t = ir2.x; t < ir2.x + ir2.y; ++t) {
-                const AfT<R> F = recs[t];
-                if (!(r < F.rc)) continue;
-                R c, dc;
-                af_term<R>(F, r, c, dc);
-                other += dc * W[(size_t)F.group * A.n + j];
-            }
-            const R ir = R(1) / r;
             const R cf = (own + other) * ir;
             fx += cf * x;
             fy += cf * y;
@@ -242,9 +242,38 @@ void fold_atom_factors(pg_context* ctx, const std::map<int, int>& gmap) {
                 F.rs = std::min(ctx->af_soft[r], ctx->af_cut[r]);
                 F.a = p[0];
                 F.n = p[1];
+                F.ni = F.kind == 1 ? integral_exponent(p[1]) : PG_NOT_INT;
+                F.flags = 0;
                 recs.push_back(F);
             }
             ix.y = (int)recs.size() - ix.x;
+        }
+    // force records: per (k type, j type) every two-target record with k at
+    // position 1 and j at 2 (k's factor) or j at 1 and k at 2 (j's factor)
+    std::vector<AfT<double>> frecs;
+    std::vector<int2> findex((size_t)T * T, make_int2(0, 0));
+    for (int tk = 0; tk < T; ++tk)
+        for (int tj = 0; tj < T; ++tj) {
+            int2& ix = findex[(size_t)tk * T + tj];
+            ix.x = (int)frecs.size();
+            for (int r = 0; r < nr; ++r) {
+                if (ctx->af_kind[r] > 1) continue;
+                const bool own = has(ctx->af_m1[r], tk) && has(ctx->af_m2[r], tj);
+                const bool other = has(ctx->af_m1[r], tj) && has(ctx->af_m2[r], tk);
+                if (!own && !other) continue;
+                const double* p = &ctx->af_params[5 * (size_t)r];
+                AfT<double> F{};
+                F.kind = ctx->af_kind[r];
+                F.group = gmap.at(ctx->af_group[r]);
+                F.rc = ctx->af_cut[r];
+                F.rs = std::min(ctx->af_soft[r], ctx->af_cut[r]);
+                F.a = p[0];
+                F.n = p[1];
+                F.ni = F.kind == 1 ? integral_exponent(p[1]) : PG_NOT_INT;
+                F.flags = (own ? 1 : 0) | (other ? 2 : 0);
+                frecs.push_back(F);
+            }
+            ix.y = (int)frecs.size() - ix.x;
         }
     const int ng = std::max(ctx->n_agroups, 1);
     std::vector<AfPostT<double>> post((size_t)ng * T);
@@ -258,10 +287,13 @@ void fold_atom_factors(pg_context* ctx, const std::map<int, int>& gmap) {
             for (int c = 0; c < 5; ++c) q.p[c] = ctx->af_params[5 * (size_t)r + c];
         }
     if (recs.empty()) recs.push_back(AfT<double>{});
-    std::vector<AfT<float>> recs32(recs.size());
-    for (size_t q = 0; q < recs.size(); ++q)
-        recs32[q] = AfT<float>{recs[q].kind, recs[q].group, (float)recs[q].rc, (float)recs[q].rs, (float)recs[q].a,
-                               (float)recs[q].n};
+    if (frecs.empty()) frecs.push_back(AfT<double>{});
+    auto to32 = [](const AfT<double>& q) {
+        return AfT<float>{q.kind, q.group, (float)q.rc, (float)q.rs, (float)q.a, (float)q.n, q.ni, q.flags};
+    };
+    std::vector<AfT<float>> recs32(recs.size()), frecs32(frecs.size());
+    for (size_t q = 0; q < recs.size(); ++q) recs32[q] = to32(recs[q]);
+    for (size_t q = 0; q < frecs.size(); ++q) frecs32[q] = to32(frecs[q]);
     std::vector<AfPostT<float>> post32(post.size());
     for (size_t q = 0; q < post.size(); ++q) {
         post32[q].kind = post[q].kind;
@@ -271,6 +303,9 @@ void fold_atom_factors(pg_context* ctx, const std::map<int, int>& gmap) {
     ctx->d_af.upload(recs.data(), recs.size(), st);
     ctx->d_af32.upload(recs32.data(), recs32.size(), st);
     ctx->d_af_index.upload(index.data(), index.size(), st);
+    ctx->d_aff.upload(frecs.data(), frecs.size(), st);
+    ctx->d_aff32.upload(frecs32.data(), frecs32.size(), st);
+    ctx->d_aff_index.upload(findex.data(), findex.size(), st);
     ctx->d_af_post.upload(post.data(), post.size(), st);
     ctx->d_af_post32.upload(post32.data(), post32.size(), st);
 }
@@ -284,6 +319,8 @@ void set_atom_factor_args(pg_context* ctx, int precision, PairArgs& A) {
     ctx->af_W.resize(m);
     A.af = precision == PG_PREC_FP64 ? (const void*)ctx->d_af.p : (const void*)ctx->d_af32.p;
     A.af_index = ctx->d_af_index.p;
+    A.aff = precision == PG_PREC_FP64 ? (const void*)ctx->d_aff.p : (const void*)ctx->d_aff32.p;
+    A.aff_index = ctx->d_aff_index.p;
     A.af_post = precision == PG_PREC_FP64 ? (const void*)ctx->d_af_post.p : (const void*)ctx->d_af_post32.p;
     A.afB = ctx->af_B.p;
     A.afS = ctx->af_S.p;

@@ -136,7 +136,16 @@ struct PairT {
     int t0, tn;          // tabulated: first row and row count in the context's table rows
     unsigned long long first;  // charge_pair: types of the unpermuted first target (original_elements(1))
     int agroup;          // -1, or the per-atom bond-order group whose factors scale the term
+    int ni;              // power / shift_power: the exponent when it is an integer, else PG_NOT_INT
 };
+
+// marks a non-integer exponent (general pow instead of repeated squaring)
+constexpr int PG_NOT_INT = -1000000;
+
+// the exponent as an int when it is integral and small, else PG_NOT_INT
+inline int integral_exponent(double x) {
+    return (x == (double)(long long)x && x >= -64.0 && x <= 64.0) ? (int)x : PG_NOT_INT;
+}
 
 // Per-atom (level-1) bond-order factors: at most this many groups (Coordinators
 // of per-atom factors) per calculator.
@@ -149,6 +158,8 @@ template <typename R>
 struct AfT {
     int kind, group;  // group: level-1 group index
     R rc, rs, a, n;
+    int ni;     // n when it is an integer, else PG_NOT_INT
+    int flags;  // force records: 1 the first atom's factor, 2 the second atom's, 3 both
 };
 
 // Post-processing of a level-1 group's sum for one atom type: kind -1 none,
@@ -188,7 +199,7 @@ struct TriT {
 template <typename R, typename S>
 inline PairT<R> cast_pair(const PairT<S>& a) {
     return PairT<R>{a.kind, a.group, a.smooth, a.in_bond_kernel, (R)a.p0, (R)a.p1, (R)a.p2, (R)a.p3, (R)a.rc, (R)a.rs,
-                    a.t0, a.tn, a.first, a.agroup};
+                    a.t0, a.tn, a.first, a.agroup, a.ni};
 }
 template <typename R, typename S>
 inline TripT<R> cast_trip(const TripT<S>& a) {
@@ -331,11 +342,15 @@ struct pg_context {
     std::vector<double> af_params, af_cut, af_soft;
     std::vector<uint64_t> af_m1, af_m2;
     std::vector<int> sr_group;           // per single record: coordinator group or -1
+    int pair_lanes = 0;                  // lanes per atom of the full-list kernels (0: by list length)
     int n_agroups = 0;                   // level-1 groups in use
     std::map<int, int> agroup_of;        // coordinator group -> level-1 group
     pg::DevBuf<pg::AfT<double>> d_af;    // folded per oriented type pair, FP64 and FP32
     pg::DevBuf<pg::AfT<float>> d_af32;
     pg::DevBuf<int2> d_af_index;         // per (atom1 type, atom2 type): offset, count into d_af
+    pg::DevBuf<pg::AfT<double>> d_aff;   // force records per (type k, type j), own / partner flags
+    pg::DevBuf<pg::AfT<float>> d_aff32;
+    pg::DevBuf<int2> d_aff_index;
     pg::DevBuf<pg::AfPostT<double>> d_af_post;  // per (group, type)
     pg::DevBuf<pg::AfPostT<float>> d_af_post32;
     // per (group, atom), in the working precision: the factor B, dB/dsum and

@@ -22,6 +22,22 @@ __device__ __forceinline__ float pow_(float x, float y) { return powf(x, y); }
 __device__ __forceinline__ double pow_(double x, double y) { return pow(x, y); }
 __device__ __forceinline__ float sqrt_(float x) { return sqrtf(x); }
 __device__ __forceinline__ double sqrt_(double x) { return sqrt(x); }
+
+// x^k by repeated squaring for an integer k, or pow(x, y) otherwise (k =
+// PG_NOT_INT): power-law terms whose exponent is integral skip the general pow
+template <typename R>
+__device__ __forceinline__ R powk(R x, R y, int k) {
+    if (k == PG_NOT_INT) return pow_(x, y);
+    unsigned a = k < 0 ? (unsigned)(-k) : (unsigned)k;
+    R r = R(1);
+    while (a) {
+        if (a & 1u) r *= x;
+        x *= x;
+        a >>= 1;
+    }
+    return k < 0 ? R(1) / r : r;
+}
+
 __device__ __forceinline__ float erfc_(float x) { return erfcf(x); }
 __device__ __forceinline__ double erfc_(double x) { return erfc(x); }
 // reciprocal: the FP32 path uses the fast approximate division (a few ulp),
@@ -90,7 +106,7 @@ __device__ __forceinline__ void pair_eval(const PairT<R>& P, R r, R& V, R& dV, c
             break;
         }
         case 4: {  // power: eps (a/r)^n (4119-4152)
-            const R t = p0 * pow_(p1 / r, p2);
+            const R t = p0 * powk(p1 / r, p2, P.ni);
             V = t;
             dV = -p2 * t / r;
             break;
@@ -98,8 +114,8 @@ __device__ __forceinline__ void pair_eval(const PairT<R>& P, R r, R& V, R& dV, c
         case 5: {  // shift_power: eps ((r1 - r)/(r1 - r2))^n (4803-4842)
             const R w = p1 - p2;
             const R x = (p1 - r) / w;
-            V = p0 * pow_(x, P.p3);
-            dV = -p0 * P.p3 / w * pow_(x, P.p3 - R(1));
+            V = p0 * powk(x, P.p3, P.ni);
+            dV = -p0 * P.p3 / w * powk(x, P.p3 - R(1), P.ni == PG_NOT_INT ? PG_NOT_INT : P.ni - 1);
             break;
         }
         case 6: {  // tabulated: cubic Hermite on rows (V, d), range p0, scale p1 (4227-4298);

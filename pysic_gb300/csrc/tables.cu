@@ -148,6 +148,7 @@ void fold_tables(pg_context* ctx) {
                     t.p1 = t.p3;  // scale
                 }
                 t.first = r < (int)ctx->pr_first.size() ? ctx->pr_first[r] : 0ull;
+                t.ni = t.kind == 4 ? integral_exponent(t.p2) : t.kind == 5 ? integral_exponent(t.p3) : PG_NOT_INT;
                 t.rc = ctx->pr_cut[r];
                 const double soft = ctx->pr_soft[r];
                 if (soft > 0.0 && soft < t.rc) {

@@ -214,6 +214,9 @@ class Engine:
         L.check(self.lib.pg_get_bond_zeta(self.ctx, L.dptr(z), n.value, ctypes.byref(n)))
         return z[:n.value]
 
+    def set_pair_lanes(self, lanes):
+        L.check(self.lib.pg_set_pair_lanes(self.ctx, int(lanes)))
+
     def set_lanes(self, lanes):
         L.check(self.lib.pg_set_lanes_per_atom(self.ctx, int(lanes)))
 
