@@ -122,7 +122,9 @@ int pg_set_bond_order_factors(pg_context* ctx, int32_t n_records, const double* 
 /* add_bond_order_factor(...) (PyInterface.f90:482-526) for the per-atom
  * (level-1) factors, one record per target tuple, unpermuted: kind 0 neighbors,
  * 1 power_bond (params a, n), 2 c_scale (epsilon, N, C, gamma, min),
- * 3 sqrt_scale (epsilon) (Potentials.f90:5581-5673, 5972-6063, 6223-6436);
+ * 3 sqrt_scale (epsilon), 4 table_bond and 5 table_scale (first row in the
+ * rows of pg_set_pair_tables, rows, range, scale) (Potentials.f90:5581-5673,
+ * 5972-6063, 6223-6765);
  * params 5 per record; mask2 is unused by the one-target scalers; group: the
  * Coordinator's group, shared with the pair and single-atom records.  At most 4
  * such groups; a group cannot also hold Tersoff factors. */

@@ -578,12 +578,43 @@ static double post_process(const ctx_t* X, int t, int group, double raw) {
 
 /* ---- per-atom (level-1) bond-order factors ---- */
 
-/* evaluate_bond_order_factor_coordination (Potentials.f90:5631-5645) and
- * _power (6293-6306): the symmetric two-target factor c(r) */
+/* kinds 0 neighbors, 1 power_bond, 4 table_bond act on pairs; 2 c_scale,
+ * 3 sqrt_scale, 5 table_scale post-process an atom's sum */
+static int afac_two_target(int kind) { return kind == 0 || kind == 1 || kind == 4; }
+
+/* The cubic Hermite form of the tabulated factors (Potentials.f90:6496-6576,
+ * 6663-6765): rows (V, d) from p[0], p[1] rows, range p[2], scale p[3]; value
+ * and derivative at x < range. */
+static void afac_hermite(const double* table, const double* p, double x, double* v, double* dv) {
+    const double* T = table + 2 * (int64_t)p[0];
+    const int n_values = (int)p[1];
+    const double max_r = p[2];
+    const double dr = max_r / (n_values - 1);
+    const int l = (int)floor(x / dr); /* lower_index - 1 */
+    const double t = x / dr - l, t2 = t * t, t3 = t2 * t;
+    *v = p[3] * (T[2 * l] * (2 * t3 - 3 * t2 + 1) + T[2 * l + 1] * dr / max_r * (t3 - 2 * t2 + t) +
+                 T[2 * l + 2] * (3 * t2 - 2 * t3) + T[2 * l + 3] * dr / max_r * (t3 - t2));
+    *dv = p[3] * (T[2 * l] / dr * 6 * (t2 - t) + T[2 * l + 1] / max_r * (3 * t2 - 4 * t + 1) +
+                  T[2 * l + 2] / dr * 6 * (t - t2) + T[2 * l + 3] / max_r * (3 * t2 - 2 * t));
+}
+
+static double afac_table_last(const double* table, const double* p) {
+    return table[2 * ((int64_t)p[0] + (int64_t)p[1] - 1)];
+}
+
+/* evaluate_bond_order_factor_coordination (Potentials.f90:5631-5645), _power
+ * (6293-6306) and _table (6663-6700; beyond the range the last value, neither
+ * scaled nor smoothed): the symmetric two-target factor c(r) */
 static double afac_value(const orc_model* m, int r, double d) {
     const double* p = m->afac_params + 5 * (size_t)r;
     const double f = smooth_factor(d, m->afac_cutoff[r], m->afac_soft[r]);
     if (m->afac_kind[r] == 0) return f;
+    if (m->afac_kind[r] == 4) {
+        if (d >= p[2]) return afac_table_last(m->pair_table, p);
+        double v, dv;
+        afac_hermite(m->pair_table, p, d, &v, &dv);
+        return v * f;
+    }
     return f * pow(p[0] / d, p[1]);
 }
 
@@ -602,6 +633,22 @@ static void afac_gradient(const orc_model* m, int r, const double sep[3], double
         }
         return;
     }
+    if (m->afac_kind[r] == 4) {
+        /* evaluate_bond_order_gradient_table (6711-6765): zero beyond the range;
+           the cut factor's gradient enters inside the smoothing band only.
+           The reference leaves t3 unassigned in this routine; t^3 is used. */
+        for (int c = 0; c < 3; ++c) g11[c] = g12[c] = 0.0;
+        if (d >= p[2]) return;
+        double v, dvv;
+        afac_hermite(m->pair_table, p, d, &v, &dvv);
+        const double decay = smooth_factor(d, m->afac_cutoff[r], m->afac_soft[r]);
+        const double factor = (decay > 0.0 && decay < 1.0) ? v : 0.0;
+        for (int c = 0; c < 3; ++c) {
+            g11[c] = -t[c] * factor - decay * dvv * inv * sep[c];
+            g12[c] = -g11[c];
+        }
+        return;
+    }
     const double n = p[1], ratio_n = pow(p[0] * inv, n);
     const double decay = smooth_factor(d, m->afac_cutoff[r], m->afac_soft[r]);
     for (int c = 0; c < 3; ++c) {
@@ -614,15 +661,23 @@ static void afac_gradient(const orc_model* m, int r, const double sep[3], double
  * (core_post_process_bond_order_factors, Core.f90:2697-2712) */
 static int afac_post_index(const orc_model* m, int t, int group) {
     for (int r = 0; r < m->n_afac; ++r)
-        if ((m->afac_kind[r] == 2 || m->afac_kind[r] == 3) && has(m->afac_mask1[r], t) && m->afac_group[r] == group)
-            return r;
+        if (!afac_two_target(m->afac_kind[r]) && has(m->afac_mask1[r], t) && m->afac_group[r] == group) return r;
     return -1;
 }
 
-/* post_process_bond_order_factor_scaler_1 (Potentials.f90:6021-6035) and _sqrt (6402-6414) */
+/* post_process_bond_order_factor_scaler_1 (Potentials.f90:6021-6035), _sqrt
+ * (6402-6414) and _table (6496-6532: 0 for sums <= 0, the last value, unscaled,
+ * beyond the range) */
 static double afac_post(const orc_model* m, int r, double raw) {
     const double* p = m->afac_params + 5 * (size_t)r;
     if (m->afac_kind[r] == 3) return raw <= 0.0 ? 0.0 : p[0] * sqrt(raw);
+    if (m->afac_kind[r] == 5) {
+        if (raw <= 0.0) return 0.0;
+        if (raw >= p[2]) return afac_table_last(m->pair_table, p);
+        double v, dv;
+        afac_hermite(m->pair_table, p, raw, &v, &dv);
+        return v;
+    }
     const double dN = (raw - p[1]) * p[2];
     return dN > p[4] ? p[0] * dN / (1.0 + exp(p[3] * dN)) : 0.0;
 }
@@ -631,6 +686,12 @@ static double afac_post(const orc_model* m, int r, double raw) {
 static double afac_post_grad(const orc_model* m, int r, double raw, double g) {
     const double* p = m->afac_params + 5 * (size_t)r;
     if (m->afac_kind[r] == 3) return raw <= 0.0 ? 0.0 : p[0] / (2.0 * sqrt(raw)) * g;
+    if (m->afac_kind[r] == 5) { /* 6541-6576 */
+        if (raw <= 0.0 || raw >= p[2]) return 0.0;
+        double v, dv;
+        afac_hermite(m->pair_table, p, raw, &v, &dv);
+        return dv * g;
+    }
     const double dN = (raw - p[1]) * p[2];
     if (!(dN > p[4])) return 0.0;
     const double expo = exp(p[3] * dN), inv_exp = 1.0 / (1.0 + expo);
@@ -662,7 +723,7 @@ static void afac_sums(ctx_t* X) {
                 if (!(d < X->maxbr[i])) continue;
                 const int tj = s->type[j];
                 for (int r = 0; r < m->n_afac; ++r) {
-                    if (m->afac_kind[r] > 1 || !has(m->afac_mask1[r], ti)) continue;
+                    if (!afac_two_target(m->afac_kind[r]) || !has(m->afac_mask1[r], ti)) continue;
                     if (m->afac_group[r] != g || !(m->afac_cutoff[r] > d)) continue;
                     if (!has(m->afac_mask2[r], tj)) continue;
                     const double c = afac_value(m, r, d);
@@ -702,7 +763,7 @@ static void afac_forces(const ctx_t* X, int group, int a, double prefactor, doub
         const int tj = s->type[j];
         for (int r = 0; r < m->n_afac; ++r) {
             if (!has(m->afac_mask1[r], ta) || m->afac_group[r] != group || !(m->afac_cutoff[r] > d)) continue;
-            if (!has(m->afac_mask2[r], tj) || m->afac_kind[r] > 1) continue;
+            if (!has(m->afac_mask2[r], tj) || !afac_two_target(m->afac_kind[r])) continue;
             double g11[3], g12[3], n1[3], n2[3];
             afac_gradient(m, r, sep, d, g11, g12);
             for (int c = 0; c < 3; ++c) {

@@ -82,9 +82,11 @@ typedef struct {
        unpermuted (calculator.py:1372-1430); they share the group numbering of
        pair_group / bond_group */
     int32_t n_afac;
-    const int32_t* afac_kind;     /* 0 neighbors, 1 power_bond, 2 c_scale, 3 sqrt_scale */
+    const int32_t* afac_kind;     /* 0 neighbors, 1 power_bond, 2 c_scale, 3 sqrt_scale, 4 table_bond,
+                                     5 table_scale */
     const double* afac_params;    /* 5 per record: power_bond (a, n); c_scale (epsilon, N, C, gamma, min);
-                                     sqrt_scale (epsilon) */
+                                     sqrt_scale (epsilon); table_bond / table_scale (first row in
+                                     pair_table, rows, range, scale) */
     const double* afac_cutoff;
     const double* afac_soft;
     const uint64_t* afac_mask1;

@@ -505,7 +505,7 @@ int pg_set_atom_factors(pg_context* ctx, int32_t n, const int32_t* kind, const d
         pg::require(n == 0 || (kind && params && cutoff && soft && mask1 && mask2 && group), PG_ERR_INVALID,
                     "null record arrays");
         for (int r = 0; r < n; ++r) {
-            pg::require(kind[r] >= 0 && kind[r] <= 3, PG_ERR_UNSUPPORTED, "unknown per-atom bond-order factor kind");
+            pg::require(kind[r] >= 0 && kind[r] <= 5, PG_ERR_UNSUPPORTED, "unknown per-atom bond-order factor kind");
             pg::require(std::isfinite(cutoff[r]) && std::isfinite(soft[r]) && group[r] >= 0, PG_ERR_INVALID,
                         "invalid per-atom bond-order factor record");
         }

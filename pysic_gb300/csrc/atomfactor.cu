@@ -1,5 +1,5 @@
 // atomfactor.cu -- per-atom (level-1) bond-order factors: neighbors,
-// power_bond, c_scale, sqrt_scale.
+// power_bond, table_bond, c_scale, sqrt_scale, table_scale.
 //
 // Replaces, for Coordinators of per-atom factors, core_calculate_bond_order_
 // factors (Core.f90:2015-2404, the two-target level-1 part),
@@ -46,15 +46,45 @@ __device__ __forceinline__ void add_at(R (&a)[PG_MAX_AGROUPS], int g, R v) {
         if (q == g) a[q] += v;
 }
 
-// c(r) and dc/dr of a two-target record (evaluate_bond_order_factor_ /
-// _gradient_coordination, Potentials.f90:5631-5673; _power, 6293-6347)
+// Cubic Hermite value and derivative at x < range on rows (V, d)
+// (Potentials.f90:6496-6576, 6663-6765)
 template <typename R>
-__device__ __forceinline__ void af_term(const AfT<R>& F, R r, R ir, R& c, R& dc) {
+__device__ __forceinline__ void af_hermite(const R* T, int nv, R range, R scale, R x, R& v, R& dv) {
+    const R dr = range / (R)(nv - 1);
+    const R u = x / dr;
+    const int l = min(max((int)u, 0), nv - 2);
+    const R t = u - (R)l, t2 = t * t, t3 = t2 * t;
+    const R* a = T + 2 * l;
+    v = scale * (a[0] * (R(2) * t3 - R(3) * t2 + R(1)) + a[1] * dr / range * (t3 - R(2) * t2 + t) +
+                 a[2] * (R(3) * t2 - R(2) * t3) + a[3] * dr / range * (t3 - t2));
+    dv = scale * (a[0] / dr * R(6) * (t2 - t) + a[1] / range * (R(3) * t2 - R(4) * t + R(1)) +
+                  a[2] / dr * R(6) * (t - t2) + a[3] / range * (R(3) * t2 - R(2) * t));
+}
+
+// c(r) and dc/dr of a two-target record (evaluate_bond_order_factor_ /
+// _gradient_coordination, Potentials.f90:5631-5673; _power, 6293-6347;
+// _table, 6663-6765: beyond the range the last value, neither scaled nor
+// smoothed, with zero gradient)
+template <typename R>
+__device__ __forceinline__ void af_term(const AfT<R>& F, R r, R ir, const R* tab, R& c, R& dc) {
     R f, fp;
     smooth<R>(r, F.rc, F.rs, f, fp);
     if (F.kind == 0) {
         c = f;
         dc = fp;
+        return;
+    }
+    if (F.kind == 4) {
+        const R* T = tab + 2 * (long long)F.t0;
+        if (r >= F.a) {
+            c = T[2 * (F.tn - 1)];
+            dc = R(0);
+            return;
+        }
+        R v, dv;
+        af_hermite<R>(T, F.tn, F.a, F.n, r, v, dv);
+        c = v * f;
+        dc = v * fp + f * dv;
         return;
     }
     const R rn = powk(F.a * ir, F.n, F.ni);
@@ -94,7 +124,7 @@ __global__ void __launch_bounds__(256) af_sum(const __grid_constant__ PairArgs A
                 const AfT<R> F = recs[t];
                 if (!(r < F.rc)) continue;
                 R c, dc;
-                af_term<R>(F, r, ir, c, dc);
+                af_term<R>(F, r, ir, (const R*)A.tab, c, dc);
                 add_at<R>(b, F.group, c);
             }
         }
@@ -118,6 +148,17 @@ __global__ void __launch_bounds__(256) af_sum(const __grid_constant__ PairArgs A
                 const R sq = sqrt_(raw);
                 B = P.p[0] * sq;
                 S = P.p[0] / (R(2) * sq);
+            }
+        } else if (P.kind == 5) {  // table_scale: 0 for b <= 0, the last value (unscaled) beyond the range
+            const R* T = (const R*)A.tab + 2 * (long long)P.t0;
+            if (raw <= R(0)) {
+                B = R(0);
+                S = R(0);
+            } else if (raw >= P.p[2]) {
+                B = T[2 * (P.tn - 1)];
+                S = R(0);
+            } else {
+                af_hermite<R>(T, P.tn, P.p[2], P.p[3], raw, B, S);
             }
         } else if (P.kind == 2) {  // c_scale: epsilon dN / (1 + exp(gamma dN)), dN = C (b - N) > min
             const R dN = (raw - P.p[1]) * P.p[2];
@@ -181,7 +222,7 @@ __global__ void __launch_bounds__(256) af_force(const __grid_constant__ PairArgs
                 const AfT<R> F = recs[t];
                 if (!(r < F.rc)) continue;
                 R c, dc;
-                af_term<R>(F, r, ir, c, dc);
+                af_term<R>(F, r, ir, (const R*)A.tab, c, dc);
                 if (F.flags & 1) {
                     R wg = 0;
 #pragma unroll
@@ -225,6 +266,20 @@ void fold_atom_factors(pg_context* ctx, const std::map<int, int>& gmap) {
     const int T = std::max(ctx->n_types, 1);
     const int nr = (int)ctx->af_kind.size();
     auto has = [](uint64_t m, int t) { return ((m >> t) & 1ull) != 0; };
+    auto two_target = [](int kind) { return kind == 0 || kind == 1 || kind == 4; };
+    // tabulated factors: params first row, rows, range, scale; the kernels read
+    // rows t0 .. t0 + tn - 1 only, checked here
+    const size_t rows = ctx->pr_table.size() / 2;
+    for (int r = 0; r < nr; ++r)
+        if (ctx->af_kind[r] == 4 || ctx->af_kind[r] == 5) {
+            const double* p = &ctx->af_params[5 * (size_t)r];
+            require(p[0] >= 0.0 && p[1] >= 2.0 && p[0] + p[1] <= (double)rows && p[2] > 0.0, PG_ERR_INVALID,
+                    "tabulated bond-order factor: table rows or range out of bounds");
+        }
+    auto set_table = [&](auto& F, const double* p) {
+        F.t0 = (int)p[0];
+        F.tn = (int)p[1];
+    };
     std::vector<AfT<double>> recs;
     std::vector<int2> index((size_t)T * T, make_int2(0, 0));
     for (int ta = 0; ta < T; ++ta)
@@ -232,7 +287,7 @@ void fold_atom_factors(pg_context* ctx, const std::map<int, int>& gmap) {
             int2& ix = index[(size_t)ta * T + tb];
             ix.x = (int)recs.size();
             for (int r = 0; r < nr; ++r) {
-                if (ctx->af_kind[r] > 1 || !has(ctx->af_m1[r], ta) || !has(ctx->af_m2[r], tb)) continue;
+                if (!two_target(ctx->af_kind[r]) || !has(ctx->af_m1[r], ta) || !has(ctx->af_m2[r], tb)) continue;
                 const double* p = &ctx->af_params[5 * (size_t)r];
                 AfT<double> F{};
                 F.kind = ctx->af_kind[r];
@@ -240,10 +295,11 @@ void fold_atom_factors(pg_context* ctx, const std::map<int, int>& gmap) {
                 F.rc = ctx->af_cut[r];
                 // smoothening_factor with soft = cutoff - margin; evaluated below the cutoff only
                 F.rs = std::min(ctx->af_soft[r], ctx->af_cut[r]);
-                F.a = p[0];
-                F.n = p[1];
+                F.a = F.kind == 4 ? p[2] : p[0];
+                F.n = F.kind == 4 ? p[3] : p[1];
                 F.ni = F.kind == 1 ? integral_exponent(p[1]) : PG_NOT_INT;
                 F.flags = 0;
+                if (F.kind == 4) set_table(F, p);
                 recs.push_back(F);
             }
             ix.y = (int)recs.size() - ix.x;
@@ -257,7 +313,7 @@ void fold_atom_factors(pg_context* ctx, const std::map<int, int>& gmap) {
             int2& ix = findex[(size_t)tk * T + tj];
             ix.x = (int)frecs.size();
             for (int r = 0; r < nr; ++r) {
-                if (ctx->af_kind[r] > 1) continue;
+                if (!two_target(ctx->af_kind[r])) continue;
                 const bool own = has(ctx->af_m1[r], tk) && has(ctx->af_m2[r], tj);
                 const bool other = has(ctx->af_m1[r], tj) && has(ctx->af_m2[r], tk);
                 if (!own && !other) continue;
@@ -267,29 +323,31 @@ void fold_atom_factors(pg_context* ctx, const std::map<int, int>& gmap) {
                 F.group = gmap.at(ctx->af_group[r]);
                 F.rc = ctx->af_cut[r];
                 F.rs = std::min(ctx->af_soft[r], ctx->af_cut[r]);
-                F.a = p[0];
-                F.n = p[1];
+                F.a = F.kind == 4 ? p[2] : p[0];
+                F.n = F.kind == 4 ? p[3] : p[1];
                 F.ni = F.kind == 1 ? integral_exponent(p[1]) : PG_NOT_INT;
                 F.flags = (own ? 1 : 0) | (other ? 2 : 0);
+                if (F.kind == 4) set_table(F, p);
                 frecs.push_back(F);
             }
             ix.y = (int)frecs.size() - ix.x;
         }
     const int ng = std::max(ctx->n_agroups, 1);
     std::vector<AfPostT<double>> post((size_t)ng * T);
-    for (auto& q : post) q = AfPostT<double>{-1, {0, 0, 0, 0, 0}};
+    for (auto& q : post) q = AfPostT<double>{-1, {0, 0, 0, 0, 0}, 0, 0};
     for (int t = 0; t < T; ++t)
         for (int r = 0; r < nr; ++r) {
-            if (ctx->af_kind[r] < 2 || !has(ctx->af_m1[r], t)) continue;
+            if (two_target(ctx->af_kind[r]) || !has(ctx->af_m1[r], t)) continue;
             AfPostT<double>& q = post[(size_t)gmap.at(ctx->af_group[r]) * T + t];
             if (q.kind >= 0) continue;  // the first scaler of the element in the group
             q.kind = ctx->af_kind[r];
             for (int c = 0; c < 5; ++c) q.p[c] = ctx->af_params[5 * (size_t)r + c];
+            if (q.kind == 5) set_table(q, &ctx->af_params[5 * (size_t)r]);
         }
     if (recs.empty()) recs.push_back(AfT<double>{});
     if (frecs.empty()) frecs.push_back(AfT<double>{});
     auto to32 = [](const AfT<double>& q) {
-        return AfT<float>{q.kind, q.group, (float)q.rc, (float)q.rs, (float)q.a, (float)q.n, q.ni, q.flags};
+        return AfT<float>{q.kind, q.group, (float)q.rc, (float)q.rs, (float)q.a, (float)q.n, q.ni, q.flags, q.t0, q.tn};
     };
     std::vector<AfT<float>> recs32(recs.size()), frecs32(frecs.size());
     for (size_t q = 0; q < recs.size(); ++q) recs32[q] = to32(recs[q]);
@@ -298,6 +356,8 @@ void fold_atom_factors(pg_context* ctx, const std::map<int, int>& gmap) {
     for (size_t q = 0; q < post.size(); ++q) {
         post32[q].kind = post[q].kind;
         for (int c = 0; c < 5; ++c) post32[q].p[c] = (float)post[q].p[c];
+        post32[q].t0 = post[q].t0;
+        post32[q].tn = post[q].tn;
     }
     cudaStream_t st = ctx->stream;
     ctx->d_af.upload(recs.data(), recs.size(), st);

@@ -156,10 +156,11 @@ constexpr int PG_MAX_AGROUPS = 4;
 // (Potentials.f90:5631-5645, 6293-6306).
 template <typename R>
 struct AfT {
-    int kind, group;  // group: level-1 group index
-    R rc, rs, a, n;
+    int kind, group;  // kind 0 neighbors, 1 power_bond, 4 table_bond; group: level-1 group index
+    R rc, rs, a, n;   // power_bond: a, n; table_bond: range, scale
     int ni;     // n when it is an integer, else PG_NOT_INT
     int flags;  // force records: 1 the first atom's factor, 2 the second atom's, 3 both
+    int t0, tn; // table_bond: first row and rows in the context's table rows
 };
 
 // Post-processing of a level-1 group's sum for one atom type: kind -1 none,
@@ -167,8 +168,9 @@ struct AfT {
 // (Potentials.f90:6021-6063, 6402-6436).
 template <typename R>
 struct AfPostT {
-    int kind;
+    int kind;   // 5: table_scale, p[2] range, p[3] scale, rows t0 .. t0 + tn - 1
     R p[5];
+    int t0, tn;
 };
 
 // Tersoff triplet parameters for (centre type, j type, k type) of group 0.

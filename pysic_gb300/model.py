@@ -285,6 +285,10 @@ def compile_model(atoms, potentials, coulomb=None):
                 # per-atom factors keep the reference's global order (coordinator,
                 # factor, target tuple): the first scaler of an element wins
                 # (core_post_process_bond_order_factors, Core.f90:2697-2712)
+                if bkind in ("table_bond", "table_scale"):
+                    # [id, range, scale] -> [first row, rows, range, scale] (create_bond_order_factor
+                    # reads table_XXXX.txt like the tabulated potential, Potentials.f90:5200-5213)
+                    flat = _table_record(M, flat)
                 for tg in bond.get_symbols() or []:
                     M.afac_kind.append(core.ATOM_FACTOR_KIND[bkind])
                     M.afac_params.append((flat + [0.0] * 5)[:5])

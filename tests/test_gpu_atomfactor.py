@@ -143,3 +143,31 @@ def test_many_system_launch_rejects_per_atom_factors():
     calc = pysic.Pysic(atoms, _pieces(W.sutton_chen_potentials(("Cu",))))
     with pytest.raises(EngineError):
         BatchedPysic([calc]).evaluate("fp64")
+
+
+@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+def test_tabulated_factors_parity(precision, tmp_path, monkeypatch):
+    """table_bond summed per atom and post-processed by table_scale
+    (Potentials.f90:6496-6765), scaling a constant and a pair potential, on
+    two elements, against the oracle."""
+    monkeypatch.chdir(tmp_path)
+    r = np.linspace(0.0, 6.0, 161)
+    v = np.exp(-r / 1.1)
+    np.savetxt(str(tmp_path / "table_0011.txt"), np.column_stack([v, 6.0 * (-v / 1.1)]))
+    x = np.linspace(0.0, 3.0, 121)
+    np.savetxt(str(tmp_path / "table_0012.txt"), np.column_stack([np.sqrt(x + 0.2), 1.5 / np.sqrt(x + 0.2)]))
+    atoms = W.fcc_alloy(4, symbols=("Cu", "Ag"), noise=0.08, seed=19)
+    bond = pysic.BondOrderParameters("table_bond", parameters=[[], [11, 6.0, 0.9]], cutoff=4.0, cutoff_margin=0.6,
+                                     symbols=[["Cu", "Cu"], ["Cu", "Ag"], ["Ag", "Ag"]])
+    scale = pysic.BondOrderParameters("table_scale", parameters=[[12, 3.0, -1.3], []], symbols=[["Cu"]])
+    P = pysic.Potential
+    pots = [P("constant", parameters=[0.7], symbols=[["Cu"], ["Ag"]], coordinator=pysic.Coordinator([scale, bond])),
+            P("exponential", symbols=[["Ag", "Ag"]], parameters=[0.4, 1.3], cutoff=4.2,
+              coordinator=pysic.Coordinator([scale, bond]))]
+    if precision == "fp64":
+        _check_fp64(atoms, pots)
+        return
+    ref = oracle_all(atoms, pots)
+    got = engine_all(atoms, pots, None, "mixed")
+    assert abs(got["energy"] - ref["energy"]) / len(atoms) <= 1e-5
+    assert np.abs(got["forces"] - ref["forces"]).max() <= 1e-4 * max(1.0, np.abs(ref["forces"]).max())

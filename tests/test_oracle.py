@@ -406,3 +406,34 @@ def test_oracle_atom_factor_sums_follow_the_picked_pair():
     np.testing.assert_array_equal(raw, expect)
     np.testing.assert_array_equal(fac, expect)
     assert oracle_all(atoms, [pot])["energy"] == pytest.approx(expect[sym == "Cu"].sum(), abs=1e-12)
+
+
+def test_oracle_tabulated_factors_gradient(tmp_path, monkeypatch):
+    """table_bond (Potentials.f90:6663-6765) summed per atom and post-processed
+    by table_scale (6496-6576), scaling a constant: forces are minus the energy
+    gradient (one element), and a sum beyond table_scale's range gives the last
+    tabulated value, unscaled."""
+    monkeypatch.chdir(tmp_path)
+    _write_exp_table(str(tmp_path), 11, 6.0, 161, A=1.0, rho=1.1)
+    x = np.linspace(0.0, 3.0, 121)
+    np.savetxt(str(tmp_path / "table_0012.txt"), np.column_stack([np.sqrt(x + 0.2), 3.0 * 0.5 / np.sqrt(x + 0.2)]))
+    atoms = W.fcc_alloy(4, a0=3.61, symbols=("Cu",), noise=0.08, seed=8)
+    bond = pysic.BondOrderParameters("table_bond", parameters=[[], [11, 6.0, 0.9]], cutoff=4.0, cutoff_margin=0.6,
+                                     symbols=[["Cu", "Cu"]])
+    scale = pysic.BondOrderParameters("table_scale", parameters=[[12, 3.0, -1.3], []], symbols=[["Cu"]])
+    pot = pysic.Potential("constant", parameters=[0.7], symbols=[["Cu"]], coordinator=pysic.Coordinator([scale, bond]))
+    model = compile_model(atoms, [pot])
+    lists = oracle_lists(atoms, [pot])
+    raw, fac = oracle.atom_factors(atoms.get_positions(), atoms.get_cell(), atoms.get_pbc(), model, *lists)
+    assert 0.5 < raw.min() and raw.max() < 3.0
+    np.testing.assert_allclose(fac, -1.3 * np.sqrt(raw + 0.2), rtol=1e-6)
+    for idx in (2, 40):
+        fd, f = _fd_forces(atoms, [pot], idx, h=1e-5)
+        np.testing.assert_allclose(f, fd, atol=2e-7, rtol=1e-6)
+    # a range the sums exceed: the last row's value, unscaled
+    short = pysic.BondOrderParameters("table_scale", parameters=[[12, 0.5, -1.3], []], symbols=[["Cu"]])
+    pot2 = pysic.Potential("constant", parameters=[0.7], symbols=[["Cu"]],
+                           coordinator=pysic.Coordinator([short, bond]))
+    _, fac2 = oracle.atom_factors(atoms.get_positions(), atoms.get_cell(), atoms.get_pbc(),
+                                  compile_model(atoms, [pot2]), *lists)
+    np.testing.assert_allclose(fac2, np.sqrt(3.0 + 0.2), rtol=1e-15)
