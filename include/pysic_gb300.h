@@ -236,6 +236,13 @@ int pg_optimize_charges(pg_context* ctx, int32_t precision, int32_t max_iteratio
  * itself without a scaler; zeros for a group without per-atom factors.
  * n entries. */
 int pg_get_atom_factors(pg_context* ctx, int32_t precision, int32_t group, double* factors);
+/* Gradients of a Coordinator group's per-atom factors at the current positions
+ * (calculate_bond_order_gradients / _of_factor, PyInterface.f90:605-650, over
+ * core_calculate_bond_order_gradients, Core.f90:1157-1989): of_factor 0, the
+ * gradient of every atom's factor with respect to moving `atom`; 1, of `atom`'s
+ * factor with respect to moving every atom.  gradients: n x 3 (0-based atom). */
+int pg_get_atom_factor_gradients(pg_context* ctx, int32_t precision, int32_t group, int32_t atom, int32_t of_factor,
+                                 double* gradients);
 
 /* Per ordered bond (CSR entry of the engine's short list) Tersoff sums zeta_ij of
  * group 0: the quantity core_calculate_pair_bond_order_factor (Core.f90:2439-2637)

@@ -1490,3 +1490,51 @@ int orc_atom_factors(const orc_system* s, const orc_model* m, const orc_nblist* 
     free_ctx(&X);
     return 0;
 }
+
+/* core_calculate_bond_order_gradients (Core.f90:1157-1644, two-target level-1
+ * part) with core_post_process_bond_order_gradients (2842-2934): the gradient of
+ * every atom's factor with respect to moving atom a (of_factor = 0), or, as
+ * core_calculate_bond_order_gradients_of_factor (1979-1989) with
+ * core_post_process_bond_order_gradients_of_factor (2972-3080), the gradient of
+ * atom a's factor with respect to moving every atom (of_factor = 1).  Records of
+ * a's element at position 1, over all of a's neighbours; out is n x 3. */
+int orc_atom_factor_gradients(const orc_system* s, const orc_model* m, const orc_nblist* nb, int group, int a,
+                              int of_factor, double* out) {
+    if (a < 0 || a >= s->n) return -1;
+    ctx_t X;
+    setup_ctx(&X, s, m, nb);
+    const int n = s->n;
+    double* temp = (double*)calloc(3 * (size_t)(n ? n : 1), sizeof(double));
+    const int ta = s->type[a];
+    for (int e = nb->start[a]; e < nb->start[a + 1]; ++e) {
+        const int j = nb->idx[e];
+        double sep[3];
+        separation(&X.C, s->pos + 3 * (size_t)a, s->pos + 3 * (size_t)j, nb->off + 3 * (size_t)e, sep);
+        const double d = sqrt(dot3(sep, sep));
+        if (!(d < X.maxbr[a])) continue;
+        const int tj = s->type[j];
+        for (int r = 0; r < m->n_afac; ++r) {
+            if (!has(m->afac_mask1[r], ta) || m->afac_group[r] != group || !(m->afac_cutoff[r] > d)) continue;
+            if (!has(m->afac_mask2[r], tj) || !afac_two_target(m->afac_kind[r])) continue;
+            double g11[3], g12[3];
+            afac_gradient(m, r, sep, d, g11, g12);
+            for (int c = 0; c < 3; ++c) {
+                temp[3 * (size_t)a + c] += g11[c];
+                /* the factor is symmetric: the gradient of atom 2's term with
+                   respect to atom 1 is g11, with respect to atom 2 it is g12 */
+                temp[3 * (size_t)j + c] += of_factor ? g12[c] : g11[c];
+            }
+        }
+    }
+    for (int i = 0; i < n; ++i) {
+        const int owner = of_factor ? a : i;
+        const int post = afac_post_index(m, s->type[owner], group);
+        const double raw = group < X.n_groups ? X.af_raw[(size_t)group * n + owner] : 0.0;
+        for (int c = 0; c < 3; ++c)
+            out[3 * (size_t)i + c] = post >= 0 ? afac_post_grad(m, post, raw, temp[3 * (size_t)i + c])
+                                               : temp[3 * (size_t)i + c];
+    }
+    free(temp);
+    free_ctx(&X);
+    return 0;
+}

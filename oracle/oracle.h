@@ -120,6 +120,12 @@ int orc_evaluate(const orc_system* sys, const orc_model* model, const orc_nblist
 int orc_atom_factors(const orc_system* sys, const orc_model* model, const orc_nblist* nb,
                      int group, double* raw, double* factor);
 
+/* Gradients of the per-atom factors of group g (Core.f90:1157-1644, 2842-3080):
+ * of_factor 0: of every atom's factor with respect to moving atom a; 1: of atom
+ * a's factor with respect to moving every atom.  out: n x 3. */
+int orc_atom_factor_gradients(const orc_system* sys, const orc_model* model, const orc_nblist* nb,
+                              int group, int atom, int of_factor, double* out);
+
 int orc_bond_zeta(const orc_system* sys, const orc_model* model, const orc_nblist* nb,
                   int group, double* zeta_per_entry);
 

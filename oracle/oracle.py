@@ -246,6 +246,21 @@ def atom_factors(positions, cell, pbc, model, counts, idx, off, group=0):
     return raw[:s.n], fac[:s.n]
 
 
+def atom_factor_gradients(positions, cell, pbc, model, counts, idx, off, group, atom, of_factor=False):
+    """Gradients of one group's per-atom factors (n x 3): of every factor with
+    respect to moving `atom`, or of `atom`'s factor with respect to every atom."""
+    keep = _Keep()
+    s = _system(keep, positions, None, model.types, cell, pbc)
+    m = _model(keep, model, s.n)
+    nb = _nblist(keep, counts, idx, off)
+    out = np.zeros((max(s.n, 1), 3))
+    rc = lib().orc_atom_factor_gradients(ctypes.byref(s), ctypes.byref(m), ctypes.byref(nb), int(group), int(atom),
+                                         1 if of_factor else 0, _d(out))
+    if rc != 0:
+        raise ValueError("atom index out of range")
+    return out[:s.n]
+
+
 def bond_zeta(positions, cell, pbc, model, counts, idx, off, group=0):
     keep = _Keep()
     s = _system(keep, positions, None, model.types, cell, pbc)

@@ -58,6 +58,8 @@ _SIGNATURES = {
     "pg_set_single_groups": (ctypes.c_int, [_ctx, ctypes.c_int32, _c_int_p]),
     "pg_set_pair_lanes": (ctypes.c_int, [_ctx, ctypes.c_int32]),
     "pg_get_atom_factors": (ctypes.c_int, [_ctx, ctypes.c_int32, ctypes.c_int32, _c_double_p]),
+    "pg_get_atom_factor_gradients": (ctypes.c_int, [_ctx, ctypes.c_int32, ctypes.c_int32, ctypes.c_int32,
+                                                    ctypes.c_int32, _c_double_p]),
     "pg_set_atom_factors": (ctypes.c_int, [_ctx, ctypes.c_int32, _c_int_p, _c_double_p, _c_double_p, _c_double_p,
                                            _c_u64_p, _c_u64_p, _c_int_p]),
     "pg_set_bond_order_factors": (ctypes.c_int, [_ctx, ctypes.c_int32, _c_double_p, _c_double_p, _c_double_p,

@@ -663,6 +663,18 @@ int pg_get_atom_factors(pg_context* ctx, int32_t precision, int32_t group, doubl
     });
 }
 
+int pg_get_atom_factor_gradients(pg_context* ctx, int32_t precision, int32_t group, int32_t atom, int32_t of_factor,
+                                 double* gradients) {
+    return guarded([&] {
+        check_ctx(ctx);
+        use_device(ctx);
+        pg::require(gradients != nullptr, PG_ERR_INVALID, "null output");
+        pg::require(atom >= 0 && atom < ctx->n, PG_ERR_INVALID, "atom index out of range");
+        pg::evaluate(ctx, precision, PG_WANT_ENERGY);  // the sums and dB/dsum at the current positions
+        pg::atom_factor_gradients(ctx, precision, group, atom, of_factor ? 1 : 0, gradients);
+    });
+}
+
 int pg_calculate_energy(pg_context* ctx, int32_t precision, double* energy) {
     return pg_calculate(ctx, precision, PG_WANT_ENERGY, energy, nullptr, nullptr, nullptr);
 }

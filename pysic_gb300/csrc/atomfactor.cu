@@ -258,7 +258,72 @@ __global__ void __launch_bounds__(256) af_force(const __grid_constant__ PairArgs
     }
 }
 
+// Gradients of group g's factors (core_calculate_bond_order_gradients and
+// _of_factor, Core.f90:1157-1989, with the post-processing of 2842-3080): one
+// thread walks atom a's list in order, so the sums are deterministic; out is
+// n x 3, zeroed by the caller.  of_factor 0: every factor with respect to
+// moving a; 1: a's factor with respect to moving every atom.
+template <typename R>
+__global__ void af_grad(const __grid_constant__ PairArgs A, int g, int a, int of_factor, double* __restrict__ out) {
+    if (blockIdx.x != 0 || threadIdx.x != 0) return;
+    const int ta = A.type[a];
+    double xa = 0, ya = 0, za = 0;
+    if constexpr (sizeof(R) == 8) {
+        xa = A.pos[3 * a];
+        ya = A.pos[3 * a + 1];
+        za = A.pos[3 * a + 2];
+    }
+    const AfT<R>* recs = (const AfT<R>*)A.af;
+    for (int e = A.start[a]; e < A.start[a + 1]; ++e) {
+        const int j = A.idx[e];
+        R x, y, z;
+        pair_vector<R>(A, a, e, xa, ya, za, x, y, z);
+        const R r = sqrt_(x * x + y * y + z * z);
+        if (r == R(0)) continue;
+        const R ir = rcp_(r);
+        const int2 ix = A.af_index[ta * A.T + A.type[j]];
+        for (int t = ix.x; t < ix.x + ix.y; ++t) {
+            const AfT<R> F = recs[t];
+            if (F.group != g || !(r < F.rc)) continue;
+            R c, dc;
+            af_term<R>(F, r, ir, (const R*)A.tab, c, dc);
+            // gradient of the pair's factor with respect to a: -c'(r) u
+            const double s = -(double)(dc * ir);
+            const double gx = s * (double)x, gy = s * (double)y, gz = s * (double)z;
+            out[3 * a] += gx;
+            out[3 * a + 1] += gy;
+            out[3 * a + 2] += gz;
+            const double sj = of_factor ? -1.0 : 1.0;
+            out[3 * j] += sj * gx;
+            out[3 * j + 1] += sj * gy;
+            out[3 * j + 2] += sj * gz;
+        }
+    }
+    const R* S = (const R*)A.afS + (size_t)g * A.n;
+    for (int i = 0; i < A.n; ++i) {
+        const double f = (double)S[of_factor ? a : i];
+        out[3 * i] *= f;
+        out[3 * i + 1] *= f;
+        out[3 * i + 2] *= f;
+    }
+}
+
 }  // namespace
+
+void atom_factor_gradients(pg_context* ctx, int precision, int group, int atom, int of_factor, double* out) {
+    const size_t n = (size_t)std::max(ctx->n, 1);
+    ctx->af_grad.resize(3 * n);
+    PG_CUDA(cudaMemsetAsync(ctx->af_grad.p, 0, sizeof(double) * 3 * n, ctx->stream));
+    auto it = ctx->agroup_of.find(group);
+    if (it != ctx->agroup_of.end()) {
+        const PairArgs A = make_pair_args(ctx, precision, PG_WANT_FORCES, true, true, nullptr, nullptr);
+        if (precision == PG_PREC_FP64) af_grad<double><<<1, 32, 0, ctx->stream>>>(A, it->second, atom, of_factor, ctx->af_grad.p);
+        else af_grad<float><<<1, 32, 0, ctx->stream>>>(A, it->second, atom, of_factor, ctx->af_grad.p);
+        PG_CHECK_LAUNCH();
+    }
+    ctx->af_grad.download(out, 3 * (size_t)ctx->n, ctx->stream);
+    PG_CUDA(cudaStreamSynchronize(ctx->stream));
+}
 
 // Fold the per-atom factor records into per-(atom1 type, atom2 type) lists and
 // per-(group, type) scalers.  gmap: coordinator group id -> level-1 index.

@@ -358,6 +358,7 @@ struct pg_context {
     // per (group, atom), in the working precision: the factor B, dB/dsum and
     // W = (the atom's prefactor) dB/dsum
     pg::DevBuf<double> af_B, af_S, af_W;
+    pg::DevBuf<double> af_grad;          // n x 3: factor gradients handed to the caller
 
     // Ewald
     bool ewald = false;
@@ -557,6 +558,7 @@ void launch_chi_cache_apply(pg_context* ctx, int precision, const int* skip);
 // factors (before the pair kernel), stage 1 adds their forces and virial
 void fold_atom_factors(pg_context* ctx, const std::map<int, int>& gmap);
 void launch_atom_factors(pg_context* ctx, int precision, int stage, bool first_f, FxAcc* acc, const int* skip);
+void atom_factor_gradients(pg_context* ctx, int precision, int group, int atom, int of_factor, double* out);
 // triplet.cu: three-body potentials (bond_bend)
 constexpr int PG_MAX_TRIPLET_RECORDS = 64;
 void launch_triplets(pg_context* ctx, int precision, int flags, bool first_f, FxAcc* acc, const int* skip);

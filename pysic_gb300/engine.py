@@ -207,6 +207,13 @@ class Engine:
         L.check(self.lib.pg_get_atom_factors(self.ctx, int(precision), int(group), L.dptr(out)))
         return out[:self.n]
 
+    def atom_factor_gradients(self, group, atom, of_factor=False, precision=L.PREC_FP64):
+        """n x 3 gradients of a Coordinator group's per-atom factors."""
+        out = np.zeros((max(self.n, 1), 3))
+        L.check(self.lib.pg_get_atom_factor_gradients(self.ctx, int(precision), int(group), int(atom),
+                                                      1 if of_factor else 0, L.dptr(out)))
+        return out[:self.n]
+
     def bond_zeta(self):
         n = ctypes.c_int64(0)
         L.check(self.lib.pg_get_bond_zeta(self.ctx, None, 0, ctypes.byref(n)))

@@ -418,6 +418,25 @@ class Coordinator:
     def get_bond_order_factors(self):
         return self.bond_order_factors
 
+    def get_bond_order_gradients(self, atom_index):
+        """Gradients (n x 3) of every atom's factor of this group with respect to
+        moving atom `atom_index` (bondorder.py:508-519), computed on the device."""
+        calc = self._attached()
+        return calc.engine.atom_factor_gradients(self.group_index, atom_index, False, calc._prec())
+
+    def get_bond_order_gradients_of_factor(self, atom_index):
+        """Gradients (n x 3) of atom `atom_index`'s factor of this group with
+        respect to moving every atom (bondorder.py:521-534)."""
+        calc = self._attached()
+        return calc.engine.atom_factor_gradients(self.group_index, atom_index, True, calc._prec())
+
+    def _attached(self):
+        calc = self._calculator
+        if calc is None:
+            raise InvalidCoordinatorError("The coordinator is not attached to a calculator.")
+        calc.set_core()
+        return calc
+
 
 class CoulombSummation:
     """Ewald summation parameters (pysic/interactions/coulomb.py:6-176):

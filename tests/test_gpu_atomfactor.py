@@ -171,3 +171,25 @@ def test_tabulated_factors_parity(precision, tmp_path, monkeypatch):
     got = engine_all(atoms, pots, None, "mixed")
     assert abs(got["energy"] - ref["energy"]) / len(atoms) <= 1e-5
     assert np.abs(got["forces"] - ref["forces"]).max() <= 1e-4 * max(1.0, np.abs(ref["forces"]).max())
+
+
+def test_coordinator_gradients_match_the_oracle():
+    """Coordinator.get_bond_order_gradients / _of_factor (bondorder.py:508-534)
+    on the device against the oracle's restatement of
+    core_calculate_bond_order_gradients (Core.f90:1157-1989), two elements."""
+    atoms = W.fcc_alloy(4, symbols=("Cu", "Ag"), noise=0.06, seed=20)
+    pots = _pieces(W.sutton_chen_potentials(("Cu", "Ag")))
+    calc = pysic.Pysic(atoms, pots, precision="fp64")
+    atoms.set_calculator(calc)
+    model = compile_model(atoms, pots)
+    lists = oracle_lists(atoms, pots)
+    args = (atoms.get_positions(), atoms.get_cell(), atoms.get_pbc(), model) + tuple(lists)
+    for c in [p.get_coordinator() for p in pots if p.get_coordinator() is not None]:
+        g = c.get_group_index()
+        for a in (0, 33, 101):
+            got = c.get_bond_order_gradients(a)
+            want = oracle.atom_factor_gradients(*args, group=g, atom=a)
+            np.testing.assert_allclose(got, want, rtol=1e-10, atol=1e-12)
+            got = c.get_bond_order_gradients_of_factor(a)
+            want = oracle.atom_factor_gradients(*args, group=g, atom=a, of_factor=True)
+            np.testing.assert_allclose(got, want, rtol=1e-10, atol=1e-12)

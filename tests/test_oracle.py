@@ -437,3 +437,38 @@ def test_oracle_tabulated_factors_gradient(tmp_path, monkeypatch):
     _, fac2 = oracle.atom_factors(atoms.get_positions(), atoms.get_cell(), atoms.get_pbc(),
                                   compile_model(atoms, [pot2]), *lists)
     np.testing.assert_allclose(fac2, np.sqrt(3.0 + 0.2), rtol=1e-15)
+
+
+def test_oracle_atom_factor_gradients_match_finite_differences():
+    """core_calculate_bond_order_gradients and _of_factor (Core.f90:1157-1989)
+    restated: for one element, the gradient of every atom's Sutton-Chen density
+    factor with respect to one atom, and of one atom's factor with respect to
+    every atom, equal finite differences of the factors."""
+    atoms = W.fcc_alloy(4, a0=3.61, symbols=("Cu",), noise=0.07, seed=9)
+    calc = pysic.Pysic()
+    calc.add_potential(W.sutton_chen_potentials(("Cu",)))
+    pots = calc.get_potentials()
+    model = compile_model(atoms, pots)
+    lists = oracle_lists(atoms, pots)
+    cell, pbc = atoms.get_cell(), atoms.get_pbc()
+    pos0 = atoms.get_positions()
+    a, h = 17, 1e-6
+    g_all = oracle.atom_factor_gradients(pos0, cell, pbc, model, *lists, group=0, atom=a)
+    g_of = oracle.atom_factor_gradients(pos0, cell, pbc, model, *lists, group=0, atom=a, of_factor=True)
+    num_all = np.zeros((len(atoms), 3))
+    for c in range(3):
+        p1, p2 = pos0.copy(), pos0.copy()
+        p1[a, c] += h
+        p2[a, c] -= h
+        f1 = oracle.atom_factors(p1, cell, pbc, model, *lists)[1]
+        f2 = oracle.atom_factors(p2, cell, pbc, model, *lists)[1]
+        num_all[:, c] = (f1 - f2) / (2 * h)
+    np.testing.assert_allclose(g_all, num_all, atol=1e-6)
+    for b in [a] + list(np.nonzero(np.abs(g_of).sum(axis=1))[0][:4]):
+        for c in range(3):
+            p1, p2 = pos0.copy(), pos0.copy()
+            p1[b, c] += h
+            p2[b, c] -= h
+            d = (oracle.atom_factors(p1, cell, pbc, model, *lists)[1][a] -
+                 oracle.atom_factors(p2, cell, pbc, model, *lists)[1][a]) / (2 * h)
+            assert g_of[b, c] == pytest.approx(d, abs=1e-6)
