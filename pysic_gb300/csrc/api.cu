@@ -171,7 +171,7 @@ void enqueue_evaluation(pg_context* ctx, int precision, int flags, int G, const 
         if (wantF) first_f = false;
         if (wantC) first_chi = false;
     }
-    if (run_af && wantF) {
+    if (run_af && wantF && !ctx->af_fused) {
         launch_atom_factors(ctx, precision, 1, first_f, acc, skip);
         first_f = false;
     }

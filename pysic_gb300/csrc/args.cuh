@@ -40,7 +40,8 @@ struct PairArgs {
     const int2* aff_index; // per (type k, type j)
     void* afB;             // per (group, atom), R: factor
     void* afS;             // dB/dsum
-    void* afW;             // prefactor times dB/dsum (written by the pair kernel)
+    void* afW;             // prefactor times dB/dsum (written by the pair kernel, or by af_sum when fused)
+    int af_fused;          // no scaled pair term: af_sum writes W, the pair kernel adds the factor forces
 };
 
 template <typename R>

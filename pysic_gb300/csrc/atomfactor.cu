@@ -34,6 +34,7 @@
 #include "common.cuh"
 #include "kernels.cuh"
 #include "pairvec.cuh"
+#include "atomfactor.cuh"
 
 namespace pg {
 
@@ -44,52 +45,6 @@ __device__ __forceinline__ void add_at(R (&a)[PG_MAX_AGROUPS], int g, R v) {
 #pragma unroll
     for (int q = 0; q < PG_MAX_AGROUPS; ++q)
         if (q == g) a[q] += v;
-}
-
-// Cubic Hermite value and derivative at x < range on rows (V, d)
-// (Potentials.f90:6496-6576, 6663-6765)
-template <typename R>
-__device__ __forceinline__ void af_hermite(const R* T, int nv, R range, R scale, R x, R& v, R& dv) {
-    const R dr = range / (R)(nv - 1);
-    const R u = x / dr;
-    const int l = min(max((int)u, 0), nv - 2);
-    const R t = u - (R)l, t2 = t * t, t3 = t2 * t;
-    const R* a = T + 2 * l;
-    v = scale * (a[0] * (R(2) * t3 - R(3) * t2 + R(1)) + a[1] * dr / range * (t3 - R(2) * t2 + t) +
-                 a[2] * (R(3) * t2 - R(2) * t3) + a[3] * dr / range * (t3 - t2));
-    dv = scale * (a[0] / dr * R(6) * (t2 - t) + a[1] / range * (R(3) * t2 - R(4) * t + R(1)) +
-                  a[2] / dr * R(6) * (t - t2) + a[3] / range * (R(3) * t2 - R(2) * t));
-}
-
-// c(r) and dc/dr of a two-target record (evaluate_bond_order_factor_ /
-// _gradient_coordination, Potentials.f90:5631-5673; _power, 6293-6347;
-// _table, 6663-6765: beyond the range the last value, neither scaled nor
-// smoothed, with zero gradient)
-template <typename R>
-__device__ __forceinline__ void af_term(const AfT<R>& F, R r, R ir, const R* tab, R& c, R& dc) {
-    R f, fp;
-    smooth<R>(r, F.rc, F.rs, f, fp);
-    if (F.kind == 0) {
-        c = f;
-        dc = fp;
-        return;
-    }
-    if (F.kind == 4) {
-        const R* T = tab + 2 * (long long)F.t0;
-        if (r >= F.a) {
-            c = T[2 * (F.tn - 1)];
-            dc = R(0);
-            return;
-        }
-        R v, dv;
-        af_hermite<R>(T, F.tn, F.a, F.n, r, v, dv);
-        c = v * f;
-        dc = v * fp + f * dv;
-        return;
-    }
-    const R rn = powk(F.a * ir, F.n, F.ni);
-    c = f * rn;
-    dc = rn * (fp - F.n * f * ir);
 }
 
 template <typename R, int G>
@@ -176,6 +131,19 @@ __global__ void __launch_bounds__(256) af_sum(const __grid_constant__ PairArgs A
         }
         Bv[(size_t)g * A.n + i] = B;
         Sv[(size_t)g * A.n + i] = S;
+        if (A.af_fused) {
+            // no scaled pair term: the prefactor is the scaled singlets' V, known
+            // here, and the pair kernel adds the factor forces in its own pass
+            double V = 0.0;
+            const int2 sx = A.sindex[ti];
+            for (int t = sx.x; t < sx.x + sx.y; ++t) {
+                const SingleTerm T1 = A.sterms[t];
+                if (T1.agroup != g) continue;
+                V += T1.kind == 1 ? T1.p[0]
+                                  : -(T1.p[0] * A.pos[3 * i] + T1.p[1] * A.pos[3 * i + 1] + T1.p[2] * A.pos[3 * i + 2]);
+            }
+            ((R*)A.afW)[(size_t)g * A.n + i] = (R)((double)S * V);
+        }
     }
 }
 
@@ -204,39 +172,17 @@ __global__ void __launch_bounds__(256) af_force(const __grid_constant__ PairArgs
             yk = A.pos[3 * k + 1];
             zk = A.pos[3 * k + 2];
         }
-        // one list per (k type, j type): the records of k's factor (k at position
-        // 1, flag 1) and of j's factor (j at position 1, flag 2), a record that is
-        // both evaluated once
-        const AfT<R>* recs = (const AfT<R>*)A.aff;
         for (int e = A.start[k] + lane; e < A.start[k + 1]; e += G) {
             const int j = A.idx[e];
             R x, y, z;
             pair_vector<R>(A, k, e, xk, yk, zk, x, y, z);
             const R r = sqrt_(x * x + y * y + z * z);
             if (r == R(0)) continue;
-            const int tj = A.type[j];
-            const R ir = rcp_(r);
-            R own = 0, other = 0;
-            const int2 io = A.aff_index[tk * A.T + tj];
-            for (int t = io.x; t < io.x + io.y; ++t) {
-                const AfT<R> F = recs[t];
-                if (!(r < F.rc)) continue;
-                R c, dc;
-                af_term<R>(F, r, ir, (const R*)A.tab, c, dc);
-                if (F.flags & 1) {
-                    R wg = 0;
-#pragma unroll
-                    for (int q = 0; q < PG_MAX_AGROUPS; ++q)
-                        if (q == F.group) wg = wk[q];
-                    own += dc * wg;
-                }
-                if (F.flags & 2) other += dc * W[(size_t)F.group * A.n + j];
-            }
-            const R cf = (own + other) * ir;
+            R cf, h;
+            af_entry<R>(A, wk, tk, j, A.type[j], r, rcp_(r), cf, h);
             fx += cf * x;
             fy += cf * y;
             fz += cf * z;
-            const R h = -own * ir;
             w0 += h * x * x;
             w1 += h * y * y;
             w2 += h * z * z;
@@ -450,6 +396,7 @@ void set_atom_factor_args(pg_context* ctx, int precision, PairArgs& A) {
     A.afB = ctx->af_B.p;
     A.afS = ctx->af_S.p;
     A.afW = ctx->af_W.p;
+    A.af_fused = ctx->af_fused ? 1 : 0;
 }
 
 // stage 0: the sums and factors (before the pair kernel); stage 1: the forces

@@ -346,6 +346,7 @@ struct pg_context {
     std::vector<int> sr_group;           // per single record: coordinator group or -1
     int pair_lanes = 0;                  // lanes per atom of the full-list kernels (0: by list length)
     int n_agroups = 0;                   // level-1 groups in use
+    bool af_fused = false;               // no scaled pair term: factor forces inside the pair kernel
     std::map<int, int> agroup_of;        // coordinator group -> level-1 group
     pg::DevBuf<pg::AfT<double>> d_af;    // folded per oriented type pair, FP64 and FP32
     pg::DevBuf<pg::AfT<float>> d_af32;

@@ -17,6 +17,7 @@
 #include "common.cuh"
 #include "kernels.cuh"
 #include "pairvec.cuh"
+#include "atomfactor.cuh"
 
 namespace pg {
 
@@ -27,7 +28,8 @@ __device__ __forceinline__ double powi_(double x, int n) {
     return r;
 }
 
-template <typename R, int G>
+// AF: also add the per-atom factor forces (no scaled pair term; W from af_sum)
+template <typename R, int G, bool AF = false>
 __device__ __forceinline__ void pair_body(const PairArgs& A, int blk) {
     __shared__ Fx128 wsum[256 / 32][7];
     __shared__ unsigned done;
@@ -43,8 +45,14 @@ __device__ __forceinline__ void pair_body(const PairArgs& A, int blk) {
     R pre[PG_MAX_AGROUPS] = {};  // per-atom factor groups: this atom's prefactors (half of each pair's V f)
     const bool wantE = A.flags & PG_WANT_ENERGY, wantF = A.flags & PG_WANT_FORCES, wantC = A.flags & PG_WANT_ENEGS;
     int ti = 0;
+    R wk[PG_MAX_AGROUPS] = {};
     if (act) {
         ti = A.type[i];
+        if constexpr (AF) {
+#pragma unroll
+            for (int g = 0; g < PG_MAX_AGROUPS; ++g)
+                if (g < A.ng) wk[g] = ((const R*)A.afW)[(size_t)g * A.n + i];
+        }
         const R qi = charge_of<R>(A, i);
         const R ew_rc = (R)A.ew_rc, ew_is2 = (R)A.ew_is2, ew_k = (R)A.ew_k, ew_c2 = (R)A.ew_c2,
                 ew_isq2 = (R)A.ew_isq2;
@@ -120,11 +128,19 @@ __device__ __forceinline__ void pair_body(const PairArgs& A, int blk) {
             }
             en += R(0.5) * U;
             // force on i: U'(r) r_hat; half of the pair virial sep (x) F_j, F_j = -U' r_hat
-            const R c = dU * ir;
+            R c = dU * ir;
+            R h = R(-0.5) * c;
+            if constexpr (AF) {
+                if (wantF) {
+                    R cf, hv;
+                    af_entry<R>(A, wk, ti, j, tj, r, ir, cf, hv);
+                    c += cf;
+                    h += hv;
+                }
+            }
             fx += c * x;
             fy += c * y;
             fz += c * z;
-            const R h = R(-0.5) * c;
             w0 += h * x * x;
             w1 += h * y * y;
             w2 += h * z * z;
@@ -170,7 +186,7 @@ __device__ __forceinline__ void pair_body(const PairArgs& A, int blk) {
         }
     }
     // W_i = dB/dsum times the prefactor, for the per-atom factor forces
-    if (wantF && A.ng > 0) {
+    if (wantF && A.ng > 0 && !AF) {
 #pragma unroll
         for (int q = 0; q < PG_MAX_AGROUPS; ++q) {
             if (q >= A.ng) break;
@@ -215,9 +231,9 @@ __device__ __forceinline__ void pair_body(const PairArgs& A, int blk) {
     }
 }
 
-template <typename R, int G>
+template <typename R, int G, bool AF>
 __global__ void __launch_bounds__(256) pair_kernel(const __grid_constant__ PairArgs A) {
-    pair_body<R, G>(A, blockIdx.x);
+    pair_body<R, G, AF>(A, blockIdx.x);
 }
 
 // many systems in one launch (tiles[t] = system, block of that system)
@@ -347,7 +363,13 @@ void launch_pair_kernel_skip(pg_context* ctx, int precision, int flags, bool fir
     const int nbk = pair_kernel_blocks(ctx->n, G);
     const int threads = pair_atoms_per_block(ctx->n, G) * G;
     cudaStream_t st = ctx->stream;
-#define PG_PAIR_LAUNCH(R_, G_) pair_kernel<R_, G_><<<nbk, threads, 0, st>>>(A)
+#define PG_PAIR_LAUNCH(R_, G_)                                                   \
+    do {                                                                         \
+        if (A.af_fused && (flags & PG_WANT_FORCES))                              \
+            pair_kernel<R_, G_, true><<<nbk, threads, 0, st>>>(A);               \
+        else                                                                     \
+            pair_kernel<R_, G_, false><<<nbk, threads, 0, st>>>(A);              \
+    } while (0)
     if (precision == PG_PREC_FP64) {
         if (G == 8) PG_PAIR_LAUNCH(double, 8);
         else if (G == 16) PG_PAIR_LAUNCH(double, 16);

@@ -192,6 +192,11 @@ void fold_tables(pg_context* ctx) {
         sindex[t].y = (int)sterms.size() - sindex[t].x;
     }
     ctx->have_singles = !sterms.empty();
+    {
+        bool scaled_pairs = false;
+        for (const auto& t : terms) scaled_pairs = scaled_pairs || t.agroup >= 0;
+        ctx->af_fused = ctx->n_agroups > 0 && !scaled_pairs;
+    }
     ctx->have_pair_kernel_terms = pair_kernel_terms;
     ctx->have_charge_pairs = charge_pairs;
 
