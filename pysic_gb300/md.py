@@ -10,6 +10,12 @@ update, operation for operation, but the steps run on the GPU
 neighbour list is rebuilt when an atom has moved more than skin/2 (the
 FastNeighborList / ASE update policy), and the host is visited only for
 rebuilds and for observers.  ASE itself is not needed.
+
+With a ChargeRelaxation attached to the calculator, every force call of the
+reference relaxes the charges first (Pysic.get_forces ->
+ChargeRelaxation.charge_relaxation).  The steps then alternate host-side kicks
+and drifts (the same update, operation for operation) with the calculator's
+device relaxation loop and force evaluation.
 """
 import math
 
@@ -62,10 +68,31 @@ class VelocityVerlet:
         calc._invalidate()
         return r
 
+    def _run_relaxing(self, steps):
+        """ASE's update around the calculator's relaxation and forces."""
+        atoms = self.atoms
+        if self.nsteps == 0:
+            self.call_observers()
+        forces = atoms.get_forces()
+        for _ in range(int(steps)):
+            p = atoms.get_momenta()
+            p += 0.5 * self.dt * forces
+            masses = atoms.get_masses()[:, np.newaxis]
+            r = atoms.get_positions()
+            atoms.set_positions(r + self.dt * p / masses)
+            atoms.set_momenta(p)
+            forces = atoms.get_forces()
+            atoms.set_momenta(atoms.get_momenta() + 0.5 * self.dt * forces)
+            self.nsteps += 1
+            self.call_observers()
+        return True
+
     def run(self, steps=50):
         calc = self.atoms.get_calculator()
         if calc is None:
             raise MissingAtomsError("the atoms have no Pysic calculator")
+        if calc.get_charge_relaxation() is not None:
+            return self._run_relaxing(steps)
         calc.set_atoms(self.atoms)
         calc.set_core()  # engine, tables and lists up to date for these atoms
         eng = calc.engine

@@ -110,3 +110,41 @@ def test_energy_is_conserved():
     dyn.run(400)
     kinetic = 0.5 * float((atoms.get_momenta() ** 2 / m).sum())
     assert max(abs(e - e0) for e in energies) < 2e-3 * kinetic
+
+
+def test_verlet_relaxes_the_charges_at_every_step():
+    """With a ChargeRelaxation on the calculator every force call relaxes the
+    charges first (Pysic.get_forces); the dynamics do the same at every step:
+    the same trajectory and charges as ASE's update around get_forces, and the
+    final charges equalise the electronegativities."""
+    from pysic_gb300 import workloads as W
+
+    def make():
+        atoms = W.sio2_box(60, seed=31)
+        atoms.set_initial_charges(np.zeros(len(atoms)))
+        rng = np.random.default_rng(31)
+        m = atoms.get_masses()[:, None]
+        p = rng.normal(0.0, 1.0, (len(atoms), 3)) * np.sqrt(m * 8.617333e-5 * 300.0)
+        atoms.set_momenta(p - p.mean(axis=0))
+        pots, coul = W.sio2_potentials(real_cutoff=5.5, sigma=1.6)
+        calc = pysic.Pysic(atoms, pots, coulomb=coul, precision="fp64")
+        pysic.ChargeRelaxation("dynamic", calculator=calc, parameters=[2000, 0.05, 1.0, 3.0, 1e-7])
+        return atoms, calc
+
+    dt, steps = 0.5 * FS, 6
+    a_host, c_host = make()
+    r_h, p_h = _host_verlet(a_host, c_host, dt, steps)
+    a_dev, c_dev = make()
+    a_dev.set_calculator(c_dev)
+    seen = []
+    dyn = pysic.VelocityVerlet(a_dev, dt)
+    dyn.attach(lambda: seen.append(c_dev.get_atoms().get_initial_charges().copy()), interval=2)
+    dyn.run(steps)
+    assert np.array_equal(a_dev.get_positions(), r_h)
+    assert np.array_equal(a_dev.get_momenta(), p_h)
+    q = c_dev.get_atoms().get_initial_charges()
+    assert np.array_equal(q, c_host.get_atoms().get_initial_charges())
+    assert np.abs(q).max() > 0.1 and len(seen) == 4
+    assert not np.array_equal(seen[1], seen[3])  # the charges follow the moving atoms
+    chi = c_dev.get_electronegativities()
+    assert np.abs(chi - chi.mean()).max() < 1e-6
