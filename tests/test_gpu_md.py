@@ -128,7 +128,7 @@ def test_verlet_relaxes_the_charges_at_every_step():
         atoms.set_momenta(p - p.mean(axis=0))
         pots, coul = W.sio2_potentials(real_cutoff=5.5, sigma=1.6)
         calc = pysic.Pysic(atoms, pots, coulomb=coul, precision="fp64")
-        pysic.ChargeRelaxation("dynamic", calculator=calc, parameters=[2000, 0.05, 1.0, 3.0, 1e-7])
+        calc.set_charge_relaxation(pysic.ChargeRelaxation("dynamic", parameters=[2000, 0.05, 1.0, 3.0, 1e-7]))
         return atoms, calc
 
     dt, steps = 0.5 * FS, 6
