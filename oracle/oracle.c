@@ -972,11 +972,56 @@ static void* loop_range(void* arg) {
                 if (!has(m->pair_mask2[r], tj)) continue;
                 const int kind = m->pair_kind[r];
                 /* non-charge pair potentials have zero electronegativity */
-                if (J->what == 2 && kind != 7) continue;
+                if (J->what == 2 && kind < 7) continue;
                 const double* p = m->pair_params + 4 * (size_t)r;
                 const int grp = m->pair_group[r];
                 const int sm = X->smoothened[r];
                 const double rc = m->pair_cutoff[r], rs = X->smooth_soft[r];
+                if (kind == 8) {
+                    /* charge_exp, Potentials.f90:3691-3903: epsilon exp((xi_1 D_1 + xi_2 D_2)/2),
+                       D(q) = Rmax + |beta (Qmax - q)|^eta, parameters swapped unless atom1
+                       is the unpermuted first target; rows from p[0] hold eps, Rmax1, Rmin1,
+                       Qmax1, Qmin1, Rmax2, Rmin2, Qmax2, Qmin2, xi1, xi2, eta1, eta2, beta1,
+                       beta2; no force routine, so only the cut factor's gradient acts */
+                    const double* c = m->pair_table + 2 * (int64_t)p[0];
+                    const double q1 = s->charge[i], q2 = s->charge[j];
+                    const int direct = has(m->pair_first[r], ti);
+                    const double r2 = c[direct ? 1 : 5], r3 = c[direct ? 5 : 1];
+                    const double r4 = c[direct ? 3 : 7], r5 = c[direct ? 7 : 3];
+                    const double r6 = c[direct ? 11 : 12], r7 = c[direct ? 12 : 11];
+                    const double r8 = c[direct ? 13 : 14], r9 = c[direct ? 14 : 13];
+                    const double d3 = c[direct ? 9 : 10], d4 = c[direct ? 10 : 9];
+                    const double d5 = r8 * (r4 - q1), d6 = r9 * (r5 - q2);
+                    const double d1 = r2 + pow(fabs(d5), r6), d2 = r3 + pow(fabs(d6), r7);
+                    const double v = c[0] * exp(0.5 * (d3 * d1 + d4 * d2));
+                    const double cut = sm ? smooth_factor(d, rc, rs) : 1.0;
+                    if (J->what == 0) {
+                        J->energy += v * cut;
+                    } else if (J->what == 1) {
+                        if (sm) {
+                            const double dv = smooth_deriv(d, rc, rs);
+                            double p2[3];
+                            for (int c3 = 0; c3 < 3; ++c3) {
+                                const double g = dir[c3] * dv;
+                                F[3 * (size_t)i + c3] += v * g;
+                                p2[c3] = -v * g;
+                                F[3 * (size_t)j + c3] += p2[c3];
+                            }
+                            st[0] += sep[0] * p2[0];
+                            st[1] += sep[1] * p2[1];
+                            st[2] += sep[2] * p2[2];
+                            st[3] += sep[1] * p2[2];
+                            st[4] += sep[0] * p2[2];
+                            st[5] += sep[0] * p2[1];
+                        }
+                    } else {
+                        const double e2 = v * d4 * 0.5 * r7 * pow(fabs(d6), r7 - 1.0) * copysign(1.0, d6) * r9;
+                        const double e1 = v * d3 * 0.5 * r6 * pow(fabs(d5), r6 - 1.0) * copysign(1.0, d5) * r8;
+                        chi[i] += e1 * cut;
+                        chi[j] += e2 * cut;
+                    }
+                    continue;
+                }
                 if (kind == 7) {
                     /* charge_pair, Potentials.f90:4415-4513: epsilon q1^n1 q2^n2, the
                        exponents swapped unless atom1 is the unpermuted first target;

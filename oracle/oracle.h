@@ -43,7 +43,9 @@ typedef struct {
     int32_t n_pair;
     const int32_t* pair_kind;     /* 0 LJ, 1 exponential, 2 Buckingham, 3 spring, 4 power, 5 shift_power,
                                      6 tabulated (params: first row, rows, range, scale),
-                                     7 charge_pair (epsilon, n1, n2) */
+                                     7 charge_pair (epsilon, n1, n2),
+                                     8 charge_exp (first of 8 pair_table rows holding its 11 parameters
+                                     and the derived eta1, eta2, beta1, beta2) */
     const double* pair_params;    /* 4 per record */
     const double* pair_cutoff;
     const double* pair_soft;      /* cutoff - cutoff_margin, as passed to add_potential */

@@ -108,6 +108,33 @@ __device__ __forceinline__ void pair_body(const PairArgs& A, int blk) {
                     }
                     continue;
                 }
+                if (P.kind == 8) {
+                    // charge_exp, V = eps exp((xi_1 D_1(q_1) + xi_2 D_2(q_2))/2),
+                    // D(q) = Rmax + |beta (Qmax - q)|^eta, with the parameters of the
+                    // unpermuted first target on the pair's atom1 when its type is that
+                    // target's (Potentials.f90:3691-3903; no r dependence but the cut)
+                    const R* c = (const R*)A.tab + 2 * (long long)P.t0;
+                    const bool first = pick(i, j, A.off[3 * e], A.off[3 * e + 1], A.off[3 * e + 2]);
+                    const R qj = charge_of<R>(A, j);
+                    const R q1 = first ? qi : qj, q2 = first ? qj : qi;
+                    const bool direct = (P.first >> (first ? ti : tj)) & 1ull;
+                    const int a1 = direct ? 0 : 4, a2 = direct ? 4 : 0;  // Rmax at 1 + a, Qmax at 3 + a
+                    const R eta1 = c[direct ? 11 : 12], eta2 = c[direct ? 12 : 11];
+                    const R beta1 = c[direct ? 13 : 14], beta2 = c[direct ? 14 : 13];
+                    const R xi1 = c[direct ? 9 : 10], xi2 = c[direct ? 10 : 9];
+                    const R d5 = beta1 * (c[3 + a1] - q1), d6 = beta2 * (c[3 + a2] - q2);
+                    const R D1 = c[1 + a1] + pow_(fabs(d5), eta1), D2 = c[1 + a2] + pow_(fabs(d6), eta2);
+                    R f = R(1), fp = R(0);
+                    if (P.smooth) smooth<R>(r, P.rc, P.rs, f, fp);
+                    const R v = c[0] * exp_(R(0.5) * (xi1 * D1 + xi2 * D2));
+                    U += v * f;
+                    dU += v * fp;
+                    if (wantC) {
+                        chi += first ? v * xi1 * R(0.5) * eta1 * pow_(fabs(d5), eta1 - R(1)) * copysign(R(1), d5) * beta1 * f
+                                     : v * xi2 * R(0.5) * eta2 * pow_(fabs(d6), eta2 - R(1)) * copysign(R(1), d6) * beta2 * f;
+                    }
+                    continue;
+                }
                 if (!(wantE || wantF)) continue;
                 R V, dV;
                 pair_term<R>(P, r, V, dV, (const R*)A.tab);

@@ -131,12 +131,18 @@ void fold_tables(pg_context* ctx) {
                 const int g = ctx->pr_group[r];
                 t.group = g >= 0 && g == tersoff_gid ? 0 : -1;
                 t.agroup = g >= 0 && g != tersoff_gid ? gmap.at(g) : -1;
-                require(!(t.agroup >= 0 && t.kind == 7), PG_ERR_UNSUPPORTED,
+                require(!(t.agroup >= 0 && t.kind >= 7), PG_ERR_UNSUPPORTED,
                         "bond-order scaling of charge_pair is not evaluated by the GB300 engine");
                 t.p0 = ctx->pr_params[4 * (size_t)r];
                 t.p1 = ctx->pr_params[4 * (size_t)r + 1];
                 t.p2 = ctx->pr_params[4 * (size_t)r + 2];
                 t.p3 = ctx->pr_params[4 * (size_t)r + 3];
+                if (t.kind == 8) {  // charge_exp: its 15 parameters as 8 rows of the table array
+                    t.t0 = (int)t.p0;
+                    t.tn = 8;
+                    require(t.t0 >= 0 && (size_t)t.t0 + 8 <= ctx->pr_table.size() / 2, PG_ERR_INVALID,
+                            "charge_exp: parameter rows out of bounds");
+                }
                 if (t.kind == 6) {  // tabulated: params first row, rows, range, scale
                     t.t0 = (int)t.p0;
                     t.tn = (int)t.p1;
@@ -159,8 +165,8 @@ void fold_tables(pg_context* ctx) {
                     t.rs = t.rc;
                 }
                 // charge-dependent pair terms stay in the pair kernel (electronegativities)
-                t.in_bond_kernel = bond && t.kind != 7 && t.agroup < 0 && (t.group >= 0 || t.rc <= bo_radius);
-                if (t.kind == 7) charge_pairs = true;
+                t.in_bond_kernel = bond && t.kind < 7 && t.agroup < 0 && (t.group >= 0 || t.rc <= bo_radius);
+                if (t.kind >= 7) charge_pairs = true;
                 if (!t.in_bond_kernel) pair_kernel_terms = true;
                 terms.push_back(t);
             }

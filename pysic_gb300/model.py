@@ -177,6 +177,25 @@ def _table_record(M, params):
     return [float(first), float(len(rows)), float(params[1]), float(params[2])]
 
 
+def _charge_exp_record(M, params):
+    """charge_exp's 11 parameters and the derived eta1, eta2, beta1, beta2
+    (calculate_derived_parameters_charge_exp, Potentials.f90:3751-3766) as 8
+    rows of the table array; the record keeps the first row."""
+    p = [np.float64(x) for x in params]
+    with np.errstate(all="ignore"):  # C pow semantics: a negative base needs an integral exponent
+        eta1 = np.log(p[1] / (p[1] - p[2])) / np.log(p[3] / (p[3] - p[4]))
+        eta2 = np.log(p[5] / (p[5] - p[6])) / np.log(p[7] / (p[7] - p[8]))
+        beta1 = np.power(p[2] - p[1], 1.0 / eta1) / (p[3] - p[4])
+        beta2 = np.power(p[6] - p[5], 1.0 / eta2) / (p[7] - p[8])
+    p = [float(x) for x in p]
+    block = p + [float(eta1), float(eta2), float(beta1), float(beta2), 0.0]
+    if not all(np.isfinite(block)):
+        raise InvalidParametersError("charge_exp: parameters give no finite eta / beta")
+    first = len(M.pair_table) // 2
+    M.pair_table.extend(block)
+    return [float(first), 0.0, 0.0, 0.0]
+
+
 def compile_model(atoms, potentials, coulomb=None):
     potentials = list(potentials or [])
     M = Model()
@@ -230,8 +249,10 @@ def compile_model(atoms, potentials, coulomb=None):
                 raise InvalidPotentialError("'{0}' is not a pair potential of the GB300 engine".format(kind))
             if kind == "tabulated":
                 params = _table_record(M, params)
-            if kind == "charge_pair" and grp >= 0:
-                raise InvalidPotentialError("bond-order scaling of charge_pair is not evaluated by the GB300 engine")
+            if kind == "charge_exp":
+                params = _charge_exp_record(M, params)
+            if kind in ("charge_pair", "charge_exp") and grp >= 0:
+                raise InvalidPotentialError("bond-order scaling of {0} is not evaluated by the GB300 engine".format(kind))
             for tg, first in zip(targets, firsts):
                 M.pair_first.append(_mask(sigs, *first))
                 M.pair_kind.append(core.PAIR_KIND[kind])

@@ -263,3 +263,47 @@ def test_charge_pair_mixed_and_relaxation():
     np.testing.assert_allclose(q_gpu, r["charges"], atol=1e-8)
     # not quadratic in the charges: 'optimize' leaves the device solver
     assert calc.engine.optimize_charges(0, 10, 1e-4) is None
+
+
+def _qexp_case():
+    atoms = W.sio2_box(100, seed=27)
+    q = np.where(np.array(atoms.get_chemical_symbols()) == "Si", 0.5, -0.25)
+    atoms.set_initial_charges(q + np.random.default_rng(5).normal(0.0, 0.05, len(q)))
+    pots, coul = W.sio2_potentials(real_cutoff=5.5, sigma=1.6)
+    P = pysic.Potential
+    # Rmax / (Rmax - Rmin) = Qmax / (Qmax - Qmin): eta = 1, a finite beta
+    pots = pots + [P("charge_exp", symbols=[["Si", "O"]],
+                     parameters=[0.3, 2.0, 1.0, 2.0, 1.0, 3.0, 1.5, 2.4, 1.2, 0.6, 0.4], cutoff=3.0,
+                     cutoff_margin=0.8),
+                   P("charge_exp", symbols=[["O", "O"]],
+                     parameters=[0.2, 2.5, 1.25, 1.8, 0.9, 2.5, 1.25, 1.8, 0.9, 0.5, 0.5], cutoff=2.6,
+                     cutoff_margin=0.5)]
+    return atoms, pots, coul
+
+
+def test_charge_exp_parity_and_relaxation():
+    """charge_exp (Potentials.f90:3691-3903) beside Ewald and charge_self:
+    FP64 energy, smooth-cutoff forces, virial and electronegativities against
+    the oracle, the mixed path within its tolerance, and the damped relaxation
+    on its electronegativities."""
+    atoms, pots, coul = _qexp_case()
+    ref = oracle_all(atoms, pots, coul)
+    got = engine_all(atoms, pots, coul, "fp64")
+    assert got["energy"] == pytest.approx(ref["energy"], rel=1e-11)
+    assert np.abs(got["forces"] - ref["forces"]).max() < 1e-9 * max(1.0, np.abs(ref["forces"]).max())
+    np.testing.assert_allclose(got["stress"], ref["stress"], rtol=1e-9, atol=1e-9 * np.abs(ref["stress"]).max())
+    assert np.abs(got["enegs"] - ref["enegs"]).max() < 1e-9
+    mixed = engine_all(atoms, pots, coul, "mixed")
+    assert abs(mixed["energy"] - ref["energy"]) / len(atoms) <= 1e-5
+    assert np.abs(mixed["enegs"] - ref["enegs"]).max() < 1e-4
+    params = dict(n_steps=600, timestep=0.05, inertia=1.0, friction=3.0, tolerance=1e-4)
+    calc = pysic.Pysic(atoms.copy(), pots, coulomb=coul, precision="fp64")
+    rel = pysic.ChargeRelaxation("dynamic", calculator=calc,
+                                 parameters=[params[k] for k in ("n_steps", "timestep", "inertia", "friction",
+                                                                 "tolerance")])
+    q_gpu = rel.charge_relaxation()
+    model = compile_model(atoms, pots, coul)
+    r = oracle.relax_charges(atoms.get_positions(), atoms.get_initial_charges(), atoms.get_cell(), atoms.get_pbc(),
+                             model, *oracle_lists(atoms, pots, coul), **params)
+    assert rel.last_steps == r["steps"]
+    np.testing.assert_allclose(q_gpu, r["charges"], atol=1e-8)

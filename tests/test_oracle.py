@@ -472,3 +472,46 @@ def test_oracle_atom_factor_gradients_match_finite_differences():
             d = (oracle.atom_factors(p1, cell, pbc, model, *lists)[1][a] -
                  oracle.atom_factors(p2, cell, pbc, model, *lists)[1][a]) / (2 * h)
             assert g_of[b, c] == pytest.approx(d, abs=1e-6)
+
+
+def _charge_exp_case():
+    atoms = W.sio2_box(12, seed=26)
+    q = np.random.default_rng(4).normal(0.0, 0.4, len(atoms))
+    atoms.set_initial_charges(q)
+    # Rmax / (Rmax - Rmin) = Qmax / (Qmax - Qmin) gives eta = 1 (a finite beta)
+    pots = [pysic.Potential("charge_exp", symbols=[["Si", "O"]],
+                            parameters=[0.3, 2.0, 1.0, 2.0, 1.0, 3.0, 1.5, 2.4, 1.2, 0.6, 0.4],
+                            cutoff=3.0, cutoff_margin=0.8),
+            pysic.Potential("charge_exp", symbols=[["O", "O"]],
+                            parameters=[0.2, 2.5, 1.25, 1.8, 0.9, 2.5, 1.25, 1.8, 0.9, 0.5, 0.5],
+                            cutoff=2.6, cutoff_margin=0.5)]
+    return atoms, pots
+
+
+def test_oracle_charge_exp_derivatives():
+    """charge_exp (Potentials.f90:3691-3903) in the oracle: electronegativities
+    are minus the charge derivatives of the energy (with the parameter swap of
+    the unpermuted first target), forces minus the position gradient (the cut
+    factor's only)."""
+    atoms, pots = _charge_exp_case()
+    model = compile_model(atoms, pots)
+    lists = oracle_lists(atoms, pots)
+    pos, q = atoms.get_positions(), atoms.get_initial_charges()
+
+    def ev(p, qq, what):
+        return oracle.evaluate(p, qq, atoms.get_cell(), atoms.get_pbc(), model, *lists, what=what)
+
+    chi = ev(pos, q, "enegs")
+    f, _ = ev(pos, q, "forces")
+    assert np.abs(chi).max() > 0.01 and np.abs(f).max() > 1e-3
+    h = 1e-6
+    for a in (0, 5, 17):
+        q1, q2 = q.copy(), q.copy()
+        q1[a] += h
+        q2[a] -= h
+        assert chi[a] == pytest.approx(-(ev(pos, q1, "energy") - ev(pos, q2, "energy")) / (2 * h), abs=1e-7)
+        for c in range(3):
+            p1, p2 = pos.copy(), pos.copy()
+            p1[a, c] += h
+            p2[a, c] -= h
+            assert f[a, c] == pytest.approx(-(ev(p1, q, "energy") - ev(p2, q, "energy")) / (2 * h), abs=1e-7)
