@@ -977,6 +977,65 @@ static void* loop_range(void* arg) {
                 const int grp = m->pair_group[r];
                 const int sm = X->smoothened[r];
                 const double rc = m->pair_cutoff[r], rs = X->smooth_soft[r];
+                if (kind == 9) {
+                    /* charge_abs, Potentials.f90:4525-4728: sqrt(f1(q1) f2(q2)), f(q) = a + b |q - Q|^n
+                       (negative f taken as 0), parameters (a, b, Q, n) of the unpermuted first
+                       target on atom1 when its type is that target's; rows from p[0] hold
+                       a1, b1, Q1, n1, a2, b2, Q2, n2; only the cut factor's gradient acts */
+                    const double* c = m->pair_table + 2 * (int64_t)p[0];
+                    const int direct = has(m->pair_first[r], ti);
+                    const double* s1 = c + (direct ? 0 : 4);
+                    const double* s2 = c + (direct ? 4 : 0);
+                    const double qq1 = s->charge[i], qq2 = s->charge[j];
+                    double v;
+                    if (J->what == 2) {
+                        const double abs1 = fabs(qq1 - s1[2]), abs2 = fabs(qq2 - s2[2]);
+                        const double pow1 = pow(abs1, s1[3] - 1), pow2 = pow(abs2, s2[3] - 1);
+                        double f1 = s1[0] + s1[1] * abs1 * pow1, f2 = s2[0] + s2[1] * abs2 * pow2;
+                        const double d1 = -s1[3] * pow1 * copysign(1.0, qq1 - s1[2]) * s1[1];
+                        const double d2 = -s2[3] * pow2 * copysign(1.0, qq2 - s2[2]) * s2[1];
+                        double inv_sqrt = 0.5 / sqrt(f1 * f2);
+                        if (f1 < 0.0) {
+                            f1 = 0.0;
+                            inv_sqrt = 0.0;
+                        }
+                        if (f2 < 0.0) {
+                            f2 = 0.0;
+                            inv_sqrt = 0.0;
+                        }
+                        const double cut = sm ? smooth_factor(d, rc, rs) : 1.0;
+                        chi[i] += inv_sqrt * d1 * f2 * cut;
+                        chi[j] += inv_sqrt * d2 * f1 * cut;
+                        continue;
+                    }
+                    {
+                        double f1 = s1[0] + s1[1] * pow(fabs(qq1 - s1[2]), s1[3]);
+                        double f2 = s2[0] + s2[1] * pow(fabs(qq2 - s2[2]), s2[3]);
+                        if (f1 < 0.0) f1 = 0.0;
+                        if (f2 < 0.0) f2 = 0.0;
+                        v = sqrt(f1 * f2);
+                    }
+                    const double cut = sm ? smooth_factor(d, rc, rs) : 1.0;
+                    if (J->what == 0) {
+                        J->energy += v * cut;
+                    } else if (sm) {
+                        const double dv = smooth_deriv(d, rc, rs);
+                        double p2[3];
+                        for (int c3 = 0; c3 < 3; ++c3) {
+                            const double g = dir[c3] * dv;
+                            F[3 * (size_t)i + c3] += v * g;
+                            p2[c3] = -v * g;
+                            F[3 * (size_t)j + c3] += p2[c3];
+                        }
+                        st[0] += sep[0] * p2[0];
+                        st[1] += sep[1] * p2[1];
+                        st[2] += sep[2] * p2[2];
+                        st[3] += sep[1] * p2[2];
+                        st[4] += sep[0] * p2[2];
+                        st[5] += sep[0] * p2[1];
+                    }
+                    continue;
+                }
                 if (kind == 8) {
                     /* charge_exp, Potentials.f90:3691-3903: epsilon exp((xi_1 D_1 + xi_2 D_2)/2),
                        D(q) = Rmax + |beta (Qmax - q)|^eta, parameters swapped unless atom1

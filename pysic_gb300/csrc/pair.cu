@@ -135,6 +135,44 @@ __device__ __forceinline__ void pair_body(const PairArgs& A, int blk) {
                     }
                     continue;
                 }
+                if (P.kind == 9) {
+                    // charge_abs, V = sqrt(f_1(q_1) f_2(q_2)), f(q) = a + b |q - Q|^n, f < 0
+                    // taken as 0, parameters (a, b, Q, n) of the unpermuted first target on
+                    // atom1 when its type is that target's (Potentials.f90:4525-4728); no
+                    // r dependence but the cut
+                    const R* c = (const R*)A.tab + 2 * (long long)P.t0;
+                    const bool first = pick(i, j, A.off[3 * e], A.off[3 * e + 1], A.off[3 * e + 2]);
+                    const R qj = charge_of<R>(A, j);
+                    const R q1 = first ? qi : qj, q2 = first ? qj : qi;
+                    const bool direct = (P.first >> (first ? ti : tj)) & 1ull;
+                    const R* s1 = c + (direct ? 0 : 4);
+                    const R* s2 = c + (direct ? 4 : 0);
+                    const R ab1 = fabs(q1 - s1[2]), ab2 = fabs(q2 - s2[2]);
+                    const R pw1 = pow_(ab1, s1[3] - R(1)), pw2 = pow_(ab2, s2[3] - R(1));
+                    R f1 = s1[0] + s1[1] * ab1 * pw1, f2 = s2[0] + s2[1] * ab2 * pw2;
+                    R is = R(0.5) / sqrt_(f1 * f2);
+                    if (f1 < R(0)) {
+                        f1 = R(0);
+                        is = R(0);
+                    }
+                    if (f2 < R(0)) {
+                        f2 = R(0);
+                        is = R(0);
+                    }
+                    R f = R(1), fp = R(0);
+                    if (P.smooth) smooth<R>(r, P.rc, P.rs, f, fp);
+                    // the energy routine takes |q - Q|^n directly
+                    const R e1 = fmax(s1[0] + s1[1] * pow_(ab1, s1[3]), R(0));
+                    const R e2 = fmax(s2[0] + s2[1] * pow_(ab2, s2[3]), R(0));
+                    const R v = sqrt_(e1 * e2);
+                    U += v * f;
+                    dU += v * fp;
+                    if (wantC) {
+                        chi += first ? is * (-s1[3] * pw1 * copysign(R(1), q1 - s1[2]) * s1[1]) * f2 * f
+                                     : is * (-s2[3] * pw2 * copysign(R(1), q2 - s2[2]) * s2[1]) * f1 * f;
+                    }
+                    continue;
+                }
                 if (!(wantE || wantF)) continue;
                 R V, dV;
                 pair_term<R>(P, r, V, dV, (const R*)A.tab);

@@ -137,11 +137,11 @@ void fold_tables(pg_context* ctx) {
                 t.p1 = ctx->pr_params[4 * (size_t)r + 1];
                 t.p2 = ctx->pr_params[4 * (size_t)r + 2];
                 t.p3 = ctx->pr_params[4 * (size_t)r + 3];
-                if (t.kind == 8) {  // charge_exp: its 15 parameters as 8 rows of the table array
+                if (t.kind == 8 || t.kind == 9) {  // charge_exp / charge_abs: parameters as rows of the table array
                     t.t0 = (int)t.p0;
-                    t.tn = 8;
-                    require(t.t0 >= 0 && (size_t)t.t0 + 8 <= ctx->pr_table.size() / 2, PG_ERR_INVALID,
-                            "charge_exp: parameter rows out of bounds");
+                    t.tn = t.kind == 8 ? 8 : 4;
+                    require(t.t0 >= 0 && (size_t)t.t0 + (size_t)t.tn <= ctx->pr_table.size() / 2, PG_ERR_INVALID,
+                            "charge_exp / charge_abs: parameter rows out of bounds");
                 }
                 if (t.kind == 6) {  // tabulated: params first row, rows, range, scale
                     t.t0 = (int)t.p0;

@@ -251,7 +251,11 @@ def compile_model(atoms, potentials, coulomb=None):
                 params = _table_record(M, params)
             if kind == "charge_exp":
                 params = _charge_exp_record(M, params)
-            if kind in ("charge_pair", "charge_exp") and grp >= 0:
+            if kind == "charge_abs":  # (a, b, Q, n) of both targets as 4 rows of the table array
+                first = len(M.pair_table) // 2
+                M.pair_table.extend([float(x) for x in params[:8]])
+                params = [float(first), 0.0, 0.0, 0.0]
+            if kind in ("charge_pair", "charge_exp", "charge_abs") and grp >= 0:
                 raise InvalidPotentialError("bond-order scaling of {0} is not evaluated by the GB300 engine".format(kind))
             for tg, first in zip(targets, firsts):
                 M.pair_first.append(_mask(sigs, *first))

@@ -100,8 +100,7 @@ def test_types_fold_tags_and_indices():
     assert len(M.pair_kind) == 3  # (1,1) once, (0,2) and (2,0)
 
 
-@pytest.mark.parametrize("kind,symbols", [("step", [["Si", "Si"]]), ("charge_abs", [["Si", "Si"]]),
-                                          ("dihedral", [["Si", "Si", "Si", "Si"]])])
+@pytest.mark.parametrize("kind,symbols", [("step", [["Si", "Si"]]), ("dihedral", [["Si", "Si", "Si", "Si"]])])
 def test_unsupported_potential_rejected_at_compile(kind, symbols):
     atoms = W.diamond_si(1)
     with pytest.raises(pysic.InvalidPotentialError):

@@ -307,3 +307,27 @@ def test_charge_exp_parity_and_relaxation():
                              model, *oracle_lists(atoms, pots, coul), **params)
     assert rel.last_steps == r["steps"]
     np.testing.assert_allclose(q_gpu, r["charges"], atol=1e-8)
+
+
+def test_charge_abs_parity():
+    """charge_abs (Potentials.f90:4525-4728) beside Ewald and charge_self: FP64
+    energy, cut-factor forces, virial and electronegativities against the
+    oracle; the mixed path within its tolerance."""
+    atoms = W.sio2_box(100, seed=29)
+    q = np.where(np.array(atoms.get_chemical_symbols()) == "Si", 0.5, -0.25)
+    atoms.set_initial_charges(q + np.random.default_rng(7).normal(0.0, 0.05, len(q)))
+    pots, coul = W.sio2_potentials(real_cutoff=5.5, sigma=1.6)
+    P = pysic.Potential
+    pots = pots + [P("charge_abs", symbols=[["Si", "O"]], parameters=[1.0, 0.5, 0.3, 2.0, 0.8, 0.7, -0.2, 1.5],
+                     cutoff=3.0, cutoff_margin=0.8),
+                   P("charge_abs", symbols=[["O", "O"]], parameters=[0.6, 0.4, -0.1, 2.5, 0.6, 0.4, -0.1, 2.5],
+                     cutoff=2.6, cutoff_margin=0.5)]
+    ref = oracle_all(atoms, pots, coul)
+    got = engine_all(atoms, pots, coul, "fp64")
+    assert got["energy"] == pytest.approx(ref["energy"], rel=1e-11)
+    assert np.abs(got["forces"] - ref["forces"]).max() < 1e-9 * max(1.0, np.abs(ref["forces"]).max())
+    np.testing.assert_allclose(got["stress"], ref["stress"], rtol=1e-9, atol=1e-9 * np.abs(ref["stress"]).max())
+    assert np.abs(got["enegs"] - ref["enegs"]).max() < 1e-9
+    mixed = engine_all(atoms, pots, coul, "mixed")
+    assert abs(mixed["energy"] - ref["energy"]) / len(atoms) <= 1e-5
+    assert np.abs(mixed["enegs"] - ref["enegs"]).max() < 1e-4

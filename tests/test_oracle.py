@@ -515,3 +515,38 @@ def test_oracle_charge_exp_derivatives():
             p1[a, c] += h
             p2[a, c] -= h
             assert f[a, c] == pytest.approx(-(ev(p1, q, "energy") - ev(p2, q, "energy")) / (2 * h), abs=1e-7)
+
+
+def test_oracle_charge_abs_derivatives():
+    """charge_abs (Potentials.f90:4525-4728) in the oracle: electronegativities
+    are minus the charge derivatives of the energy, forces minus the position
+    gradient (the cut factor's only), exponents swapped with the unpermuted
+    first target."""
+    atoms = W.sio2_box(12, seed=28)
+    q = np.random.default_rng(6).normal(0.0, 0.4, len(atoms))
+    atoms.set_initial_charges(q)
+    pots = [pysic.Potential("charge_abs", symbols=[["Si", "O"]], parameters=[1.0, 0.5, 0.3, 2.0, 0.8, 0.7, -0.2, 1.5],
+                            cutoff=3.0, cutoff_margin=0.8),
+            pysic.Potential("charge_abs", symbols=[["O", "O"]], parameters=[0.6, 0.4, -0.1, 2.5, 0.6, 0.4, -0.1, 2.5],
+                            cutoff=2.6, cutoff_margin=0.5)]
+    model = compile_model(atoms, pots)
+    lists = oracle_lists(atoms, pots)
+    pos = atoms.get_positions()
+
+    def ev(p, qq, what):
+        return oracle.evaluate(p, qq, atoms.get_cell(), atoms.get_pbc(), model, *lists, what=what)
+
+    chi = ev(pos, q, "enegs")
+    f, _ = ev(pos, q, "forces")
+    assert np.abs(chi).max() > 0.01 and np.abs(f).max() > 1e-3
+    h = 1e-6
+    for a in (0, 5, 17):
+        q1, q2 = q.copy(), q.copy()
+        q1[a] += h
+        q2[a] -= h
+        assert chi[a] == pytest.approx(-(ev(pos, q1, "energy") - ev(pos, q2, "energy")) / (2 * h), abs=1e-7)
+        for c in range(3):
+            p1, p2 = pos.copy(), pos.copy()
+            p1[a, c] += h
+            p2[a, c] -= h
+            assert f[a, c] == pytest.approx(-(ev(p1, q, "energy") - ev(p2, q, "energy")) / (2 * h), abs=1e-7)
