@@ -38,7 +38,19 @@ METRIC = "Tersoff-Si atom-steps/s mixed vs FP64 on GPU @1e-5 eV/atom; charge-rel
 # (16 B), neighbour entries (4 x 8 B), forces (24 B) = 72 B/atom; ~2.0 kFLOP/atom
 TERSOFF_BYTES_PER_ATOM = 72.0
 TERSOFF_FLOP_PER_ATOM = 2.0e3
-FP32_NOMINAL_TFLOPS = 152 * 128 * 2 * 2.07e9 / 1e12  # 152 SMs x 128 FP32 lanes x FMA x max clock
+
+
+def fp32_peak(device):
+    """FP32 TFLOP/s of this GPU, measured now: the engine's FMA-chain kernel on
+    every SM (pg_measure_fp32_peak), best of six timed launches."""
+    import ctypes
+
+    from pysic_gb300 import _lib as L
+
+    lib = L.load()
+    tf, ms = ctypes.c_double(0.0), ctypes.c_double(0.0)
+    L.check(lib.pg_measure_fp32_peak(int(device), ctypes.byref(tf), ctypes.byref(ms)))
+    return tf.value
 
 
 def workload(name):
@@ -231,13 +243,31 @@ def cpu_baseline(name, seconds, threads):
     evals = 0
     t0 = time.perf_counter()
     while True:
-        oracle.evaluate(*args, what="energy", threads=threads)
-        oracle.evaluate(*args, what="forces", threads=threads)
+        e = oracle.evaluate(*args, what="energy", threads=threads)
+        f, st = oracle.evaluate(*args, what="forces", threads=threads)
         evals += 1
         dt = time.perf_counter() - t0
         if dt >= seconds:
             break
-    return len(atoms) * evals / dt, evals, dt, len(atoms)
+    return len(atoms) * evals / dt, evals, dt, len(atoms), {"energy": e, "forces": f, "stress": st}
+
+
+def accuracy(r, ref, n):
+    """Errors of an engine result against a reference result (energy per atom,
+    largest force component, virial relative to its largest component)."""
+    return {"energy_err_eV_per_atom": abs(r["energy"] - ref["energy"]) / n,
+            "max_force_err_eV_per_A": float(np.abs(r["forces"] - ref["forces"]).max()),
+            "virial_rel_err": float(np.abs(r["stress"] - ref["stress"]).max() /
+                                    max(1e-30, np.abs(ref["stress"]).max()))}
+
+
+def common_config(name, atoms_n, desc, precision, implementation):
+    """The config object both arms print (the same keys and values apart from
+    precision and implementation), so that their lines can be matched."""
+    return {"workload": name, "atoms": atoms_n, "structure": desc,
+            "neighbor_list": "built once before timing (fixed positions)",
+            "l2": "GPU arm: flushed before every step (256 MB write); CPU arm: not applicable",
+            "precision": precision, "implementation": implementation}
 
 
 def dist_env():
@@ -279,9 +309,9 @@ def run_reference(args):
     line = {"impl": "reference", "metric": METRIC, "value": value, "unit": "atom-steps/s", "n_gpus": args.gpus,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * dt / args.steps,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-            "config": {"workload": args.workload, "atoms": len(atoms), "structure": desc,
-                       "implementation": "C restatement of the Fortran core loops (oracle/oracle.c), "
-                                         "energy pass + force pass per step, as the reference does"},
+            "config": common_config(args.workload, len(atoms), desc, "fp64",
+                                    "C restatement of the Fortran core loops (oracle/oracle.c), energy pass + "
+                                    "force pass per step, as the reference does"),
             "cpu_baseline": {"value": value, "unit": "atom-steps/s", "cores": threads, "kind": "port",
                              "sample": "{0} full energy+force evaluations of {1} atoms".format(args.steps,
                                                                                                 len(atoms)),
@@ -346,7 +376,32 @@ def md_throughput(name, precision, device, steps):
             "note": "wall clock; the host-driven loop is ASE's VelocityVerlet update around Pysic.get_forces"}
 
 
-def charge_relax_gain(n_configs, device):
+def relax_cpu_baseline(threads):
+    """The reference's 'dynamic' loop (relaxation.py:417-450) as the oracle
+    restates it, FP64 on the host cores, on the first held-out SiO2 box from
+    zero charges to the same tolerance: steps and wall time."""
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import oracle
+    from pysic_gb300 import workloads as W
+    from pysic_gb300.model import compile_model, individual_cutoffs
+    from pysic_gb300.train_warm_start import RELAX
+
+    atoms = W.sio2_box(1000, seed=0)
+    pots, coul = W.sio2_potentials()
+    model = compile_model(atoms, pots, coul)
+    cuts = np.array(individual_cutoffs(atoms, pots, coul)) + 0.5
+    lists = oracle.neighbors(atoms.get_positions(), atoms.get_cell(), atoms.get_pbc(), cuts)
+    t0 = time.perf_counter()
+    r = oracle.relax_charges(atoms.get_positions(), np.zeros(len(atoms)), atoms.get_cell(), atoms.get_pbc(), model,
+                             *lists, threads=threads, **RELAX)
+    dt = time.perf_counter() - t0
+    return {"steps": r["steps"], "wall_ms": 1e3 * dt, "cores": threads, "kind": "port", "precision": "fp64",
+            "sample": "one 3000-atom box (seed 0), 'dynamic' relaxation from zero charges to the same tolerance "
+                      "(oracle: the reference's loop restated, every step a full electronegativity evaluation)",
+            "mpi_ranks": 0}
+
+
+def charge_relax_gain(n_configs, device, cpu_threads=0):
     """The metric's second part: plain 'dynamic' charge relaxation of SiO2
     boxes (1000 Si + 2000 O, seeds 0.. held out from training) from zero
     charges against the same relaxation started from the trained network's
@@ -397,7 +452,12 @@ def charge_relax_gain(n_configs, device):
         calc.get_atoms().set_initial_charges(np.zeros(len(atoms)))
         rmse.append(float(np.sqrt(np.mean((net.predict_charges(calc) - q_cold) ** 2))))
         dq.append(float(np.abs(q_warm - q_cold).max()))
+    cpu = relax_cpu_baseline(cpu_threads) if cpu_threads > 0 else None
+    if cpu is not None:
+        cpu["gpu_cold_ms_same_box"] = 1e3 * cold_t[0]
+        cpu["gpu_cold_steps_same_box"] = cold_s[0]
     return {"configs": n_configs, "atoms": 3000, "settings": RELAX, "precision": "mixed",
+            "cpu_baseline": cpu,
             "cold_steps_mean": float(np.mean(cold_s)), "warm_steps_mean": float(np.mean(warm_s)),
             "cold_ms_mean": 1e3 * float(np.mean(cold_t)), "warm_ms_mean": 1e3 * float(np.mean(warm_t)),
             "wall_time_gain": float(np.sum(cold_t) / np.sum(warm_t)),
@@ -480,19 +540,27 @@ def run_ours(args):
     t_k = kt.get(kname, kt[dominant]) / 1e3
     achieved = alg_bytes / t_k / 1e9
     traffic = profile_traffic(kname, args.workload)
-    roof = {"bound": "hbm", "kernel": kname, "achieved": achieved, "peak": peak, "unit": "GB/s",
-            "frac": achieved / peak, "traffic": traffic, "peak_source": peak_kind,
-            "note": "not HBM-bound: the working set stays in L2; the FP32 pipe figure is in 'pipe'"}
+    hbm = {"bound": "hbm", "kernel": kname, "achieved": achieved, "peak": peak, "unit": "GB/s",
+           "frac": achieved / peak, "traffic": traffic, "peak_source": peak_kind}
     if alg_flop:
-        extra["pipe"] = {"kernel": kname, "achieved_tflops_fp32": alg_flop / t_k / 1e12,
-                         "nominal_peak_tflops_fp32": FP32_NOMINAL_TFLOPS,
-                         "frac_of_nominal": alg_flop / t_k / 1e12 / FP32_NOMINAL_TFLOPS}
+        # the bond-order pass is bound by FP32 issue and dependency latency (its
+        # working set stays in L2): its roofline is the FP32 rate measured now
+        p32 = fp32_peak(local)
+        a32 = alg_flop / t_k / 1e12
+        roof = {"bound": "fp32", "kernel": kname, "achieved": a32, "peak": p32, "unit": "TFLOP/s",
+                "frac": a32 / p32, "traffic": traffic,
+                "peak_source": "measured in this run: independent FMA chains on every SM (pg_measure_fp32_peak)",
+                "algorithmic": "{0:.0f} FLOP/atom x {1} atoms per launch".format(TERSOFF_FLOP_PER_ATOM, n),
+                "hbm": hbm}
+    else:
+        roof = hbm
     extra["kernel_ms"] = kt
 
     # end to end through the C ABI with host buffers
     e2e_dt, h2d, d2h = e2e_time(torch, engine, atoms, prec, flags, args.steps, args.warmup)
     if world == 1 and args.workload.startswith("tersoff_si_32768") and args.relax_configs > 0:
-        extra["charge_relax"] = charge_relax_gain(args.relax_configs, local)
+        extra["charge_relax"] = charge_relax_gain(args.relax_configs, local,
+                                                  0 if args.no_cpu_baseline else (os.cpu_count() or 1))
     if world == 1 and args.workload.startswith("tersoff_si") and args.md_steps > 0:
         extra["md"] = md_throughput(args.workload, args.precision, local, args.md_steps)
     e2e = {"value": n * args.steps / e2e_dt, "unit": "atom-steps/s", "h2d_bytes_per_step": h2d,
@@ -501,22 +569,25 @@ def run_ours(args):
     cpu = None
     if world == 1 and rank == 0 and not args.no_cpu_baseline:
         threads = os.cpu_count() or 1
-        v, evals, dt, natoms = cpu_baseline(args.workload, args.cpu_seconds, threads)
+        v, evals, dt, natoms, ref = cpu_baseline(args.workload, args.cpu_seconds, threads)
         cpu = {"value": v, "unit": "atom-steps/s", "cores": threads, "kind": "port",
                "sample": "{0} full energy+force evaluations of {1} atoms in {2:.1f} s (oracle, FP64)".format(
                    evals, natoms, dt), "mpi_ranks": 0}
+        # the engine against the CPU restatement of the reference path on the same structure
+        extra["accuracy_vs_oracle"] = {"mixed": accuracy(r_mixed, ref, n), "fp64": accuracy(r_64, ref, n),
+                                       "note": "engine results against the FP64 oracle (the reference's loops "
+                                               "restated in C) evaluated in the cpu_baseline sample"}
 
     if rank == 0:
         line = {"metric": METRIC, "value": value, "unit": "atom-steps/s", "n_gpus": world, "steps": args.steps,
                 "warmup": args.warmup, "ms_per_step": total_ms / args.steps, "higher_is_better": True,
                 "scaling": "weak", "vs_baseline": None, "dtype": "f32" if prec == L.PREC_MIXED else "f64",
                 "data": "synthetic",
-                "config": {"workload": args.workload, "atoms": n, "structure": desc,
-                           "precision": args.precision + (" (FP32 per pair/triplet, FP64 accumulation)"
+                "config": common_config(args.workload, n, desc,
+                                        args.precision + (" (FP32 per pair/triplet, exact fixed-point accumulation)"
                                                           if prec == L.PREC_MIXED else ""),
-                           "l2": "flushed before every step (256 MB write)",
-                           "neighbor_list": "built once before timing (fixed positions)",
-                           "lanes_per_atom": engine.get_lanes(), "replicas": world},
+                                        "sm_103a CUDA kernels through the C ABI (pysic_gb300)"),
+                "tiles": {"lanes_per_atom": engine.get_lanes()}, "replicas": world,
                 "e2e": e2e, "gpu_launches": launches, "roofline": roof, "cpu_baseline": cpu, "clocks": clocks,
                 "wall_s_timed_region": t_wall}
         line.update(extra)

@@ -284,8 +284,11 @@ int pg_get_stream(pg_context* ctx, void** stream);
  *    charge or out-of-bond pair terms): PG_ERR_UNSUPPORTED otherwise.
  *  - Tables and lists must be current: call pg_calculate once after the last
  *    change of potentials, lists or lanes (PG_ERR_NOT_READY otherwise).
- *  - The first call on a device looks up the static array's address; make it
- *    before any stream capture.
+ *  - The first call on each context looks up the static array's device
+ *    address (in the CUDA context then current) and keeps it; make that call
+ *    before any stream capture.  A pg_context created before a device reset
+ *    (cudaDeviceReset) must not be used after it.
+ *  - An empty system writes zero totals and launches nothing.
  *  - The array is shared by every context on the device: calls that overlap in
  *    time race on it and must be ordered by the caller. */
 #define PG_NOALLOC_SCRATCH_BYTES (32u << 20)
@@ -349,6 +352,16 @@ int pg_batch_synchronize(pg_batch* batch);
 int pg_batch_get_stream(pg_batch* batch, void** stream);
 int pg_batch_last_launch_count(pg_batch* batch, int32_t* launches);
 
+/* FP32 rate of this GPU: a kernel of independent fused multiply-add chains on
+ * every SM (cudaDevAttrMultiProcessorCount), best of several timed launches.
+ * *tflops receives TFLOP/s, *ms (may be null) the best launch's duration.  The
+ * benchmark's roofline denominator for the FP32-bound bond-order kernels.  No
+ * counterpart in the reference; device < 0 keeps the current device. */
+int pg_measure_fp32_peak(int32_t device, double* tflops, double* ms);
+/* Device allocations (cudaMalloc of a growing buffer) made by this library in
+ * this process so far; diagnostic, so that a caller can check that a call
+ * allocated nothing.  No counterpart in the reference. */
+int pg_device_allocation_count(uint64_t* count);
 /* Kernel launches issued by the last pg_device_evaluate / pg_calculate. */
 int pg_last_launch_count(pg_context* ctx, int32_t* launches);
 /* Record CUDA events around the kernel groups of each evaluation;

@@ -98,6 +98,8 @@ _SIGNATURES = {
     "pg_device_positions": (ctypes.c_int, [_ctx, ctypes.POINTER(_c_double_p)]),
     "pg_get_stream": (ctypes.c_int, [_ctx, ctypes.POINTER(ctypes.c_void_p)]),
     "pg_bond_order_noalloc": (ctypes.c_int, [_ctx, ctypes.c_int32, ctypes.c_void_p, ctypes.c_void_p]),
+    "pg_device_allocation_count": (ctypes.c_int, [_c_u64_p]),
+    "pg_measure_fp32_peak": (ctypes.c_int, [ctypes.c_int32, _c_double_p, _c_double_p]),
     "pg_last_launch_count": (ctypes.c_int, [_ctx, _c_int_p]),
     "pg_set_kernel_timing": (ctypes.c_int, [_ctx, ctypes.c_int32]),
     "pg_get_kernel_times": (ctypes.c_int, [_ctx, ctypes.POINTER(ctypes.c_float)]),

@@ -30,7 +30,13 @@ int guarded(F&& f) {
     }
 }
 
-void use_device(pg_context* ctx) { PG_CUDA(cudaSetDevice(ctx->device)); }
+void set_device(pg_context* ctx) { PG_CUDA(cudaSetDevice(ctx->device)); }
+
+// the context's device, and any outstanding coordinate update finished
+void use_device(pg_context* ctx) {
+    set_device(ctx);
+    pg::settle_coordinates(ctx);
+}
 
 void check_ctx(pg_context* ctx) { pg::require(ctx != nullptr, PG_ERR_INVALID, "null context"); }
 }  // namespace
@@ -120,25 +126,49 @@ __global__ void coords_commit(const double* __restrict__ in, double* __restrict_
 
 }  // namespace
 
-// New coordinates for the context: copied to a staging buffer, checked for
-// non-finite values on the device and moved into place only if all are
-// finite, so that a rejected update leaves the old coordinates.  One
-// synchronisation; the host never walks the array.
-static void update_coordinates(pg_context* ctx, const double* positions) {
+// The device-side check and commit of new coordinates: the staged values are
+// checked for non-finite entries and moved into place only if all are finite,
+// so that a rejected update leaves the old coordinates.  Enqueued in front of
+// an evaluation (and captured with it into its graph) or on its own.
+static void enqueue_coordinate_commit(pg_context* ctx) {
     const long long m = 3ll * ctx->n;
-    if (m == 0) return;
     cudaStream_t st = ctx->stream;
-    ctx->pos_in.upload(positions, (size_t)m, st);
-    ctx->pos_bad.resize(1);
     PG_CUDA(cudaMemsetAsync(ctx->pos_bad.p, 0, sizeof(int), st));
-    const int blocks = (int)std::min<long long>((m + 255) / 256, 4 * 152);
+    const int blocks = (int)std::min<long long>((m + 255) / 256, 4 * (long long)sm_count());
     coords_finite<<<blocks, 256, 0, st>>>(ctx->pos_in.p, m, ctx->pos_bad.p);
     coords_commit<<<blocks, 256, 0, st>>>(ctx->pos_in.p, ctx->pos.p, m, ctx->pos_bad.p);
     PG_CHECK_LAUNCH();
+    ctx->launches += 2;
+}
+
+// Finish an outstanding coordinate update: check and commit it if no
+// evaluation has done so, read the check's verdict, fail if it rejected the
+// update.  Every entry point that reads the device coordinates outside an
+// evaluation calls this first.
+void settle_coordinates(pg_context* ctx) {
+    if (ctx->upd_state == PG_UPD_NONE) return;
+    if (ctx->upd_state == PG_UPD_STAGED) enqueue_coordinate_commit(ctx);
     int* bad = ctx->h_flag.get(1);
-    PG_CUDA(cudaMemcpyAsync(bad, ctx->pos_bad.p, sizeof(int), cudaMemcpyDeviceToHost, st));
-    PG_CUDA(cudaStreamSynchronize(st));
-    require(*bad == 0, PG_ERR_INVALID, "non-finite atom position");
+    PG_CUDA(cudaMemcpyAsync(bad, ctx->pos_bad.p, sizeof(int), cudaMemcpyDeviceToHost, ctx->stream));
+    PG_CUDA(cudaStreamSynchronize(ctx->stream));
+    ctx->upd_state = PG_UPD_NONE;
+    require(*bad == 0, PG_ERR_INVALID, "non-finite atom position: the coordinate update was not applied");
+}
+
+// New coordinates for the context: copied to a staging buffer on the
+// context's stream, without waiting.  The next evaluation checks and commits
+// them in front of its kernels (in its captured graph) and pg_calculate reads
+// the verdict together with the results, so an update followed by an
+// evaluation costs one synchronisation.  Page-locked host memory is read
+// asynchronously (cudaMemcpyAsync): it must stay unchanged until the next call
+// on the context that returns results; pageable memory is consumed on return.
+static void update_coordinates(pg_context* ctx, const double* positions) {
+    const long long m = 3ll * ctx->n;
+    if (m == 0) return;
+    if (ctx->upd_state != PG_UPD_NONE) settle_coordinates(ctx);  // one outstanding update at a time
+    ctx->pos_in.upload(positions, (size_t)m, ctx->stream);
+    ctx->pos_bad.resize(1);
+    ctx->upd_state = PG_UPD_STAGED;
 }
 
 // skip (may be null): a device flag every kernel reads first; nonzero makes the
@@ -234,7 +264,14 @@ static int autotune_lanes(pg_context* ctx, int precision, int flags) {
 
 void evaluate(pg_context* ctx, int precision, int flags) {
     require(precision == PG_PREC_FP64 || precision == PG_PREC_MIXED, PG_ERR_INVALID, "unknown precision");
+    // staged coordinates are committed in front of the evaluation's kernels,
+    // unless set-up work that reads them comes first
+    if (ctx->upd_state == PG_UPD_STAGED &&
+        (ctx->tables_dirty || ctx->sep0_epoch != ctx->list_epoch || (ctx->have_bond_terms && ctx->short_dirty) ||
+         (ctx->ewald && ctx->ew_tables_dirty) || !ctx->have_list))
+        settle_coordinates(ctx);
     prepare(ctx);
+    const bool commit = ctx->upd_state == PG_UPD_STAGED;
     if (ctx->n == 0) {  // no atoms: zero totals, nothing to launch
         ctx->out_acc.resize(8);
         PG_CUDA(cudaMemsetAsync(ctx->out_acc.p, 0, sizeof(FxAcc) * 8, ctx->stream));
@@ -247,15 +284,20 @@ void evaluate(pg_context* ctx, int precision, int flags) {
         G = ctx->tuned_lanes[precision];
     }
     if (G == 0) G = 8;
+    auto sequence = [&] {
+        if (commit) enqueue_coordinate_commit(ctx);
+        enqueue_evaluation(ctx, precision, flags, G, nullptr);
+    };
+    if (commit) ctx->upd_state = PG_UPD_CHECKED;  // the verdict is read with the results
     // events recorded inside a capture cannot be waited on: time with direct launches
     if (!ctx->use_graphs || ctx->timing) {
         ctx->launches = 0;
-        enqueue_evaluation(ctx, precision, flags, G, nullptr);
+        sequence();
         return;
     }
     // replay a captured sequence if nothing it depends on has changed
     for (auto it = ctx->graphs.begin(); it != ctx->graphs.end(); ++it) {
-        if (it->precision != precision || it->flags != flags || it->lanes != G) continue;
+        if (it->precision != precision || it->flags != flags || it->lanes != G || it->commit != commit) continue;
         if (it->state == ctx->state_epoch && it->alloc == alloc_epoch()) {
             PG_CUDA(cudaGraphLaunch(it->exec, ctx->stream));
             ctx->launches = it->launches;
@@ -266,14 +308,15 @@ void evaluate(pg_context* ctx, int precision, int flags) {
         break;
     }
     // run once directly (sizes every buffer), then capture the same sequence
+    // (without running it: the direct run was this call's evaluation)
     ctx->launches = 0;
-    enqueue_evaluation(ctx, precision, flags, G, nullptr);
+    sequence();
     const int launches = ctx->launches;
     const unsigned long long alloc_before = alloc_epoch();
     cudaGraph_t graph = nullptr;
     PG_CUDA(cudaStreamBeginCapture(ctx->stream, cudaStreamCaptureModeThreadLocal));
     try {
-        enqueue_evaluation(ctx, precision, flags, G, nullptr);
+        sequence();
     } catch (...) {
         cudaStreamEndCapture(ctx->stream, &graph);
         if (graph) cudaGraphDestroy(graph);
@@ -289,19 +332,31 @@ void evaluate(pg_context* ctx, int precision, int flags) {
     cudaError_t e = cudaGraphInstantiate(&exec, graph, 0);
     cudaGraphDestroy(graph);
     PG_CUDA(e);
-    ctx->graphs.push_back(pg_context::Graph{precision, flags, G, launches, ctx->state_epoch, alloc_epoch(), exec});
+    ctx->graphs.push_back(
+        pg_context::Graph{precision, flags, G, launches, commit, ctx->state_epoch, alloc_epoch(), exec});
     ctx->launches = launches;
 }
 
+// The results of the last evaluation into host memory, and the verdict of a
+// coordinate update that the evaluation committed: one synchronisation.
 static void copy_results(pg_context* ctx, int flags, double* energy, double* forces, double* stress, double* enegs) {
     FxAcc* acc = ctx->h_acc.get(8);
     std::memset((void*)acc, 0, sizeof(FxAcc) * 8);
     double tot[8] = {0};
     cudaStream_t st = ctx->stream;
+    const bool verdict = ctx->upd_state == PG_UPD_CHECKED;
+    int* bad = ctx->h_flag.get(1);
+    if (verdict) PG_CUDA(cudaMemcpyAsync(bad, ctx->pos_bad.p, sizeof(int), cudaMemcpyDeviceToHost, st));
     if (energy || stress) PG_CUDA(cudaMemcpyAsync(acc, ctx->out_acc.p, sizeof(FxAcc) * 8, cudaMemcpyDeviceToHost, st));
     if (forces && (flags & PG_WANT_FORCES)) ctx->out_f.download(forces, 3 * (size_t)ctx->n, st);
     if (enegs && (flags & PG_WANT_ENEGS)) ctx->out_chi.download(enegs, (size_t)ctx->n, st);
     PG_CUDA(cudaStreamSynchronize(st));
+    if (verdict) {
+        ctx->upd_state = PG_UPD_NONE;
+        require(*bad == 0, PG_ERR_INVALID,
+                "non-finite atom position: the coordinate update was not applied (results are of the previous "
+                "coordinates)");
+    }
     for (int c = 0; c < 7; ++c) tot[c] = fx_to_double(fx_from_limbs(acc[c]));
     if (energy && (flags & PG_WANT_ENERGY)) *energy = tot[0];
     if (stress && (flags & PG_WANT_FORCES))
@@ -364,7 +419,7 @@ int pg_create_atoms(pg_context* ctx, int32_t n, const double* positions, const d
                     const int32_t* types) {
     return guarded([&] {
         check_ctx(ctx);
-        use_device(ctx);
+        set_device(ctx);
         pg::require(n >= 0, PG_ERR_INVALID, "negative atom count");
         pg::require(n == 0 || (positions && charges && types), PG_ERR_INVALID, "null atom arrays");
         for (int i = 0; i < n; ++i) pg::require(types[i] >= 0 && types[i] < 64, PG_ERR_INVALID, "type out of range");
@@ -375,6 +430,7 @@ int pg_create_atoms(pg_context* ctx, int32_t n, const double* positions, const d
         ctx->type.upload(types, (size_t)n, ctx->stream);
         ctx->h_type.assign(types, types + n);
         PG_CUDA(cudaStreamSynchronize(ctx->stream));
+        ctx->upd_state = pg::PG_UPD_NONE;  // new atoms replace any outstanding update
         ctx->have_atoms = true;
         ctx->state_epoch++;
         ctx->have_list = false;
@@ -384,7 +440,7 @@ int pg_create_atoms(pg_context* ctx, int32_t n, const double* positions, const d
 int pg_update_atom_coordinates(pg_context* ctx, const double* positions) {
     return guarded([&] {
         check_ctx(ctx);
-        use_device(ctx);
+        set_device(ctx);
         pg::require(ctx->have_atoms, PG_ERR_NOT_READY, "no atoms");
         pg::require(ctx->n == 0 || positions != nullptr, PG_ERR_INVALID, "null positions");
         pg::update_coordinates(ctx, positions);
@@ -630,7 +686,7 @@ int pg_calculate(pg_context* ctx, int32_t precision, int32_t flags, double* ener
                  double* enegs) {
     return guarded([&] {
         check_ctx(ctx);
-        use_device(ctx);
+        set_device(ctx);
         pg::evaluate(ctx, precision, flags);
         pg::copy_results(ctx, flags, energy, forces, stress, enegs);
     });
@@ -815,7 +871,7 @@ int pg_get_lanes_per_atom(pg_context* ctx, int32_t* lanes) {
 int pg_device_evaluate(pg_context* ctx, int32_t precision, int32_t flags) {
     return guarded([&] {
         check_ctx(ctx);
-        use_device(ctx);
+        set_device(ctx);
         pg::evaluate(ctx, precision, flags);
     });
 }
@@ -830,7 +886,7 @@ int pg_device_synchronize(pg_context* ctx) {
 int pg_device_results(pg_context* ctx, double* energy, double* forces, double* stress, double* enegs) {
     return guarded([&] {
         check_ctx(ctx);
-        use_device(ctx);
+        set_device(ctx);
         pg::copy_results(ctx, PG_WANT_ENERGY | PG_WANT_FORCES | PG_WANT_ENEGS, energy, forces, stress, enegs);
     });
 }
@@ -838,6 +894,7 @@ int pg_device_results(pg_context* ctx, double* energy, double* forces, double* s
 int pg_device_positions(pg_context* ctx, double** device_ptr) {
     return guarded([&] {
         check_ctx(ctx);
+        use_device(ctx);
         pg::require(ctx->have_atoms, PG_ERR_NOT_READY, "no atoms");
         *device_ptr = ctx->pos.p;
     });
@@ -855,6 +912,17 @@ int pg_bond_order_noalloc(pg_context* ctx, int32_t precision, double* d_forces, 
         check_ctx(ctx);
         use_device(ctx);
         pg::bond_order_noalloc(ctx, precision, d_forces, d_totals);
+    });
+}
+
+int pg_measure_fp32_peak(int32_t device, double* tflops, double* ms) {
+    return guarded([&] { pg::measure_fp32_peak(device, tflops, ms); });
+}
+
+int pg_device_allocation_count(uint64_t* count) {
+    return guarded([&] {
+        pg::require(count != nullptr, PG_ERR_INVALID, "null output pointer");
+        *count = pg::alloc_epoch();
     });
 }
 

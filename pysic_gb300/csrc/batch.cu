@@ -66,6 +66,7 @@ unsigned long long state_sum(const pg_batch* b) {
 void size_buffers(pg_batch* b, int precision) {
     for (pg_context* c : b->sys) {
         require(c->device == b->device, PG_ERR_INVALID, "every system of a batch must live on the batch's device");
+        settle_coordinates(c);
         prepare(c);
         require(!c->ewald && !c->have_triplets && c->n_agroups == 0, PG_ERR_UNSUPPORTED,
                 "the many-system launch covers pair and Tersoff bond-order terms; evaluate Ewald, three-body or "
@@ -129,7 +130,7 @@ void build(pg_batch* b, int precision, int flags, int pg_lanes, int bg_lanes) {
 }
 
 void enqueue(pg_batch* b, int precision, int pg_lanes, int bg_lanes) {
-    const int sms = 152;
+    const int sms = sm_count();
     launch_disp_batch(b->d_disp.p, b->t_disp.p, b->n_disp, std::min(b->n_disp, sms * 8), b->stream);
     if (b->n_pair)
         launch_pair_batch(b->d_pair.p, b->t_pair.p, b->n_pair, std::min(b->n_pair, sms * 12), PAIR_THREADS,

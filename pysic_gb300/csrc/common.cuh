@@ -47,6 +47,22 @@ inline unsigned long long& alloc_epoch() {
     return e;
 }
 
+// Streaming multiprocessors of the current device (cudaDevAttrMultiProcessorCount),
+// queried once per device; grids are sized in multiples of it.
+inline int sm_count() {
+    constexpr int MAXDEV = 64;
+    static int cache[MAXDEV] = {};
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess || dev < 0) dev = 0;
+    if (dev >= MAXDEV) dev = MAXDEV - 1;
+    int v = __atomic_load_n(&cache[dev], __ATOMIC_RELAXED);
+    if (v == 0) {
+        if (cudaDeviceGetAttribute(&v, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess || v <= 0) v = 1;
+        __atomic_store_n(&cache[dev], v, __ATOMIC_RELAXED);
+    }
+    return v;
+}
+
 // Grow-only device buffer.
 template <typename T>
 struct DevBuf {
@@ -236,6 +252,11 @@ inline void launch_pdl(void (*kernel)(KArgs...), dim3 grid, dim3 block, cudaStre
     PG_CUDA(cudaLaunchKernelEx(&cfg, kernel, std::forward<Args>(args)...));
 }
 
+// State of a coordinate update (pg_update_atom_coordinates): none
+// outstanding; staged on the device, not yet checked; checked and committed by
+// an evaluation whose verdict the host has not read yet.
+constexpr int PG_UPD_NONE = 0, PG_UPD_STAGED = 1, PG_UPD_CHECKED = 2;
+
 // Parameters of the single-species Tersoff fast path, by index.
 constexpr int PG_SPEC_MAX_TERMS = 3;
 enum SpecIndex {
@@ -285,6 +306,7 @@ struct pg_context {
     pg::DevBuf<double> pos;     // n x 3
     pg::DevBuf<double> pos_in;  // coordinate updates land here first and are checked on the device
     pg::DevBuf<int> pos_bad;    // 1 element: nonzero when an update held a non-finite value
+    int upd_state = 0;          // pg::PG_UPD_*: an outstanding coordinate update
     pg::PinnedBuf<pg::FxAcc> h_acc; // energy / virial totals on their way to the host
     pg::PinnedBuf<int> h_flag;
     pg::DevBuf<double> charge;  // n
@@ -438,10 +460,14 @@ struct pg_context {
     bool md_ready = false, md_pending = false;  // state set; a step waits for its forces after a rebuild
 
     int launches = 0;
+    // device address of the no-allocation call's static scratch array in this
+    // context's CUDA context (noalloc.cu), looked up on its first call
+    void* noalloc_scratch = nullptr;
 
     // captured evaluation sequences (one per precision / flags / lanes)
     struct Graph {
         int precision, flags, lanes, launches;
+        bool commit;  // begins with the check and commit of staged coordinates
         unsigned long long state, alloc;
         cudaGraphExec_t exec;
     };
@@ -573,6 +599,10 @@ void relax_charges(pg_context* ctx, int precision, int mode, int n_steps, double
 // api.cu
 void evaluate(pg_context* ctx, int precision, int flags);
 void prepare(pg_context* ctx);  // fold tables, start a list generation, short list, Ewald tables
+void settle_coordinates(pg_context* ctx);  // finish an outstanding coordinate update (may throw)
+
+// peak.cu: FP32 rate of independent FMA chains on every SM (TFLOP/s, best launch ms)
+void measure_fp32_peak(int device, double* tflops, double* ms);
 
 // utilities
 void exclusive_scan_int(const int* in, int* out, int n, cudaStream_t s, DevBuf<int>& tmp, int* total_host);

@@ -559,12 +559,12 @@ static void ew_shape(const pg_context* ctx, int& chunks, int& chunk, int& splits
     const int n = std::max(ctx->n, 1);
     const int nseg = std::max(ctx->ew_nseg, 1);
     const int seg_blocks = cdiv(nseg, EW_THREADS);
-    chunks = std::max(1, std::min(64, cdiv(4 * 152, seg_blocks)));
+    chunks = std::max(1, std::min(64, cdiv(4 * sm_count(), seg_blocks)));
     chunks = std::min(chunks, std::max(1, n / 32));
     chunk = cdiv(n, chunks);
     chunks = cdiv(n, chunk);
     const int atom_blocks = cdiv(n, EW_THREADS * FIELD_ATOMS);
-    splits = std::max(1, std::min(32, cdiv(4 * 152, atom_blocks)));
+    splits = std::max(1, std::min(32, cdiv(4 * sm_count(), atom_blocks)));
     splits = std::min(splits, nseg);
     sps = cdiv(nseg, splits);
     splits = cdiv(nseg, sps);

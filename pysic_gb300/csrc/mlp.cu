@@ -407,7 +407,7 @@ inline int cdiv(long long a, long long b) { return (int)((a + b - 1) / b); }
 
 // blocks of the inference kernel: at most two per SM, each reading the
 // parameters into shared memory once
-inline int infer_blocks(long long n) { return std::max(1, std::min(cdiv(n, INF_WARPS), 2 * 152)); }
+inline int infer_blocks(long long n) { return std::max(1, std::min(cdiv(n, INF_WARPS), 2 * sm_count())); }
 
 }  // namespace
 

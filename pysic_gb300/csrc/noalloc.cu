@@ -8,17 +8,19 @@
 // g_scratch, a file-scope __device__ array of PG_NOALLOC_SCRATCH_BYTES, and
 // writes its results into device buffers the caller owns.
 //
-// Set-up: the first call on a device, with that device current, looks up the
-// array's address once with cudaGetSymbolAddress (which may load this
-// library's device code); make that first call before any stream capture.
+// Set-up: the first call on each context, with the context's device current,
+// looks up the array's address with cudaGetSymbolAddress (which may load this
+// library's device code) and keeps it in the context; make that first call
+// before any stream capture.  The address belongs to the CUDA context that was
+// current at the look-up: a context created after a device reset looks it up
+// anew, while one created before the reset must not be used after it.
 // Zeroing: only the 128-bit energy / virial totals must start at zero; they are
 // cleared with cudaMemsetAsync at the start of every call.  Every other region
-// is written before it is read within the call.
+// is written before it is read within the call.  An empty system writes zero
+// totals and launches nothing.
 // Concurrency: the array is shared by every context on the device, so two calls
 // that overlap in time (other threads, other streams) race on it; callers must
 // order them.
-#include <mutex>
-
 #include "common.cuh"
 
 namespace pg {
@@ -30,19 +32,16 @@ namespace {
 
 static __device__ __align__(256) unsigned char g_scratch[PG_NOALLOC_SCRATCH_BYTES];
 
-constexpr int MAX_DEVICES = 64;
-std::mutex g_mu;
-void* g_addr[MAX_DEVICES] = {};
-
-void* scratch_address(int device) {
-    require(device >= 0 && device < MAX_DEVICES, PG_ERR_INVALID, "device index out of range");
-    std::lock_guard<std::mutex> lock(g_mu);
-    if (g_addr[device] == nullptr) {
+// the array's device address in the CUDA context current on the context's
+// device, looked up on the context's first call (the host-side symbol is not
+// a device address)
+void* scratch_address(pg_context* ctx) {
+    if (ctx->noalloc_scratch == nullptr) {
         void* p = nullptr;
         PG_CUDA(cudaGetSymbolAddress(&p, g_scratch));
-        g_addr[device] = p;
+        ctx->noalloc_scratch = p;
     }
-    return g_addr[device];
+    return ctx->noalloc_scratch;
 }
 
 size_t align256(size_t b) { return (b + 255) & ~(size_t)255; }
@@ -68,13 +67,19 @@ void bond_order_noalloc(pg_context* ctx, int precision, double* d_forces, double
             PG_ERR_NOT_READY,
             "tables or lists are not prepared: evaluate once with pg_calculate after the last change, "
             "then use the no-allocation call");
+    unsigned char* base = (unsigned char*)scratch_address(ctx);
+    if (ctx->n == 0) {  // no atoms: zero totals, nothing to launch
+        PG_CUDA(cudaMemsetAsync(d_totals, 0, 7 * sizeof(double), ctx->stream));
+        return;
+    }
     int G = ctx->lanes != 0 ? ctx->lanes : ctx->tuned_lanes[precision];
     if (G == 0) G = 8;
-    const size_t n = (size_t)std::max(ctx->n, 1);
+    const size_t n = (size_t)ctx->n;
     const size_t ne = (size_t)std::max<long long>(ctx->sh_total, 1);
     const size_t rec = precision == PG_PREC_FP64 ? sizeof(D4) : sizeof(F4);
     const size_t b_acc = align256(8 * sizeof(FxAcc));
-    const size_t b_disp = align256(n * sizeof(F4));
+    // the displacement records exist only in the mixed path
+    const size_t b_disp = precision == PG_PREC_MIXED ? align256(n * sizeof(F4)) : 0;
     const size_t b_fc = align256(3 * n * sizeof(double));
     const size_t b_bonds = align256(4 * ne * rec);
     const size_t need = b_acc + b_disp + b_fc + b_bonds;
@@ -82,7 +87,6 @@ void bond_order_noalloc(pg_context* ctx, int precision, double* d_forces, double
         throw Error(PG_ERR_INVALID, "the no-allocation bond-order call needs " + std::to_string(need) +
                                         " bytes of scratch for this system; its static limit is " +
                                         std::to_string((size_t)PG_NOALLOC_SCRATCH_BYTES) + " bytes");
-    unsigned char* base = (unsigned char*)scratch_address(ctx->device);
     FxAcc* acc = (FxAcc*)base;
     F4* disp = (F4*)(base + b_acc);
     void* fc = base + b_acc + b_disp;

@@ -369,7 +369,8 @@ __global__ void __launch_bounds__(256) chi_cache_apply(const __grid_constant__ P
 // atoms per block: enough blocks to cover every SM twice, at most 256 threads
 int pair_atoms_per_block(int n, int G) {
     const int maxa = 256 / G;
-    int a = (n + 2 * 152 - 1) / (2 * 152);
+    const int sms = sm_count();
+    int a = (n + 2 * sms - 1) / (2 * sms);
     if (a < 1) a = 1;
     if (a > maxa) a = maxa;
     const int warp_atoms = 32 / G > 0 ? 32 / G : 1;  // whole warps

@@ -16,7 +16,13 @@
 // per atom1, lanes over atom1's list entries (atom2), each lane the two atom3
 // loops of its pair.  Forces on the three atoms go to per-atom 2^-40 fixed-point
 // accumulators by 64-bit integer atomics (order-independent, so results do
-// not depend on scheduling), energy and the reference's virial
+// not depend on scheduling).  A signed 64-bit word in these units holds
+// magnitudes below 2^23 (8.4e6 eV/A) exactly; beside the three components
+// every atom has a magnitude word, the sum of |Fx| + |Fy| + |Fz| of its terms
+// in units of 2^-8 (rounded up), with its top bit set by any non-finite term
+// or term of 2^30 eV/A or more.  While that sum stays below 2^23 eV/A no
+// component can have wrapped; otherwise the atom's force reads back as NaN
+// instead of a wrong value.  Energy and the reference's virial
 // (sep1 (x) F_centre + (sep1 + sep2) (x) F_3, Core.f90:6980-6991) to the exact
 // block totals.  The centre's smooth-cutoff gradient terms are those of
 // 6860-6888.
@@ -71,11 +77,25 @@ __device__ __forceinline__ V3<float> entry_vector<float>(const TriArgs& A, int a
     return V3<float>{s0.x + (dj.x - da.x), s0.y + (dj.y - da.y), s0.z + (dj.z - da.z)};
 }
 
+// magnitude words (one per atom after the 3 n components): the top bit marks
+// a term that cannot be accumulated; sums from 2^23 eV/A (2^31 units of 2^-8)
+// on may have wrapped a component
+constexpr unsigned long long MAG_BAD = 1ull << 63;
+constexpr unsigned long long MAG_LIMIT = 1ull << 31;
+
 __device__ __forceinline__ long long fix40(float v) { return __float2ll_rn(v * 1099511627776.0f); }
 __device__ __forceinline__ long long fix40(double v) { return __double2ll_rn(v * FIX40); }
 
+// facc: 3 n components, then n magnitude words
 template <typename R>
-__device__ __forceinline__ void add_force(long long* facc, int a, const V3<R>& f) {
+__device__ __forceinline__ void add_force(long long* facc, int n, int a, const V3<R>& f) {
+    const R m = fabs(f.x) + fabs(f.y) + fabs(f.z);
+    unsigned long long* mag = (unsigned long long*)(facc + 3 * (size_t)n + a);
+    if (!(m < R(1073741824))) {  // 2^30 eV/A, infinities and NaN: nothing is added
+        atomicOr(mag, MAG_BAD);
+        return;
+    }
+    atomicAdd(mag, (unsigned long long)ceil(m * R(256)));
     atomicAdd((unsigned long long*)(facc + 3 * a), (unsigned long long)fix40(f.x));
     atomicAdd((unsigned long long*)(facc + 3 * a + 1), (unsigned long long)fix40(f.y));
     atomicAdd((unsigned long long*)(facc + 3 * a + 2), (unsigned long long)fix40(f.z));
@@ -141,9 +161,9 @@ __global__ void __launch_bounds__(TT) tri_kernel(const __grid_constant__ TriArgs
         R e;
         bend_term<R>(T, s1, d1, s2, d2, fx, fc, fy, e);
         En += e;
-        add_force(A.facc, x, fx);
-        add_force(A.facc, c, fc);
-        add_force(A.facc, y, fy);
+        add_force(A.facc, A.n, x, fx);
+        add_force(A.facc, A.n, c, fc);
+        add_force(A.facc, A.n, y, fy);
         const V3<R> s12{s1.x + s2.x, s1.y + s2.y, s1.z + s2.z};
         W0 += s1.x * fc.x + s12.x * fy.x;
         W1 += s1.y * fc.y + s12.y * fy.y;
@@ -213,9 +233,17 @@ __global__ void tri_forces(int n, long long* __restrict__ facc, double* __restri
     if (skip && *skip) return;
     const int q = blockIdx.x * blockDim.x + threadIdx.x;
     if (q >= 3 * n) return;
-    const double v = (double)facc[q] * (1.0 / FIX40);
+    const unsigned long long mag = (unsigned long long)facc[3 * (size_t)n + q / 3];
+    const double v = mag >= MAG_LIMIT ? fx_nan() : (double)facc[q] * (1.0 / FIX40);
     facc[q] = 0;
     out_f[q] = first ? v : out_f[q] + v;
+}
+
+// the magnitude words back to zero (after tri_forces has read them)
+__global__ void tri_clear_mag(int n, long long* __restrict__ facc, const int* skip) {
+    if (skip && *skip) return;
+    const int a = blockIdx.x * blockDim.x + threadIdx.x;
+    if (a < n) facc[3 * (size_t)n + a] = 0;
 }
 
 }  // namespace
@@ -224,11 +252,10 @@ void launch_triplets(pg_context* ctx, int precision, int flags, bool first_f, Fx
     const int n = ctx->n;
     if (n == 0 || ctx->n_tri == 0) return;
     cudaStream_t st = ctx->stream;
-    if (ctx->tri_facc.cap < 3 * (size_t)n) {
-        ctx->tri_facc.resize(3 * (size_t)n);
-        PG_CUDA(cudaMemsetAsync(ctx->tri_facc.p, 0, sizeof(long long) * 3 * (size_t)n, st));
+    if (ctx->tri_facc.n != 4 * (size_t)n) {  // 3 n components, n magnitude words; zero between calls
+        ctx->tri_facc.resize(4 * (size_t)n);
+        PG_CUDA(cudaMemsetAsync(ctx->tri_facc.p, 0, sizeof(long long) * 4 * (size_t)n, st));
     }
-    ctx->tri_facc.n = 3 * (size_t)n;
     TriArgs A{};
     A.n = n;
     A.pos = ctx->pos.p;
@@ -251,12 +278,14 @@ void launch_triplets(pg_context* ctx, int precision, int flags, bool first_f, Fx
         A.rec = ctx->d_tri32.p;
         tri_kernel<float><<<blocks, TT, 0, st>>>(A);
     }
-    if (flags & PG_WANT_FORCES)
+    if (flags & PG_WANT_FORCES) {
         tri_forces<<<(3 * n + 255) / 256, 256, 0, st>>>(n, ctx->tri_facc.p, ctx->out_f.p, first_f ? 1 : 0, skip);
-    else  // energy only: the accumulated forces are dropped
-        PG_CUDA(cudaMemsetAsync(ctx->tri_facc.p, 0, sizeof(long long) * 3 * (size_t)n, st));
+        tri_clear_mag<<<(n + 255) / 256, 256, 0, st>>>(n, ctx->tri_facc.p, skip);
+    } else {  // energy only: the accumulated forces are dropped
+        PG_CUDA(cudaMemsetAsync(ctx->tri_facc.p, 0, sizeof(long long) * 4 * (size_t)n, st));
+    }
     PG_CHECK_LAUNCH();
-    ctx->launches += (flags & PG_WANT_FORCES) ? 2 : 1;
+    ctx->launches += (flags & PG_WANT_FORCES) ? 3 : 1;
 }
 
 }  // namespace pg

@@ -121,9 +121,11 @@ def oracle_cases():
 
 def main():
     ap = argparse.ArgumentParser()
-    ap.add_argument("--reference-root", default=os.environ.get("REFERENCE_ROOT", "/root/reference"))
+    ap.add_argument("--reference-root", default=os.environ.get("REFERENCE_ROOT"),
+                    help="checkout of the reference (thynnine/pysic) whose doc/ holds the documented values; "
+                         "default: the REFERENCE_ROOT environment variable")
     args = ap.parse_args()
-    if os.path.isdir(os.path.join(args.reference_root, "doc")):
+    if args.reference_root and os.path.isdir(os.path.join(args.reference_root, "doc")):
         docs = reference_docs(args.reference_root)
         with open(os.path.join(HERE, "reference_docs.json"), "w") as fh:
             json.dump(docs, fh, indent=1)

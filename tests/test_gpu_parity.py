@@ -199,8 +199,10 @@ def test_md_style_position_update():
 
 
 def test_rejected_coordinate_update_keeps_the_old_positions():
-    """pg_update_atom_coordinates checks the new coordinates on the device and
-    moves them into place only when every value is finite."""
+    """pg_update_atom_coordinates stages the new coordinates; the device checks
+    them in front of the next evaluation (or before any other call that reads
+    them) and moves them into place only when every value is finite.  The
+    verdict comes with the next call that waits on the device."""
     from pysic_gb300 import _lib as L
 
     atoms = W.diamond_si(2, noise=0.1, seed=3)
@@ -211,12 +213,26 @@ def test_rejected_coordinate_update_keeps_the_old_positions():
     for bad in (np.nan, np.inf, -np.inf):
         pos = atoms.get_positions()
         pos[5, 1] = bad
-        with pytest.raises(L.EngineError) as err:
-            eng.update_positions(pos)
-        assert err.value.status == L.PG_ERR_INVALID
+        for precision in (L.PREC_FP64, L.PREC_MIXED):  # a fresh graph and its replay
+            with pytest.raises(L.EngineError) as err:
+                eng.update_positions(pos)
+                eng.calculate(precision, energy=True, forces=True)
+            assert err.value.status == L.PG_ERR_INVALID
         r = eng.calculate(L.PREC_FP64, energy=True, forces=True)
         assert r["energy"] == e0
         assert np.array_equal(r["forces"], f0)
+        # a call that reads the coordinates outside an evaluation reports it too
+        eng.update_positions(pos)
+        with pytest.raises(L.EngineError) as err:
+            eng.neighbor_lists()
+        assert err.value.status == L.PG_ERR_INVALID
+        # and so does the device-resident route, with the results
+        eng.update_positions(pos)
+        eng.device_evaluate(L.PREC_FP64, L.WANT_ENERGY | L.WANT_FORCES)
+        with pytest.raises(L.EngineError):
+            eng.device_results()
+        r = eng.calculate(L.PREC_FP64, energy=True, forces=True)
+        assert r["energy"] == e0
     # a valid update afterwards is taken
     moved = atoms.get_positions() + 0.01
     eng.update_positions(moved)

@@ -26,18 +26,27 @@ def _calc(n_cells, precision):
     return atoms, calc
 
 
+def _allocations(lib):
+    count = ctypes.c_uint64(0)
+    assert lib.pg_device_allocation_count(ctypes.byref(count)) == L.PG_OK
+    return count.value
+
+
 def _noalloc(calc, prec, n):
+    """One call through the C ABI; the library's allocation count must not move."""
     import torch
 
-    f = torch.zeros((n, 3), dtype=torch.float64, device="cuda")
-    t = torch.zeros(7, dtype=torch.float64, device="cuda")
+    f = torch.full((max(n, 1), 3), float("nan"), dtype=torch.float64, device="cuda")
+    t = torch.full((7,), float("nan"), dtype=torch.float64, device="cuda")
     torch.cuda.synchronize()
     eng = calc.engine
+    before = _allocations(eng.lib)
     st = eng.lib.pg_bond_order_noalloc(eng.ctx, prec, ctypes.c_void_p(f.data_ptr()), ctypes.c_void_p(t.data_ptr()))
     msg = eng.lib.pg_last_error().decode() if st else ""
     if st == L.PG_OK:
         eng.device_synchronize()
-    return st, msg, f.cpu().numpy(), t.cpu().numpy()
+    assert _allocations(eng.lib) == before, "the no-allocation call allocated device memory"
+    return st, msg, f.cpu().numpy()[:n], t.cpu().numpy()
 
 
 @pytest.mark.parametrize("precision", ["fp64", "mixed"])
@@ -59,8 +68,22 @@ def test_noalloc_matches_regular_call_twice(precision):
     assert np.array_equal(results[0][1], results[1][1])
 
 
+@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+def test_noalloc_empty_system(precision):
+    atoms = pysic.Atoms([], np.zeros((0, 3)), cell=np.eye(3) * 10.0, pbc=True)
+    calc = pysic.Pysic(atoms, W.tersoff_si_potentials(), precision=precision)
+    assert calc.get_potential_energy() == 0.0
+    for _ in range(2):
+        st, msg, f, t = _noalloc(calc, calc._prec(), 0)
+        assert st == L.PG_OK, msg
+        assert f.shape == (0, 3)
+        assert np.array_equal(t, np.zeros(7))
+
+
 def test_noalloc_rejects_systems_beyond_the_static_limit():
-    atoms, calc = _calc(24, "fp64")  # 110592 atoms: about 48 MB of FP64 scratch
+    # 110592 atoms at ~4.1 short-list entries each: 4 x 32 B per entry plus
+    # 24 B per atom, about 61 MB of FP64 scratch against the 32 MiB array
+    atoms, calc = _calc(24, "fp64")
     calc.engine.calculate(L.PREC_FP64, energy=True, forces=False)
     st, msg, _, _ = _noalloc(calc, L.PREC_FP64, len(atoms))
     assert st == L.PG_ERR_INVALID
