@@ -72,7 +72,14 @@ int pg_create_cell(pg_context* ctx, const double* cell, const double* inv, const
  * Elements and tags arrive already folded into atom types (0 .. 63). */
 int pg_create_atoms(pg_context* ctx, int32_t n, const double* positions, const double* charges,
                     const int32_t* types);
-/* update_atom_coordinates(positions, momenta), PyInterface.f90:277-286 */
+/* update_atom_coordinates(positions, momenta), PyInterface.f90:277-286.
+ * Enqueues the copy and a check for non-finite values without waiting; the
+ * next evaluation commits the coordinates in front of its kernels.  A rejected
+ * update (non-finite value) keeps the old coordinates and is reported by the
+ * next call that waits on the device (pg_calculate* with PG_ERR_INVALID, or
+ * any call that reads the coordinates).  The copy is cudaMemcpyAsync:
+ * page-locked positions are read asynchronously and must stay unchanged until
+ * that call; pageable memory is consumed before the function returns. */
 int pg_update_atom_coordinates(pg_context* ctx, const double* positions);
 /* update_atom_charges(charges), PyInterface.f90:295-302 */
 int pg_update_atom_charges(pg_context* ctx, const double* charges);
@@ -175,7 +182,8 @@ int pg_calculate_forces(pg_context* ctx, int32_t precision, double* forces, doub
 int pg_calculate_electronegativities(pg_context* ctx, int32_t precision, double* enegs);
 /* One fused evaluation of any of energy, forces + virial and electronegativities
  * (flags: PG_WANT_*).  The reference needs one full pass per quantity
- * (calculator.py:940, 968).  Null output pointers are skipped. */
+ * (calculator.py:940, 968).  Null output pointers are skipped; one
+ * synchronisation per call. */
 int pg_calculate(pg_context* ctx, int32_t precision, int32_t flags, double* energy, double* forces,
                  double* stress, double* enegs);
 

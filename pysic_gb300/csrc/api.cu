@@ -108,12 +108,36 @@ static bool all_finite(const double* v, size_t n) {
 
 namespace {
 
-// any non-finite value in p[0, n) sets *bad (every writer stores the same 1)
-__global__ void coords_finite(const double* __restrict__ p, long long n, int* __restrict__ bad) {
+// n doubles from src to dst (dst may be null: check only); any non-finite value
+// sets *bad (every writer stores the same 1; bad may be null).  vec: both
+// pointers 16-byte aligned, the loop moves double2 pairs.
+__global__ void copy_check(const double* __restrict__ src, double* __restrict__ dst, long long n,
+                           int* __restrict__ bad, int vec) {
     int b = 0;
-    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x)
-        b |= !isfinite(p[i]);
-    if (__syncthreads_or(b) && threadIdx.x == 0) *bad = 1;
+    const long long stride = (long long)gridDim.x * blockDim.x;
+    const long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+    if (vec) {
+        const long long n2 = n / 2;
+        const double2* s2 = (const double2*)src;
+        double2* d2 = (double2*)dst;
+        for (long long i = t; i < n2; i += stride) {
+            const double2 v = s2[i];
+            b |= !isfinite(v.x) | !isfinite(v.y);
+            if (dst) d2[i] = v;
+        }
+        if (t == 0 && (n & 1)) {
+            const double v = src[n - 1];
+            b |= !isfinite(v);
+            if (dst) dst[n - 1] = v;
+        }
+    } else {
+        for (long long i = t; i < n; i += stride) {
+            const double v = src[i];
+            b |= !isfinite(v);
+            if (dst) dst[i] = v;
+        }
+    }
+    if (bad != nullptr && __syncthreads_or(b) && threadIdx.x == 0) *bad = 1;
 }
 
 // the checked coordinates into place, unless the check failed
@@ -124,26 +148,42 @@ __global__ void coords_commit(const double* __restrict__ in, double* __restrict_
         out[i] = in[i];
 }
 
-}  // namespace
-
-// The device-side check and commit of new coordinates: the staged values are
-// checked for non-finite entries and moved into place only if all are finite,
-// so that a rejected update leaves the old coordinates.  Enqueued in front of
-// an evaluation (and captured with it into its graph) or on its own.
-static void enqueue_coordinate_commit(pg_context* ctx) {
-    const long long m = 3ll * ctx->n;
-    cudaStream_t st = ctx->stream;
-    PG_CUDA(cudaMemsetAsync(ctx->pos_bad.p, 0, sizeof(int), st));
-    const int blocks = (int)std::min<long long>((m + 255) / 256, 4 * (long long)sm_count());
-    coords_finite<<<blocks, 256, 0, st>>>(ctx->pos_in.p, m, ctx->pos_bad.p);
-    coords_commit<<<blocks, 256, 0, st>>>(ctx->pos_in.p, ctx->pos.p, m, ctx->pos_bad.p);
-    PG_CHECK_LAUNCH();
-    ctx->launches += 2;
+int copy_blocks(long long n) {
+    return (int)std::max<long long>(1, std::min<long long>((n + 255) / 256, 4ll * sm_count()));
 }
 
-// Finish an outstanding coordinate update: check and commit it if no
-// evaluation has done so, read the check's verdict, fail if it rejected the
-// update.  Every entry point that reads the device coordinates outside an
+}  // namespace
+
+// n doubles from host to device (to_device) or device to host through the DMA
+// engine (cudaMemcpyAsync); bad (may be null, host to device only): a check
+// kernel over the staged copy sets it if any value is not finite.  (A copy
+// kernel reading page-locked host memory through the host link measured no
+// faster than the DMA engine for these sizes, about 7 us per 786 KB.)
+static void host_copy(pg_context* ctx, const double* src, double* dst, long long n, bool to_device, int* bad) {
+    if (n <= 0) return;
+    cudaStream_t st = ctx->stream;
+    PG_CUDA(cudaMemcpyAsync(dst, src, sizeof(double) * (size_t)n,
+                            to_device ? cudaMemcpyHostToDevice : cudaMemcpyDeviceToHost, st));
+    if (to_device && bad != nullptr) {
+        const int vec = (((uintptr_t)dst) & 15u) == 0 ? 1 : 0;
+        copy_check<<<copy_blocks(vec ? n / 2 : n), 256, 0, st>>>(dst, nullptr, n, bad, vec);
+        PG_CHECK_LAUNCH();
+    }
+}
+
+// The commit of staged coordinates, checked for non-finite values when they
+// were staged: moved into place only if all were finite, so that a rejected
+// update leaves the old coordinates.  Enqueued in front of an evaluation (and
+// captured with it into its graph) or on its own.
+static void enqueue_coordinate_commit(pg_context* ctx) {
+    const long long m = 3ll * ctx->n;
+    coords_commit<<<copy_blocks(m), 256, 0, ctx->stream>>>(ctx->pos_in.p, ctx->pos.p, m, ctx->pos_bad.p);
+    PG_CHECK_LAUNCH();
+    ctx->launches += 1;
+}
+
+// Finish an outstanding coordinate update: commit it if no evaluation has done
+// so, read the verdict of its check, fail if the check rejected the update.  Every entry point that reads the device coordinates outside an
 // evaluation calls this first.
 void settle_coordinates(pg_context* ctx) {
     if (ctx->upd_state == PG_UPD_NONE) return;
@@ -155,19 +195,22 @@ void settle_coordinates(pg_context* ctx) {
     require(*bad == 0, PG_ERR_INVALID, "non-finite atom position: the coordinate update was not applied");
 }
 
-// New coordinates for the context: copied to a staging buffer on the
-// context's stream, without waiting.  The next evaluation checks and commits
-// them in front of its kernels (in its captured graph) and pg_calculate reads
-// the verdict together with the results, so an update followed by an
-// evaluation costs one synchronisation.  Page-locked host memory is read
-// asynchronously (cudaMemcpyAsync): it must stay unchanged until the next call
-// on the context that returns results; pageable memory is consumed on return.
+// New coordinates for the context: copied to a staging buffer and checked for
+// non-finite values on the context's stream, without waiting.  The next
+// evaluation commits them in front of its kernels (in its captured graph) and
+// pg_calculate reads the verdict together with the results, so an update
+// followed by an evaluation costs one synchronisation.  The copy is
+// cudaMemcpyAsync: page-locked host memory is read asynchronously and must
+// stay unchanged until the next call on the context that returns results;
+// pageable memory is consumed on return.
 static void update_coordinates(pg_context* ctx, const double* positions) {
     const long long m = 3ll * ctx->n;
     if (m == 0) return;
     if (ctx->upd_state != PG_UPD_NONE) settle_coordinates(ctx);  // one outstanding update at a time
-    ctx->pos_in.upload(positions, (size_t)m, ctx->stream);
+    ctx->pos_in.resize((size_t)m);
     ctx->pos_bad.resize(1);
+    PG_CUDA(cudaMemsetAsync(ctx->pos_bad.p, 0, sizeof(int), ctx->stream));
+    host_copy(ctx, positions, ctx->pos_in.p, m, true, ctx->pos_bad.p);  // staged and checked
     ctx->upd_state = PG_UPD_STAGED;
 }
 
@@ -348,8 +391,8 @@ static void copy_results(pg_context* ctx, int flags, double* energy, double* for
     int* bad = ctx->h_flag.get(1);
     if (verdict) PG_CUDA(cudaMemcpyAsync(bad, ctx->pos_bad.p, sizeof(int), cudaMemcpyDeviceToHost, st));
     if (energy || stress) PG_CUDA(cudaMemcpyAsync(acc, ctx->out_acc.p, sizeof(FxAcc) * 8, cudaMemcpyDeviceToHost, st));
-    if (forces && (flags & PG_WANT_FORCES)) ctx->out_f.download(forces, 3 * (size_t)ctx->n, st);
-    if (enegs && (flags & PG_WANT_ENEGS)) ctx->out_chi.download(enegs, (size_t)ctx->n, st);
+    if (forces && (flags & PG_WANT_FORCES)) host_copy(ctx, ctx->out_f.p, forces, 3ll * ctx->n, false, nullptr);
+    if (enegs && (flags & PG_WANT_ENEGS)) host_copy(ctx, ctx->out_chi.p, enegs, (long long)ctx->n, false, nullptr);
     PG_CUDA(cudaStreamSynchronize(st));
     if (verdict) {
         ctx->upd_state = PG_UPD_NONE;

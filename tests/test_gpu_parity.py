@@ -328,3 +328,43 @@ def test_bond_bend_results_are_bit_reproducible():
     b = engine_all(atoms, _bend_pots(), None, "fp64")
     assert a["energy"] == b["energy"]
     assert np.array_equal(a["forces"], b["forces"])
+
+
+def test_page_locked_buffers_match_pageable_ones():
+    """Page-locked host arrays (read and written asynchronously) give the
+    results of pageable ones, and a non-finite coordinate in a page-locked
+    update is rejected the same way."""
+    import torch
+
+    from pysic_gb300 import _lib as L
+
+    atoms = W.diamond_si(3, noise=0.1, seed=13)
+    calc = pysic.Pysic(atoms, W.tersoff_si_potentials())
+    calc.get_potential_energy()
+    eng = calc.engine
+    n = len(atoms)
+    flags = L.WANT_ENERGY | L.WANT_FORCES | L.WANT_ENEGS
+
+    def pinned(shape):
+        return torch.zeros(shape, dtype=torch.float64, pin_memory=True).numpy()
+
+    moved = atoms.get_positions() + np.random.default_rng(4).normal(0, 0.02, (n, 3))
+    for prec in (L.PREC_FP64, L.PREC_MIXED):
+        eng.update_positions(moved)
+        ref = eng.calculate(prec, energy=True, forces=True, enegs=True)
+        pos = pinned((n, 3))
+        pos[:] = moved
+        e, f, s, c = pinned(1), pinned((n, 3)), pinned(6), pinned(n)
+        for _ in range(2):
+            eng.update_positions(pos)
+            eng.calculate_into(prec, flags, e, f, s, c)
+            assert e[0] == ref["energy"]
+            assert np.array_equal(f, ref["forces"])
+            assert np.array_equal(s, ref["stress"])
+        pos[7, 2] = np.nan
+        with pytest.raises(L.EngineError) as err:
+            eng.update_positions(pos)
+            eng.calculate_into(prec, flags, e, f, s, c)
+        assert err.value.status == L.PG_ERR_INVALID
+        eng.calculate_into(prec, flags, e, f, s, c)
+        assert e[0] == ref["energy"] and np.array_equal(f, ref["forces"])
