@@ -257,8 +257,10 @@ int pg_get_atom_factor_gradients(pg_context* ctx, int32_t precision, int32_t gro
  * accumulates.  Diagnostic; n_entries receives the short-list length. */
 int pg_get_bond_zeta(pg_context* ctx, double* zeta, int64_t capacity, int64_t* n_entries);
 
-/* Tile size of the bond-order kernels: lanes per atom (4, 8, 16 or 32); 0 lets the
- * built-in autotuner choose on the next evaluation. */
+/* Tile of the bond-order kernels: lanes per atom (4, 8, 16 or 32), one bond per
+ * lane; PG_LANES_TRIPLET, 16 lanes per atom with one (bond, neighbour) pair per
+ * lane; 0 lets the built-in autotuner choose on the next evaluation. */
+#define PG_LANES_TRIPLET 64
 int pg_set_lanes_per_atom(pg_context* ctx, int32_t lanes);
 /* Tile size of the full-list kernels (pair, per-atom factors, cached Ewald
  * matrix): lanes per atom (8, 16 or 32); 0 chooses by list length and atom

@@ -29,6 +29,7 @@ PREC_MIXED = 1
 WANT_ENERGY = 1
 WANT_FORCES = 2
 WANT_ENEGS = 4
+LANES_TRIPLET = 64  # bond-order tile: 16 lanes per atom, one (bond, neighbour) pair per lane
 
 _c_double_p = ctypes.POINTER(ctypes.c_double)
 _c_int_p = ctypes.POINTER(ctypes.c_int32)

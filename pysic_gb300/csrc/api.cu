@@ -275,13 +275,13 @@ void enqueue_evaluation(pg_context* ctx, int precision, int flags, int G, const 
 // timed over several single evaluations (device events around each) and
 // judged by its fastest one, so that host launch jitter does not decide.
 static int autotune_lanes(pg_context* ctx, int precision, int flags) {
-    const int options[4] = {4, 8, 16, 32};
+    const int options[5] = {4, 8, 16, 32, PG_LANES_TRIPLET};
     constexpr int REPS = 6;
     cudaEvent_t ev[REPS + 1];
     for (auto& e : ev) PG_CUDA(cudaEventCreate(&e));
     int best = 8;
     float best_ms = 1e30f;
-    for (int o = 0; o < 4; ++o) {
+    for (int o = 0; o < 5; ++o) {
         const int G = options[o];
         enqueue_evaluation(ctx, precision, flags, G, nullptr);  // warm-up
         for (int r = 0; r < REPS; ++r) {
@@ -886,8 +886,8 @@ int pg_get_bond_zeta(pg_context* ctx, double* zeta, int64_t capacity, int64_t* n
 int pg_set_lanes_per_atom(pg_context* ctx, int32_t lanes) {
     return guarded([&] {
         check_ctx(ctx);
-        pg::require(lanes == 0 || lanes == 4 || lanes == 8 || lanes == 16 || lanes == 32, PG_ERR_INVALID,
-                    "lanes per atom must be 0, 4, 8, 16 or 32");
+        pg::require(lanes == 0 || lanes == 4 || lanes == 8 || lanes == 16 || lanes == 32 || lanes == PG_LANES_TRIPLET,
+                    PG_ERR_INVALID, "lanes per atom must be 0, 4, 8, 16, 32 or PG_LANES_TRIPLET (64)");
         ctx->lanes = lanes;
         ctx->state_epoch++;
     });

@@ -11,8 +11,9 @@
 // its own context (pg_device_results reads them).
 //
 // Tiles: lanes per atom of the pair kernel (atoms per warp 32/G, 128 threads
-// per block) and of the bond-order kernels are chosen by timing the candidate
-// pairs on the batch itself, unless set explicitly.
+// per block) and of the bond-order kernels (one bond per lane, or the triplet
+// tile) are chosen by timing the candidate pairs on the batch itself, unless
+// set explicitly.
 #include <algorithm>
 #include <vector>
 
@@ -179,7 +180,7 @@ void run(pg_batch* b, int precision, int flags, int pgl, int bgl, bool use_graph
 // several timed evaluations
 void autotune(pg_batch* b, int precision, int flags, int& pgl, int& bgl) {
     const int pair_opts[3] = {8, 16, 32};
-    const int bond_opts[2] = {4, 8};
+    const int bond_opts[3] = {4, 8, PG_LANES_TRIPLET};
     cudaEvent_t e0, e1;
     PG_CUDA(cudaEventCreate(&e0));
     PG_CUDA(cudaEventCreate(&e1));
@@ -235,8 +236,9 @@ void batch_add(pg_batch* b, pg_context* c) {
 void batch_set_lanes(pg_batch* b, int pair_lanes, int bond_lanes) {
     require(pair_lanes == 0 || pair_lanes == 8 || pair_lanes == 16 || pair_lanes == 32, PG_ERR_INVALID,
             "pair lanes per atom: 0 (autotune), 8, 16 or 32");
-    require(bond_lanes == 0 || bond_lanes == 4 || bond_lanes == 8 || bond_lanes == 16 || bond_lanes == 32,
-            PG_ERR_INVALID, "bond-order lanes per atom: 0 (autotune), 4, 8, 16 or 32");
+    require(bond_lanes == 0 || bond_lanes == 4 || bond_lanes == 8 || bond_lanes == 16 || bond_lanes == 32 ||
+                bond_lanes == PG_LANES_TRIPLET,
+            PG_ERR_INVALID, "bond-order lanes per atom: 0 (autotune), 4, 8, 16, 32 or PG_LANES_TRIPLET (64)");
     b->pair_lanes = pair_lanes;
     b->bond_lanes = bond_lanes;
 }

@@ -39,6 +39,7 @@
 #include <type_traits>
 
 #include "args.cuh"
+#include "bond.cuh"
 #include "common.cuh"
 #include "kernels.cuh"
 
@@ -69,41 +70,6 @@ __global__ void disp_pass_batch(const DispArgs* __restrict__ sys, const int2* __
         disp_body(sys[tl.x], tl.y * blockDim.x + threadIdx.x);
     }
 }
-
-template <typename R>
-__device__ __forceinline__ typename Vec4T<R>::T bond_vector(const BondArgs& A, int i, int e, double xi, double yi,
-                                                            double zi);
-
-template <>
-__device__ __forceinline__ D4 bond_vector<double>(const BondArgs& A, int i, int e, double xi, double yi, double zi) {
-    const int j = A.idx[e];
-    const double o0 = A.off[3 * e], o1 = A.off[3 * e + 1], o2 = A.off[3 * e + 2];
-    double sx = A.pos[3 * j] - xi, sy = A.pos[3 * j + 1] - yi, sz = A.pos[3 * j + 2] - zi;
-    sx += o0 * A.C.vc[0][0] + o1 * A.C.vc[0][1] + o2 * A.C.vc[0][2];
-    sy += o0 * A.C.vc[1][0] + o1 * A.C.vc[1][1] + o2 * A.C.vc[1][2];
-    sz += o0 * A.C.vc[2][0] + o1 * A.C.vc[2][1] + o2 * A.C.vc[2][2];
-    return D4{sx, sy, sz, sqrt(sx * sx + sy * sy + sz * sz)};
-}
-
-template <>
-__device__ __forceinline__ F4 bond_vector<float>(const BondArgs& A, int i, int e, double, double, double) {
-    const int j = A.idx[e];
-    const F4 s0 = A.sep0[e];
-    const F4 dj = A.disp[j], di = A.disp[i];
-    const float x = s0.x + (dj.x - di.x), y = s0.y + (dj.y - di.y), z = s0.z + (dj.z - di.z);
-    return F4{x, y, z, sqrtf(x * x + y * y + z * z)};
-}
-
-template <typename R>
-struct Vec2T;
-template <>
-struct Vec2T<float> {
-    using T = float2;
-};
-template <>
-struct Vec2T<double> {
-    using T = double2;
-};
 
 // SPEC: single-species Tersoff, every parameter a kernel argument (no table
 // lookups per bond or triplet); the same arithmetic as the table path.
@@ -554,7 +520,12 @@ __global__ void __launch_bounds__(128)
     }
 }
 
-int bond_blocks(int n, int G) { return (n + (128 / G) - 1) / (128 / G); }
+// blocks of 128 threads over n atoms at G lanes per atom (the triplet tile: 16
+// lanes, 8 atoms per block)
+int bond_blocks(int n, int G) {
+    const int ap = G == PG_LANES_TRIPLET ? 8 : 128 / G;
+    return (n + ap - 1) / ap;
+}
 
 void prepare_bond_scratch(pg_context* ctx, int precision) {
     const size_t ne = (size_t)std::max<long long>(ctx->sh_total, 1);
@@ -646,9 +617,19 @@ static void launch_pair(const BondArgs& A, int n, cudaStream_t st, bool forces, 
     if (forces) launch_pdl(gather_pass<R, G>, grid, block, st, A);
 }
 
+void launch_tri_pass(const BondArgs& A, int n, int precision, cudaStream_t st);  // tersoff_tri.cu
+void launch_tri_batch(const BondArgs* sys, const int2* tiles, int ntiles, int grid, int precision, bool spec,
+                      cudaStream_t st);
+
 template <typename R>
 static void launch_by_lanes(const BondArgs& A, int n, cudaStream_t st, int G, bool forces,
                             const std::function<void()>& between) {
+    if (G == PG_LANES_TRIPLET) {  // triplet tile, then the 4-lane gather
+        launch_tri_pass(A, n, sizeof(R) == 8 ? PG_PREC_FP64 : PG_PREC_MIXED, st);
+        between();
+        if (forces) launch_pdl(gather_pass<R, 4>, dim3(bond_blocks(n, 4)), dim3(128), st, A);
+        return;
+    }
     switch (G) {
         case 4: launch_pair<R, 4>(A, n, st, forces, between); break;
         case 8: launch_pair<R, 8>(A, n, st, forces, between); break;
@@ -717,6 +698,15 @@ void bond_zeta_diag(pg_context* ctx) {
 void launch_bond_batch(const BondArgs* sys, const int2* tiles, int ntiles, int grid, int precision, int G, bool spec,
                        bool forces, cudaStream_t st) {
     const dim3 g(grid), b(128);
+    if (G == PG_LANES_TRIPLET) {  // triplet tile (8 atoms per tile), then the gather
+        launch_tri_batch(sys, tiles, ntiles, grid, precision, spec, st);
+        if (forces) {  // 16 lanes per atom: the gather's tiles are the bond tiles (8 atoms each)
+            if (precision == PG_PREC_FP64) launch_pdl(gather_pass_batch<double, 16>, g, b, st, sys, tiles, ntiles);
+            else launch_pdl(gather_pass_batch<float, 16>, g, b, st, sys, tiles, ntiles);
+        }
+        PG_CHECK_LAUNCH();
+        return;
+    }
     auto go = [&](auto rtag, auto gtag) {
         using R = decltype(rtag);
         constexpr int GG = decltype(gtag)::value;

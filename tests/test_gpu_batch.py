@@ -30,7 +30,7 @@ def _single(calcs, precision):
     return [c.engine.calculate(prec, energy=True, forces=True) for c in calcs]
 
 
-@pytest.mark.parametrize("lanes", [(0, 0), (8, 4), (32, 8)])
+@pytest.mark.parametrize("lanes", [(0, 0), (8, 4), (32, 8), (16, 64)])  # 64: the triplet tile
 def test_batch_matches_each_system_fp64(lanes):
     calcs = _systems("fp64")
     ref = _single(calcs, "fp64")

@@ -109,7 +109,7 @@ def test_lj_fcc_fp64_parity():
     _check_fp64(W.lj_fcc(), W.lj_potentials())
 
 
-@pytest.mark.parametrize("lanes", [4, 8, 16, 32])
+@pytest.mark.parametrize("lanes", [4, 8, 16, 32, 64])  # 64: the triplet tile
 def test_tersoff_fp64_parity(lanes):
     _check_fp64(W.diamond_si(3, seed=11), W.tersoff_si_potentials(), lanes=lanes)
 
@@ -133,7 +133,7 @@ def _two_species_tersoff():
     return [rep, att]
 
 
-@pytest.mark.parametrize("lanes", [4, 8])
+@pytest.mark.parametrize("lanes", [4, 8, 64])
 def test_tersoff_table_path_matches_fast_path(lanes):
     atoms = W.diamond_si(3, seed=14)
     mixed_atoms = atoms.copy()
@@ -146,6 +146,38 @@ def test_tersoff_table_path_matches_fast_path(lanes):
     mixed = engine_all(mixed_atoms, _two_species_tersoff(), precision="mixed", lanes=lanes)
     assert abs(mixed["energy"] - got["energy"]) / len(atoms) < 1e-5
     assert np.abs(mixed["forces"] - got["forces"]).max() < 1e-4
+
+
+def _long_range_tersoff(R=3.6):
+    """Silicon Tersoff with the cutoff moved out to R + D = 3.9 A: 11 to 24
+    bonds per atom in a random box, so the triplet tile runs several blocks of
+    4 bonds and keeps atoms with more than 16 bonds in global memory."""
+    p = dict(W.TERSOFF_SI)
+    p["R"] = R
+    return W.tersoff_si_potentials(p)
+
+
+@pytest.mark.parametrize("lanes", [8, 64])
+def test_tersoff_many_bonds_fp64_parity(lanes):
+    atoms = W.random_box(["Si"] * 120, W.SI_DENSITY, 2.0, 9)
+    ref, got = _check_fp64(atoms, _long_range_tersoff(), lanes=lanes)
+    c = ref["lists"][0]
+    assert c.max() > 16 and c.min() < 16
+    mixed = engine_all(atoms, _long_range_tersoff(), precision="mixed", lanes=lanes)
+    fmax = max(1.0, np.abs(got["forces"]).max())
+    assert abs(mixed["energy"] - got["energy"]) / len(atoms) < 1e-5
+    assert np.abs(mixed["forces"] - got["forces"]).max() < 1e-4 * fmax
+
+
+@pytest.mark.parametrize("lanes", [0, 4, 64])
+def test_tersoff_mixed_accuracy_32768_each_tile(lanes):
+    atoms = W.diamond_si(16, seed=0)
+    pots = W.tersoff_si_potentials()
+    m = engine_all(atoms, pots, precision="mixed", lanes=lanes)
+    d = engine_all(atoms, pots, precision="fp64", lanes=lanes)
+    n = len(atoms)
+    assert abs(m["energy"] - d["energy"]) / n < 1e-5
+    assert np.abs(m["forces"] - d["forces"]).max() < 1e-4
 
 
 def test_tersoff_mixed_accuracy_4096():
@@ -172,11 +204,14 @@ def test_tersoff_zeta_matches_oracle():
     np.testing.assert_allclose(z, zr, rtol=1e-11, atol=1e-9)
 
 
-def test_results_are_bit_reproducible():
+@pytest.mark.parametrize("lanes", [0, 64])
+def test_results_are_bit_reproducible(lanes):
     atoms = W.diamond_si(4, seed=14)
     pots = W.tersoff_si_potentials()
     calc = pysic.Pysic(atoms, pots, precision="mixed")
     calc.set_core()
+    if lanes:
+        calc.engine.set_lanes(lanes)
     a = calc.engine.calculate(calc._prec())
     b = calc.engine.calculate(calc._prec())
     assert a["energy"] == b["energy"]
