@@ -713,6 +713,21 @@ def run_profile(args):
     from pysic_gb300 import _lib as L
 
     prec = L.PREC_MIXED if args.precision == "mixed" else L.PREC_FP64
+    if args.workload == "relax_sio2_3000":
+        # plain 'dynamic' relaxations of the first held-out SiO2 box (3000 atoms) from zero charges
+        import pysic_gb300 as pysic
+        from pysic_gb300 import workloads as W
+        from pysic_gb300.train_warm_start import relax
+
+        pots, coul = W.sio2_potentials()
+        calc = pysic.Pysic(W.sio2_box(1000, seed=0), pots, coulomb=coul, precision=args.precision)
+        calc.set_core()
+        steps = []
+        for _ in range(max(1, args.steps)):
+            _, rel = relax(calc)
+            steps.append(rel.last_steps)
+        print(json.dumps({"profile_run": args.workload, "precision": args.precision, "relax_steps": steps}))
+        return
     if args.workload == "batched_si_512":
         # the batched launches only: set-up, then `--steps` evaluations of all 512 systems
         batch, n_atoms = _build_batch(args.precision, args.systems)

@@ -1,0 +1,80 @@
+"""The f2py drop-in (pysic_gb300.pf_shim) on the CPU: records registered one
+at a time in the reference's order fold into the same engine records as the
+package's own compile step."""
+import numpy as np
+import pytest
+
+import pf_driver
+import pysic_gb300 as pysic
+from pysic_gb300 import pf_shim
+from pysic_gb300 import workloads as W
+from pysic_gb300.model import compile_model
+
+
+class _NoEngine(pf_shim.PysicInterface):
+    """the record bookkeeping only: no device context"""
+
+    def _eng(self):
+        class Null:
+            def __getattr__(self, name):
+                return lambda *a, **k: None
+        return Null()
+
+
+def _cases():
+    yield "tersoff", W.diamond_si(2, seed=1), W.tersoff_si_potentials(), None
+    pots, coul = W.nacl_potentials(cutoff=5.0, sigma=1.4, real_cutoff=5.0)
+    yield "ewald", W.rocksalt_nacl(2, seed=2), pots, coul
+    pots, coul = W.sio2_potentials(real_cutoff=5.0, sigma=1.5)
+    yield "sio2", W.sio2_box(20, seed=3), pots, coul
+    a = W.fcc_alloy(2, symbols=("Cu", "Ag"), seed=4)
+    calc = pysic.Pysic()
+    calc.add_potential(W.sutton_chen_potentials(("Cu", "Ag")))
+    yield "sutton_chen", a, calc.get_potentials(), None
+    a = W.lj_fcc(2, seed=5)
+    a.set_tags(np.arange(len(a)) % 3)
+    yield "tags_indices", a, [pysic.Potential("LJ", tags=[[0, 1]], parameters=[0.01, 3.0], cutoff=5.0),
+                             pysic.Potential("LJ", indices=[[2, 7]], parameters=[0.02, 2.5], cutoff=5.0),
+                             pysic.Potential("LJ", symbols=[["X", "X"]], parameters=[0.005, 3.2], cutoff=5.0)], None
+
+
+def _pair_rows(a):
+    # the same records; the reference's own set() of permutations fixes no order
+    n = len(a["pair_kind"])
+    if n == 0:
+        return []
+    keys = [k for k in sorted(a) if k.startswith("pair_") and k != "pair_table"]
+    return sorted(map(tuple, np.column_stack([np.asarray(a[k], dtype=np.float64).reshape(n, -1) for k in keys])))
+
+
+@pytest.mark.parametrize("case", list(_cases()), ids=lambda c: c[0])
+def test_shim_records_equal_compiled_records(case):
+    _, atoms, pots, coul = case
+    pi = _NoEngine()
+    pf_driver.load(pi, atoms, pots, coul)
+    got = pi.build_model()
+    ref = compile_model(atoms, pots, coul)
+    assert got.n_types == ref.n_types
+    assert np.array_equal(got.types, ref.types)
+    ga, ra = got.arrays(), ref.arrays()
+    assert _pair_rows(ga) == _pair_rows(ra)
+    assert np.array_equal(ga["pair_table"], ra["pair_table"])
+    for key in ra:
+        if not key.startswith("pair_"):
+            assert np.array_equal(ga[key], ra[key]), key
+    if coul is not None:
+        for k in ("rc", "kc", "sigma", "eps"):
+            assert got.ewald[k] == ref.ewald[k]
+        assert np.array_equal(got.ewald["kmax"], ref.ewald["kmax"])
+
+
+def test_shim_signature_conventions():
+    pi = _NoEngine()
+    assert pi.is_potential("LJ") and not pi.is_potential("nonsense")
+    assert pi.number_of_targets_of_bond_order_factor("tersoff") == 3
+    assert pi.level_of_bond_order_factor("tersoff") == 2
+    assert pi.number_of_parameters_of_bond_order_factor("tersoff", 2) == 5
+    # products of potentials are refused with the reference's success flag
+    assert pi.add_potential("LJ", np.array([1.0, 1.0]), 5.0, 5.0, np.zeros((2, 2)), np.array([-9, -9]),
+                            np.array([-9, -9]), np.zeros((2, 2)), np.array([-9, -9]), np.array([-9, -9]), -1,
+                            True) is False
