@@ -563,6 +563,9 @@ def run_ours(args):
                                                   0 if args.no_cpu_baseline else (os.cpu_count() or 1))
     if world == 1 and args.workload.startswith("tersoff_si") and args.md_steps > 0:
         extra["md"] = md_throughput(args.workload, args.precision, local, args.md_steps)
+    if world == 1 and args.workload.startswith("tersoff_si_32768") and not args.no_other_configs:
+        extra["other_configs"] = other_configs(local, min(args.steps, 50), args.warmup, os.cpu_count() or 1)
+        extra["batched"] = batch_measure(args.precision, min(args.steps, 20), args.warmup)
     e2e = {"value": n * args.steps / e2e_dt, "unit": "atom-steps/s", "h2d_bytes_per_step": h2d,
            "d2h_bytes_per_step": d2h, "ms_per_step": 1e3 * e2e_dt / args.steps}
 
@@ -633,22 +636,23 @@ def _build_batch(precision, systems=512):
     return BatchedPysic(calcs), sum(len(p) for p, _ in structs)
 
 
-def run_batch(args):
+def batch_measure(precision, steps, warmup):
     """512 uneven silicon boxes (Tersoff + LJ): one launch per kernel for all
-    systems (graph replay) against one evaluation per system."""
-    batch, n_atoms = _build_batch(args.precision)
+    systems (graph replay) against one evaluation per system.  Device-timed
+    ms per evaluation of all systems (L2 flushed before each), wall-clock
+    comparison with per-system evaluation, and the FP64 kernels."""
+    batch, n_atoms = _build_batch(precision)
     import torch
 
     flush = torch.empty(64 * 1024 * 1024, dtype=torch.float32, device="cuda")
     stream = torch.cuda.ExternalStream(batch.stream_handle())
 
-    def timed(prec, steps):
-        for _ in range(args.warmup):
+    def timed(prec, k_steps):
+        for _ in range(warmup):
             batch.evaluate(prec)
         batch.synchronize()
-        ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(steps)]
-        t0 = time.perf_counter()
-        for k in range(steps):
+        ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(k_steps)]
+        for k in range(k_steps):
             with torch.cuda.stream(stream):
                 flush.fill_(float(k))
                 ev[k][0].record(stream)
@@ -656,55 +660,101 @@ def run_batch(args):
             with torch.cuda.stream(stream):
                 ev[k][1].record(stream)
         batch.synchronize()
-        wall = time.perf_counter() - t0
-        return [a.elapsed_time(b) for a, b in ev], wall
+        return [a.elapsed_time(b) for a, b in ev]
 
     sampler = ClockSampler(0)
     sampler.start()
-    times, _ = timed(args.precision, args.steps)
+    times = timed(precision, steps)
     clocks = sampler.stop()
     launches = batch.launch_count()
     ms = statistics.mean(times)
-    # one evaluation per system (each context's own captured graph on its own stream)
-    for _ in range(args.warmup):
-        batch.evaluate(args.precision, mode="each")
-    batch.synchronize()
-    t0 = time.perf_counter()
-    for _ in range(args.steps):
-        batch.evaluate(args.precision, mode="each")
-    batch.synchronize()
-    wall_each = (time.perf_counter() - t0) / args.steps
+
+    def wall(mode):
+        for _ in range(warmup):
+            batch.evaluate(precision, mode=mode)
+        batch.synchronize()
+        t0 = time.perf_counter()
+        for _ in range(steps):
+            batch.evaluate(precision, mode=mode)
+        batch.synchronize()
+        return (time.perf_counter() - t0) / steps
+
+    wall_each = wall("each")
     launches_each = batch.launch_count()
-    # the batched launch timed the same way (no flush, no events: wall clock)
-    for _ in range(args.warmup):
-        batch.evaluate(args.precision)
-    batch.synchronize()
-    t0 = time.perf_counter()
-    for _ in range(args.steps):
-        batch.evaluate(args.precision)
-    batch.synchronize()
-    wall_batched = (time.perf_counter() - t0) / args.steps
-    t64, _ = timed("fp64", max(5, args.steps // 4))
-    pl, bl = batch.get_lanes(args.precision)
-    line = {"metric": METRIC, "value": n_atoms / (ms / 1e3), "unit": "atom-steps/s", "n_gpus": 1,
-            "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True,
+    wall_batched = wall("batched")
+    t64 = timed("fp64", max(5, steps // 4))
+    pl, bl = batch.get_lanes(precision)
+    out = {"systems": 512, "atoms": n_atoms, "precision": precision, "ms_per_step": ms,
+           "atom_steps_per_s": n_atoms / (ms / 1e3), "systems_per_s": 512 / (ms / 1e3),
+           "launches_per_step": launches, "batched_wall_ms_per_step": 1e3 * wall_batched,
+           "per_system": {"wall_ms_per_step": 1e3 * wall_each, "atom_steps_per_s": n_atoms / wall_each,
+                          "launches_per_step": launches_each,
+                          "note": "every system evaluated on its own: its own captured graph on its own stream"},
+           "batched_vs_per_system_wall": wall_each / wall_batched,
+           "fp64": {"atom_steps_per_s": n_atoms / (statistics.mean(t64) / 1e3), "ms_per_step": statistics.mean(t64)},
+           "tiles": {"pair_lanes": pl, "bond_lanes": bl}, "clocks": clocks,
+           "structure": "Si boxes, atom counts log-uniform in [64, 2048], 2.33 g/cm^3, random with rejection below "
+                        "2.0 A; Tersoff + LJ (0.01 eV, 2.1 A, cutoff 5)",
+           "l2": "flushed before every step (256 MB write)"}
+    out["speedup_vs_fp64"] = out["atom_steps_per_s"] / out["fp64"]["atom_steps_per_s"]
+    return out
+
+
+def run_batch(args):
+    """The many-system workload as the line's own metric."""
+    b = batch_measure(args.precision, args.steps, args.warmup)
+    line = {"metric": METRIC, "value": b["atom_steps_per_s"], "unit": "atom-steps/s", "n_gpus": 1,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": b["ms_per_step"], "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f32" if args.precision == "mixed" else "f64",
             "data": "synthetic",
-            "config": {"workload": "batched_si_512", "systems": 512, "atoms": n_atoms,
-                       "structure": "Si boxes, atom counts log-uniform in [64, 2048], 2.33 g/cm^3, random with "
-                                    "rejection below 2.0 A; Tersoff + LJ (0.01 eV, 2.1 A, cutoff 5)",
-                       "precision": args.precision, "l2": "flushed before every step (256 MB write)",
-                       "tiles": {"pair_lanes": pl, "bond_lanes": bl}},
-            "systems_per_s": 512 / (ms / 1e3), "gpu_launches": launches * args.steps,
-            "batched_wall_ms_per_step": 1e3 * wall_batched,
-            "per_system": {"wall_ms_per_step": 1e3 * wall_each, "atom_steps_per_s": n_atoms / wall_each,
-                           "launches_per_step": launches_each,
-                           "note": "every system evaluated on its own: its own captured graph on its own stream"},
-            "batched_vs_per_system_wall": wall_each / wall_batched,
-            "fp64": {"value": n_atoms / (statistics.mean(t64) / 1e3), "ms_per_step": statistics.mean(t64)},
-            "clocks": clocks}
-    line["speedup_vs_fp64"] = line["value"] / line["fp64"]["value"]
+            "config": {"workload": "batched_si_512", "systems": 512, "atoms": b["atoms"],
+                       "structure": b["structure"], "precision": args.precision, "l2": b["l2"]},
+            "gpu_launches": b["launches_per_step"] * args.steps, "clocks": b["clocks"], "batched": b}
     print(json.dumps(line))
+
+
+def other_configs(device, steps, warmup, threads):
+    """The other single-system benchmark configurations, device-timed the same
+    way (L2 flushed before every step), each against the oracle on the same
+    structure: LJ fcc 864 atoms in FP64 (config 1) and rock-salt NaCl 8000
+    ions with Buckingham + Ewald (config 3) in mixed precision and FP64."""
+    import torch
+
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import oracle
+    from pysic_gb300 import _lib as L
+    from pysic_gb300.model import compile_model, individual_cutoffs
+
+    flush = torch.empty(64 * 1024 * 1024, dtype=torch.float32, device="cuda:%d" % device)
+    out = {}
+    for name, precisions in (("lj_fcc_864", ("fp64",)), ("ewald_nacl_8000", ("mixed", "fp64"))):
+        atoms, pots, coul, desc = workload(name)
+        model = compile_model(atoms, pots, coul)
+        cuts = np.array(individual_cutoffs(atoms, pots, coul)) + 0.5
+        lists = oracle.neighbors(atoms.get_positions(), atoms.get_cell(), atoms.get_pbc(), cuts)
+        a = (atoms.get_positions(), atoms.get_initial_charges(), atoms.get_cell(), atoms.get_pbc(), model) + \
+            tuple(lists)
+        t0 = time.perf_counter()
+        ref = {"energy": oracle.evaluate(*a, what="energy", threads=threads)}
+        ref["forces"], ref["stress"] = oracle.evaluate(*a, what="forces", threads=threads)
+        t_cpu = time.perf_counter() - t0
+        n = len(atoms)
+        block = {"atoms": n, "structure": desc,
+                 "cpu_baseline": {"atom_steps_per_s": n / t_cpu, "cores": threads, "kind": "port",
+                                  "sample": "one energy + force evaluation (oracle, FP64)"}}
+        for prec_name in precisions:
+            _, calc, _ = setup(name, prec_name, device)
+            eng = calc.engine
+            prec = L.PREC_MIXED if prec_name == "mixed" else L.PREC_FP64
+            r = eng.calculate(prec)
+            t, _ = device_time(torch, eng, prec, L.WANT_ENERGY | L.WANT_FORCES, steps, warmup, flush)
+            ms = statistics.mean(t)
+            block[prec_name] = {"ms_per_step": ms, "atom_steps_per_s": n / (ms / 1e3),
+                                "accuracy_vs_oracle": accuracy(r, ref, n)}
+        if "mixed" in block:
+            block["speedup_vs_fp64"] = block["mixed"]["atom_steps_per_s"] / block["fp64"]["atom_steps_per_s"]
+        out[name] = block
+    return out
 
 
 def run_profile(args):
@@ -761,6 +811,8 @@ def main():
     p.add_argument("--precision", choices=["mixed", "fp64"], default="mixed")
     p.add_argument("--cpu-seconds", type=float, default=12.0)
     p.add_argument("--no-cpu-baseline", action="store_true")
+    p.add_argument("--no-other-configs", action="store_true",
+                   help="skip the LJ 864, NaCl 8000 and 512-system blocks of the default line")
     p.add_argument("--relax-configs", type=int, default=3, help="SiO2 boxes for the charge-relax gain (0: skip)")
     p.add_argument("--md-steps", type=int, default=300, help="device velocity Verlet steps reported beside the metric "
                                                               "(0: skip)")

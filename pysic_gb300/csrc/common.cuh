@@ -498,6 +498,8 @@ struct pg_mlp {
     pg::DevBuf<int> order;             // sample order of the current epoch
     pg::DevBuf<float> h1, h2, out, dz1, dz2, dy, lpart;  // per-batch activations
     pg::DevBuf<float> px, py;          // prediction scratch
+    pg::DevBuf<float> gpart;           // tensor-core training: per-block partial gradients
+    pg::DevBuf<double> dloss;          // summed squared error of an epoch, on the device
     long long step = 0;
     ~pg_mlp() {
         if (stream) cudaStreamDestroy(stream);
@@ -553,6 +555,9 @@ void mlp_clear_samples(pg_mlp* M);
 void mlp_train(pg_mlp* M, int epochs, int batch, float lr, unsigned long long seed, float* epoch_loss);
 void mlp_gradients(pg_mlp* M, const float* x, const float* y, long long n, float* grad, double* loss);
 void mlp_predict(pg_mlp* M, const float* x, long long n, float* y);
+// mlp_tc.cu: the tensor-core training step (two hidden layers of 64 units, <= 64 inputs)
+bool mlp_tc_eligible(const pg_mlp* M);
+void mlp_tc_batch_grad(pg_mlp* M, const float* x, const float* y, const int* rows, int nb, double* loss_dev);
 void mlp_predict_charges(pg_mlp* M, pg_context* ctx, int n_gauss, double r0, double r1, double width, double cutoff,
                          int n_elements, const int* type_element, const float* x_mean, const float* x_scale,
                          double y_mean, double y_scale, double total_charge, double* charges);

@@ -13,11 +13,14 @@
 //             exp(-(r_ij - mu_k)^2 / (2 w^2)) * 1/2 (1 + cos(pi r_ij / rc)),
 // mu_k evenly spaced on [r0, r1].  One warp per atom, lanes over features.
 //
-// Network: z1 = W1 x + b1, h1 = tanh(z1), z2 = W2 h1 + b2, h2 = tanh(z2),
-// y = w3 . h2 + b3.  Parameters are kept in FP32 (Adam's master copy) and as a
-// BF16 copy that every forward pass reads; all sums are FP32.  Loss: mean
-// squared error.  Every reduction over samples runs in a fixed order (one
-// thread per parameter), so training is deterministic.
+// Network: z1 = W1 x~ + b1, h1 = tanh(z1), z2 = W2 h1~ + b2, h2 = tanh(z2),
+// y = w3 . h2 + b3, where x~ and h1~ are the inputs and the first-layer
+// activations rounded to BF16 (the operands of the tensor-core path,
+// mlp_tc.cu, which trains networks of two 64-unit layers; every path here
+// computes the same function).  Parameters are kept in FP32 (Adam's master
+// copy) and as a BF16 copy that every forward pass reads; all sums are FP32.
+// Loss: mean squared error.  Every reduction over samples runs in a fixed
+// order, so training is deterministic.
 #include <algorithm>
 #include <cmath>
 #include <cstring>
@@ -137,6 +140,9 @@ __global__ void desc_kernel_lanes(DescArgs A) {
 
 // ---- network -----------------------------------------------------------------
 
+// v rounded to the nearest BF16 (ties to even), as an FP32 value
+__device__ __forceinline__ float rbf(float v) { return __bfloat162float(__float2bfloat16_rn(v)); }
+
 // parameters (BF16) into shared memory as FP32
 __device__ __forceinline__ void load_params(float* sw, const __nv_bfloat16* wb, int total) {
     for (int q = threadIdx.x; q < total; q += blockDim.x) sw[q] = __bfloat162float(wb[q]);
@@ -155,7 +161,7 @@ __global__ void __launch_bounds__(MLP_THREADS) mlp_forward(Layout Lp, const __nv
     if (s >= nb) return;
     const long long row = rows ? rows[s] : s;
     float xin[MAX_IN], h1[MAX_H];
-    for (int a = 0; a < Lp.n_in; ++a) xin[a] = x[row * Lp.n_in + a];
+    for (int a = 0; a < Lp.n_in; ++a) xin[a] = rbf(x[row * Lp.n_in + a]);
     for (int j = 0; j < Lp.n_h1; ++j) {
         const float* wr = sw + Lp.w1() + j * Lp.n_in;
         float z = sw[Lp.b1() + j];
@@ -167,7 +173,7 @@ __global__ void __launch_bounds__(MLP_THREADS) mlp_forward(Layout Lp, const __nv
     for (int k = 0; k < Lp.n_h2; ++k) {
         const float* wr = sw + Lp.w2() + k * Lp.n_h1;
         float z = sw[Lp.b2() + k];
-        for (int j = 0; j < Lp.n_h1; ++j) z = fmaf(wr[j], h1[j], z);
+        for (int j = 0; j < Lp.n_h1; ++j) z = fmaf(wr[j], rbf(h1[j]), z);
         const float h2 = tanhf(z);
         if (TRAIN) h2o[(long long)s * Lp.n_h2 + k] = h2;
         y = fmaf(sw[Lp.w3() + k], h2, y);
@@ -228,14 +234,14 @@ __global__ void mlp_grad(Layout Lp, const float* __restrict__ x, const int* __re
         const int j = p / Lp.n_in, a = p % Lp.n_in;
         for (int s = 0; s < nb; ++s) {
             const long long row = rows ? rows[s] : s;
-            g = fmaf(dz1[(long long)s * Lp.n_h1 + j], x[row * Lp.n_in + a], g);
+            g = fmaf(dz1[(long long)s * Lp.n_h1 + j], rbf(x[row * Lp.n_in + a]), g);
         }
     } else if (p < Lp.w2()) {
         const int j = p - Lp.b1();
         for (int s = 0; s < nb; ++s) g += dz1[(long long)s * Lp.n_h1 + j];
     } else if (p < Lp.b2()) {
         const int q = p - Lp.w2(), k = q / Lp.n_h1, j = q % Lp.n_h1;
-        for (int s = 0; s < nb; ++s) g = fmaf(dz2[(long long)s * Lp.n_h2 + k], h1[(long long)s * Lp.n_h1 + j], g);
+        for (int s = 0; s < nb; ++s) g = fmaf(dz2[(long long)s * Lp.n_h2 + k], rbf(h1[(long long)s * Lp.n_h1 + j]), g);
     } else if (p < Lp.w3()) {
         const int k = p - Lp.b2();
         for (int s = 0; s < nb; ++s) g += dz2[(long long)s * Lp.n_h2 + k];
@@ -347,14 +353,14 @@ __global__ void __launch_bounds__(INF_THREADS) mlp_infer(Layout L0, const __nv_b
             } else {
                 v = x[(long long)s * L0.n_in + a];
             }
-            sx[w][a] = v;
+            sx[w][a] = rbf(v);
         }
         __syncwarp();
         for (int j = lane; j < L0.n_h1; j += 32) {
             const float* wr = sw + P.w1() + j * P.p1;
             float z = sw[P.b1() + j];
             for (int a = 0; a < L0.n_in; ++a) z = fmaf(wr[a], sx[w][a], z);
-            sh1[w][j] = tanhf(z);
+            sh1[w][j] = rbf(tanhf(z));
         }
         __syncwarp();
         for (int k = lane; k < L0.n_h2; k += 32) {
@@ -554,6 +560,15 @@ void mlp_clear_samples(pg_mlp* M) { M->n_samples = 0; }
 // forward + backward of one batch (rows into the sample arrays, or the first
 // nb samples); leaves the gradient in M->grad and returns the summed squared error
 static double batch_grad(pg_mlp* M, const float* x, const float* y, const int* rows, int nb) {
+    if (mlp_tc_eligible(M)) {
+        M->dloss.resize(1);
+        PG_CUDA(cudaMemsetAsync(M->dloss.p, 0, sizeof(double), M->stream));
+        mlp_tc_batch_grad(M, x, y, rows, nb, M->dloss.p);
+        double l = 0.0;
+        M->dloss.download(&l, 1, M->stream);
+        PG_CUDA(cudaStreamSynchronize(M->stream));
+        return l;
+    }
     const Layout Lp = mlp_layout(M);
     const size_t smem = mlp_smem(M);
     M->h1.resize((size_t)nb * M->n_h1);
@@ -588,18 +603,27 @@ void mlp_train(pg_mlp* M, int epochs, int batch, float lr, unsigned long long se
     std::mt19937_64 rng(seed);
     M->order.resize((size_t)n);
     const float b1 = 0.9f, b2 = 0.999f, eps = 1e-8f;
+    const bool tc = mlp_tc_eligible(M);
+    M->dloss.resize(1);
     for (int ep = 0; ep < epochs; ++ep) {
         std::shuffle(order.begin(), order.end(), rng);
         M->order.upload(order.data(), order.size(), M->stream);
         double loss = 0.0;
+        // tensor-core path: the epoch's loss stays on the device until its end
+        if (tc) PG_CUDA(cudaMemsetAsync(M->dloss.p, 0, sizeof(double), M->stream));
         for (long long b0 = 0; b0 < n; b0 += batch) {
             const int nb = (int)std::min<long long>(batch, n - b0);
-            loss += batch_grad(M, M->x.p, M->y.p, M->order.p + b0, nb);
+            if (tc) mlp_tc_batch_grad(M, M->x.p, M->y.p, M->order.p + b0, nb, M->dloss.p);
+            else loss += batch_grad(M, M->x.p, M->y.p, M->order.p + b0, nb);
             M->step++;
             const float c1 = 1.0f - std::pow(b1, (float)M->step), c2 = 1.0f - std::pow(b2, (float)M->step);
             mlp_adam<<<cdiv(M->n_params, 256), 256, 0, M->stream>>>((int)M->n_params, M->w.p, M->m.p, M->v.p,
                                                                     M->grad.p, M->wb.p, lr, b1, b2, eps, c1, c2);
             PG_CHECK_LAUNCH();
+        }
+        if (tc) {
+            M->dloss.download(&loss, 1, M->stream);
+            PG_CUDA(cudaStreamSynchronize(M->stream));
         }
         if (epoch_loss) epoch_loss[ep] = (float)(loss / (double)n);
     }

@@ -69,6 +69,40 @@ def test_gradients_match_oracle():
     assert np.abs(g - ref_g).max() <= 1e-4 * np.abs(ref_g).max()
 
 
+@pytest.mark.parametrize("n_in", [34, 35, 64])
+def test_tensor_core_gradients_match_oracle(n_in):
+    """Networks of two 64-unit layers train on the tensor cores (BF16 products,
+    FP32 sums): against the oracle with the same BF16 layer errors to 1e-4 of
+    the largest component, against the oracle without them to 2e-2."""
+    net, pb = _net(n_in, 64, 64, seed=6)
+    rng = np.random.default_rng(7)
+    x = rng.normal(0, 1, (1000, n_in)).astype(np.float32)  # 15 full tiles of 64 samples and a ragged one
+    y = rng.normal(0, 1, 1000).astype(np.float32)
+    loss, g = net.gradients(x, y)
+    ref_loss, ref_g = MO.loss_and_grad(pb, x, y, n_in, 64, 64, tensor_core=True)
+    assert loss == pytest.approx(ref_loss, rel=1e-5)
+    assert np.abs(g - ref_g).max() <= 1e-4 * np.abs(ref_g).max()
+    _, plain = MO.loss_and_grad(pb, x, y, n_in, 64, 64)
+    assert np.abs(g - plain).max() <= 2e-2 * np.abs(plain).max()
+    loss2, g2 = net.gradients(x, y)  # deterministic
+    assert loss2 == loss and np.array_equal(g2, g)
+
+
+def test_tensor_core_training_reduces_loss_and_is_deterministic():
+    rng = np.random.default_rng(8)
+    x = rng.normal(0, 1, (20000, 34)).astype(np.float32)
+    w = rng.normal(0, 1, 34)
+    y = np.tanh(x @ w / 6.0).astype(np.float32)
+    runs = []
+    for _ in range(2):
+        net, _ = _net(34, 64, 64, seed=9)
+        net.add_samples(x, y)
+        losses = net.train(6, batch=1024, learning_rate=2e-3, seed=13)
+        runs.append((losses, net.get_params()))
+    assert runs[0][0][-1] < 0.3 * runs[0][0][0]
+    assert np.array_equal(runs[0][0], runs[1][0]) and np.array_equal(runs[0][1], runs[1][1])
+
+
 @pytest.mark.parametrize("n_gauss", [8, 16])
 def test_descriptors_match_oracle(n_gauss):
     sys.path.insert(0, GOLDEN)

@@ -12,14 +12,16 @@ def test_oracle_gradient_matches_finite_differences():
     p = rng.normal(0, 0.5, h1 * n_in + h1 + h2 * h1 + h2 + h2 + 1)
     x = rng.normal(0, 1, (17, n_in))
     y = rng.normal(0, 1, 17)
-    _, g = M.loss_and_grad(p, x, y, n_in, h1, h2)
+    # the calculus of the gradient, without the BF16 operand rounding (piecewise constant)
+    _, g = M.loss_and_grad(p, x, y, n_in, h1, h2, exact=True)
     eps = 1e-6
     fd = np.zeros_like(p)
     for k in range(len(p)):
         a, b = p.copy(), p.copy()
         a[k] += eps
         b[k] -= eps
-        fd[k] = (M.loss_and_grad(a, x, y, n_in, h1, h2)[0] - M.loss_and_grad(b, x, y, n_in, h1, h2)[0]) / (2 * eps)
+        fd[k] = (M.loss_and_grad(a, x, y, n_in, h1, h2, exact=True)[0] -
+                 M.loss_and_grad(b, x, y, n_in, h1, h2, exact=True)[0]) / (2 * eps)
     np.testing.assert_allclose(g, fd, rtol=1e-6, atol=1e-8)
 
 
