@@ -452,12 +452,43 @@ def charge_relax_gain(n_configs, device, cpu_threads=0):
         calc.get_atoms().set_initial_charges(np.zeros(len(atoms)))
         rmse.append(float(np.sqrt(np.mean((net.predict_charges(calc) - q_cold) ** 2))))
         dq.append(float(np.abs(q_warm - q_cold).max()))
+    # steps against the starting error: the converged charges of box 0 plus
+    # seeded Gaussian noise (sum kept at zero), relaxed again to the same tolerance
+    calc = pysic.Pysic(W.sio2_box(1000, seed=0), pots, coulomb=coul, precision="mixed")
+    calc.set_core()
+    q_exact, rc0 = relax(calc)
+    curve = []
+    for sigma in (0.1, 0.05, 0.02, 0.01, 0.005, 0.002, 0.001, 0.0005, 0.0002, 0.0001):
+        st = []
+        for rep in range(2):
+            dq = np.random.default_rng(1000 + rep).normal(0.0, sigma, len(q_exact))
+            q0 = q_exact + dq - dq.mean()
+            calc.get_atoms().set_initial_charges(q0)
+            rel = pysic.ChargeRelaxation("dynamic", calculator=calc,
+                                         parameters=[RELAX[k] for k in ("n_steps", "timestep", "inertia", "friction",
+                                                                        "tolerance")])
+            rel.charge_relaxation()
+            st.append(rel.last_steps)
+        curve.append({"start_rmse_e": sigma, "steps": float(np.mean(st)),
+                      "step_gain": rc0.last_steps / float(np.mean(st))})
+    # the starting error at which the step gain reaches 3 (log-linear between the measured points)
+    need = None
+    for a, b in zip(curve, curve[1:]):
+        if a["step_gain"] < 3.0 <= b["step_gain"]:
+            t = (3.0 - a["step_gain"]) / (b["step_gain"] - a["step_gain"])
+            need = float(np.exp(np.log(a["start_rmse_e"]) + t * (np.log(b["start_rmse_e"]) - np.log(a["start_rmse_e"]))))
+            break
+    gain_curve = {"box": "seed 0", "cold_steps": rc0.last_steps, "points": curve,
+                  "start_rmse_for_3x_step_gain_e": need,
+                  "network_rmse_e": float(np.mean(rmse)),
+                  "note": "white noise on the converged charges; the damped dynamics converge linearly at the rate "
+                          "of the softest charge mode, so steps grow with log(start error / tolerance)"}
     cpu = relax_cpu_baseline(cpu_threads) if cpu_threads > 0 else None
     if cpu is not None:
         cpu["gpu_cold_ms_same_box"] = 1e3 * cold_t[0]
         cpu["gpu_cold_steps_same_box"] = cold_s[0]
     return {"configs": n_configs, "atoms": 3000, "settings": RELAX, "precision": "mixed",
-            "cpu_baseline": cpu,
+            "cpu_baseline": cpu, "gain_vs_start_error": gain_curve,
             "cold_steps_mean": float(np.mean(cold_s)), "warm_steps_mean": float(np.mean(warm_s)),
             "cold_ms_mean": 1e3 * float(np.mean(cold_t)), "warm_ms_mean": 1e3 * float(np.mean(warm_t)),
             "wall_time_gain": float(np.sum(cold_t) / np.sum(warm_t)),

@@ -1,10 +1,12 @@
 """GPU checks of the learned warm start (csrc/mlp.cu) against the FP64 NumPy
 oracle (oracle/mlp_oracle.py).
 
-Tolerances: the engine reads BF16 weights and sums in FP32, the oracle uses
-the same BF16-rounded weights in FP64, so forward values agree to ~1e-6
-relative and gradients (sums over the batch) to 1e-4 relative to the largest
-component.  Descriptors: FP32 against FP64, 1e-5 relative.
+Tolerances: the engine reads BF16 weights, rounds inputs and first-layer
+activations to BF16 and sums in FP32; the oracle does the same in FP64, so
+forward values agree to ~1e-6 relative except where a first-layer activation
+falls on the other side of a BF16 rounding boundary (one BF16 step, rare), and
+gradients (sums over the batch) to 1e-4 relative to the largest component.
+Descriptors: FP32 against FP64, 1e-5 relative.
 """
 import os
 import sys
@@ -38,7 +40,12 @@ def test_forward_matches_oracle(sizes):
     x = rng.normal(0, 1, (2001, n_in)).astype(np.float32)
     got = net.predict(x)  # identity normalisation
     ref, _, _ = MO.forward(pb, x, n_in, h1, h2)
-    np.testing.assert_allclose(got, ref, rtol=1e-5, atol=1e-5)
+    # the first-layer activations are rounded to BF16: where FP32 tanh (device)
+    # and FP64 tanh (oracle) fall on either side of a rounding boundary, one
+    # activation differs by one BF16 step (2^-8 relative); everything else agrees
+    close = np.abs(got - ref) <= 1e-5 + 1e-5 * np.abs(ref)
+    assert close.mean() >= 0.99
+    assert np.abs(got - ref).max() <= 1e-2 * max(1.0, np.abs(ref).max())
 
 
 def test_device_warm_start_matches_host_path():
@@ -134,6 +141,25 @@ def test_training_reduces_loss_and_is_deterministic():
     losses, p = runs[0]
     assert losses[-1] < 0.25 * losses[0]
     assert np.array_equal(p, runs[1][1])
+
+
+def test_shipped_network_cuts_relaxation_steps_on_a_held_out_box():
+    """The shipped SiO2 network (trained on boxes of seeds 100000 and up) on a
+    held-out 3000-atom box with the benchmark's relaxation settings: strictly
+    fewer damped-dynamics steps to the same tolerance, the same charges."""
+    from pysic_gb300.train_warm_start import RELAX, relax
+
+    net = ChargeNetwork.load(os.path.join(os.path.dirname(pysic.__file__), "data", "sio2_warm_start.npz"))
+    pots, coul = W.sio2_potentials()
+    calc = pysic.Pysic(W.sio2_box(1000, seed=1), pots, coulomb=coul, precision="mixed")
+    q_cold, cold = relax(calc, RELAX)
+    q_warm, warm = relax(calc, RELAX, network=net)
+    assert cold.last_converged and warm.last_converged
+    print("held-out box: cold %d steps, warm %d steps, prediction RMSE %.4f e" % (
+        cold.last_steps, warm.last_steps,
+        float(np.sqrt(np.mean((net.predict_charges(calc) - q_cold) ** 2)))))
+    assert warm.last_steps < cold.last_steps
+    np.testing.assert_allclose(q_warm, q_cold, atol=2e-4)
 
 
 def test_warm_start_relaxation_reaches_the_same_charges():
