@@ -108,6 +108,18 @@ int pg_set_pair_potentials(pg_context* ctx, int32_t n_types, int32_t n_records, 
 int pg_set_triplet_potentials(pg_context* ctx, int32_t n_records, const int32_t* kind, const double* params,
                               const double* cutoff, const double* soft, const uint64_t* mask1,
                               const uint64_t* mask2, const uint64_t* mask3, const uint64_t* center);
+/* Products of pair potentials (ProductPotential, pysic/interactions/local.py:7-283;
+ * add_potential with is_multiplier, PyInterface.f90:433-480, Core.f90:909-953),
+ * set after pg_set_pair_potentials (which clears them): per pair record the
+ * number of factors besides the record itself (0: a plain record, at most 8)
+ * and the index of its first factor; per factor its kind and 4 parameters (as
+ * for pair records) and the types of the product's first target, which decide
+ * the parameter order of charge-dependent factors.  Energy, forces and
+ * electronegativities follow the product rule (Potentials.f90:2512-2700); the
+ * record's own smooth cutoff multiplies the whole product.  Products cannot
+ * carry a bond-order factor (PG_ERR_UNSUPPORTED). */
+int pg_set_pair_products(pg_context* ctx, int32_t n_records, const int32_t* n_mul, const int32_t* mul0,
+                         int32_t n_factors, const int32_t* kind, const double* params, const uint64_t* first);
 /* Per pair record: the types of its unpermuted first target
  * (original_elements(1) of create_potential, Potentials.f90:2353-2472), which
  * decide charge_pair's exponent order (Potentials.f90:4415-4513). */

@@ -365,6 +365,107 @@ static void pair_force(int kind, const double* p, double cut, const double sep[3
     }
 }
 
+static inline int has(uint64_t mask, int t) { return (int)((mask >> t) & 1u); }
+
+/* One factor of a product potential for the pair (atom1, atom2) as the loop
+ * picks it: its energy, its force on atom 1 and its electronegativities of
+ * atoms 1 and 2, without any cut factor (evaluate_energy_component,
+ * evaluate_force_component, evaluate_electronegativity_component,
+ * Potentials.f90:2512-2890).  Charge terms have no force routine; other terms
+ * no electronegativity. */
+static void product_component(const orc_model* m, int kind, const double* p, uint64_t first, double rc, int t1,
+                              double q1, double q2, const double sep[3], double d, double* e, double f[3],
+                              double en[2]) {
+    for (int c = 0; c < 3; ++c) f[c] = 0.0;
+    en[0] = en[1] = 0.0;
+    if (kind < 7) {
+        *e = pair_energy(kind, p, rc, d, m->pair_table);
+        pair_force(kind, p, rc, sep, d, f, m->pair_table);
+        return;
+    }
+    const int direct = has(first, t1);
+    if (kind == 7) {
+        const int n1 = direct ? (int)p[1] : (int)p[2], n2 = direct ? (int)p[2] : (int)p[1];
+        *e = p[0] * (__builtin_powi(q1, n1) * __builtin_powi(q2, n2));
+        en[0] = n1 > 0 ? -p[0] * (n1 * __builtin_powi(q1, n1 - 1) * __builtin_powi(q2, n2)) : 0.0;
+        en[1] = n2 > 0 ? -p[0] * (n2 * __builtin_powi(q1, n1) * __builtin_powi(q2, n2 - 1)) : 0.0;
+    } else if (kind == 8) {
+        const double* c = m->pair_table + 2 * (int64_t)p[0];
+        const double r2 = c[direct ? 1 : 5], r3 = c[direct ? 5 : 1];
+        const double r4 = c[direct ? 3 : 7], r5 = c[direct ? 7 : 3];
+        const double r6 = c[direct ? 11 : 12], r7 = c[direct ? 12 : 11];
+        const double r8 = c[direct ? 13 : 14], r9 = c[direct ? 14 : 13];
+        const double d3 = c[direct ? 9 : 10], d4 = c[direct ? 10 : 9];
+        const double d5 = r8 * (r4 - q1), d6 = r9 * (r5 - q2);
+        const double d1 = r2 + pow(fabs(d5), r6), d2 = r3 + pow(fabs(d6), r7);
+        const double v = c[0] * exp(0.5 * (d3 * d1 + d4 * d2));
+        *e = v;
+        en[0] = v * d3 * 0.5 * r6 * pow(fabs(d5), r6 - 1.0) * copysign(1.0, d5) * r8;
+        en[1] = v * d4 * 0.5 * r7 * pow(fabs(d6), r7 - 1.0) * copysign(1.0, d6) * r9;
+    } else {
+        const double* c = m->pair_table + 2 * (int64_t)p[0];
+        const double* s1 = c + (direct ? 0 : 4);
+        const double* s2 = c + (direct ? 4 : 0);
+        double f1 = s1[0] + s1[1] * pow(fabs(q1 - s1[2]), s1[3]);
+        double f2 = s2[0] + s2[1] * pow(fabs(q2 - s2[2]), s2[3]);
+        if (f1 < 0.0) f1 = 0.0;
+        if (f2 < 0.0) f2 = 0.0;
+        *e = sqrt(f1 * f2);
+        const double abs1 = fabs(q1 - s1[2]), abs2 = fabs(q2 - s2[2]);
+        const double pow1 = pow(abs1, s1[3] - 1), pow2 = pow(abs2, s2[3] - 1);
+        double g1 = s1[0] + s1[1] * abs1 * pow1, g2 = s2[0] + s2[1] * abs2 * pow2;
+        const double dd1 = -s1[3] * pow1 * copysign(1.0, q1 - s1[2]) * s1[1];
+        const double dd2 = -s2[3] * pow2 * copysign(1.0, q2 - s2[2]) * s2[1];
+        double inv_sqrt = 0.5 / sqrt(g1 * g2);
+        if (g1 < 0.0) {
+            g1 = 0.0;
+            inv_sqrt = 0.0;
+        }
+        if (g2 < 0.0) {
+            g2 = 0.0;
+            inv_sqrt = 0.0;
+        }
+        en[0] = inv_sqrt * dd1 * g2;
+        en[1] = inv_sqrt * dd2 * g1;
+    }
+}
+
+/* A product of n factors (the record itself, then its components): energy,
+ * force on atom 1 and electronegativities combined as evaluate_energy /
+ * evaluate_forces / evaluate_electronegativity do for n_product > 1
+ * (Potentials.f90:2512-2700): each factor's force and electronegativity
+ * weighted by E / E_k, or by the product of the others where E_k = 0. */
+static void product_term(const orc_model* m, int r, int t1, double q1, double q2, const double sep[3], double d,
+                         double* e, double f[3], double en[2]) {
+    const int n = 1 + m->pair_nmul[r];
+    double ek[16], fk[16][3], nk[16][2];
+    for (int k = 0; k < n && k < 16; ++k) {
+        const int c = m->pair_mul0[r] + k - 1;
+        const int kind = k == 0 ? m->pair_kind[r] : m->mul_kind[c];
+        const double* p = k == 0 ? m->pair_params + 4 * (size_t)r : m->mul_params + 4 * (size_t)c;
+        const uint64_t first = k == 0 ? m->pair_first[r] : m->mul_first[c];
+        product_component(m, kind, p, first, m->pair_cutoff[r], t1, q1, q2, sep, d, &ek[k], fk[k], nk[k]);
+    }
+    double energy = 1.0;
+    for (int k = 0; k < n; ++k) energy *= ek[k];
+    *e = energy;
+    for (int c = 0; c < 3; ++c) f[c] = 0.0;
+    en[0] = en[1] = 0.0;
+    for (int k = 0; k < n; ++k) {
+        double w;
+        if (ek[k] != 0.0) {
+            w = energy / ek[k];
+        } else {
+            w = 1.0;
+            for (int q = 0; q < n; ++q)
+                if (q != k) w *= ek[q];
+        }
+        for (int c = 0; c < 3; ++c) f[c] += w * fk[k][c];
+        en[0] += w * nk[k][0];
+        en[1] += w * nk[k][1];
+    }
+}
+
 /* evaluate_pair_bond_order_factor_tersoff, Potentials.f90:5744-5795.
  * sep1 = separations(:,1), sep2 = separations(:,2) */
 static double tersoff_factor(const double* bp, double cut, double soft, const double sep1[3], const double sep2[3],
@@ -467,7 +568,6 @@ typedef struct {
     double* af_fac;    /* n_groups x n: post-processed per-atom factors (saved_bond_order_factors) */
 } ctx_t;
 
-static inline int has(uint64_t mask, int t) { return (int)((mask >> t) & 1u); }
 
 /* first post-processing factor of the atom's element in the group:
  * core_post_process_pair_bond_order_factor, Core.f90:2763-2807 */
@@ -971,6 +1071,41 @@ static void* loop_range(void* arg) {
                 if (!(m->pair_cutoff[r] > d)) continue;
                 if (!has(m->pair_mask2[r], tj)) continue;
                 const int kind = m->pair_kind[r];
+                if (m->pair_nmul && m->pair_nmul[r] > 0) {
+                    /* a product of potentials (n_product > 1): the product's energy, force and
+                       electronegativities times the record's smooth cut (Core.f90:4257-4385,
+                       5371-5606, 5622-5775); products carry no bond-order factor */
+                    const int smp = X->smoothened[r];
+                    const double rcp = m->pair_cutoff[r], rsp = X->smooth_soft[r];
+                    double v, fp[3], en[2];
+                    product_term(m, r, ti, qi, s->charge[j], sep, d, &v, fp, en);
+                    const double cut = smp ? smooth_factor(d, rcp, rsp) : 1.0;
+                    if (J->what == 0) {
+                        J->energy += v * cut;
+                    } else if (J->what == 1) {
+                        double cg[3] = {0, 0, 0}, p2[3];
+                        if (smp) {
+                            const double dv = smooth_deriv(d, rcp, rsp);
+                            for (int c = 0; c < 3; ++c) cg[c] = dir[c] * dv;
+                        }
+                        for (int c = 0; c < 3; ++c) {
+                            const double p1 = fp[c] * cut + v * cg[c];
+                            p2[c] = -fp[c] * cut - v * cg[c];
+                            F[3 * (size_t)i + c] += p1;
+                            F[3 * (size_t)j + c] += p2[c];
+                        }
+                        st[0] += sep[0] * p2[0];
+                        st[1] += sep[1] * p2[1];
+                        st[2] += sep[2] * p2[2];
+                        st[3] += sep[1] * p2[2];
+                        st[4] += sep[0] * p2[2];
+                        st[5] += sep[0] * p2[1];
+                    } else {
+                        chi[i] += en[0] * cut;
+                        chi[j] += en[1] * cut;
+                    }
+                    continue;
+                }
                 /* non-charge pair potentials have zero electronegativity */
                 if (J->what == 2 && kind < 7) continue;
                 const double* p = m->pair_params + 4 * (size_t)r;

@@ -95,6 +95,15 @@ typedef struct {
     const uint64_t* afac_mask2;   /* 0 for the one-target scalers */
     const int32_t* afac_group;
     const int32_t* single_group;  /* per single record: -1 or the group of its coordinator (null: all -1) */
+    /* products of pair potentials (ProductPotential, pysic/interactions/local.py:7-283): per pair record
+       the number of multiplying components (0: a plain record) and the index of its first component;
+       per component its kind, 4 parameters (table rows as for pair records) and the types of the
+       product's first target (null pair_nmul: no products) */
+    const int32_t* pair_nmul;
+    const int32_t* pair_mul0;
+    const int32_t* mul_kind;
+    const double* mul_params;
+    const uint64_t* mul_first;
 } orc_model;
 
 /* CSR neighbour list: entries of atom i are [start[i], start[i+1]). */

@@ -40,7 +40,8 @@ class _Model(ctypes.Structure):
                 ("tri_cutoff", _dp), ("tri_soft", _dp), ("tri_mask1", _up), ("tri_mask2", _up), ("tri_mask3", _up),
                 ("tri_center", _up), ("pair_first", _up), ("n_afac", ctypes.c_int32), ("afac_kind", _ip),
                 ("afac_params", _dp), ("afac_cutoff", _dp), ("afac_soft", _dp), ("afac_mask1", _up),
-                ("afac_mask2", _up), ("afac_group", _ip), ("single_group", _ip)]
+                ("afac_mask2", _up), ("afac_group", _ip), ("single_group", _ip), ("pair_nmul", _ip),
+                ("pair_mul0", _ip), ("mul_kind", _ip), ("mul_params", _dp), ("mul_first", _up)]
 
 
 class _NbList(ctypes.Structure):
@@ -154,6 +155,11 @@ def _model(keep, M, n):
     m.single_params = _d(keep.f64(a["single_params"]))
     m.single_mask = _u(keep.u64(a["single_mask"]))
     m.single_group = _i(keep.i32(a["single_group"]))
+    m.pair_nmul = _i(keep.i32(a["pair_nmul"] if len(a["pair_nmul"]) else np.zeros(1)))
+    m.pair_mul0 = _i(keep.i32(a["pair_mul0"] if len(a["pair_mul0"]) else np.zeros(1)))
+    m.mul_kind = _i(keep.i32(a["mul_kind"] if len(a["mul_kind"]) else np.zeros(1)))
+    m.mul_params = _d(keep.f64(a["mul_params"] if len(a["mul_params"]) else np.zeros((1, 4))))
+    m.mul_first = _u(keep.u64(a["mul_first"] if len(a["mul_first"]) else np.zeros(1)))
     m.n_afac = len(a["afac_kind"])
     m.afac_kind = _i(keep.i32(a["afac_kind"]))
     m.afac_params = _d(keep.f64(a["afac_params"]))

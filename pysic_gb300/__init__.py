@@ -11,12 +11,12 @@ from .calculator import FastNeighborList, Pysic
 from .core import *  # noqa: F401,F403  descriptor queries of pysic.core
 from .error import *  # noqa: F401,F403
 from .interactions import (BondOrderParameters, CompoundPotential, Coordinator, CoulombSummation, Potential,
-                           SuttonChenPotential, estimate_ewald_parameters)
+                           ProductPotential, SuttonChenPotential, estimate_ewald_parameters)
 from .md import VelocityVerlet
 from .relaxation import ChargeRelaxation
 
 __version__ = "0.1.0"
 
-__all__ = ["Atoms", "Pysic", "VelocityVerlet", "FastNeighborList", "Potential", "BondOrderParameters", "Coordinator",
+__all__ = ["Atoms", "Pysic", "VelocityVerlet", "FastNeighborList", "Potential", "ProductPotential", "BondOrderParameters", "Coordinator",
            "CoulombSummation", "ChargeRelaxation", "estimate_ewald_parameters", "CompoundPotential",
            "SuttonChenPotential"]

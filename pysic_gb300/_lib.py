@@ -51,6 +51,8 @@ _SIGNATURES = {
     "pg_get_atom_charges": (ctypes.c_int, [_ctx, _c_double_p]),
     "pg_set_pair_potentials": (ctypes.c_int, [_ctx, ctypes.c_int32, ctypes.c_int32, _c_int_p, _c_double_p,
                                               _c_double_p, _c_double_p, _c_u64_p, _c_u64_p, _c_int_p]),
+    "pg_set_pair_products": (ctypes.c_int, [_ctx, ctypes.c_int32, _c_int_p, _c_int_p, ctypes.c_int32, _c_int_p,
+                                            _c_double_p, _c_u64_p]),
     "pg_set_pair_tables": (ctypes.c_int, [_ctx, ctypes.c_int64, _c_double_p]),
     "pg_set_pair_first_targets": (ctypes.c_int, [_ctx, ctypes.c_int32, _c_u64_p]),
     "pg_set_triplet_potentials": (ctypes.c_int, [_ctx, ctypes.c_int32, _c_int_p, _c_double_p, _c_double_p,

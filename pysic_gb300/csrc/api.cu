@@ -527,6 +527,34 @@ int pg_set_pair_potentials(pg_context* ctx, int32_t n_types, int32_t n, const in
         ctx->pr_m1.assign(mask1, mask1 + n);
         ctx->pr_m2.assign(mask2, mask2 + n);
         ctx->pr_group.assign(group, group + n);
+        ctx->pr_nmul.clear();  // products are set after the records they extend
+        ctx->pr_mul0.clear();
+        ctx->tables_dirty = true;
+    });
+}
+
+int pg_set_pair_products(pg_context* ctx, int32_t n_records, const int32_t* n_mul, const int32_t* mul0,
+                         int32_t n_factors, const int32_t* kind, const double* params, const uint64_t* first) {
+    return guarded([&] {
+        check_ctx(ctx);
+        pg::require(n_records == (int)ctx->pr_kind.size(), PG_ERR_INVALID,
+                    "one product entry per pair record set by pg_set_pair_potentials");
+        pg::require(n_factors >= 0 && (n_factors == 0 || (kind && params && first)), PG_ERR_INVALID,
+                    "invalid product factors");
+        pg::require(n_records == 0 || (n_mul && mul0), PG_ERR_INVALID, "null product arrays");
+        for (int r = 0; r < n_records; ++r) {
+            pg::require(n_mul[r] >= 0 && n_mul[r] <= 8 && mul0[r] >= 0 && mul0[r] + n_mul[r] <= n_factors,
+                        PG_ERR_INVALID, "product factors out of range (at most 8 factors besides the lead)");
+            pg::require(n_mul[r] == 0 || ctx->pr_group[r] < 0, PG_ERR_UNSUPPORTED,
+                        "bond-order scaled products of potentials are not evaluated by the GB300 engine");
+        }
+        for (int c = 0; c < n_factors; ++c)
+            pg::require(kind[c] >= 0 && kind[c] <= 9, PG_ERR_UNSUPPORTED, "unknown pair potential kind in a product");
+        ctx->pr_nmul.assign(n_mul, n_mul + n_records);
+        ctx->pr_mul0.assign(mul0, mul0 + n_records);
+        ctx->pm_kind.assign(kind, kind + n_factors);
+        ctx->pm_params.assign(params, params + 4 * (size_t)n_factors);
+        ctx->pm_first.assign(first, first + n_factors);
         ctx->tables_dirty = true;
     });
 }

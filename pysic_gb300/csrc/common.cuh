@@ -153,6 +153,8 @@ struct PairT {
     unsigned long long first;  // charge_pair: types of the unpermuted first target (original_elements(1))
     int agroup;          // -1, or the per-atom bond-order group whose factors scale the term
     int ni;              // power / shift_power: the exponent when it is an integer, else PG_NOT_INT
+    int mul0, nmul;      // a product of potentials: its nmul other factors are the records mul0 .. (never
+                         // evaluated on their own; kept after every type pair's records)
 };
 
 // marks a non-integer exponent (general pow instead of repeated squaring)
@@ -217,7 +219,7 @@ struct TriT {
 template <typename R, typename S>
 inline PairT<R> cast_pair(const PairT<S>& a) {
     return PairT<R>{a.kind, a.group, a.smooth, a.in_bond_kernel, (R)a.p0, (R)a.p1, (R)a.p2, (R)a.p3, (R)a.rc, (R)a.rs,
-                    a.t0, a.tn, a.first, a.agroup, a.ni};
+                    a.t0, a.tn, a.first, a.agroup, a.ni, a.mul0, a.nmul};
 }
 template <typename R, typename S>
 inline TripT<R> cast_trip(const TripT<S>& a) {
@@ -333,6 +335,10 @@ struct pg_context {
     pg::DevBuf<int2> d_pair_index;     // per (ti, tj): offset, count into d_pair_terms
     std::vector<double> pr_table;      // tabulated potentials: rows (V, d) of every table, concatenated
     std::vector<uint64_t> pr_first;    // per pair record: types of its unpermuted first target
+    std::vector<int> pr_nmul, pr_mul0; // per pair record: factors of a product (0: a plain record), first factor
+    std::vector<int> pm_kind;          // product factors: kind, 4 parameters, types of the product's first target
+    std::vector<double> pm_params;
+    std::vector<uint64_t> pm_first;
     bool have_charge_pairs = false;    // a charge-dependent pair term (charge_pair)
     pg::DevBuf<double> d_tab64;        // the rows on the device, FP64 and FP32
     pg::DevBuf<float> d_tab32;

@@ -118,8 +118,33 @@ void fold_tables(pg_context* ctx) {
     ctx->bo_radius = bo_radius;
 
     std::vector<PairT<double>> terms;
+    std::vector<PairT<double>> factors;  // product factors, appended after every type pair's records
     std::vector<int2> index((size_t)T * T, make_int2(0, 0));
     bool pair_kernel_terms = false, charge_pairs = false;
+    // one pair term from a kind and 4 parameters (table rows checked here: the
+    // kernels index rows t0 .. t0 + tn - 1 only)
+    auto fill_params = [&](PairT<double>& t, const double* p4) {
+        t.p0 = p4[0];
+        t.p1 = p4[1];
+        t.p2 = p4[2];
+        t.p3 = p4[3];
+        if (t.kind == 8 || t.kind == 9) {  // charge_exp / charge_abs: parameters as rows of the table array
+            t.t0 = (int)t.p0;
+            t.tn = t.kind == 8 ? 8 : 4;
+            require(t.t0 >= 0 && (size_t)t.t0 + (size_t)t.tn <= ctx->pr_table.size() / 2, PG_ERR_INVALID,
+                    "charge_exp / charge_abs: parameter rows out of bounds");
+        }
+        if (t.kind == 6) {  // tabulated: params first row, rows, range, scale
+            t.t0 = (int)t.p0;
+            t.tn = (int)t.p1;
+            require(t.t0 >= 0 && t.tn >= 2 && (size_t)t.t0 + (size_t)t.tn <= ctx->pr_table.size() / 2 && t.p2 > 0.0,
+                    PG_ERR_INVALID, "tabulated potential: table rows or range out of bounds");
+            t.p0 = t.p2;  // range
+            t.p1 = t.p3;  // scale
+        }
+        t.ni = t.kind == 4 ? integral_exponent(t.p2) : t.kind == 5 ? integral_exponent(t.p3) : PG_NOT_INT;
+    };
+    const bool have_products = (int)ctx->pr_nmul.size() == np;
     for (int ti = 0; ti < T; ++ti)
         for (int tj = 0; tj < T; ++tj) {
             int2& ix = index[(size_t)ti * T + tj];
@@ -133,29 +158,23 @@ void fold_tables(pg_context* ctx) {
                 t.agroup = g >= 0 && g != tersoff_gid ? gmap.at(g) : -1;
                 require(!(t.agroup >= 0 && t.kind >= 7), PG_ERR_UNSUPPORTED,
                         "bond-order scaling of charge_pair is not evaluated by the GB300 engine");
-                t.p0 = ctx->pr_params[4 * (size_t)r];
-                t.p1 = ctx->pr_params[4 * (size_t)r + 1];
-                t.p2 = ctx->pr_params[4 * (size_t)r + 2];
-                t.p3 = ctx->pr_params[4 * (size_t)r + 3];
-                if (t.kind == 8 || t.kind == 9) {  // charge_exp / charge_abs: parameters as rows of the table array
-                    t.t0 = (int)t.p0;
-                    t.tn = t.kind == 8 ? 8 : 4;
-                    require(t.t0 >= 0 && (size_t)t.t0 + (size_t)t.tn <= ctx->pr_table.size() / 2, PG_ERR_INVALID,
-                            "charge_exp / charge_abs: parameter rows out of bounds");
-                }
-                if (t.kind == 6) {  // tabulated: params first row, rows, range, scale
-                    t.t0 = (int)t.p0;
-                    t.tn = (int)t.p1;
-                    // the kernels index rows t0 .. t0 + tn - 1 only: checked here
-                    require(t.t0 >= 0 && t.tn >= 2 && (size_t)t.t0 + (size_t)t.tn <= ctx->pr_table.size() / 2 &&
-                                t.p2 > 0.0,
-                            PG_ERR_INVALID, "tabulated potential: table rows or range out of bounds");
-                    t.p0 = t.p2;  // range
-                    t.p1 = t.p3;  // scale
-                }
+                fill_params(t, &ctx->pr_params[4 * (size_t)r]);
                 t.first = r < (int)ctx->pr_first.size() ? ctx->pr_first[r] : 0ull;
-                t.ni = t.kind == 4 ? integral_exponent(t.p2) : t.kind == 5 ? integral_exponent(t.p3) : PG_NOT_INT;
                 t.rc = ctx->pr_cut[r];
+                // a product: its factors, in the record's own order
+                t.nmul = have_products ? ctx->pr_nmul[r] : 0;
+                t.mul0 = (int)factors.size();
+                for (int c = 0; c < t.nmul; ++c) {
+                    const int f = ctx->pr_mul0[r] + c;
+                    PairT<double> u{};
+                    u.kind = ctx->pm_kind[f];
+                    u.group = u.agroup = -1;
+                    fill_params(u, &ctx->pm_params[4 * (size_t)f]);
+                    u.first = ctx->pm_first[f];
+                    u.rc = u.rs = ctx->pr_cut[r];  // a spring factor is shifted at the product's cutoff
+                    if (u.kind >= 7) charge_pairs = true;
+                    factors.push_back(u);
+                }
                 const double soft = ctx->pr_soft[r];
                 if (soft > 0.0 && soft < t.rc) {
                     t.smooth = 1;
@@ -165,13 +184,21 @@ void fold_tables(pg_context* ctx) {
                     t.rs = t.rc;
                 }
                 // charge-dependent pair terms stay in the pair kernel (electronegativities)
-                t.in_bond_kernel = bond && t.kind < 7 && t.agroup < 0 && (t.group >= 0 || t.rc <= bo_radius);
+                t.in_bond_kernel =
+                    bond && t.kind < 7 && t.nmul == 0 && t.agroup < 0 && (t.group >= 0 || t.rc <= bo_radius);
                 if (t.kind >= 7) charge_pairs = true;
                 if (!t.in_bond_kernel) pair_kernel_terms = true;
                 terms.push_back(t);
             }
             ix.y = (int)terms.size() - ix.x;
         }
+    // the factors after all records; the records' factor indices point there
+    {
+        const int base = (int)terms.size();
+        for (auto& t : terms)
+            if (t.nmul > 0) t.mul0 += base;
+        terms.insert(terms.end(), factors.begin(), factors.end());
+    }
     // single-atom terms
     std::vector<SingleTerm> sterms;
     std::vector<int2> sindex(T, make_int2(0, 0));

@@ -75,6 +75,13 @@ class Engine:
             self.ctx, model.n_types, npair, L.iptr(a["pair_kind"]), L.dptr(a["pair_params"]),
             L.dptr(a["pair_cutoff"]), L.dptr(a["pair_soft"]), L.u64ptr(a["pair_mask1"]), L.u64ptr(a["pair_mask2"]),
             L.iptr(a["pair_group"])))
+        nm = L.as_i32(a["pair_nmul"]) if len(a["pair_nmul"]) else np.zeros(max(npair, 1), dtype=np.int32)
+        m0 = L.as_i32(a["pair_mul0"]) if len(a["pair_mul0"]) else np.zeros(max(npair, 1), dtype=np.int32)
+        mk = L.as_i32(a["mul_kind"]) if len(a["mul_kind"]) else np.zeros(1, dtype=np.int32)
+        mp = L.as_f64(a["mul_params"]) if len(a["mul_params"]) else np.zeros(4)
+        mf = L.as_u64(a["mul_first"]) if len(a["mul_first"]) else np.zeros(1, dtype=np.uint64)
+        L.check(self.lib.pg_set_pair_products(self.ctx, npair, L.iptr(nm), L.iptr(m0), len(a["mul_kind"]), L.iptr(mk),
+                                              L.dptr(mp), L.u64ptr(mf)))
         L.check(self.lib.pg_set_single_potentials(
             self.ctx, len(a["single_kind"]), L.iptr(a["single_kind"]), L.dptr(a["single_params"]),
             L.u64ptr(a["single_mask"])))

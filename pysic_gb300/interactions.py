@@ -209,6 +209,76 @@ class Potential(object):
                                       self.indices)
 
 
+class ProductPotential:
+    """A potential that is the product of several potentials with the same
+    number of targets (pysic/interactions/local.py:7-283).  The first potential
+    leads: its targets, cutoff, cutoff margin and coordinator are the
+    product's; the others only multiply (``is_multiplier``).  Energies,
+    forces and electronegativities follow the product rule
+    (Potentials.f90:2512-2700), the leading potential's smooth cutoff applies
+    to the whole product."""
+
+    def __init__(self, potentials):
+        self.potentials = []
+        self.n_targets = None
+        self.add_potential(potentials)
+
+    def __eq__(self, other):
+        try:
+            return self.n_targets == other.n_targets and self.potentials == other.potentials
+        except AttributeError:
+            return False
+
+    def __ne__(self, other):
+        return not self.__eq__(other)
+
+    def __repr__(self):
+        return "ProductPotential({0})".format(self.potentials)
+
+    def set_potentials(self, potentials):
+        self.potentials = []
+        self.n_targets = None
+        self.add_potential(potentials)
+
+    def add_potential(self, potential):
+        """Adds a potential, a list of potentials or the factors of another product."""
+        for pot in (potential if isinstance(potential, list) else [potential]):
+            if self.n_targets is None:
+                self.n_targets = pot.get_number_of_targets()
+            elif self.n_targets != pot.get_number_of_targets():
+                raise InvalidPotentialError("You may only multiply potentials with the same number of targets.")
+            for p in pot.get_potentials():
+                self.potentials.append(copy.deepcopy(p))
+
+    def get_potentials(self):
+        return self.potentials
+
+    def is_multiplier(self):
+        return [False] + [True] * (len(self.potentials) - 1)
+
+    def get_potential_type(self):
+        return self.potentials[0].get_potential_type()
+
+    def get_number_of_targets(self):
+        return self.n_targets
+
+    def accepts_target_list(self, targets):
+        return self.potentials[0].accepts_target_list(targets)
+
+    def __getattr__(self, name):
+        # targets, cutoffs and the coordinator are those of the leading potential
+        if name in ("get_symbols", "get_tags", "get_indices", "get_different_symbols", "get_different_tags",
+                    "get_different_indices", "get_cutoff", "get_cutoff_margin", "get_soft_cutoff",
+                    "get_coordinator", "set_coordinator", "set_symbols", "set_tags", "set_indices",
+                    "add_symbols", "add_tags", "add_indices", "set_cutoff", "set_cutoff_margin",
+                    "set_soft_cutoff"):
+            pots = self.__dict__.get("potentials")
+            if not pots:
+                raise InvalidPotentialError("an empty product of potentials")
+            return getattr(pots[0], name)
+        raise AttributeError(name)
+
+
 class BondOrderParameters:
     """Parameters of one bond-order factor (pysic/interactions/bondorder.py:7-376).
 

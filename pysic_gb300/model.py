@@ -46,6 +46,14 @@ class Model:
         self.pair_mask1 = []
         self.pair_mask2 = []
         self.pair_group = []
+        # products of pair potentials: per pair record the number of multiplying
+        # components and the index of its first one; per component its kind,
+        # parameters and the types of the product's first target
+        self.pair_nmul = []
+        self.pair_mul0 = []
+        self.mul_kind = []
+        self.mul_params = []
+        self.mul_first = []
         self.single_kind = []
         self.single_params = []
         self.single_mask = []
@@ -91,6 +99,11 @@ class Model:
         d["pair_mask1"] = np.array(self.pair_mask1, dtype=np.uint64)
         d["pair_mask2"] = np.array(self.pair_mask2, dtype=np.uint64)
         d["pair_group"] = np.array(self.pair_group, dtype=np.int32)
+        d["pair_nmul"] = np.array(self.pair_nmul, dtype=np.int32)
+        d["pair_mul0"] = np.array(self.pair_mul0, dtype=np.int32)
+        d["mul_kind"] = np.array(self.mul_kind, dtype=np.int32)
+        d["mul_params"] = np.array(self.mul_params, dtype=np.float64).reshape(-1, 4)
+        d["mul_first"] = np.array(self.mul_first, dtype=np.uint64)
         d["single_kind"] = np.array(self.single_kind, dtype=np.int32)
         d["single_params"] = np.array(self.single_params, dtype=np.float64).reshape(-1, 4)
         d["single_mask"] = np.array(self.single_mask, dtype=np.uint64)
@@ -224,12 +237,52 @@ def compile_model(atoms, potentials, coulomb=None):
                 return g
         return -1
 
+    def pair_params_of(kind, params):
+        """the parameters of one pair term as the engine stores them"""
+        if kind == "tabulated":
+            return _table_record(M, params)
+        if kind == "charge_exp":
+            return _charge_exp_record(M, params)
+        if kind == "charge_abs":  # (a, b, Q, n) of both targets as 4 rows of the table array
+            first = len(M.pair_table) // 2
+            M.pair_table.extend([float(x) for x in params[:8]])
+            return [float(first), 0.0, 0.0, 0.0]
+        return params
+
     for pot in potentials:
-        kind = pot.get_potential_type()
+        factors = pot.get_potentials()
+        lead = factors[0]
+        kind = lead.get_potential_type()
         core.check_engine_support(kind)
         nt = pot.get_number_of_targets()
-        params = [float(x) for x in pot.get_parameter_values()]
+        params = [float(x) for x in lead.get_parameter_values()]
         grp = group_of(pot)
+        # a product: the leading potential's records carry the other factors
+        # (calculator.py:1208-1360; the factors take the product's first target
+        # tuple as their own, unpermuted)
+        mul0, nmul = len(M.mul_kind), len(factors) - 1
+        if nmul:
+            if nt != 2:
+                raise InvalidPotentialError("products of {0}-body potentials are not evaluated by the GB300 engine"
+                                            .format(nt))
+            if grp >= 0:
+                raise InvalidPotentialError("bond-order scaled products of potentials are not evaluated by the "
+                                            "GB300 engine")
+            lead_first = next((t for t in (pot.get_symbols(), pot.get_tags(), pot.get_indices()) if t), None)
+            if lead_first is None:
+                raise InvalidPotentialError("a product of potentials without targets")
+            t0 = lead_first[0][0]
+            fmask = _mask(sigs, *((t0, None, None) if pot.get_symbols() else
+                                  (None, int(t0), None) if pot.get_tags() else (None, None, int(t0))))
+            for fac in factors[1:]:
+                fk = fac.get_potential_type()
+                core.check_engine_support(fk)
+                if fk not in core.PAIR_KIND:
+                    raise InvalidPotentialError("'{0}' is not a pair potential of the GB300 engine".format(fk))
+                M.mul_kind.append(core.PAIR_KIND[fk])
+                M.mul_params.append((pair_params_of(fk, [float(x) for x in fac.get_parameter_values()]) +
+                                     [0.0] * 4)[:4])
+                M.mul_first.append(fmask)
         targets = []  # (position filters) tuples of (element, tag, index) per position
         firsts = []   # the unpermuted tuple's first target of each record (original_elements(1))
         for t in pot.get_symbols() or []:
@@ -247,14 +300,7 @@ def compile_model(atoms, potentials, coulomb=None):
         if nt == 2:
             if kind not in core.PAIR_KIND:
                 raise InvalidPotentialError("'{0}' is not a pair potential of the GB300 engine".format(kind))
-            if kind == "tabulated":
-                params = _table_record(M, params)
-            if kind == "charge_exp":
-                params = _charge_exp_record(M, params)
-            if kind == "charge_abs":  # (a, b, Q, n) of both targets as 4 rows of the table array
-                first = len(M.pair_table) // 2
-                M.pair_table.extend([float(x) for x in params[:8]])
-                params = [float(first), 0.0, 0.0, 0.0]
+            params = pair_params_of(kind, params)
             if kind in ("charge_pair", "charge_exp", "charge_abs") and grp >= 0:
                 raise InvalidPotentialError("bond-order scaling of {0} is not evaluated by the GB300 engine".format(kind))
             for tg, first in zip(targets, firsts):
@@ -266,6 +312,8 @@ def compile_model(atoms, potentials, coulomb=None):
                 M.pair_mask1.append(_mask(sigs, *tg[0]))
                 M.pair_mask2.append(_mask(sigs, *tg[1]))
                 M.pair_group.append(grp)
+                M.pair_nmul.append(nmul)
+                M.pair_mul0.append(mul0)
         elif nt == 1:
             if kind not in core.SINGLE_KIND:
                 raise InvalidPotentialError("'{0}' is not a single-atom term of the GB300 engine".format(kind))

@@ -108,6 +108,7 @@ class PysicInterface:
 
     def _reset_records(self):
         self._pots = []  # raw add_potential records
+        self._multipliers = []  # factors of the next product record
         self._bonds = []  # raw add_bond_order_factor records
         self._ewald = None
         self._model = None
@@ -167,7 +168,7 @@ class PysicInterface:
         pass
 
     def clear_potential_multipliers(self):
-        pass
+        self._multipliers = []
 
     def add_potential(self, pot_name, parameters, cutoff, smooth_cut, elements, tags, indices, orig_elements,
                       orig_tags, orig_indices, pot_index, is_multiplier):
@@ -175,14 +176,20 @@ class PysicInterface:
         (calculator.py:1255-1360).  Returns the success flag; products of
         potentials (is_multiplier) are not evaluated by this engine."""
         name = str(pot_name)
-        if name not in core.POTENTIALS or bool(is_multiplier):
+        if name not in core.POTENTIALS:
             return False
         nt = core.POTENTIALS[name][0]
-        self._pots.append({"name": name, "params": [float(x) for x in np.asarray(parameters).reshape(-1)],
-                           "cutoff": float(cutoff), "soft": float(smooth_cut),
-                           "elements": _codes(elements, nt), "tags": _ints(tags, nt), "indices": _ints(indices, nt),
-                           "orig_elements": _codes(orig_elements, nt), "orig_tags": _ints(orig_tags, nt),
-                           "orig_indices": _ints(orig_indices, nt), "group": int(pot_index)})
+        rec = {"name": name, "params": [float(x) for x in np.asarray(parameters).reshape(-1)],
+               "cutoff": float(cutoff), "soft": float(smooth_cut),
+               "elements": _codes(elements, nt), "tags": _ints(tags, nt), "indices": _ints(indices, nt),
+               "orig_elements": _codes(orig_elements, nt), "orig_tags": _ints(orig_tags, nt),
+               "orig_indices": _ints(orig_indices, nt), "group": int(pot_index)}
+        if bool(is_multiplier):
+            # a factor of a product: kept until its leading record arrives (Core.f90:909-953)
+            self._multipliers.append(rec)
+            return True
+        rec["multipliers"] = list(self._multipliers)
+        self._pots.append(rec)
         self._records_dirty = True
         return True
 
@@ -287,6 +294,29 @@ class PysicInterface:
                 M.pair_mask1.append(mask(target(rec, 0)))
                 M.pair_mask2.append(mask(target(rec, 1)))
                 M.pair_group.append(grp)
+                muls = rec.get("multipliers", [])
+                M.pair_nmul.append(len(muls))
+                M.pair_mul0.append(len(M.mul_kind))
+                if muls and grp >= 0:
+                    raise core.InvalidPotentialError("bond-order scaled products of potentials are not evaluated by "
+                                                     "the GB300 engine")
+                for mr in muls:
+                    mk = mr["name"]
+                    core.check_engine_support(mk)
+                    if mk not in core.PAIR_KIND:
+                        raise core.InvalidPotentialError("'{0}' is not a pair potential of the GB300 engine".format(mk))
+                    mp = list(mr["params"])
+                    if mk == "tabulated":
+                        mp = _table_record(M, mp)
+                    elif mk == "charge_exp":
+                        mp = _charge_exp_record(M, mp)
+                    elif mk == "charge_abs":
+                        first = len(M.pair_table) // 2
+                        M.pair_table.extend([float(x) for x in mp[:8]])
+                        mp = [float(first), 0.0, 0.0, 0.0]
+                    M.mul_kind.append(core.PAIR_KIND[mk])
+                    M.mul_params.append((mp + [0.0] * 4)[:4])
+                    M.mul_first.append(mask(target(mr, 0, orig=True)))
             elif nt == 1:
                 if kind not in core.SINGLE_KIND:
                     raise core.InvalidPotentialError("'{0}' is not a single-atom term of the GB300 engine".format(kind))

@@ -213,3 +213,31 @@ def sio2_potentials(real_cutoff=10.0, sigma=2.5, k_cutoff=None, half_hardness=Fa
         k_cutoff = ewald_kcut(sigma)
     coul = CoulombSummation("ewald", [real_cutoff, k_cutoff, sigma, EPS0])
     return pots, coul
+
+
+def product_cases():
+    """Small structures with products of pair potentials (ProductPotential,
+    pysic/interactions/local.py:7-283): a smooth-cut LJ x exponential x
+    Buckingham product on an fcc crystal, and on random SiO2 boxes with
+    charges the charge-dependent products of the COMB repulsion (charge_exp x
+    exponential, the pysic COMB compound's form, pysic/interactions/comb.py:
+    901-977) and a charge_pair x power product, next to plain terms."""
+    P = Potential
+    from .interactions import ProductPotential
+
+    a1 = lj_fcc(2, noise=0.08, seed=41)
+    prod1 = ProductPotential([P("LJ", symbols=[["X", "X"]], parameters=[0.02, 2.9], cutoff=5.0, cutoff_margin=0.7),
+                              P("exponential", symbols=[["X", "X"]], parameters=[1.5, 0.3]),
+                              P("Buckingham", symbols=[["X", "X"]], parameters=[2.0, 0.5, 1.1])])
+    yield "lj_exp_buck", a1, [prod1, P("LJ", symbols=[["X", "X"]], parameters=[0.01, 3.1], cutoff=4.5)]
+    a2 = sio2_box(12, seed=42)
+    q = np.random.default_rng(5).normal(0.0, 0.4, len(a2))
+    a2.set_initial_charges(q - q.mean())
+    cexp = P("charge_exp", symbols=[["Si", "O"], ["O", "O"]],
+             parameters=[0.3, 2.0, 1.0, 2.0, 1.0, 3.0, 1.5, 2.4, 1.2, 0.6, 0.4], cutoff=3.2, cutoff_margin=0.6)
+    prod2 = ProductPotential([cexp, P("exponential", symbols=[["Si", "O"]], parameters=[40.0, 1.8])])
+    prod3 = ProductPotential([P("charge_pair", symbols=[["Si", "Si"], ["Si", "O"]], parameters=[0.4, 2, 1],
+                                cutoff=3.0, cutoff_margin=0.5),
+                              P("power", symbols=[["Si", "Si"]], parameters=[0.8, 2.0, 3.0])])
+    yield "comb_repulsion", a2, [prod2, prod3, P("exponential", symbols=[["O", "O"]], parameters=[10.0, 2.0],
+                                                   cutoff=2.8, cutoff_margin=0.4)]

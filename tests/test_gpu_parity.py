@@ -403,3 +403,20 @@ def test_page_locked_buffers_match_pageable_ones():
         assert err.value.status == L.PG_ERR_INVALID
         eng.calculate_into(prec, flags, e, f, s, c)
         assert e[0] == ref["energy"] and np.array_equal(f, ref["forces"])
+
+
+@pytest.mark.parametrize("case", [c[0] for c in W.product_cases()])
+def test_product_potentials_parity(case):
+    """Products of pair potentials (ProductPotential): FP64 against the oracle
+    (energy 1e-12 relative, forces 1e-10 of the largest force, virial 1e-9,
+    electronegativities 1e-9), mixed precision against FP64 (1e-5 eV/atom,
+    1e-4 of the largest force)."""
+    _, atoms, pots = next(c for c in W.product_cases() if c[0] == case)
+    ref, got = _check_fp64(atoms, pots)
+    assert np.abs(got["enegs"] - ref["enegs"]).max() < 1e-9
+    if case == "comb_repulsion":
+        assert np.abs(ref["enegs"]).max() > 1e-3
+    m = engine_all(atoms, pots, None, "mixed")
+    fmax = max(1.0, np.abs(got["forces"]).max())
+    assert abs(m["energy"] - got["energy"]) / len(atoms) < 1e-5
+    assert np.abs(m["forces"] - got["forces"]).max() < 1e-4 * fmax

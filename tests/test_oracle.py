@@ -550,3 +550,37 @@ def test_oracle_charge_abs_derivatives():
             p1[a, c] += h
             p2[a, c] -= h
             assert f[a, c] == pytest.approx(-(ev(p1, q, "energy") - ev(p2, q, "energy")) / (2 * h), abs=1e-7)
+
+
+# ---- products of potentials ---------------------------------------------------
+
+@pytest.mark.parametrize("case", [c[0] for c in W.product_cases()])
+def test_oracle_product_derivatives(case):
+    """Products of pair potentials in the oracle (Potentials.f90:2512-2700):
+    forces are minus the position gradient of the energy and electronegativities
+    minus its charge derivatives, by finite differences."""
+    _, atoms, pots = next(c for c in W.product_cases() if c[0] == case)
+    model = compile_model(atoms, pots)
+    assert max(model.pair_nmul) > 0
+    lists = oracle_lists(atoms, pots)
+    pos, q = atoms.get_positions(), atoms.get_initial_charges()
+
+    def ev(p, qq, what):
+        return oracle.evaluate(p, qq, atoms.get_cell(), atoms.get_pbc(), model, *lists, what=what)
+
+    f, _ = ev(pos, q, "forces")
+    chi = ev(pos, q, "enegs")
+    assert np.abs(f).max() > 1e-3
+    h = 1e-6
+    scale = max(1.0, np.abs(f).max())
+    for a in (0, 5, 17):
+        for c in range(3):
+            p1, p2 = pos.copy(), pos.copy()
+            p1[a, c] += h
+            p2[a, c] -= h
+            assert f[a, c] == pytest.approx(-(ev(p1, q, "energy") - ev(p2, q, "energy")) / (2 * h), abs=1e-6 * scale)
+        if case == "comb_repulsion":
+            q1, q2 = q.copy(), q.copy()
+            q1[a] += h
+            q2[a] -= h
+            assert chi[a] == pytest.approx(-(ev(pos, q1, "energy") - ev(pos, q2, "energy")) / (2 * h), abs=1e-6)

@@ -74,7 +74,10 @@ def test_shim_signature_conventions():
     assert pi.number_of_targets_of_bond_order_factor("tersoff") == 3
     assert pi.level_of_bond_order_factor("tersoff") == 2
     assert pi.number_of_parameters_of_bond_order_factor("tersoff", 2) == 5
-    # products of potentials are refused with the reference's success flag
-    assert pi.add_potential("LJ", np.array([1.0, 1.0]), 5.0, 5.0, np.zeros((2, 2)), np.array([-9, -9]),
-                            np.array([-9, -9]), np.zeros((2, 2)), np.array([-9, -9]), np.array([-9, -9]), -1,
-                            True) is False
+    # a factor of a product waits for its leading record, which takes it (Core.f90:909-953)
+    none, xx = np.array([-9, -9]), np.array([pf_driver.codes("X")] * 2).T
+    assert pi.add_potential("exponential", np.array([2.0, 0.5]), 5.0, 5.0, xx, none, none, xx, none, none, -1, True)
+    assert pi.add_potential("LJ", np.array([1.0, 1.0]), 5.0, 5.0, xx, none, none, xx, none, none, -1, False)
+    pi.clear_potential_multipliers()
+    assert [m["name"] for m in pi._pots[-1]["multipliers"]] == ["exponential"]
+    assert pi.add_potential("nonsense", np.array([1.0]), 5.0, 5.0, xx, none, none, xx, none, none, -1, False) is False
