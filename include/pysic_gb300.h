@@ -108,6 +108,17 @@ int pg_set_pair_potentials(pg_context* ctx, int32_t n_types, int32_t n_records, 
 int pg_set_triplet_potentials(pg_context* ctx, int32_t n_records, const int32_t* kind, const double* params,
                               const double* cutoff, const double* soft, const uint64_t* mask1,
                               const uint64_t* mask2, const uint64_t* mask3, const uint64_t* center);
+/* add_potential(...) for four-body records (kind 0: dihedral, params k, phi_0;
+ * V = k/2 (cos phi - cos phi_0)^2, Potentials.f90:3329-3611), one record per
+ * distinct permutation of each target tuple as calculator.py adds them: per
+ * record 4 type masks of target positions 1..4 (masks[4 r + t]) and 4 of the
+ * unpermuted tuple (orig[4 r + t]), which the evaluator matches forwards or
+ * backwards along the chain.  At most 64 records.  Chains are found as
+ * core_loop_over_local_interactions finds them (Core.f90:3540-3943): from
+ * every triplet, the fourth atom among the neighbours of either end. */
+int pg_set_quad_potentials(pg_context* ctx, int32_t n_records, const int32_t* kind, const double* params,
+                           const double* cutoff, const double* soft, const uint64_t* masks,
+                           const uint64_t* orig);
 /* Products of pair potentials (ProductPotential, pysic/interactions/local.py:7-283;
  * add_potential with is_multiplier, PyInterface.f90:433-480, Core.f90:909-953),
  * set after pg_set_pair_potentials (which clears them): per pair record the

@@ -911,6 +911,10 @@ static int ipow_i(double x, int k, double* out) {
     return 0;
 }
 
+static void quad_chain(const orc_model* m, const orc_system* s, uint64_t qm, loop_job* J, const int x[4],
+                       const int tp[3], const double s1[3], double d1, const double s2[3], double d2,
+                       const double s3[3], double d3);
+
 static void tri_term(const orc_model* m, int r, loop_job* J, int x, int c, int y, const double s1[3], double d1,
                      const double s2[3], double d2) {
     const double* p = m->tri_params + 4 * (size_t)r;
@@ -1309,13 +1313,18 @@ static void* loop_range(void* arg) {
             }
             /* three-body records (Core.f90:3540-3943): the doublet routines flag
                the many-body potentials of this pair, then the two triplet loops */
-            if (m->n_tri > 0 && d != 0.0) {
-                uint64_t rm = 0;
+            if ((m->n_tri > 0 || m->n_quad > 0) && d != 0.0) {
+                uint64_t rm = 0, qm = 0;
                 for (int r = 0; r < m->n_tri; ++r) {
                     const uint64_t many = m->tri_mask1[r] | m->tri_mask2[r] | m->tri_mask3[r];
                     if (m->tri_cutoff[r] > d && has(many, ti) && has(m->tri_mask2[r], tj)) rm |= 1ull << r;
                 }
-                if (rm) {
+                for (int r = 0; r < m->n_quad; ++r) {
+                    const uint64_t* mk = m->quad_mask + 4 * (size_t)r;
+                    if (m->quad_cutoff[r] > d && has(mk[0] | mk[1] | mk[2] | mk[3], ti) && has(mk[1], tj))
+                        qm |= 1ull << r;
+                }
+                if (rm || qm) {
                     const double s21[3] = {-sep[0], -sep[1], -sep[2]};
                     /* atom2 - atom1 - atom3, atom3 among atom1's neighbours */
                     for (int l = nb->start[i]; l < nb->start[i + 1]; ++l) {
@@ -1332,6 +1341,30 @@ static void* loop_range(void* arg) {
                             if (((rm >> r) & 1) && has(m->tri_mask3[r], tk) && has(m->tri_center[r], ti) &&
                                 m->tri_cutoff[r] > d13)
                                 tri_term(m, r, J, j, i, k, s21, d, s13, d13);
+                        if (!qm) continue;
+                        /* atom4 - atom2 - atom1 - atom3, atom4 among atom2's neighbours (Core.f90:3614-3690) */
+                        for (int q = nb->start[j]; q < nb->start[j + 1]; ++q) {
+                            const int w = nb->idx[q];
+                            const int* oq = nb->off + 3 * (size_t)q;
+                            const int o34[3] = {oq[0] - o23[0], oq[1] - o23[1], oq[2] - o23[2]};
+                            if (!pick(k, w, o34) || w == i) continue;
+                            const int mo[3] = {-oq[0], -oq[1], -oq[2]};
+                            double s42[3];
+                            separation(&X->C, s->pos + 3 * (size_t)w, s->pos + 3 * (size_t)j, mo, s42);
+                            const int x[4] = {w, j, i, k}, tp[3] = {0, 1, 3};
+                            quad_chain(m, s, qm, J, x, tp, s42, sqrt(dot3(s42, s42)), s21, d, s13, d13);
+                        }
+                        /* atom2 - atom1 - atom3 - atom4, atom4 among atom3's neighbours (3695-3750) */
+                        for (int q = nb->start[k]; q < nb->start[k + 1]; ++q) {
+                            const int w = nb->idx[q];
+                            const int* oq = nb->off + 3 * (size_t)q;
+                            const int o24[3] = {oq[0] + o23[0], oq[1] + o23[1], oq[2] + o23[2]};
+                            if (!pick(j, w, o24) || w == i) continue;
+                            double s34[3];
+                            separation(&X->C, s->pos + 3 * (size_t)k, s->pos + 3 * (size_t)w, oq, s34);
+                            const int x[4] = {j, i, k, w}, tp[3] = {0, 2, 3};
+                            quad_chain(m, s, qm, J, x, tp, s21, d, s13, d13, s34, sqrt(dot3(s34, s34)));
+                        }
                     }
                     /* atom1 - atom2 - atom3, atom3 among atom2's neighbours */
                     for (int l = nb->start[j]; l < nb->start[j + 1]; ++l) {
@@ -1348,12 +1381,153 @@ static void* loop_range(void* arg) {
                             if (((rm >> r) & 1) && has(m->tri_mask3[r], tk) && has(m->tri_center[r], tj) &&
                                 m->tri_cutoff[r] > d23)
                                 tri_term(m, r, J, i, j, k, sep, d, s23, d23);
+                        if (!qm) continue;
+                        /* atom4 - atom1 - atom2 - atom3, atom4 among atom1's neighbours (3807-3880) */
+                        for (int q = nb->start[i]; q < nb->start[i + 1]; ++q) {
+                            const int w = nb->idx[q];
+                            const int* oq = nb->off + 3 * (size_t)q;
+                            const int o34[3] = {oq[0] - o13[0], oq[1] - o13[1], oq[2] - o13[2]};
+                            if (!pick(k, w, o34) || w == j) continue;
+                            const int mo[3] = {-oq[0], -oq[1], -oq[2]};
+                            double s41[3];
+                            separation(&X->C, s->pos + 3 * (size_t)w, s->pos + 3 * (size_t)i, mo, s41);
+                            const int x[4] = {w, i, j, k}, tp[3] = {0, 2, 3};
+                            quad_chain(m, s, qm, J, x, tp, s41, sqrt(dot3(s41, s41)), sep, d, s23, d23);
+                        }
+                        /* atom1 - atom2 - atom3 - atom4, atom4 among atom3's neighbours (3885-3940) */
+                        for (int q = nb->start[k]; q < nb->start[k + 1]; ++q) {
+                            const int w = nb->idx[q];
+                            const int* oq = nb->off + 3 * (size_t)q;
+                            const int o14[3] = {oq[0] + o13[0], oq[1] + o13[1], oq[2] + o13[2]};
+                            if (!pick(i, w, o14) || w == j) continue;
+                            double s34[3];
+                            separation(&X->C, s->pos + 3 * (size_t)k, s->pos + 3 * (size_t)w, oq, s34);
+                            const int x[4] = {i, j, k, w}, tp[3] = {1, 2, 3};
+                            quad_chain(m, s, qm, J, x, tp, sep, d, s23, d23, s34, sqrt(dot3(s34, s34)));
+                        }
                     }
                 }
             }
         }
     }
     return NULL;
+}
+
+/* evaluate_energy_dihedral / evaluate_force_dihedral, Potentials.f90:3380-3611:
+ * V = k/2 (cos phi - cos phi_0)^2 of the chain 1-2-3-4 (v12, v23, v34 its
+ * separations), cos phi from the projections of v12 and v34 perpendicular to
+ * v23; zero unless the atoms' types match the unpermuted targets forwards or
+ * backwards.  f[a] is the force on chain atom a. */
+static int dihedral(const orc_model* m, int r, const int t[4], const double v12[3], const double v23[3],
+                    const double v34[3], double* e, double f[4][3]) {
+    const uint64_t* o = m->quad_orig + 4 * (size_t)r;
+    const int ok = (has(o[0], t[0]) && has(o[1], t[1]) && has(o[2], t[2]) && has(o[3], t[3])) ||
+                   (has(o[0], t[3]) && has(o[1], t[2]) && has(o[2], t[1]) && has(o[3], t[0]));
+    *e = 0.0;
+    for (int a = 0; a < 4; ++a)
+        for (int c = 0; c < 3; ++c) f[a][c] = 0.0;
+    if (!ok) return 0;
+    const double k = m->quad_params[4 * (size_t)r], cos0 = cos(m->quad_params[4 * (size_t)r + 1]);
+    const double r2 = sqrt(dot3(v23, v23));
+    const double inv_r2 = 1.0 / (r2 * r2);
+    const double a12 = dot3(v12, v23), a34 = dot3(v34, v23);
+    double p1[3], p2[3];
+    for (int c = 0; c < 3; ++c) {
+        p1[c] = -(v12[c] - a12 * inv_r2 * v23[c]);
+        p2[c] = v34[c] - a34 * inv_r2 * v23[c];
+    }
+    const double dot = dot3(p1, p2);
+    const double inv_p1 = 1.0 / sqrt(dot3(p1, p1)), inv_p2 = 1.0 / sqrt(dot3(p2, p2));
+    const double ratio = inv_p1 * inv_p2;
+    const double off = dot * ratio - cos0;
+    *e = 0.5 * k * off * off;
+    double dd[4][3], dq1[4][3], dq2[4][3];
+    for (int c = 0; c < 3; ++c) {
+        dd[0][c] = -(v34[c] - a34 * inv_r2 * v23[c]);
+        dd[1][c] = v34[c] - a34 * inv_r2 * (v23[c] - v12[c]) + a12 * inv_r2 * v34[c] -
+                   2.0 * a12 * a34 * inv_r2 * inv_r2 * v23[c];
+        dd[2][c] = -(v12[c] + a34 * inv_r2 * v12[c] + a12 * inv_r2 * (v34[c] - v23[c]) -
+                     2.0 * a12 * a34 * inv_r2 * inv_r2 * v23[c]);
+        dd[3][c] = v12[c] - a12 * inv_r2 * v23[c];
+        dq2[0][c] = 0.0;
+        dq2[1][c] = a34 * inv_r2 * v34[c] - a34 * a34 * inv_r2 * inv_r2 * v23[c];
+        dq2[2][c] = -v34[c] + a34 * inv_r2 * (v23[c] - v34[c]) + a34 * a34 * inv_r2 * inv_r2 * v23[c];
+        dq2[3][c] = v34[c] - a34 * inv_r2 * v23[c];
+        dq1[0][c] = -v12[c] + a12 * inv_r2 * v23[c];
+        dq1[1][c] = v12[c] - a12 * inv_r2 * (v23[c] - v12[c]) - a12 * a12 * inv_r2 * inv_r2 * v23[c];
+        dq1[2][c] = -a12 * inv_r2 * v12[c] + a12 * a12 * inv_r2 * inv_r2 * v23[c];
+        dq1[3][c] = 0.0;
+    }
+    const double pre = k * off * ratio;
+    for (int a = 0; a < 4; ++a)
+        for (int c = 0; c < 3; ++c)
+            f[a][c] = pre * (dd[a][c] + dq1[a][c] * dot * inv_p1 * inv_p1 + dq2[a][c] * dot * inv_p2 * inv_p2);
+    return 1;
+}
+
+/* core_evaluate_local_quadruplet_B (Core.f90:7450-7883) for the chain x[0..3]
+ * with separations s1, s2, s3 and distances d1..d3: the records the doublet
+ * flagged (qm), the types of chain positions tp[0..2] tested as target
+ * positions 2, 3, 4, every bond within the record's cutoff; energy times the
+ * three cut factors, forces with the cut gradients, and the virial
+ * s1 (x) F2 + (s1 + s2) (x) F3 + (s1 + s2 + s3) (x) F4. */
+static void quad_chain(const orc_model* m, const orc_system* s, uint64_t qm, loop_job* J, const int x[4],
+                       const int tp[3], const double s1[3], double d1, const double s2[3], double d2,
+                       const double s3[3], double d3) {
+    const int t[4] = {s->type[x[0]], s->type[x[1]], s->type[x[2]], s->type[x[3]]};
+    for (int r = 0; r < m->n_quad; ++r) {
+        if (!((qm >> r) & 1)) continue;
+        const uint64_t* mk = m->quad_mask + 4 * (size_t)r;
+        const double rc = m->quad_cutoff[r], soft = m->quad_soft[r];
+        if (!(has(mk[1], t[tp[0]]) && rc > d1 && has(mk[2], t[tp[1]]) && has(mk[3], t[tp[2]]) && rc > d2 &&
+              rc > d3))
+            continue;
+        if (d1 == 0.0 || d2 == 0.0 || d3 == 0.0) continue;
+        double e, fq[4][3];
+        dihedral(m, r, t, s1, s2, s3, &e, fq);
+        const int sm = soft > 0.0 && soft < rc;
+        const double c1 = sm ? smooth_factor(d1, rc, soft) : 1.0, c2 = sm ? smooth_factor(d2, rc, soft) : 1.0,
+                     c3 = sm ? smooth_factor(d3, rc, soft) : 1.0;
+        if (J->what == 0) {
+            J->energy += e * c1 * c2 * c3;
+            continue;
+        }
+        if (J->what != 1) continue;  /* no electronegativity */
+        double g1[3] = {0, 0, 0}, g2[3] = {0, 0, 0}, g3[3] = {0, 0, 0};
+        if (sm) {
+            const double q1 = smooth_deriv(d1, rc, soft), q2 = smooth_deriv(d2, rc, soft),
+                         q3 = smooth_deriv(d3, rc, soft);
+            for (int c = 0; c < 3; ++c) {
+                g1[c] = q1 * s1[c] / d1;
+                g2[c] = q2 * s2[c] / d2;
+                g3[c] = q3 * s3[c] / d3;
+            }
+        } else {
+            e = 0.0;  /* the energy enters the forces only through the cut gradients */
+        }
+        double qf[4][3];
+        for (int c = 0; c < 3; ++c) {
+            qf[0][c] = fq[0][c] * c1 * c2 * c3 + g1[c] * c2 * c3 * e;
+            qf[1][c] = fq[1][c] * c1 * c2 * c3 + (-g1[c] * c2 * c3 + g2[c] * c1 * c3) * e;
+            qf[2][c] = fq[2][c] * c1 * c2 * c3 + (g3[c] * c1 * c2 - g2[c] * c1 * c3) * e;
+            qf[3][c] = fq[3][c] * c1 * c2 * c3 - g3[c] * c1 * c2 * e;
+        }
+        double* F = J->F;
+        for (int a = 0; a < 4; ++a)
+            for (int c = 0; c < 3; ++c) F[3 * (size_t)x[a] + c] += qf[a][c];
+        double s12[3], s123[3];
+        for (int c = 0; c < 3; ++c) {
+            s12[c] = s1[c] + s2[c];
+            s123[c] = s12[c] + s3[c];
+        }
+        double* st = J->stress;
+        st[0] += s1[0] * qf[1][0] + s12[0] * qf[2][0] + s123[0] * qf[3][0];
+        st[1] += s1[1] * qf[1][1] + s12[1] * qf[2][1] + s123[1] * qf[3][1];
+        st[2] += s1[2] * qf[1][2] + s12[2] * qf[2][2] + s123[2] * qf[3][2];
+        st[3] += s1[1] * qf[1][2] + s12[1] * qf[2][2] + s123[1] * qf[3][2];
+        st[4] += s1[0] * qf[1][2] + s12[0] * qf[2][2] + s123[0] * qf[3][2];
+        st[5] += s1[0] * qf[1][1] + s12[0] * qf[2][1] + s123[0] * qf[3][1];
+    }
 }
 
 /* k-space Ewald: calculate_ewald_energy (Potentials.f90:1428-1653),

@@ -104,6 +104,15 @@ typedef struct {
     const int32_t* mul_kind;
     const double* mul_params;
     const uint64_t* mul_first;
+    /* four-body records (dihedral, Potentials.f90:3329-3611), one per distinct permutation of each
+       target tuple: params (k, theta_0), cutoffs, the type masks of target positions 1-4 of the
+       permuted record and of the unpermuted tuple (the evaluator's forward / reverse check) */
+    int32_t n_quad;
+    const double* quad_params;   /* 4 per record */
+    const double* quad_cutoff;
+    const double* quad_soft;
+    const uint64_t* quad_mask;   /* 4 per record: positions 1-4 */
+    const uint64_t* quad_orig;   /* 4 per record: unpermuted positions 1-4 */
 } orc_model;
 
 /* CSR neighbour list: entries of atom i are [start[i], start[i+1]). */

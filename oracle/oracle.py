@@ -41,7 +41,9 @@ class _Model(ctypes.Structure):
                 ("tri_center", _up), ("pair_first", _up), ("n_afac", ctypes.c_int32), ("afac_kind", _ip),
                 ("afac_params", _dp), ("afac_cutoff", _dp), ("afac_soft", _dp), ("afac_mask1", _up),
                 ("afac_mask2", _up), ("afac_group", _ip), ("single_group", _ip), ("pair_nmul", _ip),
-                ("pair_mul0", _ip), ("mul_kind", _ip), ("mul_params", _dp), ("mul_first", _up)]
+                ("pair_mul0", _ip), ("mul_kind", _ip), ("mul_params", _dp), ("mul_first", _up),
+                ("n_quad", ctypes.c_int32), ("quad_params", _dp), ("quad_cutoff", _dp), ("quad_soft", _dp),
+                ("quad_mask", _up), ("quad_orig", _up)]
 
 
 class _NbList(ctypes.Structure):
@@ -160,6 +162,12 @@ def _model(keep, M, n):
     m.mul_kind = _i(keep.i32(a["mul_kind"] if len(a["mul_kind"]) else np.zeros(1)))
     m.mul_params = _d(keep.f64(a["mul_params"] if len(a["mul_params"]) else np.zeros((1, 4))))
     m.mul_first = _u(keep.u64(a["mul_first"] if len(a["mul_first"]) else np.zeros(1)))
+    m.n_quad = len(a["quad_kind"])
+    m.quad_params = _d(keep.f64(a["quad_params"] if len(a["quad_kind"]) else np.zeros((1, 4))))
+    m.quad_cutoff = _d(keep.f64(a["quad_cutoff"] if len(a["quad_kind"]) else np.zeros(1)))
+    m.quad_soft = _d(keep.f64(a["quad_soft"] if len(a["quad_kind"]) else np.zeros(1)))
+    m.quad_mask = _u(keep.u64(a["quad_mask"] if len(a["quad_kind"]) else np.zeros((1, 4))))
+    m.quad_orig = _u(keep.u64(a["quad_orig"] if len(a["quad_kind"]) else np.zeros((1, 4))))
     m.n_afac = len(a["afac_kind"])
     m.afac_kind = _i(keep.i32(a["afac_kind"]))
     m.afac_params = _d(keep.f64(a["afac_params"]))

@@ -57,6 +57,8 @@ _SIGNATURES = {
     "pg_set_pair_first_targets": (ctypes.c_int, [_ctx, ctypes.c_int32, _c_u64_p]),
     "pg_set_triplet_potentials": (ctypes.c_int, [_ctx, ctypes.c_int32, _c_int_p, _c_double_p, _c_double_p,
                                                  _c_double_p, _c_u64_p, _c_u64_p, _c_u64_p, _c_u64_p]),
+    "pg_set_quad_potentials": (ctypes.c_int, [_ctx, ctypes.c_int32, _c_int_p, _c_double_p, _c_double_p,
+                                              _c_double_p, _c_u64_p, _c_u64_p]),
     "pg_set_single_potentials": (ctypes.c_int, [_ctx, ctypes.c_int32, _c_int_p, _c_double_p, _c_u64_p]),
     "pg_set_single_groups": (ctypes.c_int, [_ctx, ctypes.c_int32, _c_int_p]),
     "pg_set_pair_lanes": (ctypes.c_int, [_ctx, ctypes.c_int32]),

@@ -50,10 +50,12 @@ PAIR_KIND = {"LJ": 0, "exponential": 1, "Buckingham": 2, "spring": 3, "power": 4
              "charge_pair": 7, "charge_exp": 8, "charge_abs": 9}
 SINGLE_KIND = {"charge_self": 0, "constant": 1, "force": 2}
 TRIPLET_KIND = {"bond_bend": 0}
+QUAD_KIND = {"dihedral": 0}
 BOND_KIND = {"tersoff": 0}
 ATOM_FACTOR_KIND = {"neighbors": 0, "power_bond": 1, "c_scale": 2, "sqrt_scale": 3, "table_bond": 4,
                     "table_scale": 5}
-ENGINE_SUPPORTED = set(PAIR_KIND) | set(SINGLE_KIND) | set(TRIPLET_KIND) | set(BOND_KIND) | set(ATOM_FACTOR_KIND)
+ENGINE_SUPPORTED = (set(PAIR_KIND) | set(SINGLE_KIND) | set(TRIPLET_KIND) | set(QUAD_KIND) | set(BOND_KIND) |
+                    set(ATOM_FACTOR_KIND))
 
 
 def list_potentials():

@@ -581,6 +581,26 @@ int pg_set_triplet_potentials(pg_context* ctx, int32_t n, const int32_t* kind, c
     });
 }
 
+int pg_set_quad_potentials(pg_context* ctx, int32_t n, const int32_t* kind, const double* params,
+                           const double* cutoff, const double* soft, const uint64_t* masks,
+                           const uint64_t* orig) {
+    return guarded([&] {
+        check_ctx(ctx);
+        pg::require(n >= 0 && n <= pg::PG_MAX_QUAD_RECORDS, PG_ERR_UNSUPPORTED,
+                    "four-body records: at most 64 (distinct permutations of all target tuples)");
+        pg::require(n == 0 || (kind && params && cutoff && soft && masks && orig), PG_ERR_INVALID,
+                    "null record arrays");
+        for (int r = 0; r < n; ++r) pg::require(kind[r] == 0, PG_ERR_UNSUPPORTED, "unknown four-body kind");
+        ctx->qd_kind.assign(kind, kind + n);
+        ctx->qd_params.assign(params, params + 4 * (size_t)n);
+        ctx->qd_cut.assign(cutoff, cutoff + n);
+        ctx->qd_soft.assign(soft, soft + n);
+        ctx->qd_mask.assign(masks, masks + 4 * (size_t)n);
+        ctx->qd_orig.assign(orig, orig + 4 * (size_t)n);
+        ctx->tables_dirty = true;
+    });
+}
+
 int pg_set_pair_first_targets(pg_context* ctx, int32_t n, const uint64_t* masks) {
     return guarded([&] {
         check_ctx(ctx);

@@ -216,6 +216,18 @@ struct TriT {
     unsigned long long m2, m3, many, center;
 };
 
+// Four-body record (dihedral: V = k/2 (cos phi - cos phi_0)^2,
+// Potentials.f90:3329-3611): the masks of the permuted record's target
+// positions 2, 3, 4, the types at any position, and the unpermuted tuple's
+// types (the evaluator's forward / backward match).
+template <typename R>
+struct QuadT {
+    R k, cos0, rc, rs;
+    int smooth, kind;
+    unsigned long long m2, m3, m4, many;
+    unsigned long long orig[4];
+};
+
 template <typename R, typename S>
 inline PairT<R> cast_pair(const PairT<S>& a) {
     return PairT<R>{a.kind, a.group, a.smooth, a.in_bond_kernel, (R)a.p0, (R)a.p1, (R)a.p2, (R)a.p3, (R)a.rc, (R)a.rs,
@@ -352,6 +364,12 @@ struct pg_context {
     pg::DevBuf<pg::TriT<double>> d_tri;  // folded records, FP64 and FP32
     pg::DevBuf<pg::TriT<float>> d_tri32;
     int n_tri = 0;
+    std::vector<int> qd_kind;            // four-body records as set through the C ABI
+    std::vector<double> qd_params, qd_cut, qd_soft;
+    std::vector<uint64_t> qd_mask, qd_orig;  // 4 per record
+    pg::DevBuf<pg::QuadT<double>> d_quad;    // folded records, FP64 and FP32
+    pg::DevBuf<pg::QuadT<float>> d_quad32;
+    int n_quad = 0;
     pg::DevBuf<long long> tri_facc;      // per atom x 3: three-body forces in 2^-40 fixed point
     pg::DevBuf<double> d_maxbr;          // per type: max bond-order cutoff (max_bond_radius)
     pg::DevBuf<float> d_maxbr32;
@@ -599,6 +617,7 @@ void launch_atom_factors(pg_context* ctx, int precision, int stage, bool first_f
 void atom_factor_gradients(pg_context* ctx, int precision, int group, int atom, int of_factor, double* out);
 // triplet.cu: three-body potentials (bond_bend)
 constexpr int PG_MAX_TRIPLET_RECORDS = 64;
+constexpr int PG_MAX_QUAD_RECORDS = 64;
 void launch_triplets(pg_context* ctx, int precision, int flags, bool first_f, FxAcc* acc, const int* skip);
 // optimize.cu: the constrained energy minimum over the charges (quadratic energies)
 void optimize_charges(pg_context* ctx, int precision, int max_iter, double tolerance, double* charges, int* iterations,

@@ -324,10 +324,41 @@ void fold_tables(pg_context* ctx) {
                                            t.kind, t.m2, t.m3, t.many, t.center};
         }
         ctx->n_tri = nt3;
-        ctx->have_triplets = nt3 > 0;
         ctx->d_tri.upload(tri.data(), tri.size(), st);
         ctx->d_tri32.upload(tri32.data(), tri32.size(), st);
     }
+    // four-body records: cos(phi_0) once per record (the evaluator's cos(params(2)),
+    // Potentials.f90:3407)
+    {
+        const int nq = (int)ctx->qd_kind.size();
+        std::vector<QuadT<double>> quad((size_t)std::max(nq, 1));
+        std::vector<QuadT<float>> quad32((size_t)std::max(nq, 1));
+        for (int r = 0; r < nq; ++r) {
+            const double* p = ctx->qd_params.data() + 4 * (size_t)r;
+            const uint64_t* mk = ctx->qd_mask.data() + 4 * (size_t)r;
+            QuadT<double> q{};
+            q.kind = ctx->qd_kind[r];
+            q.k = p[0];
+            q.cos0 = std::cos(p[1]);
+            q.rc = ctx->qd_cut[r];
+            const double soft = ctx->qd_soft[r];
+            q.smooth = soft > 0.0 && soft < q.rc;
+            q.rs = q.smooth ? soft : q.rc;
+            q.m2 = mk[1];
+            q.m3 = mk[2];
+            q.m4 = mk[3];
+            q.many = mk[0] | mk[1] | mk[2] | mk[3];
+            for (int t = 0; t < 4; ++t) q.orig[t] = ctx->qd_orig[4 * (size_t)r + t];
+            quad[(size_t)r] = q;
+            QuadT<float> q32{(float)q.k, (float)q.cos0, (float)q.rc, (float)q.rs, q.smooth, q.kind,
+                             q.m2, q.m3, q.m4, q.many, {q.orig[0], q.orig[1], q.orig[2], q.orig[3]}};
+            quad32[(size_t)r] = q32;
+        }
+        ctx->n_quad = nq;
+        ctx->d_quad.upload(quad.data(), quad.size(), st);
+        ctx->d_quad32.upload(quad32.data(), quad32.size(), st);
+    }
+    ctx->have_triplets = ctx->n_tri > 0 || ctx->n_quad > 0;
     {
         std::vector<double> t64 = ctx->pr_table;
         if (t64.empty()) t64.assign(2, 0.0);

@@ -26,6 +26,22 @@
 // (sep1 (x) F_centre + (sep1 + sep2) (x) F_3, Core.f90:6980-6991) to the exact
 // block totals.  The centre's smooth-cutoff gradient terms are those of
 // 6860-6888.
+//
+// Four-body (dihedral) chains come from the same loops (Core.f90:3614-3940):
+// every triplet x - c - y above is extended by a fourth atom among the
+// neighbours of either end, giving the chains
+//   A1 w - atom2 - atom1 - atom3   (w among atom2's neighbours),
+//   A2 atom2 - atom1 - atom3 - w   (w among atom3's neighbours),
+//   B1 w - atom1 - atom2 - atom3   (w among atom1's neighbours),
+//   B2 atom1 - atom2 - atom3 - w   (w among atom3's neighbours),
+// each pair of a chain picked once by its image offset, w never the triplet's
+// far end.  core_evaluate_local_quadruplet_B (7450-7883) tests three of the
+// chain's types as the record's target positions 2, 3, 4 (which three depends
+// on the loop: the list positions as the reference passes them), every bond
+// within the cutoff; the dihedral evaluator (Potentials.f90:3380-3611) then
+// requires the unpermuted target tuple along the chain, forwards or
+// backwards.  The quadruplet variant of the kernel is a separate
+// instantiation, so bond_bend-only models keep the smaller kernel.
 #include <algorithm>
 #include <cmath>
 
@@ -52,6 +68,8 @@ struct TriArgs {
     const F4* disp;   // mixed path: displacements since the build
     const void* rec;  // TriT<R>
     int nrec;
+    const void* qrec;  // QuadT<R>
+    int nqrec;
     long long* facc;  // n x 3 fixed-point forces
     FxAcc* acc;       // energy, virial totals (null: none)
     const int* skip;
@@ -146,6 +164,54 @@ __device__ __forceinline__ void bend_term(const TriT<R>& T, const V3<R>& s1, R d
 __device__ __forceinline__ bool bit(unsigned long long m, int t) { return (m >> t) & 1ull; }
 
 template <typename R>
+__device__ __forceinline__ R dot(const V3<R>& a, const V3<R>& b) {
+    return a.x * b.x + a.y * b.y + a.z * b.z;
+}
+
+// One dihedral term of the chain 1-2-3-4 with separations v12, v23, v34
+// (evaluate_energy_dihedral / evaluate_force_dihedral, Potentials.f90:
+// 3380-3611): V = k/2 (cos phi - cos phi_0)^2, cos phi the cosine between the
+// parts of v12 (reversed) and v34 perpendicular to v23; f[a] the force on
+// chain atom a, without the cut factors.  With p1, p2 those parts and
+// c = p1.p2 / (|p1| |p2|), F_a = k (c - cos phi_0) / (|p1| |p2|)
+// (D_a + c |p2| / |p1| Q1_a + c |p1| / |p2| Q2_a), where D_a, Q1_a, Q2_a are
+// minus the gradients of p1.p2, |p1|^2 / 2, |p2|^2 / 2 with respect to atom a.
+template <typename R>
+__device__ __forceinline__ void dihedral_term(const QuadT<R>& Q, const V3<R>& v12, const V3<R>& v23,
+                                              const V3<R>& v34, R& e, V3<R> f[4]) {
+    const R ir = R(1) / dot(v23, v23);
+    const R a12 = dot(v12, v23), a34 = dot(v34, v23);
+    const R u = a12 * ir, w = a34 * ir;
+    const V3<R> p1{-(v12.x - u * v23.x), -(v12.y - u * v23.y), -(v12.z - u * v23.z)};
+    const V3<R> p2{v34.x - w * v23.x, v34.y - w * v23.y, v34.z - w * v23.z};
+    const R pp = dot(p1, p2);
+    const R i1 = R(1) / sqrt_(dot(p1, p1)), i2 = R(1) / sqrt_(dot(p2, p2));
+    const R ratio = i1 * i2;
+    const R off = pp * ratio - Q.cos0;
+    e = R(0.5) * Q.k * off * off;
+    const R pre = Q.k * off * ratio;
+    const R g1 = pp * i1 * i1, g2 = pp * i2 * i2;  // weights of Q1_a, Q2_a
+    const R uw2 = R(2) * u * w, uu = u * u, ww = w * w;
+    // atom 1: D = -p2, Q1 = p1, Q2 = 0; atom 4: D = -p1, Q1 = 0, Q2 = p2
+    f[0] = V3<R>{pre * (-p2.x + g1 * p1.x), pre * (-p2.y + g1 * p1.y), pre * (-p2.z + g1 * p1.z)};
+    f[3] = V3<R>{pre * (-p1.x + g2 * p2.x), pre * (-p1.y + g2 * p2.y), pre * (-p1.z + g2 * p2.z)};
+    // atoms 2 and 3 (the centre bond)
+    auto mid = [&](R a, R b, R c, R& r2, R& r3) {  // components of v12, v23, v34
+        const R d2 = c - w * (b - a) + u * c - uw2 * b;
+        const R q22 = w * c - ww * b;
+        const R q12 = a - u * (b - a) - uu * b;
+        r2 = pre * (d2 + q12 * g1 + q22 * g2);
+        const R d3 = -(a + w * a + u * (c - b) - uw2 * b);
+        const R q23 = -c + w * (b - c) + ww * b;
+        const R q13 = -u * a + uu * b;
+        r3 = pre * (d3 + q13 * g1 + q23 * g2);
+    };
+    mid(v12.x, v23.x, v34.x, f[1].x, f[2].x);
+    mid(v12.y, v23.y, v34.y, f[1].y, f[2].y);
+    mid(v12.z, v23.z, v34.z, f[1].z, f[2].z);
+}
+
+template <typename R, bool QUAD>
 __global__ void __launch_bounds__(TT) tri_kernel(const __grid_constant__ TriArgs A) {
     __shared__ Fx128 wsum[TT / 32][7];
     __shared__ unsigned done;
@@ -172,6 +238,55 @@ __global__ void __launch_bounds__(TT) tri_kernel(const __grid_constant__ TriArgs
         W4 += s1.x * fc.z + s12.x * fy.z;
         W5 += s1.x * fc.y + s12.x * fy.y;
     };
+    const QuadT<R>* qrecs = (const QuadT<R>*)A.qrec;
+    // the chain x[0..3] with separations s1, s2, s3: the records of qm whose
+    // target positions 2, 3, 4 hold the types of chain positions tp0, tp1, tp2
+    auto chain = [&](unsigned long long qm, const int x[4], int tp0, int tp1, int tp2, const V3<R>& s1, R d1,
+                     const V3<R>& s2, R d2, const V3<R>& s3, R d3) {
+        if (d1 == R(0) || d2 == R(0) || d3 == R(0)) return;
+        const int t[4] = {A.type[x[0]], A.type[x[1]], A.type[x[2]], A.type[x[3]]};
+        for (unsigned long long q = qm; q; q &= q - 1) {
+            const QuadT<R>& Q = qrecs[__ffsll((long long)q) - 1];
+            if (!(bit(Q.m2, t[tp0]) && bit(Q.m3, t[tp1]) && bit(Q.m4, t[tp2]) && Q.rc > d1 && Q.rc > d2 &&
+                  Q.rc > d3))
+                continue;
+            const bool fwd = bit(Q.orig[0], t[0]) && bit(Q.orig[1], t[1]) && bit(Q.orig[2], t[2]) &&
+                             bit(Q.orig[3], t[3]);
+            const bool bwd = bit(Q.orig[0], t[3]) && bit(Q.orig[1], t[2]) && bit(Q.orig[2], t[1]) &&
+                             bit(Q.orig[3], t[0]);
+            if (!fwd && !bwd) continue;
+            R e;
+            V3<R> f[4];
+            dihedral_term<R>(Q, s1, s2, s3, e, f);
+            if (Q.smooth) {  // cut factors of the three bonds and their gradients (Core.f90:7587-7725)
+                R c1, g1, c2, g2, c3, g3;
+                smooth<R>(d1, Q.rc, Q.rs, c1, g1);
+                smooth<R>(d2, Q.rc, Q.rs, c2, g2);
+                smooth<R>(d3, Q.rc, Q.rs, c3, g3);
+                const R c123 = c1 * c2 * c3;
+                const R h1 = g1 / d1 * c2 * c3 * e, h2 = g2 / d2 * c1 * c3 * e, h3 = g3 / d3 * c1 * c2 * e;
+                f[0] = V3<R>{f[0].x * c123 + h1 * s1.x, f[0].y * c123 + h1 * s1.y, f[0].z * c123 + h1 * s1.z};
+                f[1] = V3<R>{f[1].x * c123 - h1 * s1.x + h2 * s2.x, f[1].y * c123 - h1 * s1.y + h2 * s2.y,
+                             f[1].z * c123 - h1 * s1.z + h2 * s2.z};
+                f[2] = V3<R>{f[2].x * c123 - h2 * s2.x + h3 * s3.x, f[2].y * c123 - h2 * s2.y + h3 * s3.y,
+                             f[2].z * c123 - h2 * s2.z + h3 * s3.z};
+                f[3] = V3<R>{f[3].x * c123 - h3 * s3.x, f[3].y * c123 - h3 * s3.y, f[3].z * c123 - h3 * s3.z};
+                e *= c123;
+            }
+            En += e;
+            for (int a = 0; a < 4; ++a) add_force(A.facc, A.n, x[a], f[a]);
+            // virial s1 (x) F2 + (s1 + s2) (x) F3 + (s1 + s2 + s3) (x) F4
+            const V3<R> u2{s1.x + s2.x, s1.y + s2.y, s1.z + s2.z};
+            const V3<R> u3{u2.x + s3.x, u2.y + s3.y, u2.z + s3.z};
+            W0 += s1.x * f[1].x + u2.x * f[2].x + u3.x * f[3].x;
+            W1 += s1.y * f[1].y + u2.y * f[2].y + u3.y * f[3].y;
+            W2 += s1.z * f[1].z + u2.z * f[2].z + u3.z * f[3].z;
+            W3 += s1.y * f[1].z + u2.y * f[2].z + u3.y * f[3].z;
+            W4 += s1.x * f[1].z + u2.x * f[2].z + u3.x * f[3].z;
+            W5 += s1.x * f[1].y + u2.x * f[2].y + u3.x * f[3].y;
+        }
+    };
+    auto norm = [](const V3<R>& v) { return sqrt_(v.x * v.x + v.y * v.y + v.z * v.z); };
     if (i < A.n) {
         const int ti = A.type[i];
         const int b1 = A.start[i], e1 = A.start[i + 1];
@@ -187,7 +302,11 @@ __global__ void __launch_bounds__(TT) tri_kernel(const __grid_constant__ TriArgs
             unsigned long long rm = 0;
             for (int r = 0; r < A.nrec; ++r)
                 if (recs[r].rc > d12 && bit(recs[r].many, ti) && bit(recs[r].m2, tj)) rm |= 1ull << r;
-            if (!rm) continue;
+            unsigned long long qm = 0;
+            if (QUAD)
+                for (int r = 0; r < A.nqrec; ++r)
+                    if (qrecs[r].rc > d12 && bit(qrecs[r].many, ti) && bit(qrecs[r].m2, tj)) qm |= 1ull << r;
+            if (!rm && !qm) continue;
             const V3<R> s21{-s12.x, -s12.y, -s12.z};
             // A: atom2 - atom1 - atom3 over atom1's neighbours
             for (int l = b1; l < e1; ++l) {
@@ -201,6 +320,24 @@ __global__ void __launch_bounds__(TT) tri_kernel(const __grid_constant__ TriArgs
                 for (unsigned long long q = rm; q; q &= q - 1) {
                     const TriT<R>& T = recs[__ffsll((long long)q) - 1];
                     if (bit(T.m3, tk) && bit(T.center, ti) && T.rc > d13) account(T, j, i, k, s21, d12, s13, d13);
+                }
+                if (!QUAD || !qm) continue;
+                // A1: w - atom2 - atom1 - atom3, w among atom2's neighbours
+                for (int q = A.start[j]; q < A.start[j + 1]; ++q) {
+                    const int w = A.idx[q];
+                    if (w == i || !pick(k, w, A.off[3 * q] - p0, A.off[3 * q + 1] - p1, A.off[3 * q + 2] - p2)) continue;
+                    const V3<R> v = entry_vector<R>(A, j, q);
+                    const V3<R> s42{-v.x, -v.y, -v.z};
+                    const int x[4] = {w, j, i, k};
+                    chain(qm, x, 0, 1, 3, s42, norm(s42), s21, d12, s13, d13);
+                }
+                // A2: atom2 - atom1 - atom3 - w, w among atom3's neighbours
+                for (int q = A.start[k]; q < A.start[k + 1]; ++q) {
+                    const int w = A.idx[q];
+                    if (w == i || !pick(j, w, A.off[3 * q] + p0, A.off[3 * q + 1] + p1, A.off[3 * q + 2] + p2)) continue;
+                    const V3<R> s34 = entry_vector<R>(A, k, q);
+                    const int x[4] = {j, i, k, w};
+                    chain(qm, x, 0, 2, 3, s21, d12, s13, d13, s34, norm(s34));
                 }
             }
             // B: atom1 - atom2 - atom3 over atom2's neighbours
@@ -216,6 +353,24 @@ __global__ void __launch_bounds__(TT) tri_kernel(const __grid_constant__ TriArgs
                 for (unsigned long long q = rm; q; q &= q - 1) {
                     const TriT<R>& T = recs[__ffsll((long long)q) - 1];
                     if (bit(T.m3, tk) && bit(T.center, tj) && T.rc > d23) account(T, i, j, k, s12, d12, s23, d23);
+                }
+                if (!QUAD || !qm) continue;
+                // B1: w - atom1 - atom2 - atom3, w among atom1's neighbours
+                for (int q = b1; q < e1; ++q) {
+                    const int w = A.idx[q];
+                    if (w == j || !pick(k, w, A.off[3 * q] - p0, A.off[3 * q + 1] - p1, A.off[3 * q + 2] - p2)) continue;
+                    const V3<R> v = entry_vector<R>(A, i, q);
+                    const V3<R> s41{-v.x, -v.y, -v.z};
+                    const int x[4] = {w, i, j, k};
+                    chain(qm, x, 0, 2, 3, s41, norm(s41), s12, d12, s23, d23);
+                }
+                // B2: atom1 - atom2 - atom3 - w, w among atom3's neighbours
+                for (int q = A.start[k]; q < A.start[k + 1]; ++q) {
+                    const int w = A.idx[q];
+                    if (w == j || !pick(i, w, A.off[3 * q] + p0, A.off[3 * q + 1] + p1, A.off[3 * q + 2] + p2)) continue;
+                    const V3<R> s34 = entry_vector<R>(A, k, q);
+                    const int x[4] = {i, j, k, w};
+                    chain(qm, x, 1, 2, 3, s12, d12, s23, d23, s34, norm(s34));
                 }
             }
         }
@@ -250,7 +405,7 @@ __global__ void tri_clear_mag(int n, long long* __restrict__ facc, const int* sk
 
 void launch_triplets(pg_context* ctx, int precision, int flags, bool first_f, FxAcc* acc, const int* skip) {
     const int n = ctx->n;
-    if (n == 0 || ctx->n_tri == 0) return;
+    if (n == 0 || ctx->n_tri + ctx->n_quad == 0) return;
     cudaStream_t st = ctx->stream;
     if (ctx->tri_facc.n != 4 * (size_t)n) {  // 3 n components, n magnitude words; zero between calls
         ctx->tri_facc.resize(4 * (size_t)n);
@@ -267,16 +422,22 @@ void launch_triplets(pg_context* ctx, int precision, int flags, bool first_f, Fx
     A.sep0 = ctx->nb_sep0.p;
     A.disp = ctx->disp32.p;
     A.nrec = ctx->n_tri;
+    A.nqrec = ctx->n_quad;
     A.facc = ctx->tri_facc.p;
     A.acc = (flags & (PG_WANT_ENERGY | PG_WANT_FORCES)) ? acc : nullptr;
     A.skip = skip;
     const int blocks = (int)(((long long)n * 32 + TT - 1) / TT);
+    const bool quad = ctx->n_quad > 0;
     if (precision == PG_PREC_FP64) {
         A.rec = ctx->d_tri.p;
-        tri_kernel<double><<<blocks, TT, 0, st>>>(A);
+        A.qrec = ctx->d_quad.p;
+        if (quad) tri_kernel<double, true><<<blocks, TT, 0, st>>>(A);
+        else tri_kernel<double, false><<<blocks, TT, 0, st>>>(A);
     } else {
         A.rec = ctx->d_tri32.p;
-        tri_kernel<float><<<blocks, TT, 0, st>>>(A);
+        A.qrec = ctx->d_quad32.p;
+        if (quad) tri_kernel<float, true><<<blocks, TT, 0, st>>>(A);
+        else tri_kernel<float, false><<<blocks, TT, 0, st>>>(A);
     }
     if (flags & PG_WANT_FORCES) {
         tri_forces<<<(3 * n + 255) / 256, 256, 0, st>>>(n, ctx->tri_facc.p, ctx->out_f.p, first_f ? 1 : 0, skip);

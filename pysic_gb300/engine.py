@@ -70,6 +70,9 @@ class Engine:
             self.ctx, len(a["tri_kind"]), L.iptr(a["tri_kind"]), L.dptr(a["tri_params"]), L.dptr(a["tri_cutoff"]),
             L.dptr(a["tri_soft"]), L.u64ptr(a["tri_mask1"]), L.u64ptr(a["tri_mask2"]), L.u64ptr(a["tri_mask3"]),
             L.u64ptr(a["tri_center"])))
+        L.check(self.lib.pg_set_quad_potentials(
+            self.ctx, len(a["quad_kind"]), L.iptr(a["quad_kind"]), L.dptr(a["quad_params"]),
+            L.dptr(a["quad_cutoff"]), L.dptr(a["quad_soft"]), L.u64ptr(a["quad_mask"]), L.u64ptr(a["quad_orig"])))
         npair = len(a["pair_kind"])
         L.check(self.lib.pg_set_pair_potentials(
             self.ctx, model.n_types, npair, L.iptr(a["pair_kind"]), L.dptr(a["pair_params"]),

@@ -83,6 +83,15 @@ class Model:
         self.tri_mask2 = []
         self.tri_mask3 = []
         self.tri_center = []  # types whose element is the tuple's middle one (original_elements(2))
+        # four-body potentials (dihedral), one record per distinct permutation of
+        # each target tuple: masks of positions 1-4 of the permuted record and of
+        # the unpermuted tuple
+        self.quad_kind = []
+        self.quad_params = []
+        self.quad_cutoff = []
+        self.quad_soft = []
+        self.quad_mask = []
+        self.quad_orig = []
         self.n_groups = 0
         self.coordinators = []
         self.ewald = None
@@ -130,6 +139,12 @@ class Model:
         d["tri_mask2"] = np.array(self.tri_mask2, dtype=np.uint64)
         d["tri_mask3"] = np.array(self.tri_mask3, dtype=np.uint64)
         d["tri_center"] = np.array(self.tri_center, dtype=np.uint64)
+        d["quad_kind"] = np.array(self.quad_kind, dtype=np.int32)
+        d["quad_params"] = np.array(self.quad_params, dtype=np.float64).reshape(-1, 4)
+        d["quad_cutoff"] = np.array(self.quad_cutoff, dtype=np.float64)
+        d["quad_soft"] = np.array(self.quad_soft, dtype=np.float64)
+        d["quad_mask"] = np.array(self.quad_mask, dtype=np.uint64).reshape(-1, 4)
+        d["quad_orig"] = np.array(self.quad_orig, dtype=np.uint64).reshape(-1, 4)
         return d
 
 
@@ -346,6 +361,25 @@ def compile_model(atoms, potentials, coulomb=None):
                     M.tri_mask2.append(_mask(sigs, perm[1], None, None))
                     M.tri_mask3.append(_mask(sigs, perm[2], None, None))
                     M.tri_center.append(centre)
+        elif nt == 4:
+            if kind not in core.QUAD_KIND:
+                raise InvalidPotentialError("'{0}' is not a four-body potential of the GB300 engine".format(kind))
+            if grp >= 0:
+                raise InvalidPotentialError("bond-order scaling of four-body potentials is not evaluated by the "
+                                            "GB300 engine")
+            if pot.get_tags() or pot.get_indices():
+                raise InvalidPotentialError("four-body potentials are evaluated for element targets only")
+            # create_potential keeps the unpermuted tuple (original_elements), which the
+            # dihedral evaluator matches forwards or backwards (Potentials.f90:3380-3611)
+            for t in pot.get_symbols() or []:
+                orig = [_mask(sigs, e, None, None) for e in t]
+                for perm in _distinct_permutations(t):
+                    M.quad_kind.append(core.QUAD_KIND[kind])
+                    M.quad_params.append((params + [0.0] * 4)[:4])
+                    M.quad_cutoff.append(float(pot.get_cutoff()))
+                    M.quad_soft.append(float(pot.get_soft_cutoff()))
+                    M.quad_mask.append([_mask(sigs, e, None, None) for e in perm])
+                    M.quad_orig.append(orig)
         else:
             raise InvalidPotentialError("{0}-body potentials are not evaluated by the GB300 engine".format(nt))
 

@@ -331,6 +331,9 @@ class PysicInterface:
                 if kind not in core.TRIPLET_KIND:
                     raise core.InvalidPotentialError("'{0}' is not a three-body potential of the GB300 engine"
                                                      .format(kind))
+                if grp >= 0:
+                    raise core.InvalidPotentialError("bond-order scaling of three-body potentials is not evaluated "
+                                                     "by the GB300 engine")
                 M.tri_kind.append(core.TRIPLET_KIND[kind])
                 M.tri_params.append((params + [0.0] * 4)[:4])
                 M.tri_cutoff.append(rec["cutoff"])
@@ -339,6 +342,19 @@ class PysicInterface:
                 M.tri_mask2.append(mask(target(rec, 1)))
                 M.tri_mask3.append(mask(target(rec, 2)))
                 M.tri_center.append(mask(target(rec, 1, orig=True)))
+            elif nt == 4:
+                if kind not in core.QUAD_KIND:
+                    raise core.InvalidPotentialError("'{0}' is not a four-body potential of the GB300 engine"
+                                                     .format(kind))
+                if grp >= 0:
+                    raise core.InvalidPotentialError("bond-order scaling of four-body potentials is not evaluated "
+                                                     "by the GB300 engine")
+                M.quad_kind.append(core.QUAD_KIND[kind])
+                M.quad_params.append((params + [0.0] * 4)[:4])
+                M.quad_cutoff.append(rec["cutoff"])
+                M.quad_soft.append(rec["soft"])
+                M.quad_mask.append([mask(target(rec, t)) for t in range(4)])
+                M.quad_orig.append([mask(target(rec, t, orig=True)) for t in range(4)])
             else:
                 raise core.InvalidPotentialError("{0}-body potentials are not evaluated by the GB300 engine".format(nt))
         for rec in bonds:

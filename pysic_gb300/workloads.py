@@ -241,3 +241,22 @@ def product_cases():
                               P("power", symbols=[["Si", "Si"]], parameters=[0.8, 2.0, 3.0])])
     yield "comb_repulsion", a2, [prod2, prod3, P("exponential", symbols=[["O", "O"]], parameters=[10.0, 2.0],
                                                    cutoff=2.8, cutoff_margin=0.4)]
+
+
+def dihedral_cases():
+    """Structures with four-body dihedral terms (Potentials.f90:3329-3611):
+    a single-element chain network (a distorted diamond crystal, every
+    permutation of the one-element tuple the same record) and a two-element
+    random box with an unsymmetric target tuple (several distinct
+    permutations, the forward / backward element match) next to a bond_bend
+    and a pair term, both with smooth cutoffs."""
+    P = Potential
+    a1 = diamond_si(2, noise=0.12, seed=51)
+    yield "si_dihedral", a1, [P("dihedral", symbols=[["Si", "Si", "Si", "Si"]], parameters=[0.3, 1.1],
+                                 cutoff=2.9, cutoff_margin=0.4)]
+    a2 = sio2_box(10, seed=52)
+    yield "sio_dihedral", a2, [P("dihedral", symbols=[["Si", "O", "O", "Si"], ["O", "Si", "O", "O"]],
+                                  parameters=[0.4, 2.0], cutoff=2.6, cutoff_margin=0.5),
+                               P("bond_bend", symbols=[["O", "Si", "O"]], parameters=[0.2, 1.9, 1, 2], cutoff=2.6,
+                                 cutoff_margin=0.4),
+                               P("exponential", symbols=[["Si", "O"]], parameters=[5.0, 1.5], cutoff=2.6)]

@@ -100,11 +100,24 @@ def test_types_fold_tags_and_indices():
     assert len(M.pair_kind) == 3  # (1,1) once, (0,2) and (2,0)
 
 
-@pytest.mark.parametrize("kind,symbols", [("step", [["Si", "Si"]]), ("dihedral", [["Si", "Si", "Si", "Si"]])])
+@pytest.mark.parametrize("kind,symbols", [("step", [["Si", "Si"]])])
 def test_unsupported_potential_rejected_at_compile(kind, symbols):
     atoms = W.diamond_si(1)
     with pytest.raises(pysic.InvalidPotentialError):
         compile_model(atoms, [pysic.Potential(kind, symbols=symbols, cutoff=3.0)])
+
+
+def test_four_body_records_compile():
+    """dihedral: one record per distinct permutation of each target tuple, the
+    unpermuted tuple kept for the evaluator's forward / backward match; tag
+    targets are refused."""
+    atoms = W.sio2_box(6, seed=1)
+    M = compile_model(atoms, [pysic.Potential("dihedral", symbols=[["Si", "O", "O", "Si"]], parameters=[0.5, 1.2],
+                                              cutoff=3.0)])
+    assert len(M.quad_kind) == 6  # 4! / (2! 2!)
+    assert all(list(o) == list(M.quad_orig[0]) for o in M.quad_orig)
+    with pytest.raises(pysic.InvalidPotentialError):
+        compile_model(atoms, [pysic.Potential("dihedral", tags=[[0, 0, 0, 0]], parameters=[0.5, 1.2], cutoff=3.0)])
 
 
 def test_new_pair_and_single_kinds_compile():

@@ -103,3 +103,11 @@ def test_shim_coordinator_queries():
                                       c, i, o, 0, 4, of_factor=False)
     assert g.shape == (3, n)
     np.testing.assert_allclose(g.T, rg, rtol=1e-10, atol=1e-12)
+
+
+@pytest.mark.parametrize("precision", [pf_shim.PREC_FP64, pf_shim.PREC_MIXED])
+def test_shim_dihedral_and_bend(precision):
+    """Four-body records through add_potential (four-element targets and
+    originals, as calculator.py passes them) with bond_bend and a pair term."""
+    _, atoms, pots = list(W.dihedral_cases())[1]
+    _check(atoms, pots, precision=precision)

@@ -584,3 +584,39 @@ def test_oracle_product_derivatives(case):
             q1[a] += h
             q2[a] -= h
             assert chi[a] == pytest.approx(-(ev(pos, q1, "energy") - ev(pos, q2, "energy")) / (2 * h), abs=1e-6)
+
+
+@pytest.mark.parametrize("case", [c[0] for c in W.dihedral_cases()])
+def test_oracle_dihedral_forces_and_stress(case):
+    """dihedral in the oracle (Potentials.f90:3329-3611 evaluated on the
+    chains of Core.f90:3540-3943): forces minus the position gradient of the
+    energy, the virial the strain derivative, by finite differences."""
+    _, atoms, pots = next(c for c in W.dihedral_cases() if c[0] == case)
+    model = compile_model(atoms, pots)
+    lists = oracle_lists(atoms, pots, skin=1.0)
+    pos = atoms.get_positions()
+
+    def energy(p, cell=None):
+        return oracle.evaluate(p, atoms.get_initial_charges(), atoms.get_cell() if cell is None else cell,
+                               atoms.get_pbc(), model, *lists, what="energy")
+
+    e0 = energy(pos)
+    f, st = oracle.evaluate(pos, atoms.get_initial_charges(), atoms.get_cell(), atoms.get_pbc(), model, *lists,
+                            what="forces")
+    assert np.abs(f).max() > 1e-3
+    h = 1e-6
+    for a in (0, 3, 11, 20):
+        for c in range(3):
+            p1, p2 = pos.copy(), pos.copy()
+            p1[a, c] += h
+            p2[a, c] -= h
+            assert f[a, c] == pytest.approx(-(energy(p1) - energy(p2)) / (2 * h), abs=1e-6 * max(1, abs(f).max()))
+    # virial sum(r_a F_b): minus the energy's derivative with respect to a homogeneous strain
+    cell = np.asarray(atoms.get_cell())
+    for (a, b), k in (((0, 0), 0), ((1, 1), 1), ((2, 2), 2)):
+        eps = np.eye(3)
+        eps[a, b] += h
+        em = np.eye(3)
+        em[a, b] -= h
+        de = (energy(pos @ eps.T, cell @ eps.T) - energy(pos @ em.T, cell @ em.T)) / (2 * h)
+        assert st[k] == pytest.approx(-de, abs=1e-6 * max(1.0, abs(e0)))

@@ -36,6 +36,8 @@ def _cases():
     yield "tags_indices", a, [pysic.Potential("LJ", tags=[[0, 1]], parameters=[0.01, 3.0], cutoff=5.0),
                              pysic.Potential("LJ", indices=[[2, 7]], parameters=[0.02, 2.5], cutoff=5.0),
                              pysic.Potential("LJ", symbols=[["X", "X"]], parameters=[0.005, 3.2], cutoff=5.0)], None
+    _, a, pots = list(W.dihedral_cases())[1]
+    yield "dihedral_bend", a, pots, None
 
 
 def _pair_rows(a):
