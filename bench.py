@@ -668,8 +668,9 @@ def _build_batch(precision, systems=512):
 
 
 def batch_measure(precision, steps, warmup):
-    """512 uneven silicon boxes (Tersoff + LJ): one launch per kernel for all
-    systems (graph replay) against one evaluation per system.  Device-timed
+    """512 uneven silicon boxes (Tersoff + LJ): one persistent launch for all
+    systems (graph replay) against one launch per phase and one evaluation per
+    system.  Device-timed
     ms per evaluation of all systems (L2 flushed before each), wall-clock
     comparison with per-system evaluation, and the FP64 kernels."""
     batch, n_atoms = _build_batch(precision)
@@ -678,16 +679,16 @@ def batch_measure(precision, steps, warmup):
     flush = torch.empty(64 * 1024 * 1024, dtype=torch.float32, device="cuda")
     stream = torch.cuda.ExternalStream(batch.stream_handle())
 
-    def timed(prec, k_steps):
+    def timed(prec, k_steps, mode="batched"):
         for _ in range(warmup):
-            batch.evaluate(prec)
+            batch.evaluate(prec, mode=mode)
         batch.synchronize()
         ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(k_steps)]
         for k in range(k_steps):
             with torch.cuda.stream(stream):
                 flush.fill_(float(k))
                 ev[k][0].record(stream)
-            batch.evaluate(prec)
+            batch.evaluate(prec, mode=mode)
             with torch.cuda.stream(stream):
                 ev[k][1].record(stream)
         batch.synchronize()
@@ -713,8 +714,11 @@ def batch_measure(precision, steps, warmup):
     wall_each = wall("each")
     launches_each = batch.launch_count()
     wall_batched = wall("batched")
+    t_phases = timed(precision, steps, "phases")
+    launches_phases = batch.launch_count()
     t64 = timed("fp64", max(5, steps // 4))
-    pl, bl = batch.get_lanes(precision)
+    pl, bl, cells = batch.get_tiles(precision)
+    ppl, pbl, _ = batch.get_tiles(precision, "phases")
     out = {"systems": 512, "atoms": n_atoms, "precision": precision, "ms_per_step": ms,
            "atom_steps_per_s": n_atoms / (ms / 1e3), "systems_per_s": 512 / (ms / 1e3),
            "launches_per_step": launches, "batched_wall_ms_per_step": 1e3 * wall_batched,
@@ -723,7 +727,13 @@ def batch_measure(precision, steps, warmup):
                           "note": "every system evaluated on its own: its own captured graph on its own stream"},
            "batched_vs_per_system_wall": wall_each / wall_batched,
            "fp64": {"atom_steps_per_s": n_atoms / (statistics.mean(t64) / 1e3), "ms_per_step": statistics.mean(t64)},
-           "tiles": {"pair_lanes": pl, "bond_lanes": bl}, "clocks": clocks,
+           "phase_launches": {"ms_per_step": statistics.mean(t_phases), "launches_per_step": launches_phases,
+                              "tiles": {"pair_lanes": ppl, "bond_lanes": pbl},
+                              "note": "the same tiles with one launch per phase (displacement, pair, bond, gather)"},
+           "tiles": {"pair_lanes": pl, "bond_lanes": bl, "cells_per_tile": cells,
+                     "note": "one persistent launch; chosen by the batch's autotuner over pair lanes {8, 16} x bond "
+                             "lanes {4, 8, triplet tile} x cells per tile {1, 2, 4}"},
+           "clocks": clocks,
            "structure": "Si boxes, atom counts log-uniform in [64, 2048], 2.33 g/cm^3, random with rejection below "
                         "2.0 A; Tersoff + LJ (0.01 eV, 2.1 A, cutoff 5)",
            "l2": "flushed before every step (256 MB write)"}
@@ -812,11 +822,15 @@ def run_profile(args):
     if args.workload == "batched_si_512":
         # the batched launches only: set-up, then `--steps` evaluations of all 512 systems
         batch, n_atoms = _build_batch(args.precision, args.systems)
+        if args.bond_lanes:  # fixed tiles: no autotuner launches
+            batch.set_lanes(args.lanes, args.bond_lanes)
+            batch.set_tile_blocks(args.cells)
         for _ in range(args.steps):
-            batch.evaluate(args.precision)
+            batch.evaluate(args.precision, mode=args.batch_mode)
         batch.synchronize()
         print(json.dumps({"profile_run": args.workload, "precision": args.precision, "systems": args.systems,
-                          "atoms": n_atoms}))
+                          "atoms": n_atoms, "mode": args.batch_mode, "tiles": batch.get_tiles(args.precision,
+                                                                                             args.batch_mode)}))
         return
     atoms, calc, _ = setup(args.workload, args.precision, 0)
     eng = calc.engine
@@ -834,6 +848,11 @@ def main():
     p.add_argument("--profile", action="store_true", help="short fixed run for ncu captures")
     p.add_argument("--lanes", type=int, default=8, help="lanes per atom in --profile mode")
     p.add_argument("--systems", type=int, default=512, help="systems of the many-system workload in --profile mode")
+    p.add_argument("--bond-lanes", type=int, default=0,
+                   help="--profile of the many-system workload: bond lanes (with --lanes as pair lanes; 0: autotune)")
+    p.add_argument("--cells", type=int, default=1, help="--profile of the many-system workload: cells per tile")
+    p.add_argument("--batch-mode", default="batched", choices=("batched", "phases"),
+                   help="--profile of the many-system workload: one persistent launch or one launch per phase")
     p.add_argument("--gpus", type=int, default=1)
     p.add_argument("--steps", type=int, default=100)
     p.add_argument("--warmup", type=int, default=5)

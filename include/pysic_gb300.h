@@ -370,17 +370,36 @@ int pg_mlp_predict_charges(pg_mlp* mlp, pg_context* ctx, int32_t n_gauss, double
 /* ---- many independent systems ------------------------------------------------
  * No counterpart in the reference, which holds one system per process.  A batch
  * borrows fully set-up contexts (same device; pair and bond-order terms, no
- * Ewald) and evaluates them all with one launch per kernel over a tile list
- * (system, block), replayed from a CUDA graph (mode 0), or each on its own
- * (mode 1, one pg_device_evaluate per context).  Results stay in each context:
- * read them with pg_device_results after pg_batch_synchronize.  Lanes per atom
- * of the pair and bond-order kernels: 0 lets the batch time the candidates. */
+ * Ewald) and evaluates them all
+ *   mode 0: in ONE persistent launch, replayed from a CUDA graph: resident
+ *           blocks take (phase, system, cells) tiles in dependency order
+ *           (displacements, pair terms, bond pass, gather) with bounded
+ *           per-system waits; a wait that runs out makes pg_batch_synchronize
+ *           return PG_ERR_TIMEOUT;
+ *   mode 1: each on its own (one pg_device_evaluate per context);
+ *   mode 2: with one launch per phase over the tile list of all systems.
+ * Results stay in each context: read them with pg_device_results after
+ * pg_batch_synchronize.  Tiles -- lanes per atom of the pair body (8 or 16 in
+ * mode 0; 8, 16 or 32 in mode 2), of the bond-order body (4, 8, or
+ * PG_LANES_TRIPLET) and, in mode 0, the cells of 128 threads' atoms that one
+ * ticket hands a block (1..64) -- are timed on the batch itself when left 0;
+ * pg_batch_get_tiles reports the ones in use. */
 int pg_batch_create(pg_batch** batch, int32_t device);
 int pg_batch_destroy(pg_batch* batch);
 int pg_batch_add(pg_batch* batch, pg_context* ctx);
 int pg_batch_set_lanes(pg_batch* batch, int32_t pair_lanes, int32_t bond_lanes);
 int pg_batch_get_lanes(pg_batch* batch, int32_t precision, int32_t* pair_lanes, int32_t* bond_lanes);
+int pg_batch_set_tile_blocks(pg_batch* batch, int32_t blocks);
+int pg_batch_get_tiles(pg_batch* batch, int32_t precision, int32_t mode, int32_t* pair_lanes, int32_t* bond_lanes,
+                       int32_t* blocks);
 int pg_batch_evaluate(pg_batch* batch, int32_t precision, int32_t flags, int32_t mode);
+/* Test of the persistent launch's bounded waits: from the next mode-0
+ * evaluation on, the pair and bond tiles of `system` wait for a displacement
+ * tile that never comes, so every such wait runs out after wait_seconds (at
+ * most 1 s) and pg_batch_synchronize returns PG_ERR_TIMEOUT; the kernel ends
+ * normally and the context stays usable.  system = -1 ends the test (the wait
+ * limit stays as given; the default is 0.5 s). */
+int pg_batch_test_stall(pg_batch* batch, int32_t system, double wait_seconds);
 int pg_batch_synchronize(pg_batch* batch);
 int pg_batch_get_stream(pg_batch* batch, void** stream);
 int pg_batch_last_launch_count(pg_batch* batch, int32_t* launches);

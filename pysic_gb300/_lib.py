@@ -114,6 +114,9 @@ _SIGNATURES = {
     "pg_batch_add": (ctypes.c_int, [ctypes.c_void_p, _ctx]),
     "pg_batch_set_lanes": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int32, ctypes.c_int32]),
     "pg_batch_get_lanes": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int32, _c_int_p, _c_int_p]),
+    "pg_batch_set_tile_blocks": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int32]),
+    "pg_batch_get_tiles": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int32, ctypes.c_int32, _c_int_p, _c_int_p, _c_int_p]),
+    "pg_batch_test_stall": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int32, ctypes.c_double]),
     "pg_batch_evaluate": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int32, ctypes.c_int32, ctypes.c_int32]),
     "pg_batch_synchronize": (ctypes.c_int, [ctypes.c_void_p]),
     "pg_batch_get_stream": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(ctypes.c_void_p)]),

@@ -1165,6 +1165,33 @@ int pg_batch_get_lanes(pg_batch* batch, int32_t precision, int32_t* pair_lanes, 
     });
 }
 
+int pg_batch_set_tile_blocks(pg_batch* batch, int32_t blocks) {
+    return guarded([&] {
+        check_batch(batch);
+        pg::batch_set_tile_blocks(batch, blocks);
+    });
+}
+
+int pg_batch_test_stall(pg_batch* batch, int32_t system, double wait_seconds) {
+    return guarded([&] {
+        check_batch(batch);
+        pg::batch_test_stall(batch, system, wait_seconds);
+    });
+}
+
+int pg_batch_get_tiles(pg_batch* batch, int32_t precision, int32_t mode, int32_t* pair_lanes, int32_t* bond_lanes,
+                       int32_t* blocks) {
+    return guarded([&] {
+        check_batch(batch);
+        pg::require(pair_lanes && bond_lanes && blocks, PG_ERR_INVALID, "null output");
+        int p = 0, q = 0, c = 0;
+        pg::batch_get_tiles(batch, precision, mode, &p, &q, &c);
+        *pair_lanes = p;
+        *bond_lanes = q;
+        *blocks = c;
+    });
+}
+
 int pg_batch_evaluate(pg_batch* batch, int32_t precision, int32_t flags, int32_t mode) {
     return guarded([&] {
         check_batch(batch);

@@ -592,6 +592,9 @@ void batch_destroy(pg_batch* b);
 void batch_add(pg_batch* b, pg_context* c);
 void batch_set_lanes(pg_batch* b, int pair_lanes, int bond_lanes);
 void batch_get_lanes(pg_batch* b, int precision, int* pair_lanes, int* bond_lanes);
+void batch_set_tile_blocks(pg_batch* b, int blocks);
+void batch_test_stall(pg_batch* b, int system, double wait_seconds);
+void batch_get_tiles(pg_batch* b, int precision, int mode, int* pair_lanes, int* bond_lanes, int* blocks);
 void batch_evaluate(pg_batch* b, int precision, int flags, int mode);
 void batch_synchronize(pg_batch* b);
 int batch_launches(const pg_batch* b);

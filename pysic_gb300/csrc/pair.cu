@@ -18,381 +18,10 @@
 #include "kernels.cuh"
 #include "pairvec.cuh"
 #include "atomfactor.cuh"
+#include "pair_body.cuh"
 
 namespace pg {
 
-
-__device__ __forceinline__ double powi_(double x, int n) {
-    double r = 1.0;
-    for (int k = 0; k < n; ++k) r *= x;
-    return r;
-}
-
-// One factor of a product of potentials for the pair (i, j): its value V, dV/dr
-// and its electronegativity of atom i (-dV/dq_i), without any cut factor
-// (evaluate_energy_component / _force_component /
-// _electronegativity_component, Potentials.f90:2512-2890).  first: i is the
-// pair's atom1 as the reference's loop picks it; charge-dependent factors take
-// the parameters of the product's first target on atom1 when its type is that
-// target's, as their plain records do below.
-template <typename R>
-__device__ __forceinline__ void factor_raw(const PairT<R>& P, const PairArgs& A, R r, R qi, R qj, bool first, int ti,
-                                           int tj, R& V, R& dV, R& en) {
-    en = R(0);
-    if (P.kind < 7) {
-        pair_eval<R>(P, r, V, dV, (const R*)A.tab);
-        return;
-    }
-    dV = R(0);
-    const R q1 = first ? qi : qj, q2 = first ? qj : qi;
-    const bool direct = (P.first >> (first ? ti : tj)) & 1ull;
-    if (P.kind == 7) {  // charge_pair
-        const int n1 = direct ? (int)P.p1 : (int)P.p2, n2 = direct ? (int)P.p2 : (int)P.p1;
-        V = P.p0 * (ipow(q1, n1) * ipow(q2, n2));
-        const int nm = first ? n1 : n2;
-        if (nm > 0)
-            en = -(first ? P.p0 * (R(n1) * ipow(q1, n1 - 1) * ipow(q2, n2))
-                         : P.p0 * (R(n2) * ipow(q1, n1) * ipow(q2, n2 - 1)));
-    } else if (P.kind == 8) {  // charge_exp
-        const R* c = (const R*)A.tab + 2 * (long long)P.t0;
-        const int a1 = direct ? 0 : 4, a2 = direct ? 4 : 0;
-        const R eta1 = c[direct ? 11 : 12], eta2 = c[direct ? 12 : 11];
-        const R beta1 = c[direct ? 13 : 14], beta2 = c[direct ? 14 : 13];
-        const R xi1 = c[direct ? 9 : 10], xi2 = c[direct ? 10 : 9];
-        const R d5 = beta1 * (c[3 + a1] - q1), d6 = beta2 * (c[3 + a2] - q2);
-        const R D1 = c[1 + a1] + pow_(fabs(d5), eta1), D2 = c[1 + a2] + pow_(fabs(d6), eta2);
-        V = c[0] * exp_(R(0.5) * (xi1 * D1 + xi2 * D2));
-        en = first ? V * xi1 * R(0.5) * eta1 * pow_(fabs(d5), eta1 - R(1)) * copysign(R(1), d5) * beta1
-                   : V * xi2 * R(0.5) * eta2 * pow_(fabs(d6), eta2 - R(1)) * copysign(R(1), d6) * beta2;
-    } else {  // charge_abs
-        const R* c = (const R*)A.tab + 2 * (long long)P.t0;
-        const R* s1 = c + (direct ? 0 : 4);
-        const R* s2 = c + (direct ? 4 : 0);
-        const R ab1 = fabs(q1 - s1[2]), ab2 = fabs(q2 - s2[2]);
-        const R pw1 = pow_(ab1, s1[3] - R(1)), pw2 = pow_(ab2, s2[3] - R(1));
-        R f1 = s1[0] + s1[1] * ab1 * pw1, f2 = s2[0] + s2[1] * ab2 * pw2;
-        R is = R(0.5) / sqrt_(f1 * f2);
-        if (f1 < R(0)) {
-            f1 = R(0);
-            is = R(0);
-        }
-        if (f2 < R(0)) {
-            f2 = R(0);
-            is = R(0);
-        }
-        const R e1 = fmax(s1[0] + s1[1] * pow_(ab1, s1[3]), R(0));
-        const R e2 = fmax(s2[0] + s2[1] * pow_(ab2, s2[3]), R(0));
-        V = sqrt_(e1 * e2);
-        en = first ? is * (-s1[3] * pw1 * copysign(R(1), q1 - s1[2]) * s1[1]) * f2
-                   : is * (-s2[3] * pw2 * copysign(R(1), q2 - s2[2]) * s2[1]) * f1;
-    }
-}
-
-// most factors of one product (the record and 8 more)
-constexpr int PG_MAX_FACTORS = 9;
-
-// AF: also add the per-atom factor forces (no scaled pair term; W from af_sum)
-template <typename R, int G, bool AF = false>
-__device__ __forceinline__ void pair_body(const PairArgs& A, int blk) {
-    __shared__ Fx128 wsum[256 / 32][7];
-    __shared__ unsigned done;
-    if (threadIdx.x == 0) done = 0u;
-    __syncthreads();
-    const int lane = threadIdx.x % G;
-    const int slot = threadIdx.x / G;
-    const int i = blk * (blockDim.x / G) + slot;
-    if (A.skip && *A.skip) return;
-    const bool act = i < A.n;
-    R fx = 0, fy = 0, fz = 0, en = 0, chi = 0;
-    R w0 = 0, w1 = 0, w2 = 0, w3 = 0, w4 = 0, w5 = 0;
-    R pre[PG_MAX_AGROUPS] = {};  // per-atom factor groups: this atom's prefactors (half of each pair's V f)
-    const bool wantE = A.flags & PG_WANT_ENERGY, wantF = A.flags & PG_WANT_FORCES, wantC = A.flags & PG_WANT_ENEGS;
-    int ti = 0;
-    R wk[PG_MAX_AGROUPS] = {};
-    if (act) {
-        ti = A.type[i];
-        if constexpr (AF) {
-#pragma unroll
-            for (int g = 0; g < PG_MAX_AGROUPS; ++g)
-                if (g < A.ng) wk[g] = ((const R*)A.afW)[(size_t)g * A.n + i];
-        }
-        const R qi = charge_of<R>(A, i);
-        const R ew_rc = (R)A.ew_rc, ew_is2 = (R)A.ew_is2, ew_k = (R)A.ew_k, ew_c2 = (R)A.ew_c2,
-                ew_isq2 = (R)A.ew_isq2;
-        double xi = 0, yi = 0, zi = 0;
-        if constexpr (sizeof(R) == 8) {
-            xi = A.pos[3 * i];
-            yi = A.pos[3 * i + 1];
-            zi = A.pos[3 * i + 2];
-        }
-        const int e1 = A.start[i + 1];
-        for (int e = A.start[i] + lane; e < e1; e += G) {
-            const int j = A.idx[e];
-            R x, y, z;
-            pair_vector<R>(A, i, e, xi, yi, zi, x, y, z);
-            const R r = sqrt_(x * x + y * y + z * z);
-            if (r == R(0)) continue;
-            const R ir = R(1) / r;
-            R U = 0, dU = 0;
-            if (A.ewald && r < ew_rc) {
-                const R qj = charge_of<R>(A, j);
-                const R qq = qi * qj;
-                const R ec = erfc_(r * ew_is2);
-                U += ew_k * qq * ec * ir;
-                if (wantF) dU -= ew_k * qq * (ec * ir * ir + ew_c2 * exp_(-r * r * ew_isq2) * ir);
-                if (wantC) chi -= qj * ew_k * ec * ir;
-            }
-            const int tj = A.type[j];
-            // charge-independent pair terms have zero electronegativity
-            const int2 ix = (wantE || wantF || (wantC && A.qpair)) ? A.index[ti * A.T + tj] : make_int2(0, 0);
-            for (int t = ix.x; t < ix.x + ix.y; ++t) {
-                const PairT<R> P = ((const PairT<R>*)A.terms)[t];
-                if (P.in_bond_kernel || !(r < P.rc)) continue;
-                if (P.nmul > 0) {
-                    // a product of potentials: V = prod V_k, V' and the electronegativity by
-                    // the product rule (each factor's with the product of the others),
-                    // then the record's smooth cut (Potentials.f90:2512-2700)
-                    const bool first = pick(i, j, A.off[3 * e], A.off[3 * e + 1], A.off[3 * e + 2]);
-                    const R qj = charge_of<R>(A, j);
-                    const PairT<R>* TT = (const PairT<R>*)A.terms;
-                    const int nf = P.nmul + 1;
-                    R ek[PG_MAX_FACTORS], dk[PG_MAX_FACTORS], nk[PG_MAX_FACTORS];
-#pragma unroll
-                    for (int k = 0; k < PG_MAX_FACTORS; ++k) {
-                        ek[k] = R(1);
-                        dk[k] = nk[k] = R(0);
-                        if (k < nf) factor_raw<R>(k == 0 ? P : TT[P.mul0 + k - 1], A, r, qi, qj, first, ti, tj, ek[k],
-                                                  dk[k], nk[k]);
-                    }
-                    R V = R(1), dV = R(0), en = R(0);
-#pragma unroll
-                    for (int k = 0; k < PG_MAX_FACTORS; ++k) V *= ek[k];
-#pragma unroll
-                    for (int k = 0; k < PG_MAX_FACTORS; ++k) {
-                        R w = R(1);
-#pragma unroll
-                        for (int q = 0; q < PG_MAX_FACTORS; ++q)
-                            if (q != k) w *= ek[q];
-                        dV += w * dk[k];
-                        en += w * nk[k];
-                    }
-                    R f = R(1), fp = R(0);
-                    if (P.smooth) smooth<R>(r, P.rc, P.rs, f, fp);
-                    U += V * f;
-                    dU += dV * f + V * fp;
-                    if (wantC) chi += en * f;
-                    continue;
-                }
-                if (P.kind == 7) {
-                    // charge_pair: eps q1^n1 q2^n2 of the pair's (atom1, atom2) as the
-                    // reference's loop picks them; the exponents follow the unpermuted
-                    // first target (evaluate_energy/electronegativity_charge_pair,
-                    // Potentials.f90:4415-4513).  No r dependence but the smooth cutoff.
-                    const bool first = pick(i, j, A.off[3 * e], A.off[3 * e + 1], A.off[3 * e + 2]);
-                    const R qj = charge_of<R>(A, j);
-                    const R q1 = first ? qi : qj, q2 = first ? qj : qi;
-                    const bool direct = (P.first >> (first ? ti : tj)) & 1ull;
-                    const int n1 = direct ? (int)P.p1 : (int)P.p2, n2 = direct ? (int)P.p2 : (int)P.p1;
-                    R f = R(1), fp = R(0);
-                    if (P.smooth) smooth<R>(r, P.rc, P.rs, f, fp);
-                    const R v = P.p0 * (ipow(q1, n1) * ipow(q2, n2));
-                    U += v * f;
-                    dU += v * fp;
-                    if (wantC) {
-                        const int nm = first ? n1 : n2;  // the exponent of this atom's charge
-                        if (nm > 0)
-                            chi -= (first ? P.p0 * (R(n1) * ipow(q1, n1 - 1) * ipow(q2, n2))
-                                          : P.p0 * (R(n2) * ipow(q1, n1) * ipow(q2, n2 - 1))) * f;
-                    }
-                    continue;
-                }
-                if (P.kind == 8) {
-                    // charge_exp, V = eps exp((xi_1 D_1(q_1) + xi_2 D_2(q_2))/2),
-                    // D(q) = Rmax + |beta (Qmax - q)|^eta, with the parameters of the
-                    // unpermuted first target on the pair's atom1 when its type is that
-                    // target's (Potentials.f90:3691-3903; no r dependence but the cut)
-                    const R* c = (const R*)A.tab + 2 * (long long)P.t0;
-                    const bool first = pick(i, j, A.off[3 * e], A.off[3 * e + 1], A.off[3 * e + 2]);
-                    const R qj = charge_of<R>(A, j);
-                    const R q1 = first ? qi : qj, q2 = first ? qj : qi;
-                    const bool direct = (P.first >> (first ? ti : tj)) & 1ull;
-                    const int a1 = direct ? 0 : 4, a2 = direct ? 4 : 0;  // Rmax at 1 + a, Qmax at 3 + a
-                    const R eta1 = c[direct ? 11 : 12], eta2 = c[direct ? 12 : 11];
-                    const R beta1 = c[direct ? 13 : 14], beta2 = c[direct ? 14 : 13];
-                    const R xi1 = c[direct ? 9 : 10], xi2 = c[direct ? 10 : 9];
-                    const R d5 = beta1 * (c[3 + a1] - q1), d6 = beta2 * (c[3 + a2] - q2);
-                    const R D1 = c[1 + a1] + pow_(fabs(d5), eta1), D2 = c[1 + a2] + pow_(fabs(d6), eta2);
-                    R f = R(1), fp = R(0);
-                    if (P.smooth) smooth<R>(r, P.rc, P.rs, f, fp);
-                    const R v = c[0] * exp_(R(0.5) * (xi1 * D1 + xi2 * D2));
-                    U += v * f;
-                    dU += v * fp;
-                    if (wantC) {
-                        chi += first ? v * xi1 * R(0.5) * eta1 * pow_(fabs(d5), eta1 - R(1)) * copysign(R(1), d5) * beta1 * f
-                                     : v * xi2 * R(0.5) * eta2 * pow_(fabs(d6), eta2 - R(1)) * copysign(R(1), d6) * beta2 * f;
-                    }
-                    continue;
-                }
-                if (P.kind == 9) {
-                    // charge_abs, V = sqrt(f_1(q_1) f_2(q_2)), f(q) = a + b |q - Q|^n, f < 0
-                    // taken as 0, parameters (a, b, Q, n) of the unpermuted first target on
-                    // atom1 when its type is that target's (Potentials.f90:4525-4728); no
-                    // r dependence but the cut
-                    const R* c = (const R*)A.tab + 2 * (long long)P.t0;
-                    const bool first = pick(i, j, A.off[3 * e], A.off[3 * e + 1], A.off[3 * e + 2]);
-                    const R qj = charge_of<R>(A, j);
-                    const R q1 = first ? qi : qj, q2 = first ? qj : qi;
-                    const bool direct = (P.first >> (first ? ti : tj)) & 1ull;
-                    const R* s1 = c + (direct ? 0 : 4);
-                    const R* s2 = c + (direct ? 4 : 0);
-                    const R ab1 = fabs(q1 - s1[2]), ab2 = fabs(q2 - s2[2]);
-                    const R pw1 = pow_(ab1, s1[3] - R(1)), pw2 = pow_(ab2, s2[3] - R(1));
-                    R f1 = s1[0] + s1[1] * ab1 * pw1, f2 = s2[0] + s2[1] * ab2 * pw2;
-                    R is = R(0.5) / sqrt_(f1 * f2);
-                    if (f1 < R(0)) {
-                        f1 = R(0);
-                        is = R(0);
-                    }
-                    if (f2 < R(0)) {
-                        f2 = R(0);
-                        is = R(0);
-                    }
-                    R f = R(1), fp = R(0);
-                    if (P.smooth) smooth<R>(r, P.rc, P.rs, f, fp);
-                    // the energy routine takes |q - Q|^n directly
-                    const R e1 = fmax(s1[0] + s1[1] * pow_(ab1, s1[3]), R(0));
-                    const R e2 = fmax(s2[0] + s2[1] * pow_(ab2, s2[3]), R(0));
-                    const R v = sqrt_(e1 * e2);
-                    U += v * f;
-                    dU += v * fp;
-                    if (wantC) {
-                        chi += first ? is * (-s1[3] * pw1 * copysign(R(1), q1 - s1[2]) * s1[1]) * f2 * f
-                                     : is * (-s2[3] * pw2 * copysign(R(1), q2 - s2[2]) * s2[1]) * f1 * f;
-                    }
-                    continue;
-                }
-                if (!(wantE || wantF)) continue;
-                R V, dV;
-                pair_term<R>(P, r, V, dV, (const R*)A.tab);
-                if (P.agroup >= 0) {
-                    // scaled by the pair's mean per-atom factor (B_i + B_j)/2
-                    // (Core.f90:4345-4350, 5553-5560); half of V f is each atom's
-                    // prefactor of the gradient of its factor (5486-5491)
-                    const R* B = (const R*)A.afB + (size_t)P.agroup * A.n;
-                    const R bm = R(0.5) * (B[i] + B[j]);
-#pragma unroll
-                    for (int q = 0; q < PG_MAX_AGROUPS; ++q)
-                        if (q == P.agroup) pre[q] += R(0.5) * V;
-                    V *= bm;
-                    dV *= bm;
-                }
-                U += V;
-                dU += dV;
-            }
-            en += R(0.5) * U;
-            // force on i: U'(r) r_hat; half of the pair virial sep (x) F_j, F_j = -U' r_hat
-            R c = dU * ir;
-            R h = R(-0.5) * c;
-            if constexpr (AF) {
-                if (wantF) {
-                    R cf, hv;
-                    af_entry<R>(A, wk, ti, j, tj, r, ir, cf, hv);
-                    c += cf;
-                    h += hv;
-                }
-            }
-            fx += c * x;
-            fy += c * y;
-            fz += c * z;
-            w0 += h * x * x;
-            w1 += h * y * y;
-            w2 += h * z * z;
-            w3 += h * y * z;
-            w4 += h * x * z;
-            w5 += h * x * y;
-        }
-    }
-    // single-atom terms in FP64, added by the group's lane 0
-    // (core_evaluate_local_singlet, Core.f90:4095-4239): charge_self eps q^n with
-    // chi = -eps n q^(n-1) (Potentials.f90:4341-4375), constant V (3959-3966),
-    // constant force F with energy -F . r at the absolute position (3122-3147);
-    // singlets add nothing to the virial
-    // With a per-atom factor (constant and force only) the energy is V B_i and the
-    // term's own force gives way to -V grad B_i (V joins the prefactor).
-    double cs = 0.0, es = 0.0, sf0 = 0.0, sf1 = 0.0, sf2 = 0.0;
-    double spre[PG_MAX_AGROUPS] = {};
-    if (act && lane == 0) {
-        const int2 sx = A.sindex[ti];
-        for (int t = sx.x; t < sx.x + sx.y; ++t) {
-            const SingleTerm S = A.sterms[t];
-            if (S.kind == 0) {
-                const double qd = A.charge[i];
-                es += S.p[0] * powi_(qd, S.n);
-                cs += -(S.p[0] * S.n * powi_(qd, S.n - 1));
-            } else {
-                const double V =
-                    S.kind == 1 ? S.p[0] : -(S.p[0] * A.pos[3 * i] + S.p[1] * A.pos[3 * i + 1] + S.p[2] * A.pos[3 * i + 2]);
-                if (S.agroup >= 0) {
-                    if (wantE || wantF) es += V * (double)((const R*)A.afB)[(size_t)S.agroup * A.n + i];
-#pragma unroll
-                    for (int q = 0; q < PG_MAX_AGROUPS; ++q)
-                        if (q == S.agroup) spre[q] += V;
-                } else {
-                    es += V;
-                    if (S.kind == 2) {
-                        sf0 += S.p[0];
-                        sf1 += S.p[1];
-                        sf2 += S.p[2];
-                    }
-                }
-            }
-        }
-    }
-    // W_i = dB/dsum times the prefactor, for the per-atom factor forces
-    if (wantF && A.ng > 0 && !AF) {
-#pragma unroll
-        for (int q = 0; q < PG_MAX_AGROUPS; ++q) {
-            if (q >= A.ng) break;
-            const auto sp = group_sum_f<G>(pre[q]);
-            if (act && lane == 0) {
-                const size_t o = (size_t)q * A.n + i;
-                ((R*)A.afW)[o] = (R)(((const R*)A.afS)[o] * (sp.d() + spre[q]));
-            }
-        }
-    }
-    if (wantF) {
-        auto sfx = group_sum_f<G>(fx), sfy = group_sum_f<G>(fy), sfz = group_sum_f<G>(fz);
-        if (act && lane == 0) {
-            if constexpr (sizeof(R) == 4) {
-                sfx.f += fix_from_double(sf0);
-                sfy.f += fix_from_double(sf1);
-                sfz.f += fix_from_double(sf2);
-            } else {
-                sfx.s += sf0;
-                sfy.s += sf1;
-                sfz.s += sf2;
-            }
-            store_sum(A.out_f + 3 * i, sfx, A.first_f);
-            store_sum(A.out_f + 3 * i + 1, sfy, A.first_f);
-            store_sum(A.out_f + 3 * i + 2, sfz, A.first_f);
-        }
-    }
-    if (wantC) {
-        auto schi = group_sum_f<G>(chi);
-        if (act && lane == 0) {
-            if constexpr (sizeof(R) == 4) schi.f += fix_from_double(cs);
-            else schi.s += cs;
-            store_sum(A.out_chi + i, schi, A.first_chi);
-        }
-    }
-    // energy and virial: warp sums, exact from there on
-    if (A.acc && (wantE || wantF)) {
-        // the single-atom energies join the total exactly, outside the working precision
-        const Fx128 v[7] = {fx_add(warp_total(en), fx_warp_sum(fx_from_double(es))), warp_total(w0), warp_total(w1),
-                            warp_total(w2), warp_total(w3), warp_total(w4), warp_total(w5)};
-        block_totals_publish(v, wsum, &done, A.acc);
-    }
-}
 
 template <typename R, int G, bool AF>
 __global__ void __launch_bounds__(256) pair_kernel(const __grid_constant__ PairArgs A) {
