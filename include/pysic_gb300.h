@@ -244,6 +244,19 @@ int pg_relax_charges_potentiostat(pg_context* ctx, int32_t precision, int32_t n_
  * which completes that step first.  *steps_done counts completed steps.
  * pg_md_get_state downloads momenta and positions (either may be null). */
 int pg_md_set_state(pg_context* ctx, const double* masses, const double* momenta);
+/* The same dynamics for exactly n_steps steps, the neighbour lists rebuilt on
+ * the device whenever an atom has moved more than skin/2 since the last build
+ * (the FastNeighborList policy, calculator.py:29-189), with the cutoffs and
+ * the builder (cell list or all pairs) of the last pg_generate_neighbor_lists /
+ * pg_generate_all_pairs_lists call; the host only launches and reads a flag
+ * word per chunk of steps.  *rebuilds counts the rebuilds; the positions of the
+ * last build are read with pg_get_list_positions.  Lists installed from the
+ * host (pg_create_neighbor_lists) give PG_ERR_NOT_READY: use pg_md_verlet. */
+int pg_md_run(pg_context* ctx, int32_t precision, int32_t n_steps, double timestep, double skin, int32_t* steps_done,
+              int32_t* rebuilds);
+/* The positions (N x 3) at which the current neighbour lists were built (the
+ * reference positions of FastNeighborList's skin test). */
+int pg_get_list_positions(pg_context* ctx, double* positions);
 int pg_md_verlet(pg_context* ctx, int32_t precision, int32_t n_steps, double timestep, double skin,
                  int32_t* steps_done, int32_t* rebuild);
 int pg_md_get_state(pg_context* ctx, double* momenta, double* positions);

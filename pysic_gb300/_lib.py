@@ -86,6 +86,9 @@ _SIGNATURES = {
                                         ctypes.c_double, ctypes.c_double, _c_double_p, _c_double_p, _c_int_p,
                                         _c_double_p, _c_double_p]),
     "pg_md_set_state": (ctypes.c_int, [_ctx, _c_double_p, _c_double_p]),
+    "pg_md_run": (ctypes.c_int, [_ctx, ctypes.c_int32, ctypes.c_int32, ctypes.c_double, ctypes.c_double, _c_int_p,
+                                  _c_int_p]),
+    "pg_get_list_positions": (ctypes.c_int, [_ctx, _c_double_p]),
     "pg_md_verlet": (ctypes.c_int, [_ctx, ctypes.c_int32, ctypes.c_int32, ctypes.c_double, ctypes.c_double,
                                     _c_int_p, _c_int_p]),
     "pg_md_get_state": (ctypes.c_int, [_ctx, _c_double_p, _c_double_p]),

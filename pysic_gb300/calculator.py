@@ -66,19 +66,45 @@ class FastNeighborList:
         self.skin = float(skin)
         self.cutoffs = np.asarray(cutoffs, dtype=np.float64) + self.skin
         self.nupdates = 0
-        self.counts = None
-        self.neighbors = []
-        self.displacements = []
+        self._flat = None       # (counts, neighbour indices, offsets) as the engine returns them
+        self._lists = None      # per-atom arrays, made from _flat on first use
+        self._source = None     # engine whose lists have not been downloaded yet
         self.positions = None
         self.pbc = None
         self.cell = None
         self.all_pairs = False
 
     def _store(self, counts, idx, off):
-        self.counts = counts
-        starts = np.concatenate([[0], np.cumsum(counts)])
-        self.neighbors = [idx[starts[i]:starts[i + 1]].copy() for i in range(len(counts))]
-        self.displacements = [off[starts[i]:starts[i + 1]].copy() for i in range(len(counts))]
+        self._flat = (counts, idx, off)
+        self._lists = None
+        self._source = None
+
+    def _per_atom(self):
+        """The per-atom neighbour and offset arrays, downloaded and split on
+        first use (a long run of device rebuilds needs none of them)."""
+        if self._source is not None:
+            self._store(*self._source.neighbor_lists())
+        if self._lists is None:
+            if self._flat is None:
+                return [], []
+            counts, idx, off = self._flat
+            starts = np.concatenate([[0], np.cumsum(counts)])
+            self._lists = ([idx[starts[i]:starts[i + 1]].copy() for i in range(len(counts))],
+                           [off[starts[i]:starts[i + 1]].copy() for i in range(len(counts))])
+        return self._lists
+
+    @property
+    def counts(self):
+        self._per_atom()
+        return None if self._flat is None else self._flat[0]
+
+    @property
+    def neighbors(self):
+        return self._per_atom()[0]
+
+    @property
+    def displacements(self):
+        return self._per_atom()[1]
 
     def build(self, atoms, engine=None):
         """Build the list for ``atoms`` (calculator.py:62-108).  With no engine
@@ -92,8 +118,11 @@ class FastNeighborList:
             engine.build_all_pairs(self.cutoffs, self.skin)
         else:
             engine.build_neighbors(self.cutoffs, self.skin)
-        counts, idx, off = engine.neighbor_lists()
-        self._store(counts, idx, off)
+        if own:
+            self._store(*engine.neighbor_lists())
+        else:
+            self._source = engine  # downloaded when first asked for
+            self._lists = None
         self.positions = np.array(atoms.get_positions())
         self.pbc = np.array(atoms.get_pbc())
         self.cell = np.array(atoms.get_cell())
@@ -125,8 +154,10 @@ class FastNeighborList:
         self.nupdates += 1
 
     def refresh_from(self, engine):
-        counts, idx, off = engine.neighbor_lists()
-        self._store(counts, idx, off)
+        """The engine's current lists become this list's (downloaded when
+        first asked for)."""
+        self._source = engine
+        self._lists = None
 
     def update(self, atoms, engine=None):
         if self.needs_update(atoms):

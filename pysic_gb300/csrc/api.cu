@@ -899,6 +899,32 @@ int pg_md_verlet(pg_context* ctx, int32_t precision, int32_t n_steps, double tim
     });
 }
 
+int pg_md_run(pg_context* ctx, int32_t precision, int32_t n_steps, double timestep, double skin, int32_t* steps_done,
+              int32_t* rebuilds) {
+    return guarded([&] {
+        check_ctx(ctx);
+        use_device(ctx);
+        pg::require(steps_done && rebuilds, PG_ERR_INVALID, "null output pointer");
+        pg::require(n_steps >= 0, PG_ERR_INVALID, "negative step count");
+        int s = 0, r = 0;
+        pg::md_run_rebuilding(ctx, precision, n_steps, timestep, skin, &s, &r);
+        *steps_done = s;
+        *rebuilds = r;
+    });
+}
+
+int pg_get_list_positions(pg_context* ctx, double* positions) {
+    return guarded([&] {
+        check_ctx(ctx);
+        use_device(ctx);
+        pg::require(positions != nullptr, PG_ERR_INVALID, "null output pointer");
+        pg::require(ctx->have_list && ctx->sep0_epoch == ctx->list_epoch, PG_ERR_NOT_READY,
+                    "no list generation on the device yet (evaluate once after building the lists)");
+        ctx->pos0.download(positions, 3 * (size_t)ctx->n, ctx->stream);
+        PG_CUDA(cudaStreamSynchronize(ctx->stream));
+    });
+}
+
 int pg_relax_charges_potentiostat(pg_context* ctx, int32_t precision, int32_t n_steps, double timestep,
                                   double inertia, double potential, double* rates, double* charges, double* max_dchi) {
     return guarded([&] {

@@ -449,7 +449,7 @@ struct pg_context {
     pg::DevBuf<pg::F4> disp32;
     unsigned long long list_epoch = 0, sep0_epoch = ~0ull;
     long long sh_total = 0;
-    int sh_maxn = 0;
+    long long bo_stride = 0;  // entries per section of the bond-pass scratch (>= sh_total)
 
     // neighbour-build scratch
     pg::DevBuf<int> cell_of, cell_start, sorted_atoms, wrap, keys_a, keys_b, vals_a, vals_b, radix_hist, count_tmp,
@@ -459,6 +459,10 @@ struct pg_context {
     pg::DevBuf<int> g0_start;
     pg::DevBuf<double> cutoffs;
     pg::DevBuf<int> scan_tmp;
+    pg::DevBuf<int> nb_totals;     // build totals on the device: out-of-range atoms, entries, lower-index entries
+    pg::PinnedBuf<int> h_totals;   // their host copy (one synchronisation per build)
+    std::vector<double> h_cutoffs;  // cutoffs of the last engine build (rebuilds on the device coordinates)
+    int list_kind = 0;              // PG_LIST_*: who built the lists
 
     // bond-order scratch
     pg::DevBuf<pg::F4> bo_fj;             // mixed precision: 4 records per short entry
@@ -482,6 +486,8 @@ struct pg_context {
     pg::DevBuf<double> md_p, md_m;  // dynamics: momenta (n x 3), masses
     pg::DevBuf<int> md_flag;
     bool md_ready = false, md_pending = false;  // state set; a step waits for its forces after a rebuild
+    cudaGraphExec_t md_exec = nullptr;          // the captured step of the rebuilding loop
+    unsigned long long md_sig = 0;              // what its kernel arguments were captured from
 
     int launches = 0;
     // device address of the no-allocation call's static scratch array in this
@@ -504,6 +510,7 @@ struct pg_context {
 
     ~pg_context() {
         for (auto& g : graphs) cudaGraphExecDestroy(g.exec);
+        if (md_exec) cudaGraphExecDestroy(md_exec);
         for (auto& e : tev)
             if (e) cudaEventDestroy(e);
     }
@@ -607,6 +614,8 @@ constexpr int PG_RELAX_DYNAMIC = 0, PG_RELAX_POTENTIOSTAT = 1;
 void md_set_state(pg_context* ctx, const double* masses, const double* momenta);
 void md_get_state(pg_context* ctx, double* momenta, double* positions);
 void md_run(pg_context* ctx, int precision, int n_steps, double dt, double skin, int* steps_done, int* rebuild);
+void md_run_rebuilding(pg_context* ctx, int precision, int n_steps, double dt, double skin, int* steps_done,
+                       int* rebuilds);
 void evaluate(pg_context* ctx, int precision, int flags);
 // api.cu: lanes per atom of the pair kernel for this context's list lengths
 int pair_lanes_for(const pg_context* ctx);
@@ -621,6 +630,11 @@ void atom_factor_gradients(pg_context* ctx, int precision, int group, int atom, 
 // triplet.cu: three-body potentials (bond_bend)
 constexpr int PG_MAX_TRIPLET_RECORDS = 64;
 constexpr int PG_MAX_QUAD_RECORDS = 64;
+// origin of the neighbour lists
+constexpr int PG_LIST_NONE = 0;
+constexpr int PG_LIST_CELLS = 1;      // the engine's cell-list build
+constexpr int PG_LIST_ALL_PAIRS = 2;  // the engine's all-pairs build
+constexpr int PG_LIST_INSTALLED = 3;  // installed from the host
 void launch_triplets(pg_context* ctx, int precision, int flags, bool first_f, FxAcc* acc, const int* skip);
 // optimize.cu: the constrained energy minimum over the charges (quadratic energies)
 void optimize_charges(pg_context* ctx, int precision, int max_iter, double tolerance, double* charges, int* iterations,

@@ -19,6 +19,7 @@
 // kick).  Momenta and masses live on the device between calls.
 #include <algorithm>
 #include <cmath>
+#include <cstring>
 
 #include "common.cuh"
 
@@ -209,6 +210,167 @@ void md_run(pg_context* ctx, int precision, int n_steps, double dt, double skin,
     }
     PG_CUDA(cudaStreamSynchronize(st));
     *steps_done = done;
+}
+
+// The lists again from the device coordinates, with the cutoffs and the
+// builder of the last build (the rebuild FastNeighborList makes when an atom
+// has moved more than skin/2, calculator.py:29-189), then the list
+// generation's reference positions and bond vectors and the short list.
+static void rebuild_lists(pg_context* ctx) {
+    require(ctx->list_kind == PG_LIST_CELLS || ctx->list_kind == PG_LIST_ALL_PAIRS, PG_ERR_NOT_READY,
+            "the lists were installed from the host: rebuild them there (pg_md_verlet)");
+    if (ctx->list_kind == PG_LIST_CELLS) build_neighbor_lists(ctx, ctx->h_cutoffs.data());
+    else build_allpairs_lists(ctx, ctx->h_cutoffs.data());
+    build_full_sep0(ctx);
+    if (ctx->have_bond_terms) build_short_list(ctx);
+}
+
+// what the captured step's kernel arguments depend on beyond the context's
+// fixed state: buffer addresses (any growth moves them), the pair kernel's lanes
+// and the sections of the bond-pass scratch
+static unsigned long long step_signature(const pg_context* ctx, int precision, int G) {
+    unsigned long long h = alloc_epoch();
+    h = h * 1000003ull + (unsigned long long)pair_lanes_for(ctx);
+    h = h * 1000003ull + (unsigned long long)ctx->bo_stride;
+    h = h * 1000003ull + (unsigned long long)(precision * 131 + G);
+    return h;
+}
+
+void md_run_rebuilding(pg_context* ctx, int precision, int n_steps, double dt, double skin, int* steps_done,
+                       int* rebuilds) {
+    require(ctx->md_ready, PG_ERR_NOT_READY, "no dynamics state: call pg_md_set_state first");
+    require(std::isfinite(dt) && std::isfinite(skin) && skin >= 0.0, PG_ERR_INVALID, "invalid time step or skin");
+    require(ctx->list_kind == PG_LIST_CELLS || ctx->list_kind == PG_LIST_ALL_PAIRS, PG_ERR_NOT_READY,
+            "the lists were installed from the host: run pg_md_verlet and rebuild them there");
+    *steps_done = 0;
+    *rebuilds = 0;
+    const int n = ctx->n;
+    cudaStream_t st = ctx->stream;
+    const int flags = PG_WANT_FORCES;
+    int done = 0, nreb = 0;
+    // a step left pending by pg_md_verlet: rebuild here and finish it
+    if (ctx->md_pending) {
+        rebuild_lists(ctx);
+        ++nreb;
+    }
+    // the forces at the current positions (and the lanes, buffers and tables
+    // every later launch uses)
+    evaluate(ctx, precision, flags);
+    if (n == 0 || n_steps <= 0) {
+        PG_CUDA(cudaStreamSynchronize(st));
+        *rebuilds = nreb;
+        return;
+    }
+    int G = ctx->lanes != 0 ? ctx->lanes : ctx->tuned_lanes[precision];
+    if (G == 0) G = 8;
+    ctx->md_flag.resize(8);
+    MdArgs A{};
+    A.n = n;
+    A.pos = ctx->pos.p;
+    A.pos0 = ctx->pos0.p;
+    A.p = ctx->md_p.p;
+    A.m = ctx->md_m.p;
+    A.f = ctx->out_f.p;
+    A.dt = dt;
+    A.half = 0.5 * dt;
+    A.skin2 = (0.5 * skin) * (0.5 * skin);
+    A.flag = ctx->md_flag.p;
+    const int nb = (n + MT - 1) / MT;
+    if (ctx->md_pending) {
+        md_finish_step<<<nb, MT, 0, st>>>(A);
+        PG_CHECK_LAUNCH();
+        ctx->md_pending = false;
+        done = 1;
+    }
+    auto one_step = [&] {
+        md_kick_drift<<<nb, MT, 0, st>>>(A);
+        enqueue_evaluation(ctx, precision, flags, G, A.flag);
+        md_kick<<<nb, MT, 0, st>>>(A);
+    };
+    // the step graph: kept by the context, refreshed (cudaGraphExecUpdate, or
+    // instantiated anew) only when what its arguments come from has changed
+    auto refresh_graph = [&] {
+        if (!ctx->use_graphs) return;
+        A.pos0 = ctx->pos0.p;
+        A.f = ctx->out_f.p;
+        unsigned long long bits[2];
+        std::memcpy(&bits[0], &A.dt, sizeof(double));
+        std::memcpy(&bits[1], &A.skin2, sizeof(double));
+        const unsigned long long sig = (step_signature(ctx, precision, G) * 1000003ull + bits[0]) * 1000003ull + bits[1];
+        if (ctx->md_exec && ctx->md_sig == sig) return;
+        cudaGraph_t g = nullptr;
+        PG_CUDA(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
+        try {
+            one_step();
+        } catch (...) {
+            cudaStreamEndCapture(st, &g);
+            if (g) cudaGraphDestroy(g);
+            throw;
+        }
+        PG_CUDA(cudaStreamEndCapture(st, &g));
+        bool updated = false;
+        if (ctx->md_exec) {
+            cudaGraphExecUpdateResultInfo info{};
+            updated = cudaGraphExecUpdate(ctx->md_exec, g, &info) == cudaSuccess;
+            if (!updated) {
+                (void)cudaGetLastError();  // a failed update leaves no sticky error
+                cudaGraphExecDestroy(ctx->md_exec);
+                ctx->md_exec = nullptr;
+            }
+        }
+        if (!updated) {
+            const cudaError_t e = cudaGraphInstantiate(&ctx->md_exec, g, 0);
+            if (e != cudaSuccess) ctx->md_exec = nullptr;
+            cudaGraphDestroy(g);
+            PG_CUDA(e);
+        } else {
+            cudaGraphDestroy(g);
+        }
+        ctx->md_sig = sig;
+    };
+    // flags: [0] skip, [1] rebuild requested, [2] steps done, [3] target, [5] finished
+    int* hf = ctx->h_flag.get(8);
+    std::fill(hf, hf + 8, 0);
+    hf[2] = done;
+    hf[3] = n_steps;
+    PG_CUDA(cudaMemcpyAsync(A.flag, hf, sizeof(int) * 8, cudaMemcpyHostToDevice, st));
+    refresh_graph();
+    int chunk = 8, since = 0;
+    while (done < n_steps) {
+        const int k = std::max(1, std::min(chunk, n_steps - done));
+        for (int s = 0; s < k; ++s) {
+            if (ctx->md_exec) PG_CUDA(cudaGraphLaunch(ctx->md_exec, st));
+            else one_step();
+        }
+        PG_CHECK_LAUNCH();
+        PG_CUDA(cudaMemcpyAsync(hf, A.flag, sizeof(int) * 8, cudaMemcpyDeviceToHost, st));
+        PG_CUDA(cudaStreamSynchronize(st));
+        since += hf[2] - done;
+        done = hf[2];
+        if (!hf[5]) {  // the chunk ran through
+            chunk = std::min(2 * chunk, 64);
+            continue;
+        }
+        if (!hf[1]) break;  // the target reached
+        // an atom moved more than skin/2: new lists at the drifted positions,
+        // then the step's forces and second kick, then on
+        rebuild_lists(ctx);
+        ++nreb;
+        enqueue_evaluation(ctx, precision, flags, G, nullptr);
+        md_finish_step<<<nb, MT, 0, st>>>(A);
+        PG_CHECK_LAUNCH();
+        ++done;
+        chunk = std::max(2, std::min(since, 64));  // about one list generation per chunk
+        since = 0;
+        std::fill(hf, hf + 8, 0);
+        hf[2] = done;
+        hf[3] = n_steps;
+        PG_CUDA(cudaMemcpyAsync(A.flag, hf, sizeof(int) * 8, cudaMemcpyHostToDevice, st));
+        refresh_graph();
+    }
+    PG_CUDA(cudaStreamSynchronize(st));
+    *steps_done = done;
+    *rebuilds = nreb;
 }
 
 }  // namespace pg

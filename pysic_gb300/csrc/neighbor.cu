@@ -243,7 +243,7 @@ struct ScanArgs {
     const int* sorted;
     const int* invisible;
     const int* inv_list;
-    int n_inv;
+    const int* n_inv;  // device: atoms in out-of-range periodic subcells
     CellK C;
     Split S;
     // outputs
@@ -363,11 +363,12 @@ __global__ void __launch_bounds__(SCAN_THREADS) nb_scan(ScanArgs A) {
     }
     // lower-index atoms in out-of-range subcells of a periodic axis: their
     // sweep can reach a, but a's stencil never reaches them
-    if (visible && A.n_inv > 0) {
-        for (int q0 = 0; q0 < A.n_inv; q0 += 32) {
+    const int n_inv = *A.n_inv;
+    if (visible && n_inv > 0) {
+        for (int q0 = 0; q0 < n_inv; q0 += 32) {
             const int q = q0 + lane;
             int cnt = 0;
-            int b = q < A.n_inv ? A.inv_list[q] : a;
+            int b = q < n_inv ? A.inv_list[q] : a;
             long long keys[27];
             int4 vals[27];
             if (b < a) {
@@ -511,6 +512,24 @@ __global__ void short_reverse(int n, const int* __restrict__ start, const int* _
     }
 }
 
+// sort keys of the slot order: the atom's short-list count, the atom itself
+__global__ void order_keys(int n, const int* __restrict__ cnt, int* __restrict__ keys, int* __restrict__ vals) {
+    const int a = blockIdx.x * blockDim.x + threadIdx.x;
+    if (a >= n) return;
+    keys[a] = min(cnt[a], 65535);
+    vals[a] = a;
+}
+
+// slot k: atom m = sorted[k], its first short-list entry and its count
+__global__ void order_slots(int n, const int* __restrict__ sorted, const int* __restrict__ start,
+                            const int* __restrict__ cnt, int* __restrict__ order, int4* __restrict__ slot) {
+    const int k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= n) return;
+    const int m = sorted[k];
+    order[k] = m;
+    slot[k] = make_int4(m, start[m], cnt[m], 0);
+}
+
 __global__ void max_reduce(int n, const int* __restrict__ v, int* __restrict__ out) {
     __shared__ int sm[1024];
     int m = 0;
@@ -632,7 +651,7 @@ void build_neighbor_lists(pg_context* ctx, const double* h_cutoffs) {
     const int ncell = S.nx * S.ny * S.nz;
     CellK C = cell_kernel_view(ctx->cell);
 
-    ctx->cutoffs.upload(h_cutoffs, n, st);
+    if (h_cutoffs != ctx->h_cutoffs.data()) ctx->cutoffs.upload(h_cutoffs, n, st);  // else: on the device already
     ctx->cell_of.resize(3 * (size_t)std::max(n, 1));
     ctx->wrap.resize(3 * (size_t)std::max(n, 1));
     ctx->keys_a.resize(std::max(n, 1));
@@ -672,12 +691,13 @@ void build_neighbor_lists(pg_context* ctx, const double* h_cutoffs) {
     if (n > 0)
         PG_CUDA(cudaMemcpyAsync(ctx->sorted_atoms.p, sorted_vals, sizeof(int) * n, cudaMemcpyDeviceToDevice, st));
 
-    // atoms in out-of-range periodic subcells
+    // atoms in out-of-range periodic subcells: their count stays on the device
     ctx->scan_tmp.resize(std::max(n, 1) + 1);
-    int n_inv = 0;
-    exclusive_scan_int(ctx->invisible.p, ctx->scan_tmp.p, n, st, ctx->count_tmp, &n_inv);
+    ctx->nb_totals.resize(4);  // [0] out-of-range atoms, [1] list entries, [2] lower-index entries
+    scan_single_block<int, int><<<1, 1024, 0, st>>>(ctx->invisible.p, ctx->scan_tmp.p, n, ctx->nb_totals.p, 0);
+    PG_CHECK_LAUNCH();
     DevBuf<int>& inv_list = ctx->keys_b;  // free after the sort
-    if (n_inv > 0) {
+    if (n > 0) {
         compact_flags<<<blocks(n, 256), 256, 0, st>>>(n, ctx->invisible.p, ctx->scan_tmp.p, inv_list.p);
         PG_CHECK_LAUNCH();
     }
@@ -693,7 +713,7 @@ void build_neighbor_lists(pg_context* ctx, const double* h_cutoffs) {
     A.sorted = ctx->sorted_atoms.p;
     A.invisible = ctx->invisible.p;
     A.inv_list = inv_list.p;
-    A.n_inv = n_inv;
+    A.n_inv = ctx->nb_totals.p;
     A.C = C;
     A.S = S;
     ctx->nb_g0.resize(std::max(n, 1));
@@ -712,9 +732,15 @@ void build_neighbor_lists(pg_context* ctx, const double* h_cutoffs) {
         add_counts<<<blocks(n, 256), 256, 0, st>>>(n, ctx->nb_g0.p, ctx->vals_a.p, ctx->keys_a.p);
         PG_CHECK_LAUNCH();
     }
-    int total = 0, total0 = 0;
-    exclusive_scan_int(ctx->keys_a.p, ctx->nb_start.p, n, st, ctx->count_tmp, &total);
-    exclusive_scan_int(ctx->nb_g0.p, ctx->g0_start.p, n, st, ctx->count_tmp, &total0);
+    // both scans' totals come back with one synchronisation
+    scan_single_block<int, int><<<1, 1024, 0, st>>>(ctx->keys_a.p, ctx->nb_start.p, n, ctx->nb_totals.p + 1, 0);
+    PG_CHECK_LAUNCH();
+    scan_single_block<int, int><<<1, 1024, 0, st>>>(ctx->nb_g0.p, ctx->g0_start.p, n, ctx->nb_totals.p + 2, 0);
+    PG_CHECK_LAUNCH();
+    int* ht = ctx->h_totals.get(4);
+    PG_CUDA(cudaMemcpyAsync(ht, ctx->nb_totals.p, sizeof(int) * 4, cudaMemcpyDeviceToHost, st));
+    PG_CUDA(cudaStreamSynchronize(st));
+    const int total = ht[1], total0 = ht[2];
     ctx->nb_total = total;
     ctx->nb_idx.resize(std::max(total, 1));
     ctx->nb_off.resize(3 * (size_t)std::max(total, 1));
@@ -734,7 +760,9 @@ void build_neighbor_lists(pg_context* ctx, const double* h_cutoffs) {
                                                                   ctx->nb_off.p);
         PG_CHECK_LAUNCH();
     }
-    PG_CUDA(cudaStreamSynchronize(st));
+    // the cutoffs (host copy) for rebuilds on the device coordinates
+    if (h_cutoffs != ctx->h_cutoffs.data()) ctx->h_cutoffs.assign(h_cutoffs, h_cutoffs + n);
+    ctx->list_kind = PG_LIST_CELLS;
     ctx->have_list = true;
     ctx->list_epoch++;
     ctx->state_epoch++;
@@ -770,7 +798,7 @@ void build_allpairs_lists(pg_context* ctx, const double* h_cutoffs) {
         require(ni[i] <= 64, PG_ERR_INVALID, "cutoff spans too many periodic images");
     }
     CellK C = cell_kernel_view(Cc);
-    ctx->cutoffs.upload(h_cutoffs, n, st);
+    if (h_cutoffs != ctx->h_cutoffs.data()) ctx->cutoffs.upload(h_cutoffs, n, st);
     ctx->nb_g0.resize(std::max(n, 1));
     ctx->nb_start.resize(n + 1);
     const int3 nimg = make_int3(ni[0], ni[1], ni[2]);
@@ -789,7 +817,8 @@ void build_allpairs_lists(pg_context* ctx, const double* h_cutoffs) {
                                                             nullptr, ctx->nb_idx.p, ctx->nb_off.p);
         PG_CHECK_LAUNCH();
     }
-    PG_CUDA(cudaStreamSynchronize(st));
+    if (h_cutoffs != ctx->h_cutoffs.data()) ctx->h_cutoffs.assign(h_cutoffs, h_cutoffs + n);
+    ctx->list_kind = PG_LIST_ALL_PAIRS;
     ctx->have_list = true;
     ctx->list_epoch++;
     ctx->state_epoch++;
@@ -815,6 +844,7 @@ void install_neighbor_lists(pg_context* ctx, const int32_t* counts, const int32_
     }
     PG_CUDA(cudaStreamSynchronize(ctx->stream));
     ctx->nb_total = total;
+    ctx->list_kind = PG_LIST_INSTALLED;
     ctx->have_list = true;
     ctx->list_epoch++;
     ctx->state_epoch++;
@@ -878,43 +908,51 @@ void build_short_list(pg_context* ctx) {
                                                                     ctx->sh_type.p);
         PG_CHECK_LAUNCH();
     }
-    DevBuf<int> mx;
-    mx.resize(2);
-    max_reduce<<<1, 1024, 0, st>>>(n, ctx->sh_count.p, mx.p);
-    PG_CHECK_LAUNCH();
-    // every short entry must have its reverse entry
-    min_reduce<<<1, 1024, 0, st>>>(std::max(total, 1) * (total > 0), ctx->sh_rev.p, mx.p + 1);
-    PG_CHECK_LAUNCH();
-    int h[2] = {0, 0};
-    PG_CUDA(cudaMemcpyAsync(h, mx.p, sizeof(int) * 2, cudaMemcpyDeviceToHost, st));
-    PG_CUDA(cudaStreamSynchronize(st));
-    ctx->sh_maxn = h[0];
-    require(total == 0 || h[1] >= 0, PG_ERR_INVALID,
-            "neighbour lists are not symmetric: a bond has no reverse entry (lists must be built both ways)");
-    // atoms grouped by list length (stable counting sort), so that the lane
-    // groups of one warp loop over the same number of bonds
-    std::vector<int> cnt((size_t)std::max(n, 1)), order((size_t)std::max(n, 1));
-    if (n > 0) PG_CUDA(cudaMemcpyAsync(cnt.data(), ctx->sh_count.p, sizeof(int) * n, cudaMemcpyDeviceToHost, st));
-    PG_CUDA(cudaStreamSynchronize(st));
-    {
-        std::vector<int> first((size_t)h[0] + 2, 0);
-        for (int m = 0; m < n; ++m) first[(size_t)cnt[m] + 1]++;
-        for (size_t c = 1; c < first.size(); ++c) first[c] += first[c - 1];
-        for (int m = 0; m < n; ++m) order[(size_t)first[(size_t)cnt[m]]++] = m;
+    // Lists from the host may lack reverse entries: checked before use.  The
+    // engine's own builds are symmetric by construction.
+    if (ctx->list_kind == PG_LIST_INSTALLED) {
+        DevBuf<int> mx;
+        mx.resize(1);
+        min_reduce<<<1, 1024, 0, st>>>(std::max(total, 1) * (total > 0), ctx->sh_rev.p, mx.p);
+        PG_CHECK_LAUNCH();
+        int h = 0;
+        PG_CUDA(cudaMemcpyAsync(&h, mx.p, sizeof(int), cudaMemcpyDeviceToHost, st));
+        PG_CUDA(cudaStreamSynchronize(st));
+        require(total == 0 || h >= 0, PG_ERR_INVALID,
+                "neighbour lists are not symmetric: a bond has no reverse entry (lists must be built both ways)");
     }
-    ctx->sh_order.upload(order.data(), order.size(), st);
-    // the same order with each atom's entry range, for a single load per slot
-    std::vector<int4> slot((size_t)std::max(n, 1), make_int4(0, 0, 0, 0));
-    {
-        std::vector<int> first((size_t)std::max(n, 1), 0);
-        for (int m = 1; m < n; ++m) first[(size_t)m] = first[(size_t)m - 1] + cnt[(size_t)m - 1];
-        for (int k = 0; k < n; ++k) {
-            const int m = order[(size_t)k];
-            slot[(size_t)k] = make_int4(m, first[(size_t)m], cnt[(size_t)m], 0);
+    // atoms grouped by list length, stably (ties in index order), so that the
+    // lane groups of one warp loop over the same number of bonds: a two-digit
+    // radix sort of (count, atom) on the device (counts below 65536), then per
+    // slot (atom, first entry, count)
+    ctx->sh_order.resize(std::max(n, 1));
+    ctx->sh_slot.resize(std::max(n, 1));
+    if (n > 0) {
+        ctx->keys_a.resize(n);
+        ctx->keys_b.resize(n);
+        ctx->vals_a.resize(n);
+        ctx->vals_b.resize(n);
+        const int nblk = std::max(1, blocks(n, RS_TILE));
+        ctx->radix_hist.resize((size_t)256 * nblk + 1);
+        ctx->count_tmp.resize((size_t)256 * nblk + 1);
+        order_keys<<<blocks(n, 256), 256, 0, st>>>(n, ctx->sh_count.p, ctx->keys_a.p, ctx->vals_a.p);
+        PG_CHECK_LAUNCH();
+        int *k_in = ctx->keys_a.p, *v_in = ctx->vals_a.p, *k_out = ctx->keys_b.p, *v_out = ctx->vals_b.p;
+        for (int pass = 0; pass < 2; ++pass) {
+            radix_hist<<<nblk, RS_THREADS, 0, st>>>(n, k_in, 8 * pass, nblk, ctx->radix_hist.p);
+            PG_CHECK_LAUNCH();
+            scan_single_block<int, int><<<1, 1024, 0, st>>>(ctx->radix_hist.p, ctx->count_tmp.p, 256 * nblk, nullptr,
+                                                            0);
+            PG_CHECK_LAUNCH();
+            radix_scatter<<<nblk, RS_THREADS, 0, st>>>(n, k_in, v_in, 8 * pass, nblk, ctx->count_tmp.p, k_out, v_out);
+            PG_CHECK_LAUNCH();
+            std::swap(k_in, k_out);
+            std::swap(v_in, v_out);
         }
+        order_slots<<<blocks(n, 256), 256, 0, st>>>(n, v_in, ctx->sh_start.p, ctx->sh_count.p, ctx->sh_order.p,
+                                                    ctx->sh_slot.p);
+        PG_CHECK_LAUNCH();
     }
-    ctx->sh_slot.upload(slot.data(), slot.size(), st);
-    PG_CUDA(cudaStreamSynchronize(st));
     ctx->short_dirty = false;
     ctx->state_epoch++;
 }

@@ -96,8 +96,17 @@ int bond_blocks(int n, int G) {
     return (n + ap - 1) / ap;
 }
 
+// Entries per section of the bond-pass scratch: the short list's length with
+// headroom, kept while the list fits, so that the sections (and the captured
+// kernels' arguments) stay put across list rebuilds of similar length.
+static size_t bond_stride(pg_context* ctx) {
+    const long long need = std::max<long long>(ctx->sh_total, 1);
+    if (ctx->bo_stride < need) ctx->bo_stride = need + need / 4 + 64;
+    return (size_t)ctx->bo_stride;
+}
+
 void prepare_bond_scratch(pg_context* ctx, int precision) {
-    const size_t ne = (size_t)std::max<long long>(ctx->sh_total, 1);
+    const size_t ne = bond_stride(ctx);
     // per short-list entry: bond geometry | force from the partner's bonds | k-part
     // sums | unstaged j parts
     if (precision == PG_PREC_FP64) ctx->bo_fj64.resize(4 * ne);
@@ -143,7 +152,7 @@ BondArgs make_bond_args(pg_context* ctx, int precision, int flags, bool first_f,
     }
     A.flags = flags;
     A.first_f = first_f;
-    const size_t ne = (size_t)std::max<long long>(ctx->sh_total, 1);
+    const size_t ne = bond_stride(ctx);
     if (precision == PG_PREC_FP64) {
         A.terms = ctx->d_pair_terms.p;
         A.tab = ctx->d_tab64.p;

@@ -181,6 +181,21 @@ class Engine:
                                       ctypes.byref(s), ctypes.byref(r)))
         return s.value, bool(r.value)
 
+    def md_run(self, precision, n_steps, timestep, skin):
+        """Exactly n_steps velocity Verlet steps with the lists rebuilt on the
+        device as needed; (steps completed, list rebuilds)."""
+        s = ctypes.c_int32(0)
+        r = ctypes.c_int32(0)
+        L.check(self.lib.pg_md_run(self.ctx, precision, int(n_steps), float(timestep), float(skin), ctypes.byref(s),
+                                   ctypes.byref(r)))
+        return s.value, r.value
+
+    def list_positions(self):
+        """The positions at which the current lists were built."""
+        r = np.zeros((self.n, 3))
+        L.check(self.lib.pg_get_list_positions(self.ctx, L.dptr(r)))
+        return r
+
     def md_get_state(self):
         p = np.zeros((self.n, 3))
         r = np.zeros((self.n, 3))

@@ -5,11 +5,12 @@ VelocityVerlet.step (ase/md/verlet.py) reads the momenta, asks the Pysic
 calculator for forces and writes the positions back, every step crossing into
 the Fortran core.  ``VelocityVerlet`` here keeps ASE's interface (timestep in
 ASE units, ``run(steps)``, ``attach(function, interval)``, ``nsteps``) and its
-update, operation for operation, but the steps run on the GPU
-(pg_md_verlet): forces, both kicks and the drift stay in device memory, the
-neighbour list is rebuilt when an atom has moved more than skin/2 (the
-FastNeighborList / ASE update policy), and the host is visited only for
-rebuilds and for observers.  ASE itself is not needed.
+update, operation for operation, but the steps run on the GPU (pg_md_run):
+forces, both kicks and the drift stay in device memory, the neighbour list is
+rebuilt on the device when an atom has moved more than skin/2 (the
+FastNeighborList / ASE update policy), and the host only launches captured
+steps, reads a flag word per chunk and serves observers.  ASE itself is not
+needed.
 
 With a ChargeRelaxation attached to the calculator, every force call of the
 reference relaxes the charges first (Pysic.get_forces ->
@@ -106,15 +107,15 @@ class VelocityVerlet:
         rebuilt = False
         while left > 0:
             k = left if stride is None else min(left, stride - self.nsteps % stride)
-            while k > 0:
-                done, rebuild = eng.md_verlet(prec, k, self.dt, nl.skin)
-                k -= done
-                left -= done
-                self.nsteps += done
-                if rebuild:
-                    _, r = eng.md_get_state()
-                    nl.rebuild_on_device(eng, r)
-                    rebuilt = True
+            # k steps, the lists rebuilt on the device whenever an atom has moved
+            # more than skin/2 (pg_md_run)
+            done, rebuilds = eng.md_run(prec, k, self.dt, nl.skin)
+            left -= done
+            self.nsteps += done
+            if rebuilds:
+                nl.positions = eng.list_positions()
+                nl.nupdates += rebuilds
+                rebuilt = True
             if stride is not None:
                 self._sync_atoms(calc, eng)
                 self.call_observers()

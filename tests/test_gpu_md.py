@@ -1,5 +1,5 @@
-"""Velocity Verlet on the device (pg_md_verlet) against ASE's update written
-out on the host around the same force evaluations.
+"""Velocity Verlet on the device (pg_md_run, pg_md_verlet) against ASE's
+update written out on the host around the same force evaluations.
 
 The host loop is VelocityVerlet.step of ase/md/verlet.py in NumPy:
 p += 0.5 dt F; r = r + dt p / m; F = calc.get_forces(); p += 0.5 dt F, with
@@ -68,6 +68,52 @@ def test_device_verlet_matches_the_host_loop_with_rebuilds(precision):
     np.testing.assert_array_equal(a_dev.get_momenta(), p_h)
     # the calculator answers for the final positions without a stale result
     np.testing.assert_array_equal(a_dev.get_forces(), calc_h.get_forces(a_host))
+
+
+def test_stop_at_rebuild_loop_matches_the_rebuilding_loop():
+    """pg_md_verlet (stops when a rebuild is due; the host rebuilds and calls
+    again) gives the trajectory of pg_md_run (rebuilds on the device), bit for
+    bit; lists installed from the host are refused by pg_md_run."""
+    from pysic_gb300 import _lib as L
+
+    dt, steps = 2.0 * FS, 30
+
+    def fresh():
+        a = _hot_silicon(seed=11)
+        c = pysic.Pysic(a, W.tersoff_si_potentials(), precision="mixed")
+        c.set_core()
+        c.engine.set_lanes(4)
+        c.get_forces()
+        eng = c.engine
+        eng.md_set_state(a.get_masses(), a.get_momenta())
+        return c, eng
+
+    c1, e1 = fresh()
+    nl = c1.get_neighbor_lists()
+    left, host_rebuilds = steps, 0
+    while left > 0:
+        done, rebuild = e1.md_verlet(L.PREC_MIXED, left, dt, nl.skin)
+        left -= done
+        if rebuild:
+            e1.build_neighbors(nl.cutoffs, nl.skin)
+            host_rebuilds += 1
+    p1, r1 = e1.md_get_state()
+
+    c2, e2 = fresh()
+    done, rebuilds = e2.md_run(L.PREC_MIXED, steps, dt, c2.get_neighbor_lists().skin)
+    p2, r2 = e2.md_get_state()
+    assert done == steps and rebuilds == host_rebuilds > 0
+    np.testing.assert_array_equal(r1, r2)
+    np.testing.assert_array_equal(p1, p2)
+    # the reference positions of the last list generation
+    lp = e2.list_positions()
+    assert np.abs(lp - r2).max() <= 0.5 * c2.get_neighbor_lists().skin
+
+    counts, idx, off = e2.neighbor_lists()
+    e2.install_neighbors(counts, idx, off, c2.get_neighbor_lists().skin)
+    with pytest.raises(L.EngineError) as err:
+        e2.md_run(L.PREC_MIXED, 2, dt, c2.get_neighbor_lists().skin)
+    assert err.value.status == L.PG_ERR_NOT_READY
 
 
 def test_observers_cut_the_run_without_changing_it():
