@@ -978,6 +978,61 @@ static void tri_term(const orc_model* m, int r, loop_job* J, int x, int c, int y
     st[5] += s1[0] * fc[1] + (s1[0] + s2[0]) * fy[1];
 }
 
+/* A pair record (r) of the picked pair (i = atom1, j = atom2) that depends on
+ * the charges or is a product, with the record's group of bond-order factors:
+ * V (v), the force on i from V (fp, without the cut factor) and the
+ * electronegativities of i and j (en); the energy v f (b_i + b_j + B_ij +
+ * B_ji) / 2 with the per-atom factors b and the pair factors B of the group
+ * (core_evaluate_local_doublet_energy_B, Core.f90:4257-4385), its forces with
+ * the factors' gradients (_forces_B, 5371-5606) and the electronegativities
+ * en f times the same mean factor (_electronegativities_B, 5622-5775). */
+static void scaled_charge_term(const ctx_t* X, loop_job* J, int r, int i, int j, double v, const double fp[3],
+                               const double en[2], const double sep[3], double d, const double dir[3]) {
+    const orc_system* s = X->s;
+    const orc_model* m = X->m;
+    const int grp = m->pair_group[r];
+    const int sm = X->smoothened[r];
+    const double rc = m->pair_cutoff[r], rs = X->smooth_soft[r];
+    const double cut = sm ? smooth_factor(d, rc, rs) : 1.0;
+    double sums[2];
+    pair_bo_sums(X, i, j, sep, d, grp, sums);
+    const double B1 = post_process(X, s->type[i], grp, sums[0]);
+    const double B2 = post_process(X, s->type[j], grp, sums[1]);
+    const double bsum = (saved_factor(X, grp, i) + saved_factor(X, grp, j) + B1 + B2) * 0.5;
+    if (J->what == 0) {
+        J->energy += v * cut * bsum;
+        return;
+    }
+    if (J->what == 2) {
+        J->chi[i] += en[0] * cut * bsum;
+        J->chi[j] += en[1] * cut * bsum;
+        return;
+    }
+    double* F = J->F;
+    double* st = J->stress;
+    afac_forces(X, grp, i, 0.5 * v * cut, F, st);
+    afac_forces(X, grp, j, 0.5 * v * cut, F, st);
+    pair_bo_forces(X, i, j, 0.5 * v * cut, sep, d, grp, sums, F, st);
+    double cg[3] = {0, 0, 0};
+    if (sm) {
+        const double dv = smooth_deriv(d, rc, rs);
+        for (int c = 0; c < 3; ++c) cg[c] = dir[c] * dv;
+    }
+    double p2[3];
+    for (int c = 0; c < 3; ++c) {
+        const double p1 = (fp[c] * cut + v * cg[c]) * bsum;
+        p2[c] = -p1;
+        F[3 * (size_t)i + c] += p1;
+        F[3 * (size_t)j + c] += p2[c];
+    }
+    st[0] += sep[0] * p2[0];
+    st[1] += sep[1] * p2[1];
+    st[2] += sep[2] * p2[2];
+    st[3] += sep[1] * p2[2];
+    st[4] += sep[0] * p2[2];
+    st[5] += sep[0] * p2[1];
+}
+
 /* The per-atom body of core_loop_over_local_interactions, Core.f90:3249-3946,
  * for atoms [a0, a1). Singlets: core_evaluate_local_singlet (4095-4239);
  * inline Ewald real space (3416-3460); doublets: core_evaluate_local_doublet_
@@ -1075,6 +1130,15 @@ static void* loop_range(void* arg) {
                 if (!(m->pair_cutoff[r] > d)) continue;
                 if (!has(m->pair_mask2[r], tj)) continue;
                 const int kind = m->pair_kind[r];
+                if (m->pair_group[r] >= 0 && ((m->pair_nmul && m->pair_nmul[r] > 0) || kind >= 7)) {
+                    /* a charge-dependent term or product scaled by bond-order factors
+                       (the doublet routines with bo_factors and pair_bo_factors,
+                       Core.f90:4257-4385, 5371-5606, 5622-5775) */
+                    double v, fp[3], en[2];
+                    product_term(m, r, ti, qi, s->charge[j], sep, d, &v, fp, en);
+                    scaled_charge_term(X, J, r, i, j, v, fp, en, sep, d, dir);
+                    continue;
+                }
                 if (m->pair_nmul && m->pair_nmul[r] > 0) {
                     /* a product of potentials (n_product > 1): the product's energy, force and
                        electronegativities times the record's smooth cut (Core.f90:4257-4385,

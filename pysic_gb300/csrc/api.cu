@@ -225,6 +225,7 @@ void enqueue_evaluation(pg_context* ctx, int precision, int flags, int G, const 
     const bool run_pair = ctx->have_pair_kernel_terms || ctx->ewald || ctx->have_singles || ctx->n_agroups > 0;
     const bool run_bond = ctx->have_bond_terms && (wantE || wantF);
     const bool run_tri = ctx->have_triplets && (wantE || wantF);
+    const bool run_bchi = ctx->have_bond_charge_terms && wantC;  // Tersoff-scaled charge terms' chi
     const int Gp = pair_lanes_for(ctx);
     FxAcc* acc = ctx->out_acc.p;
     bool first_f = true, first_chi = true;
@@ -234,7 +235,7 @@ void enqueue_evaluation(pg_context* ctx, int precision, int flags, int G, const 
     mark(0);
     // the totals are integers that every kernel adds to: clear them first (the
     // mixed path's displacement pass does it on the way)
-    if (precision == PG_PREC_MIXED && (run_pair || run_bond || run_tri)) launch_disp(ctx, skip, acc);
+    if (precision == PG_PREC_MIXED && (run_pair || run_bond || run_tri || run_bchi)) launch_disp(ctx, skip, acc);
     else PG_CUDA(cudaMemsetAsync(acc, 0, sizeof(FxAcc) * 8, ctx->stream));
     // per-atom bond-order factors: B and dB/dsum before the terms they scale
     const bool run_af = ctx->n_agroups > 0 && (wantE || wantF);
@@ -253,6 +254,7 @@ void enqueue_evaluation(pg_context* ctx, int precision, int flags, int G, const 
         launch_bond_order_impl(ctx, precision, flags, first_f, G, acc, [&] { mark(2); }, skip);
         if (wantF) first_f = false;
     } else {
+        if (run_bchi) launch_bond_b(ctx, precision, G, skip);  // the bonds' B for bond_chi
         mark(2);
     }
     if (run_tri) {
@@ -264,6 +266,10 @@ void enqueue_evaluation(pg_context* ctx, int precision, int flags, int G, const 
         launch_ewald_kspace_skip(ctx, precision, flags, first_f, first_chi, acc, skip);
         if (wantF) first_f = false;
         if (wantC) first_chi = false;
+    }
+    if (run_bchi) {
+        launch_bond_chi(ctx, precision, first_chi, skip);
+        first_chi = false;
     }
     mark(4);
     if (wantF && first_f) PG_CUDA(cudaMemsetAsync(ctx->out_f.p, 0, sizeof(double) * 3 * n, ctx->stream));
@@ -545,8 +551,6 @@ int pg_set_pair_products(pg_context* ctx, int32_t n_records, const int32_t* n_mu
         for (int r = 0; r < n_records; ++r) {
             pg::require(n_mul[r] >= 0 && n_mul[r] <= 8 && mul0[r] >= 0 && mul0[r] + n_mul[r] <= n_factors,
                         PG_ERR_INVALID, "product factors out of range (at most 8 factors besides the lead)");
-            pg::require(n_mul[r] == 0 || ctx->pr_group[r] < 0, PG_ERR_UNSUPPORTED,
-                        "bond-order scaled products of potentials are not evaluated by the GB300 engine");
         }
         for (int c = 0; c < n_factors; ++c)
             pg::require(kind[c] >= 0 && kind[c] <= 9, PG_ERR_UNSUPPORTED, "unknown pair potential kind in a product");

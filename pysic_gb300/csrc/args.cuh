@@ -93,6 +93,8 @@ struct BondArgs {
     FxAcc* acc;        // global energy / virial totals (null: not wanted)
     double* zeta_out;
     const int* skip;   // optional device flag: nonzero = do nothing
+    const double* q;   // FP64 charges (the mixed path reads the FP32 copy in disp .w)
+    void* b_out;       // per entry: B of the bond (R; null: not kept), for the electronegativity pass
 };
 
 struct DispArgs {

@@ -86,7 +86,7 @@ void size_buffers(pg_batch* b, int precision) {
         require(c->device == b->device, PG_ERR_INVALID, "every system of a batch must live on the batch's device");
         settle_coordinates(c);
         prepare(c);
-        require(!c->ewald && !c->have_triplets && c->n_agroups == 0, PG_ERR_UNSUPPORTED,
+        require(!c->ewald && !c->have_triplets && c->n_agroups == 0 && !c->have_bond_charge_terms, PG_ERR_UNSUPPORTED,
                 "the many-system launch covers pair and Tersoff bond-order terms; evaluate Ewald, three-body or "
                 "per-atom bond-order systems one by one");
         const size_t n = (size_t)std::max(c->n, 1);

@@ -41,4 +41,32 @@ struct Vec2T<double> {
     using T = double2;
 };
 
+// A bond-order scaled charge-dependent or product term of short-list entry
+// `ent` (atom i -> its partner): V f, d(V f)/dr and f times the
+// electronegativity of atom i (-dV/dq_i), with the pair's atom1 as the
+// reference's loop picks it (pick on the entry's image offset) and the charges
+// of both atoms (FP64 charges, or the FP32 copy of the mixed path).
+template <typename R>
+__device__ __forceinline__ void bond_charge_term(const BondArgs& A, const PairT<R>& PT, const PairT<R>* terms, int i,
+                                                 int ent, int ti, int tj, R r, R& V, R& dV, R& en) {
+    const int j = A.idx[ent];
+    const bool first = pick(i, j, A.off[3 * ent], A.off[3 * ent + 1], A.off[3 * ent + 2]);
+    R qi, qj;
+    if constexpr (sizeof(R) == 4) {
+        qi = A.disp[i].w;
+        qj = A.disp[j].w;
+    } else {
+        qi = A.q[i];
+        qj = A.q[j];
+    }
+    product_value<R>(PT, terms, (const R*)A.tab, r, qi, qj, first, ti, tj, V, dV, en);
+    if (PT.smooth) {
+        R f, fp;
+        smooth<R>(r, PT.rc, PT.rs, f, fp);
+        dV = dV * f + V * fp;
+        V *= f;
+        en *= f;
+    }
+}
+
 }  // namespace pg

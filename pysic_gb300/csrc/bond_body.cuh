@@ -232,6 +232,7 @@ __device__ __forceinline__ void bond_body(const BondArgs& A, int blk, int nblk) 
             if (A.zeta_out) A.zeta_out[s + e] = (double)zeta;
             if (!any || r == R(0)) {
                 bacc[e] = V4{0, 0, 0, 0};
+                if (A.b_out) ((R*)A.b_out)[s + e] = R(1);
                 continue;
             }
             if (bo) {
@@ -241,6 +242,7 @@ __device__ __forceinline__ void bond_body(const BondArgs& A, int blk, int nblk) 
                     dB = 1;
                 }
             }
+            if (A.b_out) ((R*)A.b_out)[s + e] = B;
             R U = 0, dU = 0, P = 0;
             if constexpr (SPEC) {
                 // exponential terms p0 exp(-p1 r) with the bond-order cutoff
@@ -275,7 +277,10 @@ __device__ __forceinline__ void bond_body(const BondArgs& A, int blk, int nblk) 
                 const PairT<R>& PT = terms[t];
                 if (!PT.in_bond_kernel || !(r < PT.rc)) continue;
                 R V, dV;
-                if (PT.smooth && PT.rc == bc.x && PT.rs == bc.y) {
+                if (PT.kind >= 7 || PT.nmul > 0) {  // charge-dependent or product (bond-order scaled)
+                    R en;
+                    bond_charge_term<R>(A, PT, terms, i, s + e, ti, tj, r, V, dV, en);
+                } else if (PT.smooth && PT.rc == bc.x && PT.rs == bc.y) {
                     pair_eval<R>(PT, r, V, dV, (const R*)A.tab);
                     const V2 fc = cut[e];
                     dV = dV * fc.x + V * fc.y;

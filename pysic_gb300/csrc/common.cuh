@@ -352,6 +352,8 @@ struct pg_context {
     std::vector<double> pm_params;
     std::vector<uint64_t> pm_first;
     bool have_charge_pairs = false;    // a charge-dependent pair term (charge_pair)
+    bool have_bond_charge_terms = false;  // a Tersoff-scaled charge-dependent or product term
+    pg::DevBuf<double> bo_b;           // per short entry: B of the bond (R), for bond_chi
     pg::DevBuf<double> d_tab64;        // the rows on the device, FP64 and FP32
     pg::DevBuf<float> d_tab32;
     pg::DevBuf<pg::TripT<double>> d_trip;  // n_types^3
@@ -619,6 +621,8 @@ void md_run_rebuilding(pg_context* ctx, int precision, int n_steps, double dt, d
 void evaluate(pg_context* ctx, int precision, int flags);
 // api.cu: lanes per atom of the pair kernel for this context's list lengths
 int pair_lanes_for(const pg_context* ctx);
+void launch_bond_b(pg_context* ctx, int precision, int G, const int* skip);
+void launch_bond_chi(pg_context* ctx, int precision, bool first, const int* skip);
 // pair.cu: the fixed real-space Ewald electronegativity matrix of a relaxation loop
 bool chi_cache_prepare(pg_context* ctx, int precision);
 void launch_chi_cache_apply(pg_context* ctx, int precision, const int* skip);

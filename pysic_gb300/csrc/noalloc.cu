@@ -58,10 +58,11 @@ void bond_order_noalloc(pg_context* ctx, int precision, double* d_forces, double
     require(precision == PG_PREC_FP64 || precision == PG_PREC_MIXED, PG_ERR_INVALID, "unknown precision");
     require(d_forces != nullptr && d_totals != nullptr, PG_ERR_INVALID, "null output pointer");
     require(ctx->have_bond_terms, PG_ERR_NOT_READY, "no bond-order factors");
-    require(!ctx->have_pair_kernel_terms && !ctx->ewald && !ctx->have_singles && !ctx->have_triplets,
+    require(!ctx->have_pair_kernel_terms && !ctx->ewald && !ctx->have_singles && !ctx->have_triplets &&
+                !ctx->have_bond_charge_terms,
             PG_ERR_UNSUPPORTED,
             "the no-allocation call covers contexts whose every term runs in the bond-order kernels "
-            "(no Ewald, single-atom or out-of-bond pair terms)");
+            "(no Ewald, single-atom, out-of-bond pair or charge-dependent terms)");
     // everything the regular path builds lazily must already exist
     require(ctx->have_list && !ctx->tables_dirty && ctx->sep0_epoch == ctx->list_epoch && !ctx->short_dirty,
             PG_ERR_NOT_READY,

@@ -18,66 +18,6 @@ __device__ __forceinline__ double powi_(double x, int n) {
     return r;
 }
 
-// One factor of a product of potentials for the pair (i, j): its value V, dV/dr
-// and its electronegativity of atom i (-dV/dq_i), without any cut factor
-// (evaluate_energy_component / _force_component /
-// _electronegativity_component, Potentials.f90:2512-2890).  first: i is the
-// pair's atom1 as the reference's loop picks it; charge-dependent factors take
-// the parameters of the product's first target on atom1 when its type is that
-// target's, as their plain records do below.
-template <typename R>
-__device__ __forceinline__ void factor_raw(const PairT<R>& P, const PairArgs& A, R r, R qi, R qj, bool first, int ti,
-                                           int tj, R& V, R& dV, R& en) {
-    en = R(0);
-    if (P.kind < 7) {
-        pair_eval<R>(P, r, V, dV, (const R*)A.tab);
-        return;
-    }
-    dV = R(0);
-    const R q1 = first ? qi : qj, q2 = first ? qj : qi;
-    const bool direct = (P.first >> (first ? ti : tj)) & 1ull;
-    if (P.kind == 7) {  // charge_pair
-        const int n1 = direct ? (int)P.p1 : (int)P.p2, n2 = direct ? (int)P.p2 : (int)P.p1;
-        V = P.p0 * (ipow(q1, n1) * ipow(q2, n2));
-        const int nm = first ? n1 : n2;
-        if (nm > 0)
-            en = -(first ? P.p0 * (R(n1) * ipow(q1, n1 - 1) * ipow(q2, n2))
-                         : P.p0 * (R(n2) * ipow(q1, n1) * ipow(q2, n2 - 1)));
-    } else if (P.kind == 8) {  // charge_exp
-        const R* c = (const R*)A.tab + 2 * (long long)P.t0;
-        const int a1 = direct ? 0 : 4, a2 = direct ? 4 : 0;
-        const R eta1 = c[direct ? 11 : 12], eta2 = c[direct ? 12 : 11];
-        const R beta1 = c[direct ? 13 : 14], beta2 = c[direct ? 14 : 13];
-        const R xi1 = c[direct ? 9 : 10], xi2 = c[direct ? 10 : 9];
-        const R d5 = beta1 * (c[3 + a1] - q1), d6 = beta2 * (c[3 + a2] - q2);
-        const R D1 = c[1 + a1] + pow_(fabs(d5), eta1), D2 = c[1 + a2] + pow_(fabs(d6), eta2);
-        V = c[0] * exp_(R(0.5) * (xi1 * D1 + xi2 * D2));
-        en = first ? V * xi1 * R(0.5) * eta1 * pow_(fabs(d5), eta1 - R(1)) * copysign(R(1), d5) * beta1
-                   : V * xi2 * R(0.5) * eta2 * pow_(fabs(d6), eta2 - R(1)) * copysign(R(1), d6) * beta2;
-    } else {  // charge_abs
-        const R* c = (const R*)A.tab + 2 * (long long)P.t0;
-        const R* s1 = c + (direct ? 0 : 4);
-        const R* s2 = c + (direct ? 4 : 0);
-        const R ab1 = fabs(q1 - s1[2]), ab2 = fabs(q2 - s2[2]);
-        const R pw1 = pow_(ab1, s1[3] - R(1)), pw2 = pow_(ab2, s2[3] - R(1));
-        R f1 = s1[0] + s1[1] * ab1 * pw1, f2 = s2[0] + s2[1] * ab2 * pw2;
-        R is = R(0.5) / sqrt_(f1 * f2);
-        if (f1 < R(0)) {
-            f1 = R(0);
-            is = R(0);
-        }
-        if (f2 < R(0)) {
-            f2 = R(0);
-            is = R(0);
-        }
-        const R e1 = fmax(s1[0] + s1[1] * pow_(ab1, s1[3]), R(0));
-        const R e2 = fmax(s2[0] + s2[1] * pow_(ab2, s2[3]), R(0));
-        V = sqrt_(e1 * e2);
-        en = first ? is * (-s1[3] * pw1 * copysign(R(1), q1 - s1[2]) * s1[1]) * f2
-                   : is * (-s2[3] * pw2 * copysign(R(1), q2 - s2[2]) * s2[1]) * f1;
-    }
-}
-
 // AF: also add the per-atom factor forces (no scaled pair term; W from af_sum)
 template <typename R, int G, bool AF = false>
 __device__ __forceinline__ void pair_body(const PairArgs& A, int blk) {
@@ -136,22 +76,12 @@ __device__ __forceinline__ void pair_body(const PairArgs& A, int blk) {
                 const PairT<R> P = ((const PairT<R>*)A.terms)[t];
                 if (P.in_bond_kernel || !(r < P.rc)) continue;
                 if (P.nmul > 0) {
-                    // a product of potentials: V = prod V_k, V' and the electronegativity by
-                    // the product rule (each factor's with the product of the others),
-                    // then the record's smooth cut (Potentials.f90:2512-2700)
+                    // a product of potentials (Potentials.f90:2512-2700), then the
+                    // record's smooth cut
                     const bool first = pick(i, j, A.off[3 * e], A.off[3 * e + 1], A.off[3 * e + 2]);
-                    const R qj = charge_of<R>(A, j);
-                    const PairT<R>* TT = (const PairT<R>*)A.terms;
-                    // running product rule: after factor k, V = prod_{q<=k} V_q and dV, en
-                    // the derivatives of that partial product
-                    R V = R(1), dV = R(0), en = R(0);
-                    for (int k = 0; k <= P.nmul; ++k) {
-                        R ek, dk, nk;
-                        factor_raw<R>(k == 0 ? P : TT[P.mul0 + k - 1], A, r, qi, qj, first, ti, tj, ek, dk, nk);
-                        dV = dV * ek + V * dk;
-                        en = en * ek + V * nk;
-                        V *= ek;
-                    }
+                    R V, dV, en;
+                    product_value<R>(P, (const PairT<R>*)A.terms, (const R*)A.tab, r, qi, charge_of<R>(A, j), first,
+                                     ti, tj, V, dV, en);
                     R f = R(1), fp = R(0);
                     if (P.smooth) smooth<R>(r, P.rc, P.rs, f, fp);
                     U += V * f;

@@ -145,6 +145,9 @@ static void enqueue_chi(pg_context* ctx, int precision, const int* skip, bool ca
         launch_pair_kernel_skip(ctx, precision, PG_WANT_ENEGS, true, true, G, nullptr, skip);
     }
     if (ctx->ewald) launch_ewald_kspace_skip(ctx, precision, PG_WANT_ENEGS, true, false, nullptr, skip);
+    // Tersoff-scaled charge terms: B of every bond is fixed while the
+    // positions are, kept from the loop's start
+    if (ctx->have_bond_charge_terms) launch_bond_chi(ctx, precision, false, skip);
 }
 
 // results of a finished loop to the host; not converging is an error status
@@ -222,6 +225,10 @@ void relax_charges(pg_context* ctx, int precision, int mode, int n_steps, double
         A.disp = ctx->disp32.p;
     }
     const bool cached = chi_cache_prepare(ctx, precision);
+    if (ctx->have_bond_charge_terms) {  // the bonds' B, fixed with the positions
+        int G = ctx->lanes != 0 ? ctx->lanes : ctx->tuned_lanes[precision];
+        launch_bond_b(ctx, precision, G == 0 ? 8 : G, nullptr);
+    }
     // initial differences (relaxation.py:433) and the first update; the
     // potentiostat subtracts its fixed potential instead of the mean
     enqueue_chi(ctx, precision, A.flag, cached);

@@ -120,7 +120,7 @@ void fold_tables(pg_context* ctx) {
     std::vector<PairT<double>> terms;
     std::vector<PairT<double>> factors;  // product factors, appended after every type pair's records
     std::vector<int2> index((size_t)T * T, make_int2(0, 0));
-    bool pair_kernel_terms = false, charge_pairs = false;
+    bool pair_kernel_terms = false, charge_pairs = false, bond_charge_terms = false;
     // one pair term from a kind and 4 parameters (table rows checked here: the
     // kernels index rows t0 .. t0 + tn - 1 only)
     auto fill_params = [&](PairT<double>& t, const double* p4) {
@@ -157,7 +157,9 @@ void fold_tables(pg_context* ctx) {
                 t.group = g >= 0 && g == tersoff_gid ? 0 : -1;
                 t.agroup = g >= 0 && g != tersoff_gid ? gmap.at(g) : -1;
                 require(!(t.agroup >= 0 && t.kind >= 7), PG_ERR_UNSUPPORTED,
-                        "bond-order scaling of charge_pair is not evaluated by the GB300 engine");
+                        "per-atom bond-order scaling of charge-dependent terms is not evaluated by the GB300 engine");
+                require(!(t.agroup >= 0 && have_products && ctx->pr_nmul[r] > 0), PG_ERR_UNSUPPORTED,
+                        "per-atom bond-order scaling of products is not evaluated by the GB300 engine");
                 fill_params(t, &ctx->pr_params[4 * (size_t)r]);
                 t.first = r < (int)ctx->pr_first.size() ? ctx->pr_first[r] : 0ull;
                 t.rc = ctx->pr_cut[r];
@@ -183,9 +185,13 @@ void fold_tables(pg_context* ctx) {
                     t.smooth = 0;
                     t.rs = t.rc;
                 }
-                // charge-dependent pair terms stay in the pair kernel (electronegativities)
-                t.in_bond_kernel =
-                    bond && t.kind < 7 && t.nmul == 0 && t.agroup < 0 && (t.group >= 0 || t.rc <= bo_radius);
+                // unscaled charge-dependent and product terms stay in the pair kernel;
+                // Tersoff-scaled ones go to the bond-order kernels, which then also
+                // give their electronegativities (bond_chi)
+                const bool qterm = t.kind >= 7 || t.nmul > 0;
+                t.in_bond_kernel = bond && t.agroup < 0 &&
+                                   (qterm ? t.group >= 0 : (t.group >= 0 || t.rc <= bo_radius));
+                if (t.in_bond_kernel && qterm) bond_charge_terms = true;
                 if (t.kind >= 7) charge_pairs = true;
                 if (!t.in_bond_kernel) pair_kernel_terms = true;
                 terms.push_back(t);
@@ -232,6 +238,7 @@ void fold_tables(pg_context* ctx) {
     }
     ctx->have_pair_kernel_terms = pair_kernel_terms;
     ctx->have_charge_pairs = charge_pairs;
+    ctx->have_bond_charge_terms = bond_charge_terms;
 
     // Single-species Tersoff (one type, one triplet, exponential pair terms that
     // all share the bond-order cutoff): the bond-order kernels take every

@@ -47,6 +47,45 @@
 namespace pg {
 
 
+// Electronegativities of the Tersoff-scaled charge-dependent and product
+// terms (core_evaluate_local_doublet_electronegativities_B with bond-order
+// factors, Core.f90:5622-5775): per atom i and short-list entry i -> j,
+// chi_i += -dV/dq_i f (B_ij + B_ji) / 2, the B of both directions kept by the
+// bond pass (B[e], B[rev e]).  One thread per atom; the sum is a gather.
+template <typename R>
+__global__ void bond_chi(const __grid_constant__ BondArgs A, const R* __restrict__ B, int first,
+                         double* __restrict__ out_chi) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= A.n) return;
+    if (A.skip && *A.skip) return;
+    const PairT<R>* terms = (const PairT<R>*)A.terms;
+    const int ti = A.type[i];
+    const int s = A.start[i], s1 = A.start[i + 1];
+    double xi = 0, yi = 0, zi = 0;
+    if constexpr (sizeof(R) == 8) {
+        xi = A.pos[3 * i];
+        yi = A.pos[3 * i + 1];
+        zi = A.pos[3 * i + 2];
+    }
+    R chi = 0;
+    for (int e = s; e < s1; ++e) {
+        const auto g = bond_vector<R>(A, i, e, xi, yi, zi);
+        const R r = g.w;
+        if (r == R(0)) continue;
+        const int tj = A.etype[e];
+        const int2 ix = A.index[ti * A.T + tj];
+        const R bsum = R(0.5) * (B[e] + B[A.rev[e]]);
+        for (int t = ix.x; t < ix.x + ix.y; ++t) {
+            const PairT<R>& PT = terms[t];
+            if (!PT.in_bond_kernel || PT.group < 0 || !(PT.kind >= 7 || PT.nmul > 0) || !(r < PT.rc)) continue;
+            R V, dV, en;
+            bond_charge_term<R>(A, PT, terms, i, e, ti, tj, r, V, dV, en);
+            chi += en * bsum;
+        }
+    }
+    out_chi[i] = first ? (double)chi : out_chi[i] + (double)chi;
+}
+
 __global__ void disp_pass(const __grid_constant__ DispArgs A) {
     pdl_trigger();
     disp_body(A, blockIdx.x * blockDim.x + threadIdx.x);
@@ -107,6 +146,7 @@ static size_t bond_stride(pg_context* ctx) {
 
 void prepare_bond_scratch(pg_context* ctx, int precision) {
     const size_t ne = bond_stride(ctx);
+    if (ctx->have_bond_charge_terms) ctx->bo_b.resize(ne);
     // per short-list entry: bond geometry | force from the partner's bonds | k-part
     // sums | unstaged j parts
     if (precision == PG_PREC_FP64) ctx->bo_fj64.resize(4 * ne);
@@ -182,6 +222,8 @@ BondArgs make_bond_args(pg_context* ctx, int precision, int flags, bool first_f,
     A.out_f = ctx->out_f.p;
     A.acc = acc;
     A.zeta_out = nullptr;
+    A.q = ctx->charge.p;
+    A.b_out = nullptr;
     return A;
 }
 
@@ -222,6 +264,7 @@ void launch_bond_order_impl(pg_context* ctx, int precision, int flags, bool firs
     prepare_bond_scratch(ctx, precision);
     BondArgs A = make_bond_args(ctx, precision, flags, first_f, acc);
     A.skip = skip;
+    if (ctx->have_bond_charge_terms) A.b_out = ctx->bo_b.p;  // kept for bond_chi
     const bool forces = (flags & PG_WANT_FORCES) != 0;
     if (precision == PG_PREC_FP64) launch_by_lanes<double>(A, ctx->n, ctx->stream, G, forces, between);
     else launch_by_lanes<float>(A, ctx->n, ctx->stream, G, forces, between);
@@ -253,6 +296,34 @@ void launch_bond_order_scratch(pg_context* ctx, int precision, int G, void* bond
         launch_by_lanes<float>(A, ctx->n, ctx->stream, G, true, none);
     }
     PG_CHECK_LAUNCH();
+}
+
+// The bond pass for its B values only (no totals, no forces): the
+// electronegativity pass of a relaxation, whose positions stay fixed, needs
+// them once per loop.
+void launch_bond_b(pg_context* ctx, int precision, int G, const int* skip) {
+    prepare_bond_scratch(ctx, precision);
+    BondArgs A = make_bond_args(ctx, precision, PG_WANT_ENERGY, true, nullptr);
+    A.skip = skip;
+    A.b_out = ctx->bo_b.p;
+    auto none = [] {};
+    if (precision == PG_PREC_FP64) launch_by_lanes<double>(A, ctx->n, ctx->stream, G, false, none);
+    else launch_by_lanes<float>(A, ctx->n, ctx->stream, G, false, none);
+    PG_CHECK_LAUNCH();
+    ctx->launches++;
+}
+
+// bond_chi into out_chi (written when first, added otherwise)
+void launch_bond_chi(pg_context* ctx, int precision, bool first, const int* skip) {
+    BondArgs A = make_bond_args(ctx, precision, PG_WANT_ENEGS, true, nullptr);
+    A.skip = skip;
+    const int blocks = (ctx->n + 127) / 128;
+    if (precision == PG_PREC_FP64)
+        bond_chi<double><<<blocks, 128, 0, ctx->stream>>>(A, (const double*)ctx->bo_b.p, first ? 1 : 0, ctx->out_chi.p);
+    else
+        bond_chi<float><<<blocks, 128, 0, ctx->stream>>>(A, (const float*)ctx->bo_b.p, first ? 1 : 0, ctx->out_chi.p);
+    PG_CHECK_LAUNCH();
+    ctx->launches++;
 }
 
 void launch_disp(pg_context* ctx, const int* skip, FxAcc* zero8) {

@@ -190,6 +190,7 @@ __device__ __forceinline__ void tri_atom(const BondArgs& A, int gslot, TriStage<
         }
         const R zeta = group_sum<4>(zp);
         if (A.zeta_out && ve && b == 0) A.zeta_out[s + e] = (double)zeta;
+        if (A.b_out && ve && b == 0 && (!any || r == R(0))) ((R*)A.b_out)[s + e] = R(1);
         if (!ve || !any || r == R(0)) continue;
         R B = 1, dB = 0;
         if (bo) {
@@ -203,6 +204,7 @@ __device__ __forceinline__ void tri_atom(const BondArgs& A, int gslot, TriStage<
                 dB = 1;
             }
         }
+        if (A.b_out && b == 0) ((R*)A.b_out)[s + e] = B;
         R U = 0, dU = 0, P = 0;
         if constexpr (SPEC) {
             R f, fp;
@@ -235,7 +237,10 @@ __device__ __forceinline__ void tri_atom(const BondArgs& A, int gslot, TriStage<
                 const PairT<R>& PT = terms[q];
                 if (!PT.in_bond_kernel || !(r < PT.rc)) continue;
                 R V, dV;
-                if (PT.smooth && PT.rc == bc.x && PT.rs == bc.y) {
+                if (PT.kind >= 7 || PT.nmul > 0) {  // charge-dependent or product (bond-order scaled)
+                    R en;
+                    bond_charge_term<R>(A, PT, terms, i, s + e, ti, tj, r, V, dV, en);
+                } else if (PT.smooth && PT.rc == bc.x && PT.rs == bc.y) {
                     pair_eval<R>(PT, r, V, dV, (const R*)A.tab);
                     const V2 fc = S.cut[e];
                     dV = dV * fc.x + V * fc.y;

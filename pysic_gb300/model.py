@@ -252,6 +252,12 @@ def compile_model(atoms, potentials, coulomb=None):
                 return g
         return -1
 
+    def pair_level(g):
+        """a group of pair (Tersoff) bond-order factors, which the bond-order
+        kernels evaluate with any pair term they scale"""
+        return g >= 0 and all(core.level_of_factor(b.get_bond_order_type()) == 2
+                              for b in coords[g].get_bond_order_parameters())
+
     def pair_params_of(kind, params):
         """the parameters of one pair term as the engine stores them"""
         if kind == "tabulated":
@@ -280,8 +286,8 @@ def compile_model(atoms, potentials, coulomb=None):
             if nt != 2:
                 raise InvalidPotentialError("products of {0}-body potentials are not evaluated by the GB300 engine"
                                             .format(nt))
-            if grp >= 0:
-                raise InvalidPotentialError("bond-order scaled products of potentials are not evaluated by the "
+            if grp >= 0 and not pair_level(grp):
+                raise InvalidPotentialError("products scaled by per-atom bond-order factors are not evaluated by the "
                                             "GB300 engine")
             lead_first = next((t for t in (pot.get_symbols(), pot.get_tags(), pot.get_indices()) if t), None)
             if lead_first is None:
@@ -289,7 +295,9 @@ def compile_model(atoms, potentials, coulomb=None):
             t0 = lead_first[0][0]
             fmask = _mask(sigs, *((t0, None, None) if pot.get_symbols() else
                                   (None, int(t0), None) if pot.get_tags() else (None, None, int(t0))))
-            for fac in factors[1:]:
+            # the reference registers a product's factors last to first and the core
+            # keeps them in that order (calculator.py:1208-1213, Core.f90:925-944)
+            for fac in reversed(factors[1:]):
                 fk = fac.get_potential_type()
                 core.check_engine_support(fk)
                 if fk not in core.PAIR_KIND:
@@ -316,8 +324,9 @@ def compile_model(atoms, potentials, coulomb=None):
             if kind not in core.PAIR_KIND:
                 raise InvalidPotentialError("'{0}' is not a pair potential of the GB300 engine".format(kind))
             params = pair_params_of(kind, params)
-            if kind in ("charge_pair", "charge_exp", "charge_abs") and grp >= 0:
-                raise InvalidPotentialError("bond-order scaling of {0} is not evaluated by the GB300 engine".format(kind))
+            if kind in ("charge_pair", "charge_exp", "charge_abs") and grp >= 0 and not pair_level(grp):
+                raise InvalidPotentialError("per-atom bond-order scaling of {0} is not evaluated by the GB300 engine"
+                                            .format(kind))
             for tg, first in zip(targets, firsts):
                 M.pair_first.append(_mask(sigs, *first))
                 M.pair_kind.append(core.PAIR_KIND[kind])

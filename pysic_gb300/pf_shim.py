@@ -173,8 +173,9 @@ class PysicInterface:
     def add_potential(self, pot_name, parameters, cutoff, smooth_cut, elements, tags, indices, orig_elements,
                       orig_tags, orig_indices, pot_index, is_multiplier):
         """One interaction record, targets already permuted by the caller
-        (calculator.py:1255-1360).  Returns the success flag; products of
-        potentials (is_multiplier) are not evaluated by this engine."""
+        (calculator.py:1255-1360).  Returns the success flag.  Factors of a
+        product (is_multiplier) are kept, in arrival order, and attached to
+        every following record until clear_potential_multipliers."""
         name = str(pot_name)
         if name not in core.POTENTIALS:
             return False
@@ -266,6 +267,10 @@ class PysicInterface:
         gids = sorted({b["group"] for b in bonds})
         gmap = {g: k for k, g in enumerate(gids)}
         M.n_groups = len(gids)
+        # groups of pair (Tersoff) factors only: the bond-order kernels scale any pair term with them
+        pair_level = {gmap[g] for g in gids
+                      if all(core.level_of_factor(b["name"]) == 2 for b in bonds if b["group"] == g)}
+        mul_blocks = {}  # first factor record of each product's factor list
         for rec in pots:
             kind = rec["name"]
             core.check_engine_support(kind)
@@ -275,8 +280,8 @@ class PysicInterface:
             if nt == 2:
                 if kind not in core.PAIR_KIND:
                     raise core.InvalidPotentialError("'{0}' is not a pair potential of the GB300 engine".format(kind))
-                if kind in ("charge_pair", "charge_exp", "charge_abs") and grp >= 0:
-                    raise core.InvalidPotentialError("bond-order scaling of {0} is not evaluated by the GB300 "
+                if kind in ("charge_pair", "charge_exp", "charge_abs") and grp >= 0 and grp not in pair_level:
+                    raise core.InvalidPotentialError("per-atom bond-order scaling of {0} is not evaluated by the GB300 "
                                                      "engine".format(kind))
                 if kind == "tabulated":
                     params = _table_record(M, params)
@@ -295,12 +300,16 @@ class PysicInterface:
                 M.pair_mask2.append(mask(target(rec, 1)))
                 M.pair_group.append(grp)
                 muls = rec.get("multipliers", [])
+                key = tuple(id(mr) for mr in muls)
+                shared = key in mul_blocks  # every permuted record of one product shares its factors
                 M.pair_nmul.append(len(muls))
-                M.pair_mul0.append(len(M.mul_kind))
-                if muls and grp >= 0:
-                    raise core.InvalidPotentialError("bond-order scaled products of potentials are not evaluated by "
+                M.pair_mul0.append(mul_blocks[key] if shared else len(M.mul_kind))
+                if muls and not shared:
+                    mul_blocks[key] = len(M.mul_kind)
+                if muls and grp >= 0 and grp not in pair_level:
+                    raise core.InvalidPotentialError("products scaled by per-atom bond-order factors are not evaluated by "
                                                      "the GB300 engine")
-                for mr in muls:
+                for mr in ([] if shared else muls):
                     mk = mr["name"]
                     core.check_engine_support(mk)
                     if mk not in core.PAIR_KIND:

@@ -260,3 +260,35 @@ def dihedral_cases():
                                P("bond_bend", symbols=[["O", "Si", "O"]], parameters=[0.2, 1.9, 1, 2], cutoff=2.6,
                                  cutoff_margin=0.4),
                                P("exponential", symbols=[["Si", "O"]], parameters=[5.0, 1.5], cutoff=2.6)]
+
+
+def comb_style_cases():
+    """Tersoff bond-order factors scaling charge-dependent products, the form
+    of COMB's attraction (pysic/interactions/comb.py:660-900: charge_exp x
+    charge_abs x exponential with a Coordinator of 'tersoff' factors), on a
+    random SiO2 box with random charges: one Coordinator over every Si / O
+    triplet (the post-processing beta, eta shared by each centre element),
+    the scaled product on Si-O and O-O pairs, a scaled charge_exp on Si-Si
+    pairs, and an unscaled repulsion.  Energies, forces, virial and
+    electronegativities all depend on the bond orders and the charges."""
+    P = Potential
+    from .interactions import ProductPotential
+
+    a = sio2_box(12, seed=61)
+    q = np.random.default_rng(62).normal(0.0, 0.5, len(a))
+    a.set_initial_charges(q - q.mean())
+    sio = [[x, y, z] for x in ("Si", "O") for y in ("Si", "O") for z in ("Si", "O")]
+    bo = BondOrderParameters("tersoff", cutoff=3.0, cutoff_margin=0.6, symbols=sio,
+                             parameters=[[0.8, 0.9], [0.0, 2.0, 1.5, -0.4, 1.0]])
+    crd = Coordinator([bo])
+    cexp = P("charge_exp", symbols=[["Si", "O"], ["O", "O"]],
+             parameters=[0.3, 2.0, 1.0, 2.0, 1.0, 3.0, 1.5, 2.4, 1.2, 0.6, 0.4], cutoff=3.0, cutoff_margin=0.6)
+    cabs = P("charge_abs", symbols=[["Si", "O"], ["O", "O"]], parameters=[1.2, 0.3, 0.2, 2.0, 1.5, 0.4, -0.3, 2.0])
+    expo = P("exponential", symbols=[["Si", "O"], ["O", "O"]], parameters=[-8.0, 1.2])
+    prod = ProductPotential([cexp, cabs, expo])
+    prod.set_coordinator(crd)
+    si = P("charge_exp", symbols=[["Si", "Si"]], parameters=[-0.5, 2.0, 1.0, 2.0, 1.0, 3.0, 1.5, 2.4, 1.2, 0.6, 0.4],
+           cutoff=3.0, cutoff_margin=0.6, coordinator=crd)
+    rep = P("exponential", symbols=[["Si", "O"], ["O", "O"], ["Si", "Si"]], parameters=[30.0, 2.5], cutoff=3.0,
+            cutoff_margin=0.6)
+    yield "comb_attraction", a, [prod, si, rep]

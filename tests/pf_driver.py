@@ -42,6 +42,14 @@ def load(pi, atoms, pots, coulomb=None):
             if c is not None else -1
         nt = p.get_number_of_targets()
         none = np.array(nt * [-9])
+        # a product's factors first, last to first, once each with the first
+        # unpermuted target tuple (calculator.py:1208-1213, 1255-1280)
+        for fac in reversed(p.get_potentials()[1:]):
+            t = p.get_symbols()[0]
+            assert pi.add_potential(fac.get_potential_type(), np.array(fac.get_parameter_values()), p.get_cutoff(),
+                                    p.get_soft_cutoff(), np.array([codes(s) for s in t]).T, none, none,
+                                    np.array([codes(s) for s in t]).T, none, none, grp, True)
+        p = p.get_potentials()[0] if len(p.get_potentials()) > 1 else p
         for t in p.get_symbols() or []:
             for perm in _perms(t):
                 assert pi.add_potential(p.get_potential_type(), np.array(p.get_parameter_values()), p.get_cutoff(),
@@ -57,6 +65,7 @@ def load(pi, atoms, pots, coulomb=None):
                 assert pi.add_potential(p.get_potential_type(), np.array(p.get_parameter_values()), p.get_cutoff(),
                                         p.get_soft_cutoff(), np.array(nt * [codes("xx")]).T, none, np.array(perm),
                                         np.array(nt * [codes("xx")]).T, none, np.array(t), grp, False)
+        pi.clear_potential_multipliers()
     pi.allocate_bond_order_factors(0)
     for c, g in coords:
         for b in c.get_bond_order_parameters():

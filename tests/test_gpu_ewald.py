@@ -331,3 +331,42 @@ def test_charge_abs_parity():
     mixed = engine_all(atoms, pots, coul, "mixed")
     assert abs(mixed["energy"] - ref["energy"]) / len(atoms) <= 1e-5
     assert np.abs(mixed["enegs"] - ref["enegs"]).max() < 1e-4
+
+
+def test_tersoff_scaled_charge_products_parity_and_relaxation():
+    """A Tersoff Coordinator on charge-dependent products and on a charge_exp
+    (COMB's attraction form, comb.py:660-900), evaluated in the bond-order
+    kernels: FP64 energy, forces, virial and electronegativities against the
+    oracle (energy 1e-11 relative, forces 1e-9 of the largest, virial 1e-9,
+    electronegativities 1e-9), mixed precision within 1e-5 eV/atom, 1e-4 of
+    the largest force and 1e-4 eV/e, and the damped relaxation on these
+    electronegativities (bond orders fixed with the positions) against the
+    oracle's loop: same steps, charges within 1e-8 e."""
+    _, atoms, pots = next(W.comb_style_cases())
+    ref = oracle_all(atoms, pots)
+    for lanes in (4, 8, 64):
+        got = engine_all(atoms, pots, None, "fp64", lanes)
+        assert got["energy"] == pytest.approx(ref["energy"], rel=1e-11)
+        assert np.abs(got["forces"] - ref["forces"]).max() < 1e-9 * max(1.0, np.abs(ref["forces"]).max())
+        np.testing.assert_allclose(got["stress"], ref["stress"], rtol=1e-9, atol=1e-9 * np.abs(ref["stress"]).max())
+        assert np.abs(got["enegs"] - ref["enegs"]).max() < 1e-9
+    mixed = engine_all(atoms, pots, None, "mixed")
+    fmax = max(1.0, np.abs(ref["forces"]).max())
+    assert abs(mixed["energy"] - ref["energy"]) / len(atoms) <= 1e-5
+    assert np.abs(mixed["forces"] - ref["forces"]).max() < 1e-4 * fmax
+    assert np.abs(mixed["enegs"] - ref["enegs"]).max() < 1e-4
+    # the charges' self-energies (the SiO2 workload's chi q + J q^2) give the
+    # relaxation its minimum
+    pots = pots + [pysic.Potential("charge_self", symbols=[[e]], parameters=[c, n])
+                   for e, (chi, hard) in W.SIO2_CHARGE_PARAMS.items() for c, n in ((chi, 1), (hard, 2))]
+    params = dict(n_steps=400, timestep=0.05, inertia=1.0, friction=3.0, tolerance=1e-4)
+    calc = pysic.Pysic(atoms.copy(), pots, precision="fp64")
+    rel = pysic.ChargeRelaxation("dynamic", calculator=calc,
+                                 parameters=[params[k] for k in ("n_steps", "timestep", "inertia", "friction",
+                                                                 "tolerance")])
+    q_gpu = rel.charge_relaxation()
+    model = compile_model(atoms, pots)
+    r = oracle.relax_charges(atoms.get_positions(), atoms.get_initial_charges(), atoms.get_cell(), atoms.get_pbc(),
+                             model, *oracle_lists(atoms, pots), **params)
+    assert rel.last_steps == r["steps"] > 1
+    np.testing.assert_allclose(q_gpu, r["charges"], atol=1e-8)

@@ -111,3 +111,12 @@ def test_shim_dihedral_and_bend(precision):
     originals, as calculator.py passes them) with bond_bend and a pair term."""
     _, atoms, pots = list(W.dihedral_cases())[1]
     _check(atoms, pots, precision=precision)
+
+
+def test_shim_tersoff_scaled_charge_products():
+    """Products registered as the reference does (factors last to first with
+    is_multiplier, then the lead's permuted records, clear_potential_multipliers)
+    under a Tersoff Coordinator: energy, forces and electronegativities against
+    the oracle."""
+    _, atoms, pots = next(W.comb_style_cases())
+    _check(atoms, pots)

@@ -620,3 +620,42 @@ def test_oracle_dihedral_forces_and_stress(case):
         em[a, b] -= h
         de = (energy(pos @ eps.T, cell @ eps.T) - energy(pos @ em.T, cell @ em.T)) / (2 * h)
         assert st[k] == pytest.approx(-de, abs=1e-6 * max(1.0, abs(e0)))
+
+
+def test_oracle_tersoff_scaled_charge_products():
+    """A Tersoff Coordinator on charge-dependent products (COMB's attraction
+    form, comb.py:660-900) in the oracle: forces minus the position gradient
+    of the energy, the virial its strain derivative and the electronegativities
+    minus its charge derivatives, by finite differences (the bond-order factors
+    depend on the positions only)."""
+    _, atoms, pots = next(W.comb_style_cases())
+    model = compile_model(atoms, pots)
+    assert max(model.pair_nmul) > 0 and max(model.pair_group) >= 0
+    lists = oracle_lists(atoms, pots)
+    pos, q, cell = atoms.get_positions(), atoms.get_initial_charges(), np.asarray(atoms.get_cell())
+
+    def ev(p, qq, what, c=None):
+        return oracle.evaluate(p, qq, cell if c is None else c, atoms.get_pbc(), model, *lists, what=what)
+
+    e0 = ev(pos, q, "energy")
+    f, st = ev(pos, q, "forces")
+    chi = ev(pos, q, "enegs")
+    assert np.abs(f).max() > 1e-2 and np.abs(chi).max() > 1e-2
+    h = 1e-6
+    scale = max(1.0, np.abs(f).max())
+    for a in (0, 4, 13, 30):
+        for c in range(3):
+            p1, p2 = pos.copy(), pos.copy()
+            p1[a, c] += h
+            p2[a, c] -= h
+            assert f[a, c] == pytest.approx(-(ev(p1, q, "energy") - ev(p2, q, "energy")) / (2 * h), abs=1e-6 * scale)
+        q1, q2 = q.copy(), q.copy()
+        q1[a] += h
+        q2[a] -= h
+        assert chi[a] == pytest.approx(-(ev(pos, q1, "energy") - ev(pos, q2, "energy")) / (2 * h), abs=1e-6)
+    for k, (a, b) in enumerate(((0, 0), (1, 1), (2, 2))):
+        ep, em = np.eye(3), np.eye(3)
+        ep[a, b] += h
+        em[a, b] -= h
+        de = (ev(pos @ ep.T, q, "energy", cell @ ep.T) - ev(pos @ em.T, q, "energy", cell @ em.T)) / (2 * h)
+        assert st[k] == pytest.approx(-de, abs=1e-6 * max(1.0, abs(e0)))
