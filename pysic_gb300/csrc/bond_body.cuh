@@ -187,7 +187,6 @@ __device__ __forceinline__ void bond_body(const BondArgs& A, int blk, int nblk) 
     if (act) {
         PostT<R> pp{};
         if constexpr (SPEC) pp = PostT<R>{SPV(SP_BETA), SPV(SP_ETA), 1};
-        else pp = ((const PostT<R>*)A.post)[ti];
         for (int e = lane; e < ni; e += G) {
             const V4 gij = geo[e];
             const V3<R> a{gij.x, gij.y, gij.z};
@@ -236,6 +235,8 @@ __device__ __forceinline__ void bond_body(const BondArgs& A, int blk, int nblk) 
                 continue;
             }
             if (bo) {
+                // post-processing of the centre type in the pair type's group
+                if constexpr (!SPEC) pp = ((const PostT<R>*)A.post)[ti * A.T + tj];
                 if (pp.valid) post_process<R>(pp.beta, pp.eta, zeta, B, dB);
                 else {
                     B = zeta;

@@ -358,7 +358,7 @@ struct pg_context {
     pg::DevBuf<float> d_tab32;
     pg::DevBuf<pg::TripT<double>> d_trip;  // n_types^3
     pg::DevBuf<pg::TripT<float>> d_trip32;
-    pg::DevBuf<pg::PostT<double>> d_post;  // n_types
+    pg::DevBuf<pg::PostT<double>> d_post;  // n_types x n_types (centre, partner)
     pg::DevBuf<pg::PostT<float>> d_post32;
     std::vector<int> tr_kind;            // three-body records as set through the C ABI
     std::vector<double> tr_params, tr_cut, tr_soft;

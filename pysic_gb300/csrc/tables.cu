@@ -5,11 +5,13 @@
 // (core_evaluate_local_doublet_*_B, Core.f90:4257-5606 with
 // potential_affects_atom, Potentials.f90:1195-1259).  Here that test is done
 // once per pair of atom types: table[ti][tj] lists the pair terms that apply,
-// trip[ti][tj][tk] the Tersoff parameters of a triplet, post[ti] the
+// trip[ti][tj][tk] the Tersoff parameters of a triplet, post[ti][tj] the
 // B(zeta) parameters of a centre type (core_post_process_pair_bond_order_factor,
 // Core.f90:2763-2807: the first matching factor), maxbr[ti] the largest
 // bond-order cutoff of the type (max_bond_radius, Core.f90:1030-1067).
 #include <algorithm>
+#include <map>
+#include <set>
 #include <vector>
 
 #include "common.cuh"
@@ -24,19 +26,36 @@ void fold_tables(pg_context* ctx) {
     for (int t : ctx->h_type)
         require(t < T, PG_ERR_INVALID, "atom type outside the interaction tables (set the potentials after the atoms)");
     const int nb = (int)ctx->br_cut.size();
-    // Coordinator groups: the one group of Tersoff factors (evaluated by the
-    // bond-order kernels as group 0) and up to PG_MAX_AGROUPS groups of per-atom
-    // factors (atomfactor.cu)
-    int tersoff_gid = -1;
+    // Coordinator groups: groups of Tersoff factors (evaluated by the
+    // bond-order kernels; each pair type takes the factors and post-processing
+    // of the group its scaled terms name) and up to PG_MAX_AGROUPS groups of
+    // per-atom factors (atomfactor.cu)
+    std::set<int> tersoff_groups;
     for (int b = 0; b < nb; ++b) {
-        if (tersoff_gid < 0) tersoff_gid = ctx->br_group[b];
-        require(ctx->br_group[b] == tersoff_gid && tersoff_gid >= 0, PG_ERR_UNSUPPORTED,
-                "the GB300 engine evaluates one group (one Coordinator) of Tersoff factors per calculator");
+        require(ctx->br_group[b] >= 0, PG_ERR_INVALID, "a Tersoff factor without a group");
+        tersoff_groups.insert(ctx->br_group[b]);
     }
+    const int np0 = (int)ctx->pr_cut.size();
+    // the Tersoff group of each (ti, tj) pair type: the one its scaled terms name
+    std::vector<int> owner((size_t)T * T, -1);
+    for (int r = 0; r < np0; ++r) {
+        const int g = ctx->pr_group[r];
+        if (!tersoff_groups.count(g)) continue;
+        for (int ti = 0; ti < T; ++ti)
+            for (int tj = 0; tj < T; ++tj) {
+                if (!has(ctx->pr_m1[r], ti) || !has(ctx->pr_m2[r], tj)) continue;
+                int& o = owner[(size_t)ti * T + tj];
+                require(o < 0 || o == g, PG_ERR_UNSUPPORTED,
+                        "one pair type scaled by two Coordinators of Tersoff factors is not evaluated by the GB300 "
+                        "engine (one Tersoff group per element pair)");
+                o = g;
+            }
+    }
+    const int tersoff_gid = tersoff_groups.empty() ? -1 : *tersoff_groups.begin();
     std::map<int, int> gmap;  // coordinator group -> per-atom factor group
     for (size_t r = 0; r < ctx->af_kind.size(); ++r) {
         const int g = ctx->af_group[r];
-        require(g >= 0 && g != tersoff_gid, PG_ERR_UNSUPPORTED,
+        require(g >= 0 && !tersoff_groups.count(g), PG_ERR_UNSUPPORTED,
                 "a Coordinator mixing per-atom and Tersoff factors is not evaluated by the GB300 engine");
         if (!gmap.count(g)) {
             require((int)gmap.size() < PG_MAX_AGROUPS, PG_ERR_UNSUPPORTED,
@@ -51,17 +70,26 @@ void fold_tables(pg_context* ctx) {
     // bond-order tables
     std::vector<TripT<double>> trip((size_t)T * T * T);
     for (auto& t : trip) t = TripT<double>{};
-    std::vector<PostT<double>> post(T, PostT<double>{0, 0, 0});
+    // per (ti, tj): the post-processing of the first factor of the pair type's
+    // group centred on ti (core_post_process_pair_bond_order_factor, Core.f90:
+    // 2763-2807); pair types no scaled term names take the first group's
+    std::vector<PostT<double>> post((size_t)T * T, PostT<double>{0, 0, 0});
     std::vector<double> maxbr(T, 0.0);
     double bo_radius = 0.0;
+    auto group_of_pair = [&](int ti, int tj) {
+        const int o = owner[(size_t)ti * T + tj];
+        return o >= 0 ? o : tersoff_gid;
+    };
     for (int b = 0; b < nb; ++b) {
         const double* p = &ctx->br_params[7 * (size_t)b];
         bo_radius = std::max(bo_radius, ctx->br_cut[b]);
         for (int ti = 0; ti < T; ++ti) {
             if (!has(ctx->br_m1[b], ti)) continue;
             if (ctx->br_cut[b] > maxbr[ti]) maxbr[ti] = ctx->br_cut[b];
-            if (!post[ti].valid) post[ti] = PostT<double>{p[0], p[1], 1};
             for (int tj = 0; tj < T; ++tj) {
+                if (ctx->br_group[b] != group_of_pair(ti, tj)) continue;
+                PostT<double>& pp = post[(size_t)ti * T + tj];
+                if (!pp.valid) pp = PostT<double>{p[0], p[1], 1};
                 if (!has(ctx->br_m2[b], tj)) continue;
                 for (int tk = 0; tk < T; ++tk) {
                     if (!has(ctx->br_m3[b], tk)) continue;
@@ -109,9 +137,9 @@ void fold_tables(pg_context* ctx) {
     const int np = (int)ctx->pr_cut.size();
     for (int r = 0; r < np; ++r)
         if (ctx->pr_group[r] >= 0) {
-            require(ctx->pr_group[r] == tersoff_gid || gmap.count(ctx->pr_group[r]), PG_ERR_INVALID,
+            require(tersoff_groups.count(ctx->pr_group[r]) || gmap.count(ctx->pr_group[r]), PG_ERR_INVALID,
                     "a potential has a coordinator without bond-order factors");
-            if (ctx->pr_group[r] == tersoff_gid) bo_radius = std::max(bo_radius, ctx->pr_cut[r]);
+            if (tersoff_groups.count(ctx->pr_group[r])) bo_radius = std::max(bo_radius, ctx->pr_cut[r]);
         }
     const bool bond = nb > 0;
     ctx->have_bond_terms = bond;
@@ -154,8 +182,8 @@ void fold_tables(pg_context* ctx) {
                 PairT<double> t{};
                 t.kind = ctx->pr_kind[r];
                 const int g = ctx->pr_group[r];
-                t.group = g >= 0 && g == tersoff_gid ? 0 : -1;
-                t.agroup = g >= 0 && g != tersoff_gid ? gmap.at(g) : -1;
+                t.group = g >= 0 && tersoff_groups.count(g) ? 0 : -1;
+                t.agroup = g >= 0 && !tersoff_groups.count(g) ? gmap.at(g) : -1;
                 require(!(t.agroup >= 0 && t.kind >= 7), PG_ERR_UNSUPPORTED,
                         "per-atom bond-order scaling of charge-dependent terms is not evaluated by the GB300 engine");
                 require(!(t.agroup >= 0 && have_products && ctx->pr_nmul[r] > 0), PG_ERR_UNSUPPORTED,

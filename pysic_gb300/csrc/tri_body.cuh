@@ -196,7 +196,7 @@ __device__ __forceinline__ void tri_atom(const BondArgs& A, int gslot, TriStage<
         if (bo) {
             PostT<R> pp{};
             if constexpr (SPEC) pp = PostT<R>{SPV(SP_BETA), SPV(SP_ETA), 1};
-            else pp = ((const PostT<R>*)A.post)[ti];
+            else pp = ((const PostT<R>*)A.post)[ti * T + tj];  // the pair type's group
             if (pp.valid) {
                 post_process<R>(pp.beta, pp.eta, zeta, B, dB);
             } else {

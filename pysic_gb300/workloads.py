@@ -265,12 +265,14 @@ def dihedral_cases():
 def comb_style_cases():
     """Tersoff bond-order factors scaling charge-dependent products, the form
     of COMB's attraction (pysic/interactions/comb.py:660-900: charge_exp x
-    charge_abs x exponential with a Coordinator of 'tersoff' factors), on a
-    random SiO2 box with random charges: one Coordinator over every Si / O
-    triplet (the post-processing beta, eta shared by each centre element),
-    the scaled product on Si-O and O-O pairs, a scaled charge_exp on Si-Si
-    pairs, and an unscaled repulsion.  Energies, forces, virial and
-    electronegativities all depend on the bond orders and the charges."""
+    charge_abs x exponential with a Coordinator of 'tersoff' factors), on
+    random SiO2 boxes with random charges: first one Coordinator over every
+    Si / O triplet (the post-processing beta, eta shared by each centre
+    element), the scaled product on Si-O and O-O pairs, a scaled charge_exp on
+    Si-Si pairs, and an unscaled repulsion; then COMB's layout of one
+    Coordinator per element pair with its own factors and post-processing.
+    Energies, forces, virial and electronegativities all depend on the bond
+    orders and the charges."""
     P = Potential
     from .interactions import ProductPotential
 
@@ -292,3 +294,28 @@ def comb_style_cases():
     rep = P("exponential", symbols=[["Si", "O"], ["O", "O"], ["Si", "Si"]], parameters=[30.0, 2.5], cutoff=3.0,
             cutoff_margin=0.6)
     yield "comb_attraction", a, [prod, si, rep]
+    # COMB's layout: one Coordinator per element pair (comb.py:700-900), each
+    # with its own Tersoff factors and post-processing, on Si-Si, O-O and Si-O
+    a2 = sio2_box(14, seed=63)
+    q2 = np.random.default_rng(64).normal(0.0, 0.5, len(a2))
+    a2.set_initial_charges(q2 - q2.mean())
+
+    def crd(triples, beta, eta, h):
+        return Coordinator([BondOrderParameters("tersoff", cutoff=3.0, cutoff_margin=0.6, symbols=triples,
+                                                parameters=[[beta, eta], [0.0, 2.0, 1.5, h, 1.0]])])
+
+    pots = []
+    for pair, triples, beta, eta, h in (
+            (["Si", "Si"], [["Si", "Si", "Si"], ["Si", "Si", "O"]], 0.8, 0.9, -0.4),
+            (["O", "O"], [["O", "O", "O"], ["O", "O", "Si"]], 0.5, 1.3, 0.2),
+            (["Si", "O"], [["Si", "O", "O"], ["Si", "O", "Si"], ["O", "Si", "Si"], ["O", "Si", "O"]], 1.1, 0.7,
+             -0.1)):
+        f1 = P("charge_exp", symbols=[pair], parameters=[0.3, 2.0, 1.0, 2.0, 1.0, 3.0, 1.5, 2.4, 1.2, 0.6, 0.4],
+               cutoff=3.0, cutoff_margin=0.6)
+        f2 = P("charge_abs", symbols=[pair], parameters=[1.2, 0.3, 0.2, 2.0, 1.5, 0.4, -0.3, 2.0])
+        f3 = P("exponential", symbols=[pair], parameters=[-8.0, 1.2])
+        prod = ProductPotential([f1, f2, f3])
+        prod.set_coordinator(crd(triples, beta, eta, h))
+        pots.append(prod)
+    pots.append(rep)
+    yield "comb_groups", a2, pots

@@ -333,7 +333,8 @@ def test_charge_abs_parity():
     assert np.abs(mixed["enegs"] - ref["enegs"]).max() < 1e-4
 
 
-def test_tersoff_scaled_charge_products_parity_and_relaxation():
+@pytest.mark.parametrize("case", [c[0] for c in W.comb_style_cases()])
+def test_tersoff_scaled_charge_products_parity_and_relaxation(case):
     """A Tersoff Coordinator on charge-dependent products and on a charge_exp
     (COMB's attraction form, comb.py:660-900), evaluated in the bond-order
     kernels: FP64 energy, forces, virial and electronegativities against the
@@ -341,8 +342,9 @@ def test_tersoff_scaled_charge_products_parity_and_relaxation():
     electronegativities 1e-9), mixed precision within 1e-5 eV/atom, 1e-4 of
     the largest force and 1e-4 eV/e, and the damped relaxation on these
     electronegativities (bond orders fixed with the positions) against the
-    oracle's loop: same steps, charges within 1e-8 e."""
-    _, atoms, pots = next(W.comb_style_cases())
+    oracle's loop: same steps, charges within 1e-8 e.  The second case has
+    COMB's layout: one Coordinator per element pair."""
+    _, atoms, pots = next(c for c in W.comb_style_cases() if c[0] == case)
     ref = oracle_all(atoms, pots)
     for lanes in (4, 8, 64):
         got = engine_all(atoms, pots, None, "fp64", lanes)

@@ -113,10 +113,11 @@ def test_shim_dihedral_and_bend(precision):
     _check(atoms, pots, precision=precision)
 
 
-def test_shim_tersoff_scaled_charge_products():
+@pytest.mark.parametrize("case", [c[0] for c in W.comb_style_cases()])
+def test_shim_tersoff_scaled_charge_products(case):
     """Products registered as the reference does (factors last to first with
     is_multiplier, then the lead's permuted records, clear_potential_multipliers)
     under a Tersoff Coordinator: energy, forces and electronegativities against
     the oracle."""
-    _, atoms, pots = next(W.comb_style_cases())
+    _, atoms, pots = next(c for c in W.comb_style_cases() if c[0] == case)
     _check(atoms, pots)

@@ -622,13 +622,14 @@ def test_oracle_dihedral_forces_and_stress(case):
         assert st[k] == pytest.approx(-de, abs=1e-6 * max(1.0, abs(e0)))
 
 
-def test_oracle_tersoff_scaled_charge_products():
+@pytest.mark.parametrize("case", [c[0] for c in W.comb_style_cases()])
+def test_oracle_tersoff_scaled_charge_products(case):
     """A Tersoff Coordinator on charge-dependent products (COMB's attraction
     form, comb.py:660-900) in the oracle: forces minus the position gradient
     of the energy, the virial its strain derivative and the electronegativities
     minus its charge derivatives, by finite differences (the bond-order factors
     depend on the positions only)."""
-    _, atoms, pots = next(W.comb_style_cases())
+    _, atoms, pots = next(c for c in W.comb_style_cases() if c[0] == case)
     model = compile_model(atoms, pots)
     assert max(model.pair_nmul) > 0 and max(model.pair_group) >= 0
     lists = oracle_lists(atoms, pots)

@@ -38,8 +38,8 @@ def _cases():
                              pysic.Potential("LJ", symbols=[["X", "X"]], parameters=[0.005, 3.2], cutoff=5.0)], None
     _, a, pots = list(W.dihedral_cases())[1]
     yield "dihedral_bend", a, pots, None
-    _, a, pots = next(W.comb_style_cases())
-    yield "tersoff_scaled_products", a, pots, None
+    for name, a, pots in W.comb_style_cases():
+        yield name, a, pots, None
 
 
 # rows of the table array behind a record's first parameter: tabulated
