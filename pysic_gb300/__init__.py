@@ -8,6 +8,7 @@ pysic`` is the intended use.
 """
 from .atoms import Atoms
 from .calculator import FastNeighborList, Pysic
+from .comb import CombPotential
 from .core import *  # noqa: F401,F403  descriptor queries of pysic.core
 from .error import *  # noqa: F401,F403
 from .interactions import (BondOrderParameters, CompoundPotential, Coordinator, CoulombSummation, Potential,
@@ -19,4 +20,4 @@ __version__ = "0.1.0"
 
 __all__ = ["Atoms", "Pysic", "VelocityVerlet", "FastNeighborList", "Potential", "ProductPotential", "BondOrderParameters", "Coordinator",
            "CoulombSummation", "ChargeRelaxation", "estimate_ewald_parameters", "CompoundPotential",
-           "SuttonChenPotential"]
+           "SuttonChenPotential", "CombPotential"]

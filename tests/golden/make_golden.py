@@ -8,7 +8,10 @@ reference_docs.json
     (default location: the REFERENCE_ROOT environment variable):
       * He2 Lennard-Jones, doc/run examples.rst:141-145 (energy and forces),
       * C-O-H with two LJ potentials, doc/pysic class.rst:130-157 (energies
-        and forces of pot1 alone, pot2 alone, and both in one calculator).
+        and forces of pot1 alone, pot2 alone, and both in one calculator),
+      * the COMB10 default parameters of pysic/interactions/comb.py:81-517
+        (read from the source text: literal values, and the mixed Si-O values
+        from the two rules used there, geometric mean and arithmetic mean).
     Without the reference tree the committed file is kept as it is.
 
 oracle_cases.npz
@@ -82,7 +85,32 @@ def reference_docs(ref_root):
             "printed_digits": 8,
         },
     }
+    out["comb10_parameters"] = {"source": "pysic/interactions/comb.py:81-517",
+                                "values": comb10_parameters(ref_root)}
     return out
+
+
+def comb10_parameters(ref_root):
+    """name -> default value of CombPotential's parameter table, parsed from
+    the reference's source text (no code of it is run)."""
+    text = open(os.path.join(ref_root, "pysic", "interactions", "comb.py")).read()
+    body = text[text.index("def __init__"):text.index("def get_parameter_value")]
+    values, name = {}, None
+    for m in re.finditer(r"newparam = '([^']+)'|self\.params\[newparam\] = (.*?)\n\s*self\.n_params", body, re.S):
+        if m.group(1):
+            name = m.group(1)
+            continue
+        expr = " ".join(m.group(2).replace("\\", " ").split())
+        refs = re.findall(r"self\.params\['([^']+)'\]", expr)
+        if not refs:
+            values[name] = float(expr)
+        elif expr.startswith("math.sqrt(") and len(refs) == 2 and "*" in expr:
+            values[name] = float(np.sqrt(values[refs[0]] * values[refs[1]]))
+        elif expr.endswith("* 0.5") and len(refs) == 2 and "+" in expr:
+            values[name] = (values[refs[0]] + values[refs[1]]) * 0.5
+        else:
+            raise ValueError("unexpected parameter expression for %r: %s" % (name, expr))
+    return values
 
 
 def oracle_cases():
