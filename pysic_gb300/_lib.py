@@ -7,6 +7,7 @@ with an error that says how to build it.
 """
 import ctypes
 import os
+import weakref
 
 import numpy as np
 
@@ -145,7 +146,17 @@ _SIGNATURES = {
                                               ctypes.c_double, _c_double_p]),
 }
 
+# The two calls of a force-evaluation step, bound a second time with plain
+# addresses (c_void_p) so that a step passes integers instead of building a
+# ctypes pointer object per array (about 2 us each).
+_ADDR_SIGNATURES = {
+    "pg_update_atom_coordinates": (ctypes.c_int, [_ctx, ctypes.c_void_p]),
+    "pg_calculate": (ctypes.c_int, [_ctx, ctypes.c_int32, ctypes.c_int32, ctypes.c_void_p, ctypes.c_void_p,
+                                    ctypes.c_void_p, ctypes.c_void_p]),
+}
+
 _lib = None
+_addr_lib = None
 
 
 def exported_symbols():
@@ -165,8 +176,49 @@ def load(path=LIB_PATH):
         fn = getattr(lib, name)
         fn.restype = res
         fn.argtypes = args
+    global _addr_lib
+    alib = ctypes.CDLL(path)  # separate function objects with their own argument types
+    for name, (res, args) in _ADDR_SIGNATURES.items():
+        fn = getattr(alib, name)
+        fn.restype = res
+        fn.argtypes = args
+    _addr_lib = alib
     _lib = lib
     return lib
+
+
+def addr_lib():
+    """The step calls bound with plain addresses (see _ADDR_SIGNATURES)."""
+    load()
+    return _addr_lib
+
+
+class AddressCache:
+    """Data addresses of float64 C-contiguous arrays passed again and again
+    (a caller's step buffers), looked up by identity through weak references,
+    so that the arrays are not kept alive here and a recycled id is never
+    mistaken for the old array."""
+
+    def __init__(self, size=8):
+        self.size = size
+        self._d = {}
+
+    def __call__(self, a):
+        if a is None:
+            return None
+        e = self._d.get(id(a))
+        if e is not None and e[0]() is a:
+            return e[1]
+        if not (isinstance(a, np.ndarray) and a.dtype == np.float64 and a.flags.c_contiguous):
+            raise TypeError("expected a C-contiguous float64 array")
+        addr = a.__array_interface__["data"][0]
+        if len(self._d) >= self.size:
+            self._d.pop(next(iter(self._d)))
+        try:
+            self._d[id(a)] = (weakref.ref(a), addr)
+        except TypeError:  # not weak-referenceable: no caching
+            pass
+        return addr
 
 
 def check(status):

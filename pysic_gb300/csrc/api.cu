@@ -148,6 +148,18 @@ __global__ void coords_commit(const double* __restrict__ in, double* __restrict_
         out[i] = in[i];
 }
 
+// The totals of an evaluation as doubles and the verdict of the coordinate
+// update it committed (bad may be null: none), written straight into
+// page-locked host memory: one small store instead of two copy-engine
+// transfers.
+__global__ void publish_totals(pg::HostTotals* __restrict__ out, const pg::FxAcc* __restrict__ acc,
+                               const int* __restrict__ bad) {
+    const int c = threadIdx.x;
+    if (c < 7) out->totals[c] = pg::fx_to_double(pg::fx_from_limbs(acc[c]));
+    if (c == 7) out->bad = bad != nullptr ? *bad : 0;
+    __threadfence_system();
+}
+
 int copy_blocks(long long n) {
     return (int)std::max<long long>(1, std::min<long long>((n + 255) / 256, 4ll * sm_count()));
 }
@@ -177,9 +189,19 @@ static void host_copy(pg_context* ctx, const double* src, double* dst, long long
 // captured with it into its graph) or on its own.
 static void enqueue_coordinate_commit(pg_context* ctx) {
     const long long m = 3ll * ctx->n;
+    const int vec = (((uintptr_t)ctx->pos_in.p) & 15u) == 0 ? 1 : 0;
+    copy_check<<<copy_blocks(vec ? (m + 1) / 2 : m), 256, 0, ctx->stream>>>(ctx->pos_in.p, nullptr, m,
+                                                                            ctx->pos_bad.p, vec);
+    PG_CHECK_LAUNCH();
     coords_commit<<<copy_blocks(m), 256, 0, ctx->stream>>>(ctx->pos_in.p, ctx->pos.p, m, ctx->pos_bad.p);
     PG_CHECK_LAUNCH();
-    ctx->launches += 1;
+    ctx->launches += 2;
+}
+
+// A rejected update leaves the check flag set: clear it for the next one
+// (enqueued after the verdict was read, so no kernel reads it meanwhile).
+static void clear_check_flag(pg_context* ctx) {
+    PG_CUDA(cudaMemsetAsync(ctx->pos_bad.p, 0, sizeof(int), ctx->stream));
 }
 
 // Finish an outstanding coordinate update: commit it if no evaluation has done
@@ -192,14 +214,16 @@ void settle_coordinates(pg_context* ctx) {
     PG_CUDA(cudaMemcpyAsync(bad, ctx->pos_bad.p, sizeof(int), cudaMemcpyDeviceToHost, ctx->stream));
     PG_CUDA(cudaStreamSynchronize(ctx->stream));
     ctx->upd_state = PG_UPD_NONE;
+    if (*bad) clear_check_flag(ctx);
     require(*bad == 0, PG_ERR_INVALID, "non-finite atom position: the coordinate update was not applied");
 }
 
-// New coordinates for the context: copied to a staging buffer and checked for
-// non-finite values on the context's stream, without waiting.  The next
-// evaluation commits them in front of its kernels (in its captured graph) and
-// pg_calculate reads the verdict together with the results, so an update
-// followed by an evaluation costs one synchronisation.  The copy is
+// New coordinates for the context: copied to a staging buffer on the
+// context's stream, without waiting.  The next evaluation checks them for
+// non-finite values and commits them in front of its kernels (in its captured
+// graph), and pg_calculate reads the verdict together with the results, so an
+// update followed by an evaluation costs one copy in, one copy out and one
+// synchronisation.  The copy is
 // cudaMemcpyAsync: page-locked host memory is read asynchronously and must
 // stay unchanged until the next call on the context that returns results;
 // pageable memory is consumed on return.
@@ -208,9 +232,11 @@ static void update_coordinates(pg_context* ctx, const double* positions) {
     if (m == 0) return;
     if (ctx->upd_state != PG_UPD_NONE) settle_coordinates(ctx);  // one outstanding update at a time
     ctx->pos_in.resize((size_t)m);
-    ctx->pos_bad.resize(1);
-    PG_CUDA(cudaMemsetAsync(ctx->pos_bad.p, 0, sizeof(int), ctx->stream));
-    host_copy(ctx, positions, ctx->pos_in.p, m, true, ctx->pos_bad.p);  // staged and checked
+    if (ctx->pos_bad.n == 0) {  // the check flag stays clear between updates (clear_check_flag)
+        ctx->pos_bad.resize(1);
+        PG_CUDA(cudaMemsetAsync(ctx->pos_bad.p, 0, sizeof(int), ctx->stream));
+    }
+    host_copy(ctx, positions, ctx->pos_in.p, m, true, nullptr);  // staged; checked at the commit
     ctx->upd_state = PG_UPD_STAGED;
 }
 
@@ -311,7 +337,11 @@ static int autotune_lanes(pg_context* ctx, int precision, int flags) {
     return best;
 }
 
-void evaluate(pg_context* ctx, int precision, int flags) {
+// One evaluation enqueued on the context's stream, replayed from a captured
+// graph when nothing it depends on has changed; a staged coordinate update is
+// checked and committed in front of its kernels.  publish: a last kernel
+// writes the totals and the update verdict into h_tot (pg_calculate).
+static void evaluate_impl(pg_context* ctx, int precision, int flags, bool publish) {
     require(precision == PG_PREC_FP64 || precision == PG_PREC_MIXED, PG_ERR_INVALID, "unknown precision");
     // staged coordinates are committed in front of the evaluation's kernels,
     // unless set-up work that reads them comes first
@@ -333,9 +363,19 @@ void evaluate(pg_context* ctx, int precision, int flags) {
         G = ctx->tuned_lanes[precision];
     }
     if (G == 0) G = 8;
+    // the verdict published: that of an update committed now or by an
+    // evaluation whose results were not read yet
+    const bool verdict = ctx->upd_state != PG_UPD_NONE;
+    pg::HostTotals* dtot = nullptr;
+    if (publish) PG_CUDA(cudaHostGetDevicePointer((void**)&dtot, (void*)ctx->h_tot.get(1), 0));
     auto sequence = [&] {
         if (commit) enqueue_coordinate_commit(ctx);
         enqueue_evaluation(ctx, precision, flags, G, nullptr);
+        if (publish) {
+            publish_totals<<<1, 32, 0, ctx->stream>>>(dtot, ctx->out_acc.p, verdict ? ctx->pos_bad.p : nullptr);
+            PG_CHECK_LAUNCH();
+            ctx->launches += 1;
+        }
     };
     if (commit) ctx->upd_state = PG_UPD_CHECKED;  // the verdict is read with the results
     // events recorded inside a capture cannot be waited on: time with direct launches
@@ -346,7 +386,9 @@ void evaluate(pg_context* ctx, int precision, int flags) {
     }
     // replay a captured sequence if nothing it depends on has changed
     for (auto it = ctx->graphs.begin(); it != ctx->graphs.end(); ++it) {
-        if (it->precision != precision || it->flags != flags || it->lanes != G || it->commit != commit) continue;
+        if (it->precision != precision || it->flags != flags || it->lanes != G || it->commit != commit ||
+            it->pub != (publish && verdict) + publish * 2)
+            continue;
         if (it->state == ctx->state_epoch && it->alloc == alloc_epoch()) {
             PG_CUDA(cudaGraphLaunch(it->exec, ctx->stream));
             ctx->launches = it->launches;
@@ -381,10 +423,12 @@ void evaluate(pg_context* ctx, int precision, int flags) {
     cudaError_t e = cudaGraphInstantiate(&exec, graph, 0);
     cudaGraphDestroy(graph);
     PG_CUDA(e);
-    ctx->graphs.push_back(
-        pg_context::Graph{precision, flags, G, launches, commit, ctx->state_epoch, alloc_epoch(), exec});
+    ctx->graphs.push_back(pg_context::Graph{precision, flags, G, launches, commit, (publish && verdict) + publish * 2,
+                                            ctx->state_epoch, alloc_epoch(), exec});
     ctx->launches = launches;
 }
+
+void evaluate(pg_context* ctx, int precision, int flags) { evaluate_impl(ctx, precision, flags, false); }
 
 // The results of the last evaluation into host memory, and the verdict of a
 // coordinate update that the evaluation committed: one synchronisation.
@@ -402,6 +446,7 @@ static void copy_results(pg_context* ctx, int flags, double* energy, double* for
     PG_CUDA(cudaStreamSynchronize(st));
     if (verdict) {
         ctx->upd_state = PG_UPD_NONE;
+        if (*bad) clear_check_flag(ctx);
         require(*bad == 0, PG_ERR_INVALID,
                 "non-finite atom position: the coordinate update was not applied (results are of the previous "
                 "coordinates)");
@@ -410,6 +455,34 @@ static void copy_results(pg_context* ctx, int flags, double* energy, double* for
     if (energy && (flags & PG_WANT_ENERGY)) *energy = tot[0];
     if (stress && (flags & PG_WANT_FORCES))
         for (int c = 0; c < 6; ++c) stress[c] = tot[1 + c];
+}
+
+// pg_calculate: the evaluation ends with a kernel that writes the totals and
+// the update verdict into page-locked memory (h_tot), so that only the
+// per-atom arrays travel by the copy engine; one synchronisation.
+static void calculate(pg_context* ctx, int precision, int flags, double* energy, double* forces, double* stress,
+                      double* enegs) {
+    if (ctx->n == 0 || ctx->timing) {
+        evaluate(ctx, precision, flags);
+        copy_results(ctx, flags, energy, forces, stress, enegs);
+        return;
+    }
+    const bool verdict = ctx->upd_state != PG_UPD_NONE;
+    evaluate_impl(ctx, precision, flags, true);
+    if (forces && (flags & PG_WANT_FORCES)) host_copy(ctx, ctx->out_f.p, forces, 3ll * ctx->n, false, nullptr);
+    if (enegs && (flags & PG_WANT_ENEGS)) host_copy(ctx, ctx->out_chi.p, enegs, (long long)ctx->n, false, nullptr);
+    PG_CUDA(cudaStreamSynchronize(ctx->stream));
+    const HostTotals* t = ctx->h_tot.p;
+    if (verdict) {
+        ctx->upd_state = PG_UPD_NONE;
+        if (t->bad) clear_check_flag(ctx);
+        require(t->bad == 0, PG_ERR_INVALID,
+                "non-finite atom position: the coordinate update was not applied (results are of the previous "
+                "coordinates)");
+    }
+    if (energy && (flags & PG_WANT_ENERGY)) *energy = t->totals[0];
+    if (stress && (flags & PG_WANT_FORCES))
+        for (int c = 0; c < 6; ++c) stress[c] = t->totals[1 + c];
 }
 
 }  // namespace pg
@@ -782,8 +855,7 @@ int pg_calculate(pg_context* ctx, int32_t precision, int32_t flags, double* ener
     return guarded([&] {
         check_ctx(ctx);
         set_device(ctx);
-        pg::evaluate(ctx, precision, flags);
-        pg::copy_results(ctx, flags, energy, forces, stress, enegs);
+        pg::calculate(ctx, precision, flags, energy, forces, stress, enegs);
     });
 }
 

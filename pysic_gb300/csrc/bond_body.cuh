@@ -45,7 +45,7 @@ __device__ __forceinline__ void bond_body(const BondArgs& A, int blk, int nblk) 
     __shared__ TripT<R> strip[64];
     __shared__ PairT<R> sterm[32];
     __shared__ int2 sindex[64];
-    __shared__ Fx128 wsum[128 / 32][7];
+    __shared__ R wpart[128 / 32][7];
     __shared__ unsigned done;
     // small interaction tables in shared memory
     const PairT<R>* terms = (const PairT<R>*)A.terms;
@@ -400,9 +400,8 @@ __device__ __forceinline__ void bond_body(const BondArgs& A, int blk, int nblk) 
     }
     // energy and virial: warp sums (empty slots hold zeros), exact from there on
     if (A.acc) {
-        const Fx128 v[7] = {warp_total(En), warp_total(W0), warp_total(W1), warp_total(W2),
-                            warp_total(W3), warp_total(W4), warp_total(W5)};
-        block_totals_publish(v, wsum, &done, A.acc);
+        const R t[7] = {En, W0, W1, W2, W3, W4, W5};
+        block_totals_add(t, wpart, &done, A.acc);
     }
 }
 

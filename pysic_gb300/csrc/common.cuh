@@ -271,6 +271,16 @@ inline void launch_pdl(void (*kernel)(KArgs...), dim3 grid, dim3 block, cudaStre
 // an evaluation whose verdict the host has not read yet.
 constexpr int PG_UPD_NONE = 0, PG_UPD_STAGED = 1, PG_UPD_CHECKED = 2;
 
+// Page-locked, device-mapped record that the last kernel of a pg_calculate
+// sequence fills: the totals as doubles and the verdict of the coordinate
+// update it committed, so that only the per-atom arrays travel by the copy
+// engine.
+struct HostTotals {
+    double totals[8];  // energy, virial (xx, yy, zz, yz, xz, xy), spare
+    int bad;           // the committed update held a non-finite value
+    int pad;
+};
+
 // Parameters of the single-species Tersoff fast path, by index.
 constexpr int PG_SPEC_MAX_TERMS = 3;
 enum SpecIndex {
@@ -323,6 +333,7 @@ struct pg_context {
     int upd_state = 0;          // pg::PG_UPD_*: an outstanding coordinate update
     pg::PinnedBuf<pg::FxAcc> h_acc; // energy / virial totals on their way to the host
     pg::PinnedBuf<int> h_flag;
+    pg::PinnedBuf<pg::HostTotals> h_tot;  // filled by the results kernel of pg_calculate sequences
     pg::DevBuf<double> charge;  // n
     pg::DevBuf<int> type;       // n
     std::vector<int> h_type;
@@ -500,6 +511,7 @@ struct pg_context {
     struct Graph {
         int precision, flags, lanes, launches;
         bool commit;  // begins with the check and commit of staged coordinates
+        int pub;      // ends with the totals (2) and the update verdict (+1) written to h_tot
         unsigned long long state, alloc;
         cudaGraphExec_t exec;
     };

@@ -441,6 +441,43 @@ __device__ __forceinline__ DSum group_sum_f(double v) {
 __device__ __forceinline__ Fx128 warp_total(float v) { return fx_from_float(group_sum<32>(v)); }
 __device__ __forceinline__ Fx128 warp_total(double v) { return fx_from_double(group_sum<32>(v)); }
 
+__device__ __forceinline__ Fx128 fx_from(float v) { return fx_from_float(v); }
+__device__ __forceinline__ Fx128 fx_from(double v) { return fx_from_double(v); }
+
+// Adds a block's energy and virial to the global totals acc[0..6] (null: none)
+// from every lane's 7 terms t, with the result of block_totals_publish: each
+// warp sums its lanes in the working precision by the same shuffle tree as
+// warp_total and leaves the 7 sums in shared memory (wpart); the last warp of
+// the block to arrive widens them exactly, lane c taking value c over the
+// block's warps in warp order, and sends value c's limbs to acc from lane c.
+// Only one warp per block converts, and the 7 values go out in parallel.
+// `done` is a shared counter set to zero before the block's first barrier.
+template <typename R>
+__device__ __forceinline__ void block_totals_add(const R (&t)[7], R (*wpart)[7], unsigned* done, FxAcc* acc) {
+    if (acc == nullptr) return;
+    const int wl = threadIdx.x & 31, w = threadIdx.x >> 5, nw = blockDim.x >> 5;
+    R s[7];
+#pragma unroll
+    for (int c = 0; c < 7; ++c) s[c] = group_sum<32>(t[c]);
+    unsigned last = 0;
+    if (wl == 0) {
+#pragma unroll
+        for (int c = 0; c < 7; ++c) wpart[w][c] = s[c];
+        __threadfence_block();
+        last = atomicAdd(done, 1u) == (unsigned)(nw - 1) ? 1u : 0u;
+    }
+    if (__shfl_sync(0xffffffffu, last, 0) == 0u) return;
+    __threadfence_block();
+    if (wl < 7) {
+        Fx128 x = fx_zero();
+        for (int k = 0; k < nw; ++k) {
+            const volatile R* q = &wpart[k][wl];
+            x = fx_add(x, fx_from((R)*q));
+        }
+        fx_red(&acc[wl], x);
+    }
+}
+
 // write (first) or add a group sum into a per-atom FP64 output; the mixed
 // path adds in fixed point
 __device__ __forceinline__ void store_sum(double* p, const XSum& v, bool first) {

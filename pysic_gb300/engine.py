@@ -21,6 +21,8 @@ class Engine:
         L.check(self.lib.pg_create_on(ctypes.byref(ctx), int(device)))
         self.ctx = ctx
         self.n = 0
+        self._alib = L.addr_lib()
+        self._addr = L.AddressCache()
 
     def close(self):
         if getattr(self, "ctx", None) is not None and self.ctx.value:
@@ -48,6 +50,10 @@ class Engine:
         L.check(self.lib.pg_create_atoms(self.ctx, self.n, L.dptr(pos), L.dptr(q), L.iptr(t)))
 
     def update_positions(self, positions):
+        if isinstance(positions, np.ndarray) and positions.dtype == np.float64 and positions.flags.c_contiguous \
+                and positions.size == 3 * self.n:
+            L.check(self._alib.pg_update_atom_coordinates(self.ctx, self._addr(positions)))
+            return
         pos = L.as_f64(positions, (-1, 3))
         L.check(self.lib.pg_update_atom_coordinates(self.ctx, L.dptr(pos)))
 
@@ -308,9 +314,10 @@ class Engine:
         L.check(self.lib.pg_set_graphs(self.ctx, 1 if enable else 0))
 
     def calculate_into(self, precision, flags, energy, forces, stress, enegs):
-        """pg_calculate into caller-provided (e.g. pinned) host arrays."""
-        L.check(self.lib.pg_calculate(self.ctx, precision, flags, L.dptr(energy), L.dptr(forces), L.dptr(stress),
-                                      L.dptr(enegs)))
+        """pg_calculate into caller-provided (e.g. page-locked) C-contiguous
+        float64 host arrays (any of them may be None)."""
+        a = self._addr
+        L.check(self._alib.pg_calculate(self.ctx, precision, flags, a(energy), a(forces), a(stress), a(enegs)))
 
 
 __all__ = ["Engine", "EngineError"]

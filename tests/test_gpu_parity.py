@@ -405,6 +405,81 @@ def test_page_locked_buffers_match_pageable_ones():
         assert e[0] == ref["energy"] and np.array_equal(f, ref["forces"])
 
 
+def test_page_locked_step_buffers_in_every_combination():
+    """Page-locked coordinates are read asynchronously after the update call
+    returns: a page-locked coordinate buffer rewritten in place gives each new
+    configuration's results, page-locked and pageable inputs and outputs mix
+    freely, a page-locked update is committed by calls that are not
+    evaluations, and a non-finite value in it is rejected there too, with the
+    old coordinates kept.  Every result is bit-identical to the pageable
+    path's."""
+    import torch
+
+    from pysic_gb300 import _lib as L
+
+    atoms = W.diamond_si(3, noise=0.1, seed=17)
+    calc = pysic.Pysic(atoms, W.tersoff_si_potentials())
+    calc.get_potential_energy()
+    eng = calc.engine
+    n = len(atoms)
+    flags = L.WANT_ENERGY | L.WANT_FORCES | L.WANT_ENEGS
+
+    def pinned(shape):
+        return torch.zeros(shape, dtype=torch.float64, pin_memory=True).numpy()
+
+    rng = np.random.default_rng(5)
+    configs = [atoms.get_positions() + rng.normal(0, 0.03, (n, 3)) for _ in range(4)]
+    for prec in (L.PREC_FP64, L.PREC_MIXED):
+        refs = []
+        for x in configs:
+            eng.update_positions(x.copy())
+            refs.append(eng.calculate(prec, energy=True, forces=True, enegs=True))
+        pos = pinned((n, 3))
+        outs = {"pinned": (pinned(1), pinned((n, 3)), pinned(6), pinned(n)),
+                "pageable": (np.zeros(1), np.zeros((n, 3)), np.zeros(6), np.zeros(n))}
+        for step, (x, ref) in enumerate(zip(configs, refs)):
+            for src in ("pinned", "pageable"):
+                for dst in ("pinned", "pageable"):
+                    e, f, s, c = outs[dst]
+                    if src == "pinned":
+                        pos[:] = x  # the same buffer, new values
+                        eng.update_positions(pos)
+                    else:
+                        eng.update_positions(x.copy())
+                    eng.calculate_into(prec, flags, e, f, s, c)
+                    assert e[0] == ref["energy"], (step, src, dst)
+                    assert np.array_equal(f, ref["forces"]) and np.array_equal(s, ref["stress"])
+                    assert np.array_equal(c, ref["enegs"])
+        # a page-locked update committed by a call that is not an evaluation
+        # (the list-positions query settles outstanding updates first)
+        pos[:] = configs[1]
+        eng.update_positions(pos)
+        eng.list_positions()
+        r = eng.calculate(prec, energy=True, forces=True, enegs=True)
+        assert r["energy"] == refs[1]["energy"] and np.array_equal(r["forces"], refs[1]["forces"])
+        # rejected: when settled outside an evaluation, with results copied by
+        # the copy engine, and with results published
+        pos[3, 0] = np.inf
+        eng.update_positions(pos)
+        with pytest.raises(L.EngineError) as err:
+            eng.list_positions()
+        assert err.value.status == L.PG_ERR_INVALID
+        eng.update_positions(pos)
+        with pytest.raises(L.EngineError) as err:
+            eng.calculate(prec, energy=True, forces=True, enegs=True)
+        assert err.value.status == L.PG_ERR_INVALID
+        r = eng.calculate(prec, energy=True, forces=True, enegs=True)
+        assert r["energy"] == refs[1]["energy"] and np.array_equal(r["forces"], refs[1]["forces"])
+        pos[3, 0] = np.nan
+        e, f, s, c = outs["pinned"]
+        with pytest.raises(L.EngineError) as err:
+            eng.update_positions(pos)
+            eng.calculate_into(prec, flags, e, f, s, c)
+        assert err.value.status == L.PG_ERR_INVALID
+        eng.calculate_into(prec, flags, e, f, s, c)
+        assert e[0] == refs[1]["energy"] and np.array_equal(f, refs[1]["forces"])
+
+
 @pytest.mark.parametrize("case", [c[0] for c in W.product_cases()])
 def test_product_potentials_parity(case):
     """Products of pair potentials (ProductPotential): FP64 against the oracle
