@@ -47,6 +47,35 @@ inline unsigned long long& alloc_epoch() {
     return e;
 }
 
+// FNV-1a over the values a captured launch sequence was built from.
+struct SigHash {
+    unsigned long long h = 1469598103934665603ull;
+    template <typename T>
+    SigHash& add(const T& v) {
+        const unsigned char* p = (const unsigned char*)&v;
+        for (size_t i = 0; i < sizeof(T); ++i) {
+            h ^= p[i];
+            h *= 1099511628211ull;
+        }
+        return *this;
+    }
+};
+
+// A launch sequence kept as an instantiated CUDA graph (the list-build
+// stages): replayed while the values it was built from (sig: buffer
+// addresses through alloc_epoch, sizes, kernel arguments) are unchanged,
+// otherwise captured anew and the executable graph updated in place.
+struct SegGraph {
+    cudaGraphExec_t exec = nullptr;
+    unsigned long long sig = 0;
+    SegGraph() = default;
+    SegGraph(const SegGraph&) = delete;
+    SegGraph& operator=(const SegGraph&) = delete;
+    ~SegGraph() {
+        if (exec) cudaGraphExecDestroy(exec);
+    }
+};
+
 // Streaming multiprocessors of the current device (cudaDevAttrMultiProcessorCount),
 // queried once per device; grids are sized in multiples of it.
 inline int sm_count() {
@@ -465,6 +494,7 @@ struct pg_context {
     long long bo_stride = 0;  // entries per section of the bond-pass scratch (>= sh_total)
 
     // neighbour-build scratch
+    pg::DevBuf<float4> nb_posf;     // positions rounded to FP32 for the stencil scan's screen
     pg::DevBuf<int> cell_of, cell_start, sorted_atoms, wrap, keys_a, keys_b, vals_a, vals_b, radix_hist, count_tmp,
         invisible;
     pg::DevBuf<long long> g0_keys;
@@ -475,6 +505,7 @@ struct pg_context {
     pg::DevBuf<int> nb_totals;     // build totals on the device: out-of-range atoms, entries, lower-index entries
     pg::PinnedBuf<int> h_totals;   // their host copy (one synchronisation per build)
     std::vector<double> h_cutoffs;  // cutoffs of the last engine build (rebuilds on the device coordinates)
+    pg::SegGraph seg_g[6];          // captured stages of the list build (neighbor.cu)
     int list_kind = 0;              // PG_LIST_*: who built the lists
 
     // bond-order scratch
@@ -559,7 +590,9 @@ CellK cell_kernel_view(const Cell& C);
 
 // neighbor.cu
 void build_neighbor_lists(pg_context* ctx, const double* h_cutoffs);
-void build_short_list(pg_context* ctx);
+// same_positions: pos0 holds the positions the cell-list build ran at (the
+// list generation's reference positions were taken right after it)
+void build_short_list(pg_context* ctx, bool same_positions = false);
 void build_full_sep0(pg_context* ctx);
 void launch_disp(pg_context* ctx, const int* skip, FxAcc* zero8 = nullptr);
 void build_allpairs_lists(pg_context* ctx, const double* h_cutoffs);

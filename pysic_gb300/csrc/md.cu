@@ -222,7 +222,7 @@ static void rebuild_lists(pg_context* ctx) {
     if (ctx->list_kind == PG_LIST_CELLS) build_neighbor_lists(ctx, ctx->h_cutoffs.data());
     else build_allpairs_lists(ctx, ctx->h_cutoffs.data());
     build_full_sep0(ctx);
-    if (ctx->have_bond_terms) build_short_list(ctx);
+    if (ctx->have_bond_terms) build_short_list(ctx, true);
 }
 
 // what the captured step's kernel arguments depend on beyond the context's

@@ -41,10 +41,11 @@ struct Split {
 // wrapped_coordinates + find_subcell_for_atom (Geometry.f90:597-619, 884-924)
 __global__ void nb_assign(int n, const double* __restrict__ pos, CellK C, Split S, int* __restrict__ cell_of,
                           int* __restrict__ key, int* __restrict__ val, int* __restrict__ wrap,
-                          int* __restrict__ invisible) {
+                          int* __restrict__ invisible, float4* __restrict__ posf) {
     int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
     double p[3] = {pos[3 * i], pos[3 * i + 1], pos[3 * i + 2]};
+    posf[i] = make_float4((float)p[0], (float)p[1], (float)p[2], 0.0f);  // the stencil scan's FP32 screen
     double rel[3];
     for (int r = 0; r < 3; ++r)
         rel[r] = __dadd_rn(__dadd_rn(__dmul_rn(C.ic[r][0], p[0]), __dmul_rn(C.ic[r][1], p[1])),
@@ -157,36 +158,58 @@ __global__ void cell_starts(int n, int ncell, const int* __restrict__ skeys, int
     for (int c = lo + 1; c <= hi && c <= ncell; ++c) start[c] = p;
 }
 
-// single-block exclusive scan (build-time sizes only)
+// Single-block exclusive scan (build-time sizes): out[0..n-1] the exclusive
+// prefix sums of in (of its squares with square), out[n] and *total (may be
+// null) the sum.  The block walks the input in tiles of blockDim.x x 8
+// consecutive elements per thread, scans each tile with warp shuffles and
+// carries the running sum; integer sums, so the result is independent of the
+// order.
 template <typename T, typename U>
-__global__ void scan_single_block(const T* __restrict__ in, U* __restrict__ out, int n, U* __restrict__ total,
-                                  int square) {
-    __shared__ U part[1024];
-    const int t = threadIdx.x, nt = blockDim.x;
-    const long long per = ((long long)n + nt - 1) / nt;
-    long long b = per * t, e = min((long long)n, b + per);
-    U s = 0;
-    for (long long i = b; i < e; ++i) {
-        U v = (U)in[i];
-        s += square ? v * v : v;
-    }
-    part[t] = s;
-    __syncthreads();
-    for (int off = 1; off < nt; off <<= 1) {
-        U v = t >= off ? part[t - off] : 0;
+__global__ void __launch_bounds__(1024) scan_single_block(const T* __restrict__ in, U* __restrict__ out, int n,
+                                                           U* __restrict__ total, int square) {
+    constexpr int PER = 8;
+    __shared__ U wsum[32];
+    const int t = threadIdx.x, lane = t & 31, w = t >> 5, nw = blockDim.x >> 5;
+    U carry = 0;
+    for (long long base = 0; base < n; base += (long long)blockDim.x * PER) {
+        const long long i0 = base + (long long)t * PER;
+        U v[PER];
+        U s = 0;
+#pragma unroll
+        for (int k = 0; k < PER; ++k) {
+            U x = i0 + k < n ? (U)in[i0 + k] : (U)0;
+            if (square) x *= x;
+            v[k] = s;
+            s += x;
+        }
+        U incl = s;  // inclusive over the warp's threads
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            const U y = __shfl_up_sync(0xffffffffu, incl, o);
+            if (lane >= o) incl += y;
+        }
+        if (lane == 31) wsum[w] = incl;
         __syncthreads();
-        part[t] += v;
+        if (w == 0) {
+            U x = lane < nw ? wsum[lane] : (U)0;
+#pragma unroll
+            for (int o = 1; o < 32; o <<= 1) {
+                const U y = __shfl_up_sync(0xffffffffu, x, o);
+                if (lane >= o) x += y;
+            }
+            if (lane < nw) wsum[lane] = x;  // inclusive over warps
+        }
         __syncthreads();
+        const U pre = carry + (w > 0 ? wsum[w - 1] : (U)0) + (incl - s);
+#pragma unroll
+        for (int k = 0; k < PER; ++k)
+            if (i0 + k < n) out[i0 + k] = pre + v[k];
+        carry += wsum[nw - 1];
+        __syncthreads();  // wsum is rewritten by the next tile
     }
-    U run = t == 0 ? 0 : part[t - 1];
-    for (long long i = b; i < e; ++i) {
-        out[i] = run;
-        U v = (U)in[i];
-        run += square ? v * v : v;
-    }
-    if (t == nt - 1) {
-        out[n] = part[nt - 1];
-        if (total) *total = part[nt - 1];
+    if (t == 0) {
+        out[n] = carry;
+        if (total) *total = carry;
     }
 }
 
@@ -227,6 +250,39 @@ __device__ __forceinline__ double sep_d2(const CellK& C, const double* ra, const
     return __dadd_rn(__dadd_rn(__dmul_rn(s[0], s[0]), __dmul_rn(s[1], s[1])), __dmul_rn(s[2], s[2]));
 }
 
+// FP32 screen of the FP64 test sep_d2(...) < cut2, so that the FP64 pipe (a
+// small fraction of the FP32 rate on this GPU) sees only the candidates near
+// the cutoff: 1 when the FP64 test surely passes, 0 when it surely fails, -1
+// when the FP32 value lies within its rounding band (the caller decides in
+// FP64).  ra, rb: the positions rounded to FP32; vc: the cell rounded to FP32.
+// Each component of the separation is a sum of terms of size at most m (the
+// largest |coordinate|, |offset term| or |separation|), so its FP32 error is
+// below 8 u m (u = 2^-24), and that of d2 below 28 u m sqrt(d2) + 3 u d2 + 200
+// u^2 m^2; the band used is more than twice that (and covers the rounding of
+// cut2 to FP32), so a certain verdict is the FP64 one.
+__device__ __forceinline__ int screen_d2(const float ra[3], const float4 rb, const int o[3], const float (&vc)[3][3],
+                                         float cut2) {
+    float s[3] = {rb.x - ra[0], rb.y - ra[1], rb.z - ra[2]};
+    float m = fmaxf(fmaxf(fabsf(ra[0]), fabsf(ra[1])), fabsf(ra[2]));
+    m = fmaxf(m, fmaxf(fmaxf(fabsf(rb.x), fabsf(rb.y)), fabsf(rb.z)));
+    if (o[0] | o[1] | o[2]) {
+        const float of[3] = {(float)o[0], (float)o[1], (float)o[2]};
+        for (int c = 0; c < 3; ++c) {
+            const float t0 = of[0] * vc[c][0], t1 = of[1] * vc[c][1], t2 = of[2] * vc[c][2];
+            m = fmaxf(m, fabsf(t0) + fabsf(t1) + fabsf(t2));
+            s[c] += (t0 + t1) + t2;
+        }
+    }
+    const float d2 = s[0] * s[0] + s[1] * s[1] + s[2] * s[2];
+    const float D = fmaxf(d2, cut2);
+    const float rD = sqrtf(D);
+    m = fmaxf(m, rD);
+    const float tol = 1.1920929e-7f * (32.0f * m * rD + 8.0f * D) + 2.3283064e-10f * m * m;
+    if (d2 < cut2 - tol) return 1;
+    if (d2 > cut2 + tol) return 0;
+    return -1;
+}
+
 __device__ __forceinline__ bool lex_positive(const int o[3]) {
     if (o[0] != 0) return o[0] > 0;
     if (o[1] != 0) return o[1] > 0;
@@ -236,6 +292,8 @@ __device__ __forceinline__ bool lex_positive(const int o[3]) {
 struct ScanArgs {
     int n;
     const double* pos;
+    const float4* posf;  // positions rounded to FP32 (screen)
+    float vcf[3][3];     // cell rounded to FP32 (screen)
     const double* cut;
     const int* cell_of;
     const int* wrap;
@@ -270,6 +328,9 @@ __global__ void __launch_bounds__(SCAN_THREADS) nb_scan(ScanArgs A) {
     if (a >= A.n) return;  // whole warps
     const double ra[3] = {A.pos[3 * a], A.pos[3 * a + 1], A.pos[3 * a + 2]};
     const double cut2 = __dmul_rn(A.cut[a], A.cut[a]);
+    const float4 pa = A.posf[a];
+    const float raf[3] = {pa.x, pa.y, pa.z};
+    const float cut2f = (float)cut2;
     const int ci[3] = {A.cell_of[3 * a], A.cell_of[3 * a + 1], A.cell_of[3 * a + 2]};
     const int wa[3] = {A.wrap[3 * a], A.wrap[3 * a + 1], A.wrap[3 * a + 2]};
     const bool visible = A.invisible[a] == 0;
@@ -332,8 +393,13 @@ __global__ void __launch_bounds__(SCAN_THREADS) nb_scan(ScanArgs A) {
             }
             if (mult) {
                 for (int q = 0; q < 3; ++q) o[q] = noff[q] - wa[q] + A.wrap[3 * b + q];
-                const double rb[3] = {A.pos[3 * b], A.pos[3 * b + 1], A.pos[3 * b + 2]};
-                if (!(sep_d2(A.C, ra, rb, o) < cut2)) mult = 0;
+                const int v = screen_d2(raf, A.posf[b], o, A.vcf, cut2f);
+                if (v == 0) {
+                    mult = 0;
+                } else if (v < 0) {
+                    const double rb[3] = {A.pos[3 * b], A.pos[3 * b + 1], A.pos[3 * b + 2]};
+                    if (!(sep_d2(A.C, ra, rb, o) < cut2)) mult = 0;
+                }
             }
         }
         const unsigned m0 = __ballot_sync(0xffffffffu, mult && grp == 0);
@@ -489,9 +555,12 @@ __global__ void short_sep0(int n, const double* __restrict__ pos, CellK C, const
     }
 }
 
-__global__ void entry_types(int m, const int* __restrict__ idx, const int* __restrict__ type, int* __restrict__ out) {
-    int e = blockIdx.x * blockDim.x + threadIdx.x;
-    if (e < m) out[e] = type[idx[e]];
+// partner type of every short-list entry; the entry count is read on the
+// device, so that the launch does not depend on it
+__global__ void entry_types(const int* __restrict__ m_dev, const int* __restrict__ idx, const int* __restrict__ type,
+                            int* __restrict__ out) {
+    const int m = *m_dev;
+    for (int e = blockIdx.x * blockDim.x + threadIdx.x; e < m; e += gridDim.x * blockDim.x) out[e] = type[idx[e]];
 }
 
 __global__ void short_reverse(int n, const int* __restrict__ start, const int* __restrict__ idx,
@@ -594,6 +663,8 @@ __global__ void allpairs_scan(int n, const double* __restrict__ pos, const doubl
 }
 
 inline int blocks(long long n, int t) { return (int)((n + t - 1) / t); }
+// a grid-stride launch over about 8 entries per atom, at most 4 blocks per SM
+inline int copy_grid(int n) { return std::max(1, std::min(blocks(8ll * n, 256), 4 * sm_count())); }
 
 }  // namespace
 
@@ -630,6 +701,59 @@ void exclusive_scan_int(const int* in, int* out, int n, cudaStream_t s, DevBuf<i
     }
 }
 
+// Run seq on the context's stream from its captured graph g when sig matches
+// the values the graph was built from; otherwise capture seq anew (updating
+// the executable graph in place when the topology allows) and launch it.
+// Host work (buffer sizing) happens before, outside seq.
+template <typename F>
+static void run_segment(pg_context* ctx, SegGraph& g, unsigned long long sig, F&& seq) {
+    if (!ctx->use_graphs) {
+        seq();
+        return;
+    }
+    if (g.exec && g.sig == sig) {
+        PG_CUDA(cudaGraphLaunch(g.exec, ctx->stream));
+        return;
+    }
+    cudaGraph_t graph = nullptr;
+    PG_CUDA(cudaStreamBeginCapture(ctx->stream, cudaStreamCaptureModeThreadLocal));
+    try {
+        seq();
+    } catch (...) {
+        cudaStreamEndCapture(ctx->stream, &graph);
+        if (graph) cudaGraphDestroy(graph);
+        throw;
+    }
+    PG_CUDA(cudaStreamEndCapture(ctx->stream, &graph));
+    bool updated = false;
+    if (g.exec) {
+        cudaGraphExecUpdateResultInfo info{};
+        updated = cudaGraphExecUpdate(g.exec, graph, &info) == cudaSuccess;
+        if (!updated) {
+            (void)cudaGetLastError();  // a failed update leaves no sticky error
+            cudaGraphExecDestroy(g.exec);
+            g.exec = nullptr;
+        }
+    }
+    if (!updated) {
+        const cudaError_t e = cudaGraphInstantiate(&g.exec, graph, 0);
+        if (e != cudaSuccess) g.exec = nullptr;
+        cudaGraphDestroy(graph);
+        PG_CUDA(e);
+    } else {
+        cudaGraphDestroy(graph);
+    }
+    g.sig = sig;
+    PG_CUDA(cudaGraphLaunch(g.exec, ctx->stream));
+}
+
+static SigHash& add_cell(SigHash& h, const CellK& C) {
+    for (int r = 0; r < 3; ++r)
+        for (int c = 0; c < 3; ++c) h.add(C.vc[r][c]).add(C.ic[r][c]);
+    for (int a = 0; a < 3; ++a) h.add(C.pbc[a]);
+    return h;
+}
+
 void build_neighbor_lists(pg_context* ctx, const double* h_cutoffs) {
     const int n = ctx->n;
     cudaStream_t st = ctx->stream;
@@ -660,52 +784,28 @@ void build_neighbor_lists(pg_context* ctx, const double* h_cutoffs) {
     ctx->vals_b.resize(std::max(n, 1));
     ctx->invisible.resize(std::max(n, 1) + 1);
     ctx->cell_start.resize(ncell + 1);
-    if (n > 0) {
-        nb_assign<<<blocks(n, 256), 256, 0, st>>>(n, ctx->pos.p, C, S, ctx->cell_of.p, ctx->keys_a.p, ctx->vals_a.p,
-                                                  ctx->wrap.p, ctx->invisible.p);
-        PG_CHECK_LAUNCH();
-    }
-    // radix sort by subcell id
+    ctx->nb_posf.resize(std::max(n, 1));
     int bits = 1;
     while ((1 << bits) < ncell) ++bits;
     const int passes = (bits + 7) / 8;
     const int nblk = std::max(1, blocks(n, RS_TILE));
     ctx->radix_hist.resize((size_t)256 * nblk + 1);
     ctx->count_tmp.resize((size_t)256 * nblk + 1);
-    int *k_in = ctx->keys_a.p, *v_in = ctx->vals_a.p, *k_out = ctx->keys_b.p, *v_out = ctx->vals_b.p;
-    for (int p = 0; p < passes && n > 0; ++p) {
-        radix_hist<<<nblk, RS_THREADS, 0, st>>>(n, k_in, 8 * p, nblk, ctx->radix_hist.p);
-        PG_CHECK_LAUNCH();
-        scan_single_block<int, int><<<1, 1024, 0, st>>>(ctx->radix_hist.p, ctx->count_tmp.p, 256 * nblk, nullptr, 0);
-        PG_CHECK_LAUNCH();
-        radix_scatter<<<nblk, RS_THREADS, 0, st>>>(n, k_in, v_in, 8 * p, nblk, ctx->count_tmp.p, k_out, v_out);
-        PG_CHECK_LAUNCH();
-        std::swap(k_in, k_out);
-        std::swap(v_in, v_out);
-    }
-    const int* sorted_keys = k_in;
-    const int* sorted_vals = v_in;
-    cell_starts<<<blocks(n + 1, 256), 256, 0, st>>>(n, ncell, sorted_keys, ctx->cell_start.p);
-    PG_CHECK_LAUNCH();
     ctx->sorted_atoms.resize(std::max(n, 1));
-    if (n > 0)
-        PG_CUDA(cudaMemcpyAsync(ctx->sorted_atoms.p, sorted_vals, sizeof(int) * n, cudaMemcpyDeviceToDevice, st));
-
-    // atoms in out-of-range periodic subcells: their count stays on the device
     ctx->scan_tmp.resize(std::max(n, 1) + 1);
     ctx->nb_totals.resize(4);  // [0] out-of-range atoms, [1] list entries, [2] lower-index entries
-    scan_single_block<int, int><<<1, 1024, 0, st>>>(ctx->invisible.p, ctx->scan_tmp.p, n, ctx->nb_totals.p, 0);
-    PG_CHECK_LAUNCH();
+    ctx->nb_g0.resize(std::max(n, 1));
+    ctx->nb_start.resize(n + 1);
+    ctx->g0_start.resize(n + 1);
+    int* ht = ctx->h_totals.get(4);
     DevBuf<int>& inv_list = ctx->keys_b;  // free after the sort
-    if (n > 0) {
-        compact_flags<<<blocks(n, 256), 256, 0, st>>>(n, ctx->invisible.p, ctx->scan_tmp.p, inv_list.p);
-        PG_CHECK_LAUNCH();
-    }
-    // inv_list may alias the sort's output buffer: copy the sorted atoms first (done above)
 
     ScanArgs A{};
     A.n = n;
     A.pos = ctx->pos.p;
+    A.posf = ctx->nb_posf.p;
+    for (int r = 0; r < 3; ++r)
+        for (int c = 0; c < 3; ++c) A.vcf[r][c] = (float)C.vc[r][c];
     A.cut = ctx->cutoffs.p;
     A.cell_of = ctx->cell_of.p;
     A.wrap = ctx->wrap.p;
@@ -716,29 +816,57 @@ void build_neighbor_lists(pg_context* ctx, const double* h_cutoffs) {
     A.n_inv = ctx->nb_totals.p;
     A.C = C;
     A.S = S;
-    ctx->nb_g0.resize(std::max(n, 1));
-    ctx->vals_a.resize(std::max(n, 1));
     A.g0count = ctx->nb_g0.p;
     A.g1count = ctx->vals_a.p;
-    if (n > 0) {
-        nb_scan<false><<<blocks((long long)n * 32, SCAN_THREADS), SCAN_THREADS, 0, st>>>(A);
+
+    // stage 1: subcells, the sort by subcell, the counting scan and both
+    // prefix sums, whose totals come back with one synchronisation
+    auto stage1 = [&] {
+        if (n > 0) {
+            nb_assign<<<blocks(n, 256), 256, 0, st>>>(n, ctx->pos.p, C, S, ctx->cell_of.p, ctx->keys_a.p,
+                                                      ctx->vals_a.p, ctx->wrap.p, ctx->invisible.p, ctx->nb_posf.p);
+            PG_CHECK_LAUNCH();
+        }
+        // radix sort by subcell id
+        int *k_in = ctx->keys_a.p, *v_in = ctx->vals_a.p, *k_out = ctx->keys_b.p, *v_out = ctx->vals_b.p;
+        for (int p = 0; p < passes && n > 0; ++p) {
+            radix_hist<<<nblk, RS_THREADS, 0, st>>>(n, k_in, 8 * p, nblk, ctx->radix_hist.p);
+            PG_CHECK_LAUNCH();
+            scan_single_block<int, int><<<1, 1024, 0, st>>>(ctx->radix_hist.p, ctx->count_tmp.p, 256 * nblk, nullptr,
+                                                            0);
+            PG_CHECK_LAUNCH();
+            radix_scatter<<<nblk, RS_THREADS, 0, st>>>(n, k_in, v_in, 8 * p, nblk, ctx->count_tmp.p, k_out, v_out);
+            PG_CHECK_LAUNCH();
+            std::swap(k_in, k_out);
+            std::swap(v_in, v_out);
+        }
+        cell_starts<<<blocks(n + 1, 256), 256, 0, st>>>(n, ncell, k_in, ctx->cell_start.p);
         PG_CHECK_LAUNCH();
-    }
-    // CSR starts and lower-index key buffer starts
-    ctx->nb_start.resize(n + 1);
-    ctx->g0_start.resize(n + 1);
-    ctx->keys_a.resize(std::max(n, 1));
-    if (n > 0) {
-        add_counts<<<blocks(n, 256), 256, 0, st>>>(n, ctx->nb_g0.p, ctx->vals_a.p, ctx->keys_a.p);
+        if (n > 0)
+            PG_CUDA(cudaMemcpyAsync(ctx->sorted_atoms.p, v_in, sizeof(int) * n, cudaMemcpyDeviceToDevice, st));
+        // atoms in out-of-range periodic subcells: their count stays on the device
+        scan_single_block<int, int><<<1, 1024, 0, st>>>(ctx->invisible.p, ctx->scan_tmp.p, n, ctx->nb_totals.p, 0);
         PG_CHECK_LAUNCH();
-    }
-    // both scans' totals come back with one synchronisation
-    scan_single_block<int, int><<<1, 1024, 0, st>>>(ctx->keys_a.p, ctx->nb_start.p, n, ctx->nb_totals.p + 1, 0);
-    PG_CHECK_LAUNCH();
-    scan_single_block<int, int><<<1, 1024, 0, st>>>(ctx->nb_g0.p, ctx->g0_start.p, n, ctx->nb_totals.p + 2, 0);
-    PG_CHECK_LAUNCH();
-    int* ht = ctx->h_totals.get(4);
-    PG_CUDA(cudaMemcpyAsync(ht, ctx->nb_totals.p, sizeof(int) * 4, cudaMemcpyDeviceToHost, st));
+        // inv_list may alias the sort's output buffer: the sorted atoms were copied first
+        if (n > 0) {
+            compact_flags<<<blocks(n, 256), 256, 0, st>>>(n, ctx->invisible.p, ctx->scan_tmp.p, inv_list.p);
+            PG_CHECK_LAUNCH();
+            nb_scan<false><<<blocks((long long)n * 32, SCAN_THREADS), SCAN_THREADS, 0, st>>>(A);
+            PG_CHECK_LAUNCH();
+            // CSR starts and lower-index key buffer starts
+            add_counts<<<blocks(n, 256), 256, 0, st>>>(n, ctx->nb_g0.p, ctx->vals_a.p, ctx->keys_a.p);
+            PG_CHECK_LAUNCH();
+        }
+        scan_single_block<int, int><<<1, 1024, 0, st>>>(ctx->keys_a.p, ctx->nb_start.p, n, ctx->nb_totals.p + 1, 0);
+        PG_CHECK_LAUNCH();
+        scan_single_block<int, int><<<1, 1024, 0, st>>>(ctx->nb_g0.p, ctx->g0_start.p, n, ctx->nb_totals.p + 2, 0);
+        PG_CHECK_LAUNCH();
+        PG_CUDA(cudaMemcpyAsync(ht, ctx->nb_totals.p, sizeof(int) * 4, cudaMemcpyDeviceToHost, st));
+    };
+    SigHash h1;
+    h1.add(alloc_epoch()).add(n).add(ncell).add(passes).add(nblk).add(S).add(ht);
+    add_cell(h1, C);
+    run_segment(ctx, ctx->seg_g[0], h1.h, stage1);
     PG_CUDA(cudaStreamSynchronize(st));
     const int total = ht[1], total0 = ht[2];
     ctx->nb_total = total;
@@ -752,14 +880,21 @@ void build_neighbor_lists(pg_context* ctx, const double* h_cutoffs) {
     A.g0val = ctx->g0_vals.p;
     A.idx = ctx->nb_idx.p;
     A.off = ctx->nb_off.p;
-    if (n > 0) {
-        nb_scan<true><<<blocks((long long)n * 32, SCAN_THREADS), SCAN_THREADS, 0, st>>>(A);
-        PG_CHECK_LAUNCH();
-        nb_sort_g0<<<blocks((long long)n * 32, 256), 256, 0, st>>>(n, ctx->nb_g0.p, ctx->g0_start.p, ctx->nb_start.p,
-                                                                  ctx->g0_keys.p, ctx->g0_vals.p, ctx->nb_idx.p,
-                                                                  ctx->nb_off.p);
-        PG_CHECK_LAUNCH();
-    }
+    // stage 2: the filling scan and the order of the lower-index entries
+    auto stage2 = [&] {
+        if (n > 0) {
+            nb_scan<true><<<blocks((long long)n * 32, SCAN_THREADS), SCAN_THREADS, 0, st>>>(A);
+            PG_CHECK_LAUNCH();
+            nb_sort_g0<<<blocks((long long)n * 32, 256), 256, 0, st>>>(n, ctx->nb_g0.p, ctx->g0_start.p,
+                                                                      ctx->nb_start.p, ctx->g0_keys.p, ctx->g0_vals.p,
+                                                                      ctx->nb_idx.p, ctx->nb_off.p);
+            PG_CHECK_LAUNCH();
+        }
+    };
+    SigHash h2;
+    h2.add(alloc_epoch()).add(n).add(S);
+    add_cell(h2, C);
+    run_segment(ctx, ctx->seg_g[1], h2.h, stage2);
     // the cutoffs (host copy) for rebuilds on the device coordinates
     if (h_cutoffs != ctx->h_cutoffs.data()) ctx->h_cutoffs.assign(h_cutoffs, h_cutoffs + n);
     ctx->list_kind = PG_LIST_CELLS;
@@ -768,7 +903,6 @@ void build_neighbor_lists(pg_context* ctx, const double* h_cutoffs) {
     ctx->state_epoch++;
     ctx->short_dirty = true;
 }
-
 
 void build_allpairs_lists(pg_context* ctx, const double* h_cutoffs) {
     const int n = ctx->n;
@@ -860,17 +994,22 @@ void build_full_sep0(pg_context* ctx) {
     ctx->pos0.resize(3 * (size_t)std::max(n, 1));
     ctx->nb_sep0.resize((size_t)std::max<long long>(ctx->nb_total, 1));
     if (n > 0) {
-        PG_CUDA(cudaMemcpyAsync(ctx->pos0.p, ctx->pos.p, sizeof(double) * 3 * n, cudaMemcpyDeviceToDevice, st));
-        short_sep0<<<blocks(n, 128), 128, 0, st>>>(n, ctx->pos0.p, C, ctx->nb_start.p, ctx->nb_idx.p, ctx->nb_off.p,
-                                                  ctx->nb_sep0.p);
-        PG_CHECK_LAUNCH();
+        SigHash h;
+        h.add(alloc_epoch()).add(n);
+        add_cell(h, C);
+        run_segment(ctx, ctx->seg_g[2], h.h, [&] {
+            PG_CUDA(cudaMemcpyAsync(ctx->pos0.p, ctx->pos.p, sizeof(double) * 3 * n, cudaMemcpyDeviceToDevice, st));
+            short_sep0<<<blocks(n, 128), 128, 0, st>>>(n, ctx->pos0.p, C, ctx->nb_start.p, ctx->nb_idx.p,
+                                                      ctx->nb_off.p, ctx->nb_sep0.p);
+            PG_CHECK_LAUNCH();
+        });
     }
     ctx->sep0_epoch = ctx->list_epoch;
     ctx->short_dirty = true;
     ctx->state_epoch++;
 }
 
-void build_short_list(pg_context* ctx) {
+void build_short_list(pg_context* ctx, bool same_positions) {
     const int n = ctx->n;
     cudaStream_t st = ctx->stream;
     const double r = ctx->bo_radius + ctx->skin;
@@ -878,63 +1017,96 @@ void build_short_list(pg_context* ctx) {
     const double* p0 = ctx->pos0.p;  // positions of this list generation
     ctx->sh_count.resize(std::max(n, 1));
     ctx->sh_start.resize(n + 1);
-    if (n > 0) {
-        short_count<<<blocks(n, 128), 128, 0, st>>>(n, p0, C, ctx->nb_start.p, ctx->nb_idx.p, ctx->nb_off.p,
-                                                   r * r, ctx->sh_count.p);
+    ctx->nb_totals.resize(4);
+    int* ht = ctx->h_totals.get(4);
+    // The short list is the full list itself when the cell-list build ran at
+    // the generation's reference positions and no atom's list radius exceeds
+    // r: every entry passed the same FP64 test (sep_d2) against a radius <= r,
+    // so it passes against r (silicon: 3.0 + 0.5 A both).  Its entries and
+    // bond vectors are then copied, and the count and its synchronisation
+    // skipped.
+    double max_cut = 0.0;
+    for (double c : ctx->h_cutoffs) max_cut = std::max(max_cut, c);
+    const bool copy_full = same_positions && ctx->list_kind == PG_LIST_CELLS && n > 0 &&
+                           (int)ctx->h_cutoffs.size() == n && max_cut <= r && ctx->sep0_epoch == ctx->list_epoch;
+    // stage 1: the short lists' lengths and starts; the total comes back
+    auto stage1 = [&] {
+        if (n > 0) {
+            short_count<<<blocks(n, 128), 128, 0, st>>>(n, p0, C, ctx->nb_start.p, ctx->nb_idx.p, ctx->nb_off.p,
+                                                       r * r, ctx->sh_count.p);
+            PG_CHECK_LAUNCH();
+        }
+        scan_single_block<int, int><<<1, 1024, 0, st>>>(ctx->sh_count.p, ctx->sh_start.p, n, ctx->nb_totals.p + 3, 0);
         PG_CHECK_LAUNCH();
-    }
+        PG_CUDA(cudaMemcpyAsync(ht + 3, ctx->nb_totals.p + 3, sizeof(int), cudaMemcpyDeviceToHost, st));
+    };
     int total = 0;
-    exclusive_scan_int(ctx->sh_count.p, ctx->sh_start.p, n, st, ctx->count_tmp, &total);
-    ctx->sh_total = total;
-    ctx->sh_idx.resize(std::max(total, 1));
-    ctx->sh_off.resize(3 * (size_t)std::max(total, 1));
-    ctx->sh_rev.resize(std::max(total, 1));
-    if (n > 0) {
-        short_fill<<<blocks(n, 128), 128, 0, st>>>(n, p0, C, ctx->nb_start.p, ctx->nb_idx.p, ctx->nb_off.p,
-                                                  r * r, ctx->sh_start.p, ctx->sh_idx.p, ctx->sh_off.p);
-        PG_CHECK_LAUNCH();
-        short_reverse<<<blocks(n, 128), 128, 0, st>>>(n, ctx->sh_start.p, ctx->sh_idx.p, ctx->sh_off.p, ctx->sh_rev.p,
-                                                     ctx->sh_count.p);
-        PG_CHECK_LAUNCH();
-    }
-    // bond vectors of this list generation and partner types
-    ctx->sh_sep0.resize(std::max(total, 1));
-    ctx->sh_type.resize(std::max(total, 1));
-    if (n > 0) {
-        short_sep0<<<blocks(n, 128), 128, 0, st>>>(n, p0, C, ctx->sh_start.p, ctx->sh_idx.p, ctx->sh_off.p,
-                                                  ctx->sh_sep0.p);
-        PG_CHECK_LAUNCH();
-        entry_types<<<blocks(std::max(total, 1), 256), 256, 0, st>>>(total, ctx->sh_idx.p, ctx->type.p,
-                                                                    ctx->sh_type.p);
-        PG_CHECK_LAUNCH();
-    }
-    // Lists from the host may lack reverse entries: checked before use.  The
-    // engine's own builds are symmetric by construction.
-    if (ctx->list_kind == PG_LIST_INSTALLED) {
-        DevBuf<int> mx;
-        mx.resize(1);
-        min_reduce<<<1, 1024, 0, st>>>(std::max(total, 1) * (total > 0), ctx->sh_rev.p, mx.p);
-        PG_CHECK_LAUNCH();
-        int h = 0;
-        PG_CUDA(cudaMemcpyAsync(&h, mx.p, sizeof(int), cudaMemcpyDeviceToHost, st));
+    if (copy_full) {
+        total = (int)ctx->nb_total;
+    } else {
+        SigHash h1;
+        h1.add(alloc_epoch()).add(n).add(r).add(ht);
+        add_cell(h1, C);
+        run_segment(ctx, ctx->seg_g[3], h1.h, stage1);
         PG_CUDA(cudaStreamSynchronize(st));
-        require(total == 0 || h >= 0, PG_ERR_INVALID,
-                "neighbour lists are not symmetric: a bond has no reverse entry (lists must be built both ways)");
+        total = ht[3];
     }
-    // atoms grouped by list length, stably (ties in index order), so that the
-    // lane groups of one warp loop over the same number of bonds: a two-digit
-    // radix sort of (count, atom) on the device (counts below 65536), then per
-    // slot (atom, first entry, count)
+    ctx->sh_total = total;
+    if (copy_full) {  // room for whole copies of the full list's buffers: sizes that do not move with the total
+        ctx->sh_idx.resize(ctx->nb_idx.cap);
+        ctx->sh_off.resize(ctx->nb_off.cap);
+        ctx->sh_sep0.resize(ctx->nb_sep0.cap);
+    } else {
+        ctx->sh_idx.resize(std::max(total, 1));
+        ctx->sh_off.resize(3 * (size_t)std::max(total, 1));
+        ctx->sh_sep0.resize(std::max(total, 1));  // bond vectors of this list generation
+    }
+    ctx->sh_rev.resize(std::max(total, 1));
+    ctx->sh_type.resize(std::max(total, 1));
     ctx->sh_order.resize(std::max(n, 1));
     ctx->sh_slot.resize(std::max(n, 1));
+    const int nblk = std::max(1, blocks(n, RS_TILE));
     if (n > 0) {
         ctx->keys_a.resize(n);
         ctx->keys_b.resize(n);
         ctx->vals_a.resize(n);
         ctx->vals_b.resize(n);
-        const int nblk = std::max(1, blocks(n, RS_TILE));
         ctx->radix_hist.resize((size_t)256 * nblk + 1);
         ctx->count_tmp.resize((size_t)256 * nblk + 1);
+    }
+    // stage 2: fill, reverse entries, bond vectors, partner types, and the
+    // atoms grouped by list length, stably (ties in index order), so that the
+    // lane groups of one warp loop over the same number of bonds: a two-digit
+    // radix sort of (count, atom) on the device (counts below 65536), then per
+    // slot (atom, first entry, count).  No launch depends on the total.
+    auto stage2 = [&] {
+        if (n == 0) return;
+        if (copy_full) {
+            PG_CUDA(cudaMemcpyAsync(ctx->sh_start.p, ctx->nb_start.p, sizeof(int) * (n + 1), cudaMemcpyDeviceToDevice,
+                                    st));
+            PG_CUDA(cudaMemcpyAsync(ctx->sh_idx.p, ctx->nb_idx.p, sizeof(int) * ctx->nb_idx.cap,
+                                    cudaMemcpyDeviceToDevice, st));
+            PG_CUDA(cudaMemcpyAsync(ctx->sh_off.p, ctx->nb_off.p, sizeof(int) * ctx->nb_off.cap,
+                                    cudaMemcpyDeviceToDevice, st));
+            PG_CUDA(cudaMemcpyAsync(ctx->sh_sep0.p, ctx->nb_sep0.p, sizeof(F4) * ctx->nb_sep0.cap,
+                                    cudaMemcpyDeviceToDevice, st));
+            PG_CUDA(cudaMemcpyAsync(ctx->nb_totals.p + 3, ctx->nb_totals.p + 1, sizeof(int), cudaMemcpyDeviceToDevice,
+                                    st));
+        } else {
+            short_fill<<<blocks(n, 128), 128, 0, st>>>(n, p0, C, ctx->nb_start.p, ctx->nb_idx.p, ctx->nb_off.p,
+                                                      r * r, ctx->sh_start.p, ctx->sh_idx.p, ctx->sh_off.p);
+            PG_CHECK_LAUNCH();
+        }
+        short_reverse<<<blocks(n, 128), 128, 0, st>>>(n, ctx->sh_start.p, ctx->sh_idx.p, ctx->sh_off.p,
+                                                     ctx->sh_rev.p, ctx->sh_count.p);
+        PG_CHECK_LAUNCH();
+        if (!copy_full) {
+            short_sep0<<<blocks(n, 128), 128, 0, st>>>(n, p0, C, ctx->sh_start.p, ctx->sh_idx.p, ctx->sh_off.p,
+                                                      ctx->sh_sep0.p);
+            PG_CHECK_LAUNCH();
+        }
+        entry_types<<<copy_grid(n), 256, 0, st>>>(ctx->nb_totals.p + 3, ctx->sh_idx.p, ctx->type.p, ctx->sh_type.p);
+        PG_CHECK_LAUNCH();
         order_keys<<<blocks(n, 256), 256, 0, st>>>(n, ctx->sh_count.p, ctx->keys_a.p, ctx->vals_a.p);
         PG_CHECK_LAUNCH();
         int *k_in = ctx->keys_a.p, *v_in = ctx->vals_a.p, *k_out = ctx->keys_b.p, *v_out = ctx->vals_b.p;
@@ -952,6 +1124,23 @@ void build_short_list(pg_context* ctx) {
         order_slots<<<blocks(n, 256), 256, 0, st>>>(n, v_in, ctx->sh_start.p, ctx->sh_count.p, ctx->sh_order.p,
                                                     ctx->sh_slot.p);
         PG_CHECK_LAUNCH();
+    };
+    SigHash h2;
+    h2.add(alloc_epoch()).add(n).add(r).add(nblk).add(copy_full);
+    add_cell(h2, C);
+    run_segment(ctx, ctx->seg_g[copy_full ? 5 : 4], h2.h, stage2);
+    // Lists from the host may lack reverse entries: checked before use.  The
+    // engine's own builds are symmetric by construction.
+    if (ctx->list_kind == PG_LIST_INSTALLED) {
+        DevBuf<int> mx;
+        mx.resize(1);
+        min_reduce<<<1, 1024, 0, st>>>(std::max(total, 1) * (total > 0), ctx->sh_rev.p, mx.p);
+        PG_CHECK_LAUNCH();
+        int hm = 0;
+        PG_CUDA(cudaMemcpyAsync(&hm, mx.p, sizeof(int), cudaMemcpyDeviceToHost, st));
+        PG_CUDA(cudaStreamSynchronize(st));
+        require(total == 0 || hm >= 0, PG_ERR_INVALID,
+                "neighbour lists are not symmetric: a bond has no reverse entry (lists must be built both ways)");
     }
     ctx->short_dirty = false;
     ctx->state_epoch++;
