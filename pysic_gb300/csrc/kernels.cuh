@@ -452,8 +452,11 @@ __device__ __forceinline__ Fx128 fx_from(double v) { return fx_from_double(v); }
 // block's warps in warp order, and sends value c's limbs to acc from lane c.
 // Only one warp per block converts, and the 7 values go out in parallel.
 // `done` is a shared counter set to zero before the block's first barrier.
+// x0, wx (both null, or both set): an exact 128-bit warp total (the same in
+// every lane) added to value 0, through the per-warp shared slots wx.
 template <typename R>
-__device__ __forceinline__ void block_totals_add(const R (&t)[7], R (*wpart)[7], unsigned* done, FxAcc* acc) {
+__device__ __forceinline__ void block_totals_add(const R (&t)[7], R (*wpart)[7], unsigned* done, FxAcc* acc,
+                                                 const Fx128* x0 = nullptr, Fx128* wx = nullptr) {
     if (acc == nullptr) return;
     const int wl = threadIdx.x & 31, w = threadIdx.x >> 5, nw = blockDim.x >> 5;
     R s[7];
@@ -463,6 +466,7 @@ __device__ __forceinline__ void block_totals_add(const R (&t)[7], R (*wpart)[7],
     if (wl == 0) {
 #pragma unroll
         for (int c = 0; c < 7; ++c) wpart[w][c] = s[c];
+        if (x0) wx[w] = *x0;
         __threadfence_block();
         last = atomicAdd(done, 1u) == (unsigned)(nw - 1) ? 1u : 0u;
     }
@@ -473,6 +477,10 @@ __device__ __forceinline__ void block_totals_add(const R (&t)[7], R (*wpart)[7],
         for (int k = 0; k < nw; ++k) {
             const volatile R* q = &wpart[k][wl];
             x = fx_add(x, fx_from((R)*q));
+            if (x0 && wl == 0) {
+                const volatile Fx128* e = &wx[k];
+                x = fx_add(x, Fx128{e->lo, e->hi});
+            }
         }
         fx_red(&acc[wl], x);
     }

@@ -21,7 +21,8 @@ __device__ __forceinline__ double powi_(double x, int n) {
 // AF: also add the per-atom factor forces (no scaled pair term; W from af_sum)
 template <typename R, int G, bool AF = false>
 __device__ __forceinline__ void pair_body(const PairArgs& A, int blk) {
-    __shared__ Fx128 wsum[256 / 32][7];
+    __shared__ R wpart[256 / 32][7];
+    __shared__ Fx128 wx[256 / 32];
     __shared__ unsigned done;
     if (threadIdx.x == 0) done = 0u;
     __syncthreads();
@@ -294,9 +295,11 @@ __device__ __forceinline__ void pair_body(const PairArgs& A, int blk) {
     // energy and virial: warp sums, exact from there on
     if (A.acc && (wantE || wantF)) {
         // the single-atom energies join the total exactly, outside the working precision
-        const Fx128 v[7] = {fx_add(warp_total(en), fx_warp_sum(fx_from_double(es))), warp_total(w0), warp_total(w1),
-                            warp_total(w2), warp_total(w3), warp_total(w4), warp_total(w5)};
-        block_totals_publish(v, wsum, &done, A.acc);
+        // (skipped, as zero, when no lane of the warp has one)
+        Fx128 xs = fx_zero();
+        if (__any_sync(0xffffffffu, es != 0.0)) xs = fx_warp_sum(fx_from_double(es));
+        const R t[7] = {en, w0, w1, w2, w3, w4, w5};
+        block_totals_add(t, wpart, &done, A.acc, &xs, wx);
     }
 }
 
