@@ -160,35 +160,37 @@ __global__ void cell_starts(int n, int ncell, const int* __restrict__ skeys, int
 
 // Single-block exclusive scan (build-time sizes): out[0..n-1] the exclusive
 // prefix sums of in (of its squares with square), out[n] and *total (may be
-// null) the sum.  The block walks the input in tiles of blockDim.x x 8
-// consecutive elements per thread, scans each tile with warp shuffles and
-// carries the running sum; integer sums, so the result is independent of the
-// order.
+// null) the sum.  The block walks the input in tiles of 32 x blockDim.x
+// elements: warp w takes 32 rows of 32 consecutive elements (coalesced loads
+// and stores), scans each row with shuffles and carries its running sum, then
+// the warps' sums are scanned and the tile's sum carried.  Integer sums: the
+// result does not depend on the order.
 template <typename T, typename U>
 __global__ void __launch_bounds__(1024) scan_single_block(const T* __restrict__ in, U* __restrict__ out, int n,
                                                            U* __restrict__ total, int square) {
-    constexpr int PER = 8;
+    constexpr int ROWS = 32;
     __shared__ U wsum[32];
     const int t = threadIdx.x, lane = t & 31, w = t >> 5, nw = blockDim.x >> 5;
     U carry = 0;
-    for (long long base = 0; base < n; base += (long long)blockDim.x * PER) {
-        const long long i0 = base + (long long)t * PER;
-        U v[PER];
-        U s = 0;
+    for (long long base = 0; base < n; base += (long long)blockDim.x * ROWS) {
+        const long long chunk = base + (long long)w * 32 * ROWS;
+        U v[ROWS];
+        U run = 0;
 #pragma unroll
-        for (int k = 0; k < PER; ++k) {
-            U x = i0 + k < n ? (U)in[i0 + k] : (U)0;
+        for (int k = 0; k < ROWS; ++k) {
+            const long long i = chunk + 32 * k + lane;
+            U x = i < n ? (U)in[i] : (U)0;
             if (square) x *= x;
-            v[k] = s;
-            s += x;
-        }
-        U incl = s;  // inclusive over the warp's threads
+            U incl = x;
 #pragma unroll
-        for (int o = 1; o < 32; o <<= 1) {
-            const U y = __shfl_up_sync(0xffffffffu, incl, o);
-            if (lane >= o) incl += y;
+            for (int o = 1; o < 32; o <<= 1) {
+                const U y = __shfl_up_sync(0xffffffffu, incl, o);
+                if (lane >= o) incl += y;
+            }
+            v[k] = run + incl - x;
+            run += __shfl_sync(0xffffffffu, incl, 31);
         }
-        if (lane == 31) wsum[w] = incl;
+        if (lane == 0) wsum[w] = run;
         __syncthreads();
         if (w == 0) {
             U x = lane < nw ? wsum[lane] : (U)0;
@@ -200,10 +202,12 @@ __global__ void __launch_bounds__(1024) scan_single_block(const T* __restrict__ 
             if (lane < nw) wsum[lane] = x;  // inclusive over warps
         }
         __syncthreads();
-        const U pre = carry + (w > 0 ? wsum[w - 1] : (U)0) + (incl - s);
+        const U pre = carry + (w > 0 ? wsum[w - 1] : (U)0);
 #pragma unroll
-        for (int k = 0; k < PER; ++k)
-            if (i0 + k < n) out[i0 + k] = pre + v[k];
+        for (int k = 0; k < ROWS; ++k) {
+            const long long i = chunk + 32 * k + lane;
+            if (i < n) out[i] = pre + v[k];
+        }
         carry += wsum[nw - 1];
         __syncthreads();  // wsum is rewritten by the next tile
     }
@@ -507,6 +511,9 @@ __global__ void compact_flags(int n, const int* __restrict__ flag, const int* __
 }
 
 // ---- short list for bond-order terms -----------------------------------------
+// lanes per atom of the reverse-entry search (short_reverse)
+constexpr int ENTRY_LANES = 4;
+
 __device__ __forceinline__ double entry_d2(const CellK& C, const double* __restrict__ pos, int a, int b, const int* o) {
     const double ra[3] = {pos[3 * a], pos[3 * a + 1], pos[3 * a + 2]};
     const double rb[3] = {pos[3 * b], pos[3 * b + 1], pos[3 * b + 2]};
@@ -543,7 +550,7 @@ __global__ void short_fill(int n, const double* __restrict__ pos, CellK C, const
 // separation_vector (Geometry.f90:449-466) of every short-list entry, rounded to FP32
 __global__ void short_sep0(int n, const double* __restrict__ pos, CellK C, const int* __restrict__ start,
                            const int* __restrict__ idx, const int* __restrict__ off, F4* __restrict__ sep0) {
-    int a = blockIdx.x * blockDim.x + threadIdx.x;
+    const int a = blockIdx.x * blockDim.x + threadIdx.x;
     if (a >= n) return;
     for (int e = start[a]; e < start[a + 1]; ++e) {
         const int b = idx[e];
@@ -565,10 +572,11 @@ __global__ void entry_types(const int* __restrict__ m_dev, const int* __restrict
 
 __global__ void short_reverse(int n, const int* __restrict__ start, const int* __restrict__ idx,
                               const int* __restrict__ off, int* __restrict__ rev, int* __restrict__ cnt) {
-    int a = blockIdx.x * blockDim.x + threadIdx.x;
+    const long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+    const int a = (int)(t / ENTRY_LANES), l = (int)(t % ENTRY_LANES);
     if (a >= n) return;
-    cnt[a] = start[a + 1] - start[a];
-    for (int e = start[a]; e < start[a + 1]; ++e) {
+    if (l == 0) cnt[a] = start[a + 1] - start[a];
+    for (int e = start[a] + l; e < start[a + 1]; e += ENTRY_LANES) {
         const int b = idx[e];
         int r = -1;
         for (int f = start[b]; f < start[b + 1]; ++f)
@@ -1097,7 +1105,7 @@ void build_short_list(pg_context* ctx, bool same_positions) {
                                                       r * r, ctx->sh_start.p, ctx->sh_idx.p, ctx->sh_off.p);
             PG_CHECK_LAUNCH();
         }
-        short_reverse<<<blocks(n, 128), 128, 0, st>>>(n, ctx->sh_start.p, ctx->sh_idx.p, ctx->sh_off.p,
+        short_reverse<<<blocks((long long)n * ENTRY_LANES, 128), 128, 0, st>>>(n, ctx->sh_start.p, ctx->sh_idx.p, ctx->sh_off.p,
                                                      ctx->sh_rev.p, ctx->sh_count.p);
         PG_CHECK_LAUNCH();
         if (!copy_full) {
