@@ -92,7 +92,9 @@ int pg_get_atom_charges(pg_context* ctx, double* charges);
  * value at the cutoff), 4 power (epsilon, a, n), 5 shift_power (epsilon, r1, r2,
  * n), 6 tabulated (first row, row count, range, scale; rows set with
  * pg_set_pair_tables), 7 charge_pair (epsilon, n1, n2: epsilon q1^n1 q2^n2 with
- * the first-target types of pg_set_pair_first_targets); params: 4 per record
+ * the first-target types of pg_set_pair_first_targets), 10 step (e1, e2, r1, r2;
+ * the reference's force, c (1, 1, 1) on the pair's atom 1 and -c (1, 1, 1) on
+ * atom 2, Potentials.f90:4917-4967; unscaled, outside products); params: 4 per record
  * (unused tail zero); soft: cutoff - cutoff_margin; group: bond-order group
  * (-1 none). */
 int pg_set_pair_potentials(pg_context* ctx, int32_t n_types, int32_t n_records, const int32_t* kind,

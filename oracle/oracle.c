@@ -311,6 +311,10 @@ static double pair_energy(int kind, const double* p, double cut, double r1, cons
         return p[0] * pow(ratio, p[2]);
     } else if (kind == 5) {
         return p[0] * pow((p[1] - r1) / (p[1] - p[2]), p[3]);
+    } else if (kind == 10) { /* evaluate_energy_step (4946-4967): e1, e2, r1, r2 */
+        if (r1 < p[2]) return p[0];
+        if (r1 > p[3]) return p[1];
+        return (p[0] + p[1]) * 0.5 * (1.0 + 0.5 * cos(PI * (r1 - p[2]) / (p[3] - p[2])));
     } else { /* evaluate_energy_table (4267-4298): rows (V, d) from p[0], p[1] rows, range p[2], scale p[3] */
         const double* T = table + 2 * (int64_t)p[0];
         const int n_values = (int)p[1];
@@ -350,6 +354,12 @@ static void pair_force(int kind, const double* p, double cut, const double sep[3
     } else if (kind == 5) {
         double a = p[1], b = p[2], n = p[3];
         for (int c = 0; c < 3; ++c) f[c] = -p[0] * n / (a - b) * pow((a - r1) / (a - b), n - 1.0) * sep[c] / r1;
+    } else if (kind == 10) { /* evaluate_force_step (4917-4937): the same value on all three
+                                components, not along the bond, as the reference has it */
+        const double v = (r1 < p[2] || r1 > p[3])
+                             ? 0.0
+                             : (p[0] + p[1]) * 0.25 * PI / (p[3] - p[2]) * sin(PI * (r1 - p[2]) / (p[3] - p[2]));
+        for (int c = 0; c < 3; ++c) f[c] = v;
     } else { /* evaluate_force_table (4227-4258) */
         const double* T = table + 2 * (int64_t)p[0];
         const int n_values = (int)p[1];
@@ -1175,7 +1185,7 @@ static void* loop_range(void* arg) {
                     continue;
                 }
                 /* non-charge pair potentials have zero electronegativity */
-                if (J->what == 2 && kind < 7) continue;
+                if (J->what == 2 && (kind < 7 || kind == 10)) continue;
                 const double* p = m->pair_params + 4 * (size_t)r;
                 const int grp = m->pair_group[r];
                 const int sm = X->smoothened[r];

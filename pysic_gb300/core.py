@@ -47,7 +47,7 @@ BOND_ORDER_FACTORS = {
 
 # kinds understood by the GB300 engine (codes of the C ABI, include/pysic_gb300.h)
 PAIR_KIND = {"LJ": 0, "exponential": 1, "Buckingham": 2, "spring": 3, "power": 4, "shift_power": 5, "tabulated": 6,
-             "charge_pair": 7, "charge_exp": 8, "charge_abs": 9}
+             "charge_pair": 7, "charge_exp": 8, "charge_abs": 9, "step": 10}
 SINGLE_KIND = {"charge_self": 0, "constant": 1, "force": 2}
 TRIPLET_KIND = {"bond_bend": 0}
 QUAD_KIND = {"dihedral": 0}

@@ -597,7 +597,7 @@ int pg_set_pair_potentials(pg_context* ctx, int32_t n_types, int32_t n, const in
         pg::require(n_types >= 0 && n_types <= 64, PG_ERR_INVALID, "n_types must be within 0..64");
         pg::require(n >= 0, PG_ERR_INVALID, "negative record count");
         for (int r = 0; r < n; ++r)
-            pg::require(kind[r] >= 0 && kind[r] <= 9, PG_ERR_UNSUPPORTED, "unknown pair potential kind");
+            pg::require(kind[r] >= 0 && kind[r] <= 10, PG_ERR_UNSUPPORTED, "unknown pair potential kind");
         ctx->n_types = n_types;
         ctx->pr_kind.assign(kind, kind + n);
         ctx->pr_params.assign(params, params + 4 * (size_t)n);

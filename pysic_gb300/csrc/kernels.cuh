@@ -16,6 +16,10 @@ struct V3 {
 
 __device__ __forceinline__ void sincospi_(float x, float* s, float* c) { sincospif(x, s, c); }
 __device__ __forceinline__ void sincospi_(double x, double* s, double* c) { sincospi(x, s, c); }
+__device__ __forceinline__ float sinpi_(float x) { return sinpif(x); }
+__device__ __forceinline__ double sinpi_(double x) { return sinpi(x); }
+__device__ __forceinline__ float cospi_(float x) { return cospif(x); }
+__device__ __forceinline__ double cospi_(double x) { return cospi(x); }
 __device__ __forceinline__ float exp_(float x) { return expf(x); }
 __device__ __forceinline__ double exp_(double x) { return exp(x); }
 __device__ __forceinline__ float pow_(float x, float y) { return powf(x, y); }
@@ -138,11 +142,30 @@ __device__ __forceinline__ void pair_eval(const PairT<R>& P, R r, R& V, R& dV, c
             }
             break;
         }
+        case 10: {  // step: e1 below r1, e2 above r2, (e1 + e2)/2 (1 + cos(pi t)/2) between
+                    // (evaluate_energy_step, 4946-4967); its force is not radial: the pair
+                    // kernel adds it (step_force), dV is 0
+            V = r < P.p2 ? p0 : r > P.p3 ? p1 : (p0 + p1) * R(0.5) * (R(1) + R(0.5) * cospi_((r - P.p2) / (P.p3 - P.p2)));
+            dV = R(0);
+            break;
+        }
         default:  // charge-dependent terms are evaluated by the pair kernel itself
             V = R(0);
             dV = R(0);
             break;
     }
+}
+
+// The step potential's force as the reference evaluates it (evaluate_force_step,
+// Potentials.f90:4917-4937): the same value c on all three components of the
+// force on the pair's atom 1, -c on atom 2, c = (e1 + e2) pi/(4 (r2 - r1))
+// sin(pi (r - r1)/(r2 - r1)) on [r1, r2], else 0 (not the gradient of the
+// energy, and not along the bond).
+template <typename R>
+__device__ __forceinline__ R step_force(const PairT<R>& P, R r) {
+    if (r < P.p2 || r > P.p3) return R(0);
+    const R w = P.p3 - P.p2;
+    return (P.p0 + P.p1) * R(0.25) * R(3.14159265358979323846) / w * sinpi_((r - P.p2) / w);
 }
 
 // pick (Core.f90): each pair once -- the higher index, or for one atom and

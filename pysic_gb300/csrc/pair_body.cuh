@@ -62,6 +62,7 @@ __device__ __forceinline__ void pair_body(const PairArgs& A, int blk) {
             if (r == R(0)) continue;
             const R ir = R(1) / r;
             R U = 0, dU = 0;
+            R gs = 0;  // step terms: the same force on every component (not radial)
             if (A.ewald && r < ew_rc) {
                 const R qj = charge_of<R>(A, j);
                 const R qq = qi * qj;
@@ -181,6 +182,14 @@ __device__ __forceinline__ void pair_body(const PairArgs& A, int blk) {
                 if (!(wantE || wantF)) continue;
                 R V, dV;
                 pair_term<R>(P, r, V, dV, (const R*)A.tab);
+                if (P.kind == 10 && wantF) {
+                    // force (c, c, c) on the pair's atom 1, -(c, c, c) on atom 2, times the cut
+                    const bool first = pick(i, j, A.off[3 * e], A.off[3 * e + 1], A.off[3 * e + 2]);
+                    R f = R(1), fp = R(0);
+                    if (P.smooth) smooth<R>(r, P.rc, P.rs, f, fp);
+                    const R c = step_force<R>(P, r) * f;
+                    gs += first ? c : -c;
+                }
                 if (P.agroup >= 0) {
                     // scaled by the pair's mean per-atom factor (B_i + B_j)/2
                     // (Core.f90:4345-4350, 5553-5560); half of V f is each atom's
@@ -217,6 +226,21 @@ __device__ __forceinline__ void pair_body(const PairArgs& A, int blk) {
             w3 += h * y * z;
             w4 += h * x * z;
             w5 += h * x * y;
+            if (gs != R(0)) {
+                // half of the reference's stress term sep12 (x) F2 taken component by
+                // component (xx, yy, zz, yz, xz, xy; Core.f90:5593-5598) for F2 = -(gs, gs, gs)
+                // seen from atom 1, the same from either side
+                const R hg = R(-0.5) * gs;
+                fx += gs;
+                fy += gs;
+                fz += gs;
+                w0 += hg * x;
+                w1 += hg * y;
+                w2 += hg * z;
+                w3 += hg * y;
+                w4 += hg * x;
+                w5 += hg * x;
+            }
         }
     }
     // single-atom terms in FP64, added by the group's lane 0

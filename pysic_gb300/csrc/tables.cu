@@ -184,6 +184,9 @@ void fold_tables(pg_context* ctx) {
                 const int g = ctx->pr_group[r];
                 t.group = g >= 0 && tersoff_groups.count(g) ? 0 : -1;
                 t.agroup = g >= 0 && !tersoff_groups.count(g) ? gmap.at(g) : -1;
+                require(!(t.kind == 10 && (g >= 0 || (have_products && ctx->pr_nmul[r] > 0))), PG_ERR_UNSUPPORTED,
+                        "step: bond-order scaling and products are not evaluated by the GB300 engine (its force is "
+                        "not radial)");
                 require(!(t.agroup >= 0 && t.kind >= 7), PG_ERR_UNSUPPORTED,
                         "per-atom bond-order scaling of charge-dependent terms is not evaluated by the GB300 engine");
                 require(!(t.agroup >= 0 && have_products && ctx->pr_nmul[r] > 0), PG_ERR_UNSUPPORTED,
@@ -198,11 +201,13 @@ void fold_tables(pg_context* ctx) {
                     const int f = ctx->pr_mul0[r] + c;
                     PairT<double> u{};
                     u.kind = ctx->pm_kind[f];
+                    require(u.kind != 10, PG_ERR_UNSUPPORTED,
+                            "step: products are not evaluated by the GB300 engine (its force is not radial)");
                     u.group = u.agroup = -1;
                     fill_params(u, &ctx->pm_params[4 * (size_t)f]);
                     u.first = ctx->pm_first[f];
                     u.rc = u.rs = ctx->pr_cut[r];  // a spring factor is shifted at the product's cutoff
-                    if (u.kind >= 7) charge_pairs = true;
+                    if (u.kind >= 7 && u.kind <= 9) charge_pairs = true;
                     factors.push_back(u);
                 }
                 const double soft = ctx->pr_soft[r];
@@ -216,11 +221,13 @@ void fold_tables(pg_context* ctx) {
                 // unscaled charge-dependent and product terms stay in the pair kernel;
                 // Tersoff-scaled ones go to the bond-order kernels, which then also
                 // give their electronegativities (bond_chi)
-                const bool qterm = t.kind >= 7 || t.nmul > 0;
-                t.in_bond_kernel = bond && t.agroup < 0 &&
+                // (step, kind 10, has a force that is not radial: it stays in the pair kernel)
+                const bool charge = t.kind >= 7 && t.kind <= 9;
+                const bool qterm = charge || t.nmul > 0;
+                t.in_bond_kernel = bond && t.agroup < 0 && t.kind != 10 &&
                                    (qterm ? t.group >= 0 : (t.group >= 0 || t.rc <= bo_radius));
                 if (t.in_bond_kernel && qterm) bond_charge_terms = true;
-                if (t.kind >= 7) charge_pairs = true;
+                if (charge) charge_pairs = true;
                 if (!t.in_bond_kernel) pair_kernel_terms = true;
                 terms.push_back(t);
             }

@@ -26,6 +26,12 @@ from .error import InvalidParametersError, InvalidPotentialError
 MAX_TYPES = 64
 
 
+# The reference's step force is not the gradient of its energy and not along
+# the bond (Potentials.f90:4917-4937); the engine evaluates it for plain
+# records only.
+_STEP_ONLY_PLAIN = ("the step potential is evaluated by the GB300 engine as a plain pair term only "
+                    "(no bond-order scaling, no products): its force is not radial")
+
 def _distinct_permutations(targets):
     return list(dict.fromkeys(permutations(targets)))
 
@@ -300,6 +306,8 @@ def compile_model(atoms, potentials, coulomb=None):
             for fac in reversed(factors[1:]):
                 fk = fac.get_potential_type()
                 core.check_engine_support(fk)
+                if fk == "step":
+                    raise InvalidPotentialError(_STEP_ONLY_PLAIN)
                 if fk not in core.PAIR_KIND:
                     raise InvalidPotentialError("'{0}' is not a pair potential of the GB300 engine".format(fk))
                 M.mul_kind.append(core.PAIR_KIND[fk])
@@ -324,6 +332,8 @@ def compile_model(atoms, potentials, coulomb=None):
             if kind not in core.PAIR_KIND:
                 raise InvalidPotentialError("'{0}' is not a pair potential of the GB300 engine".format(kind))
             params = pair_params_of(kind, params)
+            if kind == "step" and (grp >= 0 or nmul):
+                raise InvalidPotentialError(_STEP_ONLY_PLAIN)
             if kind in ("charge_pair", "charge_exp", "charge_abs") and grp >= 0 and not pair_level(grp):
                 raise InvalidPotentialError("per-atom bond-order scaling of {0} is not evaluated by the GB300 engine"
                                             .format(kind))

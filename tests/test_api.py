@@ -100,11 +100,15 @@ def test_types_fold_tags_and_indices():
     assert len(M.pair_kind) == 3  # (1,1) once, (0,2) and (2,0)
 
 
-@pytest.mark.parametrize("kind,symbols", [("step", [["Si", "Si"]])])
-def test_unsupported_potential_rejected_at_compile(kind, symbols):
+def test_unsupported_factor_rejected_at_compile():
+    """The three-target per-atom 'triplet' factor (whose forces the reference
+    itself does not evaluate, Core.f90:4908-4912) is refused when compiled."""
     atoms = W.diamond_si(1)
-    with pytest.raises(pysic.InvalidPotentialError):
-        compile_model(atoms, [pysic.Potential(kind, symbols=symbols, cutoff=3.0)])
+    pot = pysic.Potential("constant", symbols=[["Si"]], parameters=[1.0])
+    pot.set_coordinator(pysic.Coordinator([pysic.BondOrderParameters("triplet", cutoff=3.0,
+                                                                     symbols=[["Si", "Si", "Si"]])]))
+    with pytest.raises((pysic.InvalidPotentialError, pysic.InvalidCoordinatorError)):
+        compile_model(atoms, [pot])
 
 
 def test_four_body_records_compile():

@@ -307,6 +307,34 @@ def test_spring_power_shift_power_constant_force_mixed():
     assert np.abs(got["forces"] - ref["forces"]).max() <= 1e-4 * max(1.0, np.abs(ref["forces"]).max())
 
 
+@pytest.mark.parametrize("margin", [0.0, 1.0])
+def test_step_potential_parity(margin):
+    """step (Potentials.f90:4858-4967) with the reference's force (the same
+    value on all three components, +c on the pair's atom 1 and -c on atom 2,
+    as the reference's loop picks them) and its stress terms, beside LJ, with
+    and without a smooth cut: FP64 against the oracle, mixed precision within
+    1e-5 eV/atom and 1e-4 of the largest force, over pair-kernel lane counts."""
+    P = pysic.Potential
+    atoms = W.lj_fcc(3, noise=0.08, seed=37)
+    pots = [P("step", symbols=[["X", "X"]], parameters=[0.04, -0.01, 3.0, 5.0], cutoff=5.5, cutoff_margin=margin),
+            P("LJ", symbols=[["X", "X"]], parameters=[0.0104, 3.4], cutoff=6.0)]
+    ref, got = _check_fp64(atoms, pots)
+    assert abs(ref["forces"].sum(axis=0)).max() < 1e-9  # third law holds pair by pair
+    n = len(atoms)
+    for lanes in (8, 32):
+        calc = pysic.Pysic(atoms, pots, precision="fp64")
+        calc.set_core()
+        calc.engine.set_pair_lanes(lanes)
+        r = calc.engine.calculate(calc._prec(), energy=True, forces=True)
+        assert r["energy"] == pytest.approx(ref["energy"], rel=1e-12, abs=1e-11)
+        assert np.abs(r["forces"] - ref["forces"]).max() < 1e-10
+        np.testing.assert_allclose(r["stress"], ref["stress"], rtol=1e-9, atol=1e-9 * np.abs(ref["stress"]).max())
+    mixed = engine_all(atoms, pots, None, "mixed")
+    assert abs(mixed["energy"] - ref["energy"]) / n <= 1e-5
+    assert np.abs(mixed["forces"] - ref["forces"]).max() <= 1e-4 * max(1.0, np.abs(ref["forces"]).max())
+    np.testing.assert_allclose(mixed["stress"], ref["stress"], rtol=1e-4, atol=1e-4 * np.abs(ref["stress"]).max())
+
+
 @pytest.mark.parametrize("precision", ["fp64", "mixed"])
 def test_tabulated_potential_parity(precision, tmp_path, monkeypatch):
     """'tabulated' (Potentials.f90:4227-4298) from table_0003.txt, smoothed at

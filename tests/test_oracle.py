@@ -660,3 +660,50 @@ def test_oracle_tersoff_scaled_charge_products(case):
         em[a, b] -= h
         de = (ev(pos @ ep.T, q, "energy", cell @ ep.T) - ev(pos @ em.T, q, "energy", cell @ em.T)) / (2 * h)
         assert st[k] == pytest.approx(-de, abs=1e-6 * max(1.0, abs(e0)))
+
+
+def test_oracle_step_potential_is_the_references_formula():
+    """step (Potentials.f90:4858-4967): e1 below r1, e2 above r2 and
+    (e1 + e2)/2 (1 + cos(pi t)/2) between, t = (r - r1)/(r2 - r1); its force
+    on the pair's atom 1 is c (1, 1, 1), c = (e1 + e2) pi/(4 (r2 - r1))
+    sin(pi t), and -c (1, 1, 1) on atom 2 -- the reference's own force, which is
+    neither the energy's gradient nor along the bond.  Without a margin there
+    is no cut factor; with one, the smooth cut's radial term is added
+    (Core.f90:5530-5560)."""
+    e1, e2, r1, r2 = 0.3, -0.1, 2.0, 4.0
+    u = np.array([0.48, -0.6, 0.64])
+    u /= np.linalg.norm(u)
+    for d, margin in ((1.5, 0.0), (3.0, 0.0), (3.3, 0.0), (4.5, 0.0), (3.3, 1.5)):
+        atoms = pysic.Atoms("He2", [[0.0, 0.0, 0.0], list(d * u)])
+        pot = pysic.Potential("step", symbols=[["He", "He"]], parameters=[e1, e2, r1, r2], cutoff=6.0,
+                              cutoff_margin=margin)
+        r = _nonperiodic(atoms, [pot])
+        t = (d - r1) / (r2 - r1)
+        v = e1 if d < r1 else e2 if d > r2 else (e1 + e2) * 0.5 * (1 + 0.5 * np.cos(np.pi * t))
+        c = 0.0 if (d < r1 or d > r2) else (e1 + e2) * 0.25 * np.pi / (r2 - r1) * np.sin(np.pi * t)
+        f, fp = 1.0, 0.0
+        if margin > 0.0 and d > 6.0 - margin:
+            w = (d - (6.0 - margin)) / margin
+            f, fp = 0.5 * (1 + np.cos(np.pi * w)), -0.5 * np.pi / margin * np.sin(np.pi * w)
+        assert r["energy"] == pytest.approx(v * f, rel=1e-12, abs=1e-15)
+        f1 = c * f * np.ones(3) + v * fp * u  # atom 1 (index 0): u points from it to atom 2
+        np.testing.assert_allclose(r["forces"][0], f1, rtol=1e-12, atol=1e-15)
+        np.testing.assert_allclose(r["forces"][1], -f1, rtol=1e-12, atol=1e-15)
+
+
+def test_step_potential_refused_where_its_force_cannot_be_carried():
+    """The engine evaluates step as a plain pair term: a Coordinator or a
+    product around it is refused at compile time (its force is not radial)."""
+    atoms = W.lj_fcc(2, noise=0.05, seed=3)
+    step = pysic.Potential("step", symbols=[["X", "X"]], parameters=[0.1, 0.0, 3.0, 4.0], cutoff=5.0)
+    lj = pysic.Potential("LJ", symbols=[["X", "X"]], parameters=[0.01, 3.4], cutoff=5.0)
+    compile_model(atoms, [step, lj])
+    with pytest.raises(pysic.InvalidPotentialError):
+        compile_model(atoms, [pysic.ProductPotential([step, lj])])
+    with pytest.raises(pysic.InvalidPotentialError):
+        compile_model(atoms, [pysic.ProductPotential([lj, step])])
+    scaled = pysic.Potential("step", symbols=[["X", "X"]], parameters=[0.1, 0.0, 3.0, 4.0], cutoff=5.0)
+    scaled.set_coordinator(pysic.Coordinator([pysic.BondOrderParameters("neighbors", cutoff=4.0,
+                                                                        symbols=[["X", "X"]])]))
+    with pytest.raises(pysic.InvalidPotentialError):
+        compile_model(atoms, [scaled])
