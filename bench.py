@@ -72,6 +72,19 @@ def workload(name):
         calc.add_potential(W.sutton_chen_potentials(("Cu",), cutoff=5.0, cutoff_margin=0.5))
         return (W.fcc_alloy(20, symbols=("Cu",), noise=0.05, seed=0), calc.get_potentials(), None,
                 "fcc Cu 20x20x20 cells, a=3.61, noise 0.05, Sutton-Chen (cutoff 5.0, margin 0.5)")
+    if name == "comb_sio2_3000":
+        # the COMB compound (COMB10 parameters, 12 A Coulomb and field ranges,
+        # screened real-space Ewald) on a random SiO2 box with random charges
+        from pysic_gb300 import CombPotential, Pysic
+
+        atoms = W.sio2_box(1000, seed=81)
+        q = np.random.default_rng(82).normal(0.0, 0.4, len(atoms))
+        atoms.set_initial_charges(q - q.mean())
+        calc = Pysic()
+        CombPotential().set_calculator(calc, True)
+        return (atoms, calc.get_potentials(), calc.get_coulomb_summation(),
+                "random SiO2 1000 Si + 2000 O at 2.2 g/cm^3, random charges (0.4 e), COMB10 compound "
+                "(40 pieces, 12 A ranges)")
     raise SystemExit("unknown workload " + name)
 
 
@@ -757,8 +770,9 @@ def run_batch(args):
 def other_configs(device, steps, warmup, threads):
     """The other single-system benchmark configurations, device-timed the same
     way (L2 flushed before every step), each against the oracle on the same
-    structure: LJ fcc 864 atoms in FP64 (config 1) and rock-salt NaCl 8000
-    ions with Buckingham + Ewald (config 3) in mixed precision and FP64."""
+    structure: LJ fcc 864 atoms in FP64 (config 1), rock-salt NaCl 8000
+    ions with Buckingham + Ewald (config 3) and the COMB compound on a
+    3000-atom SiO2 box, in mixed precision and FP64."""
     import torch
 
     sys.path.insert(0, os.path.join(ROOT, "oracle"))
@@ -768,7 +782,8 @@ def other_configs(device, steps, warmup, threads):
 
     flush = torch.empty(64 * 1024 * 1024, dtype=torch.float32, device="cuda:%d" % device)
     out = {}
-    for name, precisions in (("lj_fcc_864", ("fp64",)), ("ewald_nacl_8000", ("mixed", "fp64"))):
+    for name, precisions in (("lj_fcc_864", ("fp64",)), ("ewald_nacl_8000", ("mixed", "fp64")),
+                             ("comb_sio2_3000", ("mixed", "fp64"))):
         atoms, pots, coul, desc = workload(name)
         model = compile_model(atoms, pots, coul)
         cuts = np.array(individual_cutoffs(atoms, pots, coul)) + 0.5
