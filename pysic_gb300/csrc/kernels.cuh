@@ -67,6 +67,25 @@ __device__ __forceinline__ void smooth(R r, R rc, R rs, R& f, R& fp) {
         fp = R(-0.5) * R(3.14159265358979323846) / w * s;
     }
 }
+// FP32: one approximate reciprocal of the band width (a few ulp) in place of
+// two IEEE divisions, which cost more than the sine and cosine themselves in
+// the bond pass's per-bond set-up
+template <>
+__device__ __forceinline__ void smooth<float>(float r, float rc, float rs, float& f, float& fp) {
+    if (r > rc) {
+        f = 0.0f;
+        fp = 0.0f;
+    } else if (r < rs) {
+        f = 1.0f;
+        fp = 0.0f;
+    } else {
+        const float iw = __fdividef(1.0f, rc - rs);
+        float s, c;
+        sincospif((r - rs) * iw, &s, &c);
+        f = 0.5f * (1.0f + c);
+        fp = -0.5f * 3.14159265358979323846f * iw * s;
+    }
+}
 
 // V(r) and the radial derivative dV/dr of LJ (Potentials.f90:2971-3005),
 // exponential (3643-3680) and Buckingham (4009-4045); no factor 4 in LJ.
