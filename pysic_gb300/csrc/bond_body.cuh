@@ -299,17 +299,9 @@ __device__ __forceinline__ void bond_body(const BondArgs& A, int blk, int nblk) 
                 }
             }
             En += R(0.5) * U;
-            // radial part: force on i = +1/2 U' r_hat, on j the opposite
+            // radial part: force on j = -1/2 U' r_hat (on i the opposite, added
+            // with everything else from the entry records below)
             const R c = R(0.5) * dU * i1;
-            Fx += c * a.x;
-            Fy += c * a.y;
-            Fz += c * a.z;
-            W0 -= a.x * c * a.x;
-            W1 -= a.y * c * a.y;
-            W2 -= a.z * c * a.z;
-            W3 -= a.y * c * a.z;
-            W4 -= a.x * c * a.z;
-            W5 -= a.x * c * a.y;
             bacc[e] = V4{-c * a.x, -c * a.y, -c * a.z, bo ? R(0.5) * P * dB : R(0)};
         }
     }
@@ -358,15 +350,6 @@ __device__ __forceinline__ void bond_body(const BondArgs& A, int blk, int nblk) 
                     kx += qx;
                     ky += qy;
                     kz += qz;
-                    Fx -= jx + qx;
-                    Fy -= jy + qy;
-                    Fz -= jz + qz;
-                    W0 += gij.x * jx + gik.x * qx;
-                    W1 += gij.y * jy + gik.y * qy;
-                    W2 += gij.z * jz + gik.z * qz;
-                    W3 += gij.y * jz + gik.y * qz;
-                    W4 += gij.x * jz + gik.x * qz;
-                    W5 += gij.x * jy + gik.x * qy;
                 }
             }
         }
@@ -375,12 +358,24 @@ __device__ __forceinline__ void bond_body(const BondArgs& A, int blk, int nblk) 
         kz = group_sum<G>(kz);
         if (k < ni && lane == k % G) kacc[k] = V4{kx, ky, kz, 0};
     }
-    // per entry i->x: the force of this atom's bonds on x (j part + k parts),
-    // stored in x's own entry x->i (the reverse), so that the gather pass reads
-    // each atom's records contiguously
+    // per entry i->x: the force F_x of this atom's bonds on x (j part + k
+    // parts), stored in x's own entry x->i (the reverse), so that the gather
+    // pass reads each atom's records contiguously.  The force on i is minus
+    // their sum and the virial the sum of r_ix (x) F_x (components xx, yy, zz,
+    // yz, xz, xy), once per entry instead of once per triplet term.
     for (int e = lane; e < ni; e += G) {
-        const V4 be = bacc[e], ke = kacc[e];
-        fj[A.rev[s + e]] = V4{be.x + ke.x, be.y + ke.y, be.z + ke.z, 0};
+        const V4 be = bacc[e], ke = kacc[e], g = geo[e];
+        const R x = be.x + ke.x, y = be.y + ke.y, z = be.z + ke.z;
+        fj[A.rev[s + e]] = V4{x, y, z, 0};
+        Fx -= x;
+        Fy -= y;
+        Fz -= z;
+        W0 += g.x * x;
+        W1 += g.y * y;
+        W2 += g.z * z;
+        W3 += g.y * z;
+        W4 += g.x * z;
+        W5 += g.x * y;
     }
     const auto d0 = group_sum_f<G>(Fx), d1 = group_sum_f<G>(Fy), d2 = group_sum_f<G>(Fz);
     if (lane == 0) {
