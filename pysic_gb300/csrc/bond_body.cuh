@@ -311,6 +311,19 @@ __device__ __forceinline__ void bond_body(const BondArgs& A, int blk, int nblk) 
     // The lanes of a warp run to the warp's longest list (empty turns for the
     // shorter ones) because the shuffles need every lane.
     const int nloop = (int)__reduce_max_sync(0xffffffffu, (unsigned)ni);
+    // the lane's first bond stays in registers through the k loop (its
+    // geometry, unit vector, type and the force on its partner so far)
+    const bool own = act && lane < ni;
+    V4 b0{}, g0{};
+    V3<R> u0{};
+    R i0 = 0;
+    int t0 = 0;
+    if (own) {
+        b0 = bacc[lane];
+        g0 = geo[lane];
+        unit_of(lane, g0, u0, i0);
+        t0 = type_of(lane);
+    }
     for (int k = 0; k < nloop; ++k) {
         R kx = 0, ky = 0, kz = 0;
         if (k < ni) {
@@ -320,36 +333,41 @@ __device__ __forceinline__ void bond_body(const BondArgs& A, int blk, int nblk) 
                 V3<R> ub;
                 R i2;
                 unit_of(k, gik, ub, i2);
-                for (int e = lane; e < ni; e += G) {
-                    if (e == k) continue;
-                    V4 be = bacc[e];
+                V2 ck{R(0), R(0)};
+                if (cached_cut) ck = cut[k];
+                // one triplet term (bond e = gij, k): its j part onto be, its k part onto k
+                auto term = [&](const V4& gij, const V3<R>& ua, R i1, int te, V4& be) {
                     const R pref = be.w;
-                    if (pref == R(0)) continue;
-                    const TripT<R>& TT = trip_of(type_of(e), tk);
-                    if (!TT.valid) continue;
+                    if (pref == R(0)) return;
+                    const TripT<R>& TT = trip_of(te, tk);
+                    if (!TT.valid) return;
                     R f, fp;
                     if (cached_cut) {
-                        const V2 cc = cut[k];
-                        f = cc.x;
-                        fp = cc.y;
+                        f = ck.x;
+                        fp = ck.y;
                     } else {
                         smooth<R>(gik.w, TT.rc, TT.rs, f, fp);
                     }
-                    if (f == R(0) && fp == R(0)) continue;
+                    if (f == R(0) && fp == R(0)) return;
+                    V3<R> gj, gk;
+                    tersoff_grad_c<R>(TT, ua, gij.w, i1, ub, gik.w, i2, f, fp, gj, gk);
+                    be.x -= pref * gj.x;
+                    be.y -= pref * gj.y;
+                    be.z -= pref * gj.z;
+                    kx -= pref * gk.x;
+                    ky -= pref * gk.y;
+                    kz -= pref * gk.z;
+                };
+                if (own && lane != k) term(g0, u0, i0, t0, b0);
+                for (int e = lane + G; e < ni; e += G) {
+                    if (e == k) continue;
+                    V4 be = bacc[e];
                     const V4 gij = geo[e];
-                    V3<R> ua, gj, gk;
+                    V3<R> ua;
                     R i1;
                     unit_of(e, gij, ua, i1);
-                    tersoff_grad_c<R>(TT, ua, gij.w, i1, ub, gik.w, i2, f, fp, gj, gk);
-                    const R jx = -pref * gj.x, jy = -pref * gj.y, jz = -pref * gj.z;
-                    const R qx = -pref * gk.x, qy = -pref * gk.y, qz = -pref * gk.z;
-                    be.x += jx;
-                    be.y += jy;
-                    be.z += jz;
+                    term(gij, ua, i1, type_of(e), be);
                     bacc[e] = be;
-                    kx += qx;
-                    ky += qy;
-                    kz += qz;
                 }
             }
         }
@@ -358,6 +376,7 @@ __device__ __forceinline__ void bond_body(const BondArgs& A, int blk, int nblk) 
         kz = group_sum<G>(kz);
         if (k < ni && lane == k % G) kacc[k] = V4{kx, ky, kz, 0};
     }
+    if (own) bacc[lane] = b0;
     // per entry i->x: the force F_x of this atom's bonds on x (j part + k
     // parts), stored in x's own entry x->i (the reverse), so that the gather
     // pass reads each atom's records contiguously.  The force on i is minus
