@@ -189,6 +189,7 @@ static void host_copy(pg_context* ctx, const double* src, double* dst, long long
 // captured with it into its graph) or on its own.
 static void enqueue_coordinate_commit(pg_context* ctx) {
     const long long m = 3ll * ctx->n;
+    ctx->commit_in_disp = false;
     const int vec = (((uintptr_t)ctx->pos_in.p) & 15u) == 0 ? 1 : 0;
     copy_check<<<copy_blocks(vec ? (m + 1) / 2 : m), 256, 0, ctx->stream>>>(ctx->pos_in.p, nullptr, m,
                                                                             ctx->pos_bad.p, vec);
@@ -199,9 +200,15 @@ static void enqueue_coordinate_commit(pg_context* ctx) {
 }
 
 // A rejected update leaves the check flag set: clear it for the next one
-// (enqueued after the verdict was read, so no kernel reads it meanwhile).
+// (enqueued after the verdict was read, so no kernel reads it meanwhile), and
+// put the old coordinates back if the displacement pass had committed the
+// update.
 static void clear_check_flag(pg_context* ctx) {
     PG_CUDA(cudaMemsetAsync(ctx->pos_bad.p, 0, sizeof(int), ctx->stream));
+    if (ctx->commit_in_disp)
+        PG_CUDA(cudaMemcpyAsync(ctx->pos.p, ctx->pos_prev.p, sizeof(double) * 3 * (size_t)ctx->n,
+                                cudaMemcpyDeviceToDevice, ctx->stream));
+    ctx->commit_in_disp = false;
 }
 
 // Finish an outstanding coordinate update: commit it if no evaluation has done
@@ -232,6 +239,7 @@ static void update_coordinates(pg_context* ctx, const double* positions) {
     if (m == 0) return;
     if (ctx->upd_state != PG_UPD_NONE) settle_coordinates(ctx);  // one outstanding update at a time
     ctx->pos_in.resize((size_t)m);
+    ctx->pos_prev.resize((size_t)m);
     if (ctx->pos_bad.n == 0) {  // the check flag stays clear between updates (clear_check_flag)
         ctx->pos_bad.resize(1);
         PG_CUDA(cudaMemsetAsync(ctx->pos_bad.p, 0, sizeof(int), ctx->stream));
@@ -240,9 +248,26 @@ static void update_coordinates(pg_context* ctx, const double* positions) {
     ctx->upd_state = PG_UPD_STAGED;
 }
 
+// The mixed path's displacement pass runs in front of the evaluation's other
+// kernels (it also clears the totals).
+static bool displacement_pass_runs(pg_context* ctx, int precision, int flags) {
+    const bool wantF = flags & PG_WANT_FORCES, wantC = flags & PG_WANT_ENEGS, wantE = flags & PG_WANT_ENERGY;
+    const bool run_pair = ctx->have_pair_kernel_terms || ctx->ewald || ctx->have_singles || ctx->n_agroups > 0;
+    const bool run_bond = ctx->have_bond_terms && (wantE || wantF);
+    const bool run_tri = ctx->have_triplets && (wantE || wantF);
+    const bool run_bchi = ctx->have_bond_charge_terms && wantC;
+    return precision == PG_PREC_MIXED && (run_pair || run_bond || run_tri || run_bchi);
+}
+
 // skip (may be null): a device flag every kernel reads first; nonzero makes the
-// whole evaluation a no-op (loops replayed from a graph stop this way)
-void enqueue_evaluation(pg_context* ctx, int precision, int flags, int G, const int* skip) {
+// whole evaluation a no-op (loops replayed from a graph stop this way).
+// commit: a staged coordinate update goes into place first -- inside the
+// displacement pass when it runs, else by the check and commit kernels.
+// pub (may be null): where the totals and the update verdict (pub_bad) go in
+// page-locked memory; true when the evaluation's last kernel (the gather pass)
+// has written them, false when the caller still has to.
+static bool enqueue_evaluation_commit(pg_context* ctx, int precision, int flags, int G, const int* skip,
+                                      bool commit, HostTotals* pub = nullptr, const int* pub_bad = nullptr) {
     const int n = ctx->n;
     const bool wantF = flags & PG_WANT_FORCES, wantC = flags & PG_WANT_ENEGS, wantE = flags & PG_WANT_ENERGY;
     ctx->out_f.resize(3 * (size_t)std::max(n, 1));
@@ -261,8 +286,12 @@ void enqueue_evaluation(pg_context* ctx, int precision, int flags, int G, const 
     mark(0);
     // the totals are integers that every kernel adds to: clear them first (the
     // mixed path's displacement pass does it on the way)
-    if (precision == PG_PREC_MIXED && (run_pair || run_bond || run_tri || run_bchi)) launch_disp(ctx, skip, acc);
-    else PG_CUDA(cudaMemsetAsync(acc, 0, sizeof(FxAcc) * 8, ctx->stream));
+    if (displacement_pass_runs(ctx, precision, flags)) {
+        launch_disp(ctx, skip, acc, commit);
+    } else {
+        if (commit) enqueue_coordinate_commit(ctx);
+        PG_CUDA(cudaMemsetAsync(acc, 0, sizeof(FxAcc) * 8, ctx->stream));
+    }
     // per-atom bond-order factors: B and dB/dsum before the terms they scale
     const bool run_af = ctx->n_agroups > 0 && (wantE || wantF);
     if (run_af) launch_atom_factors(ctx, precision, 0, false, nullptr, skip);
@@ -276,8 +305,11 @@ void enqueue_evaluation(pg_context* ctx, int precision, int flags, int G, const 
         first_f = false;
     }
     mark(1);
+    // the gather pass is the last kernel to touch the totals: it publishes them
+    const bool gather_last = pub != nullptr && run_bond && wantF && !run_tri && !ctx->ewald && !run_bchi;
     if (run_bond) {
-        launch_bond_order_impl(ctx, precision, flags, first_f, G, acc, [&] { mark(2); }, skip);
+        launch_bond_order_impl(ctx, precision, flags, first_f, G, acc, [&] { mark(2); }, skip,
+                               gather_last ? pub : nullptr, pub_bad);
         if (wantF) first_f = false;
     } else {
         if (run_bchi) launch_bond_b(ctx, precision, G, skip);  // the bonds' B for bond_chi
@@ -301,6 +333,11 @@ void enqueue_evaluation(pg_context* ctx, int precision, int flags, int G, const 
     if (wantF && first_f) PG_CUDA(cudaMemsetAsync(ctx->out_f.p, 0, sizeof(double) * 3 * n, ctx->stream));
     if (wantC && first_chi) PG_CUDA(cudaMemsetAsync(ctx->out_chi.p, 0, sizeof(double) * n, ctx->stream));
     mark(5);
+    return gather_last;
+}
+
+void enqueue_evaluation(pg_context* ctx, int precision, int flags, int G, const int* skip) {
+    enqueue_evaluation_commit(ctx, precision, flags, G, skip, false);
 }
 
 // Pick the lanes-per-atom tile of the bond-order kernels: each candidate is
@@ -368,10 +405,11 @@ static void evaluate_impl(pg_context* ctx, int precision, int flags, bool publis
     const bool verdict = ctx->upd_state != PG_UPD_NONE;
     pg::HostTotals* dtot = nullptr;
     if (publish) PG_CUDA(cudaHostGetDevicePointer((void**)&dtot, (void*)ctx->h_tot.get(1), 0));
+    if (commit) ctx->commit_in_disp = displacement_pass_runs(ctx, precision, flags);
     auto sequence = [&] {
-        if (commit) enqueue_coordinate_commit(ctx);
-        enqueue_evaluation(ctx, precision, flags, G, nullptr);
-        if (publish) {
+        const bool published = enqueue_evaluation_commit(ctx, precision, flags, G, nullptr, commit,
+                                                         publish ? dtot : nullptr, verdict ? ctx->pos_bad.p : nullptr);
+        if (publish && !published) {
             publish_totals<<<1, 32, 0, ctx->stream>>>(dtot, ctx->out_acc.p, verdict ? ctx->pos_bad.p : nullptr);
             PG_CHECK_LAUNCH();
             ctx->launches += 1;

@@ -95,6 +95,11 @@ struct BondArgs {
     const int* skip;   // optional device flag: nonzero = do nothing
     const double* q;   // FP64 charges (the mixed path reads the FP32 copy in disp .w)
     void* b_out;       // per entry: B of the bond (R; null: not kept), for the electronegativity pass
+    // the gather pass as an evaluation's last kernel: its block 0 writes the
+    // final totals and the verdict (pub_bad, may be null) of the coordinate
+    // update into page-locked host memory (null: not this kernel's job)
+    HostTotals* pub;
+    const int* pub_bad;
 };
 
 struct DispArgs {
@@ -105,6 +110,13 @@ struct DispArgs {
     F4* d;             // null: only clear the totals
     const int* skip;
     FxAcc* zero8;
+    // a staged coordinate update committed on the way (pos_in null: none): the
+    // new coordinates from pos_in into pos_out, the old ones kept in pos_prev
+    // until the verdict is read, bad set if any new value is not finite
+    const double* pos_in;
+    double* pos_out;
+    double* pos_prev;
+    int* bad;
 };
 
 // argument records of one system (pair.cu, tersoff.cu)

@@ -14,15 +14,34 @@ namespace pg {
 // per-atom displacement since the list build (FP64 difference rounded to FP32)
 // and the FP32 charge, one 16-byte record per atom for the mixed-path kernels;
 // block 0 also clears the energy / virial totals (zero8, 8 records; may be null)
-// that the kernels after it add to
+// that the kernels after it add to.  With a staged coordinate update (pos_in)
+// each thread commits its atom's new coordinates first: no separate check and
+// commit kernels in front of the evaluation.  A non-finite value sets the
+// verdict flag; the host puts pos_prev back when it reads that verdict, so a
+// rejected update still leaves the old coordinates.
 __device__ __forceinline__ void disp_body(const DispArgs& A, int i) {
     if (A.zero8 && i < 8) A.zero8[i] = FxAcc{{0ull, 0ull, 0ull}};
     if (A.skip && *A.skip) return;
     if (i >= A.n || A.d == nullptr) return;
-    const double* pos = A.pos;
     const double* pos0 = A.pos0;
-    A.d[i] = F4{(float)(pos[3 * i] - pos0[3 * i]), (float)(pos[3 * i + 1] - pos0[3 * i + 1]),
-                (float)(pos[3 * i + 2] - pos0[3 * i + 2]), (float)A.q[i]};
+    double x, y, z;
+    if (A.pos_in) {
+        x = A.pos_in[3 * i];
+        y = A.pos_in[3 * i + 1];
+        z = A.pos_in[3 * i + 2];
+        if (!(isfinite(x) && isfinite(y) && isfinite(z))) *A.bad = 1;
+        A.pos_prev[3 * i] = A.pos[3 * i];
+        A.pos_prev[3 * i + 1] = A.pos[3 * i + 1];
+        A.pos_prev[3 * i + 2] = A.pos[3 * i + 2];
+        A.pos_out[3 * i] = x;
+        A.pos_out[3 * i + 1] = y;
+        A.pos_out[3 * i + 2] = z;
+    } else {
+        x = A.pos[3 * i];
+        y = A.pos[3 * i + 1];
+        z = A.pos[3 * i + 2];
+    }
+    A.d[i] = F4{(float)(x - pos0[3 * i]), (float)(y - pos0[3 * i + 1]), (float)(z - pos0[3 * i + 2]), (float)A.q[i]};
 }
 
 // SPEC: single-species Tersoff, every parameter a kernel argument (no table
@@ -434,6 +453,13 @@ __device__ __forceinline__ void gather_body(const BondArgs& A, int blk, int nblk
     const int s = act ? A.start[m] : 0, nm = act ? A.start[m + 1] - s : 0;
     pdl_wait();  // the bond pass's records
     if (A.skip && *A.skip) return;
+    if (A.pub && blk == 0 && threadIdx.x < 8) {
+        // every kernel that adds to the totals has completed (the bond pass
+        // waited for the ones before it)
+        if (threadIdx.x < 7) A.pub->totals[threadIdx.x] = fx_to_double(fx_from_limbs(A.acc[threadIdx.x]));
+        else A.pub->bad = A.pub_bad ? *A.pub_bad : 0;
+        __threadfence_system();
+    }
     if (act) {
         // every neighbour x left the force of its bonds on m in m's entry m->x
         for (int e = lane; e < nm; e += G) {

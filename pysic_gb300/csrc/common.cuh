@@ -359,6 +359,8 @@ struct pg_context {
     pg::DevBuf<double> pos;     // n x 3
     pg::DevBuf<double> pos_in;  // coordinate updates land here first and are checked on the device
     pg::DevBuf<int> pos_bad;    // 1 element: nonzero when an update held a non-finite value
+    pg::DevBuf<double> pos_prev;  // the coordinates before an update the displacement pass committed
+    bool commit_in_disp = false;  // the outstanding update was committed by the displacement pass
     int upd_state = 0;          // pg::PG_UPD_*: an outstanding coordinate update
     pg::PinnedBuf<pg::FxAcc> h_acc; // energy / virial totals on their way to the host
     pg::PinnedBuf<int> h_flag;
@@ -594,7 +596,7 @@ void build_neighbor_lists(pg_context* ctx, const double* h_cutoffs);
 // list generation's reference positions were taken right after it)
 void build_short_list(pg_context* ctx, bool same_positions = false);
 void build_full_sep0(pg_context* ctx);
-void launch_disp(pg_context* ctx, const int* skip, FxAcc* zero8 = nullptr);
+void launch_disp(pg_context* ctx, const int* skip, FxAcc* zero8 = nullptr, bool commit = false);
 void build_allpairs_lists(pg_context* ctx, const double* h_cutoffs);
 void install_neighbor_lists(pg_context* ctx, const int32_t* counts, const int32_t* idx, const int32_t* off);
 
@@ -612,7 +614,8 @@ void launch_pair_kernel_skip(pg_context* ctx, int precision, int flags, bool fir
 
 int bond_blocks(int n, int G);
 void launch_bond_order_impl(pg_context* ctx, int precision, int flags, bool first_f, int G, FxAcc* acc,
-                            const std::function<void()>& between, const int* skip = nullptr);
+                            const std::function<void()>& between, const int* skip = nullptr,
+                            HostTotals* pub = nullptr, const int* pub_bad = nullptr);
 void bond_zeta_diag(pg_context* ctx);
 // noalloc.cu: the bond-order passes on static scratch (pg_bond_order_noalloc)
 void bond_order_noalloc(pg_context* ctx, int precision, double* d_forces, double* d_totals);

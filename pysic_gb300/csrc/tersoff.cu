@@ -260,10 +260,13 @@ static void launch_by_lanes(const BondArgs& A, int n, cudaStream_t st, int G, bo
 
 // `between` runs between the two passes
 void launch_bond_order_impl(pg_context* ctx, int precision, int flags, bool first_f, int G, FxAcc* acc,
-                            const std::function<void()>& between, const int* skip) {
+                            const std::function<void()>& between, const int* skip, HostTotals* pub,
+                            const int* pub_bad) {
     prepare_bond_scratch(ctx, precision);
     BondArgs A = make_bond_args(ctx, precision, flags, first_f, acc);
     A.skip = skip;
+    A.pub = pub;
+    A.pub_bad = pub_bad;
     if (ctx->have_bond_charge_terms) A.b_out = ctx->bo_b.p;  // kept for bond_chi
     const bool forces = (flags & PG_WANT_FORCES) != 0;
     if (precision == PG_PREC_FP64) launch_by_lanes<double>(A, ctx->n, ctx->stream, G, forces, between);
@@ -326,9 +329,16 @@ void launch_bond_chi(pg_context* ctx, int precision, bool first, const int* skip
     ctx->launches++;
 }
 
-void launch_disp(pg_context* ctx, const int* skip, FxAcc* zero8) {
+void launch_disp(pg_context* ctx, const int* skip, FxAcc* zero8, bool commit) {
     ctx->disp32.resize((size_t)std::max(ctx->n, 1));
-    disp_pass<<<(ctx->n + 255) / 256, 256, 0, ctx->stream>>>(make_disp_args(ctx, ctx->disp32.p, skip, zero8));
+    DispArgs A = make_disp_args(ctx, ctx->disp32.p, skip, zero8);
+    if (commit) {  // the staged coordinates (pos_in) committed by the same pass
+        A.pos_in = ctx->pos_in.p;
+        A.pos_out = ctx->pos.p;
+        A.pos_prev = ctx->pos_prev.p;
+        A.bad = ctx->pos_bad.p;
+    }
+    disp_pass<<<(ctx->n + 255) / 256, 256, 0, ctx->stream>>>(A);
     PG_CHECK_LAUNCH();
     ctx->launches++;
 }

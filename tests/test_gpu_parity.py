@@ -245,6 +245,9 @@ def test_rejected_coordinate_update_keeps_the_old_positions():
     e0 = calc.get_potential_energy()
     f0 = calc.get_forces()
     eng = calc.engine
+    # the mixed path commits an update inside its displacement pass and puts
+    # the old coordinates back when the verdict is read
+    m0 = eng.calculate(L.PREC_MIXED, energy=True, forces=True)
     for bad in (np.nan, np.inf, -np.inf):
         pos = atoms.get_positions()
         pos[5, 1] = bad
@@ -256,16 +259,28 @@ def test_rejected_coordinate_update_keeps_the_old_positions():
         r = eng.calculate(L.PREC_FP64, energy=True, forces=True)
         assert r["energy"] == e0
         assert np.array_equal(r["forces"], f0)
+        r = eng.calculate(L.PREC_MIXED, energy=True, forces=True)
+        assert r["energy"] == m0["energy"]
+        assert np.array_equal(r["forces"], m0["forces"])
         # a call that reads the coordinates outside an evaluation reports it too
         eng.update_positions(pos)
         with pytest.raises(L.EngineError) as err:
             eng.neighbor_lists()
         assert err.value.status == L.PG_ERR_INVALID
         # and so does the device-resident route, with the results
+        for precision in (L.PREC_FP64, L.PREC_MIXED):
+            eng.update_positions(pos)
+            eng.device_evaluate(precision, L.WANT_ENERGY | L.WANT_FORCES)
+            with pytest.raises(L.EngineError):
+                eng.device_results()
+        r = eng.calculate(L.PREC_FP64, energy=True, forces=True)
+        assert r["energy"] == e0
+        # an update committed by the displacement pass whose verdict is read by
+        # a call outside an evaluation
         eng.update_positions(pos)
-        eng.device_evaluate(L.PREC_FP64, L.WANT_ENERGY | L.WANT_FORCES)
+        eng.device_evaluate(L.PREC_MIXED, L.WANT_ENERGY | L.WANT_FORCES)
         with pytest.raises(L.EngineError):
-            eng.device_results()
+            eng.neighbor_lists()
         r = eng.calculate(L.PREC_FP64, energy=True, forces=True)
         assert r["energy"] == e0
     # a valid update afterwards is taken
