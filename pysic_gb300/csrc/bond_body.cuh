@@ -4,6 +4,8 @@
 // its citations are those described at the top of tersoff.cu.
 #pragma once
 
+#include <type_traits>
+
 #include "args.cuh"
 #include "bond.cuh"
 #include "common.cuh"
@@ -460,6 +462,16 @@ __device__ __forceinline__ void gather_body(const BondArgs& A, int blk, int nblk
         else A.pub->bad = A.pub_bad ? *A.pub_bad : 0;
         __threadfence_system();
     }
+    // the part on m as a centre, left by the bond pass (2^-32 fixed point in the
+    // mixed path), fetched together with the records rather than after the sums
+    using C = typename std::conditional<sizeof(R) == 4, long long, double>::type;
+    C c0 = 0, c1 = 0, c2 = 0;
+    if (act && lane == 0) {
+        const C* fc = (const C*)A.fc + 3 * m;
+        c0 = fc[0];
+        c1 = fc[1];
+        c2 = fc[2];
+    }
     if (act) {
         // every neighbour x left the force of its bonds on m in m's entry m->x
         for (int e = lane; e < nm; e += G) {
@@ -471,17 +483,14 @@ __device__ __forceinline__ void gather_body(const BondArgs& A, int blk, int nblk
     }
     auto sx = group_sum_f<G>(Fx), sy = group_sum_f<G>(Fy), sz = group_sum_f<G>(Fz);
     if (act && lane == 0) {
-        // plus the part on m as a centre, left by the bond pass
         if constexpr (sizeof(R) == 4) {
-            const long long* fc = (const long long*)A.fc + 3 * m;
-            sx.f += fc[0];
-            sy.f += fc[1];
-            sz.f += fc[2];
+            sx.f += c0;
+            sy.f += c1;
+            sz.f += c2;
         } else {
-            const double* fc = (const double*)A.fc + 3 * m;
-            sx.s += fc[0];
-            sy.s += fc[1];
-            sz.s += fc[2];
+            sx.s += c0;
+            sy.s += c1;
+            sz.s += c2;
         }
         store_sum(A.out_f + 3 * m, sx, A.first_f);
         store_sum(A.out_f + 3 * m + 1, sy, A.first_f);
