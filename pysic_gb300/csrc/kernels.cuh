@@ -486,29 +486,58 @@ __device__ __forceinline__ Fx128 warp_total(double v) { return fx_from_double(gr
 __device__ __forceinline__ Fx128 fx_from(float v) { return fx_from_float(v); }
 __device__ __forceinline__ Fx128 fx_from(double v) { return fx_from_double(v); }
 
+// Sums 8 values over the 32 lanes of a warp with 9 shuffles instead of 8 x 5:
+// at each of the first three levels (lane distance 16, 8, 4) a lane keeps half
+// of its values and trades the other half with its partner, then the last two
+// levels sum the one value left.  Lane l ends with the warp total of value
+// `which` = 4 b4 + 2 b3 + b2 (b: the bits of l); a fixed order, so the result
+// is reproducible.
+template <typename R>
+__device__ __forceinline__ R warp_sum8(const R (&v)[8], int& which) {
+    const int l = threadIdx.x & 31;
+    const bool h4 = (l & 16) != 0, h3 = (l & 8) != 0, h2 = (l & 4) != 0;
+    R a[4];
+#pragma unroll
+    for (int j = 0; j < 4; ++j) {
+        const R keep = h4 ? v[j + 4] : v[j], send = h4 ? v[j] : v[j + 4];
+        a[j] = keep + __shfl_xor_sync(0xffffffffu, send, 16);
+    }
+    R b[2];
+#pragma unroll
+    for (int j = 0; j < 2; ++j) {
+        const R keep = h3 ? a[j + 2] : a[j], send = h3 ? a[j] : a[j + 2];
+        b[j] = keep + __shfl_xor_sync(0xffffffffu, send, 8);
+    }
+    R c = (h2 ? b[1] : b[0]) + __shfl_xor_sync(0xffffffffu, h2 ? b[0] : b[1], 4);
+    c += __shfl_xor_sync(0xffffffffu, c, 2);
+    c += __shfl_xor_sync(0xffffffffu, c, 1);
+    which = (h4 ? 4 : 0) + (h3 ? 2 : 0) + (h2 ? 1 : 0);
+    return c;
+}
+
 // Adds a block's energy and virial to the global totals acc[0..6] (null: none)
 // from every lane's 7 terms t, with the result of block_totals_publish: each
-// warp sums its lanes in the working precision by the same shuffle tree as
-// warp_total and leaves the 7 sums in shared memory (wpart); the last warp of
-// the block to arrive widens them exactly, lane c taking value c over the
-// block's warps in warp order, and sends value c's limbs to acc from lane c.
-// Only one warp per block converts, and the 7 values go out in parallel.
-// `done` is a shared counter set to zero before the block's first barrier.
-// x0, wx (both null, or both set): an exact 128-bit warp total (the same in
-// every lane) added to value 0, through the per-warp shared slots wx.
+// warp sums its lanes in the working precision (warp_sum8) and leaves the 7
+// sums in shared memory (wpart); the last warp of the block to arrive widens
+// them exactly, lane c taking value c over the block's warps in warp order,
+// and sends value c's limbs to acc from lane c.  Only one warp per block
+// converts, and the 7 values go out in parallel.  `done` is a shared counter
+// set to zero before the block's first barrier.  x0, wx (both null, or both
+// set): an exact 128-bit warp total (the same in every lane) added to value 0,
+// through the per-warp shared slots wx.
 template <typename R>
 __device__ __forceinline__ void block_totals_add(const R (&t)[7], R (*wpart)[7], unsigned* done, FxAcc* acc,
                                                  const Fx128* x0 = nullptr, Fx128* wx = nullptr) {
     if (acc == nullptr) return;
     const int wl = threadIdx.x & 31, w = threadIdx.x >> 5, nw = blockDim.x >> 5;
-    R s[7];
-#pragma unroll
-    for (int c = 0; c < 7; ++c) s[c] = group_sum<32>(t[c]);
+    const R t8[8] = {t[0], t[1], t[2], t[3], t[4], t[5], t[6], R(0)};
+    int which;
+    const R tot = warp_sum8(t8, which);
+    if ((wl & 3) == 0 && which < 7) wpart[w][which] = tot;
+    if (x0 && wl == 0) wx[w] = *x0;
+    __syncwarp();
     unsigned last = 0;
     if (wl == 0) {
-#pragma unroll
-        for (int c = 0; c < 7; ++c) wpart[w][c] = s[c];
-        if (x0) wx[w] = *x0;
         __threadfence_block();
         last = atomicAdd(done, 1u) == (unsigned)(nw - 1) ? 1u : 0u;
     }
