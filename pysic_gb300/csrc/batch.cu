@@ -59,6 +59,10 @@ struct pg_batch {
     };
     bool have_key = false;
     Key key{};
+    // the systems' states (state_sum, alloc_epoch) when their own streams were
+    // last waited for
+    bool synced = false;
+    unsigned long long synced_state = 0, synced_alloc = 0;
     cudaGraphExec_t graph = nullptr;
     int launches = 0;
     ~pg_batch() {
@@ -95,6 +99,17 @@ void size_buffers(pg_batch* b, int precision) {
         c->out_acc.resize(8);
         if (precision == PG_PREC_MIXED) c->disp32.resize(n);
         if (c->have_bond_terms) prepare_bond_scratch(c, precision);
+    }
+    // The batch runs on its own stream and reads what the systems' streams
+    // wrote: a list build or an upload may still be in flight there (the
+    // short-list build returns without waiting).  Whenever a system's state
+    // or any buffer changed, wait for every system's stream first.
+    const unsigned long long st = state_sum(b), al = alloc_epoch();
+    if (!b->synced || st != b->synced_state || al != b->synced_alloc) {
+        for (pg_context* c : b->sys) PG_CUDA(cudaStreamSynchronize(c->stream));
+        b->synced = true;
+        b->synced_state = st;
+        b->synced_alloc = al;
     }
 }
 

@@ -497,6 +497,10 @@ struct pg_context {
 
     // neighbour-build scratch
     pg::DevBuf<float4> nb_posf;     // positions rounded to FP32 for the stencil scan's screen
+    // the multi-block prefix scans' tile records and ticket / done counters
+    // (zero between scans: the last block of each scan clears them)
+    pg::DevBuf<unsigned long long> scan_rec;
+    pg::DevBuf<unsigned> scan_ctr;
     pg::DevBuf<int> cell_of, cell_start, sorted_atoms, wrap, keys_a, keys_b, vals_a, vals_b, radix_hist, count_tmp,
         invisible;
     pg::DevBuf<long long> g0_keys;

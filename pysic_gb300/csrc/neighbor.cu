@@ -217,6 +217,128 @@ __global__ void __launch_bounds__(1024) scan_single_block(const T* __restrict__ 
     }
 }
 
+// The same exclusive scan (out[0..n-1], out[n] = total, *total) over many
+// blocks in one pass (decoupled look-back): each block takes the next tile of
+// LB_TILE values in order from a ticket, sums it, publishes the tile's sum
+// (flag 1), then its first warp reads the records of the 32 tiles before it at
+// once and adds their sums back to the nearest one that carries its inclusive
+// prefix (flag 2), a window further back at a time; the block publishes its
+// own inclusive prefix and writes its part.  A tile only waits on tiles with
+// smaller tickets, whose blocks are already running, so every wait ends; each
+// wait is also bounded, and a scan whose wait ran out writes -1 as its total
+// (the host checks the totals it reads).  The last block to finish clears the
+// records and counters (ctr: ticket, done, failed) for the next scan.  Thread
+// t of a tile holds values 8t .. 8t + 7; the sums are of integers, so exact.
+constexpr int LB_THREADS = 256, LB_PER = 8, LB_TILE = LB_THREADS * LB_PER;
+constexpr unsigned long long LB_AGG = 1ull << 62, LB_INC = 2ull << 62, LB_VAL = (1ull << 32) - 1;
+constexpr unsigned LB_POLLS = 1u << 22;
+
+__global__ void __launch_bounds__(LB_THREADS) scan_lookback(const int* __restrict__ in, int* __restrict__ out, int n,
+                                                            int* __restrict__ total, unsigned long long* rec,
+                                                            unsigned* ctr, int ntiles) {
+    __shared__ int s_tile, s_excl, s_last;
+    __shared__ int s_wsum[LB_THREADS / 32];
+    const int t = threadIdx.x, lane = t & 31, w = t >> 5;
+    if (t == 0) s_tile = (int)atomicAdd(&ctr[0], 1u);
+    __syncthreads();
+    const int tile = s_tile;
+    const long long base = (long long)tile * LB_TILE + (long long)t * LB_PER;
+    int v[LB_PER];
+    int run = 0;
+#pragma unroll
+    for (int k = 0; k < LB_PER; ++k) {
+        const long long i = base + k;
+        v[k] = run;
+        run += i < n ? in[i] : 0;
+    }
+    // exclusive prefix of the thread sums over the tile
+    int incl = run;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        const int y = __shfl_up_sync(0xffffffffu, incl, o);
+        if (lane >= o) incl += y;
+    }
+    if (lane == 31) s_wsum[w] = incl;
+    __syncthreads();
+    int wpre = 0, agg = 0;
+#pragma unroll
+    for (int q = 0; q < LB_THREADS / 32; ++q) {
+        if (q < w) wpre += s_wsum[q];
+        agg += s_wsum[q];
+    }
+    if (w == 0) {
+        int excl = 0;
+        bool ok = true;
+        if (tile == 0) {
+            if (lane == 0) atomicExch(&rec[0], LB_INC | (unsigned)agg);
+        } else {
+            if (lane == 0) atomicExch(&rec[tile], LB_AGG | (unsigned)agg);
+            for (int p = tile - 1;; p -= 32) {
+                // lane l reads tile p - l (tiles before the first count as
+                // inclusive prefixes of zero)
+                const int q = p - lane;
+                unsigned long long r = LB_INC;
+                if (q >= 0) {
+                    for (unsigned it = 0;; ++it) {
+                        r = atomicAdd(&rec[q], 0ull);
+                        if (r >> 62) break;
+                        if (it >= LB_POLLS) break;
+                        __nanosleep(64);
+                    }
+                }
+                if (__any_sync(0xffffffffu, (r >> 62) == 0ull)) {
+                    ok = false;
+                    break;
+                }
+                const unsigned incs = __ballot_sync(0xffffffffu, (r >> 62) == 2ull);
+                const int first = incs ? __ffs(incs) - 1 : 32;
+                int c = lane <= first ? (int)(unsigned)(r & LB_VAL) : 0;
+#pragma unroll
+                for (int o = 16; o > 0; o >>= 1) c += __shfl_xor_sync(0xffffffffu, c, o);
+                excl += c;
+                if (incs) break;
+            }
+            if (lane == 0) {
+                if (!ok) atomicExch(&ctr[2], 1u);
+                atomicExch(&rec[tile], LB_INC | (unsigned)(excl + agg));
+            }
+        }
+        if (lane == 0) s_excl = excl;
+    }
+    __syncthreads();
+    const int excl = s_excl;
+    const int pre = excl + wpre + incl - run;
+#pragma unroll
+    for (int k = 0; k < LB_PER; ++k) {
+        const long long i = base + k;
+        if (i < n) out[i] = pre + v[k];
+    }
+    if (tile == ntiles - 1 && t == 0) {
+        out[n] = excl + agg;
+        if (total) *total = excl + agg;
+    }
+    // the last block to finish marks a failed scan and clears the records
+    __syncthreads();
+    if (t == 0) {
+        __threadfence();
+        s_last = atomicAdd(&ctr[1], 1u) == (unsigned)(ntiles - 1) ? 1 : 0;
+    }
+    __syncthreads();
+    if (s_last) {
+        for (int q = t; q < ntiles; q += LB_THREADS) rec[q] = 0ull;
+        if (t == 0) {
+            __threadfence();
+            if (atomicAdd(&ctr[2], 0u)) {
+                out[n] = -1;
+                if (total) *total = -1;
+            }
+            ctr[0] = 0u;
+            ctr[1] = 0u;
+            ctr[2] = 0u;
+        }
+    }
+}
+
 // subcell stencil of divide_cell (Geometry.f90:820-858)
 __device__ __forceinline__ bool stencil(const int ci[3], int s, const int sp[3], const int pbc[3], int nb[3],
                                         int noff[3]) {
@@ -674,6 +796,31 @@ inline int blocks(long long n, int t) { return (int)((n + t - 1) / t); }
 // a grid-stride launch over about 8 entries per atom, at most 4 blocks per SM
 inline int copy_grid(int n) { return std::max(1, std::min(blocks(8ll * n, 256), 4 * sm_count())); }
 
+// The look-back scan's records for arrays of up to maxn values, sized and
+// cleared on the host side of a build (never inside a capture).
+void scan_prepare(pg_context* ctx, long long maxn) {
+    const size_t ntiles = (size_t)std::max<long long>(1, (maxn + LB_TILE - 1) / LB_TILE);
+    if (ctx->scan_ctr.n == 0) {
+        ctx->scan_ctr.resize(3);
+        PG_CUDA(cudaMemsetAsync(ctx->scan_ctr.p, 0, sizeof(unsigned) * ctx->scan_ctr.cap, ctx->stream));
+    }
+    if (ctx->scan_rec.n < ntiles) {
+        ctx->scan_rec.resize(ntiles);
+        PG_CUDA(cudaMemsetAsync(ctx->scan_rec.p, 0, sizeof(unsigned long long) * ctx->scan_rec.cap, ctx->stream));
+    }
+}
+
+// Exclusive scan of n ints into out[0..n] (out[n] and *total, may be null: the
+// sum): one block for short arrays, the multi-block look-back scan otherwise.
+void scan_ints(pg_context* ctx, const int* in, int* out, int n, int* total, cudaStream_t st) {
+    const int ntiles = (n + LB_TILE - 1) / LB_TILE;
+    if (ntiles <= 2 || ctx->scan_rec.n < (size_t)ntiles || ctx->scan_ctr.n < 3)
+        scan_single_block<int, int><<<1, 1024, 0, st>>>(in, out, n, total, 0);
+    else
+        scan_lookback<<<ntiles, LB_THREADS, 0, st>>>(in, out, n, total, ctx->scan_rec.p, ctx->scan_ctr.p, ntiles);
+    PG_CHECK_LAUNCH();
+}
+
 }  // namespace
 
 // get_optimal_splitting, Geometry.f90:679-707 (host, no fused multiply-add)
@@ -799,6 +946,7 @@ void build_neighbor_lists(pg_context* ctx, const double* h_cutoffs) {
     const int nblk = std::max(1, blocks(n, RS_TILE));
     ctx->radix_hist.resize((size_t)256 * nblk + 1);
     ctx->count_tmp.resize((size_t)256 * nblk + 1);
+    scan_prepare(ctx, std::max<long long>(n, 256ll * nblk));
     ctx->sorted_atoms.resize(std::max(n, 1));
     ctx->scan_tmp.resize(std::max(n, 1) + 1);
     ctx->nb_totals.resize(4);  // [0] out-of-range atoms, [1] list entries, [2] lower-index entries
@@ -840,9 +988,7 @@ void build_neighbor_lists(pg_context* ctx, const double* h_cutoffs) {
         for (int p = 0; p < passes && n > 0; ++p) {
             radix_hist<<<nblk, RS_THREADS, 0, st>>>(n, k_in, 8 * p, nblk, ctx->radix_hist.p);
             PG_CHECK_LAUNCH();
-            scan_single_block<int, int><<<1, 1024, 0, st>>>(ctx->radix_hist.p, ctx->count_tmp.p, 256 * nblk, nullptr,
-                                                            0);
-            PG_CHECK_LAUNCH();
+            scan_ints(ctx, ctx->radix_hist.p, ctx->count_tmp.p, 256 * nblk, nullptr, st);
             radix_scatter<<<nblk, RS_THREADS, 0, st>>>(n, k_in, v_in, 8 * p, nblk, ctx->count_tmp.p, k_out, v_out);
             PG_CHECK_LAUNCH();
             std::swap(k_in, k_out);
@@ -853,8 +999,7 @@ void build_neighbor_lists(pg_context* ctx, const double* h_cutoffs) {
         if (n > 0)
             PG_CUDA(cudaMemcpyAsync(ctx->sorted_atoms.p, v_in, sizeof(int) * n, cudaMemcpyDeviceToDevice, st));
         // atoms in out-of-range periodic subcells: their count stays on the device
-        scan_single_block<int, int><<<1, 1024, 0, st>>>(ctx->invisible.p, ctx->scan_tmp.p, n, ctx->nb_totals.p, 0);
-        PG_CHECK_LAUNCH();
+        scan_ints(ctx, ctx->invisible.p, ctx->scan_tmp.p, n, ctx->nb_totals.p, st);
         // inv_list may alias the sort's output buffer: the sorted atoms were copied first
         if (n > 0) {
             compact_flags<<<blocks(n, 256), 256, 0, st>>>(n, ctx->invisible.p, ctx->scan_tmp.p, inv_list.p);
@@ -865,10 +1010,8 @@ void build_neighbor_lists(pg_context* ctx, const double* h_cutoffs) {
             add_counts<<<blocks(n, 256), 256, 0, st>>>(n, ctx->nb_g0.p, ctx->vals_a.p, ctx->keys_a.p);
             PG_CHECK_LAUNCH();
         }
-        scan_single_block<int, int><<<1, 1024, 0, st>>>(ctx->keys_a.p, ctx->nb_start.p, n, ctx->nb_totals.p + 1, 0);
-        PG_CHECK_LAUNCH();
-        scan_single_block<int, int><<<1, 1024, 0, st>>>(ctx->nb_g0.p, ctx->g0_start.p, n, ctx->nb_totals.p + 2, 0);
-        PG_CHECK_LAUNCH();
+        scan_ints(ctx, ctx->keys_a.p, ctx->nb_start.p, n, ctx->nb_totals.p + 1, st);
+        scan_ints(ctx, ctx->nb_g0.p, ctx->g0_start.p, n, ctx->nb_totals.p + 2, st);
         PG_CUDA(cudaMemcpyAsync(ht, ctx->nb_totals.p, sizeof(int) * 4, cudaMemcpyDeviceToHost, st));
     };
     SigHash h1;
@@ -877,6 +1020,7 @@ void build_neighbor_lists(pg_context* ctx, const double* h_cutoffs) {
     run_segment(ctx, ctx->seg_g[0], h1.h, stage1);
     PG_CUDA(cudaStreamSynchronize(st));
     const int total = ht[1], total0 = ht[2];
+    require(ht[0] >= 0 && total >= 0 && total0 >= 0, PG_ERR_CUDA, "neighbour-list prefix scan did not complete");
     ctx->nb_total = total;
     ctx->nb_idx.resize(std::max(total, 1));
     ctx->nb_off.resize(3 * (size_t)std::max(total, 1));
@@ -1026,6 +1170,7 @@ void build_short_list(pg_context* ctx, bool same_positions) {
     ctx->sh_count.resize(std::max(n, 1));
     ctx->sh_start.resize(n + 1);
     ctx->nb_totals.resize(4);
+    scan_prepare(ctx, std::max<long long>(n, 256ll * std::max(1, blocks(n, RS_TILE))));
     int* ht = ctx->h_totals.get(4);
     // The short list is the full list itself when the cell-list build ran at
     // the generation's reference positions and no atom's list radius exceeds
@@ -1044,8 +1189,7 @@ void build_short_list(pg_context* ctx, bool same_positions) {
                                                        r * r, ctx->sh_count.p);
             PG_CHECK_LAUNCH();
         }
-        scan_single_block<int, int><<<1, 1024, 0, st>>>(ctx->sh_count.p, ctx->sh_start.p, n, ctx->nb_totals.p + 3, 0);
-        PG_CHECK_LAUNCH();
+        scan_ints(ctx, ctx->sh_count.p, ctx->sh_start.p, n, ctx->nb_totals.p + 3, st);
         PG_CUDA(cudaMemcpyAsync(ht + 3, ctx->nb_totals.p + 3, sizeof(int), cudaMemcpyDeviceToHost, st));
     };
     int total = 0;
@@ -1058,6 +1202,7 @@ void build_short_list(pg_context* ctx, bool same_positions) {
         run_segment(ctx, ctx->seg_g[3], h1.h, stage1);
         PG_CUDA(cudaStreamSynchronize(st));
         total = ht[3];
+        require(total >= 0, PG_ERR_CUDA, "short-list prefix scan did not complete");
     }
     ctx->sh_total = total;
     if (copy_full) {  // room for whole copies of the full list's buffers: sizes that do not move with the total
@@ -1121,9 +1266,7 @@ void build_short_list(pg_context* ctx, bool same_positions) {
         for (int pass = 0; pass < 2; ++pass) {
             radix_hist<<<nblk, RS_THREADS, 0, st>>>(n, k_in, 8 * pass, nblk, ctx->radix_hist.p);
             PG_CHECK_LAUNCH();
-            scan_single_block<int, int><<<1, 1024, 0, st>>>(ctx->radix_hist.p, ctx->count_tmp.p, 256 * nblk, nullptr,
-                                                            0);
-            PG_CHECK_LAUNCH();
+            scan_ints(ctx, ctx->radix_hist.p, ctx->count_tmp.p, 256 * nblk, nullptr, st);
             radix_scatter<<<nblk, RS_THREADS, 0, st>>>(n, k_in, v_in, 8 * pass, nblk, ctx->count_tmp.p, k_out, v_out);
             PG_CHECK_LAUNCH();
             std::swap(k_in, k_out);
